@@ -1,0 +1,1125 @@
+// bp_capi.cu - host side of the C ABI (include/bubblephysics.h).
+//
+// A single world (bp_world) and a batch (bp_batch) share one implementation, WorldSet: every resident world's bubbles,
+// segments and bodies live back to back in SoA device arrays, with a per-world table (DWorld) of offsets. Worlds of up
+// to kCtaMaxBubbles bubbles are stepped one thread block per world, grouped into power-of-two size classes (one launch
+// per class and step, all classes of a step captured into one CUDA graph); larger worlds use a cooperative launch over
+// the whole GPU. The plain per-world path launches each world on its own, one after another (what the reference does:
+// one command-buffer pair per world and frame, NativeMetalSubstepLoop.swift:216-273).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "bp_device.cuh"
+
+namespace bp {
+cudaError_t launch_batch(const DState& S, const uint32_t* dWorldList, uint32_t count, uint32_t threads, uint32_t B,
+                         uint32_t maxN, cudaStream_t stream);
+int large_max_blocks(int threads);
+cudaError_t launch_large(const DState& S, uint32_t wi, uint32_t B, int blocks, int threads, cudaStream_t stream);
+cudaError_t launch_contact_law(uint32_t mode, const float* in, float* out, uint32_t count, cudaStream_t stream);
+cudaError_t launch_accumulate(const bp_step_report* reports, bp_step_report* acc, const uint32_t* sizes,
+                              unsigned long long* total, uint32_t count, cudaStream_t stream);
+cudaError_t launch_write_state(const float4* in, float2* pos, float2* vel, float2* ppos, float2* pvel, uint64_t n,
+                               cudaStream_t stream);
+cudaError_t launch_read_state(float4* out, const float2* ppos, const float2* pvel, uint64_t n, cudaStream_t stream);
+void prepare_kernels();
+}  // namespace bp
+
+using namespace bp;
+
+static_assert(sizeof(bp_bubble) == 80, "bp_bubble layout");
+static_assert(sizeof(bp_segment) == 64, "bp_segment layout");
+static_assert(sizeof(bp_body) == 80, "bp_body layout");
+static_assert(sizeof(bp_force_field) == 64, "bp_force_field layout");
+static_assert(sizeof(bp_band) == 24 && sizeof(bp_motor) == 24, "band / motor layout");
+static_assert(sizeof(bp_world_desc) == 64, "bp_world_desc layout");
+static_assert(sizeof(bp_step_report) == 96, "bp_step_report layout");
+static_assert(sizeof(bp_contact) == 64, "bp_contact layout");
+static_assert(sizeof(bp_candidate_key) == 24, "bp_candidate_key layout");
+static_assert(offsetof(bp_bubble, center) == 8 && offsetof(bp_bubble, flags) == 60, "bp_bubble offsets");
+static_assert(offsetof(bp_step_report, limiter_object) == 40, "bp_step_report offsets");
+
+namespace {
+
+constexpr uint32_t kCtaMaxBubbles = 4096;
+constexpr uint32_t kClasses = 9;  // class c: worlds of at most 2^(c+4) bubbles
+constexpr int kLargeThreads = 512;
+
+struct DeviceGuard {
+    int previous = -1;
+    explicit DeviceGuard(int device) {
+        cudaGetDevice(&previous);
+        if (previous != device) cudaSetDevice(device);
+    }
+    ~DeviceGuard() {
+        int now = -1;
+        cudaGetDevice(&now);
+        if (previous >= 0 && now != previous) cudaSetDevice(previous);
+    }
+};
+
+uint32_t next_pow2(uint32_t v) {
+    uint32_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+uint32_t size_class(uint32_t n) {
+    uint32_t c = 0;
+    while (c + 1 < kClasses && n > (16u << c)) ++c;
+    return c;
+}
+uint32_t default_threads(uint32_t maxN) {
+    // enough threads for one or two bubbles each, at least two warps
+    uint32_t t = next_pow2(std::max<uint32_t>(maxN / 2, 64u));
+    return std::min<uint32_t>(t, 512u);
+}
+
+}  // namespace
+
+struct bp_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t start = nullptr, stop = nullptr;
+    std::vector<cudaStream_t> side;
+    int sms = 0;
+};
+
+struct WorldSet {
+    bp_context* ctx = nullptr;
+    uint32_t nWorlds = 0;
+    uint32_t flags = 0;
+    uint32_t fixedThreads = 0;
+    std::vector<DWorld> hWorlds;
+    std::vector<bp_bubble> hBubbles;        // as uploaded (static fields for readback)
+    std::vector<int64_t> hSegIds, hBodyIds;
+    uint64_t totalBubbles = 0, totalRows = 0, totalBodyRows = 0, totalContacts = 0;
+    uint32_t totalSegments = 0, totalBodies = 0;
+    DState S{};
+    DWorld* dWorlds = nullptr;
+    bp_step_report* dReports = nullptr;
+    bp_step_report* dAcc = nullptr;
+    uint32_t* dSizes = nullptr;
+    unsigned long long* dTotal = nullptr;
+    float4* dStaging = nullptr;
+    std::vector<void*> allocations;
+    // scheduling
+    std::vector<uint32_t> classWorlds[kClasses];
+    uint32_t* dClassList[kClasses] = {};
+    uint32_t classThreads[kClasses] = {};
+    uint32_t classMaxN[kClasses] = {};
+    std::vector<uint32_t> largeWorlds;
+    uint32_t largeB = 0, largeMaxN = 0;
+    int largeBlocks = 0;
+    uint32_t* dSingle = nullptr;            // world index list for per-world launches
+    cudaGraphExec_t graph = nullptr;
+    bool tuned = false;
+    bool inflight = false;
+    uint64_t bubbleSubsteps = 0, launches = 0;
+    std::vector<float> lastHistory;
+
+    ~WorldSet() {
+        if (graph) cudaGraphExecDestroy(graph);
+        for (void* p : allocations) cudaFree(p);
+    }
+    template <class T> T* alloc(uint64_t count, cudaError_t& err) {
+        if (err != cudaSuccess) return nullptr;
+        void* p = nullptr;
+        size_t bytes = std::max<uint64_t>(count, 1) * sizeof(T);
+        err = cudaMalloc(&p, bytes);
+        if (err != cudaSuccess) return nullptr;
+        allocations.push_back(p);
+        err = cudaMemsetAsync(p, 0, bytes, ctx->stream);
+        return (T*)p;
+    }
+};
+
+struct bp_world {
+    WorldSet set;
+};
+struct bp_batch {
+    WorldSet set;
+};
+
+namespace {
+
+int cuda_status(cudaError_t e) {
+    if (e == cudaSuccess) return BP_OK;
+    if (e == cudaErrorMemoryAllocation) return BP_E_ALLOC;
+    return BP_E_CUDA;
+}
+
+template <class T> cudaError_t upload(T* dst, const T* src, uint64_t count, cudaStream_t stream) {
+    if (count == 0) return cudaSuccess;
+    return cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyHostToDevice, stream);
+}
+
+int validate(const bp_world_desc& d, const bp_world_input& in) {
+    if (!(d.time_step > 0.0f) || !std::isfinite(d.time_step)) return BP_E_INVALID;
+    if (d.candidate_limit > 128u) return BP_E_CAPACITY;
+    if (in.bubble_count && !in.bubbles) return BP_E_INVALID;
+    if (in.segment_count && !in.segments) return BP_E_INVALID;
+    if (in.body_count && !in.bodies) return BP_E_INVALID;
+    for (uint32_t i = 0; i < in.bubble_count; ++i) {
+        const bp_bubble& b = in.bubbles[i];
+        if (i > 0 && !(in.bubbles[i - 1].id < b.id)) return BP_E_INVALID;  // sorted by id (NativePublicWorld.swift:248)
+        if (!std::isfinite(b.center[0]) || !std::isfinite(b.center[1]) || !std::isfinite(b.velocity[0]) ||
+            !std::isfinite(b.velocity[1]) || !(b.radius > 0.0f) || !std::isfinite(b.radius) || !std::isfinite(b.mass))
+            return BP_E_INVALID;
+    }
+    for (uint32_t j = 1; j < in.segment_count; ++j)
+        if (!(in.segments[j - 1].id < in.segments[j].id)) return BP_E_INVALID;
+    for (uint32_t b = 0; b < in.body_count; ++b) {
+        const bp_body& r = in.bodies[b];
+        if (!(r.flags & (BP_BODY_STATIC | BP_BODY_KINEMATIC))) return BP_E_INVALID;  // dynamic bodies: not with bubbles
+        if ((uint64_t)r.vertex_offset + r.vertex_count > in.body_vertex_count) return BP_E_INVALID;
+        if ((uint64_t)r.triangle_offset + r.triangle_count > in.body_triangle_count) return BP_E_INVALID;
+        if (r.vertex_count == 0) return BP_E_INVALID;
+    }
+    for (uint32_t b = 0; b < in.body_count; ++b) {
+        const bp_body& r = in.bodies[b];
+        for (uint64_t t = 0; t < 3ull * r.triangle_count; ++t)
+            if (in.body_triangles[3ull * r.triangle_offset + t] >= r.vertex_count) return BP_E_INVALID;
+    }
+    for (uint32_t f = 0; f < in.field_count; ++f) {
+        const bp_force_field& r = in.fields[f];
+        if ((uint64_t)r.vertex_offset + r.vertex_count > in.field_vertex_count) return BP_E_INVALID;
+        if (r.has_filter && (uint64_t)r.filter_offset + r.filter_count > in.field_object_id_count) return BP_E_INVALID;
+    }
+    if (in.joint_entity_count && in.joint_entity_count > in.bubble_count + in.body_count) return BP_E_INVALID;
+    return BP_OK;
+}
+
+int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc* descs, const bp_world_input* inputs,
+              bool single) {
+    ws.ctx = ctx;
+    ws.nWorlds = count;
+    DeviceGuard guard(ctx->device);
+    // totals and validation
+    uint64_t nb = 0, rows = 0, brows = 0, contacts = 0;
+    uint64_t ns = 0, nbo = 0, nbv = 0, nbt = 0, nf = 0, nfv = 0, nfi = 0, nband = 0, nmotor = 0, njr = 0, njp = 0;
+    for (uint32_t w = 0; w < count; ++w) {
+        int st = validate(descs[w], inputs[w]);
+        if (st != BP_OK) return st;
+        const bp_world_input& in = inputs[w];
+        uint32_t k = descs[w].candidate_limit == 0 ? 128u : descs[w].candidate_limit;
+        nb += in.bubble_count;
+        rows += (uint64_t)in.bubble_count * k;
+        brows += (uint64_t)in.body_count * k;
+        contacts += single ? (uint64_t)in.bubble_count * k + 64 : (uint64_t)in.bubble_count * 16 + 64;
+        ns += in.segment_count; nbo += in.body_count; nbv += in.body_vertex_count; nbt += in.body_triangle_count;
+        nf += in.field_count; nfv += in.field_vertex_count; nfi += in.field_object_id_count;
+        nband += in.band_count; nmotor += in.motor_count;
+        njr += in.joint_ranges ? in.joint_entity_count : 0; njp += in.joint_partners ? in.joint_partner_count : 0;
+    }
+    if (nb > 0x3fffffffull || ns > 0x3fffffffull) return BP_E_CAPACITY;
+    ws.totalBubbles = nb;
+    ws.totalRows = rows;
+    ws.totalBodyRows = brows;
+    ws.totalContacts = contacts;
+    ws.totalSegments = (uint32_t)ns;
+    ws.totalBodies = (uint32_t)nbo;
+
+    // host staging in device layout
+    std::vector<float2> pos(nb), start(nb), vel(nb), rotw(nb);
+    std::vector<float4> phys(nb);
+    std::vector<int64_t> ids(nb);
+    std::vector<uint32_t> flags(nb);
+    std::vector<uint2> filter(nb);
+    std::vector<DSegment> segs(ns);
+    std::vector<DBody> bodies(nbo);
+    std::vector<float2> bverts(nbv);
+    std::vector<uint32_t> btris(3 * nbt);
+    std::vector<DField> fields(nf);
+    std::vector<float2> fverts(nfv);
+    std::vector<int64_t> fids(nfi);
+    std::vector<bp_band> bands(nband);
+    std::vector<bp_motor> motors(nmotor);
+    std::vector<uint2> jranges(njr);
+    std::vector<int64_t> jpartners(njp);
+    ws.hWorlds.resize(count);
+    ws.hBubbles.resize(nb);
+    ws.hSegIds.resize(ns);
+    ws.hBodyIds.resize(nbo);
+    uint64_t ob = 0, orow = 0, obrow = 0, ocon = 0, os = 0, obo = 0, obv = 0, obt = 0, of = 0, ofv = 0, ofi = 0, oband = 0,
+             omotor = 0, ojr = 0, ojp = 0;
+    for (uint32_t w = 0; w < count; ++w) {
+        const bp_world_desc& d = descs[w];
+        const bp_world_input& in = inputs[w];
+        DWorld& W = ws.hWorlds[w];
+        std::memset(&W, 0, sizeof(W));
+        W.boff = (uint32_t)ob; W.n = in.bubble_count;
+        W.soff = (uint32_t)os; W.s = in.segment_count;
+        W.bodyOff = (uint32_t)obo; W.nb = in.body_count;
+        W.foff = (uint32_t)of; W.nf = in.field_count;
+        W.bandOff = (uint32_t)oband; W.nbands = in.band_count;
+        W.motorOff = (uint32_t)omotor; W.nmotors = in.motor_count;
+        W.jrOff = (uint32_t)ojr; W.njEnt = in.joint_ranges ? in.joint_entity_count : 0;
+        W.k = d.candidate_limit == 0 ? 128u : d.candidate_limit;
+        W.flags = d.flags;
+        W.injectSubstep = 0;
+        W.contactCap = single ? in.bubble_count * W.k + 64 : in.bubble_count * 16 + 64;
+        W.rowOff = orow; W.bodyRowOff = obrow; W.contactOff = ocon;
+        W.dt = d.time_step; W.sepTol = d.separation_tolerance; W.contactTol = d.contact_tolerance;
+        W.split = d.substep_split_multiplier;
+        W.rmin = make_float2(d.region[0], d.region[1]); W.rmax = make_float2(d.region[2], d.region[3]);
+        W.gforce = make_float2(d.global_force[0], d.global_force[1]);
+        W.gravity = make_float2(d.gravity[0], d.gravity[1]);
+        W.injectPos = make_float2(0.0f, 0.0f);
+        W.injectObject = d.inject_object;
+        for (uint32_t i = 0; i < in.bubble_count; ++i) {
+            const bp_bubble& b = in.bubbles[i];
+            uint64_t g = ob + i;
+            pos[g] = make_float2(b.center[0], b.center[1]);
+            start[g] = make_float2(b.previous_center[0], b.previous_center[1]);
+            vel[g] = make_float2(b.velocity[0], b.velocity[1]);
+            rotw[g] = make_float2(b.rotation, b.angular_velocity);
+            phys[g] = make_float4(b.radius, b.inverse_mass, b.contact_stiffness, b.damping);
+            ids[g] = b.id;
+            flags[g] = b.flags & 0xffu;
+            filter[g] = make_uint2(b.category, b.mask);
+            ws.hBubbles[g] = b;
+        }
+        for (uint32_t j = 0; j < in.segment_count; ++j) {
+            const bp_segment& r = in.segments[j];
+            DSegment& sg = segs[os + j];
+            std::memset(&sg, 0, sizeof(sg));
+            sg.a = make_float2(r.a[0], r.a[1]); sg.b = make_float2(r.b[0], r.b[1]);
+            sg.prev = make_float2(r.previous_start[0], r.previous_start[1]);
+            sg.outward = r.outward_sign; sg.allowed = r.allowed_side;
+            sg.flags = r.flags; sg.cat = r.category; sg.mask = r.mask;
+            sg.id = r.id; sg.owner = r.owner_id;
+            ws.hSegIds[os + j] = r.id;
+        }
+        for (uint32_t v = 0; v < in.body_vertex_count; ++v)
+            bverts[obv + v] = make_float2(in.body_vertices[2 * v], in.body_vertices[2 * v + 1]);
+        for (uint64_t t = 0; t < 3ull * in.body_triangle_count; ++t) btris[3 * obt + t] = in.body_triangles[t];
+        for (uint32_t b = 0; b < in.body_count; ++b) {
+            const bp_body& r = in.bodies[b];
+            DBody& B = bodies[obo + b];
+            std::memset(&B, 0, sizeof(B));
+            B.pos = make_float2(r.position[0], r.position[1]);
+            B.prev = B.pos;
+            B.angle = r.angle; B.prevAngle = r.angle;
+            B.vel = make_float2(r.velocity[0], r.velocity[1]);
+            B.omega = r.angular_velocity; B.radius = r.bounding_radius; B.coreRadius = r.core_radius;
+            // rotation of the pose, computed on the host (the CPU oracle does the same)
+            B.cosEnd = std::cos(r.angle); B.sinEnd = std::sin(r.angle);
+            B.cosPrev = B.cosEnd; B.sinPrev = B.sinEnd;
+            B.kind = r.kind; B.flags = r.flags;
+            B.voff = (uint32_t)(obv + r.vertex_offset); B.vcount = r.vertex_count;
+            B.toff = (uint32_t)(obt + r.triangle_offset); B.tcount = r.triangle_count;
+            B.cat = r.category; B.mask = r.mask; B.id = r.id;
+            ws.hBodyIds[obo + b] = r.id;
+        }
+        for (uint32_t v = 0; v < in.field_vertex_count; ++v)
+            fverts[ofv + v] = make_float2(in.field_vertices[2 * v], in.field_vertices[2 * v + 1]);
+        for (uint32_t v = 0; v < in.field_object_id_count; ++v) fids[ofi + v] = in.field_object_ids[v];
+        for (uint32_t f = 0; f < in.field_count; ++f) {
+            const bp_force_field& r = in.fields[f];
+            DField& F = fields[of + f];
+            std::memset(&F, 0, sizeof(F));
+            F.pos = make_float2(r.position[0], r.position[1]);
+            F.cosr = std::cos(r.rotation); F.sinr = std::sin(r.rotation);
+            F.falloff = r.falloff; F.strength = r.strength; F.radius = r.radius;
+            F.dir = make_float2(r.direction[0], r.direction[1]);
+            F.kind = r.kind; F.voff = (uint32_t)(ofv + r.vertex_offset); F.vcount = r.vertex_count;
+            F.foff = (uint32_t)(ofi + r.filter_offset); F.fcount = r.filter_count; F.hasFilter = r.has_filter;
+        }
+        for (uint32_t q = 0; q < in.band_count; ++q) bands[oband + q] = in.bands[q];
+        for (uint32_t q = 0; q < in.motor_count; ++q) motors[omotor + q] = in.motors[q];
+        if (in.joint_ranges)
+            for (uint32_t e = 0; e < in.joint_entity_count; ++e)
+                jranges[ojr + e] = make_uint2((uint32_t)(ojp + in.joint_ranges[2 * e]), in.joint_ranges[2 * e + 1]);
+        if (in.joint_partners)
+            for (uint32_t q = 0; q < in.joint_partner_count; ++q) jpartners[ojp + q] = in.joint_partners[q];
+        ob += in.bubble_count; orow += (uint64_t)in.bubble_count * W.k; obrow += (uint64_t)in.body_count * W.k;
+        ocon += W.contactCap; os += in.segment_count; obo += in.body_count; obv += in.body_vertex_count;
+        obt += in.body_triangle_count; of += in.field_count; ofv += in.field_vertex_count; ofi += in.field_object_id_count;
+        oband += in.band_count; omotor += in.motor_count;
+        ojr += in.joint_ranges ? in.joint_entity_count : 0; ojp += in.joint_partners ? in.joint_partner_count : 0;
+    }
+
+    // device allocations
+    cudaError_t err = cudaSuccess;
+    cudaStream_t st = ctx->stream;
+    DState& S = ws.S;
+    ws.dWorlds = ws.alloc<DWorld>(count, err);
+    ws.dReports = ws.alloc<bp_step_report>(count, err);
+    ws.dAcc = ws.alloc<bp_step_report>(count, err);
+    ws.dSizes = ws.alloc<uint32_t>(count, err);
+    ws.dTotal = ws.alloc<unsigned long long>(1, err);
+    S.worlds = ws.dWorlds;
+    S.reports = ws.dReports;
+    S.history = ws.alloc<float>((uint64_t)count * kFrameLimit, err);
+    S.contactCount = ws.alloc<uint32_t>(count, err);
+    S.pos = ws.alloc<float2>(nb, err); S.start = ws.alloc<float2>(nb, err); S.vel = ws.alloc<float2>(nb, err);
+    S.acc = ws.alloc<float2>(nb, err); S.a0 = ws.alloc<float2>(nb, err); S.ref = ws.alloc<float2>(nb, err);
+    S.rotw = ws.alloc<float2>(nb, err);
+    S.phys = ws.alloc<float4>(nb, err);
+    S.margin = ws.alloc<float>(nb, err);
+    int64_t* dIds = ws.alloc<int64_t>(nb, err);
+    S.id = dIds;
+    S.flags = ws.alloc<uint32_t>(nb, err); S.result = ws.alloc<uint32_t>(nb, err);
+    uint2* dFilter = ws.alloc<uint2>(nb, err);
+    S.filter = dFilter;
+    S.cell = ws.alloc<longlong2>(nb, err); S.acell = ws.alloc<longlong2>(nb, err);
+    S.candRow = ws.alloc<uint32_t>(rows, err); S.candCount = ws.alloc<uint2>(nb, err);
+    S.pairTotal = ws.alloc<uint32_t>(nb, err);
+    S.adj = ws.alloc<uint32_t>(rows, err); S.deg = ws.alloc<uint32_t>(nb, err);
+    S.pPos = ws.alloc<float2>(nb, err); S.pStart = ws.alloc<float2>(nb, err); S.pVel = ws.alloc<float2>(nb, err);
+    S.pRotw = ws.alloc<float2>(nb, err); S.pResult = ws.alloc<uint32_t>(nb, err); S.pFlags = ws.alloc<uint32_t>(nb, err);
+    DSegment* dSeg = ws.alloc<DSegment>(ns, err);
+    S.seg = dSeg;
+    S.body = ws.alloc<DBody>(nbo, err); S.pBody = ws.alloc<DBody>(nbo, err);
+    float2* dBv = ws.alloc<float2>(nbv, err);
+    S.bverts = dBv;
+    uint32_t* dBt = ws.alloc<uint32_t>(3 * nbt, err);
+    S.btris = dBt;
+    S.bodyRow = ws.alloc<uint32_t>(brows, err); S.bodyTotal = ws.alloc<uint32_t>(nbo, err);
+    DField* dF = ws.alloc<DField>(nf, err);
+    S.fields = dF;
+    float2* dFv = ws.alloc<float2>(nfv, err);
+    S.fverts = dFv;
+    int64_t* dFi = ws.alloc<int64_t>(nfi, err);
+    S.fids = dFi;
+    bp_band* dBand = ws.alloc<bp_band>(nband, err);
+    S.bands = dBand;
+    bp_motor* dMotor = ws.alloc<bp_motor>(nmotor, err);
+    S.motors = dMotor;
+    uint2* dJr = ws.alloc<uint2>(njr, err);
+    S.jranges = dJr;
+    int64_t* dJp = ws.alloc<int64_t>(njp, err);
+    S.jpartners = dJp;
+    S.contacts = ws.alloc<DContact>(contacts, err);
+    S.failed = ws.alloc<uint32_t>(count, err);
+    S.scanA = ws.alloc<uint32_t>(nb, err); S.scanB = ws.alloc<uint32_t>(nb, err);
+    // scheduling: size classes and large worlds
+    for (uint32_t w = 0; w < count; ++w) {
+        uint32_t n = ws.hWorlds[w].n;
+        if (n > kCtaMaxBubbles || (ws.hWorlds[w].flags & BP_WORLD_FORCE_MULTI_CTA)) ws.largeWorlds.push_back(w);
+        else {
+            uint32_t c = size_class(n);
+            ws.classWorlds[c].push_back(w);
+            ws.classMaxN[c] = std::max(ws.classMaxN[c], n);
+        }
+    }
+    for (uint32_t c = 0; c < kClasses; ++c) {
+        // biggest worlds first so the tail of the launch holds the short ones
+        std::stable_sort(ws.classWorlds[c].begin(), ws.classWorlds[c].end(),
+                         [&](uint32_t a, uint32_t b) { return ws.hWorlds[a].n > ws.hWorlds[b].n; });
+        if (!ws.classWorlds[c].empty()) {
+            ws.dClassList[c] = ws.alloc<uint32_t>(ws.classWorlds[c].size(), err);
+            ws.classThreads[c] = default_threads(ws.classMaxN[c]);
+        }
+    }
+    ws.dSingle = ws.alloc<uint32_t>(count, err);
+    for (uint32_t w : ws.largeWorlds) ws.largeMaxN = std::max(ws.largeMaxN, ws.hWorlds[w].n);
+    ws.largeB = next_pow2(std::max<uint32_t>(2u * ws.largeMaxN, 64u));
+    ws.largeBlocks = ws.largeWorlds.empty() ? 0 : large_max_blocks(kLargeThreads);
+    S.gpv = ws.alloc<float>(2ull * std::max(ws.largeBlocks, 1), err);
+    S.gpo = ws.alloc<uint32_t>(2ull * std::max(ws.largeBlocks, 1), err);
+    S.gbuckets = ws.alloc<uint32_t>(ws.largeWorlds.empty() ? 1 : ws.largeB, err);
+    S.gentries = ws.alloc<uint32_t>(std::max<uint32_t>(ws.largeMaxN, 1u), err);
+    S.barrier = ws.alloc<unsigned int>(2, err);
+    S.errorFlag = ws.alloc<uint32_t>(1, err);
+    if (err != cudaSuccess) return cuda_status(err);
+
+    std::vector<uint32_t> sizes(count), identity(count);
+    for (uint32_t w = 0; w < count; ++w) { sizes[w] = ws.hWorlds[w].n; identity[w] = w; }
+    err = upload(ws.dWorlds, ws.hWorlds.data(), count, st);
+    if (!err) err = upload(ws.dSizes, sizes.data(), count, st);
+    if (!err) err = upload(ws.dSingle, identity.data(), count, st);
+    for (uint32_t c = 0; c < kClasses && !err; ++c)
+        if (!ws.classWorlds[c].empty()) err = upload(ws.dClassList[c], ws.classWorlds[c].data(), ws.classWorlds[c].size(), st);
+    if (!err) err = upload(S.pos, pos.data(), nb, st);
+    if (!err) err = upload(S.pPos, pos.data(), nb, st);
+    if (!err) err = upload(S.start, start.data(), nb, st);
+    if (!err) err = upload(S.pStart, start.data(), nb, st);
+    if (!err) err = upload(S.vel, vel.data(), nb, st);
+    if (!err) err = upload(S.pVel, vel.data(), nb, st);
+    if (!err) err = upload(S.rotw, rotw.data(), nb, st);
+    if (!err) err = upload(S.pRotw, rotw.data(), nb, st);
+    if (!err) err = upload(S.phys, phys.data(), nb, st);
+    if (!err) err = upload(dIds, ids.data(), nb, st);
+    if (!err) err = upload(S.flags, flags.data(), nb, st);
+    if (!err) err = upload(S.pFlags, flags.data(), nb, st);
+    if (!err) err = upload(dFilter, filter.data(), nb, st);
+    if (!err) err = upload(dSeg, segs.data(), ns, st);
+    if (!err) err = upload(S.body, bodies.data(), nbo, st);
+    if (!err) err = upload(S.pBody, bodies.data(), nbo, st);
+    if (!err) err = upload(dBv, bverts.data(), nbv, st);
+    if (!err) err = upload(dBt, btris.data(), 3 * nbt, st);
+    if (!err) err = upload(dF, fields.data(), nf, st);
+    if (!err) err = upload(dFv, fverts.data(), nfv, st);
+    if (!err) err = upload(dFi, fids.data(), nfi, st);
+    if (!err) err = upload(dBand, bands.data(), nband, st);
+    if (!err) err = upload(dMotor, motors.data(), nmotor, st);
+    if (!err) err = upload(dJr, jranges.data(), njr, st);
+    if (!err) err = upload(dJp, jpartners.data(), njp, st);
+    if (!err) err = cudaStreamSynchronize(st);
+    return cuda_status(err);
+}
+
+// Launches one step of every world of the set (or of one world when `only` < nWorlds).
+cudaError_t launch_step(WorldSet& ws, bool perWorld, uint32_t only = 0xffffffffu) {
+    cudaError_t err = cudaSuccess;
+    cudaStream_t st = ws.ctx->stream;
+    auto one = [&](uint32_t w) -> cudaError_t {
+        const DWorld& W = ws.hWorlds[w];
+        ws.launches++;
+        if (W.n > kCtaMaxBubbles || (W.flags & BP_WORLD_FORCE_MULTI_CTA))
+            return launch_large(ws.S, w, ws.largeB, ws.largeBlocks, kLargeThreads, st);
+        uint32_t c = size_class(W.n);
+        uint32_t maxN = std::max<uint32_t>(W.n, 1u);
+        uint32_t B = next_pow2(std::max<uint32_t>(2u * maxN, 32u));
+        uint32_t threads = ws.fixedThreads ? ws.fixedThreads : (ws.classThreads[c] ? ws.classThreads[c] : default_threads(maxN));
+        return launch_batch(ws.S, ws.dSingle + w, 1, threads, B, maxN, st);
+    };
+    if (only < ws.nWorlds) return one(only);
+    if (perWorld) {
+        for (uint32_t w = 0; w < ws.nWorlds && err == cudaSuccess; ++w) err = one(w);
+        return err;
+    }
+    for (uint32_t c = 0; c < kClasses && err == cudaSuccess; ++c) {
+        if (ws.classWorlds[c].empty()) continue;
+        uint32_t maxN = std::max<uint32_t>(ws.classMaxN[c], 1u);
+        uint32_t B = next_pow2(std::max<uint32_t>(2u * maxN, 32u));
+        uint32_t threads = ws.fixedThreads ? ws.fixedThreads : ws.classThreads[c];
+        ws.launches++;
+        err = launch_batch(ws.S, ws.dClassList[c], (uint32_t)ws.classWorlds[c].size(), threads, B, maxN, st);
+    }
+    for (uint32_t w : ws.largeWorlds) {
+        if (err != cudaSuccess) break;
+        ws.launches++;
+        err = launch_large(ws.S, w, ws.largeB, ws.largeBlocks, kLargeThreads, st);
+    }
+    return err;
+}
+
+// Snapshot / restore of the dynamic state (for the autotuner's trial steps).
+struct Snapshot {
+    std::vector<std::pair<void*, size_t>> parts;
+    std::vector<void*> copies;
+};
+cudaError_t take_snapshot(WorldSet& ws, Snapshot& snap) {
+    DState& S = ws.S;
+    uint64_t nb = ws.totalBubbles;
+    snap.parts = {{S.pos, nb * 8}, {S.start, nb * 8}, {S.vel, nb * 8}, {S.acc, nb * 8}, {S.rotw, nb * 8},
+                  {S.flags, nb * 4}, {S.result, nb * 4}, {S.pPos, nb * 8}, {S.pStart, nb * 8}, {S.pVel, nb * 8},
+                  {S.pRotw, nb * 8}, {S.pResult, nb * 4}, {S.pFlags, nb * 4}, {S.body, ws.totalBodies * sizeof(DBody)},
+                  {S.pBody, ws.totalBodies * sizeof(DBody)}, {S.failed, ws.nWorlds * 4ull}};
+    cudaError_t err = cudaSuccess;
+    for (auto& p : snap.parts) {
+        void* c = nullptr;
+        if (p.second) {
+            err = cudaMalloc(&c, p.second);
+            if (!err) err = cudaMemcpyAsync(c, p.first, p.second, cudaMemcpyDeviceToDevice, ws.ctx->stream);
+        }
+        snap.copies.push_back(c);
+        if (err) return err;
+    }
+    return err;
+}
+cudaError_t restore_snapshot(WorldSet& ws, Snapshot& snap) {
+    cudaError_t err = cudaSuccess;
+    for (size_t q = 0; q < snap.parts.size() && !err; ++q)
+        if (snap.copies[q]) err = cudaMemcpyAsync(snap.parts[q].first, snap.copies[q], snap.parts[q].second,
+                                                  cudaMemcpyDeviceToDevice, ws.ctx->stream);
+    return err;
+}
+void free_snapshot(Snapshot& snap) {
+    for (void* c : snap.copies)
+        if (c) cudaFree(c);
+    snap.copies.clear();
+}
+
+// Project autotuner: per size class, time one step at each candidate block width from the same saved state and keep
+// the fastest; the state is restored afterwards so tuning does not advance the simulation.
+cudaError_t autotune(WorldSet& ws) {
+    if (ws.tuned) return cudaSuccess;
+    ws.tuned = true;
+    if (ws.fixedThreads) return cudaSuccess;
+    Snapshot snap;
+    cudaError_t err = take_snapshot(ws, snap);
+    cudaStream_t st = ws.ctx->stream;
+    const uint32_t candidates[] = {64, 128, 256, 512, 1024};
+    for (uint32_t c = 0; c < kClasses && !err; ++c) {
+        if (ws.classWorlds[c].empty()) continue;
+        uint32_t maxN = std::max<uint32_t>(ws.classMaxN[c], 1u);
+        uint32_t B = next_pow2(std::max<uint32_t>(2u * maxN, 32u));
+        float best = 1e30f;
+        uint32_t bestT = ws.classThreads[c];
+        for (uint32_t t : candidates) {
+            if (t > 64 && t > 2 * next_pow2(maxN)) break;
+            for (int rep = 0; rep < 2 && !err; ++rep) {  // the first run warms up
+                err = restore_snapshot(ws, snap);
+                if (err) break;
+                cudaEventRecord(ws.ctx->start, st);
+                err = launch_batch(ws.S, ws.dClassList[c], (uint32_t)ws.classWorlds[c].size(), t, B, maxN, st);
+                cudaEventRecord(ws.ctx->stop, st);
+                if (!err) err = cudaEventSynchronize(ws.ctx->stop);
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, ws.ctx->start, ws.ctx->stop);
+                if (!err && rep == 1 && ms < best) { best = ms; bestT = t; }
+            }
+        }
+        ws.classThreads[c] = bestT;
+    }
+    cudaError_t rerr = restore_snapshot(ws, snap);
+    if (!rerr) rerr = cudaStreamSynchronize(st);
+    free_snapshot(snap);
+    return err ? err : rerr;
+}
+
+int read_reports(WorldSet& ws, bp_step_report* out, uint32_t count) {
+    cudaError_t err = cudaMemcpyAsync(out, ws.dReports, count * sizeof(bp_step_report), cudaMemcpyDeviceToHost, ws.ctx->stream);
+    if (!err) err = cudaStreamSynchronize(ws.ctx->stream);
+    return cuda_status(err);
+}
+
+int step_set(WorldSet& ws, uint32_t steps, bp_step_report* reports, bool perWorld, bool useGraph, bool perStepReports) {
+    if (ws.inflight) return BP_E_INFLIGHT;
+    ws.inflight = true;
+    struct Clear { bool& f; ~Clear() { f = false; } } clear{ws.inflight};
+    DeviceGuard guard(ws.ctx->device);
+    cudaStream_t st = ws.ctx->stream;
+    cudaError_t err = cudaSuccess;
+    if ((ws.flags & BP_BATCH_AUTOTUNE) && !ws.tuned && !perWorld) {
+        err = autotune(ws);
+        if (err) return cuda_status(err);
+    }
+    err = cudaMemsetAsync(ws.dAcc, 0, ws.nWorlds * sizeof(bp_step_report), st);
+    if (!err) err = cudaMemsetAsync(ws.dTotal, 0, sizeof(unsigned long long), st);
+    if (err) return cuda_status(err);
+    bool graphed = useGraph && !perWorld && ws.largeWorlds.empty();
+    if (graphed && !ws.graph) {
+        cudaGraph_t g = nullptr;
+        err = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+        if (!err) {
+            uint64_t before = ws.launches;
+            cudaError_t le = launch_step(ws, false);
+            le = le ? le : launch_accumulate(ws.dReports, ws.dAcc, ws.dSizes, ws.dTotal, ws.nWorlds, st);
+            err = cudaStreamEndCapture(st, &g);
+            ws.launches = before;
+            if (!err) err = le;
+        }
+        if (!err) err = cudaGraphInstantiate(&ws.graph, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (err) return cuda_status(err);
+    }
+    uint32_t launchesPerStep = 0;
+    for (uint32_t c = 0; c < kClasses; ++c) launchesPerStep += ws.classWorlds[c].empty() ? 0u : 1u;
+    launchesPerStep += (uint32_t)ws.largeWorlds.size();
+    int status = BP_OK;
+    for (uint32_t s = 0; s < steps && !err; ++s) {
+        if (graphed) {
+            err = cudaGraphLaunch(ws.graph, st);
+            ws.launches += launchesPerStep;
+        } else {
+            err = launch_step(ws, perWorld);
+            if (!err) err = launch_accumulate(ws.dReports, ws.dAcc, ws.dSizes, ws.dTotal, ws.nWorlds, st);
+        }
+        if (perStepReports && reports && !err) {
+            int rs = read_reports(ws, reports + (uint64_t)s * ws.nWorlds, ws.nWorlds);
+            if (rs) return rs;
+            for (uint32_t w = 0; w < ws.nWorlds; ++w)
+                if (reports[(uint64_t)s * ws.nWorlds + w].status != BP_OK) status = reports[(uint64_t)s * ws.nWorlds + w].status;
+            if (status != BP_OK && ws.nWorlds == 1) break;
+        }
+    }
+    if (err) return cuda_status(err);
+    unsigned long long total = 0;
+    err = cudaMemcpyAsync(&total, ws.dTotal, sizeof(total), cudaMemcpyDeviceToHost, st);
+    if (!err && reports && !perStepReports) err = cudaMemcpyAsync(reports, ws.dAcc, ws.nWorlds * sizeof(bp_step_report), cudaMemcpyDeviceToHost, st);
+    if (!err) err = cudaStreamSynchronize(st);
+    if (!err) {
+        uint32_t flag = 0;
+        cudaMemcpy(&flag, ws.S.errorFlag, sizeof(flag), cudaMemcpyDeviceToHost);
+        if (flag) {
+            cudaMemset(ws.S.barrier, 0, 2 * sizeof(unsigned int));
+            cudaMemset(ws.S.errorFlag, 0, sizeof(uint32_t));
+            return BP_E_TIMEOUT;
+        }
+    }
+    if (err) return cuda_status(err);
+    ws.bubbleSubsteps += total;
+    if (reports && !perStepReports)
+        for (uint32_t w = 0; w < ws.nWorlds; ++w)
+            if (reports[w].status != BP_OK && status == BP_OK) status = reports[w].status;
+    return status;
+}
+
+int read_bubbles(WorldSet& ws, uint32_t world, bp_bubble* out, uint32_t capacity, uint32_t* count) {
+    if (world >= ws.nWorlds) return BP_E_INVALID;
+    const DWorld& W = ws.hWorlds[world];
+    if (count) *count = W.n;
+    if (!out) return BP_OK;
+    DeviceGuard guard(ws.ctx->device);
+    uint32_t m = std::min(W.n, capacity);
+    std::vector<float2> pos(m), start(m), vel(m), rotw(m);
+    std::vector<uint32_t> result(m), flags(m);
+    cudaError_t err = cudaSuccess;
+    if (m) {
+        err = cudaMemcpy(pos.data(), ws.S.pPos + W.boff, m * 8, cudaMemcpyDeviceToHost);
+        if (!err) err = cudaMemcpy(start.data(), ws.S.pStart + W.boff, m * 8, cudaMemcpyDeviceToHost);
+        if (!err) err = cudaMemcpy(vel.data(), ws.S.pVel + W.boff, m * 8, cudaMemcpyDeviceToHost);
+        if (!err) err = cudaMemcpy(rotw.data(), ws.S.pRotw + W.boff, m * 8, cudaMemcpyDeviceToHost);
+        if (!err) err = cudaMemcpy(result.data(), ws.S.pResult + W.boff, m * 4, cudaMemcpyDeviceToHost);
+        if (!err) err = cudaMemcpy(flags.data(), ws.S.pFlags + W.boff, m * 4, cudaMemcpyDeviceToHost);
+    }
+    if (err) return cuda_status(err);
+    for (uint32_t i = 0; i < m; ++i) {
+        bp_bubble b = ws.hBubbles[W.boff + i];
+        b.center[0] = pos[i].x; b.center[1] = pos[i].y;
+        b.previous_center[0] = start[i].x; b.previous_center[1] = start[i].y;
+        b.velocity[0] = vel[i].x; b.velocity[1] = vel[i].y;
+        b.rotation = rotw[i].x; b.angular_velocity = rotw[i].y;
+        b.region_result = result[i];
+        b.flags = flags[i] & 0xffu;
+        out[i] = b;
+    }
+    return BP_OK;
+}
+
+}  // namespace
+
+// ================================================================================================================
+// C ABI
+// ================================================================================================================
+extern "C" {
+
+int bp_abi_version(void) { return BP_ABI_VERSION; }
+
+const char* bp_status_string(int status) {
+    switch (status) {
+        case BP_OK: return "ok";
+        case BP_E_INVALID: return "invalid snapshot";
+        case BP_E_SUBSTEP_LIMIT: return "substep limit exceeded";
+        case BP_E_NONFINITE: return "non-finite values";
+        case BP_E_CONTACT_VIOLATION: return "contact violation";
+        case BP_E_INFLIGHT: return "frame in flight";
+        case BP_E_TIMEOUT: return "bounded device wait timed out";
+        case BP_E_CUDA: return "CUDA command failed";
+        case BP_E_CAPACITY: return "capacity overflow";
+        case BP_E_UNAVAILABLE: return "CUDA device unavailable";
+        case BP_E_ALLOC: return "allocation failed";
+        case BP_E_WORLD_FAILED: return "world failed in an earlier step";
+        default: return "unknown status";
+    }
+}
+
+int bp_device_available(int device) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) return BP_E_UNAVAILABLE;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return BP_E_UNAVAILABLE;
+    return prop.major >= 10 ? BP_OK : BP_E_UNAVAILABLE;
+}
+
+int bp_context_create(int device, uint32_t flags, bp_context** out) {
+    (void)flags;
+    if (!out) return BP_E_INVALID;
+    int st = bp_device_available(device);
+    if (st != BP_OK) return st;
+    DeviceGuard guard(device);
+    bp_context* c = new (std::nothrow) bp_context();
+    if (!c) return BP_E_ALLOC;
+    c->device = device;
+    cudaError_t err = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (!err) err = cudaEventCreate(&c->start);
+    if (!err) err = cudaEventCreate(&c->stop);
+    if (!err) err = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
+    if (err) { delete c; return cuda_status(err); }
+    prepare_kernels();
+    *out = c;
+    return BP_OK;
+}
+
+int bp_context_destroy(bp_context* c) {
+    if (!c) return BP_OK;
+    DeviceGuard guard(c->device);
+    cudaStreamSynchronize(c->stream);
+    cudaEventDestroy(c->start);
+    cudaEventDestroy(c->stop);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return BP_OK;
+}
+
+int bp_world_create(bp_context* context, const bp_world_desc* desc, const bp_world_input* input, bp_world** out) {
+    if (!context || !desc || !input || !out) return BP_E_INVALID;
+    bp_world* w = new (std::nothrow) bp_world();
+    if (!w) return BP_E_ALLOC;
+    int st = build_set(w->set, context, 1, desc, input, true);
+    if (st != BP_OK) { delete w; return st; }
+    w->set.fixedThreads = 0;
+    *out = w;
+    return BP_OK;
+}
+
+int bp_world_destroy(bp_world* world) {
+    if (!world) return BP_OK;
+    DeviceGuard guard(world->set.ctx->device);
+    cudaStreamSynchronize(world->set.ctx->stream);
+    delete world;
+    return BP_OK;
+}
+
+int bp_world_write_bubbles(bp_world* world, const bp_bubble* bubbles, uint32_t count) {
+    if (!world || (!bubbles && count)) return BP_E_INVALID;
+    WorldSet& ws = world->set;
+    if (count != ws.hWorlds[0].n) return BP_E_INVALID;
+    for (uint32_t i = 0; i < count; ++i)
+        if (bubbles[i].id != ws.hBubbles[i].id) return BP_E_INVALID;
+    DeviceGuard guard(ws.ctx->device);
+    std::vector<float2> pos(count), start(count), vel(count), rotw(count);
+    std::vector<float4> phys(count);
+    std::vector<uint32_t> flags(count);
+    std::vector<uint2> filter(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        const bp_bubble& b = bubbles[i];
+        pos[i] = make_float2(b.center[0], b.center[1]);
+        start[i] = make_float2(b.previous_center[0], b.previous_center[1]);
+        vel[i] = make_float2(b.velocity[0], b.velocity[1]);
+        rotw[i] = make_float2(b.rotation, b.angular_velocity);
+        phys[i] = make_float4(b.radius, b.inverse_mass, b.contact_stiffness, b.damping);
+        flags[i] = b.flags & 0xffu;
+        filter[i] = make_uint2(b.category, b.mask);
+        ws.hBubbles[i] = b;
+    }
+    cudaStream_t st = ws.ctx->stream;
+    cudaError_t err = upload(ws.S.pos, pos.data(), count, st);
+    if (!err) err = upload(ws.S.pPos, pos.data(), count, st);
+    if (!err) err = upload(ws.S.start, start.data(), count, st);
+    if (!err) err = upload(ws.S.pStart, start.data(), count, st);
+    if (!err) err = upload(ws.S.vel, vel.data(), count, st);
+    if (!err) err = upload(ws.S.pVel, vel.data(), count, st);
+    if (!err) err = upload(ws.S.rotw, rotw.data(), count, st);
+    if (!err) err = upload(ws.S.pRotw, rotw.data(), count, st);
+    if (!err) err = upload(ws.S.phys, phys.data(), count, st);
+    if (!err) err = upload(ws.S.flags, flags.data(), count, st);
+    if (!err) err = upload(ws.S.pFlags, flags.data(), count, st);
+    if (!err) err = upload((uint2*)ws.S.filter, filter.data(), count, st);
+    if (!err) err = cudaMemsetAsync(ws.S.failed, 0, sizeof(uint32_t), st);
+    if (!err) err = cudaStreamSynchronize(st);
+    return cuda_status(err);
+}
+
+int bp_world_set_diagnostics(bp_world* world, const bp_world_diagnostics* d) {
+    if (!world || !d) return BP_E_INVALID;
+    WorldSet& ws = world->set;
+    ws.hWorlds[0].injectSubstep = d->inject_substep;
+    ws.hWorlds[0].injectPos = make_float2(d->inject_position[0], d->inject_position[1]);
+    DeviceGuard guard(ws.ctx->device);
+    cudaError_t err = upload(ws.dWorlds, ws.hWorlds.data(), 1, ws.ctx->stream);
+    if (!err) err = cudaStreamSynchronize(ws.ctx->stream);
+    return cuda_status(err);
+}
+
+int bp_world_step(bp_world* world, uint32_t steps, bp_step_report* reports) {
+    if (!world) return BP_E_INVALID;
+    WorldSet& ws = world->set;
+    std::vector<bp_step_report> local(steps ? steps : 1);
+    bp_step_report* out = reports ? reports : local.data();
+    std::memset(out, 0, sizeof(bp_step_report) * steps);
+    DeviceGuard guard(ws.ctx->device);
+    cudaStream_t st = ws.ctx->stream;
+    int status = BP_OK;
+    for (uint32_t s = 0; s < steps; ++s) {
+        cudaEventRecord(ws.ctx->start, st);
+        cudaError_t err = launch_step(ws, true);
+        cudaEventRecord(ws.ctx->stop, st);
+        if (err) return cuda_status(err);
+        int rs = read_reports(ws, out + s, 1);
+        if (rs) return rs;
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, ws.ctx->start, ws.ctx->stop);
+        out[s].gpu_ms = ms;
+        uint32_t flag = 0;
+        cudaMemcpy(&flag, ws.S.errorFlag, sizeof(flag), cudaMemcpyDeviceToHost);
+        if (flag) {
+            out[s].status = BP_E_TIMEOUT;
+            cudaMemset(ws.S.barrier, 0, 2 * sizeof(unsigned int));
+            cudaMemset(ws.S.errorFlag, 0, sizeof(uint32_t));
+            return BP_E_TIMEOUT;
+        }
+        ws.bubbleSubsteps += (uint64_t)out[s].substep_count * ws.hWorlds[0].n;
+        status = out[s].status;
+        if (status != BP_OK) break;
+    }
+    return status;
+}
+
+int bp_world_read_bubbles(bp_world* world, bp_bubble* out, uint32_t capacity, uint32_t* count) {
+    if (!world) return BP_E_INVALID;
+    return read_bubbles(world->set, 0, out, capacity, count);
+}
+
+int bp_world_read_contacts(bp_world* world, bp_contact* out, uint32_t capacity, uint32_t* count) {
+    if (!world) return BP_E_INVALID;
+    WorldSet& ws = world->set;
+    DeviceGuard guard(ws.ctx->device);
+    uint32_t c = 0;
+    cudaError_t err = cudaMemcpy(&c, ws.S.contactCount, sizeof(c), cudaMemcpyDeviceToHost);
+    if (err) return cuda_status(err);
+    if (count) *count = c;
+    if (!out) return BP_OK;
+    uint32_t m = std::min(c, capacity);
+    std::vector<DContact> rec(m);
+    if (m) err = cudaMemcpy(rec.data(), ws.S.contacts + ws.hWorlds[0].contactOff, m * sizeof(DContact), cudaMemcpyDeviceToHost);
+    if (err) return cuda_status(err);
+    for (uint32_t q = 0; q < m; ++q) {
+        bp_contact& o = out[q];
+        std::memset(&o, 0, sizeof(o));
+        const DContact& r = rec[q];
+        o.participants[0] = ws.hBubbles[r.a].id;
+        o.participants[1] = r.kind == 0 ? ws.hBubbles[r.other].id : ws.hSegIds[ws.hWorlds[0].soff + r.other];
+        o.kind = r.kind;
+        o.feature = r.feature;
+        o.normal[0] = r.normal.x; o.normal[1] = r.normal.y;
+        o.point[0] = r.point.x; o.point[1] = r.point.y;
+        o.impulse = r.impulse;
+        o.penetration = r.penetration;
+        o.allowed_side = r.allowed;
+    }
+    return BP_OK;
+}
+
+int bp_world_read_candidates(bp_world* world, bp_candidate_key* out, uint32_t capacity, uint32_t* count) {
+    if (!world) return BP_E_INVALID;
+    WorldSet& ws = world->set;
+    const DWorld& W = ws.hWorlds[0];
+    DeviceGuard guard(ws.ctx->device);
+    std::vector<uint32_t> rows((uint64_t)W.n * W.k), brows((uint64_t)W.nb * W.k), btotal(W.nb), flags(W.n);
+    std::vector<uint2> cc(W.n);
+    cudaError_t err = cudaSuccess;
+    if (W.n) err = cudaMemcpy(rows.data(), ws.S.candRow + W.rowOff, rows.size() * 4, cudaMemcpyDeviceToHost);
+    if (!err && W.n) err = cudaMemcpy(cc.data(), ws.S.candCount + W.boff, W.n * sizeof(uint2), cudaMemcpyDeviceToHost);
+    if (!err && W.n) err = cudaMemcpy(flags.data(), ws.S.flags + W.boff, W.n * 4, cudaMemcpyDeviceToHost);
+    if (!err && W.nb) err = cudaMemcpy(brows.data(), ws.S.bodyRow + W.bodyRowOff, brows.size() * 4, cudaMemcpyDeviceToHost);
+    if (!err && W.nb) err = cudaMemcpy(btotal.data(), ws.S.bodyTotal + W.bodyOff, W.nb * 4, cudaMemcpyDeviceToHost);
+    if (err) return cuda_status(err);
+    std::vector<bp_candidate_key> keys;
+    for (uint32_t i = 0; i < W.n; ++i) {
+        if (flags[i] & kRemoved) continue;
+        for (uint32_t e = 0; e < cc[i].x + cc[i].y; ++e) {
+            uint32_t v = rows[(uint64_t)i * W.k + e];
+            if (e < cc[i].x) keys.push_back({0u, 0u, ws.hBubbles[i].id, ws.hBubbles[v].id});
+            else keys.push_back({1u, 0u, ws.hBubbles[i].id, ws.hSegIds[W.soff + (v & kIndexMask)]});
+        }
+    }
+    for (uint32_t b = 0; b < W.nb; ++b)
+        for (uint32_t e = 0; e < std::min(btotal[b], W.k); ++e)
+            keys.push_back({2u, 0u, ws.hBubbles[brows[(uint64_t)b * W.k + e]].id, ws.hBodyIds[W.bodyOff + b]});
+    std::sort(keys.begin(), keys.end(), [](const bp_candidate_key& a, const bp_candidate_key& b) {
+        if (a.kind != b.kind) return a.kind < b.kind;
+        if (a.first != b.first) return a.first < b.first;
+        return a.second < b.second;
+    });
+    if (count) *count = (uint32_t)keys.size();
+    if (out)
+        for (uint32_t q = 0; q < keys.size() && q < capacity; ++q) out[q] = keys[q];
+    return BP_OK;
+}
+
+int bp_world_read_cells(bp_world* world, int64_t* out, uint32_t capacity, uint32_t* count) {
+    if (!world) return BP_E_INVALID;
+    WorldSet& ws = world->set;
+    const DWorld& W = ws.hWorlds[0];
+    if (count) *count = W.n;
+    if (!out) return BP_OK;
+    DeviceGuard guard(ws.ctx->device);
+    uint32_t m = std::min(W.n, capacity);
+    cudaError_t err = m ? cudaMemcpy(out, ws.S.cell + W.boff, m * sizeof(longlong2), cudaMemcpyDeviceToHost) : cudaSuccess;
+    return cuda_status(err);
+}
+
+int bp_world_read_substeps(bp_world* world, float* out, uint32_t capacity, uint32_t* count) {
+    if (!world) return BP_E_INVALID;
+    WorldSet& ws = world->set;
+    DeviceGuard guard(ws.ctx->device);
+    bp_step_report rep;
+    int st = read_reports(ws, &rep, 1);
+    if (st) return st;
+    uint32_t n = std::min<uint32_t>(rep.substep_count, kFrameLimit);
+    if (count) *count = n;
+    if (!out) return BP_OK;
+    cudaError_t err = cudaMemcpy(out, ws.S.history, std::min(n, capacity) * sizeof(float), cudaMemcpyDeviceToHost);
+    return cuda_status(err);
+}
+
+// ---- batch ----------------------------------------------------------------------------------------------------
+
+int bp_batch_create(bp_context* context, uint32_t world_count, const bp_world_desc* descs, const bp_world_input* inputs,
+                    const bp_batch_config* config, bp_batch** out) {
+    if (!context || !descs || !inputs || !out || world_count == 0) return BP_E_INVALID;
+    bp_batch* b = new (std::nothrow) bp_batch();
+    if (!b) return BP_E_ALLOC;
+    int st = build_set(b->set, context, world_count, descs, inputs, false);
+    if (st != BP_OK) { delete b; return st; }
+    if (config) {
+        b->set.flags = config->flags;
+        if (config->threads_per_world) {
+            uint32_t t = config->threads_per_world;
+            if (t % 32u || t > 1024u) { delete b; return BP_E_INVALID; }
+            b->set.fixedThreads = t;
+        }
+    }
+    *out = b;
+    return BP_OK;
+}
+
+int bp_batch_destroy(bp_batch* batch) {
+    if (!batch) return BP_OK;
+    DeviceGuard guard(batch->set.ctx->device);
+    cudaStreamSynchronize(batch->set.ctx->stream);
+    delete batch;
+    return BP_OK;
+}
+
+int bp_batch_step(bp_batch* batch, uint32_t steps, bp_step_report* reports) {
+    if (!batch) return BP_E_INVALID;
+    WorldSet& ws = batch->set;
+    bool perWorld = (ws.flags & BP_BATCH_PER_WORLD_LAUNCH) != 0;
+    bool graph = (ws.flags & BP_BATCH_USE_GRAPH) != 0;
+    int st = step_set(ws, steps, reports, perWorld, graph, false);
+    return st;
+}
+
+int bp_batch_counters(bp_batch* batch, uint64_t* bubble_count, uint64_t* bubble_substeps, uint64_t* launches) {
+    if (!batch) return BP_E_INVALID;
+    if (bubble_count) *bubble_count = batch->set.totalBubbles;
+    if (bubble_substeps) *bubble_substeps = batch->set.bubbleSubsteps;
+    if (launches) *launches = batch->set.launches;
+    return BP_OK;
+}
+
+int bp_batch_read_bubbles(bp_batch* batch, uint32_t world, bp_bubble* out, uint32_t capacity, uint32_t* count) {
+    if (!batch) return BP_E_INVALID;
+    return read_bubbles(batch->set, world, out, capacity, count);
+}
+
+int bp_batch_write_state(bp_batch* batch, const float* cv, uint64_t bubble_count) {
+    if (!batch || !cv) return BP_E_INVALID;
+    WorldSet& ws = batch->set;
+    if (bubble_count != ws.totalBubbles) return BP_E_INVALID;
+    DeviceGuard guard(ws.ctx->device);
+    cudaError_t err = cudaSuccess;
+    if (!ws.dStaging) ws.dStaging = ws.alloc<float4>(ws.totalBubbles, err);
+    if (!err) err = cudaMemcpyAsync(ws.dStaging, cv, bubble_count * sizeof(float4), cudaMemcpyHostToDevice, ws.ctx->stream);
+    if (!err) err = launch_write_state(ws.dStaging, ws.S.pos, ws.S.vel, ws.S.pPos, ws.S.pVel, bubble_count, ws.ctx->stream);
+    return cuda_status(err);
+}
+
+int bp_batch_read_state(bp_batch* batch, float* cv, uint64_t bubble_count) {
+    if (!batch || !cv) return BP_E_INVALID;
+    WorldSet& ws = batch->set;
+    if (bubble_count != ws.totalBubbles) return BP_E_INVALID;
+    DeviceGuard guard(ws.ctx->device);
+    cudaError_t err = cudaSuccess;
+    if (!ws.dStaging) ws.dStaging = ws.alloc<float4>(ws.totalBubbles, err);
+    if (!err) err = launch_read_state(ws.dStaging, ws.S.pPos, ws.S.pVel, bubble_count, ws.ctx->stream);
+    if (!err) err = cudaMemcpyAsync(cv, ws.dStaging, bubble_count * sizeof(float4), cudaMemcpyDeviceToHost, ws.ctx->stream);
+    if (!err) err = cudaStreamSynchronize(ws.ctx->stream);
+    return cuda_status(err);
+}
+
+int bp_batch_tuning(bp_batch* batch, uint32_t* threads, uint32_t class_count) {
+    if (!batch || !threads) return BP_E_INVALID;
+    for (uint32_t c = 0; c < class_count && c < kClasses; ++c)
+        threads[c] = batch->set.fixedThreads ? batch->set.fixedThreads : batch->set.classThreads[c];
+    return BP_OK;
+}
+
+// ---- host helpers ----------------------------------------------------------------------------------------------
+
+// NativeStaticPolygonEdges.segments (NativeStaticPolygonEdges.swift:16-72): signed area and collinear merge in double.
+int bp_static_polygon_edges(const float* xy, uint32_t count, int64_t first_id, int64_t owner_id, uint32_t has_owner,
+                            bp_segment* out, uint32_t capacity, uint32_t* out_count) {
+    if (!xy && count) return BP_E_INVALID;
+    struct P { float x, y; };
+    std::vector<P> pts(count);
+    for (uint32_t i = 0; i < count; ++i) pts[i] = {xy[2 * i], xy[2 * i + 1]};
+    auto crossd = [](P u, P v) { return (double)u.x * (double)v.y - (double)u.y * (double)v.x; };
+    auto subp = [](P a, P b) { return P{a.x - b.x, a.y - b.y}; };
+    double area = 0.0;
+    if (count >= 3)
+        for (uint32_t i = 1; i + 1 < count; ++i) area += crossd(subp(pts[i], pts[0]), subp(pts[i + 1], pts[0]));
+    auto segment = [&](int64_t id, P a, P b) {
+        bp_segment s;
+        std::memset(&s, 0, sizeof(s));
+        s.id = id;
+        s.owner_id = has_owner ? owner_id : 0;
+        s.a[0] = a.x; s.a[1] = a.y; s.b[0] = b.x; s.b[1] = b.y;
+        s.flags = has_owner ? BP_SEGMENT_HAS_OWNER : 0u;
+        s.category = 1u;
+        s.mask = 0xffffffffu;
+        return s;
+    };
+    std::vector<bp_segment> result;
+    if (count < 3 || area == 0.0) {
+        for (uint32_t i = 0; i < count; ++i) result.push_back(segment(first_id + i, pts[i], pts[(i + 1) % count]));
+    } else {
+        std::vector<P> ring = pts;
+        bool removedAny = true;
+        while (removedAny && ring.size() > 3) {
+            removedAny = false;
+            size_t index = 0;
+            while (index < ring.size() && ring.size() > 3) {
+                size_t c = ring.size();
+                P incoming = subp(ring[index], ring[(index + c - 1) % c]), outgoing = subp(ring[(index + 1) % c], ring[index]);
+                double lengths = (double)std::sqrt(incoming.x * incoming.x + incoming.y * incoming.y) *
+                                 (double)std::sqrt(outgoing.x * outgoing.x + outgoing.y * outgoing.y);
+                double dt = (double)incoming.x * (double)outgoing.x + (double)incoming.y * (double)outgoing.y;
+                if (lengths > 0 && dt > 0 && std::fabs(crossd(incoming, outgoing)) <= 1e-5 * lengths) {
+                    ring.erase(ring.begin() + index);
+                    removedAny = true;
+                } else {
+                    ++index;
+                }
+            }
+        }
+        double orientation = area > 0 ? 1.0 : -1.0;
+        size_t c = ring.size();
+        for (size_t index = 0; index < c; ++index) {
+            P previous = ring[(index + c - 1) % c], a = ring[index], b = ring[(index + 1) % c], next = ring[(index + 2) % c];
+            bp_segment s = segment(first_id + (int64_t)index, a, b);
+            bool convexStart = crossd(subp(a, previous), subp(b, a)) * orientation > 0;
+            bool convexEnd = crossd(subp(b, a), subp(next, b)) * orientation > 0;
+            s.flags |= BP_SEGMENT_POLYGON_EDGE | (convexStart ? BP_SEGMENT_CONVEX_START : 0u) | (convexEnd ? BP_SEGMENT_CONVEX_END : 0u);
+            s.outward_sign = area > 0 ? -1.0f : 1.0f;
+            s.previous_start[0] = previous.x;
+            s.previous_start[1] = previous.y;
+            result.push_back(s);
+        }
+    }
+    if (out_count) *out_count = (uint32_t)result.size();
+    if (out)
+        for (uint32_t q = 0; q < result.size() && q < capacity; ++q) out[q] = result[q];
+    return result.size() > capacity && out ? BP_E_CAPACITY : BP_OK;
+}
+
+int bp_device_contact_law(bp_context* context, uint32_t mode, const float* in, float* out, uint32_t count) {
+    if (!context || (!in && count) || (!out && count) || mode > 2) return BP_E_INVALID;
+    DeviceGuard guard(context->device);
+    float *dIn = nullptr, *dOut = nullptr;
+    size_t bytes = (size_t)std::max<uint32_t>(count, 1) * 8 * sizeof(float);
+    cudaError_t err = cudaMalloc(&dIn, bytes);
+    if (!err) err = cudaMalloc(&dOut, bytes);
+    if (!err && count) err = cudaMemcpyAsync(dIn, in, (size_t)count * 8 * sizeof(float), cudaMemcpyHostToDevice, context->stream);
+    if (!err) err = launch_contact_law(mode, dIn, dOut, count, context->stream);
+    if (!err && count) err = cudaMemcpyAsync(out, dOut, (size_t)count * 8 * sizeof(float), cudaMemcpyDeviceToHost, context->stream);
+    if (!err) err = cudaStreamSynchronize(context->stream);
+    if (dIn) cudaFree(dIn);
+    if (dOut) cudaFree(dOut);
+    return cuda_status(err);
+}
+
+}  // extern "C"

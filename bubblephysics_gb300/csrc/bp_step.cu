@@ -1,0 +1,1117 @@
+// bp_step.cu - the bubble step on sm_103a.
+//
+// One world is stepped by one "team": a thread block (batches of small and medium worlds, one block per world, all
+// worlds of a batch in one launch) or the whole grid of a cooperative launch (one large world). The team runs the
+// complete step of the reference's single-group kernel nativeSubstepLoopSingleGroup (NFK:1236-1307) - broadphase,
+// initial forces, the adaptive substep loop with in-step grid rebuilds, and the end-of-step work - so a batch costs
+// one launch per step whatever the substep counts of its worlds are.
+//
+// Per-bubble arithmetic follows NFK / NGK operation order exactly; reductions pick the largest / smallest value with
+// the lower bubble index winning ties, which is order-independent, so every team shape gives bit-identical results.
+#include "bp_team.cuh"
+
+namespace bp {
+
+constexpr uint32_t kValid = 0x40000000u;  // bubble is in the grid of the current build
+constexpr uint32_t kLive = 0xffu;         // mask of the public flags
+
+struct Ctl {  // NativeSubstepControl (NFK:22-26), kept identical in every thread of the team
+    float timeX, timeY, timeZ, timeW;
+    uint32_t cX, cY, cZ, cW;
+    int64_t limObj;
+    uint32_t limTerm;
+};
+
+__device__ __forceinline__ uint32_t grid_hash(long long cx, long long cy, uint32_t buckets) {
+    return ((uint32_t)cx * 73856093u ^ (uint32_t)cy * 19349663u) & (buckets - 1u);
+}
+
+__device__ __forceinline__ bool removed(const DState& S, uint32_t g) { return (S.flags[g] & kRemoved) != 0u; }
+// nativeIsStatic / nativeInverseMass / nativeIsForceDriven / nativeEffectiveVelocity, NFK:388-392
+__device__ __forceinline__ bool is_static(uint32_t flags, float invMass) {
+    return !(invMass > 0.0f) || ((flags & BP_BUBBLE_ENABLED) && (flags & BP_BUBBLE_STATIC));
+}
+__device__ __forceinline__ float inv_mass(const DState& S, uint32_t g) {
+    float im = S.phys[g].y;
+    return is_static(S.flags[g], im) ? 0.0f : im;
+}
+__device__ __forceinline__ float2 eff_vel(const DState& S, uint32_t g) {
+    return is_static(S.flags[g], S.phys[g].y) ? f2(0.0f, 0.0f) : S.vel[g];
+}
+
+// nativeJointExcluded, NGK:254-258 (entity: bubble index, or bubble count + body index)
+__device__ __forceinline__ bool joint_excluded(const DState& S, const DWorld& W, uint32_t entity, int64_t partner) {
+    if (entity >= W.njEnt) return false;
+    uint2 r = S.jranges[W.jrOff + entity];
+    for (uint32_t i = 0; i < r.y; ++i)
+        if (S.jpartners[r.x + i] == partner) return true;
+    return false;
+}
+
+// Field force (nativeFieldForce, NFK:395-409)
+__device__ float2 field_force(const DState& S, const DField& f, float2 point) {
+    float2 delta = sub(point, f.pos);
+    float c = f.cosr, s = f.sinr;
+    float2 local = f2(c * delta.x + s * delta.y, -s * delta.x + c * delta.y);
+    float distance = len2(local), radius = f.radius;
+    if (f.vcount == 0u) {
+        if (!(distance <= radius)) return f2(0.0f, 0.0f);
+    } else {
+        bool inside = false;
+        for (uint32_t i = 0; i < f.vcount; ++i) {
+            float2 a = S.fverts[f.voff + i], b = S.fverts[f.voff + (i + 1) % f.vcount];
+            if ((a.y > local.y) != (b.y > local.y) && local.x < (b.x - a.x) * (local.y - a.y) / (b.y - a.y) + a.x) inside = !inside;
+        }
+        if (!inside) return f2(0.0f, 0.0f);
+    }
+    if (f.kind == 0u) return f2(c * f.dir.x - s * f.dir.y, s * f.dir.x + c * f.dir.y);
+    if (!(distance > 0.0f)) return f2(0.0f, 0.0f);
+    float profile = f.falloff == 0.0f ? 1.0f : powf(fmaxf(0.0f, 1.0f - distance / radius), f.falloff);
+    float scale = f.strength * profile / distance;
+    return f.kind == 2u ? mul(f2(-delta.y, delta.x), scale) : mul(delta, scale);
+}
+__device__ bool field_affects(const DState& S, const DField& f, int64_t id) {
+    if (!f.hasFilter) return true;
+    uint32_t low = f.foff, end = f.foff + f.fcount, high = end;
+    while (low < high) {
+        uint32_t mid = low + (high - low) / 2;
+        if (S.fids[mid] < id) low = mid + 1; else high = mid;
+    }
+    return low < end && S.fids[low] == id;
+}
+template <class R> __device__ const R* find_by_bubble(const R* v, uint32_t count, int64_t id) {
+    uint32_t low = 0, high = count;
+    while (low < high) {
+        uint32_t mid = low + (high - low) / 2;
+        if (v[mid].bubble_id < id) low = mid + 1; else high = mid;
+    }
+    return low < count && v[low].bubble_id == id ? v + low : nullptr;
+}
+// nativeNonContactAcceleration, NFK:450-470, plus the world's gravity acceleration
+__device__ float2 non_contact_acc(const DState& S, const DWorld& W, uint32_t g, float2 position) {
+    float im = inv_mass(S, g);
+    if (!(S.flags[g] & BP_BUBBLE_FORCE_DRIVEN) || !(im > 0.0f)) return f2(0.0f, 0.0f);
+    float2 force = W.gforce;
+    int64_t id = S.id[g];
+    for (uint32_t i = 0; i < W.nf; ++i) {
+        DField f = S.fields[W.foff + i];
+        if (field_affects(S, f, id)) force = add(force, field_force(S, f, position));
+    }
+    if (W.nbands) {
+        const bp_band* band = find_by_bubble(S.bands + W.bandOff, W.nbands, id);
+        if (band) {
+            float2 bf = mul(sub(f2(band->target[0], band->target[1]), position), band->stiffness);
+            float lim = band->maximum_force, magnitude = len2(bf);
+            if (lim > 0.0f && magnitude > lim) bf = mul(bf, lim / magnitude);
+            force = add(force, bf);
+        }
+    }
+    if (W.nmotors) {
+        const bp_motor* motor = find_by_bubble(S.motors + W.motorOff, W.nmotors, id);
+        if (motor) force = add(force, f2(motor->force[0], motor->force[1]));
+    }
+    float2 a = mul(force, im);
+    if (W.gravity.x != 0.0f || W.gravity.y != 0.0f) a = add(a, W.gravity);
+    return a;
+}
+
+// ------------------------------------------------------------------------------------------------------------------
+// Per-bubble substep terms (NFK:216-243, 510-614)
+// ------------------------------------------------------------------------------------------------------------------
+__device__ __forceinline__ const uint32_t* adj_row(const DState& S, const DWorld& W, uint32_t i) {
+    return S.adj + W.rowOff + (uint64_t)i * W.k;
+}
+
+__device__ float2 contact_force(const DState& S, const DWorld& W, uint32_t i, float fraction) {
+    const uint32_t g = W.boff + i;
+    float2 total = f2(0.0f, 0.0f);
+    const float2 p = S.pos[g];
+    const float4 ph = S.phys[g];
+    const uint32_t* row = adj_row(S, W, i);
+    const uint32_t d = S.deg[g];
+    for (uint32_t e = 0; e < d; ++e) {
+        uint32_t entry = row[e], kind = entry >> kKindShift, j = entry & kIndexMask;
+        if (kind == 0u) {
+            uint32_t low = min(i, j), high = max(i, j);
+            uint32_t gl = W.boff + low, gh = W.boff + high;
+            float2 delta = sub(S.pos[gh], S.pos[gl]);
+            float dist = len2(delta);
+            float2 normal = dist > 0.0f ? dvd(delta, dist) : f2(1.0f, 0.0f);
+            float4 pl = S.phys[gl], phh = S.phys[gh];
+            Law law = pair_law(pl.z, pl.x, phh.z, phh.x, dist);
+            total = add(total, mul(normal, i == low ? -law.force : law.force));
+        } else if (kind == 1u) {
+            float2 normal;
+            float dist;
+            if (!wall_region(S.seg[W.soff + j], p, normal, dist) || !(dist < ph.x)) continue;
+            total = add(total, mul(normal, wall_law(ph.z, ph.x, dist).force));
+        } else {
+            Obstacle o = body_obstacle(S.bverts, S.btris, S.body[W.bodyOff + j], fraction, p);
+            total = add(total, mul(o.normal, wall_law(ph.z, ph.x, o.distance).force));
+        }
+    }
+    return total;
+}
+
+__device__ float omega_squared(const DState& S, const DWorld& W, uint32_t i, float fraction) {
+    const uint32_t g = W.boff + i;
+    float im = inv_mass(S, g);
+    if (!(im > 0.0f)) return 0.0f;
+    const float2 p = S.pos[g];
+    const float4 ph = S.phys[g];
+    float total = 0.0f;
+    if (W.nbands) {
+        const bp_band* band = find_by_bubble(S.bands + W.bandOff, W.nbands, S.id[g]);
+        if (band) total = total + band->stiffness * im;
+    }
+    const uint32_t* row = adj_row(S, W, i);
+    const uint32_t d = S.deg[g];
+    for (uint32_t e = 0; e < d; ++e) {
+        uint32_t entry = row[e], kind = entry >> kKindShift, j = entry & kIndexMask;
+        if (kind == 0u) {
+            uint32_t low = min(i, j), high = max(i, j);
+            uint32_t gl = W.boff + low, gh = W.boff + high;
+            float dist = len2(sub(S.pos[gh], S.pos[gl]));
+            float4 pl = S.phys[gl], phh = S.phys[gh];
+            Law law = pair_law(pl.z, pl.x, phh.z, phh.x, dist);
+            total = total + law.stiffness * (im + sqrtf(im * inv_mass(S, W.boff + j)));
+        } else if (kind == 1u) {
+            float2 normal;
+            float dist;
+            if (!wall_region(S.seg[W.soff + j], p, normal, dist) || !(dist < ph.x)) continue;
+            total = total + wall_law(ph.z, ph.x, dist).stiffness * im;
+        } else {
+            Obstacle o = body_obstacle(S.bverts, S.btris, S.body[W.bodyOff + j], fraction, p);
+            total = total + wall_law(ph.z, ph.x, o.distance).stiffness * im;
+        }
+    }
+    return total;
+}
+
+__device__ float distance_bound(const DState& S, const DWorld& W, uint32_t i, float hMax, float fraction) {
+    const uint32_t g = W.boff + i;
+    const float inf = __int_as_float(0x7f800000);
+    if (!(inv_mass(S, g) > 0.0f)) return inf;
+    const float2 p = S.pos[g], velocity = S.vel[g];
+    const float radius = S.phys[g].x;
+    const float accSelf = len2(S.acc[g]);
+    float best = inf;
+    const uint32_t* row = adj_row(S, W, i);
+    const uint32_t d = S.deg[g];
+    for (uint32_t e = 0; e < d; ++e) {
+        uint32_t entry = row[e], kind = entry >> kKindShift, j = entry & kIndexMask;
+        float dist, approach, accSum, reach, bodySpeed = 0.0f;
+        if (kind == 0u) {
+            uint32_t gj = W.boff + j;
+            float2 delta = sub(S.pos[gj], p);
+            dist = len2(delta);
+            float2 normal = dist > 0.0f ? dvd(delta, dist) : f2(1.0f, 0.0f);
+            approach = dot2(sub(velocity, eff_vel(S, gj)), normal);
+            accSum = accSelf + len2(S.acc[gj]);
+            reach = radius + S.phys[gj].x;
+        } else if (kind == 1u) {
+            float2 normal;
+            if (!wall_region(S.seg[W.soff + j], p, normal, dist)) continue;
+            approach = -dot2(velocity, normal);
+            accSum = accSelf;
+            reach = radius;
+        } else {
+            Obstacle o = body_obstacle(S.bverts, S.btris, S.body[W.bodyOff + j], fraction, p);
+            dist = o.distance;
+            approach = -dot2(velocity, o.normal);
+            bodySpeed = o.speedBound;
+            accSum = accSelf;
+            reach = radius;
+        }
+        bool active = dist < reach;
+        float dd = fmaxf(dist, reach * 1e-6f);
+        float speed;
+        if (active) speed = fabsf(approach) + bodySpeed;
+        else {
+            if (approach + bodySpeed + accSum * hMax * 0.5f <= 0.0f) continue;
+            speed = approach + bodySpeed;
+        }
+        float sq = sqrtf(speed * speed + accSum * dd * 0.5f);
+        float denominator = sq + speed;
+        if (!(denominator > 0.0f)) continue;
+        best = fminf(best, dd / (2.0f * denominator));
+    }
+    return best;
+}
+
+__device__ __forceinline__ float margin_bound(const DState& S, uint32_t g) {
+    const float inf = __int_as_float(0x7f800000);
+    if (!(inv_mass(S, g) > 0.0f)) return inf;
+    float left = S.margin[g] - len2(sub(S.pos[g], S.ref[g]));
+    if (isnan(left)) return inf;
+    if (left <= 0.0f) return 0.0f;
+    float speed = len2(S.vel[g]), a = len2(S.acc[g]);
+    float denominator = speed + sqrtf(speed * speed + 2.0f * a * left);
+    return denominator > 0.0f ? 2.0f * left / denominator : inf;
+}
+
+// ------------------------------------------------------------------------------------------------------------------
+// Broadphase pieces
+// ------------------------------------------------------------------------------------------------------------------
+// nativeBubblePairCandidate range test for the pair (low, high) in row `low` (NGK:262-273)
+__device__ __forceinline__ bool pair_accepts(const DState& S, const DWorld& W, uint32_t low, uint32_t high) {
+    uint32_t gl = W.boff + low, gh = W.boff + high;
+    if (!filter_accepts(S.filter[gl], S.filter[gh])) return false;
+    if (W.njEnt && joint_excluded(S, W, low, S.id[gh])) return false;
+    float reach = S.phys[gl].x + S.phys[gh].x + S.margin[gl] + S.margin[gh] + W.sepTol;
+    float2 a = S.pos[gl], b = S.pos[gh];
+    return fabsf(a.x - b.x) <= reach && fabsf(a.y - b.y) <= reach;
+}
+// segment rule of nativeFinishBubbleRow (NGK:279-290)
+__device__ __forceinline__ bool segment_accepts(const DState& S, const DWorld& W, uint32_t i, uint32_t sj) {
+    uint32_t g = W.boff + i;
+    const DSegment& sg = S.seg[W.soff + sj];
+    if (!filter_accepts(S.filter[g], make_uint2(sg.cat, sg.mask))) return false;
+    if ((sg.flags & BP_SEGMENT_HAS_OWNER) && W.njEnt && joint_excluded(S, W, i, sg.owner)) return false;
+    float reach = S.phys[g].x + S.margin[g] + W.sepTol;
+    float2 lower = sub(vmin2(sg.a, sg.b), f2(reach, reach));
+    float2 upper = add(vmax2(sg.a, sg.b), f2(reach, reach));
+    float2 p = S.pos[g];
+    return p.x >= lower.x && p.y >= lower.y && p.x <= upper.x && p.y <= upper.y;
+}
+// bubble obstacle rule of nativeEmitBodyCandidates (NGK:361-378)
+__device__ __forceinline__ bool body_is_obstacle(const DBody& b) {
+    return (b.flags & BP_BODY_STATIC) ? b.kind != BP_BODY_POLYGON : (b.flags & BP_BODY_KINEMATIC) != 0u;
+}
+__device__ __forceinline__ bool body_accepts(const DState& S, const DWorld& W, const DBody& b, uint32_t bi, uint32_t i) {
+    uint32_t g = W.boff + i;
+    if (!filter_accepts(S.filter[g], make_uint2(b.cat, b.mask))) return false;
+    if (W.njEnt && joint_excluded(S, W, W.n + bi, S.id[g])) return false;
+    float2 bodyLow = sub(vmin2(b.pos, b.prev), f2(b.radius, b.radius));
+    float2 bodyHigh = add(vmax2(b.pos, b.prev), f2(b.radius, b.radius));
+    float reach = S.phys[g].x + fmaxf(S.margin[g], 0.0f);
+    float2 c = S.pos[g];
+    float2 lo = sub(c, f2(reach, reach)), hi = add(c, f2(reach, reach));
+    return !(hi.x < bodyLow.x || hi.y < bodyLow.y || bodyHigh.x < lo.x || bodyHigh.y < lo.y);
+}
+
+// Insert `value` into a row kept sorted ascending with at most `limit` entries (nativeInsertCandidate, NGK:238-251).
+__device__ __forceinline__ void insert_sorted(uint32_t* row, uint32_t& count, uint32_t limit, uint32_t value) {
+    uint32_t loc;
+    if (count < limit) loc = count++;
+    else {
+        if (!(value < row[limit - 1])) return;
+        loc = limit - 1;
+    }
+    while (loc > 0 && value < row[loc - 1]) { row[loc] = row[loc - 1]; --loc; }
+    row[loc] = value;
+}
+
+__device__ __forceinline__ bool row_contains(const uint32_t* row, uint32_t count, uint32_t value) {
+    uint32_t low = 0, high = count;
+    while (low < high) {
+        uint32_t mid = (low + high) >> 1;
+        if (row[mid] < value) low = mid + 1; else high = mid;
+    }
+    return low < count && row[low] == value;
+}
+
+// Visits every bubble j registered in cell (tx, ty) of the hash grid.
+template <class F>
+__device__ __forceinline__ void for_each_in_cell(const longlong2* cells, const DWorld& W, const uint32_t* buckets,
+                                                 const uint32_t* entries, uint32_t B, long long tx, long long ty, F&& f) {
+    uint32_t h = grid_hash(tx, ty, B);
+    uint32_t begin = h == 0u ? 0u : buckets[h - 1], end = buckets[h];
+    for (uint32_t e = begin; e < end; ++e) {
+        uint32_t j = entries[e];
+        longlong2 c = cells[W.boff + j];
+        if (c.x == tx && c.y == ty) f(j);
+    }
+}
+
+// Forward candidate row of bubble i: pairs with j > i, then segments; k smallest keys (NGK:300-330).
+__device__ void emit_row(const DState& S, const DWorld& W, const uint32_t* buckets, const uint32_t* entries, uint32_t B,
+                         uint32_t i, uint32_t& overflow, uint32_t& maxPer) {
+    const uint32_t g = W.boff + i, k = W.k;
+    uint32_t* row = S.candRow + W.rowOff + (uint64_t)i * k;
+    if (!(S.flags[g] & kValid) || !finite2(S.start[g])) {
+        S.candCount[g] = make_uint2(0u, 0u);
+        S.pairTotal[g] = 0u;
+        return;
+    }
+    longlong2 c = S.cell[g];
+    uint32_t count = 0, total = 0;
+    for (int dx = -1; dx <= 1; ++dx)
+        for (int dy = -1; dy <= 1; ++dy)
+            for_each_in_cell(S.cell, W, buckets, entries, B, c.x + dx, c.y + dy, [&](uint32_t j) {
+                if (j <= i) return;
+                if (!pair_accepts(S, W, i, j)) return;
+                ++total;
+                insert_sorted(row, count, k, j);
+            });
+    const uint32_t pairs = count;
+    uint32_t segTotal = 0;
+    for (uint32_t sj = 0; sj < W.s; ++sj) {
+        if (!segment_accepts(S, W, i, sj)) continue;
+        ++segTotal;
+        if (count < k) row[count++] = (1u << kKindShift) | sj;
+    }
+    S.candCount[g] = make_uint2(pairs, count - pairs);
+    S.pairTotal[g] = total;
+    uint32_t all = total + segTotal;
+    overflow += all - count;
+    maxPer = max(maxPer, all);
+}
+
+// Body row of body bi built by one warp: the first k accepting bubbles in index order (NGK:350-392).
+__device__ void emit_body_row(const DState& S, const DWorld& W, uint32_t bi, uint32_t lane, uint32_t& overflow, uint32_t& maxPer) {
+    const DBody b = S.body[W.bodyOff + bi];
+    const uint32_t k = W.k;
+    uint32_t* row = S.bodyRow + W.bodyRowOff + (uint64_t)bi * k;
+    uint32_t total = 0;
+    if (body_is_obstacle(b)) {
+        for (uint32_t base = 0; base < W.n; base += 32) {
+            uint32_t i = base + lane;
+            bool hit = i < W.n && !removed(S, W.boff + i) && body_accepts(S, W, b, bi, i);
+            uint32_t mask = __ballot_sync(0xffffffffu, hit);
+            uint32_t rank = __popc(mask & ((1u << lane) - 1u));
+            if (hit && total + rank < k) row[total + rank] = i;
+            total += __popc(mask);
+        }
+    }
+    if (lane == 0) {
+        S.bodyTotal[W.bodyOff + bi] = total;
+        overflow += total > k ? total - k : 0u;
+        maxPer = max(maxPer, total);
+    }
+}
+
+// Adjacency row of bubble i, sorted by (kind, neighbour), first k kept (NFK:298-331, NCK:222-238).
+__device__ void build_adjacency(const DState& S, const DWorld& W, const uint32_t* buckets, const uint32_t* entries,
+                                uint32_t B, uint32_t i, uint32_t& overflow, uint32_t& maxPer) {
+    const uint32_t g = W.boff + i, k = W.k;
+    uint32_t* row = S.adj + W.rowOff + (uint64_t)i * k;
+    uint32_t deg = 0, demanded = 0;
+    if (removed(S, g)) { S.deg[g] = 0u; return; }
+    if (S.flags[g] & kValid) {
+        longlong2 c = S.cell[g];
+        // pairs (j, i) with j < i held in row j
+        for (int dx = -1; dx <= 1; ++dx)
+            for (int dy = -1; dy <= 1; ++dy)
+                for_each_in_cell(S.cell, W, buckets, entries, B, c.x + dx, c.y + dy, [&](uint32_t j) {
+                    if (j >= i) return;
+                    uint32_t gj = W.boff + j;
+                    if (!finite2(S.start[gj])) return;
+                    if (!pair_accepts(S, W, j, i)) return;
+                    if (S.pairTotal[gj] > k && !row_contains(S.candRow + W.rowOff + (uint64_t)j * k, S.candCount[gj].x, i)) return;
+                    ++demanded;
+                    insert_sorted(row, deg, k, j);
+                });
+    }
+    // own row: pairs (j > i), then segments
+    const uint2 cc = S.candCount[g];
+    const uint32_t* crow = S.candRow + W.rowOff + (uint64_t)i * k;
+    for (uint32_t e = 0; e < cc.x + cc.y; ++e) {
+        ++demanded;
+        if (deg < k) row[deg++] = crow[e];
+    }
+    // bodies holding i in their row
+    for (uint32_t bi = 0; bi < W.nb; ++bi) {
+        const DBody& b = S.body[W.bodyOff + bi];
+        if (!body_is_obstacle(b) || !body_accepts(S, W, b, bi, i)) continue;
+        uint32_t total = S.bodyTotal[W.bodyOff + bi];
+        if (total > k && !row_contains(S.bodyRow + W.bodyRowOff + (uint64_t)bi * k, k, i)) continue;
+        ++demanded;
+        if (deg < k) row[deg++] = (2u << kKindShift) | bi;
+    }
+    S.deg[g] = deg;
+    overflow += demanded - deg;
+    maxPer = max(maxPer, demanded);
+}
+
+// ------------------------------------------------------------------------------------------------------------------
+// Grid build + candidates + adjacency (one build of nativeBroadphaseInGroup, NFK:1040-1134)
+// ------------------------------------------------------------------------------------------------------------------
+template <class Team>
+__device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, const Team& team, uint32_t* buckets,
+                            uint32_t* entries, uint32_t B, uint32_t& buildOverflow, uint32_t& maxPerAll) {
+    const uint32_t n = W.n, T = team.size(), r = team.rank();
+    // a0, margin and x0 (nativeBubbleAcceleration + nativeBubbleMargin, NFK:472-499)
+    const float t = fmaxf(c.timeX - c.timeY, 0.0f);
+    float cwl = W.sepTol;
+    for (uint32_t i = r; i < n; i += T) {
+        uint32_t g = W.boff + i;
+        if (removed(S, g)) continue;
+        float2 p = S.pos[g];
+        float2 a0 = non_contact_acc(S, W, g, p);
+        S.a0[g] = a0;
+        float radius = S.phys[g].x;
+        float travel = len2(eff_vel(S, g)) * t + 0.5f * len2(a0) * t * t;
+        float m = (W.flags & BP_WORLD_MINIMUM_MARGIN_ONLY) ? 0.25f * radius : fmaxf(1.05f * travel, 0.25f * radius);
+        S.margin[g] = m;
+        S.ref[g] = p;
+        cwl = fmaxf(cwl, 2.0f * (radius + m) + W.sepTol);  // nativePrepareGrid, NGK:163-177
+    }
+    float cw = team.fmax(cwl);
+    cw = fmaxf(cw, kFltMin);
+    for (uint32_t b = r; b < B; b += T) buckets[b] = 0u;
+    team.sync();
+    // cells (nativeBuildGrid, NGK:179-189) and bucket counts
+    for (uint32_t i = r; i < n; i += T) {
+        uint32_t g = W.boff + i;
+        uint32_t f = S.flags[g] & ~kValid;
+        float2 p = S.pos[g];
+        bool valid = !(f & kRemoved) && finite2(p);
+        long long cx = 0, cy = 0;
+        if (valid) {
+            cx = (long long)clampf(floorf(p.x / cw), -4.0e18f, 4.0e18f);
+            cy = (long long)clampf(floorf(p.y / cw), -4.0e18f, 4.0e18f);
+            f |= kValid;
+            atomicAdd(buckets + grid_hash(cx, cy, B), 1u);
+        }
+        S.cell[g] = make_longlong2(cx, cy);
+        S.flags[g] = f;
+    }
+    team.sync();
+    team.scan_inplace(buckets, B);
+    for (uint32_t i = r; i < n; i += T) {
+        uint32_t g = W.boff + i;
+        if (!(S.flags[g] & kValid)) continue;
+        longlong2 cc = S.cell[g];
+        uint32_t slot = atomicAdd(buckets + grid_hash(cc.x, cc.y, B), 1u);
+        entries[slot] = i;
+    }
+    team.sync();
+    uint32_t overflow = 0, maxPer = 0;
+    for (uint32_t i = r; i < n; i += T) emit_row(S, W, buckets, entries, B, i, overflow, maxPer);
+    {
+        const uint32_t lane = threadIdx.x & 31u, warp = r >> 5, warps = T >> 5;
+        for (uint32_t bi = warp; bi < W.nb; bi += warps) emit_body_row(S, W, bi, lane, overflow, maxPer);
+    }
+    team.sync();
+    for (uint32_t i = r; i < n; i += T) build_adjacency(S, W, buckets, entries, B, i, overflow, maxPer);
+    buildOverflow = team.sum(overflow);
+    maxPerAll = max(maxPerAll, team.umax(maxPer));
+    return cw;
+}
+
+// Contact forces from the current state, then the start-of-build acceleration (phase 2, NFK:776-779).
+template <class Team> __device__ void initial_forces(const DState& S, const DWorld& W, const Ctl& c, const Team& team) {
+    const float fraction = c.timeX > 0.0f ? clampf(c.timeY / c.timeX, 0.0f, 1.0f) : 1.0f;
+    for (uint32_t i = team.rank(); i < W.n; i += team.size()) {
+        uint32_t g = W.boff + i;
+        if (removed(S, g)) continue;
+        float2 F = contact_force(S, W, i, fraction);
+        S.acc[g] = add(mul(F, inv_mass(S, g)), S.a0[g]);
+    }
+    team.sync();
+}
+
+// nativeReduceSubstepInGroup, NFK:625-736
+template <class Team> __device__ void reduce_substep(const DState& S, const DWorld& W, Ctl& c, const Team& team, float* history) {
+    const float inf = __int_as_float(0x7f800000);
+    float remaining = c.timeX - c.timeY;
+    bool over = !(remaining > 0.0f), stopped = c.cZ != 0u || c.cW != 0u, limited = c.cY >= kFrameLimit;
+    if (over || stopped || limited) {
+        if (limited && !over && !stopped) c.cW = 1u;
+        c.timeZ = 0.0f;
+        return;
+    }
+    const float fraction = c.timeX > 0.0f ? clampf(c.timeY / c.timeX, 0.0f, 1.0f) : 1.0f;
+    ValOwner w2{-1.0f, 0u}, mg{inf, 0u};
+    for (uint32_t i = team.rank(); i < W.n; i += team.size()) {
+        uint32_t g = W.boff + i;
+        if (removed(S, g)) continue;
+        float v = omega_squared(S, W, i, fraction);
+        if (v > w2.v) { w2.v = v; w2.o = i; }
+        float m = margin_bound(S, g);
+        if (m < mg.v) { mg.v = m; mg.o = i; }
+    }
+    w2 = team.template pick<true>(w2);
+    mg = team.template pick<false>(mg);
+    const float stiffnessBound = w2.v > 0.0f ? 1.0f / sqrtf(w2.v) : inf;
+    const float hMax = fminf(remaining, stiffnessBound);
+    ValOwner db{inf, 0u};
+    for (uint32_t i = team.rank(); i < W.n; i += team.size()) {
+        uint32_t g = W.boff + i;
+        if (removed(S, g)) continue;
+        float v = distance_bound(S, W, i, hMax, fraction);
+        if (v < db.v) { db.v = v; db.o = i; }
+    }
+    db = team.template pick<false>(db);
+    if (mg.v <= 0.0f) {
+        c.cZ = 1u;
+        c.timeZ = 0.0f;
+        c.limObj = S.id[W.boff + mg.o];
+        c.limTerm = BP_TERM_MARGIN;
+        return;
+    }
+    float split = fmaxf(c.timeW, 1.0f);
+    float h = remaining;
+    uint32_t term = BP_TERM_REMAINING;
+    int64_t object = 0;
+    if (split > 1.0f && c.timeX / split < h) h = c.timeX / split;
+    if (stiffnessBound / split < h) { h = stiffnessBound / split; term = BP_TERM_STIFFNESS; object = S.id[W.boff + w2.o]; }
+    if (db.v / split < h) { h = db.v / split; term = BP_TERM_DISTANCE; object = S.id[W.boff + db.o]; }
+    if (mg.v < h) { h = mg.v; term = BP_TERM_MARGIN; object = S.id[W.boff + mg.o]; c.cZ = 1u; }
+    h = fmaxf(h, c.timeX * 1e-7f);
+    uint32_t frameSubstep = c.cY;
+    if (h >= remaining || remaining - h <= c.timeX * 1e-5f) { h = remaining; c.timeY = c.timeX; }
+    else c.timeY = c.timeY + h;
+    c.timeZ = h;
+    c.cX += 1u;
+    c.cY = frameSubstep + 1u;
+    c.limObj = object;
+    c.limTerm = term;
+    if (team.leader() && frameSubstep < kFrameLimit) history[frameSubstep] = h;
+}
+
+// Phase 0 of nativeIntegratePhase (NFK:784-797): half kick with the previous acceleration, drift, rotation.
+__device__ __forceinline__ void kick_drift(const DState& S, const DWorld& W, uint32_t i, float h) {
+    const uint32_t g = W.boff + i;
+    float im = inv_mass(S, g);
+    if (!(im > 0.0f)) return;
+    uint32_t f = S.flags[g];
+    float halfStep = 0.5f * h;
+    float gamma = (f & BP_BUBBLE_FORCE_DRIVEN) ? fmaxf(S.phys[g].w, 0.0f) : 0.0f;
+    float decay = expf(-gamma * halfStep), factor = half_impulse(gamma, halfStep);
+    float2 velocity = add(mul(S.vel[g], decay), mul(S.acc[g], factor));
+    float2 rw = S.rotw[g];
+    float angular = rw.y * expf(-gamma * h);
+    if (W.nmotors && (f & BP_BUBBLE_FORCE_DRIVEN)) {
+        const bp_motor* motor = find_by_bubble(S.motors + W.motorOff, W.nmotors, S.id[g]);
+        if (motor && motor->inertia > 0.0f) angular = angular + motor->torque / motor->inertia * half_impulse(gamma, h);
+    }
+    S.pos[g] = add(S.pos[g], mul(velocity, h));
+    S.vel[g] = velocity;
+    S.rotw[g] = f2(rw.x + rw.y * h, angular);
+}
+
+// Contact forces from the new state and phase 1 (NFK:798-801): a = F / m + a0(x), second half kick.
+__device__ __forceinline__ void force_kick(const DState& S, const DWorld& W, uint32_t i, float h, float fraction) {
+    const uint32_t g = W.boff + i;
+    float im = inv_mass(S, g);
+    if (!(im > 0.0f)) return;
+    float2 F = contact_force(S, W, i, fraction);
+    uint32_t f = S.flags[g];
+    float halfStep = 0.5f * h;
+    float gamma = (f & BP_BUBBLE_FORCE_DRIVEN) ? fmaxf(S.phys[g].w, 0.0f) : 0.0f;
+    float decay = expf(-gamma * halfStep), factor = half_impulse(gamma, halfStep);
+    float2 a = add(mul(F, im), non_contact_acc(S, W, g, S.pos[g]));
+    S.vel[g] = add(mul(S.vel[g], decay), mul(a, factor));
+    S.acc[g] = a;
+}
+
+// ------------------------------------------------------------------------------------------------------------------
+// Contact assertion (NFK:865-918): the violation of the lowest bubble index.
+// ------------------------------------------------------------------------------------------------------------------
+struct Viol {
+    uint32_t kind;
+    int64_t a, b, edge;
+    float distance;
+};
+
+__device__ bool assert_bubble(const DState& S, const DWorld& W, const uint32_t* buckets, const uint32_t* entries, uint32_t B,
+                              float fraction, uint32_t i, Viol& v) {
+    const uint32_t g = W.boff + i;
+    float2 center = S.pos[g], start = S.start[g];
+    if (!finite2(center) || S.result[g] == 1u || removed(S, g)) return false;
+    bool movable = inv_mass(S, g) > 0.0f;
+    uint2 fi = S.filter[g];
+    // pairs with d <= 0 have coincident centres: same or adjacent cell of the current-position grid
+    longlong2 c = S.acell[g];
+    uint32_t bestJ = 0xffffffffu;
+    float bestD = 0.0f;
+    for (int dx = -1; dx <= 1; ++dx)
+        for (int dy = -1; dy <= 1; ++dy)
+            for_each_in_cell(S.acell, W, buckets, entries, B, c.x + dx, c.y + dy, [&](uint32_t j) {
+                if (j <= i || j >= bestJ) return;
+                uint32_t gj = W.boff + j;
+                if (S.result[gj] == 1u || removed(S, gj)) return;
+                if (!filter_accepts(fi, S.filter[gj])) return;
+                if (!movable && !(inv_mass(S, gj) > 0.0f)) return;
+                float d = len2(sub(S.pos[gj], center));
+                if (d <= 0.0f) { bestJ = j; bestD = d; }
+            });
+    if (bestJ != 0xffffffffu) {
+        v.kind = BP_VIOLATION_PAIR; v.a = S.id[g]; v.b = S.id[W.boff + bestJ]; v.edge = 0; v.distance = bestD;
+        return true;
+    }
+    if (!movable) return false;
+    for (uint32_t bi = 0; bi < W.nb; ++bi) {
+        const DBody& b = S.body[W.bodyOff + bi];
+        if (!filter_accepts(fi, make_uint2(b.cat, b.mask))) continue;
+        if (rigid_inside(S.bverts, S.btris, center, b, body_at(b, fraction))) {
+            v.kind = BP_VIOLATION_INSIDE_BODY; v.a = S.id[g]; v.b = b.id; v.edge = 0; v.distance = 0.0f;
+            return true;
+        }
+    }
+    for (uint32_t e = 0; e < W.s; ++e) {
+        const DSegment& sg = S.seg[W.soff + e];
+        if (!(sg.flags & BP_SEGMENT_POLYGON_EDGE) || !filter_accepts(fi, make_uint2(sg.cat, sg.mask))) continue;
+        float2 edge = sub(sg.b, sg.a);
+        float lsq = dot2(edge, edge);
+        if (!(lsq > 0.0f)) continue;
+        float2 outward = mul(dvd(f2(-edge.y, edge.x), sqrtf(lsq)), sg.outward);
+        float before = dot2(sub(start, sg.a), outward), after = dot2(sub(center, sg.a), outward);
+        if (!(before > 0.0f) || !(after <= 0.0f)) continue;
+        float2 crossing = add(start, mul(sub(center, start), before / (before - after)));
+        float along = dot2(sub(crossing, sg.a), edge) / lsq;
+        if (along < 0.0f || along > 1.0f) continue;
+        v.kind = BP_VIOLATION_EDGE_SIDE; v.a = S.id[g]; v.b = sg.owner; v.edge = sg.id; v.distance = after;
+        return true;
+    }
+    return false;
+}
+
+// Hash grid of the current centres (cells of width cw) for the assertion; reuses the bucket memory and keeps its own
+// cells so the cells of the last build stay readable.
+template <class Team>
+__device__ void assertion_grid(const DState& S, const DWorld& W, const Team& team, uint32_t* buckets, uint32_t* entries,
+                               uint32_t B, float cw) {
+    const uint32_t n = W.n, T = team.size(), r = team.rank();
+    const long long none = (long long)0x8000000000000000ull;
+    for (uint32_t b = r; b < B; b += T) buckets[b] = 0u;
+    team.sync();
+    for (uint32_t i = r; i < n; i += T) {
+        uint32_t g = W.boff + i;
+        float2 p = S.pos[g];
+        long long cx = none, cy = 0;
+        if (!removed(S, g) && finite2(p)) {
+            cx = (long long)clampf(floorf(p.x / cw), -4.0e18f, 4.0e18f);
+            cy = (long long)clampf(floorf(p.y / cw), -4.0e18f, 4.0e18f);
+            atomicAdd(buckets + grid_hash(cx, cy, B), 1u);
+        }
+        S.acell[g] = make_longlong2(cx, cy);
+    }
+    team.sync();
+    team.scan_inplace(buckets, B);
+    for (uint32_t i = r; i < n; i += T) {
+        uint32_t g = W.boff + i;
+        longlong2 cc = S.acell[g];
+        if (cc.x == none) continue;
+        entries[atomicAdd(buckets + grid_hash(cc.x, cc.y, B), 1u)] = i;
+    }
+    team.sync();
+}
+
+// Runs the assertion over the world; the thread that owns the violating bubble of the lowest index writes the details
+// into the report. Returns 1 in every thread when a violation exists.
+template <class Team>
+__device__ uint32_t assert_contacts(const DState& S, const DWorld& W, const Team& team, uint32_t* buckets, uint32_t* entries,
+                                    uint32_t B, float cw, float fraction, bp_step_report* rep) {
+    assertion_grid(S, W, team, buckets, entries, B, cw);
+    Viol mine{0u, 0, 0, 0, 0.0f};
+    ValOwner first{__int_as_float(0x7f800000), 0xffffffffu};
+    for (uint32_t i = team.rank(); i < W.n; i += team.size()) {
+        Viol v;
+        if (assert_bubble(S, W, buckets, entries, B, fraction, i, v)) {
+            first.v = 0.0f;
+            first.o = i;
+            mine = v;
+            break;  // later indices of this thread are larger
+        }
+    }
+    ValOwner winner = team.template pick<false>(first);
+    if (winner.o != 0xffffffffu && winner.o == first.o) {
+        rep->violation_kind = mine.kind;
+        rep->violation_objects[0] = mine.a;
+        rep->violation_objects[1] = mine.b;
+        rep->violation_edge = mine.edge;
+        rep->violation_distance = mine.distance;
+    }
+    return winner.o != 0xffffffffu ? 1u : 0u;
+}
+
+// ------------------------------------------------------------------------------------------------------------------
+// End of step: region (NPK:536-568), contact records (NGK:683-728 + NCK:146-160 + NFK:261-280)
+// ------------------------------------------------------------------------------------------------------------------
+__device__ bool apply_region(const DState& S, const DWorld& W, uint32_t g, uint32_t& removedCount, uint32_t& wrapped) {
+    uint32_t f = S.flags[g];
+    if ((f & kRemoved) || !(f & BP_BUBBLE_ENABLED) || (f & BP_BUBBLE_STATIC)) return true;
+    float2 p = S.pos[g];
+    float r = S.phys[g].x;
+    float2 nearest = vmin2(vmax2(p, W.rmin), W.rmax);
+    if (len2(sub(p, nearest)) <= r) return true;
+    if (!(f & BP_BUBBLE_WRAP)) { S.result[g] = 1u; ++removedCount; return true; }
+    float2 span = add(sub(W.rmax, W.rmin), f2(2.0f * r, 2.0f * r));
+    float dl[2] = {0.0f, 0.0f};
+    float pp[2] = {p.x, p.y}, lo[2] = {W.rmin.x, W.rmin.y}, hi[2] = {W.rmax.x, W.rmax.y}, sp[2] = {span.x, span.y};
+#pragma unroll
+    for (int axis = 0; axis < 2; ++axis) {
+        if (pp[axis] > hi[axis]) dl[axis] = -sp[axis] * fmaxf(1.0f, ceilf((pp[axis] - r - hi[axis]) / sp[axis]));
+        else if (pp[axis] < lo[axis]) dl[axis] = sp[axis] * fmaxf(1.0f, ceilf((lo[axis] - r - pp[axis]) / sp[axis]));
+    }
+    float2 delta = f2(dl[0], dl[1]);
+    float2 w = add(p, delta);
+    float2 nw = vmin2(vmax2(w, W.rmin), W.rmax);
+    if (len2(sub(w, nw)) > r) delta = add(delta, sub(nw, w));
+    float2 np = add(p, delta), ns = add(S.start[g], delta);
+    S.pos[g] = np;
+    S.start[g] = ns;
+    if (!finite2(np) || !finite2(ns)) return false;
+    S.result[g] = 2u;
+    ++wrapped;
+    return true;
+}
+
+// Contact record of candidate (i, kind, other); returns false when inactive (penetration <= -sepTol).
+__device__ bool contact_record(const DState& S, const DWorld& W, uint32_t i, uint32_t kind, uint32_t other, DContact& out) {
+    const uint32_t g = W.boff + i;
+    float2 apos = S.pos[g];
+    float4 pa = S.phys[g];
+    float ar = pa.x;
+    float2 normal, point;
+    float pen, allowed = 0.0f;
+    uint32_t feature = 0;
+    if (kind == 0u) {
+        uint32_t go = W.boff + other;
+        float2 delta = sub(S.pos[go], apos);
+        float d = len2(delta);
+        normal = d > 0.0f ? dvd(delta, d) : f2(1.0f, 0.0f);
+        point = add(apos, mul(normal, ar));
+        pen = ar + S.phys[go].x - d;
+    } else {
+        const DSegment& sg = S.seg[W.soff + other];
+        float2 edge = sub(sg.b, sg.a);
+        float lsq = dot2(edge, edge);
+        float t = lsq > 0.0f ? clampf(dot2(sub(apos, sg.a), edge) / lsq, 0.0f, 1.0f) : 0.0f;
+        point = add(sg.a, mul(edge, t));
+        float2 delta = sub(apos, point);
+        float d = len2(delta), edgeLength = len2(edge);
+        float2 base = edgeLength > 0.0f ? dvd(f2(-edge.y, edge.x), edgeLength) : f2(0.0f, 1.0f);
+        float sign = ((S.id[g] ^ sg.id) & 1) == 0 ? 1.0f : -1.0f;
+        bool fixedSide = (sg.flags & BP_SEGMENT_ALLOWED_SIDE) != 0u;
+        normal = fixedSide ? mul(base, sg.allowed) : (d > 0.0f ? dvd(delta, d) : mul(base, sign));
+        allowed = fixedSide ? sg.allowed : 0.0f;
+        pen = ar - d;
+        if (sg.flags & BP_SEGMENT_POLYGON_EDGE) {
+            float2 outward = mul(base, sg.outward);
+            float2 start = sg.a, end = sg.b;
+            float along = dot2(sub(apos, start), sub(end, start));
+            bool convexStart = (sg.flags & BP_SEGMENT_CONVEX_START) != 0u;
+            if (convexStart && along <= 0.0f && past_segment_end(apos, sg.prev, start)) feature = 2u;
+            else {
+                bool interior = along > 0.0f && !past_segment_end(apos, start, end);
+                feature = dot2(sub(apos, start), outward) >= 0.0f && interior ? 1u : 0u;
+            }
+            if (feature == 1u) {
+                normal = outward;
+                point = sub(apos, mul(outward, dot2(sub(apos, sg.a), outward)));
+                pen = ar - dot2(sub(apos, sg.a), outward);
+            } else if (feature == 2u) {
+                point = sg.a;
+                delta = sub(apos, point);
+                d = len2(delta);
+                normal = d > 0.0f ? dvd(delta, d) : outward;
+                pen = ar - d;
+            } else {
+                normal = outward;
+                point = sg.a;
+                pen = -kFltMax;
+            }
+        }
+    }
+    if (!(pen > -W.sepTol)) return false;
+    float force;
+    if (kind == 0u) {
+        float4 pb = S.phys[W.boff + other];
+        force = pair_law(pa.z, ar, pb.z, pb.x, ar + pb.x - pen).force;
+    } else {
+        force = wall_law(pa.z, ar, ar - pen).force;
+    }
+    out.a = i;
+    out.other = other;
+    out.kind = kind;
+    out.feature = feature;
+    out.normal = normal;
+    out.point = point;
+    out.impulse = force * W.dt * W.dt;
+    out.penetration = pen;
+    out.allowed = allowed;
+    return true;
+}
+
+// ------------------------------------------------------------------------------------------------------------------
+// One complete step of one world (nativeBeginStep -> substep loop -> end of step)
+// ------------------------------------------------------------------------------------------------------------------
+template <class Team>
+__device__ void world_step(const DState& S, uint32_t wi, const Team& team, uint32_t* buckets, uint32_t* entries, uint32_t B) {
+    const DWorld W = S.worlds[wi];
+    const uint32_t n = W.n, T = team.size(), r = team.rank();
+    bp_step_report* rep = S.reports + wi;
+    if (S.failed[wi]) {
+        if (team.leader()) { rep->status = BP_E_WORLD_FAILED; rep->substep_count = 0u; }
+        return;
+    }
+    // nativeBeginStep (NFK:285-293)
+    uint32_t liveLocal = 0;
+    for (uint32_t i = r; i < n; i += T) {
+        uint32_t g = W.boff + i;
+        uint32_t f = S.flags[g];
+        if (f & kRemoved) continue;
+        ++liveLocal;
+        S.result[g] = 0u;
+        S.start[g] = S.pos[g];
+        if ((f & BP_BUBBLE_ENABLED) && (f & BP_BUBBLE_STATIC)) {
+            S.vel[g] = f2(0.0f, 0.0f);
+            S.rotw[g].y = 0.0f;
+        }
+    }
+    // kinematic advance of static / kinematic bodies (nativeRigidPredict, NPK:65-80)
+    for (uint32_t bi = r; bi < W.nb; bi += T) {
+        DBody b = S.body[W.bodyOff + bi];
+        b.prev = b.pos;
+        b.prevAngle = b.angle;
+        b.cosPrev = b.cosEnd;
+        b.sinPrev = b.sinEnd;
+        if (b.flags & BP_BODY_STATIC) {
+            b.vel = f2(0.0f, 0.0f);
+            b.omega = 0.0f;
+        } else {
+            b.pos = add(b.pos, mul(b.vel, W.dt));
+            b.angle = b.angle + b.omega * W.dt;
+            if (b.angle != b.prevAngle) { b.cosEnd = cosf(b.angle); b.sinEnd = sinf(b.angle); }
+        }
+        S.body[W.bodyOff + bi] = b;
+    }
+    const uint32_t live = team.sum(liveLocal);
+    Ctl c;
+    c.timeX = W.dt;
+    c.timeY = live == 0u ? W.dt : 0.0f;
+    c.timeZ = 0.0f;
+    c.timeW = W.split;
+    c.cX = c.cY = c.cZ = c.cW = 0u;
+    c.limObj = 0;
+    c.limTerm = 0u;
+    float* history = S.history + (uint64_t)wi * kFrameLimit;
+    uint32_t buildOverflow = 0, overflowMax = 0, maxPer = 0, rebuilds = 0;
+    float cw = broadphase(S, W, c, team, buckets, entries, B, buildOverflow, maxPer);
+    initial_forces(S, W, c, team);
+    uint32_t violated = 0u;
+    for (uint32_t iteration = 0; iteration < 2u * kFrameLimit + 2u; ++iteration) {
+        if (!team.ok()) break;
+        reduce_substep(S, W, c, team, history);
+        const float h = c.timeZ;
+        const bool limited = c.cW != 0u, finished = !(c.timeX - c.timeY > 0.0f), rebuild = c.cZ != 0u;
+        if (!(h > 0.0f)) {
+            if (limited || finished || !rebuild) break;
+            c.cX = 0u;
+            c.cZ = 0u;
+            overflowMax = max(overflowMax, buildOverflow);
+            ++rebuilds;
+            cw = broadphase(S, W, c, team, buckets, entries, B, buildOverflow, maxPer);
+            initial_forces(S, W, c, team);
+            continue;
+        }
+        const float fraction = c.timeX > 0.0f ? clampf(c.timeY / c.timeX, 0.0f, 1.0f) : 1.0f;
+        for (uint32_t i = r; i < n; i += T)
+            if (!removed(S, W.boff + i)) kick_drift(S, W, i, h);
+        team.sync();
+        for (uint32_t i = r; i < n; i += T)
+            if (!removed(S, W.boff + i)) force_kick(S, W, i, h, fraction);
+        team.sync();
+        if (W.flags & BP_WORLD_INJECT_STATE) {
+            if (c.cY == W.injectSubstep + 1u)
+                for (uint32_t i = r; i < n; i += T)
+                    if (S.id[W.boff + i] == W.injectObject) S.pos[W.boff + i] = W.injectPos;
+            team.sync();
+        }
+        if ((W.flags & BP_WORLD_ASSERT_EVERY_SUBSTEP) && !violated)
+            violated = assert_contacts(S, W, team, buckets, entries, B, cw, c.timeX > 0.0f ? clampf(c.timeY / c.timeX, 0.0f, 1.0f) : 1.0f, rep);
+    }
+    overflowMax = max(overflowMax, buildOverflow);
+
+    // ---- end of step ----
+    uint32_t removedCount = 0, wrapped = 0, nonfinite = 0;
+    const bool stepDone = c.cW == 0u;
+    if (stepDone && (W.flags & BP_WORLD_HAS_REGION))
+        for (uint32_t i = r; i < n; i += T)
+            if (!apply_region(S, W, W.boff + i, removedCount, wrapped)) nonfinite = 1u;
+    team.sync();
+    // contact records: count per bubble, scan, write (kind-major candidate order)
+    uint32_t pairsLocal = 0, segsLocal = 0;
+    for (uint32_t i = r; i < n; i += T) {
+        uint32_t g = W.boff + i;
+        uint32_t cp = 0, cs = 0;
+        if (!removed(S, g)) {
+            uint2 cc = S.candCount[g];
+            const uint32_t* crow = S.candRow + W.rowOff + (uint64_t)i * W.k;
+            DContact tmp;
+            for (uint32_t e = 0; e < cc.x; ++e) cp += contact_record(S, W, i, 0u, crow[e], tmp) ? 1u : 0u;
+            for (uint32_t e = cc.x; e < cc.x + cc.y; ++e) cs += contact_record(S, W, i, 1u, crow[e] & kIndexMask, tmp) ? 1u : 0u;
+        }
+        S.scanA[g] = cp;
+        S.scanB[g] = cs;
+        pairsLocal += cp;
+        segsLocal += cs;
+    }
+    const uint32_t pairsAll = team.sum(pairsLocal);
+    const uint32_t segsAll = team.sum(segsLocal);
+    team.scan_inplace(S.scanA + W.boff, n);
+    team.scan_inplace(S.scanB + W.boff, n);
+    uint32_t droppedLocal = 0;
+    for (uint32_t i = r; i < n; i += T) {
+        uint32_t g = W.boff + i;
+        if (removed(S, g)) continue;
+        uint2 cc = S.candCount[g];
+        const uint32_t* crow = S.candRow + W.rowOff + (uint64_t)i * W.k;
+        uint32_t op = S.scanA[g], os = pairsAll + S.scanB[g];
+        DContact rec;
+        for (uint32_t e = 0; e < cc.x + cc.y; ++e) {
+            uint32_t kind = e < cc.x ? 0u : 1u;
+            if (!contact_record(S, W, i, kind, crow[e] & kIndexMask, rec)) continue;
+            uint32_t slot = kind == 0u ? op++ : os++;
+            if (!finite2(rec.normal) || !finite2(rec.point) || !isfinite(rec.impulse) || !isfinite(rec.penetration)) nonfinite = 1u;
+            if (slot < W.contactCap) S.contacts[W.contactOff + slot] = rec;
+            else ++droppedLocal;
+        }
+    }
+    // non-finite state (nativeCheckFinite, NPK:5-27)
+    for (uint32_t i = r; i < n; i += T) {
+        uint32_t g = W.boff + i;
+        if (removed(S, g)) continue;
+        if (!finite2(S.pos[g]) || !finite2(S.start[g]) || !finite2(S.vel[g]) || !finite2(S.rotw[g])) nonfinite = 1u;
+    }
+    const uint32_t anyNonfinite = team.umax(nonfinite);
+    const uint32_t contactDropped = team.sum(droppedLocal);
+    if (!violated && stepDone && !(W.flags & BP_WORLD_NO_END_ASSERTION))
+        violated = assert_contacts(S, W, team, buckets, entries, B, cw, 1.0f, rep);
+    int status = BP_OK;
+    if (c.cW != 0u) status = BP_E_SUBSTEP_LIMIT;
+    else if (anyNonfinite) status = BP_E_NONFINITE;
+    else if (violated) status = BP_E_CONTACT_VIOLATION;
+    const uint32_t removedAll = team.sum(removedCount);
+    const uint32_t wrappedAll = team.sum(wrapped);
+    uint32_t candLocal = 0, bodyCandLocal = 0;
+    for (uint32_t i = r; i < n; i += T) {
+        uint2 cc = S.candCount[W.boff + i];
+        if (!removed(S, W.boff + i)) candLocal += cc.x + cc.y;
+    }
+    for (uint32_t bi = r; bi < W.nb; bi += T) bodyCandLocal += min(S.bodyTotal[W.bodyOff + bi], W.k);
+    const uint32_t candAll = team.sum(candLocal);
+    const uint32_t bodyCandAll = team.sum(bodyCandLocal);
+    if (team.leader()) {
+        rep->status = status;
+        rep->substep_count = c.cY;
+        rep->rebuild_count = rebuilds;
+        rep->candidate_count = candAll;
+        rep->body_candidate_count = bodyCandAll;
+        rep->candidate_overflow = overflowMax;
+        rep->max_candidates_per_object = maxPer;
+        rep->contact_count = min(pairsAll + segsAll, W.contactCap);
+        rep->limiter_term = c.limTerm;
+        rep->limiter_object = c.limObj;
+        rep->cell_width = cw;
+        rep->removed_count = removedAll;
+        rep->wrapped_count = wrappedAll;
+        rep->contact_overflow = contactDropped;
+        if (!violated) {
+            rep->violation_kind = 0u;
+            rep->violation_objects[0] = 0;
+            rep->violation_objects[1] = 0;
+            rep->violation_edge = 0;
+            rep->violation_distance = 0.0f;
+        }
+        S.contactCount[wi] = min(pairsAll + segsAll, W.contactCap);
+    }
+    // publish on success, restore the published state on failure (CompleteStep.swift:5-7)
+    if (status == BP_OK) {
+        for (uint32_t i = r; i < n; i += T) {
+            uint32_t g = W.boff + i;
+            uint32_t f = S.flags[g] & ~kValid;
+            if (S.result[g] == 1u) f |= kRemoved;
+            S.flags[g] = f;
+            S.pFlags[g] = f;
+            S.pPos[g] = S.pos[g];
+            S.pStart[g] = S.start[g];
+            S.pVel[g] = S.vel[g];
+            S.pRotw[g] = S.rotw[g];
+            S.pResult[g] = S.result[g];
+        }
+        for (uint32_t bi = r; bi < W.nb; bi += T) S.pBody[W.bodyOff + bi] = S.body[W.bodyOff + bi];
+    } else {
+        for (uint32_t i = r; i < n; i += T) {
+            uint32_t g = W.boff + i;
+            S.flags[g] = S.pFlags[g];
+            S.pos[g] = S.pPos[g];
+            S.start[g] = S.pStart[g];
+            S.vel[g] = S.pVel[g];
+            S.rotw[g] = S.pRotw[g];
+            S.result[g] = S.pResult[g];
+        }
+        for (uint32_t bi = r; bi < W.nb; bi += T) S.body[W.bodyOff + bi] = S.pBody[W.bodyOff + bi];
+        if (team.leader()) S.failed[wi] = 1u;
+    }
+}
+
+// ------------------------------------------------------------------------------------------------------------------
+// Kernels
+// ------------------------------------------------------------------------------------------------------------------
+extern __shared__ uint32_t g_dynamic_smem[];
+
+// One block per world of `worldList`; dynamic shared memory holds the hash grid: B bucket ends, then maxN entries.
+template <int kMaxThreads>
+__global__ void __launch_bounds__(kMaxThreads) batch_step_kernel(DState S, const uint32_t* worldList, uint32_t B) {
+    __shared__ BlockScratch sh;
+    CtaTeam team{&sh};
+    const uint32_t wi = worldList[blockIdx.x];
+    world_step(S, wi, team, g_dynamic_smem, g_dynamic_smem + B, B);
+}
+
+// Cooperative launch: every block steps world `wi` together; the hash grid lives in global memory.
+__global__ void __launch_bounds__(512) large_step_kernel(DState S, uint32_t wi, uint32_t B) {
+    __shared__ BlockScratch sh;
+    GridTeam team{&sh, S.barrier, S.errorFlag, S.gpv, S.gpo, nullptr, 0u, false};
+    world_step(S, wi, team, S.gbuckets, S.gentries, B);
+}
+
+// Contact law known-answer kernel: mode 0 eps(q), 1 wall law, 2 pair law; 8 floats in / out per case.
+__global__ void contact_law_kernel(uint32_t mode, const float* in, float* out, uint32_t count) {
+    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= count) return;
+    const float* a = in + 8 * c;
+    float* o = out + 8 * c;
+    for (int q = 0; q < 8; ++q) o[q] = 0.0f;
+    if (mode == 0u) o[0] = eps_from_ratio(a[0]);
+    else if (mode == 1u) { Law l = wall_law(a[0], a[1], a[2]); o[0] = l.force; o[1] = l.epsA; o[2] = l.stiffness; }
+    else { Law l = pair_law(a[0], a[1], a[2], a[3], a[4]); o[0] = l.force; o[1] = l.epsA; o[2] = l.epsB; o[3] = l.stiffness; }
+}
+
+// ------------------------------------------------------------------------------------------------------------------
+// Host launchers
+// ------------------------------------------------------------------------------------------------------------------
+cudaError_t launch_batch(const DState& S, const uint32_t* dWorldList, uint32_t count, uint32_t threads, uint32_t B,
+                         uint32_t maxN, cudaStream_t stream) {
+    if (count == 0u) return cudaSuccess;
+    size_t smem = (size_t)(B + maxN) * sizeof(uint32_t);
+    if (threads <= 256u) batch_step_kernel<256><<<count, threads, smem, stream>>>(S, dWorldList, B);
+    else batch_step_kernel<1024><<<count, threads, smem, stream>>>(S, dWorldList, B);
+    return cudaGetLastError();
+}
+
+// Function attributes are set once per process before any launch (never inside a stream capture).
+void prepare_kernels() {
+    static bool done = false;
+    if (done) return;
+    done = true;
+    cudaFuncSetAttribute(batch_step_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(batch_step_kernel<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+}
+
+int large_max_blocks(int threads) {
+    int device = 0, sms = 0, perSm = 0;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, large_step_kernel, threads, 0);
+    return sms * (perSm > 0 ? perSm : 1);
+}
+
+cudaError_t launch_large(const DState& S, uint32_t wi, uint32_t B, int blocks, int threads, cudaStream_t stream) {
+    DState copy = S;
+    void* args[] = {&copy, &wi, &B};
+    return cudaLaunchCooperativeKernel((const void*)large_step_kernel, dim3(blocks), dim3(threads), args, 0, stream);
+}
+
+cudaError_t launch_contact_law(uint32_t mode, const float* in, float* out, uint32_t count, cudaStream_t stream) {
+    if (count == 0u) return cudaSuccess;
+    contact_law_kernel<<<(count + 127) / 128, 128, 0, stream>>>(mode, in, out, count);
+    return cudaGetLastError();
+}
+
+}  // namespace bp

@@ -1,0 +1,299 @@
+// bp_team.cuh - execution teams for the world step: a CTA (one world per thread block) or the whole grid of a
+// cooperative launch (one large world). Both provide sync, deterministic (value, owner) reductions with the lower
+// index winning ties, exclusive scans and sums. The grid barrier is bounded: a wait that runs out sets the error
+// flag and every block leaves the kernel at its next check, so no launch can spin forever.
+#pragma once
+
+#include "bp_device.cuh"
+
+namespace bp {
+
+constexpr unsigned long long kBarrierSpinLimit = 20000000ull;  // about 1-4 s of __nanosleep(64) polls
+
+struct ValOwner {
+    float v;
+    uint32_t o;
+};
+
+__device__ __forceinline__ ValOwner pick_max(ValOwner a, ValOwner b) {
+    return (b.v > a.v || (b.v == a.v && b.o < a.o)) ? b : a;
+}
+__device__ __forceinline__ ValOwner pick_min(ValOwner a, ValOwner b) {
+    return (b.v < a.v || (b.v == a.v && b.o < a.o)) ? b : a;
+}
+
+template <bool kMax> __device__ __forceinline__ ValOwner warp_pick(ValOwner x) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        ValOwner y;
+        y.v = __shfl_xor_sync(0xffffffffu, x.v, off);
+        y.o = __shfl_xor_sync(0xffffffffu, x.o, off);
+        x = kMax ? pick_max(x, y) : pick_min(x, y);
+    }
+    return x;
+}
+
+__device__ __forceinline__ uint32_t warp_sum(uint32_t x) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+    return x;
+}
+__device__ __forceinline__ uint32_t warp_max(uint32_t x) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) x = max(x, __shfl_xor_sync(0xffffffffu, x, off));
+    return x;
+}
+__device__ __forceinline__ float warp_fmax(float x) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, off));
+    return x;
+}
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x) {
+    const uint32_t lane = threadIdx.x & 31u;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= (uint32_t)off) x += y;
+    }
+    return x;
+}
+
+// Shared scratch used by the block-level primitives (one per CTA).
+struct BlockScratch {
+    float fv[32];
+    uint32_t uo[32];
+    uint32_t u[33];
+    float bcastF[4];
+    uint32_t bcastU[8];
+};
+
+// Block-wide (value, owner) reduction; result broadcast to every thread.
+template <bool kMax> __device__ __forceinline__ ValOwner block_pick(ValOwner x, BlockScratch& sh) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = (blockDim.x + 31u) >> 5;
+    x = warp_pick<kMax>(x);
+    __syncthreads();
+    if (lane == 0) { sh.fv[warp] = x.v; sh.uo[warp] = x.o; }
+    __syncthreads();
+    if (warp == 0) {
+        ValOwner y = lane < nw ? ValOwner{sh.fv[lane], sh.uo[lane]} : x;
+        y = warp_pick<kMax>(y);
+        if (lane == 0) { sh.fv[0] = y.v; sh.uo[0] = y.o; }
+    }
+    __syncthreads();
+    return ValOwner{sh.fv[0], sh.uo[0]};
+}
+
+__device__ __forceinline__ uint32_t block_sum(uint32_t x, BlockScratch& sh) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = (blockDim.x + 31u) >> 5;
+    x = warp_sum(x);
+    __syncthreads();
+    if (lane == 0) sh.u[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t y = lane < nw ? sh.u[lane] : 0u;
+        y = warp_sum(y);
+        if (lane == 0) sh.u[32] = y;
+    }
+    __syncthreads();
+    return sh.u[32];
+}
+__device__ __forceinline__ uint32_t block_max(uint32_t x, BlockScratch& sh) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = (blockDim.x + 31u) >> 5;
+    x = warp_max(x);
+    __syncthreads();
+    if (lane == 0) sh.u[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t y = lane < nw ? sh.u[lane] : 0u;
+        y = warp_max(y);
+        if (lane == 0) sh.u[32] = y;
+    }
+    __syncthreads();
+    return sh.u[32];
+}
+__device__ __forceinline__ float block_fmax(float x, BlockScratch& sh) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = (blockDim.x + 31u) >> 5;
+    x = warp_fmax(x);
+    __syncthreads();
+    if (lane == 0) sh.fv[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        float y = lane < nw ? sh.fv[lane] : x;
+        y = warp_fmax(y);
+        if (lane == 0) sh.fv[0] = y;
+    }
+    __syncthreads();
+    return sh.fv[0];
+}
+// Exclusive scan of one value per thread; *total receives the block total.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t* total, BlockScratch& sh) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = (blockDim.x + 31u) >> 5;
+    uint32_t incl = warp_incl_scan(x);
+    __syncthreads();
+    if (lane == 31u || threadIdx.x == blockDim.x - 1) sh.u[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t y = lane < nw ? sh.u[lane] : 0u;
+        uint32_t s = warp_incl_scan(y);
+        if (lane < nw) sh.u[lane] = s - y;
+        if (lane == nw - 1) sh.u[32] = s;
+    }
+    __syncthreads();
+    *total = sh.u[32];
+    return sh.u[warp] + incl - x;
+}
+
+// ----------------------------------------------------------------------------------------------------------------
+// CTA team: one thread block owns the world.
+// ----------------------------------------------------------------------------------------------------------------
+struct CtaTeam {
+    BlockScratch* sh;
+    __device__ uint32_t rank() const { return threadIdx.x; }
+    __device__ uint32_t size() const { return blockDim.x; }
+    __device__ bool leader() const { return threadIdx.x == 0; }
+    __device__ bool sync() const { __syncthreads(); return true; }
+    __device__ bool ok() const { return true; }
+    template <bool kMax> __device__ ValOwner pick(ValOwner x) const { return block_pick<kMax>(x, *sh); }
+    __device__ uint32_t sum(uint32_t x) const { return block_sum(x, *sh); }
+    __device__ uint32_t umax(uint32_t x) const { return block_max(x, *sh); }
+    __device__ float fmax(float x) const { return block_fmax(x, *sh); }
+    // Exclusive scan of `count` values in place (values live in memory visible to the whole team).
+    __device__ void scan_inplace(uint32_t* values, uint32_t count) const {
+        uint32_t per = (count + blockDim.x - 1) / blockDim.x;
+        uint32_t first = min(threadIdx.x * per, count), last = min(first + per, count);
+        uint32_t local = 0;
+        for (uint32_t i = first; i < last; ++i) local += values[i];
+        uint32_t total;
+        uint32_t running = block_excl_scan(local, &total, *sh);
+        for (uint32_t i = first; i < last; ++i) { uint32_t own = values[i]; values[i] = running; running += own; }
+        __syncthreads();
+    }
+};
+
+// ----------------------------------------------------------------------------------------------------------------
+// Grid team: every block of a cooperative launch works on one world. Partials go through global memory with
+// alternating parity so a reduction never overwrites partials another block may still read.
+// ----------------------------------------------------------------------------------------------------------------
+struct GridTeam {
+    BlockScratch* sh;
+    unsigned int* bar;       // [0] arrivals, [1] generation
+    uint32_t* err;
+    float* pv;               // 2 x gridDim.x partial values
+    uint32_t* po;            // 2 x gridDim.x partial owners / counts
+    uint32_t* parity;        // per-thread copy lives in registers; this is unused storage
+    mutable uint32_t par;
+    mutable bool failed;
+
+    __device__ uint32_t rank() const { return blockIdx.x * blockDim.x + threadIdx.x; }
+    __device__ uint32_t size() const { return gridDim.x * blockDim.x; }
+    __device__ bool leader() const { return blockIdx.x == 0 && threadIdx.x == 0; }
+    __device__ bool ok() const { return !failed; }
+
+    // Bounded grid barrier (generation counter). Returns false when any block gave up waiting.
+    __device__ bool sync() const {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            volatile unsigned int* gen = bar + 1;
+            unsigned int g = *gen;
+            __threadfence();
+            unsigned int arrived = atomicAdd(bar, 1u);
+            if (arrived == gridDim.x - 1) {
+                atomicExch(bar, 0u);
+                __threadfence();
+                atomicAdd(bar + 1, 1u);
+            } else {
+                unsigned long long spins = 0;
+                while (*gen == g) {
+                    if (*(volatile uint32_t*)err != 0u) break;
+                    if (++spins > kBarrierSpinLimit) { atomicOr(err, 1u); break; }
+                    __nanosleep(64);
+                }
+            }
+            __threadfence();
+            sh->bcastU[7] = *(volatile uint32_t*)err;
+        }
+        __syncthreads();
+        failed = sh->bcastU[7] != 0u;
+        return !failed;
+    }
+
+    template <bool kMax> __device__ ValOwner pick(ValOwner x) const {
+        x = block_pick<kMax>(x, *sh);
+        uint32_t base = par * gridDim.x;
+        if (threadIdx.x == 0) { pv[base + blockIdx.x] = x.v; po[base + blockIdx.x] = x.o; }
+        par ^= 1u;
+        sync();
+        if (threadIdx.x < 32) {
+            ValOwner y{kMax ? -__int_as_float(0x7f800000) : __int_as_float(0x7f800000), 0xffffffffu};
+            for (uint32_t b = threadIdx.x; b < gridDim.x; b += 32) {
+                ValOwner z{__ldcg(pv + base + b), __ldcg(po + base + b)};
+                y = kMax ? pick_max(y, z) : pick_min(y, z);
+            }
+            y = warp_pick<kMax>(y);
+            if (threadIdx.x == 0) { sh->bcastF[0] = y.v; sh->bcastU[0] = y.o; }
+        }
+        __syncthreads();
+        return ValOwner{sh->bcastF[0], sh->bcastU[0]};
+    }
+    __device__ uint32_t reduce_u(uint32_t x, bool isMax) const {
+        x = isMax ? block_max(x, *sh) : block_sum(x, *sh);
+        uint32_t base = par * gridDim.x;
+        if (threadIdx.x == 0) po[base + blockIdx.x] = x;
+        par ^= 1u;
+        sync();
+        if (threadIdx.x < 32) {
+            uint32_t y = 0;
+            for (uint32_t b = threadIdx.x; b < gridDim.x; b += 32) {
+                uint32_t z = __ldcg(po + base + b);
+                y = isMax ? max(y, z) : y + z;
+            }
+            y = isMax ? warp_max(y) : warp_sum(y);
+            if (threadIdx.x == 0) sh->bcastU[1] = y;
+        }
+        __syncthreads();
+        return sh->bcastU[1];
+    }
+    __device__ uint32_t sum(uint32_t x) const { return reduce_u(x, false); }
+    __device__ uint32_t umax(uint32_t x) const { return reduce_u(x, true); }
+    __device__ float fmax(float x) const {
+        x = block_fmax(x, *sh);
+        uint32_t base = par * gridDim.x;
+        if (threadIdx.x == 0) pv[base + blockIdx.x] = x;
+        par ^= 1u;
+        sync();
+        if (threadIdx.x < 32) {
+            float y = -__int_as_float(0x7f800000);
+            for (uint32_t b = threadIdx.x; b < gridDim.x; b += 32) y = fmaxf(y, __ldcg(pv + base + b));
+            y = warp_fmax(y);
+            if (threadIdx.x == 0) sh->bcastF[1] = y;
+        }
+        __syncthreads();
+        return sh->bcastF[1];
+    }
+    // Exclusive scan of `count` values in global memory: each block scans a contiguous chunk.
+    __device__ void scan_inplace(uint32_t* values, uint32_t count) const {
+        uint32_t per = (count + gridDim.x - 1) / gridDim.x;
+        uint32_t first = min(blockIdx.x * per, count), last = min(first + per, count);
+        uint32_t tper = (last - first + blockDim.x - 1) / blockDim.x;
+        uint32_t tf = min(first + threadIdx.x * tper, last), tl = min(tf + tper, last);
+        uint32_t local = 0;
+        for (uint32_t i = tf; i < tl; ++i) local += __ldcg(values + i);
+        uint32_t total;
+        uint32_t running = block_excl_scan(local, &total, *sh);
+        uint32_t base = par * gridDim.x;
+        if (threadIdx.x == 0) po[base + blockIdx.x] = total;
+        par ^= 1u;
+        sync();
+        if (threadIdx.x == 0) {
+            uint32_t off = 0;
+            for (uint32_t b = 0; b < blockIdx.x; ++b) off += __ldcg(po + base + b);
+            sh->bcastU[2] = off;
+        }
+        __syncthreads();
+        running += sh->bcastU[2];
+        for (uint32_t i = tf; i < tl; ++i) { uint32_t own = __ldcg(values + i); values[i] = running; running += own; }
+        sync();
+    }
+};
+
+}  // namespace bp

@@ -1,0 +1,313 @@
+"""Seeded synthetic worlds with the shapes and value distributions of the benchmark workloads.
+
+No dataset is involved: every world is generated from a numpy PCG64 stream. Materials follow the reference's public
+defaults: contact stiffness K_c = 229 (the stress scenes' material) and damping gamma = 0; gravity is an acceleration
+(0, -980) on force-driven bubbles. Walls are static thin rectangles just outside the region, turned into one-sided
+polygon edges exactly like NativeStaticPolygonEdges.segments.
+
+Resolutions of infeasible or unspecified parts of the workload descriptions (stated once here):
+ - plain_world (256 bubbles, r ~ U[8,24] in 375 x 700): the bubbles cover ~85 % of the region, so strict non-overlap
+   rejection sampling cannot finish; the sampler shrinks the required centre distance by 5 % after every 2000 failed
+   tries (soft contact resolves the initial overlap).
+ - large_world (65,536 bubbles, log-normal radii): 60 % area fraction is met locally by a jittered grid in a square
+   block at the bottom of the 8192^2 region (the bubbles' total area is only ~15 % of the region); the grid is rebuilt
+   almost every substep through the minimum-margin switch.
+ - batched worlds: placement is a jittered grid at 40 % area fraction, bubble mass 8, velocities N(0, 30^2); bubbles
+   whose centre would lie inside a rigid body are dropped; bodies are static (circles, capsules, polygons) or kinematic
+   (any shape, slow constant drive), since the reference rejects dynamic bodies next to bubbles.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import _native as N
+from .spec import WorldSpec, make_bubbles
+
+K_C = 229.0
+GRAVITY = (0.0, -980.0)
+DT = 1.0 / 60.0
+
+
+def polygon_edges(points, first_id: int, owner_id: int | None = None) -> np.ndarray:
+    """One-sided edges of a static polygon; numpy restatement of NativeStaticPolygonEdges.segments
+    (Sources/BubblePhysicsNativeMetal/NativeStaticPolygonEdges.swift:16-72)."""
+    pts = np.asarray(points, np.float32).reshape(-1, 2)
+    n = pts.shape[0]
+
+    def cross(u, v):
+        return float(u[0]) * float(v[1]) - float(u[1]) * float(v[0])
+
+    area = 0.0
+    if n >= 3:
+        for i in range(1, n - 1):
+            area += cross(pts[i] - pts[0], pts[i + 1] - pts[0])
+    out = []
+
+    def seg(sid, a, b):
+        s = np.zeros(1, N.SEGMENT_DTYPE)[0]
+        s["id"] = sid
+        s["owner_id"] = owner_id if owner_id is not None else 0
+        s["a"] = a
+        s["b"] = b
+        s["flags"] = N.SEGMENT_HAS_OWNER if owner_id is not None else 0
+        s["category"] = 1
+        s["mask"] = 0xFFFFFFFF
+        return s
+
+    if n < 3 or area == 0.0:
+        for i in range(n):
+            out.append(seg(first_id + i, pts[i], pts[(i + 1) % n]))
+        return np.array(out, N.SEGMENT_DTYPE)
+    ring = [p.copy() for p in pts]
+    removed = True
+    while removed and len(ring) > 3:
+        removed = False
+        index = 0
+        while index < len(ring) and len(ring) > 3:
+            c = len(ring)
+            incoming = ring[index] - ring[(index + c - 1) % c]
+            outgoing = ring[(index + 1) % c] - ring[index]
+            lengths = float(np.float32(math.sqrt(float(incoming[0] * incoming[0] + incoming[1] * incoming[1])))) * \
+                float(np.float32(math.sqrt(float(outgoing[0] * outgoing[0] + outgoing[1] * outgoing[1]))))
+            dt = float(incoming[0]) * float(outgoing[0]) + float(incoming[1]) * float(outgoing[1])
+            if lengths > 0 and dt > 0 and abs(cross(incoming, outgoing)) <= 1e-5 * lengths:
+                ring.pop(index)
+                removed = True
+            else:
+                index += 1
+    orientation = 1.0 if area > 0 else -1.0
+    c = len(ring)
+    for index in range(c):
+        previous, a, b, nxt = ring[(index + c - 1) % c], ring[index], ring[(index + 1) % c], ring[(index + 2) % c]
+        s = seg(first_id + index, a, b)
+        convex_start = cross(a - previous, b - a) * orientation > 0
+        convex_end = cross(b - a, nxt - b) * orientation > 0
+        s["flags"] |= N.SEGMENT_POLYGON_EDGE | (N.SEGMENT_CONVEX_START if convex_start else 0) | \
+            (N.SEGMENT_CONVEX_END if convex_end else 0)
+        s["outward_sign"] = -1.0 if area > 0 else 1.0
+        s["previous_start"] = previous
+        out.append(s)
+    return np.array(out, N.SEGMENT_DTYPE)
+
+
+def wall_segments(region, thickness=32.0, first_id=1_000_000, owner_base=2_000_000) -> np.ndarray:
+    """Four static thin rectangles just outside the region edges, as one-sided polygon edges."""
+    x0, y0, x1, y1 = region
+    t = thickness
+    rects = [((x0 - t, y0 - t), (x1 + t, y0)), ((x0 - t, y1), (x1 + t, y1 + t)),
+             ((x0 - t, y0), (x0, y1)), ((x1, y0), (x1 + t, y1))]
+    segs = []
+    sid = first_id
+    for k, ((ax, ay), (bx, by)) in enumerate(rects):
+        poly = [(ax, ay), (bx, ay), (bx, by), (ax, by)]
+        e = polygon_edges(poly, sid, owner_base + k)
+        sid += len(e)
+        segs.append(e)
+    return np.concatenate(segs)
+
+
+def _rejection_place(rng, radii, region, max_tries=2000):
+    x0, y0, x1, y1 = region
+    n = radii.shape[0]
+    centers = np.zeros((n, 2), np.float64)
+    placed = 0
+    scale = 1.0
+    cell = 2.0 * float(radii.max())
+    grid: dict = {}
+    while placed < n:
+        r = radii[placed]
+        ok = False
+        for _ in range(max_tries):
+            c = np.array([rng.uniform(x0 + r, x1 - r), rng.uniform(y0 + r, y1 - r)])
+            gx, gy = int(c[0] // cell), int(c[1] // cell)
+            clash = False
+            for dx in (-1, 0, 1):
+                for dy in (-1, 0, 1):
+                    for j in grid.get((gx + dx, gy + dy), ()):
+                        if np.hypot(*(centers[j] - c)) < (radii[j] + r) * scale:
+                            clash = True
+                            break
+                    if clash:
+                        break
+                if clash:
+                    break
+            if not clash:
+                ok = True
+                break
+        if not ok:
+            scale *= 0.95
+            continue
+        centers[placed] = c
+        grid.setdefault((int(c[0] // cell), int(c[1] // cell)), []).append(placed)
+        placed += 1
+    return centers
+
+
+def plain_world(seed: int = 1, n: int = 256) -> WorldSpec:
+    """Plain single world: region [0,375] x [0,700] with static walls, 256 bubbles r ~ U[8,24], mass 8,
+    velocities N(0, 30^2), K_c 229, gamma 0, gravity (0,-980), dt 1/60."""
+    rng = np.random.default_rng(seed)
+    region = (0.0, 0.0, 375.0, 700.0)
+    radii = rng.uniform(8.0, 24.0, n)
+    centers = _rejection_place(rng, radii, region)
+    vel = rng.normal(0.0, 30.0, (n, 2))
+    b = make_bubbles(centers, radii, velocities=vel, masses=8.0, stiffness=K_C, damping=0.0,
+                     flags=N.BUBBLE_FORCE_DRIVEN | N.BUBBLE_ENABLED)
+    return WorldSpec(bubbles=b, segments=wall_segments(region), region=region, gravity=GRAVITY, time_step=DT)
+
+
+def large_world(seed: int = 2, n: int = 65536, side: float = 8192.0) -> WorldSpec:
+    """Plain single large world: 8192^2 with walls, log-normal radii (median 6, sigma 0.4, clipped [3,20]),
+    mass proportional to r^2 (mass 1 at r = 6), jittered grid at 60 % local area fraction at the bottom, velocities
+    N(0, 30^2), minimum-margin switch so the grid is rebuilt almost every substep."""
+    rng = np.random.default_rng(seed)
+    region = (0.0, 0.0, side, side)
+    radii = np.clip(rng.lognormal(math.log(6.0), 0.4, n), 3.0, 20.0)
+    per = math.pi * float(np.mean(radii ** 2)) / 0.6
+    spacing = math.sqrt(per)
+    cols = int(math.ceil(math.sqrt(n)))
+    ij = np.stack(np.divmod(np.arange(n), cols), axis=1)[:, ::-1].astype(np.float64)
+    jitter = rng.uniform(-0.25, 0.25, (n, 2)) * spacing
+    centers = (ij + 0.5) * spacing + jitter + np.array([spacing, spacing])
+    vel = rng.normal(0.0, 30.0, (n, 2))
+    masses = (radii / 6.0) ** 2
+    b = make_bubbles(centers, radii, velocities=vel, masses=masses, stiffness=K_C, damping=0.0,
+                     flags=N.BUBBLE_FORCE_DRIVEN | N.BUBBLE_ENABLED)
+    return WorldSpec(bubbles=b, segments=wall_segments(region), region=region, gravity=GRAVITY, time_step=DT,
+                     flags=N.WORLD_MINIMUM_MARGIN_ONLY)
+
+
+def _regular_polygon(rng, sides, half):
+    angles = np.sort(rng.uniform(0, 2 * math.pi, sides))
+    angles = np.linspace(0, 2 * math.pi, sides, endpoint=False) + rng.uniform(0, 2 * math.pi / sides)
+    radius = half * rng.uniform(0.7, 1.0, sides)
+    return np.stack([np.cos(angles) * radius, np.sin(angles) * radius], axis=1)
+
+
+def _body_geometry(kind, rng, half):
+    """Local geometry of a body about its centre of mass (NativeRigidGeometry, NativeRigidPolygonState.swift:76-158):
+    vertices, fan triangles of a convex ring, bounding radius, core radius."""
+    if kind == N.BODY_CIRCLE:
+        return np.zeros((1, 2), np.float32), np.zeros((0, 3), np.uint32), half, half, 0.0
+    if kind == N.BODY_CAPSULE:
+        r = half * 0.4
+        h = half - r
+        return np.array([[-h, 0.0], [h, 0.0]], np.float32), np.zeros((0, 3), np.uint32), h + r, r, h
+    sides = int(rng.integers(3, 9))
+    pts = _regular_polygon(rng, sides, half)
+    # centroid of the polygon (area-weighted) so vertices are local to the centre of mass
+    x, y = pts[:, 0], pts[:, 1]
+    xn, yn = np.roll(x, -1), np.roll(y, -1)
+    cr = x * yn - xn * y
+    area = cr.sum() / 2.0
+    cx = ((x + xn) * cr).sum() / (6.0 * area)
+    cy = ((y + yn) * cr).sum() / (6.0 * area)
+    local = (pts - np.array([cx, cy])).astype(np.float32)
+    tris = np.array([[0, i, i + 1] for i in range(1, sides - 1)], np.uint32)
+    bound = float(np.sqrt((local.astype(np.float64) ** 2).sum(axis=1)).max())
+    return local, tris, bound, 0.0, 0.0
+
+
+def add_bodies(rng, count, region, size_range, first_id, kinematic_fraction=0.25, speed=20.0):
+    """Random static / kinematic bodies (1/3 polygons, 1/3 circles, 1/3 capsules). Static polygons become one-sided
+    edges (like NativePublicWorld.step); static circles / capsules and every kinematic body are obstacle bodies."""
+    x0, y0, x1, y1 = region
+    bodies, verts, tris, segs = [], [], [], []
+    vcount = tcount = 0
+    seg_id = first_id * 16
+    for k in range(count):
+        kind = [N.BODY_POLYGON, N.BODY_CIRCLE, N.BODY_CAPSULE][k % 3]
+        half = float(rng.uniform(*size_range))
+        local, tri, bound, core, hl = _body_geometry(kind, rng, half)
+        pos = np.array([rng.uniform(x0 + bound, x1 - bound), rng.uniform(y0 + bound, y1 - bound)])
+        angle = float(rng.uniform(0, 2 * math.pi))
+        kinematic = rng.uniform() < kinematic_fraction
+        bid = first_id + k
+        if kind == N.BODY_POLYGON and not kinematic:
+            c, s = math.cos(angle), math.sin(angle)
+            world = np.stack([local[:, 0] * c - local[:, 1] * s, local[:, 0] * s + local[:, 1] * c], 1) + pos
+            e = polygon_edges(world.astype(np.float32), seg_id, bid)
+            seg_id += len(e)
+            segs.append(e)
+            bodies.append(None)
+            continue
+        rec = np.zeros(1, N.BODY_DTYPE)[0]
+        rec["id"] = bid
+        rec["position"] = pos
+        rec["angle"] = angle
+        rec["bounding_radius"] = bound
+        rec["kind"] = kind
+        rec["core_radius"] = core
+        rec["half_length"] = hl
+        rec["flags"] = N.BODY_KINEMATIC if kinematic else N.BODY_STATIC
+        if kinematic:
+            rec["velocity"] = rng.uniform(-speed, speed, 2)
+            rec["angular_velocity"] = float(rng.uniform(-0.5, 0.5))
+        rec["vertex_offset"] = vcount
+        rec["vertex_count"] = local.shape[0]
+        rec["triangle_offset"] = tcount
+        rec["triangle_count"] = tri.shape[0]
+        rec["category"] = 1
+        rec["mask"] = 0xFFFFFFFF
+        verts.append(local)
+        tris.append(tri)
+        vcount += local.shape[0]
+        tcount += tri.shape[0]
+        bodies.append(rec)
+    recs = [b for b in bodies if b is not None]
+    body_arr = np.array(recs, N.BODY_DTYPE) if recs else np.zeros(0, N.BODY_DTYPE)
+    vert_arr = np.concatenate(verts).astype(np.float32) if verts else np.zeros((0, 2), np.float32)
+    tri_arr = np.concatenate(tris).astype(np.uint32) if tris else np.zeros((0, 3), np.uint32)
+    seg_arr = np.concatenate(segs) if segs else np.zeros(0, N.SEGMENT_DTYPE)
+    return body_arr, vert_arr, tri_arr, seg_arr
+
+
+def _clear_of_bodies(centers, radii, bodies, segs):
+    keep = np.ones(centers.shape[0], bool)
+    for b in bodies:
+        d = np.hypot(centers[:, 0] - b["position"][0], centers[:, 1] - b["position"][1])
+        keep &= d > b["bounding_radius"] + radii + 1.0
+    if segs.size:
+        # static polygon edges: drop bubbles near any edge's bounding box
+        lo = np.minimum(segs["a"], segs["b"])
+        hi = np.maximum(segs["a"], segs["b"])
+        for q in range(segs.shape[0]):
+            inside = (centers[:, 0] > lo[q, 0] - radii - 1) & (centers[:, 0] < hi[q, 0] + radii + 1) & \
+                     (centers[:, 1] > lo[q, 1] - radii - 1) & (centers[:, 1] < hi[q, 1] + radii + 1)
+            keep &= ~inside
+    return keep
+
+
+def batched_world(rng, n_target: int, *, world_index: int = 0, max_bodies: int = 32) -> WorldSpec:
+    """One world of the batched workload: n ~ given, r ~ U[6,24], region sized to 40 % area fraction, 0-32 bodies
+    (half-extents U[8,40]), jittered-grid placement, mass 8, velocities N(0, 30^2)."""
+    radii = rng.uniform(6.0, 24.0, n_target)
+    area = math.pi * float(np.mean(radii ** 2)) * n_target / 0.4
+    side = math.sqrt(area)
+    region = (0.0, 0.0, side, side)
+    nb = int(rng.integers(0, max_bodies + 1))
+    bodies, bverts, btris, bsegs = add_bodies(rng, nb, region, (8.0, 40.0), first_id=10_000 + 64 * world_index)
+    cols = int(math.ceil(math.sqrt(n_target)))
+    spacing = side / cols
+    ij = np.stack(np.divmod(np.arange(n_target), cols), axis=1)[:, ::-1].astype(np.float64)
+    centers = (ij + 0.5) * spacing + rng.uniform(-0.2, 0.2, (n_target, 2)) * spacing
+    keep = _clear_of_bodies(centers, radii, bodies, bsegs)
+    centers, radii = centers[keep], radii[keep]
+    n = centers.shape[0]
+    vel = rng.normal(0.0, 30.0, (n, 2))
+    b = make_bubbles(centers, radii, velocities=vel, masses=8.0, stiffness=K_C, damping=0.0,
+                     flags=N.BUBBLE_FORCE_DRIVEN | N.BUBBLE_ENABLED)
+    walls = wall_segments(region)
+    segs = np.concatenate([walls, bsegs]) if bsegs.size else walls
+    segs = np.sort(segs, order="id")
+    return WorldSpec(bubbles=b, segments=segs, bodies=bodies, body_vertices=bverts, body_triangles=btris,
+                     region=region, gravity=GRAVITY, time_step=DT)
+
+
+def batched_worlds(count: int = 4096, seed: int = 3, n_min: int = 16, n_max: int = 1024, max_bodies: int = 32):
+    """The batched workload: `count` worlds, bubble counts log-uniform in [n_min, n_max]."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(math.log(n_min), math.log(n_max), count)).astype(np.int64)
+    return [batched_world(rng, int(s), world_index=w, max_bodies=max_bodies) for w, s in enumerate(sizes)]

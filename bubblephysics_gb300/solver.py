@@ -1,0 +1,217 @@
+"""Native solver handles over the C ABI: Context, World (plain single world), Batch (many independent worlds).
+
+World mirrors the reference's persistent NativeMetalSolver + executeFrame seam
+(Sources/BubblePhysicsNativeMetal/NativeMetalSolver.swift:380-1218): state stays resident on the GPU between steps,
+each step returns a report, a failed step publishes nothing and stops the world.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .spec import PackedInput, WorldSpec
+
+
+class Context:
+    """One CUDA device + one stream (bp_context)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = N.library()
+        handle = C.c_void_p()
+        N.check(self.lib.bp_context_create(device, 0, C.byref(handle)), "bp_context_create")
+        self.handle = handle
+        self.device = device
+
+    def close(self):
+        if self.handle:
+            self.lib.bp_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def contact_law(self, mode: int, cases: np.ndarray) -> np.ndarray:
+        """Contact law on the device (known-answer tests): cases (n, 8) float32 -> (n, 8) float32."""
+        cases = np.ascontiguousarray(cases, np.float32).reshape(-1, 8)
+        out = np.zeros_like(cases)
+        N.check(self.lib.bp_device_contact_law(self.handle, mode, N.ptr(cases, C.c_float), N.ptr(out, C.c_float),
+                                               cases.shape[0]), "bp_device_contact_law")
+        return out
+
+
+_default_context: Context | None = None
+
+
+def default_context() -> Context:
+    global _default_context
+    if _default_context is None:
+        _default_context = Context(0)
+    return _default_context
+
+
+class World:
+    """A single world stepped by the plain per-world launch path."""
+
+    def __init__(self, spec: WorldSpec, context: Context | None = None):
+        self.ctx = context or default_context()
+        self.lib = self.ctx.lib
+        self.spec = spec
+        packed = PackedInput(spec)
+        handle = C.c_void_p()
+        N.check(self.lib.bp_world_create(self.ctx.handle, C.byref(packed.desc), C.byref(packed.input), C.byref(handle)),
+                "bp_world_create")
+        self.handle = handle
+        self.n = spec.bubble_count
+
+    def close(self):
+        if self.handle:
+            self.lib.bp_world_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_injection(self, substep: int, position):
+        d = N.WorldDiagnostics()
+        d.inject_substep = substep
+        d.inject_position[:] = [float(position[0]), float(position[1])]
+        N.check(self.lib.bp_world_set_diagnostics(self.handle, C.byref(d)), "bp_world_set_diagnostics")
+
+    def step(self, steps: int = 1) -> tuple[int, np.ndarray]:
+        """Advances `steps` steps; returns (status, reports[steps]). Stops at the first failed step."""
+        reports = np.zeros(max(steps, 1), N.REPORT_DTYPE)
+        status = self.lib.bp_world_step(self.handle, steps, C.c_void_p(reports.ctypes.data))
+        if status in (N.E_CUDA, N.E_ALLOC, N.E_INVALID, N.E_INFLIGHT, N.E_UNAVAILABLE):
+            raise N.NativeError(status, "bp_world_step")
+        return status, reports[:steps]
+
+    def write_bubbles(self, bubbles: np.ndarray):
+        b = np.ascontiguousarray(bubbles, N.BUBBLE_DTYPE)
+        N.check(self.lib.bp_world_write_bubbles(self.handle, C.c_void_p(b.ctypes.data), b.shape[0]),
+                "bp_world_write_bubbles")
+
+    def bubbles(self) -> np.ndarray:
+        out = np.zeros(self.n, N.BUBBLE_DTYPE)
+        count = C.c_uint32()
+        N.check(self.lib.bp_world_read_bubbles(self.handle, C.c_void_p(out.ctypes.data), self.n, C.byref(count)),
+                "bp_world_read_bubbles")
+        return out
+
+    def _read(self, fn, dtype, where):
+        count = C.c_uint32()
+        N.check(fn(self.handle, None, 0, C.byref(count)), where)
+        out = np.zeros(count.value, dtype)
+        if count.value:
+            N.check(fn(self.handle, C.c_void_p(out.ctypes.data), count.value, C.byref(count)), where)
+        return out
+
+    def contacts(self) -> np.ndarray:
+        return self._read(self.lib.bp_world_read_contacts, N.CONTACT_DTYPE, "bp_world_read_contacts")
+
+    def candidates(self) -> np.ndarray:
+        return self._read(self.lib.bp_world_read_candidates, N.KEY_DTYPE, "bp_world_read_candidates")
+
+    def cells(self) -> np.ndarray:
+        out = np.zeros((self.n, 2), np.int64)
+        count = C.c_uint32()
+        N.check(self.lib.bp_world_read_cells(self.handle, C.c_void_p(out.ctypes.data), self.n, C.byref(count)),
+                "bp_world_read_cells")
+        return out
+
+    def substeps(self) -> np.ndarray:
+        return self._read(self.lib.bp_world_read_substeps, np.float32, "bp_world_read_substeps")
+
+
+class Batch:
+    """Many independent worlds stepped together: one fused launch per size class and step (or, with
+    per_world_launch=True, the plain path: one launch per world, one after another)."""
+
+    def __init__(self, specs: list[WorldSpec], context: Context | None = None, *, per_world_launch=False,
+                 use_graph=True, autotune=False, threads_per_world=0):
+        self.ctx = context or default_context()
+        self.lib = self.ctx.lib
+        self.specs = specs
+        packed = [PackedInput(s) for s in specs]
+        descs = (N.WorldDesc * len(specs))(*[p.desc for p in packed])
+        inputs = (N.WorldInput * len(specs))(*[p.input for p in packed])
+        cfg = N.BatchConfig()
+        cfg.flags = (N.BATCH_PER_WORLD_LAUNCH if per_world_launch else 0) | (N.BATCH_USE_GRAPH if use_graph else 0) | \
+                    (N.BATCH_AUTOTUNE if autotune else 0)
+        cfg.threads_per_world = threads_per_world
+        handle = C.c_void_p()
+        N.check(self.lib.bp_batch_create(self.ctx.handle, len(specs), descs, inputs, C.byref(cfg), C.byref(handle)),
+                "bp_batch_create")
+        self.handle = handle
+        self.sizes = np.array([s.bubble_count for s in specs], np.int64)
+        self.total_bubbles = int(self.sizes.sum())
+
+    def close(self):
+        if self.handle:
+            self.lib.bp_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, steps: int = 1) -> tuple[int, np.ndarray]:
+        reports = np.zeros(len(self.specs), N.REPORT_DTYPE)
+        status = self.lib.bp_batch_step(self.handle, steps, C.c_void_p(reports.ctypes.data))
+        if status in (N.E_CUDA, N.E_ALLOC, N.E_INVALID, N.E_INFLIGHT, N.E_UNAVAILABLE, N.E_TIMEOUT):
+            raise N.NativeError(status, "bp_batch_step")
+        return status, reports
+
+    def counters(self) -> tuple[int, int, int]:
+        a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        N.check(self.lib.bp_batch_counters(self.handle, C.byref(a), C.byref(b), C.byref(c)), "bp_batch_counters")
+        return a.value, b.value, c.value
+
+    def bubbles(self, world: int) -> np.ndarray:
+        n = int(self.sizes[world])
+        out = np.zeros(n, N.BUBBLE_DTYPE)
+        count = C.c_uint32()
+        N.check(self.lib.bp_batch_read_bubbles(self.handle, world, C.c_void_p(out.ctypes.data), n, C.byref(count)),
+                "bp_batch_read_bubbles")
+        return out
+
+    def write_state(self, center_velocity: np.ndarray):
+        """Bulk host -> device write of (center.xy, velocity.xy) float32 for every bubble, worlds in order."""
+        assert center_velocity.dtype == np.float32 and center_velocity.flags["C_CONTIGUOUS"]
+        N.check(self.lib.bp_batch_write_state(self.handle, C.c_void_p(center_velocity.ctypes.data), self.total_bubbles),
+                "bp_batch_write_state")
+
+    def read_state(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.zeros((self.total_bubbles, 4), np.float32)
+        N.check(self.lib.bp_batch_read_state(self.handle, C.c_void_p(out.ctypes.data), self.total_bubbles),
+                "bp_batch_read_state")
+        return out
+
+    def tuning(self) -> list[int]:
+        out = (C.c_uint32 * 9)()
+        N.check(self.lib.bp_batch_tuning(self.handle, out, 9), "bp_batch_tuning")
+        return list(out)
+
+
+def static_polygon_edges(points, first_id: int, owner_id: int | None = None) -> np.ndarray:
+    """One-sided edges of a static polygon (NativeStaticPolygonEdges.segments) computed by the native library."""
+    lib = N.library()
+    pts = np.ascontiguousarray(points, np.float32).reshape(-1, 2)
+    count = C.c_uint32()
+    cap = max(pts.shape[0], 1)
+    out = np.zeros(cap, N.SEGMENT_DTYPE)
+    N.check(lib.bp_static_polygon_edges(N.ptr(pts, C.c_float), pts.shape[0], first_id, owner_id or 0,
+                                        1 if owner_id is not None else 0,
+                                        C.cast(out.ctypes.data, C.POINTER(N.Segment)), cap, C.byref(count)),
+            "bp_static_polygon_edges")
+    return out[:count.value]

@@ -1,0 +1,350 @@
+/*
+ * bubblephysics.h - C ABI of the GB300-native bubble step (grid broadphase, radius-bounded
+ * contact forces K_c / gamma, adaptive-substep damped leapfrog, LBVH rigid broadphase).
+ *
+ * This is the drop-in boundary for the reference's solver seam
+ *   NativeMetalFrameExecuting.executeFrame(input: NativeSolverInput, scenarioStep:) -> NativeSolverFrame
+ *   (Sources/BubblePhysicsNativeMetal/NativeSolverInput.swift:257-260)
+ * which BubbleWorld.advance(by:) reaches through CompleteStepper.completeStep and NativePublicWorld.step
+ * (Sources/BubblePhysicsPublic/BubbleWorld.swift:270-283, Sources/BubblePhysicsNativeMetal/NativePublicWorld.swift:162-258).
+ *
+ * Conventions
+ *  - Plain C: no torch or CUDA types. Every pointer argument is HOST memory owned by the caller; the library owns
+ *    all device memory. Records are plain structs whose sizes are pinned by static asserts in the implementation.
+ *  - Bubbles are passed sorted by id (signed 64-bit, strictly increasing), segments sorted by id, like
+ *    NativePublicWorld.step sorts them (NativePublicWorld.swift:248-249). Indices in every output refer to that order.
+ *  - Every function returns an int status (bp_status). A step that fails publishes nothing: the world keeps the
+ *    state of the last successful step (Sources/BubblePhysicsRuntime/CompleteStep.swift:5-7).
+ *  - Calls are thread-compatible: one in-flight step per world / batch. Every device wait is bounded.
+ */
+#ifndef BUBBLEPHYSICS_GB300_H
+#define BUBBLEPHYSICS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BP_ABI_VERSION 1
+
+/* Status codes. Mirrors NativeMetalSolverError / NativeMetalWorldError
+ * (NativeMetalSolver.swift:5-6, NativeSolverInput.swift:266-272). */
+typedef enum bp_status {
+    BP_OK = 0,
+    BP_E_INVALID = 1,           /* invalidSnapshot: bad input record, unsorted ids, non-finite input */
+    BP_E_SUBSTEP_LIMIT = 2,     /* substepLimitExceeded: 1024 substeps used with step time left */
+    BP_E_NONFINITE = 3,         /* nonFinite: a bubble or contact field became non-finite */
+    BP_E_CONTACT_VIOLATION = 4, /* contactViolation: pair d <= 0, centre inside immovable body, edge side change */
+    BP_E_INFLIGHT = 5,          /* frameInFlight: a second step was requested while one is running */
+    BP_E_TIMEOUT = 6,           /* a bounded device wait ran out (reported, context stays usable) */
+    BP_E_CUDA = 7,              /* commandFailed: a CUDA runtime call failed */
+    BP_E_CAPACITY = 8,          /* capacityOverflow: a size beyond the library's limits */
+    BP_E_UNAVAILABLE = 9,       /* unavailable: no CUDA device / extension not built for this GPU */
+    BP_E_ALLOC = 10,            /* allocationFailed */
+    BP_E_WORLD_FAILED = 11      /* the world failed in an earlier step and is stopped */
+} bp_status;
+
+/* Substep limiter term (NativeMetalSubstepTerm, NativeSolverInput.swift:275). */
+typedef enum bp_term { BP_TERM_REMAINING = 0, BP_TERM_STIFFNESS = 1, BP_TERM_DISTANCE = 2, BP_TERM_MARGIN = 3 } bp_term;
+
+/* Contact-assertion violation kinds (NativeForceKernels nativeViolation*). */
+typedef enum bp_violation { BP_VIOLATION_NONE = 0, BP_VIOLATION_PAIR = 1, BP_VIOLATION_INSIDE_BODY = 2,
+                            BP_VIOLATION_EDGE_SIDE = 3 } bp_violation;
+
+/* ---- records ------------------------------------------------------------------------------------------------ */
+
+/* Bubble flags: NativePublicProperties.flags (NativePublicWorld.swift:69) + contact.w force-driven marker. */
+enum {
+    BP_BUBBLE_ENABLED = 1u,      /* publicFlags.x: the region policy applies */
+    BP_BUBBLE_STATIC = 2u,       /* publicFlags.y: motion role .static (infinite mass, never moves) */
+    BP_BUBBLE_WRAP = 4u,         /* publicFlags.z: region exit policy .wrap (else .remove) */
+    BP_BUBBLE_FORCE_DRIVEN = 8u  /* contact.w: dynamic / motor / player roles feel global force, fields, gamma */
+};
+
+/* One bubble (NativeSolverBubble + NativePublicProperties; NativeMetalBufferLayout.swift:4-25). 80 bytes. */
+typedef struct bp_bubble {
+    int64_t id;                  /* ObjectID bit pattern as signed Int (NativePublicWorld.swift:194) */
+    float center[2];
+    float previous_center[2];    /* out: centre at the start of the last step (position.zw) */
+    float velocity[2];
+    float mass;
+    float inverse_mass;          /* 0 = static */
+    float radius;                /* target radius */
+    float rotation;
+    float angular_velocity;
+    float contact_stiffness;     /* K_c (> 0 for contact) */
+    float damping;               /* gamma, 1/s */
+    uint32_t flags;              /* BP_BUBBLE_* */
+    uint32_t category;           /* collision filter category bits */
+    uint32_t mask;               /* collision filter mask bits */
+    uint32_t region_result;      /* out: 0 unchanged, 1 removed by the region, 2 wrapped (publicFlags.w) */
+    uint32_t reserved;
+} bp_bubble;
+
+/* Segment flags (NativeMetalSegment.flags, NativeMetalBufferLayout.swift:63-79). */
+enum {
+    BP_SEGMENT_POLYGON_EDGE = 1u,  /* flags.w bit 0: one-sided static polygon edge with regions */
+    BP_SEGMENT_CONVEX_START = 2u,  /* flags.w bit 1 */
+    BP_SEGMENT_CONVEX_END = 4u,    /* flags.w bit 2 (informational) */
+    BP_SEGMENT_HAS_OWNER = 8u,     /* flags.y */
+    BP_SEGMENT_ALLOWED_SIDE = 16u, /* flags.z: fixed contact normal side (allowed_side) */
+    BP_SEGMENT_KINEMATIC = 32u     /* flags.x (informational; segments do not move inside a step) */
+};
+
+/* One static segment (NativeSolverSegment + NativeSolverPolygonEdge). 64 bytes. */
+typedef struct bp_segment {
+    int64_t id;
+    int64_t owner_id;
+    float a[2];
+    float b[2];
+    float previous_start[2];     /* polygon edge: start of the previous edge of the ring (region.xy) */
+    float outward_sign;          /* polygon edge: outward normal = left normal * sign (region.z) */
+    float allowed_side;          /* collision.x when BP_SEGMENT_ALLOWED_SIDE */
+    uint32_t flags;              /* BP_SEGMENT_* */
+    uint32_t category;
+    uint32_t mask;
+    uint32_t reserved;
+} bp_segment;
+
+enum { BP_BODY_POLYGON = 0u, BP_BODY_CIRCLE = 1u, BP_BODY_CAPSULE = 2u };
+enum { BP_BODY_STATIC = 1u, BP_BODY_KINEMATIC = 2u };
+
+/* One rigid body that bubbles see as an obstacle: a static circle or capsule, or any kinematic body
+ * (NativeRigidBody, NativeRigidPolygonState.swift:25-40). Dynamic bodies are rejected with bubbles
+ * (NativeCompleteStepper.swift:71-88). Pose is the centre of mass at the START of the step; a kinematic body
+ * advances by its velocity over the step inside the library (nativeRigidPredict, NativePostSolveKernels:65-80).
+ * Vertices are local to the centre of mass. 80 bytes. */
+typedef struct bp_body {
+    int64_t id;
+    float position[2];
+    float angle;
+    float bounding_radius;       /* physical.z: radius of the circle around the whole body */
+    float velocity[2];
+    float angular_velocity;
+    float core_radius;           /* shape.y: circle / capsule radius around the core, 0 for a polygon */
+    float half_length;           /* shape.z: capsule half axis */
+    uint32_t kind;               /* BP_BODY_POLYGON / CIRCLE / CAPSULE */
+    uint32_t flags;              /* BP_BODY_STATIC / BP_BODY_KINEMATIC */
+    uint32_t vertex_offset;      /* into bp_world_input.body_vertices (float2 pairs) */
+    uint32_t vertex_count;       /* polygon ring, 1 for a circle, 2 for a capsule */
+    uint32_t triangle_offset;    /* into bp_world_input.body_triangles (uint32 triples) */
+    uint32_t triangle_count;
+    uint32_t category;
+    uint32_t mask;
+    uint32_t reserved;
+} bp_body;
+
+/* Force field (NativeForceField, NativeForceKernels:11-17). 64 bytes. */
+typedef struct bp_force_field {
+    float position[2];
+    float rotation;
+    float falloff;
+    float direction[2];          /* directional strength (local frame) */
+    float strength;              /* radial / vortex strength */
+    float radius;                /* reach of a circle field */
+    uint32_t kind;               /* 0 directional, 1 radial, 2 vortex */
+    uint32_t vertex_offset;      /* polygon shape: into field_vertices */
+    uint32_t vertex_count;       /* 0 = circle */
+    uint32_t filter_offset;      /* into field_object_ids (sorted) */
+    uint32_t filter_count;
+    uint32_t has_filter;
+    uint32_t reserved[2];
+} bp_force_field;
+
+/* Rubber band of a player-driven bubble (NativeBandDrive). Sorted by bubble_id. 24 bytes. */
+typedef struct bp_band {
+    int64_t bubble_id;
+    float target[2];
+    float stiffness;             /* K_band */
+    float maximum_force;         /* 0 = unlimited */
+} bp_band;
+
+/* Motor of a motor-driven bubble (NativeMotor). Sorted by bubble_id. 24 bytes. */
+typedef struct bp_motor {
+    int64_t bubble_id;
+    float force[2];
+    float torque;
+    float inertia;
+} bp_motor;
+
+/* World flags (package switches of NativeMetalConfiguration, NativeMetalSubstepLoop.swift:276-308). */
+enum {
+    BP_WORLD_HAS_REGION = 1u,          /* apply the public region exit policy at the end of the step */
+    BP_WORLD_MINIMUM_MARGIN_ONLY = 2u, /* minimumMarginOnly: margin r/4 only (a rebuild almost every substep) */
+    BP_WORLD_ASSERT_EVERY_SUBSTEP = 4u,/* assertEverySubstep */
+    BP_WORLD_INJECT_STATE = 8u,        /* injectedSubstepState (diagnostic, host-chosen position) */
+    BP_WORLD_NO_END_ASSERTION = 16u,   /* skip the end-of-step contact assertion (it is on by default) */
+    BP_WORLD_FORCE_MULTI_CTA = 32u     /* forceMultipleDispatches: step on the whole-GPU path even when small */
+};
+
+/* Per-world configuration (NativeSolverConfiguration + NativeMetalConfiguration). 64 bytes. */
+typedef struct bp_world_desc {
+    float time_step;                 /* dt of one step */
+    float separation_tolerance;      /* sepTol, default 0.002 */
+    float contact_tolerance;         /* default 0.001 */
+    float substep_split_multiplier;  /* < 1 means 1 */
+    float region[4];                 /* min.xy, max.xy (with BP_WORLD_HAS_REGION) */
+    float global_force[2];           /* force on every force-driven bubble (then x inverse mass) */
+    float gravity[2];                /* acceleration added to force-driven bubbles (0 = reference behaviour) */
+    uint32_t candidate_limit;        /* k: candidates / neighbours per object, 1..128 (default 128) */
+    uint32_t flags;                  /* BP_WORLD_* */
+    int64_t inject_object;           /* BP_WORLD_INJECT_STATE: bubble id */
+} bp_world_desc;
+
+typedef struct bp_world_diagnostics {
+    uint32_t inject_substep;         /* substep of the frame (from 0) after which the state is injected */
+    float inject_position[2];
+    uint32_t reserved;
+} bp_world_diagnostics;
+
+/* Everything a world needs besides its configuration. Arrays may be NULL when their count is 0. */
+typedef struct bp_world_input {
+    const bp_bubble* bubbles;        uint32_t bubble_count;
+    const bp_segment* segments;      uint32_t segment_count;
+    const bp_body* bodies;           uint32_t body_count;
+    const float* body_vertices;      uint32_t body_vertex_count;    /* float2 pairs */
+    const uint32_t* body_triangles;  uint32_t body_triangle_count;  /* uint32 triples */
+    const bp_force_field* fields;    uint32_t field_count;
+    const float* field_vertices;     uint32_t field_vertex_count;   /* float2 pairs */
+    const int64_t* field_object_ids; uint32_t field_object_id_count;
+    const bp_band* bands;            uint32_t band_count;
+    const bp_motor* motors;          uint32_t motor_count;
+    /* Joint exclusion lists (pairs joined without collideConnected have no contact; nativeJointExcluded).
+     * One (start, count) pair per entity: bubbles first, then bodies; partners are object ids. */
+    const uint32_t* joint_ranges;    uint32_t joint_entity_count;
+    const int64_t* joint_partners;   uint32_t joint_partner_count;
+} bp_world_input;
+
+/* Result of one step (NativeMetalFrameTelemetry + failure detail, NativeMetalSubstepLoop.swift:346-396). 96 bytes. */
+typedef struct bp_step_report {
+    int32_t status;                  /* bp_status of this step */
+    uint32_t substep_count;          /* substeps of this step (adaptive) */
+    uint32_t rebuild_count;          /* grid rebuilds forced by the margin inside the step */
+    uint32_t candidate_count;        /* candidates of the last grid build (pairs + segments) */
+    uint32_t body_candidate_count;   /* bubble-body candidates of the last build */
+    uint32_t candidate_overflow;     /* candidates dropped by the per-object limit k (max over builds) */
+    uint32_t max_candidates_per_object;
+    uint32_t contact_count;          /* active end-of-step contact records */
+    uint32_t limiter_term;           /* bp_term of the last substep */
+    uint32_t violation_kind;         /* bp_violation */
+    int64_t limiter_object;          /* bubble id that set h in the last substep */
+    int64_t violation_objects[2];
+    int64_t violation_edge;          /* segment id (edge side violation) */
+    float violation_distance;
+    float cell_width;                /* grid cell width of the last build */
+    float gpu_ms;                    /* device time of the step (batch: of the whole launch) */
+    uint32_t removed_count;          /* bubbles removed by the region this step */
+    uint32_t wrapped_count;
+    uint32_t contact_overflow;       /* contact records beyond the world's record capacity (dropped) */
+} bp_step_report;
+
+/* End-of-step contact record (NativeContactCache, NativeGeometryKernels:26-29). 64 bytes. */
+typedef struct bp_contact {
+    int64_t participants[2];         /* bubble id, bubble id / segment id */
+    uint32_t kind;                   /* 0 bubble-bubble, 1 bubble-segment */
+    uint32_t feature;                /* polygon edge feature: 0 none, 1 interior, 2 convex start vertex */
+    float normal[2];
+    float point[2];
+    float impulse;                   /* F * dt^2 (response.x) */
+    float penetration;               /* response.y */
+    float allowed_side;              /* response.z */
+    uint32_t reserved[3];
+} bp_contact;
+
+/* Candidate key (NativeContactKey, NativeMetalBufferLayout.swift:83-103): kind 0 pair, 1 segment, 2 body. 24 bytes. */
+typedef struct bp_candidate_key {
+    uint32_t kind;
+    uint32_t reserved;
+    int64_t first;
+    int64_t second;
+} bp_candidate_key;
+
+/* ---- context ------------------------------------------------------------------------------------------------ */
+
+typedef struct bp_context bp_context;
+typedef struct bp_world bp_world;
+typedef struct bp_batch bp_batch;
+
+/* Version of this ABI (BP_ABI_VERSION). */
+int bp_abi_version(void);
+/* Human-readable name of a status code (static string). */
+const char* bp_status_string(int status);
+/* Whether a CUDA device usable by this build is present (BP_OK) or not (BP_E_UNAVAILABLE). */
+int bp_device_available(int device);
+
+/* A context binds one CUDA device and one stream (NativeMetalSolver(device:), NativeMetalSolver.swift:355). */
+int bp_context_create(int device, uint32_t flags, bp_context** out);
+int bp_context_destroy(bp_context* context);
+
+/* ---- single world (plain per-world launch path; NativeMetalSolver.executeFrame) ------------------------------- */
+
+/* Creates a world with its state resident on the device. Replaces NativeMetalSolver persistent state
+ * (NativeMetalSolver.swift:122-139) + the first executeSnapshot upload (NativeMetalSolver.swift:461-466). */
+int bp_world_create(bp_context* context, const bp_world_desc* desc, const bp_world_input* input, bp_world** out);
+int bp_world_destroy(bp_world* world);
+/* Overwrites the bubble records (same count and ids as created; e.g. a host-side transaction). */
+int bp_world_write_bubbles(bp_world* world, const bp_bubble* bubbles, uint32_t count);
+int bp_world_set_diagnostics(bp_world* world, const bp_world_diagnostics* diagnostics);
+/* Advances `steps` steps of time_step each (one executeFrame per step; NativeMetalSubstepLoop.run,
+ * NativeMetalSubstepLoop.swift:216-273). reports may be NULL, else holds `steps` entries. Stops at the first
+ * failed step and returns its status. */
+int bp_world_step(bp_world* world, uint32_t steps, bp_step_report* reports);
+/* Readback of the published state (NativeMetalSolver.swift:1061-1067). */
+int bp_world_read_bubbles(bp_world* world, bp_bubble* out, uint32_t capacity, uint32_t* count);
+/* End-of-step contact records of the last step (NativeMetalSolver.swift:1041-1060). */
+int bp_world_read_contacts(bp_world* world, bp_contact* out, uint32_t capacity, uint32_t* count);
+/* Test seams: candidate keys of the last grid build sorted by key (NativeMetalSolver.swift:292-296) and the grid
+ * cell (int64 x, y) of every bubble in the last build (nativeBuildGrid, NativeGeometryKernels:179-189). */
+int bp_world_read_candidates(bp_world* world, bp_candidate_key* out, uint32_t capacity, uint32_t* count);
+int bp_world_read_cells(bp_world* world, int64_t* out_xy, uint32_t capacity, uint32_t* count);
+/* h of every substep of the last step (stepHistory, NativeForceKernels:730). */
+int bp_world_read_substeps(bp_world* world, float* out, uint32_t capacity, uint32_t* count);
+
+/* ---- batch of independent worlds (one fused launch per step for all worlds) ----------------------------------- */
+
+enum {
+    BP_BATCH_PER_WORLD_LAUNCH = 1u, /* step each world with its own launch, one after another (the plain path) */
+    BP_BATCH_USE_GRAPH = 2u,        /* capture the per-step launches in a CUDA graph and replay it */
+    BP_BATCH_AUTOTUNE = 4u          /* choose threads per world per size class by timing on first use */
+};
+
+typedef struct bp_batch_config {
+    uint32_t flags;                  /* BP_BATCH_* */
+    uint32_t threads_per_world;      /* 0 = automatic (autotuner or size rule) */
+    uint32_t reserved[2];
+} bp_batch_config;
+
+int bp_batch_create(bp_context* context, uint32_t world_count, const bp_world_desc* descs,
+                    const bp_world_input* inputs, const bp_batch_config* config, bp_batch** out);
+int bp_batch_destroy(bp_batch* batch);
+/* Advances every live world `steps` steps. reports may be NULL, else world_count entries (status of the first
+ * failure, or the last step; substep_count summed over the steps). Worlds that fail stop; the others go on. */
+int bp_batch_step(bp_batch* batch, uint32_t steps, bp_step_report* reports);
+/* Total bubbles and total substeps x bubbles advanced since creation (for throughput). */
+int bp_batch_counters(bp_batch* batch, uint64_t* bubble_count, uint64_t* bubble_substeps, uint64_t* launches);
+int bp_batch_read_bubbles(bp_batch* batch, uint32_t world, bp_bubble* out, uint32_t capacity, uint32_t* count);
+/* Bulk dynamic state of all worlds in world order: float4 (center.xy, velocity.xy) per bubble. */
+int bp_batch_write_state(bp_batch* batch, const float* center_velocity, uint64_t bubble_count);
+int bp_batch_read_state(bp_batch* batch, float* center_velocity, uint64_t bubble_count);
+/* Threads per world chosen for each size class (class c holds worlds of 2^(c+4) bubbles at most). */
+int bp_batch_tuning(bp_batch* batch, uint32_t* threads_per_class, uint32_t class_count);
+
+/* ---- host helpers (reference host logic that feeds the path) -------------------------------------------------- */
+
+/* One-sided edges of a static polygon (NativeStaticPolygonEdges.segments, NativeStaticPolygonEdges.swift:16-37):
+ * signed area in double, collinear merge at tolerance 1e-5, convex start/end, previous start. Writes at most
+ * `capacity` segments with ids first_id, first_id+1, ... and returns the count in *count. */
+int bp_static_polygon_edges(const float* points_xy, uint32_t point_count, int64_t first_id, int64_t owner_id,
+                            uint32_t has_owner, bp_segment* out, uint32_t capacity, uint32_t* count);
+
+/* Contact law on the device for known-answer tests (NativeMetalContactLawTests.swift:74-218).
+ * mode 0: epsilon(q) of in[i].x; mode 1: wall law (K, r, d) -> (F, eps, k, 0);
+ * mode 2: pair law (K_a, r_a, K_b, r_b, d) -> (F, eps_a, eps_b, k). in/out hold 8 floats per case. */
+int bp_device_contact_law(bp_context* context, uint32_t mode, const float* in, float* out, uint32_t count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BUBBLEPHYSICS_GB300_H */

@@ -1,0 +1,1501 @@
+// bp_oracle.cpp - CPU ORACLE for the bubble step. TEST INFRASTRUCTURE ONLY.
+//
+// This file restates, in plain scalar C++ and in the reference's operation order, the per-step bubble simulation
+// of BubblePhysics v4 (Metal kernels under Sources/BubblePhysicsNativeMetal/Shaders/). It is the checker the CUDA
+// path is compared against; the product never links, loads or calls it. Only tests/, __graft_entry__.smoke() and the
+// cpu_baseline / reference legs of bench.py use it.
+//
+// It is templated on the arithmetic type: T = float is the parity build (bit-for-bit the same formulas the GPU
+// runs), T = double is the FP64 rerun used to report the FP32 error. Build with -ffp-contract=off so no
+// multiply-add is fused behind our back; the one explicit fma of the reference (nativePastSegmentEnd) is kept.
+//
+// Abbreviations in citations: NFK = NativeForceKernels.metal-source, NGK = NativeGeometryKernels.metal-source,
+// NCK = NativeContactKernels.metal-source, NPK = NativePostSolveKernels.metal-source (all under
+// Sources/BubblePhysicsNativeMetal/Shaders/).
+//
+// Deliberate, documented differences from the reference (both the oracle and the CUDA path follow them):
+//  - gravity: an acceleration added to the non-contact acceleration of force-driven bubbles (the reference only has a
+//    per-bubble global force; with gravity = 0 nothing changes);
+//  - adjacency overflow keeps the first k neighbours in (kind, neighbour) order; the reference keeps an
+//    atomic-order-dependent subset (NCK:186-195 says so itself), the dropped count is the same;
+//  - the contact assertion reports the violation of the lowest bubble index (the reference: whichever thread wins a
+//    compare-and-swap, NFK:848-854).
+
+#include "../include/bubblephysics.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <new>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+template <typename T> struct V2 {
+    T x, y;
+};
+template <typename T> inline V2<T> mk(T x, T y) { return V2<T>{x, y}; }
+template <typename T> inline V2<T> operator+(V2<T> a, V2<T> b) { return {a.x + b.x, a.y + b.y}; }
+template <typename T> inline V2<T> operator-(V2<T> a, V2<T> b) { return {a.x - b.x, a.y - b.y}; }
+template <typename T> inline V2<T> operator*(V2<T> a, T s) { return {a.x * s, a.y * s}; }
+template <typename T> inline V2<T> operator*(T s, V2<T> a) { return {s * a.x, s * a.y}; }
+template <typename T> inline V2<T> operator/(V2<T> a, T s) { return {a.x / s, a.y / s}; }
+template <typename T> inline V2<T> operator-(V2<T> a) { return {-a.x, -a.y}; }
+template <typename T> inline T dot(V2<T> a, V2<T> b) { return a.x * b.x + a.y * b.y; }
+template <typename T> inline T len(V2<T> a) { return std::sqrt(a.x * a.x + a.y * a.y); }
+template <typename T> inline V2<T> vmin(V2<T> a, V2<T> b) { return {std::fmin(a.x, b.x), std::fmin(a.y, b.y)}; }
+template <typename T> inline V2<T> vmax(V2<T> a, V2<T> b) { return {std::fmax(a.x, b.x), std::fmax(a.y, b.y)}; }
+template <typename T> inline V2<T> vclamp(V2<T> a, V2<T> lo, V2<T> hi) { return vmin(vmax(a, lo), hi); }
+template <typename T> inline T clampv(T v, T lo, T hi) { return std::fmin(std::fmax(v, lo), hi); }
+template <typename T> inline bool finite2(V2<T> a) { return std::isfinite(a.x) && std::isfinite(a.y); }
+template <typename T> inline T cross(V2<T> a, V2<T> b) { return a.x * b.y - a.y * b.x; }
+
+template <typename T> struct Lim {
+    static T tiny() { return std::numeric_limits<T>::min(); }  // FLT_MIN of the reference
+    static T inf() { return std::numeric_limits<T>::infinity(); }
+    static T big() { return std::numeric_limits<T>::max(); }   // FLT_MAX
+};
+
+constexpr uint32_t kFrameLimit = 1024;  // nativeSubstepFrameLimit, NFK:384
+constexpr uint32_t kNewtonSteps = 12;   // nativePairNewtonSteps, NFK:39
+constexpr uint32_t kRemovedFlag = 0x80000000u;
+
+// ---------------------------------------------------------------------------------------------------------------
+// Contact law (NFK:36-102)
+// ---------------------------------------------------------------------------------------------------------------
+template <typename T> struct Law {
+    T force, epsA, epsB, stiffness;
+};
+
+// nativeEpsilonFromForceRatio, NFK:50-53
+template <typename T> T epsilon_from_ratio(T q) {
+    if (!(q > 0)) return 0;
+    return T(2) * q / ((T(2) * q + T(1)) + std::sqrt(T(4) * q + T(1)));
+}
+// nativeRestFromForceRatio, NFK:55-57
+template <typename T> T rest_from_ratio(T q) { return T(2) / (T(1) + std::sqrt(std::fmax(T(4) * q, T(0)) + T(1))); }
+
+// nativeWallContactLaw, NFK:60-69
+template <typename T> Law<T> wall_law(T K, T r, T distance) {
+    Law<T> law{0, 0, 0, 0};
+    T d = std::fmax(distance, r * T(1e-6));
+    if (!(K > 0) || !(r > 0) || !(d < r)) return law;
+    T rest = d / r;
+    law.epsA = (r - d) / r;
+    law.force = K * (r - d) * r / (d * d);
+    law.stiffness = K * (T(1) + law.epsA) / (r * rest * rest * rest);
+    return law;
+}
+
+// nativePairContactLaw, NFK:75-102
+template <typename T> Law<T> pair_law(T Ka, T ra, T Kb, T rb, T distance) {
+    Law<T> law{0, 0, 0, 0};
+    T R = ra + rb;
+    T d = std::fmax(distance, R * T(1e-6));
+    T overlap = R - d;
+    if (!(Ka > 0) || !(Kb > 0) || !(overlap > 0)) return law;
+    T lowest = std::fmin(Ka, Kb) * overlap * R / (d * d);
+    T force = lowest;
+    if (Ka != Kb) {
+        for (uint32_t step = 0; step < kNewtonSteps; ++step) {
+            T qa = force / Ka, qb = force / Kb;
+            T ea = epsilon_from_ratio(qa), eb = epsilon_from_ratio(qb);
+            T rsa = rest_from_ratio(qa), rsb = rest_from_ratio(qb);
+            T residual = ra * ea + rb * eb - overlap;
+            T slope = ra * rsa * rsa * rsa / ((T(1) + ea) * Ka) + rb * rsb * rsb * rsb / ((T(1) + eb) * Kb);
+            if (!(slope > Lim<T>::tiny())) break;
+            force = std::fmax(force - residual / slope, lowest);
+        }
+    }
+    T qa = force / Ka, qb = force / Kb;
+    T ea = epsilon_from_ratio(qa), eb = epsilon_from_ratio(qb);
+    T rsa = rest_from_ratio(qa), rsb = rest_from_ratio(qb);
+    T compliance = ra * rsa * rsa * rsa / ((T(1) + ea) * Ka) + rb * rsb * rsb * rsb / ((T(1) + eb) * Kb);
+    law.force = force;
+    law.epsA = ea;
+    law.epsB = eb;
+    law.stiffness = compliance > Lim<T>::tiny() ? T(1) / compliance : T(0);
+    return law;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// World state
+// ---------------------------------------------------------------------------------------------------------------
+template <typename T> struct Body {
+    int64_t id;
+    V2<T> pos, prev;          // end-of-step pose (after the kinematic advance) and start-of-step pose
+    T angle, prevAngle;
+    V2<T> vel;
+    T omega;
+    T radius;                 // bounding radius (physical.z)
+    T coreRadius;
+    uint32_t kind, flags, voff, vcount, toff, tcount, cat, mask;
+    T cosPrev, sinPrev, cosEnd, sinEnd;  // host-computed rotation of both poses (same in the CUDA path)
+};
+
+template <typename T> struct Field {
+    V2<T> pos;
+    T cosr, sinr, falloff;
+    V2<T> dir;
+    T strength, radius;
+    uint32_t kind, voff, vcount, foff, fcount, hasFilter;
+};
+
+template <typename T> struct World {
+    // configuration
+    T dt, sepTol, contactTol, split;
+    V2<T> rmin, rmax, globalForce, gravity;
+    uint32_t limit, flags;
+    int64_t injectObject;
+    uint32_t injectSubstep;
+    V2<T> injectPos;
+    bool failed = false;
+
+    // bubbles (sorted by id)
+    uint32_t n;
+    std::vector<int64_t> id;
+    std::vector<V2<T>> pos, start, vel, acc, a0, ref, force;
+    std::vector<T> rot, omega, mass, invMass, radius, K, gamma, margin;
+    std::vector<uint32_t> flags_, cat, mask, result;
+
+    // published copy (a failed step publishes nothing)
+    std::vector<V2<T>> pPos, pStart, pVel;
+    std::vector<T> pRot, pOmega;
+    std::vector<uint32_t> pResult, pFlags;
+
+    // segments
+    uint32_t s;
+    std::vector<int64_t> sid, sowner;
+    std::vector<V2<T>> sa, sb, sprev;
+    std::vector<T> soutward, sallowed;
+    std::vector<uint32_t> sflags, scat, smask;
+
+    // bodies
+    std::vector<Body<T>> bodies;
+    std::vector<Body<T>> pBodies;
+    std::vector<V2<T>> bverts;
+    std::vector<uint32_t> btris;
+
+    // forces
+    std::vector<Field<T>> fields;
+    std::vector<V2<T>> fverts;
+    std::vector<int64_t> fids;
+    std::vector<bp_band> bands;
+    std::vector<bp_motor> motors;
+    std::vector<uint32_t> jranges;
+    std::vector<int64_t> jpartners;
+
+    // step control (NativeSubstepControl, NFK:22-26)
+    T timeX, timeY, timeZ, timeW;
+    uint32_t countsX, countsY, countsZ, countsW;
+    int64_t limiterObject;
+    uint32_t limiterTerm;
+    std::vector<T> history;
+
+    // broadphase products of the last build
+    T cellWidth;
+    std::vector<int64_t> cellX, cellY;
+    std::vector<uint8_t> cellValid;
+    // forward candidate row per bubble: pair neighbours (index > i) then segment indices, both ascending
+    std::vector<std::vector<uint32_t>> rowPairs, rowSegs;
+    // body rows: bubble indices ascending
+    std::vector<std::vector<uint32_t>> bodyRows;
+    // adjacency (kind << 30 | neighbour), sorted, capped at k
+    std::vector<std::vector<uint32_t>> adj;
+    uint32_t overflowBuild = 0, overflowMax = 0, maxPerObject = 0, rebuilds = 0;
+
+    // end-of-step
+    std::vector<bp_contact> contacts;
+    bp_step_report lastReport{};
+};
+
+template <typename T> inline bool is_removed(const World<T>& w, uint32_t i) { return (w.flags_[i] & kRemovedFlag) != 0; }
+// nativeIsStatic / nativeInverseMass / nativeIsForceDriven / nativeEffectiveVelocity, NFK:388-392
+template <typename T> inline bool is_static(const World<T>& w, uint32_t i) {
+    return !(w.invMass[i] > 0) || ((w.flags_[i] & BP_BUBBLE_ENABLED) && (w.flags_[i] & BP_BUBBLE_STATIC));
+}
+template <typename T> inline T inv_mass(const World<T>& w, uint32_t i) { return is_static(w, i) ? T(0) : w.invMass[i]; }
+template <typename T> inline bool force_driven(const World<T>& w, uint32_t i) { return (w.flags_[i] & BP_BUBBLE_FORCE_DRIVEN) != 0; }
+template <typename T> inline V2<T> eff_vel(const World<T>& w, uint32_t i) { return is_static(w, i) ? mk<T>(0, 0) : w.vel[i]; }
+
+// nativeFilterAccepts, NGK:124-126
+inline bool filter_accepts(uint32_t ca, uint32_t ma, uint32_t cb, uint32_t mb) { return (ca & mb) != 0 && (cb & ma) != 0; }
+
+// nativeJointExcluded, NGK:254-258
+template <typename T> bool joint_excluded(const World<T>& w, uint32_t entity, int64_t partner) {
+    if (entity >= w.jranges.size() / 2) return false;
+    uint32_t start = w.jranges[2 * entity], count = w.jranges[2 * entity + 1];
+    for (uint32_t i = 0; i < count; ++i)
+        if (w.jpartners[start + i] == partner) return true;
+    return false;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Geometry helpers (NGK:430-500, 660-681)
+// ---------------------------------------------------------------------------------------------------------------
+// nativeClosestPoint, NGK:437-441
+template <typename T> V2<T> closest_point(V2<T> p, V2<T> a, V2<T> b) {
+    V2<T> edge = b - a;
+    T square = dot(edge, edge);
+    T t = square > Lim<T>::tiny() ? clampv(dot(p - a, edge) / square, T(0), T(1)) : T(0);
+    return a + edge * t;
+}
+// nativePastSegmentEnd, NGK:665-668 (explicit fma)
+template <typename T> bool past_segment_end(V2<T> center, V2<T> from, V2<T> to) {
+    V2<T> edge = to - from, rel = center - from;
+    return std::fma(rel.x, edge.x, rel.y * edge.y) >= std::fma(edge.x, edge.x, edge.y * edge.y);
+}
+template <typename T> V2<T> rotate_cs(V2<T> p, T c, T s) { return {p.x * c - p.y * s, p.x * s + p.y * c}; }
+
+// nativeWallRegion, NFK:112-136
+template <typename T> bool wall_region(const World<T>& w, uint32_t si, V2<T> center, V2<T>& normal, T& distance) {
+    V2<T> start = w.sa[si], end = w.sb[si], edge = end - start;
+    T edgeLength = len(edge);
+    V2<T> base = edgeLength > 0 ? mk(-edge.y, edge.x) / edgeLength : mk<T>(0, 1);
+    if (w.sflags[si] & BP_SEGMENT_POLYGON_EDGE) {
+        V2<T> outward = base * w.soutward[si];
+        T along = dot(center - start, edge);
+        bool convexStart = (w.sflags[si] & BP_SEGMENT_CONVEX_START) != 0;
+        if (convexStart && along <= 0 && past_segment_end(center, w.sprev[si], start)) {
+            V2<T> delta = center - start;
+            distance = len(delta);
+            normal = distance > 0 ? delta / distance : outward;
+        } else if (along > 0 && !past_segment_end(center, start, end) && dot(center - start, outward) >= 0) {
+            normal = outward;
+            distance = dot(center - start, outward);
+        } else {
+            return false;
+        }
+    } else {
+        V2<T> delta = center - closest_point(center, start, end);
+        distance = len(delta);
+        normal = distance > 0 ? delta / distance : base;
+    }
+    return true;
+}
+template <typename T> bool wall_contact(const World<T>& w, uint32_t si, V2<T> center, T radius, V2<T>& normal, T& d) {
+    return wall_region(w, si, center, normal, d) && d < radius;
+}
+
+// Body pose at a fraction of the step (nativeBodyAtFraction, NFK:155-159) with its rotation.
+template <typename T> struct Pose {
+    V2<T> pos;
+    T c, s;
+};
+template <typename T> Pose<T> body_at(const Body<T>& b, T fraction) {
+    Pose<T> p;
+    p.pos = b.prev + (b.pos - b.prev) * fraction;
+    T angle = b.prevAngle + (b.angle - b.prevAngle) * fraction;
+    if (angle == b.prevAngle) { p.c = b.cosPrev; p.s = b.sinPrev; }
+    else if (angle == b.angle) { p.c = b.cosEnd; p.s = b.sinEnd; }
+    else { p.c = std::cos(angle); p.s = std::sin(angle); }
+    return p;
+}
+template <typename T> V2<T> body_vertex(const World<T>& w, const Body<T>& b, const Pose<T>& p, uint32_t i) {
+    return p.pos + rotate_cs(w.bverts[b.voff + i], p.c, p.s);
+}
+// nativeRigidInside, NGK:477-490
+template <typename T> bool rigid_inside(const World<T>& w, V2<T> pt, const Body<T>& b, const Pose<T>& p) {
+    if (b.kind != BP_BODY_POLYGON) {
+        V2<T> ca = body_vertex(w, b, p, 0), cb = b.vcount > 1 ? body_vertex(w, b, p, 1) : ca;
+        return len(pt - closest_point(pt, ca, cb)) <= b.coreRadius;
+    }
+    V2<T> local = rotate_cs(pt - p.pos, p.c, -p.s);
+    for (uint32_t i = 0; i < b.tcount; ++i) {
+        const uint32_t* t = &w.btris[3 * (b.toff + i)];
+        V2<T> a = w.bverts[b.voff + t[0]], bb = w.bverts[b.voff + t[1]], c = w.bverts[b.voff + t[2]];
+        if (cross(bb - a, local - a) >= 0 && cross(c - bb, local - bb) >= 0 && cross(a - c, local - c) >= 0) return true;
+    }
+    return false;
+}
+
+template <typename T> struct Obstacle {
+    V2<T> normal;
+    T distance;
+    V2<T> velocity;
+    T speedBound;
+};
+// nativeBodyObstacle, NFK:170-210
+template <typename T> Obstacle<T> body_obstacle(const World<T>& w, const Body<T>& b, T fraction, V2<T> center) {
+    Pose<T> p = body_at(b, fraction);
+    Obstacle<T> o;
+    V2<T> point, normal;
+    T distance;
+    if (b.kind != BP_BODY_POLYGON) {
+        V2<T> ca = body_vertex(w, b, p, 0), cb = b.vcount > 1 ? body_vertex(w, b, p, 1) : ca;
+        point = closest_point(center, ca, cb);
+        V2<T> delta = center - point;
+        T away = len(delta);
+        V2<T> axis = cb - ca;
+        T axisLength = len(axis);
+        V2<T> fallback = axisLength > T(1e-6) ? mk(-axis.y, axis.x) / axisLength : mk<T>(0, 1);
+        normal = away > T(1e-7) ? delta / away : fallback;
+        distance = away - b.coreRadius;
+        point = point + normal * b.coreRadius;
+    } else {
+        T best = Lim<T>::inf();
+        V2<T> nearest = mk<T>(0, 0), outward = mk<T>(0, 1);
+        for (uint32_t e = 0; e < b.vcount; ++e) {
+            V2<T> pp = body_vertex(w, b, p, e), q = body_vertex(w, b, p, (e + 1) % b.vcount);
+            V2<T> cand = closest_point(center, pp, q);
+            T d = len(center - cand);
+            if (d < best) {
+                best = d;
+                nearest = cand;
+                V2<T> edge = q - pp;
+                T size = len(edge);
+                outward = size > Lim<T>::tiny() ? mk(edge.y, -edge.x) / size : mk<T>(0, 1);
+            }
+        }
+        bool inside = rigid_inside(w, center, b, p);
+        normal = inside ? outward : (best > T(1e-7) ? (center - nearest) / best : outward);
+        distance = inside ? -best : best;
+        point = nearest;
+    }
+    V2<T> arm = point - p.pos;
+    o.normal = normal;
+    o.distance = distance;
+    o.velocity = b.vel + mk(-arm.y, arm.x) * b.omega;
+    o.speedBound = len(b.vel) + std::fabs(b.omega) * len(arm);
+    return o;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Non-contact acceleration (NFK:389-470)
+// ---------------------------------------------------------------------------------------------------------------
+template <typename T> V2<T> field_force(const World<T>& w, const Field<T>& f, V2<T> point) {
+    V2<T> delta = point - f.pos;
+    T c = f.cosr, s = f.sinr;
+    V2<T> local = mk(c * delta.x + s * delta.y, -s * delta.x + c * delta.y);
+    T distance = len(local), radius = f.radius;
+    if (f.vcount == 0) {
+        if (!(distance <= radius)) return mk<T>(0, 0);
+    } else {
+        bool inside = false;
+        for (uint32_t i = 0; i < f.vcount; ++i) {
+            V2<T> a = w.fverts[f.voff + i], b = w.fverts[f.voff + (i + 1) % f.vcount];
+            if ((a.y > local.y) != (b.y > local.y) && local.x < (b.x - a.x) * (local.y - a.y) / (b.y - a.y) + a.x) inside = !inside;
+        }
+        if (!inside) return mk<T>(0, 0);
+    }
+    if (f.kind == 0) return mk(c * f.dir.x - s * f.dir.y, s * f.dir.x + c * f.dir.y);
+    if (!(distance > 0)) return mk<T>(0, 0);
+    T profile = f.falloff == 0 ? T(1) : std::pow(std::fmax(T(0), T(1) - distance / radius), f.falloff);
+    T scale = f.strength * profile / distance;
+    return f.kind == 2 ? mk(-delta.y, delta.x) * scale : delta * scale;
+}
+template <typename T> bool field_affects(const World<T>& w, const Field<T>& f, int64_t id) {
+    if (!f.hasFilter) return true;
+    uint32_t low = f.foff, end = f.foff + f.fcount, high = end;
+    while (low < high) {
+        uint32_t mid = low + (high - low) / 2;
+        if (w.fids[mid] < id) low = mid + 1; else high = mid;
+    }
+    return low < end && w.fids[low] == id;
+}
+template <typename R> const R* find_by_bubble(const std::vector<R>& v, int64_t id) {
+    uint32_t low = 0, high = (uint32_t)v.size();
+    while (low < high) {
+        uint32_t mid = low + (high - low) / 2;
+        if (v[mid].bubble_id < id) low = mid + 1; else high = mid;
+    }
+    return low < v.size() && v[low].bubble_id == id ? &v[low] : nullptr;
+}
+// nativeNonContactAcceleration, NFK:450-470 (+ the gravity acceleration of this framework)
+template <typename T> V2<T> non_contact_acc(const World<T>& w, uint32_t i, V2<T> position) {
+    T im = inv_mass(w, i);
+    if (!force_driven(w, i) || !(im > 0)) return mk<T>(0, 0);
+    V2<T> f = w.globalForce;
+    int64_t id = w.id[i];
+    for (const Field<T>& fl : w.fields)
+        if (field_affects(w, fl, id)) f = f + field_force(w, fl, position);
+    if (!w.bands.empty()) {
+        const bp_band* band = find_by_bubble(w.bands, id);
+        if (band) {
+            V2<T> bf = (mk<T>(band->target[0], band->target[1]) - position) * T(band->stiffness);
+            T lim = band->maximum_force, magnitude = len(bf);
+            if (lim > 0 && magnitude > lim) bf = bf * (lim / magnitude);
+            f = f + bf;
+        }
+    }
+    if (!w.motors.empty()) {
+        const bp_motor* motor = find_by_bubble(w.motors, id);
+        if (motor) f = f + mk<T>(motor->force[0], motor->force[1]);
+    }
+    V2<T> a = f * im;
+    if (w.gravity.x != 0 || w.gravity.y != 0) a = a + w.gravity;
+    return a;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Broadphase (NFK:492-506, NGK:163-426, NCK:181-246, NFK:298-331)
+// ---------------------------------------------------------------------------------------------------------------
+template <typename T> void broadphase(World<T>& w) {
+    const uint32_t n = w.n, k = w.limit;
+    // a0, margin, x0 (nativeBubbleAcceleration + nativeBubbleMargin, NFK:472-499)
+    T t = std::fmax(w.timeX - w.timeY, T(0));
+    for (uint32_t i = 0; i < n; ++i) {
+        w.a0[i] = non_contact_acc(w, i, w.pos[i]);
+        T travel = len(eff_vel(w, i)) * t + T(0.5) * len(w.a0[i]) * t * t;
+        w.margin[i] = (w.flags & BP_WORLD_MINIMUM_MARGIN_ONLY) ? T(0.25) * w.radius[i]
+                                                              : std::fmax(T(1.05) * travel, T(0.25) * w.radius[i]);
+        w.ref[i] = w.pos[i];
+    }
+    // cell width (nativePrepareGrid, NGK:163-177)
+    T cw = w.sepTol;
+    for (uint32_t i = 0; i < n; ++i) {
+        if (is_removed(w, i)) continue;
+        cw = std::fmax(cw, T(2) * (w.radius[i] + w.margin[i]) + w.sepTol);
+    }
+    cw = std::fmax(cw, Lim<T>::tiny());
+    w.cellWidth = cw;
+    // cells (nativeBuildGrid, NGK:179-189)
+    std::vector<uint32_t> order;
+    order.reserve(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        bool valid = !is_removed(w, i) && finite2(w.pos[i]);
+        w.cellValid[i] = valid;
+        if (valid) {
+            T fx = std::floor(w.pos[i].x / cw), fy = std::floor(w.pos[i].y / cw);
+            const T lim = T(4.0e18);
+            w.cellX[i] = (int64_t)clampv(fx, -lim, lim);
+            w.cellY[i] = (int64_t)clampv(fy, -lim, lim);
+            order.push_back(i);
+        } else {
+            w.cellX[i] = 0;
+            w.cellY[i] = 0;
+        }
+    }
+    // sort by (cell.x, cell.y, index) (nativeGridLess, NGK:191-196)
+    std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+        if (w.cellX[a] != w.cellX[b]) return w.cellX[a] < w.cellX[b];
+        if (w.cellY[a] != w.cellY[b]) return w.cellY[a] < w.cellY[b];
+        return a < b;
+    });
+    uint32_t buildOverflow = 0;
+    // candidate rows (nativeEmitBubbleCandidates + nativeFinishBubbleRow, NGK:262-330)
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : buildOverflow) if (n > 4096)
+    for (uint32_t i = 0; i < n; ++i) {
+        std::vector<uint32_t>& rp = w.rowPairs[i];
+        std::vector<uint32_t>& rs = w.rowSegs[i];
+        rp.clear();
+        rs.clear();
+        if (!w.cellValid[i] || !finite2(w.start[i])) continue;
+        int64_t cx = w.cellX[i], cy = w.cellY[i];
+        for (int dx = -1; dx <= 1; ++dx) {
+            int64_t tx = cx + dx, ty = cy - 1;
+            // lower bound of (tx, ty) in the sorted grid
+            uint32_t low = 0, high = (uint32_t)order.size();
+            while (low < high) {
+                uint32_t mid = low + (high - low) / 2;
+                uint32_t e = order[mid];
+                if (w.cellX[e] < tx || (w.cellX[e] == tx && w.cellY[e] < ty)) low = mid + 1; else high = mid;
+            }
+            for (uint32_t q = low; q < order.size() && w.cellX[order[q]] == tx && w.cellY[order[q]] <= ty + 2; ++q) {
+                uint32_t j = order[q];
+                if (j <= i) continue;
+                // nativeBubblePairCandidate, NGK:262-273
+                if (!filter_accepts(w.cat[i], w.mask[i], w.cat[j], w.mask[j])) continue;
+                if (joint_excluded(w, i, w.id[j])) continue;
+                T reach = w.radius[i] + w.radius[j] + w.margin[i] + w.margin[j] + w.sepTol;
+                if (std::fabs(w.pos[i].x - w.pos[j].x) <= reach && std::fabs(w.pos[i].y - w.pos[j].y) <= reach) rp.push_back(j);
+            }
+        }
+        std::sort(rp.begin(), rp.end());
+        // segments (nativeFinishBubbleRow, NGK:276-290)
+        for (uint32_t j = 0; j < w.s; ++j) {
+            if (!filter_accepts(w.cat[i], w.mask[i], w.scat[j], w.smask[j])) continue;
+            if ((w.sflags[j] & BP_SEGMENT_HAS_OWNER) && joint_excluded(w, i, w.sowner[j])) continue;
+            T reach = w.radius[i] + w.margin[i] + w.sepTol;
+            V2<T> lower = vmin(w.sa[j], w.sb[j]) - mk(reach, reach);
+            V2<T> upper = vmax(w.sa[j], w.sb[j]) + mk(reach, reach);
+            V2<T> p = w.pos[i];
+            if (p.x >= lower.x && p.y >= lower.y && p.x <= upper.x && p.y <= upper.y) rs.push_back(j);
+        }
+        // keep the k smallest keys (nativeInsertCandidate, NGK:238-251): pairs sort before segments
+        uint32_t total = (uint32_t)(rp.size() + rs.size());
+        if (total > k) {
+            buildOverflow += total - k;
+            if (rp.size() >= k) { rp.resize(k); rs.clear(); }
+            else rs.resize(k - rp.size());
+        }
+#pragma omp critical
+        w.maxPerObject = std::max(w.maxPerObject, total);
+    }
+    // body rows (nativeEmitBodyCandidates, NGK:350-415, mode bit 1 = no body pairs)
+    for (size_t b = 0; b < w.bodies.size(); ++b) {
+        const Body<T>& body = w.bodies[b];
+        std::vector<uint32_t>& row = w.bodyRows[b];
+        row.clear();
+        bool obstacle = (body.flags & BP_BODY_STATIC) ? body.kind != BP_BODY_POLYGON : (body.flags & BP_BODY_KINEMATIC) != 0;
+        if (!obstacle) continue;
+        V2<T> bodyLow = vmin(body.pos, body.prev) - mk(body.radius, body.radius);
+        V2<T> bodyHigh = vmax(body.pos, body.prev) + mk(body.radius, body.radius);
+        uint32_t entity = n + (uint32_t)b;
+        uint32_t total = 0;
+        for (uint32_t a = 0; a < n; ++a) {
+            if (is_removed(w, a)) continue;
+            if (!filter_accepts(w.cat[a], w.mask[a], body.cat, body.mask)) continue;
+            if (joint_excluded(w, entity, w.id[a])) continue;
+            T reach = w.radius[a] + std::fmax(w.margin[a], T(0));
+            V2<T> lo = w.pos[a] - mk(reach, reach), hi = w.pos[a] + mk(reach, reach);
+            bool hit = !(hi.x < bodyLow.x || hi.y < bodyLow.y || bodyHigh.x < lo.x || bodyHigh.y < lo.y);
+            if (!hit) continue;
+            ++total;
+            if (row.size() < k) row.push_back(a);
+        }
+        if (total > k) buildOverflow += total - k;
+        w.maxPerObject = std::max(w.maxPerObject, total);
+    }
+    // adjacency (nativeEmitCandidateEdges + nativeEmitBodyEdges + nativeBuildAdjacencyRow)
+    for (uint32_t i = 0; i < n; ++i) w.adj[i].clear();
+    for (uint32_t i = 0; i < n; ++i) {
+        for (uint32_t j : w.rowPairs[i]) {
+            w.adj[i].push_back(j);
+            w.adj[j].push_back(i);
+        }
+        for (uint32_t sg : w.rowSegs[i]) w.adj[i].push_back((1u << 30) | sg);
+    }
+    for (size_t b = 0; b < w.bodies.size(); ++b)
+        for (uint32_t a : w.bodyRows[b]) w.adj[a].push_back((2u << 30) | (uint32_t)b);
+    for (uint32_t i = 0; i < n; ++i) {
+        std::vector<uint32_t>& row = w.adj[i];
+        std::sort(row.begin(), row.end());  // (kind, neighbour) order: kind is in the top bits
+        uint32_t demanded = (uint32_t)row.size();
+        if (demanded > k) {
+            buildOverflow += demanded - k;
+            row.resize(k);
+        }
+        w.maxPerObject = std::max(w.maxPerObject, demanded);
+    }
+    w.overflowBuild = buildOverflow;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Substep functions
+// ---------------------------------------------------------------------------------------------------------------
+template <typename T> T step_fraction(const World<T>& w) {
+    return w.timeX > 0 ? clampv(w.timeY / w.timeX, T(0), T(1)) : T(1);  // nativeStepFraction, NFK:150-152
+}
+
+// nativeBubbleContactForce, NFK:216-243
+template <typename T> V2<T> contact_force(const World<T>& w, uint32_t i, T fraction) {
+    V2<T> total = mk<T>(0, 0);
+    T radius = w.radius[i], K = w.K[i];
+    for (uint32_t e : w.adj[i]) {
+        uint32_t kind = e >> 30, j = e & 0x3fffffffu;
+        if (kind == 0) {
+            uint32_t low = std::min(i, j), high = std::max(i, j);
+            V2<T> delta = w.pos[high] - w.pos[low];
+            T d = len(delta);
+            V2<T> normal = d > 0 ? delta / d : mk<T>(1, 0);
+            Law<T> law = pair_law(w.K[low], w.radius[low], w.K[high], w.radius[high], d);
+            total = total + normal * (i == low ? -law.force : law.force);
+        } else if (kind == 1) {
+            V2<T> normal;
+            T d;
+            if (!wall_contact(w, j, w.pos[i], radius, normal, d)) continue;
+            total = total + normal * wall_law(K, radius, d).force;
+        } else {
+            Obstacle<T> o = body_obstacle(w, w.bodies[j], fraction, w.pos[i]);
+            total = total + o.normal * wall_law(K, radius, o.distance).force;
+        }
+    }
+    return total;
+}
+
+// nativeBubbleOmegaSquared, NFK:510-541
+template <typename T> T omega_squared(const World<T>& w, uint32_t i, T fraction) {
+    T im = inv_mass(w, i);
+    if (!(im > 0)) return 0;
+    T radius = w.radius[i], K = w.K[i], total = 0;
+    if (!w.bands.empty()) {
+        const bp_band* band = find_by_bubble(w.bands, w.id[i]);
+        if (band) total = total + T(band->stiffness) * im;
+    }
+    for (uint32_t e : w.adj[i]) {
+        uint32_t kind = e >> 30, j = e & 0x3fffffffu;
+        if (kind == 0) {
+            uint32_t low = std::min(i, j), high = std::max(i, j);
+            T d = len(w.pos[high] - w.pos[low]);
+            Law<T> law = pair_law(w.K[low], w.radius[low], w.K[high], w.radius[high], d);
+            total = total + law.stiffness * (im + std::sqrt(im * inv_mass(w, j)));
+        } else if (kind == 1) {
+            V2<T> normal;
+            T d;
+            if (!wall_contact(w, j, w.pos[i], radius, normal, d)) continue;
+            total = total + wall_law(K, radius, d).stiffness * im;
+        } else {
+            Obstacle<T> o = body_obstacle(w, w.bodies[j], fraction, w.pos[i]);
+            total = total + wall_law(K, radius, o.distance).stiffness * im;
+        }
+    }
+    return total;
+}
+
+// nativeBubbleDistanceBound, NFK:550-598
+template <typename T> T distance_bound(const World<T>& w, uint32_t i, T hMax, T fraction) {
+    if (!(inv_mass(w, i) > 0)) return Lim<T>::inf();
+    V2<T> velocity = w.vel[i];
+    T radius = w.radius[i], best = Lim<T>::inf();
+    for (uint32_t e : w.adj[i]) {
+        uint32_t kind = e >> 30, j = e & 0x3fffffffu;
+        T distance, approach, accSum, reach, bodySpeed = 0;
+        if (kind == 0) {
+            V2<T> delta = w.pos[j] - w.pos[i];
+            distance = len(delta);
+            V2<T> normal = distance > 0 ? delta / distance : mk<T>(1, 0);
+            approach = dot(velocity - eff_vel(w, j), normal);
+            accSum = len(w.acc[i]) + len(w.acc[j]);
+            reach = radius + w.radius[j];
+        } else if (kind == 1) {
+            V2<T> normal;
+            if (!wall_region(w, j, w.pos[i], normal, distance)) continue;
+            approach = -dot(velocity, normal);
+            accSum = len(w.acc[i]);
+            reach = radius;
+        } else {
+            Obstacle<T> o = body_obstacle(w, w.bodies[j], fraction, w.pos[i]);
+            distance = o.distance;
+            approach = -dot(velocity, o.normal);
+            bodySpeed = o.speedBound;
+            accSum = len(w.acc[i]);
+            reach = radius;
+        }
+        bool active = distance < reach;
+        T d = std::fmax(distance, reach * T(1e-6));
+        T speed;
+        if (active) speed = std::fabs(approach) + bodySpeed;
+        else {
+            if (approach + bodySpeed + accSum * hMax * T(0.5) <= 0) continue;
+            speed = approach + bodySpeed;
+        }
+        T sq = std::sqrt(speed * speed + accSum * d * T(0.5));
+        T denominator = sq + speed;
+        if (!(denominator > 0)) continue;
+        best = std::fmin(best, d / (T(2) * denominator));
+    }
+    return best;
+}
+
+// nativeBubbleMarginBound, NFK:604-614
+template <typename T> T margin_bound(const World<T>& w, uint32_t i) {
+    if (!(inv_mass(w, i) > 0)) return Lim<T>::inf();
+    T left = w.margin[i] - len(w.pos[i] - w.ref[i]);
+    if (std::isnan(left)) return Lim<T>::inf();
+    if (left <= 0) return 0;
+    T speed = len(w.vel[i]), a = len(w.acc[i]);
+    T denominator = speed + std::sqrt(speed * speed + T(2) * a * left);
+    return denominator > 0 ? T(2) * left / denominator : Lim<T>::inf();
+}
+
+// nativeHalfImpulseFactor, NFK:754-758
+template <typename T> T half_impulse(T gamma, T halfStep) {
+    T x = gamma * halfStep;
+    if (x < T(0.05))
+        return halfStep * (T(1) - x * T(0.5) + x * x * (T(1) / T(6)) - x * x * x * (T(1) / T(24)) + x * x * x * x * (T(1) / T(120)));
+    return (T(1) - std::exp(-x)) / gamma;
+}
+
+// All bubble-level phases skip removed bubbles: the reference host drops them from the world.
+template <typename T> void contact_forces_all(World<T>& w) {
+    T fraction = step_fraction(w);
+#pragma omp parallel for schedule(static) if (w.n > 4096)
+    for (uint32_t i = 0; i < w.n; ++i) w.force[i] = is_removed(w, i) ? mk<T>(0, 0) : contact_force(w, i, fraction);
+}
+
+// nativeIntegratePhase, NFK:765-802
+template <typename T> void integrate(World<T>& w, uint32_t phase) {
+#pragma omp parallel for schedule(static) if (w.n > 4096)
+    for (uint32_t i = 0; i < w.n; ++i) {
+        if (is_removed(w, i)) continue;
+        T im = inv_mass(w, i);
+        if (phase == 2) {
+            w.acc[i] = w.force[i] * im + w.a0[i];
+            continue;
+        }
+        T h = w.timeZ;
+        if (!(h > 0)) continue;
+        T halfStep = T(0.5) * h;
+        T gamma = force_driven(w, i) ? std::fmax(w.gamma[i], T(0)) : T(0);
+        T decay = std::exp(-gamma * halfStep), factor = half_impulse(gamma, halfStep);
+        if (phase == 0) {
+            if (!(im > 0)) continue;
+            V2<T> velocity = w.vel[i] * decay + w.acc[i] * factor;
+            T angular = w.omega[i] * std::exp(-gamma * h);
+            if (!w.motors.empty() && force_driven(w, i)) {
+                const bp_motor* motor = find_by_bubble(w.motors, w.id[i]);
+                if (motor && motor->inertia > 0) angular = angular + T(motor->torque) / T(motor->inertia) * half_impulse(gamma, h);
+            }
+            w.pos[i] = w.pos[i] + velocity * h;
+            w.rot[i] = w.rot[i] + w.omega[i] * h;
+            w.vel[i] = velocity;
+            w.omega[i] = angular;
+            continue;
+        }
+        if (im > 0) {
+            V2<T> a = w.force[i] * im + non_contact_acc(w, i, w.pos[i]);
+            w.vel[i] = w.vel[i] * decay + a * factor;
+            w.acc[i] = a;
+        }
+    }
+}
+
+// nativeReduceSubstepInGroup, NFK:625-736 (reductions: max / min with the lower index winning ties)
+template <typename T> void reduce(World<T>& w) {
+    T remaining = w.timeX - w.timeY;
+    bool over = !(remaining > 0), stopped = w.countsZ != 0 || w.countsW != 0;
+    bool limited = w.countsY >= kFrameLimit;
+    if (over || stopped || limited) {
+        if (limited && !over && !stopped) w.countsW = 1;
+        w.timeZ = 0;
+        return;
+    }
+    const uint32_t n = w.n;
+    T fraction = step_fraction(w);
+    std::vector<T> v1(n), v2(n), v3(n);
+#pragma omp parallel for schedule(static) if (n > 4096)
+    for (uint32_t i = 0; i < n; ++i) {
+        v1[i] = is_removed(w, i) ? T(-1) : omega_squared(w, i, fraction);
+        v3[i] = is_removed(w, i) ? Lim<T>::inf() : margin_bound(w, i);
+    }
+    T best = -1;
+    uint32_t owner = 0;
+    for (uint32_t i = 0; i < n; ++i)
+        if (v1[i] > best) { best = v1[i]; owner = i; }
+    T omegaSq = best;
+    uint32_t omegaOwner = owner;
+    T stiffnessBound = omegaSq > 0 ? T(1) / std::sqrt(omegaSq) : Lim<T>::inf();
+    T hMax = std::fmin(remaining, stiffnessBound);
+#pragma omp parallel for schedule(static) if (n > 4096)
+    for (uint32_t i = 0; i < n; ++i) v2[i] = is_removed(w, i) ? Lim<T>::inf() : distance_bound(w, i, hMax, fraction);
+    best = Lim<T>::inf();
+    owner = 0;
+    for (uint32_t i = 0; i < n; ++i)
+        if (v2[i] < best) { best = v2[i]; owner = i; }
+    T distanceBound = best;
+    uint32_t distanceOwner = owner;
+    best = Lim<T>::inf();
+    owner = 0;
+    for (uint32_t i = 0; i < n; ++i)
+        if (v3[i] < best) { best = v3[i]; owner = i; }
+    T marginBound = best;
+    uint32_t marginOwner = owner;
+    if (marginBound <= 0) {
+        w.countsZ = 1;
+        w.timeZ = 0;
+        w.limiterObject = w.id[marginOwner];
+        w.limiterTerm = BP_TERM_MARGIN;
+        return;
+    }
+    T split = std::fmax(w.timeW, T(1));
+    T h = remaining;
+    uint32_t term = BP_TERM_REMAINING;
+    int64_t object = 0;
+    if (split > 1 && w.timeX / split < h) h = w.timeX / split;
+    if (stiffnessBound / split < h) { h = stiffnessBound / split; term = BP_TERM_STIFFNESS; object = w.id[omegaOwner]; }
+    if (distanceBound / split < h) { h = distanceBound / split; term = BP_TERM_DISTANCE; object = w.id[distanceOwner]; }
+    if (marginBound < h) { h = marginBound; term = BP_TERM_MARGIN; object = w.id[marginOwner]; w.countsZ = 1; }
+    h = std::fmax(h, w.timeX * T(1e-7));
+    uint32_t frameSubstep = w.countsY;
+    if (h >= remaining || remaining - h <= w.timeX * T(1e-5)) { h = remaining; w.timeY = w.timeX; }
+    else w.timeY = w.timeY + h;
+    w.timeZ = h;
+    w.countsX += 1;
+    w.countsY = frameSubstep + 1;
+    w.limiterObject = object;
+    w.limiterTerm = term;
+    w.history.push_back(h);
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Contact assertion (NFK:865-918): violation of the lowest bubble index.
+// ---------------------------------------------------------------------------------------------------------------
+struct Violation {
+    uint32_t kind = 0;
+    uint32_t index = 0xffffffffu;
+    int64_t a = 0, b = 0, edge = 0;
+    double distance = 0;
+};
+
+template <typename T> bool assert_bubble(const World<T>& w, uint32_t i, const std::vector<uint32_t>* sameCell, Violation& v) {
+    V2<T> center = w.pos[i], start = w.start[i];
+    if (!finite2(center) || w.result[i] == 1 || is_removed(w, i)) return false;
+    bool movable = inv_mass(w, i) > 0;
+    auto checkPair = [&](uint32_t other) -> bool {
+        if (is_removed(w, other) || w.result[other] == 1) return false;
+        if (!filter_accepts(w.cat[i], w.mask[i], w.cat[other], w.mask[other])) return false;
+        if (!movable && !(inv_mass(w, other) > 0)) return false;
+        T d = len(w.pos[other] - center);
+        if (d <= 0) {
+            v.kind = BP_VIOLATION_PAIR; v.index = i; v.a = w.id[i]; v.b = w.id[other]; v.distance = (double)d;
+            return true;
+        }
+        return false;
+    };
+    if (sameCell) {
+        for (uint32_t other : *sameCell)
+            if (other > i && checkPair(other)) return true;
+    } else {
+        for (uint32_t other = i + 1; other < w.n; ++other)
+            if (checkPair(other)) return true;
+    }
+    if (!movable) return false;
+    T fraction = step_fraction(w);
+    for (const Body<T>& b : w.bodies) {
+        if (!filter_accepts(w.cat[i], w.mask[i], b.cat, b.mask)) continue;
+        if (rigid_inside(w, center, b, body_at(b, fraction))) {
+            v.kind = BP_VIOLATION_INSIDE_BODY; v.index = i; v.a = w.id[i]; v.b = b.id;
+            return true;
+        }
+    }
+    for (uint32_t e = 0; e < w.s; ++e) {
+        if (!(w.sflags[e] & BP_SEGMENT_POLYGON_EDGE) || !filter_accepts(w.cat[i], w.mask[i], w.scat[e], w.smask[e])) continue;
+        V2<T> edge = w.sb[e] - w.sa[e];
+        T lsq = dot(edge, edge);
+        if (!(lsq > 0)) continue;
+        V2<T> outward = mk(-edge.y, edge.x) / std::sqrt(lsq) * w.soutward[e];
+        T before = dot(start - w.sa[e], outward), after = dot(center - w.sa[e], outward);
+        if (!(before > 0) || !(after <= 0)) continue;
+        V2<T> crossing = start + (center - start) * (before / (before - after));
+        T along = dot(crossing - w.sa[e], edge) / lsq;
+        if (along < 0 || along > 1) continue;
+        v.kind = BP_VIOLATION_EDGE_SIDE; v.index = i; v.a = w.id[i]; v.b = w.sowner[e]; v.edge = w.sid[e]; v.distance = (double)after;
+        return true;
+    }
+    return false;
+}
+
+// Pairs with d <= 0 have (numerically) coincident centres, so only bubbles of the same exact centre bit pattern or
+// within 1e-18 can violate. Large worlds group candidates by a coarse cell of the final positions first.
+template <typename T> Violation assert_contacts(const World<T>& w) {
+    Violation v;
+    const uint32_t n = w.n;
+    if (n <= 8192) {
+        for (uint32_t i = 0; i < n; ++i)
+            if (assert_bubble(w, i, nullptr, v)) return v;
+        return v;
+    }
+    // coarse grid of final centres (cell 1.0); a pair with |delta| < 1 is in the same or an adjacent cell
+    std::vector<std::pair<std::pair<int64_t, int64_t>, uint32_t>> cells;
+    cells.reserve(n);
+    for (uint32_t i = 0; i < n; ++i)
+        if (finite2(w.pos[i]))
+            cells.push_back({{(int64_t)clampv(std::floor((double)w.pos[i].x), -4.0e18, 4.0e18),
+                              (int64_t)clampv(std::floor((double)w.pos[i].y), -4.0e18, 4.0e18)}, i});
+    std::sort(cells.begin(), cells.end());
+    std::vector<std::vector<uint32_t>> near(n);
+    for (size_t a = 0; a < cells.size(); ++a) {
+        for (int dx = -1; dx <= 1; ++dx)
+            for (int dy = -1; dy <= 1; ++dy) {
+                std::pair<int64_t, int64_t> key{cells[a].first.first + dx, cells[a].first.second + dy};
+                auto it = std::lower_bound(cells.begin(), cells.end(), std::make_pair(key, 0u));
+                for (; it != cells.end() && it->first == key; ++it) near[cells[a].second].push_back(it->second);
+            }
+        std::sort(near[cells[a].second].begin(), near[cells[a].second].end());
+    }
+    for (uint32_t i = 0; i < n; ++i)
+        if (assert_bubble(w, i, &near[i], v)) return v;
+    return v;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// End of step: region (NPK:536-568), contact records (NGK:683-728, NCK:146-160, NFK:261-280), finite check (NPK:5-27)
+// ---------------------------------------------------------------------------------------------------------------
+template <typename T> bool apply_region(World<T>& w, uint32_t& removed, uint32_t& wrapped) {
+    bool finite = true;
+    for (uint32_t i = 0; i < w.n; ++i) {
+        if (is_removed(w, i)) continue;
+        uint32_t f = w.flags_[i];
+        if (!(f & BP_BUBBLE_ENABLED) || (f & BP_BUBBLE_STATIC)) continue;
+        V2<T> nearest = vclamp(w.pos[i], w.rmin, w.rmax);
+        T r = w.radius[i];
+        if (len(w.pos[i] - nearest) <= r) continue;
+        if (!(f & BP_BUBBLE_WRAP)) { w.result[i] = 1; ++removed; continue; }
+        V2<T> delta = mk<T>(0, 0);
+        V2<T> span = (w.rmax - w.rmin) + mk(T(2) * r, T(2) * r);
+        T p[2] = {w.pos[i].x, w.pos[i].y}, lo[2] = {w.rmin.x, w.rmin.y}, hi[2] = {w.rmax.x, w.rmax.y}, sp[2] = {span.x, span.y};
+        T dl[2] = {0, 0};
+        for (int axis = 0; axis < 2; ++axis) {
+            if (p[axis] > hi[axis]) dl[axis] = -sp[axis] * std::fmax(T(1), std::ceil((p[axis] - r - hi[axis]) / sp[axis]));
+            else if (p[axis] < lo[axis]) dl[axis] = sp[axis] * std::fmax(T(1), std::ceil((lo[axis] - r - p[axis]) / sp[axis]));
+        }
+        delta = mk(dl[0], dl[1]);
+        V2<T> wrappedPos = w.pos[i] + delta;
+        V2<T> nearestWrapped = vclamp(wrappedPos, w.rmin, w.rmax);
+        if (len(wrappedPos - nearestWrapped) > r) delta = delta + (nearestWrapped - wrappedPos);
+        w.pos[i] = w.pos[i] + delta;
+        w.start[i] = w.start[i] + delta;
+        if (!finite2(w.pos[i]) || !finite2(w.start[i])) { finite = false; continue; }
+        w.result[i] = 2;
+        ++wrapped;
+    }
+    return finite;
+}
+
+template <typename T> void build_contacts(World<T>& w) {
+    w.contacts.clear();
+    T dt = w.timeX;
+    auto record = [&](uint32_t ai, uint32_t kind, uint32_t other) {
+        V2<T> apos = w.pos[ai];
+        T ar = w.radius[ai];
+        V2<T> normal, point;
+        T pen, allowed = 0;
+        uint32_t feature = 0;
+        int64_t second;
+        if (kind == 0) {
+            V2<T> delta = w.pos[other] - apos;
+            T d = len(delta);
+            normal = d > 0 ? delta / d : mk<T>(1, 0);
+            point = apos + normal * ar;
+            pen = ar + w.radius[other] - d;
+            second = w.id[other];
+        } else {
+            uint32_t s = other;
+            second = w.sid[s];
+            V2<T> edge = w.sb[s] - w.sa[s];
+            T lsq = dot(edge, edge);
+            T t = lsq > 0 ? clampv(dot(apos - w.sa[s], edge) / lsq, T(0), T(1)) : T(0);
+            point = w.sa[s] + edge * t;
+            V2<T> delta = apos - point;
+            T d = len(delta), edgeLength = len(edge);
+            V2<T> base = edgeLength > 0 ? mk(-edge.y, edge.x) / edgeLength : mk<T>(0, 1);
+            T sign = ((w.id[ai] ^ w.sid[s]) & 1) == 0 ? T(1) : T(-1);
+            bool fixedSide = (w.sflags[s] & BP_SEGMENT_ALLOWED_SIDE) != 0;
+            normal = fixedSide ? base * w.sallowed[s] : (d > 0 ? delta / d : base * sign);
+            allowed = fixedSide ? w.sallowed[s] : T(0);
+            pen = ar - d;
+            if (w.sflags[s] & BP_SEGMENT_POLYGON_EDGE) {
+                V2<T> outward = base * w.soutward[s];
+                // nativePolygonEdgeFeature, NGK:674-681
+                V2<T> start = w.sa[s], end = w.sb[s];
+                T along = dot(apos - start, end - start);
+                bool convexStart = (w.sflags[s] & BP_SEGMENT_CONVEX_START) != 0;
+                if (convexStart && along <= 0 && past_segment_end(apos, w.sprev[s], start)) feature = 2;
+                else {
+                    bool interior = along > 0 && !past_segment_end(apos, start, end);
+                    feature = dot(apos - start, outward) >= 0 && interior ? 1 : 0;
+                }
+                if (feature == 1) {
+                    normal = outward;
+                    point = apos - outward * dot(apos - w.sa[s], outward);
+                    pen = ar - dot(apos - w.sa[s], outward);
+                } else if (feature == 2) {
+                    point = w.sa[s];
+                    delta = apos - point;
+                    d = len(delta);
+                    normal = d > 0 ? delta / d : outward;
+                    pen = ar - d;
+                } else {
+                    normal = outward;
+                    point = w.sa[s];
+                    pen = -Lim<T>::big();
+                }
+            }
+        }
+        // nativePrepareContactFlags / nativeCompactActiveContacts: active = penetration > -sepTol
+        if (!(pen > -w.sepTol)) return;
+        // nativeContactImpulses, NFK:261-280
+        T f;
+        if (kind == 0) f = pair_law(w.K[ai], ar, w.K[other], w.radius[other], ar + w.radius[other] - pen).force;
+        else f = wall_law(w.K[ai], ar, ar - pen).force;
+        bp_contact c{};
+        c.participants[0] = w.id[ai];
+        c.participants[1] = second;
+        c.kind = kind;
+        c.feature = feature;
+        c.normal[0] = (float)normal.x; c.normal[1] = (float)normal.y;
+        c.point[0] = (float)point.x; c.point[1] = (float)point.y;
+        c.impulse = (float)(f * dt * dt);
+        c.penetration = (float)pen;
+        c.allowed_side = (float)allowed;
+        w.contacts.push_back(c);
+    };
+    for (uint32_t i = 0; i < w.n; ++i)
+        for (uint32_t j : w.rowPairs[i]) record(i, 0, j);
+    for (uint32_t i = 0; i < w.n; ++i)
+        for (uint32_t sg : w.rowSegs[i]) record(i, 1, sg);
+}
+
+template <typename T> bool finite_state(const World<T>& w) {
+    for (uint32_t i = 0; i < w.n; ++i) {
+        if (is_removed(w, i)) continue;
+        if (!finite2(w.pos[i]) || !finite2(w.start[i]) || !finite2(w.vel[i]) || !std::isfinite(w.rot[i]) ||
+            !std::isfinite(w.omega[i]))
+            return false;
+    }
+    for (const bp_contact& c : w.contacts)
+        if (!std::isfinite(c.normal[0]) || !std::isfinite(c.normal[1]) || !std::isfinite(c.point[0]) ||
+            !std::isfinite(c.point[1]) || !std::isfinite(c.impulse) || !std::isfinite(c.penetration))
+            return false;
+    return true;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// One step (NativeMetalSolver.executeSnapshot + nativeSubstepLoopSingleGroup, NFK:1236-1307)
+// ---------------------------------------------------------------------------------------------------------------
+template <typename T> void kinematic_advance(World<T>& w) {
+    // nativeRigidPredict for static and kinematic bodies (NPK:65-80): previous <- pose; pose += velocity * dt.
+    for (Body<T>& b : w.bodies) {
+        b.prev = b.pos;
+        b.prevAngle = b.angle;
+        b.cosPrev = b.cosEnd;
+        b.sinPrev = b.sinEnd;
+        if (b.flags & BP_BODY_STATIC) {
+            b.vel = mk<T>(0, 0);
+            b.omega = 0;
+            continue;
+        }
+        b.pos = b.pos + b.vel * w.dt;
+        b.angle = b.angle + b.omega * w.dt;
+        if (b.angle != b.prevAngle) {
+            b.cosEnd = std::cos(b.angle);
+            b.sinEnd = std::sin(b.angle);
+        }
+    }
+}
+
+template <typename T> int step(World<T>& w, bp_step_report& rep) {
+    std::memset(&rep, 0, sizeof(rep));
+    if (w.failed) { rep.status = BP_E_WORLD_FAILED; return BP_E_WORLD_FAILED; }
+    const uint32_t n = w.n;
+    // nativeBeginStep, NFK:285-293
+    for (uint32_t i = 0; i < n; ++i) {
+        if (is_removed(w, i)) continue;
+        w.result[i] = 0;
+        w.start[i] = w.pos[i];
+        if ((w.flags_[i] & BP_BUBBLE_ENABLED) && (w.flags_[i] & BP_BUBBLE_STATIC)) {
+            w.vel[i] = mk<T>(0, 0);
+            w.omega[i] = 0;
+        }
+    }
+    kinematic_advance(w);
+    uint32_t live = 0;
+    for (uint32_t i = 0; i < n; ++i) live += is_removed(w, i) ? 0 : 1;
+    w.timeX = w.dt;
+    w.timeY = live == 0 ? w.dt : T(0);
+    w.timeZ = 0;
+    w.timeW = w.split;
+    w.countsX = w.countsY = w.countsZ = w.countsW = 0;
+    w.limiterObject = 0;
+    w.limiterTerm = 0;
+    w.history.clear();
+    w.overflowMax = 0;
+    w.maxPerObject = 0;
+    w.rebuilds = 0;
+    Violation substepViolation;
+    broadphase(w);
+    contact_forces_all(w);
+    integrate(w, 2);
+    for (uint32_t iteration = 0; iteration < 2 * kFrameLimit + 2; ++iteration) {
+        reduce(w);
+        T h = w.timeZ;
+        bool limited = w.countsW != 0, finished = !(w.timeX - w.timeY > 0), rebuild = w.countsZ != 0;
+        if (!(h > 0)) {
+            if (limited || finished || !rebuild) break;
+            w.countsX = 0;
+            w.countsZ = 0;
+            w.overflowMax = std::max(w.overflowMax, w.overflowBuild);
+            w.rebuilds += 1;
+            broadphase(w);
+            contact_forces_all(w);
+            integrate(w, 2);
+            continue;
+        }
+        integrate(w, 0);
+        contact_forces_all(w);
+        integrate(w, 1);
+        if (w.flags & BP_WORLD_INJECT_STATE) {
+            if (w.countsY == w.injectSubstep + 1)
+                for (uint32_t i = 0; i < n; ++i)
+                    if (w.id[i] == w.injectObject) w.pos[i] = w.injectPos;
+        }
+        if ((w.flags & BP_WORLD_ASSERT_EVERY_SUBSTEP) && substepViolation.kind == 0) substepViolation = assert_contacts(w);
+    }
+    w.overflowMax = std::max(w.overflowMax, w.overflowBuild);
+    // end of step
+    uint32_t removed = 0, wrapped = 0;
+    bool finite = true;
+    if (w.countsW == 0 && (w.flags & BP_WORLD_HAS_REGION)) finite = apply_region(w, removed, wrapped);
+    build_contacts(w);
+    finite = finite && finite_state(w);
+    Violation v = substepViolation;
+    if (v.kind == 0 && w.countsW == 0 && !(w.flags & BP_WORLD_NO_END_ASSERTION)) v = assert_contacts(w);
+
+    rep.substep_count = w.countsY;
+    rep.rebuild_count = w.rebuilds;
+    uint32_t cand = 0;
+    for (uint32_t i = 0; i < n; ++i) cand += (uint32_t)(w.rowPairs[i].size() + w.rowSegs[i].size());
+    rep.candidate_count = cand;
+    uint32_t bodyCand = 0;
+    for (auto& row : w.bodyRows) bodyCand += (uint32_t)row.size();
+    rep.body_candidate_count = bodyCand;
+    rep.candidate_overflow = w.overflowMax;
+    rep.max_candidates_per_object = w.maxPerObject;
+    rep.contact_count = (uint32_t)w.contacts.size();
+    rep.limiter_term = w.limiterTerm;
+    rep.limiter_object = w.limiterObject;
+    rep.cell_width = (float)w.cellWidth;
+    rep.removed_count = removed;
+    rep.wrapped_count = wrapped;
+    rep.violation_kind = v.kind;
+    rep.violation_objects[0] = v.a;
+    rep.violation_objects[1] = v.b;
+    rep.violation_edge = v.edge;
+    rep.violation_distance = (float)v.distance;
+    // failure order (NativeMetalSolver.swift:1026-1040): substep limit, non-finite, contact violation
+    int status = BP_OK;
+    if (w.countsW != 0) status = BP_E_SUBSTEP_LIMIT;
+    else if (!finite) status = BP_E_NONFINITE;
+    else if (v.kind != 0) status = BP_E_CONTACT_VIOLATION;
+    rep.status = status;
+    if (status != BP_OK) {
+        // publish nothing: restore the last published state, the world is stopped
+        w.pos = w.pPos; w.start = w.pStart; w.vel = w.pVel; w.rot = w.pRot; w.omega = w.pOmega;
+        w.result = w.pResult; w.flags_ = w.pFlags; w.bodies = w.pBodies;
+        w.failed = true;
+        return status;
+    }
+    for (uint32_t i = 0; i < n; ++i)
+        if (w.result[i] == 1) w.flags_[i] |= kRemovedFlag;
+    w.pPos = w.pos; w.pStart = w.start; w.pVel = w.vel; w.pRot = w.rot; w.pOmega = w.omega;
+    w.pResult = w.result; w.pFlags = w.flags_; w.pBodies = w.bodies;
+    w.lastReport = rep;
+    return BP_OK;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Construction from the C records
+// ---------------------------------------------------------------------------------------------------------------
+template <typename T> World<T>* create(const bp_world_desc* d, const bp_world_input* in) {
+    World<T>* w = new (std::nothrow) World<T>();
+    if (!w) return nullptr;
+    w->dt = d->time_step;
+    w->sepTol = d->separation_tolerance;
+    w->contactTol = d->contact_tolerance;
+    w->split = d->substep_split_multiplier;
+    w->rmin = mk<T>(d->region[0], d->region[1]);
+    w->rmax = mk<T>(d->region[2], d->region[3]);
+    w->globalForce = mk<T>(d->global_force[0], d->global_force[1]);
+    w->gravity = mk<T>(d->gravity[0], d->gravity[1]);
+    w->limit = d->candidate_limit == 0 ? 128u : std::min(d->candidate_limit, 128u);
+    w->flags = d->flags;
+    w->injectObject = d->inject_object;
+    w->injectSubstep = 0;
+    w->injectPos = mk<T>(0, 0);
+    const uint32_t n = in->bubble_count;
+    w->n = n;
+    auto resize = [&](auto& v) { v.resize(n); };
+    resize(w->id); resize(w->pos); resize(w->start); resize(w->vel); resize(w->acc); resize(w->a0); resize(w->ref);
+    resize(w->force); resize(w->rot); resize(w->omega); resize(w->mass); resize(w->invMass); resize(w->radius);
+    resize(w->K); resize(w->gamma); resize(w->margin); resize(w->flags_); resize(w->cat); resize(w->mask);
+    resize(w->result); resize(w->cellX); resize(w->cellY); resize(w->cellValid); resize(w->rowPairs);
+    resize(w->rowSegs); resize(w->adj);
+    for (uint32_t i = 0; i < n; ++i) {
+        const bp_bubble& b = in->bubbles[i];
+        w->id[i] = b.id;
+        w->pos[i] = mk<T>(b.center[0], b.center[1]);
+        w->start[i] = mk<T>(b.previous_center[0], b.previous_center[1]);
+        w->vel[i] = mk<T>(b.velocity[0], b.velocity[1]);
+        w->acc[i] = mk<T>(0, 0);
+        w->rot[i] = b.rotation;
+        w->omega[i] = b.angular_velocity;
+        w->mass[i] = b.mass;
+        w->invMass[i] = b.inverse_mass;
+        w->radius[i] = b.radius;
+        w->K[i] = b.contact_stiffness;
+        w->gamma[i] = b.damping;
+        w->flags_[i] = b.flags & 0xffu;
+        w->cat[i] = b.category;
+        w->mask[i] = b.mask;
+        w->result[i] = 0;
+    }
+    w->s = in->segment_count;
+    const uint32_t s = w->s;
+    w->sid.resize(s); w->sowner.resize(s); w->sa.resize(s); w->sb.resize(s); w->sprev.resize(s);
+    w->soutward.resize(s); w->sallowed.resize(s); w->sflags.resize(s); w->scat.resize(s); w->smask.resize(s);
+    for (uint32_t j = 0; j < s; ++j) {
+        const bp_segment& g = in->segments[j];
+        w->sid[j] = g.id;
+        w->sowner[j] = g.owner_id;
+        w->sa[j] = mk<T>(g.a[0], g.a[1]);
+        w->sb[j] = mk<T>(g.b[0], g.b[1]);
+        w->sprev[j] = mk<T>(g.previous_start[0], g.previous_start[1]);
+        w->soutward[j] = g.outward_sign;
+        w->sallowed[j] = g.allowed_side;
+        w->sflags[j] = g.flags;
+        w->scat[j] = g.category;
+        w->smask[j] = g.mask;
+    }
+    w->bverts.resize(in->body_vertex_count);
+    for (uint32_t v = 0; v < in->body_vertex_count; ++v)
+        w->bverts[v] = mk<T>(in->body_vertices[2 * v], in->body_vertices[2 * v + 1]);
+    w->btris.assign(in->body_triangles, in->body_triangles + 3 * (size_t)in->body_triangle_count);
+    for (uint32_t b = 0; b < in->body_count; ++b) {
+        const bp_body& r = in->bodies[b];
+        Body<T> body;
+        body.id = r.id;
+        body.pos = mk<T>(r.position[0], r.position[1]);
+        body.prev = body.pos;
+        body.angle = r.angle;
+        body.prevAngle = r.angle;
+        body.vel = mk<T>(r.velocity[0], r.velocity[1]);
+        body.omega = r.angular_velocity;
+        body.radius = r.bounding_radius;
+        body.coreRadius = r.core_radius;
+        body.kind = r.kind;
+        body.flags = r.flags;
+        body.voff = r.vertex_offset;
+        body.vcount = r.vertex_count;
+        body.toff = r.triangle_offset;
+        body.tcount = r.triangle_count;
+        body.cat = r.category;
+        body.mask = r.mask;
+        body.cosEnd = std::cos((T)r.angle);
+        body.sinEnd = std::sin((T)r.angle);
+        body.cosPrev = body.cosEnd;
+        body.sinPrev = body.sinEnd;
+        w->bodies.push_back(body);
+    }
+    w->bodyRows.resize(in->body_count);
+    w->fverts.resize(in->field_vertex_count);
+    for (uint32_t v = 0; v < in->field_vertex_count; ++v)
+        w->fverts[v] = mk<T>(in->field_vertices[2 * v], in->field_vertices[2 * v + 1]);
+    w->fids.assign(in->field_object_ids, in->field_object_ids + in->field_object_id_count);
+    for (uint32_t f = 0; f < in->field_count; ++f) {
+        const bp_force_field& r = in->fields[f];
+        Field<T> fl;
+        fl.pos = mk<T>(r.position[0], r.position[1]);
+        fl.cosr = std::cos((T)r.rotation);
+        fl.sinr = std::sin((T)r.rotation);
+        fl.falloff = r.falloff;
+        fl.dir = mk<T>(r.direction[0], r.direction[1]);
+        fl.strength = r.strength;
+        fl.radius = r.radius;
+        fl.kind = r.kind;
+        fl.voff = r.vertex_offset;
+        fl.vcount = r.vertex_count;
+        fl.foff = r.filter_offset;
+        fl.fcount = r.filter_count;
+        fl.hasFilter = r.has_filter;
+        w->fields.push_back(fl);
+    }
+    w->bands.assign(in->bands, in->bands + in->band_count);
+    w->motors.assign(in->motors, in->motors + in->motor_count);
+    if (in->joint_ranges && in->joint_entity_count)
+        w->jranges.assign(in->joint_ranges, in->joint_ranges + 2 * (size_t)in->joint_entity_count);
+    if (in->joint_partners && in->joint_partner_count)
+        w->jpartners.assign(in->joint_partners, in->joint_partners + in->joint_partner_count);
+    w->pPos = w->pos; w->pStart = w->start; w->pVel = w->vel; w->pRot = w->rot; w->pOmega = w->omega;
+    w->pResult = w->result; w->pFlags = w->flags_; w->pBodies = w->bodies;
+    w->cellWidth = 0;
+    return w;
+}
+
+struct Handle {
+    int precision;
+    void* world;
+};
+
+template <typename T> void write_bubbles(const World<T>& w, bp_bubble* out, uint32_t count) {
+    for (uint32_t i = 0; i < count && i < w.n; ++i) {
+        bp_bubble& b = out[i];
+        std::memset(&b, 0, sizeof(b));
+        b.id = w.id[i];
+        b.center[0] = (float)w.pPos[i].x; b.center[1] = (float)w.pPos[i].y;
+        b.previous_center[0] = (float)w.pStart[i].x; b.previous_center[1] = (float)w.pStart[i].y;
+        b.velocity[0] = (float)w.pVel[i].x; b.velocity[1] = (float)w.pVel[i].y;
+        b.mass = (float)w.mass[i];
+        b.inverse_mass = (float)w.invMass[i];
+        b.radius = (float)w.radius[i];
+        b.rotation = (float)w.pRot[i];
+        b.angular_velocity = (float)w.pOmega[i];
+        b.contact_stiffness = (float)w.K[i];
+        b.damping = (float)w.gamma[i];
+        b.flags = w.pFlags[i] & 0xffu;
+        b.category = w.cat[i];
+        b.mask = w.mask[i];
+        b.region_result = w.pResult[i];
+    }
+}
+
+template <typename T> uint32_t candidate_keys(const World<T>& w, bp_candidate_key* out, uint32_t capacity) {
+    std::vector<bp_candidate_key> keys;
+    for (uint32_t i = 0; i < w.n; ++i) {
+        for (uint32_t j : w.rowPairs[i]) keys.push_back({0, 0, w.id[i], w.id[j]});
+        for (uint32_t sg : w.rowSegs[i]) keys.push_back({1, 0, w.id[i], w.sid[sg]});
+    }
+    for (size_t b = 0; b < w.bodies.size(); ++b)
+        for (uint32_t a : w.bodyRows[b]) keys.push_back({2, 0, w.id[a], w.bodies[b].id});
+    std::sort(keys.begin(), keys.end(), [](const bp_candidate_key& a, const bp_candidate_key& b) {
+        if (a.kind != b.kind) return a.kind < b.kind;
+        if (a.first != b.first) return a.first < b.first;
+        return a.second < b.second;
+    });
+    uint32_t count = (uint32_t)keys.size();
+    for (uint32_t i = 0; i < count && i < capacity; ++i) out[i] = keys[i];
+    return count;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------------------------
+// C entry points of the oracle (loaded by tests and by bench.py's CPU legs through ctypes)
+// ---------------------------------------------------------------------------------------------------------------
+extern "C" {
+
+int bpo_world_create(const bp_world_desc* desc, const bp_world_input* input, int precision, void** out) {
+    if (!desc || !input || !out) return BP_E_INVALID;
+    Handle* h = new Handle{precision, nullptr};
+    h->world = precision == 64 ? (void*)create<double>(desc, input) : (void*)create<float>(desc, input);
+    if (!h->world) { delete h; return BP_E_ALLOC; }
+    *out = h;
+    return BP_OK;
+}
+
+void bpo_world_destroy(void* handle) {
+    Handle* h = (Handle*)handle;
+    if (!h) return;
+    if (h->precision == 64) delete (World<double>*)h->world; else delete (World<float>*)h->world;
+    delete h;
+}
+
+int bpo_world_set_injection(void* handle, uint32_t substep, float x, float y) {
+    Handle* h = (Handle*)handle;
+    if (h->precision == 64) { auto* w = (World<double>*)h->world; w->injectSubstep = substep; w->injectPos = mk<double>(x, y); }
+    else { auto* w = (World<float>*)h->world; w->injectSubstep = substep; w->injectPos = mk<float>(x, y); }
+    return BP_OK;
+}
+
+int bpo_world_step(void* handle, uint32_t steps, bp_step_report* reports) {
+    Handle* h = (Handle*)handle;
+    bp_step_report rep;
+    int status = BP_OK;
+    for (uint32_t s = 0; s < steps; ++s) {
+        status = h->precision == 64 ? step(*(World<double>*)h->world, rep) : step(*(World<float>*)h->world, rep);
+        if (reports) reports[s] = rep;
+        if (status != BP_OK) break;
+    }
+    return status;
+}
+
+// Steps many independent worlds, OpenMP over worlds (the CPU baseline of the batched path).
+int bpo_worlds_step(void** handles, uint32_t count, uint32_t steps, int threads, uint64_t* bubble_substeps) {
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#endif
+    uint64_t total = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : total)
+    for (uint32_t wi = 0; wi < count; ++wi) {
+        Handle* h = (Handle*)handles[wi];
+        bp_step_report rep;
+        for (uint32_t s = 0; s < steps; ++s) {
+            int status = h->precision == 64 ? step(*(World<double>*)h->world, rep) : step(*(World<float>*)h->world, rep);
+            uint32_t n = h->precision == 64 ? ((World<double>*)h->world)->n : ((World<float>*)h->world)->n;
+            total += (uint64_t)rep.substep_count * n;
+            if (status != BP_OK) break;
+        }
+    }
+    if (bubble_substeps) *bubble_substeps = total;
+    return BP_OK;
+}
+
+int bpo_set_threads(int threads) {
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+    return omp_get_max_threads();
+#else
+    (void)threads;
+    return 1;
+#endif
+}
+
+int bpo_world_read_bubbles(void* handle, bp_bubble* out, uint32_t capacity, uint32_t* count) {
+    Handle* h = (Handle*)handle;
+    if (h->precision == 64) { auto* w = (World<double>*)h->world; write_bubbles(*w, out, capacity); if (count) *count = w->n; }
+    else { auto* w = (World<float>*)h->world; write_bubbles(*w, out, capacity); if (count) *count = w->n; }
+    return BP_OK;
+}
+
+// Double-precision state of the FP64 rerun (center.xy, velocity.xy) for error reporting.
+int bpo_world_read_state64(void* handle, double* out, uint32_t capacity) {
+    Handle* h = (Handle*)handle;
+    if (h->precision == 64) {
+        auto* w = (World<double>*)h->world;
+        for (uint32_t i = 0; i < w->n && i < capacity; ++i) {
+            out[4 * i] = w->pPos[i].x; out[4 * i + 1] = w->pPos[i].y; out[4 * i + 2] = w->pVel[i].x; out[4 * i + 3] = w->pVel[i].y;
+        }
+    } else {
+        auto* w = (World<float>*)h->world;
+        for (uint32_t i = 0; i < w->n && i < capacity; ++i) {
+            out[4 * i] = w->pPos[i].x; out[4 * i + 1] = w->pPos[i].y; out[4 * i + 2] = w->pVel[i].x; out[4 * i + 3] = w->pVel[i].y;
+        }
+    }
+    return BP_OK;
+}
+
+int bpo_world_read_contacts(void* handle, bp_contact* out, uint32_t capacity, uint32_t* count) {
+    Handle* h = (Handle*)handle;
+    const std::vector<bp_contact>& c = h->precision == 64 ? ((World<double>*)h->world)->contacts : ((World<float>*)h->world)->contacts;
+    for (uint32_t i = 0; i < c.size() && i < capacity; ++i) out[i] = c[i];
+    if (count) *count = (uint32_t)c.size();
+    return BP_OK;
+}
+
+int bpo_world_read_candidates(void* handle, bp_candidate_key* out, uint32_t capacity, uint32_t* count) {
+    Handle* h = (Handle*)handle;
+    uint32_t c = h->precision == 64 ? candidate_keys(*(World<double>*)h->world, out, capacity)
+                                    : candidate_keys(*(World<float>*)h->world, out, capacity);
+    if (count) *count = c;
+    return BP_OK;
+}
+
+int bpo_world_read_cells(void* handle, int64_t* out, uint32_t capacity, uint32_t* count) {
+    Handle* h = (Handle*)handle;
+    auto fill = [&](auto* w) {
+        for (uint32_t i = 0; i < w->n && i < capacity; ++i) { out[2 * i] = w->cellX[i]; out[2 * i + 1] = w->cellY[i]; }
+        if (count) *count = w->n;
+    };
+    if (h->precision == 64) fill((World<double>*)h->world); else fill((World<float>*)h->world);
+    return BP_OK;
+}
+
+int bpo_world_read_substeps(void* handle, double* out, uint32_t capacity, uint32_t* count) {
+    Handle* h = (Handle*)handle;
+    auto fill = [&](auto* w) {
+        for (uint32_t i = 0; i < w->history.size() && i < capacity; ++i) out[i] = (double)w->history[i];
+        if (count) *count = (uint32_t)w->history.size();
+    };
+    if (h->precision == 64) fill((World<double>*)h->world); else fill((World<float>*)h->world);
+    return BP_OK;
+}
+
+// Contact law known-answer entry (same layout as bp_device_contact_law): 8 floats in and out per case.
+int bpo_contact_law(uint32_t mode, int precision, const double* in, double* out, uint32_t count) {
+    for (uint32_t c = 0; c < count; ++c) {
+        const double* a = in + 8 * c;
+        double* o = out + 8 * c;
+        for (int q = 0; q < 8; ++q) o[q] = 0;
+        if (precision == 64) {
+            if (mode == 0) o[0] = epsilon_from_ratio<double>(a[0]);
+            else if (mode == 1) { Law<double> l = wall_law<double>(a[0], a[1], a[2]); o[0] = l.force; o[1] = l.epsA; o[2] = l.stiffness; }
+            else { Law<double> l = pair_law<double>(a[0], a[1], a[2], a[3], a[4]); o[0] = l.force; o[1] = l.epsA; o[2] = l.epsB; o[3] = l.stiffness; }
+        } else {
+            if (mode == 0) o[0] = epsilon_from_ratio<float>((float)a[0]);
+            else if (mode == 1) { Law<float> l = wall_law<float>((float)a[0], (float)a[1], (float)a[2]); o[0] = l.force; o[1] = l.epsA; o[2] = l.stiffness; }
+            else {
+                Law<float> l = pair_law<float>((float)a[0], (float)a[1], (float)a[2], (float)a[3], (float)a[4]);
+                o[0] = l.force; o[1] = l.epsA; o[2] = l.epsB; o[3] = l.stiffness;
+            }
+        }
+    }
+    return BP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,144 @@
+"""ctypes loader of the CPU oracle (liboracle built from bp_oracle.cpp). TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU legs use this module, and only as the checker / the timed CPU
+baseline. The product package never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+from bubblephysics_gb300 import _native as N
+from bubblephysics_gb300.spec import PackedInput, WorldSpec
+
+ORACLE_DIR = Path(__file__).resolve().parent
+ORACLE_LIB = ORACLE_DIR / "libbp_oracle.so"
+
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    """Builds the oracle shared library with its Makefile (gcc, -ffp-contract=off, OpenMP)."""
+    src = ORACLE_DIR / "bp_oracle.cpp"
+    header = ORACLE_DIR.parent / "include" / "bubblephysics.h"
+    if force or not ORACLE_LIB.exists() or ORACLE_LIB.stat().st_mtime < max(src.stat().st_mtime, header.stat().st_mtime):
+        subprocess.run(["make", "-s", "-B" if force else "-s", "-C", str(ORACLE_DIR)], check=True)
+    return ORACLE_LIB
+
+
+def library() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        lib = C.CDLL(str(ORACLE_LIB))
+        P = C.c_void_p
+        sig = {
+            "bpo_world_create": (C.c_int, [C.POINTER(N.WorldDesc), C.POINTER(N.WorldInput), C.c_int, C.POINTER(P)]),
+            "bpo_world_destroy": (None, [P]),
+            "bpo_world_set_injection": (C.c_int, [P, C.c_uint32, C.c_float, C.c_float]),
+            "bpo_world_step": (C.c_int, [P, C.c_uint32, P]),
+            "bpo_worlds_step": (C.c_int, [C.POINTER(P), C.c_uint32, C.c_uint32, C.c_int, C.POINTER(C.c_uint64)]),
+            "bpo_set_threads": (C.c_int, [C.c_int]),
+            "bpo_world_read_bubbles": (C.c_int, [P, P, C.c_uint32, C.POINTER(C.c_uint32)]),
+            "bpo_world_read_state64": (C.c_int, [P, P, C.c_uint32]),
+            "bpo_world_read_contacts": (C.c_int, [P, P, C.c_uint32, C.POINTER(C.c_uint32)]),
+            "bpo_world_read_candidates": (C.c_int, [P, P, C.c_uint32, C.POINTER(C.c_uint32)]),
+            "bpo_world_read_cells": (C.c_int, [P, P, C.c_uint32, C.POINTER(C.c_uint32)]),
+            "bpo_world_read_substeps": (C.c_int, [P, P, C.c_uint32, C.POINTER(C.c_uint32)]),
+            "bpo_contact_law": (C.c_int, [C.c_uint32, C.c_int, P, P, C.c_uint32]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+class OracleWorld:
+    """The oracle's counterpart of bubblephysics_gb300.solver.World (same methods, CPU, float or double)."""
+
+    def __init__(self, spec: WorldSpec, precision: int = 32):
+        self.lib = library()
+        self.spec = spec
+        packed = PackedInput(spec)
+        handle = C.c_void_p()
+        st = self.lib.bpo_world_create(C.byref(packed.desc), C.byref(packed.input), precision, C.byref(handle))
+        if st != 0:
+            raise N.NativeError(st, "bpo_world_create")
+        self.handle = handle
+        self.n = spec.bubble_count
+        self.precision = precision
+
+    def __del__(self):
+        try:
+            if self.handle:
+                self.lib.bpo_world_destroy(self.handle)
+                self.handle = None
+        except Exception:
+            pass
+
+    def set_injection(self, substep: int, position):
+        self.lib.bpo_world_set_injection(self.handle, substep, float(position[0]), float(position[1]))
+
+    def step(self, steps: int = 1):
+        reports = np.zeros(max(steps, 1), N.REPORT_DTYPE)
+        status = self.lib.bpo_world_step(self.handle, steps, C.c_void_p(reports.ctypes.data))
+        return status, reports[:steps]
+
+    def bubbles(self) -> np.ndarray:
+        out = np.zeros(self.n, N.BUBBLE_DTYPE)
+        count = C.c_uint32()
+        self.lib.bpo_world_read_bubbles(self.handle, C.c_void_p(out.ctypes.data), self.n, C.byref(count))
+        return out
+
+    def state64(self) -> np.ndarray:
+        out = np.zeros((self.n, 4), np.float64)
+        self.lib.bpo_world_read_state64(self.handle, C.c_void_p(out.ctypes.data), self.n)
+        return out
+
+    def _read(self, fn, dtype):
+        count = C.c_uint32()
+        fn(self.handle, None, 0, C.byref(count))
+        out = np.zeros(count.value, dtype)
+        if count.value:
+            fn(self.handle, C.c_void_p(out.ctypes.data), count.value, C.byref(count))
+        return out
+
+    def contacts(self) -> np.ndarray:
+        return self._read(self.lib.bpo_world_read_contacts, N.CONTACT_DTYPE)
+
+    def candidates(self) -> np.ndarray:
+        return self._read(self.lib.bpo_world_read_candidates, N.KEY_DTYPE)
+
+    def cells(self) -> np.ndarray:
+        out = np.zeros((self.n, 2), np.int64)
+        count = C.c_uint32()
+        self.lib.bpo_world_read_cells(self.handle, C.c_void_p(out.ctypes.data), self.n, C.byref(count))
+        return out
+
+    def substeps(self) -> np.ndarray:
+        return self._read(self.lib.bpo_world_read_substeps, np.float64)
+
+
+def step_worlds(worlds: list[OracleWorld], steps: int, threads: int = 0) -> int:
+    """Steps many oracle worlds with OpenMP over worlds; returns bubble-substeps advanced."""
+    lib = library()
+    arr = (C.c_void_p * len(worlds))(*[w.handle.value for w in worlds])
+    total = C.c_uint64()
+    lib.bpo_worlds_step(arr, len(worlds), steps, threads, C.byref(total))
+    return total.value
+
+
+def set_threads(threads: int) -> int:
+    return library().bpo_set_threads(threads)
+
+
+def contact_law(mode: int, cases: np.ndarray, precision: int = 32) -> np.ndarray:
+    cases = np.ascontiguousarray(cases, np.float64).reshape(-1, 8)
+    out = np.zeros_like(cases)
+    library().bpo_contact_law(mode, precision, C.c_void_p(cases.ctypes.data), C.c_void_p(out.ctypes.data), cases.shape[0])
+    return out
