@@ -1,0 +1,332 @@
+#!/usr/bin/env python
+"""bench.py - bubble-substeps/s of the batched bubble step on GB300 (one JSON line on rank 0).
+
+Workload (one "step" = one step of every world of the batch): 4,096 independent worlds, bubble counts log-uniform in
+[16, 1024], radii U[6, 24] at 40 % area fraction, 0-32 rigid bodies each (polygons, circles, capsules; half-extents
+U[8, 40]; static or kinematic), walls, gravity (0, -980), dt = 1/60; seeded synthetic data.
+
+  value        whole-job bubble-substeps/s of the batched path (one fused launch per size class and step, CUDA graph),
+               inputs resident in HBM; device time from CUDA events on the library's stream
+  e2e          the same metric through the C ABI with HOST buffers: every step writes (centre, velocity) of all bubbles
+               from pinned host memory, steps, and reads them back
+  per_world    the plain per-world launch path on the same worlds (one launch per world, one after another)
+  latency      p50 / p99 device time of one batched step
+  roofline     algorithmic bytes of the dominant kernel (batch_step_kernel) per second against the measured HBM peak
+  cpu_baseline the CPU oracle (C++ restatement of the reference's algorithm, OpenMP over worlds) on a bounded sample
+
+--impl reference times the reference algorithm on the host cores (the oracle port: the reference itself is Swift +
+Metal and cannot run here) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "bubble-substeps/s (batched worlds, 1 GB300)"
+UNIT = "bubble-substeps/s"
+PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
+PROFILE_FILE = ROOT / "profiles" / "batch_step_kernel.json"
+
+
+def env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def algorithmic_bytes(bubble_substeps: float, bubble_builds: float, mean_degree: float) -> float:
+    """Bytes one bubble-substep must move without cache reuse: own state 48 B, constants 28 B, neighbour indices
+    4 B x k x 2 passes, neighbour state 16 B x k x 2 passes -> 76 + 40 k; a grid build adds 96 + 8 k per bubble."""
+    return bubble_substeps * (76.0 + 40.0 * mean_degree) + bubble_builds * (96.0 + 8.0 * mean_degree)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def pinned_buffer(count: int):
+    """A page-locked host buffer of `count` float4 records (torch's pinned allocator; plain numpy otherwise)."""
+    try:
+        import torch
+        t = torch.empty((count, 4), dtype=torch.float32, pin_memory=True)
+        return t.numpy(), t
+    except Exception:
+        a = np.zeros((count, 4), np.float32)
+        return a, None
+
+
+def cpu_sample(specs, max_seconds=12.0, threads=0):
+    """Oracle on a bounded sample: steps the sample worlds until ~max_seconds of CPU work; bubble-substeps/s."""
+    from oracle import oracle
+    used = oracle.set_threads(threads if threads > 0 else (os.cpu_count() or 1))
+    worlds = [oracle.OracleWorld(s, 32) for s in specs]
+    total, steps, t0 = 0, 0, time.perf_counter()
+    while True:
+        total += oracle.step_worlds(worlds, 1, 0)
+        steps += 1
+        if time.perf_counter() - t0 > max_seconds or steps >= 50:
+            break
+    dt = time.perf_counter() - t0
+    return total / dt, used, steps, dt, total
+
+
+def load_peak():
+    try:
+        peaks = json.loads(PEAKS_FILE.read_text())
+        return float(peaks["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return 0
+    from bubblephysics_gb300 import scenes
+    sample = max(1, args.sample_worlds)
+    specs = scenes.batched_worlds(args.worlds, seed=3, limit=sample)
+    from oracle import oracle
+    cores = oracle.set_threads(os.cpu_count() or 1)
+    worlds = [oracle.OracleWorld(s, 32) for s in specs]
+    for _ in range(args.warmup):
+        oracle.step_worlds(worlds, 1, 0)
+    t0 = time.perf_counter()
+    total = 0
+    for _ in range(args.steps):
+        total += oracle.step_worlds(worlds, 1, 0)
+    dt = time.perf_counter() - t0
+    value = total / dt
+    nb = sum(s.bubble_count for s in specs)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1000.0 / max(args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"batched worlds ({args.worlds} worlds, N~LogUniform[16,1024], r~U[6,24], "
+                                   f"0-32 bodies, dt=1/60)", "sample_worlds": sample, "sample_bubbles": nb},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"first {sample} worlds ({nb} bubbles) of the batched workload, "
+                                       f"{args.steps} timed steps; the reference is Swift + Metal (no toolchain, no "
+                                       f"Metal) so its algorithm runs as the C++ oracle port"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, rank, world_size, local_rank):
+    from bubblephysics_gb300 import scenes
+    from bubblephysics_gb300.solver import Batch, Context
+
+    dist = None
+    if world_size > 1:
+        import torch.distributed as dist_mod
+        dist = dist_mod
+        dist.init_process_group("gloo")
+
+    ctx = Context(local_rank)
+    specs = scenes.batched_worlds(args.worlds, seed=3 + rank)
+    total_bubbles = sum(s.bubble_count for s in specs)
+    batch = Batch(specs, ctx, use_graph=True, autotune=True)
+    st, _ = batch.step(args.warmup)
+    _, subs0, launches0 = batch.counters()
+    if dist:
+        dist.barrier()
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    step_ms, statuses = [], []
+    rebuild_bubbles = 0
+    for _ in range(args.steps):
+        status, reps = batch.step(1)
+        statuses.append(status)
+        step_ms.append(float(reps["gpu_ms"][0]))
+        rebuild_bubbles += int((reps["rebuild_count"].astype(np.int64) * batch.sizes).sum())
+    clocks = sampler.stop()
+    _, subs1, launches1 = batch.counters()
+    device_s = sum(step_ms) / 1000.0
+    bubble_substeps = subs1 - subs0
+    degree_sum = batch.adjacency_entries()
+    mean_degree = degree_sum / max(total_bubbles, 1)
+    builds = total_bubbles * args.steps + rebuild_bubbles
+    alg_bytes = algorithmic_bytes(bubble_substeps, builds, mean_degree)
+    kernel_launches = (launches1 - launches0)
+    gpu_launches = kernel_launches + args.steps  # + the report-accumulation kernel of each step
+    if dist:
+        import torch
+        t = torch.tensor([device_s, float(bubble_substeps)], dtype=torch.float64)
+        mx = t.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        sm = t.clone()
+        dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+        device_s_all, substeps_all = float(mx[0]), float(sm[1])
+    else:
+        device_s_all, substeps_all = device_s, float(bubble_substeps)
+    value = substeps_all / device_s_all if device_s_all > 0 else 0.0
+
+    # end to end through the C ABI with host buffers
+    host, keep = pinned_buffer(total_bubbles)
+    batch.read_state(host)
+    _, e2e_s0, _ = batch.counters()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        batch.write_state(host)
+        batch.step(1)
+        batch.read_state(host)
+    e2e_wall = time.perf_counter() - t0
+    _, e2e_s1, _ = batch.counters()
+    e2e_value = (e2e_s1 - e2e_s0) / e2e_wall if e2e_wall > 0 else 0.0
+
+    # the plain per-world launch path on the same worlds, from the same initial state
+    per_world = None
+    if args.per_world_steps > 0:
+        plain = Batch(specs, ctx, per_world_launch=True, use_graph=False)
+        plain.step(1)
+        _, p0, pl0 = plain.counters()
+        _, preps = plain.step(args.per_world_steps)
+        _, p1, pl1 = plain.counters()
+        pms = float(preps["gpu_ms"][0])
+        fused = Batch(specs, ctx, use_graph=True)
+        fused.step(1)
+        _, f0, _ = fused.counters()
+        _, freps = fused.step(args.per_world_steps)
+        _, f1, _ = fused.counters()
+        fms = float(freps["gpu_ms"][0])
+        per_world = {"value": (p1 - p0) / (pms / 1000.0), "unit": UNIT, "launches_per_step": (pl1 - pl0) // args.per_world_steps,
+                     "ms_per_step": pms / args.per_world_steps,
+                     "batched_same_steps": (f1 - f0) / (fms / 1000.0),
+                     "speedup_batched_vs_per_world": ((f1 - f0) / fms) / ((p1 - p0) / pms) if pms > 0 and p1 > p0 else None,
+                     "steps": args.per_world_steps}
+        plain.close()
+        fused.close()
+
+    if rank != 0:
+        if dist:
+            dist.barrier()
+        return 0
+
+    peak, peak_kind = load_peak()
+    achieved = alg_bytes / device_s / 1e9 if device_s > 0 else 0.0
+    traffic = None
+    try:
+        prof = json.loads(PROFILE_FILE.read_text())
+        # dram bytes per bubble-substep measured by ncu on a smaller batch, scaled to one launch of this workload
+        per_unit = float(prof["dram_bytes_per_bubble_substep"])
+        traffic = per_unit * bubble_substeps / max(kernel_launches, 1)
+    except Exception:
+        traffic = None
+    alg_per_launch = alg_bytes / max(kernel_launches, 1)
+    cpu_specs = specs[:args.cpu_sample_worlds]
+    cpu_value, cores, cpu_steps, cpu_dt, cpu_total = cpu_sample(cpu_specs, max_seconds=args.cpu_seconds)
+    lat = sorted(step_ms)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": device_s_all * 1000.0 / max(args.steps, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"batched worlds ({args.worlds} worlds per GPU, N~LogUniform[16,1024], r~U[6,24], "
+                               f"0-32 bodies, dt=1/60)", "worlds": args.worlds, "bubbles": total_bubbles,
+                   "l2": "inputs larger than L2: every step touches the state of all worlds (>129 MB)",
+                   "substeps_per_step_mean": bubble_substeps / max(total_bubbles * args.steps, 1),
+                   "mean_adjacency_degree": mean_degree, "statuses": sorted(set(statuses))},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": total_bubbles * 16,
+                "d2h_bytes_per_step": total_bubbles * 16, "steps": args.e2e_steps,
+                "note": "C ABI bp_batch_write_state + bp_batch_step + bp_batch_read_state from pinned host memory, wall clock"},
+        "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)],
+                       "max": lat[-1]},
+        "per_world_launch": per_world,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "kernel": "batch_step_kernel", "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": alg_per_launch,
+                     "bytes_model": "76 + 40*k per bubble-substep, 96 + 8*k per bubble grid build (k = mean degree)"},
+        "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"first {len(cpu_specs)} worlds of the workload, {cpu_steps} steps, {cpu_dt:.1f} s"},
+        "clocks": clocks,
+        "gpu_launches": gpu_launches,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+    return 0
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=30)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--worlds", type=int, default=4096)
+    p.add_argument("--e2e-steps", type=int, default=10)
+    p.add_argument("--per-world-steps", type=int, default=2)
+    p.add_argument("--cpu-sample-worlds", type=int, default=256)
+    p.add_argument("--cpu-seconds", type=float, default=10.0)
+    p.add_argument("--sample-worlds", type=int, default=1024)
+    args = p.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank = env_int("RANK", 0)
+    world_size = env_int("WORLD_SIZE", 1)
+    local_rank = env_int("LOCAL_RANK", 0)
+    if args.impl == "reference":
+        return run_reference(args, rank)
+    return run_ours(args, rank, world_size, local_rank)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

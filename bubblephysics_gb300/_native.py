@@ -201,6 +201,7 @@ _SIGNATURES = {
     "bp_batch_write_state": (C.c_int, [_P, _P, C.c_uint64]),
     "bp_batch_read_state": (C.c_int, [_P, _P, C.c_uint64]),
     "bp_batch_tuning": (C.c_int, [_P, C.POINTER(C.c_uint32), C.c_uint32]),
+    "bp_batch_adjacency_entries": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "bp_static_polygon_edges": (C.c_int, [C.POINTER(C.c_float), C.c_uint32, C.c_int64, C.c_int64, C.c_uint32,
                                           C.POINTER(Segment), C.c_uint32, C.POINTER(C.c_uint32)]),
     "bp_device_contact_law": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint32]),

@@ -14,8 +14,10 @@ __global__ void accumulate_kernel(const bp_step_report* rep, bp_step_report* acc
         bp_step_report r = rep[w];
         bp_step_report a = acc[w];
         uint32_t sum = a.substep_count + r.substep_count;
+        uint32_t rebuilds = a.rebuild_count + r.rebuild_count;
         if (a.status == BP_OK) a = r;
         a.substep_count = sum;
+        a.rebuild_count = rebuilds;
         acc[w] = a;
         local = (unsigned long long)sizes[w] * r.substep_count;
     }
@@ -37,6 +39,21 @@ __global__ void read_state_kernel(float4* out, const float2* ppos, const float2*
     if (i >= n) return;
     float2 p = ppos[i], u = pvel[i];
     out[i] = make_float4(p.x, p.y, u.x, u.y);
+}
+
+__global__ void sum_kernel(const uint32_t* v, uint64_t n, unsigned long long* total) {
+    unsigned long long local = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        local += v[i];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) local += __shfl_xor_sync(0xffffffffu, local, off);
+    if ((threadIdx.x & 31u) == 0u && local) atomicAdd(total, local);
+}
+
+cudaError_t launch_sum(const uint32_t* v, uint64_t n, unsigned long long* total, cudaStream_t stream) {
+    if (!n) return cudaSuccess;
+    sum_kernel<<<256, 256, 0, stream>>>(v, n, total);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_accumulate(const bp_step_report* reports, bp_step_report* acc, const uint32_t* sizes,

@@ -19,8 +19,8 @@
 #include "bp_device.cuh"
 
 namespace bp {
-cudaError_t launch_batch(const DState& S, const uint32_t* dWorldList, uint32_t count, uint32_t threads, uint32_t B,
-                         uint32_t maxN, cudaStream_t stream);
+cudaError_t launch_persistent(const DState& S, const QueueArgs& q, uint32_t threads, uint32_t blocks, cudaStream_t stream);
+uint32_t persistent_blocks(const QueueArgs& q, uint32_t threads);
 int large_max_blocks(int threads);
 cudaError_t launch_large(const DState& S, uint32_t wi, uint32_t B, int blocks, int threads, cudaStream_t stream);
 cudaError_t launch_contact_law(uint32_t mode, const float* in, float* out, uint32_t count, cudaStream_t stream);
@@ -30,6 +30,7 @@ cudaError_t launch_write_state(const float4* in, float2* pos, float2* vel, float
                                cudaStream_t stream);
 cudaError_t launch_read_state(float4* out, const float2* ppos, const float2* pvel, uint64_t n, cudaStream_t stream);
 void prepare_kernels();
+cudaError_t launch_sum(const uint32_t* v, uint64_t n, unsigned long long* total, cudaStream_t stream);
 }  // namespace bp
 
 using namespace bp;
@@ -49,8 +50,9 @@ static_assert(offsetof(bp_step_report, limiter_object) == 40, "bp_step_report of
 namespace {
 
 constexpr uint32_t kCtaMaxBubbles = 4096;
-constexpr uint32_t kClasses = 9;  // class c: worlds of at most 2^(c+4) bubbles
 constexpr int kLargeThreads = 512;
+constexpr uint32_t kDefaultThreads = 256;
+constexpr uint32_t kDefaultWarpMax = 64;
 
 struct DeviceGuard {
     int previous = -1;
@@ -70,16 +72,7 @@ uint32_t next_pow2(uint32_t v) {
     while (p < v) p <<= 1;
     return p;
 }
-uint32_t size_class(uint32_t n) {
-    uint32_t c = 0;
-    while (c + 1 < kClasses && n > (16u << c)) ++c;
-    return c;
-}
-uint32_t default_threads(uint32_t maxN) {
-    // enough threads for one or two bubbles each, at least two warps
-    uint32_t t = next_pow2(std::max<uint32_t>(maxN / 2, 64u));
-    return std::min<uint32_t>(t, 512u);
-}
+uint32_t grid_buckets(uint32_t maxN) { return next_pow2(std::max<uint32_t>(2u * maxN, 32u)); }
 
 }  // namespace
 
@@ -109,11 +102,15 @@ struct WorldSet {
     unsigned long long* dTotal = nullptr;
     float4* dStaging = nullptr;
     std::vector<void*> allocations;
-    // scheduling
-    std::vector<uint32_t> classWorlds[kClasses];
-    uint32_t* dClassList[kClasses] = {};
-    uint32_t classThreads[kClasses] = {};
-    uint32_t classMaxN[kClasses] = {};
+    // scheduling: worlds stepped by a block (CTA team) or by one warp (warp team), largest first
+    std::vector<uint32_t> ctaWorlds, warpWorlds;
+    uint32_t* dCtaList = nullptr;
+    uint32_t* dWarpList = nullptr;
+    uint32_t* dQueue = nullptr;
+    uint32_t threads = kDefaultThreads;
+    uint32_t warpMax = kDefaultWarpMax;
+    uint32_t blocks = 0;
+    QueueArgs queue{};
     std::vector<uint32_t> largeWorlds;
     uint32_t largeB = 0, largeMaxN = 0;
     int largeBlocks = 0;
@@ -194,6 +191,38 @@ int validate(const bp_world_desc& d, const bp_world_input& in) {
     }
     if (in.joint_entity_count && in.joint_entity_count > in.bubble_count + in.body_count) return BP_E_INVALID;
     return BP_OK;
+}
+
+// Splits the non-large worlds into the CTA and warp queues (largest first) for a block width and warp-team threshold.
+cudaError_t schedule(WorldSet& ws, uint32_t threads, uint32_t warpMax) {
+    ws.threads = threads;
+    ws.warpMax = warpMax;
+    ws.ctaWorlds.clear();
+    ws.warpWorlds.clear();
+    for (uint32_t w = 0; w < ws.nWorlds; ++w) {
+        const DWorld& W = ws.hWorlds[w];
+        if (W.n > kCtaMaxBubbles || (W.flags & BP_WORLD_FORCE_MULTI_CTA)) continue;
+        (W.n <= warpMax ? ws.warpWorlds : ws.ctaWorlds).push_back(w);
+    }
+    auto bySize = [&](uint32_t a, uint32_t b) { return ws.hWorlds[a].n > ws.hWorlds[b].n; };
+    std::stable_sort(ws.ctaWorlds.begin(), ws.ctaWorlds.end(), bySize);
+    std::stable_sort(ws.warpWorlds.begin(), ws.warpWorlds.end(), bySize);
+    QueueArgs& q = ws.queue;
+    q.ctaList = ws.dCtaList;
+    q.warpList = ws.dWarpList;
+    q.queue = ws.dQueue;
+    q.nCta = (uint32_t)ws.ctaWorlds.size();
+    q.nWarp = (uint32_t)ws.warpWorlds.size();
+    q.ctaMaxN = q.nCta ? std::max<uint32_t>(ws.hWorlds[ws.ctaWorlds[0]].n, 1u) : 0u;
+    q.warpMaxN = q.nWarp ? std::max<uint32_t>(ws.hWorlds[ws.warpWorlds[0]].n, 1u) : 0u;
+    q.ctaB = q.nCta ? grid_buckets(q.ctaMaxN) : 0u;
+    q.warpB = q.nWarp ? grid_buckets(q.warpMaxN) : 0u;
+    cudaError_t err = upload(ws.dCtaList, ws.ctaWorlds.data(), ws.ctaWorlds.size(), ws.ctx->stream);
+    if (!err) err = upload(ws.dWarpList, ws.warpWorlds.data(), ws.warpWorlds.size(), ws.ctx->stream);
+    if (!err) err = cudaStreamSynchronize(ws.ctx->stream);
+    ws.blocks = persistent_blocks(q, threads);
+    if (ws.graph) { cudaGraphExecDestroy(ws.graph); ws.graph = nullptr; }
+    return err;
 }
 
 int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc* descs, const bp_world_input* inputs,
@@ -316,6 +345,13 @@ int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc
             B.voff = (uint32_t)(obv + r.vertex_offset); B.vcount = r.vertex_count;
             B.toff = (uint32_t)(obt + r.triangle_offset); B.tcount = r.triangle_count;
             B.cat = r.category; B.mask = r.mask; B.id = r.id;
+            // hull radius: farthest core vertex plus the core radius (pre-filter of the inside-body assertion)
+            float hull = 0.0f;
+            for (uint32_t v = 0; v < r.vertex_count; ++v) {
+                float x = in.body_vertices[2 * (r.vertex_offset + v)], y = in.body_vertices[2 * (r.vertex_offset + v) + 1];
+                hull = std::max(hull, std::sqrt(x * x + y * y));
+            }
+            B.pad = hull + r.core_radius;
             ws.hBodyIds[obo + b] = r.id;
         }
         for (uint32_t v = 0; v < in.field_vertex_count; ++v)
@@ -400,25 +436,14 @@ int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc
     S.contacts = ws.alloc<DContact>(contacts, err);
     S.failed = ws.alloc<uint32_t>(count, err);
     S.scanA = ws.alloc<uint32_t>(nb, err); S.scanB = ws.alloc<uint32_t>(nb, err);
-    // scheduling: size classes and large worlds
+    // scheduling: large worlds go to the cooperative path, the others to the persistent kernel's queues
     for (uint32_t w = 0; w < count; ++w) {
         uint32_t n = ws.hWorlds[w].n;
         if (n > kCtaMaxBubbles || (ws.hWorlds[w].flags & BP_WORLD_FORCE_MULTI_CTA)) ws.largeWorlds.push_back(w);
-        else {
-            uint32_t c = size_class(n);
-            ws.classWorlds[c].push_back(w);
-            ws.classMaxN[c] = std::max(ws.classMaxN[c], n);
-        }
     }
-    for (uint32_t c = 0; c < kClasses; ++c) {
-        // biggest worlds first so the tail of the launch holds the short ones
-        std::stable_sort(ws.classWorlds[c].begin(), ws.classWorlds[c].end(),
-                         [&](uint32_t a, uint32_t b) { return ws.hWorlds[a].n > ws.hWorlds[b].n; });
-        if (!ws.classWorlds[c].empty()) {
-            ws.dClassList[c] = ws.alloc<uint32_t>(ws.classWorlds[c].size(), err);
-            ws.classThreads[c] = default_threads(ws.classMaxN[c]);
-        }
-    }
+    ws.dCtaList = ws.alloc<uint32_t>(count, err);
+    ws.dWarpList = ws.alloc<uint32_t>(count, err);
+    ws.dQueue = ws.alloc<uint32_t>(2, err);
     ws.dSingle = ws.alloc<uint32_t>(count, err);
     for (uint32_t w : ws.largeWorlds) ws.largeMaxN = std::max(ws.largeMaxN, ws.hWorlds[w].n);
     ws.largeB = next_pow2(std::max<uint32_t>(2u * ws.largeMaxN, 64u));
@@ -429,6 +454,11 @@ int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc
     S.gentries = ws.alloc<uint32_t>(std::max<uint32_t>(ws.largeMaxN, 1u), err);
     S.barrier = ws.alloc<unsigned int>(2, err);
     S.errorFlag = ws.alloc<uint32_t>(1, err);
+#ifdef BP_PHASE_TIMING
+    S.phaseCycles = ws.alloc<unsigned long long>((uint64_t)count * kPhaseCount, err);
+#else
+    S.phaseCycles = nullptr;
+#endif
     if (err != cudaSuccess) return cuda_status(err);
 
     std::vector<uint32_t> sizes(count), identity(count);
@@ -436,8 +466,6 @@ int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc
     err = upload(ws.dWorlds, ws.hWorlds.data(), count, st);
     if (!err) err = upload(ws.dSizes, sizes.data(), count, st);
     if (!err) err = upload(ws.dSingle, identity.data(), count, st);
-    for (uint32_t c = 0; c < kClasses && !err; ++c)
-        if (!ws.classWorlds[c].empty()) err = upload(ws.dClassList[c], ws.classWorlds[c].data(), ws.classWorlds[c].size(), st);
     if (!err) err = upload(S.pos, pos.data(), nb, st);
     if (!err) err = upload(S.pPos, pos.data(), nb, st);
     if (!err) err = upload(S.start, start.data(), nb, st);
@@ -464,6 +492,7 @@ int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc
     if (!err) err = upload(dJr, jranges.data(), njr, st);
     if (!err) err = upload(dJp, jpartners.data(), njp, st);
     if (!err) err = cudaStreamSynchronize(st);
+    if (!err) err = schedule(ws, ws.threads, ws.warpMax);
     return cuda_status(err);
 }
 
@@ -476,24 +505,21 @@ cudaError_t launch_step(WorldSet& ws, bool perWorld, uint32_t only = 0xffffffffu
         ws.launches++;
         if (W.n > kCtaMaxBubbles || (W.flags & BP_WORLD_FORCE_MULTI_CTA))
             return launch_large(ws.S, w, ws.largeB, ws.largeBlocks, kLargeThreads, st);
-        uint32_t c = size_class(W.n);
+        QueueArgs q{};
+        q.queue = ws.dQueue;
         uint32_t maxN = std::max<uint32_t>(W.n, 1u);
-        uint32_t B = next_pow2(std::max<uint32_t>(2u * maxN, 32u));
-        uint32_t threads = ws.fixedThreads ? ws.fixedThreads : (ws.classThreads[c] ? ws.classThreads[c] : default_threads(maxN));
-        return launch_batch(ws.S, ws.dSingle + w, 1, threads, B, maxN, st);
+        if (W.n <= ws.warpMax) { q.warpList = ws.dSingle + w; q.nWarp = 1; q.warpMaxN = maxN; q.warpB = grid_buckets(maxN); }
+        else { q.ctaList = ws.dSingle + w; q.nCta = 1; q.ctaMaxN = maxN; q.ctaB = grid_buckets(maxN); }
+        return launch_persistent(ws.S, q, W.n <= ws.warpMax ? 32u : ws.threads, 1u, st);
     };
     if (only < ws.nWorlds) return one(only);
     if (perWorld) {
         for (uint32_t w = 0; w < ws.nWorlds && err == cudaSuccess; ++w) err = one(w);
         return err;
     }
-    for (uint32_t c = 0; c < kClasses && err == cudaSuccess; ++c) {
-        if (ws.classWorlds[c].empty()) continue;
-        uint32_t maxN = std::max<uint32_t>(ws.classMaxN[c], 1u);
-        uint32_t B = next_pow2(std::max<uint32_t>(2u * maxN, 32u));
-        uint32_t threads = ws.fixedThreads ? ws.fixedThreads : ws.classThreads[c];
+    if (ws.queue.nCta + ws.queue.nWarp) {
         ws.launches++;
-        err = launch_batch(ws.S, ws.dClassList[c], (uint32_t)ws.classWorlds[c].size(), threads, B, maxN, st);
+        err = launch_persistent(ws.S, ws.queue, ws.threads, ws.blocks, st);
     }
     for (uint32_t w : ws.largeWorlds) {
         if (err != cudaSuccess) break;
@@ -540,8 +566,8 @@ void free_snapshot(Snapshot& snap) {
     snap.copies.clear();
 }
 
-// Project autotuner: per size class, time one step at each candidate block width from the same saved state and keep
-// the fastest; the state is restored afterwards so tuning does not advance the simulation.
+// Project autotuner: times one step of the whole batch for each (block width, warp-team threshold) candidate from the
+// same saved state and keeps the fastest; the state is restored afterwards so tuning does not advance the simulation.
 cudaError_t autotune(WorldSet& ws) {
     if (ws.tuned) return cudaSuccess;
     ws.tuned = true;
@@ -549,29 +575,28 @@ cudaError_t autotune(WorldSet& ws) {
     Snapshot snap;
     cudaError_t err = take_snapshot(ws, snap);
     cudaStream_t st = ws.ctx->stream;
-    const uint32_t candidates[] = {64, 128, 256, 512, 1024};
-    for (uint32_t c = 0; c < kClasses && !err; ++c) {
-        if (ws.classWorlds[c].empty()) continue;
-        uint32_t maxN = std::max<uint32_t>(ws.classMaxN[c], 1u);
-        uint32_t B = next_pow2(std::max<uint32_t>(2u * maxN, 32u));
-        float best = 1e30f;
-        uint32_t bestT = ws.classThreads[c];
-        for (uint32_t t : candidates) {
-            if (t > 64 && t > 2 * next_pow2(maxN)) break;
+    const uint32_t widths[] = {128, 256, 512};
+    const uint32_t warpMaxes[] = {0, 32, 64, 128};
+    float best = 1e30f;
+    uint32_t bestT = ws.threads, bestW = ws.warpMax;
+    for (uint32_t t : widths) {
+        for (uint32_t wm : warpMaxes) {
+            if (err) break;
+            err = schedule(ws, t, wm);
             for (int rep = 0; rep < 2 && !err; ++rep) {  // the first run warms up
                 err = restore_snapshot(ws, snap);
                 if (err) break;
                 cudaEventRecord(ws.ctx->start, st);
-                err = launch_batch(ws.S, ws.dClassList[c], (uint32_t)ws.classWorlds[c].size(), t, B, maxN, st);
+                err = launch_persistent(ws.S, ws.queue, ws.threads, ws.blocks, st);
                 cudaEventRecord(ws.ctx->stop, st);
                 if (!err) err = cudaEventSynchronize(ws.ctx->stop);
                 float ms = 0.0f;
                 cudaEventElapsedTime(&ms, ws.ctx->start, ws.ctx->stop);
-                if (!err && rep == 1 && ms < best) { best = ms; bestT = t; }
+                if (!err && rep == 1 && ms < best) { best = ms; bestT = t; bestW = wm; }
             }
         }
-        ws.classThreads[c] = bestT;
     }
+    if (!err) err = schedule(ws, bestT, bestW);
     cudaError_t rerr = restore_snapshot(ws, snap);
     if (!rerr) rerr = cudaStreamSynchronize(st);
     free_snapshot(snap);
@@ -614,10 +639,9 @@ int step_set(WorldSet& ws, uint32_t steps, bp_step_report* reports, bool perWorl
         if (g) cudaGraphDestroy(g);
         if (err) return cuda_status(err);
     }
-    uint32_t launchesPerStep = 0;
-    for (uint32_t c = 0; c < kClasses; ++c) launchesPerStep += ws.classWorlds[c].empty() ? 0u : 1u;
-    launchesPerStep += (uint32_t)ws.largeWorlds.size();
+    uint32_t launchesPerStep = (ws.queue.nCta + ws.queue.nWarp ? 1u : 0u) + (uint32_t)ws.largeWorlds.size();
     int status = BP_OK;
+    cudaEventRecord(ws.ctx->start, st);
     for (uint32_t s = 0; s < steps && !err; ++s) {
         if (graphed) {
             err = cudaGraphLaunch(ws.graph, st);
@@ -634,6 +658,7 @@ int step_set(WorldSet& ws, uint32_t steps, bp_step_report* reports, bool perWorl
             if (status != BP_OK && ws.nWorlds == 1) break;
         }
     }
+    cudaEventRecord(ws.ctx->stop, st);
     if (err) return cuda_status(err);
     unsigned long long total = 0;
     err = cudaMemcpyAsync(&total, ws.dTotal, sizeof(total), cudaMemcpyDeviceToHost, st);
@@ -650,9 +675,13 @@ int step_set(WorldSet& ws, uint32_t steps, bp_step_report* reports, bool perWorl
     }
     if (err) return cuda_status(err);
     ws.bubbleSubsteps += total;
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ws.ctx->start, ws.ctx->stop);
     if (reports && !perStepReports)
-        for (uint32_t w = 0; w < ws.nWorlds; ++w)
+        for (uint32_t w = 0; w < ws.nWorlds; ++w) {
+            reports[w].gpu_ms = ms;
             if (reports[w].status != BP_OK && status == BP_OK) status = reports[w].status;
+        }
     return status;
 }
 
@@ -759,7 +788,6 @@ int bp_world_create(bp_context* context, const bp_world_desc* desc, const bp_wor
     if (!w) return BP_E_ALLOC;
     int st = build_set(w->set, context, 1, desc, input, true);
     if (st != BP_OK) { delete w; return st; }
-    w->set.fixedThreads = 0;
     *out = w;
     return BP_OK;
 }
@@ -968,8 +996,9 @@ int bp_batch_create(bp_context* context, uint32_t world_count, const bp_world_de
         b->set.flags = config->flags;
         if (config->threads_per_world) {
             uint32_t t = config->threads_per_world;
-            if (t % 32u || t > 1024u) { delete b; return BP_E_INVALID; }
+            if (t % 32u || t > 512u) { delete b; return BP_E_INVALID; }
             b->set.fixedThreads = t;
+            if (schedule(b->set, t, b->set.warpMax) != cudaSuccess) { delete b; return BP_E_CUDA; }
         }
     }
     *out = b;
@@ -1031,10 +1060,34 @@ int bp_batch_read_state(bp_batch* batch, float* cv, uint64_t bubble_count) {
     return cuda_status(err);
 }
 
-int bp_batch_tuning(bp_batch* batch, uint32_t* threads, uint32_t class_count) {
-    if (!batch || !threads) return BP_E_INVALID;
-    for (uint32_t c = 0; c < class_count && c < kClasses; ++c)
-        threads[c] = batch->set.fixedThreads ? batch->set.fixedThreads : batch->set.classThreads[c];
+int bp_batch_adjacency_entries(bp_batch* batch, uint64_t* entries) {
+    if (!batch || !entries) return BP_E_INVALID;
+    WorldSet& ws = batch->set;
+    DeviceGuard guard(ws.ctx->device);
+    cudaError_t err = cudaMemsetAsync(ws.dTotal, 0, sizeof(unsigned long long), ws.ctx->stream);
+    if (!err) err = launch_sum(ws.S.deg, ws.totalBubbles, ws.dTotal, ws.ctx->stream);
+    unsigned long long total = 0;
+    if (!err) err = cudaMemcpyAsync(&total, ws.dTotal, sizeof(total), cudaMemcpyDeviceToHost, ws.ctx->stream);
+    if (!err) err = cudaStreamSynchronize(ws.ctx->stream);
+    *entries = total;
+    return cuda_status(err);
+}
+
+#ifdef BP_PHASE_TIMING
+// Profiling builds only: accumulated cycles per phase and world (world_count x kPhaseCount).
+int bp_debug_phase_cycles(bp_batch* batch, unsigned long long* out) {
+    WorldSet& ws = batch->set;
+    cudaError_t err = cudaMemcpy(out, ws.S.phaseCycles, ws.nWorlds * kPhaseCount * sizeof(unsigned long long),
+                                 cudaMemcpyDeviceToHost);
+    return cuda_status(err);
+}
+#endif
+
+int bp_batch_tuning(bp_batch* batch, uint32_t* values, uint32_t count) {
+    if (!batch || !values) return BP_E_INVALID;
+    const WorldSet& ws = batch->set;
+    uint32_t v[5] = {ws.threads, ws.warpMax, ws.blocks, ws.queue.nCta, ws.queue.nWarp};
+    for (uint32_t q = 0; q < count && q < 5; ++q) values[q] = v[q];
     return BP_OK;
 }
 

@@ -124,6 +124,18 @@ struct DState {
     uint32_t* gentries;        // hash grid entries
     unsigned int* barrier;     // grid barrier counters [arrivals, generation]
     uint32_t* errorFlag;       // bounded-wait failures
+    unsigned long long* phaseCycles;  // kPhaseCount per world when built with BP_PHASE_TIMING, else null
+};
+
+constexpr uint32_t kPhaseCount = 12;
+
+// Work queues of one persistent step launch (see persistent_step_kernel).
+struct QueueArgs {
+    const uint32_t* ctaList;   // worlds stepped by a whole block, largest first
+    const uint32_t* warpList;  // worlds stepped by one warp, largest first
+    uint32_t* queue;           // [0] next CTA world, [1] next warp world; zeroed before each launch
+    uint32_t nCta, ctaB, ctaMaxN;
+    uint32_t nWarp, warpB, warpMaxN;
 };
 
 // ------------------------------------------------------------------------------------------------------------------

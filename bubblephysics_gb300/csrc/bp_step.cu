@@ -15,6 +15,22 @@ namespace bp {
 constexpr uint32_t kValid = 0x40000000u;  // bubble is in the grid of the current build
 constexpr uint32_t kLive = 0xffu;         // mask of the public flags
 
+// Optional per-phase cycle counters (leader thread's clock) for profiling builds (-DBP_PHASE_TIMING).
+#ifdef BP_PHASE_TIMING
+#define BP_PHASE(id)                                                                                  \
+    do {                                                                                              \
+        if (team.leader() && S.phaseCycles) {                                                         \
+            long long now_ = clock64();                                                               \
+            S.phaseCycles[(uint64_t)wi * kPhaseCount + (id)] += (unsigned long long)(now_ - phaseMark); \
+            phaseMark = now_;                                                                         \
+        }                                                                                             \
+    } while (0)
+#define BP_PHASE_START long long phaseMark = clock64()
+#else
+#define BP_PHASE(id) do { } while (0)
+#define BP_PHASE_START do { } while (0)
+#endif
+
 struct Ctl {  // NativeSubstepControl (NFK:22-26), kept identical in every thread of the team
     float timeX, timeY, timeZ, timeW;
     uint32_t cX, cY, cZ, cW;
@@ -150,6 +166,51 @@ __device__ float2 contact_force(const DState& S, const DWorld& W, uint32_t i, fl
             total = add(total, mul(o.normal, wall_law(ph.z, ph.x, o.distance).force));
         }
     }
+    return total;
+}
+
+// One pass over the adjacency row giving both the contact force (nativeBubbleContactForce, NFK:216-243) and omega^2
+// (nativeBubbleOmegaSquared, NFK:510-541) from the same law evaluations: positions are the same in both, so each term
+// is bit-identical to evaluating the two functions separately; the sums keep their own row order.
+__device__ float2 contact_terms(const DState& S, const DWorld& W, uint32_t i, float fraction, float im, float& omega2) {
+    const uint32_t g = W.boff + i;
+    float2 total = f2(0.0f, 0.0f);
+    float w2 = 0.0f;
+    const float2 p = S.pos[g];
+    const float4 ph = S.phys[g];
+    if (im > 0.0f && W.nbands) {
+        const bp_band* band = find_by_bubble(S.bands + W.bandOff, W.nbands, S.id[g]);
+        if (band) w2 = w2 + band->stiffness * im;
+    }
+    const uint32_t* row = adj_row(S, W, i);
+    const uint32_t d = S.deg[g];
+    for (uint32_t e = 0; e < d; ++e) {
+        uint32_t entry = row[e], kind = entry >> kKindShift, j = entry & kIndexMask;
+        if (kind == 0u) {
+            uint32_t low = min(i, j), high = max(i, j);
+            uint32_t gl = W.boff + low, gh = W.boff + high;
+            float2 delta = sub(S.pos[gh], S.pos[gl]);
+            float dist = len2(delta);
+            float2 normal = dist > 0.0f ? dvd(delta, dist) : f2(1.0f, 0.0f);
+            float4 pl = S.phys[gl], phh = S.phys[gh];
+            Law law = pair_law(pl.z, pl.x, phh.z, phh.x, dist);
+            total = add(total, mul(normal, i == low ? -law.force : law.force));
+            if (im > 0.0f) w2 = w2 + law.stiffness * (im + sqrtf(im * inv_mass(S, W.boff + j)));
+        } else if (kind == 1u) {
+            float2 normal;
+            float dist;
+            if (!wall_region(S.seg[W.soff + j], p, normal, dist) || !(dist < ph.x)) continue;
+            Law wl = wall_law(ph.z, ph.x, dist);
+            total = add(total, mul(normal, wl.force));
+            w2 = w2 + wl.stiffness * im;
+        } else {
+            Obstacle o = body_obstacle(S.bverts, S.btris, S.body[W.bodyOff + j], fraction, p);
+            Law wl = wall_law(ph.z, ph.x, o.distance);
+            total = add(total, mul(o.normal, wl.force));
+            w2 = w2 + wl.stiffness * im;
+        }
+    }
+    omega2 = im > 0.0f ? w2 : 0.0f;
     return total;
 }
 
@@ -490,20 +551,30 @@ __device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, cons
     return cw;
 }
 
-// Contact forces from the current state, then the start-of-build acceleration (phase 2, NFK:776-779).
-template <class Team> __device__ void initial_forces(const DState& S, const DWorld& W, const Ctl& c, const Team& team) {
+// Contact forces from the current state, then the start-of-build acceleration (phase 2, NFK:776-779). Also gives
+// each thread its share of the first reduction: (max omega^2, owner) and (min margin bound, owner).
+template <class Team>
+__device__ void initial_forces(const DState& S, const DWorld& W, const Ctl& c, const Team& team, ValOwner& w2, ValOwner& mg) {
     const float fraction = c.timeX > 0.0f ? clampf(c.timeY / c.timeX, 0.0f, 1.0f) : 1.0f;
+    w2 = ValOwner{-1.0f, 0u};
+    mg = ValOwner{__int_as_float(0x7f800000), 0u};
     for (uint32_t i = team.rank(); i < W.n; i += team.size()) {
         uint32_t g = W.boff + i;
         if (removed(S, g)) continue;
-        float2 F = contact_force(S, W, i, fraction);
-        S.acc[g] = add(mul(F, inv_mass(S, g)), S.a0[g]);
+        float im = inv_mass(S, g), omega2;
+        float2 F = contact_terms(S, W, i, fraction, im, omega2);
+        S.acc[g] = add(mul(F, im), S.a0[g]);
+        if (omega2 > w2.v) { w2.v = omega2; w2.o = i; }
+        float m = margin_bound(S, g);
+        if (m < mg.v) { mg.v = m; mg.o = i; }
     }
     team.sync();
 }
 
 // nativeReduceSubstepInGroup, NFK:625-736
-template <class Team> __device__ void reduce_substep(const DState& S, const DWorld& W, Ctl& c, const Team& team, float* history) {
+template <class Team>
+__device__ void reduce_substep(const DState& S, const DWorld& W, Ctl& c, const Team& team, float* history, ValOwner w2,
+                               ValOwner mg) {
     const float inf = __int_as_float(0x7f800000);
     float remaining = c.timeX - c.timeY;
     bool over = !(remaining > 0.0f), stopped = c.cZ != 0u || c.cW != 0u, limited = c.cY >= kFrameLimit;
@@ -513,14 +584,18 @@ template <class Team> __device__ void reduce_substep(const DState& S, const DWor
         return;
     }
     const float fraction = c.timeX > 0.0f ? clampf(c.timeY / c.timeX, 0.0f, 1.0f) : 1.0f;
-    ValOwner w2{-1.0f, 0u}, mg{inf, 0u};
-    for (uint32_t i = team.rank(); i < W.n; i += team.size()) {
-        uint32_t g = W.boff + i;
-        if (removed(S, g)) continue;
-        float v = omega_squared(S, W, i, fraction);
-        if (v > w2.v) { w2.v = v; w2.o = i; }
-        float m = margin_bound(S, g);
-        if (m < mg.v) { mg.v = m; mg.o = i; }
+    if (W.flags & BP_WORLD_INJECT_STATE) {
+        // an injected position invalidates the partials of the force pass: evaluate the terms afresh
+        w2 = ValOwner{-1.0f, 0u};
+        mg = ValOwner{inf, 0u};
+        for (uint32_t i = team.rank(); i < W.n; i += team.size()) {
+            uint32_t g = W.boff + i;
+            if (removed(S, g)) continue;
+            float v = omega_squared(S, W, i, fraction);
+            if (v > w2.v) { w2.v = v; w2.o = i; }
+            float m = margin_bound(S, g);
+            if (m < mg.v) { mg.v = m; mg.o = i; }
+        }
     }
     w2 = team.template pick<true>(w2);
     mg = team.template pick<false>(mg);
@@ -582,12 +657,18 @@ __device__ __forceinline__ void kick_drift(const DState& S, const DWorld& W, uin
     S.rotw[g] = f2(rw.x + rw.y * h, angular);
 }
 
-// Contact forces from the new state and phase 1 (NFK:798-801): a = F / m + a0(x), second half kick.
-__device__ __forceinline__ void force_kick(const DState& S, const DWorld& W, uint32_t i, float h, float fraction) {
+// Contact forces from the new state and phase 1 (NFK:798-801): a = F / m + a0(x), second half kick. The same pass
+// gives omega^2 and the margin bound of the next reduction (same positions, velocities and accelerations it would read).
+__device__ __forceinline__ void force_kick(const DState& S, const DWorld& W, uint32_t i, float h, float fraction,
+                                           ValOwner& w2, ValOwner& mg) {
     const uint32_t g = W.boff + i;
     float im = inv_mass(S, g);
-    if (!(im > 0.0f)) return;
-    float2 F = contact_force(S, W, i, fraction);
+    if (!(im > 0.0f)) {
+        if (0.0f > w2.v) { w2.v = 0.0f; w2.o = i; }
+        return;
+    }
+    float omega2;
+    float2 F = contact_terms(S, W, i, fraction, im, omega2);
     uint32_t f = S.flags[g];
     float halfStep = 0.5f * h;
     float gamma = (f & BP_BUBBLE_FORCE_DRIVEN) ? fmaxf(S.phys[g].w, 0.0f) : 0.0f;
@@ -595,6 +676,9 @@ __device__ __forceinline__ void force_kick(const DState& S, const DWorld& W, uin
     float2 a = add(mul(F, im), non_contact_acc(S, W, g, S.pos[g]));
     S.vel[g] = add(mul(S.vel[g], decay), mul(a, factor));
     S.acc[g] = a;
+    if (omega2 > w2.v) { w2.v = omega2; w2.o = i; }
+    float m = margin_bound(S, g);
+    if (m < mg.v) { mg.v = m; mg.o = i; }
 }
 
 // ------------------------------------------------------------------------------------------------------------------
@@ -636,14 +720,28 @@ __device__ bool assert_bubble(const DState& S, const DWorld& W, const uint32_t* 
     for (uint32_t bi = 0; bi < W.nb; ++bi) {
         const DBody& b = S.body[W.bodyOff + bi];
         if (!filter_accepts(fi, make_uint2(b.cat, b.mask))) continue;
-        if (rigid_inside(S.bverts, S.btris, center, b, body_at(b, fraction))) {
+        Pose pose = body_at(b, fraction);
+        // a centre inside the body is within its hull radius (conservative margin for rounding)
+        float2 rel = sub(center, pose.pos);
+        float reachHull = b.pad * 1.0001f + 1e-3f;
+        if (fabsf(rel.x) > reachHull || fabsf(rel.y) > reachHull) continue;
+        if (rigid_inside(S.bverts, S.btris, center, b, pose)) {
             v.kind = BP_VIOLATION_INSIDE_BODY; v.a = S.id[g]; v.b = b.id; v.edge = 0; v.distance = 0.0f;
             return true;
         }
     }
+    // a crossing point lies on both the chord start -> centre and the edge: their boxes must overlap (conservative
+    // margin for rounding) before the exact test runs
+    const float2 pathLo = vmin2(start, center), pathHi = vmax2(start, center);
+    const float slack = 1e-3f + 1e-5f * fmaxf(fmaxf(fabsf(pathLo.x), fabsf(pathLo.y)), fmaxf(fabsf(pathHi.x), fabsf(pathHi.y)));
     for (uint32_t e = 0; e < W.s; ++e) {
         const DSegment& sg = S.seg[W.soff + e];
-        if (!(sg.flags & BP_SEGMENT_POLYGON_EDGE) || !filter_accepts(fi, make_uint2(sg.cat, sg.mask))) continue;
+        if (!(sg.flags & BP_SEGMENT_POLYGON_EDGE)) continue;
+        float2 segLo = vmin2(sg.a, sg.b), segHi = vmax2(sg.a, sg.b);
+        if (segLo.x > pathHi.x + slack || segLo.y > pathHi.y + slack || segHi.x < pathLo.x - slack ||
+            segHi.y < pathLo.y - slack)
+            continue;
+        if (!filter_accepts(fi, make_uint2(sg.cat, sg.mask))) continue;
         float2 edge = sub(sg.b, sg.a);
         float lsq = dot2(edge, edge);
         if (!(lsq > 0.0f)) continue;
@@ -839,6 +937,7 @@ __device__ void world_step(const DState& S, uint32_t wi, const Team& team, uint3
         if (team.leader()) { rep->status = BP_E_WORLD_FAILED; rep->substep_count = 0u; }
         return;
     }
+    BP_PHASE_START;
     // nativeBeginStep (NFK:285-293)
     uint32_t liveLocal = 0;
     for (uint32_t i = r; i < n; i += T) {
@@ -881,12 +980,17 @@ __device__ void world_step(const DState& S, uint32_t wi, const Team& team, uint3
     c.limTerm = 0u;
     float* history = S.history + (uint64_t)wi * kFrameLimit;
     uint32_t buildOverflow = 0, overflowMax = 0, maxPer = 0, rebuilds = 0;
+    BP_PHASE(0);
     float cw = broadphase(S, W, c, team, buckets, entries, B, buildOverflow, maxPer);
-    initial_forces(S, W, c, team);
+    BP_PHASE(1);
+    ValOwner w2, mg;
+    initial_forces(S, W, c, team, w2, mg);
+    BP_PHASE(2);
     uint32_t violated = 0u;
     for (uint32_t iteration = 0; iteration < 2u * kFrameLimit + 2u; ++iteration) {
         if (!team.ok()) break;
-        reduce_substep(S, W, c, team, history);
+        reduce_substep(S, W, c, team, history, w2, mg);
+        BP_PHASE(3);
         const float h = c.timeZ;
         const bool limited = c.cW != 0u, finished = !(c.timeX - c.timeY > 0.0f), rebuild = c.cZ != 0u;
         if (!(h > 0.0f)) {
@@ -896,16 +1000,20 @@ __device__ void world_step(const DState& S, uint32_t wi, const Team& team, uint3
             overflowMax = max(overflowMax, buildOverflow);
             ++rebuilds;
             cw = broadphase(S, W, c, team, buckets, entries, B, buildOverflow, maxPer);
-            initial_forces(S, W, c, team);
+            initial_forces(S, W, c, team, w2, mg);
+            BP_PHASE(1);
             continue;
         }
         const float fraction = c.timeX > 0.0f ? clampf(c.timeY / c.timeX, 0.0f, 1.0f) : 1.0f;
         for (uint32_t i = r; i < n; i += T)
             if (!removed(S, W.boff + i)) kick_drift(S, W, i, h);
         team.sync();
+        w2 = ValOwner{-1.0f, 0u};
+        mg = ValOwner{__int_as_float(0x7f800000), 0u};
         for (uint32_t i = r; i < n; i += T)
-            if (!removed(S, W.boff + i)) force_kick(S, W, i, h, fraction);
+            if (!removed(S, W.boff + i)) force_kick(S, W, i, h, fraction, w2, mg);
         team.sync();
+        BP_PHASE(4);
         if (W.flags & BP_WORLD_INJECT_STATE) {
             if (c.cY == W.injectSubstep + 1u)
                 for (uint32_t i = r; i < n; i += T)
@@ -916,6 +1024,7 @@ __device__ void world_step(const DState& S, uint32_t wi, const Team& team, uint3
             violated = assert_contacts(S, W, team, buckets, entries, B, cw, c.timeX > 0.0f ? clampf(c.timeY / c.timeX, 0.0f, 1.0f) : 1.0f, rep);
     }
     overflowMax = max(overflowMax, buildOverflow);
+    BP_PHASE(5);
 
     // ---- end of step ----
     uint32_t removedCount = 0, wrapped = 0, nonfinite = 0;
@@ -941,6 +1050,7 @@ __device__ void world_step(const DState& S, uint32_t wi, const Team& team, uint3
         pairsLocal += cp;
         segsLocal += cs;
     }
+    BP_PHASE(6);
     const uint32_t pairsAll = team.sum(pairsLocal);
     const uint32_t segsAll = team.sum(segsLocal);
     team.scan_inplace(S.scanA + W.boff, n);
@@ -962,6 +1072,7 @@ __device__ void world_step(const DState& S, uint32_t wi, const Team& team, uint3
             else ++droppedLocal;
         }
     }
+    BP_PHASE(7);
     // non-finite state (nativeCheckFinite, NPK:5-27)
     for (uint32_t i = r; i < n; i += T) {
         uint32_t g = W.boff + i;
@@ -970,8 +1081,10 @@ __device__ void world_step(const DState& S, uint32_t wi, const Team& team, uint3
     }
     const uint32_t anyNonfinite = team.umax(nonfinite);
     const uint32_t contactDropped = team.sum(droppedLocal);
+    BP_PHASE(8);
     if (!violated && stepDone && !(W.flags & BP_WORLD_NO_END_ASSERTION))
         violated = assert_contacts(S, W, team, buckets, entries, B, cw, 1.0f, rep);
+    BP_PHASE(9);
     int status = BP_OK;
     if (c.cW != 0u) status = BP_E_SUBSTEP_LIMIT;
     else if (anyNonfinite) status = BP_E_NONFINITE;
@@ -1038,6 +1151,7 @@ __device__ void world_step(const DState& S, uint32_t wi, const Team& team, uint3
         for (uint32_t bi = r; bi < W.nb; bi += T) S.body[W.bodyOff + bi] = S.pBody[W.bodyOff + bi];
         if (team.leader()) S.failed[wi] = 1u;
     }
+    BP_PHASE(10);
 }
 
 // ------------------------------------------------------------------------------------------------------------------
@@ -1045,13 +1159,34 @@ __device__ void world_step(const DState& S, uint32_t wi, const Team& team, uint3
 // ------------------------------------------------------------------------------------------------------------------
 extern __shared__ uint32_t g_dynamic_smem[];
 
-// One block per world of `worldList`; dynamic shared memory holds the hash grid: B bucket ends, then maxN entries.
-template <int kMaxThreads>
-__global__ void __launch_bounds__(kMaxThreads) batch_step_kernel(DState S, const uint32_t* worldList, uint32_t B) {
+// Persistent step kernel: blocks pull worlds from two queues. CTA-team worlds (largest first) are stepped by a whole
+// block; then every warp pulls warp-team worlds (small worlds, one warp each). Dynamic shared memory holds the hash
+// grid: for a CTA world B bucket ends then its entries; for a warp world a slice per warp of the same layout.
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads, 2) persistent_step_kernel(DState S, QueueArgs q) {
     __shared__ BlockScratch sh;
-    CtaTeam team{&sh};
-    const uint32_t wi = worldList[blockIdx.x];
-    world_step(S, wi, team, g_dynamic_smem, g_dynamic_smem + B, B);
+    __shared__ uint32_t next;
+    CtaTeam cta{&sh};
+    for (;;) {
+        if (threadIdx.x == 0) next = atomicAdd(q.queue, 1u);
+        __syncthreads();
+        const uint32_t slot = next;
+        __syncthreads();
+        if (slot >= q.nCta) break;
+        world_step(S, q.ctaList[slot], cta, g_dynamic_smem, g_dynamic_smem + q.ctaB, q.ctaB);
+        __syncthreads();
+    }
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    uint32_t* mine = g_dynamic_smem + warp * (q.warpB + q.warpMaxN);
+    WarpTeam wt;
+    for (;;) {
+        uint32_t slot = 0;
+        if (lane == 0) slot = atomicAdd(q.queue + 1, 1u);
+        slot = __shfl_sync(0xffffffffu, slot, 0);
+        if (slot >= q.nWarp) break;
+        world_step(S, q.warpList[slot], wt, mine, mine + q.warpB, q.warpB);
+        __syncwarp();
+    }
 }
 
 // Cooperative launch: every block steps world `wi` together; the hash grid lives in global memory.
@@ -1076,13 +1211,33 @@ __global__ void contact_law_kernel(uint32_t mode, const float* in, float* out, u
 // ------------------------------------------------------------------------------------------------------------------
 // Host launchers
 // ------------------------------------------------------------------------------------------------------------------
-cudaError_t launch_batch(const DState& S, const uint32_t* dWorldList, uint32_t count, uint32_t threads, uint32_t B,
-                         uint32_t maxN, cudaStream_t stream) {
-    if (count == 0u) return cudaSuccess;
-    size_t smem = (size_t)(B + maxN) * sizeof(uint32_t);
-    if (threads <= 256u) batch_step_kernel<256><<<count, threads, smem, stream>>>(S, dWorldList, B);
-    else batch_step_kernel<1024><<<count, threads, smem, stream>>>(S, dWorldList, B);
+size_t persistent_smem(const QueueArgs& q, uint32_t threads) {
+    size_t cta = (size_t)(q.nCta ? q.ctaB + q.ctaMaxN : 0);
+    size_t warp = (size_t)(q.nWarp ? (threads / 32u) * (q.warpB + q.warpMaxN) : 0);
+    return (cta > warp ? cta : warp) * sizeof(uint32_t);
+}
+
+cudaError_t launch_persistent(const DState& S, const QueueArgs& q, uint32_t threads, uint32_t blocks, cudaStream_t stream) {
+    if (q.nCta + q.nWarp == 0u) return cudaSuccess;
+    size_t smem = persistent_smem(q, threads);
+    cudaError_t err = cudaMemsetAsync(q.queue, 0, 2 * sizeof(uint32_t), stream);
+    if (err) return err;
+    if (threads <= 128u) persistent_step_kernel<128><<<blocks, threads, smem, stream>>>(S, q);
+    else if (threads <= 256u) persistent_step_kernel<256><<<blocks, threads, smem, stream>>>(S, q);
+    else persistent_step_kernel<512><<<blocks, threads, smem, stream>>>(S, q);
     return cudaGetLastError();
+}
+
+// Blocks of the persistent kernel that fit on the GPU at once (the grid size of a full launch).
+uint32_t persistent_blocks(const QueueArgs& q, uint32_t threads) {
+    int device = 0, sms = 0, perSm = 0;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    size_t smem = persistent_smem(q, threads);
+    if (threads <= 128u) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, persistent_step_kernel<128>, threads, smem);
+    else if (threads <= 256u) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, persistent_step_kernel<256>, threads, smem);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, persistent_step_kernel<512>, threads, smem);
+    return (uint32_t)(sms * (perSm > 0 ? perSm : 1));
 }
 
 // Function attributes are set once per process before any launch (never inside a stream capture).
@@ -1090,8 +1245,9 @@ void prepare_kernels() {
     static bool done = false;
     if (done) return;
     done = true;
-    cudaFuncSetAttribute(batch_step_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-    cudaFuncSetAttribute(batch_step_kernel<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(persistent_step_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(persistent_step_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(persistent_step_kernel<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
 }
 
 int large_max_blocks(int threads) {

@@ -171,6 +171,39 @@ struct CtaTeam {
 };
 
 // ----------------------------------------------------------------------------------------------------------------
+// Warp team: one warp owns a small world; syncs are __syncwarp and reductions are shuffles (no block barrier).
+// ----------------------------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t warp_excl_scan(uint32_t x, uint32_t* total) {
+    uint32_t incl = warp_incl_scan(x);
+    *total = __shfl_sync(0xffffffffu, incl, 31);
+    return incl - x;
+}
+
+struct WarpTeam {
+    __device__ uint32_t rank() const { return threadIdx.x & 31u; }
+    __device__ uint32_t size() const { return 32u; }
+    __device__ bool leader() const { return (threadIdx.x & 31u) == 0u; }
+    __device__ bool sync() const { __syncwarp(); return true; }
+    __device__ bool ok() const { return true; }
+    template <bool kMax> __device__ ValOwner pick(ValOwner x) const { return warp_pick<kMax>(x); }
+    __device__ uint32_t sum(uint32_t x) const { return warp_sum(x); }
+    __device__ uint32_t umax(uint32_t x) const { return warp_max(x); }
+    __device__ float fmax(float x) const { return warp_fmax(x); }
+    __device__ void scan_inplace(uint32_t* values, uint32_t count) const {
+        const uint32_t lane = threadIdx.x & 31u;
+        uint32_t per = (count + 31u) / 32u;
+        uint32_t first = min(lane * per, count), last = min(first + per, count);
+        uint32_t local = 0;
+        __syncwarp();
+        for (uint32_t i = first; i < last; ++i) local += values[i];
+        uint32_t total;
+        uint32_t running = warp_excl_scan(local, &total);
+        for (uint32_t i = first; i < last; ++i) { uint32_t own = values[i]; values[i] = running; running += own; }
+        __syncwarp();
+    }
+};
+
+// ----------------------------------------------------------------------------------------------------------------
 // Grid team: every block of a cooperative launch works on one world. Partials go through global memory with
 // alternating parity so a reduction never overwrites partials another block may still read.
 // ----------------------------------------------------------------------------------------------------------------

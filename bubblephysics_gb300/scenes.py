@@ -12,9 +12,11 @@ Resolutions of infeasible or unspecified parts of the workload descriptions (sta
  - large_world (65,536 bubbles, log-normal radii): 60 % area fraction is met locally by a jittered grid in a square
    block at the bottom of the 8192^2 region (the bubbles' total area is only ~15 % of the region); the grid is rebuilt
    almost every substep through the minimum-margin switch.
- - batched worlds: placement is a jittered grid at 40 % area fraction, bubble mass 8, velocities N(0, 30^2); bubbles
-   whose centre would lie inside a rigid body are dropped; bodies are static (circles, capsules, polygons) or kinematic
-   (any shape, slow constant drive), since the reference rejects dynamic bodies next to bubbles.
+ - batched worlds: the description gives no gravity and no mass, so there is none and masses follow the reference's
+   crowd scenes (m = r^2 / 400, Tests/BubblePhysicsRuntimeTests/CrowdSceneSupport.swift:71); placement is a jittered
+   grid at 40 % area fraction, velocities N(0, 30^2); bubbles whose centre would lie inside a rigid body are dropped;
+   bodies are static (circles, capsules, polygons) or kinematic (any shape, slow constant drive), since the reference
+   rejects dynamic bodies next to bubbles.
 """
 from __future__ import annotations
 
@@ -280,9 +282,9 @@ def _clear_of_bodies(centers, radii, bodies, segs):
     return keep
 
 
-def batched_world(rng, n_target: int, *, world_index: int = 0, max_bodies: int = 32) -> WorldSpec:
+def batched_world(rng, n_target: int, *, world_index: int = 0, max_bodies: int = 32, gravity=(0.0, 0.0)) -> WorldSpec:
     """One world of the batched workload: n ~ given, r ~ U[6,24], region sized to 40 % area fraction, 0-32 bodies
-    (half-extents U[8,40]), jittered-grid placement, mass 8, velocities N(0, 30^2)."""
+    (half-extents U[8,40]), jittered-grid placement, mass r^2/400, velocities N(0, 30^2), no gravity."""
     radii = rng.uniform(6.0, 24.0, n_target)
     area = math.pi * float(np.mean(radii ** 2)) * n_target / 0.4
     side = math.sqrt(area)
@@ -297,17 +299,20 @@ def batched_world(rng, n_target: int, *, world_index: int = 0, max_bodies: int =
     centers, radii = centers[keep], radii[keep]
     n = centers.shape[0]
     vel = rng.normal(0.0, 30.0, (n, 2))
-    b = make_bubbles(centers, radii, velocities=vel, masses=8.0, stiffness=K_C, damping=0.0,
+    b = make_bubbles(centers, radii, velocities=vel, masses=radii * radii / 400.0, stiffness=K_C, damping=0.0,
                      flags=N.BUBBLE_FORCE_DRIVEN | N.BUBBLE_ENABLED)
     walls = wall_segments(region)
     segs = np.concatenate([walls, bsegs]) if bsegs.size else walls
     segs = np.sort(segs, order="id")
     return WorldSpec(bubbles=b, segments=segs, bodies=bodies, body_vertices=bverts, body_triangles=btris,
-                     region=region, gravity=GRAVITY, time_step=DT)
+                     region=region, gravity=gravity, time_step=DT)
 
 
-def batched_worlds(count: int = 4096, seed: int = 3, n_min: int = 16, n_max: int = 1024, max_bodies: int = 32):
-    """The batched workload: `count` worlds, bubble counts log-uniform in [n_min, n_max]."""
+def batched_worlds(count: int = 4096, seed: int = 3, n_min: int = 16, n_max: int = 1024, max_bodies: int = 32,
+                   limit: int | None = None):
+    """The batched workload: `count` worlds, bubble counts log-uniform in [n_min, n_max]. `limit` returns only the
+    first worlds of the same sequence (a bounded sample of the workload)."""
     rng = np.random.default_rng(seed)
     sizes = np.exp(rng.uniform(math.log(n_min), math.log(n_max), count)).astype(np.int64)
-    return [batched_world(rng, int(s), world_index=w, max_bodies=max_bodies) for w, s in enumerate(sizes)]
+    take = count if limit is None else min(limit, count)
+    return [batched_world(rng, int(sizes[w]), world_index=w, max_bodies=max_bodies) for w in range(take)]

@@ -197,10 +197,15 @@ class Batch:
                 "bp_batch_read_state")
         return out
 
-    def tuning(self) -> list[int]:
-        out = (C.c_uint32 * 9)()
-        N.check(self.lib.bp_batch_tuning(self.handle, out, 9), "bp_batch_tuning")
-        return list(out)
+    def adjacency_entries(self) -> int:
+        v = C.c_uint64()
+        N.check(self.lib.bp_batch_adjacency_entries(self.handle, C.byref(v)), "bp_batch_adjacency_entries")
+        return v.value
+
+    def tuning(self) -> dict:
+        out = (C.c_uint32 * 5)()
+        N.check(self.lib.bp_batch_tuning(self.handle, out, 5), "bp_batch_tuning")
+        return dict(zip(["threads", "warp_max", "blocks", "cta_worlds", "warp_worlds"], list(out)))
 
 
 def static_polygon_edges(points, first_id: int, owner_id: int | None = None) -> np.ndarray:

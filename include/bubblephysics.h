@@ -312,7 +312,7 @@ enum {
 
 typedef struct bp_batch_config {
     uint32_t flags;                  /* BP_BATCH_* */
-    uint32_t threads_per_world;      /* 0 = automatic (autotuner or size rule) */
+    uint32_t threads_per_world;      /* threads per block of the persistent launch, 0 = automatic (autotuner or 256) */
     uint32_t reserved[2];
 } bp_batch_config;
 
@@ -320,7 +320,8 @@ int bp_batch_create(bp_context* context, uint32_t world_count, const bp_world_de
                     const bp_world_input* inputs, const bp_batch_config* config, bp_batch** out);
 int bp_batch_destroy(bp_batch* batch);
 /* Advances every live world `steps` steps. reports may be NULL, else world_count entries (status of the first
- * failure, or the last step; substep_count summed over the steps). Worlds that fail stop; the others go on. */
+ * failure, or the last step; substep_count and rebuild_count summed over the steps; gpu_ms = device time of the
+ * whole call, measured with events on the library's stream). Worlds that fail stop; the others go on. */
 int bp_batch_step(bp_batch* batch, uint32_t steps, bp_step_report* reports);
 /* Total bubbles and total substeps x bubbles advanced since creation (for throughput). */
 int bp_batch_counters(bp_batch* batch, uint64_t* bubble_count, uint64_t* bubble_substeps, uint64_t* launches);
@@ -328,8 +329,12 @@ int bp_batch_read_bubbles(bp_batch* batch, uint32_t world, bp_bubble* out, uint3
 /* Bulk dynamic state of all worlds in world order: float4 (center.xy, velocity.xy) per bubble. */
 int bp_batch_write_state(bp_batch* batch, const float* center_velocity, uint64_t bubble_count);
 int bp_batch_read_state(bp_batch* batch, float* center_velocity, uint64_t bubble_count);
-/* Threads per world chosen for each size class (class c holds worlds of 2^(c+4) bubbles at most). */
-int bp_batch_tuning(bp_batch* batch, uint32_t* threads_per_class, uint32_t class_count);
+/* Sum of the adjacency degrees of all bubbles of the last grid build (mean degree = sum / bubbles); used to count
+ * the algorithmic bytes of a substep. */
+int bp_batch_adjacency_entries(bp_batch* batch, uint64_t* entries);
+/* Schedule of the batched launch: [0] threads per block, [1] largest world stepped by one warp, [2] blocks of the
+ * persistent launch, [3] worlds stepped by a whole block, [4] worlds stepped by one warp. */
+int bp_batch_tuning(bp_batch* batch, uint32_t* values, uint32_t count);
 
 /* ---- host helpers (reference host logic that feeds the path) -------------------------------------------------- */
 
