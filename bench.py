@@ -172,6 +172,19 @@ def run_reference(args, rank):
     return 0
 
 
+def combine_ranks(device_s: float, bubble_substeps: float, dist=None) -> tuple[float, float]:
+    """Whole-job timing over ranks: the slowest rank's device time and the sum of all ranks' bubble-substeps."""
+    if dist is None:
+        return device_s, bubble_substeps
+    import torch
+    t = torch.tensor([device_s, float(bubble_substeps)], dtype=torch.float64)
+    mx = t.clone()
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    sm = t.clone()
+    dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+    return float(mx[0]), float(sm[1])
+
+
 def run_ours(args, rank, world_size, local_rank):
     from bubblephysics_gb300 import scenes
     from bubblephysics_gb300.solver import Batch, Context
@@ -209,16 +222,7 @@ def run_ours(args, rank, world_size, local_rank):
     alg_bytes = algorithmic_bytes(bubble_substeps, builds, mean_degree)
     kernel_launches = (launches1 - launches0)
     gpu_launches = kernel_launches + args.steps  # + the report-accumulation kernel of each step
-    if dist:
-        import torch
-        t = torch.tensor([device_s, float(bubble_substeps)], dtype=torch.float64)
-        mx = t.clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        sm = t.clone()
-        dist.all_reduce(sm, op=dist.ReduceOp.SUM)
-        device_s_all, substeps_all = float(mx[0]), float(sm[1])
-    else:
-        device_s_all, substeps_all = device_s, float(bubble_substeps)
+    device_s_all, substeps_all = combine_ranks(device_s, float(bubble_substeps), dist)
     value = substeps_all / device_s_all if device_s_all > 0 else 0.0
 
     # end to end through the C ABI with host buffers

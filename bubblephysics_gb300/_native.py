@@ -123,7 +123,8 @@ class CandidateKey(C.Structure):
 
 
 class BatchConfig(C.Structure):
-    _fields_ = [("flags", C.c_uint32), ("threads_per_world", C.c_uint32), ("reserved", C.c_uint32 * 2)]
+    _fields_ = [("flags", C.c_uint32), ("threads_per_world", C.c_uint32), ("warp_world_max", C.c_uint32),
+                ("reserved", C.c_uint32)]
 
 
 RECORD_SIZES = {Bubble: 80, Segment: 64, Body: 80, ForceField: 64, Band: 24, Motor: 24, WorldDesc: 64,

@@ -994,11 +994,12 @@ int bp_batch_create(bp_context* context, uint32_t world_count, const bp_world_de
     if (st != BP_OK) { delete b; return st; }
     if (config) {
         b->set.flags = config->flags;
-        if (config->threads_per_world) {
-            uint32_t t = config->threads_per_world;
-            if (t % 32u || t > 512u) { delete b; return BP_E_INVALID; }
+        uint32_t t = config->threads_per_world ? config->threads_per_world : b->set.threads;
+        uint32_t wm = config->warp_world_max == 0xffffffffu ? 0u : (config->warp_world_max ? config->warp_world_max : b->set.warpMax);
+        if (t % 32u || t > 512u || wm > kCtaMaxBubbles) { delete b; return BP_E_INVALID; }
+        if (config->threads_per_world || config->warp_world_max) {
             b->set.fixedThreads = t;
-            if (schedule(b->set, t, b->set.warpMax) != cudaSuccess) { delete b; return BP_E_CUDA; }
+            if (schedule(b->set, t, wm) != cudaSuccess) { delete b; return BP_E_CUDA; }
         }
     }
     *out = b;

@@ -135,7 +135,7 @@ class Batch:
     per_world_launch=True, the plain path: one launch per world, one after another)."""
 
     def __init__(self, specs: list[WorldSpec], context: Context | None = None, *, per_world_launch=False,
-                 use_graph=True, autotune=False, threads_per_world=0):
+                 use_graph=True, autotune=False, threads_per_world=0, warp_world_max=0):
         self.ctx = context or default_context()
         self.lib = self.ctx.lib
         self.specs = specs
@@ -146,6 +146,7 @@ class Batch:
         cfg.flags = (N.BATCH_PER_WORLD_LAUNCH if per_world_launch else 0) | (N.BATCH_USE_GRAPH if use_graph else 0) | \
                     (N.BATCH_AUTOTUNE if autotune else 0)
         cfg.threads_per_world = threads_per_world
+        cfg.warp_world_max = warp_world_max
         handle = C.c_void_p()
         N.check(self.lib.bp_batch_create(self.ctx.handle, len(specs), descs, inputs, C.byref(cfg), C.byref(handle)),
                 "bp_batch_create")

@@ -313,7 +313,9 @@ enum {
 typedef struct bp_batch_config {
     uint32_t flags;                  /* BP_BATCH_* */
     uint32_t threads_per_world;      /* threads per block of the persistent launch, 0 = automatic (autotuner or 256) */
-    uint32_t reserved[2];
+    uint32_t warp_world_max;         /* worlds of at most this many bubbles are stepped by one warp; 0 = automatic
+                                        (autotuner or 64); UINT32_MAX = no warp teams */
+    uint32_t reserved;
 } bp_batch_config;
 
 int bp_batch_create(bp_context* context, uint32_t world_count, const bp_world_desc* descs,

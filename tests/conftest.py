@@ -20,3 +20,7 @@ def ctx():
     if status != N.OK:
         pytest.fail("GPU test without a usable CUDA device: " + N.STATUS_NAMES[status])
     return Context(0)
+
+TESTS = Path(__file__).resolve().parent
+if str(TESTS) not in sys.path:
+    sys.path.insert(0, str(TESTS))
