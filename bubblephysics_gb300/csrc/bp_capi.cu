@@ -21,6 +21,8 @@
 namespace bp {
 cudaError_t launch_persistent(const DState& S, const QueueArgs& q, uint32_t threads, uint32_t blocks, cudaStream_t stream);
 uint32_t persistent_blocks(const QueueArgs& q, uint32_t threads);
+cudaError_t launch_schedule(const DState& S, const uint32_t* candidates, uint32_t count, uint32_t warpMax,
+                            uint32_t warpSubsteps, uint32_t* ctaList, uint32_t* warpList, uint32_t* queue, cudaStream_t stream);
 int large_max_blocks(int threads);
 cudaError_t launch_large(const DState& S, uint32_t wi, uint32_t B, int blocks, int threads, cudaStream_t stream);
 cudaError_t launch_contact_law(uint32_t mode, const float* in, float* out, uint32_t count, cudaStream_t stream);
@@ -53,6 +55,10 @@ constexpr uint32_t kCtaMaxBubbles = 4096;
 constexpr int kLargeThreads = 512;
 constexpr uint32_t kDefaultThreads = 256;
 constexpr uint32_t kDefaultWarpMax = 64;
+constexpr uint32_t kWarpSubsteps = 16;   // a world that took more substeps last step gets a whole block
+constexpr uint32_t kCtaWorkspaceCap = 96u * 1024u;   // shared-memory workspace of a block team (2 blocks per SM)
+constexpr uint32_t kWarpWorkspaceCap = 12u * 1024u;  // per warp team
+constexpr uint32_t kMaxDynamicSmem = 200u * 1024u;   // per block, set on the kernels by prepare_kernels()
 
 struct DeviceGuard {
     int previous = -1;
@@ -73,10 +79,13 @@ uint32_t next_pow2(uint32_t v) {
     return p;
 }
 uint32_t grid_buckets(uint32_t maxN) { return next_pow2(std::max<uint32_t>(2u * maxN, 32u)); }
+uint32_t round4(uint32_t v) { return (v + 3u) & ~3u; }
 
 }  // namespace
 
 struct bp_context {
+    int refs = 0;            // live worlds and batches that use this context
+    bool released = false;   // bp_context_destroy was called; freed when the last user goes
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t start = nullptr, stop = nullptr;
@@ -107,7 +116,11 @@ struct WorldSet {
     uint32_t* dCtaList = nullptr;
     uint32_t* dWarpList = nullptr;
     uint32_t* dQueue = nullptr;
+    uint32_t* dQueueSingle = nullptr;       // queue of the one-world launches of the per-world path
+    uint32_t* dCandidates = nullptr;        // worlds of the persistent kernel (all but the large ones)
+    uint32_t nCandidates = 0;
     uint32_t threads = kDefaultThreads;
+    bool staging = true;                    // keep worlds resident in shared memory during a step
     uint32_t warpMax = kDefaultWarpMax;
     uint32_t blocks = 0;
     QueueArgs queue{};
@@ -193,16 +206,35 @@ int validate(const bp_world_desc& d, const bp_world_input& in) {
     return BP_OK;
 }
 
-// Splits the non-large worlds into the CTA and warp queues (largest first) for a block width and warp-team threshold.
+// Initial split of the non-large worlds into the CTA and warp queues (largest first) for a block width and warp-team
+// threshold; after every batched step the on-device scheduler reorders both queues by predicted cost. Shared memory
+// is sized so any world can be a CTA world and any world up to the threshold a warp world.
 cudaError_t schedule(WorldSet& ws, uint32_t threads, uint32_t warpMax) {
     ws.threads = threads;
     ws.warpMax = warpMax;
     ws.ctaWorlds.clear();
     ws.warpWorlds.clear();
+    std::vector<uint32_t> candidates;
+    uint32_t maxN = 1, maxWarpN = 0, ctaWs = 0, warpWs = 0;
     for (uint32_t w = 0; w < ws.nWorlds; ++w) {
         const DWorld& W = ws.hWorlds[w];
         if (W.n > kCtaMaxBubbles || (W.flags & BP_WORLD_FORCE_MULTI_CTA)) continue;
+        candidates.push_back(w);
+        maxN = std::max(maxN, W.n);
+        if (W.n <= warpMax) maxWarpN = std::max(maxWarpN, W.n);
         (W.n <= warpMax ? ws.warpWorlds : ws.ctaWorlds).push_back(w);
+    }
+    // workspace caps that keep one block within the dynamic shared memory limit
+    const uint32_t ctaGridBytes = 4u * round4(grid_buckets(maxN) + maxN);
+    const uint32_t warpGridBytes = maxWarpN ? 4u * round4(grid_buckets(maxWarpN) + maxWarpN) : 0u;
+    const uint32_t ctaCap = std::min(kCtaWorkspaceCap, kMaxDynamicSmem - std::min(kMaxDynamicSmem, ctaGridBytes));
+    const uint32_t perWarp = kMaxDynamicSmem / std::max(threads / 32u, 1u);
+    const uint32_t warpCap = std::min(kWarpWorkspaceCap, perWarp > warpGridBytes + 16u ? perWarp - warpGridBytes - 16u : 0u);
+    for (uint32_t w : candidates) {
+        const DWorld& W = ws.hWorlds[w];
+        uint32_t bytes = workspace_bytes(W.n, W.s, W.nb);
+        if (bytes <= ctaCap) ctaWs = std::max(ctaWs, bytes);
+        if (W.n <= warpMax && bytes <= warpCap) warpWs = std::max(warpWs, bytes);
     }
     auto bySize = [&](uint32_t a, uint32_t b) { return ws.hWorlds[a].n > ws.hWorlds[b].n; };
     std::stable_sort(ws.ctaWorlds.begin(), ws.ctaWorlds.end(), bySize);
@@ -213,12 +245,21 @@ cudaError_t schedule(WorldSet& ws, uint32_t threads, uint32_t warpMax) {
     q.queue = ws.dQueue;
     q.nCta = (uint32_t)ws.ctaWorlds.size();
     q.nWarp = (uint32_t)ws.warpWorlds.size();
-    q.ctaMaxN = q.nCta ? std::max<uint32_t>(ws.hWorlds[ws.ctaWorlds[0]].n, 1u) : 0u;
-    q.warpMaxN = q.nWarp ? std::max<uint32_t>(ws.hWorlds[ws.warpWorlds[0]].n, 1u) : 0u;
-    q.ctaB = q.nCta ? grid_buckets(q.ctaMaxN) : 0u;
-    q.warpB = q.nWarp ? grid_buckets(q.warpMaxN) : 0u;
+    q.ctaMaxN = candidates.empty() ? 0u : maxN;
+    q.ctaB = candidates.empty() ? 0u : grid_buckets(maxN);
+    q.warpMaxN = maxWarpN;
+    q.warpB = maxWarpN ? grid_buckets(maxWarpN) : 0u;
+    q.countsOnDevice = 1u;
+    q.ctaWsWords = ws.staging ? (ctaWs + 3u) / 4u : 0u;
+    q.warpWsWords = ws.staging ? (warpWs + 3u) / 4u : 0u;
+    q.ctaWsWords = (q.ctaWsWords + 3u) & ~3u;
+    q.warpWsWords = (q.warpWsWords + 3u) & ~3u;
+    ws.nCandidates = (uint32_t)candidates.size();
+    uint32_t counts[2] = {q.nCta, q.nWarp};
     cudaError_t err = upload(ws.dCtaList, ws.ctaWorlds.data(), ws.ctaWorlds.size(), ws.ctx->stream);
     if (!err) err = upload(ws.dWarpList, ws.warpWorlds.data(), ws.warpWorlds.size(), ws.ctx->stream);
+    if (!err) err = upload(ws.dCandidates, candidates.data(), candidates.size(), ws.ctx->stream);
+    if (!err) err = upload(ws.dQueue + 2, counts, 2, ws.ctx->stream);
     if (!err) err = cudaStreamSynchronize(ws.ctx->stream);
     ws.blocks = persistent_blocks(q, threads);
     if (ws.graph) { cudaGraphExecDestroy(ws.graph); ws.graph = nullptr; }
@@ -443,7 +484,12 @@ int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc
     }
     ws.dCtaList = ws.alloc<uint32_t>(count, err);
     ws.dWarpList = ws.alloc<uint32_t>(count, err);
-    ws.dQueue = ws.alloc<uint32_t>(2, err);
+    ws.dQueue = ws.alloc<uint32_t>(4, err);
+    ws.dQueueSingle = ws.alloc<uint32_t>(4, err);
+    ws.dCandidates = ws.alloc<uint32_t>(count, err);
+    S.bpose = ws.alloc<float4>(nbo, err);
+    S.segBox = ws.alloc<RigidBox>(ns, err);
+    S.bodyBox = ws.alloc<RigidBox>(nbo, err);
     ws.dSingle = ws.alloc<uint32_t>(count, err);
     for (uint32_t w : ws.largeWorlds) ws.largeMaxN = std::max(ws.largeMaxN, ws.hWorlds[w].n);
     ws.largeB = next_pow2(std::max<uint32_t>(2u * ws.largeMaxN, 64u));
@@ -506,10 +552,14 @@ cudaError_t launch_step(WorldSet& ws, bool perWorld, uint32_t only = 0xffffffffu
         if (W.n > kCtaMaxBubbles || (W.flags & BP_WORLD_FORCE_MULTI_CTA))
             return launch_large(ws.S, w, ws.largeB, ws.largeBlocks, kLargeThreads, st);
         QueueArgs q{};
-        q.queue = ws.dQueue;
+        q.queue = ws.dQueueSingle;
+        q.countsOnDevice = 0u;
         uint32_t maxN = std::max<uint32_t>(W.n, 1u);
-        if (W.n <= ws.warpMax) { q.warpList = ws.dSingle + w; q.nWarp = 1; q.warpMaxN = maxN; q.warpB = grid_buckets(maxN); }
-        else { q.ctaList = ws.dSingle + w; q.nCta = 1; q.ctaMaxN = maxN; q.ctaB = grid_buckets(maxN); }
+        uint32_t bytes = workspace_bytes(W.n, W.s, W.nb);
+        bool warpTeam = W.n <= ws.warpMax;
+        uint32_t wsWords = ws.staging && bytes <= (warpTeam ? kWarpWorkspaceCap : kCtaWorkspaceCap) ? ((bytes + 15u) / 16u) * 4u : 0u;
+        if (warpTeam) { q.warpList = ws.dSingle + w; q.nWarp = 1; q.warpMaxN = maxN; q.warpB = grid_buckets(maxN); q.warpWsWords = wsWords; }
+        else { q.ctaList = ws.dSingle + w; q.nCta = 1; q.ctaMaxN = maxN; q.ctaB = grid_buckets(maxN); q.ctaWsWords = wsWords; }
         return launch_persistent(ws.S, q, W.n <= ws.warpMax ? 32u : ws.threads, 1u, st);
     };
     if (only < ws.nWorlds) return one(only);
@@ -631,6 +681,8 @@ int step_set(WorldSet& ws, uint32_t steps, bp_step_report* reports, bool perWorl
             uint64_t before = ws.launches;
             cudaError_t le = launch_step(ws, false);
             le = le ? le : launch_accumulate(ws.dReports, ws.dAcc, ws.dSizes, ws.dTotal, ws.nWorlds, st);
+            le = le ? le : launch_schedule(ws.S, ws.dCandidates, ws.nCandidates, ws.warpMax, kWarpSubsteps, ws.dCtaList,
+                                           ws.dWarpList, ws.dQueue, st);
             err = cudaStreamEndCapture(st, &g);
             ws.launches = before;
             if (!err) err = le;
@@ -649,6 +701,9 @@ int step_set(WorldSet& ws, uint32_t steps, bp_step_report* reports, bool perWorl
         } else {
             err = launch_step(ws, perWorld);
             if (!err) err = launch_accumulate(ws.dReports, ws.dAcc, ws.dSizes, ws.dTotal, ws.nWorlds, st);
+            if (!err && !perWorld)
+                err = launch_schedule(ws.S, ws.dCandidates, ws.nCandidates, ws.warpMax, kWarpSubsteps, ws.dCtaList,
+                                      ws.dWarpList, ws.dQueue, st);
         }
         if (perStepReports && reports && !err) {
             int rs = read_reports(ws, reports + (uint64_t)s * ws.nWorlds, ws.nWorlds);
@@ -771,14 +826,25 @@ int bp_context_create(int device, uint32_t flags, bp_context** out) {
     return BP_OK;
 }
 
-int bp_context_destroy(bp_context* c) {
-    if (!c) return BP_OK;
+static void context_free(bp_context* c) {
     DeviceGuard guard(c->device);
     cudaStreamSynchronize(c->stream);
     cudaEventDestroy(c->start);
     cudaEventDestroy(c->stop);
     cudaStreamDestroy(c->stream);
     delete c;
+}
+
+// The context lives until it is released and every world / batch created on it is destroyed, whatever the order of
+// the destroy calls.
+static void context_unref(bp_context* c) {
+    if (--c->refs == 0 && c->released) context_free(c);
+}
+
+int bp_context_destroy(bp_context* c) {
+    if (!c) return BP_OK;
+    c->released = true;
+    if (c->refs == 0) context_free(c);
     return BP_OK;
 }
 
@@ -786,17 +852,22 @@ int bp_world_create(bp_context* context, const bp_world_desc* desc, const bp_wor
     if (!context || !desc || !input || !out) return BP_E_INVALID;
     bp_world* w = new (std::nothrow) bp_world();
     if (!w) return BP_E_ALLOC;
+    context->refs++;
     int st = build_set(w->set, context, 1, desc, input, true);
-    if (st != BP_OK) { delete w; return st; }
+    if (st != BP_OK) { delete w; context_unref(context); return st; }
     *out = w;
     return BP_OK;
 }
 
 int bp_world_destroy(bp_world* world) {
     if (!world) return BP_OK;
-    DeviceGuard guard(world->set.ctx->device);
-    cudaStreamSynchronize(world->set.ctx->stream);
-    delete world;
+    bp_context* c = world->set.ctx;
+    {
+        DeviceGuard guard(c->device);
+        cudaStreamSynchronize(c->stream);
+        delete world;
+    }
+    context_unref(c);
     return BP_OK;
 }
 
@@ -990,16 +1061,17 @@ int bp_batch_create(bp_context* context, uint32_t world_count, const bp_world_de
     if (!context || !descs || !inputs || !out || world_count == 0) return BP_E_INVALID;
     bp_batch* b = new (std::nothrow) bp_batch();
     if (!b) return BP_E_ALLOC;
+    context->refs++;
     int st = build_set(b->set, context, world_count, descs, inputs, false);
-    if (st != BP_OK) { delete b; return st; }
+    if (st != BP_OK) { delete b; context_unref(context); return st; }
     if (config) {
         b->set.flags = config->flags;
         uint32_t t = config->threads_per_world ? config->threads_per_world : b->set.threads;
         uint32_t wm = config->warp_world_max == 0xffffffffu ? 0u : (config->warp_world_max ? config->warp_world_max : b->set.warpMax);
-        if (t % 32u || t > 512u || wm > kCtaMaxBubbles) { delete b; return BP_E_INVALID; }
+        if (t % 32u || t > 512u || wm > kCtaMaxBubbles) { delete b; context_unref(context); return BP_E_INVALID; }
         if (config->threads_per_world || config->warp_world_max) {
             b->set.fixedThreads = t;
-            if (schedule(b->set, t, wm) != cudaSuccess) { delete b; return BP_E_CUDA; }
+            if (schedule(b->set, t, wm) != cudaSuccess) { delete b; context_unref(context); return BP_E_CUDA; }
         }
     }
     *out = b;
@@ -1008,9 +1080,13 @@ int bp_batch_create(bp_context* context, uint32_t world_count, const bp_world_de
 
 int bp_batch_destroy(bp_batch* batch) {
     if (!batch) return BP_OK;
-    DeviceGuard guard(batch->set.ctx->device);
-    cudaStreamSynchronize(batch->set.ctx->stream);
-    delete batch;
+    bp_context* c = batch->set.ctx;
+    {
+        DeviceGuard guard(c->device);
+        cudaStreamSynchronize(c->stream);
+        delete batch;
+    }
+    context_unref(c);
     return BP_OK;
 }
 

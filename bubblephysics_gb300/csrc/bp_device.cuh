@@ -70,6 +70,13 @@ struct DField {
     uint32_t kind, voff, vcount, foff, fcount, hasFilter;
 };
 
+// Compact box of a rigid object for the broadphase tests: a segment's [min(a,b), max(a,b)] or a body's swept box
+// [min(pos, prev) - R, max(pos, prev) + R]; `flags` holds the segment flags / the body-is-obstacle bit.
+struct RigidBox {
+    float4 box;  // lo.xy, hi.xy
+    uint32_t cat, mask, flags, pad;
+};
+
 // End-of-step contact record, index form (ids are looked up on the host).
 struct DContact {
     uint32_t a, other, kind, feature;
@@ -125,18 +132,31 @@ struct DState {
     unsigned int* barrier;     // grid barrier counters [arrivals, generation]
     uint32_t* errorFlag;       // bounded-wait failures
     unsigned long long* phaseCycles;  // kPhaseCount per world when built with BP_PHASE_TIMING, else null
+    float4* bpose;             // per body: pose at the current step fraction (position.xy, cos, sin)
+    RigidBox* segBox;          // per segment
+    RigidBox* bodyBox;         // per body (rebuilt every step: kinematic bodies move)
 };
 
-constexpr uint32_t kPhaseCount = 12;
+constexpr uint32_t kPhaseCount = 24;
 
-// Work queues of one persistent step launch (see persistent_step_kernel).
+// Work queues of one persistent step launch (see persistent_step_kernel). The lists and their lengths live in device
+// memory so the on-device scheduler can reorder them between steps without a host round trip.
 struct QueueArgs {
-    const uint32_t* ctaList;   // worlds stepped by a whole block, largest first
-    const uint32_t* warpList;  // worlds stepped by one warp, largest first
-    uint32_t* queue;           // [0] next CTA world, [1] next warp world; zeroed before each launch
-    uint32_t nCta, ctaB, ctaMaxN;
+    const uint32_t* ctaList;   // worlds stepped by a whole block, most expensive first
+    const uint32_t* warpList;  // worlds stepped by one warp, most expensive first
+    uint32_t* queue;           // [0] next CTA world, [1] next warp world (zeroed before each launch),
+                               // [2] CTA list length, [3] warp list length
+    uint32_t nCta, ctaB, ctaMaxN;     // ctaMaxN / warpMaxN size the shared-memory grid of one team
     uint32_t nWarp, warpB, warpMaxN;
+    uint32_t countsOnDevice;          // 1: list lengths are queue[2], queue[3]; 0: nCta, nWarp
+    uint32_t ctaWsWords, warpWsWords; // shared-memory workspace of one team (32-bit words) after its grid
 };
+
+// Bytes of a world's shared-memory workspace: per bubble 88 B of hot state, per segment and body a 32 B box, per body
+// a 16 B pose; the 15 parts are each padded to 16 bytes.
+__host__ __device__ inline uint32_t workspace_bytes(uint32_t n, uint32_t s, uint32_t nb) {
+    return n * 88u + s * 32u + nb * 48u + 15u * 16u;
+}
 
 // ------------------------------------------------------------------------------------------------------------------
 // float2 helpers (Metal semantics restated: length = sqrt(x*x + y*y), min/max = fmin/fmax)
@@ -292,9 +312,8 @@ struct Obstacle {
     float speedBound;
 };
 // nativeBodyObstacle, NFK:170-210 (the point velocity is not used by the step)
-__device__ __forceinline__ Obstacle body_obstacle(const float2* verts, const uint32_t* tris, const DBody& b, float fraction,
+__device__ __forceinline__ Obstacle body_obstacle(const float2* verts, const uint32_t* tris, const DBody& b, const Pose& p,
                                                   float2 center) {
-    Pose p = body_at(b, fraction);
     Obstacle o;
     float2 point, normal;
     float distance;

@@ -26,9 +26,19 @@ constexpr uint32_t kLive = 0xffu;         // mask of the public flags
         }                                                                                             \
     } while (0)
 #define BP_PHASE_START long long phaseMark = clock64()
+#define BP_SUBPHASE(id)                                                                                     \
+    do {                                                                                                    \
+        if (team.leader() && S.phaseCycles) {                                                               \
+            long long now_ = clock64();                                                                     \
+            S.phaseCycles[(uint64_t)subWorld * kPhaseCount + (id)] += \
+                (unsigned long long)(now_ - subMark);                                                       \
+            subMark = now_;                                                                                 \
+        }                                                                                                   \
+    } while (0)
 #else
 #define BP_PHASE(id) do { } while (0)
 #define BP_PHASE_START do { } while (0)
+#define BP_SUBPHASE(id) do { } while (0)
 #endif
 
 struct Ctl {  // NativeSubstepControl (NFK:22-26), kept identical in every thread of the team
@@ -132,6 +142,23 @@ __device__ float2 non_contact_acc(const DState& S, const DWorld& W, uint32_t g, 
 }
 
 // ------------------------------------------------------------------------------------------------------------------
+// Body poses at the current step fraction, memoized once per body (nativeBodyAtFraction, NFK:155-159): every
+// (bubble, body) term then reads the same values body_at would compute.
+template <class Team> __device__ void refresh_poses(const DState& S, const DWorld& W, const Team& team, float fraction) {
+    for (uint32_t bi = team.rank(); bi < W.nb; bi += team.size()) {
+        Pose p = body_at(S.body[W.bodyOff + bi], fraction);
+        S.bpose[W.bodyOff + bi] = make_float4(p.pos.x, p.pos.y, p.c, p.s);
+    }
+}
+__device__ __forceinline__ Pose cached_pose(const DState& S, const DWorld& W, uint32_t bi) {
+    float4 v = S.bpose[W.bodyOff + bi];
+    Pose p;
+    p.pos = f2(v.x, v.y);
+    p.c = v.z;
+    p.s = v.w;
+    return p;
+}
+
 // Per-bubble substep terms (NFK:216-243, 510-614)
 // ------------------------------------------------------------------------------------------------------------------
 __device__ __forceinline__ const uint32_t* adj_row(const DState& S, const DWorld& W, uint32_t i) {
@@ -162,7 +189,7 @@ __device__ float2 contact_force(const DState& S, const DWorld& W, uint32_t i, fl
             if (!wall_region(S.seg[W.soff + j], p, normal, dist) || !(dist < ph.x)) continue;
             total = add(total, mul(normal, wall_law(ph.z, ph.x, dist).force));
         } else {
-            Obstacle o = body_obstacle(S.bverts, S.btris, S.body[W.bodyOff + j], fraction, p);
+            Obstacle o = body_obstacle(S.bverts, S.btris, S.body[W.bodyOff + j], cached_pose(S, W, j), p);
             total = add(total, mul(o.normal, wall_law(ph.z, ph.x, o.distance).force));
         }
     }
@@ -204,7 +231,7 @@ __device__ float2 contact_terms(const DState& S, const DWorld& W, uint32_t i, fl
             total = add(total, mul(normal, wl.force));
             w2 = w2 + wl.stiffness * im;
         } else {
-            Obstacle o = body_obstacle(S.bverts, S.btris, S.body[W.bodyOff + j], fraction, p);
+            Obstacle o = body_obstacle(S.bverts, S.btris, S.body[W.bodyOff + j], cached_pose(S, W, j), p);
             Law wl = wall_law(ph.z, ph.x, o.distance);
             total = add(total, mul(o.normal, wl.force));
             w2 = w2 + wl.stiffness * im;
@@ -242,7 +269,7 @@ __device__ float omega_squared(const DState& S, const DWorld& W, uint32_t i, flo
             if (!wall_region(S.seg[W.soff + j], p, normal, dist) || !(dist < ph.x)) continue;
             total = total + wall_law(ph.z, ph.x, dist).stiffness * im;
         } else {
-            Obstacle o = body_obstacle(S.bverts, S.btris, S.body[W.bodyOff + j], fraction, p);
+            Obstacle o = body_obstacle(S.bverts, S.btris, S.body[W.bodyOff + j], cached_pose(S, W, j), p);
             total = total + wall_law(ph.z, ph.x, o.distance).stiffness * im;
         }
     }
@@ -277,7 +304,7 @@ __device__ float distance_bound(const DState& S, const DWorld& W, uint32_t i, fl
             accSum = accSelf;
             reach = radius;
         } else {
-            Obstacle o = body_obstacle(S.bverts, S.btris, S.body[W.bodyOff + j], fraction, p);
+            Obstacle o = body_obstacle(S.bverts, S.btris, S.body[W.bodyOff + j], cached_pose(S, W, j), p);
             dist = o.distance;
             approach = -dot2(velocity, o.normal);
             bodySpeed = o.speedBound;
@@ -326,12 +353,12 @@ __device__ __forceinline__ bool pair_accepts(const DState& S, const DWorld& W, u
 // segment rule of nativeFinishBubbleRow (NGK:279-290)
 __device__ __forceinline__ bool segment_accepts(const DState& S, const DWorld& W, uint32_t i, uint32_t sj) {
     uint32_t g = W.boff + i;
-    const DSegment& sg = S.seg[W.soff + sj];
-    if (!filter_accepts(S.filter[g], make_uint2(sg.cat, sg.mask))) return false;
-    if ((sg.flags & BP_SEGMENT_HAS_OWNER) && W.njEnt && joint_excluded(S, W, i, sg.owner)) return false;
+    const RigidBox rb = S.segBox[W.soff + sj];
+    if (!filter_accepts(S.filter[g], make_uint2(rb.cat, rb.mask))) return false;
+    if ((rb.flags & BP_SEGMENT_HAS_OWNER) && W.njEnt && joint_excluded(S, W, i, S.seg[W.soff + sj].owner)) return false;
     float reach = S.phys[g].x + S.margin[g] + W.sepTol;
-    float2 lower = sub(vmin2(sg.a, sg.b), f2(reach, reach));
-    float2 upper = add(vmax2(sg.a, sg.b), f2(reach, reach));
+    float2 lower = sub(f2(rb.box.x, rb.box.y), f2(reach, reach));
+    float2 upper = add(f2(rb.box.z, rb.box.w), f2(reach, reach));
     float2 p = S.pos[g];
     return p.x >= lower.x && p.y >= lower.y && p.x <= upper.x && p.y <= upper.y;
 }
@@ -339,12 +366,12 @@ __device__ __forceinline__ bool segment_accepts(const DState& S, const DWorld& W
 __device__ __forceinline__ bool body_is_obstacle(const DBody& b) {
     return (b.flags & BP_BODY_STATIC) ? b.kind != BP_BODY_POLYGON : (b.flags & BP_BODY_KINEMATIC) != 0u;
 }
-__device__ __forceinline__ bool body_accepts(const DState& S, const DWorld& W, const DBody& b, uint32_t bi, uint32_t i) {
+__device__ __forceinline__ bool body_accepts(const DState& S, const DWorld& W, const RigidBox& rb, uint32_t bi, uint32_t i) {
     uint32_t g = W.boff + i;
-    if (!filter_accepts(S.filter[g], make_uint2(b.cat, b.mask))) return false;
+    if (!filter_accepts(S.filter[g], make_uint2(rb.cat, rb.mask))) return false;
     if (W.njEnt && joint_excluded(S, W, W.n + bi, S.id[g])) return false;
-    float2 bodyLow = sub(vmin2(b.pos, b.prev), f2(b.radius, b.radius));
-    float2 bodyHigh = add(vmax2(b.pos, b.prev), f2(b.radius, b.radius));
+    float2 bodyLow = f2(rb.box.x, rb.box.y);
+    float2 bodyHigh = f2(rb.box.z, rb.box.w);
     float reach = S.phys[g].x + fmaxf(S.margin[g], 0.0f);
     float2 c = S.pos[g];
     float2 lo = sub(c, f2(reach, reach)), hi = add(c, f2(reach, reach));
@@ -421,14 +448,14 @@ __device__ void emit_row(const DState& S, const DWorld& W, const uint32_t* bucke
 
 // Body row of body bi built by one warp: the first k accepting bubbles in index order (NGK:350-392).
 __device__ void emit_body_row(const DState& S, const DWorld& W, uint32_t bi, uint32_t lane, uint32_t& overflow, uint32_t& maxPer) {
-    const DBody b = S.body[W.bodyOff + bi];
+    const RigidBox rb = S.bodyBox[W.bodyOff + bi];
     const uint32_t k = W.k;
     uint32_t* row = S.bodyRow + W.bodyRowOff + (uint64_t)bi * k;
     uint32_t total = 0;
-    if (body_is_obstacle(b)) {
+    if (rb.flags) {
         for (uint32_t base = 0; base < W.n; base += 32) {
             uint32_t i = base + lane;
-            bool hit = i < W.n && !removed(S, W.boff + i) && body_accepts(S, W, b, bi, i);
+            bool hit = i < W.n && !removed(S, W.boff + i) && body_accepts(S, W, rb, bi, i);
             uint32_t mask = __ballot_sync(0xffffffffu, hit);
             uint32_t rank = __popc(mask & ((1u << lane) - 1u));
             if (hit && total + rank < k) row[total + rank] = i;
@@ -473,8 +500,8 @@ __device__ void build_adjacency(const DState& S, const DWorld& W, const uint32_t
     }
     // bodies holding i in their row
     for (uint32_t bi = 0; bi < W.nb; ++bi) {
-        const DBody& b = S.body[W.bodyOff + bi];
-        if (!body_is_obstacle(b) || !body_accepts(S, W, b, bi, i)) continue;
+        const RigidBox rb = S.bodyBox[W.bodyOff + bi];
+        if (!rb.flags || !body_accepts(S, W, rb, bi, i)) continue;
         uint32_t total = S.bodyTotal[W.bodyOff + bi];
         if (total > k && !row_contains(S.bodyRow + W.bodyRowOff + (uint64_t)bi * k, k, i)) continue;
         ++demanded;
@@ -490,8 +517,11 @@ __device__ void build_adjacency(const DState& S, const DWorld& W, const uint32_t
 // ------------------------------------------------------------------------------------------------------------------
 template <class Team>
 __device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, const Team& team, uint32_t* buckets,
-                            uint32_t* entries, uint32_t B, uint32_t& buildOverflow, uint32_t& maxPerAll) {
+                            uint32_t* entries, uint32_t B, uint32_t& buildOverflow, uint32_t& maxPerAll, uint32_t subWorld) {
     const uint32_t n = W.n, T = team.size(), r = team.rank();
+#ifdef BP_PHASE_TIMING
+    long long subMark = clock64();
+#endif
     // a0, margin and x0 (nativeBubbleAcceleration + nativeBubbleMargin, NFK:472-499)
     const float t = fmaxf(c.timeX - c.timeY, 0.0f);
     float cwl = W.sepTol;
@@ -508,10 +538,12 @@ __device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, cons
         S.ref[g] = p;
         cwl = fmaxf(cwl, 2.0f * (radius + m) + W.sepTol);  // nativePrepareGrid, NGK:163-177
     }
+    BP_SUBPHASE(12);
     float cw = team.fmax(cwl);
     cw = fmaxf(cw, kFltMin);
     for (uint32_t b = r; b < B; b += T) buckets[b] = 0u;
     team.sync();
+    BP_SUBPHASE(13);
     // cells (nativeBuildGrid, NGK:179-189) and bucket counts
     for (uint32_t i = r; i < n; i += T) {
         uint32_t g = W.boff + i;
@@ -538,16 +570,23 @@ __device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, cons
         entries[slot] = i;
     }
     team.sync();
+    BP_SUBPHASE(14);
     uint32_t overflow = 0, maxPer = 0;
     for (uint32_t i = r; i < n; i += T) emit_row(S, W, buckets, entries, B, i, overflow, maxPer);
+    team.sync();
+    BP_SUBPHASE(15);
     {
         const uint32_t lane = threadIdx.x & 31u, warp = r >> 5, warps = T >> 5;
         for (uint32_t bi = warp; bi < W.nb; bi += warps) emit_body_row(S, W, bi, lane, overflow, maxPer);
     }
     team.sync();
+    BP_SUBPHASE(16);
     for (uint32_t i = r; i < n; i += T) build_adjacency(S, W, buckets, entries, B, i, overflow, maxPer);
+    team.sync();
+    BP_SUBPHASE(17);
     buildOverflow = team.sum(overflow);
     maxPerAll = max(maxPerAll, team.umax(maxPer));
+    BP_SUBPHASE(18);
     return cw;
 }
 
@@ -556,6 +595,10 @@ __device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, cons
 template <class Team>
 __device__ void initial_forces(const DState& S, const DWorld& W, const Ctl& c, const Team& team, ValOwner& w2, ValOwner& mg) {
     const float fraction = c.timeX > 0.0f ? clampf(c.timeY / c.timeX, 0.0f, 1.0f) : 1.0f;
+    if (W.nb) {
+        refresh_poses(S, W, team, fraction);
+        team.sync();
+    }
     w2 = ValOwner{-1.0f, 0u};
     mg = ValOwner{__int_as_float(0x7f800000), 0u};
     for (uint32_t i = team.rank(); i < W.n; i += team.size()) {
@@ -735,13 +778,13 @@ __device__ bool assert_bubble(const DState& S, const DWorld& W, const uint32_t* 
     const float2 pathLo = vmin2(start, center), pathHi = vmax2(start, center);
     const float slack = 1e-3f + 1e-5f * fmaxf(fmaxf(fabsf(pathLo.x), fabsf(pathLo.y)), fmaxf(fabsf(pathHi.x), fabsf(pathHi.y)));
     for (uint32_t e = 0; e < W.s; ++e) {
-        const DSegment& sg = S.seg[W.soff + e];
-        if (!(sg.flags & BP_SEGMENT_POLYGON_EDGE)) continue;
-        float2 segLo = vmin2(sg.a, sg.b), segHi = vmax2(sg.a, sg.b);
-        if (segLo.x > pathHi.x + slack || segLo.y > pathHi.y + slack || segHi.x < pathLo.x - slack ||
-            segHi.y < pathLo.y - slack)
+        const RigidBox rb = S.segBox[W.soff + e];
+        if (!(rb.flags & BP_SEGMENT_POLYGON_EDGE)) continue;
+        if (rb.box.x > pathHi.x + slack || rb.box.y > pathHi.y + slack || rb.box.z < pathLo.x - slack ||
+            rb.box.w < pathLo.y - slack)
             continue;
-        if (!filter_accepts(fi, make_uint2(sg.cat, sg.mask))) continue;
+        if (!filter_accepts(fi, make_uint2(rb.cat, rb.mask))) continue;
+        const DSegment& sg = S.seg[W.soff + e];
         float2 edge = sub(sg.b, sg.a);
         float lsq = dot2(edge, edge);
         if (!(lsq > 0.0f)) continue;
@@ -926,17 +969,99 @@ __device__ bool contact_record(const DState& S, const DWorld& W, uint32_t i, uin
 }
 
 // ------------------------------------------------------------------------------------------------------------------
+// Shared-memory residency: a team that owns a small enough world keeps the world's hot state in its shared-memory
+// workspace for the whole step (staged in here, written back when the step publishes). S is redirected so the same
+// per-bubble code indexes shared memory; worlds that do not fit run the identical code on global memory.
+// ------------------------------------------------------------------------------------------------------------------
+template <class T> __device__ __forceinline__ T* carve(char*& p, uint32_t count) {
+    T* out = (T*)p;
+    p += ((size_t)count * sizeof(T) + 15u) & ~(size_t)15u;
+    return out;
+}
+
+template <class Team>
+__device__ bool stage_world(const DState& G, DState& S, const DWorld& W, const Team& team, uint32_t* ws, uint32_t wsWords) {
+    if (ws == nullptr || workspace_bytes(W.n, W.s, W.nb) > wsWords * 4u) return false;
+    const uint32_t n = W.n, T = team.size(), r = team.rank();
+    char* p = (char*)ws;
+    float4* phys = carve<float4>(p, n);
+    float2* pos = carve<float2>(p, n);
+    float2* vel = carve<float2>(p, n);
+    float2* acc = carve<float2>(p, n);
+    float2* ref = carve<float2>(p, n);
+    float2* a0 = carve<float2>(p, n);
+    uint2* filter = carve<uint2>(p, n);
+    uint2* candCount = carve<uint2>(p, n);
+    float* margin = carve<float>(p, n);
+    uint32_t* flags = carve<uint32_t>(p, n);
+    uint32_t* deg = carve<uint32_t>(p, n);
+    uint32_t* pairTotal = carve<uint32_t>(p, n);
+    RigidBox* segBox = carve<RigidBox>(p, W.s);
+    RigidBox* bodyBox = carve<RigidBox>(p, W.nb);
+    float4* bpose = carve<float4>(p, W.nb);
+    for (uint32_t i = r; i < n; i += T) {
+        uint32_t g = W.boff + i;
+        phys[i] = G.phys[g];
+        pos[i] = G.pos[g];
+        vel[i] = G.vel[g];
+        filter[i] = G.filter[g];
+        flags[i] = G.flags[g];
+    }
+    S.phys = phys - W.boff;
+    S.pos = pos - W.boff;
+    S.vel = vel - W.boff;
+    S.acc = acc - W.boff;
+    S.ref = ref - W.boff;
+    S.a0 = a0 - W.boff;
+    S.filter = filter - W.boff;
+    S.candCount = candCount - W.boff;
+    S.margin = margin - W.boff;
+    S.flags = flags - W.boff;
+    S.deg = deg - W.boff;
+    S.pairTotal = pairTotal - W.boff;
+    S.segBox = segBox - W.soff;
+    S.bodyBox = bodyBox - W.bodyOff;
+    S.bpose = bpose - W.bodyOff;
+    team.sync();
+    return true;
+}
+
+// Boxes of the world's segments and (after the kinematic advance) bodies for this step.
+template <class Team> __device__ void build_boxes(const DState& S, const DWorld& W, const Team& team) {
+    for (uint32_t j = team.rank(); j < W.s; j += team.size()) {
+        const DSegment& sg = S.seg[W.soff + j];
+        float2 lo = vmin2(sg.a, sg.b), hi = vmax2(sg.a, sg.b);
+        RigidBox rb;
+        rb.box = make_float4(lo.x, lo.y, hi.x, hi.y);
+        rb.cat = sg.cat; rb.mask = sg.mask; rb.flags = sg.flags; rb.pad = 0u;
+        S.segBox[W.soff + j] = rb;
+    }
+    for (uint32_t bi = team.rank(); bi < W.nb; bi += team.size()) {
+        const DBody& b = S.body[W.bodyOff + bi];
+        float2 lo = sub(vmin2(b.pos, b.prev), f2(b.radius, b.radius));
+        float2 hi = add(vmax2(b.pos, b.prev), f2(b.radius, b.radius));
+        RigidBox rb;
+        rb.box = make_float4(lo.x, lo.y, hi.x, hi.y);
+        rb.cat = b.cat; rb.mask = b.mask; rb.flags = body_is_obstacle(b) ? 1u : 0u; rb.pad = 0u;
+        S.bodyBox[W.bodyOff + bi] = rb;
+    }
+}
+
+// ------------------------------------------------------------------------------------------------------------------
 // One complete step of one world (nativeBeginStep -> substep loop -> end of step)
 // ------------------------------------------------------------------------------------------------------------------
 template <class Team>
-__device__ void world_step(const DState& S, uint32_t wi, const Team& team, uint32_t* buckets, uint32_t* entries, uint32_t B) {
-    const DWorld W = S.worlds[wi];
+__device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint32_t* buckets, uint32_t* entries, uint32_t B,
+                           uint32_t* ws, uint32_t wsWords) {
+    const DWorld W = G.worlds[wi];
     const uint32_t n = W.n, T = team.size(), r = team.rank();
-    bp_step_report* rep = S.reports + wi;
-    if (S.failed[wi]) {
+    bp_step_report* rep = G.reports + wi;
+    if (G.failed[wi]) {
         if (team.leader()) { rep->status = BP_E_WORLD_FAILED; rep->substep_count = 0u; }
         return;
     }
+    DState S = G;
+    stage_world(G, S, W, team, ws, wsWords);
     BP_PHASE_START;
     // nativeBeginStep (NFK:285-293)
     uint32_t liveLocal = 0;
@@ -969,6 +1094,8 @@ __device__ void world_step(const DState& S, uint32_t wi, const Team& team, uint3
         }
         S.body[W.bodyOff + bi] = b;
     }
+    team.sync();
+    build_boxes(S, W, team);
     const uint32_t live = team.sum(liveLocal);
     Ctl c;
     c.timeX = W.dt;
@@ -981,7 +1108,7 @@ __device__ void world_step(const DState& S, uint32_t wi, const Team& team, uint3
     float* history = S.history + (uint64_t)wi * kFrameLimit;
     uint32_t buildOverflow = 0, overflowMax = 0, maxPer = 0, rebuilds = 0;
     BP_PHASE(0);
-    float cw = broadphase(S, W, c, team, buckets, entries, B, buildOverflow, maxPer);
+    float cw = broadphase(S, W, c, team, buckets, entries, B, buildOverflow, maxPer, wi);
     BP_PHASE(1);
     ValOwner w2, mg;
     initial_forces(S, W, c, team, w2, mg);
@@ -999,7 +1126,7 @@ __device__ void world_step(const DState& S, uint32_t wi, const Team& team, uint3
             c.cZ = 0u;
             overflowMax = max(overflowMax, buildOverflow);
             ++rebuilds;
-            cw = broadphase(S, W, c, team, buckets, entries, B, buildOverflow, maxPer);
+            cw = broadphase(S, W, c, team, buckets, entries, B, buildOverflow, maxPer, wi);
             initial_forces(S, W, c, team, w2, mg);
             BP_PHASE(1);
             continue;
@@ -1007,6 +1134,7 @@ __device__ void world_step(const DState& S, uint32_t wi, const Team& team, uint3
         const float fraction = c.timeX > 0.0f ? clampf(c.timeY / c.timeX, 0.0f, 1.0f) : 1.0f;
         for (uint32_t i = r; i < n; i += T)
             if (!removed(S, W.boff + i)) kick_drift(S, W, i, h);
+        refresh_poses(S, W, team, fraction);
         team.sync();
         w2 = ValOwner{-1.0f, 0u};
         mg = ValOwner{__int_as_float(0x7f800000), 0u};
@@ -1123,33 +1251,44 @@ __device__ void world_step(const DState& S, uint32_t wi, const Team& team, uint3
         }
         S.contactCount[wi] = min(pairsAll + segsAll, W.contactCap);
     }
-    // publish on success, restore the published state on failure (CompleteStep.swift:5-7)
+    // publish on success, restore the published state on failure (CompleteStep.swift:5-7); staged state goes back
+    // to global memory here
     if (status == BP_OK) {
         for (uint32_t i = r; i < n; i += T) {
             uint32_t g = W.boff + i;
             uint32_t f = S.flags[g] & ~kValid;
-            if (S.result[g] == 1u) f |= kRemoved;
-            S.flags[g] = f;
-            S.pFlags[g] = f;
-            S.pPos[g] = S.pos[g];
-            S.pStart[g] = S.start[g];
-            S.pVel[g] = S.vel[g];
-            S.pRotw[g] = S.rotw[g];
-            S.pResult[g] = S.result[g];
+            if (G.result[g] == 1u) f |= kRemoved;
+            float2 p = S.pos[g], v = S.vel[g];
+            G.flags[g] = f;
+            G.pFlags[g] = f;
+            G.pos[g] = p;
+            G.pPos[g] = p;
+            G.vel[g] = v;
+            G.pVel[g] = v;
+            G.acc[g] = S.acc[g];
+            G.pStart[g] = G.start[g];
+            G.pRotw[g] = G.rotw[g];
+            G.pResult[g] = G.result[g];
+            G.candCount[g] = S.candCount[g];
+            G.pairTotal[g] = S.pairTotal[g];
+            G.deg[g] = S.deg[g];
         }
-        for (uint32_t bi = r; bi < W.nb; bi += T) S.pBody[W.bodyOff + bi] = S.body[W.bodyOff + bi];
+        for (uint32_t bi = r; bi < W.nb; bi += T) G.pBody[W.bodyOff + bi] = G.body[W.bodyOff + bi];
     } else {
         for (uint32_t i = r; i < n; i += T) {
             uint32_t g = W.boff + i;
-            S.flags[g] = S.pFlags[g];
-            S.pos[g] = S.pPos[g];
-            S.start[g] = S.pStart[g];
-            S.vel[g] = S.pVel[g];
-            S.rotw[g] = S.pRotw[g];
-            S.result[g] = S.pResult[g];
+            G.flags[g] = G.pFlags[g];
+            G.pos[g] = G.pPos[g];
+            G.start[g] = G.pStart[g];
+            G.vel[g] = G.pVel[g];
+            G.rotw[g] = G.pRotw[g];
+            G.result[g] = G.pResult[g];
+            G.candCount[g] = S.candCount[g];
+            G.pairTotal[g] = S.pairTotal[g];
+            G.deg[g] = S.deg[g];
         }
-        for (uint32_t bi = r; bi < W.nb; bi += T) S.body[W.bodyOff + bi] = S.pBody[W.bodyOff + bi];
-        if (team.leader()) S.failed[wi] = 1u;
+        for (uint32_t bi = r; bi < W.nb; bi += T) G.body[W.bodyOff + bi] = G.pBody[W.bodyOff + bi];
+        if (team.leader()) G.failed[wi] = 1u;
     }
     BP_PHASE(10);
 }
@@ -1157,7 +1296,9 @@ __device__ void world_step(const DState& S, uint32_t wi, const Team& team, uint3
 // ------------------------------------------------------------------------------------------------------------------
 // Kernels
 // ------------------------------------------------------------------------------------------------------------------
-extern __shared__ uint32_t g_dynamic_smem[];
+extern __shared__ __align__(16) uint32_t g_dynamic_smem[];
+
+__host__ __device__ inline uint32_t round4(uint32_t v) { return (v + 3u) & ~3u; }
 
 // Persistent step kernel: blocks pull worlds from two queues. CTA-team worlds (largest first) are stepped by a whole
 // block; then every warp pulls warp-team worlds (small worlds, one warp each). Dynamic shared memory holds the hash
@@ -1167,24 +1308,29 @@ __global__ void __launch_bounds__(kThreads, 2) persistent_step_kernel(DState S, 
     __shared__ BlockScratch sh;
     __shared__ uint32_t next;
     CtaTeam cta{&sh};
+    const uint32_t nCta = q.countsOnDevice ? *(volatile uint32_t*)(q.queue + 2) : q.nCta;
+    const uint32_t nWarp = q.countsOnDevice ? *(volatile uint32_t*)(q.queue + 3) : q.nWarp;
     for (;;) {
         if (threadIdx.x == 0) next = atomicAdd(q.queue, 1u);
         __syncthreads();
         const uint32_t slot = next;
         __syncthreads();
-        if (slot >= q.nCta) break;
-        world_step(S, q.ctaList[slot], cta, g_dynamic_smem, g_dynamic_smem + q.ctaB, q.ctaB);
+        if (slot >= nCta) break;
+        world_step(S, q.ctaList[slot], cta, g_dynamic_smem, g_dynamic_smem + q.ctaB, q.ctaB,
+                   q.ctaWsWords ? g_dynamic_smem + round4(q.ctaB + q.ctaMaxN) : nullptr, q.ctaWsWords);
         __syncthreads();
     }
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    uint32_t* mine = g_dynamic_smem + warp * (q.warpB + q.warpMaxN);
+    const uint32_t slice = round4(q.warpB + q.warpMaxN) + q.warpWsWords;
+    uint32_t* mine = g_dynamic_smem + warp * slice;
     WarpTeam wt;
     for (;;) {
         uint32_t slot = 0;
         if (lane == 0) slot = atomicAdd(q.queue + 1, 1u);
         slot = __shfl_sync(0xffffffffu, slot, 0);
-        if (slot >= q.nWarp) break;
-        world_step(S, q.warpList[slot], wt, mine, mine + q.warpB, q.warpB);
+        if (slot >= nWarp) break;
+        world_step(S, q.warpList[slot], wt, mine, mine + q.warpB, q.warpB,
+                   q.warpWsWords ? mine + round4(q.warpB + q.warpMaxN) : nullptr, q.warpWsWords);
         __syncwarp();
     }
 }
@@ -1193,7 +1339,7 @@ __global__ void __launch_bounds__(kThreads, 2) persistent_step_kernel(DState S, 
 __global__ void __launch_bounds__(512) large_step_kernel(DState S, uint32_t wi, uint32_t B) {
     __shared__ BlockScratch sh;
     GridTeam team{&sh, S.barrier, S.errorFlag, S.gpv, S.gpo, nullptr, 0u, false};
-    world_step(S, wi, team, S.gbuckets, S.gentries, B);
+    world_step(S, wi, team, S.gbuckets, S.gentries, B, nullptr, 0u);
 }
 
 // Contact law known-answer kernel: mode 0 eps(q), 1 wall law, 2 pair law; 8 floats in / out per case.
@@ -1211,15 +1357,87 @@ __global__ void contact_law_kernel(uint32_t mode, const float* in, float* out, u
 // ------------------------------------------------------------------------------------------------------------------
 // Host launchers
 // ------------------------------------------------------------------------------------------------------------------
+// On-device scheduler, run after every batched step: predicted cost of a world = bubbles x (last step's substeps + 2)
+// (the +2 stands for the grid build and the end-of-step work); worlds are sorted by cost, most expensive first, and
+// split into the warp queue (at most warpMax bubbles and at most warpSubsteps substeps last step) and the CTA queue.
+// One block; keys (inverted cost << 32 | world) are sorted bitonically in shared memory.
+__global__ void __launch_bounds__(1024) schedule_kernel(const DWorld* worlds, const bp_step_report* reports,
+                                                        const uint32_t* failed, const uint32_t* candidates, uint32_t count,
+                                                        uint32_t warpMax, uint32_t warpSubsteps, uint32_t* ctaList,
+                                                        uint32_t* warpList, uint32_t* queue) {
+    extern __shared__ unsigned long long keys[];
+    __shared__ BlockScratch sh;
+    uint32_t P = 1;
+    while (P < count) P <<= 1;
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+        unsigned long long key = ~0ull;
+        if (i < count) {
+            uint32_t w = candidates[i];
+            uint32_t n = worlds[w].n;
+            uint32_t sub = failed[w] ? 0u : reports[w].substep_count;
+            unsigned long long cost = failed[w] ? 0ull : (unsigned long long)n * (sub + 2u);
+            uint32_t c32 = cost > 0xffffffffull ? 0xffffffffu : (uint32_t)cost;
+            key = ((unsigned long long)(0xffffffffu - c32) << 32) | w;
+        }
+        keys[i] = key;
+    }
+    __syncthreads();
+    for (uint32_t size = 2; size <= P; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+                uint32_t j = i ^ stride;
+                if (j > i) {
+                    bool up = (i & size) == 0;
+                    unsigned long long a = keys[i], b = keys[j];
+                    if ((a > b) == up) { keys[i] = b; keys[j] = a; }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // stable split into the two queues, in cost order
+    uint32_t nCta = 0, nWarp = 0;
+    for (uint32_t base = 0; base < count; base += blockDim.x) {
+        uint32_t i = base + threadIdx.x;
+        uint32_t w = 0, isWarp = 0, valid = i < count ? 1u : 0u;
+        if (valid) {
+            w = (uint32_t)(keys[i] & 0xffffffffull);
+            uint32_t sub = reports[w].substep_count;
+            isWarp = (worlds[w].n <= warpMax && sub <= warpSubsteps) ? 1u : 0u;
+        }
+        uint32_t tw, tc;
+        uint32_t pw = block_excl_scan(valid & isWarp, &tw, sh);
+        uint32_t pc = block_excl_scan(valid & (isWarp ^ 1u), &tc, sh);
+        if (valid) {
+            if (isWarp) warpList[nWarp + pw] = w;
+            else ctaList[nCta + pc] = w;
+        }
+        nWarp += tw;
+        nCta += tc;
+    }
+    if (threadIdx.x == 0) { queue[2] = nCta; queue[3] = nWarp; }
+}
+
+cudaError_t launch_schedule(const DState& S, const uint32_t* candidates, uint32_t count, uint32_t warpMax,
+                            uint32_t warpSubsteps, uint32_t* ctaList, uint32_t* warpList, uint32_t* queue, cudaStream_t stream) {
+    if (count == 0u || count > 16384u) return cudaSuccess;
+    uint32_t P = 1;
+    while (P < count) P <<= 1;
+    schedule_kernel<<<1, 1024, (size_t)P * sizeof(unsigned long long), stream>>>(
+        S.worlds, S.reports, S.failed, candidates, count, warpMax, warpSubsteps, ctaList, warpList, queue);
+    return cudaGetLastError();
+}
+
 size_t persistent_smem(const QueueArgs& q, uint32_t threads) {
-    size_t cta = (size_t)(q.nCta ? q.ctaB + q.ctaMaxN : 0);
-    size_t warp = (size_t)(q.nWarp ? (threads / 32u) * (q.warpB + q.warpMaxN) : 0);
+    size_t cta = (size_t)(q.nCta ? round4(q.ctaB + q.ctaMaxN) + q.ctaWsWords : 0);
+    size_t warp = (size_t)(q.nWarp ? (threads / 32u) * (round4(q.warpB + q.warpMaxN) + q.warpWsWords) : 0);
     return (cta > warp ? cta : warp) * sizeof(uint32_t);
 }
 
 cudaError_t launch_persistent(const DState& S, const QueueArgs& q, uint32_t threads, uint32_t blocks, cudaStream_t stream) {
     if (q.nCta + q.nWarp == 0u) return cudaSuccess;
     size_t smem = persistent_smem(q, threads);
+    if (smem > 200u * 1024u) return cudaErrorInvalidValue;  // schedule() keeps every configuration below this
     cudaError_t err = cudaMemsetAsync(q.queue, 0, 2 * sizeof(uint32_t), stream);
     if (err) return err;
     if (threads <= 128u) persistent_step_kernel<128><<<blocks, threads, smem, stream>>>(S, q);
@@ -1245,9 +1463,10 @@ void prepare_kernels() {
     static bool done = false;
     if (done) return;
     done = true;
-    cudaFuncSetAttribute(persistent_step_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-    cudaFuncSetAttribute(persistent_step_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-    cudaFuncSetAttribute(persistent_step_kernel<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(persistent_step_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(persistent_step_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(persistent_step_kernel<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(schedule_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 16384 * 8);
 }
 
 int large_max_blocks(int threads) {

@@ -182,10 +182,11 @@ def large_world(seed: int = 2, n: int = 65536, side: float = 8192.0) -> WorldSpe
 
 
 def _regular_polygon(rng, sides, half):
-    angles = np.sort(rng.uniform(0, 2 * math.pi, sides))
-    angles = np.linspace(0, 2 * math.pi, sides, endpoint=False) + rng.uniform(0, 2 * math.pi / sides)
-    radius = half * rng.uniform(0.7, 1.0, sides)
-    return np.stack([np.cos(angles) * radius, np.sin(angles) * radius], axis=1)
+    """Convex polygon: vertices on a circle of radius `half` (a cyclic polygon is convex), angles jittered by at most
+    a quarter of the even spacing so no edge degenerates."""
+    step = 2 * math.pi / sides
+    angles = np.arange(sides) * step + rng.uniform(-0.25, 0.25, sides) * step + rng.uniform(0, 2 * math.pi)
+    return np.stack([np.cos(angles) * half, np.sin(angles) * half], axis=1)
 
 
 def _body_geometry(kind, rng, half):
@@ -212,20 +213,37 @@ def _body_geometry(kind, rng, half):
     return local, tris, bound, 0.0, 0.0
 
 
-def add_bodies(rng, count, region, size_range, first_id, kinematic_fraction=0.25, speed=20.0):
+def add_bodies(rng, count, region, size_range, first_id, kinematic_fraction=0.25, speed=5.0, spin=0.2,
+               horizon=5.0, clearance=80.0, gap=50.0):
     """Random static / kinematic bodies (1/3 polygons, 1/3 circles, 1/3 capsules). Static polygons become one-sided
-    edges (like NativePublicWorld.step); static circles / capsules and every kinematic body are obstacle bodies."""
+    edges (like NativePublicWorld.step); static circles / capsules and every kinematic body are obstacle bodies.
+    Every body keeps `gap` (more than a bubble diameter) from other bodies and from the region edge, so no bubble is
+    trapped in a narrow gap; a kinematic body keeps `clearance` plus its travel over `horizon` seconds, so it never
+    closes a gap onto a bubble (a squeeze a world cannot survive). A body without such room is left out."""
     x0, y0, x1, y1 = region
     bodies, verts, tris, segs = [], [], [], []
+    placed = []  # (position, bounding radius, keep-out radius)
+    polygons = []  # world vertices of the static polygons
     vcount = tcount = 0
     seg_id = first_id * 16
     for k in range(count):
         kind = [N.BODY_POLYGON, N.BODY_CIRCLE, N.BODY_CAPSULE][k % 3]
         half = float(rng.uniform(*size_range))
         local, tri, bound, core, hl = _body_geometry(kind, rng, half)
-        pos = np.array([rng.uniform(x0 + bound, x1 - bound), rng.uniform(y0 + bound, y1 - bound)])
-        angle = float(rng.uniform(0, 2 * math.pi))
         kinematic = rng.uniform() < kinematic_fraction
+        keep = bound + gap + (clearance + speed * math.sqrt(2.0) * horizon if kinematic else 0.0)
+        pos = None
+        for _ in range(40):
+            if x1 - x0 <= 2 * keep or y1 - y0 <= 2 * keep:
+                break
+            cand = np.array([rng.uniform(x0 + keep, x1 - keep), rng.uniform(y0 + keep, y1 - keep)])
+            if all(np.hypot(*(cand - p)) >= max(keep + rb, kb + bound) for p, rb, kb in placed):
+                pos = cand
+                break
+        if pos is None:
+            continue
+        placed.append((pos, bound, keep))
+        angle = float(rng.uniform(0, 2 * math.pi))
         bid = first_id + k
         if kind == N.BODY_POLYGON and not kinematic:
             c, s = math.cos(angle), math.sin(angle)
@@ -233,6 +251,7 @@ def add_bodies(rng, count, region, size_range, first_id, kinematic_fraction=0.25
             e = polygon_edges(world.astype(np.float32), seg_id, bid)
             seg_id += len(e)
             segs.append(e)
+            polygons.append(world)
             bodies.append(None)
             continue
         rec = np.zeros(1, N.BODY_DTYPE)[0]
@@ -246,7 +265,7 @@ def add_bodies(rng, count, region, size_range, first_id, kinematic_fraction=0.25
         rec["flags"] = N.BODY_KINEMATIC if kinematic else N.BODY_STATIC
         if kinematic:
             rec["velocity"] = rng.uniform(-speed, speed, 2)
-            rec["angular_velocity"] = float(rng.uniform(-0.5, 0.5))
+            rec["angular_velocity"] = float(rng.uniform(-spin, spin))
         rec["vertex_offset"] = vcount
         rec["vertex_count"] = local.shape[0]
         rec["triangle_offset"] = tcount
@@ -263,22 +282,26 @@ def add_bodies(rng, count, region, size_range, first_id, kinematic_fraction=0.25
     vert_arr = np.concatenate(verts).astype(np.float32) if verts else np.zeros((0, 2), np.float32)
     tri_arr = np.concatenate(tris).astype(np.uint32) if tris else np.zeros((0, 3), np.uint32)
     seg_arr = np.concatenate(segs) if segs else np.zeros(0, N.SEGMENT_DTYPE)
-    return body_arr, vert_arr, tri_arr, seg_arr
+    return body_arr, vert_arr, tri_arr, seg_arr, polygons
 
 
-def _clear_of_bodies(centers, radii, bodies, segs):
+def _clear_of_bodies(centers, radii, bodies, polygons):
+    """Bubbles that start clear of every obstacle body and static polygon (more than r + 1 away)."""
     keep = np.ones(centers.shape[0], bool)
     for b in bodies:
         d = np.hypot(centers[:, 0] - b["position"][0], centers[:, 1] - b["position"][1])
         keep &= d > b["bounding_radius"] + radii + 1.0
-    if segs.size:
-        # static polygon edges: drop bubbles near any edge's bounding box
-        lo = np.minimum(segs["a"], segs["b"])
-        hi = np.maximum(segs["a"], segs["b"])
-        for q in range(segs.shape[0]):
-            inside = (centers[:, 0] > lo[q, 0] - radii - 1) & (centers[:, 0] < hi[q, 0] + radii + 1) & \
-                     (centers[:, 1] > lo[q, 1] - radii - 1) & (centers[:, 1] < hi[q, 1] + radii + 1)
-            keep &= ~inside
+    for poly in polygons:
+        # convex polygon: the largest signed distance to its edge lines bounds the distance to it from below
+        p = np.asarray(poly, np.float64)
+        q = np.roll(p, -1, axis=0)
+        e = q - p
+        area = np.sum(p[:, 0] * q[:, 1] - q[:, 0] * p[:, 1])
+        normal = np.stack([e[:, 1], -e[:, 0]], 1) * (1.0 if area > 0 else -1.0)
+        normal /= np.linalg.norm(normal, axis=1, keepdims=True)
+        rel = centers[:, None, :] - p[None, :, :]
+        signed = (rel * normal[None, :, :]).sum(-1).max(axis=1)
+        keep &= signed > radii + 1.0
     return keep
 
 
@@ -290,12 +313,12 @@ def batched_world(rng, n_target: int, *, world_index: int = 0, max_bodies: int =
     side = math.sqrt(area)
     region = (0.0, 0.0, side, side)
     nb = int(rng.integers(0, max_bodies + 1))
-    bodies, bverts, btris, bsegs = add_bodies(rng, nb, region, (8.0, 40.0), first_id=10_000 + 64 * world_index)
+    bodies, bverts, btris, bsegs, polygons = add_bodies(rng, nb, region, (8.0, 40.0), first_id=10_000 + 64 * world_index)
     cols = int(math.ceil(math.sqrt(n_target)))
     spacing = side / cols
     ij = np.stack(np.divmod(np.arange(n_target), cols), axis=1)[:, ::-1].astype(np.float64)
     centers = (ij + 0.5) * spacing + rng.uniform(-0.2, 0.2, (n_target, 2)) * spacing
-    keep = _clear_of_bodies(centers, radii, bodies, bsegs)
+    keep = _clear_of_bodies(centers, radii, bodies, polygons)
     centers, radii = centers[keep], radii[keep]
     n = centers.shape[0]
     vel = rng.normal(0.0, 30.0, (n, 2))

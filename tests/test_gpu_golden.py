@@ -126,3 +126,15 @@ def test_host_state_round_trip(ctx):
     assert np.array_equal(b.read_state(), state)
     first = b.bubbles(0)
     assert np.array_equal(first["velocity"], state[: len(first), 2:])
+
+
+def test_context_outlives_its_worlds_whatever_the_destroy_order():
+    from bubblephysics_gb300.solver import Context
+    c = Context(0)
+    w = World(fixtures.pair_bounce_scene(), c)
+    b = Batch(scenes.batched_worlds(4, seed=24), c, use_graph=False)
+    c.close()              # released first: must stay alive for w and b
+    assert w.step(1)[0] == N.OK
+    assert b.step(1)[0] == N.OK
+    w.close()
+    b.close()              # the last user frees the context
