@@ -206,6 +206,7 @@ _SIGNATURES = {
     "bp_static_polygon_edges": (C.c_int, [C.POINTER(C.c_float), C.c_uint32, C.c_int64, C.c_int64, C.c_uint32,
                                           C.POINTER(Segment), C.c_uint32, C.POINTER(C.c_uint32)]),
     "bp_device_contact_law": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint32]),
+    "bp_world_step_noalloc": (C.c_int, [C.POINTER(WorldDesc), _P, C.c_uint32, _P, C.c_uint32, C.c_uint32, _P, _P]),
 }
 EXPORTED_SYMBOLS = tuple(_SIGNATURES)
 

@@ -338,6 +338,25 @@ int bp_batch_adjacency_entries(bp_batch* batch, uint64_t* entries);
  * persistent launch, [3] worlds stepped by a whole block, [4] worlds stepped by one warp. */
 int bp_batch_tuning(bp_batch* batch, uint32_t* values, uint32_t count);
 
+/* ---- allocation-free step (no counterpart in the reference) ---------------------------------------------------- */
+
+/* For callers that cannot allocate device memory while they step a world - a host framework that owns every device
+ * allocation through its own pool, a real-time thread that must not take the driver's allocation locks, a process
+ * that reserved all its device memory up front. The call allocates nothing: `bubbles` (bubble_count records, updated
+ * in place to the published state after the steps), `segments` and `reports` (`steps` entries) are DEVICE pointers
+ * owned by the caller, and every working array comes from one fixed 1 MiB device array built into the library (it
+ * exists once on every GPU that loads the library, until the process exits).
+ * Limits: at most 1024 bubbles, 256 segments, candidate limit at most 32 (0 means 32), at most 4 contact records per
+ * bubble; no bodies, fields, bands, motors or joints; injection and multi-CTA switches are ignored. Larger inputs are
+ * rejected with BP_E_CAPACITY before anything runs.
+ * Runs on `stream` (a cudaStream_t, NULL = the default stream) on the current device and returns when the work is
+ * queued; the step statuses are in `reports`. The first call on a device looks up the array's device address (with
+ * that device current), so make that first call before any stream capture. Every call shares the one array and
+ * initialises what it needs, so calls must not overlap on the GPU: two calls in flight at once race on it. */
+int bp_world_step_noalloc(const bp_world_desc* desc, bp_bubble* bubbles, uint32_t bubble_count,
+                          const bp_segment* segments, uint32_t segment_count, uint32_t steps,
+                          bp_step_report* reports, void* stream);
+
 /* ---- host helpers (reference host logic that feeds the path) -------------------------------------------------- */
 
 /* One-sided edges of a static polygon (NativeStaticPolygonEdges.segments, NativeStaticPolygonEdges.swift:16-37):
