@@ -38,7 +38,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "bubble-substeps/s (batched worlds, 1 GB300)"
 UNIT = "bubble-substeps/s"
 PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
-PROFILE_FILE = ROOT / "profiles" / "batch_step_kernel.json"
+PROFILE_FILE = ROOT / "profiles" / "persistent_step_kernel.json"
 
 
 def env_int(name, default):
@@ -198,7 +198,7 @@ def run_ours(args, rank, world_size, local_rank):
     ctx = Context(local_rank)
     specs = scenes.batched_worlds(args.worlds, seed=3 + rank)
     total_bubbles = sum(s.bubble_count for s in specs)
-    batch = Batch(specs, ctx, use_graph=True, autotune=True)
+    batch = Batch(specs, ctx, use_graph=True, autotune=not args.no_autotune)
     st, _ = batch.step(args.warmup)
     _, subs0, launches0 = batch.counters()
     if dist:
@@ -296,7 +296,7 @@ def run_ours(args, rank, world_size, local_rank):
                        "max": lat[-1]},
         "per_world_launch": per_world,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "kernel": "batch_step_kernel", "peak_source": peak_kind,
+                     "traffic": traffic, "kernel": "persistent_step_kernel", "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": alg_per_launch,
                      "bytes_model": "76 + 40*k per bubble-substep, 96 + 8*k per bubble grid build (k = mean degree)"},
         "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": cores, "kind": "port",
@@ -322,6 +322,7 @@ def main():
     p.add_argument("--cpu-sample-worlds", type=int, default=256)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--sample-worlds", type=int, default=1024)
+    p.add_argument("--no-autotune", action="store_true", help="keep the default schedule (profiling runs)")
     args = p.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = env_int("RANK", 0)
