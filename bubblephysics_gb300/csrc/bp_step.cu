@@ -586,8 +586,10 @@ __device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, cons
     for (uint32_t i = r; i < n; i += T) build_adjacency(S, W, buckets, entries, B, i, overflow, maxPer);
     team.sync();
     BP_SUBPHASE(17);
-    buildOverflow = team.sum(overflow);
-    maxPerAll = max(maxPerAll, team.umax(maxPer));
+    uint32_t red[4] = {overflow, maxPer, 0u, 0u};
+    team.template reduce4<2u>(red);
+    buildOverflow = red[0];
+    maxPerAll = max(maxPerAll, red[1]);
     BP_SUBPHASE(18);
     return cw;
 }
@@ -736,40 +738,52 @@ struct Viol {
 };
 
 __device__ bool assert_bubble(const DState& S, const DWorld& W, const uint32_t* buckets, const uint32_t* entries, uint32_t B,
-                              float fraction, uint32_t i, Viol& v) {
+                              float fraction, uint32_t i, bool fromCandidates, Viol& v) {
     const uint32_t g = W.boff + i;
     float2 center = S.pos[g], start = S.start[g];
     if (!finite2(center) || S.result[g] == 1u || removed(S, g)) return false;
     bool movable = inv_mass(S, g) > 0.0f;
     uint2 fi = S.filter[g];
-    // pairs with d <= 0 have coincident centres: same or adjacent cell of the current-position grid
-    longlong2 c = S.acell[g];
     uint32_t bestJ = 0xffffffffu;
     float bestD = 0.0f;
-    for (int dx = -1; dx <= 1; ++dx)
-        for (int dy = -1; dy <= 1; ++dy)
-            for_each_in_cell(S.acell, W, buckets, entries, B, c.x + dx, c.y + dy, [&](uint32_t j) {
-                if (j <= i || j >= bestJ) return;
-                uint32_t gj = W.boff + j;
-                if (S.result[gj] == 1u || removed(S, gj)) return;
-                if (!filter_accepts(fi, S.filter[gj])) return;
-                if (!movable && !(inv_mass(S, gj) > 0.0f)) return;
-                float d = len2(sub(S.pos[gj], center));
-                if (d <= 0.0f) { bestJ = j; bestD = d; }
-            });
+    auto checkPair = [&](uint32_t j) {
+        if (j <= i || j >= bestJ) return;
+        uint32_t gj = W.boff + j;
+        if (S.result[gj] == 1u || removed(S, gj)) return;
+        if (!filter_accepts(fi, S.filter[gj])) return;
+        if (!movable && !(inv_mass(S, gj) > 0.0f)) return;
+        float d = len2(sub(S.pos[gj], center));
+        if (d <= 0.0f) { bestJ = j; bestD = d; }
+    };
+    if (fromCandidates) {
+        // pairs with d <= 0 are candidates of the last build (see assert_contacts)
+        const uint32_t* crow = S.candRow + W.rowOff + (uint64_t)i * W.k;
+        const uint32_t pairs = S.candCount[g].x;
+        for (uint32_t e = 0; e < pairs; ++e) checkPair(crow[e]);
+    } else {
+        // pairs with d <= 0 have coincident centres: same or adjacent cell of the current-position grid
+        longlong2 c = S.acell[g];
+        for (int dx = -1; dx <= 1; ++dx)
+            for (int dy = -1; dy <= 1; ++dy)
+                for_each_in_cell(S.acell, W, buckets, entries, B, c.x + dx, c.y + dy, checkPair);
+    }
     if (bestJ != 0xffffffffu) {
         v.kind = BP_VIOLATION_PAIR; v.a = S.id[g]; v.b = S.id[W.boff + bestJ]; v.edge = 0; v.distance = bestD;
         return true;
     }
     if (!movable) return false;
     for (uint32_t bi = 0; bi < W.nb; ++bi) {
+        // a centre inside the body lies inside its swept box widened to the hull radius (conservative slack for the
+        // rounding of the interpolated pose)
+        const RigidBox rb = S.bodyBox[W.bodyOff + bi];
+        if (!filter_accepts(fi, make_uint2(rb.cat, rb.mask))) continue;
+        const float extra = __uint_as_float(rb.pad);
+        const float cs = 1e-3f + 1e-5f * fmaxf(fabsf(center.x), fabsf(center.y));
+        if (center.x < rb.box.x - extra - cs || center.y < rb.box.y - extra - cs || center.x > rb.box.z + extra + cs ||
+            center.y > rb.box.w + extra + cs)
+            continue;
         const DBody& b = S.body[W.bodyOff + bi];
-        if (!filter_accepts(fi, make_uint2(b.cat, b.mask))) continue;
         Pose pose = body_at(b, fraction);
-        // a centre inside the body is within its hull radius (conservative margin for rounding)
-        float2 rel = sub(center, pose.pos);
-        float reachHull = b.pad * 1.0001f + 1e-3f;
-        if (fabsf(rel.x) > reachHull || fabsf(rel.y) > reachHull) continue;
         if (rigid_inside(S.bverts, S.btris, center, b, pose)) {
             v.kind = BP_VIOLATION_INSIDE_BODY; v.a = S.id[g]; v.b = b.id; v.edge = 0; v.distance = 0.0f;
             return true;
@@ -835,15 +849,30 @@ __device__ void assertion_grid(const DState& S, const DWorld& W, const Team& tea
 
 // Runs the assertion over the world; the thread that owns the violating bubble of the lowest index writes the details
 // into the report. Returns 1 in every thread when a violation exists.
+// The pair part can use the candidate rows of the last build instead of a fresh grid when that is complete: two
+// centres closer than any rounding can only meet if their build positions were within m_i + m_j plus the distance each
+// moved since the build, so when every bubble is within margin + r/2 of its build position the pair passed the
+// candidate test (reach = r_i + r_j + m_i + m_j + sepTol). Truncated rows, joint exclusions, injected states and region
+// wraps void that argument and take the grid path.
 template <class Team>
 __device__ uint32_t assert_contacts(const DState& S, const DWorld& W, const Team& team, uint32_t* buckets, uint32_t* entries,
-                                    uint32_t B, float cw, float fraction, bp_step_report* rep) {
-    assertion_grid(S, W, team, buckets, entries, B, cw);
+                                    uint32_t B, float cw, float fraction, bp_step_report* rep, bool rowsComplete) {
+    uint32_t unsafe = (!rowsComplete || W.njEnt || (W.flags & BP_WORLD_INJECT_STATE)) ? 1u : 0u;
+    if (!unsafe) {
+        for (uint32_t i = team.rank(); i < W.n; i += team.size()) {
+            uint32_t g = W.boff + i;
+            if (removed(S, g)) continue;
+            if (S.result[g] == 2u || !(len2(sub(S.pos[g], S.ref[g])) <= S.margin[g] + 0.5f * S.phys[g].x)) unsafe = 1u;
+        }
+        unsafe = team.umax(unsafe);
+    }
+    const bool fromCandidates = unsafe == 0u;
+    if (!fromCandidates) assertion_grid(S, W, team, buckets, entries, B, cw);
     Viol mine{0u, 0, 0, 0, 0.0f};
     ValOwner first{__int_as_float(0x7f800000), 0xffffffffu};
     for (uint32_t i = team.rank(); i < W.n; i += team.size()) {
         Viol v;
-        if (assert_bubble(S, W, buckets, entries, B, fraction, i, v)) {
+        if (assert_bubble(S, W, buckets, entries, B, fraction, i, fromCandidates, v)) {
             first.v = 0.0f;
             first.o = i;
             mine = v;
@@ -1044,7 +1073,8 @@ template <class Team> __device__ void build_boxes(const DState& S, const DWorld&
         float2 hi = add(vmax2(b.pos, b.prev), f2(b.radius, b.radius));
         RigidBox rb;
         rb.box = make_float4(lo.x, lo.y, hi.x, hi.y);
-        rb.cat = b.cat; rb.mask = b.mask; rb.flags = body_is_obstacle(b) ? 1u : 0u; rb.pad = 0u;
+        rb.cat = b.cat; rb.mask = b.mask; rb.flags = body_is_obstacle(b) ? 1u : 0u;
+        rb.pad = __float_as_uint(fmaxf(b.pad - b.radius, 0.0f));  // hull radius beyond the bounding radius
         S.bodyBox[W.bodyOff + bi] = rb;
     }
 }
@@ -1151,7 +1181,8 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
             team.sync();
         }
         if ((W.flags & BP_WORLD_ASSERT_EVERY_SUBSTEP) && !violated)
-            violated = assert_contacts(S, W, team, buckets, entries, B, cw, c.timeX > 0.0f ? clampf(c.timeY / c.timeX, 0.0f, 1.0f) : 1.0f, rep);
+            violated = assert_contacts(S, W, team, buckets, entries, B, cw, c.timeX > 0.0f ? clampf(c.timeY / c.timeX, 0.0f, 1.0f) : 1.0f, rep,
+                                       buildOverflow == 0u);
     }
     overflowMax = max(overflowMax, buildOverflow);
     BP_PHASE(5);
@@ -1181,8 +1212,10 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
         segsLocal += cs;
     }
     BP_PHASE(6);
-    const uint32_t pairsAll = team.sum(pairsLocal);
-    const uint32_t segsAll = team.sum(segsLocal);
+    uint32_t pc[4] = {pairsLocal, segsLocal, 0u, 0u};
+    team.template reduce4<0u>(pc);
+    const uint32_t pairsAll = pc[0];
+    const uint32_t segsAll = pc[1];
     team.scan_inplace(S.scanA + W.boff, n);
     team.scan_inplace(S.scanB + W.boff, n);
     uint32_t droppedLocal = 0;
@@ -1209,26 +1242,30 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
         if (removed(S, g)) continue;
         if (!finite2(S.pos[g]) || !finite2(S.start[g]) || !finite2(S.vel[g]) || !finite2(S.rotw[g])) nonfinite = 1u;
     }
-    const uint32_t anyNonfinite = team.umax(nonfinite);
-    const uint32_t contactDropped = team.sum(droppedLocal);
+    uint32_t nf[4] = {nonfinite, droppedLocal, 0u, 0u};
+    team.template reduce4<1u>(nf);
+    const uint32_t anyNonfinite = nf[0];
+    const uint32_t contactDropped = nf[1];
     BP_PHASE(8);
     if (!violated && stepDone && !(W.flags & BP_WORLD_NO_END_ASSERTION))
-        violated = assert_contacts(S, W, team, buckets, entries, B, cw, 1.0f, rep);
+        violated = assert_contacts(S, W, team, buckets, entries, B, cw, 1.0f, rep, buildOverflow == 0u);
     BP_PHASE(9);
     int status = BP_OK;
     if (c.cW != 0u) status = BP_E_SUBSTEP_LIMIT;
     else if (anyNonfinite) status = BP_E_NONFINITE;
     else if (violated) status = BP_E_CONTACT_VIOLATION;
-    const uint32_t removedAll = team.sum(removedCount);
-    const uint32_t wrappedAll = team.sum(wrapped);
     uint32_t candLocal = 0, bodyCandLocal = 0;
     for (uint32_t i = r; i < n; i += T) {
         uint2 cc = S.candCount[W.boff + i];
         if (!removed(S, W.boff + i)) candLocal += cc.x + cc.y;
     }
     for (uint32_t bi = r; bi < W.nb; bi += T) bodyCandLocal += min(S.bodyTotal[W.bodyOff + bi], W.k);
-    const uint32_t candAll = team.sum(candLocal);
-    const uint32_t bodyCandAll = team.sum(bodyCandLocal);
+    uint32_t counts4[4] = {removedCount, wrapped, candLocal, bodyCandLocal};
+    team.template reduce4<0u>(counts4);
+    const uint32_t removedAll = counts4[0];
+    const uint32_t wrappedAll = counts4[1];
+    const uint32_t candAll = counts4[2];
+    const uint32_t bodyCandAll = counts4[3];
     if (team.leader()) {
         rep->status = status;
         rep->substep_count = c.cY;

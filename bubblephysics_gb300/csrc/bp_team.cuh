@@ -65,7 +65,32 @@ struct BlockScratch {
     uint32_t u[33];
     float bcastF[4];
     uint32_t bcastU[8];
+    uint32_t u4[4][33];
 };
+
+// Four sums (kMaxMask bit c set: maximum instead of sum for component c) in one block reduction.
+template <uint32_t kMaxMask> __device__ __forceinline__ void block_reduce4(uint32_t (&v)[4], BlockScratch& sh) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = (blockDim.x + 31u) >> 5;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) v[c] = ((kMaxMask >> c) & 1u) ? warp_max(v[c]) : warp_sum(v[c]);
+    __syncthreads();
+    if (lane == 0) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) sh.u4[c][warp] = v[c];
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            uint32_t y = lane < nw ? sh.u4[c][lane] : 0u;
+            y = ((kMaxMask >> c) & 1u) ? warp_max(y) : warp_sum(y);
+            if (lane == 0) sh.u4[c][32] = y;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < 4; ++c) v[c] = sh.u4[c][32];
+}
 
 // Block-wide (value, owner) reduction; result broadcast to every thread.
 template <bool kMax> __device__ __forceinline__ ValOwner block_pick(ValOwner x, BlockScratch& sh) {
@@ -157,6 +182,7 @@ struct CtaTeam {
     __device__ uint32_t sum(uint32_t x) const { return block_sum(x, *sh); }
     __device__ uint32_t umax(uint32_t x) const { return block_max(x, *sh); }
     __device__ float fmax(float x) const { return block_fmax(x, *sh); }
+    template <uint32_t kMaxMask> __device__ void reduce4(uint32_t (&v)[4]) const { block_reduce4<kMaxMask>(v, *sh); }
     // Exclusive scan of `count` values in place (values live in memory visible to the whole team).
     __device__ void scan_inplace(uint32_t* values, uint32_t count) const {
         uint32_t per = (count + blockDim.x - 1) / blockDim.x;
@@ -189,6 +215,10 @@ struct WarpTeam {
     __device__ uint32_t sum(uint32_t x) const { return warp_sum(x); }
     __device__ uint32_t umax(uint32_t x) const { return warp_max(x); }
     __device__ float fmax(float x) const { return warp_fmax(x); }
+    template <uint32_t kMaxMask> __device__ void reduce4(uint32_t (&v)[4]) const {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) v[c] = ((kMaxMask >> c) & 1u) ? warp_max(v[c]) : warp_sum(v[c]);
+    }
     __device__ void scan_inplace(uint32_t* values, uint32_t count) const {
         const uint32_t lane = threadIdx.x & 31u;
         uint32_t per = (count + 31u) / 32u;
@@ -288,6 +318,10 @@ struct GridTeam {
     }
     __device__ uint32_t sum(uint32_t x) const { return reduce_u(x, false); }
     __device__ uint32_t umax(uint32_t x) const { return reduce_u(x, true); }
+    template <uint32_t kMaxMask> __device__ void reduce4(uint32_t (&v)[4]) const {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) v[c] = reduce_u(v[c], ((kMaxMask >> c) & 1u) != 0u);
+    }
     __device__ float fmax(float x) const {
         x = block_fmax(x, *sh);
         uint32_t base = par * gridDim.x;
