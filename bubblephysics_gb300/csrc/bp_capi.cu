@@ -56,8 +56,8 @@ constexpr int kLargeThreads = 512;
 constexpr uint32_t kDefaultThreads = 256;
 constexpr uint32_t kDefaultWarpMax = 64;
 constexpr uint32_t kWarpSubsteps = 16;   // a world that took more substeps last step gets a whole block
-constexpr uint32_t kCtaWorkspaceCap = 96u * 1024u;   // shared-memory workspace of a block team (2 blocks per SM)
-constexpr uint32_t kWarpWorkspaceCap = 12u * 1024u;  // per warp team
+constexpr uint32_t kCtaWorkspaceCap = 80u * 1024u;   // shared-memory workspace of a block team (2 blocks per SM, L1 keeps ~90 KB)
+constexpr uint32_t kWarpWorkspaceCap = 10u * 1024u;  // per warp team
 constexpr uint32_t kMaxDynamicSmem = 200u * 1024u;   // per block, set on the kernels by prepare_kernels()
 
 struct DeviceGuard {
