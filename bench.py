@@ -172,6 +172,45 @@ def run_reference(args, rank):
     return 0
 
 
+def single_world_rate(spec, ctx, steps: int, warmup: int) -> dict:
+    """One world stepped through bp_world_step: device time per step (CUDA events on the library's stream) and
+    bubble-substeps per second over `steps` timed steps after `warmup` untimed ones."""
+    from bubblephysics_gb300.solver import World
+    world = World(spec, ctx)
+    status, _ = world.step(warmup)
+    statuses, ms, subs = [status], [], 0
+    for _ in range(steps):
+        status, reps = world.step(1)
+        statuses.append(status)
+        ms.append(float(reps["gpu_ms"][0]))
+        subs += int(reps["substep_count"][0]) * spec.bubble_count
+    keys = world.rigid_keys().size
+    world.close()
+    total_s = sum(ms) / 1000.0
+    return {"bubbles": spec.bubble_count, "segments": len(spec.segments), "bodies": len(spec.bodies),
+            "steps": steps, "warmup": warmup, "ms_per_step": total_s * 1000.0 / max(steps, 1),
+            "substeps_per_step": subs / max(spec.bubble_count * steps, 1),
+            "value": subs / total_s if total_s > 0 else 0.0, "unit": UNIT, "statuses": sorted(set(statuses)),
+            "rigid_tree_leaves": keys}
+
+
+def single_worlds(ctx, steps: int) -> dict:
+    """The single-world workloads beside the batched headline: the large plain world (65,536 bubbles in 8192^2, grid
+    rebuilt almost every substep; whole-GPU team) and the rigid world (16,384 bubbles, ~4,000 static / kinematic
+    bodies in 4096^2, rigid candidates through the LBVH, and the same world by brute force for comparison)."""
+    import dataclasses
+    from bubblephysics_gb300 import _native as N
+    from bubblephysics_gb300 import scenes
+    out = {"large_world": single_world_rate(scenes.large_world(), ctx, steps, 3)}
+    rigid = scenes.rigid_world()
+    out["rigid_world"] = single_world_rate(rigid, ctx, steps, 3)
+    brute = dataclasses.replace(rigid, flags=rigid.flags | N.WORLD_NO_RIGID_TREE)
+    out["rigid_world_brute_force"] = single_world_rate(brute, ctx, steps, 3)
+    t, b = out["rigid_world"]["ms_per_step"], out["rigid_world_brute_force"]["ms_per_step"]
+    out["rigid_world"]["speedup_vs_brute_force"] = b / t if t > 0 else None
+    return out
+
+
 def combine_ranks(device_s: float, bubble_substeps: float, dist=None) -> tuple[float, float]:
     """Whole-job timing over ranks: the slowest rank's device time and the sum of all ranks' bubble-substeps."""
     if dist is None:
@@ -266,6 +305,7 @@ def run_ours(args, rank, world_size, local_rank):
             dist.barrier()
         return 0
 
+    singles = single_worlds(ctx, args.single_steps) if args.single_steps > 0 else None
     peak, peak_kind = load_peak()
     achieved = alg_bytes / device_s / 1e9 if device_s > 0 else 0.0
     traffic = None
@@ -303,6 +343,7 @@ def run_ours(args, rank, world_size, local_rank):
                          "sample": f"first {len(cpu_specs)} worlds of the workload, {cpu_steps} steps, {cpu_dt:.1f} s"},
         "clocks": clocks,
         "gpu_launches": gpu_launches,
+        "single_worlds": singles,
     }
     print(json.dumps(line), flush=True)
     if dist:
@@ -322,6 +363,7 @@ def main():
     p.add_argument("--cpu-sample-worlds", type=int, default=256)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--sample-worlds", type=int, default=1024)
+    p.add_argument("--single-steps", type=int, default=10, help="timed steps of each single-world workload (0: skip)")
     p.add_argument("--no-autotune", action="store_true", help="keep the default schedule (profiling runs)")
     args = p.parse_args()
     args.warmup = max(args.warmup, 3)

@@ -25,7 +25,7 @@ SEGMENT_POLYGON_EDGE, SEGMENT_CONVEX_START, SEGMENT_CONVEX_END, SEGMENT_HAS_OWNE
 BODY_POLYGON, BODY_CIRCLE, BODY_CAPSULE = 0, 1, 2
 BODY_STATIC, BODY_KINEMATIC = 1, 2
 WORLD_HAS_REGION, WORLD_MINIMUM_MARGIN_ONLY, WORLD_ASSERT_EVERY_SUBSTEP, WORLD_INJECT_STATE, \
-    WORLD_NO_END_ASSERTION, WORLD_FORCE_MULTI_CTA = 1, 2, 4, 8, 16, 32
+    WORLD_NO_END_ASSERTION, WORLD_FORCE_MULTI_CTA, WORLD_RIGID_TREE, WORLD_NO_RIGID_TREE = 1, 2, 4, 8, 16, 32, 64, 128
 BATCH_PER_WORLD_LAUNCH, BATCH_USE_GRAPH, BATCH_AUTOTUNE = 1, 2, 4
 TERM_REMAINING, TERM_STIFFNESS, TERM_DISTANCE, TERM_MARGIN = range(4)
 VIOLATION_NONE, VIOLATION_PAIR, VIOLATION_INSIDE_BODY, VIOLATION_EDGE_SIDE = range(4)
@@ -192,6 +192,7 @@ _SIGNATURES = {
     "bp_world_read_contacts": (C.c_int, [_P, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
     "bp_world_read_candidates": (C.c_int, [_P, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
     "bp_world_read_cells": (C.c_int, [_P, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
+    "bp_world_read_rigid_keys": (C.c_int, [_P, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
     "bp_world_read_substeps": (C.c_int, [_P, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
     "bp_batch_create": (C.c_int, [_P, C.c_uint32, C.POINTER(WorldDesc), C.POINTER(WorldInput),
                                   C.POINTER(BatchConfig), C.POINTER(_P)]),

@@ -59,6 +59,7 @@ constexpr uint32_t kWarpSubsteps = 16;   // a world that took more substeps last
 constexpr uint32_t kCtaWorkspaceCap = 80u * 1024u;   // shared-memory workspace of a block team (2 blocks per SM, L1 keeps ~90 KB)
 constexpr uint32_t kWarpWorkspaceCap = 10u * 1024u;  // per warp team
 constexpr uint32_t kMaxDynamicSmem = 200u * 1024u;   // per block, set on the kernels by prepare_kernels()
+constexpr uint32_t kTreeMinLeaves = 128;             // segments + bodies from which rigid candidates use the LBVH
 
 struct DeviceGuard {
     int previous = -1;
@@ -103,6 +104,7 @@ struct WorldSet {
     std::vector<int64_t> hSegIds, hBodyIds;
     uint64_t totalBubbles = 0, totalRows = 0, totalBodyRows = 0, totalContacts = 0;
     uint32_t totalSegments = 0, totalBodies = 0;
+    uint64_t totalTreeLeaves = 0;
     DState S{};
     DWorld* dWorlds = nullptr;
     bp_step_report* dReports = nullptr;
@@ -250,6 +252,8 @@ cudaError_t schedule(WorldSet& ws, uint32_t threads, uint32_t warpMax) {
     q.warpMaxN = maxWarpN;
     q.warpB = maxWarpN ? grid_buckets(maxWarpN) : 0u;
     q.countsOnDevice = 1u;
+    q.tree = 0u;
+    for (uint32_t w : candidates) q.tree |= ws.hWorlds[w].tree;
     q.ctaWsWords = ws.staging ? (ctaWs + 3u) / 4u : 0u;
     q.warpWsWords = ws.staging ? (warpWs + 3u) / 4u : 0u;
     q.ctaWsWords = (q.ctaWsWords + 3u) & ~3u;
@@ -317,6 +321,7 @@ int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc
     ws.hBubbles.resize(nb);
     ws.hSegIds.resize(ns);
     ws.hBodyIds.resize(nbo);
+    uint64_t otree = 0;
     uint64_t ob = 0, orow = 0, obrow = 0, ocon = 0, os = 0, obo = 0, obv = 0, obt = 0, of = 0, ofv = 0, ofi = 0, oband = 0,
              omotor = 0, ojr = 0, ojp = 0;
     for (uint32_t w = 0; w < count; ++w) {
@@ -333,6 +338,12 @@ int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc
         W.jrOff = (uint32_t)ojr; W.njEnt = in.joint_ranges ? in.joint_entity_count : 0;
         W.k = d.candidate_limit == 0 ? 128u : d.candidate_limit;
         W.flags = d.flags;
+        const uint32_t leaves = in.segment_count + in.body_count;
+        const bool tree = leaves > 0u && !(d.flags & BP_WORLD_NO_RIGID_TREE) &&
+                          ((d.flags & BP_WORLD_RIGID_TREE) || leaves >= kTreeMinLeaves);
+        W.tree = tree ? 1u : 0u;
+        W.treeOff = tree ? (uint32_t)otree : 0u;
+        if (tree) otree += leaves;
         W.injectSubstep = 0;
         W.contactCap = single ? in.bubble_count * W.k + 64 : in.bubble_count * 16 + 64;
         W.rowOff = orow; W.bodyRowOff = obrow; W.contactOff = ocon;
@@ -460,6 +471,11 @@ int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc
     uint32_t* dBt = ws.alloc<uint32_t>(3 * nbt, err);
     S.btris = dBt;
     S.bodyRow = ws.alloc<uint32_t>(brows, err); S.bodyTotal = ws.alloc<uint32_t>(nbo, err);
+    S.tKeys = ws.alloc<unsigned long long>(otree, err); S.tKeysAlt = ws.alloc<unsigned long long>(otree, err);
+    S.tCounts = ws.alloc<uint32_t>(16ull * otree, err); S.tNodes = ws.alloc<TreeNode>(otree, err);
+    S.tLeafParent = ws.alloc<uint32_t>(otree, err); S.tVisit = ws.alloc<uint32_t>(otree, err);
+    S.tValid = ws.alloc<uint32_t>(count, err);
+    ws.totalTreeLeaves = otree;
     DField* dF = ws.alloc<DField>(nf, err);
     S.fields = dF;
     float2* dFv = ws.alloc<float2>(nfv, err);
@@ -554,6 +570,7 @@ cudaError_t launch_step(WorldSet& ws, bool perWorld, uint32_t only = 0xffffffffu
         QueueArgs q{};
         q.queue = ws.dQueueSingle;
         q.countsOnDevice = 0u;
+        q.tree = W.tree;
         uint32_t maxN = std::max<uint32_t>(W.n, 1u);
         uint32_t bytes = workspace_bytes(W.n, W.s, W.nb);
         bool warpTeam = W.n <= ws.warpMax;
@@ -1037,6 +1054,22 @@ int bp_world_read_cells(bp_world* world, int64_t* out, uint32_t capacity, uint32
     DeviceGuard guard(ws.ctx->device);
     uint32_t m = std::min(W.n, capacity);
     cudaError_t err = m ? cudaMemcpy(out, ws.S.cell + W.boff, m * sizeof(longlong2), cudaMemcpyDeviceToHost) : cudaSuccess;
+    return cuda_status(err);
+}
+
+int bp_world_read_rigid_keys(bp_world* world, uint64_t* out, uint32_t capacity, uint32_t* count) {
+    if (!world) return BP_E_INVALID;
+    WorldSet& ws = world->set;
+    const DWorld& W = ws.hWorlds[0];
+    DeviceGuard guard(ws.ctx->device);
+    uint32_t valid = 0;
+    cudaError_t err = W.tree ? cudaMemcpy(&valid, ws.S.tValid, sizeof(valid), cudaMemcpyDeviceToHost) : cudaSuccess;
+    if (err) return cuda_status(err);
+    const uint32_t leaves = valid ? W.s + W.nb : 0u;
+    if (count) *count = leaves;
+    if (!out) return BP_OK;
+    uint32_t m = std::min(leaves, capacity);
+    err = m ? cudaMemcpy(out, ws.S.tKeys + W.treeOff, m * sizeof(uint64_t), cudaMemcpyDeviceToHost) : cudaSuccess;
     return cuda_status(err);
 }
 

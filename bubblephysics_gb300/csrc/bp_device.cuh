@@ -36,14 +36,14 @@ struct DWorld {
     uint32_t bodyOff, nb, foff, nf;
     uint32_t bandOff, nbands, motorOff, nmotors;
     uint32_t jrOff, njEnt, k, flags;
-    uint32_t injectSubstep, contactCap, threads, pad0;
+    uint32_t injectSubstep, contactCap, threads, treeOff;  // treeOff: first leaf of the world's LBVH arrays
     uint64_t rowOff;       // candidate / adjacency rows: entries rowOff + i * k
     uint64_t bodyRowOff;   // body rows: bodyRowOff + b * k
     uint64_t contactOff;   // contact records
     float dt, sepTol, contactTol, split;
     float2 rmin, rmax, gforce, gravity, injectPos;
     int64_t injectObject;
-    uint32_t failed, pad1;
+    uint32_t failed, tree;  // tree: 1 when rigid candidates go through the LBVH
 };
 
 struct DSegment {
@@ -76,6 +76,15 @@ struct RigidBox {
     float4 box;  // lo.xy, hi.xy
     uint32_t cat, mask, flags, pad;
 };
+
+// Internal node of a world's LBVH over its rigid leaves, child boxes stored inline so a traversal reads one node to
+// test both children. A child index with kTreeLeaf set is a sorted leaf position, otherwise an internal node.
+struct TreeNode {
+    float4 box[2];     // lo.xy, hi.xy of the left and right child (leaf boxes widened by the body hull radius)
+    uint32_t child[2];
+    uint32_t parent, pad;
+};
+constexpr uint32_t kTreeLeaf = 0x80000000u;
 
 // End-of-step contact record, index form (ids are looked up on the host).
 struct DContact {
@@ -135,6 +144,14 @@ struct DState {
     float4* bpose;             // per body: pose at the current step fraction (position.xy, cos, sin)
     RigidBox* segBox;          // per segment
     RigidBox* bodyBox;         // per body (rebuilt every step: kinematic bodies move)
+    // LBVH over the rigid leaves of worlds with W.tree set (entries from W.treeOff, s + nb per world)
+    unsigned long long* tKeys;     // sorted keys (morton << 32 | leaf)
+    unsigned long long* tKeysAlt;  // radix-sort ping-pong
+    uint32_t* tCounts;             // 16 digit counters per leaf (radix-sort scratch)
+    TreeNode* tNodes;              // s + nb - 1 internal nodes (node 0 is the root)
+    uint32_t* tLeafParent;         // per sorted leaf: (parent node << 1) | side
+    uint32_t* tVisit;              // per internal node: children finished (bottom-up refit)
+    uint32_t* tValid;              // per world: 1 when the last step built its tree
 };
 
 constexpr uint32_t kPhaseCount = 24;
@@ -150,6 +167,7 @@ struct QueueArgs {
     uint32_t nWarp, warpB, warpMaxN;
     uint32_t countsOnDevice;          // 1: list lengths are queue[2], queue[3]; 0: nCta, nWarp
     uint32_t ctaWsWords, warpWsWords; // shared-memory workspace of one team (32-bit words) after its grid
+    uint32_t tree;                    // 1: some world uses the LBVH (launch the tree-capable kernel)
 };
 
 // Bytes of a world's shared-memory workspace: per bubble 88 B of hot state, per segment and body a 32 B box, per body

@@ -11,6 +11,7 @@
 #include <mutex>
 
 #include "bp_team.cuh"
+#include "bp_tree.cuh"
 
 namespace bp {
 
@@ -414,7 +415,16 @@ __device__ __forceinline__ void for_each_in_cell(const longlong2* cells, const D
     }
 }
 
-// Forward candidate row of bubble i: pairs with j > i, then segments; k smallest keys (NGK:300-330).
+// Body-row hits of bubble i found through the tree: slots are taken in arrival order and put in index order (or
+// rebuilt by brute force when the row overflows) by fix_body_row.
+__device__ __forceinline__ void body_hit(const DState& S, const DWorld& W, uint32_t bi, uint32_t i) {
+    const uint32_t slot = atomicAdd(S.bodyTotal + W.bodyOff + bi, 1u);
+    if (slot < W.k) S.bodyRow[W.bodyRowOff + (uint64_t)bi * W.k + slot] = i;
+}
+
+// Forward candidate row of bubble i: pairs with j > i, then segments; k smallest keys (NGK:300-330). With the tree,
+// the same traversal also registers i in the rows of the bodies that accept it.
+template <bool kTree>
 __device__ void emit_row(const DState& S, const DWorld& W, const uint32_t* buckets, const uint32_t* entries, uint32_t B,
                          uint32_t i, uint32_t& overflow, uint32_t& maxPer) {
     const uint32_t g = W.boff + i, k = W.k;
@@ -422,6 +432,18 @@ __device__ void emit_row(const DState& S, const DWorld& W, const uint32_t* bucke
     if (!(S.flags[g] & kValid) || !finite2(S.start[g])) {
         S.candCount[g] = make_uint2(0u, 0u);
         S.pairTotal[g] = 0u;
+        if (kTree && W.nb && !removed(S, g)) {
+            // a bubble without a valid cell still meets the body rule (a non-finite centre fails no comparison)
+            const float reach = S.phys[g].x + fmaxf(S.margin[g], 0.0f);
+            const float2 c = S.pos[g], lo = sub(c, f2(reach, reach)), hi = add(c, f2(reach, reach));
+            tree_query(S, W, [&](float4 nb) { return !(hi.x < nb.x || hi.y < nb.y || nb.z < lo.x || nb.w < lo.y); },
+                       [&](uint32_t leaf) {
+                           if (leaf < W.s) return;
+                           const uint32_t bi = leaf - W.s;
+                           const RigidBox rb = S.bodyBox[W.bodyOff + bi];
+                           if (rb.flags && body_accepts(S, W, rb, bi, i)) body_hit(S, W, bi, i);
+                       });
+        }
         return;
     }
     longlong2 c = S.cell[g];
@@ -436,10 +458,41 @@ __device__ void emit_row(const DState& S, const DWorld& W, const uint32_t* bucke
             });
     const uint32_t pairs = count;
     uint32_t segTotal = 0;
-    for (uint32_t sj = 0; sj < W.s; ++sj) {
-        if (!segment_accepts(S, W, i, sj)) continue;
-        ++segTotal;
-        if (count < k) row[count++] = (1u << kKindShift) | sj;
+    if (kTree) {
+        // segments kept in index order up to the free slots, as the brute-force loop below appends them
+        uint32_t* segRow = row + pairs;
+        const uint32_t segLimit = k - pairs;
+        uint32_t segKept = 0;
+        const float2 p = S.pos[g];
+        const float reachS = S.phys[g].x + S.margin[g] + W.sepTol;
+        const float reachB = S.phys[g].x + fmaxf(S.margin[g], 0.0f);
+        const float2 lo = sub(p, f2(reachB, reachB)), hi = add(p, f2(reachB, reachB));
+        const bool wantBodies = W.nb != 0u;
+        tree_query(S, W,
+                   [&](float4 nb) {
+                       const bool seg = p.x >= nb.x - reachS && p.y >= nb.y - reachS && p.x <= nb.z + reachS &&
+                                        p.y <= nb.w + reachS;
+                       const bool body = wantBodies && !(hi.x < nb.x || hi.y < nb.y || nb.z < lo.x || nb.w < lo.y);
+                       return seg || body;
+                   },
+                   [&](uint32_t leaf) {
+                       if (leaf < W.s) {
+                           if (!segment_accepts(S, W, i, leaf)) return;
+                           ++segTotal;
+                           if (segLimit) insert_sorted(segRow, segKept, segLimit, (1u << kKindShift) | leaf);
+                           return;
+                       }
+                       const uint32_t bi = leaf - W.s;
+                       const RigidBox rb = S.bodyBox[W.bodyOff + bi];
+                       if (rb.flags && body_accepts(S, W, rb, bi, i)) body_hit(S, W, bi, i);
+                   });
+        count += segKept;
+    } else {
+        for (uint32_t sj = 0; sj < W.s; ++sj) {
+            if (!segment_accepts(S, W, i, sj)) continue;
+            ++segTotal;
+            if (count < k) row[count++] = (1u << kKindShift) | sj;
+        }
     }
     S.candCount[g] = make_uint2(pairs, count - pairs);
     S.pairTotal[g] = total;
@@ -471,7 +524,28 @@ __device__ void emit_body_row(const DState& S, const DWorld& W, uint32_t bi, uin
     }
 }
 
+// Body row bi after the tree pass: hits arrived in any order; a row that fits is sorted (the first k accepting bubbles
+// in index order are then all of them), an overflowing row is rebuilt by the brute-force scan.
+__device__ void fix_body_row(const DState& S, const DWorld& W, uint32_t bi, uint32_t lane, uint32_t& overflow, uint32_t& maxPer) {
+    const uint32_t total = S.bodyTotal[W.bodyOff + bi];
+    if (total > W.k) {
+        emit_body_row(S, W, bi, lane, overflow, maxPer);
+        return;
+    }
+    if (lane == 0) {
+        uint32_t* row = S.bodyRow + W.bodyRowOff + (uint64_t)bi * W.k;
+        for (uint32_t e = 1; e < total; ++e) {
+            const uint32_t value = row[e];
+            uint32_t loc = e;
+            while (loc > 0 && value < row[loc - 1]) { row[loc] = row[loc - 1]; --loc; }
+            row[loc] = value;
+        }
+        maxPer = max(maxPer, total);
+    }
+}
+
 // Adjacency row of bubble i, sorted by (kind, neighbour), first k kept (NFK:298-331, NCK:222-238).
+template <bool kTree>
 __device__ void build_adjacency(const DState& S, const DWorld& W, const uint32_t* buckets, const uint32_t* entries,
                                 uint32_t B, uint32_t i, uint32_t& overflow, uint32_t& maxPer) {
     const uint32_t g = W.boff + i, k = W.k;
@@ -501,7 +575,23 @@ __device__ void build_adjacency(const DState& S, const DWorld& W, const uint32_t
         if (deg < k) row[deg++] = crow[e];
     }
     // bodies holding i in their row
-    for (uint32_t bi = 0; bi < W.nb; ++bi) {
+    if (kTree) {
+        if (W.nb) {
+            const float reach = S.phys[g].x + fmaxf(S.margin[g], 0.0f);
+            const float2 c = S.pos[g], lo = sub(c, f2(reach, reach)), hi = add(c, f2(reach, reach));
+            tree_query(S, W, [&](float4 nb) { return !(hi.x < nb.x || hi.y < nb.y || nb.z < lo.x || nb.w < lo.y); },
+                       [&](uint32_t leaf) {
+                           if (leaf < W.s) return;
+                           const uint32_t bi = leaf - W.s;
+                           const RigidBox rb = S.bodyBox[W.bodyOff + bi];
+                           if (!rb.flags || !body_accepts(S, W, rb, bi, i)) return;
+                           const uint32_t total = S.bodyTotal[W.bodyOff + bi];
+                           if (total > k && !row_contains(S.bodyRow + W.bodyRowOff + (uint64_t)bi * k, k, i)) return;
+                           ++demanded;
+                           insert_sorted(row, deg, k, (2u << kKindShift) | bi);
+                       });
+        }
+    } else for (uint32_t bi = 0; bi < W.nb; ++bi) {
         const RigidBox rb = S.bodyBox[W.bodyOff + bi];
         if (!rb.flags || !body_accepts(S, W, rb, bi, i)) continue;
         uint32_t total = S.bodyTotal[W.bodyOff + bi];
@@ -517,7 +607,7 @@ __device__ void build_adjacency(const DState& S, const DWorld& W, const uint32_t
 // ------------------------------------------------------------------------------------------------------------------
 // Grid build + candidates + adjacency (one build of nativeBroadphaseInGroup, NFK:1040-1134)
 // ------------------------------------------------------------------------------------------------------------------
-template <class Team>
+template <class Team, bool kTree>
 __device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, const Team& team, uint32_t* buckets,
                             uint32_t* entries, uint32_t B, uint32_t& buildOverflow, uint32_t& maxPerAll, uint32_t subWorld) {
     const uint32_t n = W.n, T = team.size(), r = team.rank();
@@ -544,6 +634,8 @@ __device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, cons
     float cw = team.fmax(cwl);
     cw = fmaxf(cw, kFltMin);
     for (uint32_t b = r; b < B; b += T) buckets[b] = 0u;
+    if (kTree)
+        for (uint32_t bi = r; bi < W.nb; bi += T) S.bodyTotal[W.bodyOff + bi] = 0u;
     team.sync();
     BP_SUBPHASE(13);
     // cells (nativeBuildGrid, NGK:179-189) and bucket counts
@@ -574,16 +666,19 @@ __device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, cons
     team.sync();
     BP_SUBPHASE(14);
     uint32_t overflow = 0, maxPer = 0;
-    for (uint32_t i = r; i < n; i += T) emit_row(S, W, buckets, entries, B, i, overflow, maxPer);
+    for (uint32_t i = r; i < n; i += T) emit_row<kTree>(S, W, buckets, entries, B, i, overflow, maxPer);
     team.sync();
     BP_SUBPHASE(15);
     {
         const uint32_t lane = threadIdx.x & 31u, warp = r >> 5, warps = T >> 5;
-        for (uint32_t bi = warp; bi < W.nb; bi += warps) emit_body_row(S, W, bi, lane, overflow, maxPer);
+        if (kTree)
+            for (uint32_t bi = warp; bi < W.nb; bi += warps) fix_body_row(S, W, bi, lane, overflow, maxPer);
+        else
+            for (uint32_t bi = warp; bi < W.nb; bi += warps) emit_body_row(S, W, bi, lane, overflow, maxPer);
     }
     team.sync();
     BP_SUBPHASE(16);
-    for (uint32_t i = r; i < n; i += T) build_adjacency(S, W, buckets, entries, B, i, overflow, maxPer);
+    for (uint32_t i = r; i < n; i += T) build_adjacency<kTree>(S, W, buckets, entries, B, i, overflow, maxPer);
     team.sync();
     BP_SUBPHASE(17);
     uint32_t red[4] = {overflow, maxPer, 0u, 0u};
@@ -737,6 +832,7 @@ struct Viol {
     float distance;
 };
 
+template <bool kTree>
 __device__ bool assert_bubble(const DState& S, const DWorld& W, const uint32_t* buckets, const uint32_t* entries, uint32_t B,
                               float fraction, uint32_t i, bool fromCandidates, Viol& v) {
     const uint32_t g = W.boff + i;
@@ -772,45 +868,88 @@ __device__ bool assert_bubble(const DState& S, const DWorld& W, const uint32_t* 
         return true;
     }
     if (!movable) return false;
-    for (uint32_t bi = 0; bi < W.nb; ++bi) {
-        // a centre inside the body lies inside its swept box widened to the hull radius (conservative slack for the
-        // rounding of the interpolated pose)
+    // a centre inside the body lies inside its swept box widened to the hull radius (conservative slack for the
+    // rounding of the interpolated pose)
+    const float cs = 1e-3f + 1e-5f * fmaxf(fabsf(center.x), fabsf(center.y));
+    auto insideBody = [&](uint32_t bi) {
         const RigidBox rb = S.bodyBox[W.bodyOff + bi];
-        if (!filter_accepts(fi, make_uint2(rb.cat, rb.mask))) continue;
+        if (!filter_accepts(fi, make_uint2(rb.cat, rb.mask))) return false;
         const float extra = __uint_as_float(rb.pad);
-        const float cs = 1e-3f + 1e-5f * fmaxf(fabsf(center.x), fabsf(center.y));
         if (center.x < rb.box.x - extra - cs || center.y < rb.box.y - extra - cs || center.x > rb.box.z + extra + cs ||
             center.y > rb.box.w + extra + cs)
-            continue;
+            return false;
         const DBody& b = S.body[W.bodyOff + bi];
         Pose pose = body_at(b, fraction);
-        if (rigid_inside(S.bverts, S.btris, center, b, pose)) {
-            v.kind = BP_VIOLATION_INSIDE_BODY; v.a = S.id[g]; v.b = b.id; v.edge = 0; v.distance = 0.0f;
-            return true;
-        }
+        return rigid_inside(S.bverts, S.btris, center, b, pose);
+    };
+    // the reported body is the lowest index the centre is inside of, whichever way the bodies are visited
+    uint32_t insideOf = 0xffffffffu;
+    if (kTree) {
+        if (W.nb)
+            tree_query(S, W,
+                       [&](float4 nb) {
+                           return !(center.x < nb.x - cs || center.y < nb.y - cs || center.x > nb.z + cs ||
+                                    center.y > nb.w + cs);
+                       },
+                       [&](uint32_t leaf) {
+                           if (leaf < W.s || leaf - W.s >= insideOf) return;
+                           if (insideBody(leaf - W.s)) insideOf = leaf - W.s;
+                       });
+    } else {
+        for (uint32_t bi = 0; bi < W.nb; ++bi)
+            if (insideBody(bi)) { insideOf = bi; break; }
+    }
+    if (insideOf != 0xffffffffu) {
+        v.kind = BP_VIOLATION_INSIDE_BODY; v.a = S.id[g]; v.b = S.body[W.bodyOff + insideOf].id; v.edge = 0; v.distance = 0.0f;
+        return true;
     }
     // a crossing point lies on both the chord start -> centre and the edge: their boxes must overlap (conservative
     // margin for rounding) before the exact test runs
     const float2 pathLo = vmin2(start, center), pathHi = vmax2(start, center);
     const float slack = 1e-3f + 1e-5f * fmaxf(fmaxf(fabsf(pathLo.x), fabsf(pathLo.y)), fmaxf(fabsf(pathHi.x), fabsf(pathHi.y)));
-    for (uint32_t e = 0; e < W.s; ++e) {
+    auto crossesEdge = [&](uint32_t e, float& after) {
         const RigidBox rb = S.segBox[W.soff + e];
-        if (!(rb.flags & BP_SEGMENT_POLYGON_EDGE)) continue;
+        if (!(rb.flags & BP_SEGMENT_POLYGON_EDGE)) return false;
         if (rb.box.x > pathHi.x + slack || rb.box.y > pathHi.y + slack || rb.box.z < pathLo.x - slack ||
             rb.box.w < pathLo.y - slack)
-            continue;
-        if (!filter_accepts(fi, make_uint2(rb.cat, rb.mask))) continue;
+            return false;
+        if (!filter_accepts(fi, make_uint2(rb.cat, rb.mask))) return false;
         const DSegment& sg = S.seg[W.soff + e];
         float2 edge = sub(sg.b, sg.a);
         float lsq = dot2(edge, edge);
-        if (!(lsq > 0.0f)) continue;
+        if (!(lsq > 0.0f)) return false;
         float2 outward = mul(dvd(f2(-edge.y, edge.x), sqrtf(lsq)), sg.outward);
-        float before = dot2(sub(start, sg.a), outward), after = dot2(sub(center, sg.a), outward);
-        if (!(before > 0.0f) || !(after <= 0.0f)) continue;
+        float before = dot2(sub(start, sg.a), outward);
+        after = dot2(sub(center, sg.a), outward);
+        if (!(before > 0.0f) || !(after <= 0.0f)) return false;
         float2 crossing = add(start, mul(sub(center, start), before / (before - after)));
         float along = dot2(sub(crossing, sg.a), edge) / lsq;
-        if (along < 0.0f || along > 1.0f) continue;
-        v.kind = BP_VIOLATION_EDGE_SIDE; v.a = S.id[g]; v.b = sg.owner; v.edge = sg.id; v.distance = after;
+        return !(along < 0.0f || along > 1.0f);
+    };
+    // the reported edge is the lowest segment index crossed
+    uint32_t crossed = 0xffffffffu;
+    float crossedAfter = 0.0f;
+    if (kTree) {
+        if (W.s)
+            tree_query(S, W,
+                       [&](float4 nb) {
+                           return !(nb.x > pathHi.x + slack || nb.y > pathHi.y + slack || nb.z < pathLo.x - slack ||
+                                    nb.w < pathLo.y - slack);
+                       },
+                       [&](uint32_t leaf) {
+                           float after;
+                           if (leaf >= W.s || leaf >= crossed) return;
+                           if (crossesEdge(leaf, after)) { crossed = leaf; crossedAfter = after; }
+                       });
+    } else {
+        for (uint32_t e = 0; e < W.s; ++e) {
+            float after;
+            if (crossesEdge(e, after)) { crossed = e; crossedAfter = after; break; }
+        }
+    }
+    if (crossed != 0xffffffffu) {
+        const DSegment& sg = S.seg[W.soff + crossed];
+        v.kind = BP_VIOLATION_EDGE_SIDE; v.a = S.id[g]; v.b = sg.owner; v.edge = sg.id; v.distance = crossedAfter;
         return true;
     }
     return false;
@@ -854,7 +993,7 @@ __device__ void assertion_grid(const DState& S, const DWorld& W, const Team& tea
 // moved since the build, so when every bubble is within margin + r/2 of its build position the pair passed the
 // candidate test (reach = r_i + r_j + m_i + m_j + sepTol). Truncated rows, joint exclusions, injected states and region
 // wraps void that argument and take the grid path.
-template <class Team>
+template <class Team, bool kTree>
 __device__ uint32_t assert_contacts(const DState& S, const DWorld& W, const Team& team, uint32_t* buckets, uint32_t* entries,
                                     uint32_t B, float cw, float fraction, bp_step_report* rep, bool rowsComplete) {
     uint32_t unsafe = (!rowsComplete || W.njEnt || (W.flags & BP_WORLD_INJECT_STATE)) ? 1u : 0u;
@@ -872,7 +1011,7 @@ __device__ uint32_t assert_contacts(const DState& S, const DWorld& W, const Team
     ValOwner first{__int_as_float(0x7f800000), 0xffffffffu};
     for (uint32_t i = team.rank(); i < W.n; i += team.size()) {
         Viol v;
-        if (assert_bubble(S, W, buckets, entries, B, fraction, i, fromCandidates, v)) {
+        if (assert_bubble<kTree>(S, W, buckets, entries, B, fraction, i, fromCandidates, v)) {
             first.v = 0.0f;
             first.o = i;
             mine = v;
@@ -1082,7 +1221,7 @@ template <class Team> __device__ void build_boxes(const DState& S, const DWorld&
 // ------------------------------------------------------------------------------------------------------------------
 // One complete step of one world (nativeBeginStep -> substep loop -> end of step)
 // ------------------------------------------------------------------------------------------------------------------
-template <class Team>
+template <class Team, bool kTreeCapable>
 __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint32_t* buckets, uint32_t* entries, uint32_t B,
                            uint32_t* ws, uint32_t wsWords) {
     const DWorld W = G.worlds[wi];
@@ -1129,6 +1268,8 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
     team.sync();
     build_boxes(S, W, team);
     const uint32_t live = team.sum(liveLocal);
+    // the tree-capable instantiation carries the LBVH code; a kernel for worlds without trees is compiled without it
+    const bool useTree = kTreeCapable && W.tree && build_rigid_tree(S, W, wi, team);
     Ctl c;
     c.timeX = W.dt;
     c.timeY = live == 0u ? W.dt : 0.0f;
@@ -1140,7 +1281,8 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
     float* history = S.history + (uint64_t)wi * kFrameLimit;
     uint32_t buildOverflow = 0, overflowMax = 0, maxPer = 0, rebuilds = 0;
     BP_PHASE(0);
-    float cw = broadphase(S, W, c, team, buckets, entries, B, buildOverflow, maxPer, wi);
+    float cw = useTree ? broadphase<Team, true>(S, W, c, team, buckets, entries, B, buildOverflow, maxPer, wi)
+                       : broadphase<Team, false>(S, W, c, team, buckets, entries, B, buildOverflow, maxPer, wi);
     BP_PHASE(1);
     ValOwner w2, mg;
     initial_forces(S, W, c, team, w2, mg);
@@ -1158,7 +1300,8 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
             c.cZ = 0u;
             overflowMax = max(overflowMax, buildOverflow);
             ++rebuilds;
-            cw = broadphase(S, W, c, team, buckets, entries, B, buildOverflow, maxPer, wi);
+            cw = useTree ? broadphase<Team, true>(S, W, c, team, buckets, entries, B, buildOverflow, maxPer, wi)
+                         : broadphase<Team, false>(S, W, c, team, buckets, entries, B, buildOverflow, maxPer, wi);
             initial_forces(S, W, c, team, w2, mg);
             BP_PHASE(1);
             continue;
@@ -1180,9 +1323,11 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
                     if (S.id[W.boff + i] == W.injectObject) S.pos[W.boff + i] = W.injectPos;
             team.sync();
         }
-        if ((W.flags & BP_WORLD_ASSERT_EVERY_SUBSTEP) && !violated)
-            violated = assert_contacts(S, W, team, buckets, entries, B, cw, c.timeX > 0.0f ? clampf(c.timeY / c.timeX, 0.0f, 1.0f) : 1.0f, rep,
-                                       buildOverflow == 0u);
+        if ((W.flags & BP_WORLD_ASSERT_EVERY_SUBSTEP) && !violated) {
+            const float at = c.timeX > 0.0f ? clampf(c.timeY / c.timeX, 0.0f, 1.0f) : 1.0f;
+            violated = useTree ? assert_contacts<Team, true>(S, W, team, buckets, entries, B, cw, at, rep, buildOverflow == 0u)
+                               : assert_contacts<Team, false>(S, W, team, buckets, entries, B, cw, at, rep, buildOverflow == 0u);
+        }
     }
     overflowMax = max(overflowMax, buildOverflow);
     BP_PHASE(5);
@@ -1248,7 +1393,8 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
     const uint32_t contactDropped = nf[1];
     BP_PHASE(8);
     if (!violated && stepDone && !(W.flags & BP_WORLD_NO_END_ASSERTION))
-        violated = assert_contacts(S, W, team, buckets, entries, B, cw, 1.0f, rep, buildOverflow == 0u);
+        violated = useTree ? assert_contacts<Team, true>(S, W, team, buckets, entries, B, cw, 1.0f, rep, buildOverflow == 0u)
+                           : assert_contacts<Team, false>(S, W, team, buckets, entries, B, cw, 1.0f, rep, buildOverflow == 0u);
     BP_PHASE(9);
     int status = BP_OK;
     if (c.cW != 0u) status = BP_E_SUBSTEP_LIMIT;
@@ -1342,7 +1488,7 @@ __host__ __device__ inline uint32_t round4(uint32_t v) { return (v + 3u) & ~3u; 
 // Persistent step kernel: blocks pull worlds from two queues. CTA-team worlds (largest first) are stepped by a whole
 // block; then every warp pulls warp-team worlds (small worlds, one warp each). Dynamic shared memory holds the hash
 // grid: for a CTA world B bucket ends then its entries; for a warp world a slice per warp of the same layout.
-template <int kThreads>
+template <int kThreads, bool kTree>
 __global__ void __launch_bounds__(kThreads, 2) persistent_step_kernel(DState S, QueueArgs q) {
     __shared__ BlockScratch sh;
     __shared__ uint32_t next;
@@ -1355,7 +1501,7 @@ __global__ void __launch_bounds__(kThreads, 2) persistent_step_kernel(DState S, 
         const uint32_t slot = next;
         __syncthreads();
         if (slot >= nCta) break;
-        world_step(S, q.ctaList[slot], cta, g_dynamic_smem, g_dynamic_smem + q.ctaB, q.ctaB,
+        world_step<CtaTeam, kTree>(S, q.ctaList[slot], cta, g_dynamic_smem, g_dynamic_smem + q.ctaB, q.ctaB,
                    q.ctaWsWords ? g_dynamic_smem + round4(q.ctaB + q.ctaMaxN) : nullptr, q.ctaWsWords);
         __syncthreads();
     }
@@ -1368,7 +1514,7 @@ __global__ void __launch_bounds__(kThreads, 2) persistent_step_kernel(DState S, 
         if (lane == 0) slot = atomicAdd(q.queue + 1, 1u);
         slot = __shfl_sync(0xffffffffu, slot, 0);
         if (slot >= nWarp) break;
-        world_step(S, q.warpList[slot], wt, mine, mine + q.warpB, q.warpB,
+        world_step<WarpTeam, kTree>(S, q.warpList[slot], wt, mine, mine + q.warpB, q.warpB,
                    q.warpWsWords ? mine + round4(q.warpB + q.warpMaxN) : nullptr, q.warpWsWords);
         __syncwarp();
     }
@@ -1378,7 +1524,7 @@ __global__ void __launch_bounds__(kThreads, 2) persistent_step_kernel(DState S, 
 __global__ void __launch_bounds__(512) large_step_kernel(DState S, uint32_t wi, uint32_t B) {
     __shared__ BlockScratch sh;
     GridTeam team{&sh, S.barrier, S.errorFlag, S.gpv, S.gpo, nullptr, 0u, false};
-    world_step(S, wi, team, S.gbuckets, S.gentries, B, nullptr, 0u);
+    world_step<GridTeam, true>(S, wi, team, S.gbuckets, S.gentries, B, nullptr, 0u);
 }
 
 // Contact law known-answer kernel: mode 0 eps(q), 1 wall law, 2 pair law; 8 floats in / out per case.
@@ -1479,9 +1625,15 @@ cudaError_t launch_persistent(const DState& S, const QueueArgs& q, uint32_t thre
     if (smem > 200u * 1024u) return cudaErrorInvalidValue;  // schedule() keeps every configuration below this
     cudaError_t err = cudaMemsetAsync(q.queue, 0, 2 * sizeof(uint32_t), stream);
     if (err) return err;
-    if (threads <= 128u) persistent_step_kernel<128><<<blocks, threads, smem, stream>>>(S, q);
-    else if (threads <= 256u) persistent_step_kernel<256><<<blocks, threads, smem, stream>>>(S, q);
-    else persistent_step_kernel<512><<<blocks, threads, smem, stream>>>(S, q);
+    if (q.tree) {
+        if (threads <= 128u) persistent_step_kernel<128, true><<<blocks, threads, smem, stream>>>(S, q);
+        else if (threads <= 256u) persistent_step_kernel<256, true><<<blocks, threads, smem, stream>>>(S, q);
+        else persistent_step_kernel<512, true><<<blocks, threads, smem, stream>>>(S, q);
+    } else {
+        if (threads <= 128u) persistent_step_kernel<128, false><<<blocks, threads, smem, stream>>>(S, q);
+        else if (threads <= 256u) persistent_step_kernel<256, false><<<blocks, threads, smem, stream>>>(S, q);
+        else persistent_step_kernel<512, false><<<blocks, threads, smem, stream>>>(S, q);
+    }
     return cudaGetLastError();
 }
 
@@ -1491,9 +1643,15 @@ uint32_t persistent_blocks(const QueueArgs& q, uint32_t threads) {
     cudaGetDevice(&device);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     size_t smem = persistent_smem(q, threads);
-    if (threads <= 128u) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, persistent_step_kernel<128>, threads, smem);
-    else if (threads <= 256u) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, persistent_step_kernel<256>, threads, smem);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, persistent_step_kernel<512>, threads, smem);
+    if (q.tree) {
+        if (threads <= 128u) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, persistent_step_kernel<128, true>, threads, smem);
+        else if (threads <= 256u) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, persistent_step_kernel<256, true>, threads, smem);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, persistent_step_kernel<512, true>, threads, smem);
+    } else {
+        if (threads <= 128u) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, persistent_step_kernel<128, false>, threads, smem);
+        else if (threads <= 256u) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, persistent_step_kernel<256, false>, threads, smem);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, persistent_step_kernel<512, false>, threads, smem);
+    }
     return (uint32_t)(sms * (perSm > 0 ? perSm : 1));
 }
 
@@ -1502,9 +1660,12 @@ void prepare_kernels() {
     static bool done = false;
     if (done) return;
     done = true;
-    cudaFuncSetAttribute(persistent_step_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(persistent_step_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(persistent_step_kernel<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(persistent_step_kernel<128, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(persistent_step_kernel<256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(persistent_step_kernel<512, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(persistent_step_kernel<128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(persistent_step_kernel<256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(persistent_step_kernel<512, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(schedule_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 16384 * 8);
 }
 
@@ -1651,7 +1812,7 @@ __global__ void __launch_bounds__(256) noalloc_step_kernel(DState S, DWorld W, b
             reports[s] = zero;
         }
         __syncthreads();
-        world_step(step, 0u, team, buckets, entries, B, ws, wsWords);
+        world_step<CtaTeam, false>(step, 0u, team, buckets, entries, B, ws, wsWords);
         __syncthreads();
         if (S.failed[0]) {  // a failed step publishes nothing and stops the world: later steps report it
             for (uint32_t q = s + 1 + r; q < steps; q += T) {

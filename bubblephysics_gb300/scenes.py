@@ -214,7 +214,7 @@ def _body_geometry(kind, rng, half):
 
 
 def add_bodies(rng, count, region, size_range, first_id, kinematic_fraction=0.25, speed=5.0, spin=0.2,
-               horizon=5.0, clearance=80.0, gap=50.0):
+               horizon=5.0, clearance=80.0, gap=50.0, tries=40):
     """Random static / kinematic bodies (1/3 polygons, 1/3 circles, 1/3 capsules). Static polygons become one-sided
     edges (like NativePublicWorld.step); static circles / capsules and every kinematic body are obstacle bodies.
     Every body keeps `gap` (more than a bubble diameter) from other bodies and from the region edge, so no bubble is
@@ -222,7 +222,14 @@ def add_bodies(rng, count, region, size_range, first_id, kinematic_fraction=0.25
     closes a gap onto a bubble (a squeeze a world cannot survive). A body without such room is left out."""
     x0, y0, x1, y1 = region
     bodies, verts, tris, segs = [], [], [], []
-    placed = []  # (position, bounding radius, keep-out radius)
+    placed_pos = np.zeros((count, 2))  # placed bodies: position, bounding radius, keep-out radius
+    placed_bound = np.zeros(count)
+    placed_keep = np.zeros(count)
+    nplaced = 0
+    # placed bodies by cell of a coarse grid: a candidate only needs the bodies within its largest keep-out reach
+    cell = 64.0
+    buckets: dict = {}
+    max_bound = max_keep = 0.0
     polygons = []  # world vertices of the static polygons
     vcount = tcount = 0
     seg_id = first_id * 16
@@ -233,16 +240,25 @@ def add_bodies(rng, count, region, size_range, first_id, kinematic_fraction=0.25
         kinematic = rng.uniform() < kinematic_fraction
         keep = bound + gap + (clearance + speed * math.sqrt(2.0) * horizon if kinematic else 0.0)
         pos = None
-        for _ in range(40):
+        for _ in range(tries):
             if x1 - x0 <= 2 * keep or y1 - y0 <= 2 * keep:
                 break
             cand = np.array([rng.uniform(x0 + keep, x1 - keep), rng.uniform(y0 + keep, y1 - keep)])
-            if all(np.hypot(*(cand - p)) >= max(keep + rb, kb + bound) for p, rb, kb in placed):
+            reach = max(keep + max_bound, max_keep + bound)
+            gx0, gx1 = int(math.floor((cand[0] - reach) / cell)), int(math.floor((cand[0] + reach) / cell))
+            gy0, gy1 = int(math.floor((cand[1] - reach) / cell)), int(math.floor((cand[1] + reach) / cell))
+            near = [j for gx in range(gx0, gx1 + 1) for gy in range(gy0, gy1 + 1) for j in buckets.get((gx, gy), ())]
+            near = np.array(near, np.int64)
+            d = np.hypot(placed_pos[near, 0] - cand[0], placed_pos[near, 1] - cand[1])
+            if np.all(d >= np.maximum(keep + placed_bound[near], placed_keep[near] + bound)):
                 pos = cand
                 break
         if pos is None:
             continue
-        placed.append((pos, bound, keep))
+        placed_pos[nplaced], placed_bound[nplaced], placed_keep[nplaced] = pos, bound, keep
+        buckets.setdefault((int(math.floor(pos[0] / cell)), int(math.floor(pos[1] / cell))), []).append(nplaced)
+        max_bound, max_keep = max(max_bound, bound), max(max_keep, keep)
+        nplaced += 1
         angle = float(rng.uniform(0, 2 * math.pi))
         bid = first_id + k
         if kind == N.BODY_POLYGON and not kinematic:
@@ -286,11 +302,24 @@ def add_bodies(rng, count, region, size_range, first_id, kinematic_fraction=0.25
 
 
 def _clear_of_bodies(centers, radii, bodies, polygons):
-    """Bubbles that start clear of every obstacle body and static polygon (more than r + 1 away)."""
+    """Bubbles that start clear of every obstacle body and static polygon (more than r + 1 away). Each obstacle only
+    tests the centres inside a box that holds every centre it could reject."""
     keep = np.ones(centers.shape[0], bool)
+    if centers.shape[0] == 0:
+        return keep
+    rmax = float(radii.max()) + 1.0
+    order = np.argsort(centers[:, 0], kind="stable")
+    xs = centers[order, 0]
+
+    def near(x, y, reach):
+        lo, hi = np.searchsorted(xs, x - reach, "left"), np.searchsorted(xs, x + reach, "right")
+        idx = order[lo:hi]
+        return idx[np.abs(centers[idx, 1] - y) <= reach]
+
     for b in bodies:
-        d = np.hypot(centers[:, 0] - b["position"][0], centers[:, 1] - b["position"][1])
-        keep &= d > b["bounding_radius"] + radii + 1.0
+        idx = near(b["position"][0], b["position"][1], float(b["bounding_radius"]) + rmax)
+        d = np.hypot(centers[idx, 0] - b["position"][0], centers[idx, 1] - b["position"][1])
+        keep[idx] &= d > b["bounding_radius"] + radii[idx] + 1.0
     for poly in polygons:
         # convex polygon: the largest signed distance to its edge lines bounds the distance to it from below
         p = np.asarray(poly, np.float64)
@@ -299,9 +328,15 @@ def _clear_of_bodies(centers, radii, bodies, polygons):
         area = np.sum(p[:, 0] * q[:, 1] - q[:, 0] * p[:, 1])
         normal = np.stack([e[:, 1], -e[:, 0]], 1) * (1.0 if area > 0 else -1.0)
         normal /= np.linalg.norm(normal, axis=1, keepdims=True)
-        rel = centers[:, None, :] - p[None, :, :]
+        # a centre it rejects lies in the polygon offset by rmax: the hull of the vertices moved along the bisectors
+        nprev = np.roll(normal, 1, axis=0)
+        corner = p + rmax * (normal + nprev) / (1.0 + (normal * nprev).sum(axis=1, keepdims=True))
+        lo, hi = corner.min(axis=0) - 1.0, corner.max(axis=0) + 1.0
+        centre, half = (lo + hi) / 2.0, float((hi - lo).max()) / 2.0
+        idx = near(centre[0], centre[1], half)
+        rel = centers[idx, None, :] - p[None, :, :]
         signed = (rel * normal[None, :, :]).sum(-1).max(axis=1)
-        keep &= signed > radii + 1.0
+        keep[idx] &= signed > radii[idx] + 1.0
     return keep
 
 
@@ -329,6 +364,39 @@ def batched_world(rng, n_target: int, *, world_index: int = 0, max_bodies: int =
     segs = np.sort(segs, order="id")
     return WorldSpec(bubbles=b, segments=segs, bodies=bodies, body_vertices=bverts, body_triangles=btris,
                      region=region, gravity=gravity, time_step=DT)
+
+
+def rigid_world(seed: int = 4, n: int = 16384, bodies: int = 4096, side: float = 4096.0,
+                size_range=(4.0, 48.0), kinematic_fraction: float = 0.25) -> WorldSpec:
+    """Rigid-heavy single world: `bodies` static or kinematic bodies (1/3 polygons, 1/3 circles, 1/3 capsules, extent
+    U[4,48], i.e. half-extent U[2,24]) and `n` bubbles (r ~ U[4,10], mass r^2/400, velocities N(0, 30^2)) in a
+    side x side walled region. Static polygons become one-sided edges, so the world has thousands of segments and
+    bodies: the rigid candidates go through the LBVH. Bodies keep 10 units from each other (18 + their travel when
+    kinematic, drive speed <= 2 over 5 s); bubbles sit on a jittered grid in the free space."""
+    rng = np.random.default_rng(seed)
+    region = (0.0, 0.0, side, side)
+    half = (size_range[0] / 2.0, size_range[1] / 2.0)
+    body_arr, bverts, btris, bsegs, polygons = add_bodies(rng, bodies, region, half, first_id=3_000_000,
+                                                          kinematic_fraction=kinematic_fraction, speed=2.0, spin=0.1,
+                                                          horizon=5.0, clearance=8.0, gap=10.0, tries=1000)
+    cols = int(math.ceil(math.sqrt(2.0 * n)))
+    spacing = side / cols
+    ij = np.stack(np.divmod(np.arange(cols * cols), cols), axis=1)[:, ::-1].astype(np.float64)
+    centers = (ij + 0.5) * spacing + rng.uniform(-0.1, 0.1, (cols * cols, 2)) * spacing
+    radii = rng.uniform(4.0, 10.0, cols * cols)
+    inside = (centers.min(axis=1) > radii + 1.0) & (centers.max(axis=1) < side - radii - 1.0)
+    keep = inside & _clear_of_bodies(centers, radii, body_arr, polygons)
+    idx = np.flatnonzero(keep)
+    idx = np.sort(rng.choice(idx, size=min(n, idx.size), replace=False))
+    centers, radii = centers[idx], radii[idx]
+    vel = rng.normal(0.0, 30.0, (idx.size, 2))
+    b = make_bubbles(centers, radii, velocities=vel, masses=radii * radii / 400.0, stiffness=K_C, damping=0.0,
+                     flags=N.BUBBLE_FORCE_DRIVEN | N.BUBBLE_ENABLED)
+    walls = wall_segments(region)
+    segs = np.concatenate([walls, bsegs]) if bsegs.size else walls
+    segs = np.sort(segs, order="id")
+    return WorldSpec(bubbles=b, segments=segs, bodies=body_arr, body_vertices=bverts, body_triangles=btris,
+                     region=region, time_step=DT)
 
 
 def batched_worlds(count: int = 4096, seed: int = 3, n_min: int = 16, n_max: int = 1024, max_bodies: int = 32,

@@ -129,6 +129,10 @@ class World:
     def substeps(self) -> np.ndarray:
         return self._read(self.lib.bp_world_read_substeps, np.float32, "bp_world_read_substeps")
 
+    def rigid_keys(self) -> np.ndarray:
+        """Sorted LBVH keys (Morton code << 32 | leaf) of the last step; empty when the step used no tree."""
+        return self._read(self.lib.bp_world_read_rigid_keys, np.uint64, "bp_world_read_rigid_keys")
+
 
 class Batch:
     """Many independent worlds stepped together: one fused launch per size class and step (or, with

@@ -176,7 +176,9 @@ enum {
     BP_WORLD_ASSERT_EVERY_SUBSTEP = 4u,/* assertEverySubstep */
     BP_WORLD_INJECT_STATE = 8u,        /* injectedSubstepState (diagnostic, host-chosen position) */
     BP_WORLD_NO_END_ASSERTION = 16u,   /* skip the end-of-step contact assertion (it is on by default) */
-    BP_WORLD_FORCE_MULTI_CTA = 32u     /* forceMultipleDispatches: step on the whole-GPU path even when small */
+    BP_WORLD_FORCE_MULTI_CTA = 32u,    /* forceMultipleDispatches: step on the whole-GPU path even when small */
+    BP_WORLD_RIGID_TREE = 64u,         /* find rigid candidates through the LBVH whatever the world's size */
+    BP_WORLD_NO_RIGID_TREE = 128u      /* find rigid candidates by brute force whatever the world's size */
 };
 
 /* Per-world configuration (NativeSolverConfiguration + NativeMetalConfiguration). 64 bytes. */
@@ -301,6 +303,12 @@ int bp_world_read_candidates(bp_world* world, bp_candidate_key* out, uint32_t ca
 int bp_world_read_cells(bp_world* world, int64_t* out_xy, uint32_t capacity, uint32_t* count);
 /* h of every substep of the last step (stepHistory, NativeForceKernels:730). */
 int bp_world_read_substeps(bp_world* world, float* out, uint32_t capacity, uint32_t* count);
+/* Sorted LBVH keys of the last step: (Morton code << 32) | leaf, leaves numbered segments first, then bodies; the
+ * Morton code interleaves 15-bit quantized centres of the leaf boxes (x in the even bits) over the box of all centres.
+ * Replaces the brute-force loops of nativeEmitBodyCandidates (NativeGeometryKernels:350-415) and the segment rule of
+ * nativeFinishBubbleRow (NativeGeometryKernels:279-290) with a tree; *count = 0 when the last step used none
+ * (fewer leaves than the automatic threshold, BP_WORLD_NO_RIGID_TREE, or a non-finite leaf box). */
+int bp_world_read_rigid_keys(bp_world* world, uint64_t* out, uint32_t capacity, uint32_t* count);
 
 /* ---- batch of independent worlds (one fused launch per step for all worlds) ----------------------------------- */
 

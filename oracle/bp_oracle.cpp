@@ -1348,6 +1348,60 @@ template <typename T> uint32_t candidate_keys(const World<T>& w, bp_candidate_ke
 // ---------------------------------------------------------------------------------------------------------------
 // C entry points of the oracle (loaded by tests and by bench.py's CPU legs through ctypes)
 // ---------------------------------------------------------------------------------------------------------------
+// ---------------------------------------------------------------------------------------------------------------
+// LBVH keys of the rigid leaves for the step just taken. The reference has no tree (its rigid candidates are brute
+// force, NGK:279-290 and NGK:350-415), so this restates the key rule of the CUDA path, in float, to check it bit for
+// bit: leaves are the segments then the bodies; a leaf box is the segment's [min(a,b), max(a,b)] or the body's swept
+// box [min(pos, prev) - R, max(pos, prev) + R]; centre = (lo + hi) * 0.5; q = trunc(clamp((c - min c) * (32767 /
+// extent), 0, 32767)) per axis (scale 0 for a zero extent); code = q.x in the even bits, q.y in the odd bits; key =
+// code << 32 | leaf, sorted ascending. No keys when a leaf box is not finite.
+// ---------------------------------------------------------------------------------------------------------------
+static uint32_t spread_bits15(uint32_t v) {
+    v &= 0x7fffu;
+    v = (v | (v << 8)) & 0x00ff00ffu;
+    v = (v | (v << 4)) & 0x0f0f0f0fu;
+    v = (v | (v << 2)) & 0x33333333u;
+    v = (v | (v << 1)) & 0x55555555u;
+    return v;
+}
+
+template <typename T> std::vector<uint64_t> rigid_keys(const World<T>& w) {
+    struct Box { float lx, ly, hx, hy; };
+    std::vector<Box> boxes;
+    for (uint32_t j = 0; j < w.s; ++j) {
+        float ax = (float)w.sa[j].x, ay = (float)w.sa[j].y, bx = (float)w.sb[j].x, by = (float)w.sb[j].y;
+        boxes.push_back({std::fmin(ax, bx), std::fmin(ay, by), std::fmax(ax, bx), std::fmax(ay, by)});
+    }
+    for (const Body<T>& b : w.bodies) {
+        float r = (float)b.radius;
+        float px = (float)b.pos.x, py = (float)b.pos.y, qx = (float)b.prev.x, qy = (float)b.prev.y;
+        boxes.push_back({std::fmin(px, qx) - r, std::fmin(py, qy) - r, std::fmax(px, qx) + r, std::fmax(py, qy) + r});
+    }
+    std::vector<uint64_t> keys;
+    if (boxes.empty()) return keys;
+    float lox = 0, loy = 0, hix = 0, hiy = 0;
+    for (size_t p = 0; p < boxes.size(); ++p) {
+        const Box& b = boxes[p];
+        if (!std::isfinite(b.lx) || !std::isfinite(b.ly) || !std::isfinite(b.hx) || !std::isfinite(b.hy)) return {};
+        float cx = (b.lx + b.hx) * 0.5f, cy = (b.ly + b.hy) * 0.5f;
+        if (p == 0) { lox = hix = cx; loy = hiy = cy; continue; }
+        lox = std::fmin(lox, cx); hix = std::fmax(hix, cx);
+        loy = std::fmin(loy, cy); hiy = std::fmax(hiy, cy);
+    }
+    float ex = hix - lox, ey = hiy - loy;
+    float sx = ex > 0.0f ? 32767.0f / ex : 0.0f, sy = ey > 0.0f ? 32767.0f / ey : 0.0f;
+    for (size_t p = 0; p < boxes.size(); ++p) {
+        const Box& b = boxes[p];
+        float cx = (b.lx + b.hx) * 0.5f, cy = (b.ly + b.hy) * 0.5f;
+        uint32_t qx = (uint32_t)std::fmin(std::fmax((cx - lox) * sx, 0.0f), 32767.0f);
+        uint32_t qy = (uint32_t)std::fmin(std::fmax((cy - loy) * sy, 0.0f), 32767.0f);
+        uint32_t code = spread_bits15(qx) | (spread_bits15(qy) << 1);
+        keys.push_back(((uint64_t)code << 32) | (uint64_t)p);
+    }
+    std::sort(keys.begin(), keys.end());
+    return keys;
+}
+
 extern "C" {
 
 int bpo_world_create(const bp_world_desc* desc, const bp_world_input* input, int precision, void** out) {
@@ -1404,6 +1458,14 @@ int bpo_worlds_step(void** handles, uint32_t count, uint32_t steps, int threads,
     }
     if (bubble_substeps) *bubble_substeps = total;
     return BP_OK;
+}
+
+// Sorted LBVH keys of the rigid leaves for the last step (see rigid_keys); returns the number of keys.
+uint32_t bpo_world_rigid_keys(void* handle, uint64_t* out, uint32_t capacity) {
+    Handle* h = (Handle*)handle;
+    std::vector<uint64_t> keys = h->precision == 64 ? rigid_keys(*(World<double>*)h->world) : rigid_keys(*(World<float>*)h->world);
+    for (uint32_t i = 0; i < keys.size() && i < capacity; ++i) out[i] = keys[i];
+    return (uint32_t)keys.size();
 }
 
 int bpo_set_threads(int threads) {

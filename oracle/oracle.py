@@ -47,6 +47,7 @@ def library() -> C.CDLL:
             "bpo_world_read_contacts": (C.c_int, [P, P, C.c_uint32, C.POINTER(C.c_uint32)]),
             "bpo_world_read_candidates": (C.c_int, [P, P, C.c_uint32, C.POINTER(C.c_uint32)]),
             "bpo_world_read_cells": (C.c_int, [P, P, C.c_uint32, C.POINTER(C.c_uint32)]),
+            "bpo_world_rigid_keys": (C.c_uint32, [P, P, C.c_uint32]),
             "bpo_world_read_substeps": (C.c_int, [P, P, C.c_uint32, C.POINTER(C.c_uint32)]),
             "bpo_contact_law": (C.c_int, [C.c_uint32, C.c_int, P, P, C.c_uint32]),
         }
@@ -122,6 +123,14 @@ class OracleWorld:
 
     def substeps(self) -> np.ndarray:
         return self._read(self.lib.bpo_world_read_substeps, np.float64)
+
+    def rigid_keys(self) -> np.ndarray:
+        """Sorted LBVH keys of the rigid leaves for the last step (the CUDA path's key rule restated in float)."""
+        count = self.lib.bpo_world_rigid_keys(self.handle, None, 0)
+        out = np.zeros(count, np.uint64)
+        if count:
+            self.lib.bpo_world_rigid_keys(self.handle, C.c_void_p(out.ctypes.data), count)
+        return out
 
 
 def step_worlds(worlds: list[OracleWorld], steps: int, threads: int = 0) -> int:
