@@ -211,6 +211,96 @@ def single_worlds(ctx, steps: int) -> dict:
     return out
 
 
+def log(message: str):
+    """Progress of the run on stderr (the JSON line alone goes to stdout)."""
+    print(f"[bench {time.strftime('%H:%M:%S')}] {message}", file=sys.stderr, flush=True)
+
+
+def percentile(values, q):
+    v = sorted(values)
+    return v[min(len(v) - 1, max(0, int(math.ceil(q * len(v))) - 1))] if v else None
+
+
+def serve_stream(server, arrivals, targets) -> dict:
+    """Submits request i when its arrival time has passed, runs the loop in between, then drains. Latency of a
+    request = its completion time - its scheduled arrival time (submission lag included)."""
+    first = None
+    comps = []
+    t0 = server.clock()
+    i, count = 0, len(arrivals)
+    while i < count:
+        now = server.clock() - t0
+        while i < count and arrivals[i] <= now:
+            rid = server.submit(int(targets[i]), 1)
+            first = rid if first is None else first
+            i += 1
+        if server.progress(0):
+            comps.append(server.poll())
+    comps.append(server.drain(wait_us=50))
+    t1 = server.clock()
+    done = np.concatenate(comps)
+    idx = (done["request_id"] - first).astype(np.int64)
+    latency = (done["completed_s"] - (t0 + arrivals[idx])) * 1000.0
+    return {"latency_ms": latency, "wall_s": t1 - t0, "statuses": sorted(set(done["status"].tolist()))}
+
+
+def serving(ctx, args) -> dict:
+    """The serving stream: a pool of worlds (N ~ LogUniform[16,4096], batched-world distributions) admitted under a
+    120 GB device budget; requests of one step for uniformly random worlds arrive as a Poisson stream. Every world is
+    stepped once before the timed stream so the pool starts resident. Measured twice: batched continuous serving and
+    the plain per-world path (one launch per world step); plus the saturated throughput of each (all requests at
+    once)."""
+    from bubblephysics_gb300 import scenes
+    from bubblephysics_gb300.solver import Server
+    log("serving: generating worlds")
+    worlds = scenes.serving_worlds(args.serve_worlds, seed=5, processes=min(os.cpu_count() or 1, 16))
+    bubbles = np.array([w.bubble_count for w in worlds], np.int64)
+    rng = np.random.default_rng(11)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, args.serve_requests))
+    targets = rng.integers(0, len(worlds), args.serve_requests)
+    out = {"workload": f"{len(worlds)} resident worlds, N~LogUniform[16,4096], {args.serve_requests} one-step "
+                       f"requests, Poisson arrivals at {args.serve_rate:.0f}/s, uniform world choice, 120 GB budget",
+           "worlds": len(worlds), "bubbles": int(bubbles.sum()), "requests": args.serve_requests,
+           "arrival_rate_per_s": args.serve_rate}
+    for mode in ("batched", "per_world"):
+        log(f"serving: {mode} pool")
+        server = Server(len(worlds), ctx, hbm_budget_bytes=120 << 30, per_world=(mode == "per_world"))
+        for spec in worlds:
+            server.add_world(spec)
+        for w in range(len(worlds)):
+            server.submit(w, 1)
+        warm = server.drain()
+        st0 = server.stats()
+        log(f"serving: {mode} stream")
+        stream = serve_stream(server, arrivals, targets)
+        st1 = server.stats()
+        lat = stream["latency_ms"].tolist()
+        subs = st1["bubble_substeps"] - st0["bubble_substeps"]
+        # saturated: every request of the stream at once
+        t0 = server.clock()
+        for w in targets:
+            server.submit(int(w), 1)
+        server.drain(wait_us=50)
+        t1 = server.clock()
+        st2 = server.stats()
+        sat = (st2["bubble_substeps"] - st1["bubble_substeps"]) / (t1 - t0)
+        out[mode] = {"latency_ms": {"p50": percentile(lat, 0.50), "p99": percentile(lat, 0.99), "max": max(lat)},
+                     "stream_bubble_substeps_per_s": subs / stream["wall_s"], "stream_wall_s": stream["wall_s"],
+                     "saturated_bubble_substeps_per_s": sat, "saturated_wall_s": t1 - t0,
+                     "requests_per_s_saturated": len(targets) / (t1 - t0),
+                     "batches": st1["batches"] - st0["batches"],
+                     "mean_worlds_per_batch": (st1["batched_worlds"] - st0["batched_worlds"]) /
+                                              max(st1["batches"] - st0["batches"], 1),
+                     "resident_worlds": st1["resident"], "resident_gb": st1["resident_bytes"] / 1e9,
+                     "evictions": st2["evictions"], "statuses": stream["statuses"],
+                     "warmup_statuses": sorted(set(warm["status"].tolist()))}
+        server.close()
+    b, p = out["batched"], out["per_world"]
+    out["saturated_speedup_batched_vs_per_world"] = (b["saturated_bubble_substeps_per_s"] /
+                                                     p["saturated_bubble_substeps_per_s"])
+    return out
+
+
 def combine_ranks(device_s: float, bubble_substeps: float, dist=None) -> tuple[float, float]:
     """Whole-job timing over ranks: the slowest rank's device time and the sum of all ranks' bubble-substeps."""
     if dist is None:
@@ -306,6 +396,7 @@ def run_ours(args, rank, world_size, local_rank):
         return 0
 
     singles = single_worlds(ctx, args.single_steps) if args.single_steps > 0 else None
+    served = serving(ctx, args) if args.serve_requests > 0 else None
     peak, peak_kind = load_peak()
     achieved = alg_bytes / device_s / 1e9 if device_s > 0 else 0.0
     traffic = None
@@ -344,6 +435,7 @@ def run_ours(args, rank, world_size, local_rank):
         "clocks": clocks,
         "gpu_launches": gpu_launches,
         "single_worlds": singles,
+        "serving": served,
     }
     print(json.dumps(line), flush=True)
     if dist:
@@ -364,6 +456,9 @@ def main():
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--sample-worlds", type=int, default=1024)
     p.add_argument("--single-steps", type=int, default=10, help="timed steps of each single-world workload (0: skip)")
+    p.add_argument("--serve-worlds", type=int, default=8192)
+    p.add_argument("--serve-requests", type=int, default=20000, help="requests of the serving stream (0: skip)")
+    p.add_argument("--serve-rate", type=float, default=50000.0, help="Poisson arrival rate of the serving stream")
     p.add_argument("--no-autotune", action="store_true", help="keep the default schedule (profiling runs)")
     args = p.parse_args()
     args.warmup = max(args.warmup, 3)

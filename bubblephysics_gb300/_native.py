@@ -127,7 +127,28 @@ class BatchConfig(C.Structure):
                 ("reserved", C.c_uint32)]
 
 
-RECORD_SIZES = {Bubble: 80, Segment: 64, Body: 80, ForceField: 64, Band: 24, Motor: 24, WorldDesc: 64,
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_worlds", C.c_uint32), ("max_batch_worlds", C.c_uint32),
+                ("streams", C.c_uint32), ("threads_per_world", C.c_uint32), ("warp_world_max", C.c_uint32),
+                ("flags", C.c_uint32)]
+
+
+class ServerCompletion(C.Structure):
+    _fields_ = [("request_id", C.c_uint64), ("world", C.c_uint32), ("status", C.c_int32), ("steps", C.c_uint32),
+                ("substeps", C.c_uint32), ("submitted_s", C.c_double), ("completed_s", C.c_double),
+                ("report", StepReport)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("worlds", C.c_uint32), ("resident", C.c_uint32), ("resident_bytes", C.c_uint64),
+                ("hbm_budget_bytes", C.c_uint64), ("admissions", C.c_uint64), ("evictions", C.c_uint64),
+                ("batches", C.c_uint64), ("batched_worlds", C.c_uint64), ("requests_done", C.c_uint64),
+                ("bubble_substeps", C.c_uint64), ("device_ms", C.c_double)]
+
+
+SERVER_PER_WORLD = 1
+
+RECORD_SIZES = {ServerConfig: 32, ServerCompletion: 136, ServerStats: 80, Bubble: 80, Segment: 64, Body: 80, ForceField: 64, Band: 24, Motor: 24, WorldDesc: 64,
                 StepReport: 96, Contact: 64, CandidateKey: 24}
 for _t, _n in RECORD_SIZES.items():
     assert C.sizeof(_t) == _n, f"{_t.__name__} is {C.sizeof(_t)} bytes, the C ABI says {_n}"
@@ -208,6 +229,16 @@ _SIGNATURES = {
                                           C.POINTER(Segment), C.c_uint32, C.POINTER(C.c_uint32)]),
     "bp_device_contact_law": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint32]),
     "bp_world_step_noalloc": (C.c_int, [C.POINTER(WorldDesc), _P, C.c_uint32, _P, C.c_uint32, C.c_uint32, _P, _P]),
+    "bp_server_create": (C.c_int, [_P, C.POINTER(ServerConfig), C.POINTER(_P)]),
+    "bp_server_destroy": (C.c_int, [_P]),
+    "bp_server_add_world": (C.c_int, [_P, C.POINTER(WorldDesc), C.POINTER(WorldInput), C.POINTER(C.c_uint32)]),
+    "bp_server_submit": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint64)]),
+    "bp_server_progress": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_uint32)]),
+    "bp_server_poll": (C.c_int, [_P, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
+    "bp_server_pending": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    "bp_server_read_bubbles": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
+    "bp_server_read_stats": (C.c_int, [_P, C.POINTER(ServerStats)]),
+    "bp_server_clock": (C.c_double, []),
 }
 EXPORTED_SYMBOLS = tuple(_SIGNATURES)
 

@@ -16,26 +16,11 @@
 #include <string>
 #include <vector>
 
-#include "bp_device.cuh"
+#include "bp_host.h"
 
-namespace bp {
-cudaError_t launch_persistent(const DState& S, const QueueArgs& q, uint32_t threads, uint32_t blocks, cudaStream_t stream);
-uint32_t persistent_blocks(const QueueArgs& q, uint32_t threads);
-cudaError_t launch_schedule(const DState& S, const uint32_t* candidates, uint32_t count, uint32_t warpMax,
-                            uint32_t warpSubsteps, uint32_t* ctaList, uint32_t* warpList, uint32_t* queue, cudaStream_t stream);
-int large_max_blocks(int threads);
-cudaError_t launch_large(const DState& S, uint32_t wi, uint32_t B, int blocks, int threads, cudaStream_t stream);
-cudaError_t launch_contact_law(uint32_t mode, const float* in, float* out, uint32_t count, cudaStream_t stream);
-cudaError_t launch_accumulate(const bp_step_report* reports, bp_step_report* acc, const uint32_t* sizes,
-                              unsigned long long* total, uint32_t count, cudaStream_t stream);
-cudaError_t launch_write_state(const float4* in, float2* pos, float2* vel, float2* ppos, float2* pvel, uint64_t n,
-                               cudaStream_t stream);
-cudaError_t launch_read_state(float4* out, const float2* ppos, const float2* pvel, uint64_t n, cudaStream_t stream);
-void prepare_kernels();
-cudaError_t launch_sum(const uint32_t* v, uint64_t n, unsigned long long* total, cudaStream_t stream);
-}  // namespace bp
 
 using namespace bp;
+using namespace bp_host;
 
 static_assert(sizeof(bp_bubble) == 80, "bp_bubble layout");
 static_assert(sizeof(bp_segment) == 64, "bp_segment layout");
@@ -49,108 +34,8 @@ static_assert(sizeof(bp_candidate_key) == 24, "bp_candidate_key layout");
 static_assert(offsetof(bp_bubble, center) == 8 && offsetof(bp_bubble, flags) == 60, "bp_bubble offsets");
 static_assert(offsetof(bp_step_report, limiter_object) == 40, "bp_step_report offsets");
 
-namespace {
 
-constexpr uint32_t kCtaMaxBubbles = 4096;
-constexpr int kLargeThreads = 512;
-constexpr uint32_t kDefaultThreads = 256;
-constexpr uint32_t kDefaultWarpMax = 64;
-constexpr uint32_t kWarpSubsteps = 16;   // a world that took more substeps last step gets a whole block
-constexpr uint32_t kCtaWorkspaceCap = 80u * 1024u;   // shared-memory workspace of a block team (2 blocks per SM, L1 keeps ~90 KB)
-constexpr uint32_t kWarpWorkspaceCap = 10u * 1024u;  // per warp team
-constexpr uint32_t kMaxDynamicSmem = 200u * 1024u;   // per block, set on the kernels by prepare_kernels()
-constexpr uint32_t kTreeMinLeaves = 128;             // segments + bodies from which rigid candidates use the LBVH
 
-struct DeviceGuard {
-    int previous = -1;
-    explicit DeviceGuard(int device) {
-        cudaGetDevice(&previous);
-        if (previous != device) cudaSetDevice(device);
-    }
-    ~DeviceGuard() {
-        int now = -1;
-        cudaGetDevice(&now);
-        if (previous >= 0 && now != previous) cudaSetDevice(previous);
-    }
-};
-
-uint32_t next_pow2(uint32_t v) {
-    uint32_t p = 1;
-    while (p < v) p <<= 1;
-    return p;
-}
-uint32_t grid_buckets(uint32_t maxN) { return next_pow2(std::max<uint32_t>(2u * maxN, 32u)); }
-uint32_t round4(uint32_t v) { return (v + 3u) & ~3u; }
-
-}  // namespace
-
-struct bp_context {
-    int refs = 0;            // live worlds and batches that use this context
-    bool released = false;   // bp_context_destroy was called; freed when the last user goes
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t start = nullptr, stop = nullptr;
-    std::vector<cudaStream_t> side;
-    int sms = 0;
-};
-
-struct WorldSet {
-    bp_context* ctx = nullptr;
-    uint32_t nWorlds = 0;
-    uint32_t flags = 0;
-    uint32_t fixedThreads = 0;
-    std::vector<DWorld> hWorlds;
-    std::vector<bp_bubble> hBubbles;        // as uploaded (static fields for readback)
-    std::vector<int64_t> hSegIds, hBodyIds;
-    uint64_t totalBubbles = 0, totalRows = 0, totalBodyRows = 0, totalContacts = 0;
-    uint32_t totalSegments = 0, totalBodies = 0;
-    uint64_t totalTreeLeaves = 0;
-    DState S{};
-    DWorld* dWorlds = nullptr;
-    bp_step_report* dReports = nullptr;
-    bp_step_report* dAcc = nullptr;
-    uint32_t* dSizes = nullptr;
-    unsigned long long* dTotal = nullptr;
-    float4* dStaging = nullptr;
-    std::vector<void*> allocations;
-    // scheduling: worlds stepped by a block (CTA team) or by one warp (warp team), largest first
-    std::vector<uint32_t> ctaWorlds, warpWorlds;
-    uint32_t* dCtaList = nullptr;
-    uint32_t* dWarpList = nullptr;
-    uint32_t* dQueue = nullptr;
-    uint32_t* dQueueSingle = nullptr;       // queue of the one-world launches of the per-world path
-    uint32_t* dCandidates = nullptr;        // worlds of the persistent kernel (all but the large ones)
-    uint32_t nCandidates = 0;
-    uint32_t threads = kDefaultThreads;
-    bool staging = true;                    // keep worlds resident in shared memory during a step
-    uint32_t warpMax = kDefaultWarpMax;
-    uint32_t blocks = 0;
-    QueueArgs queue{};
-    std::vector<uint32_t> largeWorlds;
-    uint32_t largeB = 0, largeMaxN = 0;
-    int largeBlocks = 0;
-    uint32_t* dSingle = nullptr;            // world index list for per-world launches
-    cudaGraphExec_t graph = nullptr;
-    bool tuned = false;
-    bool inflight = false;
-    uint64_t bubbleSubsteps = 0, launches = 0;
-    std::vector<float> lastHistory;
-
-    ~WorldSet() {
-        if (graph) cudaGraphExecDestroy(graph);
-        for (void* p : allocations) cudaFree(p);
-    }
-    template <class T> T* alloc(uint64_t count, cudaError_t& err) {
-        if (err != cudaSuccess) return nullptr;
-        void* p = nullptr;
-        size_t bytes = std::max<uint64_t>(count, 1) * sizeof(T);
-        err = cudaMalloc(&p, bytes);
-        if (err != cudaSuccess) return nullptr;
-        allocations.push_back(p);
-        err = cudaMemsetAsync(p, 0, bytes, ctx->stream);
-        return (T*)p;
-    }
-};
 
 struct bp_world {
     WorldSet set;
@@ -159,18 +44,7 @@ struct bp_batch {
     WorldSet set;
 };
 
-namespace {
-
-int cuda_status(cudaError_t e) {
-    if (e == cudaSuccess) return BP_OK;
-    if (e == cudaErrorMemoryAllocation) return BP_E_ALLOC;
-    return BP_E_CUDA;
-}
-
-template <class T> cudaError_t upload(T* dst, const T* src, uint64_t count, cudaStream_t stream) {
-    if (count == 0) return cudaSuccess;
-    return cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyHostToDevice, stream);
-}
+namespace bp_host {
 
 int validate(const bp_world_desc& d, const bp_world_input& in) {
     if (!(d.time_step > 0.0f) || !std::isfinite(d.time_step)) return BP_E_INVALID;
@@ -523,6 +397,8 @@ int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc
 #endif
     if (err != cudaSuccess) return cuda_status(err);
 
+    if (ws.measureOnly) return BP_OK;
+
     std::vector<uint32_t> sizes(count), identity(count);
     for (uint32_t w = 0; w < count; ++w) { sizes[w] = ws.hWorlds[w].n; identity[w] = w; }
     err = upload(ws.dWorlds, ws.hWorlds.data(), count, st);
@@ -554,7 +430,7 @@ int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc
     if (!err) err = upload(dJr, jranges.data(), njr, st);
     if (!err) err = upload(dJp, jpartners.data(), njp, st);
     if (!err) err = cudaStreamSynchronize(st);
-    if (!err) err = schedule(ws, ws.threads, ws.warpMax);
+    if (!err && !ws.planOnly) err = schedule(ws, ws.threads, ws.warpMax);
     return cuda_status(err);
 }
 
@@ -597,17 +473,18 @@ cudaError_t launch_step(WorldSet& ws, bool perWorld, uint32_t only = 0xffffffffu
 }
 
 // Snapshot / restore of the dynamic state (for the autotuner's trial steps).
-struct Snapshot {
-    std::vector<std::pair<void*, size_t>> parts;
-    std::vector<void*> copies;
-};
-cudaError_t take_snapshot(WorldSet& ws, Snapshot& snap) {
+std::vector<std::pair<void*, size_t>> persistent_parts(WorldSet& ws) {
     DState& S = ws.S;
     uint64_t nb = ws.totalBubbles;
-    snap.parts = {{S.pos, nb * 8}, {S.start, nb * 8}, {S.vel, nb * 8}, {S.acc, nb * 8}, {S.rotw, nb * 8},
-                  {S.flags, nb * 4}, {S.result, nb * 4}, {S.pPos, nb * 8}, {S.pStart, nb * 8}, {S.pVel, nb * 8},
-                  {S.pRotw, nb * 8}, {S.pResult, nb * 4}, {S.pFlags, nb * 4}, {S.body, ws.totalBodies * sizeof(DBody)},
-                  {S.pBody, ws.totalBodies * sizeof(DBody)}, {S.failed, ws.nWorlds * 4ull}};
+    // order of PersistentPart
+    return {{S.pos, nb * 8}, {S.start, nb * 8}, {S.vel, nb * 8}, {S.acc, nb * 8}, {S.rotw, nb * 8},
+            {S.flags, nb * 4}, {S.result, nb * 4}, {S.pPos, nb * 8}, {S.pStart, nb * 8}, {S.pVel, nb * 8},
+            {S.pRotw, nb * 8}, {S.pResult, nb * 4}, {S.pFlags, nb * 4}, {S.body, ws.totalBodies * sizeof(DBody)},
+            {S.pBody, ws.totalBodies * sizeof(DBody)}, {S.failed, ws.nWorlds * 4ull}};
+}
+
+cudaError_t take_snapshot(WorldSet& ws, Snapshot& snap) {
+    snap.parts = persistent_parts(ws);
     cudaError_t err = cudaSuccess;
     for (auto& p : snap.parts) {
         void* c = nullptr;
@@ -789,7 +666,22 @@ int read_bubbles(WorldSet& ws, uint32_t world, bp_bubble* out, uint32_t capacity
     return BP_OK;
 }
 
-}  // namespace
+}  // namespace bp_host
+
+static void context_free(bp_context* c) {
+    DeviceGuard guard(c->device);
+    cudaStreamSynchronize(c->stream);
+    cudaEventDestroy(c->start);
+    cudaEventDestroy(c->stop);
+    cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+// The context lives until it is released and every world / batch created on it is destroyed, whatever the order of
+// the destroy calls.
+void bp_host::context_unref(bp_context* c) {
+    if (--c->refs == 0 && c->released) context_free(c);
+}
 
 // ================================================================================================================
 // C ABI
@@ -841,21 +733,6 @@ int bp_context_create(int device, uint32_t flags, bp_context** out) {
     prepare_kernels();
     *out = c;
     return BP_OK;
-}
-
-static void context_free(bp_context* c) {
-    DeviceGuard guard(c->device);
-    cudaStreamSynchronize(c->stream);
-    cudaEventDestroy(c->start);
-    cudaEventDestroy(c->stop);
-    cudaStreamDestroy(c->stream);
-    delete c;
-}
-
-// The context lives until it is released and every world / batch created on it is destroyed, whatever the order of
-// the destroy calls.
-static void context_unref(bp_context* c) {
-    if (--c->refs == 0 && c->released) context_free(c);
 }
 
 int bp_context_destroy(bp_context* c) {

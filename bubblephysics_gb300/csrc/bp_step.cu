@@ -1520,6 +1520,45 @@ __global__ void __launch_bounds__(kThreads, 2) persistent_step_kernel(DState S, 
     }
 }
 
+// Served step kernel: the same two queues over a batch of resident worlds that each keep their own device arrays.
+// Entry e of the batch is world 0 of the state `sets[entrySlot[e]]`; its report goes to reports[e].
+template <int kThreads, bool kTree>
+__global__ void __launch_bounds__(kThreads, 2) served_step_kernel(const DState* sets, const uint32_t* entrySlot,
+                                                                   bp_step_report* reports, QueueArgs q) {
+    __shared__ BlockScratch sh;
+    __shared__ uint32_t next;
+    CtaTeam cta{&sh};
+    for (;;) {
+        if (threadIdx.x == 0) next = atomicAdd(q.queue, 1u);
+        __syncthreads();
+        const uint32_t slot = next;
+        __syncthreads();
+        if (slot >= q.nCta) break;
+        const uint32_t e = q.ctaList[slot];
+        DState G = sets[entrySlot[e]];
+        G.reports = reports + e;
+        world_step<CtaTeam, kTree>(G, 0u, cta, g_dynamic_smem, g_dynamic_smem + q.ctaB, q.ctaB,
+                                   q.ctaWsWords ? g_dynamic_smem + round4(q.ctaB + q.ctaMaxN) : nullptr, q.ctaWsWords);
+        __syncthreads();
+    }
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t slice = round4(q.warpB + q.warpMaxN) + q.warpWsWords;
+    uint32_t* mine = g_dynamic_smem + warp * slice;
+    WarpTeam wt;
+    for (;;) {
+        uint32_t slot = 0;
+        if (lane == 0) slot = atomicAdd(q.queue + 1, 1u);
+        slot = __shfl_sync(0xffffffffu, slot, 0);
+        if (slot >= q.nWarp) break;
+        const uint32_t e = q.warpList[slot];
+        DState G = sets[entrySlot[e]];
+        G.reports = reports + e;
+        world_step<WarpTeam, kTree>(G, 0u, wt, mine, mine + q.warpB, q.warpB,
+                                    q.warpWsWords ? mine + round4(q.warpB + q.warpMaxN) : nullptr, q.warpWsWords);
+        __syncwarp();
+    }
+}
+
 // Cooperative launch: every block steps world `wi` together; the hash grid lives in global memory.
 __global__ void __launch_bounds__(512) large_step_kernel(DState S, uint32_t wi, uint32_t B) {
     __shared__ BlockScratch sh;
@@ -1637,6 +1676,25 @@ cudaError_t launch_persistent(const DState& S, const QueueArgs& q, uint32_t thre
     return cudaGetLastError();
 }
 
+cudaError_t launch_served(const DState* sets, const uint32_t* entrySlot, bp_step_report* reports, const QueueArgs& q,
+                          uint32_t threads, uint32_t blocks, cudaStream_t stream) {
+    if (q.nCta + q.nWarp == 0u) return cudaSuccess;
+    size_t smem = persistent_smem(q, threads);
+    if (smem > 200u * 1024u) return cudaErrorInvalidValue;
+    cudaError_t err = cudaMemsetAsync(q.queue, 0, 2 * sizeof(uint32_t), stream);
+    if (err) return err;
+    if (q.tree) {
+        if (threads <= 128u) served_step_kernel<128, true><<<blocks, threads, smem, stream>>>(sets, entrySlot, reports, q);
+        else if (threads <= 256u) served_step_kernel<256, true><<<blocks, threads, smem, stream>>>(sets, entrySlot, reports, q);
+        else served_step_kernel<512, true><<<blocks, threads, smem, stream>>>(sets, entrySlot, reports, q);
+    } else {
+        if (threads <= 128u) served_step_kernel<128, false><<<blocks, threads, smem, stream>>>(sets, entrySlot, reports, q);
+        else if (threads <= 256u) served_step_kernel<256, false><<<blocks, threads, smem, stream>>>(sets, entrySlot, reports, q);
+        else served_step_kernel<512, false><<<blocks, threads, smem, stream>>>(sets, entrySlot, reports, q);
+    }
+    return cudaGetLastError();
+}
+
 // Blocks of the persistent kernel that fit on the GPU at once (the grid size of a full launch).
 uint32_t persistent_blocks(const QueueArgs& q, uint32_t threads) {
     int device = 0, sms = 0, perSm = 0;
@@ -1666,6 +1724,12 @@ void prepare_kernels() {
     cudaFuncSetAttribute(persistent_step_kernel<128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(persistent_step_kernel<256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(persistent_step_kernel<512, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(served_step_kernel<128, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(served_step_kernel<256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(served_step_kernel<512, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(served_step_kernel<128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(served_step_kernel<256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(served_step_kernel<512, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(schedule_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 16384 * 8);
 }
 

@@ -244,11 +244,14 @@ def add_bodies(rng, count, region, size_range, first_id, kinematic_fraction=0.25
             if x1 - x0 <= 2 * keep or y1 - y0 <= 2 * keep:
                 break
             cand = np.array([rng.uniform(x0 + keep, x1 - keep), rng.uniform(y0 + keep, y1 - keep)])
-            reach = max(keep + max_bound, max_keep + bound)
-            gx0, gx1 = int(math.floor((cand[0] - reach) / cell)), int(math.floor((cand[0] + reach) / cell))
-            gy0, gy1 = int(math.floor((cand[1] - reach) / cell)), int(math.floor((cand[1] + reach) / cell))
-            near = [j for gx in range(gx0, gx1 + 1) for gy in range(gy0, gy1 + 1) for j in buckets.get((gx, gy), ())]
-            near = np.array(near, np.int64)
+            if nplaced < 256:
+                near = np.arange(nplaced)
+            else:
+                reach = max(keep + max_bound, max_keep + bound)
+                gx0, gx1 = int(math.floor((cand[0] - reach) / cell)), int(math.floor((cand[0] + reach) / cell))
+                gy0, gy1 = int(math.floor((cand[1] - reach) / cell)), int(math.floor((cand[1] + reach) / cell))
+                near = [j for gx in range(gx0, gx1 + 1) for gy in range(gy0, gy1 + 1) for j in buckets.get((gx, gy), ())]
+                near = np.array(near, np.int64)
             d = np.hypot(placed_pos[near, 0] - cand[0], placed_pos[near, 1] - cand[1])
             if np.all(d >= np.maximum(keep + placed_bound[near], placed_keep[near] + bound)):
                 pos = cand
@@ -397,6 +400,27 @@ def rigid_world(seed: int = 4, n: int = 16384, bodies: int = 4096, side: float =
     segs = np.sort(segs, order="id")
     return WorldSpec(bubbles=b, segments=segs, bodies=body_arr, body_vertices=bverts, body_triangles=btris,
                      region=region, time_step=DT)
+
+
+def serving_world(job) -> WorldSpec:
+    """World `w` of the serving pool: its own seeded stream, n ~ LogUniform[n_min, n_max], batched-world
+    distributions otherwise."""
+    seed, w, n_min, n_max = job
+    rng = np.random.default_rng([seed, w])
+    n = int(math.exp(rng.uniform(math.log(n_min), math.log(n_max))))
+    return batched_world(rng, n, world_index=w)
+
+
+def serving_worlds(count: int = 8192, seed: int = 5, n_min: int = 16, n_max: int = 4096, processes: int = 0):
+    """The serving pool: `count` worlds with bubble counts log-uniform in [n_min, n_max] (each world from its own seed,
+    so the pool can be generated in parallel; processes > 1 uses a spawned process pool)."""
+    jobs = [(seed, w, n_min, n_max) for w in range(count)]
+    if processes > 1 and count > 64:
+        import multiprocessing
+        from concurrent.futures import ProcessPoolExecutor
+        with ProcessPoolExecutor(processes, mp_context=multiprocessing.get_context("spawn")) as ex:
+            return list(ex.map(serving_world, jobs, chunksize=64))
+    return [serving_world(j) for j in jobs]
 
 
 def batched_worlds(count: int = 4096, seed: int = 3, n_min: int = 16, n_max: int = 1024, max_bodies: int = 32,

@@ -225,3 +225,104 @@ def static_polygon_edges(points, first_id: int, owner_id: int | None = None) -> 
                                         C.cast(out.ctypes.data, C.POINTER(N.Segment)), cap, C.byref(count)),
             "bp_static_polygon_edges")
     return out[:count.value]
+
+
+COMPLETION_DTYPE = np.dtype([("request_id", "<u8"), ("world", "<u4"), ("status", "<i4"), ("steps", "<u4"),
+                             ("substeps", "<u4"), ("submitted_s", "<f8"), ("completed_s", "<f8"),
+                             ("report", N.REPORT_DTYPE)])
+assert COMPLETION_DTYPE.itemsize == C.sizeof(N.ServerCompletion)
+
+
+class Server:
+    """Serving loop over resident worlds (bp_server): step requests for any registered world, batched continuously
+    onto the device under a device-memory budget, idle worlds evicted to pinned host memory in LRU order.
+    per_world=True serves every world step with its own launch, one at a time (the plain per-world path)."""
+
+    def __init__(self, max_worlds: int, context: Context | None = None, *, hbm_budget_bytes: int = 0,
+                 max_batch_worlds: int = 0, streams: int = 0, threads_per_world: int = 0, warp_world_max: int = 0,
+                 per_world: bool = False):
+        self.ctx = context or default_context()
+        self.lib = self.ctx.lib
+        cfg = N.ServerConfig()
+        cfg.hbm_budget_bytes = hbm_budget_bytes
+        cfg.max_worlds = max_worlds
+        cfg.max_batch_worlds = max_batch_worlds
+        cfg.streams = streams
+        cfg.threads_per_world = threads_per_world
+        cfg.warp_world_max = warp_world_max
+        cfg.flags = N.SERVER_PER_WORLD if per_world else 0
+        handle = C.c_void_p()
+        N.check(self.lib.bp_server_create(self.ctx.handle, C.byref(cfg), C.byref(handle)), "bp_server_create")
+        self.handle = handle
+        self.sizes: list[int] = []
+
+    def close(self):
+        if self.handle:
+            self.lib.bp_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_world(self, spec: WorldSpec) -> int:
+        packed = PackedInput(spec)
+        index = C.c_uint32()
+        N.check(self.lib.bp_server_add_world(self.handle, C.byref(packed.desc), C.byref(packed.input), C.byref(index)),
+                "bp_server_add_world")
+        self.sizes.append(spec.bubble_count)
+        return index.value
+
+    def submit(self, world: int, steps: int = 1) -> int:
+        rid = C.c_uint64()
+        N.check(self.lib.bp_server_submit(self.handle, world, steps, C.byref(rid)), "bp_server_submit")
+        return rid.value
+
+    def progress(self, wait_us: int = 0) -> int:
+        done = C.c_uint32()
+        N.check(self.lib.bp_server_progress(self.handle, wait_us, C.byref(done)), "bp_server_progress")
+        return done.value
+
+    def poll(self) -> np.ndarray:
+        """Every finished request not taken yet, oldest first."""
+        count = C.c_uint32()
+        N.check(self.lib.bp_server_poll(self.handle, None, 0, C.byref(count)), "bp_server_poll")
+        out = np.zeros(count.value, COMPLETION_DTYPE)
+        if count.value:
+            N.check(self.lib.bp_server_poll(self.handle, C.c_void_p(out.ctypes.data), count.value, C.byref(count)),
+                    "bp_server_poll")
+        return out[: count.value]
+
+    def pending(self) -> tuple[int, int]:
+        waiting, inflight = C.c_uint32(), C.c_uint32()
+        N.check(self.lib.bp_server_pending(self.handle, C.byref(waiting), C.byref(inflight)), "bp_server_pending")
+        return waiting.value, inflight.value
+
+    def drain(self, wait_us: int = 200, max_rounds: int = 10_000_000) -> np.ndarray:
+        """Runs the loop until every submitted request has finished; returns their completions."""
+        done = []
+        for _ in range(max_rounds):
+            if self.progress(wait_us):
+                done.append(self.poll())
+            if self.pending() == (0, 0):
+                break
+        done.append(self.poll())
+        return np.concatenate(done) if done else np.zeros(0, COMPLETION_DTYPE)
+
+    def bubbles(self, world: int) -> np.ndarray:
+        n = self.sizes[world]
+        out = np.zeros(n, N.BUBBLE_DTYPE)
+        count = C.c_uint32()
+        N.check(self.lib.bp_server_read_bubbles(self.handle, world, C.c_void_p(out.ctypes.data), n, C.byref(count)),
+                "bp_server_read_bubbles")
+        return out
+
+    def stats(self) -> dict:
+        st = N.ServerStats()
+        N.check(self.lib.bp_server_read_stats(self.handle, C.byref(st)), "bp_server_read_stats")
+        return {name: getattr(st, name) for name, _ in st._fields_}
+
+    def clock(self) -> float:
+        return self.lib.bp_server_clock()

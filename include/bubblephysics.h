@@ -346,6 +346,72 @@ int bp_batch_adjacency_entries(bp_batch* batch, uint64_t* entries);
  * persistent launch, [3] worlds stepped by a whole block, [4] worlds stepped by one warp. */
 int bp_batch_tuning(bp_batch* batch, uint32_t* values, uint32_t count);
 
+/* ---- serving loop (no counterpart in the reference) ------------------------------------------------------------ */
+
+/* A request loop over many worlds that stay resident on the device. The reference steps one world per call
+ * (NativePublicWorld.step -> executeFrame, NativeSolverInput.swift:257-260); a server takes step requests for any of
+ * its worlds as they arrive and batches them continuously: every progress call finishes the batches whose device work
+ * has ended, admits the worlds of waiting requests while the device memory budget allows (evicting the least recently
+ * used idle worlds to pinned host memory, byte for byte, and bringing them back the same way), and launches one
+ * persistent batched step over every ready world on one of its streams while earlier batches may still run. A world
+ * has at most one step in flight; a request of n steps takes n batches. Results do not depend on the batching: a
+ * world's state after its requests is the one bp_world_step gives. Worlds above 4096 bubbles are refused
+ * (BP_E_CAPACITY). */
+typedef struct bp_server bp_server;
+
+enum bp_server_flags {
+    BP_SERVER_PER_WORLD = 1u         /* one launch per world step, one at a time (the plain per-world path) */
+};
+
+/* 32 bytes. */
+typedef struct bp_server_config {
+    uint64_t hbm_budget_bytes;       /* device bytes of resident worlds; 0 = 120 GB */
+    uint32_t max_worlds;             /* worlds the server can hold (resident or evicted) */
+    uint32_t max_batch_worlds;       /* worlds per batched launch; 0 = no limit */
+    uint32_t streams;                /* batches in flight at once; 0 = 2 */
+    uint32_t threads_per_world;      /* block width for worlds stepped by a block; 0 = 256 */
+    uint32_t warp_world_max;         /* worlds of at most this many bubbles get one warp; 0 = 64, UINT32_MAX = none */
+    uint32_t flags;                  /* BP_SERVER_* */
+} bp_server_config;
+
+/* A finished request. Times are seconds of bp_server_clock(). 136 bytes. */
+typedef struct bp_server_completion {
+    uint64_t request_id;
+    uint32_t world;
+    int32_t status;                  /* first failed step's status, else BP_OK */
+    uint32_t steps;                  /* steps taken */
+    uint32_t substeps;               /* substeps summed over the steps */
+    double submitted_s, completed_s;
+    bp_step_report report;           /* report of the last step taken */
+} bp_server_completion;
+
+/* Counters since creation. 80 bytes. */
+typedef struct bp_server_stats {
+    uint32_t worlds, resident;
+    uint64_t resident_bytes, hbm_budget_bytes;
+    uint64_t admissions, evictions, batches, batched_worlds, requests_done, bubble_substeps;
+    double device_ms;                /* summed device time of the batches (events on their streams) */
+} bp_server_stats;
+
+int bp_server_create(bp_context* context, const bp_server_config* config, bp_server** out);
+/* Waits for the work in flight, then frees every world. */
+int bp_server_destroy(bp_server* server);
+/* Registers a world (copied; it becomes resident when a request needs it). *world = its index. */
+int bp_server_add_world(bp_server* server, const bp_world_desc* desc, const bp_world_input* input, uint32_t* world);
+int bp_server_submit(bp_server* server, uint32_t world, uint32_t steps, uint64_t* request_id);
+/* One round of the loop; waits up to wait_us for device work to finish when nothing else can be done.
+ * *completed = requests finished in this round (may be NULL). */
+int bp_server_progress(bp_server* server, uint32_t wait_us, uint32_t* completed);
+/* Takes finished requests (oldest first); with out = NULL, *count = how many are waiting to be taken. */
+int bp_server_poll(bp_server* server, bp_server_completion* out, uint32_t capacity, uint32_t* count);
+/* Requests not yet finished: waiting for a batch, and worlds with a step in flight. */
+int bp_server_pending(bp_server* server, uint32_t* waiting, uint32_t* in_flight);
+/* State of one world (resident or evicted) after its finished steps. */
+int bp_server_read_bubbles(bp_server* server, uint32_t world, bp_bubble* out, uint32_t capacity, uint32_t* count);
+int bp_server_read_stats(bp_server* server, bp_server_stats* out);
+/* Monotonic host clock in seconds (the time base of bp_server_completion). */
+double bp_server_clock(void);
+
 /* ---- allocation-free step (no counterpart in the reference) ---------------------------------------------------- */
 
 /* For callers that cannot allocate device memory while they step a world - a host framework that owns every device
