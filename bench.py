@@ -295,6 +295,19 @@ def serving(ctx, args) -> dict:
                      "evictions": st2["evictions"], "statuses": stream["statuses"],
                      "warmup_statuses": sorted(set(warm["status"].tolist()))}
         server.close()
+    # the same stream over the first 4,096 worlds of the pool (the resident-world count of the latency target)
+    log("serving: 4096-world pool")
+    server = Server(4096, ctx, hbm_budget_bytes=120 << 30)
+    for spec in worlds[:4096]:
+        server.add_world(spec)
+    for w in range(4096):
+        server.submit(w, 1)
+    server.drain()
+    small = serve_stream(server, arrivals, targets % 4096)
+    lat = small["latency_ms"].tolist()
+    out["batched_4096_worlds"] = {"latency_ms": {"p50": percentile(lat, 0.50), "p99": percentile(lat, 0.99),
+                                                 "max": max(lat)}, "statuses": small["statuses"]}
+    server.close()
     b, p = out["batched"], out["per_world"]
     out["saturated_speedup_batched_vs_per_world"] = (b["saturated_bubble_substeps_per_s"] /
                                                      p["saturated_bubble_substeps_per_s"])

@@ -29,7 +29,8 @@ static_assert(sizeof(bp_server_stats) == 80, "bp_server_stats layout");
 namespace {
 
 constexpr uint64_t kDefaultBudget = 120ull << 30;
-constexpr uint32_t kDefaultStreams = 2;
+constexpr uint32_t kDefaultStreams = 8;          // batches in flight: a new arrival rarely waits for a free stream
+constexpr uint32_t kDefaultServeThreads = 512;    // the widest block: the largest worlds bound a batch's latency
 
 double host_clock() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -414,7 +415,7 @@ int bp_server_create(bp_context* context, const bp_server_config* config, bp_ser
     s->cfg = *config;
     if (!s->cfg.hbm_budget_bytes) s->cfg.hbm_budget_bytes = kDefaultBudget;
     if (!s->cfg.streams) s->cfg.streams = kDefaultStreams;
-    if (!s->cfg.threads_per_world) s->cfg.threads_per_world = kDefaultThreads;
+    if (!s->cfg.threads_per_world) s->cfg.threads_per_world = kDefaultServeThreads;
     if (!s->cfg.warp_world_max) s->cfg.warp_world_max = kDefaultWarpMax;
     if (s->cfg.threads_per_world != 128 && s->cfg.threads_per_world != 256 && s->cfg.threads_per_world != 512) {
         server_free(s);
