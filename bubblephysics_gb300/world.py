@@ -1,0 +1,745 @@
+"""The reference's public world API for the bubble path, over this library's C ABI.
+
+Shapes follow Sources/BubblePhysicsPublic: BubbleWorld (BubbleWorld.swift:10-420) owns the world and a queue of
+transactions and publishes only completed steps; WorldTransaction (Model/WorldTransaction.swift:93-123) is a value
+builder whose operations apply in order at the next step boundary; WorldFrame (Model/WorldFrame.swift:130-150) is the
+last complete state with the receipts and events of the steps that produced it; advance(by:) runs a fixed-step clock
+(Sources/BubblePhysicsRuntime/FixedStepDriver.swift: backlog capped by maximum_backlog, at most 8 steps per call, time
+taken off only after a whole step). Contact events are compacted from the end-of-step contact records the way
+NativePublicWorld.contactTransitions (NativePublicWorld.swift:340-391) does: a pair begins when it has contact now and
+had none after the previous step, ends when it had contact and has none now (or one of its objects left), pairs sorted
+by (smaller id, larger id) as unsigned 64-bit ids, only for pairs with an object that asked for contact events.
+
+Kept for the bubble path: bubbles (dynamic or static, remove or wrap at the region), static circles / capsules /
+polygons (polygons become one-sided edges like NativePublicWorld.step), kinematic bodies with a constant drive,
+physics materials, global force, impulses and motion-role changes. Operations of the reference outside this path
+(merges, splits, joints, sensors, force fields, drives other than kinematic, render state) are rejected with
+TransactionRejectionReason.UNSUPPORTED_OPERATION naming the operation, so a caller sees what is missing. The world
+steps on the GPU (World, bp_world_step); there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field, replace
+from enum import Enum
+
+import numpy as np
+
+from . import _native as N
+from .solver import Context, World, default_context, static_polygon_edges
+from .spec import WorldSpec
+
+
+# ---------------------------------------------------------------------------------------------------------------------
+# Model (Sources/BubblePhysicsPublic/Model)
+# ---------------------------------------------------------------------------------------------------------------------
+@dataclass(frozen=True)
+class CollisionFilter:
+    category: int = 1
+    mask: int = 0xFFFFFFFF
+
+    def accepts(self, other: "CollisionFilter") -> bool:
+        return bool(self.category & other.mask) and bool(other.category & self.mask)
+
+
+@dataclass(frozen=True)
+class PhysicsMaterial:
+    """Contact stiffness K_c and damping gamma of a bubble material (PhysicsMaterial, Model/Resources.swift)."""
+    contact_stiffness: float
+    damping: float = 0.0
+
+
+class MotionRole(Enum):
+    DYNAMIC = "dynamic"
+    STATIC = "static"
+    KINEMATIC = "kinematic"
+
+
+class RegionExitPolicy(Enum):
+    REMOVE = "remove"
+    WRAP = "wrap"
+
+
+class EventInterest(Enum):
+    CONTACT = "contact"
+
+
+@dataclass(frozen=True)
+class BubbleDescriptor:
+    id: int
+    position: tuple
+    radius: float
+    mass: float
+    physics_material_id: str
+    velocity: tuple = (0.0, 0.0)
+    motion_role: MotionRole = MotionRole.DYNAMIC
+    region_exit_policy: RegionExitPolicy = RegionExitPolicy.REMOVE
+    filter: CollisionFilter = CollisionFilter()
+    event_interest: frozenset = frozenset()
+
+
+@dataclass(frozen=True)
+class Circle:
+    radius: float
+
+
+@dataclass(frozen=True)
+class Capsule:
+    half_length: float
+    radius: float
+
+
+@dataclass(frozen=True)
+class Polygon:
+    points: tuple  # convex, local to the centre of mass, counter-clockwise
+
+
+@dataclass(frozen=True)
+class RigidBodyDescriptor:
+    id: int
+    shape: object
+    position: tuple
+    angle: float = 0.0
+    motion_role: MotionRole = MotionRole.STATIC
+    velocity: tuple = (0.0, 0.0)          # kinematic drive
+    angular_velocity: float = 0.0
+    filter: CollisionFilter = CollisionFilter()
+    event_interest: frozenset = frozenset()
+
+
+@dataclass(frozen=True)
+class WorldConfiguration:
+    """WorldConfiguration (Model/WorldConfiguration.swift:39-66) plus the solver switches of the path."""
+    simulation_region: tuple                 # (min x, min y, max x, max y)
+    fixed_time_step: float = 1.0 / 60.0
+    global_force: tuple = (0.0, 0.0)
+    maximum_backlog: float = 0.25
+    maximum_steps_per_advance: int = 8
+    gravity: tuple = (0.0, 0.0)              # acceleration on force-driven bubbles (0: the reference's behaviour)
+    candidate_limit: int = 128
+    substep_split_multiplier: float = 1.0    # NativeMetalConfiguration.substepSplitMultiplier
+
+    def __post_init__(self):
+        if not (math.isfinite(self.fixed_time_step) and self.fixed_time_step > 0):
+            raise ValueError("fixedTimeStep must be finite and positive")
+        if not (math.isfinite(self.maximum_backlog) and self.maximum_backlog > 0):
+            raise ValueError("maximumBacklog must be finite and positive")
+
+
+class TransactionRejectionReason(Enum):
+    OBJECT_NOT_FOUND = "objectNotFound"
+    DUPLICATE_OBJECT_ID = "duplicateObjectID"
+    REPLACEMENT_ID_MISMATCH = "replacementIDMismatch"
+    PHYSICS_MATERIAL_NOT_FOUND = "physicsMaterialNotFound"
+    INCOMPATIBLE_OBJECT_KIND = "incompatibleObjectKind"
+    INVALID_VALUE = "invalidValue"
+    INVALID_PLACEMENT = "invalidPlacement"
+    UNSUPPORTED_OPERATION = "unsupportedOperation"
+
+
+@dataclass(frozen=True)
+class TransactionRejection:
+    operation_index: int
+    reason: TransactionRejectionReason
+    detail: object = None
+
+
+@dataclass(frozen=True)
+class TransactionReceipt:
+    token: int
+    created_object_ids: tuple
+    removed_object_ids: tuple
+    replaced_object_ids: tuple
+
+
+@dataclass(frozen=True)
+class ObjectState:
+    kind: str                 # "bubble", "polygon", "circle", "capsule"
+    position: tuple
+    velocity: tuple
+    rotation: float
+    angular_velocity: float
+    bounds: tuple             # (min x, min y, max x, max y)
+
+
+@dataclass(frozen=True)
+class WorldEvent:
+    """kind: transactionRejected, didAdd, didRemove, didReplace, didExitSimulationRegion, didWrap, contactBegan,
+    contactEnded."""
+    kind: str
+    objects: tuple = ()
+    point: tuple | None = None
+    normal: tuple | None = None
+    impulse: float | None = None
+    token: int | None = None
+    rejection: TransactionRejection | None = None
+
+
+@dataclass(frozen=True)
+class WorldFrame:
+    step_index: int = 0
+    simulation_time: float = 0.0
+    transaction_receipts: tuple = ()
+    events: tuple = ()
+    objects: dict = field(default_factory=dict)
+
+
+class WorldFailureReason(Enum):
+    SUBSTEP_LIMIT_EXCEEDED = "substepLimitExceeded"
+    NON_FINITE_VALUES = "nonFiniteValues"
+    CONTACT_VIOLATION = "contactViolation"
+    COMMAND_EXECUTION_FAILED = "commandExecutionFailed"
+
+
+@dataclass
+class WorldDiagnostics:
+    backlog_seconds: float = 0.0
+    discarded_backlog_seconds: float = 0.0
+    steps_in_last_advance: int = 0
+    pending_transaction_count: int = 0
+    is_paused: bool = False
+    contact_candidate_overflow: int = 0
+    maximum_contact_candidates_per_object: int = 0
+    failure_reason: WorldFailureReason | None = None
+    failure_detail: dict | None = None
+
+
+# ---------------------------------------------------------------------------------------------------------------------
+# Transactions (value builder: every method returns a copy)
+# ---------------------------------------------------------------------------------------------------------------------
+@dataclass(frozen=True)
+class WorldTransaction:
+    operations: tuple = ()
+
+    def _with(self, *op) -> "WorldTransaction":
+        return WorldTransaction(self.operations + (op,))
+
+    def add(self, obj) -> "WorldTransaction":
+        return self._with("add", obj)
+
+    def remove(self, object_id: int) -> "WorldTransaction":
+        return self._with("remove", object_id)
+
+    def replace(self, object_id: int, obj) -> "WorldTransaction":
+        return self._with("replace", object_id, obj)
+
+    def update_physics_material(self, material_id: str, material: PhysicsMaterial) -> "WorldTransaction":
+        return self._with("updatePhysicsMaterial", material_id, material)
+
+    def set_motion(self, object_id: int, role: MotionRole) -> "WorldTransaction":
+        return self._with("setMotion", object_id, role)
+
+    def set_global_force(self, force) -> "WorldTransaction":
+        return self._with("setGlobalForce", tuple(float(v) for v in force))
+
+    def apply_impulse(self, object_id: int, impulse) -> "WorldTransaction":
+        return self._with("applyImpulse", object_id, tuple(float(v) for v in impulse))
+
+    def set_kinematic_drive(self, object_id: int, velocity, angular_velocity: float = 0.0) -> "WorldTransaction":
+        return self._with("setKinematicDrive", object_id, tuple(float(v) for v in velocity), float(angular_velocity))
+
+    def operation(self, name: str, *args) -> "WorldTransaction":
+        """Any other operation of the reference's transaction (merges, splits, joints, sensors, ...): recorded, and
+        rejected at the step boundary as unsupported by this backend."""
+        return self._with(name, *args)
+
+
+# ---------------------------------------------------------------------------------------------------------------------
+# Runtime state and staging
+# ---------------------------------------------------------------------------------------------------------------------
+@dataclass
+class _Bubble:
+    desc: BubbleDescriptor
+    position: np.ndarray
+    velocity: np.ndarray
+    rotation: float = 0.0
+    angular_velocity: float = 0.0
+
+
+@dataclass
+class _Body:
+    desc: RigidBodyDescriptor
+    position: np.ndarray
+    angle: float
+
+
+@dataclass
+class _State:
+    materials: dict = field(default_factory=dict)
+    bubbles: dict = field(default_factory=dict)   # id -> _Bubble
+    bodies: dict = field(default_factory=dict)    # id -> _Body
+    global_force: tuple = (0.0, 0.0)
+
+    def copy(self) -> "_State":
+        return _State(dict(self.materials),
+                      {k: replace(v, position=v.position.copy(), velocity=v.velocity.copy()) for k, v in self.bubbles.items()},
+                      {k: replace(v, position=v.position.copy()) for k, v in self.bodies.items()},
+                      self.global_force)
+
+
+def _finite(*values) -> bool:
+    return all(math.isfinite(float(v)) for v in values)
+
+
+def _inside_body(body: _Body, point) -> bool:
+    d = np.asarray(point, np.float64) - body.position
+    c, s = math.cos(-body.angle), math.sin(-body.angle)
+    local = np.array([d[0] * c - d[1] * s, d[0] * s + d[1] * c])
+    shape = body.desc.shape
+    if isinstance(shape, Circle):
+        return float(np.hypot(*local)) <= shape.radius
+    if isinstance(shape, Capsule):
+        x = min(max(local[0], -shape.half_length), shape.half_length)
+        return float(np.hypot(local[0] - x, local[1])) <= shape.radius
+    pts = np.asarray(shape.points, np.float64)
+    edges = np.roll(pts, -1, axis=0) - pts
+    cross = edges[:, 0] * (local[1] - pts[:, 1]) - edges[:, 1] * (local[0] - pts[:, 0])
+    return bool(np.all(cross >= 0) or np.all(cross <= 0))
+
+
+def _validate_bubble(desc: BubbleDescriptor, state: _State, region) -> TransactionRejectionReason | None:
+    if desc.physics_material_id not in state.materials:
+        return TransactionRejectionReason.PHYSICS_MATERIAL_NOT_FOUND
+    if not (_finite(*desc.position, *desc.velocity, desc.radius, desc.mass) and desc.radius > 0 and desc.mass > 0):
+        return TransactionRejectionReason.INVALID_VALUE
+    if desc.motion_role == MotionRole.KINEMATIC:
+        return TransactionRejectionReason.INVALID_VALUE
+    x, y = desc.position
+    if not (region[0] <= x <= region[2] and region[1] <= y <= region[3]):
+        return TransactionRejectionReason.INVALID_PLACEMENT
+    for body in state.bodies.values():
+        if desc.filter.accepts(body.desc.filter) and _inside_body(body, desc.position):
+            return TransactionRejectionReason.INVALID_PLACEMENT
+    for other in state.bubbles.values():
+        if other.desc.id != desc.id and float(np.hypot(*(other.position - np.asarray(desc.position)))) <= 1e-4:
+            return TransactionRejectionReason.INVALID_PLACEMENT
+    return None
+
+
+def _validate_body(desc: RigidBodyDescriptor, state: _State) -> TransactionRejectionReason | None:
+    if desc.motion_role not in (MotionRole.STATIC, MotionRole.KINEMATIC):
+        return TransactionRejectionReason.UNSUPPORTED_OPERATION  # bubbles meet only static and kinematic bodies
+    shape = desc.shape
+    sizes = {Circle: lambda s: (s.radius,), Capsule: lambda s: (s.half_length, s.radius)}.get(type(shape))
+    if sizes is not None:
+        if not (_finite(*sizes(shape)) and min(sizes(shape)) > 0):
+            return TransactionRejectionReason.INVALID_VALUE
+    elif isinstance(shape, Polygon):
+        if len(shape.points) < 3 or not _finite(*np.ravel(shape.points)):
+            return TransactionRejectionReason.INVALID_VALUE
+    else:
+        return TransactionRejectionReason.INVALID_VALUE
+    if not _finite(*desc.position, desc.angle, *desc.velocity, desc.angular_velocity):
+        return TransactionRejectionReason.INVALID_VALUE
+    probe = _Body(desc, np.asarray(desc.position, np.float64), float(desc.angle))
+    for b in state.bubbles.values():
+        if b.desc.filter.accepts(desc.filter) and _inside_body(probe, b.position):
+            return TransactionRejectionReason.INVALID_PLACEMENT
+    return None
+
+
+def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None, dict]:
+    """Applies one operation to `state` (a staging copy); returns (rejection reason, {created, removed, replaced})."""
+    kind, args = op[0], op[1:]
+    touched = {"created": [], "removed": [], "replaced": []}
+    if kind in ("add", "replace"):
+        obj = args[-1]
+        if kind == "replace":
+            oid = args[0]
+            if oid not in state.bubbles and oid not in state.bodies:
+                return TransactionRejectionReason.OBJECT_NOT_FOUND, touched
+            if obj.id != oid:
+                return TransactionRejectionReason.REPLACEMENT_ID_MISMATCH, touched
+            state.bubbles.pop(oid, None)
+            state.bodies.pop(oid, None)
+        elif obj.id in state.bubbles or obj.id in state.bodies:
+            return TransactionRejectionReason.DUPLICATE_OBJECT_ID, touched
+        if isinstance(obj, BubbleDescriptor):
+            reason = _validate_bubble(obj, state, region)
+            if reason:
+                return reason, touched
+            state.bubbles[obj.id] = _Bubble(obj, np.asarray(obj.position, np.float32).copy(),
+                                            np.asarray(obj.velocity, np.float32).copy())
+        elif isinstance(obj, RigidBodyDescriptor):
+            reason = _validate_body(obj, state)
+            if reason:
+                return reason, touched
+            state.bodies[obj.id] = _Body(obj, np.asarray(obj.position, np.float32).copy(), float(obj.angle))
+        else:
+            return TransactionRejectionReason.UNSUPPORTED_OPERATION, touched
+        touched["replaced" if kind == "replace" else "created"].append(obj.id)
+        return None, touched
+    if kind == "remove":
+        oid = args[0]
+        if state.bubbles.pop(oid, None) is None and state.bodies.pop(oid, None) is None:
+            return TransactionRejectionReason.OBJECT_NOT_FOUND, touched
+        touched["removed"].append(oid)
+        return None, touched
+    if kind == "updatePhysicsMaterial":
+        mid, material = args
+        if not (_finite(material.contact_stiffness, material.damping) and material.contact_stiffness >= 0 and
+                material.damping >= 0):
+            return TransactionRejectionReason.INVALID_VALUE, touched
+        state.materials[mid] = material
+        return None, touched
+    if kind == "setMotion":
+        oid, role = args
+        b = state.bubbles.get(oid)
+        if b is None:
+            return TransactionRejectionReason.OBJECT_NOT_FOUND if oid not in state.bodies else \
+                TransactionRejectionReason.INCOMPATIBLE_OBJECT_KIND, touched
+        if role not in (MotionRole.DYNAMIC, MotionRole.STATIC):
+            return TransactionRejectionReason.INVALID_VALUE, touched
+        b.desc = replace(b.desc, motion_role=role)
+        if role == MotionRole.STATIC:
+            b.velocity[:] = 0
+        return None, touched
+    if kind == "setGlobalForce":
+        if not _finite(*args[0]):
+            return TransactionRejectionReason.INVALID_VALUE, touched
+        state.global_force = args[0]
+        return None, touched
+    if kind == "applyImpulse":
+        oid, impulse = args
+        b = state.bubbles.get(oid)
+        if b is None:
+            return TransactionRejectionReason.OBJECT_NOT_FOUND if oid not in state.bodies else \
+                TransactionRejectionReason.INCOMPATIBLE_OBJECT_KIND, touched
+        if not _finite(*impulse):
+            return TransactionRejectionReason.INVALID_VALUE, touched
+        if b.desc.motion_role == MotionRole.DYNAMIC:
+            b.velocity += (np.asarray(impulse, np.float32) / np.float32(b.desc.mass)).astype(np.float32)
+        return None, touched
+    if kind == "setKinematicDrive":
+        oid, velocity, omega = args
+        body = state.bodies.get(oid)
+        if body is None:
+            return TransactionRejectionReason.OBJECT_NOT_FOUND if oid not in state.bubbles else \
+                TransactionRejectionReason.INCOMPATIBLE_OBJECT_KIND, touched
+        if body.desc.motion_role != MotionRole.KINEMATIC or not _finite(*velocity, omega):
+            return TransactionRejectionReason.INVALID_VALUE, touched
+        body.desc = replace(body.desc, velocity=velocity, angular_velocity=omega)
+        return None, touched
+    return TransactionRejectionReason.UNSUPPORTED_OPERATION, touched
+
+
+def stage(pending: list, state: _State, region) -> tuple[_State, list, list]:
+    """TransactionStager.stageBatch for this path: each transaction applies atomically (all operations or none) in
+    submission order against the state left by the previous ones. Returns (new state, receipts, events)."""
+    receipts, events = [], []
+    current = state
+    for token, tx in pending:
+        trial = current.copy()
+        created, removed, replaced_ids = [], [], []
+        rejection = None
+        for index, op in enumerate(tx.operations):
+            reason, touched = _apply(op, trial, region)
+            if reason is not None:
+                rejection = TransactionRejection(index, reason, op[0])
+                break
+            created += touched["created"]
+            removed += touched["removed"]
+            replaced_ids += touched["replaced"]
+        if rejection is not None:
+            events.append(WorldEvent("transactionRejected", token=token, rejection=rejection))
+            continue
+        current = trial
+        receipts.append(TransactionReceipt(token, tuple(created), tuple(removed), tuple(replaced_ids)))
+        events += [WorldEvent("didAdd", (i,)) for i in created]
+        events += [WorldEvent("didRemove", (i,)) for i in removed]
+        events += [WorldEvent("didReplace", (i,)) for i in replaced_ids]
+    return current, receipts, events
+
+
+def _pair_key(a: int, b: int) -> tuple:
+    ua, ub = a & 0xFFFFFFFFFFFFFFFF, b & 0xFFFFFFFFFFFFFFFF
+    return (a, b) if ua <= ub else (b, a)
+
+
+def contact_transitions(contacts: np.ndarray, segment_owner: dict, interested: set, history: set, step: float,
+                        removed: set) -> tuple[list, set]:
+    """contactBegan / contactEnded of one step from its contact records (NativePublicWorld.swift:340-391): per pair the
+    point is the penetration-weighted mean, the normal the normalised sum (from the smaller id to the larger) and the
+    impulse the summed F dt^2 divided by the step."""
+    sums = {}
+    for c in contacts:
+        first = int(c["participants"][0])
+        second = int(c["participants"][1]) if c["kind"] == 0 else segment_owner.get(int(c["participants"][1]))
+        if second is None or not (c["penetration"] > 0 or c["impulse"] > 0):
+            continue
+        if first not in interested and second not in interested:
+            continue
+        key = _pair_key(first, second)
+        normal = np.asarray(c["normal"], np.float64) * (-1.0 if c["kind"] == 1 else 1.0)
+        if key[0] != first:
+            normal = -normal
+        weight = max(float(c["penetration"]), 0.0) + 1e-4
+        s = sums.setdefault(key, [np.zeros(2), 0.0, np.zeros(2), 0.0])
+        s[0] += np.asarray(c["point"], np.float64) * weight
+        s[1] += weight
+        s[2] += normal
+        s[3] += float(c["impulse"]) / step
+    order = lambda k: (k[0] & 0xFFFFFFFFFFFFFFFF, k[1] & 0xFFFFFFFFFFFFFFFF)
+    events = []
+    for key in sorted(sums, key=order):
+        if key in history:
+            continue
+        point, weight, normal, impulse = sums[key]
+        length = float(np.hypot(*normal))
+        events.append(WorldEvent("contactBegan", key, tuple(point / weight), tuple(normal / length) if length > 0 else (0.0, 0.0),
+                                 impulse))
+    current = set(sums)
+    for key in sorted(history, key=order):
+        if key not in current or key[0] in removed or key[1] in removed:
+            events.append(WorldEvent("contactEnded", key))
+    return events, current - {k for k in current if k[0] in removed or k[1] in removed}
+
+
+# ---------------------------------------------------------------------------------------------------------------------
+# BubbleWorld
+# ---------------------------------------------------------------------------------------------------------------------
+class BubbleWorld:
+    """Sole owner of a world and its transaction queue; publishes only completed steps."""
+
+    def __init__(self, configuration: WorldConfiguration, context: Context | None = None):
+        self.configuration = configuration
+        self._ctx = context
+        self._state = _State(global_force=tuple(configuration.global_force))
+        self._pending: list = []
+        self._next_token = 1
+        self._backlog = 0.0
+        self._discarded = 0.0
+        self._completed = 0
+        self._time = 0.0
+        self._paused = False
+        self._frame = WorldFrame()
+        self._native: World | None = None
+        self._native_ids: list = []
+        self._segment_owner: dict = {}
+        self._history: set = set()
+        self.diagnostics = WorldDiagnostics()
+
+    # -- public API ----------------------------------------------------------------------------------------------------
+    def submit(self, transaction: WorldTransaction) -> int:
+        token = self._next_token
+        self._next_token += 1
+        if self.diagnostics.failure_reason is None:
+            self._pending.append((token, transaction))
+        self.diagnostics.pending_transaction_count = len(self._pending)
+        return token
+
+    def pause(self):
+        self._paused = True
+        self.diagnostics.is_paused = True
+
+    def resume(self):
+        self._paused = False
+        self.diagnostics.is_paused = False
+
+    @property
+    def last_frame(self) -> WorldFrame:
+        return self._frame
+
+    def advance(self, seconds: float) -> WorldFrame:
+        """Runs the fixed-step clock: at most maximum_steps_per_advance steps; a call without a completed step (or
+        after a failure) returns the last complete frame."""
+        d = self.diagnostics
+        d.steps_in_last_advance = 0
+        if d.failure_reason is not None or not (math.isfinite(seconds) and seconds >= 0) or self._paused:
+            return self._frame
+        dt = self.configuration.fixed_time_step
+        backlog = self._backlog + seconds
+        if backlog > max(self.configuration.maximum_backlog, dt):
+            self._discarded += backlog - max(self.configuration.maximum_backlog, dt)
+            backlog = max(self.configuration.maximum_backlog, dt)
+        self._backlog = backlog
+        receipts, events = [], []
+        while d.steps_in_last_advance < self.configuration.maximum_steps_per_advance and self._can_step():
+            ok = self._step(receipts, events)
+            if not ok:
+                break
+            self._backlog = max(0.0, self._backlog - dt)
+            self._completed += 1
+            self._time += dt
+            d.steps_in_last_advance += 1
+            self._frame = WorldFrame(self._completed, self._time, tuple(receipts), tuple(events), self._objects())
+        d.backlog_seconds = self._backlog
+        d.discarded_backlog_seconds = self._discarded
+        d.pending_transaction_count = len(self._pending)
+        return self._frame
+
+    def close(self):
+        if self._native is not None:
+            self._native.close()
+            self._native = None
+
+    # -- internals -----------------------------------------------------------------------------------------------------
+    def _can_step(self) -> bool:
+        dt = self.configuration.fixed_time_step
+        return self._backlog >= dt or (self._backlog > 0 and dt - self._backlog <= dt * 1e-12)
+
+    def _spec(self, state: _State) -> tuple[WorldSpec, list, dict]:
+        cfg = self.configuration
+        ids = sorted(state.bubbles)
+        b = np.zeros(len(ids), N.BUBBLE_DTYPE)
+        for i, oid in enumerate(ids):
+            bub = state.bubbles[oid]
+            d = bub.desc
+            mat = state.materials[d.physics_material_id]
+            static = d.motion_role == MotionRole.STATIC
+            b[i]["id"] = oid
+            b[i]["center"] = bub.position
+            b[i]["previous_center"] = bub.position
+            b[i]["velocity"] = bub.velocity
+            b[i]["mass"] = d.mass
+            b[i]["inverse_mass"] = 0.0 if static else np.float32(1.0) / np.float32(d.mass)
+            b[i]["radius"] = d.radius
+            b[i]["rotation"] = bub.rotation
+            b[i]["angular_velocity"] = bub.angular_velocity
+            b[i]["contact_stiffness"] = mat.contact_stiffness
+            b[i]["damping"] = mat.damping
+            b[i]["flags"] = N.BUBBLE_ENABLED | (N.BUBBLE_STATIC if static else N.BUBBLE_FORCE_DRIVEN) | \
+                (N.BUBBLE_WRAP if d.region_exit_policy == RegionExitPolicy.WRAP else 0)
+            b[i]["category"] = d.filter.category
+            b[i]["mask"] = d.filter.mask
+        segs, bodies, verts, tris = [], [], [], []
+        owners = {}
+        next_seg = 1
+        for oid in sorted(state.bodies):
+            body = state.bodies[oid]
+            d, shape = body.desc, body.desc.shape
+            if isinstance(shape, Polygon) and d.motion_role == MotionRole.STATIC:
+                c, s = math.cos(body.angle), math.sin(body.angle)
+                pts = np.asarray(shape.points, np.float64)
+                world = np.stack([pts[:, 0] * c - pts[:, 1] * s, pts[:, 0] * s + pts[:, 1] * c], 1) + body.position
+                e = static_polygon_edges(world.astype(np.float32), next_seg, oid)
+                e["category"], e["mask"] = d.filter.category, d.filter.mask
+                for rec in e:
+                    owners[int(rec["id"])] = oid
+                next_seg += len(e)
+                segs.append(e)
+                continue
+            rec = np.zeros(1, N.BODY_DTYPE)[0]
+            rec["id"] = oid
+            rec["position"] = body.position
+            rec["angle"] = body.angle
+            rec["velocity"] = d.velocity if d.motion_role == MotionRole.KINEMATIC else (0.0, 0.0)
+            rec["angular_velocity"] = d.angular_velocity if d.motion_role == MotionRole.KINEMATIC else 0.0
+            rec["flags"] = N.BODY_KINEMATIC if d.motion_role == MotionRole.KINEMATIC else N.BODY_STATIC
+            rec["category"], rec["mask"] = d.filter.category, d.filter.mask
+            rec["vertex_offset"] = sum(len(v) for v in verts)
+            rec["triangle_offset"] = sum(len(t) for t in tris)
+            if isinstance(shape, Circle):
+                rec["kind"], rec["bounding_radius"], rec["core_radius"] = N.BODY_CIRCLE, shape.radius, shape.radius
+                local, tri = np.zeros((1, 2), np.float32), np.zeros((0, 3), np.uint32)
+            elif isinstance(shape, Capsule):
+                rec["kind"], rec["core_radius"], rec["half_length"] = N.BODY_CAPSULE, shape.radius, shape.half_length
+                rec["bounding_radius"] = shape.half_length + shape.radius
+                local = np.array([[-shape.half_length, 0.0], [shape.half_length, 0.0]], np.float32)
+                tri = np.zeros((0, 3), np.uint32)
+            else:
+                local = np.asarray(shape.points, np.float32)
+                tri = np.array([[0, i, i + 1] for i in range(1, len(local) - 1)], np.uint32)
+                rec["kind"] = N.BODY_POLYGON
+                rec["bounding_radius"] = float(np.sqrt((local.astype(np.float64) ** 2).sum(1)).max())
+            rec["vertex_count"], rec["triangle_count"] = len(local), len(tri)
+            verts.append(local)
+            tris.append(tri)
+            bodies.append(rec)
+        spec = WorldSpec(bubbles=b,
+                         segments=np.concatenate(segs) if segs else np.zeros(0, N.SEGMENT_DTYPE),
+                         bodies=np.array(bodies, N.BODY_DTYPE) if bodies else np.zeros(0, N.BODY_DTYPE),
+                         body_vertices=np.concatenate(verts) if verts else np.zeros((0, 2), np.float32),
+                         body_triangles=np.concatenate(tris) if tris else np.zeros((0, 3), np.uint32),
+                         region=tuple(cfg.simulation_region), global_force=tuple(state.global_force),
+                         gravity=tuple(cfg.gravity), time_step=cfg.fixed_time_step,
+                         candidate_limit=cfg.candidate_limit, substep_split_multiplier=cfg.substep_split_multiplier)
+        return spec, ids, owners
+
+    def _step(self, receipts: list, events: list) -> bool:
+        cfg = self.configuration
+        taken = len(self._pending)
+        staged, rec, ev = stage(self._pending[:taken], self._state, cfg.simulation_region)
+        changed = bool(rec) or self._native is None
+        spec, ids, owners = self._spec(staged)
+        if changed or ids != self._native_ids:
+            if self._native is not None:
+                self._native.close()
+            if len(ids) and self._ctx is None:
+                self._ctx = default_context()
+            self._native = World(spec, self._ctx) if len(ids) else None
+            self._native_ids = ids
+            self._segment_owner = owners
+        removed_now = set()
+        contacts = np.zeros(0, N.CONTACT_DTYPE)
+        if self._native is not None:
+            status, reps = self._native.step(1)
+            rep = reps[0]
+            if status != N.OK:
+                self._fail(status, rep)
+                return False
+            out = self._native.bubbles()
+            contacts = self._native.contacts()
+            for i, oid in enumerate(ids):
+                bub = staged.bubbles[oid]
+                bub.position = out[i]["center"].astype(np.float32).copy()
+                bub.velocity = out[i]["velocity"].astype(np.float32).copy()
+                bub.rotation = float(out[i]["rotation"])
+                bub.angular_velocity = float(out[i]["angular_velocity"])
+                if out[i]["region_result"] == 1:
+                    removed_now.add(oid)
+                    ev.append(WorldEvent("didExitSimulationRegion", (oid,)))
+                elif out[i]["region_result"] == 2:
+                    ev.append(WorldEvent("didWrap", (oid,)))
+            for oid in removed_now:
+                staged.bubbles.pop(oid)
+            dt = np.float32(cfg.fixed_time_step)
+            for body in staged.bodies.values():  # kinematic advance, the same float arithmetic as the device
+                if body.desc.motion_role == MotionRole.KINEMATIC:
+                    body.position = (body.position + np.asarray(body.desc.velocity, np.float32) * dt).astype(np.float32)
+                    body.angle = float(np.float32(body.angle) + np.float32(body.desc.angular_velocity) * dt)
+            self.diagnostics.contact_candidate_overflow += int(rep["candidate_overflow"])
+            self.diagnostics.maximum_contact_candidates_per_object = int(rep["max_candidates_per_object"])
+        interested = {i for i, b in staged.bubbles.items() if EventInterest.CONTACT in b.desc.event_interest}
+        interested |= {i for i, b in staged.bodies.items() if EventInterest.CONTACT in b.desc.event_interest}
+        gone = removed_now | {i for r in rec for i in r.removed_object_ids + r.replaced_object_ids}
+        contact_events, self._history = contact_transitions(contacts, self._segment_owner, interested, self._history,
+                                                            cfg.fixed_time_step, gone)
+        self._state = staged
+        del self._pending[:taken]
+        receipts += rec
+        events += ev + contact_events
+        if removed_now and self._native is not None:
+            self._native_ids = None  # the removed slots leave the device world at the next step
+        return True
+
+    def _fail(self, status: int, rep):
+        reasons = {N.E_SUBSTEP_LIMIT: WorldFailureReason.SUBSTEP_LIMIT_EXCEEDED,
+                   N.E_NONFINITE: WorldFailureReason.NON_FINITE_VALUES,
+                   N.E_CONTACT_VIOLATION: WorldFailureReason.CONTACT_VIOLATION}
+        self.diagnostics.failure_reason = reasons.get(status, WorldFailureReason.COMMAND_EXECUTION_FAILED)
+        self.diagnostics.failure_detail = {"objects": tuple(int(v) for v in rep["violation_objects"]),
+                                           "edge": int(rep["violation_edge"]),
+                                           "distance": float(rep["violation_distance"]),
+                                           "limiting_term": int(rep["limiter_term"]),
+                                           "limiting_object": int(rep["limiter_object"])}
+        self._pending.clear()
+
+    def _objects(self) -> dict:
+        out = {}
+        for oid, b in self._state.bubbles.items():
+            r = b.desc.radius
+            out[oid] = ObjectState("bubble", tuple(map(float, b.position)), tuple(map(float, b.velocity)), b.rotation,
+                                   b.angular_velocity, (float(b.position[0]) - r, float(b.position[1]) - r,
+                                                        float(b.position[0]) + r, float(b.position[1]) + r))
+        for oid, body in self._state.bodies.items():
+            shape = body.desc.shape
+            kind = {Circle: "circle", Capsule: "capsule", Polygon: "polygon"}[type(shape)]
+            reach = shape.radius if isinstance(shape, Circle) else shape.half_length + shape.radius \
+                if isinstance(shape, Capsule) else float(np.sqrt((np.asarray(shape.points) ** 2).sum(1)).max())
+            vel = body.desc.velocity if body.desc.motion_role == MotionRole.KINEMATIC else (0.0, 0.0)
+            out[oid] = ObjectState(kind, tuple(map(float, body.position)), tuple(map(float, vel)), body.angle,
+                                   body.desc.angular_velocity if body.desc.motion_role == MotionRole.KINEMATIC else 0.0,
+                                   (float(body.position[0]) - reach, float(body.position[1]) - reach,
+                                    float(body.position[0]) + reach, float(body.position[1]) + reach))
+        return out
