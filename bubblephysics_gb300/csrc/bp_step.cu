@@ -422,16 +422,38 @@ __device__ __forceinline__ void body_hit(const DState& S, const DWorld& W, uint3
     if (slot < W.k) S.bodyRow[W.bodyRowOff + (uint64_t)bi * W.k + slot] = i;
 }
 
-// Forward candidate row of bubble i: pairs with j > i, then segments; k smallest keys (NGK:300-330). With the tree,
-// the same traversal also registers i in the rows of the bodies that accept it.
+// Lower pair (j, i), j < i, of bubble i's adjacency (the pair lives in row j): the same tests as the candidate rule
+// of row j; whether row j kept i is checked once every row is built (finish_adjacency).
+__device__ __forceinline__ void lower_pair(const DState& S, const DWorld& W, uint32_t i, uint32_t j, uint32_t* adjRow,
+                                           uint32_t& kept, uint32_t& total) {
+    if (!finite2(S.start[W.boff + j])) return;
+    if (!pair_accepts(S, W, j, i)) return;
+    ++total;
+    insert_sorted(adjRow, kept, W.k, j);
+}
+
+// Forward candidate row of bubble i: pairs with j > i, then segments; k smallest keys (NGK:300-330). The same cell
+// scan collects the lower pairs j < i into the adjacency row (their count goes to deg until finish_adjacency). With
+// the tree, the rigid traversal also registers i in the rows of the bodies that accept it.
 template <bool kTree>
 __device__ void emit_row(const DState& S, const DWorld& W, const uint32_t* buckets, const uint32_t* entries, uint32_t B,
                          uint32_t i, uint32_t& overflow, uint32_t& maxPer) {
     const uint32_t g = W.boff + i, k = W.k;
     uint32_t* row = S.candRow + W.rowOff + (uint64_t)i * k;
+    uint32_t* adjRow = S.adj + W.rowOff + (uint64_t)i * k;
+    uint32_t lowerKept = 0, lowerTotal = 0;
     if (!(S.flags[g] & kValid) || !finite2(S.start[g])) {
         S.candCount[g] = make_uint2(0u, 0u);
         S.pairTotal[g] = 0u;
+        if (S.flags[g] & kValid) {  // a valid cell with a non-finite step start: no row, but lower pairs still count
+            const longlong2 c = S.cell[g];
+            for (int dx = -1; dx <= 1; ++dx)
+                for (int dy = -1; dy <= 1; ++dy)
+                    for_each_in_cell(S.cell, W, buckets, entries, B, c.x + dx, c.y + dy, [&](uint32_t j) {
+                        if (j < i) lower_pair(S, W, i, j, adjRow, lowerKept, lowerTotal);
+                    });
+        }
+        S.deg[g] = lowerTotal;
         if (kTree && W.nb && !removed(S, g)) {
             // a bubble without a valid cell still meets the body rule (a non-finite centre fails no comparison)
             const float reach = S.phys[g].x + fmaxf(S.margin[g], 0.0f);
@@ -451,11 +473,15 @@ __device__ void emit_row(const DState& S, const DWorld& W, const uint32_t* bucke
     for (int dx = -1; dx <= 1; ++dx)
         for (int dy = -1; dy <= 1; ++dy)
             for_each_in_cell(S.cell, W, buckets, entries, B, c.x + dx, c.y + dy, [&](uint32_t j) {
-                if (j <= i) return;
-                if (!pair_accepts(S, W, i, j)) return;
+                if (j < i) {
+                    lower_pair(S, W, i, j, adjRow, lowerKept, lowerTotal);
+                    return;
+                }
+                if (j == i || !pair_accepts(S, W, i, j)) return;
                 ++total;
                 insert_sorted(row, count, k, j);
             });
+    S.deg[g] = lowerTotal;
     const uint32_t pairs = count;
     uint32_t segTotal = 0;
     if (kTree) {
@@ -552,9 +578,18 @@ __device__ void build_adjacency(const DState& S, const DWorld& W, const uint32_t
     uint32_t* row = S.adj + W.rowOff + (uint64_t)i * k;
     uint32_t deg = 0, demanded = 0;
     if (removed(S, g)) { S.deg[g] = 0u; return; }
-    if (S.flags[g] & kValid) {
+    const uint32_t lowerTotal = S.deg[g];  // lower pairs found by emit_row, the first k of them in the row
+    if (lowerTotal <= k) {
+        // keep the lower pairs whose row j holds i (only a truncated row j can miss it)
+        for (uint32_t e = 0; e < lowerTotal; ++e) {
+            const uint32_t j = row[e], gj = W.boff + j;
+            if (S.pairTotal[gj] > k && !row_contains(S.candRow + W.rowOff + (uint64_t)j * k, S.candCount[gj].x, i)) continue;
+            row[deg++] = j;
+            ++demanded;
+        }
+    } else {
+        // more lower pairs than slots: which ones are kept depends on the rows j, so scan again with that check
         longlong2 c = S.cell[g];
-        // pairs (j, i) with j < i held in row j
         for (int dx = -1; dx <= 1; ++dx)
             for (int dy = -1; dy <= 1; ++dy)
                 for_each_in_cell(S.cell, W, buckets, entries, B, c.x + dx, c.y + dy, [&](uint32_t j) {
