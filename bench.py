@@ -441,7 +441,9 @@ def run_ours(args, rank, world_size, local_rank):
                 "d2h_bytes_per_step": total_bubbles * 16, "steps": args.e2e_steps,
                 "note": "C ABI bp_batch_write_state + bp_batch_step + bp_batch_read_state from pinned host memory, wall clock"},
         "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)],
-                       "max": lat[-1]},
+                       "max": lat[-1],
+                       "note": "device time of one step of all worlds together; the per-request step latency of the "
+                               "serving loop is serving.*.latency_ms"},
         "per_world_launch": per_world,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "kernel": "persistent_step_kernel", "peak_source": peak_kind,
