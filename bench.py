@@ -412,8 +412,9 @@ def run_ours(args, rank, world_size, local_rank):
             dist.barrier()
         return 0
 
-    singles = single_worlds(ctx, args.single_steps) if args.single_steps > 0 else None
-    served = serving(ctx, args) if args.serve_requests > 0 else None
+    # single-world and serving measurements are one-GPU figures: they run in one-process runs only
+    singles = single_worlds(ctx, args.single_steps) if args.single_steps > 0 and world_size == 1 else None
+    served = serving(ctx, args) if args.serve_requests > 0 and world_size == 1 else None
     peak, peak_kind = load_peak()
     achieved = alg_bytes / device_s / 1e9 if device_s > 0 else 0.0
     traffic = None

@@ -435,6 +435,14 @@ int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc
 }
 
 // Launches one step of every world of the set (or of one world when `only` < nWorlds).
+// Blocks of a whole-GPU step of a world of n bubbles: about one thread per bubble (at least 8 blocks), never more
+// than fit on the GPU at once. Every block takes part in every grid barrier, so blocks without bubbles only make the
+// barriers slower.
+int large_blocks_for(const WorldSet& ws, uint32_t n) {
+    const int want = (int)((n + kLargeThreads - 1) / kLargeThreads);
+    return std::max(1, std::min(ws.largeBlocks, std::max(want, 8)));
+}
+
 cudaError_t launch_step(WorldSet& ws, bool perWorld, uint32_t only = 0xffffffffu) {
     cudaError_t err = cudaSuccess;
     cudaStream_t st = ws.ctx->stream;
@@ -442,7 +450,7 @@ cudaError_t launch_step(WorldSet& ws, bool perWorld, uint32_t only = 0xffffffffu
         const DWorld& W = ws.hWorlds[w];
         ws.launches++;
         if (W.n > kCtaMaxBubbles || (W.flags & BP_WORLD_FORCE_MULTI_CTA))
-            return launch_large(ws.S, w, ws.largeB, ws.largeBlocks, kLargeThreads, st);
+            return launch_large(ws.S, w, ws.largeB, large_blocks_for(ws, ws.hWorlds[w].n), kLargeThreads, st);
         QueueArgs q{};
         q.queue = ws.dQueueSingle;
         q.countsOnDevice = 0u;
@@ -467,7 +475,7 @@ cudaError_t launch_step(WorldSet& ws, bool perWorld, uint32_t only = 0xffffffffu
     for (uint32_t w : ws.largeWorlds) {
         if (err != cudaSuccess) break;
         ws.launches++;
-        err = launch_large(ws.S, w, ws.largeB, ws.largeBlocks, kLargeThreads, st);
+        err = launch_large(ws.S, w, ws.largeB, large_blocks_for(ws, ws.hWorlds[w].n), kLargeThreads, st);
     }
     return err;
 }

@@ -117,6 +117,23 @@ __device__ void tree_sort(unsigned long long* keys, unsigned long long* alt, uin
     }
 }
 
+// Sort of a world's leaf keys by its team. The whole-GPU team sorts inside its first block (block barriers instead of
+// the ~32 grid barriers of eight team-wide passes: a few thousand keys sort faster than the grid can synchronise) and
+// the other blocks wait at one grid barrier.
+template <class Team>
+__device__ __forceinline__ void sort_leaf_keys(unsigned long long* keys, unsigned long long* alt, uint32_t* counts,
+                                               uint32_t count, const Team& team) {
+    tree_sort(keys, alt, counts, count, team);
+}
+__device__ __forceinline__ void sort_leaf_keys(unsigned long long* keys, unsigned long long* alt, uint32_t* counts,
+                                               uint32_t count, const GridTeam& team) {
+    if (blockIdx.x == 0) {
+        CtaTeam block{team.sh};
+        tree_sort(keys, alt, counts, count, block);
+    }
+    team.sync();
+}
+
 // Length of the common prefix of sorted keys i and j (-1 outside [0, count)); keys are unique (leaf index bits).
 __device__ __forceinline__ int tree_delta(const unsigned long long* keys, int count, int i, int j) {
     if (j < 0 || j >= count) return -1;
@@ -154,7 +171,7 @@ __device__ bool build_rigid_tree(const DState& S, const DWorld& W, uint32_t wi, 
         keys[p] = ((unsigned long long)code << 32) | p;
     }
     team.sync();
-    tree_sort(keys, S.tKeysAlt + base, S.tCounts + 16ull * base, L, team);
+    sort_leaf_keys(keys, S.tKeysAlt + base, S.tCounts + 16ull * base, L, team);
     if (L == 1u) return true;
     // hierarchy (Karras 2012, "Maximizing parallelism in the construction of BVHs, octrees and k-d trees")
     TreeNode* nodes = S.tNodes + base;
