@@ -384,8 +384,8 @@ int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc
     for (uint32_t w : ws.largeWorlds) ws.largeMaxN = std::max(ws.largeMaxN, ws.hWorlds[w].n);
     ws.largeB = next_pow2(std::max<uint32_t>(2u * ws.largeMaxN, 64u));
     ws.largeBlocks = ws.largeWorlds.empty() ? 0 : large_max_blocks(kLargeThreads);
-    S.gpv = ws.alloc<float>(2ull * std::max(ws.largeBlocks, 1), err);
-    S.gpo = ws.alloc<uint32_t>(2ull * std::max(ws.largeBlocks, 1), err);
+    S.gpv = ws.alloc<float>(8ull * std::max(ws.largeBlocks, 1), err);     // 2 parities x 4 regions per block
+    S.gpo = ws.alloc<uint32_t>(8ull * std::max(ws.largeBlocks, 1), err);
     S.gbuckets = ws.alloc<uint32_t>(ws.largeWorlds.empty() ? 1 : ws.largeB, err);
     S.gentries = ws.alloc<uint32_t>(std::max<uint32_t>(ws.largeMaxN, 1u), err);
     S.barrier = ws.alloc<unsigned int>(2, err);

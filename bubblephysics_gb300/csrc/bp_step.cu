@@ -774,8 +774,7 @@ __device__ void reduce_substep(const DState& S, const DWorld& W, Ctl& c, const T
             if (m < mg.v) { mg.v = m; mg.o = i; }
         }
     }
-    w2 = team.template pick<true>(w2);
-    mg = team.template pick<false>(mg);
+    team.template pick2<true, false>(w2, mg);
     const float stiffnessBound = w2.v > 0.0f ? 1.0f / sqrtf(w2.v) : inf;
     const float hMax = fminf(remaining, stiffnessBound);
     ValOwner db{inf, 0u};

@@ -62,6 +62,8 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x) {
 struct BlockScratch {
     float fv[32];
     uint32_t uo[32];
+    float fv2[32];
+    uint32_t uo2[32];
     uint32_t u[33];
     float bcastF[4];
     uint32_t bcastU[8];
@@ -106,6 +108,27 @@ template <bool kMax> __device__ __forceinline__ ValOwner block_pick(ValOwner x, 
     }
     __syncthreads();
     return ValOwner{sh.fv[0], sh.uo[0]};
+}
+
+// Two (value, owner) reductions in the barriers of one (kMaxA / kMaxB: maximum or minimum).
+template <bool kMaxA, bool kMaxB>
+__device__ __forceinline__ void block_pick2(ValOwner& a, ValOwner& b, BlockScratch& sh) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = (blockDim.x + 31u) >> 5;
+    a = warp_pick<kMaxA>(a);
+    b = warp_pick<kMaxB>(b);
+    __syncthreads();
+    if (lane == 0) { sh.fv[warp] = a.v; sh.uo[warp] = a.o; sh.fv2[warp] = b.v; sh.uo2[warp] = b.o; }
+    __syncthreads();
+    if (warp == 0) {
+        ValOwner x = lane < nw ? ValOwner{sh.fv[lane], sh.uo[lane]} : a;
+        ValOwner y = lane < nw ? ValOwner{sh.fv2[lane], sh.uo2[lane]} : b;
+        x = warp_pick<kMaxA>(x);
+        y = warp_pick<kMaxB>(y);
+        if (lane == 0) { sh.fv[0] = x.v; sh.uo[0] = x.o; sh.fv2[0] = y.v; sh.uo2[0] = y.o; }
+    }
+    __syncthreads();
+    a = ValOwner{sh.fv[0], sh.uo[0]};
+    b = ValOwner{sh.fv2[0], sh.uo2[0]};
 }
 
 __device__ __forceinline__ uint32_t block_sum(uint32_t x, BlockScratch& sh) {
@@ -179,6 +202,9 @@ struct CtaTeam {
     __device__ bool sync() const { __syncthreads(); return true; }
     __device__ bool ok() const { return true; }
     template <bool kMax> __device__ ValOwner pick(ValOwner x) const { return block_pick<kMax>(x, *sh); }
+    template <bool kMaxA, bool kMaxB> __device__ void pick2(ValOwner& a, ValOwner& b) const {
+        block_pick2<kMaxA, kMaxB>(a, b, *sh);
+    }
     __device__ uint32_t sum(uint32_t x) const { return block_sum(x, *sh); }
     __device__ uint32_t umax(uint32_t x) const { return block_max(x, *sh); }
     __device__ float fmax(float x) const { return block_fmax(x, *sh); }
@@ -212,6 +238,10 @@ struct WarpTeam {
     __device__ bool sync() const { __syncwarp(); return true; }
     __device__ bool ok() const { return true; }
     template <bool kMax> __device__ ValOwner pick(ValOwner x) const { return warp_pick<kMax>(x); }
+    template <bool kMaxA, bool kMaxB> __device__ void pick2(ValOwner& a, ValOwner& b) const {
+        a = warp_pick<kMaxA>(a);
+        b = warp_pick<kMaxB>(b);
+    }
     __device__ uint32_t sum(uint32_t x) const { return warp_sum(x); }
     __device__ uint32_t umax(uint32_t x) const { return warp_max(x); }
     __device__ float fmax(float x) const { return warp_fmax(x); }
@@ -235,14 +265,16 @@ struct WarpTeam {
 
 // ----------------------------------------------------------------------------------------------------------------
 // Grid team: every block of a cooperative launch works on one world. Partials go through global memory with
-// alternating parity so a reduction never overwrites partials another block may still read.
+// alternating parity so a reduction never overwrites partials another block may still read; each parity has four
+// regions of gridDim.x entries (pv: 4 x 2 x grid floats, po: 4 x 2 x grid words), so up to four values reduce
+// behind one grid barrier.
 // ----------------------------------------------------------------------------------------------------------------
 struct GridTeam {
     BlockScratch* sh;
     unsigned int* bar;       // [0] arrivals, [1] generation
     uint32_t* err;
-    float* pv;               // 2 x gridDim.x partial values
-    uint32_t* po;            // 2 x gridDim.x partial owners / counts
+    float* pv;               // 2 parities x 4 regions x gridDim.x partial values
+    uint32_t* po;            // 2 parities x 4 regions x gridDim.x partial owners / counts
     uint32_t* parity;        // per-thread copy lives in registers; this is unused storage
     mutable uint32_t par;
     mutable bool failed;
@@ -282,7 +314,7 @@ struct GridTeam {
 
     template <bool kMax> __device__ ValOwner pick(ValOwner x) const {
         x = block_pick<kMax>(x, *sh);
-        uint32_t base = par * gridDim.x;
+        uint32_t base = par * 4u * gridDim.x;
         if (threadIdx.x == 0) { pv[base + blockIdx.x] = x.v; po[base + blockIdx.x] = x.o; }
         par ^= 1u;
         sync();
@@ -298,9 +330,35 @@ struct GridTeam {
         __syncthreads();
         return ValOwner{sh->bcastF[0], sh->bcastU[0]};
     }
+    template <bool kMaxA, bool kMaxB> __device__ void pick2(ValOwner& a, ValOwner& b) const {
+        block_pick2<kMaxA, kMaxB>(a, b, *sh);
+        const uint32_t base = par * 4u * gridDim.x, G = gridDim.x;
+        if (threadIdx.x == 0) {
+            pv[base + blockIdx.x] = a.v; po[base + blockIdx.x] = a.o;
+            pv[base + G + blockIdx.x] = b.v; po[base + G + blockIdx.x] = b.o;
+        }
+        par ^= 1u;
+        sync();
+        if (threadIdx.x < 32) {
+            const float inf = __int_as_float(0x7f800000);
+            ValOwner x{kMaxA ? -inf : inf, 0xffffffffu}, y{kMaxB ? -inf : inf, 0xffffffffu};
+            for (uint32_t blk = threadIdx.x; blk < G; blk += 32) {
+                ValOwner z{__ldcg(pv + base + blk), __ldcg(po + base + blk)};
+                ValOwner w{__ldcg(pv + base + G + blk), __ldcg(po + base + G + blk)};
+                x = kMaxA ? pick_max(x, z) : pick_min(x, z);
+                y = kMaxB ? pick_max(y, w) : pick_min(y, w);
+            }
+            x = warp_pick<kMaxA>(x);
+            y = warp_pick<kMaxB>(y);
+            if (threadIdx.x == 0) { sh->bcastF[0] = x.v; sh->bcastU[0] = x.o; sh->bcastF[2] = y.v; sh->bcastU[3] = y.o; }
+        }
+        __syncthreads();
+        a = ValOwner{sh->bcastF[0], sh->bcastU[0]};
+        b = ValOwner{sh->bcastF[2], sh->bcastU[3]};
+    }
     __device__ uint32_t reduce_u(uint32_t x, bool isMax) const {
         x = isMax ? block_max(x, *sh) : block_sum(x, *sh);
-        uint32_t base = par * gridDim.x;
+        uint32_t base = par * 4u * gridDim.x;
         if (threadIdx.x == 0) po[base + blockIdx.x] = x;
         par ^= 1u;
         sync();
@@ -318,13 +376,36 @@ struct GridTeam {
     }
     __device__ uint32_t sum(uint32_t x) const { return reduce_u(x, false); }
     __device__ uint32_t umax(uint32_t x) const { return reduce_u(x, true); }
+    // Four sums / maxima behind one grid barrier (kMaxMask bit c set: maximum for component c).
     template <uint32_t kMaxMask> __device__ void reduce4(uint32_t (&v)[4]) const {
+        block_reduce4<kMaxMask>(v, *sh);
+        const uint32_t base = par * 4u * gridDim.x, G = gridDim.x;
+        if (threadIdx.x == 0) {
 #pragma unroll
-        for (int c = 0; c < 4; ++c) v[c] = reduce_u(v[c], ((kMaxMask >> c) & 1u) != 0u);
+            for (int c = 0; c < 4; ++c) po[base + c * G + blockIdx.x] = v[c];
+        }
+        par ^= 1u;
+        sync();
+        if (threadIdx.x < 32) {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const bool isMax = ((kMaxMask >> c) & 1u) != 0u;
+                uint32_t y = 0;
+                for (uint32_t blk = threadIdx.x; blk < G; blk += 32) {
+                    uint32_t z = __ldcg(po + base + c * G + blk);
+                    y = isMax ? max(y, z) : y + z;
+                }
+                y = isMax ? warp_max(y) : warp_sum(y);
+                if (threadIdx.x == 0) sh->u4[c][32] = y;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < 4; ++c) v[c] = sh->u4[c][32];
     }
     __device__ float fmax(float x) const {
         x = block_fmax(x, *sh);
-        uint32_t base = par * gridDim.x;
+        uint32_t base = par * 4u * gridDim.x;
         if (threadIdx.x == 0) pv[base + blockIdx.x] = x;
         par ^= 1u;
         sync();
@@ -347,7 +428,7 @@ struct GridTeam {
         for (uint32_t i = tf; i < tl; ++i) local += __ldcg(values + i);
         uint32_t total;
         uint32_t running = block_excl_scan(local, &total, *sh);
-        uint32_t base = par * gridDim.x;
+        uint32_t base = par * 4u * gridDim.x;
         if (threadIdx.x == 0) po[base + blockIdx.x] = total;
         par ^= 1u;
         sync();
