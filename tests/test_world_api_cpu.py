@@ -7,7 +7,7 @@ import pytest
 
 from bubblephysics_gb300 import _native as N
 from bubblephysics_gb300 import world as W
-from bubblephysics_gb300.world import (BubbleDescriptor, BubbleWorld, Circle, CollisionFilter, MotionRole,
+from bubblephysics_gb300.world import (BubbleDescriptor, BubbleWorld, Circle, MotionRole,
                                        PhysicsMaterial, RigidBodyDescriptor, TransactionRejectionReason as R,
                                        WorldConfiguration, WorldTransaction)
 
