@@ -176,7 +176,7 @@ def run_reference(args, rank):
     return 0
 
 
-def single_world_rate(spec, ctx, steps: int, warmup: int) -> dict:
+def single_world_rate(spec, ctx, steps: int, warmup: int, contours: bool = False) -> dict:
     """One world stepped through bp_world_step: device time per step (CUDA events on the library's stream) and
     bubble-substeps per second over `steps` timed steps after `warmup` untimed ones."""
     from bubblephysics_gb300.solver import World
@@ -189,13 +189,19 @@ def single_world_rate(spec, ctx, steps: int, warmup: int) -> dict:
         ms.append(float(reps["gpu_ms"][0]))
         subs += int(reps["substep_count"][0]) * spec.bubble_count
     keys = world.rigid_keys().size
+    contour = None
+    if contours:
+        # draw-only contours of the published state (bp_world_contours): device time of the contour kernel
+        world.contours()
+        _, counts, _, _, cms = world.contours()
+        contour = {"ms": cms, "samples": int(counts.sum()), "samples_per_s": float(counts.sum()) / (cms / 1e3)}
     world.close()
     total_s = sum(ms) / 1000.0
     return {"bubbles": spec.bubble_count, "segments": len(spec.segments), "bodies": len(spec.bodies),
             "steps": steps, "warmup": warmup, "ms_per_step": total_s * 1000.0 / max(steps, 1),
             "substeps_per_step": subs / max(spec.bubble_count * steps, 1),
             "value": subs / total_s if total_s > 0 else 0.0, "unit": UNIT, "statuses": sorted(set(statuses)),
-            "rigid_tree_leaves": keys}
+            "rigid_tree_leaves": keys, "contours": contour}
 
 
 def single_worlds(ctx, steps: int) -> dict:
@@ -205,7 +211,7 @@ def single_worlds(ctx, steps: int) -> dict:
     import dataclasses
     from bubblephysics_gb300 import _native as N
     from bubblephysics_gb300 import scenes
-    out = {"large_world": single_world_rate(scenes.large_world(), ctx, steps, 3)}
+    out = {"large_world": single_world_rate(scenes.large_world(), ctx, steps, 3, contours=True)}
     rigid = scenes.rigid_world()
     out["rigid_world"] = single_world_rate(rigid, ctx, steps, 3)
     brute = dataclasses.replace(rigid, flags=rigid.flags | N.WORLD_NO_RIGID_TREE)

@@ -127,6 +127,11 @@ class BatchConfig(C.Structure):
                 ("reserved", C.c_uint32)]
 
 
+class ContourConfig(C.Structure):
+    _fields_ = [("max_edge", C.c_float), ("surface_tension", C.c_float), ("clearance", C.c_float),
+                ("stride", C.c_uint32)]
+
+
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_worlds", C.c_uint32), ("max_batch_worlds", C.c_uint32),
                 ("streams", C.c_uint32), ("threads_per_world", C.c_uint32), ("warp_world_max", C.c_uint32),
@@ -148,7 +153,7 @@ class ServerStats(C.Structure):
 
 SERVER_PER_WORLD = 1
 
-RECORD_SIZES = {ServerConfig: 32, ServerCompletion: 136, ServerStats: 80, Bubble: 80, Segment: 64, Body: 80, ForceField: 64, Band: 24, Motor: 24, WorldDesc: 64,
+RECORD_SIZES = {ContourConfig: 16, ServerConfig: 32, ServerCompletion: 136, ServerStats: 80, Bubble: 80, Segment: 64, Body: 80, ForceField: 64, Band: 24, Motor: 24, WorldDesc: 64,
                 StepReport: 96, Contact: 64, CandidateKey: 24}
 for _t, _n in RECORD_SIZES.items():
     assert C.sizeof(_t) == _n, f"{_t.__name__} is {C.sizeof(_t)} bytes, the C ABI says {_n}"
@@ -229,6 +234,8 @@ _SIGNATURES = {
                                           C.POINTER(Segment), C.c_uint32, C.POINTER(C.c_uint32)]),
     "bp_device_contact_law": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint32]),
     "bp_world_step_noalloc": (C.c_int, [C.POINTER(WorldDesc), _P, C.c_uint32, _P, C.c_uint32, C.c_uint32, _P, _P]),
+    "bp_world_contours": (C.c_int, [_P, C.POINTER(ContourConfig), _P, _P, _P, _P, C.POINTER(C.c_uint32),
+                                    C.POINTER(C.c_float)]),
     "bp_server_create": (C.c_int, [_P, C.POINTER(ServerConfig), C.POINTER(_P)]),
     "bp_server_destroy": (C.c_int, [_P]),
     "bp_server_add_world": (C.c_int, [_P, C.POINTER(WorldDesc), C.POINTER(WorldInput), C.POINTER(C.c_uint32)]),

@@ -958,6 +958,48 @@ int bp_world_read_rigid_keys(bp_world* world, uint64_t* out, uint32_t capacity, 
     return cuda_status(err);
 }
 
+int bp_world_contours(bp_world* world, const bp_contour_config* config, float* points_xy, uint32_t* counts,
+                      float* level, float* shape, uint32_t* stride_out, float* gpu_ms) {
+    if (!world || !config) return BP_E_INVALID;
+    const float maxEdge = config->max_edge, tension = config->surface_tension, clearance = config->clearance;
+    if (!(maxEdge > 0.0f) || !std::isfinite(maxEdge) || !(tension >= 0.0f) || !std::isfinite(tension) ||
+        !(clearance >= 0.0f) || !std::isfinite(clearance))
+        return BP_E_INVALID;
+    WorldSet& ws = world->set;
+    const DWorld& W = ws.hWorlds[0];
+    uint32_t need = 64u;
+    for (uint32_t i = 0; i < W.n; ++i) need = std::max(need, contour_samples(ws.hBubbles[W.boff + i].radius, maxEdge, 0xffffffffu));
+    const uint32_t stride = config->stride ? config->stride : need;
+    if (stride_out) *stride_out = stride;
+    if (stride > 1024u) return BP_E_CAPACITY;
+    if (gpu_ms) *gpu_ms = 0.0f;
+    if ((!points_xy && !counts && !level && !shape) || W.n == 0u) return BP_OK;
+    DeviceGuard guard(ws.ctx->device);
+    cudaStream_t st = ws.ctx->stream;
+    const uint64_t samples = (uint64_t)W.n * stride;
+    float2* dPoints = nullptr;
+    uint32_t* dCounts = nullptr;
+    float* dLevel = nullptr;
+    float* dShape = nullptr;
+    cudaError_t err = cudaMallocAsync(&dPoints, samples * sizeof(float2), st);
+    if (!err) err = cudaMallocAsync(&dCounts, (size_t)W.n * sizeof(uint32_t), st);
+    if (!err) err = cudaMallocAsync(&dLevel, samples * sizeof(float), st);
+    if (!err) err = cudaMallocAsync(&dShape, (size_t)W.n * 6u * sizeof(float), st);
+    if (!err) err = cudaEventRecord(ws.ctx->start, st);
+    if (!err) err = launch_contours(ws.S, W, maxEdge, tension, clearance, stride, dPoints, dCounts, dLevel, dShape, st);
+    if (!err) err = cudaEventRecord(ws.ctx->stop, st);
+    if (!err && points_xy) err = cudaMemcpyAsync(points_xy, dPoints, samples * sizeof(float2), cudaMemcpyDeviceToHost, st);
+    if (!err && counts) err = cudaMemcpyAsync(counts, dCounts, (size_t)W.n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    if (!err && level) err = cudaMemcpyAsync(level, dLevel, samples * sizeof(float), cudaMemcpyDeviceToHost, st);
+    if (!err && shape) err = cudaMemcpyAsync(shape, dShape, (size_t)W.n * 6u * sizeof(float), cudaMemcpyDeviceToHost, st);
+    if (!err) err = cudaStreamSynchronize(st);
+    if (!err && gpu_ms) cudaEventElapsedTime(gpu_ms, ws.ctx->start, ws.ctx->stop);
+    for (void* p : {(void*)dPoints, (void*)dCounts, (void*)dLevel, (void*)dShape})
+        if (p) cudaFreeAsync(p, st);
+    cudaError_t fin = cudaStreamSynchronize(st);
+    return cuda_status(err ? err : fin);
+}
+
 int bp_world_read_substeps(bp_world* world, float* out, uint32_t capacity, uint32_t* count) {
     if (!world) return BP_E_INVALID;
     WorldSet& ws = world->set;

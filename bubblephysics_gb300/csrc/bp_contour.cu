@@ -1,0 +1,179 @@
+// bp_contour.cu - bubble contours of a world's published state as a headless device buffer (draw-only data: contours
+// never feed back into the physics).
+//
+// The reference builds them after the step in three passes (NativePostSolveKernels.metal-source):
+// nativeAccumulateContactPressure (:280-334) casts one ray per sample from the centre and shortens it to the nearest
+// one-sided segment and to the flat chord of every overlapping pair, which lies at r (1 - eps) from the centre with
+// eps the pair law's deflection of this end; nativeGenerateContoursFused (:353-381) smooths the radial deficits with
+// 13 Jacobi passes that never go below the hard limit; nativePrepareRenderDataGrouped (:437-527) closes the field with
+// the smallest majorant of bounded slope (two serial passes from the global maximum), then writes the points, the
+// bounds, the effective radius and the largest deficit. Here one block steps one bubble through all three, one thread
+// per sample, with the deficits in shared memory; the serial majorant runs on one thread like the reference's (a chain
+// of float subtractions whose order fixes the bits).
+#include "bp_device.cuh"
+
+namespace bp {
+
+constexpr uint32_t kContourPasses = 13;
+
+struct ContourArgs {
+    float maxEdge, tension, clearance;
+    uint32_t stride;
+};
+
+// nativeContourRayLimit (NativePostSolveKernels:268-277)
+__device__ __forceinline__ float contour_ray_limit(float2 center, float2 direction, float2 a, float2 b, float radius,
+                                                   float clearance) {
+    const float2 edge = sub(b, a), offset = sub(a, center);
+    const float denominator = cross2(direction, edge);
+    if (fabsf(denominator) < 1e-6f) return radius;
+    const float distance = cross2(offset, edge) / denominator;
+    const float fraction = cross2(offset, direction) / denominator;
+    return distance >= 0.0f && fraction >= 0.0f && fraction <= 1.0f ? fminf(radius, fmaxf(0.0f, distance - clearance))
+                                                                      : radius;
+}
+
+__global__ void __launch_bounds__(1024) contour_kernel(DState S, DWorld W, ContourArgs a, float2* points,
+                                                       uint32_t* counts, float* level, float* shape) {
+    __shared__ float lvl[1024];
+    __shared__ float part[32][6];
+    __shared__ float seedMaximum;
+    const uint32_t i = blockIdx.x, s = threadIdx.x, g = W.boff + i;
+    const float r = S.phys[g].x;
+    const bool gone = (S.flags[g] & kRemoved) != 0u || !(r > 0.0f);
+    const uint32_t count = gone ? 0u : contour_samples(r, a.maxEdge, a.stride);
+    if (s == 0) counts[i] = count;
+    if (count == 0u) return;  // uniform over the block
+    const bool active = s < count;
+    const float2 c = S.pPos[g];
+    float2 direction = f2(1.0f, 0.0f);
+    float deficit = 0.0f;
+    if (active) {
+        const float angle = 2.0f * kPiF * (float)s / (float)count;
+        direction = f2(cosf(angle), sinf(angle));
+        float limit = r;
+        const uint2 fi = S.filter[g];
+        for (uint32_t j = 0; j < W.s; ++j) {
+            const DSegment& sg = S.seg[W.soff + j];
+            if (!filter_accepts(fi, make_uint2(sg.cat, sg.mask))) continue;
+            limit = contour_ray_limit(c, direction, sg.a, sg.b, limit, a.clearance);
+        }
+        const uint32_t* row = S.adj + W.rowOff + (uint64_t)i * W.k;
+        const uint32_t deg = S.deg[g];
+        for (uint32_t e = 0; e < deg; ++e) {
+            const uint32_t key = row[e];
+            if (key >> kKindShift) continue;  // walls and segments cut the contour through the loop above
+            const uint32_t j = key & kIndexMask, gj = W.boff + j;
+            const float2 delta = sub(S.pPos[gj], c);
+            const float distance = len2(delta);
+            const float rj = S.phys[gj].x;
+            if (distance <= 1.1920929e-7f || distance >= r + rj) continue;
+            const float2 normal = dvd(delta, distance);
+            const bool lowIsSelf = i < j;
+            const float4 first = lowIsSelf ? S.phys[g] : S.phys[gj], second = lowIsSelf ? S.phys[gj] : S.phys[g];
+            const Law law = pair_law(first.z, first.x, second.z, second.x, distance);
+            const float eps = lowIsSelf ? law.epsA : law.epsB;
+            const float plane = clampf(r * (1.0f - eps), 0.0f, r);
+            const float half = sqrtf(fmaxf(0.0f, r * r - plane * plane));
+            const float2 tangent = f2(-normal.y, normal.x);
+            const float2 point = add(c, mul(normal, plane));
+            limit = contour_ray_limit(c, direction, sub(point, mul(tangent, half)), add(point, mul(tangent, half)), limit,
+                                      a.clearance);
+        }
+        deficit = clampf(1.0f - limit / r, 0.0f, 1.0f);
+    }
+    // smoothing: a convex combination with the neighbours' mean, never below the hard deficit
+    float x = deficit;
+    const float floorValue = deficit;
+    lvl[s] = active ? x : 0.0f;
+    __syncthreads();
+    const float tension = fminf(0.8f, a.tension / (a.tension + 10.0f));
+    for (uint32_t pass = 0; pass < kContourPasses; ++pass) {
+        if (active) {
+            const float neighbour = (lvl[(s + count - 1u) % count] + lvl[(s + 1u) % count]) * 0.5f;
+            x = clampf(fmaxf(floorValue, x + (neighbour - x) * tension), 0.0f, 1.0f);
+        }
+        __syncthreads();
+        lvl[s] = x;
+        __syncthreads();
+    }
+    // bounded-slope majorant from the global maximum, both ways round
+    if (s == 0) {
+        float maximum = 0.0f;
+        uint32_t anchor = 0;
+        for (uint32_t k = 0; k < count; ++k)
+            if (lvl[k] > maximum) { maximum = lvl[k]; anchor = k; }
+        const float slope = a.maxEdge / (2.0f * r);
+        float previous = maximum;
+        for (uint32_t step = 1; step < count; ++step) {
+            const uint32_t k = (anchor + step) % count;
+            const float v = fmaxf(lvl[k], previous - slope);
+            lvl[k] = v;
+            previous = v;
+        }
+        previous = maximum;
+        for (uint32_t step = 1; step < count; ++step) {
+            const uint32_t k = (anchor + count - step) % count;
+            const float v = fmaxf(lvl[k], previous - slope);
+            lvl[k] = v;
+            previous = v;
+        }
+        seedMaximum = maximum;
+    }
+    __syncthreads();
+    const float inf = __int_as_float(0x7f800000);
+    float v[6] = {inf, -inf, inf, inf, -inf, -inf};  // min |p - c|, max level, bounds min x, min y, max x, max y
+    if (active) {
+        const float l = lvl[s];
+        const float2 p = add(c, mul(direction, r * (1.0f - l)));
+        const uint64_t at = (uint64_t)i * a.stride + s;
+        points[at] = p;
+        if (level) level[at] = l;
+        v[0] = len2(sub(p, c));
+        v[1] = l;
+        v[2] = p.x; v[3] = p.y; v[4] = p.x; v[5] = p.y;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        v[0] = fminf(v[0], __shfl_xor_sync(0xffffffffu, v[0], off));
+        v[1] = fmaxf(v[1], __shfl_xor_sync(0xffffffffu, v[1], off));
+        v[2] = fminf(v[2], __shfl_xor_sync(0xffffffffu, v[2], off));
+        v[3] = fminf(v[3], __shfl_xor_sync(0xffffffffu, v[3], off));
+        v[4] = fmaxf(v[4], __shfl_xor_sync(0xffffffffu, v[4], off));
+        v[5] = fmaxf(v[5], __shfl_xor_sync(0xffffffffu, v[5], off));
+    }
+    const uint32_t lane = s & 31u, warp = s >> 5, warps = (blockDim.x + 31u) >> 5;
+    if (lane == 0)
+        for (int q = 0; q < 6; ++q) part[warp][q] = v[q];
+    __syncthreads();
+    if (s == 0) {
+        for (uint32_t w = 1; w < warps; ++w) {
+            v[0] = fminf(v[0], part[w][0]);
+            v[1] = fmaxf(v[1], part[w][1]);
+            v[2] = fminf(v[2], part[w][2]);
+            v[3] = fminf(v[3], part[w][3]);
+            v[4] = fmaxf(v[4], part[w][4]);
+            v[5] = fmaxf(v[5], part[w][5]);
+        }
+        float* out = shape + (uint64_t)i * 6u;
+        out[0] = fmaxf(seedMaximum, v[1]);       // largest deficit
+        out[1] = fminf(r, v[0]);                 // effective radius
+        out[2] = fminf(c.x, v[2]);
+        out[3] = fminf(c.y, v[3]);
+        out[4] = fmaxf(c.x, v[4]);
+        out[5] = fmaxf(c.y, v[5]);
+    }
+}
+
+cudaError_t launch_contours(const DState& S, const DWorld& W, float maxEdge, float tension, float clearance,
+                            uint32_t stride, float2* points, uint32_t* counts, float* level, float* shape,
+                            cudaStream_t stream) {
+    if (W.n == 0u) return cudaSuccess;
+    if (stride == 0u || stride > 1024u) return cudaErrorInvalidValue;
+    ContourArgs a{maxEdge, tension, clearance, stride};
+    const uint32_t threads = (stride + 31u) & ~31u;
+    contour_kernel<<<W.n, threads, 0, stream>>>(S, W, a, points, counts, level, shape);
+    return cudaGetLastError();
+}
+
+}  // namespace bp

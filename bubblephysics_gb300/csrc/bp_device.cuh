@@ -170,6 +170,17 @@ struct QueueArgs {
     uint32_t tree;                    // 1: some world uses the LBVH (launch the tree-capable kernel)
 };
 
+constexpr float kPiF = 3.14159265358979323846f;
+
+// Contour samples of a bubble of radius r (nativeAccumulateContactPressure, NativePostSolveKernels:292):
+// max(64, ceil((r / maxEdge) * 4 pi)), at most `stride`.
+__host__ __device__ inline uint32_t contour_samples(float r, float maxEdge, uint32_t stride) {
+    const float q = (r / maxEdge) * (4.0f * kPiF);
+    const uint32_t want = (uint32_t)ceilf(q);
+    const uint32_t count = want > 64u ? want : 64u;
+    return count < stride ? count : stride;
+}
+
 // Bytes of a world's shared-memory workspace: per bubble 88 B of hot state, per segment and body a 32 B box, per body
 // a 16 B pose; the 15 parts are each padded to 16 bytes.
 __host__ __device__ inline uint32_t workspace_bytes(uint32_t n, uint32_t s, uint32_t nb) {

@@ -27,6 +27,9 @@ void prepare_kernels();
 cudaError_t launch_served(const DState* sets, const uint32_t* entrySlot, bp_step_report* reports, const QueueArgs& q,
                           uint32_t threads, uint32_t blocks, cudaStream_t stream);
 cudaError_t launch_sum(const uint32_t* v, uint64_t n, unsigned long long* total, cudaStream_t stream);
+cudaError_t launch_contours(const DState& S, const DWorld& W, float maxEdge, float tension, float clearance,
+                            uint32_t stride, float2* points, uint32_t* counts, float* level, float* shape,
+                            cudaStream_t stream);
 }  // namespace bp
 
 struct bp_context {

@@ -129,6 +129,24 @@ class World:
     def substeps(self) -> np.ndarray:
         return self._read(self.lib.bp_world_read_substeps, np.float32, "bp_world_read_substeps")
 
+    def contours(self, max_edge: float = 8.0, surface_tension: float = 20.0, clearance: float = 1e-4, stride: int = 0):
+        """Contours of the published state built on the device (bp_world_contours): points (n, stride, 2), counts (n,),
+        level (n, stride), shape (n, 6: largest deficit, effective radius, bounds) and the kernel's device ms."""
+        cfg = N.ContourConfig(max_edge, surface_tension, clearance, stride)
+        used = C.c_uint32()
+        N.check(self.lib.bp_world_contours(self.handle, C.byref(cfg), None, None, None, None, C.byref(used), None),
+                "bp_world_contours")
+        s = used.value
+        points = np.zeros((self.n, s, 2), np.float32)
+        counts = np.zeros(self.n, np.uint32)
+        level = np.zeros((self.n, s), np.float32)
+        shape = np.zeros((self.n, 6), np.float32)
+        ms = C.c_float()
+        N.check(self.lib.bp_world_contours(self.handle, C.byref(cfg), C.c_void_p(points.ctypes.data),
+                                           C.c_void_p(counts.ctypes.data), C.c_void_p(level.ctypes.data),
+                                           C.c_void_p(shape.ctypes.data), C.byref(used), C.byref(ms)), "bp_world_contours")
+        return points, counts, level, shape, ms.value
+
     def rigid_keys(self) -> np.ndarray:
         """Sorted LBVH keys (Morton code << 32 | leaf) of the last step; empty when the step used no tree."""
         return self._read(self.lib.bp_world_read_rigid_keys, np.uint64, "bp_world_read_rigid_keys")

@@ -346,6 +346,27 @@ int bp_batch_adjacency_entries(bp_batch* batch, uint64_t* entries);
  * persistent launch, [3] worlds stepped by a whole block, [4] worlds stepped by one warp. */
 int bp_batch_tuning(bp_batch* batch, uint32_t* values, uint32_t count);
 
+/* ---- contours (draw-only output of the step) ------------------------------------------------------------------ */
+
+/* Contour parameters (NativeMetalContourControl.shape, NativeMetalBufferLayout.swift:175-178; defaults of
+ * ReferenceConfiguration: maxContourSegmentLength 8, contourSurfaceTension 20, positionTolerance 1e-4). 16 bytes. */
+typedef struct bp_contour_config {
+    float max_edge;                  /* longest contour edge; samples per bubble = max(64, ceil(4 pi r / max_edge)) */
+    float surface_tension;           /* smoothing weight tension / (tension + 10), at most 0.8 */
+    float clearance;                 /* rays stop this far before a segment or chord */
+    uint32_t stride;                 /* samples reserved per bubble; 0 = the largest sample count of the world */
+} bp_contour_config;
+
+/* Contours of the world's published state, built on the device (nativeAccumulateContactPressure,
+ * nativeGenerateContoursFused and nativePrepareRenderDataGrouped, NativePostSolveKernels:280-527: one ray per sample cut
+ * by the one-sided segments and by the chord r (1 - eps) of every overlapping pair, 13 smoothing passes, the
+ * bounded-slope majorant). Host outputs, each may be NULL: points_xy (bubble_count x stride float2), counts (samples
+ * of each bubble; 0 for a removed one), level (bubble_count x stride deficits), shape (bubble_count x 6: largest
+ * deficit, effective radius, bounds min.xy, max.xy). *stride_out = the stride used; with every output NULL the call
+ * only reports it. gpu_ms (may be NULL) = device time of the kernel. Samples beyond a stride of 1024: BP_E_CAPACITY. */
+int bp_world_contours(bp_world* world, const bp_contour_config* config, float* points_xy, uint32_t* counts,
+                      float* level, float* shape, uint32_t* stride_out, float* gpu_ms);
+
 /* ---- serving loop (no counterpart in the reference) ------------------------------------------------------------ */
 
 /* A request loop over many worlds that stay resident on the device. The reference steps one world per call

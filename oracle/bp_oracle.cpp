@@ -1402,6 +1402,116 @@ template <typename T> std::vector<uint64_t> rigid_keys(const World<T>& w) {
     return keys;
 }
 
+// ---------------------------------------------------------------------------------------------------------------
+// Contours of the published state (NativePostSolveKernels:268-527: nativeContourRayLimit,
+// nativeAccumulateContactPressure, nativeGenerateContoursFused, nativePrepareRenderDataGrouped), in float.
+// ---------------------------------------------------------------------------------------------------------------
+static float contour_ray_limit(float cx, float cy, float dx, float dy, float ax, float ay, float bx, float by,
+                               float radius, float clearance) {
+    float ex = bx - ax, ey = by - ay, ox = ax - cx, oy = ay - cy;
+    float denominator = dx * ey - dy * ex;
+    if (std::fabs(denominator) < 1e-6f) return radius;
+    float distance = (ox * ey - oy * ex) / denominator;
+    float fraction = (ox * dy - oy * dx) / denominator;
+    return distance >= 0.0f && fraction >= 0.0f && fraction <= 1.0f ? std::fmin(radius, std::fmax(0.0f, distance - clearance))
+                                                                      : radius;
+}
+
+static uint32_t contour_samples(float r, float maxEdge, uint32_t stride) {
+    const float pi = 3.14159265358979323846f;
+    uint32_t want = (uint32_t)std::ceil((r / maxEdge) * (4.0f * pi));
+    uint32_t count = std::max(want, 64u);
+    return std::min(count, stride);
+}
+
+static void world_contours(const World<float>& w, float maxEdge, float tension, float clearance, uint32_t stride,
+                           float* points, uint32_t* counts, float* level, float* shape) {
+    const float pi = 3.14159265358979323846f;
+    for (uint32_t i = 0; i < w.n; ++i) {
+        const float r = w.radius[i];
+        uint32_t count = (is_removed(w, i) || !(r > 0.0f)) ? 0u : contour_samples(r, maxEdge, stride);
+        counts[i] = count;
+        if (!count) continue;
+        const float cx = w.pPos[i].x, cy = w.pPos[i].y;
+        std::vector<float> dirx(count), diry(count), hard(count), lvl(count);
+        for (uint32_t s = 0; s < count; ++s) {
+            float angle = 2.0f * pi * (float)s / (float)count;
+            dirx[s] = std::cos(angle);
+            diry[s] = std::sin(angle);
+            float limit = r;
+            for (uint32_t j = 0; j < w.s; ++j) {
+                if (!filter_accepts(w.cat[i], w.mask[i], w.scat[j], w.smask[j])) continue;
+                limit = contour_ray_limit(cx, cy, dirx[s], diry[s], w.sa[j].x, w.sa[j].y, w.sb[j].x, w.sb[j].y, limit, clearance);
+            }
+            for (uint32_t key : w.adj[i]) {
+                if (key >> 30) continue;
+                uint32_t j = key & 0x3fffffffu;
+                float ddx = w.pPos[j].x - cx, ddy = w.pPos[j].y - cy;
+                float distance = std::sqrt(ddx * ddx + ddy * ddy);
+                if (distance <= 1.1920929e-7f || distance >= r + w.radius[j]) continue;
+                float nx = ddx / distance, ny = ddy / distance;
+                bool lowIsSelf = i < j;
+                uint32_t lo = lowIsSelf ? i : j, hi = lowIsSelf ? j : i;
+                Law<float> law = pair_law(w.K[lo], w.radius[lo], w.K[hi], w.radius[hi], distance);
+                float eps = lowIsSelf ? law.epsA : law.epsB;
+                float plane = std::fmin(std::fmax(r * (1.0f - eps), 0.0f), r);
+                float half = std::sqrt(std::fmax(0.0f, r * r - plane * plane));
+                float tx = -ny, ty = nx;
+                float px = cx + nx * plane, py = cy + ny * plane;
+                limit = contour_ray_limit(cx, cy, dirx[s], diry[s], px - tx * half, py - ty * half, px + tx * half,
+                                          py + ty * half, limit, clearance);
+            }
+            float deficit = std::fmin(std::fmax(1.0f - limit / r, 0.0f), 1.0f);
+            hard[s] = deficit;
+            lvl[s] = deficit;
+        }
+        const float weight = std::fmin(0.8f, tension / (tension + 10.0f));
+        std::vector<float> next(count);
+        for (int pass = 0; pass < 13; ++pass) {
+            for (uint32_t s = 0; s < count; ++s) {
+                float neighbour = (lvl[(s + count - 1) % count] + lvl[(s + 1) % count]) * 0.5f;
+                next[s] = std::fmin(std::fmax(std::fmax(hard[s], lvl[s] + (neighbour - lvl[s]) * weight), 0.0f), 1.0f);
+            }
+            lvl.swap(next);
+        }
+        float maximum = 0.0f;
+        uint32_t anchor = 0;
+        for (uint32_t s = 0; s < count; ++s)
+            if (lvl[s] > maximum) { maximum = lvl[s]; anchor = s; }
+        const float slope = maxEdge / (2.0f * r);
+        float previous = maximum;
+        for (uint32_t step = 1; step < count; ++step) {
+            uint32_t s = (anchor + step) % count;
+            float v = std::fmax(lvl[s], previous - slope);
+            lvl[s] = v;
+            previous = v;
+        }
+        previous = maximum;
+        for (uint32_t step = 1; step < count; ++step) {
+            uint32_t s = (anchor + count - step) % count;
+            float v = std::fmax(lvl[s], previous - slope);
+            lvl[s] = v;
+            previous = v;
+        }
+        float effective = r, top = maximum, bx0 = cx, by0 = cy, bx1 = cx, by1 = cy;
+        for (uint32_t s = 0; s < count; ++s) {
+            float scale = r * (1.0f - lvl[s]);
+            float px = cx + dirx[s] * scale, py = cy + diry[s] * scale;
+            uint64_t at = (uint64_t)i * stride + s;
+            points[2 * at] = px;
+            points[2 * at + 1] = py;
+            level[at] = lvl[s];
+            float ex = px - cx, ey = py - cy;
+            effective = std::fmin(effective, std::sqrt(ex * ex + ey * ey));
+            top = std::fmax(top, lvl[s]);
+            bx0 = std::fmin(bx0, px); by0 = std::fmin(by0, py);
+            bx1 = std::fmax(bx1, px); by1 = std::fmax(by1, py);
+        }
+        float* out = shape + 6ull * i;
+        out[0] = top; out[1] = effective; out[2] = bx0; out[3] = by0; out[4] = bx1; out[5] = by1;
+    }
+}
+
 extern "C" {
 
 int bpo_world_create(const bp_world_desc* desc, const bp_world_input* input, int precision, void** out) {
@@ -1466,6 +1576,15 @@ uint32_t bpo_world_rigid_keys(void* handle, uint64_t* out, uint32_t capacity) {
     std::vector<uint64_t> keys = h->precision == 64 ? rigid_keys(*(World<double>*)h->world) : rigid_keys(*(World<float>*)h->world);
     for (uint32_t i = 0; i < keys.size() && i < capacity; ++i) out[i] = keys[i];
     return (uint32_t)keys.size();
+}
+
+// Contours of a float world's published state (see world_contours); returns BP_E_INVALID for a double world.
+int bpo_world_contours(void* handle, float max_edge, float tension, float clearance, uint32_t stride, float* points,
+                       uint32_t* counts, float* level, float* shape) {
+    Handle* h = (Handle*)handle;
+    if (h->precision == 64) return BP_E_INVALID;
+    world_contours(*(World<float>*)h->world, max_edge, tension, clearance, stride, points, counts, level, shape);
+    return BP_OK;
 }
 
 int bpo_set_threads(int threads) {

@@ -48,6 +48,7 @@ def library() -> C.CDLL:
             "bpo_world_read_candidates": (C.c_int, [P, P, C.c_uint32, C.POINTER(C.c_uint32)]),
             "bpo_world_read_cells": (C.c_int, [P, P, C.c_uint32, C.POINTER(C.c_uint32)]),
             "bpo_world_rigid_keys": (C.c_uint32, [P, P, C.c_uint32]),
+            "bpo_world_contours": (C.c_int, [P, C.c_float, C.c_float, C.c_float, C.c_uint32, P, P, P, P]),
             "bpo_world_read_substeps": (C.c_int, [P, P, C.c_uint32, C.POINTER(C.c_uint32)]),
             "bpo_contact_law": (C.c_int, [C.c_uint32, C.c_int, P, P, C.c_uint32]),
         }
@@ -123,6 +124,23 @@ class OracleWorld:
 
     def substeps(self) -> np.ndarray:
         return self._read(self.lib.bpo_world_read_substeps, np.float64)
+
+    def contours(self, max_edge=8.0, surface_tension=20.0, clearance=1e-4, stride=0):
+        """Contours of the published state (the CUDA path's contour passes restated in float): points (n, stride, 2),
+        counts (n,), level (n, stride), shape (n, 6)."""
+        radii = self.bubbles()["radius"]
+        need = max([64] + [int(np.ceil(np.float32(r) / np.float32(max_edge) * np.float32(4.0 * np.float32(np.pi))))
+                           for r in radii])
+        stride = stride or need
+        points = np.zeros((self.n, stride, 2), np.float32)
+        counts = np.zeros(self.n, np.uint32)
+        level = np.zeros((self.n, stride), np.float32)
+        shape = np.zeros((self.n, 6), np.float32)
+        st = self.lib.bpo_world_contours(self.handle, max_edge, surface_tension, clearance, stride,
+                                         C.c_void_p(points.ctypes.data), C.c_void_p(counts.ctypes.data),
+                                         C.c_void_p(level.ctypes.data), C.c_void_p(shape.ctypes.data))
+        assert st == 0, st
+        return points, counts, level, shape
 
     def rigid_keys(self) -> np.ndarray:
         """Sorted LBVH keys of the rigid leaves for the last step (the CUDA path's key rule restated in float)."""
