@@ -195,6 +195,8 @@ int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc
     ws.hBubbles.resize(nb);
     ws.hSegIds.resize(ns);
     ws.hBodyIds.resize(nbo);
+    ws.hBodyLayers.resize(nbo);
+    ws.hSegLayers.resize(ns);
     uint64_t otree = 0;
     uint64_t ob = 0, orow = 0, obrow = 0, ocon = 0, os = 0, obo = 0, obv = 0, obt = 0, of = 0, ofv = 0, ofi = 0, oband = 0,
              omotor = 0, ojr = 0, ojp = 0;
@@ -251,6 +253,7 @@ int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc
             sg.flags = r.flags; sg.cat = r.category; sg.mask = r.mask;
             sg.id = r.id; sg.owner = r.owner_id;
             ws.hSegIds[os + j] = r.id;
+            ws.hSegLayers[os + j] = r.layer;
         }
         for (uint32_t v = 0; v < in.body_vertex_count; ++v)
             bverts[obv + v] = make_float2(in.body_vertices[2 * v], in.body_vertices[2 * v + 1]);
@@ -279,6 +282,7 @@ int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc
             }
             B.pad = hull + r.core_radius;
             ws.hBodyIds[obo + b] = r.id;
+            ws.hBodyLayers[obo + b] = r.layer;
         }
         for (uint32_t v = 0; v < in.field_vertex_count; ++v)
             fverts[ofv + v] = make_float2(in.field_vertices[2 * v], in.field_vertices[2 * v + 1]);
@@ -997,6 +1001,55 @@ int bp_world_contours(bp_world* world, const bp_contour_config* config, float* p
     for (void* p : {(void*)dPoints, (void*)dCounts, (void*)dLevel, (void*)dShape})
         if (p) cudaFreeAsync(p, st);
     cudaError_t fin = cudaStreamSynchronize(st);
+    return cuda_status(err ? err : fin);
+}
+
+int bp_world_hit_test(bp_world* world, const bp_contour_config* config, const float* points_xy, uint32_t count,
+                      int64_t* ids, uint32_t* layers, uint32_t* found) {
+    if (!world || !config || (count && (!points_xy || !ids || !layers || !found))) return BP_E_INVALID;
+    uint32_t stride = 0;
+    int st = bp_world_contours(world, config, nullptr, nullptr, nullptr, nullptr, &stride, nullptr);
+    if (st) return st;
+    if (count == 0u) return BP_OK;
+    WorldSet& ws = world->set;
+    const DWorld& W = ws.hWorlds[0];
+    DeviceGuard guard(ws.ctx->device);
+    cudaStream_t st0 = ws.ctx->stream;
+    const uint64_t samples = (uint64_t)std::max(W.n, 1u) * stride;
+    std::vector<uint32_t> bubbleLayers(std::max(W.n, 1u));
+    for (uint32_t i = 0; i < W.n; ++i) bubbleLayers[i] = ws.hBubbles[W.boff + i].layer;
+    float2 *dPoints = nullptr, *dQueries = nullptr;
+    uint32_t *dCounts = nullptr, *dBubbleLayers = nullptr, *dSegLayers = nullptr, *dBodyLayers = nullptr;
+    uint32_t *dLayers = nullptr, *dFound = nullptr;
+    float *dLevel = nullptr, *dShape = nullptr;
+    long long* dIds = nullptr;
+    cudaError_t err = cudaMallocAsync(&dPoints, samples * sizeof(float2), st0);
+    if (!err) err = cudaMallocAsync(&dCounts, std::max(W.n, 1u) * sizeof(uint32_t), st0);
+    if (!err) err = cudaMallocAsync(&dLevel, samples * sizeof(float), st0);
+    if (!err) err = cudaMallocAsync(&dShape, std::max(W.n, 1u) * 6ull * sizeof(float), st0);
+    if (!err) err = cudaMallocAsync(&dQueries, count * sizeof(float2), st0);
+    if (!err) err = cudaMallocAsync(&dBubbleLayers, bubbleLayers.size() * sizeof(uint32_t), st0);
+    if (!err) err = cudaMallocAsync(&dSegLayers, std::max(W.s, 1u) * sizeof(uint32_t), st0);
+    if (!err) err = cudaMallocAsync(&dBodyLayers, std::max(W.nb, 1u) * sizeof(uint32_t), st0);
+    if (!err) err = cudaMallocAsync(&dIds, count * sizeof(long long), st0);
+    if (!err) err = cudaMallocAsync(&dLayers, count * sizeof(uint32_t), st0);
+    if (!err) err = cudaMallocAsync(&dFound, count * sizeof(uint32_t), st0);
+    if (!err) err = upload(dQueries, (const float2*)points_xy, count, st0);
+    if (!err) err = upload(dBubbleLayers, bubbleLayers.data(), W.n, st0);
+    if (!err) err = upload(dSegLayers, ws.hSegLayers.data() + W.soff, W.s, st0);
+    if (!err) err = upload(dBodyLayers, ws.hBodyLayers.data() + W.bodyOff, W.nb, st0);
+    if (!err) err = launch_contours(ws.S, W, config->max_edge, config->surface_tension, config->clearance, stride, dPoints,
+                                    dCounts, dLevel, dShape, st0);
+    if (!err) err = launch_hit_test(ws.S, W, dQueries, count, dPoints, dCounts, dShape, stride, dBubbleLayers, dSegLayers,
+                                    dBodyLayers, dIds, dLayers, dFound, st0);
+    if (!err) err = cudaMemcpyAsync(ids, dIds, count * sizeof(long long), cudaMemcpyDeviceToHost, st0);
+    if (!err) err = cudaMemcpyAsync(layers, dLayers, count * sizeof(uint32_t), cudaMemcpyDeviceToHost, st0);
+    if (!err) err = cudaMemcpyAsync(found, dFound, count * sizeof(uint32_t), cudaMemcpyDeviceToHost, st0);
+    if (!err) err = cudaStreamSynchronize(st0);
+    for (void* p : {(void*)dPoints, (void*)dCounts, (void*)dLevel, (void*)dShape, (void*)dQueries, (void*)dBubbleLayers,
+                    (void*)dSegLayers, (void*)dBodyLayers, (void*)dIds, (void*)dLayers, (void*)dFound})
+        if (p) cudaFreeAsync(p, st0);
+    cudaError_t fin = cudaStreamSynchronize(st0);
     return cuda_status(err ? err : fin);
 }
 

@@ -165,6 +165,76 @@ __global__ void __launch_bounds__(1024) contour_kernel(DState S, DWorld W, Conto
     }
 }
 
+// Hit test of query points (nativeHitTest, NativeGeometryKernels:501-541): among the bubbles whose contour contains the
+// point (bounds first, then the even-odd rule over the contour, the reference's crossing formula), the bodies that
+// contain it, and the static polygons that contain it (their one-sided edges, consecutive per owner), the highest
+// (layer, id as an unsigned 64-bit value) wins.
+__global__ void hit_test_kernel(DState S, DWorld W, const float2* queries, uint32_t queryCount, const float2* cpoints,
+                                const uint32_t* ccounts, const float* shape, uint32_t stride,
+                                const uint32_t* bubbleLayers, const uint32_t* segLayers, const uint32_t* bodyLayers,
+                                long long* ids, uint32_t* layers, uint32_t* found) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= queryCount) return;
+    const float2 query = queries[q];
+    bool any = false;
+    uint32_t bestLayer = 0;
+    unsigned long long bestId = 0;
+    auto offer = [&](uint32_t layer, long long id) {
+        const unsigned long long u = (unsigned long long)id;
+        if (!any || layer > bestLayer || (layer == bestLayer && u > bestId)) { any = true; bestLayer = layer; bestId = u; }
+    };
+    for (uint32_t i = 0; i < W.n; ++i) {
+        const uint32_t g = W.boff + i;
+        if (S.flags[g] & kRemoved) continue;
+        const float* box = shape + (uint64_t)i * 6u;
+        if (query.x < box[2] || query.y < box[3] || query.x > box[4] || query.y > box[5]) continue;
+        const uint32_t count = min(ccounts[i], stride);
+        if (count < 3u) continue;
+        bool inside = false;
+        const float2* ring = cpoints + (uint64_t)i * stride;
+        for (uint32_t k = 0, j = count - 1u; k < count; j = k++) {
+            const float2 a = ring[k], b = ring[j];
+            const bool crosses = ((a.y > query.y) != (b.y > query.y)) &&
+                                 (query.x <= (b.x - a.x) * (query.y - a.y) / (b.y - a.y) + a.x);
+            inside = crosses ? !inside : inside;
+        }
+        if (inside) offer(bubbleLayers[i], S.id[g]);
+    }
+    for (uint32_t bi = 0; bi < W.nb; ++bi) {
+        const DBody& b = S.body[W.bodyOff + bi];
+        if (rigid_inside(S.bverts, S.btris, query, b, body_at(b, 1.0f))) offer(bodyLayers[bi], b.id);
+    }
+    // static polygons: even-odd over each owner's run of polygon edges
+    bool inside = false;
+    for (uint32_t j = 0; j < W.s; ++j) {
+        const DSegment& sg = S.seg[W.soff + j];
+        if ((sg.flags & (BP_SEGMENT_POLYGON_EDGE | BP_SEGMENT_HAS_OWNER)) != (BP_SEGMENT_POLYGON_EDGE | BP_SEGMENT_HAS_OWNER))
+            continue;
+        const float2 a = sg.b, b = sg.a;
+        if (((a.y > query.y) != (b.y > query.y)) && (query.x <= (b.x - a.x) * (query.y - a.y) / (b.y - a.y) + a.x))
+            inside = !inside;
+        const bool last = j + 1u == W.s || S.seg[W.soff + j + 1u].owner != sg.owner;
+        if (last) {
+            if (inside) offer(segLayers[j], sg.owner);
+            inside = false;
+        }
+    }
+    ids[q] = (long long)bestId;
+    layers[q] = bestLayer;
+    found[q] = any ? 1u : 0u;
+}
+
+cudaError_t launch_hit_test(const DState& S, const DWorld& W, const float2* queries, uint32_t queryCount,
+                            const float2* cpoints, const uint32_t* ccounts, const float* shape, uint32_t stride,
+                            const uint32_t* bubbleLayers, const uint32_t* segLayers, const uint32_t* bodyLayers,
+                            long long* ids, uint32_t* layers, uint32_t* found, cudaStream_t stream) {
+    if (queryCount == 0u) return cudaSuccess;
+    hit_test_kernel<<<(queryCount + 127u) / 128u, 128, 0, stream>>>(S, W, queries, queryCount, cpoints, ccounts, shape,
+                                                                    stride, bubbleLayers, segLayers, bodyLayers, ids,
+                                                                    layers, found);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_contours(const DState& S, const DWorld& W, float maxEdge, float tension, float clearance,
                             uint32_t stride, float2* points, uint32_t* counts, float* level, float* shape,
                             cudaStream_t stream) {

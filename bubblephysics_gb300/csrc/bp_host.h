@@ -27,6 +27,10 @@ void prepare_kernels();
 cudaError_t launch_served(const DState* sets, const uint32_t* entrySlot, bp_step_report* reports, const QueueArgs& q,
                           uint32_t threads, uint32_t blocks, cudaStream_t stream);
 cudaError_t launch_sum(const uint32_t* v, uint64_t n, unsigned long long* total, cudaStream_t stream);
+cudaError_t launch_hit_test(const DState& S, const DWorld& W, const float2* queries, uint32_t queryCount,
+                            const float2* cpoints, const uint32_t* ccounts, const float* shape, uint32_t stride,
+                            const uint32_t* bubbleLayers, const uint32_t* segLayers, const uint32_t* bodyLayers,
+                            long long* ids, uint32_t* layers, uint32_t* found, cudaStream_t stream);
 cudaError_t launch_contours(const DState& S, const DWorld& W, float maxEdge, float tension, float clearance,
                             uint32_t stride, float2* points, uint32_t* counts, float* level, float* shape,
                             cudaStream_t stream);
@@ -95,6 +99,7 @@ struct WorldSet {
     std::vector<DWorld> hWorlds;
     std::vector<bp_bubble> hBubbles;        // as uploaded (static fields for readback)
     std::vector<int64_t> hSegIds, hBodyIds;
+    std::vector<uint32_t> hSegLayers, hBodyLayers;  // drawing layers (hit tests)
     uint64_t totalBubbles = 0, totalRows = 0, totalBodyRows = 0, totalContacts = 0;
     uint32_t totalSegments = 0, totalBodies = 0;
     uint64_t totalTreeLeaves = 0;

@@ -147,6 +147,18 @@ class World:
                                            C.c_void_p(shape.ctypes.data), C.byref(used), C.byref(ms)), "bp_world_contours")
         return points, counts, level, shape, ms.value
 
+    def hit_test(self, points, max_edge: float = 8.0, surface_tension: float = 20.0, clearance: float = 1e-4):
+        """Hit test of query points on the published state (bp_world_hit_test): ids, layers, found."""
+        q = np.ascontiguousarray(points, np.float32).reshape(-1, 2)
+        ids = np.zeros(q.shape[0], np.int64)
+        layers = np.zeros(q.shape[0], np.uint32)
+        found = np.zeros(q.shape[0], np.uint32)
+        cfg = N.ContourConfig(max_edge, surface_tension, clearance, 0)
+        N.check(self.lib.bp_world_hit_test(self.handle, C.byref(cfg), C.c_void_p(q.ctypes.data), q.shape[0],
+                                           C.c_void_p(ids.ctypes.data), C.c_void_p(layers.ctypes.data),
+                                           C.c_void_p(found.ctypes.data)), "bp_world_hit_test")
+        return ids, layers, found
+
     def rigid_keys(self) -> np.ndarray:
         """Sorted LBVH keys (Morton code << 32 | leaf) of the last step; empty when the step used no tree."""
         return self._read(self.lib.bp_world_read_rigid_keys, np.uint64, "bp_world_read_rigid_keys")

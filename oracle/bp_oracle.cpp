@@ -135,7 +135,7 @@ template <typename T> struct Body {
     T omega;
     T radius;                 // bounding radius (physical.z)
     T coreRadius;
-    uint32_t kind, flags, voff, vcount, toff, tcount, cat, mask;
+    uint32_t kind, flags, voff, vcount, toff, tcount, cat, mask, layer;
     T cosPrev, sinPrev, cosEnd, sinEnd;  // host-computed rotation of both poses (same in the CUDA path)
 };
 
@@ -162,7 +162,7 @@ template <typename T> struct World {
     std::vector<int64_t> id;
     std::vector<V2<T>> pos, start, vel, acc, a0, ref, force;
     std::vector<T> rot, omega, mass, invMass, radius, K, gamma, margin;
-    std::vector<uint32_t> flags_, cat, mask, result;
+    std::vector<uint32_t> flags_, cat, mask, result, layer;
 
     // published copy (a failed step publishes nothing)
     std::vector<V2<T>> pPos, pStart, pVel;
@@ -174,7 +174,7 @@ template <typename T> struct World {
     std::vector<int64_t> sid, sowner;
     std::vector<V2<T>> sa, sb, sprev;
     std::vector<T> soutward, sallowed;
-    std::vector<uint32_t> sflags, scat, smask;
+    std::vector<uint32_t> sflags, scat, smask, slayer;
 
     // bodies
     std::vector<Body<T>> bodies;
@@ -1195,7 +1195,7 @@ template <typename T> World<T>* create(const bp_world_desc* d, const bp_world_in
     resize(w->id); resize(w->pos); resize(w->start); resize(w->vel); resize(w->acc); resize(w->a0); resize(w->ref);
     resize(w->force); resize(w->rot); resize(w->omega); resize(w->mass); resize(w->invMass); resize(w->radius);
     resize(w->K); resize(w->gamma); resize(w->margin); resize(w->flags_); resize(w->cat); resize(w->mask);
-    resize(w->result); resize(w->cellX); resize(w->cellY); resize(w->cellValid); resize(w->rowPairs);
+    resize(w->result); resize(w->layer); resize(w->cellX); resize(w->cellY); resize(w->cellValid); resize(w->rowPairs);
     resize(w->rowSegs); resize(w->adj);
     for (uint32_t i = 0; i < n; ++i) {
         const bp_bubble& b = in->bubbles[i];
@@ -1215,11 +1215,13 @@ template <typename T> World<T>* create(const bp_world_desc* d, const bp_world_in
         w->cat[i] = b.category;
         w->mask[i] = b.mask;
         w->result[i] = 0;
+        w->layer[i] = b.layer;
     }
     w->s = in->segment_count;
     const uint32_t s = w->s;
     w->sid.resize(s); w->sowner.resize(s); w->sa.resize(s); w->sb.resize(s); w->sprev.resize(s);
     w->soutward.resize(s); w->sallowed.resize(s); w->sflags.resize(s); w->scat.resize(s); w->smask.resize(s);
+    w->slayer.resize(s);
     for (uint32_t j = 0; j < s; ++j) {
         const bp_segment& g = in->segments[j];
         w->sid[j] = g.id;
@@ -1232,6 +1234,7 @@ template <typename T> World<T>* create(const bp_world_desc* d, const bp_world_in
         w->sflags[j] = g.flags;
         w->scat[j] = g.category;
         w->smask[j] = g.mask;
+        w->slayer[j] = g.layer;
     }
     w->bverts.resize(in->body_vertex_count);
     for (uint32_t v = 0; v < in->body_vertex_count; ++v)
@@ -1257,6 +1260,7 @@ template <typename T> World<T>* create(const bp_world_desc* d, const bp_world_in
         body.tcount = r.triangle_count;
         body.cat = r.category;
         body.mask = r.mask;
+        body.layer = r.layer;
         body.cosEnd = std::cos((T)r.angle);
         body.sinEnd = std::sin((T)r.angle);
         body.cosPrev = body.cosEnd;
@@ -1512,6 +1516,60 @@ static void world_contours(const World<float>& w, float maxEdge, float tension, 
     }
 }
 
+// Hit test (nativeHitTest, NativeGeometryKernels:501-541) over the contours of world_contours, the bodies at their
+// end-of-step pose and the static polygons (even-odd over each owner's consecutive polygon edges): the highest
+// (layer, id as uint64) wins.
+static void world_hit_test(const World<float>& w, float maxEdge, float tension, float clearance, const float* queries,
+                           uint32_t count, int64_t* ids, uint32_t* layers, uint32_t* found) {
+    uint32_t stride = 64;
+    for (uint32_t i = 0; i < w.n; ++i) stride = std::max(stride, contour_samples(w.radius[i], maxEdge, 0xffffffffu));
+    std::vector<float> points(2ull * w.n * stride), level((size_t)w.n * stride), shape(6ull * w.n);
+    std::vector<uint32_t> counts(w.n);
+    world_contours(w, maxEdge, tension, clearance, stride, points.data(), counts.data(), level.data(), shape.data());
+    for (uint32_t q = 0; q < count; ++q) {
+        const float qx = queries[2 * q], qy = queries[2 * q + 1];
+        bool any = false;
+        uint32_t bestLayer = 0;
+        uint64_t bestId = 0;
+        auto offer = [&](uint32_t layer, int64_t id) {
+            uint64_t u = (uint64_t)id;
+            if (!any || layer > bestLayer || (layer == bestLayer && u > bestId)) { any = true; bestLayer = layer; bestId = u; }
+        };
+        for (uint32_t i = 0; i < w.n; ++i) {
+            if (is_removed(w, i)) continue;
+            const float* box = &shape[6ull * i];
+            if (qx < box[2] || qy < box[3] || qx > box[4] || qy > box[5]) continue;
+            uint32_t c = std::min(counts[i], stride);
+            if (c < 3) continue;
+            bool inside = false;
+            const float* ring = &points[2ull * i * stride];
+            for (uint32_t k = 0, j = c - 1; k < c; j = k++) {
+                float ax = ring[2 * k], ay = ring[2 * k + 1], bx = ring[2 * j], by = ring[2 * j + 1];
+                bool crosses = ((ay > qy) != (by > qy)) && (qx <= (bx - ax) * (qy - ay) / (by - ay) + ax);
+                inside = crosses ? !inside : inside;
+            }
+            if (inside) offer(w.layer[i], w.id[i]);
+        }
+        for (const Body<float>& b : w.bodies)
+            if (rigid_inside(w, mk<float>(qx, qy), b, body_at(b, 1.0f))) offer(b.layer, b.id);
+        bool inside = false;
+        const uint32_t edge = BP_SEGMENT_POLYGON_EDGE | BP_SEGMENT_HAS_OWNER;
+        for (uint32_t j = 0; j < w.s; ++j) {
+            if ((w.sflags[j] & edge) != edge) continue;
+            float ax = w.sb[j].x, ay = w.sb[j].y, bx = w.sa[j].x, by = w.sa[j].y;
+            if (((ay > qy) != (by > qy)) && (qx <= (bx - ax) * (qy - ay) / (by - ay) + ax)) inside = !inside;
+            bool last = j + 1 == w.s || w.sowner[j + 1] != w.sowner[j];
+            if (last) {
+                if (inside) offer(w.slayer[j], w.sowner[j]);
+                inside = false;
+            }
+        }
+        ids[q] = (int64_t)bestId;
+        layers[q] = bestLayer;
+        found[q] = any ? 1u : 0u;
+    }
+}
+
 extern "C" {
 
 int bpo_world_create(const bp_world_desc* desc, const bp_world_input* input, int precision, void** out) {
@@ -1584,6 +1642,14 @@ int bpo_world_contours(void* handle, float max_edge, float tension, float cleara
     Handle* h = (Handle*)handle;
     if (h->precision == 64) return BP_E_INVALID;
     world_contours(*(World<float>*)h->world, max_edge, tension, clearance, stride, points, counts, level, shape);
+    return BP_OK;
+}
+
+int bpo_world_hit_test(void* handle, float max_edge, float tension, float clearance, const float* queries,
+                       uint32_t count, int64_t* ids, uint32_t* layers, uint32_t* found) {
+    Handle* h = (Handle*)handle;
+    if (h->precision == 64) return BP_E_INVALID;
+    world_hit_test(*(World<float>*)h->world, max_edge, tension, clearance, queries, count, ids, layers, found);
     return BP_OK;
 }
 

@@ -49,6 +49,7 @@ def library() -> C.CDLL:
             "bpo_world_read_cells": (C.c_int, [P, P, C.c_uint32, C.POINTER(C.c_uint32)]),
             "bpo_world_rigid_keys": (C.c_uint32, [P, P, C.c_uint32]),
             "bpo_world_contours": (C.c_int, [P, C.c_float, C.c_float, C.c_float, C.c_uint32, P, P, P, P]),
+            "bpo_world_hit_test": (C.c_int, [P, C.c_float, C.c_float, C.c_float, P, C.c_uint32, P, P, P]),
             "bpo_world_read_substeps": (C.c_int, [P, P, C.c_uint32, C.POINTER(C.c_uint32)]),
             "bpo_contact_law": (C.c_int, [C.c_uint32, C.c_int, P, P, C.c_uint32]),
         }
@@ -141,6 +142,18 @@ class OracleWorld:
                                          C.c_void_p(level.ctypes.data), C.c_void_p(shape.ctypes.data))
         assert st == 0, st
         return points, counts, level, shape
+
+    def hit_test(self, points, max_edge=8.0, surface_tension=20.0, clearance=1e-4):
+        """Hit test of query points (the CUDA path's rule restated in float): ids, layers, found."""
+        q = np.ascontiguousarray(points, np.float32).reshape(-1, 2)
+        ids = np.zeros(q.shape[0], np.int64)
+        layers = np.zeros(q.shape[0], np.uint32)
+        found = np.zeros(q.shape[0], np.uint32)
+        st = self.lib.bpo_world_hit_test(self.handle, max_edge, surface_tension, clearance, C.c_void_p(q.ctypes.data),
+                                         q.shape[0], C.c_void_p(ids.ctypes.data), C.c_void_p(layers.ctypes.data),
+                                         C.c_void_p(found.ctypes.data))
+        assert st == 0, st
+        return ids, layers, found
 
     def rigid_keys(self) -> np.ndarray:
         """Sorted LBVH keys of the rigid leaves for the last step (the CUDA path's key rule restated in float)."""
