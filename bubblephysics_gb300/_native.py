@@ -132,6 +132,14 @@ class ContourConfig(C.Structure):
                 ("stride", C.c_uint32)]
 
 
+class Sensor(C.Structure):
+    _fields_ = [("id", C.c_int64), ("position", f2), ("angle", C.c_float), ("radius", C.c_float),
+                ("vertex_offset", C.c_uint32), ("vertex_count", C.c_uint32), ("flags", C.c_uint32),
+                ("category", C.c_uint32), ("mask", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+SENSOR_ENTER_EVENTS, SENSOR_EXIT_EVENTS = 1, 2
+
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_worlds", C.c_uint32), ("max_batch_worlds", C.c_uint32),
                 ("streams", C.c_uint32), ("threads_per_world", C.c_uint32), ("warp_world_max", C.c_uint32),
@@ -153,7 +161,7 @@ class ServerStats(C.Structure):
 
 SERVER_PER_WORLD = 1
 
-RECORD_SIZES = {ContourConfig: 16, ServerConfig: 32, ServerCompletion: 136, ServerStats: 80, Bubble: 80, Segment: 64, Body: 80, ForceField: 64, Band: 24, Motor: 24, WorldDesc: 64,
+RECORD_SIZES = {Sensor: 48, ContourConfig: 16, ServerConfig: 32, ServerCompletion: 136, ServerStats: 80, Bubble: 80, Segment: 64, Body: 80, ForceField: 64, Band: 24, Motor: 24, WorldDesc: 64,
                 StepReport: 96, Contact: 64, CandidateKey: 24}
 for _t, _n in RECORD_SIZES.items():
     assert C.sizeof(_t) == _n, f"{_t.__name__} is {C.sizeof(_t)} bytes, the C ABI says {_n}"
@@ -181,6 +189,9 @@ CONTACT_DTYPE = np.dtype({"names": ["participants", "kind", "feature", "normal",
                           "formats": [("<i8", 2), "<u4", "<u4", ("<f4", 2), ("<f4", 2), "<f4", "<f4", "<f4",
                                       ("<u4", 3)],
                           "offsets": [0, 16, 20, 24, 32, 40, 44, 48, 52], "itemsize": 64})
+SENSOR_EVENT_DTYPE = np.dtype({"names": ["sensor", "object", "kind", "point", "reserved"],
+                               "formats": ["<i8", "<i8", "<u4", ("<f4", 2), "<u4"],
+                               "offsets": [0, 8, 16, 20, 28], "itemsize": 32})
 KEY_DTYPE = np.dtype({"names": ["kind", "reserved", "first", "second"], "formats": ["<u4", "<u4", "<i8", "<i8"],
                       "offsets": [0, 4, 8, 16], "itemsize": 24})
 REPORT_DTYPE = np.dtype({"names": [n for n, _ in StepReport._fields_],
@@ -237,6 +248,8 @@ _SIGNATURES = {
     "bp_world_contours": (C.c_int, [_P, C.POINTER(ContourConfig), _P, _P, _P, _P, C.POINTER(C.c_uint32),
                                     C.POINTER(C.c_float)]),
     "bp_world_hit_test": (C.c_int, [_P, C.POINTER(ContourConfig), _P, C.c_uint32, _P, _P, _P]),
+    "bp_world_set_sensors": (C.c_int, [_P, _P, C.c_uint32, _P, C.c_uint32]),
+    "bp_world_read_sensor_events": (C.c_int, [_P, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
     "bp_server_create": (C.c_int, [_P, C.POINTER(ServerConfig), C.POINTER(_P)]),
     "bp_server_destroy": (C.c_int, [_P]),
     "bp_server_add_world": (C.c_int, [_P, C.POINTER(WorldDesc), C.POINTER(WorldInput), C.POINTER(C.c_uint32)]),

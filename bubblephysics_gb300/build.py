@@ -17,7 +17,7 @@ PACKAGE_DIR = Path(__file__).resolve().parent
 CSRC = PACKAGE_DIR / "csrc"
 BUILD_DIR = PACKAGE_DIR / "_build"
 LIBRARY = PACKAGE_DIR / "libbubblephysics_gb300.so"
-SOURCES = ["bp_step.cu", "bp_capi.cu", "bp_aux.cu", "bp_server.cu", "bp_contour.cu"]
+SOURCES = ["bp_step.cu", "bp_capi.cu", "bp_aux.cu", "bp_server.cu", "bp_contour.cu", "bp_sensor.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
               "-Xcompiler", "-fPIC,-ffp-contract=off", "-diag-suppress", "177"]

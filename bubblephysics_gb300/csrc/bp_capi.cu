@@ -31,6 +31,8 @@ static_assert(sizeof(bp_world_desc) == 64, "bp_world_desc layout");
 static_assert(sizeof(bp_step_report) == 96, "bp_step_report layout");
 static_assert(sizeof(bp_contact) == 64, "bp_contact layout");
 static_assert(sizeof(bp_candidate_key) == 24, "bp_candidate_key layout");
+static_assert(sizeof(bp_sensor) == 48 && sizeof(bp_sensor_event) == 32, "sensor record layouts");
+static_assert(sizeof(bp_contour_config) == 16, "bp_contour_config layout");
 static_assert(offsetof(bp_bubble, center) == 8 && offsetof(bp_bubble, flags) == 60, "bp_bubble offsets");
 static_assert(offsetof(bp_step_report, limiter_object) == 40, "bp_step_report offsets");
 
@@ -856,6 +858,11 @@ int bp_world_step(bp_world* world, uint32_t steps, bp_step_report* reports) {
             return BP_E_TIMEOUT;
         }
         ws.bubbleSubsteps += (uint64_t)out[s].substep_count * ws.hWorlds[0].n;
+        if (ws.sensorCount && out[s].status == BP_OK) {
+            err = launch_sensors(ws.S, ws.hWorlds[0], ws.dSensors, ws.sensorCount, ws.dSensorVerts, ws.dSensorState,
+                                 ws.dSensorKinds, ws.dSensorEvents, ws.sensorEventCapacity, ws.dSensorCount, st);
+            if (err) return cuda_status(err);
+        }
         status = out[s].status;
         if (status != BP_OK) break;
     }
@@ -1051,6 +1058,68 @@ int bp_world_hit_test(bp_world* world, const bp_contour_config* config, const fl
         if (p) cudaFreeAsync(p, st0);
     cudaError_t fin = cudaStreamSynchronize(st0);
     return cuda_status(err ? err : fin);
+}
+
+int bp_world_set_sensors(bp_world* world, const bp_sensor* sensors, uint32_t count, const float* vertices_xy,
+                         uint32_t vertex_count) {
+    if (!world || (count && !sensors) || (vertex_count && !vertices_xy)) return BP_E_INVALID;
+    for (uint32_t k = 0; k < count; ++k) {
+        const bp_sensor& r = sensors[k];
+        if ((uint64_t)r.vertex_offset + r.vertex_count > vertex_count || r.vertex_count == 1u || r.vertex_count == 2u ||
+            !std::isfinite(r.position[0]) || !std::isfinite(r.position[1]) || !std::isfinite(r.angle) ||
+            !(r.radius >= 0.0f))
+            return BP_E_INVALID;
+    }
+    WorldSet& ws = world->set;
+    DeviceGuard guard(ws.ctx->device);
+    cudaStream_t st = ws.ctx->stream;
+    cudaError_t err = cudaStreamSynchronize(st);
+    for (void* p : ws.sensorAllocations) cudaFree(p);
+    ws.sensorAllocations.clear();
+    ws.sensorCount = 0;
+    if (err) return cuda_status(err);
+    const uint64_t pairs = (uint64_t)count * std::max(ws.hWorlds[0].n, 1u);
+    if (pairs > 0xffffffffull) return BP_E_CAPACITY;
+    auto take = [&](size_t bytes) -> void* {
+        void* p = nullptr;
+        if (err == cudaSuccess) err = cudaMalloc(&p, std::max<size_t>(bytes, 16));
+        if (err == cudaSuccess) { ws.sensorAllocations.push_back(p); err = cudaMemsetAsync(p, 0, std::max<size_t>(bytes, 16), st); }
+        return p;
+    };
+    ws.dSensors = take(count * sensor_record_bytes());
+    ws.dSensorVerts = (float2*)take(vertex_count * sizeof(float2));
+    ws.dSensorState = (uint8_t*)take(pairs);
+    ws.dSensorKinds = (uint8_t*)take(pairs);
+    ws.dSensorEvents = (bp_sensor_event*)take(pairs * sizeof(bp_sensor_event));
+    ws.dSensorCount = (uint32_t*)take(sizeof(uint32_t));
+    if (err) return cuda_status(err);
+    std::vector<unsigned char> records(count * sensor_record_bytes());
+    for (uint32_t k = 0; k < count; ++k) sensor_to_device(sensors[k], records.data() + k * sensor_record_bytes());
+    if (count) err = cudaMemcpyAsync(ws.dSensors, records.data(), records.size(), cudaMemcpyHostToDevice, st);
+    if (!err && vertex_count) err = cudaMemcpyAsync(ws.dSensorVerts, vertices_xy, vertex_count * sizeof(float2), cudaMemcpyHostToDevice, st);
+    if (!err) err = cudaStreamSynchronize(st);
+    if (err) return cuda_status(err);
+    ws.sensorCount = count;
+    ws.sensorEventCapacity = (uint32_t)pairs;
+    return BP_OK;
+}
+
+int bp_world_read_sensor_events(bp_world* world, bp_sensor_event* out, uint32_t capacity, uint32_t* count) {
+    if (!world) return BP_E_INVALID;
+    WorldSet& ws = world->set;
+    if (!ws.sensorCount) {
+        if (count) *count = 0;
+        return BP_OK;
+    }
+    DeviceGuard guard(ws.ctx->device);
+    uint32_t c = 0;
+    cudaError_t err = cudaStreamSynchronize(ws.ctx->stream);  // the last step's sensor kernels ran on it
+    if (!err) err = cudaMemcpy(&c, ws.dSensorCount, sizeof(c), cudaMemcpyDeviceToHost);
+    if (err) return cuda_status(err);
+    if (count) *count = c;
+    const uint32_t m = std::min(std::min(c, capacity), ws.sensorEventCapacity);
+    if (out && m) err = cudaMemcpy(out, ws.dSensorEvents, m * sizeof(bp_sensor_event), cudaMemcpyDeviceToHost);
+    return cuda_status(err);
 }
 
 int bp_world_read_substeps(bp_world* world, float* out, uint32_t capacity, uint32_t* count) {

@@ -31,6 +31,11 @@ cudaError_t launch_hit_test(const DState& S, const DWorld& W, const float2* quer
                             const float2* cpoints, const uint32_t* ccounts, const float* shape, uint32_t stride,
                             const uint32_t* bubbleLayers, const uint32_t* segLayers, const uint32_t* bodyLayers,
                             long long* ids, uint32_t* layers, uint32_t* found, cudaStream_t stream);
+cudaError_t launch_sensors(const DState& S, const DWorld& W, const void* sensors, uint32_t sensorCount,
+                           const float2* verts, uint8_t* state, uint8_t* kinds, bp_sensor_event* events,
+                           uint32_t capacity, uint32_t* count, cudaStream_t stream);
+size_t sensor_record_bytes();
+void sensor_to_device(const bp_sensor& in, void* out);
 cudaError_t launch_contours(const DState& S, const DWorld& W, float maxEdge, float tension, float clearance,
                             uint32_t stride, float2* points, uint32_t* counts, float* level, float* shape,
                             cudaStream_t stream);
@@ -134,6 +139,16 @@ struct WorldSet {
     uint64_t bubbleSubsteps = 0, launches = 0;
     std::vector<float> lastHistory;
 
+    // sensors of a single world (bp_world_set_sensors): device records, vertices, per-pair state and event kinds,
+    // the event list of the last step and its length
+    void* dSensors = nullptr;
+    float2* dSensorVerts = nullptr;
+    uint8_t* dSensorState = nullptr;
+    uint8_t* dSensorKinds = nullptr;
+    bp_sensor_event* dSensorEvents = nullptr;
+    uint32_t* dSensorCount = nullptr;
+    uint32_t sensorCount = 0, sensorEventCapacity = 0;
+    std::vector<void*> sensorAllocations;
     cudaMemPool_t pool = nullptr;           // stream-ordered pool (server worlds); null: plain cudaMalloc
     bool planOnly = false;                  // server worlds: built without the batch schedule
     bool measureOnly = false;               // count the device bytes of a build without allocating or uploading
@@ -141,6 +156,7 @@ struct WorldSet {
 
     ~WorldSet() {
         if (graph) cudaGraphExecDestroy(graph);
+        for (void* p : sensorAllocations) cudaFree(p);
         for (void* p : allocations) {
             if (pool) cudaFreeAsync(p, ctx->stream);
             else cudaFree(p);

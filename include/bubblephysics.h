@@ -376,6 +376,46 @@ int bp_world_contours(bp_world* world, const bp_contour_config* config, float* p
 int bp_world_hit_test(bp_world* world, const bp_contour_config* config, const float* points_xy, uint32_t count,
                       int64_t* ids, uint32_t* layers, uint32_t* found);
 
+/* ---- sensors (enter / exit events of bubbles) ------------------------------------------------------------------ */
+
+enum bp_sensor_flags {
+    BP_SENSOR_ENTER_EVENTS = 1u,     /* report bubbles that start overlapping (sensor flag bit 2 of the reference) */
+    BP_SENSOR_EXIT_EVENTS = 2u       /* report bubbles that stop overlapping (bit 3) */
+};
+
+/* A sensor (NativeSensorRecord, NativePostSolveKernels:586): a circle of `radius`, or a polygon of vertex_count local
+ * vertices from bp_world_set_sensors' vertex array, at `position` rotated by `angle`. 48 bytes. */
+typedef struct bp_sensor {
+    int64_t id;
+    float position[2];
+    float angle;
+    float radius;                    /* circle sensor (vertex_count 0) */
+    uint32_t vertex_offset;          /* polygon sensor: into the vertex array (float2 pairs) */
+    uint32_t vertex_count;
+    uint32_t flags;                  /* BP_SENSOR_* */
+    uint32_t category;               /* filter against the bubbles' filters */
+    uint32_t mask;
+    uint32_t reserved;
+} bp_sensor;
+
+/* One sensor event of the last step, in (sensor, bubble) order. 32 bytes. */
+typedef struct bp_sensor_event {
+    int64_t sensor;
+    int64_t object;                  /* bubble id */
+    uint32_t kind;                   /* 1 entered, 2 exited */
+    float point[2];                  /* bubble centre */
+    uint32_t reserved;
+} bp_sensor_event;
+
+/* Sets the world's sensors (replacing any earlier ones; overlaps start empty). Every later step compares each bubble
+ * against each sensor on the device (nativeCompactSensorEvents, NativePostSolveKernels:601-648: a circle bubble
+ * overlaps a circle sensor within the sum of the radii, a polygon sensor when its centre is inside or an edge is within
+ * its radius; removed bubbles overlap nothing) and lists the bubbles that entered or left. */
+int bp_world_set_sensors(bp_world* world, const bp_sensor* sensors, uint32_t count, const float* vertices_xy,
+                         uint32_t vertex_count);
+/* Sensor events of the last step; *count = all of them (capacity may be smaller). */
+int bp_world_read_sensor_events(bp_world* world, bp_sensor_event* out, uint32_t capacity, uint32_t* count);
+
 /* ---- serving loop (no counterpart in the reference) ------------------------------------------------------------ */
 
 /* A request loop over many worlds that stay resident on the device. The reference steps one world per call

@@ -1570,6 +1570,58 @@ static void world_hit_test(const World<float>& w, float maxEdge, float tension, 
     }
 }
 
+// Sensor events of the published state against the overlap state of the previous evaluation
+// (nativeCompactSensorEvents, NativePostSolveKernels:601-648), in (sensor, bubble) order; `state` (sensors x bubbles)
+// is updated in place. Returns the number of events (written up to `capacity`).
+static uint32_t world_sensor_events(const World<float>& w, const bp_sensor* sensors, uint32_t count, const float* verts,
+                                    uint8_t* state, bp_sensor_event* out, uint32_t capacity) {
+    uint32_t events = 0;
+    for (uint32_t si = 0; si < count; ++si) {
+        const bp_sensor& sn = sensors[si];
+        for (uint32_t i = 0; i < w.n; ++i) {
+            bool overlapping = false;
+            if (!is_removed(w, i) && filter_accepts(w.cat[i], w.mask[i], sn.category, sn.mask)) {
+                float dx = w.pPos[i].x - sn.position[0], dy = w.pPos[i].y - sn.position[1];
+                float c = std::cos(sn.angle), s = std::sin(sn.angle);
+                float lx = c * dx + s * dy, ly = -s * dx + c * dy;
+                float radius = w.radius[i];
+                if (sn.vertex_count == 0) {
+                    float reach = sn.radius + radius;
+                    overlapping = lx * lx + ly * ly <= reach * reach;
+                } else {
+                    bool inside = false;
+                    for (uint32_t j = 0; j < sn.vertex_count; ++j) {
+                        uint32_t ia = sn.vertex_offset + j, ib = sn.vertex_offset + (j + 1) % sn.vertex_count;
+                        float ax = verts[2 * ia], ay = verts[2 * ia + 1], bx = verts[2 * ib], by = verts[2 * ib + 1];
+                        if ((ay > ly) != (by > ly) && lx < (bx - ax) * (ly - ay) / (by - ay) + ax) inside = !inside;
+                        float abx = bx - ax, aby = by - ay;
+                        float t = std::fmin(std::fmax(((lx - ax) * abx + (ly - ay) * aby) / std::fmax(abx * abx + aby * aby, 1e-20f), 0.0f), 1.0f);
+                        float ex = lx - (ax + abx * t), ey = ly - (ay + aby * t);
+                        if (ex * ex + ey * ey <= radius * radius) overlapping = true;
+                    }
+                    overlapping = overlapping || inside;
+                }
+            }
+            uint8_t& was = state[(uint64_t)si * w.n + i];
+            uint32_t kind = overlapping && !was && (sn.flags & BP_SENSOR_ENTER_EVENTS) ? 1u
+                          : !overlapping && was && (sn.flags & BP_SENSOR_EXIT_EVENTS) ? 2u : 0u;
+            was = overlapping ? 1 : 0;
+            if (!kind) continue;
+            if (events < capacity) {
+                bp_sensor_event& e = out[events];
+                e.sensor = sn.id;
+                e.object = w.id[i];
+                e.kind = kind;
+                e.point[0] = w.pPos[i].x;
+                e.point[1] = w.pPos[i].y;
+                e.reserved = 0;
+            }
+            ++events;
+        }
+    }
+    return events;
+}
+
 extern "C" {
 
 int bpo_world_create(const bp_world_desc* desc, const bp_world_input* input, int precision, void** out) {
@@ -1651,6 +1703,13 @@ int bpo_world_hit_test(void* handle, float max_edge, float tension, float cleara
     if (h->precision == 64) return BP_E_INVALID;
     world_hit_test(*(World<float>*)h->world, max_edge, tension, clearance, queries, count, ids, layers, found);
     return BP_OK;
+}
+
+uint32_t bpo_world_sensor_events(void* handle, const bp_sensor* sensors, uint32_t count, const float* verts,
+                                 uint8_t* state, bp_sensor_event* out, uint32_t capacity) {
+    Handle* h = (Handle*)handle;
+    if (h->precision == 64) return 0;
+    return world_sensor_events(*(World<float>*)h->world, sensors, count, verts, state, out, capacity);
 }
 
 int bpo_set_threads(int threads) {
