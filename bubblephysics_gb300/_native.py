@@ -248,7 +248,7 @@ _SIGNATURES = {
     "bp_world_contours": (C.c_int, [_P, C.POINTER(ContourConfig), _P, _P, _P, _P, C.POINTER(C.c_uint32),
                                     C.POINTER(C.c_float)]),
     "bp_world_hit_test": (C.c_int, [_P, C.POINTER(ContourConfig), _P, C.c_uint32, _P, _P, _P]),
-    "bp_world_set_sensors": (C.c_int, [_P, _P, C.c_uint32, _P, C.c_uint32]),
+    "bp_world_set_sensors": (C.c_int, [_P, _P, C.c_uint32, _P, C.c_uint32, _P]),
     "bp_world_read_sensor_events": (C.c_int, [_P, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
     "bp_server_create": (C.c_int, [_P, C.POINTER(ServerConfig), C.POINTER(_P)]),
     "bp_server_destroy": (C.c_int, [_P]),

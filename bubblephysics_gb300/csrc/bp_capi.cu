@@ -1061,7 +1061,7 @@ int bp_world_hit_test(bp_world* world, const bp_contour_config* config, const fl
 }
 
 int bp_world_set_sensors(bp_world* world, const bp_sensor* sensors, uint32_t count, const float* vertices_xy,
-                         uint32_t vertex_count) {
+                         uint32_t vertex_count, const uint8_t* overlap_state) {
     if (!world || (count && !sensors) || (vertex_count && !vertices_xy)) return BP_E_INVALID;
     for (uint32_t k = 0; k < count; ++k) {
         const bp_sensor& r = sensors[k];
@@ -1097,6 +1097,8 @@ int bp_world_set_sensors(bp_world* world, const bp_sensor* sensors, uint32_t cou
     for (uint32_t k = 0; k < count; ++k) sensor_to_device(sensors[k], records.data() + k * sensor_record_bytes());
     if (count) err = cudaMemcpyAsync(ws.dSensors, records.data(), records.size(), cudaMemcpyHostToDevice, st);
     if (!err && vertex_count) err = cudaMemcpyAsync(ws.dSensorVerts, vertices_xy, vertex_count * sizeof(float2), cudaMemcpyHostToDevice, st);
+    if (!err && overlap_state && pairs && ws.hWorlds[0].n)
+        err = cudaMemcpyAsync(ws.dSensorState, overlap_state, pairs, cudaMemcpyHostToDevice, st);
     if (!err) err = cudaStreamSynchronize(st);
     if (err) return cuda_status(err);
     ws.sensorCount = count;

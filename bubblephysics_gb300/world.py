@@ -12,8 +12,10 @@ by (smaller id, larger id) as unsigned 64-bit ids, only for pairs with an object
 
 Kept for the bubble path: bubbles (dynamic or static, remove or wrap at the region), static circles / capsules /
 polygons (polygons become one-sided edges like NativePublicWorld.step), kinematic bodies with a constant drive,
-physics materials, global force, impulses and motion-role changes. Operations of the reference outside this path
-(merges, splits, joints, sensors, force fields, drives other than kinematic, render state) are rejected with
+sensors (circle or polygon; enteredSensor / exitedSensor events of bubbles), physics materials, global force, impulses
+and motion-role changes; each published bubble state carries its contour's effective radius and bounds
+(bp_world_contours) and hit_test answers on the published state (bp_world_hit_test). Operations of the reference
+outside this path (merges, splits, joints, force fields, drives other than kinematic, render state) are rejected with
 TransactionRejectionReason.UNSUPPORTED_OPERATION naming the operation, so a caller sees what is missing. The world
 steps on the GPU (World, bp_world_step); there is no CPU fallback.
 """
@@ -76,6 +78,7 @@ class BubbleDescriptor:
     region_exit_policy: RegionExitPolicy = RegionExitPolicy.REMOVE
     filter: CollisionFilter = CollisionFilter()
     event_interest: frozenset = frozenset()
+    layer: int = 0
 
 
 @dataclass(frozen=True)
@@ -105,6 +108,20 @@ class RigidBodyDescriptor:
     angular_velocity: float = 0.0
     filter: CollisionFilter = CollisionFilter()
     event_interest: frozenset = frozenset()
+    layer: int = 0
+
+
+@dataclass(frozen=True)
+class SensorDescriptor:
+    """A sensor (circle or polygon, local points about `position`, rotated by `angle`) reporting bubbles that enter or
+    leave it (SensorDescriptor of the reference; enteredSensor / exitedSensor events)."""
+    id: int
+    shape: object
+    position: tuple
+    angle: float = 0.0
+    filter: CollisionFilter = CollisionFilter()
+    reports_enter: bool = True
+    reports_exit: bool = True
 
 
 @dataclass(frozen=True)
@@ -118,6 +135,10 @@ class WorldConfiguration:
     gravity: tuple = (0.0, 0.0)              # acceleration on force-driven bubbles (0: the reference's behaviour)
     candidate_limit: int = 128
     substep_split_multiplier: float = 1.0    # NativeMetalConfiguration.substepSplitMultiplier
+    contours: bool = True                    # publish the contours' effective radius and bounds with each bubble
+    max_contour_segment_length: float = 8.0  # ReferenceConfiguration.maxContourSegmentLength
+    contour_surface_tension: float = 20.0    # ReferenceConfiguration.contourSurfaceTension
+    position_tolerance: float = 1e-4         # ReferenceConfiguration.positionTolerance (contour clearance)
 
     def __post_init__(self):
         if not (math.isfinite(self.fixed_time_step) and self.fixed_time_step > 0):
@@ -159,13 +180,14 @@ class ObjectState:
     velocity: tuple
     rotation: float
     angular_velocity: float
-    bounds: tuple             # (min x, min y, max x, max y)
+    bounds: tuple             # (min x, min y, max x, max y); a bubble's covers its deformed contour
+    effective_radius: float | None = None  # bubble: the contour's smallest distance from the centre
 
 
 @dataclass(frozen=True)
 class WorldEvent:
     """kind: transactionRejected, didAdd, didRemove, didReplace, didExitSimulationRegion, didWrap, contactBegan,
-    contactEnded."""
+    contactEnded, enteredSensor, exitedSensor (objects = (sensor, bubble))."""
     kind: str
     objects: tuple = ()
     point: tuple | None = None
@@ -235,6 +257,9 @@ class WorldTransaction:
     def apply_impulse(self, object_id: int, impulse) -> "WorldTransaction":
         return self._with("applyImpulse", object_id, tuple(float(v) for v in impulse))
 
+    def set_layer(self, object_id: int, layer: int) -> "WorldTransaction":
+        return self._with("setLayer", object_id, int(layer))
+
     def set_kinematic_drive(self, object_id: int, velocity, angular_velocity: float = 0.0) -> "WorldTransaction":
         return self._with("setKinematicDrive", object_id, tuple(float(v) for v in velocity), float(angular_velocity))
 
@@ -269,12 +294,13 @@ class _State:
     bubbles: dict = field(default_factory=dict)   # id -> _Bubble
     bodies: dict = field(default_factory=dict)    # id -> _Body
     global_force: tuple = (0.0, 0.0)
+    sensors: dict = field(default_factory=dict)   # id -> SensorDescriptor
 
     def copy(self) -> "_State":
         return _State(dict(self.materials),
                       {k: replace(v, position=v.position.copy(), velocity=v.velocity.copy()) for k, v in self.bubbles.items()},
                       {k: replace(v, position=v.position.copy()) for k, v in self.bodies.items()},
-                      self.global_force)
+                      self.global_force, dict(self.sensors))
 
 
 def _finite(*values) -> bool:
@@ -346,13 +372,14 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
         obj = args[-1]
         if kind == "replace":
             oid = args[0]
-            if oid not in state.bubbles and oid not in state.bodies:
+            if oid not in state.bubbles and oid not in state.bodies and oid not in state.sensors:
                 return TransactionRejectionReason.OBJECT_NOT_FOUND, touched
             if obj.id != oid:
                 return TransactionRejectionReason.REPLACEMENT_ID_MISMATCH, touched
             state.bubbles.pop(oid, None)
             state.bodies.pop(oid, None)
-        elif obj.id in state.bubbles or obj.id in state.bodies:
+            state.sensors.pop(oid, None)
+        elif obj.id in state.bubbles or obj.id in state.bodies or obj.id in state.sensors:
             return TransactionRejectionReason.DUPLICATE_OBJECT_ID, touched
         if isinstance(obj, BubbleDescriptor):
             reason = _validate_bubble(obj, state, region)
@@ -365,13 +392,22 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
             if reason:
                 return reason, touched
             state.bodies[obj.id] = _Body(obj, np.asarray(obj.position, np.float32).copy(), float(obj.angle))
+        elif isinstance(obj, SensorDescriptor):
+            shape = obj.shape
+            ok = _finite(*obj.position, obj.angle) and (
+                (isinstance(shape, Circle) and _finite(shape.radius) and shape.radius > 0) or
+                (isinstance(shape, Polygon) and len(shape.points) >= 3 and _finite(*np.ravel(shape.points))))
+            if not ok:
+                return TransactionRejectionReason.INVALID_VALUE, touched
+            state.sensors[obj.id] = obj
         else:
             return TransactionRejectionReason.UNSUPPORTED_OPERATION, touched
         touched["replaced" if kind == "replace" else "created"].append(obj.id)
         return None, touched
     if kind == "remove":
         oid = args[0]
-        if state.bubbles.pop(oid, None) is None and state.bodies.pop(oid, None) is None:
+        if state.bubbles.pop(oid, None) is None and state.bodies.pop(oid, None) is None and \
+                state.sensors.pop(oid, None) is None:
             return TransactionRejectionReason.OBJECT_NOT_FOUND, touched
         touched["removed"].append(oid)
         return None, touched
@@ -409,6 +445,18 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
             return TransactionRejectionReason.INVALID_VALUE, touched
         if b.desc.motion_role == MotionRole.DYNAMIC:
             b.velocity += (np.asarray(impulse, np.float32) / np.float32(b.desc.mass)).astype(np.float32)
+        return None, touched
+    if kind == "setLayer":
+        oid, layer = args
+        if not (0 <= layer < 2 ** 32) and (oid in state.bubbles or oid in state.bodies):
+            return TransactionRejectionReason.INVALID_VALUE, touched
+        if oid in state.bubbles:
+            state.bubbles[oid].desc = replace(state.bubbles[oid].desc, layer=layer)
+        elif oid in state.bodies:
+            state.bodies[oid].desc = replace(state.bodies[oid].desc, layer=layer)
+        else:
+            return TransactionRejectionReason.OBJECT_NOT_FOUND if oid not in state.sensors else \
+                TransactionRejectionReason.INCOMPATIBLE_OBJECT_KIND, touched
         return None, touched
     if kind == "setKinematicDrive":
         oid, velocity, omega = args
@@ -517,6 +565,8 @@ class BubbleWorld:
         self._native_ids: list = []
         self._segment_owner: dict = {}
         self._history: set = set()
+        self._sensor_pairs: set = set()   # (sensor id, bubble id) pairs overlapping after the last step
+        self._shapes: dict = {}           # bubble id -> (effective radius, bounds) of the last contours
         self.diagnostics = WorldDiagnostics()
 
     # -- public API ----------------------------------------------------------------------------------------------------
@@ -568,6 +618,16 @@ class BubbleWorld:
         d.pending_transaction_count = len(self._pending)
         return self._frame
 
+    def hit_test(self, point) -> int | None:
+        """The object at `point` on the published state (BubbleWorld.hitTest): a bubble inside its contour, a body or a
+        static polygon; the highest layer wins, then the largest id. None for empty space."""
+        if self._native is None:
+            return None
+        cfg = self.configuration
+        ids, _, found = self._native.hit_test([point], cfg.max_contour_segment_length, cfg.contour_surface_tension,
+                                              cfg.position_tolerance)
+        return int(ids[0]) if found[0] else None
+
     def close(self):
         if self._native is not None:
             self._native.close()
@@ -602,6 +662,7 @@ class BubbleWorld:
                 (N.BUBBLE_WRAP if d.region_exit_policy == RegionExitPolicy.WRAP else 0)
             b[i]["category"] = d.filter.category
             b[i]["mask"] = d.filter.mask
+            b[i]["layer"] = d.layer
         segs, bodies, verts, tris = [], [], [], []
         owners = {}
         next_seg = 1
@@ -613,7 +674,7 @@ class BubbleWorld:
                 pts = np.asarray(shape.points, np.float64)
                 world = np.stack([pts[:, 0] * c - pts[:, 1] * s, pts[:, 0] * s + pts[:, 1] * c], 1) + body.position
                 e = static_polygon_edges(world.astype(np.float32), next_seg, oid)
-                e["category"], e["mask"] = d.filter.category, d.filter.mask
+                e["category"], e["mask"], e["layer"] = d.filter.category, d.filter.mask, d.layer
                 for rec in e:
                     owners[int(rec["id"])] = oid
                 next_seg += len(e)
@@ -626,7 +687,7 @@ class BubbleWorld:
             rec["velocity"] = d.velocity if d.motion_role == MotionRole.KINEMATIC else (0.0, 0.0)
             rec["angular_velocity"] = d.angular_velocity if d.motion_role == MotionRole.KINEMATIC else 0.0
             rec["flags"] = N.BODY_KINEMATIC if d.motion_role == MotionRole.KINEMATIC else N.BODY_STATIC
-            rec["category"], rec["mask"] = d.filter.category, d.filter.mask
+            rec["category"], rec["mask"], rec["layer"] = d.filter.category, d.filter.mask, d.layer
             rec["vertex_offset"] = sum(len(v) for v in verts)
             rec["triangle_offset"] = sum(len(t) for t in tris)
             if isinstance(shape, Circle):
@@ -662,6 +723,14 @@ class BubbleWorld:
         staged, rec, ev = stage(self._pending[:taken], self._state, cfg.simulation_region)
         changed = bool(rec) or self._native is None
         spec, ids, owners = self._spec(staged)
+        # pairs whose sensor or bubble left in this batch end (the reference's missing-pair events)
+        gone_now = {i for r in rec for i in r.removed_object_ids + r.replaced_object_ids}
+        for pair in sorted(self._sensor_pairs):
+            if pair[0] in gone_now or pair[1] in gone_now:
+                sensor = self._state.sensors.get(pair[0])
+                if sensor is not None and sensor.reports_exit:
+                    ev.append(WorldEvent("exitedSensor", pair))
+                self._sensor_pairs.discard(pair)
         if changed or ids != self._native_ids:
             if self._native is not None:
                 self._native.close()
@@ -670,6 +739,8 @@ class BubbleWorld:
             self._native = World(spec, self._ctx) if len(ids) else None
             self._native_ids = ids
             self._segment_owner = owners
+            if self._native is not None and staged.sensors:
+                self._native.set_sensors(*self._sensor_records(staged, ids))
         removed_now = set()
         contacts = np.zeros(0, N.CONTACT_DTYPE)
         if self._native is not None:
@@ -700,6 +771,22 @@ class BubbleWorld:
                     body.angle = float(np.float32(body.angle) + np.float32(body.desc.angular_velocity) * dt)
             self.diagnostics.contact_candidate_overflow += int(rep["candidate_overflow"])
             self.diagnostics.maximum_contact_candidates_per_object = int(rep["max_candidates_per_object"])
+            if staged.sensors:
+                for e in self._native.sensor_events():
+                    pair, sensor = (int(e["sensor"]), int(e["object"])), staged.sensors[int(e["sensor"])]
+                    point = tuple(map(float, e["point"]))
+                    if e["kind"] == 1:  # 1 enter, 2 exit
+                        self._sensor_pairs.add(pair)
+                        if sensor.reports_enter:
+                            ev.append(WorldEvent("enteredSensor", pair, point))
+                    else:
+                        self._sensor_pairs.discard(pair)
+                        if sensor.reports_exit:
+                            ev.append(WorldEvent("exitedSensor", pair, point))
+            if cfg.contours:
+                _, _, _, shape, _ = self._native.contours(cfg.max_contour_segment_length, cfg.contour_surface_tension,
+                                                          cfg.position_tolerance)
+                self._shapes = {oid: (float(shape[i][1]), tuple(map(float, shape[i][2:6]))) for i, oid in enumerate(ids)}
         interested = {i for i, b in staged.bubbles.items() if EventInterest.CONTACT in b.desc.event_interest}
         interested |= {i for i, b in staged.bodies.items() if EventInterest.CONTACT in b.desc.event_interest}
         gone = removed_now | {i for r in rec for i in r.removed_object_ids + r.replaced_object_ids}
@@ -712,6 +799,30 @@ class BubbleWorld:
         if removed_now and self._native is not None:
             self._native_ids = None  # the removed slots leave the device world at the next step
         return True
+
+    def _sensor_records(self, state: _State, ids: list):
+        """Device records of the sensors (id order), their polygon vertices and the overlap state carried over."""
+        records, verts = [], []
+        sensor_ids = sorted(state.sensors)
+        for sid in sensor_ids:
+            d = state.sensors[sid]
+            r = N.Sensor()
+            r.id, r.position[:], r.angle = sid, [float(v) for v in d.position], float(d.angle)
+            if isinstance(d.shape, Circle):
+                r.radius, r.vertex_offset, r.vertex_count = float(d.shape.radius), 0, 0
+            else:
+                r.radius, r.vertex_offset, r.vertex_count = 0.0, len(verts), len(d.shape.points)
+                verts += [tuple(map(float, p)) for p in d.shape.points]
+            r.flags = N.SENSOR_ENTER_EVENTS | N.SENSOR_EXIT_EVENTS  # every flip comes back; the host keeps the pair set
+            r.category, r.mask = d.filter.category, d.filter.mask
+            records.append(r)
+        index = {oid: i for i, oid in enumerate(ids)}
+        row = {sid: k for k, sid in enumerate(sensor_ids)}
+        carried = np.zeros(len(sensor_ids) * len(ids), np.uint8)
+        for sid, b in self._sensor_pairs:
+            if sid in row and b in index:
+                carried[row[sid] * len(ids) + index[b]] = 1
+        return records, np.array(verts, np.float32).reshape(-1, 2), carried
 
     def _fail(self, status: int, rep):
         reasons = {N.E_SUBSTEP_LIMIT: WorldFailureReason.SUBSTEP_LIMIT_EXCEEDED,
@@ -729,9 +840,10 @@ class BubbleWorld:
         out = {}
         for oid, b in self._state.bubbles.items():
             r = b.desc.radius
+            effective, bounds = self._shapes.get(oid, (r, (float(b.position[0]) - r, float(b.position[1]) - r,
+                                                           float(b.position[0]) + r, float(b.position[1]) + r)))
             out[oid] = ObjectState("bubble", tuple(map(float, b.position)), tuple(map(float, b.velocity)), b.rotation,
-                                   b.angular_velocity, (float(b.position[0]) - r, float(b.position[1]) - r,
-                                                        float(b.position[0]) + r, float(b.position[1]) + r))
+                                   b.angular_velocity, bounds, effective)
         for oid, body in self._state.bodies.items():
             shape = body.desc.shape
             kind = {Circle: "circle", Capsule: "capsule", Polygon: "polygon"}[type(shape)]

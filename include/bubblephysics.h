@@ -407,12 +407,14 @@ typedef struct bp_sensor_event {
     uint32_t reserved;
 } bp_sensor_event;
 
-/* Sets the world's sensors (replacing any earlier ones; overlaps start empty). Every later step compares each bubble
+/* Sets the world's sensors (replacing any earlier ones). overlap_state (may be NULL: nothing overlaps) holds one byte
+ * per (sensor, bubble) pair, sensor-major, 1 where the pair overlapped before: a host that rebuilds a world carries
+ * its sensors' state over. Every later step compares each bubble
  * against each sensor on the device (nativeCompactSensorEvents, NativePostSolveKernels:601-648: a circle bubble
  * overlaps a circle sensor within the sum of the radii, a polygon sensor when its centre is inside or an edge is within
  * its radius; removed bubbles overlap nothing) and lists the bubbles that entered or left. */
 int bp_world_set_sensors(bp_world* world, const bp_sensor* sensors, uint32_t count, const float* vertices_xy,
-                         uint32_t vertex_count);
+                         uint32_t vertex_count, const uint8_t* overlap_state);
 /* Sensor events of the last step; *count = all of them (capacity may be smaller). */
 int bp_world_read_sensor_events(bp_world* world, bp_sensor_event* out, uint32_t capacity, uint32_t* count);
 

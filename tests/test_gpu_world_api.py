@@ -108,3 +108,71 @@ def test_a_failed_step_stops_the_world(ctx):
     assert world.diagnostics.failure_reason == WorldFailureReason.SUBSTEP_LIMIT_EXCEEDED
     assert frame.step_index == 0
     assert world.advance(1.0) is frame
+
+
+def sensor_world(ctx):
+    """One bubble crossing a circle sensor (both kinds of event) and a polygon sensor that reports exits only."""
+    from bubblephysics_gb300.world import SensorDescriptor
+    world = BubbleWorld(WorldConfiguration(REGION), ctx)
+    tx = WorldTransaction().update_physics_material("soft", PhysicsMaterial(229.0))
+    tx = tx.add(BubbleDescriptor(1, (100.0, 200.0), 10.0, 1.0, "soft", velocity=(120.0, 0.0)))
+    tx = tx.add(SensorDescriptor(50, Circle(20.0), (200.0, 200.0)))
+    tx = tx.add(SensorDescriptor(60, Polygon(((-10, -30), (10, -30), (10, 30), (-10, 30))), (300.0, 200.0),
+                                 reports_enter=False))
+    world.submit(tx)
+    return world
+
+
+def test_sensor_events_follow_the_published_positions(ctx):
+    world = sensor_world(ctx)
+    seen, prev = [], None
+    for step in range(135):  # x from 100 to 370, inside the region
+        frame = world.advance(1.0 / 60)
+        p = np.array(frame.objects[1].position, np.float32)
+        d = p - np.float32(200.0)
+        inside = bool(d[0] * d[0] + d[1] * d[1] <= np.float32(30.0) * np.float32(30.0))
+        for e in frame.events:
+            if e.kind.endswith("Sensor"):
+                seen.append((e.kind, e.objects))
+                if e.objects[0] == 50:
+                    assert inside == (e.kind == "enteredSensor") and prev is not None and prev != inside
+                assert e.point == tuple(map(float, frame.objects[1].position))
+        prev = inside
+    assert seen == [("enteredSensor", (50, 1)), ("exitedSensor", (50, 1)), ("exitedSensor", (60, 1))]
+
+
+def test_sensor_state_survives_a_rebuild_and_removal_ends_the_pair(ctx):
+    world = sensor_world(ctx)
+    kinds = []
+    for _ in range(45):  # inside the circle sensor by now
+        kinds += [e.kind for e in world.advance(1.0 / 60).events if e.kind.endswith("Sensor")]
+    assert kinds == ["enteredSensor"] and world._sensor_pairs == {(50, 1)}
+    world.submit(WorldTransaction().add(BubbleDescriptor(2, (50.0, 50.0), 8.0, 1.0, "soft")))  # rebuilds the device world
+    frame = world.advance(1.0 / 60)
+    assert not [e for e in frame.events if e.kind.endswith("Sensor")]
+    world.submit(WorldTransaction().remove(1))
+    frame = world.advance(1.0 / 60)
+    assert [(e.kind, e.objects) for e in frame.events if e.kind.endswith("Sensor")] == [("exitedSensor", (50, 1))]
+    assert world._sensor_pairs == set()
+
+
+def test_hit_test_and_contour_shapes(ctx):
+    world = BubbleWorld(WorldConfiguration(REGION), ctx)
+    tx = WorldTransaction().update_physics_material("soft", PhysicsMaterial(229.0))
+    tx = tx.add(BubbleDescriptor(1, (150.0, 200.0), 12.0, 1.0, "soft", velocity=(150.0, 0.0)))
+    tx = tx.add(BubbleDescriptor(2, (250.0, 200.0), 12.0, 1.0, "soft", velocity=(-150.0, 0.0)))
+    tx = tx.add(BubbleDescriptor(3, (100.0, 350.0), 10.0, 1.0, "soft"))
+    tx = tx.add(RigidBodyDescriptor(1000, Circle(30.0), (320.0, 80.0), layer=2))
+    world.submit(tx)
+    pressed = []
+    for _ in range(40):
+        frame = world.advance(1.0 / 60)
+        pressed.append(min(frame.objects[1].effective_radius, frame.objects[2].effective_radius))
+    free = frame.objects[3]
+    assert abs(free.effective_radius - 10.0) <= 1e-3
+    lo, hi = np.array(free.bounds[:2]), np.array(free.bounds[2:])
+    assert np.all(lo >= np.array(free.position) - 10.0 - 1e-3) and np.all(lo <= np.array(free.position) - 9.9)
+    assert np.all(hi <= np.array(free.position) + 10.0 + 1e-3) and np.all(hi >= np.array(free.position) + 9.9)
+    assert min(pressed) < 11.9  # the pair met and pressed in
+    assert world.hit_test(free.position) == 3 and world.hit_test((320.0, 80.0)) == 1000
+    assert world.hit_test((10.0, 390.0)) is None

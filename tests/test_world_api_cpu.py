@@ -107,3 +107,48 @@ def test_contact_pairs_order_by_unsigned_ids():
     events, _ = W.contact_transitions(c, {}, {1, 2, -1}, set(), 1.0, set())
     # -1 is 0xFFFF...FFFF as an ObjectID: the largest id
     assert [e.objects for e in events] == [(1, 2), (2, -1)]
+
+
+def test_sensors_stage_like_objects():
+    sensor = W.SensorDescriptor(50, Circle(20.0), (100.0, 100.0))
+    state, receipts, _ = W.stage([(1, soft().add(sensor).add(bubble(1, 100, 100)))], W._State(), REGION)
+    assert receipts[0].created_object_ids == (50, 1) and state.sensors[50] == sensor  # a sensor overlaps freely
+    for bad in (W.SensorDescriptor(51, Circle(0.0), (0, 0)), W.SensorDescriptor(51, W.Polygon(((0, 0), (1, 0))), (0, 0)),
+                W.SensorDescriptor(51, Circle(5.0), (float("nan"), 0))):
+        _, rec, ev = W.stage([(2, WorldTransaction().add(bad))], state, REGION)
+        assert rec == [] and ev[0].rejection.reason == R.INVALID_VALUE
+    _, _, ev = W.stage([(3, WorldTransaction().add(W.SensorDescriptor(1, Circle(5.0), (0, 0))))], state, REGION)
+    assert ev[0].rejection.reason == R.DUPLICATE_OBJECT_ID
+    moved = W.SensorDescriptor(50, W.Polygon(((-5, -5), (5, -5), (0, 5))), (30.0, 30.0))
+    replaced, rec, _ = W.stage([(4, WorldTransaction().replace(50, moved))], state, REGION)
+    assert rec[0].replaced_object_ids == (50,) and replaced.sensors[50] == moved
+    removed, rec, _ = W.stage([(5, WorldTransaction().remove(50))], state, REGION)
+    assert rec[0].removed_object_ids == (50,) and removed.sensors == {} and 50 in state.sensors
+
+
+def test_sensor_records_and_carried_overlap_state():
+    world = BubbleWorld(WorldConfiguration(REGION))
+    state, _, _ = W.stage([(1, soft().add(W.SensorDescriptor(9, W.Polygon(((0, 0), (4, 0), (0, 4))), (1.0, 2.0), 0.5,
+                                                                 filter=W.CollisionFilter(2, 6), reports_enter=False))
+                               .add(W.SensorDescriptor(4, Circle(7.0), (50.0, 60.0))))], W._State(), REGION)
+    world._sensor_pairs = {(4, 30), (9, 10), (9, 99)}  # 99 is no longer a bubble of the device world
+    records, verts, carried = world._sensor_records(state, [10, 20, 30])
+    assert [r.id for r in records] == [4, 9]
+    assert records[0].radius == 7.0 and records[0].vertex_count == 0
+    assert records[1].vertex_offset == 0 and records[1].vertex_count == 3 and records[1].angle == 0.5
+    assert (records[1].category, records[1].mask) == (2, 6)
+    assert all(r.flags == N.SENSOR_ENTER_EVENTS | N.SENSOR_EXIT_EVENTS for r in records)  # filtered on the host
+    assert verts.tolist() == [[0, 0], [4, 0], [0, 4]]
+    assert carried.tolist() == [0, 0, 1, 1, 0, 0]
+
+
+def test_set_layer():
+    state, _, _ = W.stage([(1, soft().add(bubble(1, 10, 10)).add(W.SensorDescriptor(5, Circle(3.0), (0, 0))))],
+                          W._State(), REGION)
+    layered, rec, _ = W.stage([(2, WorldTransaction().set_layer(1, 7))], state, REGION)
+    assert rec and layered.bubbles[1].desc.layer == 7 and state.bubbles[1].desc.layer == 0
+    for tx, reason in ((WorldTransaction().set_layer(1, -1), R.INVALID_VALUE),
+                       (WorldTransaction().set_layer(5, 1), R.INCOMPATIBLE_OBJECT_KIND),
+                       (WorldTransaction().set_layer(8, 1), R.OBJECT_NOT_FOUND)):
+        _, rec, ev = W.stage([(3, tx)], state, REGION)
+        assert rec == [] and ev[0].rejection.reason == reason
