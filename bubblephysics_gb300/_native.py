@@ -135,7 +135,7 @@ class ContourConfig(C.Structure):
 class Sensor(C.Structure):
     _fields_ = [("id", C.c_int64), ("position", f2), ("angle", C.c_float), ("radius", C.c_float),
                 ("vertex_offset", C.c_uint32), ("vertex_count", C.c_uint32), ("flags", C.c_uint32),
-                ("category", C.c_uint32), ("mask", C.c_uint32), ("reserved", C.c_uint32)]
+                ("reserved", C.c_uint32 * 3)]
 
 
 SENSOR_ENTER_EVENTS, SENSOR_EXIT_EVENTS = 1, 2
@@ -189,7 +189,7 @@ CONTACT_DTYPE = np.dtype({"names": ["participants", "kind", "feature", "normal",
                           "formats": [("<i8", 2), "<u4", "<u4", ("<f4", 2), ("<f4", 2), "<f4", "<f4", "<f4",
                                       ("<u4", 3)],
                           "offsets": [0, 16, 20, 24, 32, 40, 44, 48, 52], "itemsize": 64})
-SENSOR_EVENT_DTYPE = np.dtype({"names": ["sensor", "object", "kind", "point", "reserved"],
+SENSOR_EVENT_DTYPE = np.dtype({"names": ["sensor", "object", "kind", "point", "object_kind"],
                                "formats": ["<i8", "<i8", "<u4", ("<f4", 2), "<u4"],
                                "offsets": [0, 8, 16, 20, 28], "itemsize": 32})
 KEY_DTYPE = np.dtype({"names": ["kind", "reserved", "first", "second"], "formats": ["<u4", "<u4", "<i8", "<i8"],
@@ -248,7 +248,7 @@ _SIGNATURES = {
     "bp_world_contours": (C.c_int, [_P, C.POINTER(ContourConfig), _P, _P, _P, _P, C.POINTER(C.c_uint32),
                                     C.POINTER(C.c_float)]),
     "bp_world_hit_test": (C.c_int, [_P, C.POINTER(ContourConfig), _P, C.c_uint32, _P, _P, _P]),
-    "bp_world_set_sensors": (C.c_int, [_P, _P, C.c_uint32, _P, C.c_uint32, _P]),
+    "bp_world_set_sensors": (C.c_int, [_P, _P, C.c_uint32, _P, C.c_uint32, _P, _P]),
     "bp_world_read_sensor_events": (C.c_int, [_P, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
     "bp_server_create": (C.c_int, [_P, C.POINTER(ServerConfig), C.POINTER(_P)]),
     "bp_server_destroy": (C.c_int, [_P]),

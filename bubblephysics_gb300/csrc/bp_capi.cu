@@ -859,8 +859,8 @@ int bp_world_step(bp_world* world, uint32_t steps, bp_step_report* reports) {
         }
         ws.bubbleSubsteps += (uint64_t)out[s].substep_count * ws.hWorlds[0].n;
         if (ws.sensorCount && out[s].status == BP_OK) {
-            err = launch_sensors(ws.S, ws.hWorlds[0], ws.dSensors, ws.sensorCount, ws.dSensorVerts, ws.dSensorState,
-                                 ws.dSensorKinds, ws.dSensorEvents, ws.sensorEventCapacity, ws.dSensorCount, st);
+            err = launch_sensors(ws.S, ws.hWorlds[0], ws.dSensors, ws.sensorCount, ws.dSensorVerts, ws.dSensorAllowed,
+                                 ws.dSensorState, ws.dSensorKinds, ws.dSensorEvents, ws.sensorEventCapacity, ws.dSensorCount, st);
             if (err) return cuda_status(err);
         }
         status = out[s].status;
@@ -1061,7 +1061,7 @@ int bp_world_hit_test(bp_world* world, const bp_contour_config* config, const fl
 }
 
 int bp_world_set_sensors(bp_world* world, const bp_sensor* sensors, uint32_t count, const float* vertices_xy,
-                         uint32_t vertex_count, const uint8_t* overlap_state) {
+                         uint32_t vertex_count, const uint8_t* allowed, const uint8_t* overlap_state) {
     if (!world || (count && !sensors) || (vertex_count && !vertices_xy)) return BP_E_INVALID;
     for (uint32_t k = 0; k < count; ++k) {
         const bp_sensor& r = sensors[k];
@@ -1078,7 +1078,8 @@ int bp_world_set_sensors(bp_world* world, const bp_sensor* sensors, uint32_t cou
     ws.sensorAllocations.clear();
     ws.sensorCount = 0;
     if (err) return cuda_status(err);
-    const uint64_t pairs = (uint64_t)count * std::max(ws.hWorlds[0].n, 1u);
+    const uint64_t objects = (uint64_t)ws.hWorlds[0].n + ws.hWorlds[0].nb;
+    const uint64_t pairs = (uint64_t)count * objects;
     if (pairs > 0xffffffffull) return BP_E_CAPACITY;
     auto take = [&](size_t bytes) -> void* {
         void* p = nullptr;
@@ -1088,6 +1089,7 @@ int bp_world_set_sensors(bp_world* world, const bp_sensor* sensors, uint32_t cou
     };
     ws.dSensors = take(count * sensor_record_bytes());
     ws.dSensorVerts = (float2*)take(vertex_count * sizeof(float2));
+    ws.dSensorAllowed = allowed ? (uint8_t*)take(pairs) : nullptr;
     ws.dSensorState = (uint8_t*)take(pairs);
     ws.dSensorKinds = (uint8_t*)take(pairs);
     ws.dSensorEvents = (bp_sensor_event*)take(pairs * sizeof(bp_sensor_event));
@@ -1097,7 +1099,8 @@ int bp_world_set_sensors(bp_world* world, const bp_sensor* sensors, uint32_t cou
     for (uint32_t k = 0; k < count; ++k) sensor_to_device(sensors[k], records.data() + k * sensor_record_bytes());
     if (count) err = cudaMemcpyAsync(ws.dSensors, records.data(), records.size(), cudaMemcpyHostToDevice, st);
     if (!err && vertex_count) err = cudaMemcpyAsync(ws.dSensorVerts, vertices_xy, vertex_count * sizeof(float2), cudaMemcpyHostToDevice, st);
-    if (!err && overlap_state && pairs && ws.hWorlds[0].n)
+    if (!err && allowed && pairs) err = cudaMemcpyAsync(ws.dSensorAllowed, allowed, pairs, cudaMemcpyHostToDevice, st);
+    if (!err && overlap_state && pairs)
         err = cudaMemcpyAsync(ws.dSensorState, overlap_state, pairs, cudaMemcpyHostToDevice, st);
     if (!err) err = cudaStreamSynchronize(st);
     if (err) return cuda_status(err);

@@ -32,8 +32,8 @@ cudaError_t launch_hit_test(const DState& S, const DWorld& W, const float2* quer
                             const uint32_t* bubbleLayers, const uint32_t* segLayers, const uint32_t* bodyLayers,
                             long long* ids, uint32_t* layers, uint32_t* found, cudaStream_t stream);
 cudaError_t launch_sensors(const DState& S, const DWorld& W, const void* sensors, uint32_t sensorCount,
-                           const float2* verts, uint8_t* state, uint8_t* kinds, bp_sensor_event* events,
-                           uint32_t capacity, uint32_t* count, cudaStream_t stream);
+                           const float2* verts, const uint8_t* allowed, uint8_t* state, uint8_t* kinds,
+                           bp_sensor_event* events, uint32_t capacity, uint32_t* count, cudaStream_t stream);
 size_t sensor_record_bytes();
 void sensor_to_device(const bp_sensor& in, void* out);
 cudaError_t launch_contours(const DState& S, const DWorld& W, float maxEdge, float tension, float clearance,
@@ -143,6 +143,7 @@ struct WorldSet {
     // the event list of the last step and its length
     void* dSensors = nullptr;
     float2* dSensorVerts = nullptr;
+    uint8_t* dSensorAllowed = nullptr;  // null: every pair
     uint8_t* dSensorState = nullptr;
     uint8_t* dSensorKinds = nullptr;
     bp_sensor_event* dSensorEvents = nullptr;

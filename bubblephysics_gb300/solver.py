@@ -159,15 +159,17 @@ class World:
                                            C.c_void_p(found.ctypes.data)), "bp_world_hit_test")
         return ids, layers, found
 
-    def set_sensors(self, sensors, vertices=None, state=None):
-        """Sensors (a list of N.Sensor) with their polygon vertices ((m, 2) float32) and, optionally, the overlap state
-        to start from (uint8, sensors x bubbles): from the next step on, each step lists the bubbles that entered or
-        left them."""
+    def set_sensors(self, sensors, vertices=None, state=None, allowed=None):
+        """Sensors (a list of N.Sensor) with their polygon vertices ((m, 2) float32) and, optionally, per pair (uint8,
+        sensors x (bubbles, then bodies)) the overlap state to start from and which pairs the sensors' object filters
+        allow: from the next step on, each step lists the bubbles and bodies that entered or left them."""
         arr = (N.Sensor * max(len(sensors), 1))(*sensors)
         v = np.ascontiguousarray(np.zeros((0, 2)) if vertices is None else vertices, np.float32).reshape(-1, 2)
         st = None if state is None else np.ascontiguousarray(state, np.uint8)
+        ok = None if allowed is None else np.ascontiguousarray(allowed, np.uint8)
         N.check(self.lib.bp_world_set_sensors(self.handle, C.cast(arr, C.c_void_p), len(sensors),
                                               C.c_void_p(v.ctypes.data), v.shape[0],
+                                              None if ok is None else C.c_void_p(ok.ctypes.data),
                                               None if st is None else C.c_void_p(st.ctypes.data)),
                 "bp_world_set_sensors")
 

@@ -45,6 +45,15 @@ class CollisionFilter:
 
 
 @dataclass(frozen=True)
+class ObjectFilter:
+    """The objects a sensor watches (ObjectFilter of the reference): None = every object, an empty set = none."""
+    object_ids: frozenset | None = None
+
+    def takes(self, object_id: int) -> bool:
+        return self.object_ids is None or object_id in self.object_ids
+
+
+@dataclass(frozen=True)
 class PhysicsMaterial:
     """Contact stiffness K_c and damping gamma of a bubble material (PhysicsMaterial, Model/Resources.swift)."""
     contact_stiffness: float
@@ -113,13 +122,15 @@ class RigidBodyDescriptor:
 
 @dataclass(frozen=True)
 class SensorDescriptor:
-    """A sensor (circle or polygon, local points about `position`, rotated by `angle`) reporting bubbles that enter or
-    leave it (SensorDescriptor of the reference; enteredSensor / exitedSensor events)."""
+    """A sensor (circle or polygon, local points about `position`, rotated by `angle`) reporting the bubbles and bodies
+    that enter or leave it (SensorDescriptor of the reference; enteredSensor / exitedSensor events). Bodies are the
+    circles, capsules and kinematic polygons; a static polygon, held by the device world as one-sided edges, is not
+    reported."""
     id: int
     shape: object
     position: tuple
     angle: float = 0.0
-    filter: CollisionFilter = CollisionFilter()
+    filter: ObjectFilter = ObjectFilter()
     reports_enter: bool = True
     reports_exit: bool = True
 
@@ -187,7 +198,7 @@ class ObjectState:
 @dataclass(frozen=True)
 class WorldEvent:
     """kind: transactionRejected, didAdd, didRemove, didReplace, didExitSimulationRegion, didWrap, contactBegan,
-    contactEnded, enteredSensor, exitedSensor (objects = (sensor, bubble))."""
+    contactEnded, enteredSensor, exitedSensor (objects = (sensor, bubble or body))."""
     kind: str
     objects: tuple = ()
     point: tuple | None = None
@@ -740,7 +751,8 @@ class BubbleWorld:
             self._native_ids = ids
             self._segment_owner = owners
             if self._native is not None and staged.sensors:
-                self._native.set_sensors(*self._sensor_records(staged, ids))
+                records, verts, carried, allowed = self._sensor_records(staged, ids + [int(v) for v in spec.bodies["id"]])
+                self._native.set_sensors(records, verts, carried, allowed)
         removed_now = set()
         contacts = np.zeros(0, N.CONTACT_DTYPE)
         if self._native is not None:
@@ -774,7 +786,7 @@ class BubbleWorld:
             if staged.sensors:
                 for e in self._native.sensor_events():
                     pair, sensor = (int(e["sensor"]), int(e["object"])), staged.sensors[int(e["sensor"])]
-                    point = tuple(map(float, e["point"]))
+                    point = tuple(map(float, e["point"]))  # the bubble's centre or the body's position
                     if e["kind"] == 1:  # 1 enter, 2 exit
                         self._sensor_pairs.add(pair)
                         if sensor.reports_enter:
@@ -800,8 +812,10 @@ class BubbleWorld:
             self._native_ids = None  # the removed slots leave the device world at the next step
         return True
 
-    def _sensor_records(self, state: _State, ids: list):
-        """Device records of the sensors (id order), their polygon vertices and the overlap state carried over."""
+    def _sensor_records(self, state: _State, objects: list):
+        """Device records of the sensors (id order), their polygon vertices, and per (sensor, object) pair the overlap
+        state carried over and whether the sensor's filter takes the object; `objects` are the device world's bubbles,
+        then its bodies."""
         records, verts = [], []
         sensor_ids = sorted(state.sensors)
         for sid in sensor_ids:
@@ -814,15 +828,15 @@ class BubbleWorld:
                 r.radius, r.vertex_offset, r.vertex_count = 0.0, len(verts), len(d.shape.points)
                 verts += [tuple(map(float, p)) for p in d.shape.points]
             r.flags = N.SENSOR_ENTER_EVENTS | N.SENSOR_EXIT_EVENTS  # every flip comes back; the host keeps the pair set
-            r.category, r.mask = d.filter.category, d.filter.mask
             records.append(r)
-        index = {oid: i for i, oid in enumerate(ids)}
+        index = {oid: i for i, oid in enumerate(objects)}
         row = {sid: k for k, sid in enumerate(sensor_ids)}
-        carried = np.zeros(len(sensor_ids) * len(ids), np.uint8)
+        carried = np.zeros(len(sensor_ids) * len(objects), np.uint8)
         for sid, b in self._sensor_pairs:
             if sid in row and b in index:
-                carried[row[sid] * len(ids) + index[b]] = 1
-        return records, np.array(verts, np.float32).reshape(-1, 2), carried
+                carried[row[sid] * len(objects) + index[b]] = 1
+        allowed = np.array([state.sensors[sid].filter.takes(oid) for sid in sensor_ids for oid in objects], np.uint8)
+        return records, np.array(verts, np.float32).reshape(-1, 2), carried, allowed
 
     def _fail(self, status: int, rep):
         reasons = {N.E_SUBSTEP_LIMIT: WorldFailureReason.SUBSTEP_LIMIT_EXCEEDED,

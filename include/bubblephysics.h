@@ -393,28 +393,30 @@ typedef struct bp_sensor {
     uint32_t vertex_offset;          /* polygon sensor: into the vertex array (float2 pairs) */
     uint32_t vertex_count;
     uint32_t flags;                  /* BP_SENSOR_* */
-    uint32_t category;               /* filter against the bubbles' filters */
-    uint32_t mask;
-    uint32_t reserved;
+    uint32_t reserved[3];
 } bp_sensor;
 
-/* One sensor event of the last step, in (sensor, bubble) order. 32 bytes. */
+/* One sensor event of the last step, in pair order (sensor, then bubbles, then bodies). 32 bytes. */
 typedef struct bp_sensor_event {
     int64_t sensor;
-    int64_t object;                  /* bubble id */
+    int64_t object;                  /* bubble or body id */
     uint32_t kind;                   /* 1 entered, 2 exited */
-    float point[2];                  /* bubble centre */
-    uint32_t reserved;
+    float point[2];                  /* bubble centre or body position */
+    uint32_t object_kind;            /* 0 bubble, 1 body */
 } bp_sensor_event;
 
-/* Sets the world's sensors (replacing any earlier ones). overlap_state (may be NULL: nothing overlaps) holds one byte
- * per (sensor, bubble) pair, sensor-major, 1 where the pair overlapped before: a host that rebuilds a world carries
- * its sensors' state over. Every later step compares each bubble
- * against each sensor on the device (nativeCompactSensorEvents, NativePostSolveKernels:601-648: a circle bubble
- * overlaps a circle sensor within the sum of the radii, a polygon sensor when its centre is inside or an edge is within
- * its radius; removed bubbles overlap nothing) and lists the bubbles that entered or left. */
+/* Sets the world's sensors (replacing any earlier ones). A pair is a sensor and one of the world's objects: its
+ * bubbles in input order, then its bodies in input order; per-pair arrays hold one byte per pair, sensor-major.
+ * allowed (may be NULL: every pair) is 1 where the sensor's object filter takes the object (the reference's
+ * ObjectFilter.objectIDs, expanded per pair like NativeMetalSolver.swift:555-575); overlap_state (may be NULL: nothing
+ * overlaps) is 1 where the pair overlapped before, so a host that rebuilds a world carries its sensors' state over.
+ * Every later step compares each allowed pair on the device and lists the objects that entered or left: a bubble as in
+ * nativeCompactSensorEvents (NativePostSolveKernels:601-648: within the summed radii of a circle sensor, inside a
+ * polygon sensor or within its radius of an edge; removed bubbles overlap nothing), a body at its end-of-step pose as
+ * in nativeCompactPolygonSensorEvents (:740-775: a circle or capsule core within its radius, a polygon's edges crossing
+ * or touching, or either shape inside the other). */
 int bp_world_set_sensors(bp_world* world, const bp_sensor* sensors, uint32_t count, const float* vertices_xy,
-                         uint32_t vertex_count, const uint8_t* overlap_state);
+                         uint32_t vertex_count, const uint8_t* allowed, const uint8_t* overlap_state);
 /* Sensor events of the last step; *count = all of them (capacity may be smaller). */
 int bp_world_read_sensor_events(bp_world* world, bp_sensor_event* out, uint32_t capacity, uint32_t* count);
 

@@ -1570,39 +1570,138 @@ static void world_hit_test(const World<float>& w, float maxEdge, float tension, 
     }
 }
 
-// Sensor events of the published state against the overlap state of the previous evaluation
-// (nativeCompactSensorEvents, NativePostSolveKernels:601-648), in (sensor, bubble) order; `state` (sensors x bubbles)
-// is updated in place. Returns the number of events (written up to `capacity`).
+// Sensor geometry (NativePostSolveKernels:650-738), each helper restating the reference function named beside it.
+struct SensorFrame {
+    float px, py, c, s;
+    const bp_sensor* sn;
+    const float* verts;
+    V2<float> vertex(uint32_t j) const {  // world-frame ring vertex
+        uint32_t k = sn->vertex_offset + j;
+        V2<float> v = mk<float>(verts[2 * k], verts[2 * k + 1]);
+        return mk<float>(px, py) + rotate_cs(v, c, s);
+    }
+};
+// nativePointInPolygon
+template <typename F> static bool inside_ring(V2<float> p, uint32_t count, F vertex) {
+    bool inside = false;
+    for (uint32_t i = 0; i < count; ++i) {
+        V2<float> a = vertex(i), b = vertex((i + 1) % count);
+        if ((a.y > p.y) != (b.y > p.y) && p.x < (b.x - a.x) * (p.y - a.y) / (b.y - a.y) + a.x) inside = !inside;
+    }
+    return inside;
+}
+// nativePointSegmentDistanceSquared
+static float point_segment_d2(V2<float> p, V2<float> a, V2<float> b) {
+    V2<float> ab = b - a;
+    float t = std::fmin(std::fmax(dot(p - a, ab) / std::fmax(dot(ab, ab), 1e-20f), 0.0f), 1.0f);
+    V2<float> d = p - (a + ab * t);
+    return dot(d, d);
+}
+// nativeSegmentsCross
+static bool segments_cross(V2<float> a, V2<float> b, V2<float> c, V2<float> d) {
+    if (std::fmax(std::fmin(a.x, b.x), std::fmin(c.x, d.x)) > std::fmin(std::fmax(a.x, b.x), std::fmax(c.x, d.x)) ||
+        std::fmax(std::fmin(a.y, b.y), std::fmin(c.y, d.y)) > std::fmin(std::fmax(a.y, b.y), std::fmax(c.y, d.y)))
+        return false;
+    V2<float> ab = b - a, cd = d - c;
+    float p = cross(ab, c - a), q = cross(ab, d - a), r = cross(cd, a - c), s = cross(cd, b - c);
+    return ((p <= 0 && q >= 0) || (p >= 0 && q <= 0)) && ((r <= 0 && s >= 0) || (r >= 0 && s <= 0));
+}
+// nativeSegmentDistance, NativeGeometryKernels:444-462
+static float segment_distance(V2<float> a, V2<float> b, V2<float> c, V2<float> d) {
+    V2<float> r = b - a, s = d - c;
+    float denominator = cross(r, s);
+    if (std::fabs(denominator) > 1e-12f) {
+        V2<float> qp = c - a;
+        float t = cross(qp, s) / denominator, u = cross(qp, r) / denominator;
+        if (t >= 0 && t <= 1 && u >= 0 && u <= 1) return 0.0f;
+    }
+    float best = INFINITY;
+    best = std::fmin(best, len(a - closest_point(a, c, d)));
+    best = std::fmin(best, len(b - closest_point(b, c, d)));
+    best = std::fmin(best, len(c - closest_point(c, a, b)));
+    best = std::fmin(best, len(d - closest_point(d, a, b)));
+    return best;
+}
+
+// A bubble against a sensor, in the sensor's frame (nativeCompactSensorEvents, :610-632).
+static bool bubble_overlaps_sensor(const SensorFrame& f, V2<float> center, float radius) {
+    const bp_sensor& sn = *f.sn;
+    float dx = center.x - f.px, dy = center.y - f.py;
+    float lx = f.c * dx + f.s * dy, ly = -f.s * dx + f.c * dy;
+    if (sn.vertex_count == 0) {
+        float reach = sn.radius + radius;
+        return lx * lx + ly * ly <= reach * reach;
+    }
+    bool inside = false, near = false;
+    for (uint32_t j = 0; j < sn.vertex_count; ++j) {
+        uint32_t ia = sn.vertex_offset + j, ib = sn.vertex_offset + (j + 1) % sn.vertex_count;
+        float ax = f.verts[2 * ia], ay = f.verts[2 * ia + 1], bx = f.verts[2 * ib], by = f.verts[2 * ib + 1];
+        if ((ay > ly) != (by > ly) && lx < (bx - ax) * (ly - ay) / (by - ay) + ax) inside = !inside;
+        float abx = bx - ax, aby = by - ay;
+        float t = std::fmin(std::fmax(((lx - ax) * abx + (ly - ay) * aby) / std::fmax(abx * abx + aby * aby, 1e-20f), 0.0f), 1.0f);
+        float ex = lx - (ax + abx * t), ey = ly - (ay + aby * t);
+        if (ex * ex + ey * ey <= radius * radius) near = true;
+    }
+    return near || inside;
+}
+
+// A body at its end-of-step pose against a sensor (nativeRoundOverlapsSensor, nativeRigidOverlapsSensor, :677-738).
+static bool body_overlaps_sensor(const World<float>& w, const SensorFrame& f, const Body<float>& b) {
+    const bp_sensor& sn = *f.sn;
+    if (b.vcount == 0) return false;
+    Pose<float> pose;
+    pose.pos = b.pos;
+    pose.c = b.cosEnd;
+    pose.s = b.sinEnd;
+    auto bodyVertex = [&](uint32_t i) { return body_vertex(w, b, pose, i); };
+    auto sensorVertex = [&](uint32_t j) { return f.vertex(j); };
+    const V2<float> centre = mk<float>(f.px, f.py);
+    if (b.kind != BP_BODY_POLYGON) {
+        V2<float> a = bodyVertex(0), e = b.vcount > 1 ? bodyVertex(1) : a;
+        if (sn.vertex_count == 0) {
+            float reach = b.coreRadius + sn.radius;
+            return point_segment_d2(centre, a, e) <= reach * reach;
+        }
+        if (inside_ring(a, sn.vertex_count, sensorVertex)) return true;
+        for (uint32_t j = 0; j < sn.vertex_count; ++j)
+            if (segment_distance(a, e, f.vertex(j), f.vertex((j + 1) % sn.vertex_count)) <= b.coreRadius) return true;
+        return false;
+    }
+    if (sn.vertex_count == 0 && inside_ring(centre, b.vcount, bodyVertex)) return true;
+    for (uint32_t i = 0; i < b.vcount; ++i) {
+        V2<float> a = bodyVertex(i), e = bodyVertex((i + 1) % b.vcount);
+        if (sn.vertex_count == 0) {
+            if (point_segment_d2(centre, a, e) <= sn.radius * sn.radius) return true;
+        } else {
+            if (inside_ring(a, sn.vertex_count, sensorVertex)) return true;
+            for (uint32_t j = 0; j < sn.vertex_count; ++j)
+                if (segments_cross(a, e, f.vertex(j), f.vertex((j + 1) % sn.vertex_count))) return true;
+        }
+    }
+    if (sn.vertex_count) return inside_ring(f.vertex(0), b.vcount, bodyVertex);
+    return false;
+}
+
+// Sensor events of the published state against the overlap state of the previous evaluation, in pair order: for each
+// sensor its bubbles, then its bodies (nativeCompactSensorEvents and nativeCompactPolygonSensorEvents,
+// NativePostSolveKernels:601-648 and 740-775). `allowed` (may be null) and `state` hold one byte per pair,
+// sensor-major; `state` is updated in place. The rotation is cosf / sinf of the angle, as the CUDA path's host takes
+// it. Returns the number of events (written up to `capacity`).
 static uint32_t world_sensor_events(const World<float>& w, const bp_sensor* sensors, uint32_t count, const float* verts,
-                                    uint8_t* state, bp_sensor_event* out, uint32_t capacity) {
+                                    const uint8_t* allowed, uint8_t* state, bp_sensor_event* out, uint32_t capacity) {
     uint32_t events = 0;
+    const uint32_t nb = (uint32_t)w.bodies.size(), objects = w.n + nb;
     for (uint32_t si = 0; si < count; ++si) {
         const bp_sensor& sn = sensors[si];
-        for (uint32_t i = 0; i < w.n; ++i) {
+        SensorFrame f{sn.position[0], sn.position[1], std::cos(sn.angle), std::sin(sn.angle), &sn, verts};
+        for (uint32_t j = 0; j < objects; ++j) {
+            const uint64_t pair = (uint64_t)si * objects + j;
             bool overlapping = false;
-            if (!is_removed(w, i) && filter_accepts(w.cat[i], w.mask[i], sn.category, sn.mask)) {
-                float dx = w.pPos[i].x - sn.position[0], dy = w.pPos[i].y - sn.position[1];
-                float c = std::cos(sn.angle), s = std::sin(sn.angle);
-                float lx = c * dx + s * dy, ly = -s * dx + c * dy;
-                float radius = w.radius[i];
-                if (sn.vertex_count == 0) {
-                    float reach = sn.radius + radius;
-                    overlapping = lx * lx + ly * ly <= reach * reach;
-                } else {
-                    bool inside = false;
-                    for (uint32_t j = 0; j < sn.vertex_count; ++j) {
-                        uint32_t ia = sn.vertex_offset + j, ib = sn.vertex_offset + (j + 1) % sn.vertex_count;
-                        float ax = verts[2 * ia], ay = verts[2 * ia + 1], bx = verts[2 * ib], by = verts[2 * ib + 1];
-                        if ((ay > ly) != (by > ly) && lx < (bx - ax) * (ly - ay) / (by - ay) + ax) inside = !inside;
-                        float abx = bx - ax, aby = by - ay;
-                        float t = std::fmin(std::fmax(((lx - ax) * abx + (ly - ay) * aby) / std::fmax(abx * abx + aby * aby, 1e-20f), 0.0f), 1.0f);
-                        float ex = lx - (ax + abx * t), ey = ly - (ay + aby * t);
-                        if (ex * ex + ey * ey <= radius * radius) overlapping = true;
-                    }
-                    overlapping = overlapping || inside;
-                }
+            if (!allowed || allowed[pair]) {
+                if (j < w.n) overlapping = !is_removed(w, j) && bubble_overlaps_sensor(f, w.pPos[j], w.radius[j]);
+                else overlapping = body_overlaps_sensor(w, f, w.bodies[j - w.n]);
             }
-            uint8_t& was = state[(uint64_t)si * w.n + i];
+            uint8_t& was = state[pair];
             uint32_t kind = overlapping && !was && (sn.flags & BP_SENSOR_ENTER_EVENTS) ? 1u
                           : !overlapping && was && (sn.flags & BP_SENSOR_EXIT_EVENTS) ? 2u : 0u;
             was = overlapping ? 1 : 0;
@@ -1610,11 +1709,19 @@ static uint32_t world_sensor_events(const World<float>& w, const bp_sensor* sens
             if (events < capacity) {
                 bp_sensor_event& e = out[events];
                 e.sensor = sn.id;
-                e.object = w.id[i];
                 e.kind = kind;
-                e.point[0] = w.pPos[i].x;
-                e.point[1] = w.pPos[i].y;
-                e.reserved = 0;
+                if (j < w.n) {
+                    e.object = w.id[j];
+                    e.point[0] = w.pPos[j].x;
+                    e.point[1] = w.pPos[j].y;
+                    e.object_kind = 0;
+                } else {
+                    const Body<float>& b = w.bodies[j - w.n];
+                    e.object = b.id;
+                    e.point[0] = b.pos.x;
+                    e.point[1] = b.pos.y;
+                    e.object_kind = 1;
+                }
             }
             ++events;
         }
@@ -1706,10 +1813,10 @@ int bpo_world_hit_test(void* handle, float max_edge, float tension, float cleara
 }
 
 uint32_t bpo_world_sensor_events(void* handle, const bp_sensor* sensors, uint32_t count, const float* verts,
-                                 uint8_t* state, bp_sensor_event* out, uint32_t capacity) {
+                                 const uint8_t* allowed, uint8_t* state, bp_sensor_event* out, uint32_t capacity) {
     Handle* h = (Handle*)handle;
     if (h->precision == 64) return 0;
-    return world_sensor_events(*(World<float>*)h->world, sensors, count, verts, state, out, capacity);
+    return world_sensor_events(*(World<float>*)h->world, sensors, count, verts, allowed, state, out, capacity);
 }
 
 int bpo_set_threads(int threads) {

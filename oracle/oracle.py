@@ -50,7 +50,7 @@ def library() -> C.CDLL:
             "bpo_world_rigid_keys": (C.c_uint32, [P, P, C.c_uint32]),
             "bpo_world_contours": (C.c_int, [P, C.c_float, C.c_float, C.c_float, C.c_uint32, P, P, P, P]),
             "bpo_world_hit_test": (C.c_int, [P, C.c_float, C.c_float, C.c_float, P, C.c_uint32, P, P, P]),
-            "bpo_world_sensor_events": (C.c_uint32, [P, P, C.c_uint32, P, P, P, C.c_uint32]),
+            "bpo_world_sensor_events": (C.c_uint32, [P, P, C.c_uint32, P, P, P, P, C.c_uint32]),
             "bpo_world_read_substeps": (C.c_int, [P, P, C.c_uint32, C.POINTER(C.c_uint32)]),
             "bpo_contact_law": (C.c_int, [C.c_uint32, C.c_int, P, P, C.c_uint32]),
         }
@@ -156,14 +156,18 @@ class OracleWorld:
         assert st == 0, st
         return ids, layers, found
 
-    def sensor_events(self, sensors, vertices, state):
-        """Sensor events of the published state against `state` (uint8, sensors x bubbles, updated in place)."""
+    def sensor_events(self, sensors, vertices, state, allowed=None):
+        """Sensor events of the published state against `state` (uint8, sensors x (bubbles, then bodies), updated in
+        place); `allowed` (same shape, optional) masks pairs out."""
         arr = (N.Sensor * max(len(sensors), 1))(*sensors)
         v = np.ascontiguousarray(np.zeros((0, 2)) if vertices is None else vertices, np.float32).reshape(-1, 2)
-        cap = max(len(sensors) * self.n, 1)
+        cap = max(state.size, 1)
+        ok = None if allowed is None else np.ascontiguousarray(allowed, np.uint8)
         out = np.zeros(cap, N.SENSOR_EVENT_DTYPE)
         count = self.lib.bpo_world_sensor_events(self.handle, C.cast(arr, C.c_void_p), len(sensors),
-                                                 C.c_void_p(v.ctypes.data), C.c_void_p(state.ctypes.data),
+                                                 C.c_void_p(v.ctypes.data),
+                                                 None if ok is None else C.c_void_p(ok.ctypes.data),
+                                                 C.c_void_p(state.ctypes.data),
                                                  C.c_void_p(out.ctypes.data), cap)
         return out[:count]
 

@@ -176,3 +176,19 @@ def test_hit_test_and_contour_shapes(ctx):
     assert min(pressed) < 11.9  # the pair met and pressed in
     assert world.hit_test(free.position) == 3 and world.hit_test((320.0, 80.0)) == 1000
     assert world.hit_test((10.0, 390.0)) is None
+
+
+def test_body_sensor_events_and_object_filters(ctx):
+    from bubblephysics_gb300.world import ObjectFilter, SensorDescriptor
+    world = BubbleWorld(WorldConfiguration(REGION), ctx)
+    tx = WorldTransaction().update_physics_material("soft", PhysicsMaterial(229.0))
+    tx = tx.add(BubbleDescriptor(1, (50.0, 50.0), 8.0, 1.0, "soft"))
+    tx = tx.add(RigidBodyDescriptor(700, Circle(10.0), (100.0, 300.0), motion_role=MotionRole.KINEMATIC,
+                                    velocity=(120.0, 0.0)))
+    tx = tx.add(SensorDescriptor(80, Circle(20.0), (200.0, 300.0)))
+    tx = tx.add(SensorDescriptor(81, Circle(20.0), (200.0, 300.0), filter=ObjectFilter(frozenset({1}))))
+    world.submit(tx)
+    seen = []
+    for _ in range(100):
+        seen += [(e.kind, e.objects) for e in world.advance(1.0 / 60).events if e.kind.endswith("Sensor")]
+    assert seen == [("enteredSensor", (80, 700)), ("exitedSensor", (80, 700))]

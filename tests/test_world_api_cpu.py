@@ -129,17 +129,18 @@ def test_sensors_stage_like_objects():
 def test_sensor_records_and_carried_overlap_state():
     world = BubbleWorld(WorldConfiguration(REGION))
     state, _, _ = W.stage([(1, soft().add(W.SensorDescriptor(9, W.Polygon(((0, 0), (4, 0), (0, 4))), (1.0, 2.0), 0.5,
-                                                                 filter=W.CollisionFilter(2, 6), reports_enter=False))
+                                                                 filter=W.ObjectFilter(frozenset({20, 500})),
+                                                                 reports_enter=False))
                                .add(W.SensorDescriptor(4, Circle(7.0), (50.0, 60.0))))], W._State(), REGION)
-    world._sensor_pairs = {(4, 30), (9, 10), (9, 99)}  # 99 is no longer a bubble of the device world
-    records, verts, carried = world._sensor_records(state, [10, 20, 30])
+    world._sensor_pairs = {(4, 30), (9, 10), (9, 500), (9, 99)}  # 99 is no longer an object of the device world
+    records, verts, carried, allowed = world._sensor_records(state, [10, 20, 30, 500])  # three bubbles, one body
     assert [r.id for r in records] == [4, 9]
     assert records[0].radius == 7.0 and records[0].vertex_count == 0
     assert records[1].vertex_offset == 0 and records[1].vertex_count == 3 and records[1].angle == 0.5
-    assert (records[1].category, records[1].mask) == (2, 6)
     assert all(r.flags == N.SENSOR_ENTER_EVENTS | N.SENSOR_EXIT_EVENTS for r in records)  # filtered on the host
     assert verts.tolist() == [[0, 0], [4, 0], [0, 4]]
-    assert carried.tolist() == [0, 0, 1, 1, 0, 0]
+    assert carried.tolist() == [0, 0, 1, 0, 1, 0, 0, 1]
+    assert allowed.tolist() == [1, 1, 1, 1, 0, 1, 0, 1]
 
 
 def test_set_layer():

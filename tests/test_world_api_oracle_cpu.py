@@ -19,7 +19,8 @@ class OracleBackedWorld:
 
     def __init__(self, spec, context=None):
         self.o = OracleWorld(spec)
-        self.sensors, self.vertices, self.state = [], None, None
+        self.objects = spec.bubble_count + len(spec.bodies)
+        self.sensors, self.vertices, self.state, self.allowed = [], None, None, None
 
     def step(self, steps):
         return self.o.step(steps)
@@ -30,12 +31,12 @@ class OracleBackedWorld:
     def contacts(self):
         return self.o.contacts()
 
-    def set_sensors(self, sensors, vertices=None, state=None):
-        self.sensors, self.vertices = list(sensors), vertices
-        self.state = np.zeros(len(sensors) * self.o.n, np.uint8) if state is None else np.array(state, np.uint8)
+    def set_sensors(self, sensors, vertices=None, state=None, allowed=None):
+        self.sensors, self.vertices, self.allowed = list(sensors), vertices, allowed
+        self.state = np.zeros(len(sensors) * self.objects, np.uint8) if state is None else np.array(state, np.uint8)
 
     def sensor_events(self):
-        return self.o.sensor_events(self.sensors, self.vertices, self.state)
+        return self.o.sensor_events(self.sensors, self.vertices, self.state, self.allowed)
 
     def contours(self, max_edge, surface_tension, clearance):
         return (*self.o.contours(max_edge, surface_tension, clearance), 0.0)
@@ -133,3 +134,20 @@ def test_without_contours_a_bubble_state_is_its_circle(oracle_backed):
                  .add(BubbleDescriptor(3, (100.0, 350.0), 10.0, 1.0, "soft")))
     o = world.advance(1.0 / 60).objects[3]
     assert o.effective_radius == 10.0 and o.bounds == (90.0, 340.0, 110.0, 360.0)
+
+
+def test_bodies_and_object_filters(oracle_backed):
+    """A kinematic body crosses two sensors; the second one's object filter takes only bubble 1, so it reports nothing
+    of the body."""
+    world = BubbleWorld(WorldConfiguration(REGION))
+    tx = WorldTransaction().update_physics_material("soft", PhysicsMaterial(229.0))
+    tx = tx.add(BubbleDescriptor(1, (50.0, 50.0), 8.0, 1.0, "soft"))
+    tx = tx.add(RigidBodyDescriptor(700, Circle(10.0), (100.0, 300.0), motion_role=W.MotionRole.KINEMATIC,
+                                    velocity=(120.0, 0.0)))
+    tx = tx.add(SensorDescriptor(80, Circle(20.0), (200.0, 300.0)))
+    tx = tx.add(SensorDescriptor(81, Circle(20.0), (200.0, 300.0), filter=W.ObjectFilter(frozenset({1}))))
+    world.submit(tx)
+    seen = []
+    for _ in range(100):
+        seen += [(e.kind, e.objects) for e in world.advance(1.0 / 60).events if e.kind.endswith("Sensor")]
+    assert seen == [("enteredSensor", (80, 700)), ("exitedSensor", (80, 700))]
