@@ -197,6 +197,8 @@ template <typename T> struct World {
     int64_t limiterObject;
     uint32_t limiterTerm;
     std::vector<T> history;
+    bool traceOn = false;       // record every bubble's state after each substep (NativeMetalConfiguration.captureSubsteps)
+    std::vector<T> trace;       // per substep: h, then x, y, vx, vy per bubble
 
     // broadphase products of the last build
     T cellWidth;
@@ -1086,6 +1088,7 @@ template <typename T> int step(World<T>& w, bp_step_report& rep) {
     w.limiterObject = 0;
     w.limiterTerm = 0;
     w.history.clear();
+    w.trace.clear();
     w.overflowMax = 0;
     w.maxPerObject = 0;
     w.rebuilds = 0;
@@ -1117,6 +1120,13 @@ template <typename T> int step(World<T>& w, bp_step_report& rep) {
                     if (w.id[i] == w.injectObject) w.pos[i] = w.injectPos;
         }
         if ((w.flags & BP_WORLD_ASSERT_EVERY_SUBSTEP) && substepViolation.kind == 0) substepViolation = assert_contacts(w);
+        if (w.traceOn) {
+            w.trace.push_back(h);
+            for (uint32_t i = 0; i < n; ++i) {
+                w.trace.push_back(w.pos[i].x); w.trace.push_back(w.pos[i].y);
+                w.trace.push_back(w.vel[i].x); w.trace.push_back(w.vel[i].y);
+            }
+        }
     }
     w.overflowMax = std::max(w.overflowMax, w.overflowBuild);
     // end of step
@@ -1884,6 +1894,22 @@ int bpo_world_read_substeps(void* handle, double* out, uint32_t capacity, uint32
     auto fill = [&](auto* w) {
         for (uint32_t i = 0; i < w->history.size() && i < capacity; ++i) out[i] = (double)w->history[i];
         if (count) *count = (uint32_t)w->history.size();
+    };
+    if (h->precision == 64) fill((World<double>*)h->world); else fill((World<float>*)h->world);
+    return BP_OK;
+}
+
+// Substep trace of the last step: per substep its h, then x, y, vx, vy of every bubble.
+int bpo_world_set_trace(void* handle, int on) {
+    Handle* h = (Handle*)handle;
+    if (h->precision == 64) ((World<double>*)h->world)->traceOn = on != 0; else ((World<float>*)h->world)->traceOn = on != 0;
+    return BP_OK;
+}
+int bpo_world_read_trace(void* handle, double* out, uint32_t capacity, uint32_t* count) {
+    Handle* h = (Handle*)handle;
+    auto fill = [&](auto* w) {
+        for (uint32_t i = 0; i < w->trace.size() && i < capacity; ++i) out[i] = (double)w->trace[i];
+        if (count) *count = (uint32_t)w->trace.size();
     };
     if (h->precision == 64) fill((World<double>*)h->world); else fill((World<float>*)h->world);
     return BP_OK;

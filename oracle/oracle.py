@@ -52,6 +52,8 @@ def library() -> C.CDLL:
             "bpo_world_hit_test": (C.c_int, [P, C.c_float, C.c_float, C.c_float, P, C.c_uint32, P, P, P]),
             "bpo_world_sensor_events": (C.c_uint32, [P, P, C.c_uint32, P, P, P, P, C.c_uint32]),
             "bpo_world_read_substeps": (C.c_int, [P, P, C.c_uint32, C.POINTER(C.c_uint32)]),
+            "bpo_world_set_trace": (C.c_int, [P, C.c_int]),
+            "bpo_world_read_trace": (C.c_int, [P, P, C.c_uint32, C.POINTER(C.c_uint32)]),
             "bpo_contact_law": (C.c_int, [C.c_uint32, C.c_int, P, P, C.c_uint32]),
         }
         for name, (res, args) in sig.items():
@@ -123,6 +125,15 @@ class OracleWorld:
         count = C.c_uint32()
         self.lib.bpo_world_read_cells(self.handle, C.c_void_p(out.ctypes.data), self.n, C.byref(count))
         return out
+
+    def set_trace(self, on: bool = True):
+        """Record every bubble's state after each substep of the following steps."""
+        self.lib.bpo_world_set_trace(self.handle, 1 if on else 0)
+
+    def trace(self):
+        """The last step's substeps: h (substeps,) and the state after each, (substeps, n, 4: x, y, vx, vy)."""
+        t = self._read(self.lib.bpo_world_read_trace, np.float64).reshape(-1, 1 + 4 * self.n)
+        return t[:, 0], t[:, 1:].reshape(-1, self.n, 4)
 
     def substeps(self) -> np.ndarray:
         return self._read(self.lib.bpo_world_read_substeps, np.float64)

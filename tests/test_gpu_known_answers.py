@@ -1,0 +1,105 @@
+"""The reference's world-level known-answer scenes (ContactLawStaticsTests, SubstepCountTests, NoCrossingTests and
+ForceIntegrationTests, restated in test_world_known_answers_cpu.py) on the CUDA path: every frame's bubbles and
+substep count equal the oracle's bit for bit, and the reference's own bars hold on the GPU's numbers."""
+import math
+
+import numpy as np
+import pytest
+
+import clr
+from bubblephysics_gb300 import _native as N
+from bubblephysics_gb300.solver import World
+from bubblephysics_gb300.spec import make_bubbles
+from oracle.oracle import OracleWorld
+from test_world_known_answers_cpu import B7168, B128, K, TWO, WALL_X, push, spec_of, wall
+
+pytestmark = pytest.mark.gpu
+
+
+def twin(ctx, spec, frames, until=None):
+    """Steps the CUDA path and the oracle one frame at a time; returns the GPU's (substeps, bubbles) per frame."""
+    gpu, ref = World(spec, ctx), OracleWorld(spec, 32)
+    out = []
+    for k in range(frames):
+        s1, r1 = gpu.step(1)
+        s2, r2 = ref.step(1)
+        assert s1 == s2 == N.OK, (k, s1, s2)
+        b1, b2 = gpu.bubbles(), ref.bubbles()
+        assert r1[0]["substep_count"] == r2[0]["substep_count"], k
+        assert np.array_equal(b1["center"], b2["center"]) and np.array_equal(b1["velocity"], b2["velocity"]), k
+        out.append((int(r1[0]["substep_count"]), b1))
+        if until is not None and until(k, b1):
+            break
+    return out
+
+
+@pytest.mark.parametrize("kind,force", [(TWO, 100.0), (TWO, 20_000.0), (TWO, 100_000.0), (B7168, 1200.0)],
+                         ids=["2-100", "2-20000", "2-100000", "7168-1200"])
+def test_wall_equilibrium(ctx, kind, force):
+    r, m = kind
+    d_star = clr.equilibrium_distance(force, K, r)
+    wall_x = float(np.float32(d_star))
+    b = make_bubbles([(0.0, 0.0)], r, masses=m, stiffness=K)
+    for _, bub in twin(ctx, spec_of(b, wall(wall_x), global_force=(force, 0.0)), 600):
+        d = wall_x - float(bub["center"][0][0])
+        assert d > 0 and abs(d - d_star) <= 0.005 * d_star + 1e-3
+
+
+@pytest.mark.parametrize("pair,force", [((TWO, TWO), 10_000.0), ((TWO, B7168), 1200.0)], ids=["2-2", "2-7168"])
+def test_pair_equilibrium(ctx, pair, force):
+    (ra, ma), (rb, mb) = pair
+    d_star = (ra + rb) * (1 - clr.epsilon(force / K))
+    half = float(np.float32(d_star / 2))
+    b = make_bubbles([(-half, 0.0), (half, 0.0)], [ra, rb], masses=[ma, mb], stiffness=K)
+    spec = spec_of(b, fields=[push(0, (force, 0.0)), push(1, (-force, 0.0))], field_ids=[1, 2])
+    for _, bub in twin(ctx, spec, 600):
+        d = float(np.hypot(*(bub["center"][1].astype(np.float64) - bub["center"][0])))
+        assert abs(d - d_star) <= 0.005 * d_star + 1e-3
+
+
+def test_different_material_pair(ctx):
+    force, kb = 1200.0, K * 1000.0
+    d_star = 24.0 * (1 - clr.epsilon(force / K)) + 24.0 * (1 - clr.epsilon(force / kb))
+    half = float(np.float32(d_star / 2))
+    b = make_bubbles([(-half, 0.0), (half, 0.0)], 24.0, masses=1.0, stiffness=[K, kb])
+    frames = twin(ctx, spec_of(b, fields=[push(0, (force, 0.0)), push(1, (-force, 0.0))], field_ids=[1, 2]), 240)
+    mean = np.mean([np.hypot(*(bub["center"][1].astype(np.float64) - bub["center"][0])) for _, bub in frames])
+    f, _, _ = clr.pair_contact(48.0 - mean, 24.0, K, 24.0, kb)
+    assert abs(f - force) <= 0.01 * force
+
+
+def test_substep_counts(ctx):
+    centers = [(c * 46.0 - 69.0, r * 46.0 - 69.0) for r in range(4) for c in range(4)]
+    crowd = make_bubbles(centers, 24.0, masses=1.0, stiffness=K, damping=1.0)
+    assert all(n == 1 for n, _ in twin(ctx, spec_of(crowd), 120))
+    d_star = clr.equilibrium_distance(20_000.0, K, 24.0)
+    press = make_bubbles([(0.0, 0.0)], 24.0, masses=1.0, stiffness=K)
+    frames = twin(ctx, spec_of(press, wall(float(np.float32(d_star))), global_force=(20_000.0, 0.0)), 60)
+    assert all(2 <= n <= 4 for n, _ in frames[5:])
+    impact = make_bubbles([(WALL_X - 124.0, 0.0)], 24.0, velocities=[(1000.0, 0.0)], masses=1.0, stiffness=K)
+    ref = clr.WallScene(radius=24.0, mass=1.0, stiffness=K, damping=0.0, start_distance=124.0, velocity=-1000.0)
+    ref.run(40)
+    expected = max(f[0] for f in ref.frames)
+    peak = max(n for n, _ in twin(ctx, spec_of(impact, wall(WALL_X)), 40))
+    assert abs(peak - expected) <= 0.2 * expected
+
+
+@pytest.mark.parametrize("kind", [TWO, B128, B7168], ids=["2", "128", "7168"])
+@pytest.mark.parametrize("speed", [100.0, 3000.0])
+def test_wall_impact_rebounds_without_crossing(ctx, kind, speed):
+    r, m = kind
+    b = make_bubbles([(WALL_X - r - 100, 0.0)], r, velocities=[(speed, 0.0)], masses=m, stiffness=K)
+    spec = spec_of(b, wall(WALL_X))
+    spec.flags |= N.WORLD_ASSERT_EVERY_SUBSTEP  # a centre past the wall's edge in any substep fails the step
+    frames = twin(ctx, spec, 400, until=lambda k, bub: bub["velocity"][0][0] < 0 and bub["center"][0][0] < WALL_X - r)
+    v = frames[-1][1]["velocity"][0].astype(np.float64)
+    assert v[0] < 0 and abs(abs(v[0]) - speed) <= 0.02 * speed
+
+
+def test_pair_impact_never_touches_centres(ctx):
+    b = make_bubbles([(WALL_X - 148.0, 0.0), (WALL_X, 0.0)], [24.0, 24.0], velocities=[(3000.0, 0.0), (0.0, 0.0)],
+                     masses=1.0, stiffness=K)
+    spec = spec_of(b)
+    spec.flags |= N.WORLD_ASSERT_EVERY_SUBSTEP  # a pair at distance 0 in any substep fails the step
+    twin(ctx, spec, 200, until=lambda k, bub: k > 1 and bub["velocity"][1][0] > bub["velocity"][0][0] and
+         bub["center"][1][0] - bub["center"][0][0] > 48.0)
