@@ -103,3 +103,47 @@ def test_pair_impact_never_touches_centres(ctx):
     spec.flags |= N.WORLD_ASSERT_EVERY_SUBSTEP  # a pair at distance 0 in any substep fails the step
     twin(ctx, spec, 200, until=lambda k, bub: k > 1 and bub["velocity"][1][0] > bub["velocity"][0][0] and
          bub["center"][1][0] - bub["center"][0][0] > 48.0)
+
+
+def gpu_only(ctx, spec, frames):
+    """The CUDA path alone, one frame at a time (scenes with damping: expf may differ from the host's by an ulp)."""
+    w = World(spec, ctx)
+    out = []
+    for k in range(frames):
+        status, rep = w.step(1)
+        assert status == N.OK, (k, status)
+        out.append((int(rep[0]["substep_count"]), w.bubbles()))
+    return out
+
+
+def test_region_scenes_are_bit_exact(ctx):
+    """The region scenes of test_world_regions_and_walls_cpu.py (RegionPolicyTests) against the oracle."""
+    import test_world_regions_and_walls_cpu as R
+    wrap = R.region_bubble(9.0, 5.0, 4.0, wrap=True)
+    other = R.region_bubble(0.25, 5.0, 0.0, wrap=False)
+    other["id"] = 2
+    out = twin(ctx, R.region_spec(np.concatenate([wrap, other])), 3)[-1][1]
+    assert out["velocity"][0].tolist() == [4.0, 0.0] and abs(float(out["center"][0][0])) <= 1e-4
+    out = twin(ctx, R.region_spec(R.region_bubble(-25.0, 5.0, -4.0, wrap=True)), 1)[-1][1]
+    assert out["center"][0].tolist() == [10.0, 5.0] and out["previous_center"][0].tolist() == [11.0, 5.0]
+    twin(ctx, R.region_spec(R.region_bubble(10.8, 10.8, 0.0, wrap=True)), 2)
+    assert twin(ctx, R.region_spec(R.region_bubble(10.8, 10.8, 0.0, wrap=False)), 1)[0][1]["region_result"][0] == 1
+
+
+def test_squeeze_and_corner_hold_the_reference_bars(ctx):
+    """DeepSqueezeWallTests and CrowdCompressionTests (gamma 5) on the CUDA path: the squeezed bubble settles at the
+    law's deflection (2 %) before the wall's edge; the pushed crowd keeps every centre inside the frame."""
+    import test_world_regions_and_walls_cpu as R
+    band = N.Band()
+    band.bubble_id, band.stiffness, band.maximum_force = 1, 30.0, 20_000.0
+    band.target[:] = [-2000.0, 0.0]
+    squeeze = make_bubbles([(-136.0, 0.0)], 24.0, masses=1.44, stiffness=R.KC_SQUEEZE, damping=5.0)
+    depths = [(24.0 - (R.HALF[0] + float(b["center"][0][0]))) / 24.0
+              for _, b in gpu_only(ctx, R.crowd_spec(squeeze, bands=[band]), 360)]
+    expected = clr.epsilon(20_000.0 / R.KC_SQUEEZE)
+    assert abs(depths[-1] - expected) <= 0.02 * expected and max(depths) < 1
+    kc = float(np.float32(20.0) / np.float32(3e-4))
+    centers = [(140.0, 280.0)] + [(20.0 + (k % 4) * 45.0, 150.0 + (k // 4) * 45.0) for k in range(10)]
+    crowd = make_bubbles(centers, 20.0, masses=1.0, stiffness=kc, damping=5.0)
+    for _, bub in gpu_only(ctx, R.crowd_spec(crowd, motors=[R.motor(i, R.CORNER_FORCE) for i in range(1, 12)]), 300):
+        assert all(R.inside_frame(p) for p in bub["center"])
