@@ -147,3 +147,24 @@ def test_squeeze_and_corner_hold_the_reference_bars(ctx):
     crowd = make_bubbles(centers, 20.0, masses=1.0, stiffness=kc, damping=5.0)
     for _, bub in gpu_only(ctx, R.crowd_spec(crowd, motors=[R.motor(i, R.CORNER_FORCE) for i in range(1, 12)]), 300):
         assert all(R.inside_frame(p) for p in bub["center"])
+
+
+@pytest.mark.parametrize("pair,force,kb", [((TWO, TWO), 1200.0, K), ((TWO, B7168), 100.0, K), ((TWO, TWO), 1200.0, 2290.0)],
+                         ids=["2-2-1200", "2-7168-100", "2-2-Kb10"])
+def test_contour_chords_on_the_gpu(ctx, pair, force, kb):
+    """ContourChordTests on the CUDA path's own contours (bp_world_contours): the chords meet and sit at r (1 - eps)."""
+    from test_world_known_answers_cpu import chord
+    (ra, ma), (rb, mb) = pair
+    ea, eb = clr.epsilon(force / K), clr.epsilon(force / kb)
+    half = float(np.float32((ra * (1 - ea) + rb * (1 - eb)) / 2))
+    b = make_bubbles([(-half, 0.0), (half, 0.0)], [ra, rb], masses=[ma, mb], stiffness=[K, kb])
+    w = World(spec_of(b, fields=[push(0, (force, 0.0)), push(1, (-force, 0.0))], field_ids=[1, 2]), ctx)
+    assert w.step(60)[0] == N.OK
+    pts, counts, _, _, _ = w.contours()
+    c = w.bubbles()["center"].astype(np.float64)
+    distance = float(np.hypot(*(c[1] - c[0])))
+    normal = (c[1] - c[0]) / distance
+    ca, cb = chord(pts[0], counts[0], c[0], normal), chord(pts[1], counts[1], c[1], -normal)
+    radii = ra + rb
+    assert ra - ca > 0.05 and rb - cb > 0.05 and abs(ca + cb - distance) <= 1e-3 * radii
+    assert abs(ca - ra * (1 - ea)) <= 2e-3 * radii and abs(cb - rb * (1 - eb)) <= 2e-3 * radii

@@ -4,6 +4,7 @@
    distance of the law in every frame for 20 s; the mean deflection inverts the law across force ratios 1e-4..1e6;
    a same-material pair splits its deflection in proportion to the radii (measured on the contours); a pair of
    different stiffness carries the force of the Newton pair solution;
+ - ContourChordTests.swift:8-57 — the contours of a pressed pair meet on one flat chord, each at r (1 - eps);
  - SubstepCountTests.swift:17-121 — one substep per step where nothing needs a finer h (a crowd at rest, slow motion
    with a wall bounce, a bubble dragged by the band), about three under a static press of 20 000, and a peak during a
    1000 units/s impact within 20 % of the one-dimensional h-rule reference, back to one substep once d > 4 |v| dt;
@@ -121,21 +122,9 @@ def test_inverse_of_the_law_agrees_with_double_across_force_ratios():
 
 
 def chord(points, count, center, direction):
-    """Distance from `center` along `direction` to the contour ring (ForceScene.chord)."""
+    """The contour's farthest point toward `direction` from `center` (ForceScene.chord, ForceSceneSupport.swift:171-173)."""
     ring = points[:count].astype(np.float64)
-    best = math.inf
-    for k in range(count):
-        a, b = ring[k], ring[(k + 1) % count]
-        e = b - a
-        den = direction[0] * e[1] - direction[1] * e[0]
-        if abs(den) < 1e-12:
-            continue
-        w = a - center
-        t = (w[0] * e[1] - w[1] * e[0]) / den
-        u = (w[0] * direction[1] - w[1] * direction[0]) / den
-        if t > 0 and -1e-9 <= u <= 1 + 1e-9:
-            best = min(best, t)
-    return best
+    return float(((ring - center) @ np.asarray(direction, np.float64)).max())
 
 
 def test_same_material_pair_splits_the_deflection_in_proportion_to_the_radii():
@@ -165,6 +154,29 @@ def test_different_material_pair_force_matches_the_newton_reference(force, ratio
     mean = np.mean([np.hypot(*(bub["center"][1].astype(np.float64) - bub["center"][0])) for _, _, bub, _ in frames])
     f, _, _ = clr.pair_contact(ra + rb - mean, ra, K, rb, kb)
     assert abs(f - force) <= 0.01 * force, (f, force)
+
+
+@pytest.mark.parametrize("pair,force,kb", [((TWO, TWO), 100.0, K), ((TWO, TWO), 1200.0, K), ((TWO, B7168), 100.0, K),
+                                           ((TWO, B7168), 1200.0, K), ((TWO, TWO), 1200.0, 2290.0)],
+                         ids=["2-2-100", "2-2-1200", "2-7168-100", "2-7168-1200", "2-2-Kb10"])
+def test_contour_chords_of_a_pressed_pair_coincide(pair, force, kb):
+    """ContourChordTests.swift:8-57: after 60 frames the flat chords of both contours meet (their sum is the centre
+    distance within 1e-3 R, no interpenetration) and each lies at r (1 - eps) of the law within 2e-3 R."""
+    (ra, ma), (rb, mb) = pair
+    ea, eb = clr.epsilon(force / K), clr.epsilon(force / kb)
+    half = float(np.float32((ra * (1 - ea) + rb * (1 - eb)) / 2))
+    b = make_bubbles([(-half, 0.0), (half, 0.0)], [ra, rb], masses=[ma, mb], stiffness=[K, kb])
+    w = OracleWorld(spec_of(b, fields=[push(0, (force, 0.0)), push(1, (-force, 0.0))], field_ids=[1, 2]), 32)
+    assert w.step(60)[0] == N.OK
+    pts, counts, _, _ = w.contours()
+    c = w.bubbles()["center"].astype(np.float64)
+    distance = float(np.hypot(*(c[1] - c[0])))
+    normal = (c[1] - c[0]) / distance
+    ca, cb = chord(pts[0], counts[0], c[0], normal), chord(pts[1], counts[1], c[1], -normal)
+    radii = ra + rb
+    assert ra - ca > 0.05 and rb - cb > 0.05
+    assert ca + cb - distance <= 1e-3 * radii and abs(ca + cb - distance) <= 1e-3 * radii
+    assert abs(ca - ra * (1 - ea)) <= 2e-3 * radii and abs(cb - rb * (1 - eb)) <= 2e-3 * radii
 
 
 # ---- SubstepCountTests -----------------------------------------------------------------------------------------------
