@@ -39,13 +39,13 @@ class Bubble(C.Structure):
                 ("inverse_mass", C.c_float), ("radius", C.c_float), ("rotation", C.c_float),
                 ("angular_velocity", C.c_float), ("contact_stiffness", C.c_float), ("damping", C.c_float),
                 ("flags", C.c_uint32), ("category", C.c_uint32), ("mask", C.c_uint32),
-                ("region_result", C.c_uint32), ("layer", C.c_uint32)]
+                ("region_result", C.c_uint32), ("layer", C.c_int32)]
 
 
 class Segment(C.Structure):
     _fields_ = [("id", C.c_int64), ("owner_id", C.c_int64), ("a", f2), ("b", f2), ("previous_start", f2),
                 ("outward_sign", C.c_float), ("allowed_side", C.c_float), ("flags", C.c_uint32),
-                ("category", C.c_uint32), ("mask", C.c_uint32), ("layer", C.c_uint32)]
+                ("category", C.c_uint32), ("mask", C.c_uint32), ("layer", C.c_int32)]
 
 
 class Body(C.Structure):
@@ -54,7 +54,7 @@ class Body(C.Structure):
                 ("half_length", C.c_float), ("kind", C.c_uint32), ("flags", C.c_uint32),
                 ("vertex_offset", C.c_uint32), ("vertex_count", C.c_uint32), ("triangle_offset", C.c_uint32),
                 ("triangle_count", C.c_uint32), ("category", C.c_uint32), ("mask", C.c_uint32),
-                ("layer", C.c_uint32)]
+                ("layer", C.c_int32)]
 
 
 class ForceField(C.Structure):
@@ -171,18 +171,18 @@ BUBBLE_DTYPE = np.dtype({"names": ["id", "center", "previous_center", "velocity"
                                    "rotation", "angular_velocity", "contact_stiffness", "damping", "flags", "category",
                                    "mask", "region_result", "layer"],
                          "formats": ["<i8", ("<f4", 2), ("<f4", 2), ("<f4", 2), "<f4", "<f4", "<f4", "<f4", "<f4",
-                                     "<f4", "<f4", "<u4", "<u4", "<u4", "<u4", "<u4"],
+                                     "<f4", "<f4", "<u4", "<u4", "<u4", "<u4", "<i4"],
                          "offsets": [0, 8, 16, 24, 32, 36, 40, 44, 48, 52, 56, 60, 64, 68, 72, 76], "itemsize": 80})
 SEGMENT_DTYPE = np.dtype({"names": ["id", "owner_id", "a", "b", "previous_start", "outward_sign", "allowed_side",
                                     "flags", "category", "mask", "layer"],
                           "formats": ["<i8", "<i8", ("<f4", 2), ("<f4", 2), ("<f4", 2), "<f4", "<f4", "<u4", "<u4",
-                                      "<u4", "<u4"],
+                                      "<u4", "<i4"],
                           "offsets": [0, 8, 16, 24, 32, 40, 44, 48, 52, 56, 60], "itemsize": 64})
 BODY_DTYPE = np.dtype({"names": ["id", "position", "angle", "bounding_radius", "velocity", "angular_velocity",
                                  "core_radius", "half_length", "kind", "flags", "vertex_offset", "vertex_count",
                                  "triangle_offset", "triangle_count", "category", "mask", "layer"],
                        "formats": ["<i8", ("<f4", 2), "<f4", "<f4", ("<f4", 2), "<f4", "<f4", "<f4", "<u4", "<u4",
-                                   "<u4", "<u4", "<u4", "<u4", "<u4", "<u4", "<u4"],
+                                   "<u4", "<u4", "<u4", "<u4", "<u4", "<u4", "<i4"],
                        "offsets": [0, 8, 16, 20, 24, 32, 36, 40, 44, 48, 52, 56, 60, 64, 68, 72, 76], "itemsize": 80})
 CONTACT_DTYPE = np.dtype({"names": ["participants", "kind", "feature", "normal", "point", "impulse", "penetration",
                                     "allowed_side", "reserved"],

@@ -1012,7 +1012,7 @@ int bp_world_contours(bp_world* world, const bp_contour_config* config, float* p
 }
 
 int bp_world_hit_test(bp_world* world, const bp_contour_config* config, const float* points_xy, uint32_t count,
-                      int64_t* ids, uint32_t* layers, uint32_t* found) {
+                      int64_t* ids, int32_t* layers, uint32_t* found) {
     if (!world || !config || (count && (!points_xy || !ids || !layers || !found))) return BP_E_INVALID;
     uint32_t stride = 0;
     int st = bp_world_contours(world, config, nullptr, nullptr, nullptr, nullptr, &stride, nullptr);

@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(1024) contour_kernel(DState S, DWorld W, Conto
 // Hit test of query points (nativeHitTest, NativeGeometryKernels:501-541): among the bubbles whose contour contains the
 // point (bounds first, then the even-odd rule over the contour, the reference's crossing formula), the bodies that
 // contain it, and the static polygons that contain it (their one-sided edges, consecutive per owner), the highest
-// (layer, id as an unsigned 64-bit value) wins.
+// (layer as a signed 32-bit value, then id as an unsigned 64-bit value) wins.
 __global__ void hit_test_kernel(DState S, DWorld W, const float2* queries, uint32_t queryCount, const float2* cpoints,
                                 const uint32_t* ccounts, const float* shape, uint32_t stride,
                                 const uint32_t* bubbleLayers, const uint32_t* segLayers, const uint32_t* bodyLayers,
@@ -179,9 +179,10 @@ __global__ void hit_test_kernel(DState S, DWorld W, const float2* queries, uint3
     bool any = false;
     uint32_t bestLayer = 0;
     unsigned long long bestId = 0;
-    auto offer = [&](uint32_t layer, long long id) {
+    auto offer = [&](uint32_t bits, long long id) {  // layers order like Int32 (NativeMetalHitTestTests.swift:123-132)
+        const int32_t layer = (int32_t)bits, best = (int32_t)bestLayer;
         const unsigned long long u = (unsigned long long)id;
-        if (!any || layer > bestLayer || (layer == bestLayer && u > bestId)) { any = true; bestLayer = layer; bestId = u; }
+        if (!any || layer > best || (layer == best && u > bestId)) { any = true; bestLayer = bits; bestId = u; }
     };
     for (uint32_t i = 0; i < W.n; ++i) {
         const uint32_t g = W.boff + i;

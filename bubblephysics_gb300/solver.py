@@ -151,7 +151,7 @@ class World:
         """Hit test of query points on the published state (bp_world_hit_test): ids, layers, found."""
         q = np.ascontiguousarray(points, np.float32).reshape(-1, 2)
         ids = np.zeros(q.shape[0], np.int64)
-        layers = np.zeros(q.shape[0], np.uint32)
+        layers = np.zeros(q.shape[0], np.int32)
         found = np.zeros(q.shape[0], np.uint32)
         cfg = N.ContourConfig(max_edge, surface_tension, clearance, 0)
         N.check(self.lib.bp_world_hit_test(self.handle, C.byref(cfg), C.c_void_p(q.ctypes.data), q.shape[0],

@@ -459,7 +459,7 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
         return None, touched
     if kind == "setLayer":
         oid, layer = args
-        if not (0 <= layer < 2 ** 32) and (oid in state.bubbles or oid in state.bodies):
+        if not (-2 ** 31 <= layer < 2 ** 31) and (oid in state.bubbles or oid in state.bodies):  # Int32
             return TransactionRejectionReason.INVALID_VALUE, touched
         if oid in state.bubbles:
             state.bubbles[oid].desc = replace(state.bubbles[oid].desc, layer=layer)

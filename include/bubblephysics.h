@@ -80,7 +80,7 @@ typedef struct bp_bubble {
     uint32_t category;           /* collision filter category bits */
     uint32_t mask;               /* collision filter mask bits */
     uint32_t region_result;      /* out: 0 unchanged, 1 removed by the region, 2 wrapped (publicFlags.w) */
-    uint32_t layer;              /* drawing layer (setLayer): a hit test answers with the highest layer */
+    int32_t layer;               /* drawing layer (setLayer, Int32): a hit test answers with the highest layer */
 } bp_bubble;
 
 /* Segment flags (NativeMetalSegment.flags, NativeMetalBufferLayout.swift:63-79). */
@@ -105,7 +105,7 @@ typedef struct bp_segment {
     uint32_t flags;              /* BP_SEGMENT_* */
     uint32_t category;
     uint32_t mask;
-    uint32_t layer;              /* drawing layer of the owner polygon (a hit test answers with the highest layer) */
+    int32_t layer;               /* drawing layer of the owner polygon (a hit test answers with the highest layer) */
 } bp_segment;
 
 enum { BP_BODY_POLYGON = 0u, BP_BODY_CIRCLE = 1u, BP_BODY_CAPSULE = 2u };
@@ -133,7 +133,7 @@ typedef struct bp_body {
     uint32_t triangle_count;
     uint32_t category;
     uint32_t mask;
-    uint32_t layer;              /* drawing layer (setLayer): a hit test answers with the highest layer */
+    int32_t layer;               /* drawing layer (setLayer, Int32): a hit test answers with the highest layer */
 } bp_body;
 
 /* Force field (NativeForceField, NativeForceKernels:11-17). 64 bytes. */
@@ -374,7 +374,7 @@ int bp_world_contours(bp_world* world, const bp_contour_config* config, float* p
  * unsigned 64-bit value. Per query: ids[q] (a bubble or body id, or a polygon's owner id), layers[q], found[q] (0 for
  * empty space). */
 int bp_world_hit_test(bp_world* world, const bp_contour_config* config, const float* points_xy, uint32_t count,
-                      int64_t* ids, uint32_t* layers, uint32_t* found);
+                      int64_t* ids, int32_t* layers, uint32_t* found);
 
 /* ---- sensors (enter / exit events of bubbles) ------------------------------------------------------------------ */
 

@@ -1528,7 +1528,7 @@ static void world_contours(const World<float>& w, float maxEdge, float tension, 
 
 // Hit test (nativeHitTest, NativeGeometryKernels:501-541) over the contours of world_contours, the bodies at their
 // end-of-step pose and the static polygons (even-odd over each owner's consecutive polygon edges): the highest
-// (layer, id as uint64) wins.
+// (layer as int32, then id as uint64) wins.
 static void world_hit_test(const World<float>& w, float maxEdge, float tension, float clearance, const float* queries,
                            uint32_t count, int64_t* ids, uint32_t* layers, uint32_t* found) {
     uint32_t stride = 64;
@@ -1541,9 +1541,10 @@ static void world_hit_test(const World<float>& w, float maxEdge, float tension, 
         bool any = false;
         uint32_t bestLayer = 0;
         uint64_t bestId = 0;
-        auto offer = [&](uint32_t layer, int64_t id) {
+        auto offer = [&](uint32_t bits, int64_t id) {  // layers order like Int32
+            const int32_t layer = (int32_t)bits, best = (int32_t)bestLayer;
             uint64_t u = (uint64_t)id;
-            if (!any || layer > bestLayer || (layer == bestLayer && u > bestId)) { any = true; bestLayer = layer; bestId = u; }
+            if (!any || layer > best || (layer == best && u > bestId)) { any = true; bestLayer = bits; bestId = u; }
         };
         for (uint32_t i = 0; i < w.n; ++i) {
             if (is_removed(w, i)) continue;

@@ -159,7 +159,7 @@ class OracleWorld:
         """Hit test of query points (the CUDA path's rule restated in float): ids, layers, found."""
         q = np.ascontiguousarray(points, np.float32).reshape(-1, 2)
         ids = np.zeros(q.shape[0], np.int64)
-        layers = np.zeros(q.shape[0], np.uint32)
+        layers = np.zeros(q.shape[0], np.int32)
         found = np.zeros(q.shape[0], np.uint32)
         st = self.lib.bpo_world_hit_test(self.handle, max_edge, surface_tension, clearance, C.c_void_p(q.ctypes.data),
                                          q.shape[0], C.c_void_p(ids.ctypes.data), C.c_void_p(layers.ctypes.data),

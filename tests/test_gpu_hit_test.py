@@ -68,3 +68,11 @@ def test_batched_world_with_bodies_and_polygons(ctx):
     queries = np.concatenate([rng.uniform(lo, hi, (3000, 2)), spec.bodies["position"].astype(np.float64)])
     g, _ = check(spec, ctx, 4, queries)
     assert len(spec.bodies) > 0 and set(spec.bodies["id"].tolist()) & set(g[0].tolist())  # body centres hit bodies
+
+
+@pytest.mark.parametrize("name", sorted(__import__("test_hit_test_cpu").HIT_CASES))
+def test_reference_hit_test_cases_on_the_gpu(ctx, name):
+    from test_hit_test_cpu import HIT_CASES, answers
+    build, points, expected = HIT_CASES[name]
+    spec = build()
+    assert answers(spec, points, World(spec, ctx)) == expected

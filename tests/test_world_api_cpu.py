@@ -148,7 +148,8 @@ def test_set_layer():
                           W._State(), REGION)
     layered, rec, _ = W.stage([(2, WorldTransaction().set_layer(1, 7))], state, REGION)
     assert rec and layered.bubbles[1].desc.layer == 7 and state.bubbles[1].desc.layer == 0
-    for tx, reason in ((WorldTransaction().set_layer(1, -1), R.INVALID_VALUE),
+    assert W.stage([(3, WorldTransaction().set_layer(1, -5))], state, REGION)[0].bubbles[1].desc.layer == -5  # Int32
+    for tx, reason in ((WorldTransaction().set_layer(1, 2 ** 31), R.INVALID_VALUE),
                        (WorldTransaction().set_layer(5, 1), R.INCOMPATIBLE_OBJECT_KIND),
                        (WorldTransaction().set_layer(8, 1), R.OBJECT_NOT_FOUND)):
         _, rec, ev = W.stage([(3, tx)], state, REGION)
