@@ -22,6 +22,7 @@ steps on the GPU (World, bp_world_step); there is no CPU fallback.
 from __future__ import annotations
 
 import math
+import sys
 from dataclasses import dataclass, field, replace
 from enum import Enum
 
@@ -224,10 +225,20 @@ class WorldFailureReason(Enum):
     COMMAND_EXECUTION_FAILED = "commandExecutionFailed"
 
 
+class AdvanceIssue(str, Enum):
+    """Why an advance published nothing new (WorldAdvanceIssue of the reference)."""
+    WORLD_FAILED = "worldFailed"
+    INVALID_TIME_DELTA = "invalidTimeDelta"
+    TIME_ACCUMULATOR_OVERFLOW = "timeAccumulatorOverflow"
+    STEP_FAILED = "stepFailed"
+
+
 @dataclass
 class WorldDiagnostics:
     backlog_seconds: float = 0.0
     discarded_backlog_seconds: float = 0.0
+    consecutive_backlogged_advances: int = 0
+    last_advance_issue: AdvanceIssue | None = None
     steps_in_last_advance: int = 0
     pending_transaction_count: int = 0
     is_paused: bool = False
@@ -555,6 +566,75 @@ def contact_transitions(contacts: np.ndarray, segment_owner: dict, interested: s
 
 
 # ---------------------------------------------------------------------------------------------------------------------
+# Fixed-step clock
+# ---------------------------------------------------------------------------------------------------------------------
+class FixedStepDriver:
+    """The world's time accumulator (FixedStepDriver.swift): time leaves the backlog only when a whole step completes;
+    the backlog is capped at max(maximum_backlog, step) with the excess summed (saturating at the largest float); an
+    invalid or overflowing increment leaves everything unchanged; after discard_next_advance() the next increment is
+    dropped (time spent in the background is not game time)."""
+
+    def __init__(self, fixed_time_step: float, maximum_steps_per_advance: int = 8, maximum_backlog: float = math.inf):
+        if not (math.isfinite(fixed_time_step) and fixed_time_step > 0) or maximum_steps_per_advance <= 0 or \
+                not maximum_backlog > 0:
+            raise ValueError("fixed_time_step and maximum_backlog must be positive, maximum_steps_per_advance >= 1")
+        self.fixed_time_step = float(fixed_time_step)
+        self.maximum_steps_per_advance = int(maximum_steps_per_advance)
+        self.maximum_backlog = max(float(maximum_backlog), self.fixed_time_step)
+        self.backlog_seconds = 0.0
+        self.simulation_time = 0.0
+        self.completed_steps = 0
+        self.consecutive_backlogged_advances = 0
+        self.discarded_backlog_seconds = 0.0
+        self._discard_next = False
+
+    @property
+    def can_step(self) -> bool:
+        # a fraction of a step covers the rounding of many subtractions; none for a subnormal step
+        step = self.fixed_time_step
+        tolerance = 0.0 if step < sys.float_info.min else step * 1e-12
+        return self.backlog_seconds >= step or (self.backlog_seconds > 0 and step - self.backlog_seconds <= tolerance)
+
+    def accumulate(self, seconds: float) -> bool:
+        if not (math.isfinite(seconds) and seconds >= 0):
+            return False
+        if self._discard_next:
+            self._discard_next = False
+            return True
+        accumulated = self.backlog_seconds + seconds
+        if not (math.isfinite(accumulated) and math.isfinite(self.simulation_time + accumulated)):
+            return False
+        if accumulated > self.maximum_backlog:
+            total = self.discarded_backlog_seconds + (accumulated - self.maximum_backlog)
+            self.discarded_backlog_seconds = total if math.isfinite(total) else sys.float_info.max
+            self.backlog_seconds = self.maximum_backlog
+        else:
+            self.backlog_seconds = accumulated
+        return True
+
+    @property
+    def interpolation_fraction(self) -> float:
+        return min(max(self.backlog_seconds / self.fixed_time_step, 0.0), 1.0)
+
+    @property
+    def interpolation_fraction_after_next_step(self) -> float:
+        return min(max((self.backlog_seconds - self.fixed_time_step) / self.fixed_time_step, 0.0), 1.0)
+
+    def discard_next_advance(self):
+        self._discard_next = True
+
+    def complete_step(self):
+        if not self.can_step:
+            raise RuntimeError("no whole step in the backlog")
+        self.backlog_seconds = max(0.0, self.backlog_seconds - self.fixed_time_step)
+        self.simulation_time += self.fixed_time_step
+        self.completed_steps += 1
+
+    def finish_advance(self):
+        self.consecutive_backlogged_advances = self.consecutive_backlogged_advances + 1 if self.can_step else 0
+
+
+# ---------------------------------------------------------------------------------------------------------------------
 # BubbleWorld
 # ---------------------------------------------------------------------------------------------------------------------
 class BubbleWorld:
@@ -566,10 +646,8 @@ class BubbleWorld:
         self._state = _State(global_force=tuple(configuration.global_force))
         self._pending: list = []
         self._next_token = 1
-        self._backlog = 0.0
-        self._discarded = 0.0
-        self._completed = 0
-        self._time = 0.0
+        self._clock = FixedStepDriver(configuration.fixed_time_step, configuration.maximum_steps_per_advance,
+                                      configuration.maximum_backlog)
         self._paused = False
         self._frame = WorldFrame()
         self._native: World | None = None
@@ -597,6 +675,10 @@ class BubbleWorld:
         self._paused = False
         self.diagnostics.is_paused = False
 
+    def return_from_background(self):
+        """The host came back from the background: the next time increment is dropped (BubbleWorld.swift:114-120)."""
+        self._clock.discard_next_advance()
+
     @property
     def last_frame(self) -> WorldFrame:
         return self._frame
@@ -604,28 +686,33 @@ class BubbleWorld:
     def advance(self, seconds: float) -> WorldFrame:
         """Runs the fixed-step clock: at most maximum_steps_per_advance steps; a call without a completed step (or
         after a failure) returns the last complete frame."""
-        d = self.diagnostics
+        d, clock = self.diagnostics, self._clock
         d.steps_in_last_advance = 0
-        if d.failure_reason is not None or not (math.isfinite(seconds) and seconds >= 0) or self._paused:
+        d.last_advance_issue = None
+        if d.failure_reason is not None:  # the final state wins over pause and step
+            d.last_advance_issue = AdvanceIssue.WORLD_FAILED
             return self._frame
-        dt = self.configuration.fixed_time_step
-        backlog = self._backlog + seconds
-        if backlog > max(self.configuration.maximum_backlog, dt):
-            self._discarded += backlog - max(self.configuration.maximum_backlog, dt)
-            backlog = max(self.configuration.maximum_backlog, dt)
-        self._backlog = backlog
+        if not (math.isfinite(seconds) and seconds >= 0):
+            d.last_advance_issue = AdvanceIssue.INVALID_TIME_DELTA
+            return self._frame
+        if self._paused:
+            return self._frame
+        if not clock.accumulate(seconds):
+            d.last_advance_issue = AdvanceIssue.TIME_ACCUMULATOR_OVERFLOW
+            return self._frame
         receipts, events = [], []
-        while d.steps_in_last_advance < self.configuration.maximum_steps_per_advance and self._can_step():
-            ok = self._step(receipts, events)
-            if not ok:
+        while d.steps_in_last_advance < clock.maximum_steps_per_advance and clock.can_step:
+            if not self._step(receipts, events):
+                d.last_advance_issue = AdvanceIssue.STEP_FAILED
                 break
-            self._backlog = max(0.0, self._backlog - dt)
-            self._completed += 1
-            self._time += dt
+            clock.complete_step()
             d.steps_in_last_advance += 1
-            self._frame = WorldFrame(self._completed, self._time, tuple(receipts), tuple(events), self._objects())
-        d.backlog_seconds = self._backlog
-        d.discarded_backlog_seconds = self._discarded
+            self._frame = WorldFrame(clock.completed_steps, clock.simulation_time, tuple(receipts), tuple(events),
+                                     self._objects())
+        clock.finish_advance()
+        d.backlog_seconds = clock.backlog_seconds
+        d.discarded_backlog_seconds = clock.discarded_backlog_seconds
+        d.consecutive_backlogged_advances = clock.consecutive_backlogged_advances
         d.pending_transaction_count = len(self._pending)
         return self._frame
 
@@ -645,10 +732,6 @@ class BubbleWorld:
             self._native = None
 
     # -- internals -----------------------------------------------------------------------------------------------------
-    def _can_step(self) -> bool:
-        dt = self.configuration.fixed_time_step
-        return self._backlog >= dt or (self._backlog > 0 and dt - self._backlog <= dt * 1e-12)
-
     def _spec(self, state: _State) -> tuple[WorldSpec, list, dict]:
         cfg = self.configuration
         ids = sorted(state.bubbles)
