@@ -560,6 +560,8 @@ def contact_transitions(contacts: np.ndarray, segment_owner: dict, interested: s
                                  impulse))
     current = set(sums)
     for key in sorted(history, key=order):
+        if key[0] in removed and key[1] in removed:
+            continue  # nobody is left to tell (EventCompactorTests.swift:81-86)
         if key not in current or key[0] in removed or key[1] in removed:
             events.append(WorldEvent("contactEnded", key))
     return events, current - {k for k in current if k[0] in removed or k[1] in removed}

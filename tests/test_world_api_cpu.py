@@ -109,6 +109,25 @@ def test_contact_pairs_order_by_unsigned_ids():
     assert [e.objects for e in events] == [(1, 2), (2, -1)]
 
 
+def test_event_compactor_cases_of_the_reference():
+    """EventCompactorTests.swift:50-99: events sorted by pair; a begin for a pair already in the history is skipped;
+    a removed object ends its contacts for the remaining partner only; a contact between two removed objects gives no
+    event and leaves the history; an end for a removed object is not duplicated."""
+    hit = lambda a, b: (a, b, 0, 0.5, 2.0, (1.0, 0.0), (1.0, 0.0))
+    everyone = {1, 2, 3, 4}
+    events, history = W.contact_transitions(contacts(hit(3, 4), hit(1, 2)), {}, everyone, set(), 1.0, set())
+    assert [(e.kind, e.objects) for e in events] == [("contactBegan", (1, 2)), ("contactBegan", (3, 4))]
+    assert history == {(1, 2), (3, 4)}
+    events, history = W.contact_transitions(contacts(hit(1, 2)), {}, everyone, {(1, 2)}, 1.0, set())
+    assert events == [] and history == {(1, 2)}
+    events, history = W.contact_transitions(contacts(hit(3, 4)), {}, everyone, {(1, 2), (3, 4)}, 1.0, {2})
+    assert [(e.kind, e.objects) for e in events] == [("contactEnded", (1, 2))] and history == {(3, 4)}
+    events, history = W.contact_transitions(contacts(), {}, everyone, {(2, 3)}, 1.0, {2, 3})
+    assert events == [] and history == set()
+    events, history = W.contact_transitions(contacts(), {}, everyone, {(1, 2)}, 1.0, {2})
+    assert [(e.kind, e.objects) for e in events] == [("contactEnded", (1, 2))] and history == set()
+
+
 def test_sensors_stage_like_objects():
     sensor = W.SensorDescriptor(50, Circle(20.0), (100.0, 100.0))
     state, receipts, _ = W.stage([(1, soft().add(sensor).add(bubble(1, 100, 100)))], W._State(), REGION)
