@@ -329,38 +329,98 @@ def _finite(*values) -> bool:
     return all(math.isfinite(float(v)) for v in values)
 
 
-def _inside_body(body: _Body, point) -> bool:
-    d = np.asarray(point, np.float64) - body.position
-    c, s = math.cos(-body.angle), math.sin(-body.angle)
-    local = np.array([d[0] * c - d[1] * s, d[0] * s + d[1] * c])
+class PlacementIssue(str, Enum):
+    """Why a bubble's centre cannot stand at a point (PlacementIssue of the reference), in the order they are checked."""
+    OUTSIDE_REGION = "outsideRegion"
+    INSIDE_RIGID_BODY = "insideRigidBody"
+    COINCIDENT_CENTER = "coincidentCenter"
+
+
+_F = np.float32
+POSITION_TOLERANCE = _F(1e-4)  # PlacementGeometry.positionTolerance
+
+
+def _body_shape(body: _Body):
+    """The body's shape in the world at its pose, in float: ("circle", c, r), ("capsule", a, b, r) or ("polygon", ring)."""
+    c, s = _F(math.cos(body.angle)), _F(math.sin(body.angle))
+    px, py = _F(body.position[0]), _F(body.position[1])
+
+    def world(x, y):
+        x, y = _F(x), _F(y)
+        return np.array([px + x * c - y * s, py + x * s + y * c], np.float32)
     shape = body.desc.shape
     if isinstance(shape, Circle):
-        return float(np.hypot(*local)) <= shape.radius
+        return ("circle", np.array([px, py], np.float32), _F(shape.radius))
     if isinstance(shape, Capsule):
-        x = min(max(local[0], -shape.half_length), shape.half_length)
-        return float(np.hypot(local[0] - x, local[1])) <= shape.radius
-    pts = np.asarray(shape.points, np.float64)
-    edges = np.roll(pts, -1, axis=0) - pts
-    cross = edges[:, 0] * (local[1] - pts[:, 1]) - edges[:, 1] * (local[0] - pts[:, 0])
-    return bool(np.all(cross >= 0) or np.all(cross <= 0))
+        return ("capsule", world(-shape.half_length, 0.0), world(shape.half_length, 0.0), _F(shape.radius))
+    return ("polygon", [world(x, y) for x, y in shape.points])
 
 
-def _validate_bubble(desc: BubbleDescriptor, state: _State, region) -> TransactionRejectionReason | None:
+def _distance_to_segment(p, a, b):
+    e = b - a
+    sq = _F(e[0] * e[0] + e[1] * e[1])
+    t = max(_F(0), min(_F(1), _F((p[0] - a[0]) * e[0] + (p[1] - a[1]) * e[1]) / sq)) if sq > 0 else _F(0)
+    d = p - (a + e * t)
+    return _F(math.sqrt(float(d[0] * d[0] + d[1] * d[1])))
+
+
+def _contains_including_boundary(shape, p) -> bool:
+    """Point-in-shape with the boundary inside (PlacementGeometry.containsIncludingBoundary): circles and capsules by
+    distance (<=), polygons by an exact on-edge test, then the crossing parity."""
+    if shape[0] == "circle":
+        d = p - shape[1]
+        return bool(d[0] * d[0] + d[1] * d[1] <= shape[2] * shape[2])
+    if shape[0] == "capsule":
+        return bool(_distance_to_segment(p, shape[1], shape[2]) <= shape[3])
+    ring = shape[1]
+    j = len(ring) - 1
+    for i in range(len(ring)):
+        a, b = ring[i], ring[j]
+        j = i
+        cross = (b[0] - a[0]) * (p[1] - a[1]) - (b[1] - a[1]) * (p[0] - a[0])
+        if cross == 0 and min(a[0], b[0]) <= p[0] <= max(a[0], b[0]) and min(a[1], b[1]) <= p[1] <= max(a[1], b[1]):
+            return True
+    inside = False
+    j = len(ring) - 1
+    for i in range(len(ring)):
+        a, b = ring[i], ring[j]
+        if (a[1] > p[1]) != (b[1] > p[1]) and p[0] <= (b[0] - a[0]) * (p[1] - a[1]) / (b[1] - a[1]) + a[0]:
+            inside = not inside
+        j = i
+    return inside
+
+
+def placement_issue(point, radius: float, filt: CollisionFilter, state: _State, region,
+                    excluding=frozenset()) -> PlacementIssue | None:
+    """The first reason a bubble's centre cannot stand at `point` (PlacementGeometry.issue): outside the region
+    (whatever its exit policy), inside a body it collides with (boundary included), or within the coincident-centre
+    tolerance max(1e-4 min(r, r_other), 1e-4) of a bubble it collides with. Excluded ids take no part."""
+    p = np.asarray(point, np.float32)
+    if not (region[0] <= p[0] <= region[2] and region[1] <= p[1] <= region[3]):
+        return PlacementIssue.OUTSIDE_REGION
+    for oid, body in state.bodies.items():
+        if oid not in excluding and filt.accepts(body.desc.filter) and _contains_including_boundary(_body_shape(body), p):
+            return PlacementIssue.INSIDE_RIGID_BODY
+    for oid, other in state.bubbles.items():
+        if oid in excluding or not filt.accepts(other.desc.filter):
+            continue
+        tolerance = max(_F(1e-4) * min(_F(radius), _F(other.desc.radius)), POSITION_TOLERANCE)
+        d = p - np.asarray(other.position, np.float32)
+        if _F(math.sqrt(float(d[0] * d[0] + d[1] * d[1]))) < tolerance:
+            return PlacementIssue.COINCIDENT_CENTER
+    return None
+
+
+def _validate_bubble(desc: BubbleDescriptor, state: _State, region):
     if desc.physics_material_id not in state.materials:
         return TransactionRejectionReason.PHYSICS_MATERIAL_NOT_FOUND
     if not (_finite(*desc.position, *desc.velocity, desc.radius, desc.mass) and desc.radius > 0 and desc.mass > 0):
         return TransactionRejectionReason.INVALID_VALUE
     if desc.motion_role == MotionRole.KINEMATIC:
         return TransactionRejectionReason.INVALID_VALUE
-    x, y = desc.position
-    if not (region[0] <= x <= region[2] and region[1] <= y <= region[3]):
-        return TransactionRejectionReason.INVALID_PLACEMENT
-    for body in state.bodies.values():
-        if desc.filter.accepts(body.desc.filter) and _inside_body(body, desc.position):
-            return TransactionRejectionReason.INVALID_PLACEMENT
-    for other in state.bubbles.values():
-        if other.desc.id != desc.id and float(np.hypot(*(other.position - np.asarray(desc.position)))) <= 1e-4:
-            return TransactionRejectionReason.INVALID_PLACEMENT
+    issue = placement_issue(desc.position, desc.radius, desc.filter, state, region, frozenset({desc.id}))
+    if issue is not None:
+        return TransactionRejectionReason.INVALID_PLACEMENT, (desc.id, issue)
     return None
 
 
@@ -379,10 +439,14 @@ def _validate_body(desc: RigidBodyDescriptor, state: _State) -> TransactionRejec
         return TransactionRejectionReason.INVALID_VALUE
     if not _finite(*desc.position, desc.angle, *desc.velocity, desc.angular_velocity):
         return TransactionRejectionReason.INVALID_VALUE
-    probe = _Body(desc, np.asarray(desc.position, np.float64), float(desc.angle))
-    for b in state.bubbles.values():
-        if b.desc.filter.accepts(desc.filter) and _inside_body(probe, b.position):
-            return TransactionRejectionReason.INVALID_PLACEMENT
+    # a body may not cover the centre of a bubble it collides with; the smallest such id is named
+    # (PlacementGeometry.bubbleInside)
+    shape = _body_shape(_Body(desc, np.asarray(desc.position, np.float64), float(desc.angle)))
+    inside = [oid for oid, b in state.bubbles.items()
+              if b.desc.filter.accepts(desc.filter) and _contains_including_boundary(shape, np.asarray(b.position, np.float32))]
+    if inside:
+        return TransactionRejectionReason.INVALID_PLACEMENT, (min(inside, key=lambda v: v & 0xFFFFFFFFFFFFFFFF),
+                                                             PlacementIssue.INSIDE_RIGID_BODY)
     return None
 
 
@@ -505,7 +569,10 @@ def stage(pending: list, state: _State, region) -> tuple[_State, list, list]:
         for index, op in enumerate(tx.operations):
             reason, touched = _apply(op, trial, region)
             if reason is not None:
-                rejection = TransactionRejection(index, reason, op[0])
+                detail = op[0]
+                if isinstance(reason, tuple):  # a placement: (object id, PlacementIssue)
+                    reason, detail = reason
+                rejection = TransactionRejection(index, reason, detail)
                 break
             created += touched["created"]
             removed += touched["removed"]
