@@ -29,6 +29,7 @@ from enum import Enum
 import numpy as np
 
 from . import _native as N
+from .queries import QueryIndex, RaycastHit
 from .solver import Context, World, default_context, static_polygon_edges
 from .spec import WorldSpec
 
@@ -634,6 +635,18 @@ def contact_transitions(contacts: np.ndarray, segment_owner: dict, interested: s
     return events, current - {k for k in current if k[0] in removed or k[1] in removed}
 
 
+def query_index(state: _State, effective_radii: dict | None = None) -> QueryIndex:
+    """The spatial query index of a state (QueryIndex(state:)): bubbles as circles of their effective radius (the
+    target radius when none is given), bodies with their exact world shapes; sensors take no part."""
+    objects = []
+    for oid, b in state.bubbles.items():
+        r = (effective_radii or {}).get(oid, b.desc.radius)
+        objects.append((oid, b.desc.filter, ("circle", np.asarray(b.position, np.float32), np.float32(max(r, 0.0)))))
+    for oid, body in state.bodies.items():
+        objects.append((oid, body.desc.filter, _body_shape(body)))
+    return QueryIndex(objects)
+
+
 # ---------------------------------------------------------------------------------------------------------------------
 # Fixed-step clock
 # ---------------------------------------------------------------------------------------------------------------------
@@ -721,10 +734,13 @@ class BubbleWorld:
         self._frame = WorldFrame()
         self._native: World | None = None
         self._native_ids: list = []
+        self._native_order: list = []
         self._segment_owner: dict = {}
         self._history: set = set()
         self._sensor_pairs: set = set()   # (sensor id, bubble id) pairs overlapping after the last step
         self._shapes: dict = {}           # bubble id -> (effective radius, bounds) of the last contours
+        self._index: QueryIndex | None = None  # built at the first query after a publication
+        self.query_index_build_count = 0
         self.diagnostics = WorldDiagnostics()
 
     # -- public API ----------------------------------------------------------------------------------------------------
@@ -778,6 +794,7 @@ class BubbleWorld:
             d.steps_in_last_advance += 1
             self._frame = WorldFrame(clock.completed_steps, clock.simulation_time, tuple(receipts), tuple(events),
                                      self._objects())
+            self._index = None
         clock.finish_advance()
         d.backlog_seconds = clock.backlog_seconds
         d.discarded_backlog_seconds = clock.discarded_backlog_seconds
@@ -794,6 +811,37 @@ class BubbleWorld:
         ids, _, found = self._native.hit_test([point], cfg.max_contour_segment_length, cfg.contour_surface_tension,
                                               cfg.position_tolerance)
         return int(ids[0]) if found[0] else None
+
+    # -- queries on the published state (BubbleWorld.objects(at:), objects(in:), objects(inCircle:), raycast) -------
+    def _query_index(self) -> QueryIndex:
+        if self._index is None:
+            self._index = query_index(self._state, {oid: shape[0] for oid, shape in self._shapes.items()})
+            self.query_index_build_count += 1
+        return self._index
+
+    def objects_at(self, point, filter: CollisionFilter | None = None) -> list:
+        """Bubbles (circles of their effective radius) and bodies containing `point`, ascending by id."""
+        return self._query_index().objects_at(point, filter)
+
+    def objects_in(self, rectangle, filter: CollisionFilter | None = None) -> list:
+        """Objects intersecting the rectangle (min x, min y, max x, max y), ascending by id."""
+        return self._query_index().objects_in_rect(rectangle[:2], rectangle[2:], filter)
+
+    def objects_in_circle(self, center, radius: float, filter: CollisionFilter | None = None) -> list:
+        return self._query_index().objects_in_circle(center, radius, filter)
+
+    def raycast(self, start, end, filter: CollisionFilter | None = None) -> RaycastHit | None:
+        return self._query_index().raycast(start, end, filter)
+
+    def debug_contour_snapshot(self) -> dict:
+        """Every bubble's published contour (BubbleWorld.debugContourSnapshot), read from the device."""
+        if self._native is None:
+            return {}
+        cfg = self.configuration
+        points, counts, _, _, _ = self._native.contours(cfg.max_contour_segment_length, cfg.contour_surface_tension,
+                                                         cfg.position_tolerance)
+        return {oid: [tuple(map(float, p)) for p in points[i, :counts[i]]] for i, oid in enumerate(self._native_order)
+                if oid in self._state.bubbles}
 
     def close(self):
         if self._native is not None:
@@ -901,6 +949,7 @@ class BubbleWorld:
                 self._ctx = default_context()
             self._native = World(spec, self._ctx) if len(ids) else None
             self._native_ids = ids
+            self._native_order = ids  # the device world's bubble order (kept when a removal forces a rebuild)
             self._segment_owner = owners
             if self._native is not None and staged.sensors:
                 records, verts, carried, allowed = self._sensor_records(staged, ids + [int(v) for v in spec.bodies["id"]])
