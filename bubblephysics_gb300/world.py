@@ -23,6 +23,7 @@ from __future__ import annotations
 
 import math
 import sys
+import weakref
 from dataclasses import dataclass, field, replace
 from enum import Enum
 
@@ -149,6 +150,7 @@ class WorldConfiguration:
     candidate_limit: int = 128
     substep_split_multiplier: float = 1.0    # NativeMetalConfiguration.substepSplitMultiplier
     contours: bool = True                    # publish the contours' effective radius and bounds with each bubble
+    automatic_pause: bool = True             # WorldConfiguration.automaticPause: pause in the background
     max_contour_segment_length: float = 8.0  # ReferenceConfiguration.maxContourSegmentLength
     contour_surface_tension: float = 20.0    # ReferenceConfiguration.contourSurfaceTension
     position_tolerance: float = 1e-4         # ReferenceConfiguration.positionTolerance (contour clearance)
@@ -722,7 +724,9 @@ class FixedStepDriver:
 class BubbleWorld:
     """Sole owner of a world and its transaction queue; publishes only completed steps."""
 
-    def __init__(self, configuration: WorldConfiguration, context: Context | None = None):
+    def __init__(self, configuration: WorldConfiguration, context: Context | None = None, lifecycle=None):
+        """`lifecycle` (optional, LifecycleEventSource of the reference) gets two callables, will_enter_background and
+        did_become_active, that hold the world weakly; a host may also call enter_background() / become_active()."""
         self.configuration = configuration
         self._ctx = context
         self._state = _State(global_force=tuple(configuration.global_force))
@@ -730,7 +734,8 @@ class BubbleWorld:
         self._next_token = 1
         self._clock = FixedStepDriver(configuration.fixed_time_step, configuration.maximum_steps_per_advance,
                                       configuration.maximum_backlog)
-        self._paused = False
+        self._manually_paused = False
+        self._paused_in_background = False
         self._frame = WorldFrame()
         self._native: World | None = None
         self._native_ids: list = []
@@ -742,6 +747,10 @@ class BubbleWorld:
         self._index: QueryIndex | None = None  # built at the first query after a publication
         self.query_index_build_count = 0
         self.diagnostics = WorldDiagnostics()
+        if lifecycle is not None and configuration.automatic_pause:
+            ref = weakref.ref(self)
+            lifecycle.will_enter_background = lambda: (w := ref()) and w.enter_background()
+            lifecycle.did_become_active = lambda: (w := ref()) and w.become_active()
 
     # -- public API ----------------------------------------------------------------------------------------------------
     def submit(self, transaction: WorldTransaction) -> int:
@@ -752,17 +761,31 @@ class BubbleWorld:
         self.diagnostics.pending_transaction_count = len(self._pending)
         return token
 
+    @property
+    def _paused(self) -> bool:
+        return self._manually_paused or self._paused_in_background
+
     def pause(self):
-        self._paused = True
-        self.diagnostics.is_paused = True
+        self._manually_paused = True
+        self.diagnostics.is_paused = self._paused
 
     def resume(self):
-        self._paused = False
-        self.diagnostics.is_paused = False
+        self._manually_paused = False
+        self.diagnostics.is_paused = self._paused
 
-    def return_from_background(self):
-        """The host came back from the background: the next time increment is dropped (BubbleWorld.swift:114-120)."""
-        self._clock.discard_next_advance()
+    def enter_background(self):
+        """The host goes to the background: with automatic_pause the world pauses (BubbleWorld.swift:113-120)."""
+        if self.configuration.automatic_pause:
+            self._paused_in_background = True
+            self.diagnostics.is_paused = True
+
+    def become_active(self):
+        """The host is active again: a background pause lifts and the next time increment is dropped (time spent in the
+        background is not game time); a manual pause stays."""
+        if self.configuration.automatic_pause and self._paused_in_background:
+            self._paused_in_background = False
+            self._clock.discard_next_advance()
+            self.diagnostics.is_paused = self._paused
 
     @property
     def last_frame(self) -> WorldFrame:

@@ -130,6 +130,7 @@ def test_world_reports_advance_issues():
     assert w.diagnostics.last_advance_issue == AdvanceIssue.INVALID_TIME_DELTA
     w.advance(1.0 / 60)
     assert w.diagnostics.last_advance_issue is None and w.last_frame.step_index == 1
-    w.return_from_background()
+    w.enter_background()
+    w.become_active()
     w.advance(10.0)  # the time spent away is dropped
     assert w.last_frame.step_index == 1 and w.diagnostics.backlog_seconds == pytest.approx(0.0, abs=1e-12)
