@@ -67,6 +67,13 @@ class MotionRole(Enum):
     DYNAMIC = "dynamic"
     STATIC = "static"
     KINEMATIC = "kinematic"
+    MOTOR_DRIVEN = "motorDriven"
+    PLAYER_DRIVEN = "playerDriven"
+    PATH_DRIVEN = "pathDriven"
+
+
+# Roles that move a body under forces (the rigid solver's bodies): the reference refuses them next to bubbles
+DYNAMIC_ROLES = (MotionRole.DYNAMIC, MotionRole.MOTOR_DRIVEN, MotionRole.PLAYER_DRIVEN, MotionRole.PATH_DRIVEN)
 
 
 class RegionExitPolicy(Enum):
@@ -171,6 +178,9 @@ class TransactionRejectionReason(Enum):
     INVALID_VALUE = "invalidValue"
     INVALID_PLACEMENT = "invalidPlacement"
     UNSUPPORTED_OPERATION = "unsupportedOperation"
+    UNSUPPORTED_MOTION_ROLE = "unsupportedMotionRole"        # detail: (object id, role)
+    INCOMPATIBLE_MOTION_ROLE = "incompatibleMotionRole"      # detail: object id
+    UNSUPPORTED_BUBBLE_WITH_DYNAMIC_RIGID_BODY = "unsupportedBubbleWithDynamicRigidBody"
 
 
 @dataclass(frozen=True)
@@ -419,8 +429,9 @@ def _validate_bubble(desc: BubbleDescriptor, state: _State, region):
         return TransactionRejectionReason.PHYSICS_MATERIAL_NOT_FOUND
     if not (_finite(*desc.position, *desc.velocity, desc.radius, desc.mass) and desc.radius > 0 and desc.mass > 0):
         return TransactionRejectionReason.INVALID_VALUE
-    if desc.motion_role == MotionRole.KINEMATIC:
-        return TransactionRejectionReason.INVALID_VALUE
+    if desc.motion_role not in (MotionRole.DYNAMIC, MotionRole.STATIC):
+        # kinematic bubbles do not exist; motor, player and path drives of bubbles are not built here
+        return TransactionRejectionReason.UNSUPPORTED_MOTION_ROLE, (desc.id, desc.motion_role)
     issue = placement_issue(desc.position, desc.radius, desc.filter, state, region, frozenset({desc.id}))
     if issue is not None:
         return TransactionRejectionReason.INVALID_PLACEMENT, (desc.id, issue)
@@ -428,8 +439,6 @@ def _validate_bubble(desc: BubbleDescriptor, state: _State, region):
 
 
 def _validate_body(desc: RigidBodyDescriptor, state: _State) -> TransactionRejectionReason | None:
-    if desc.motion_role not in (MotionRole.STATIC, MotionRole.KINEMATIC):
-        return TransactionRejectionReason.UNSUPPORTED_OPERATION  # bubbles meet only static and kinematic bodies
     shape = desc.shape
     sizes = {Circle: lambda s: (s.radius,), Capsule: lambda s: (s.half_length, s.radius)}.get(type(shape))
     if sizes is not None:
@@ -511,10 +520,16 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
         oid, role = args
         b = state.bubbles.get(oid)
         if b is None:
-            return TransactionRejectionReason.OBJECT_NOT_FOUND if oid not in state.bodies else \
-                TransactionRejectionReason.INCOMPATIBLE_OBJECT_KIND, touched
+            body = state.bodies.get(oid)
+            if body is None:
+                return TransactionRejectionReason.OBJECT_NOT_FOUND, touched
+            if role != MotionRole.KINEMATIC:  # leaving the kinematic role discards the drive
+                body.desc = replace(body.desc, motion_role=role, velocity=(0.0, 0.0), angular_velocity=0.0)
+            else:
+                body.desc = replace(body.desc, motion_role=role)
+            return None, touched
         if role not in (MotionRole.DYNAMIC, MotionRole.STATIC):
-            return TransactionRejectionReason.INVALID_VALUE, touched
+            return (TransactionRejectionReason.UNSUPPORTED_MOTION_ROLE, (oid, role)), touched
         b.desc = replace(b.desc, motion_role=role)
         if role == MotionRole.STATIC:
             b.velocity[:] = 0
@@ -550,10 +565,11 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
     if kind == "setKinematicDrive":
         oid, velocity, omega = args
         body = state.bodies.get(oid)
-        if body is None:
-            return TransactionRejectionReason.OBJECT_NOT_FOUND if oid not in state.bubbles else \
-                TransactionRejectionReason.INCOMPATIBLE_OBJECT_KIND, touched
-        if body.desc.motion_role != MotionRole.KINEMATIC or not _finite(*velocity, omega):
+        if body is None and oid not in state.bubbles:
+            return TransactionRejectionReason.OBJECT_NOT_FOUND, touched
+        if body is None or body.desc.motion_role != MotionRole.KINEMATIC:
+            return (TransactionRejectionReason.INCOMPATIBLE_MOTION_ROLE, oid), touched
+        if not _finite(*velocity, omega):
             return TransactionRejectionReason.INVALID_VALUE, touched
         body.desc = replace(body.desc, velocity=velocity, angular_velocity=omega)
         return None, touched
@@ -580,6 +596,12 @@ def stage(pending: list, state: _State, region) -> tuple[_State, list, list]:
             created += touched["created"]
             removed += touched["removed"]
             replaced_ids += touched["replaced"]
+        if rejection is None and tx.operations and any(b.desc.motion_role in DYNAMIC_ROLES for b in trial.bodies.values()):
+            # judged on the state after the whole transaction, reported at its last operation
+            # (NativeCompleteStepper.validate; the rigid solver for worlds of dynamic bodies alone is not built here)
+            reason = TransactionRejectionReason.UNSUPPORTED_BUBBLE_WITH_DYNAMIC_RIGID_BODY if trial.bubbles else \
+                TransactionRejectionReason.UNSUPPORTED_OPERATION
+            rejection = TransactionRejection(len(tx.operations) - 1, reason, "validate")
         if rejection is not None:
             events.append(WorldEvent("transactionRejected", token=token, rejection=rejection))
             continue
