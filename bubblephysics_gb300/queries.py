@@ -64,7 +64,8 @@ def contains(shape, p) -> bool:
     return polygon_contains(shape[1], p)
 
 
-def _box(shape):
+def shape_box(shape):
+    """The axis-aligned box (low, high) of a shape."""
     if shape[0] == "circle":
         r = shape[2]
         return shape[1] - r, shape[1] + r
@@ -218,7 +219,7 @@ class QueryIndex:
     def __init__(self, objects):
         built = []
         for oid, filt, shape in objects:
-            lo, hi = _box(shape)
+            lo, hi = shape_box(shape)
             built.append((int(oid), filt, shape, lo, hi))
         built.sort(key=lambda e: e[0] & 0xFFFFFFFFFFFFFFFF)
         self.entries = built

@@ -30,7 +30,7 @@ from enum import Enum
 import numpy as np
 
 from . import _native as N
-from .queries import QueryIndex, RaycastHit
+from .queries import QueryIndex, RaycastHit, shape_box
 from .solver import Context, World, default_context, static_polygon_edges
 from .spec import WorldSpec
 
@@ -1022,11 +1022,6 @@ class BubbleWorld:
                     ev.append(WorldEvent("didWrap", (oid,)))
             for oid in removed_now:
                 staged.bubbles.pop(oid)
-            dt = np.float32(cfg.fixed_time_step)
-            for body in staged.bodies.values():  # kinematic advance, the same float arithmetic as the device
-                if body.desc.motion_role == MotionRole.KINEMATIC:
-                    body.position = (body.position + np.asarray(body.desc.velocity, np.float32) * dt).astype(np.float32)
-                    body.angle = float(np.float32(body.angle) + np.float32(body.desc.angular_velocity) * dt)
             self.diagnostics.contact_candidate_overflow += int(rep["candidate_overflow"])
             self.diagnostics.maximum_contact_candidates_per_object = int(rep["max_candidates_per_object"])
             if staged.sensors:
@@ -1045,6 +1040,11 @@ class BubbleWorld:
                 _, _, _, shape, _ = self._native.contours(cfg.max_contour_segment_length, cfg.contour_surface_tension,
                                                           cfg.position_tolerance)
                 self._shapes = {oid: (float(shape[i][1]), tuple(map(float, shape[i][2:6]))) for i, oid in enumerate(ids)}
+        dt = np.float32(cfg.fixed_time_step)
+        for body in staged.bodies.values():  # kinematic advance (with or without bubbles), the device's float arithmetic
+            if body.desc.motion_role == MotionRole.KINEMATIC:
+                body.position = (body.position + np.asarray(body.desc.velocity, np.float32) * dt).astype(np.float32)
+                body.angle = float(np.float32(body.angle) + np.float32(body.desc.angular_velocity) * dt)
         interested = {i for i, b in staged.bubbles.items() if EventInterest.CONTACT in b.desc.event_interest}
         interested |= {i for i, b in staged.bodies.items() if EventInterest.CONTACT in b.desc.event_interest}
         gone = removed_now | {i for r in rec for i in r.removed_object_ids + r.replaced_object_ids}
@@ -1107,11 +1107,9 @@ class BubbleWorld:
         for oid, body in self._state.bodies.items():
             shape = body.desc.shape
             kind = {Circle: "circle", Capsule: "capsule", Polygon: "polygon"}[type(shape)]
-            reach = shape.radius if isinstance(shape, Circle) else shape.half_length + shape.radius \
-                if isinstance(shape, Capsule) else float(np.sqrt((np.asarray(shape.points) ** 2).sum(1)).max())
+            lo, hi = shape_box(_body_shape(body))  # the box of the shape at its pose: it follows the rotation
             vel = body.desc.velocity if body.desc.motion_role == MotionRole.KINEMATIC else (0.0, 0.0)
             out[oid] = ObjectState(kind, tuple(map(float, body.position)), tuple(map(float, vel)), body.angle,
                                    body.desc.angular_velocity if body.desc.motion_role == MotionRole.KINEMATIC else 0.0,
-                                   (float(body.position[0]) - reach, float(body.position[1]) - reach,
-                                    float(body.position[0]) + reach, float(body.position[1]) + reach))
+                                   (float(lo[0]), float(lo[1]), float(hi[0]), float(hi[1])))
         return out

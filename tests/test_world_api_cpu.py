@@ -173,3 +173,32 @@ def test_set_layer():
                        (WorldTransaction().set_layer(8, 1), R.OBJECT_NOT_FOUND)):
         _, rec, ev = W.stage([(3, tx)], state, REGION)
         assert rec == [] and ev[0].rejection.reason == reason
+
+
+def test_object_states_of_bodies_follow_their_shape_and_rotation():
+    """ObjectStateTests.swift:42-145: a static square's bounds are its own box (92 / 198 for half 8 at (100, 190));
+    a square turned by pi/4 reaches 10 sqrt(2); a kinematic body moves and turns with its drive, also in a world
+    without bubbles."""
+    import math as _m
+    from bubblephysics_gb300.world import Polygon
+    w = BubbleWorld(WorldConfiguration((0.0, 0.0, 400.0, 400.0)))
+    sq = lambda h: Polygon(((-h, -h), (h, -h), (h, h), (-h, h)))
+    w.submit(WorldTransaction().add(RigidBodyDescriptor(4, sq(8.0), (100.0, 190.0)))
+             .add(RigidBodyDescriptor(7, sq(10.0), (100.0, 100.0), angle=_m.pi / 4))
+             .add(RigidBodyDescriptor(3, sq(10.0), (100.0, 150.0), motion_role=MotionRole.KINEMATIC,
+                                      velocity=(0.0, -5.0), angular_velocity=1.0)))
+    for _ in range(30):
+        frame = w.advance(1.0 / 60)
+    assert frame.step_index == 30
+    wall = frame.objects[4]
+    assert wall.position == (100.0, 190.0) and wall.bounds[0] == pytest.approx(92, abs=1e-3)
+    assert wall.bounds[3] == pytest.approx(198, abs=1e-3)
+    turned = frame.objects[7]
+    assert turned.bounds[0] == pytest.approx(100 - 10 * _m.sqrt(2), abs=1e-3)
+    assert turned.bounds[3] == pytest.approx(100 + 10 * _m.sqrt(2), abs=1e-3)
+    spinning = frame.objects[3]
+    assert spinning.kind == "polygon" and spinning.rotation != 0 and spinning.angular_velocity != 0
+    assert spinning.position[1] < 150.0
+    for state in frame.objects.values():
+        lo, hi = state.bounds[:2], state.bounds[2:]
+        assert lo[0] < hi[0] and lo[1] < hi[1] and lo[0] <= state.position[0] <= hi[0]
