@@ -98,6 +98,41 @@ class BubbleDescriptor:
     filter: CollisionFilter = CollisionFilter()
     event_interest: frozenset = frozenset()
     layer: int = 0
+    drive_policy: "BubbleDrivePolicy | None" = None
+
+
+@dataclass(frozen=True)
+class BubbleDrivePolicy:
+    """How a bubble can be grabbed by the band (BubbleDrivePolicy): F = K_band (target - x), its magnitude clamped to
+    maximum_force (None: no limit)."""
+    band_stiffness: float
+    maximum_force: float | None = None
+
+
+@dataclass(frozen=True)
+class MotorDrive:
+    """A constant force and torque on a motor-driven bubble (MotorDrive)."""
+    force: tuple = (0.0, 0.0)
+    torque: float = 0.0
+
+
+@dataclass(frozen=True)
+class DriveBlockingContact:
+    object_id: int
+    point: tuple
+    normal: tuple        # from the obstacle to the driven bubble
+
+
+@dataclass(frozen=True)
+class DriveFeedback:
+    """The running result of a player drive (DriveFeedback): its target, where the bubble got, and the first contact
+    standing against the drive."""
+    object_id: int
+    player_drive_id: int | None
+    target: tuple
+    achieved_point: tuple
+    blocking_contact: DriveBlockingContact | None = None
+    is_stopped: bool = False
 
 
 @dataclass(frozen=True)
@@ -180,6 +215,8 @@ class TransactionRejectionReason(Enum):
     UNSUPPORTED_OPERATION = "unsupportedOperation"
     UNSUPPORTED_MOTION_ROLE = "unsupportedMotionRole"        # detail: (object id, role)
     INCOMPATIBLE_MOTION_ROLE = "incompatibleMotionRole"      # detail: object id
+    DRIVE_ALREADY_ACTIVE = "driveAlreadyActive"              # detail: object id
+    DRIVE_NOT_ACTIVE = "driveNotActive"                      # detail: object id
     UNSUPPORTED_BUBBLE_WITH_DYNAMIC_RIGID_BODY = "unsupportedBubbleWithDynamicRigidBody"
 
 
@@ -229,6 +266,7 @@ class WorldFrame:
     transaction_receipts: tuple = ()
     events: tuple = ()
     objects: dict = field(default_factory=dict)
+    drive_feedback: tuple = ()                   # DriveFeedback of every active player drive, ascending by id
 
 
 class WorldFailureReason(Enum):
@@ -292,6 +330,18 @@ class WorldTransaction:
     def apply_impulse(self, object_id: int, impulse) -> "WorldTransaction":
         return self._with("applyImpulse", object_id, tuple(float(v) for v in impulse))
 
+    def set_motor_drive(self, object_id: int, drive: "MotorDrive") -> "WorldTransaction":
+        return self._with("setMotorDrive", object_id, drive)
+
+    def begin_player_drive(self, object_id: int, target) -> "WorldTransaction":
+        return self._with("beginPlayerDrive", object_id, tuple(float(v) for v in target))
+
+    def update_player_drive(self, object_id: int, target) -> "WorldTransaction":
+        return self._with("updatePlayerDrive", object_id, tuple(float(v) for v in target))
+
+    def end_player_drive(self, object_id: int) -> "WorldTransaction":
+        return self._with("endPlayerDrive", object_id)
+
     def set_layer(self, object_id: int, layer: int) -> "WorldTransaction":
         return self._with("setLayer", object_id, int(layer))
 
@@ -314,6 +364,10 @@ class _Bubble:
     velocity: np.ndarray
     rotation: float = 0.0
     angular_velocity: float = 0.0
+    motor: MotorDrive | None = None            # motor-driven
+    drive_target: tuple | None = None          # player-driven: the band's target
+    drive_id: int | None = None
+    motion_before_drive: "MotionRole | None" = None
 
 
 @dataclass
@@ -330,12 +384,14 @@ class _State:
     bodies: dict = field(default_factory=dict)    # id -> _Body
     global_force: tuple = (0.0, 0.0)
     sensors: dict = field(default_factory=dict)   # id -> SensorDescriptor
+    fixed_time_step: float = 1.0 / 60.0          # for the band's stability bound
+    next_drive_id: int = 1
 
     def copy(self) -> "_State":
         return _State(dict(self.materials),
                       {k: replace(v, position=v.position.copy(), velocity=v.velocity.copy()) for k, v in self.bubbles.items()},
                       {k: replace(v, position=v.position.copy()) for k, v in self.bodies.items()},
-                      self.global_force, dict(self.sensors))
+                      self.global_force, dict(self.sensors), self.fixed_time_step, self.next_drive_id)
 
 
 def _finite(*values) -> bool:
@@ -351,6 +407,7 @@ class PlacementIssue(str, Enum):
 
 _F = np.float32
 POSITION_TOLERANCE = _F(1e-4)  # PlacementGeometry.positionTolerance
+MAXIMUM_DRIVE_MAGNITUDE = 1e6   # TransactionStager.maximumDriveMagnitude: larger finite drives overflow float in a step
 
 
 def _body_shape(body: _Body):
@@ -429,9 +486,19 @@ def _validate_bubble(desc: BubbleDescriptor, state: _State, region):
         return TransactionRejectionReason.PHYSICS_MATERIAL_NOT_FOUND
     if not (_finite(*desc.position, *desc.velocity, desc.radius, desc.mass) and desc.radius > 0 and desc.mass > 0):
         return TransactionRejectionReason.INVALID_VALUE
-    if desc.motion_role not in (MotionRole.DYNAMIC, MotionRole.STATIC):
-        # kinematic bubbles do not exist; motor, player and path drives of bubbles are not built here
+    if desc.motion_role not in (MotionRole.DYNAMIC, MotionRole.STATIC, MotionRole.MOTOR_DRIVEN):
+        # kinematic bubbles do not exist; a player drive starts with begin_player_drive; path drives are not built here
         return TransactionRejectionReason.UNSUPPORTED_MOTION_ROLE, (desc.id, desc.motion_role)
+    policy = desc.drive_policy
+    if policy is not None:
+        if not (_finite(policy.band_stiffness) and policy.band_stiffness > 0):
+            return TransactionRejectionReason.INVALID_VALUE, "drive.bandStiffness"
+        if policy.maximum_force is not None and not (_finite(policy.maximum_force) and policy.maximum_force > 0):
+            return TransactionRejectionReason.INVALID_VALUE, "drive.maximumForce"
+        # the band stays stable while omega_band dt <= 1/4: K_band <= m / (16 dt^2), in the world's float step
+        step = float(np.float32(state.fixed_time_step))
+        if not float(np.float32(policy.band_stiffness)) * 16 * step * step <= float(np.float32(desc.mass)):
+            return TransactionRejectionReason.INVALID_VALUE, "drive.bandStiffness"
     issue = placement_issue(desc.position, desc.radius, desc.filter, state, region, frozenset({desc.id}))
     if issue is not None:
         return TransactionRejectionReason.INVALID_PLACEMENT, (desc.id, issue)
@@ -528,9 +595,12 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
             else:
                 body.desc = replace(body.desc, motion_role=role)
             return None, touched
-        if role not in (MotionRole.DYNAMIC, MotionRole.STATIC):
+        if role not in (MotionRole.DYNAMIC, MotionRole.STATIC, MotionRole.MOTOR_DRIVEN):
             return (TransactionRejectionReason.UNSUPPORTED_MOTION_ROLE, (oid, role)), touched
         b.desc = replace(b.desc, motion_role=role)
+        if role != MotionRole.MOTOR_DRIVEN:
+            b.motor = None
+        b.drive_target = b.drive_id = b.motion_before_drive = None
         if role == MotionRole.STATIC:
             b.velocity[:] = 0
         return None, touched
@@ -561,6 +631,56 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
         else:
             return TransactionRejectionReason.OBJECT_NOT_FOUND if oid not in state.sensors else \
                 TransactionRejectionReason.INCOMPATIBLE_OBJECT_KIND, touched
+        return None, touched
+    if kind == "setMotorDrive":
+        oid, drive = args
+        values = (*drive.force, drive.torque)
+        if not _finite(*values):
+            return TransactionRejectionReason.INVALID_VALUE, touched
+        if any(abs(v) > MAXIMUM_DRIVE_MAGNITUDE for v in values):
+            return (TransactionRejectionReason.INVALID_VALUE, "motor.force" if max(map(abs, drive.force)) >
+                    MAXIMUM_DRIVE_MAGNITUDE else "motor.torque"), touched
+        b = state.bubbles.get(oid)
+        if b is None:
+            return (TransactionRejectionReason.OBJECT_NOT_FOUND if oid not in state.bodies else
+                    (TransactionRejectionReason.UNSUPPORTED_MOTION_ROLE, (oid, MotionRole.MOTOR_DRIVEN))), touched
+        b.desc = replace(b.desc, motion_role=MotionRole.MOTOR_DRIVEN)
+        b.drive_target = b.drive_id = b.motion_before_drive = None
+        b.motor = drive
+        return None, touched
+    if kind in ("beginPlayerDrive", "updatePlayerDrive"):
+        oid, target = args
+        if not _finite(*target):
+            return TransactionRejectionReason.INVALID_VALUE, touched
+        b = state.bubbles.get(oid)
+        if b is None:
+            return TransactionRejectionReason.OBJECT_NOT_FOUND if oid not in state.bodies else \
+                (TransactionRejectionReason.INCOMPATIBLE_OBJECT_KIND, oid), touched
+        if kind == "beginPlayerDrive" and b.desc.drive_policy is None:
+            return (TransactionRejectionReason.INCOMPATIBLE_OBJECT_KIND, oid), touched
+        if b.desc.drive_policy is not None and any(abs(v) > MAXIMUM_DRIVE_MAGNITUDE for v in target):
+            return (TransactionRejectionReason.INVALID_VALUE, "playerDrive.target"), touched
+        if kind == "beginPlayerDrive":
+            if b.drive_target is not None:
+                return (TransactionRejectionReason.DRIVE_ALREADY_ACTIVE, oid), touched
+            b.motion_before_drive = b.desc.motion_role
+            b.desc = replace(b.desc, motion_role=MotionRole.PLAYER_DRIVEN)
+            b.drive_id = state.next_drive_id
+            state.next_drive_id += 1
+        elif b.drive_target is None:
+            return (TransactionRejectionReason.DRIVE_NOT_ACTIVE, oid), touched
+        b.drive_target = tuple(float(v) for v in target)
+        return None, touched
+    if kind == "endPlayerDrive":
+        oid = args[0]
+        b = state.bubbles.get(oid)
+        if b is None:
+            return TransactionRejectionReason.OBJECT_NOT_FOUND if oid not in state.bodies else \
+                (TransactionRejectionReason.DRIVE_NOT_ACTIVE, oid), touched
+        if b.drive_target is None:
+            return (TransactionRejectionReason.DRIVE_NOT_ACTIVE, oid), touched
+        b.desc = replace(b.desc, motion_role=b.motion_before_drive or MotionRole.DYNAMIC)
+        b.drive_target = b.drive_id = b.motion_before_drive = None
         return None, touched
     if kind == "setKinematicDrive":
         oid, velocity, omega = args
@@ -751,7 +871,8 @@ class BubbleWorld:
         did_become_active, that hold the world weakly; a host may also call enter_background() / become_active()."""
         self.configuration = configuration
         self._ctx = context
-        self._state = _State(global_force=tuple(configuration.global_force))
+        self._state = _State(global_force=tuple(configuration.global_force),
+                             fixed_time_step=configuration.fixed_time_step)
         self._pending: list = []
         self._next_token = 1
         self._clock = FixedStepDriver(configuration.fixed_time_step, configuration.maximum_steps_per_advance,
@@ -767,6 +888,7 @@ class BubbleWorld:
         self._sensor_pairs: set = set()   # (sensor id, bubble id) pairs overlapping after the last step
         self._shapes: dict = {}           # bubble id -> (effective radius, bounds) of the last contours
         self._index: QueryIndex | None = None  # built at the first query after a publication
+        self._feedback: tuple = ()
         self.query_index_build_count = 0
         self.diagnostics = WorldDiagnostics()
         if lifecycle is not None and configuration.automatic_pause:
@@ -838,7 +960,7 @@ class BubbleWorld:
             clock.complete_step()
             d.steps_in_last_advance += 1
             self._frame = WorldFrame(clock.completed_steps, clock.simulation_time, tuple(receipts), tuple(events),
-                                     self._objects())
+                                     self._objects(), self._feedback)
             self._index = None
         clock.finish_advance()
         d.backlog_seconds = clock.backlog_seconds
@@ -898,6 +1020,7 @@ class BubbleWorld:
         cfg = self.configuration
         ids = sorted(state.bubbles)
         b = np.zeros(len(ids), N.BUBBLE_DTYPE)
+        bands, motors = [], []
         for i, oid in enumerate(ids):
             bub = state.bubbles[oid]
             d = bub.desc
@@ -916,6 +1039,18 @@ class BubbleWorld:
             b[i]["damping"] = mat.damping
             b[i]["flags"] = N.BUBBLE_ENABLED | (N.BUBBLE_STATIC if static else N.BUBBLE_FORCE_DRIVEN) | \
                 (N.BUBBLE_WRAP if d.region_exit_policy == RegionExitPolicy.WRAP else 0)
+            if d.motion_role == MotionRole.PLAYER_DRIVEN and bub.drive_target is not None:
+                band = N.Band()
+                band.bubble_id, band.stiffness = oid, d.drive_policy.band_stiffness
+                band.maximum_force = d.drive_policy.maximum_force or 0.0  # 0: no limit
+                band.target[:] = list(bub.drive_target)
+                bands.append(band)
+            if d.motion_role == MotionRole.MOTOR_DRIVEN and bub.motor is not None:
+                motor = N.Motor()
+                motor.bubble_id, motor.torque = oid, bub.motor.torque
+                motor.force[:] = [float(v) for v in bub.motor.force]
+                motor.inertia = float(np.float32(0.5) * np.float32(d.mass) * np.float32(d.radius) * np.float32(d.radius))
+                motors.append(motor)
             b[i]["category"] = d.filter.category
             b[i]["mask"] = d.filter.mask
             b[i]["layer"] = d.layer
@@ -970,7 +1105,8 @@ class BubbleWorld:
                          body_triangles=np.concatenate(tris) if tris else np.zeros((0, 3), np.uint32),
                          region=tuple(cfg.simulation_region), global_force=tuple(state.global_force),
                          gravity=tuple(cfg.gravity), time_step=cfg.fixed_time_step,
-                         candidate_limit=cfg.candidate_limit, substep_split_multiplier=cfg.substep_split_multiplier)
+                         candidate_limit=cfg.candidate_limit, substep_split_multiplier=cfg.substep_split_multiplier,
+                         bands=bands, motors=motors)
         return spec, ids, owners
 
     def _step(self, receipts: list, events: list) -> bool:
@@ -1050,6 +1186,7 @@ class BubbleWorld:
         gone = removed_now | {i for r in rec for i in r.removed_object_ids + r.replaced_object_ids}
         contact_events, self._history = contact_transitions(contacts, self._segment_owner, interested, self._history,
                                                             cfg.fixed_time_step, gone)
+        self._feedback = self._drive_feedback(staged, contacts)
         self._state = staged
         del self._pending[:taken]
         receipts += rec
@@ -1057,6 +1194,33 @@ class BubbleWorld:
         if removed_now and self._native is not None:
             self._native_ids = None  # the removed slots leave the device world at the next step
         return True
+
+    def _drive_feedback(self, state: _State, contacts) -> tuple:
+        """DriveFeedback of every active player drive after a step (MotionControllers.feedback): the target, the
+        bubble's position, and its first contact whose normal (from the obstacle to the bubble) stands against the
+        drive."""
+        out = []
+        for oid in sorted(state.bubbles, key=lambda v: v & 0xFFFFFFFFFFFFFFFF):
+            b = state.bubbles[oid]
+            if b.desc.motion_role != MotionRole.PLAYER_DRIVEN or b.drive_target is None:
+                continue
+            delta = np.asarray(b.drive_target, np.float32) - b.position
+            blocker = None
+            for c in contacts:
+                a, other, kind = int(c["participants"][0]), int(c["participants"][1]), int(c["kind"])
+                if a == oid:
+                    # pair normals run from the first participant to the second, segment normals from the wall out
+                    normal = -c["normal"] if kind == 0 else c["normal"]
+                    obstacle = other if kind == 0 else self._segment_owner.get(other, other)
+                elif kind == 0 and other == oid:
+                    normal, obstacle = c["normal"], a
+                else:
+                    continue
+                if float(delta[0] * normal[0] + delta[1] * normal[1]) < -1e-4:
+                    blocker = DriveBlockingContact(obstacle, tuple(map(float, c["point"])), tuple(map(float, normal)))
+                    break
+            out.append(DriveFeedback(oid, b.drive_id, b.drive_target, tuple(map(float, b.position)), blocker))
+        return tuple(out)
 
     def _sensor_records(self, state: _State, objects: list):
         """Device records of the sensors (id order), their polygon vertices, and per (sensor, object) pair the overlap
