@@ -83,6 +83,7 @@ class RegionExitPolicy(Enum):
 
 class EventInterest(Enum):
     CONTACT = "contact"
+    DRIVE_BLOCKED = "driveBlocked"
 
 
 @dataclass(frozen=True)
@@ -249,7 +250,8 @@ class ObjectState:
 @dataclass(frozen=True)
 class WorldEvent:
     """kind: transactionRejected, didAdd, didRemove, didReplace, didExitSimulationRegion, didWrap, contactBegan,
-    contactEnded, enteredSensor, exitedSensor (objects = (sensor, bubble or body))."""
+    contactEnded, enteredSensor, exitedSensor (objects = (sensor, bubble or body)), driveBlocked (objects = (bubble,
+    obstacle))."""
     kind: str
     objects: tuple = ()
     point: tuple | None = None
@@ -889,6 +891,7 @@ class BubbleWorld:
         self._shapes: dict = {}           # bubble id -> (effective radius, bounds) of the last contours
         self._index: QueryIndex | None = None  # built at the first query after a publication
         self._feedback: tuple = ()
+        self._blockers: dict = {}          # driven bubble id -> the obstacle that blocked it in the last step
         self.query_index_build_count = 0
         self.diagnostics = WorldDiagnostics()
         if lifecycle is not None and configuration.automatic_pause:
@@ -1187,6 +1190,16 @@ class BubbleWorld:
         contact_events, self._history = contact_transitions(contacts, self._segment_owner, interested, self._history,
                                                             cfg.fixed_time_step, gone)
         self._feedback = self._drive_feedback(staged, contacts)
+        blockers = {}
+        for fb in self._feedback:  # driveBlocked when the blocker of an interested bubble changes (EventCompactor.finish)
+            bub = staged.bubbles.get(fb.object_id)
+            if fb.blocking_contact is None or bub is None or EventInterest.DRIVE_BLOCKED not in bub.desc.event_interest:
+                continue
+            blockers[fb.object_id] = fb.blocking_contact.object_id
+            if self._blockers.get(fb.object_id) != fb.blocking_contact.object_id:
+                ev.append(WorldEvent("driveBlocked", (fb.object_id, fb.blocking_contact.object_id),
+                                     fb.blocking_contact.point))
+        self._blockers = blockers
         self._state = staged
         del self._pending[:taken]
         receipts += rec

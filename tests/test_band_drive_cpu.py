@@ -26,12 +26,13 @@ def oracle_backed(monkeypatch):
     monkeypatch.setattr(W, "default_context", lambda: None)
 
 
-def crowd_world(damping):
-    """The frame of CrowdSceneSupport.swift: an interior of 360 x 640 inside four static rectangles 48 thick."""
+def crowd_world(damping, stiffness=1e9):
+    """The frame of CrowdSceneSupport.swift: an interior of 360 x 640 inside four static rectangles 48 thick; the
+    bubble material K_c = 1e9 is the scene's near-rigid one, for tests where contact is not the subject."""
     ix, iy = HALF
     ox, oy = ix + THICK, iy + THICK
     world = BubbleWorld(WorldConfiguration((-ox, -oy, ox, oy)))
-    tx = WorldTransaction().update_physics_material("soft", PhysicsMaterial(1e9, damping))
+    tx = WorldTransaction().update_physics_material("soft", PhysicsMaterial(stiffness, damping))
     for k, ((lx, ly), (hx, hy)) in enumerate([((-ox, -oy), (-ix, oy)), ((ix, -oy), (ox, oy)), ((-ix, -oy), (ix, -iy)),
                                               ((-ix, iy), (ix, oy))]):
         tx = tx.add(RigidBodyDescriptor(9001 + k, Polygon(((lx, ly), (hx, ly), (hx, hy), (lx, hy))), (0.0, 0.0)))
@@ -191,3 +192,52 @@ def test_motor_drive_pushes_with_its_force(oracle_backed):
     v2 = np.array(world.advance(DT).objects[1].velocity)
     v3 = np.array(world.advance(DT).objects[1].velocity)
     assert np.allclose(v3, v2, atol=1e-6)
+
+
+def test_drive_blocked_is_emitted_on_entry_and_feedback_stays_continuous(oracle_backed):
+    """EventCompactorTests.swift:3-20 on a world: a bubble dragged into a wall reports driveBlocked once when the wall
+    first stands against the drive, while the feedback keeps naming the blocker every step."""
+    world, tx = crowd_world(4.0, stiffness=2000.0)  # the wall-press material of BandDriveTests.swift:77
+    r = 20.0
+    x0 = -HALF[0] + r + 5.0
+    world.submit(tx.add(BubbleDescriptor(1, (x0, 0.0), r, 1.0, "soft", drive_policy=BubbleDrivePolicy(10.0, 300.0),
+                                         event_interest=frozenset({W.EventInterest.DRIVE_BLOCKED})))
+                 .begin_player_drive(1, (x0 - 40.0, 0.0)))
+    blocked, blockers = [], []
+    for _ in range(120):
+        frame = world.advance(DT)
+        blocked += [e.objects for e in frame.events if e.kind == "driveBlocked"]
+        fb = frame.drive_feedback[0]
+        blockers.append(fb.blocking_contact.object_id if fb.blocking_contact else None)
+    assert blocked == [(1, 9001)]  # the left wall
+    first = blockers.index(9001)
+    assert all(b == 9001 for b in blockers[first:])
+
+
+def pressed_against_the_wall(stretch):
+    world, tx = crowd_world(4.0, stiffness=2000.0)
+    x = -(HALF[0] - 20.0)
+    world.submit(tx.add(BubbleDescriptor(1, (x, 0.0), 20.0, 1.0, "soft", drive_policy=BubbleDrivePolicy(10.0, 300.0)))
+                 .begin_player_drive(1, (x - stretch, 0.0)))
+    for _ in range(361):
+        frame = world.advance(DT)
+        assert world.diagnostics.last_advance_issue is None
+    state, fb = frame.objects[1], frame.drive_feedback[0]
+    depth = 20.0 - (HALF[0] + state.position[0])
+    return depth, abs(fb.target[0] - fb.achieved_point[0]), speed(state)
+
+
+def test_wall_press_matches_the_band_force_below_the_limit_and_saturates_above_it(oracle_backed):
+    """BandDriveTests.swift:73-104: at rest the contact force of the law at the wall depth equals K_band times the
+    stretch (10 %) below maximum_force / K_band, and maximum_force above it, at the same depth (0.5)."""
+    import clr
+    force = lambda depth: clr.force(depth / 20.0, 2000.0)
+    for stretch in (6.0, 15.0, 24.0):
+        depth, s, v = pressed_against_the_wall(stretch)
+        assert v < 0.1 and abs(force(depth) - 10.0 * s) <= 0.1 * 10.0 * s, (stretch, depth, s)
+    saturated = []
+    for stretch in (45.0, 90.0):
+        depth, s, v = pressed_against_the_wall(stretch)
+        assert v < 0.1 and abs(force(depth) - 300.0) <= 30.0
+        saturated.append(depth)
+    assert abs(saturated[0] - saturated[1]) <= 0.5
