@@ -134,3 +134,21 @@ def test_world_reports_advance_issues():
     w.become_active()
     w.advance(10.0)  # the time spent away is dropped
     assert w.last_frame.step_index == 1 and w.diagnostics.backlog_seconds == pytest.approx(0.0, abs=1e-12)
+
+
+def test_interpolation_fraction_is_the_backlog_over_the_step():
+    """InterpolationFractionTests.swift:5-29: alpha = backlog / step, clamped to [0, 1]."""
+    d = FixedStepDriver(0.125)
+    assert d.interpolation_fraction == 0
+    assert d.accumulate(0.03125) and d.interpolation_fraction == pytest.approx(0.25, abs=1e-12)
+    assert d.accumulate(0.0625) and d.interpolation_fraction == pytest.approx(0.75, abs=1e-12)
+    d = FixedStepDriver(0.125)
+    assert d.accumulate(0.3125) and d.interpolation_fraction == 1
+    d.complete_step()
+    assert d.backlog_seconds == pytest.approx(0.1875, abs=1e-12) and d.interpolation_fraction == 1
+    d.complete_step()
+    assert d.interpolation_fraction == pytest.approx(0.5, abs=1e-12)
+    d = FixedStepDriver(0.125)
+    assert d.accumulate(0.125)
+    d.complete_step()
+    assert d.interpolation_fraction == 0
