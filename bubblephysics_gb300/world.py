@@ -137,6 +137,44 @@ class DriveFeedback:
 
 
 @dataclass(frozen=True)
+class ParameterTransition:
+    """A value moved over time (ParameterTransition): `target` is ("globalForce",), ("bubbleRadius", id) or
+    ("physicsMaterial", material id, "contactStiffness" | "damping"); `value` a float or, for the global force, a pair;
+    `curve` "linear", "easeIn", "easeOut", "easeInOut" or ("cubicBezier", x1, y1, x2, y2)."""
+    target: tuple
+    value: object
+    duration: float
+    curve: object = "linear"
+
+
+def transition_curve(curve, t):
+    """Progress along a transition curve (MotionControllers.curve), in float."""
+    t = np.float32(t)
+    one = np.float32(1)
+    if curve == "linear":
+        return t
+    if curve == "easeIn":
+        return t * t
+    if curve == "easeOut":
+        return one - (one - t) * (one - t)
+    if curve == "easeInOut":
+        return t * t * (np.float32(3) - np.float32(2) * t)
+    _, x1, y1, x2, y2 = curve
+
+    def bezier(u, a, b):
+        v = one - u
+        return np.float32(3) * v * v * u * np.float32(a) + np.float32(3) * v * u * u * np.float32(b) + u * u * u
+    low, high = np.float32(0), one
+    for _ in range(24):
+        middle = (low + high) / np.float32(2)
+        if bezier(middle, x1, x2) < t:
+            low = middle
+        else:
+            high = middle
+    return one if t == 1 else bezier((low + high) / np.float32(2), y1, y2)
+
+
+@dataclass(frozen=True)
 class Circle:
     radius: float
 
@@ -218,6 +256,7 @@ class TransactionRejectionReason(Enum):
     INCOMPATIBLE_MOTION_ROLE = "incompatibleMotionRole"      # detail: object id
     DRIVE_ALREADY_ACTIVE = "driveAlreadyActive"              # detail: object id
     DRIVE_NOT_ACTIVE = "driveNotActive"                      # detail: object id
+    INCOMPATIBLE_TRANSITION_VALUE = "incompatibleTransitionValue"
     UNSUPPORTED_BUBBLE_WITH_DYNAMIC_RIGID_BODY = "unsupportedBubbleWithDynamicRigidBody"
 
 
@@ -344,6 +383,9 @@ class WorldTransaction:
     def end_player_drive(self, object_id: int) -> "WorldTransaction":
         return self._with("endPlayerDrive", object_id)
 
+    def start_transition(self, transition: ParameterTransition) -> "WorldTransaction":
+        return self._with("startTransition", transition)
+
     def set_layer(self, object_id: int, layer: int) -> "WorldTransaction":
         return self._with("setLayer", object_id, int(layer))
 
@@ -388,12 +430,15 @@ class _State:
     sensors: dict = field(default_factory=dict)   # id -> SensorDescriptor
     fixed_time_step: float = 1.0 / 60.0          # for the band's stability bound
     next_drive_id: int = 1
+    transitions: dict = field(default_factory=dict)          # target -> ParameterTransition
+    transition_progress: dict = field(default_factory=dict)  # target -> (initial value, elapsed seconds)
 
     def copy(self) -> "_State":
         return _State(dict(self.materials),
                       {k: replace(v, position=v.position.copy(), velocity=v.velocity.copy()) for k, v in self.bubbles.items()},
                       {k: replace(v, position=v.position.copy()) for k, v in self.bodies.items()},
-                      self.global_force, dict(self.sensors), self.fixed_time_step, self.next_drive_id)
+                      self.global_force, dict(self.sensors), self.fixed_time_step, self.next_drive_id,
+                      dict(self.transitions), dict(self.transition_progress))
 
 
 def _finite(*values) -> bool:
@@ -634,6 +679,41 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
             return TransactionRejectionReason.OBJECT_NOT_FOUND if oid not in state.sensors else \
                 TransactionRejectionReason.INCOMPATIBLE_OBJECT_KIND, touched
         return None, touched
+    if kind == "startTransition":
+        tr = args[0]
+        if not math.isfinite(tr.duration) or tr.duration < 0:
+            return (TransactionRejectionReason.INVALID_VALUE, "transition.duration"), touched
+        curve = tr.curve
+        if not (curve in ("linear", "easeIn", "easeOut", "easeInOut") or
+                (isinstance(curve, tuple) and len(curve) == 5 and curve[0] == "cubicBezier" and _finite(*curve[1:]) and
+                 0 <= curve[1] <= 1 and 0 <= curve[3] <= 1 and curve[1] <= curve[3])):
+            return (TransactionRejectionReason.INVALID_VALUE, "transition.curve"), touched
+        target = tr.target
+        vector = isinstance(tr.value, (tuple, list))
+        if target[0] == "globalForce":
+            if not vector:
+                return TransactionRejectionReason.INCOMPATIBLE_TRANSITION_VALUE, touched
+        elif target[0] == "bubbleRadius":
+            if target[1] not in state.bubbles:
+                return TransactionRejectionReason.OBJECT_NOT_FOUND, touched
+            if vector:
+                return TransactionRejectionReason.INCOMPATIBLE_TRANSITION_VALUE, touched
+            if not (_finite(tr.value) and tr.value > 0):
+                return (TransactionRejectionReason.INVALID_VALUE, "transition.value"), touched
+        elif target[0] == "physicsMaterial" and len(target) == 3 and target[2] in ("contactStiffness", "damping"):
+            if target[1] not in state.materials:
+                return TransactionRejectionReason.PHYSICS_MATERIAL_NOT_FOUND, touched
+            if vector:
+                return TransactionRejectionReason.INCOMPATIBLE_TRANSITION_VALUE, touched
+            if not (_finite(tr.value) and tr.value >= 0):
+                return (TransactionRejectionReason.INVALID_VALUE, "transition.value"), touched
+        else:
+            return TransactionRejectionReason.UNSUPPORTED_OPERATION, touched  # friction / restitution: rigid solver
+        if vector and not _finite(*tr.value):
+            return (TransactionRejectionReason.INVALID_VALUE, "transition.value"), touched
+        state.transitions[target] = tr
+        state.transition_progress.pop(target, None)
+        return None, touched
     if kind == "setMotorDrive":
         oid, drive = args
         values = (*drive.force, drive.torque)
@@ -779,6 +859,56 @@ def contact_transitions(contacts: np.ndarray, segment_owner: dict, interested: s
         if key not in current or key[0] in removed or key[1] in removed:
             events.append(WorldEvent("contactEnded", key))
     return events, current - {k for k in current if k[0] in removed or k[1] in removed}
+
+
+def advance_transitions(state: _State, duration: float) -> bool:
+    """Moves every transition by one step (MotionControllers.advanceTransitions): each value is sampled from the same
+    start of step, interpolated in float from the value when the transition started, and the finished ones are dropped.
+    Returns whether anything changed."""
+    if not state.transitions:
+        return False
+    F32 = np.float32
+    starts = {}
+    for target in state.transitions:
+        if target[0] == "globalForce":
+            starts[target] = tuple(F32(v) for v in state.global_force)
+        elif target[0] == "bubbleRadius":
+            if target[1] in state.bubbles:
+                starts[target] = F32(state.bubbles[target[1]].desc.radius)
+        elif target[1] in state.materials:
+            m = state.materials[target[1]]
+            starts[target] = F32(m.contact_stiffness if target[2] == "contactStiffness" else m.damping)
+    for target, tr in list(state.transitions.items()):
+        if target not in starts:
+            continue
+        initial, elapsed = state.transition_progress.get(target, (starts[target], 0.0))
+        elapsed += duration
+        fraction = 1.0 if tr.duration == 0 else min(1.0, elapsed / tr.duration)
+        t = transition_curve(tr.curve, fraction)
+        one = F32(1)
+        if target[0] == "globalForce":
+            state.global_force = tuple(float(a * (one - t) + F32(b) * t) for a, b in zip(initial, tr.value))
+        else:
+            value = float(initial * (one - t) + F32(tr.value) * t)
+            if target[0] == "bubbleRadius":
+                b = state.bubbles[target[1]]
+                b.desc = replace(b.desc, radius=value)
+            else:
+                m = state.materials[target[1]]
+                state.materials[target[1]] = replace(m, **({"contact_stiffness": value} if target[2] == "contactStiffness"
+                                                           else {"damping": value}))
+        if fraction == 1.0:
+            del state.transitions[target]
+            state.transition_progress.pop(target, None)
+        else:
+            state.transition_progress[target] = (initial, elapsed)
+    return True
+
+
+def _drop_transitions_of(state: _State, ids):
+    for target in [t for t in state.transitions if t[0] == "bubbleRadius" and t[1] in ids]:
+        del state.transitions[target]
+        state.transition_progress.pop(target, None)
 
 
 def query_index(state: _State, effective_radii: dict | None = None) -> QueryIndex:
@@ -933,6 +1063,15 @@ class BubbleWorld:
             self._paused_in_background = False
             self._clock.discard_next_advance()
             self.diagnostics.is_paused = self._paused
+
+    @property
+    def physics_materials(self) -> dict:
+        """The published physics materials (transitions move their values step by step)."""
+        return dict(self._state.materials)
+
+    @property
+    def global_force(self) -> tuple:
+        return tuple(self._state.global_force)
 
     @property
     def last_frame(self) -> WorldFrame:
@@ -1116,7 +1255,11 @@ class BubbleWorld:
         cfg = self.configuration
         taken = len(self._pending)
         staged, rec, ev = stage(self._pending[:taken], self._state, cfg.simulation_region)
-        changed = bool(rec) or self._native is None
+        _drop_transitions_of(staged, {i for r in rec for i in r.removed_object_ids})
+        if staged.transitions and staged is self._state:
+            staged = staged.copy()
+        moved = advance_transitions(staged, cfg.fixed_time_step)
+        changed = bool(rec) or self._native is None or moved
         spec, ids, owners = self._spec(staged)
         # pairs whose sensor or bubble left in this batch end (the reference's missing-pair events)
         gone_now = {i for r in rec for i in r.removed_object_ids + r.replaced_object_ids}
@@ -1161,6 +1304,7 @@ class BubbleWorld:
                     ev.append(WorldEvent("didWrap", (oid,)))
             for oid in removed_now:
                 staged.bubbles.pop(oid)
+            _drop_transitions_of(staged, removed_now)
             self.diagnostics.contact_candidate_overflow += int(rep["candidate_overflow"])
             self.diagnostics.maximum_contact_candidates_per_object = int(rep["max_candidates_per_object"])
             if staged.sensors:
