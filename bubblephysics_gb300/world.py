@@ -923,6 +923,27 @@ def query_index(state: _State, effective_radii: dict | None = None) -> QueryInde
     return QueryIndex(objects)
 
 
+class HitTestRequest:
+    """A hit test answered on the state of the next completed step (BubbleWorld.hitTest of the reference, which
+    suspends until then): `done` turns true with `result` (an object id or None); cancel() withdraws a waiting one."""
+
+    def __init__(self, world, point):
+        self._world = weakref.ref(world)
+        self.point = (float(point[0]), float(point[1]))
+        self.done = False
+        self.result = None
+
+    def _resolve(self, result):
+        self.done, self.result = True, result
+
+    def cancel(self):
+        world = self._world()
+        if not self.done and world is not None and self in world._hit_tests:
+            world._hit_tests.remove(self)
+        if not self.done:
+            self._resolve(None)
+
+
 # ---------------------------------------------------------------------------------------------------------------------
 # Fixed-step clock
 # ---------------------------------------------------------------------------------------------------------------------
@@ -1021,6 +1042,7 @@ class BubbleWorld:
         self._shapes: dict = {}           # bubble id -> (effective radius, bounds) of the last contours
         self._index: QueryIndex | None = None  # built at the first query after a publication
         self._feedback: tuple = ()
+        self._hit_tests: list = []          # HitTestRequest waiting for the next step
         self._blockers: dict = {}          # driven bubble id -> the obstacle that blocked it in the last step
         self.query_index_build_count = 0
         self.diagnostics = WorldDiagnostics()
@@ -1110,6 +1132,32 @@ class BubbleWorld:
         d.consecutive_backlogged_advances = clock.consecutive_backlogged_advances
         d.pending_transaction_count = len(self._pending)
         return self._frame
+
+    def request_hit_test(self, point) -> HitTestRequest:
+        """The reference's asynchronous hitTest: the point goes with the next step and is answered on its state; a
+        paused world keeps it waiting; a non-finite point or a failed world answers None at once."""
+        request = HitTestRequest(self, point)
+        if not all(math.isfinite(v) for v in request.point) or self.diagnostics.failure_reason is not None:
+            request._resolve(None)
+        else:
+            self._hit_tests.append(request)
+        return request
+
+    def _host_hit(self, point):
+        """Hit test of a world without bubbles (no device world): the bodies containing the point, the highest layer
+        (Int32) then the largest id winning."""
+        p = np.asarray(point, np.float32)
+        best = None
+        for oid, body in self._state.bodies.items():
+            if _contains_including_boundary(_body_shape(body), p):
+                key = (body.desc.layer, oid & 0xFFFFFFFFFFFFFFFF)
+                if best is None or key > best[0]:
+                    best = (key, oid)
+        return None if best is None else best[1]
+
+    @property
+    def pending_hit_test_count(self) -> int:
+        return len(self._hit_tests)
 
     def hit_test(self, point) -> int | None:
         """The object at `point` on the published state (BubbleWorld.hitTest): a bubble inside its contour, a body or a
@@ -1254,6 +1302,7 @@ class BubbleWorld:
     def _step(self, receipts: list, events: list) -> bool:
         cfg = self.configuration
         taken = len(self._pending)
+        handed = list(self._hit_tests)  # the points this step answers; later requests wait for the next one
         staged, rec, ev = stage(self._pending[:taken], self._state, cfg.simulation_region)
         _drop_transitions_of(staged, {i for r in rec for i in r.removed_object_ids})
         if staged.transitions and staged is self._state:
@@ -1348,6 +1397,16 @@ class BubbleWorld:
         del self._pending[:taken]
         receipts += rec
         events += ev + contact_events
+        if handed:
+            answers = [self._host_hit(r.point) for r in handed]  # no device world: bodies only, exact shapes
+            if self._native is not None:
+                ids, _, found = self._native.hit_test([r.point for r in handed], cfg.max_contour_segment_length,
+                                                      cfg.contour_surface_tension, cfg.position_tolerance)
+                answers = [int(i) if f else None for i, f in zip(ids, found)]
+            for request, answer in zip(handed, answers):
+                if request in self._hit_tests:
+                    self._hit_tests.remove(request)
+                    request._resolve(answer)
         if removed_now and self._native is not None:
             self._native_ids = None  # the removed slots leave the device world at the next step
         return True
@@ -1410,6 +1469,9 @@ class BubbleWorld:
                    N.E_NONFINITE: WorldFailureReason.NON_FINITE_VALUES,
                    N.E_CONTACT_VIOLATION: WorldFailureReason.CONTACT_VIOLATION}
         self.diagnostics.failure_reason = reasons.get(status, WorldFailureReason.COMMAND_EXECUTION_FAILED)
+        for request in self._hit_tests:
+            request._resolve(None)
+        self._hit_tests.clear()
         self.diagnostics.failure_detail = {"objects": tuple(int(v) for v in rep["violation_objects"]),
                                            "edge": int(rep["violation_edge"]),
                                            "distance": float(rep["violation_distance"]),
