@@ -317,6 +317,16 @@ class WorldFailureReason(Enum):
     COMMAND_EXECUTION_FAILED = "commandExecutionFailed"
 
 
+class WorldRejectionReason(str, Enum):
+    """Why a step was rejected without ending the world (WorldRejectionReason): the queue and the time stay for a
+    retry."""
+    SOLVER_GUARD = "solverGuard"
+    INVALID_FRAME = "invalidFrame"
+    INVALID_SNAPSHOT = "invalidSnapshot"
+    FRAME_IN_FLIGHT = "frameInFlight"
+    UNEXPECTED = "unexpected"
+
+
 class AdvanceIssue(str, Enum):
     """Why an advance published nothing new (WorldAdvanceIssue of the reference)."""
     WORLD_FAILED = "worldFailed"
@@ -331,6 +341,7 @@ class WorldDiagnostics:
     discarded_backlog_seconds: float = 0.0
     consecutive_backlogged_advances: int = 0
     last_advance_issue: AdvanceIssue | None = None
+    last_rejection_reason: WorldRejectionReason | None = None
     steps_in_last_advance: int = 0
     pending_transaction_count: int = 0
     is_paused: bool = False
@@ -1119,8 +1130,10 @@ class BubbleWorld:
         receipts, events = [], []
         while d.steps_in_last_advance < clock.maximum_steps_per_advance and clock.can_step:
             if not self._step(receipts, events):
-                d.last_advance_issue = AdvanceIssue.STEP_FAILED
+                d.last_advance_issue = AdvanceIssue.WORLD_FAILED if d.failure_reason is not None else \
+                    AdvanceIssue.STEP_FAILED
                 break
+            d.last_rejection_reason = None
             clock.complete_step()
             d.steps_in_last_advance += 1
             self._frame = WorldFrame(clock.completed_steps, clock.simulation_time, tuple(receipts), tuple(events),
@@ -1321,9 +1334,13 @@ class BubbleWorld:
         if changed or ids != self._native_ids:
             if self._native is not None:
                 self._native.close()
+                self._native = None
             if len(ids) and self._ctx is None:
                 self._ctx = default_context()
-            self._native = World(spec, self._ctx) if len(ids) else None
+            try:
+                self._native = World(spec, self._ctx) if len(ids) else None
+            except N.NativeError as error:
+                return self._solver_error(error)
             self._native_ids = ids
             self._native_order = ids  # the device world's bubble order (kept when a removal forces a rebuild)
             self._segment_owner = owners
@@ -1333,7 +1350,10 @@ class BubbleWorld:
         removed_now = set()
         contacts = np.zeros(0, N.CONTACT_DTYPE)
         if self._native is not None:
-            status, reps = self._native.step(1)
+            try:
+                status, reps = self._native.step(1)
+            except N.NativeError as error:
+                return self._solver_error(error)
             rep = reps[0]
             if status != N.OK:
                 self._fail(status, rep)
@@ -1464,6 +1484,22 @@ class BubbleWorld:
         allowed = np.array([state.sensors[sid].filter.takes(oid) for sid in sensor_ids for oid in objects], np.uint8)
         return records, np.array(verts, np.float32).reshape(-1, 2), carried, allowed
 
+    def _solver_error(self, error) -> bool:
+        """A solver call that did not step: a failed CUDA command or device wait ends the world (the command failed);
+        a bad snapshot, a step in flight, a capacity or allocation limit only rejects this step, and the same
+        transactions and time retry at the next advance (BubbleWorld.handleAdvanceError). No device at all is
+        raised: the product never steps without its CUDA path."""
+        if error.status == N.E_UNAVAILABLE:
+            raise error
+        if error.status in (N.E_CUDA, N.E_TIMEOUT):
+            self._fail(error.status, None)
+            return False
+        self.diagnostics.last_rejection_reason = {N.E_INVALID: WorldRejectionReason.INVALID_SNAPSHOT,
+                                                  N.E_INFLIGHT: WorldRejectionReason.FRAME_IN_FLIGHT}.get(
+            error.status, WorldRejectionReason.UNEXPECTED)
+        self._native_ids = None  # rebuild the device world from the published state at the retry
+        return False
+
     def _fail(self, status: int, rep):
         reasons = {N.E_SUBSTEP_LIMIT: WorldFailureReason.SUBSTEP_LIMIT_EXCEEDED,
                    N.E_NONFINITE: WorldFailureReason.NON_FINITE_VALUES,
@@ -1472,11 +1508,10 @@ class BubbleWorld:
         for request in self._hit_tests:
             request._resolve(None)
         self._hit_tests.clear()
-        self.diagnostics.failure_detail = {"objects": tuple(int(v) for v in rep["violation_objects"]),
-                                           "edge": int(rep["violation_edge"]),
-                                           "distance": float(rep["violation_distance"]),
-                                           "limiting_term": int(rep["limiter_term"]),
-                                           "limiting_object": int(rep["limiter_object"])}
+        self.diagnostics.failure_detail = None if rep is None else {
+            "objects": tuple(int(v) for v in rep["violation_objects"]), "edge": int(rep["violation_edge"]),
+            "distance": float(rep["violation_distance"]), "limiting_term": int(rep["limiter_term"]),
+            "limiting_object": int(rep["limiter_object"])}
         self._pending.clear()
 
     def _objects(self) -> dict:
