@@ -137,6 +137,22 @@ class DriveFeedback:
 
 
 @dataclass(frozen=True)
+class ForceFieldDescriptor:
+    """A force field (ForceFieldDescriptor): `kind` "directional" (the constant `force`, turned by `angle`), "radial"
+    or "vortex" (`strength` with `falloff`) over a circle or polygon range about `position`, acting on the bubbles its
+    filter takes."""
+    id: int
+    position: tuple
+    kind: str
+    shape: object
+    angle: float = 0.0
+    force: tuple = (0.0, 0.0)
+    strength: float = 0.0
+    falloff: float = 0.0
+    filter: "ObjectFilter" = None
+
+
+@dataclass(frozen=True)
 class ParameterTransition:
     """A value moved over time (ParameterTransition): `target` is ("globalForce",), ("bubbleRadius", id) or
     ("physicsMaterial", material id, "contactStiffness" | "damping"); `value` a float or, for the global force, a pair;
@@ -443,13 +459,14 @@ class _State:
     next_drive_id: int = 1
     transitions: dict = field(default_factory=dict)          # target -> ParameterTransition
     transition_progress: dict = field(default_factory=dict)  # target -> (initial value, elapsed seconds)
+    fields: dict = field(default_factory=dict)               # id -> ForceFieldDescriptor
 
     def copy(self) -> "_State":
         return _State(dict(self.materials),
                       {k: replace(v, position=v.position.copy(), velocity=v.velocity.copy()) for k, v in self.bubbles.items()},
                       {k: replace(v, position=v.position.copy()) for k, v in self.bodies.items()},
                       self.global_force, dict(self.sensors), self.fixed_time_step, self.next_drive_id,
-                      dict(self.transitions), dict(self.transition_progress))
+                      dict(self.transitions), dict(self.transition_progress), dict(self.fields))
 
 
 def _finite(*values) -> bool:
@@ -595,14 +612,16 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
         obj = args[-1]
         if kind == "replace":
             oid = args[0]
-            if oid not in state.bubbles and oid not in state.bodies and oid not in state.sensors:
+            if oid not in state.bubbles and oid not in state.bodies and oid not in state.sensors and \
+                    oid not in state.fields:
                 return TransactionRejectionReason.OBJECT_NOT_FOUND, touched
             if obj.id != oid:
                 return TransactionRejectionReason.REPLACEMENT_ID_MISMATCH, touched
             state.bubbles.pop(oid, None)
             state.bodies.pop(oid, None)
             state.sensors.pop(oid, None)
-        elif obj.id in state.bubbles or obj.id in state.bodies or obj.id in state.sensors:
+            state.fields.pop(oid, None)
+        elif obj.id in state.bubbles or obj.id in state.bodies or obj.id in state.sensors or obj.id in state.fields:
             return TransactionRejectionReason.DUPLICATE_OBJECT_ID, touched
         if isinstance(obj, BubbleDescriptor):
             reason = _validate_bubble(obj, state, region)
@@ -615,6 +634,15 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
             if reason:
                 return reason, touched
             state.bodies[obj.id] = _Body(obj, np.asarray(obj.position, np.float32).copy(), float(obj.angle))
+        elif isinstance(obj, ForceFieldDescriptor):
+            shape = obj.shape
+            ok = obj.kind in ("directional", "radial", "vortex") and \
+                _finite(*obj.position, obj.angle, *obj.force, obj.strength, obj.falloff) and obj.falloff >= 0 and (
+                    (isinstance(shape, Circle) and _finite(shape.radius) and shape.radius > 0) or
+                    (isinstance(shape, Polygon) and len(shape.points) >= 3 and _finite(*np.ravel(shape.points))))
+            if not ok:
+                return TransactionRejectionReason.INVALID_VALUE, touched
+            state.fields[obj.id] = obj
         elif isinstance(obj, SensorDescriptor):
             shape = obj.shape
             ok = _finite(*obj.position, obj.angle) and (
@@ -630,7 +658,7 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
     if kind == "remove":
         oid = args[0]
         if state.bubbles.pop(oid, None) is None and state.bodies.pop(oid, None) is None and \
-                state.sensors.pop(oid, None) is None:
+                state.sensors.pop(oid, None) is None and state.fields.pop(oid, None) is None:
             return TransactionRejectionReason.OBJECT_NOT_FOUND, touched
         touched["removed"].append(oid)
         return None, touched
@@ -870,6 +898,40 @@ def contact_transitions(contacts: np.ndarray, segment_owner: dict, interested: s
         if key not in current or key[0] in removed or key[1] in removed:
             events.append(WorldEvent("contactEnded", key))
     return events, current - {k for k in current if k[0] in removed or k[1] in removed}
+
+
+FIELD_KINDS = {"directional": 0, "radial": 1, "vortex": 2}
+
+
+def field_records(state: _State):
+    """The device records of a state's force fields (NativeForceInput.fields, NativeForceRecords.swift:160-230): in id
+    order, the directional force or the radial / vortex strength, the range (a circle's radius or a polygon's
+    farthest vertex), the polygon's local vertices, and the filter as a range of ascending ids (an empty filter takes
+    nobody; no filter takes everyone)."""
+    records, verts, ids = [], [], []
+    for fid in sorted(state.fields, key=lambda v: v & 0xFFFFFFFFFFFFFFFF):
+        d = state.fields[fid]
+        f = N.ForceField()
+        f.position[:] = [float(v) for v in d.position]
+        f.rotation, f.falloff, f.kind = float(d.angle), float(d.falloff), FIELD_KINDS[d.kind]
+        if d.kind == "directional":
+            f.direction[:] = [float(v) for v in d.force]
+        else:
+            f.strength = float(d.strength)
+        if isinstance(d.shape, Circle):
+            f.radius, f.vertex_offset, f.vertex_count = float(d.shape.radius), 0, 0
+        else:
+            pts = np.asarray(d.shape.points, np.float32)
+            f.radius = float(np.sqrt((pts.astype(np.float32) ** 2).sum(1)).max())
+            f.vertex_offset, f.vertex_count = len(verts), len(pts)
+            verts += [tuple(map(float, p)) for p in pts]
+        taken = d.filter.object_ids if d.filter is not None else None
+        f.has_filter = 0 if taken is None else 1
+        f.filter_offset, f.filter_count = len(ids), 0 if taken is None else len(taken)
+        if taken is not None:
+            ids += sorted(int(v) for v in taken)
+        records.append(f)
+    return records, np.array(verts, np.float32).reshape(-1, 2), np.array(ids, np.int64)
 
 
 def advance_transitions(state: _State, duration: float) -> bool:
@@ -1310,6 +1372,7 @@ class BubbleWorld:
                          gravity=tuple(cfg.gravity), time_step=cfg.fixed_time_step,
                          candidate_limit=cfg.candidate_limit, substep_split_multiplier=cfg.substep_split_multiplier,
                          bands=bands, motors=motors)
+        spec.fields, spec.field_vertices, spec.field_object_ids = field_records(state)
         return spec, ids, owners
 
     def _step(self, receipts: list, events: list) -> bool:
