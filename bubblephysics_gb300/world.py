@@ -867,7 +867,7 @@ def contact_transitions(contacts: np.ndarray, segment_owner: dict, interested: s
     sums = {}
     for c in contacts:
         first = int(c["participants"][0])
-        second = int(c["participants"][1]) if c["kind"] == 0 else segment_owner.get(int(c["participants"][1]))
+        second = int(c["participants"][1]) if c["kind"] != 1 else segment_owner.get(int(c["participants"][1]))
         if second is None or not (c["penetration"] > 0 or c["impulse"] > 0):
             continue
         if first not in interested and second not in interested:
@@ -982,6 +982,76 @@ def _drop_transitions_of(state: _State, ids):
     for target in [t for t in state.transitions if t[0] == "bubbleRadius" and t[1] in ids]:
         del state.transitions[target]
         state.transition_progress.pop(target, None)
+
+
+def body_contacts(state: _State, interested: set, step: float, separation_tolerance: float = 0.002) -> np.ndarray:
+    """End-of-step contact records of bubbles against bodies (kind 2), for the pairs an event may concern. The device's
+    records cover pairs and segments (nativeBuildContacts); the reference reports bubble-body contacts from its rigid
+    solver, which is not built here, so they are taken on the host from the published poses: the signed distance d of
+    the centre to the body's surface, active while r - d > -tolerance, the normal from the bubble to the body, the
+    point on the surface and the impulse F dt^2 of the wall law F = K_c (r - d) r / d^2."""
+    from .queries import distance_to_segment, polygon_contains
+    out = []
+    F32 = np.float32
+    for bid, body in state.bodies.items():
+        if isinstance(body.desc.shape, Polygon) and body.desc.motion_role == MotionRole.STATIC:
+            continue  # static polygons are one-sided edges on the device: their records come from the step
+        shape = _body_shape(body)
+        for oid, b in state.bubbles.items():
+            if (oid not in interested and bid not in interested) or not b.desc.filter.accepts(body.desc.filter):
+                continue
+            c, r = np.asarray(b.position, np.float32), F32(b.desc.radius)
+            if shape[0] == "circle":
+                delta = c - shape[1]
+                dist = F32(math.hypot(*delta))
+                surface_normal = delta / dist if dist > 0 else np.array([0, 1], np.float32)
+                d = dist - shape[2]
+                point = shape[1] + surface_normal * shape[2]
+            elif shape[0] == "capsule":
+                a, e = shape[1], shape[2]
+                ab = e - a
+                t = max(F32(0), min(F32(1), F32(np.dot(c - a, ab)) / max(F32(np.dot(ab, ab)), F32(1e-20))))
+                nearest = a + ab * t
+                delta = c - nearest
+                dist = F32(math.hypot(*delta))
+                surface_normal = delta / dist if dist > 0 else np.array([0, 1], np.float32)
+                d = dist - shape[3]
+                point = nearest + surface_normal * shape[3]
+            else:
+                ring = shape[1]
+                best = None
+                for k in range(len(ring)):
+                    a, e = ring[k], ring[(k + 1) % len(ring)]
+                    ab = e - a
+                    t = max(F32(0), min(F32(1), F32(np.dot(c - a, ab)) / max(F32(np.dot(ab, ab)), F32(1e-20))))
+                    q = a + ab * t
+                    dist = F32(math.hypot(*(c - q)))
+                    if best is None or dist < best[0]:
+                        best = (dist, q)
+                dist, point = best
+                inside = polygon_contains(ring, c)
+                d = -dist if inside else dist
+                away = (c - point) / dist if dist > 0 else np.array([0, 1], np.float32)
+                surface_normal = -away if inside else away
+            if not (r - d > -separation_tolerance):
+                continue
+            law = float(wall_force(float(state.materials[b.desc.physics_material_id].contact_stiffness), float(r),
+                                     float(d)))
+            rec = np.zeros(1, N.CONTACT_DTYPE)[0]
+            rec["participants"] = (oid, bid)
+            rec["kind"] = 2
+            rec["normal"] = -surface_normal  # from the bubble to the body
+            rec["point"] = point
+            rec["penetration"] = float(r - d)
+            rec["impulse"] = law * step * step
+            out.append(rec)
+    return np.array(out, N.CONTACT_DTYPE) if out else np.zeros(0, N.CONTACT_DTYPE)
+
+
+def wall_force(stiffness: float, radius: float, distance: float) -> float:
+    """The wall law's force F = K_c (r - d) r / d^2 (nativeWallContactLaw, NFK:60-69), d clamped to r 1e-6."""
+    d = max(distance, radius * 1e-6)
+    return stiffness * (radius - d) * radius / (d * d) if d < radius else 0.0
 
 
 def query_index(state: _State, effective_radii: dict | None = None) -> QueryIndex:
@@ -1463,6 +1533,8 @@ class BubbleWorld:
         interested = {i for i, b in staged.bubbles.items() if EventInterest.CONTACT in b.desc.event_interest}
         interested |= {i for i, b in staged.bodies.items() if EventInterest.CONTACT in b.desc.event_interest}
         gone = removed_now | {i for r in rec for i in r.removed_object_ids + r.replaced_object_ids}
+        if interested and staged.bodies and staged.bubbles:
+            contacts = np.concatenate([contacts, body_contacts(staged, interested, cfg.fixed_time_step)])
         contact_events, self._history = contact_transitions(contacts, self._segment_owner, interested, self._history,
                                                             cfg.fixed_time_step, gone)
         self._feedback = self._drive_feedback(staged, contacts)
