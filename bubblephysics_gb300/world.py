@@ -359,6 +359,8 @@ class WorldDiagnostics:
     last_advance_issue: AdvanceIssue | None = None
     last_rejection_reason: WorldRejectionReason | None = None
     steps_in_last_advance: int = 0
+    last_step_substeps: int = 0            # NativeMetalFrameTelemetry.substepCount of the last completed step
+    last_step_rebuilds: int = 0            # its grid rebuilds
     pending_transaction_count: int = 0
     is_paused: bool = False
     contact_candidate_overflow: int = 0
@@ -1507,6 +1509,8 @@ class BubbleWorld:
             for oid in removed_now:
                 staged.bubbles.pop(oid)
             _drop_transitions_of(staged, removed_now)
+            self.diagnostics.last_step_substeps = int(rep["substep_count"])
+            self.diagnostics.last_step_rebuilds = int(rep["rebuild_count"])
             self.diagnostics.contact_candidate_overflow += int(rep["candidate_overflow"])
             self.diagnostics.maximum_contact_candidates_per_object = int(rep["max_candidates_per_object"])
             if staged.sensors:
