@@ -241,3 +241,30 @@ def test_wall_press_matches_the_band_force_below_the_limit_and_saturates_above_i
         assert v < 0.1 and abs(force(depth) - 300.0) <= 30.0
         saturated.append(depth)
     assert abs(saturated[0] - saturated[1]) <= 0.5
+
+
+def test_a_fast_small_bubble_settles_at_the_law_without_crossing_the_edge(oracle_backed):
+    """WallImpactTests.swift:12-58: a bubble r 24 pulled by the band (K 30, F_max 1200) from 150 units off the wall
+    hits it faster than max(40, 2 r) (K_c 20 / 0.0108, gamma 5), dents deeper than at rest but never reaches the edge
+    (eps < 1 in every step), and settles at the law's eps* for F_max (2 %)."""
+    import clr
+    r, kc = 24.0, float(np.float32(20.0) / np.float32(0.0108))
+    world, tx = crowd_world(5.0, stiffness=kc)
+    start = -HALF[0] + r + 150.0
+    world.submit(tx.add(BubbleDescriptor(1, (start, 0.0), r, r * r / 400, "soft",
+                                         drive_policy=BubbleDrivePolicy(30.0, 1200.0)))
+                 .begin_player_drive(1, (-2000.0, 0.0)))
+    peak, final, impact, behind = -math.inf, 0.0, 0.0, []
+    for step in range(360):
+        frame = world.advance(DT)
+        assert world.diagnostics.last_advance_issue is None and world.diagnostics.failure_reason is None
+        state = frame.objects[1]
+        ratio = (r - (HALF[0] + state.position[0])) / r
+        peak, final = max(peak, ratio), ratio
+        if ratio >= 1:
+            behind.append(step)
+        if ratio <= 0:
+            impact = max(impact, -state.velocity[0])
+    expected = clr.epsilon(1200.0 / kc)
+    assert impact > max(40.0, 2 * r) and abs(final - expected) <= 0.02 * expected
+    assert expected < peak < 1 and behind == []
