@@ -118,6 +118,24 @@ class MotorDrive:
 
 
 @dataclass(frozen=True)
+class PathDrive:
+    """A path a path-driven bubble follows at `speed` (PathDrive, Model/Motion.swift:26-35): its velocity is set at the
+    start of every step towards the current point, forces and damping do not act on it, contacts do."""
+    points: tuple
+    speed: float
+
+    def __post_init__(self):
+        points = tuple((float(x), float(y)) for x, y in self.points)
+        if not points:
+            raise ValueError("path.points must not be empty")
+        if not all(math.isfinite(v) for p in points for v in p):
+            raise ValueError("path.point must be finite")
+        if not (math.isfinite(self.speed) and self.speed > 0):
+            raise ValueError("path.speed must be finite and positive")
+        object.__setattr__(self, "points", points)
+
+
+@dataclass(frozen=True)
 class DriveBlockingContact:
     object_id: int
     point: tuple
@@ -134,6 +152,11 @@ class DriveFeedback:
     achieved_point: tuple
     blocking_contact: DriveBlockingContact | None = None
     is_stopped: bool = False
+
+    @property
+    def deviation(self) -> tuple:
+        """target - achieved point (DriveFeedback.deviation)."""
+        return (self.target[0] - self.achieved_point[0], self.target[1] - self.achieved_point[1])
 
 
 @dataclass(frozen=True)
@@ -403,6 +426,9 @@ class WorldTransaction:
     def set_motor_drive(self, object_id: int, drive: "MotorDrive") -> "WorldTransaction":
         return self._with("setMotorDrive", object_id, drive)
 
+    def set_path_drive(self, object_id: int, drive: PathDrive) -> "WorldTransaction":
+        return self._with("setPathDrive", object_id, drive)
+
     def begin_player_drive(self, object_id: int, target) -> "WorldTransaction":
         return self._with("beginPlayerDrive", object_id, tuple(float(v) for v in target))
 
@@ -441,6 +467,10 @@ class _Bubble:
     drive_target: tuple | None = None          # player-driven: the band's target
     drive_id: int | None = None
     motion_before_drive: "MotionRole | None" = None
+    path: PathDrive | None = None              # path-driven: the path, the point it heads for, and the stop
+    path_index: int = 0
+    path_stopped: bool = False
+    path_blocker: "DriveBlockingContact | None" = None
 
 
 @dataclass
@@ -558,13 +588,31 @@ def placement_issue(point, radius: float, filt: CollisionFilter, state: _State, 
     return None
 
 
+def _set_bubble_motion(b: _Bubble, oid: int, role: MotionRole):
+    """setMotion of a bubble (TransactionStager.swift:268-281): the player-driven role needs a running player drive;
+    leaving a role drops its drive (the band, the path, the motor)."""
+    if role == MotionRole.KINEMATIC:
+        return TransactionRejectionReason.UNSUPPORTED_MOTION_ROLE, (oid, role)
+    if role == MotionRole.PLAYER_DRIVEN and b.drive_target is None:
+        return TransactionRejectionReason.DRIVE_NOT_ACTIVE, oid
+    b.desc = replace(b.desc, motion_role=role)
+    if role != MotionRole.PLAYER_DRIVEN:
+        b.drive_target = b.drive_id = b.motion_before_drive = None
+    if role != MotionRole.PATH_DRIVEN:
+        b.path, b.path_index, b.path_stopped, b.path_blocker = None, 0, False, None
+    if role != MotionRole.MOTOR_DRIVEN:
+        b.motor = None
+    if role == MotionRole.STATIC:
+        b.velocity[:] = 0
+    return None
+
+
 def _validate_bubble(desc: BubbleDescriptor, state: _State, region):
     if desc.physics_material_id not in state.materials:
         return TransactionRejectionReason.PHYSICS_MATERIAL_NOT_FOUND
     if not (_finite(*desc.position, *desc.velocity, desc.radius, desc.mass) and desc.radius > 0 and desc.mass > 0):
         return TransactionRejectionReason.INVALID_VALUE
-    if desc.motion_role not in (MotionRole.DYNAMIC, MotionRole.STATIC, MotionRole.MOTOR_DRIVEN):
-        # kinematic bubbles do not exist; a player drive starts with begin_player_drive; path drives are not built here
+    if desc.motion_role == MotionRole.KINEMATIC:  # kinematic bubbles do not exist (TransactionStager.swift:510-513)
         return TransactionRejectionReason.UNSUPPORTED_MOTION_ROLE, (desc.id, desc.motion_role)
     policy = desc.drive_policy
     if policy is not None:
@@ -683,14 +731,15 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
             else:
                 body.desc = replace(body.desc, motion_role=role)
             return None, touched
-        if role not in (MotionRole.DYNAMIC, MotionRole.STATIC, MotionRole.MOTOR_DRIVEN):
-            return (TransactionRejectionReason.UNSUPPORTED_MOTION_ROLE, (oid, role)), touched
-        b.desc = replace(b.desc, motion_role=role)
-        if role != MotionRole.MOTOR_DRIVEN:
-            b.motor = None
-        b.drive_target = b.drive_id = b.motion_before_drive = None
-        if role == MotionRole.STATIC:
-            b.velocity[:] = 0
+        return _set_bubble_motion(b, oid, role), touched
+    if kind == "setPathDrive":
+        oid, drive = args
+        b = state.bubbles.get(oid)
+        if b is None:
+            return (TransactionRejectionReason.OBJECT_NOT_FOUND if oid not in state.bodies else
+                    (TransactionRejectionReason.UNSUPPORTED_MOTION_ROLE, (oid, MotionRole.PATH_DRIVEN))), touched
+        _set_bubble_motion(b, oid, MotionRole.PATH_DRIVEN)
+        b.path, b.path_index, b.path_stopped, b.path_blocker = drive, 0, False, None
         return None, touched
     if kind == "setGlobalForce":
         if not _finite(*args[0]):
@@ -767,8 +816,7 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
         if b is None:
             return (TransactionRejectionReason.OBJECT_NOT_FOUND if oid not in state.bodies else
                     (TransactionRejectionReason.UNSUPPORTED_MOTION_ROLE, (oid, MotionRole.MOTOR_DRIVEN))), touched
-        b.desc = replace(b.desc, motion_role=MotionRole.MOTOR_DRIVEN)
-        b.drive_target = b.drive_id = b.motion_before_drive = None
+        _set_bubble_motion(b, oid, MotionRole.MOTOR_DRIVEN)
         b.motor = drive
         return None, touched
     if kind in ("beginPlayerDrive", "updatePlayerDrive"):
@@ -786,7 +834,9 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
         if kind == "beginPlayerDrive":
             if b.drive_target is not None:
                 return (TransactionRejectionReason.DRIVE_ALREADY_ACTIVE, oid), touched
-            b.motion_before_drive = b.desc.motion_role
+            # a bubble added in the player-driven role goes back to dynamic (TransactionStager.swift:330)
+            b.motion_before_drive = MotionRole.DYNAMIC if b.desc.motion_role == MotionRole.PLAYER_DRIVEN else \
+                b.desc.motion_role
             b.desc = replace(b.desc, motion_role=MotionRole.PLAYER_DRIVEN)
             b.drive_id = state.next_drive_id
             state.next_drive_id += 1
@@ -978,6 +1028,37 @@ def advance_transitions(state: _State, duration: float) -> bool:
         else:
             state.transition_progress[target] = (initial, elapsed)
     return True
+
+
+def path_velocity(target, origin, speed: float, dt: float) -> np.ndarray:
+    """The velocity that takes a bubble from `origin` towards `target` at `speed`, without passing it within the
+    step (MotionControllers.swift:147-151), in float."""
+    delta = (np.asarray(target, np.float32) - np.asarray(origin, np.float32)).astype(np.float32)
+    distance = np.float32(math.sqrt(float(delta[0] * delta[0] + delta[1] * delta[1])))
+    if not distance > 0:
+        return np.zeros(2, np.float32)
+    return (delta * (min(np.float32(speed), distance / np.float32(dt)) / distance)).astype(np.float32)
+
+
+def prepare_paths(state: _State, dt: float) -> list:
+    """The start of a step for path-driven bubbles (MotionControllers.swift:85-91): the bubble heads for its path's
+    current point, moving on to the next one once within 1e-4 of it; a bubble without a path, or stopped by a blocker,
+    stands still. Returns the ids of the path-driven bubbles."""
+    ids = []
+    for oid, b in state.bubbles.items():
+        if b.desc.motion_role != MotionRole.PATH_DRIVEN:
+            continue
+        ids.append(oid)
+        if b.path is not None and not b.path_stopped:
+            points = np.asarray(b.path.points, np.float32)
+            while b.path_index < len(points) - 1 and \
+                    float(np.linalg.norm((points[b.path_index] - b.position).astype(np.float32))) <= 1e-4:
+                b.path_index += 1
+            b.velocity = path_velocity(points[b.path_index], b.position, b.path.speed, dt)
+        else:
+            b.velocity = np.zeros(2, np.float32)
+            b.angular_velocity = 0.0
+    return ids
 
 
 def _drop_transitions_of(state: _State, ids):
@@ -1374,7 +1455,10 @@ class BubbleWorld:
             b[i]["angular_velocity"] = bub.angular_velocity
             b[i]["contact_stiffness"] = mat.contact_stiffness
             b[i]["damping"] = mat.damping
-            b[i]["flags"] = N.BUBBLE_ENABLED | (N.BUBBLE_STATIC if static else N.BUBBLE_FORCE_DRIVEN) | \
+            # a path-driven bubble moves with the velocity its path set and feels contacts only: no forces, no damping
+            force_driven = d.motion_role in (MotionRole.DYNAMIC, MotionRole.MOTOR_DRIVEN, MotionRole.PLAYER_DRIVEN)
+            b[i]["flags"] = N.BUBBLE_ENABLED | (N.BUBBLE_STATIC if static else 0) | \
+                (N.BUBBLE_FORCE_DRIVEN if force_driven else 0) | \
                 (N.BUBBLE_WRAP if d.region_exit_policy == RegionExitPolicy.WRAP else 0)
             if d.motion_role == MotionRole.PLAYER_DRIVEN and bub.drive_target is not None:
                 band = N.Band()
@@ -1455,8 +1539,12 @@ class BubbleWorld:
         _drop_transitions_of(staged, {i for r in rec for i in r.removed_object_ids})
         if staged.transitions and staged is self._state:
             staged = staged.copy()
+        if staged is self._state and any(b.desc.motion_role == MotionRole.PATH_DRIVEN for b in staged.bubbles.values()):
+            staged = staged.copy()
         moved = advance_transitions(staged, cfg.fixed_time_step)
-        changed = bool(rec) or self._native is None or moved
+        paths = prepare_paths(staged, cfg.fixed_time_step)  # a path's velocity goes to the device every step
+        starts = {oid: staged.bubbles[oid].position.copy() for oid in paths}
+        changed = bool(rec) or self._native is None or moved or bool(paths)
         spec, ids, owners = self._spec(staged)
         # pairs whose sensor or bubble left in this batch end (the reference's missing-pair events)
         gone_now = {i for r in rec for i in r.removed_object_ids + r.replaced_object_ids}
@@ -1541,7 +1629,7 @@ class BubbleWorld:
             contacts = np.concatenate([contacts, body_contacts(staged, interested, cfg.fixed_time_step)])
         contact_events, self._history = contact_transitions(contacts, self._segment_owner, interested, self._history,
                                                             cfg.fixed_time_step, gone)
-        self._feedback = self._drive_feedback(staged, contacts)
+        self._feedback = self._drive_feedback(staged, contacts, starts)
         blockers = {}
         for fb in self._feedback:  # driveBlocked when the blocker of an interested bubble changes (EventCompactor.finish)
             bub = staged.bubbles.get(fb.object_id)
@@ -1570,16 +1658,22 @@ class BubbleWorld:
             self._native_ids = None  # the removed slots leave the device world at the next step
         return True
 
-    def _drive_feedback(self, state: _State, contacts) -> tuple:
-        """DriveFeedback of every active player drive after a step (MotionControllers.feedback): the target, the
-        bubble's position, and its first contact whose normal (from the obstacle to the bubble) stands against the
-        drive."""
+    def _drive_feedback(self, state: _State, contacts, starts: dict) -> tuple:
+        """DriveFeedback of every active player or path drive after a step (MotionControllers.swift:154-188): the
+        target, the bubble's position, and its first contact whose normal (from the obstacle to the bubble) stands
+        against the drive. A path-driven bubble so blocked that it moved less than 1e-4 in the step (`starts` holds
+        where it began) stops for good, and keeps reporting that blocker."""
         out = []
         for oid in sorted(state.bubbles, key=lambda v: v & 0xFFFFFFFFFFFFFFFF):
             b = state.bubbles[oid]
-            if b.desc.motion_role != MotionRole.PLAYER_DRIVEN or b.drive_target is None:
+            role = b.desc.motion_role
+            if role == MotionRole.PLAYER_DRIVEN and b.drive_target is not None:
+                target = b.drive_target
+            elif role == MotionRole.PATH_DRIVEN and b.path is not None:
+                target = b.path.points[b.path_index]
+            else:
                 continue
-            delta = np.asarray(b.drive_target, np.float32) - b.position
+            delta = np.asarray(target, np.float32) - b.position
             blocker = None
             for c in contacts:
                 a, other, kind = int(c["participants"][0]), int(c["participants"][1]), int(c["kind"])
@@ -1594,7 +1688,15 @@ class BubbleWorld:
                 if float(delta[0] * normal[0] + delta[1] * normal[1]) < -1e-4:
                     blocker = DriveBlockingContact(obstacle, tuple(map(float, c["point"])), tuple(map(float, normal)))
                     break
-            out.append(DriveFeedback(oid, b.drive_id, b.drive_target, tuple(map(float, b.position)), blocker))
+            path_active = role == MotionRole.PATH_DRIVEN
+            if path_active and blocker is not None and oid in starts and \
+                    float(np.linalg.norm((b.position - starts[oid]).astype(np.float32))) < 1e-4:
+                b.path_stopped, b.path_blocker = True, blocker
+                b.velocity[:] = 0
+                b.angular_velocity = 0.0
+            out.append(DriveFeedback(oid, b.drive_id, tuple(target), tuple(map(float, b.position)),
+                                     blocker or (b.path_blocker if path_active else None),
+                                     path_active and b.path_stopped))
         return tuple(out)
 
     def _sensor_records(self, state: _State, objects: list):
