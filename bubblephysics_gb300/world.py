@@ -136,6 +136,34 @@ class PathDrive:
 
 
 @dataclass(frozen=True)
+class KinematicDrive:
+    """The motion imposed on a kinematic body (KinematicDrive, Model/Motion.swift:74-79): `KinematicDrive.velocity`
+    (a constant linear and angular velocity, tracked as an exact pose), `KinematicDrive.path` (a PathDrive, never
+    blocked) or `KinematicDrive.target` (a pose reached in one step). Forces and contacts never move the body."""
+    kind: str
+    linear: tuple = (0.0, 0.0)
+    angular: float = 0.0
+    path_drive: PathDrive | None = None
+    target_position: tuple = (0.0, 0.0)
+    target_rotation: float = 0.0
+
+    @staticmethod
+    def velocity(linear, angular: float = 0.0) -> "KinematicDrive":
+        return KinematicDrive("velocity", linear=tuple(float(v) for v in linear), angular=float(angular))
+
+    @staticmethod
+    def path(path: PathDrive) -> "KinematicDrive":
+        return KinematicDrive("path", path_drive=path)
+
+    @staticmethod
+    def target(position, rotation: float = 0.0) -> "KinematicDrive":
+        return KinematicDrive("target", target_position=tuple(float(v) for v in position), target_rotation=float(rotation))
+
+    def values(self) -> tuple:
+        return (*self.linear, self.angular, *self.target_position, self.target_rotation)
+
+
+@dataclass(frozen=True)
 class DriveBlockingContact:
     object_id: int
     point: tuple
@@ -444,8 +472,11 @@ class WorldTransaction:
     def set_layer(self, object_id: int, layer: int) -> "WorldTransaction":
         return self._with("setLayer", object_id, int(layer))
 
-    def set_kinematic_drive(self, object_id: int, velocity, angular_velocity: float = 0.0) -> "WorldTransaction":
-        return self._with("setKinematicDrive", object_id, tuple(float(v) for v in velocity), float(angular_velocity))
+    def set_kinematic_drive(self, object_id: int, drive, angular_velocity: float = 0.0) -> "WorldTransaction":
+        """`drive` is a KinematicDrive, or a linear velocity (with `angular_velocity`) for KinematicDrive.velocity."""
+        if not isinstance(drive, KinematicDrive):
+            drive = KinematicDrive.velocity(drive, angular_velocity)
+        return self._with("setKinematicDrive", object_id, drive)
 
     def operation(self, name: str, *args) -> "WorldTransaction":
         """Any other operation of the reference's transaction (merges, splits, joints, sensors, ...): recorded, and
@@ -478,6 +509,19 @@ class _Body:
     desc: RigidBodyDescriptor
     position: np.ndarray
     angle: float
+    drive: KinematicDrive | None = None        # kinematic: the drive, this step's velocity, the exact pose it tracks
+    velocity: np.ndarray = field(default_factory=lambda: np.zeros(2, np.float32))
+    angular_velocity: float = 0.0
+    exact: tuple | None = None
+    path_index: int = 0
+
+    @staticmethod
+    def of(desc: RigidBodyDescriptor) -> "_Body":
+        """A body as added: a kinematic descriptor's velocity is its first drive."""
+        drive = None
+        if desc.motion_role == MotionRole.KINEMATIC and any(v != 0 for v in (*desc.velocity, desc.angular_velocity)):
+            drive = KinematicDrive.velocity(desc.velocity, desc.angular_velocity)
+        return _Body(desc, np.asarray(desc.position, np.float32).copy(), float(desc.angle), drive)
 
 
 @dataclass
@@ -496,7 +540,7 @@ class _State:
     def copy(self) -> "_State":
         return _State(dict(self.materials),
                       {k: replace(v, position=v.position.copy(), velocity=v.velocity.copy()) for k, v in self.bubbles.items()},
-                      {k: replace(v, position=v.position.copy()) for k, v in self.bodies.items()},
+                      {k: replace(v, position=v.position.copy(), velocity=v.velocity.copy()) for k, v in self.bodies.items()},
                       self.global_force, dict(self.sensors), self.fixed_time_step, self.next_drive_id,
                       dict(self.transitions), dict(self.transition_progress), dict(self.fields))
 
@@ -683,7 +727,7 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
             reason = _validate_body(obj, state)
             if reason:
                 return reason, touched
-            state.bodies[obj.id] = _Body(obj, np.asarray(obj.position, np.float32).copy(), float(obj.angle))
+            state.bodies[obj.id] = _Body.of(obj)
         elif isinstance(obj, ForceFieldDescriptor):
             shape = obj.shape
             ok = obj.kind in ("directional", "radial", "vortex") and \
@@ -728,6 +772,8 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
                 return TransactionRejectionReason.OBJECT_NOT_FOUND, touched
             if role != MotionRole.KINEMATIC:  # leaving the kinematic role discards the drive
                 body.desc = replace(body.desc, motion_role=role, velocity=(0.0, 0.0), angular_velocity=0.0)
+                body.drive, body.exact, body.path_index = None, None, 0
+                body.velocity, body.angular_velocity = np.zeros(2, np.float32), 0.0
             else:
                 body.desc = replace(body.desc, motion_role=role)
             return None, touched
@@ -856,15 +902,17 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
         b.drive_target = b.drive_id = b.motion_before_drive = None
         return None, touched
     if kind == "setKinematicDrive":
-        oid, velocity, omega = args
+        oid, drive = args
         body = state.bodies.get(oid)
         if body is None and oid not in state.bubbles:
             return TransactionRejectionReason.OBJECT_NOT_FOUND, touched
         if body is None or body.desc.motion_role != MotionRole.KINEMATIC:
             return (TransactionRejectionReason.INCOMPATIBLE_MOTION_ROLE, oid), touched
-        if not _finite(*velocity, omega):
+        if not _finite(*drive.values()):
             return TransactionRejectionReason.INVALID_VALUE, touched
-        body.desc = replace(body.desc, velocity=velocity, angular_velocity=omega)
+        if drive.kind == "velocity":
+            body.desc = replace(body.desc, velocity=drive.linear, angular_velocity=drive.angular)
+        body.drive, body.exact, body.path_index = drive, None, 0
         return None, touched
     return TransactionRejectionReason.UNSUPPORTED_OPERATION, touched
 
@@ -1038,6 +1086,47 @@ def path_velocity(target, origin, speed: float, dt: float) -> np.ndarray:
     if not distance > 0:
         return np.zeros(2, np.float32)
     return (delta * (min(np.float32(speed), distance / np.float32(dt)) / distance)).astype(np.float32)
+
+
+def prepare_kinematic(state: _State, duration: float) -> bool:
+    """The start of a step for kinematic bodies (MotionControllers.swift:119-145): the velocity this step imposes,
+    in float. A velocity drive tracks its pose in double and asks for the velocity that takes the float pose exactly
+    there (a pose published otherwise, by a wrap or a replace, starts a new track); a path drive heads for its current
+    point like a path-driven bubble but is never blocked; a target drive reaches its pose in one step; no drive stands
+    still. Returns whether a body's velocity changed, which the device world must then be given."""
+    dt = np.float32(duration)
+    changed = False
+    for body in state.bodies.values():
+        if body.desc.motion_role != MotionRole.KINEMATIC:
+            continue
+        v, w = np.zeros(2, np.float32), np.float32(0.0)
+        position, rotation = body.position.astype(np.float32), np.float32(body.angle)
+        d = body.drive
+        if d is not None and d.kind == "velocity":
+            exact = body.exact
+            if exact is None or np.float32(exact[0]) != position[0] or np.float32(exact[1]) != position[1] or \
+                    np.float32(exact[2]) != rotation:
+                exact = (float(position[0]), float(position[1]), float(rotation))
+            linear = [float(np.float32(x)) for x in d.linear]
+            exact = (exact[0] + linear[0] * duration, exact[1] + linear[1] * duration,
+                     exact[2] + float(np.float32(d.angular)) * duration)
+            body.exact = exact
+            v = ((np.array(exact[:2], np.float64).astype(np.float32) - position) / dt).astype(np.float32)
+            w = (np.float32(exact[2]) - rotation) / dt
+        elif d is not None and d.kind == "path":
+            points = np.asarray(d.path_drive.points, np.float32)
+            body.path_index = min(body.path_index, len(points) - 1)
+            while body.path_index < len(points) - 1 and \
+                    float(np.linalg.norm((points[body.path_index] - position).astype(np.float32))) <= 1e-4:
+                body.path_index += 1
+            v = path_velocity(points[body.path_index], position, d.path_drive.speed, duration)
+        elif d is not None and d.kind == "target":
+            v = ((np.asarray(d.target_position, np.float32) - position) / dt).astype(np.float32)
+            w = (np.float32(d.target_rotation) - rotation) / dt
+        if not (np.array_equal(v, body.velocity) and np.float32(w) == np.float32(body.angular_velocity)):
+            changed = True
+        body.velocity, body.angular_velocity = v, float(w)
+    return changed
 
 
 def prepare_paths(state: _State, dt: float) -> list:
@@ -1496,8 +1585,8 @@ class BubbleWorld:
             rec["id"] = oid
             rec["position"] = body.position
             rec["angle"] = body.angle
-            rec["velocity"] = d.velocity if d.motion_role == MotionRole.KINEMATIC else (0.0, 0.0)
-            rec["angular_velocity"] = d.angular_velocity if d.motion_role == MotionRole.KINEMATIC else 0.0
+            rec["velocity"] = body.velocity if d.motion_role == MotionRole.KINEMATIC else (0.0, 0.0)
+            rec["angular_velocity"] = body.angular_velocity if d.motion_role == MotionRole.KINEMATIC else 0.0
             rec["flags"] = N.BODY_KINEMATIC if d.motion_role == MotionRole.KINEMATIC else N.BODY_STATIC
             rec["category"], rec["mask"], rec["layer"] = d.filter.category, d.filter.mask, d.layer
             rec["vertex_offset"] = sum(len(v) for v in verts)
@@ -1539,12 +1628,14 @@ class BubbleWorld:
         _drop_transitions_of(staged, {i for r in rec for i in r.removed_object_ids})
         if staged.transitions and staged is self._state:
             staged = staged.copy()
-        if staged is self._state and any(b.desc.motion_role == MotionRole.PATH_DRIVEN for b in staged.bubbles.values()):
+        if staged is self._state and (any(b.desc.motion_role == MotionRole.PATH_DRIVEN for b in staged.bubbles.values())
+                                      or any(b.drive is not None for b in staged.bodies.values())):
             staged = staged.copy()
         moved = advance_transitions(staged, cfg.fixed_time_step)
         paths = prepare_paths(staged, cfg.fixed_time_step)  # a path's velocity goes to the device every step
+        steered = prepare_kinematic(staged, cfg.fixed_time_step)
         starts = {oid: staged.bubbles[oid].position.copy() for oid in paths}
-        changed = bool(rec) or self._native is None or moved or bool(paths)
+        changed = bool(rec) or self._native is None or moved or bool(paths) or steered
         spec, ids, owners = self._spec(staged)
         # pairs whose sensor or bubble left in this batch end (the reference's missing-pair events)
         gone_now = {i for r in rec for i in r.removed_object_ids + r.replaced_object_ids}
@@ -1620,8 +1711,8 @@ class BubbleWorld:
         dt = np.float32(cfg.fixed_time_step)
         for body in staged.bodies.values():  # kinematic advance (with or without bubbles), the device's float arithmetic
             if body.desc.motion_role == MotionRole.KINEMATIC:
-                body.position = (body.position + np.asarray(body.desc.velocity, np.float32) * dt).astype(np.float32)
-                body.angle = float(np.float32(body.angle) + np.float32(body.desc.angular_velocity) * dt)
+                body.position = (body.position + body.velocity * dt).astype(np.float32)
+                body.angle = float(np.float32(body.angle) + np.float32(body.angular_velocity) * dt)
         interested = {i for i, b in staged.bubbles.items() if EventInterest.CONTACT in b.desc.event_interest}
         interested |= {i for i, b in staged.bodies.items() if EventInterest.CONTACT in b.desc.event_interest}
         gone = removed_now | {i for r in rec for i in r.removed_object_ids + r.replaced_object_ids}
@@ -1767,8 +1858,9 @@ class BubbleWorld:
             shape = body.desc.shape
             kind = {Circle: "circle", Capsule: "capsule", Polygon: "polygon"}[type(shape)]
             lo, hi = shape_box(_body_shape(body))  # the box of the shape at its pose: it follows the rotation
-            vel = body.desc.velocity if body.desc.motion_role == MotionRole.KINEMATIC else (0.0, 0.0)
+            kinematic = body.desc.motion_role == MotionRole.KINEMATIC
+            vel = body.velocity if kinematic else (0.0, 0.0)
             out[oid] = ObjectState(kind, tuple(map(float, body.position)), tuple(map(float, vel)), body.angle,
-                                   body.desc.angular_velocity if body.desc.motion_role == MotionRole.KINEMATIC else 0.0,
+                                   body.angular_velocity if kinematic else 0.0,
                                    (float(lo[0]), float(lo[1]), float(hi[0]), float(hi[1])))
         return out

@@ -11,10 +11,9 @@ from bubblephysics_gb300.world import (BubbleDescriptor, BubbleWorld, CollisionF
 from test_world_api_oracle_cpu import OracleBackedWorld
 
 ONLY_CATEGORY_2 = CollisionFilter(1, 1 << 1)
-# KinematicMotionTests.trackTolerance is 1e-4: the reference re-anchors a velocity drive to a double-precision track
-# every step (MotionControllers.applyKinematicDrive); this path integrates the drive velocity in float on the device,
-# which drifts by about 2e-4 over 4 s at 12 units/s, so the bar here is 1e-3.
-TRACK_TOLERANCE = 1e-3
+# KinematicMotionTests.trackTolerance: a velocity drive follows an exact double-precision track, re-anchored every
+# step (MotionControllers.swift:124-134).
+TRACK_TOLERANCE = 1e-4
 
 
 @pytest.fixture(autouse=True)
