@@ -445,6 +445,11 @@ class WorldTransaction:
     def set_motion(self, object_id: int, role: MotionRole) -> "WorldTransaction":
         return self._with("setMotion", object_id, role)
 
+    def update_render_material(self, material_id, material=None) -> "WorldTransaction":
+        """Accepted and kept for the renderer, which is not part of this path; it takes its place in the operation
+        order like the reference's."""
+        return self._with("updateRenderMaterial", material_id, material)
+
     def set_global_force(self, force) -> "WorldTransaction":
         return self._with("setGlobalForce", tuple(float(v) for v in force))
 
@@ -632,6 +637,14 @@ def placement_issue(point, radius: float, filt: CollisionFilter, state: _State, 
     return None
 
 
+def _not_physical(state: _State, oid: int):
+    """The rejection for an id that names no bubble or body: a sensor or a force field has no motion
+    (TransactionStager.physicalObject), anything else is not found."""
+    if oid in state.sensors or oid in state.fields:
+        return TransactionRejectionReason.INCOMPATIBLE_OBJECT_KIND, oid
+    return TransactionRejectionReason.OBJECT_NOT_FOUND
+
+
 def _set_bubble_motion(b: _Bubble, oid: int, role: MotionRole):
     """setMotion of a bubble (TransactionStager.swift:268-281): the player-driven role needs a running player drive;
     leaving a role drops its drive (the band, the path, the motor)."""
@@ -651,6 +664,55 @@ def _set_bubble_motion(b: _Bubble, oid: int, role: MotionRole):
     return None
 
 
+STATIC_OUTSIDE = "staticGeometryOutsideSimulationRegion"
+
+
+def _circle_inside(center, radius, region) -> bool:
+    x, y, r = float(np.float32(center[0])), float(np.float32(center[1])), float(np.float32(radius))
+    return x - r >= region[0] and x + r <= region[2] and y - r >= region[1] and y + r <= region[3]
+
+
+def _range_inside(shape, position, angle, region) -> bool:
+    """A circle or polygon range about `position`, turned by `angle`, lies in the region (WorldConfiguration.swift:
+    95-119, in double)."""
+    if isinstance(shape, Circle):
+        return _circle_inside(position, shape.radius, region)
+    c, s = math.cos(float(np.float32(angle))), math.sin(float(np.float32(angle)))
+    px, py = float(np.float32(position[0])), float(np.float32(position[1]))
+    for vx, vy in shape.points:
+        vx, vy = float(np.float32(vx)), float(np.float32(vy))
+        x, y = px + vx * c - vy * s, py + vx * s + vy * c
+        if not (region[0] <= x <= region[2] and region[1] <= y <= region[3]):
+            return False
+    return True
+
+
+def static_geometry_inside(obj, region, state: _State | None = None, role=None, position=None, angle=None) -> bool:
+    """WorldConfiguration.validate for this path: a static bubble (at the largest radius a scheduled transition takes
+    it to), a static body, a sensor and a force field lie wholly in the simulation region; other roles are not held
+    to it. `role`, `position` and `angle` give the object's runtime values when they differ from its descriptor."""
+    role = role or getattr(obj, "motion_role", None)
+    position = obj.position if position is None else position
+    if isinstance(obj, (SensorDescriptor, ForceFieldDescriptor)):
+        return _range_inside(obj.shape, position, obj.angle, region)
+    if role != MotionRole.STATIC:
+        return True
+    if isinstance(obj, BubbleDescriptor):
+        radius = float(np.float32(obj.radius))
+        scheduled = state.transitions.get(("bubbleRadius", obj.id)) if state is not None else None
+        if scheduled is not None:
+            radius = max(radius, float(np.float32(scheduled.value)))
+        return _circle_inside(position, radius, region)
+    angle = obj.angle if angle is None else angle
+    shape = obj.shape
+    if isinstance(shape, Capsule):  # the axis' two ends, each with a circle of the radius
+        rot = np.float32(angle)
+        axis = np.array([np.cos(rot), np.sin(rot)], np.float32) * np.float32(shape.half_length)
+        p = np.asarray(position, np.float32)
+        return _circle_inside(p + axis, shape.radius, region) and _circle_inside(p - axis, shape.radius, region)
+    return _range_inside(shape, position, angle, region)
+
+
 def _validate_bubble(desc: BubbleDescriptor, state: _State, region):
     if desc.physics_material_id not in state.materials:
         return TransactionRejectionReason.PHYSICS_MATERIAL_NOT_FOUND
@@ -668,13 +730,15 @@ def _validate_bubble(desc: BubbleDescriptor, state: _State, region):
         step = float(np.float32(state.fixed_time_step))
         if not float(np.float32(policy.band_stiffness)) * 16 * step * step <= float(np.float32(desc.mass)):
             return TransactionRejectionReason.INVALID_VALUE, "drive.bandStiffness"
+    if not static_geometry_inside(desc, region, state):
+        return TransactionRejectionReason.INVALID_VALUE, STATIC_OUTSIDE
     issue = placement_issue(desc.position, desc.radius, desc.filter, state, region, frozenset({desc.id}))
     if issue is not None:
         return TransactionRejectionReason.INVALID_PLACEMENT, (desc.id, issue)
     return None
 
 
-def _validate_body(desc: RigidBodyDescriptor, state: _State) -> TransactionRejectionReason | None:
+def _validate_body(desc: RigidBodyDescriptor, state: _State, region) -> TransactionRejectionReason | None:
     shape = desc.shape
     sizes = {Circle: lambda s: (s.radius,), Capsule: lambda s: (s.half_length, s.radius)}.get(type(shape))
     if sizes is not None:
@@ -687,6 +751,8 @@ def _validate_body(desc: RigidBodyDescriptor, state: _State) -> TransactionRejec
         return TransactionRejectionReason.INVALID_VALUE
     if not _finite(*desc.position, desc.angle, *desc.velocity, desc.angular_velocity):
         return TransactionRejectionReason.INVALID_VALUE
+    if not static_geometry_inside(desc, region):
+        return TransactionRejectionReason.INVALID_VALUE, STATIC_OUTSIDE
     # a body may not cover the centre of a bubble it collides with; the smallest such id is named
     # (PlacementGeometry.bubbleInside)
     shape = _body_shape(_Body(desc, np.asarray(desc.position, np.float64), float(desc.angle)))
@@ -724,7 +790,7 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
             state.bubbles[obj.id] = _Bubble(obj, np.asarray(obj.position, np.float32).copy(),
                                             np.asarray(obj.velocity, np.float32).copy())
         elif isinstance(obj, RigidBodyDescriptor):
-            reason = _validate_body(obj, state)
+            reason = _validate_body(obj, state, region)
             if reason:
                 return reason, touched
             state.bodies[obj.id] = _Body.of(obj)
@@ -736,6 +802,8 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
                     (isinstance(shape, Polygon) and len(shape.points) >= 3 and _finite(*np.ravel(shape.points))))
             if not ok:
                 return TransactionRejectionReason.INVALID_VALUE, touched
+            if not static_geometry_inside(obj, region):
+                return (TransactionRejectionReason.INVALID_VALUE, STATIC_OUTSIDE), touched
             state.fields[obj.id] = obj
         elif isinstance(obj, SensorDescriptor):
             shape = obj.shape
@@ -744,6 +812,8 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
                 (isinstance(shape, Polygon) and len(shape.points) >= 3 and _finite(*np.ravel(shape.points))))
             if not ok:
                 return TransactionRejectionReason.INVALID_VALUE, touched
+            if not static_geometry_inside(obj, region):
+                return (TransactionRejectionReason.INVALID_VALUE, STATIC_OUTSIDE), touched
             state.sensors[obj.id] = obj
         else:
             return TransactionRejectionReason.UNSUPPORTED_OPERATION, touched
@@ -763,13 +833,18 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
             return TransactionRejectionReason.INVALID_VALUE, touched
         state.materials[mid] = material
         return None, touched
+    if kind == "updateRenderMaterial":
+        return None, touched
     if kind == "setMotion":
         oid, role = args
         b = state.bubbles.get(oid)
         if b is None:
             body = state.bodies.get(oid)
             if body is None:
-                return TransactionRejectionReason.OBJECT_NOT_FOUND, touched
+                return _not_physical(state, oid), touched
+            if role == MotionRole.STATIC and not static_geometry_inside(body.desc, region, role=role,
+                                                                         position=body.position, angle=body.angle):
+                return (TransactionRejectionReason.INVALID_VALUE, STATIC_OUTSIDE), touched
             if role != MotionRole.KINEMATIC:  # leaving the kinematic role discards the drive
                 body.desc = replace(body.desc, motion_role=role, velocity=(0.0, 0.0), angular_velocity=0.0)
                 body.drive, body.exact, body.path_index = None, None, 0
@@ -777,12 +852,14 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
             else:
                 body.desc = replace(body.desc, motion_role=role)
             return None, touched
+        if role == MotionRole.STATIC and not static_geometry_inside(b.desc, region, state, role, b.position):
+            return (TransactionRejectionReason.INVALID_VALUE, STATIC_OUTSIDE), touched
         return _set_bubble_motion(b, oid, role), touched
     if kind == "setPathDrive":
         oid, drive = args
         b = state.bubbles.get(oid)
         if b is None:
-            return (TransactionRejectionReason.OBJECT_NOT_FOUND if oid not in state.bodies else
+            return (_not_physical(state, oid) if oid not in state.bodies else
                     (TransactionRejectionReason.UNSUPPORTED_MOTION_ROLE, (oid, MotionRole.PATH_DRIVEN))), touched
         _set_bubble_motion(b, oid, MotionRole.PATH_DRIVEN)
         b.path, b.path_index, b.path_stopped, b.path_blocker = drive, 0, False, None
@@ -792,16 +869,23 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
             return TransactionRejectionReason.INVALID_VALUE, touched
         state.global_force = args[0]
         return None, touched
-    if kind == "applyImpulse":
+    if kind == "applyImpulse":  # TransactionStager.swift:312-324
         oid, impulse = args
+        if not _finite(*impulse):
+            return (TransactionRejectionReason.INVALID_VALUE, "impulse"), touched
         b = state.bubbles.get(oid)
         if b is None:
-            return TransactionRejectionReason.OBJECT_NOT_FOUND if oid not in state.bodies else \
-                TransactionRejectionReason.INCOMPATIBLE_OBJECT_KIND, touched
-        if not _finite(*impulse):
-            return TransactionRejectionReason.INVALID_VALUE, touched
-        if b.desc.motion_role == MotionRole.DYNAMIC:
-            b.velocity += (np.asarray(impulse, np.float32) / np.float32(b.desc.mass)).astype(np.float32)
+            if oid in state.bodies:  # static and kinematic bodies take no impulse
+                return (TransactionRejectionReason.INCOMPATIBLE_MOTION_ROLE, oid), touched
+            return (TransactionRejectionReason.INCOMPATIBLE_OBJECT_KIND, oid) if oid in state.sensors or \
+                oid in state.fields else TransactionRejectionReason.OBJECT_NOT_FOUND, touched
+        if b.desc.motion_role not in (MotionRole.DYNAMIC, MotionRole.MOTOR_DRIVEN):
+            return (TransactionRejectionReason.INCOMPATIBLE_MOTION_ROLE, oid), touched
+        mass = float(np.float32(b.desc.mass))
+        velocity = np.array([float(b.velocity[k]) + float(np.float32(impulse[k])) / mass for k in range(2)])
+        if not np.isfinite(velocity.astype(np.float32)).all():
+            return (TransactionRejectionReason.INVALID_VALUE, "velocityAfterImpulse"), touched
+        b.velocity = velocity.astype(np.float32)
         return None, touched
     if kind == "setLayer":
         oid, layer = args
@@ -819,34 +903,37 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
         tr = args[0]
         if not math.isfinite(tr.duration) or tr.duration < 0:
             return (TransactionRejectionReason.INVALID_VALUE, "transition.duration"), touched
-        curve = tr.curve
+        curve = tr.curve  # TransactionStager.swift:576-614
         if not (curve in ("linear", "easeIn", "easeOut", "easeInOut") or
                 (isinstance(curve, tuple) and len(curve) == 5 and curve[0] == "cubicBezier" and _finite(*curve[1:]) and
-                 0 <= curve[1] <= 1 and 0 <= curve[3] <= 1 and curve[1] <= curve[3])):
+                 all(0 <= v <= 1 for v in curve[1:]) and curve[1] <= curve[3])):
             return (TransactionRejectionReason.INVALID_VALUE, "transition.curve"), touched
         target = tr.target
         vector = isinstance(tr.value, (tuple, list))
-        if target[0] == "globalForce":
-            if not vector:
-                return TransactionRejectionReason.INCOMPATIBLE_TRANSITION_VALUE, touched
-        elif target[0] == "bubbleRadius":
-            if target[1] not in state.bubbles:
-                return TransactionRejectionReason.OBJECT_NOT_FOUND, touched
-            if vector:
-                return TransactionRejectionReason.INCOMPATIBLE_TRANSITION_VALUE, touched
-            if not (_finite(tr.value) and tr.value > 0):
-                return (TransactionRejectionReason.INVALID_VALUE, "transition.value"), touched
-        elif target[0] == "physicsMaterial" and len(target) == 3 and target[2] in ("contactStiffness", "damping"):
+        if target[0] == "globalForce" and vector:
+            if not _finite(*tr.value):
+                return (TransactionRejectionReason.INVALID_VALUE, "transition.globalForce"), touched
+        elif target[0] == "physicsMaterial" and len(target) == 3 and not vector:
             if target[1] not in state.materials:
                 return TransactionRejectionReason.PHYSICS_MATERIAL_NOT_FOUND, touched
-            if vector:
-                return TransactionRejectionReason.INCOMPATIBLE_TRANSITION_VALUE, touched
             if not (_finite(tr.value) and tr.value >= 0):
-                return (TransactionRejectionReason.INVALID_VALUE, "transition.value"), touched
+                return (TransactionRejectionReason.INVALID_VALUE, "transition.material"), touched
+            # K_c belongs to bubble materials only; friction and restitution to rigid ones, which this path has not
+            if target[2] not in ("contactStiffness", "damping") or (target[2] == "contactStiffness" and not tr.value > 0):
+                return (TransactionRejectionReason.INVALID_VALUE, "transition.material"), touched
+        elif target[0] == "bubbleRadius" and not vector:
+            b = state.bubbles.get(target[1])
+            if b is None:
+                return (TransactionRejectionReason.INCOMPATIBLE_OBJECT_KIND, target[1]) if target[1] in state.bodies or \
+                    target[1] in state.sensors or target[1] in state.fields else \
+                    TransactionRejectionReason.OBJECT_NOT_FOUND, touched
+            if not (_finite(tr.value) and tr.value > 0):
+                return (TransactionRejectionReason.INVALID_VALUE, "transition.radius"), touched
+            if b.desc.motion_role == MotionRole.STATIC and \
+                    not _circle_inside(b.position, tr.value, region):
+                return (TransactionRejectionReason.INVALID_VALUE, STATIC_OUTSIDE), touched
         else:
-            return TransactionRejectionReason.UNSUPPORTED_OPERATION, touched  # friction / restitution: rigid solver
-        if vector and not _finite(*tr.value):
-            return (TransactionRejectionReason.INVALID_VALUE, "transition.value"), touched
+            return TransactionRejectionReason.INCOMPATIBLE_TRANSITION_VALUE, touched
         state.transitions[target] = tr
         state.transition_progress.pop(target, None)
         return None, touched
@@ -860,7 +947,7 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
                     MAXIMUM_DRIVE_MAGNITUDE else "motor.torque"), touched
         b = state.bubbles.get(oid)
         if b is None:
-            return (TransactionRejectionReason.OBJECT_NOT_FOUND if oid not in state.bodies else
+            return (_not_physical(state, oid) if oid not in state.bodies else
                     (TransactionRejectionReason.UNSUPPORTED_MOTION_ROLE, (oid, MotionRole.MOTOR_DRIVEN))), touched
         _set_bubble_motion(b, oid, MotionRole.MOTOR_DRIVEN)
         b.motor = drive
@@ -871,7 +958,7 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
             return TransactionRejectionReason.INVALID_VALUE, touched
         b = state.bubbles.get(oid)
         if b is None:
-            return TransactionRejectionReason.OBJECT_NOT_FOUND if oid not in state.bodies else \
+            return _not_physical(state, oid) if oid not in state.bodies else \
                 (TransactionRejectionReason.INCOMPATIBLE_OBJECT_KIND, oid), touched
         if kind == "beginPlayerDrive" and b.desc.drive_policy is None:
             return (TransactionRejectionReason.INCOMPATIBLE_OBJECT_KIND, oid), touched
@@ -894,7 +981,7 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
         oid = args[0]
         b = state.bubbles.get(oid)
         if b is None:
-            return TransactionRejectionReason.OBJECT_NOT_FOUND if oid not in state.bodies else \
+            return _not_physical(state, oid) if oid not in state.bodies else \
                 (TransactionRejectionReason.DRIVE_NOT_ACTIVE, oid), touched
         if b.drive_target is None:
             return (TransactionRejectionReason.DRIVE_NOT_ACTIVE, oid), touched
@@ -908,8 +995,12 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
             return TransactionRejectionReason.OBJECT_NOT_FOUND, touched
         if body is None or body.desc.motion_role != MotionRole.KINEMATIC:
             return (TransactionRejectionReason.INCOMPATIBLE_MOTION_ROLE, oid), touched
-        if not _finite(*drive.values()):
-            return TransactionRejectionReason.INVALID_VALUE, touched
+        names = {"velocity": (("kinematicDrive.linear", drive.linear), ("kinematicDrive.angular", (drive.angular,))),
+                 "target": (("kinematicDrive.position", drive.target_position),
+                            ("kinematicDrive.rotation", (drive.target_rotation,)))}.get(drive.kind, ())
+        for name, values in names:  # TransactionStager.swift:293-302: finite and within 1e6
+            if not _finite(*values) or any(abs(float(np.float32(v))) > MAXIMUM_DRIVE_MAGNITUDE for v in values):
+                return (TransactionRejectionReason.INVALID_VALUE, name), touched
         if drive.kind == "velocity":
             body.desc = replace(body.desc, velocity=drive.linear, angular_velocity=drive.angular)
         body.drive, body.exact, body.path_index = drive, None, 0

@@ -35,7 +35,7 @@ def centroid(ring):
 
 def test_bounds_contain_the_contour_and_undented_centres_are_contour_centroids():
     rng = np.random.default_rng(0x2B60F5)
-    w = BubbleWorld(WorldConfiguration((0.0, 0.0, 375.0, 700.0), global_force=(0.0, -300.0)))
+    w = BubbleWorld(WorldConfiguration((-40.0, -40.0, 415.0, 740.0), global_force=(0.0, -300.0)))
     tx = WorldTransaction().update_physics_material("b", PhysicsMaterial(229.0, 1.0))
     for k, ((lx, ly), (hx, hy)) in enumerate([((-40, -40), (415, 0)), ((-40, 700), (415, 740)), ((-40, 0), (0, 700)),
                                               ((375, 0), (415, 700))]):

@@ -147,7 +147,7 @@ def test_sensors_stage_like_objects():
 
 def test_sensor_records_and_carried_overlap_state():
     world = BubbleWorld(WorldConfiguration(REGION))
-    state, _, _ = W.stage([(1, soft().add(W.SensorDescriptor(9, W.Polygon(((0, 0), (4, 0), (0, 4))), (1.0, 2.0), 0.5,
+    state, _, _ = W.stage([(1, soft().add(W.SensorDescriptor(9, W.Polygon(((0, 0), (4, 0), (0, 4))), (11.0, 12.0), 0.5,
                                                                  filter=W.ObjectFilter(frozenset({20, 500})),
                                                                  reports_enter=False))
                                .add(W.SensorDescriptor(4, Circle(7.0), (50.0, 60.0))))], W._State(), REGION)
@@ -163,7 +163,7 @@ def test_sensor_records_and_carried_overlap_state():
 
 
 def test_set_layer():
-    state, _, _ = W.stage([(1, soft().add(bubble(1, 10, 10)).add(W.SensorDescriptor(5, Circle(3.0), (0, 0))))],
+    state, _, _ = W.stage([(1, soft().add(bubble(1, 10, 10)).add(W.SensorDescriptor(5, Circle(3.0), (10, 50))))],
                           W._State(), REGION)
     layered, rec, _ = W.stage([(2, WorldTransaction().set_layer(1, 7))], state, REGION)
     assert rec and layered.bubbles[1].desc.layer == 7 and state.bubbles[1].desc.layer == 0
