@@ -82,8 +82,15 @@ class RegionExitPolicy(Enum):
 
 
 class EventInterest(Enum):
+    """The events an object asks for (EventInterest, Model/Identifiers.swift:27-41); none by default. Sensors report
+    entries and exits through their own `reports_enter` / `reports_exit`."""
     CONTACT = "contact"
     DRIVE_BLOCKED = "driveBlocked"
+    DID_EXIT_SIMULATION_REGION = "didExitSimulationRegion"
+    DID_WRAP = "didWrap"
+    DID_ADD = "didAdd"
+    DID_REMOVE = "didRemove"
+    DID_REPLACE = "didReplace"
 
 
 @dataclass(frozen=True)
@@ -201,6 +208,7 @@ class ForceFieldDescriptor:
     strength: float = 0.0
     falloff: float = 0.0
     filter: "ObjectFilter" = None
+    event_interest: frozenset = frozenset()
 
 
 @dataclass(frozen=True)
@@ -284,6 +292,7 @@ class SensorDescriptor:
     filter: ObjectFilter = ObjectFilter()
     reports_enter: bool = True
     reports_exit: bool = True
+    event_interest: frozenset = frozenset()  # didAdd / didRemove / didReplace of the sensor itself
 
 
 @dataclass(frozen=True)
@@ -297,6 +306,7 @@ class WorldConfiguration:
     gravity: tuple = (0.0, 0.0)              # acceleration on force-driven bubbles (0: the reference's behaviour)
     candidate_limit: int = 128
     substep_split_multiplier: float = 1.0    # NativeMetalConfiguration.substepSplitMultiplier
+    event_buffer_capacity: int = 1024        # WorldConfiguration.eventBufferCapacity: step events per step
     contours: bool = True                    # publish the contours' effective radius and bounds with each bubble
     automatic_pause: bool = True             # WorldConfiguration.automaticPause: pause in the background
     max_contour_segment_length: float = 8.0  # ReferenceConfiguration.maxContourSegmentLength
@@ -308,6 +318,8 @@ class WorldConfiguration:
             raise ValueError("fixedTimeStep must be finite and positive")
         if not (math.isfinite(self.maximum_backlog) and self.maximum_backlog > 0):
             raise ValueError("maximumBacklog must be finite and positive")
+        if not self.event_buffer_capacity > 0:
+            raise ValueError("eventBufferCapacity must be positive")
 
 
 class TransactionRejectionReason(Enum):
@@ -368,6 +380,12 @@ class WorldEvent:
 
 
 @dataclass(frozen=True)
+class WorldEventOverflow:
+    """The step events that did not fit the event buffer (WorldEventOverflow)."""
+    dropped_count: int = 0
+
+
+@dataclass(frozen=True)
 class WorldFrame:
     step_index: int = 0
     simulation_time: float = 0.0
@@ -375,6 +393,7 @@ class WorldFrame:
     events: tuple = ()
     objects: dict = field(default_factory=dict)
     drive_feedback: tuple = ()                   # DriveFeedback of every active player drive, ascending by id
+    event_overflow: WorldEventOverflow = WorldEventOverflow()
 
 
 class WorldFailureReason(Enum):
@@ -1017,7 +1036,10 @@ def stage(pending: list, state: _State, region) -> tuple[_State, list, list]:
         trial = current.copy()
         created, removed, replaced_ids = [], [], []
         rejection = None
+        tx_events = []
         for index, op in enumerate(tx.operations):
+            # the events of an operation follow the interests of the objects it touches, in operation order
+            before = _interest_of(trial, op[1]) if op[0] in ("remove", "replace") else frozenset()
             reason, touched = _apply(op, trial, region)
             if reason is not None:
                 detail = op[0]
@@ -1028,6 +1050,11 @@ def stage(pending: list, state: _State, region) -> tuple[_State, list, list]:
             created += touched["created"]
             removed += touched["removed"]
             replaced_ids += touched["replaced"]
+            tx_events += [WorldEvent("didAdd", (i,)) for i in touched["created"]
+                          if EventInterest.DID_ADD in _interest_of(trial, i)]
+            tx_events += [WorldEvent("didRemove", (i,)) for i in touched["removed"] if EventInterest.DID_REMOVE in before]
+            tx_events += [WorldEvent("didReplace", (i,)) for i in touched["replaced"]
+                          if EventInterest.DID_REPLACE in before or EventInterest.DID_REPLACE in _interest_of(trial, i)]
         if rejection is None and tx.operations and any(b.desc.motion_role in DYNAMIC_ROLES for b in trial.bodies.values()):
             # judged on the state after the whole transaction, reported at its last operation
             # (NativeCompleteStepper.validate; the rigid solver for worlds of dynamic bodies alone is not built here)
@@ -1039,10 +1066,18 @@ def stage(pending: list, state: _State, region) -> tuple[_State, list, list]:
             continue
         current = trial
         receipts.append(TransactionReceipt(token, tuple(created), tuple(removed), tuple(replaced_ids)))
-        events += [WorldEvent("didAdd", (i,)) for i in created]
-        events += [WorldEvent("didRemove", (i,)) for i in removed]
-        events += [WorldEvent("didReplace", (i,)) for i in replaced_ids]
+        events += tx_events
     return current, receipts, events
+
+
+def _interest_of(state: _State, oid) -> frozenset:
+    for table in (state.bubbles, state.bodies):
+        if oid in table:
+            return table[oid].desc.event_interest
+    for table in (state.sensors, state.fields):
+        if oid in table:
+            return table[oid].event_interest
+    return frozenset()
 
 
 def _pair_key(a: int, b: int) -> tuple:
@@ -1444,6 +1479,7 @@ class BubbleWorld:
         self._native_order: list = []
         self._segment_owner: dict = {}
         self._history: set = set()
+        self._events_dropped = 0  # step events beyond the event buffer in the current advance
         self._sensor_pairs: set = set()   # (sensor id, bubble id) pairs overlapping after the last step
         self._shapes: dict = {}           # bubble id -> (effective radius, bounds) of the last contours
         self._index: QueryIndex | None = None  # built at the first query after a publication
@@ -1523,6 +1559,7 @@ class BubbleWorld:
             d.last_advance_issue = AdvanceIssue.TIME_ACCUMULATOR_OVERFLOW
             return self._frame
         receipts, events = [], []
+        self._events_dropped = 0
         while d.steps_in_last_advance < clock.maximum_steps_per_advance and clock.can_step:
             if not self._step(receipts, events):
                 d.last_advance_issue = AdvanceIssue.WORLD_FAILED if d.failure_reason is not None else \
@@ -1532,7 +1569,7 @@ class BubbleWorld:
             clock.complete_step()
             d.steps_in_last_advance += 1
             self._frame = WorldFrame(clock.completed_steps, clock.simulation_time, tuple(receipts), tuple(events),
-                                     self._objects(), self._feedback)
+                                     self._objects(), self._feedback, WorldEventOverflow(self._events_dropped))
             self._index = None
         clock.finish_advance()
         d.backlog_seconds = clock.backlog_seconds
@@ -1716,6 +1753,7 @@ class BubbleWorld:
         taken = len(self._pending)
         handed = list(self._hit_tests)  # the points this step answers; later requests wait for the next one
         staged, rec, ev = stage(self._pending[:taken], self._state, cfg.simulation_region)
+        staged_events = len(ev)  # the stager's events; what the step adds below shares the event buffer
         _drop_transitions_of(staged, {i for r in rec for i in r.removed_object_ids})
         if staged.transitions and staged is self._state:
             staged = staged.copy()
@@ -1771,10 +1809,12 @@ class BubbleWorld:
                 bub.velocity = out[i]["velocity"].astype(np.float32).copy()
                 bub.rotation = float(out[i]["rotation"])
                 bub.angular_velocity = float(out[i]["angular_velocity"])
+                interest = bub.desc.event_interest
                 if out[i]["region_result"] == 1:
                     removed_now.add(oid)
-                    ev.append(WorldEvent("didExitSimulationRegion", (oid,)))
-                elif out[i]["region_result"] == 2:
+                    if EventInterest.DID_EXIT_SIMULATION_REGION in interest:
+                        ev.append(WorldEvent("didExitSimulationRegion", (oid,)))
+                elif out[i]["region_result"] == 2 and EventInterest.DID_WRAP in interest:
                     ev.append(WorldEvent("didWrap", (oid,)))
             for oid in removed_now:
                 staged.bubbles.pop(oid)
@@ -1825,7 +1865,18 @@ class BubbleWorld:
         self._state = staged
         del self._pending[:taken]
         receipts += rec
-        events += ev + contact_events
+        # the step's events fill the event buffer in order; the rest are counted as dropped (EventCompactor.finish):
+        # a dropped contactEnded keeps its pair for the next step, a dropped contactBegan leaves it out of the history
+        # so the pair begins again while it lasts
+        step_events = ev[staged_events:] + contact_events
+        kept, dropped = step_events[:cfg.event_buffer_capacity], step_events[cfg.event_buffer_capacity:]
+        for e in dropped:
+            if e.kind == "contactBegan":
+                self._history.discard(e.objects)
+            elif e.kind == "contactEnded" and not (e.objects[0] in gone and e.objects[1] in gone):
+                self._history.add(e.objects)
+        self._events_dropped += len(dropped)
+        events += ev[:staged_events] + kept
         if handed:
             answers = [self._host_hit(r.point) for r in handed]  # no device world: bodies only, exact shapes
             if self._native is not None:

@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 from bubblephysics_gb300 import world as W
-from bubblephysics_gb300.world import (BubbleDescriptor, BubbleWorld, ParameterTransition,
+from bubblephysics_gb300.world import (BubbleDescriptor, BubbleWorld, EventInterest, ParameterTransition,
                                        PhysicsMaterial, Polygon, RigidBodyDescriptor, WorldConfiguration,
                                        WorldTransaction, TransactionRejectionReason)
 from test_world_api_oracle_cpu import OracleBackedWorld
@@ -24,6 +24,7 @@ AREA = 360.0 * 640.0                  # CrowdScene.interiorArea
 STEP = 1.0 / 60                       # CrowdScene.step
 FRAME_TOLERANCE = 1e-3                # CrowdScene.frameTolerance
 LAST_SECOND = 60                      # CrowdScene.lastSecondSteps
+INTEREST = frozenset({EventInterest.DID_ADD, EventInterest.DID_EXIT_SIMULATION_REGION})  # CrowdScene.bubble
 
 
 @pytest.fixture(autouse=True)
@@ -72,7 +73,8 @@ def run_crowd(world, target, seed=2500, extra_steps=600, maximum_steps=8000):
                 lx, ly = (float(np.float32(h) - np.float32(initial)) for h in HALF)
                 point = (float(np.float32(rng.uniform(-lx, lx))), float(np.float32(rng.uniform(-ly, ly))))
                 mass = float(np.float32(radius) * np.float32(radius) / np.float32(400))
-                tx = WorldTransaction().add(BubbleDescriptor(next_id, point, initial, mass, "bubble"))
+                tx = WorldTransaction().add(BubbleDescriptor(next_id, point, initial, mass, "bubble",
+                                                             event_interest=INTEREST))
                 tx = tx.start_transition(ParameterTransition(("bubbleRadius", next_id), radius, 1.0))
                 pending = (world.submit(tx), next_id, radius)
             else:

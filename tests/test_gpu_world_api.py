@@ -64,7 +64,8 @@ def test_transactions_apply_at_the_step_boundary(ctx):
     frame = world.advance(1.0 / 60)
     assert [r.token for r in frame.transaction_receipts] == [token]
     assert 2 not in frame.objects and frame.objects[1].velocity != before
-    assert any(e.kind == "didRemove" and e.objects == (2,) for e in frame.events)
+    assert frame.transaction_receipts[0].removed_object_ids == (2,)
+    assert not any(e.kind == "didRemove" for e in frame.events)  # bubble 2 asked for no lifecycle events
 
 
 def test_contact_events_begin_and_end(ctx):
@@ -85,7 +86,8 @@ def test_contact_events_begin_and_end(ctx):
 def test_region_exit_removes_the_bubble(ctx):
     world = BubbleWorld(WorldConfiguration(REGION), ctx)
     tx = WorldTransaction().update_physics_material("soft", PhysicsMaterial(229.0))
-    tx = tx.add(BubbleDescriptor(1, (390.0, 200.0), 5.0, 1.0, "soft", velocity=(900.0, 0.0)))
+    tx = tx.add(BubbleDescriptor(1, (390.0, 200.0), 5.0, 1.0, "soft", velocity=(900.0, 0.0),
+                                 event_interest=frozenset({EventInterest.DID_EXIT_SIMULATION_REGION})))
     tx = tx.add(BubbleDescriptor(2, (100.0, 200.0), 5.0, 1.0, "soft"))
     world.submit(tx)
     events = []

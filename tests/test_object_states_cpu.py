@@ -9,7 +9,8 @@ import numpy as np
 import pytest
 
 from bubblephysics_gb300 import world as W
-from bubblephysics_gb300.world import (BubbleDescriptor, BubbleWorld, PhysicsMaterial, Polygon, RegionExitPolicy,
+from bubblephysics_gb300.world import (BubbleDescriptor, BubbleWorld, EventInterest, PhysicsMaterial, Polygon,
+                                       RegionExitPolicy,
                                        RigidBodyDescriptor, WorldConfiguration, WorldTransaction)
 from test_world_api_oracle_cpu import OracleBackedWorld
 
@@ -79,7 +80,8 @@ def test_a_removed_object_is_absent_from_that_frame():
 def test_a_wrapped_bubbles_bounds_move_with_its_contour():
     w, tx = small_world()
     w.submit(tx.add(BubbleDescriptor(1, (190.0, 100.0), 8.0, 1.0, "b", velocity=(900.0, 0.0),
-                                     region_exit_policy=RegionExitPolicy.WRAP)))
+                                     region_exit_policy=RegionExitPolicy.WRAP,
+                                     event_interest=frozenset({EventInterest.DID_WRAP}))))
     wrapped = False
     for _ in range(20):
         frame = w.advance(1.0 / 60)

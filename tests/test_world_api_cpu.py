@@ -7,7 +7,7 @@ import pytest
 
 from bubblephysics_gb300 import _native as N
 from bubblephysics_gb300 import world as W
-from bubblephysics_gb300.world import (BubbleDescriptor, BubbleWorld, Circle, MotionRole,
+from bubblephysics_gb300.world import (BubbleDescriptor, BubbleWorld, Circle, EventInterest, MotionRole,
                                        PhysicsMaterial, RigidBodyDescriptor, TransactionRejectionReason as R,
                                        WorldConfiguration, WorldTransaction)
 
@@ -47,12 +47,14 @@ def test_rejections_are_atomic(tx, reason):
 
 
 def test_staging_applies_transactions_in_order_against_the_staged_state():
-    txs = [(1, soft().add(bubble(1, 10, 10)).add(bubble(2, 50, 50))),
-           (2, WorldTransaction().remove(2).apply_impulse(1, (3.0, 0.0))),
+    told = frozenset({EventInterest.DID_ADD, EventInterest.DID_REMOVE})  # lifecycle events follow the interests
+    txs = [(1, soft().add(bubble(1, 10, 10, event_interest=told)).add(bubble(2, 50, 50, event_interest=told))
+            .add(bubble(3, 90, 90))),
+           (2, WorldTransaction().remove(2).apply_impulse(1, (3.0, 0.0)).remove(3)),
            (3, WorldTransaction().remove(2))]
     state, receipts, events = W.stage(txs, W._State(), REGION)
     assert [r.token for r in receipts] == [1, 2]
-    assert receipts[0].created_object_ids == (1, 2) and receipts[1].removed_object_ids == (2,)
+    assert receipts[0].created_object_ids == (1, 2, 3) and receipts[1].removed_object_ids == (2, 3)
     assert sorted(state.bubbles) == [1]
     assert np.array_equal(state.bubbles[1].velocity, np.array([3.0, 0.0], np.float32))
     kinds = [e.kind for e in events]
