@@ -1,6 +1,6 @@
 """The candidate limit's margin on the stress-300 scene, through the world API on a stand-in device world that
 forwards to the oracle, against ContactCandidateMarginTests.swift:11-25: over 300 steps no object overflows its k = 128
-candidates and the largest count seen stays at most half of k. The scene restates Stress300Scene
+candidates and the largest count seen stays at most half of k, on stress-300 and on the mixed scene. The stress-300 scene restates Stress300Scene
 (PublicWorldStressBenchmark.swift:681-827): a 375 x 700 region framed by four 1-unit static walls, 300 grid slots of
 15 columns (spacing 23 x 33.5) jittered by the scene's linear congruential generator (Knuth's MMIX constants, seed
 0x2B60F5), radius 12.42 (0.78 + 0.44 u), mass max(1, 0.02 r^2), K_c 229, less the slots under the start of a kinematic
@@ -11,8 +11,8 @@ import numpy as np
 import pytest
 
 from bubblephysics_gb300 import world as W
-from bubblephysics_gb300.world import (BubbleDescriptor, BubbleWorld, KinematicDrive, MotionRole, PathDrive,
-                                       PhysicsMaterial, Polygon, RigidBodyDescriptor, WorldConfiguration,
+from bubblephysics_gb300.world import (BubbleDescriptor, BubbleWorld, Capsule, Circle, KinematicDrive, MotionRole,
+                                       PathDrive, PhysicsMaterial, Polygon, RigidBodyDescriptor, WorldConfiguration,
                                        WorldTransaction)
 from test_world_api_oracle_cpu import OracleBackedWorld
 
@@ -93,3 +93,65 @@ def test_stress300_keeps_the_candidate_limit_with_a_twofold_margin():
         assert world.diagnostics.contact_candidate_overflow == 0, step
     assert 0 < maximum and maximum * 2 <= 128, maximum
     assert math.hypot(*(np.asarray(world.last_frame.objects[10_000].position) - WAYPOINTS[0])) > 1  # the triangle drove
+
+
+def mixed():
+    """MixedScene (PublicWorldStressBenchmark.swift:982-1088): 200 bubbles on a 20-column grid in the lower band, 55
+    kinematic bodies spinning in place on an 11 x 5 grid (rectangle, circle, capsule, triangle in turn, scaled
+    0.8-1.2), 5 kinematic bars sliding at 80 units/s and turning every 150 steps, and four 1-unit walls."""
+    rng = Lcg(0x4D1C5E)
+    spacing, body_spacing = np.float32(345.0) / np.float32(20), np.float32(345.0) / np.float32(11)
+    tx = WorldTransaction().update_physics_material(1, PhysicsMaterial(229.0))
+    for index in range(200):
+        radius = spacing * np.float32(0.4) * (np.float32(0.78) + rng.unit() * np.float32(0.44))
+        p = (float(15 + (np.float32(index % 20) + np.float32(0.5)) * spacing),
+             float(15 + (np.float32(index // 20) + np.float32(0.5)) * spacing))
+        tx = tx.add(BubbleDescriptor(index + 1, p, float(radius), max(1.0, float(radius * radius * np.float32(0.02))), 1))
+    for index in range(55):
+        scale = np.float32(0.8) + rng.unit() * np.float32(0.4)
+        rng.unit(), rng.unit()  # two draws of a linear velocity the scene no longer uses
+        spin = float((rng.unit() - np.float32(0.5)) * np.float32(6))
+        p = (float(15 + (np.float32(index % 11) + np.float32(0.5)) * body_spacing),
+             (450.0, 500.0, 550.0, 600.0, 650.0)[index // 11])
+        s = float(scale)
+        shape = (Polygon(((-9 * s, -6 * s), (9 * s, -6 * s), (9 * s, 6 * s), (-9 * s, 6 * s))), Circle(8 * s),
+                 Capsule(6 * s, 5 * s), Polygon(((-9 * s, 7 * s), (9 * s, 7 * s), (0.0, -9 * s))))[index % 4]
+        tx = tx.add(RigidBodyDescriptor(1001 + index, shape, p, motion_role=MotionRole.KINEMATIC))
+        tx = tx.set_kinematic_drive(1001 + index, KinematicDrive.velocity((0.0, 0.0), spin))
+    for index, y in enumerate((210.0, 260.0, 310.0, 360.0, 410.0)):
+        tx = tx.add(RigidBodyDescriptor(2001 + index, Polygon(((-30.0, -4.0), (30.0, -4.0), (30.0, 4.0), (-30.0, 4.0))),
+                                        (100.0, y), motion_role=MotionRole.KINEMATIC))
+        tx = tx.set_kinematic_drive(2001 + index, KinematicDrive.velocity((80.0, 0.0), 0.0))
+    for k, pts in enumerate((((0, 0), (1, 0), (1, HEIGHT), (0, HEIGHT)),
+                             ((374, 0), (375, 0), (375, HEIGHT), (374, HEIGHT)),
+                             ((0, 0), (375, 0), (375, 1), (0, 1)),
+                             ((0, HEIGHT - 1), (375, HEIGHT - 1), (375, HEIGHT), (0, HEIGHT)))):
+        tx = tx.add(RigidBodyDescriptor(10_001 + k, Polygon(tuple((float(x), float(y)) for x, y in pts)), (0.0, 0.0)))
+    return tx
+
+
+def mixed_step(step):
+    if step == 0 or step % 150:
+        return None
+    direction = 1.0 if (step // 150) % 2 == 0 else -1.0
+    tx = WorldTransaction()
+    for index in range(5):
+        tx = tx.set_kinematic_drive(2001 + index, KinematicDrive.velocity((direction * 80.0, 0.0), 0.0))
+    return tx
+
+
+def test_the_mixed_scene_keeps_the_candidate_limit_with_a_twofold_margin():
+    """ContactCandidateMarginTests.swift:27-47: body rows are candidates too."""
+    world = BubbleWorld(WorldConfiguration((0.0, 0.0, 375.0, HEIGHT), contours=False))
+    world.submit(mixed())
+    maximum = 0
+    for step in range(300):
+        tx = mixed_step(step)
+        if tx is not None:
+            world.submit(tx)
+        frame = world.advance(1.0 / 60)
+        assert world.diagnostics.last_advance_issue is None, step
+        maximum = max(maximum, world.diagnostics.maximum_contact_candidates_per_object)
+        assert world.diagnostics.contact_candidate_overflow == 0, step
+    assert len(frame.objects) == 264  # 200 bubbles, 60 bodies and 4 walls
+    assert 0 < maximum and maximum * 2 <= 128, maximum
