@@ -44,7 +44,10 @@ class CollisionFilter:
     mask: int = 0xFFFFFFFF
 
     def accepts(self, other: "CollisionFilter") -> bool:
+        """Two objects collide when each one's category is in the other's mask (CollisionFilter.collides(with:))."""
         return bool(self.category & other.mask) and bool(other.category & self.mask)
+
+    collides_with = accepts
 
 
 @dataclass(frozen=True)
