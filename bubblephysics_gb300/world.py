@@ -324,6 +324,13 @@ class WorldConfiguration:
         if not self.event_buffer_capacity > 0:
             raise ValueError("eventBufferCapacity must be positive")
 
+    def sanitized(self) -> "WorldConfiguration":
+        """The solver switches in their ranges (NativeMetalConfiguration.sanitized): k within 1...128, a split multiplier
+        below 1 (or not finite) is 1."""
+        split = self.substep_split_multiplier
+        return replace(self, candidate_limit=min(128, max(1, int(self.candidate_limit))),
+                       substep_split_multiplier=split if math.isfinite(split) and split >= 1 else 1.0)
+
 
 class TransactionRejectionReason(Enum):
     OBJECT_NOT_FOUND = "objectNotFound"
@@ -1655,7 +1662,7 @@ class BubbleWorld:
 
     # -- internals -----------------------------------------------------------------------------------------------------
     def _spec(self, state: _State) -> tuple[WorldSpec, list, dict]:
-        cfg = self.configuration
+        cfg = self.configuration.sanitized()
         ids = sorted(state.bubbles)
         b = np.zeros(len(ids), N.BUBBLE_DTYPE)
         bands, motors = [], []
