@@ -1,7 +1,9 @@
 """Events follow the objects' interests and fit the event buffer, through the world API on a stand-in device world
 that forwards to the oracle: EventInterestTests.swift:5-52 (no contact event without interest, a removed bubble leaves
-its sensor and a re-added one enters again) and the event buffer of EventCompactor.swift:11-37 (step events beyond
-eventBufferCapacity are counted as dropped; a dropped contactEnded comes with the next step)."""
+its sensor and a re-added one enters again), the event buffer of EventCompactor.swift:11-37 (step events beyond
+eventBufferCapacity are counted as dropped; a dropped contactEnded comes with the next step) and
+NativeMetalEventCompactionTests.swift:93-191 (overflow reported, removed pairs' exits within the buffer, a wrap event
+needs interest, a polygon sensor ignores distant collinear edges)."""
 import pytest
 
 from bubblephysics_gb300 import world as W
@@ -75,3 +77,58 @@ def test_step_events_beyond_the_buffer_are_dropped_and_a_dropped_end_comes_next_
     assert dropped > 0
     assert sorted(set(began)) == [(10, 20), (11, 21), (12, 22)]
     assert sorted(ended) == [(10, 20), (11, 21), (12, 22)]  # each end delivered once, late or not
+
+
+def sensor_world(capacity=1024, region=(-20.0, -20.0, 20.0, 20.0), step=STEP):
+    world = BubbleWorld(WorldConfiguration(region, fixed_time_step=step, event_buffer_capacity=capacity))
+    world.submit(WorldTransaction().update_physics_material(1, PhysicsMaterial(1e9)))
+    return world
+
+
+def test_event_buffer_overflow_is_reported_instead_of_silently_dropped():
+    """NativeMetalEventCompactionTests.swift:113-121: two bubbles enter a sensor with room for one event."""
+    world = sensor_world(capacity=1)
+    world.submit(WorldTransaction().add(BubbleDescriptor(1, (-1.0, 0.0), 1.0, 1.0, 1))
+                 .add(BubbleDescriptor(2, (1.0, 0.0), 1.0, 1.0, 1))
+                 .add(SensorDescriptor(9, Circle(3.0), (0.0, 0.0), reports_exit=False)))
+    frame = world.advance(STEP)
+    assert len(frame.events) == 1 and frame.event_overflow.dropped_count == 1
+
+
+def test_the_exits_of_removed_pairs_respect_the_event_buffer():
+    """NativeMetalEventCompactionTests.swift:93-111: both observed bubbles go at once with room for one event; the
+    lost exit is counted and not delivered later."""
+    from dataclasses import replace
+    world = sensor_world(capacity=2)
+    world.submit(WorldTransaction().add(BubbleDescriptor(1, (-1.0, 0.0), 1.0, 1.0, 1))
+                 .add(BubbleDescriptor(2, (1.0, 0.0), 1.0, 1.0, 1)).add(SensorDescriptor(9, Circle(3.0), (0.0, 0.0))))
+    world.advance(STEP)
+    world.configuration = replace(world.configuration, event_buffer_capacity=1)
+    world.submit(WorldTransaction().remove(1).remove(2))
+    removed = world.advance(STEP)
+    assert [e.kind for e in removed.events] == ["exitedSensor"] and removed.events[0].objects[0] == 9
+    assert removed.event_overflow.dropped_count == 1
+    cleared = world.advance(STEP)
+    assert not cleared.events and cleared.event_overflow.dropped_count == 0
+
+
+def test_a_wrap_event_needs_interest():
+    """NativeMetalEventCompactionTests.swift:168-176: one step of 0.25 s takes the bubble across the region's edge."""
+    world = sensor_world(region=(0.0, 0.0, 10.0, 10.0), step=0.25)
+    world.submit(WorldTransaction().add(BubbleDescriptor(1, (9.0, 5.0), 1.0, 1.0, 1, velocity=(20.0, 0.0),
+                                                         region_exit_policy=W.RegionExitPolicy.WRAP,
+                                                         event_interest=frozenset({EventInterest.DID_WRAP}))))
+    assert [(e.kind, e.objects) for e in world.advance(0.25).events] == [("didWrap", (1,))]
+
+
+def test_a_polygon_sensor_ignores_distant_collinear_edges():
+    """NativeMetalEventCompactionTests.swift:178-191: a triangle whose base lies on the line of the sensor's lower
+    edge, 5 units beyond its corner, does not enter it."""
+    from bubblephysics_gb300.world import Polygon, RigidBodyDescriptor
+    world = sensor_world()
+    world.submit(WorldTransaction()
+                 .add(SensorDescriptor(9, Polygon(((-2.0, -2.0), (2.0, -2.0), (2.0, 2.0), (-2.0, 2.0))), (0.0, 0.0),
+                                       reports_exit=False))
+                 .add(RigidBodyDescriptor(3, Polygon(((-0.5, -2.0), (0.5, -2.0), (0.0, -1.0))), (7.0, 0.0)))
+                 .add(BubbleDescriptor(1, (-15.0, 15.0), 1.0, 1.0, 1)))
+    assert not world.advance(STEP).events
