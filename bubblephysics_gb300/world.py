@@ -119,12 +119,24 @@ class BubbleDrivePolicy:
     band_stiffness: float
     maximum_force: float | None = None
 
+    def __post_init__(self):  # Model/Motion.swift:15-21
+        if not (math.isfinite(self.band_stiffness) and self.band_stiffness > 0):
+            raise ValueError("drive.bandStiffness out of range")
+        if self.maximum_force is not None and not (math.isfinite(self.maximum_force) and self.maximum_force > 0):
+            raise ValueError("drive.maximumForce out of range")
+
 
 @dataclass(frozen=True)
 class MotorDrive:
     """A constant force and torque on a motor-driven bubble (MotorDrive)."""
     force: tuple = (0.0, 0.0)
     torque: float = 0.0
+
+    def __post_init__(self):  # Model/Motion.swift:41-43
+        if not all(math.isfinite(float(v)) for v in self.force):
+            raise ValueError("motor.force must be finite")
+        if not math.isfinite(float(self.torque)):
+            raise ValueError("motor.torque must be finite")
 
 
 @dataclass(frozen=True)
