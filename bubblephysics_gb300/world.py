@@ -277,7 +277,79 @@ class Capsule:
 
 @dataclass(frozen=True)
 class Polygon:
-    points: tuple  # convex, local to the centre of mass, counter-clockwise
+    """A simple polygon (PolygonGeometry, Model/Objects.swift:18-73), local to the object's position, in either
+    orientation, convex or not: a repeated first vertex at the end is dropped; fewer than three vertices, a zero-length
+    or doubling-back edge, edges that cross or touch and a zero area are refused, all in double."""
+    points: tuple
+
+    def __post_init__(self):
+        ring = [(float(np.float32(x)), float(np.float32(y))) for x, y in self.points]
+        if not all(math.isfinite(v) for p in ring for v in p):
+            raise ValueError("polygon.vertex must be finite")
+        if len(ring) > 1 and ring[0] == ring[-1]:
+            ring.pop()
+        if len(ring) < 3:
+            raise ValueError("a polygon needs three vertices")
+        n = len(ring)
+        for i in range(n):
+            a, b, c = ring[i], ring[(i + 1) % n], ring[(i + 2) % n]
+            if a == b:
+                raise ValueError("degenerate polygon: a zero-length edge")
+            if _cross3(a, b, c) == 0 and (b[0] - a[0]) * (c[0] - b[0]) + (b[1] - a[1]) * (c[1] - b[1]) < 0:
+                raise ValueError("degenerate polygon: an edge doubles back")
+            for j in range(i + 2, n):
+                if i == 0 and j == n - 1:
+                    continue
+                if _segments_touch(a, b, ring[j], ring[(j + 1) % n]):
+                    raise ValueError("self-intersecting polygon")
+        if sum(_cross3(ring[0], ring[k], ring[k + 1]) for k in range(1, n - 1)) == 0:
+            raise ValueError("degenerate polygon: zero area")
+        object.__setattr__(self, "points", tuple(ring))
+
+
+def _cross3(a, b, c) -> float:
+    return (b[0] - a[0]) * (c[1] - a[1]) - (b[1] - a[1]) * (c[0] - a[0])
+
+
+def _segments_touch(a, b, c, d) -> bool:
+    """Whether segments ab and cd share a point (crossing, touching or overlapping), in double."""
+    def within(p, u, v):
+        return min(u[0], v[0]) <= p[0] <= max(u[0], v[0]) and min(u[1], v[1]) <= p[1] <= max(u[1], v[1])
+    abc, abd, cda, cdb = _cross3(a, b, c), _cross3(a, b, d), _cross3(c, d, a), _cross3(c, d, b)
+    if (abc == 0 and within(c, a, b)) or (abd == 0 and within(d, a, b)) or \
+            (cda == 0 and within(a, c, d)) or (cdb == 0 and within(b, c, d)):
+        return True
+    return ((abc > 0 > abd) or (abc < 0 < abd)) and ((cda > 0 > cdb) or (cda < 0 < cdb))
+
+
+def polygon_triangles(points) -> tuple[np.ndarray, np.ndarray]:
+    """A polygon body's device vertices (counter-clockwise, as the device's inside test and edge normals take them)
+    and triangles: a fan when the polygon is convex, ear clipping otherwise."""
+    local = np.asarray(points, np.float32)
+    twice = sum(_cross3(local[0], local[k], local[k + 1]) for k in range(1, len(local) - 1))
+    if twice < 0:
+        local = local[::-1].copy()
+    n = len(local)
+    if all(_cross3(local[k], local[(k + 1) % n], local[(k + 2) % n]) >= 0 for k in range(n)):
+        return local, np.array([[0, k, k + 1] for k in range(1, n - 1)], np.uint32)
+    left, tris = list(range(n)), []
+    while len(left) > 3:
+        for k in range(len(left)):
+            i, j, m = left[k - 1], left[k], left[(k + 1) % len(left)]
+            if _cross3(local[i], local[j], local[m]) <= 0:
+                continue
+            others = [q for q in left if q not in (i, j, m)]
+            if any(_cross3(local[i], local[j], local[q]) >= 0 and _cross3(local[j], local[m], local[q]) >= 0 and
+                   _cross3(local[m], local[i], local[q]) >= 0 for q in others):
+                continue
+            tris.append([i, j, m])
+            left.pop(k)
+            break
+        else:
+            break  # only collinear vertices are left
+    if len(left) == 3:
+        tris.append(left)
+    return local, np.array(tris, np.uint32).reshape(-1, 3)
 
 
 @dataclass(frozen=True)
@@ -1750,8 +1822,7 @@ class BubbleWorld:
                 local = np.array([[-shape.half_length, 0.0], [shape.half_length, 0.0]], np.float32)
                 tri = np.zeros((0, 3), np.uint32)
             else:
-                local = np.asarray(shape.points, np.float32)
-                tri = np.array([[0, i, i + 1] for i in range(1, len(local) - 1)], np.uint32)
+                local, tri = polygon_triangles(shape.points)
                 rec["kind"] = N.BODY_POLYGON
                 rec["bounding_radius"] = float(np.sqrt((local.astype(np.float64) ** 2).sum(1)).max())
             rec["vertex_count"], rec["triangle_count"] = len(local), len(tri)

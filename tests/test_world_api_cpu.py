@@ -134,8 +134,9 @@ def test_sensors_stage_like_objects():
     sensor = W.SensorDescriptor(50, Circle(20.0), (100.0, 100.0))
     state, receipts, _ = W.stage([(1, soft().add(sensor).add(bubble(1, 100, 100)))], W._State(), REGION)
     assert receipts[0].created_object_ids == (50, 1) and state.sensors[50] == sensor  # a sensor overlaps freely
-    for bad in (W.SensorDescriptor(51, Circle(0.0), (0, 0)), W.SensorDescriptor(51, W.Polygon(((0, 0), (1, 0))), (0, 0)),
-                W.SensorDescriptor(51, Circle(5.0), (float("nan"), 0))):
+    with pytest.raises(ValueError):  # a two-point polygon is refused when it is made
+        W.Polygon(((0, 0), (1, 0)))
+    for bad in (W.SensorDescriptor(51, Circle(0.0), (0, 0)), W.SensorDescriptor(51, Circle(5.0), (float("nan"), 0))):
         _, rec, ev = W.stage([(2, WorldTransaction().add(bad))], state, REGION)
         assert rec == [] and ev[0].rejection.reason == R.INVALID_VALUE
     _, _, ev = W.stage([(3, WorldTransaction().add(W.SensorDescriptor(1, Circle(5.0), (0, 0))))], state, REGION)
