@@ -111,6 +111,14 @@ class BubbleDescriptor:
     layer: int = 0
     drive_policy: "BubbleDrivePolicy | None" = None
 
+    def __post_init__(self):  # BubbleDescriptor.init, Model/Objects.swift:133-160
+        if not all(math.isfinite(float(v)) for v in (*self.position, *self.velocity)):
+            raise ValueError("bubble position and velocity must be finite")
+        if not (math.isfinite(self.radius) and self.radius > 0):
+            raise ValueError("bubble.targetRadius must be finite and positive")
+        if not (math.isfinite(self.mass) and self.mass > 0):
+            raise ValueError("bubble.mass must be finite and positive")
+
 
 @dataclass(frozen=True)
 class BubbleDrivePolicy:
@@ -268,11 +276,19 @@ def transition_curve(curve, t):
 class Circle:
     radius: float
 
+    def __post_init__(self):  # RangeGeometry.circle / RigidShape.circle: a finite, positive radius
+        if not (math.isfinite(self.radius) and self.radius > 0):
+            raise ValueError("circle.radius must be finite and positive")
+
 
 @dataclass(frozen=True)
 class Capsule:
     half_length: float
     radius: float
+
+    def __post_init__(self):
+        if not (math.isfinite(self.half_length) and self.half_length > 0 and math.isfinite(self.radius) and self.radius > 0):
+            raise ValueError("capsule.halfLength and capsule.radius must be finite and positive")
 
 
 @dataclass(frozen=True)

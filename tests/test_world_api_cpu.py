@@ -35,7 +35,8 @@ def test_transaction_builder_returns_copies_in_order():
     (soft().add(bubble(1, 500, 10)), R.INVALID_PLACEMENT),
     (soft().add(bubble(1, 10, 10)).add(bubble(2, 10, 10)), R.INVALID_PLACEMENT),
     (soft().add(RigidBodyDescriptor(7, Circle(20.0), (100, 100))).add(bubble(1, 105, 100)), R.INVALID_PLACEMENT),
-    (soft().add(BubbleDescriptor(1, (10, 10), -1.0, 1.0, "soft")), R.INVALID_VALUE),
+    (soft().add(BubbleDescriptor(1, (10, 10), 10.0, 1e-3, "soft", drive_policy=W.BubbleDrivePolicy(1000.0))),
+     R.INVALID_VALUE),
     (soft().remove(99), R.OBJECT_NOT_FOUND),
     (soft().add(RigidBodyDescriptor(7, Circle(5.0), (50, 50), motion_role=MotionRole.DYNAMIC)), R.UNSUPPORTED_OPERATION),
     (soft().operation("mergeBubbles", (1, 2)), R.UNSUPPORTED_OPERATION),
@@ -134,9 +135,10 @@ def test_sensors_stage_like_objects():
     sensor = W.SensorDescriptor(50, Circle(20.0), (100.0, 100.0))
     state, receipts, _ = W.stage([(1, soft().add(sensor).add(bubble(1, 100, 100)))], W._State(), REGION)
     assert receipts[0].created_object_ids == (50, 1) and state.sensors[50] == sensor  # a sensor overlaps freely
-    with pytest.raises(ValueError):  # a two-point polygon is refused when it is made
-        W.Polygon(((0, 0), (1, 0)))
-    for bad in (W.SensorDescriptor(51, Circle(0.0), (0, 0)), W.SensorDescriptor(51, Circle(5.0), (float("nan"), 0))):
+    for make in (lambda: W.Polygon(((0, 0), (1, 0))), lambda: Circle(0.0)):  # refused when they are made
+        with pytest.raises(ValueError):
+            make()
+    for bad in (W.SensorDescriptor(51, Circle(5.0), (float("nan"), 0)),):
         _, rec, ev = W.stage([(2, WorldTransaction().add(bad))], state, REGION)
         assert rec == [] and ev[0].rejection.reason == R.INVALID_VALUE
     _, _, ev = W.stage([(3, WorldTransaction().add(W.SensorDescriptor(1, Circle(5.0), (0, 0))))], state, REGION)
@@ -205,3 +207,12 @@ def test_object_states_of_bodies_follow_their_shape_and_rotation():
     for state in frame.objects.values():
         lo, hi = state.bounds[:2], state.bounds[2:]
         assert lo[0] < hi[0] and lo[1] < hi[1] and lo[0] <= state.position[0] <= hi[0]
+
+
+@pytest.mark.parametrize("kwargs", [dict(radius=-1.0), dict(radius=0.0), dict(radius=float("nan")), dict(mass=0.0),
+                                    dict(position=(float("nan"), 0.0)), dict(velocity=(float("inf"), 0.0))])
+def test_a_bubble_with_invalid_values_is_refused_when_it_is_made(kwargs):
+    """ModelValidationTests.swift:113-125: the descriptor checks its own values, as the reference's init throws."""
+    values = dict(position=(0.0, 0.0), radius=1.0, mass=1.0, velocity=(0.0, 0.0)) | kwargs
+    with pytest.raises(ValueError):
+        BubbleDescriptor(1, values["position"], values["radius"], values["mass"], "soft", velocity=values["velocity"])
