@@ -233,6 +233,12 @@ class ForceFieldDescriptor:
     filter: "ObjectFilter" = None
     event_interest: frozenset = frozenset()
 
+    def __post_init__(self):  # ForceFieldDescriptor.init and ForceField's parameters, Model/Objects.swift:321-340
+        if not all(math.isfinite(float(v)) for v in (*self.position, self.angle, *self.force, self.strength)):
+            raise ValueError("field position, rotation and parameters must be finite")
+        if not (math.isfinite(self.falloff) and self.falloff >= 0):
+            raise ValueError("field.falloff must be finite and non-negative")
+
 
 @dataclass(frozen=True)
 class ParameterTransition:
@@ -396,6 +402,10 @@ class SensorDescriptor:
     reports_enter: bool = True
     reports_exit: bool = True
     event_interest: frozenset = frozenset()  # didAdd / didRemove / didReplace of the sensor itself
+
+    def __post_init__(self):
+        if not all(math.isfinite(float(v)) for v in (*self.position, self.angle)):
+            raise ValueError("sensor position and rotation must be finite")
 
 
 @dataclass(frozen=True)

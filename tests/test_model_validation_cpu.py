@@ -88,3 +88,23 @@ def test_a_bubble_rests_in_the_notch_of_a_concave_kinematic_body(monkeypatch):
         frame = world.advance(1.0 / 60)
         assert world.diagnostics.last_advance_issue is None and world.diagnostics.failure_reason is None
     assert len(frame.transaction_receipts) == 0 and 1 in frame.objects
+
+
+def test_fields_and_sensors_validate_their_values_and_stay_in_the_region():
+    """ModelValidationTests.swift:127-144: a radial field is fine; a circle of radius 0, a field force that is not
+    finite, a negative falloff and a sensor at infinity are refused when made; a sensor or field reaching out of the
+    region is refused at staging."""
+    from bubblephysics_gb300.world import ForceFieldDescriptor, SensorDescriptor, TransactionRejectionReason as R, \
+        WorldTransaction
+    ForceFieldDescriptor(3, (0.0, 0.0), "radial", Circle(3.0), strength=-2.0, falloff=1.0)
+    for make in (lambda: Circle(0.0),
+                 lambda: ForceFieldDescriptor(3, (0.0, 0.0), "directional", Circle(3.0), force=(math.nan, 0.0)),
+                 lambda: ForceFieldDescriptor(3, (0.0, 0.0), "vortex", Circle(3.0), strength=1.0, falloff=-1.0),
+                 lambda: SensorDescriptor(4, Circle(3.0), (math.inf, 0.0))):
+        with pytest.raises(ValueError):
+            make()
+    for item in (SensorDescriptor(4, Circle(3.0), (0.0, 0.0)),
+                 ForceFieldDescriptor(3, (0.0, 0.0), "directional", Circle(3.0), force=(1.0, 0.0))):
+        _, receipts, events = W.stage([(1, WorldTransaction().add(item))], W._State(), (-2.0, -2.0, 2.0, 2.0))
+        assert not receipts and (events[0].rejection.reason, events[0].rejection.detail) == (R.INVALID_VALUE,
+                                                                                            W.STATIC_OUTSIDE)

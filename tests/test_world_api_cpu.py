@@ -135,12 +135,10 @@ def test_sensors_stage_like_objects():
     sensor = W.SensorDescriptor(50, Circle(20.0), (100.0, 100.0))
     state, receipts, _ = W.stage([(1, soft().add(sensor).add(bubble(1, 100, 100)))], W._State(), REGION)
     assert receipts[0].created_object_ids == (50, 1) and state.sensors[50] == sensor  # a sensor overlaps freely
-    for make in (lambda: W.Polygon(((0, 0), (1, 0))), lambda: Circle(0.0)):  # refused when they are made
+    for make in (lambda: W.Polygon(((0, 0), (1, 0))), lambda: Circle(0.0),  # refused when they are made
+                 lambda: W.SensorDescriptor(51, Circle(5.0), (float("nan"), 0))):
         with pytest.raises(ValueError):
             make()
-    for bad in (W.SensorDescriptor(51, Circle(5.0), (float("nan"), 0)),):
-        _, rec, ev = W.stage([(2, WorldTransaction().add(bad))], state, REGION)
-        assert rec == [] and ev[0].rejection.reason == R.INVALID_VALUE
     _, _, ev = W.stage([(3, WorldTransaction().add(W.SensorDescriptor(1, Circle(5.0), (0, 0))))], state, REGION)
     assert ev[0].rejection.reason == R.DUPLICATE_OBJECT_ID
     moved = W.SensorDescriptor(50, W.Polygon(((-5, -5), (5, -5), (0, 5))), (30.0, 30.0))
