@@ -387,6 +387,10 @@ class RigidBodyDescriptor:
     event_interest: frozenset = frozenset()
     layer: int = 0
 
+    def __post_init__(self):  # RigidBodyDescriptor.init: a finite pose
+        if not all(math.isfinite(float(v)) for v in (*self.position, self.angle, *self.velocity, self.angular_velocity)):
+            raise ValueError("body position, rotation and velocity must be finite")
+
 
 @dataclass(frozen=True)
 class SensorDescriptor:

@@ -108,3 +108,9 @@ def test_fields_and_sensors_validate_their_values_and_stay_in_the_region():
         _, receipts, events = W.stage([(1, WorldTransaction().add(item))], W._State(), (-2.0, -2.0, 2.0, 2.0))
         assert not receipts and (events[0].rejection.reason, events[0].rejection.detail) == (R.INVALID_VALUE,
                                                                                             W.STATIC_OUTSIDE)
+
+
+def test_a_body_with_a_pose_that_is_not_finite_is_refused_when_made():
+    """ModelValidationTests.swift:124: a polygon body turned by infinity."""
+    with pytest.raises(ValueError):
+        RigidBodyDescriptor(1, Polygon(((0.0, 0.0), (1.0, 0.0), (0.0, 1.0))), (0.0, 0.0), angle=math.inf)
