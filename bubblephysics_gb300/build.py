@@ -17,7 +17,11 @@ PACKAGE_DIR = Path(__file__).resolve().parent
 CSRC = PACKAGE_DIR / "csrc"
 BUILD_DIR = PACKAGE_DIR / "_build"
 LIBRARY = PACKAGE_DIR / "libbubblephysics_gb300.so"
-SOURCES = ["bp_step.cu", "bp_capi.cu", "bp_aux.cu", "bp_server.cu", "bp_contour.cu", "bp_sensor.cu"]
+SOURCES = ["bp_step.cu", "bp_noalloc.cu", "bp_capi.cu", "bp_aux.cu", "bp_server.cu", "bp_contour.cu", "bp_sensor.cu"]
+# bp_step_variant.cu is compiled once per (kernel, block width, tree) variant: the persistent step kernels are the
+# largest functions of the library and compile in parallel this way.
+VARIANT_SOURCE = "bp_step_variant.cu"
+VARIANTS = [(kind, threads, tree) for kind in (0, 1) for threads in (128, 256, 512) for tree in (0, 1)]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
               "-Xcompiler", "-fPIC,-ffp-contract=off", "-diag-suppress", "177"]
@@ -44,12 +48,15 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     headers = sorted(CSRC.glob("*.cuh")) + [PACKAGE_DIR.parent / "include" / "bubblephysics.h"]
     objects = []
     jobs = []
-    for name in SOURCES:
-        src = CSRC / name
-        obj = BUILD_DIR / (name + ".o")
+    units = [(CSRC / name, BUILD_DIR / (name + ".o"), []) for name in SOURCES]
+    for kind, threads, tree in VARIANTS:
+        tag = f"{'served' if kind else 'persistent'}_{threads}_{tree}"
+        units.append((CSRC / VARIANT_SOURCE, BUILD_DIR / f"bp_step_{tag}.o",
+                      [f"-DBP_VARIANT_KIND={kind}", f"-DBP_VARIANT_THREADS={threads}", f"-DBP_VARIANT_TREE={tree}"]))
+    for src, obj, defines in units:
         objects.append(obj)
         if force or _stale(obj, [src] + headers):
-            jobs.append([nvcc, *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)])
+            jobs.append([nvcc, *ARCH, *NVCC_FLAGS, *defines, "-c", str(src), "-o", str(obj)])
 
     def run(cmd):
         result = subprocess.run(cmd, capture_output=True, text=True)
@@ -58,7 +65,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         if result.returncode != 0:
             raise RuntimeError("nvcc failed: " + " ".join(cmd))
 
-    with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as pool:
+    with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 1))) as pool:
         list(pool.map(run, jobs))
     if force or jobs or _stale(LIBRARY, objects):
         tmp = LIBRARY.with_suffix(".so.tmp")
