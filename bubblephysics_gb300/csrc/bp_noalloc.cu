@@ -1,6 +1,4 @@
 // bp_noalloc.cu - the allocation-free single-world step (bp_world_step_noalloc).
-#include <mutex>
-
 #include "bp_step.cuh"
 
 // ==================================================================================================================
@@ -30,13 +28,13 @@ constexpr uint32_t kNaContacts = kNaN * BP_NOALLOC_CONTACTS_PER_BUBBLE + 64u;
 // Carves the scratch layout (all offsets 256-byte aligned) from `base`; with base == 0 it returns the size.
 struct NoAllocLayout {
     size_t bytes = 0;
-    template <class T> T* take(char* base, size_t count) {
+    template <class T> constexpr T* take(char* base, size_t count) {
         size_t off = bytes;
         bytes += (count * sizeof(T) + 255u) & ~(size_t)255u;
         return base ? (T*)(base + off) : nullptr;
     }
     DWorld* world = nullptr;
-    DState make(char* base) {
+    constexpr DState make(char* base) {
         DState S{};
         world = take<DWorld>(base, 1);
         S.worlds = world;
@@ -69,6 +67,13 @@ constexpr size_t noalloc_bytes() {
     // 1024 bubbles: ~0.5 MB of state and rows, 4160 contact records, 256 segments; rounded up generously
     return (size_t)1 << 20;
 }
+
+constexpr size_t noalloc_layout_bytes() {
+    NoAllocLayout layout;
+    layout.make(nullptr);
+    return layout.bytes;
+}
+static_assert(noalloc_layout_bytes() <= noalloc_bytes(), "the scratch layout must fit the fixed device array");
 
 }  // namespace
 
@@ -111,7 +116,18 @@ __global__ void __launch_bounds__(256) noalloc_step_kernel(DState S, DWorld W, b
         d.id = g.id; d.owner = g.owner_id;
         const_cast<DSegment*>(S.seg)[j] = d;
     }
-    __syncthreads();
+    // ids must be strictly ascending (what bp_world_create checks on the host): otherwise nothing is stepped and
+    // every report says BP_E_INVALID
+    uint32_t unsorted = 0u;
+    for (uint32_t i = r + 1; i < n; i += T) unsorted |= bubbles[i - 1].id < bubbles[i].id ? 0u : 1u;
+    if (__syncthreads_or(unsorted)) {
+        for (uint32_t q = r; q < steps; q += T) {
+            bp_step_report invalid{};
+            invalid.status = BP_E_INVALID;
+            reports[q] = invalid;
+        }
+        return;
+    }
     uint32_t* buckets = g_dynamic_smem;
     uint32_t* entries = g_dynamic_smem + B;
     uint32_t* ws = g_dynamic_smem + round4(B + (n ? n : 1u));
@@ -149,12 +165,6 @@ __global__ void __launch_bounds__(256) noalloc_step_kernel(DState S, DWorld W, b
 
 }  // namespace bp
 
-namespace {
-// Address of the scratch array on each device, taken once per device (with that device current) on the first call.
-std::mutex g_noalloc_mutex;
-void* g_noalloc_address[64] = {};
-}  // namespace
-
 extern "C" int bp_world_step_noalloc(const bp_world_desc* desc, bp_bubble* bubbles, uint32_t bubble_count,
                                      const bp_segment* segments, uint32_t segment_count, uint32_t steps,
                                      bp_step_report* reports, void* stream) {
@@ -164,24 +174,16 @@ extern "C" int bp_world_step_noalloc(const bp_world_desc* desc, bp_bubble* bubbl
     if (bubble_count > kNaN || segment_count > kNaS || k > kNaK) return BP_E_CAPACITY;
     if (!(desc->time_step > 0.0f) || !isfinite(desc->time_step)) return BP_E_INVALID;
     if (steps == 0) return BP_OK;
-    int device = -1;
-    if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= 64) return BP_E_UNAVAILABLE;
+    // The array's device address is looked up on every call, with the caller's device current: it is a host-side
+    // lookup that allocates nothing, and it stays right when the context was torn down and made again (the module
+    // is then loaded anew and the array may sit elsewhere). The shared-memory attribute is set the same way.
     void* base = nullptr;
-    {
-        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-        if (!g_noalloc_address[device]) {
-            void* address = nullptr;
-            cudaError_t err = cudaGetSymbolAddress(&address, g_noalloc_scratch);
-            if (err != cudaSuccess || !address) return BP_E_CUDA;
-            if (cudaFuncSetAttribute(noalloc_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024) != cudaSuccess)
-                return BP_E_CUDA;
-            g_noalloc_address[device] = address;
-        }
-        base = g_noalloc_address[device];
-    }
+    cudaError_t err = cudaGetSymbolAddress(&base, g_noalloc_scratch);
+    if (err != cudaSuccess || !base) return BP_E_CUDA;
+    if (cudaFuncSetAttribute(noalloc_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024) != cudaSuccess)
+        return BP_E_CUDA;
     NoAllocLayout layout;
     DState S = layout.make((char*)base);
-    if (layout.bytes > noalloc_bytes()) return BP_E_CAPACITY;
     DWorld W{};
     W.boff = 0; W.n = bubble_count; W.soff = 0; W.s = segment_count;
     W.k = k;

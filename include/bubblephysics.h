@@ -494,13 +494,21 @@ double bp_server_clock(void);
  * in place to the published state after the steps), `segments` and `reports` (`steps` entries) are DEVICE pointers
  * owned by the caller, and every working array comes from one fixed 1 MiB device array built into the library (it
  * exists once on every GPU that loads the library, until the process exits).
- * Limits: at most 1024 bubbles, 256 segments, candidate limit at most 32 (0 means 32), at most 4 contact records per
- * bubble; no bodies, fields, bands, motors or joints; injection and multi-CTA switches are ignored. Larger inputs are
- * rejected with BP_E_CAPACITY before anything runs.
+ * Limits: at most 1024 bubbles, 256 segments, candidate limit at most 32 (0 means 32); no bodies, fields, bands,
+ * motors or joints; injection and multi-CTA switches are ignored; rigid candidates always take the brute-force loops.
+ * Larger inputs are rejected with BP_E_CAPACITY before anything runs.
+ * Contact records: at most 4 per bubble + 64 are kept (contact_count stops there, the rest is counted in
+ * contact_overflow, where bp_world_step keeps k per bubble + 64), and the records themselves are not returned.
+ * Inputs: bubble ids must be strictly ascending (as bp_world_create requires); the kernel checks this and, if not,
+ * steps nothing and writes BP_E_INVALID into every report. A bubble whose region_result is 1 (removed by the region
+ * in an earlier call) stays removed, so consecutive calls continue one world; bp_world_create instead takes every
+ * input bubble as live.
  * Runs on `stream` (a cudaStream_t, NULL = the default stream) on the current device and returns when the work is
- * queued; the step statuses are in `reports`. The first call on a device looks up the array's device address (with
- * that device current), so make that first call before any stream capture. Every call shares the one array and
- * initialises what it needs, so calls must not overlap on the GPU: two calls in flight at once race on it. */
+ * queued; the step statuses are in `reports`. Every call looks up the array's device address with that device
+ * current (a host-side lookup). Under lazy module loading, the first call in a process on a device loads the
+ * library's device code, which allocates device memory for the code and the array: make that first call at setup
+ * time, before any stream capture. Every call shares the one array and initialises what it needs, so calls must not
+ * overlap on the GPU: two calls in flight at once race on it. */
 int bp_world_step_noalloc(const bp_world_desc* desc, bp_bubble* bubbles, uint32_t bubble_count,
                           const bp_segment* segments, uint32_t segment_count, uint32_t steps,
                           bp_step_report* reports, void* stream);
