@@ -1,21 +1,24 @@
 #!/usr/bin/env python
 """bench.py - bubble-substeps/s of the batched bubble step on GB300 (one JSON line on rank 0).
 
-Workload (one "step" = one step of every world of the batch): 4,096 independent worlds, bubble counts log-uniform in
-[16, 1024], radii U[6, 24] at 40 % area fraction, 0-32 rigid bodies each (polygons, circles, capsules; half-extents
-U[8, 40]; static or kinematic), walls, gravity (0, -980), dt = 1/60; seeded synthetic data.
+Workload (one "step" = one step of every world of the batch): 4,096 independent worlds (seed 3), bubble counts
+log-uniform in [16, 1024], radii U[6, 24] at 40 % area fraction, 0-32 rigid bodies each (polygons, circles, capsules;
+half-extents U[8, 40]; static or kinematic), walls, no gravity, dt = 1/60; seeded synthetic data. Defaults: 5 warm-up
+and 20 timed steps.
 
-  value        whole-job bubble-substeps/s of the batched path (one fused launch per size class and step, CUDA graph),
-               inputs resident in HBM; device time from CUDA events on the library's stream
+  value        whole-job bubble-substeps/s of the batched path (one persistent launch per step, CUDA graph), inputs
+               resident in HBM; device time from CUDA events on the library's stream
   e2e          the same metric through the C ABI with HOST buffers: every step writes (centre, velocity) of all bubbles
                from pinned host memory, steps, and reads them back
   per_world    the plain per-world launch path on the same worlds (one launch per world, one after another)
   latency      p50 / p99 device time of one batched step
-  roofline     algorithmic bytes of the dominant kernel (batch_step_kernel) per second against the measured HBM peak
-  cpu_baseline the CPU oracle (C++ restatement of the reference's algorithm, OpenMP over worlds) on a bounded sample
+  roofline     algorithmic bytes of the dominant kernel (persistent_step_kernel) per second against the measured HBM
+               peak
+  cpu_baseline the CPU oracle (C++ restatement of the reference's algorithm, OpenMP over worlds, every host thread)
+               on the same worlds with the same warm-up and timed steps: the reference arm's own measurement
 
 --impl reference times the reference algorithm on the host cores (the oracle port: the reference itself is Swift +
-Metal and cannot run here) on a bounded sample of the same workload.
+Metal and cannot run here) on the same worlds, warm-up and timed steps as the GPU arm.
 """
 from __future__ import annotations
 
@@ -55,16 +58,18 @@ def algorithmic_bytes(bubble_substeps: float, bubble_builds: float, mean_degree:
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms while the timed region runs."""
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms from start() to stop(); each sample keeps its host
+    arrival time so the samples inside a sub-window (the timed steps) can be told apart from the rest."""
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
+    NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
 
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.lines: list[str] = []
+        self.lines: list[tuple[float, str]] = []
 
     def start(self):
         try:
@@ -73,7 +78,7 @@ class ClockSampler:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
-            deadline = time.time() + 5.0  # the timed region starts once samples flow
+            deadline = time.time() + 5.0  # the measured window starts once samples flow
             while not self.lines and time.time() < deadline and self.proc.poll() is None:
                 time.sleep(0.01)
             self.lines.clear()
@@ -82,19 +87,11 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.time(), line.strip()))
 
-    def stop(self) -> dict:
-        if self.proc is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except subprocess.TimeoutExpired:
-            self.proc.kill()
+    def _summary(self, lines) -> dict:
         sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        for _, line in lines:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -103,11 +100,28 @@ class ClockSampler:
                 smax.append(float(parts[2]))
             except ValueError:
                 continue
-            for name, flag in zip(names, parts[5:9]):
+            for name, flag in zip(self.NAMES, parts[5:9]):
                 if flag.lower() == "active":
                     reasons.add(name)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+    def stop(self, timed: tuple[float, float] | None = None) -> dict:
+        """Clocks over the whole window; with `timed` = (t0, t1) host times also the samples taken within it."""
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        out = self._summary(self.lines)
+        if timed is not None:
+            inside = self._summary([x for x in self.lines if timed[0] <= x[0] <= timed[1] + 0.06])
+            out["timed_region"] = {"sm_mhz": inside["sm_mhz"], "reasons": inside["reasons"],
+                                   "samples": inside["samples"], "seconds": timed[1] - timed[0]}
+            out["window"] = "warm-up, timed steps and end-to-end steps of the batched workload (50 ms polling)"
+        return out
 
 
 def pinned_buffer(count: int):
@@ -121,19 +135,28 @@ def pinned_buffer(count: int):
         return a, None
 
 
-def cpu_sample(specs, max_seconds=12.0, threads=0):
-    """Oracle on a bounded sample: steps the sample worlds until ~max_seconds of CPU work; bubble-substeps/s."""
+def cpu_leg(specs, steps: int, warmup: int, threads: int = 0) -> dict:
+    """The reference's algorithm on the host cores (the C++ oracle port, OpenMP over worlds, every host thread): the
+    same worlds, warm-up and timed steps as the GPU arm. Returns bubble-substeps/s over the timed steps."""
     from oracle import oracle
-    used = oracle.set_threads(threads if threads > 0 else (os.cpu_count() or 1))
+    cores = oracle.set_threads(threads if threads > 0 else (os.cpu_count() or 1))
     worlds = [oracle.OracleWorld(s, 32) for s in specs]
-    total, steps, t0 = 0, 0, time.perf_counter()
-    while True:
+    for _ in range(warmup):
+        oracle.step_worlds(worlds, 1, 0)
+    t0 = time.perf_counter()
+    total = 0
+    for _ in range(steps):
         total += oracle.step_worlds(worlds, 1, 0)
-        steps += 1
-        if time.perf_counter() - t0 > max_seconds or steps >= 50:
-            break
     dt = time.perf_counter() - t0
-    return total / dt, used, steps, dt, total
+    nb = sum(s.bubble_count for s in specs)
+    return {"value": total / dt if dt > 0 else 0.0, "cores": cores, "steps": steps, "warmup": warmup, "seconds": dt,
+            "bubble_substeps": total, "worlds": len(specs), "bubbles": nb}
+
+
+def cpu_sample_text(leg: dict) -> str:
+    return (f"all {leg['worlds']} worlds ({leg['bubbles']} bubbles) of the batched workload, seed 3, {leg['warmup']} "
+            f"warm-up + {leg['steps']} timed steps ({leg['seconds']:.1f} s); the reference is Swift + Metal (no "
+            f"toolchain, no Metal on this box) so its algorithm runs as the C++ oracle port")
 
 
 def load_peak():
@@ -148,32 +171,25 @@ def run_reference(args, rank):
     if rank != 0:
         return 0
     from bubblephysics_gb300 import scenes
-    sample = max(1, args.sample_worlds)
-    specs = scenes.batched_worlds(args.worlds, seed=3, limit=sample)
-    from oracle import oracle
-    cores = oracle.set_threads(os.cpu_count() or 1)
-    worlds = [oracle.OracleWorld(s, 32) for s in specs]
-    for _ in range(args.warmup):
-        oracle.step_worlds(worlds, 1, 0)
-    t0 = time.perf_counter()
-    total = 0
-    for _ in range(args.steps):
-        total += oracle.step_worlds(worlds, 1, 0)
-    dt = time.perf_counter() - t0
-    value = total / dt
-    nb = sum(s.bubble_count for s in specs)
+    specs = scenes.batched_worlds(args.worlds, seed=3)
+    leg = cpu_leg(specs, args.steps, args.warmup)
+    value = leg["value"]
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1000.0 / max(args.steps, 1),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": leg["seconds"] * 1000.0 / max(args.steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"batched worlds ({args.worlds} worlds, N~LogUniform[16,1024], r~U[6,24], "
-                                   f"0-32 bodies, dt=1/60)", "sample_worlds": sample, "sample_bubbles": nb},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"first {sample} worlds ({nb} bubbles) of the batched workload, "
-                                       f"{args.steps} timed steps; the reference is Swift + Metal (no toolchain, no "
-                                       f"Metal) so its algorithm runs as the C++ oracle port"},
+            "config": workload_config(args, leg["bubbles"]),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": leg["cores"], "kind": "port",
+                             "sample": cpu_sample_text(leg)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def workload_config(args, bubbles: int) -> dict:
+    """The `config` object both arms print: the same workload name and sizes."""
+    return {"workload": f"batched worlds ({args.worlds} worlds per GPU, N~LogUniform[16,1024], r~U[6,24], "
+                        f"0-32 bodies, dt=1/60, seed 3)", "worlds": args.worlds, "bubbles": bubbles,
+            "l2": "inputs larger than L2: every step touches the state of all worlds (>129 MB)"}
 
 
 def single_world_rate(spec, ctx, steps: int, warmup: int, contours: bool = False) -> dict:
@@ -351,20 +367,21 @@ def run_ours(args, rank, world_size, local_rank):
     specs = scenes.batched_worlds(args.worlds, seed=3 + rank)
     total_bubbles = sum(s.bubble_count for s in specs)
     batch = Batch(specs, ctx, use_graph=True, autotune=not args.no_autotune)
+    sampler = ClockSampler(local_rank)
+    sampler.start()
     st, _ = batch.step(args.warmup)
     _, subs0, launches0 = batch.counters()
     if dist:
         dist.barrier()
-    sampler = ClockSampler(local_rank)
-    sampler.start()
     step_ms, statuses = [], []
     rebuild_bubbles = 0
+    timed0 = time.time()
     for _ in range(args.steps):
-        status, reps = batch.step(1)
+        status, reps = batch.step(1)  # returns after the step's stream synchronisation
         statuses.append(status)
         step_ms.append(float(reps["gpu_ms"][0]))
         rebuild_bubbles += int((reps["rebuild_count"].astype(np.int64) * batch.sizes).sum())
-    clocks = sampler.stop()
+    timed1 = time.time()
     _, subs1, launches1 = batch.counters()
     device_s = sum(step_ms) / 1000.0
     bubble_substeps = subs1 - subs0
@@ -373,7 +390,8 @@ def run_ours(args, rank, world_size, local_rank):
     builds = total_bubbles * args.steps + rebuild_bubbles
     alg_bytes = algorithmic_bytes(bubble_substeps, builds, mean_degree)
     kernel_launches = (launches1 - launches0)
-    gpu_launches = kernel_launches + args.steps  # + the report-accumulation kernel of each step
+    # step kernels, plus the report accumulation and the on-device scheduler of every step (one CUDA graph per step)
+    gpu_launches = kernel_launches + 2 * args.steps
     device_s_all, substeps_all = combine_ranks(device_s, float(bubble_substeps), dist)
     value = substeps_all / device_s_all if device_s_all > 0 else 0.0
 
@@ -387,6 +405,7 @@ def run_ours(args, rank, world_size, local_rank):
         batch.step(1)
         batch.read_state(host)
     e2e_wall = time.perf_counter() - t0
+    clocks = sampler.stop(timed=(timed0, timed1))
     _, e2e_s1, _ = batch.counters()
     e2e_value = (e2e_s1 - e2e_s0) / e2e_wall if e2e_wall > 0 else 0.0
 
@@ -432,18 +451,16 @@ def run_ours(args, rank, world_size, local_rank):
     except Exception:
         traffic = None
     alg_per_launch = alg_bytes / max(kernel_launches, 1)
-    cpu_specs = specs[:args.cpu_sample_worlds]
-    cpu_value, cores, cpu_steps, cpu_dt, cpu_total = cpu_sample(cpu_specs, max_seconds=args.cpu_seconds)
+    # the CPU baseline: the reference arm's measurement itself (same worlds, warm-up and timed steps)
+    leg = cpu_leg(specs, args.steps if args.cpu_steps <= 0 else min(args.cpu_steps, args.steps), args.warmup)
     lat = sorted(step_ms)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": device_s_all * 1000.0 / max(args.steps, 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"batched worlds ({args.worlds} worlds per GPU, N~LogUniform[16,1024], r~U[6,24], "
-                               f"0-32 bodies, dt=1/60)", "worlds": args.worlds, "bubbles": total_bubbles,
-                   "l2": "inputs larger than L2: every step touches the state of all worlds (>129 MB)",
-                   "substeps_per_step_mean": bubble_substeps / max(total_bubbles * args.steps, 1),
-                   "mean_adjacency_degree": mean_degree, "statuses": sorted(set(statuses))},
+        "config": dict(workload_config(args, total_bubbles),
+                       substeps_per_step_mean=bubble_substeps / max(total_bubbles * args.steps, 1),
+                       mean_adjacency_degree=mean_degree, statuses=sorted(set(statuses))),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": total_bubbles * 16,
                 "d2h_bytes_per_step": total_bubbles * 16, "steps": args.e2e_steps,
                 "note": "C ABI bp_batch_write_state + bp_batch_step + bp_batch_read_state from pinned host memory, wall clock"},
@@ -456,8 +473,8 @@ def run_ours(args, rank, world_size, local_rank):
                      "traffic": traffic, "kernel": "persistent_step_kernel", "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": alg_per_launch,
                      "bytes_model": "76 + 40*k per bubble-substep, 96 + 8*k per bubble grid build (k = mean degree)"},
-        "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"first {len(cpu_specs)} worlds of the workload, {cpu_steps} steps, {cpu_dt:.1f} s"},
+        "cpu_baseline": {"value": leg["value"], "unit": UNIT, "cores": leg["cores"], "kind": "port",
+                         "sample": cpu_sample_text(leg)},
         "clocks": clocks,
         "gpu_launches": gpu_launches,
         "single_worlds": singles,
@@ -472,15 +489,14 @@ def run_ours(args, rank, world_size, local_rank):
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=300)
+    p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--worlds", type=int, default=4096)
     p.add_argument("--e2e-steps", type=int, default=10)
     p.add_argument("--per-world-steps", type=int, default=2)
-    p.add_argument("--cpu-sample-worlds", type=int, default=256)
-    p.add_argument("--cpu-seconds", type=float, default=10.0)
-    p.add_argument("--sample-worlds", type=int, default=1024)
+    p.add_argument("--cpu-steps", type=int, default=0,
+                   help="timed steps of the CPU baseline leg (0: the same as --steps, the reference arm's sample)")
     p.add_argument("--single-steps", type=int, default=10, help="timed steps of each single-world workload (0: skip)")
     p.add_argument("--serve-worlds", type=int, default=8192)
     p.add_argument("--serve-requests", type=int, default=20000, help="requests of the serving stream (0: skip)")

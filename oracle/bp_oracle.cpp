@@ -1798,6 +1798,28 @@ int bpo_worlds_step(void** handles, uint32_t count, uint32_t steps, int threads,
     return BP_OK;
 }
 
+// The same, keeping every world's report of every step: reports[step * count + world] (steps after a failure keep
+// the failing report's status and no substeps). Used by the full-size batched parity checks.
+int bpo_worlds_step_reports(void** handles, uint32_t count, uint32_t steps, int threads, bp_step_report* reports) {
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#endif
+#pragma omp parallel for schedule(dynamic, 1)
+    for (uint32_t wi = 0; wi < count; ++wi) {
+        Handle* h = (Handle*)handles[wi];
+        bp_step_report rep{};
+        int status = BP_OK;
+        for (uint32_t s = 0; s < steps; ++s) {
+            if (status == BP_OK)
+                status = h->precision == 64 ? step(*(World<double>*)h->world, rep) : step(*(World<float>*)h->world, rep);
+            else
+                rep.substep_count = 0;
+            reports[(uint64_t)s * count + wi] = rep;
+        }
+    }
+    return BP_OK;
+}
+
 // Sorted LBVH keys of the rigid leaves for the last step (see rigid_keys); returns the number of keys.
 uint32_t bpo_world_rigid_keys(void* handle, uint64_t* out, uint32_t capacity) {
     Handle* h = (Handle*)handle;

@@ -41,6 +41,7 @@ def library() -> C.CDLL:
             "bpo_world_set_injection": (C.c_int, [P, C.c_uint32, C.c_float, C.c_float]),
             "bpo_world_step": (C.c_int, [P, C.c_uint32, P]),
             "bpo_worlds_step": (C.c_int, [C.POINTER(P), C.c_uint32, C.c_uint32, C.c_int, C.POINTER(C.c_uint64)]),
+            "bpo_worlds_step_reports": (C.c_int, [C.POINTER(P), C.c_uint32, C.c_uint32, C.c_int, P]),
             "bpo_set_threads": (C.c_int, [C.c_int]),
             "bpo_world_read_bubbles": (C.c_int, [P, P, C.c_uint32, C.POINTER(C.c_uint32)]),
             "bpo_world_read_state64": (C.c_int, [P, P, C.c_uint32]),
@@ -198,6 +199,15 @@ def step_worlds(worlds: list[OracleWorld], steps: int, threads: int = 0) -> int:
     total = C.c_uint64()
     lib.bpo_worlds_step(arr, len(worlds), steps, threads, C.byref(total))
     return total.value
+
+
+def step_worlds_reports(worlds: list[OracleWorld], steps: int, threads: int = 0) -> np.ndarray:
+    """Steps many oracle worlds with OpenMP over worlds and returns every report, shape (steps, worlds)."""
+    lib = library()
+    arr = (C.c_void_p * len(worlds))(*[w.handle.value for w in worlds])
+    out = np.zeros((max(steps, 1), len(worlds)), N.REPORT_DTYPE)
+    lib.bpo_worlds_step_reports(arr, len(worlds), steps, threads, C.c_void_p(out.ctypes.data))
+    return out[:steps]
 
 
 def set_threads(threads: int) -> int:
