@@ -124,7 +124,7 @@ class CandidateKey(C.Structure):
 
 class BatchConfig(C.Structure):
     _fields_ = [("flags", C.c_uint32), ("threads_per_world", C.c_uint32), ("warp_world_max", C.c_uint32),
-                ("reserved", C.c_uint32)]
+                ("group_width", C.c_uint32)]
 
 
 class ContourConfig(C.Structure):
@@ -143,7 +143,7 @@ SENSOR_ENTER_EVENTS, SENSOR_EXIT_EVENTS = 1, 2
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_worlds", C.c_uint32), ("max_batch_worlds", C.c_uint32),
                 ("streams", C.c_uint32), ("threads_per_world", C.c_uint32), ("warp_world_max", C.c_uint32),
-                ("flags", C.c_uint32)]
+                ("flags", C.c_uint32), ("group_width", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class ServerCompletion(C.Structure):
@@ -161,7 +161,7 @@ class ServerStats(C.Structure):
 
 SERVER_PER_WORLD = 1
 
-RECORD_SIZES = {Sensor: 48, ContourConfig: 16, ServerConfig: 32, ServerCompletion: 136, ServerStats: 80, Bubble: 80, Segment: 64, Body: 80, ForceField: 64, Band: 24, Motor: 24, WorldDesc: 64,
+RECORD_SIZES = {Sensor: 48, ContourConfig: 16, ServerConfig: 40, ServerCompletion: 136, ServerStats: 80, Bubble: 80, Segment: 64, Body: 80, ForceField: 64, Band: 24, Motor: 24, WorldDesc: 64,
                 StepReport: 96, Contact: 64, CandidateKey: 24}
 for _t, _n in RECORD_SIZES.items():
     assert C.sizeof(_t) == _n, f"{_t.__name__} is {C.sizeof(_t)} bytes, the C ABI says {_n}"

@@ -84,12 +84,24 @@ int validate(const bp_world_desc& d, const bp_world_input& in) {
     return BP_OK;
 }
 
-// Initial split of the non-large worlds into the CTA and warp queues (largest first) for a block width and warp-team
-// threshold; after every batched step the on-device scheduler reorders both queues by predicted cost. Shared memory
-// is sized so any world can be a CTA world and any world up to the threshold a warp world.
-cudaError_t schedule(WorldSet& ws, uint32_t threads, uint32_t warpMax) {
+bool group_layout(uint32_t threads, uint32_t groupWidth, uint32_t maxN, uint32_t* wsCap) {
+    const uint32_t groups = std::max(threads / std::max(groupWidth, 32u), 1u);
+    const uint32_t gridBytes = maxN ? 4u * round4(grid_buckets(maxN) + maxN) : 0u;
+    const uint32_t fixed = 4u * group_scratch_words(groupWidth) + gridBytes;
+    const uint32_t perGroup = kMaxDynamicSmem / groups;
+    if (fixed + 16u > perGroup) return false;
+    *wsCap = std::min(kWarpWorkspaceCap * std::max(groupWidth / 32u, 1u), perGroup - fixed - 16u);
+    return true;
+}
+
+// Initial split of the non-large worlds into the CTA and group queues (largest first) for a block width, group-queue
+// threshold and group width; after every batched step the on-device scheduler reorders both queues by predicted
+// cost. Shared memory is sized so any world can be a CTA world and any world up to the threshold a group world.
+cudaError_t schedule(WorldSet& ws, uint32_t threads, uint32_t warpMax, uint32_t groupWidth) {
+    groupWidth = std::min(std::max(groupWidth, 32u), threads);
     ws.threads = threads;
     ws.warpMax = warpMax;
+    ws.groupWidth = groupWidth;
     ws.ctaWorlds.clear();
     ws.warpWorlds.clear();
     std::vector<uint32_t> candidates;
@@ -104,10 +116,9 @@ cudaError_t schedule(WorldSet& ws, uint32_t threads, uint32_t warpMax) {
     }
     // workspace caps that keep one block within the dynamic shared memory limit
     const uint32_t ctaGridBytes = 4u * round4(grid_buckets(maxN) + maxN);
-    const uint32_t warpGridBytes = maxWarpN ? 4u * round4(grid_buckets(maxWarpN) + maxWarpN) : 0u;
     const uint32_t ctaCap = std::min(kCtaWorkspaceCap, kMaxDynamicSmem - std::min(kMaxDynamicSmem, ctaGridBytes));
-    const uint32_t perWarp = kMaxDynamicSmem / std::max(threads / 32u, 1u);
-    const uint32_t warpCap = std::min(kWarpWorkspaceCap, perWarp > warpGridBytes + 16u ? perWarp - warpGridBytes - 16u : 0u);
+    uint32_t warpCap = 0;
+    if (maxWarpN && !group_layout(threads, groupWidth, maxWarpN, &warpCap)) return cudaErrorInvalidValue;
     for (uint32_t w : candidates) {
         const DWorld& W = ws.hWorlds[w];
         uint32_t bytes = workspace_bytes(W.n, W.s, W.nb);
@@ -134,6 +145,7 @@ cudaError_t schedule(WorldSet& ws, uint32_t threads, uint32_t warpMax) {
     q.warpWsWords = ws.staging ? (warpWs + 3u) / 4u : 0u;
     q.ctaWsWords = (q.ctaWsWords + 3u) & ~3u;
     q.warpWsWords = (q.warpWsWords + 3u) & ~3u;
+    q.groupWidth = groupWidth;
     ws.nCandidates = (uint32_t)candidates.size();
     uint32_t counts[2] = {q.nCta, q.nWarp};
     cudaError_t err = upload(ws.dCtaList, ws.ctaWorlds.data(), ws.ctaWorlds.size(), ws.ctx->stream);
@@ -436,7 +448,7 @@ int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc
     if (!err) err = upload(dJr, jranges.data(), njr, st);
     if (!err) err = upload(dJp, jpartners.data(), njp, st);
     if (!err) err = cudaStreamSynchronize(st);
-    if (!err && !ws.planOnly) err = schedule(ws, ws.threads, ws.warpMax);
+    if (!err && !ws.planOnly) err = schedule(ws, ws.threads, ws.warpMax, ws.groupWidth);
     return cuda_status(err);
 }
 
@@ -465,7 +477,7 @@ cudaError_t launch_step(WorldSet& ws, bool perWorld, uint32_t only = 0xffffffffu
         uint32_t bytes = workspace_bytes(W.n, W.s, W.nb);
         bool warpTeam = W.n <= ws.warpMax;
         uint32_t wsWords = ws.staging && bytes <= (warpTeam ? kWarpWorkspaceCap : kCtaWorkspaceCap) ? ((bytes + 15u) / 16u) * 4u : 0u;
-        if (warpTeam) { q.warpList = ws.dSingle + w; q.nWarp = 1; q.warpMaxN = maxN; q.warpB = grid_buckets(maxN); q.warpWsWords = wsWords; }
+        if (warpTeam) { q.warpList = ws.dSingle + w; q.nWarp = 1; q.warpMaxN = maxN; q.warpB = grid_buckets(maxN); q.warpWsWords = wsWords; q.groupWidth = 32u; }
         else { q.ctaList = ws.dSingle + w; q.nCta = 1; q.ctaMaxN = maxN; q.ctaB = grid_buckets(maxN); q.ctaWsWords = wsWords; }
         return launch_persistent(ws.S, q, W.n <= ws.warpMax ? 32u : ws.threads, 1u, st);
     };
@@ -533,28 +545,35 @@ cudaError_t autotune(WorldSet& ws) {
     Snapshot snap;
     cudaError_t err = take_snapshot(ws, snap);
     cudaStream_t st = ws.ctx->stream;
-    const uint32_t widths[] = {128, 256, 512};
-    const uint32_t warpMaxes[] = {0, 32, 64, 128};
+    // block width x group-queue threshold x group width; combinations whose group grids do not fit are skipped
+    const uint32_t widths[] = {256, 512};
+    const uint32_t warpMaxes[] = {0, 64, 128, 256, 512, 1024};
+    const uint32_t groupWidths[] = {32, 64, 128};
     float best = 1e30f;
-    uint32_t bestT = ws.threads, bestW = ws.warpMax;
+    uint32_t bestT = ws.threads, bestW = ws.warpMax, bestG = ws.groupWidth;
     for (uint32_t t : widths) {
         for (uint32_t wm : warpMaxes) {
-            if (err) break;
-            err = schedule(ws, t, wm);
-            for (int rep = 0; rep < 2 && !err; ++rep) {  // the first run warms up
-                err = restore_snapshot(ws, snap);
+            for (uint32_t gw : groupWidths) {
+                uint32_t cap = 0;
                 if (err) break;
-                cudaEventRecord(ws.ctx->start, st);
-                err = launch_persistent(ws.S, ws.queue, ws.threads, ws.blocks, st);
-                cudaEventRecord(ws.ctx->stop, st);
-                if (!err) err = cudaEventSynchronize(ws.ctx->stop);
-                float ms = 0.0f;
-                cudaEventElapsedTime(&ms, ws.ctx->start, ws.ctx->stop);
-                if (!err && rep == 1 && ms < best) { best = ms; bestT = t; bestW = wm; }
+                if (wm == 0u && gw != 32u) continue;  // no group queue: the group width does not matter
+                if (wm && !group_layout(t, gw, wm, &cap)) continue;
+                err = schedule(ws, t, wm, gw);
+                for (int rep = 0; rep < 2 && !err; ++rep) {  // the first run warms up
+                    err = restore_snapshot(ws, snap);
+                    if (err) break;
+                    cudaEventRecord(ws.ctx->start, st);
+                    err = launch_persistent(ws.S, ws.queue, ws.threads, ws.blocks, st);
+                    cudaEventRecord(ws.ctx->stop, st);
+                    if (!err) err = cudaEventSynchronize(ws.ctx->stop);
+                    float ms = 0.0f;
+                    cudaEventElapsedTime(&ms, ws.ctx->start, ws.ctx->stop);
+                    if (!err && rep == 1 && ms < best) { best = ms; bestT = t; bestW = wm; bestG = gw; }
+                }
             }
         }
     }
-    if (!err) err = schedule(ws, bestT, bestW);
+    if (!err) err = schedule(ws, bestT, bestW, bestG);
     cudaError_t rerr = restore_snapshot(ws, snap);
     if (!rerr) rerr = cudaStreamSynchronize(st);
     free_snapshot(snap);
@@ -1155,10 +1174,17 @@ int bp_batch_create(bp_context* context, uint32_t world_count, const bp_world_de
         b->set.flags = config->flags;
         uint32_t t = config->threads_per_world ? config->threads_per_world : b->set.threads;
         uint32_t wm = config->warp_world_max == 0xffffffffu ? 0u : (config->warp_world_max ? config->warp_world_max : b->set.warpMax);
-        if (t % 32u || t > 512u || wm > kCtaMaxBubbles) { delete b; context_unref(context); return BP_E_INVALID; }
-        if (config->threads_per_world || config->warp_world_max) {
+        uint32_t gw = config->group_width ? config->group_width : b->set.groupWidth;
+        uint32_t cap = 0;
+        if (t % 32u || t > 512u || wm > kCtaMaxBubbles || (gw != 32u && gw != 64u && gw != 128u && gw != 256u) ||
+            gw > t || (wm && !group_layout(t, gw, wm, &cap))) {
+            delete b;
+            context_unref(context);
+            return BP_E_INVALID;
+        }
+        if (config->threads_per_world || config->warp_world_max || config->group_width) {
             b->set.fixedThreads = t;
-            if (schedule(b->set, t, wm) != cudaSuccess) { delete b; context_unref(context); return BP_E_CUDA; }
+            if (schedule(b->set, t, wm, gw) != cudaSuccess) { delete b; context_unref(context); return BP_E_CUDA; }
         }
     }
     *out = b;
@@ -1250,8 +1276,8 @@ int bp_debug_phase_cycles(bp_batch* batch, unsigned long long* out) {
 int bp_batch_tuning(bp_batch* batch, uint32_t* values, uint32_t count) {
     if (!batch || !values) return BP_E_INVALID;
     const WorldSet& ws = batch->set;
-    uint32_t v[5] = {ws.threads, ws.warpMax, ws.blocks, ws.queue.nCta, ws.queue.nWarp};
-    for (uint32_t q = 0; q < count && q < 5; ++q) values[q] = v[q];
+    uint32_t v[6] = {ws.threads, ws.warpMax, ws.blocks, ws.queue.nCta, ws.queue.nWarp, ws.groupWidth};
+    for (uint32_t q = 0; q < count && q < 6; ++q) values[q] = v[q];
     return BP_OK;
 }
 

@@ -160,15 +160,41 @@ constexpr uint32_t kPhaseCount = 24;
 // memory so the on-device scheduler can reorder them between steps without a host round trip.
 struct QueueArgs {
     const uint32_t* ctaList;   // worlds stepped by a whole block, most expensive first
-    const uint32_t* warpList;  // worlds stepped by one warp, most expensive first
+    const uint32_t* warpList;  // worlds of the group queue (one group of groupWidth threads each), most expensive first
     uint32_t* queue;           // [0] next CTA world, [1] next warp world (zeroed before each launch),
                                // [2] CTA list length, [3] warp list length
-    uint32_t nCta, ctaB, ctaMaxN;     // ctaMaxN / warpMaxN size the shared-memory grid of one team
+    uint32_t nCta, ctaB, ctaMaxN;     // ctaMaxN / warpMaxN size the shared-memory grid of one team (warp*: the group queue)
     uint32_t nWarp, warpB, warpMaxN;
     uint32_t countsOnDevice;          // 1: list lengths are queue[2], queue[3]; 0: nCta, nWarp
     uint32_t ctaWsWords, warpWsWords; // shared-memory workspace of one team (32-bit words) after its grid
     uint32_t tree;                    // 1: some world uses the LBVH (launch the tree-capable kernel)
+    uint32_t groupWidth;              // threads of one group-queue team: 32 (a warp), 64, 128 or 256 (<= block width)
 };
+
+__host__ __device__ inline uint32_t round4_words(uint32_t v) { return (v + 3u) & ~3u; }
+
+// Per-team copies of the world's table entry and state pointers, kept in SHARED memory for the whole step: S is the
+// state a team reads and writes (its hot arrays redirected into the shared-memory workspace when the world is staged),
+// G the world's arrays in global memory (the served kernel's per-world state; the batched kernels read G from their
+// parameter). In shared memory every access is a broadcast load; a per-thread copy would live in local memory, one
+// copy per thread.
+struct TeamState {
+    DState S;
+    DState G;
+    DWorld W;
+};
+constexpr uint32_t kTeamStateWords = (uint32_t)((sizeof(TeamState) + 15u) / 16u * 4u);
+
+// Shared-memory slice of one group of the group queue, in 32-bit words: the group's TeamState, its reduction scratch
+// (groups wider than a warp; a BlockScratch), then its hash grid (B bucket ends, then the entries of its largest
+// world), then its workspace.
+constexpr uint32_t kGroupScratchWords = 308;
+__host__ __device__ inline uint32_t group_scratch_words(uint32_t width) {
+    return kTeamStateWords + (width > 32u ? kGroupScratchWords : 0u);
+}
+__host__ __device__ inline uint32_t group_slice_words(const QueueArgs& q) {
+    return group_scratch_words(q.groupWidth) + round4_words(q.warpB + q.warpMaxN) + q.warpWsWords;
+}
 
 constexpr float kPiF = 3.14159265358979323846f;
 

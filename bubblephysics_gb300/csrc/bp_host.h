@@ -60,7 +60,8 @@ constexpr uint32_t kDefaultThreads = 256;
 constexpr uint32_t kDefaultWarpMax = 64;
 constexpr uint32_t kWarpSubsteps = 16;   // a world that took more substeps last step gets a whole block
 constexpr uint32_t kCtaWorkspaceCap = 80u * 1024u;   // shared-memory workspace of a block team (2 blocks per SM, L1 keeps ~90 KB)
-constexpr uint32_t kWarpWorkspaceCap = 10u * 1024u;  // per warp team
+constexpr uint32_t kWarpWorkspaceCap = 10u * 1024u;  // per warp of a group team
+constexpr uint32_t kDefaultGroupWidth = 32;
 constexpr uint32_t kMaxDynamicSmem = 200u * 1024u;   // per block, set on the kernels by prepare_kernels()
 constexpr uint32_t kTreeMinLeaves = 128;             // segments + bodies from which rigid candidates use the LBVH
 
@@ -116,7 +117,8 @@ struct WorldSet {
     unsigned long long* dTotal = nullptr;
     float4* dStaging = nullptr;
     std::vector<void*> allocations;
-    // scheduling: worlds stepped by a block (CTA team) or by one warp (warp team), largest first
+    // scheduling: worlds stepped by a block (CTA team) or by a group of groupWidth threads (group queue), largest
+    // first
     std::vector<uint32_t> ctaWorlds, warpWorlds;
     uint32_t* dCtaList = nullptr;
     uint32_t* dWarpList = nullptr;
@@ -126,7 +128,8 @@ struct WorldSet {
     uint32_t nCandidates = 0;
     uint32_t threads = kDefaultThreads;
     bool staging = true;                    // keep worlds resident in shared memory during a step
-    uint32_t warpMax = kDefaultWarpMax;
+    uint32_t warpMax = kDefaultWarpMax;     // worlds of at most this many bubbles go to the group queue
+    uint32_t groupWidth = kDefaultGroupWidth;
     uint32_t blocks = 0;
     QueueArgs queue{};
     std::vector<uint32_t> largeWorlds;
@@ -188,7 +191,10 @@ struct Snapshot {
 int validate(const bp_world_desc& d, const bp_world_input& in);
 int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc* descs, const bp_world_input* inputs,
               bool single);
-cudaError_t schedule(WorldSet& ws, uint32_t threads, uint32_t warpMax);
+cudaError_t schedule(WorldSet& ws, uint32_t threads, uint32_t warpMax, uint32_t groupWidth);
+// Shared-memory layout of the group queue for `threads`-wide blocks of groupWidth-thread groups whose largest world
+// has maxN bubbles: false when even the grids do not fit; *wsCap = the workspace bytes a group can stage.
+bool group_layout(uint32_t threads, uint32_t groupWidth, uint32_t maxN, uint32_t* wsCap);
 // Device arrays whose contents carry over from one step to the next (what a snapshot or an eviction keeps), in this
 // order: live state, published state, bodies, failed flags.
 enum PersistentPart {

@@ -22,7 +22,7 @@
 using namespace bp;
 using namespace bp_host;
 
-static_assert(sizeof(bp_server_config) == 32, "bp_server_config layout");
+static_assert(sizeof(bp_server_config) == 40, "bp_server_config layout");
 static_assert(sizeof(bp_server_completion) == 136, "bp_server_completion layout");
 static_assert(sizeof(bp_server_stats) == 80, "bp_server_stats layout");
 
@@ -269,7 +269,7 @@ uint32_t ready_worlds(bp_server* s, std::vector<uint32_t>& out, uint32_t limit) 
     return (uint32_t)out.size();
 }
 
-// Launches one batch over `entries` on flight f: the host splits the worlds into the block and warp queues (largest
+// Launches one batch over `entries` on flight f: the host splits the worlds into the block and group queues (largest
 // first) and sizes the shared memory as the batched schedule does.
 int launch(bp_server* s, Flight& f, const std::vector<uint32_t>& entries) {
     const bool perWorld = (s->cfg.flags & BP_SERVER_PER_WORLD) != 0;
@@ -291,11 +291,11 @@ int launch(bp_server* s, Flight& f, const std::vector<uint32_t>& entries) {
         else { cta[nCta++] = e; maxCta = std::max(maxCta, W.n); }
     }
     const uint32_t threads = perWorld && nCta == 0 ? 32u : s->cfg.threads_per_world;
+    const uint32_t groupWidth = std::min(s->cfg.group_width, threads);
     const uint32_t ctaGridBytes = maxCta ? 4u * round4(grid_buckets(maxCta) + maxCta) : 0u;
-    const uint32_t warpGridBytes = maxWarp ? 4u * round4(grid_buckets(maxWarp) + maxWarp) : 0u;
     const uint32_t ctaCap = std::min(kCtaWorkspaceCap, kMaxDynamicSmem - std::min(kMaxDynamicSmem, ctaGridBytes));
-    const uint32_t perWarp = kMaxDynamicSmem / std::max(threads / 32u, 1u);
-    const uint32_t warpCap = std::min(kWarpWorkspaceCap, perWarp > warpGridBytes + 16u ? perWarp - warpGridBytes - 16u : 0u);
+    uint32_t warpCap = 0;
+    if (maxWarp && !group_layout(threads, groupWidth, maxWarp, &warpCap)) return BP_E_INVALID;
     for (uint32_t e = 0; e < n; ++e) {
         const DWorld& W = s->worlds[entries[e]]->set->hWorlds[0];
         const uint32_t bytes = workspace_bytes(W.n, W.s, W.nb);
@@ -316,12 +316,13 @@ int launch(bp_server* s, Flight& f, const std::vector<uint32_t>& entries) {
     q.tree = tree;
     q.ctaWsWords = ((ctaWs + 3u) / 4u + 3u) & ~3u;
     q.warpWsWords = ((warpWs + 3u) / 4u + 3u) & ~3u;
-    const uint32_t warpsPerBlock = std::max(threads / 32u, 1u);
+    q.groupWidth = groupWidth;
+    const uint32_t groupsPerBlock = std::max(threads / groupWidth, 1u);
     const uint64_t key = ((uint64_t)q.tree << 63) | ((uint64_t)threads << 32) | persistent_smem(q, threads);
     auto known = s->blocksFor.find(key);
     const uint32_t full = known != s->blocksFor.end() ? known->second : (s->blocksFor[key] = persistent_blocks(q, threads));
     // a small batch takes only the blocks it can use, so batches on other streams keep the rest of the GPU
-    uint32_t blocks = perWorld ? 1u : std::min(full, nCta + (nWarp + warpsPerBlock - 1u) / warpsPerBlock);
+    uint32_t blocks = perWorld ? 1u : std::min(full, nCta + (nWarp + groupsPerBlock - 1u) / groupsPerBlock);
     blocks = std::max(blocks, 1u);
     cudaError_t err = cudaMemcpyAsync(f.dLists, f.hLists, 3ull * s->cap * sizeof(uint32_t), cudaMemcpyHostToDevice, f.stream);
     if (!err) err = cudaEventRecord(f.start, f.stream);
@@ -417,7 +418,10 @@ int bp_server_create(bp_context* context, const bp_server_config* config, bp_ser
     if (!s->cfg.streams) s->cfg.streams = kDefaultStreams;
     if (!s->cfg.threads_per_world) s->cfg.threads_per_world = kDefaultServeThreads;
     if (!s->cfg.warp_world_max) s->cfg.warp_world_max = kDefaultWarpMax;
-    if (s->cfg.threads_per_world != 128 && s->cfg.threads_per_world != 256 && s->cfg.threads_per_world != 512) {
+    if (!s->cfg.group_width) s->cfg.group_width = kDefaultGroupWidth;
+    const uint32_t gw = s->cfg.group_width;
+    if ((s->cfg.threads_per_world != 128 && s->cfg.threads_per_world != 256 && s->cfg.threads_per_world != 512) ||
+        (gw != 32 && gw != 64 && gw != 128 && gw != 256) || gw > s->cfg.threads_per_world) {
         server_free(s);
         return BP_E_INVALID;
     }

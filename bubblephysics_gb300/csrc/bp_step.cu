@@ -8,8 +8,9 @@ namespace bp {
 // Cooperative launch: every block steps world `wi` together; the hash grid lives in global memory.
 __global__ void __launch_bounds__(512) large_step_kernel(DState S, uint32_t wi, uint32_t B) {
     __shared__ BlockScratch sh;
+    __shared__ TeamState ts;
     GridTeam team{&sh, S.barrier, S.errorFlag, S.gpv, S.gpo, nullptr, 0u, false};
-    world_step<GridTeam, true>(S, wi, team, S.gbuckets, S.gentries, B, nullptr, 0u);
+    world_step<GridTeam, true>(S, wi, team, S.gbuckets, S.gentries, B, nullptr, 0u, ts);
 }
 
 // Contact law known-answer kernel: mode 0 eps(q), 1 wall law, 2 pair law; 8 floats in / out per case.
@@ -99,8 +100,8 @@ cudaError_t launch_schedule(const DState& S, const uint32_t* candidates, uint32_
 }
 
 size_t persistent_smem(const QueueArgs& q, uint32_t threads) {
-    size_t cta = (size_t)(q.nCta ? round4(q.ctaB + q.ctaMaxN) + q.ctaWsWords : 0);
-    size_t warp = (size_t)(q.nWarp ? (threads / 32u) * (round4(q.warpB + q.warpMaxN) + q.warpWsWords) : 0);
+    size_t cta = (size_t)(q.nCta ? round4_words(q.ctaB + q.ctaMaxN) + q.ctaWsWords : 0);
+    size_t warp = (size_t)(q.nWarp ? (threads / (q.groupWidth ? q.groupWidth : 32u)) * group_slice_words(q) : 0);
     return (cta > warp ? cta : warp) * sizeof(uint32_t);
 }
 

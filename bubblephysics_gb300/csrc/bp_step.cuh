@@ -1216,21 +1216,23 @@ __device__ bool stage_world(const DState& G, DState& S, const DWorld& W, const T
         filter[i] = G.filter[g];
         flags[i] = G.flags[g];
     }
-    S.phys = phys - W.boff;
-    S.pos = pos - W.boff;
-    S.vel = vel - W.boff;
-    S.acc = acc - W.boff;
-    S.ref = ref - W.boff;
-    S.a0 = a0 - W.boff;
-    S.filter = filter - W.boff;
-    S.candCount = candCount - W.boff;
-    S.margin = margin - W.boff;
-    S.flags = flags - W.boff;
-    S.deg = deg - W.boff;
-    S.pairTotal = pairTotal - W.boff;
-    S.segBox = segBox - W.soff;
-    S.bodyBox = bodyBox - W.bodyOff;
-    S.bpose = bpose - W.bodyOff;
+    if (team.shared_leader()) {  // S lives in the team's shared memory: one thread redirects it
+        S.phys = phys - W.boff;
+        S.pos = pos - W.boff;
+        S.vel = vel - W.boff;
+        S.acc = acc - W.boff;
+        S.ref = ref - W.boff;
+        S.a0 = a0 - W.boff;
+        S.filter = filter - W.boff;
+        S.candCount = candCount - W.boff;
+        S.margin = margin - W.boff;
+        S.flags = flags - W.boff;
+        S.deg = deg - W.boff;
+        S.pairTotal = pairTotal - W.boff;
+        S.segBox = segBox - W.soff;
+        S.bodyBox = bodyBox - W.bodyOff;
+        S.bpose = bpose - W.bodyOff;
+    }
     team.sync();
     return true;
 }
@@ -1260,17 +1262,24 @@ template <class Team> __device__ void build_boxes(const DState& S, const DWorld&
 // ------------------------------------------------------------------------------------------------------------------
 // One complete step of one world (nativeBeginStep -> substep loop -> end of step)
 // ------------------------------------------------------------------------------------------------------------------
+// `ts` is the team's TeamState in shared memory (ts.S and ts.W are written here; G may be ts.G).
 template <class Team, bool kTreeCapable>
 __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint32_t* buckets, uint32_t* entries, uint32_t B,
-                           uint32_t* ws, uint32_t wsWords) {
-    const DWorld W = G.worlds[wi];
+                           uint32_t* ws, uint32_t wsWords, TeamState& ts) {
+    if (team.shared_leader()) {
+        ts.W = G.worlds[wi];
+        ts.S = G;
+    }
+    team.shared_sync();
+    const DWorld& W = ts.W;
     const uint32_t n = W.n, T = team.size(), r = team.rank();
     bp_step_report* rep = G.reports + wi;
     if (G.failed[wi]) {
         if (team.leader()) { rep->status = BP_E_WORLD_FAILED; rep->substep_count = 0u; }
+        team.sync();
         return;
     }
-    DState S = G;
+    DState& S = ts.S;
     stage_world(G, S, W, team, ws, wsWords);
     BP_PHASE_START;
     // nativeBeginStep (NFK:285-293)
@@ -1522,41 +1531,58 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
 // ------------------------------------------------------------------------------------------------------------------
 extern __shared__ __align__(16) uint32_t g_dynamic_smem[];
 
-__host__ __device__ inline uint32_t round4(uint32_t v) { return (v + 3u) & ~3u; }
+static_assert(sizeof(BlockScratch) <= 4u * kGroupScratchWords, "a group's reduction scratch fits its slice");
 
 // Persistent step kernel: blocks pull worlds from two queues. CTA-team worlds (largest first) are stepped by a whole
-// block; then every warp pulls warp-team worlds (small worlds, one warp each). Dynamic shared memory holds the hash
-// grid: for a CTA world B bucket ends then its entries; for a warp world a slice per warp of the same layout.
+// block; then the block splits into groups of q.groupWidth threads (one warp or more), and every group pulls worlds of
+// the group queue on its own, so a block keeps blockDim / groupWidth worlds in flight. Dynamic shared memory holds the
+// hash grid: for a CTA world B bucket ends then its entries (then its workspace); for the group queue one slice per
+// group (group_slice_words).
+template <class Next>
+__device__ __forceinline__ void group_queue(const QueueArgs& q, uint32_t nGroup, BlockScratch& blockSh, uint32_t* next,
+                                            Next&& step) {
+    if (nGroup == 0u) return;
+    const uint32_t width = q.groupWidth > 32u ? q.groupWidth : 32u, group = threadIdx.x / width;
+    uint32_t* mine = g_dynamic_smem + group * group_slice_words(q);
+    const uint32_t scratch = group_scratch_words(width);
+    TeamState& ts = *(TeamState*)mine;
+    GroupTeam team{scratch > kTeamStateWords ? (BlockScratch*)(mine + kTeamStateWords) : &blockSh,
+                   GroupShape{group * width, width, 1u + group}};
+    uint32_t* grid = mine + scratch;
+    uint32_t* ws = q.warpWsWords ? grid + round4_words(q.warpB + q.warpMaxN) : nullptr;
+    for (;;) {
+        if (team.leader()) next[group] = atomicAdd(q.queue + 1, 1u);
+        team.sync();
+        const uint32_t slot = next[group];
+        team.sync();
+        if (slot >= nGroup) break;
+        step(q.warpList[slot], team, grid, grid + q.warpB, ws, ts);
+        team.sync();
+    }
+}
+
 template <int kThreads, bool kTree>
 __global__ void __launch_bounds__(kThreads, 2) persistent_step_kernel(DState S, QueueArgs q) {
     __shared__ BlockScratch sh;
-    __shared__ uint32_t next;
+    __shared__ uint32_t next[kThreads / 32];
+    __shared__ TeamState ctaState;
     CtaTeam cta{&sh};
     const uint32_t nCta = q.countsOnDevice ? *(volatile uint32_t*)(q.queue + 2) : q.nCta;
-    const uint32_t nWarp = q.countsOnDevice ? *(volatile uint32_t*)(q.queue + 3) : q.nWarp;
+    const uint32_t nGroup = q.countsOnDevice ? *(volatile uint32_t*)(q.queue + 3) : q.nWarp;
     for (;;) {
-        if (threadIdx.x == 0) next = atomicAdd(q.queue, 1u);
+        if (threadIdx.x == 0) next[0] = atomicAdd(q.queue, 1u);
         __syncthreads();
-        const uint32_t slot = next;
+        const uint32_t slot = next[0];
         __syncthreads();
         if (slot >= nCta) break;
         world_step<CtaTeam, kTree>(S, q.ctaList[slot], cta, g_dynamic_smem, g_dynamic_smem + q.ctaB, q.ctaB,
-                   q.ctaWsWords ? g_dynamic_smem + round4(q.ctaB + q.ctaMaxN) : nullptr, q.ctaWsWords);
+                   q.ctaWsWords ? g_dynamic_smem + round4_words(q.ctaB + q.ctaMaxN) : nullptr, q.ctaWsWords, ctaState);
         __syncthreads();
     }
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const uint32_t slice = round4(q.warpB + q.warpMaxN) + q.warpWsWords;
-    uint32_t* mine = g_dynamic_smem + warp * slice;
-    WarpTeam wt;
-    for (;;) {
-        uint32_t slot = 0;
-        if (lane == 0) slot = atomicAdd(q.queue + 1, 1u);
-        slot = __shfl_sync(0xffffffffu, slot, 0);
-        if (slot >= nWarp) break;
-        world_step<WarpTeam, kTree>(S, q.warpList[slot], wt, mine, mine + q.warpB, q.warpB,
-                   q.warpWsWords ? mine + round4(q.warpB + q.warpMaxN) : nullptr, q.warpWsWords);
-        __syncwarp();
-    }
+    group_queue(q, nGroup, sh, next, [&](uint32_t wi, const GroupTeam& team, uint32_t* buckets, uint32_t* entries,
+                                         uint32_t* ws, TeamState& ts) {
+        world_step<GroupTeam, kTree>(S, wi, team, buckets, entries, q.warpB, ws, q.warpWsWords, ts);
+    });
 }
 
 // Served step kernel: the same two queues over a batch of resident worlds that each keep their own device arrays.
@@ -1565,37 +1591,35 @@ template <int kThreads, bool kTree>
 __global__ void __launch_bounds__(kThreads, 2) served_step_kernel(const DState* sets, const uint32_t* entrySlot,
                                                                    bp_step_report* reports, QueueArgs q) {
     __shared__ BlockScratch sh;
-    __shared__ uint32_t next;
+    __shared__ uint32_t next[kThreads / 32];
+    __shared__ TeamState ctaState;
     CtaTeam cta{&sh};
     for (;;) {
-        if (threadIdx.x == 0) next = atomicAdd(q.queue, 1u);
+        if (threadIdx.x == 0) next[0] = atomicAdd(q.queue, 1u);
         __syncthreads();
-        const uint32_t slot = next;
+        const uint32_t slot = next[0];
         __syncthreads();
         if (slot >= q.nCta) break;
         const uint32_t e = q.ctaList[slot];
-        DState G = sets[entrySlot[e]];
-        G.reports = reports + e;
-        world_step<CtaTeam, kTree>(G, 0u, cta, g_dynamic_smem, g_dynamic_smem + q.ctaB, q.ctaB,
-                                   q.ctaWsWords ? g_dynamic_smem + round4(q.ctaB + q.ctaMaxN) : nullptr, q.ctaWsWords);
+        if (threadIdx.x == 0) {
+            ctaState.G = sets[entrySlot[e]];
+            ctaState.G.reports = reports + e;
+        }
+        __syncthreads();
+        world_step<CtaTeam, kTree>(ctaState.G, 0u, cta, g_dynamic_smem, g_dynamic_smem + q.ctaB, q.ctaB,
+                                   q.ctaWsWords ? g_dynamic_smem + round4_words(q.ctaB + q.ctaMaxN) : nullptr, q.ctaWsWords,
+                                   ctaState);
         __syncthreads();
     }
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const uint32_t slice = round4(q.warpB + q.warpMaxN) + q.warpWsWords;
-    uint32_t* mine = g_dynamic_smem + warp * slice;
-    WarpTeam wt;
-    for (;;) {
-        uint32_t slot = 0;
-        if (lane == 0) slot = atomicAdd(q.queue + 1, 1u);
-        slot = __shfl_sync(0xffffffffu, slot, 0);
-        if (slot >= q.nWarp) break;
-        const uint32_t e = q.warpList[slot];
-        DState G = sets[entrySlot[e]];
-        G.reports = reports + e;
-        world_step<WarpTeam, kTree>(G, 0u, wt, mine, mine + q.warpB, q.warpB,
-                                    q.warpWsWords ? mine + round4(q.warpB + q.warpMaxN) : nullptr, q.warpWsWords);
-        __syncwarp();
-    }
+    group_queue(q, q.nWarp, sh, next, [&](uint32_t e, const GroupTeam& team, uint32_t* buckets, uint32_t* entries,
+                                          uint32_t* ws, TeamState& ts) {
+        if (team.leader()) {
+            ts.G = sets[entrySlot[e]];
+            ts.G.reports = reports + e;
+        }
+        team.sync();
+        world_step<GroupTeam, kTree>(ts.G, 0u, team, buckets, entries, q.warpB, ws, q.warpWsWords, ts);
+    });
 }
 
 }  // namespace

@@ -1,6 +1,6 @@
-// bp_team.cuh - execution teams for the world step: a CTA (one world per thread block) or the whole grid of a
-// cooperative launch (one large world). Both provide sync, deterministic (value, owner) reductions with the lower
-// index winning ties, exclusive scans and sums. The grid barrier is bounded: a wait that runs out sets the error
+// bp_team.cuh - execution teams for the world step: a CTA (one world per thread block), a group of warps of a block
+// (one world per group, several groups per block) or the whole grid of a cooperative launch (one large world). All
+// provide sync, deterministic (value, owner) reductions with the lower index winning ties, exclusive scans and sums. The grid barrier is bounded: a wait that runs out sets the error
 // flag and every block leaves the kernel at its next check, so no launch can spin forever.
 #pragma once
 
@@ -70,17 +70,39 @@ struct BlockScratch {
     uint32_t u4[4][33];
 };
 
-// Four sums (kMaxMask bit c set: maximum instead of sum for component c) in one block reduction.
-template <uint32_t kMaxMask> __device__ __forceinline__ void block_reduce4(uint32_t (&v)[4], BlockScratch& sh) {
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = (blockDim.x + 31u) >> 5;
+// Threads that reduce together: the whole block (BlockShape), or a group of consecutive warps of it (GroupShape),
+// synchronised by a named barrier of its own so the groups of a block run independently. Every reduction below ends
+// with a synchronisation of the shape, so it also orders the shared-memory writes made before it.
+struct BlockShape {
+    __device__ __forceinline__ uint32_t tid() const { return threadIdx.x; }
+    __device__ __forceinline__ uint32_t count() const { return blockDim.x; }
+    __device__ __forceinline__ void sync() const { __syncthreads(); }
+};
+struct GroupShape {
+    uint32_t base;   // first thread of the group (a multiple of 32)
+    uint32_t width;  // threads in the group (a multiple of 32)
+    uint32_t id;     // named barrier of the group (1..15); a one-warp group synchronises with __syncwarp
+    __device__ __forceinline__ uint32_t tid() const { return threadIdx.x - base; }
+    __device__ __forceinline__ uint32_t count() const { return width; }
+    __device__ __forceinline__ void sync() const {
+        if (width == 32u) __syncwarp();
+        else asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(width) : "memory");
+    }
+};
+
+// Four sums (kMaxMask bit c set: maximum instead of sum for component c) in one reduction over the shape.
+template <uint32_t kMaxMask, class Shape>
+__device__ __forceinline__ void shape_reduce4(uint32_t (&v)[4], BlockScratch& sh, const Shape& g) {
+    const uint32_t lane = threadIdx.x & 31u, warp = g.tid() >> 5, nw = (g.count() + 31u) >> 5;
 #pragma unroll
     for (int c = 0; c < 4; ++c) v[c] = ((kMaxMask >> c) & 1u) ? warp_max(v[c]) : warp_sum(v[c]);
-    __syncthreads();
+    if (nw == 1u) { g.sync(); return; }
+    g.sync();
     if (lane == 0) {
 #pragma unroll
         for (int c = 0; c < 4; ++c) sh.u4[c][warp] = v[c];
     }
-    __syncthreads();
+    g.sync();
     if (warp == 0) {
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
@@ -89,36 +111,44 @@ template <uint32_t kMaxMask> __device__ __forceinline__ void block_reduce4(uint3
             if (lane == 0) sh.u4[c][32] = y;
         }
     }
-    __syncthreads();
+    g.sync();
 #pragma unroll
     for (int c = 0; c < 4; ++c) v[c] = sh.u4[c][32];
 }
+template <uint32_t kMaxMask> __device__ __forceinline__ void block_reduce4(uint32_t (&v)[4], BlockScratch& sh) {
+    shape_reduce4<kMaxMask>(v, sh, BlockShape{});
+}
 
-// Block-wide (value, owner) reduction; result broadcast to every thread.
-template <bool kMax> __device__ __forceinline__ ValOwner block_pick(ValOwner x, BlockScratch& sh) {
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = (blockDim.x + 31u) >> 5;
+// (value, owner) reduction over the shape; result broadcast to every thread.
+template <bool kMax, class Shape> __device__ __forceinline__ ValOwner shape_pick(ValOwner x, BlockScratch& sh, const Shape& g) {
+    const uint32_t lane = threadIdx.x & 31u, warp = g.tid() >> 5, nw = (g.count() + 31u) >> 5;
     x = warp_pick<kMax>(x);
-    __syncthreads();
+    if (nw == 1u) { g.sync(); return x; }
+    g.sync();
     if (lane == 0) { sh.fv[warp] = x.v; sh.uo[warp] = x.o; }
-    __syncthreads();
+    g.sync();
     if (warp == 0) {
         ValOwner y = lane < nw ? ValOwner{sh.fv[lane], sh.uo[lane]} : x;
         y = warp_pick<kMax>(y);
         if (lane == 0) { sh.fv[0] = y.v; sh.uo[0] = y.o; }
     }
-    __syncthreads();
+    g.sync();
     return ValOwner{sh.fv[0], sh.uo[0]};
+}
+template <bool kMax> __device__ __forceinline__ ValOwner block_pick(ValOwner x, BlockScratch& sh) {
+    return shape_pick<kMax>(x, sh, BlockShape{});
 }
 
 // Two (value, owner) reductions in the barriers of one (kMaxA / kMaxB: maximum or minimum).
-template <bool kMaxA, bool kMaxB>
-__device__ __forceinline__ void block_pick2(ValOwner& a, ValOwner& b, BlockScratch& sh) {
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = (blockDim.x + 31u) >> 5;
+template <bool kMaxA, bool kMaxB, class Shape>
+__device__ __forceinline__ void shape_pick2(ValOwner& a, ValOwner& b, BlockScratch& sh, const Shape& g) {
+    const uint32_t lane = threadIdx.x & 31u, warp = g.tid() >> 5, nw = (g.count() + 31u) >> 5;
     a = warp_pick<kMaxA>(a);
     b = warp_pick<kMaxB>(b);
-    __syncthreads();
+    if (nw == 1u) { g.sync(); return; }
+    g.sync();
     if (lane == 0) { sh.fv[warp] = a.v; sh.uo[warp] = a.o; sh.fv2[warp] = b.v; sh.uo2[warp] = b.o; }
-    __syncthreads();
+    g.sync();
     if (warp == 0) {
         ValOwner x = lane < nw ? ValOwner{sh.fv[lane], sh.uo[lane]} : a;
         ValOwner y = lane < nw ? ValOwner{sh.fv2[lane], sh.uo2[lane]} : b;
@@ -126,69 +156,89 @@ __device__ __forceinline__ void block_pick2(ValOwner& a, ValOwner& b, BlockScrat
         y = warp_pick<kMaxB>(y);
         if (lane == 0) { sh.fv[0] = x.v; sh.uo[0] = x.o; sh.fv2[0] = y.v; sh.uo2[0] = y.o; }
     }
-    __syncthreads();
+    g.sync();
     a = ValOwner{sh.fv[0], sh.uo[0]};
     b = ValOwner{sh.fv2[0], sh.uo2[0]};
 }
+template <bool kMaxA, bool kMaxB>
+__device__ __forceinline__ void block_pick2(ValOwner& a, ValOwner& b, BlockScratch& sh) {
+    shape_pick2<kMaxA, kMaxB>(a, b, sh, BlockShape{});
+}
 
-__device__ __forceinline__ uint32_t block_sum(uint32_t x, BlockScratch& sh) {
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = (blockDim.x + 31u) >> 5;
-    x = warp_sum(x);
-    __syncthreads();
+template <class Shape> __device__ __forceinline__ uint32_t shape_reduce_u(uint32_t x, bool isMax, BlockScratch& sh, const Shape& g) {
+    const uint32_t lane = threadIdx.x & 31u, warp = g.tid() >> 5, nw = (g.count() + 31u) >> 5;
+    x = isMax ? warp_max(x) : warp_sum(x);
+    if (nw == 1u) { g.sync(); return x; }
+    g.sync();
     if (lane == 0) sh.u[warp] = x;
-    __syncthreads();
+    g.sync();
     if (warp == 0) {
         uint32_t y = lane < nw ? sh.u[lane] : 0u;
-        y = warp_sum(y);
+        y = isMax ? warp_max(y) : warp_sum(y);
         if (lane == 0) sh.u[32] = y;
     }
-    __syncthreads();
+    g.sync();
     return sh.u[32];
 }
-__device__ __forceinline__ uint32_t block_max(uint32_t x, BlockScratch& sh) {
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = (blockDim.x + 31u) >> 5;
-    x = warp_max(x);
-    __syncthreads();
-    if (lane == 0) sh.u[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-        uint32_t y = lane < nw ? sh.u[lane] : 0u;
-        y = warp_max(y);
-        if (lane == 0) sh.u[32] = y;
-    }
-    __syncthreads();
-    return sh.u[32];
-}
-__device__ __forceinline__ float block_fmax(float x, BlockScratch& sh) {
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = (blockDim.x + 31u) >> 5;
+__device__ __forceinline__ uint32_t block_sum(uint32_t x, BlockScratch& sh) { return shape_reduce_u(x, false, sh, BlockShape{}); }
+__device__ __forceinline__ uint32_t block_max(uint32_t x, BlockScratch& sh) { return shape_reduce_u(x, true, sh, BlockShape{}); }
+
+template <class Shape> __device__ __forceinline__ float shape_fmax(float x, BlockScratch& sh, const Shape& g) {
+    const uint32_t lane = threadIdx.x & 31u, warp = g.tid() >> 5, nw = (g.count() + 31u) >> 5;
     x = warp_fmax(x);
-    __syncthreads();
+    if (nw == 1u) { g.sync(); return x; }
+    g.sync();
     if (lane == 0) sh.fv[warp] = x;
-    __syncthreads();
+    g.sync();
     if (warp == 0) {
         float y = lane < nw ? sh.fv[lane] : x;
         y = warp_fmax(y);
         if (lane == 0) sh.fv[0] = y;
     }
-    __syncthreads();
+    g.sync();
     return sh.fv[0];
 }
-// Exclusive scan of one value per thread; *total receives the block total.
-__device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t* total, BlockScratch& sh) {
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = (blockDim.x + 31u) >> 5;
+__device__ __forceinline__ float block_fmax(float x, BlockScratch& sh) { return shape_fmax(x, sh, BlockShape{}); }
+
+// Exclusive scan of one value per thread over the shape; *total receives the shape's total.
+template <class Shape>
+__device__ __forceinline__ uint32_t shape_excl_scan(uint32_t x, uint32_t* total, BlockScratch& sh, const Shape& g) {
+    const uint32_t lane = threadIdx.x & 31u, warp = g.tid() >> 5, nw = (g.count() + 31u) >> 5;
     uint32_t incl = warp_incl_scan(x);
-    __syncthreads();
-    if (lane == 31u || threadIdx.x == blockDim.x - 1) sh.u[warp] = incl;
-    __syncthreads();
+    if (nw == 1u) {
+        *total = __shfl_sync(0xffffffffu, incl, 31);
+        g.sync();
+        return incl - x;
+    }
+    g.sync();
+    if (lane == 31u || g.tid() == g.count() - 1) sh.u[warp] = incl;
+    g.sync();
     if (warp == 0) {
         uint32_t y = lane < nw ? sh.u[lane] : 0u;
         uint32_t s = warp_incl_scan(y);
         if (lane < nw) sh.u[lane] = s - y;
         if (lane == nw - 1) sh.u[32] = s;
     }
-    __syncthreads();
+    g.sync();
     *total = sh.u[32];
     return sh.u[warp] + incl - x;
+}
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t* total, BlockScratch& sh) {
+    return shape_excl_scan(x, total, sh, BlockShape{});
+}
+
+// Exclusive scan of `count` values in place over the shape (values in memory visible to the whole shape).
+template <class Shape> __device__ __forceinline__ void shape_scan_inplace(uint32_t* values, uint32_t count, BlockScratch& sh, const Shape& g) {
+    const uint32_t T = g.count(), r = g.tid();
+    uint32_t per = (count + T - 1) / T;
+    uint32_t first = min(r * per, count), last = min(first + per, count);
+    uint32_t local = 0;
+    if (T == 32u) __syncwarp();
+    for (uint32_t i = first; i < last; ++i) local += values[i];
+    uint32_t total;
+    uint32_t running = shape_excl_scan(local, &total, sh, g);
+    for (uint32_t i = first; i < last; ++i) { uint32_t own = values[i]; values[i] = running; running += own; }
+    g.sync();
 }
 
 // ----------------------------------------------------------------------------------------------------------------
@@ -200,6 +250,9 @@ struct CtaTeam {
     __device__ uint32_t size() const { return blockDim.x; }
     __device__ bool leader() const { return threadIdx.x == 0; }
     __device__ bool sync() const { __syncthreads(); return true; }
+    // the thread that writes the team's shared-memory records, and the barrier after it
+    __device__ bool shared_leader() const { return threadIdx.x == 0; }
+    __device__ void shared_sync() const { __syncthreads(); }
     __device__ bool ok() const { return true; }
     template <bool kMax> __device__ ValOwner pick(ValOwner x) const { return block_pick<kMax>(x, *sh); }
     template <bool kMaxA, bool kMaxB> __device__ void pick2(ValOwner& a, ValOwner& b) const {
@@ -211,56 +264,34 @@ struct CtaTeam {
     template <uint32_t kMaxMask> __device__ void reduce4(uint32_t (&v)[4]) const { block_reduce4<kMaxMask>(v, *sh); }
     // Exclusive scan of `count` values in place (values live in memory visible to the whole team).
     __device__ void scan_inplace(uint32_t* values, uint32_t count) const {
-        uint32_t per = (count + blockDim.x - 1) / blockDim.x;
-        uint32_t first = min(threadIdx.x * per, count), last = min(first + per, count);
-        uint32_t local = 0;
-        for (uint32_t i = first; i < last; ++i) local += values[i];
-        uint32_t total;
-        uint32_t running = block_excl_scan(local, &total, *sh);
-        for (uint32_t i = first; i < last; ++i) { uint32_t own = values[i]; values[i] = running; running += own; }
-        __syncthreads();
+        shape_scan_inplace(values, count, *sh, BlockShape{});
     }
 };
 
 // ----------------------------------------------------------------------------------------------------------------
-// Warp team: one warp owns a small world; syncs are __syncwarp and reductions are shuffles (no block barrier).
+// Group team: a group of consecutive warps of a block owns a world; the block's groups step different worlds at the
+// same time, each synchronised by its own named barrier (bar.sync id, width), so a block keeps several small and
+// medium worlds in flight instead of one. A one-warp group synchronises with __syncwarp and reduces with shuffles.
 // ----------------------------------------------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t warp_excl_scan(uint32_t x, uint32_t* total) {
-    uint32_t incl = warp_incl_scan(x);
-    *total = __shfl_sync(0xffffffffu, incl, 31);
-    return incl - x;
-}
-
-struct WarpTeam {
-    __device__ uint32_t rank() const { return threadIdx.x & 31u; }
-    __device__ uint32_t size() const { return 32u; }
-    __device__ bool leader() const { return (threadIdx.x & 31u) == 0u; }
-    __device__ bool sync() const { __syncwarp(); return true; }
+struct GroupTeam {
+    BlockScratch* sh;  // the group's own scratch
+    GroupShape g;
+    __device__ uint32_t rank() const { return g.tid(); }
+    __device__ uint32_t size() const { return g.width; }
+    __device__ bool leader() const { return g.tid() == 0u; }
+    __device__ bool sync() const { g.sync(); return true; }
+    __device__ bool shared_leader() const { return g.tid() == 0u; }
+    __device__ void shared_sync() const { g.sync(); }
     __device__ bool ok() const { return true; }
-    template <bool kMax> __device__ ValOwner pick(ValOwner x) const { return warp_pick<kMax>(x); }
+    template <bool kMax> __device__ ValOwner pick(ValOwner x) const { return shape_pick<kMax>(x, *sh, g); }
     template <bool kMaxA, bool kMaxB> __device__ void pick2(ValOwner& a, ValOwner& b) const {
-        a = warp_pick<kMaxA>(a);
-        b = warp_pick<kMaxB>(b);
+        shape_pick2<kMaxA, kMaxB>(a, b, *sh, g);
     }
-    __device__ uint32_t sum(uint32_t x) const { return warp_sum(x); }
-    __device__ uint32_t umax(uint32_t x) const { return warp_max(x); }
-    __device__ float fmax(float x) const { return warp_fmax(x); }
-    template <uint32_t kMaxMask> __device__ void reduce4(uint32_t (&v)[4]) const {
-#pragma unroll
-        for (int c = 0; c < 4; ++c) v[c] = ((kMaxMask >> c) & 1u) ? warp_max(v[c]) : warp_sum(v[c]);
-    }
-    __device__ void scan_inplace(uint32_t* values, uint32_t count) const {
-        const uint32_t lane = threadIdx.x & 31u;
-        uint32_t per = (count + 31u) / 32u;
-        uint32_t first = min(lane * per, count), last = min(first + per, count);
-        uint32_t local = 0;
-        __syncwarp();
-        for (uint32_t i = first; i < last; ++i) local += values[i];
-        uint32_t total;
-        uint32_t running = warp_excl_scan(local, &total);
-        for (uint32_t i = first; i < last; ++i) { uint32_t own = values[i]; values[i] = running; running += own; }
-        __syncwarp();
-    }
+    __device__ uint32_t sum(uint32_t x) const { return shape_reduce_u(x, false, *sh, g); }
+    __device__ uint32_t umax(uint32_t x) const { return shape_reduce_u(x, true, *sh, g); }
+    __device__ float fmax(float x) const { return shape_fmax(x, *sh, g); }
+    template <uint32_t kMaxMask> __device__ void reduce4(uint32_t (&v)[4]) const { shape_reduce4<kMaxMask>(v, *sh, g); }
+    __device__ void scan_inplace(uint32_t* values, uint32_t count) const { shape_scan_inplace(values, count, *sh, g); }
 };
 
 // ----------------------------------------------------------------------------------------------------------------
@@ -282,6 +313,9 @@ struct GridTeam {
     __device__ uint32_t rank() const { return blockIdx.x * blockDim.x + threadIdx.x; }
     __device__ uint32_t size() const { return gridDim.x * blockDim.x; }
     __device__ bool leader() const { return blockIdx.x == 0 && threadIdx.x == 0; }
+    // every block keeps its own copy of the team's shared-memory records
+    __device__ bool shared_leader() const { return threadIdx.x == 0; }
+    __device__ void shared_sync() const { __syncthreads(); }
     __device__ bool ok() const { return !failed; }
 
     // Bounded grid barrier (generation counter). Returns false when any block gave up waiting.

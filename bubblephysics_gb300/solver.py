@@ -186,7 +186,7 @@ class Batch:
     per_world_launch=True, the plain path: one launch per world, one after another)."""
 
     def __init__(self, specs: list[WorldSpec], context: Context | None = None, *, per_world_launch=False,
-                 use_graph=True, autotune=False, threads_per_world=0, warp_world_max=0):
+                 use_graph=True, autotune=False, threads_per_world=0, warp_world_max=0, group_width=0):
         self.ctx = context or default_context()
         self.lib = self.ctx.lib
         self.specs = specs
@@ -198,6 +198,7 @@ class Batch:
                     (N.BATCH_AUTOTUNE if autotune else 0)
         cfg.threads_per_world = threads_per_world
         cfg.warp_world_max = warp_world_max
+        cfg.group_width = group_width
         handle = C.c_void_p()
         N.check(self.lib.bp_batch_create(self.ctx.handle, len(specs), descs, inputs, C.byref(cfg), C.byref(handle)),
                 "bp_batch_create")
@@ -255,9 +256,9 @@ class Batch:
         return v.value
 
     def tuning(self) -> dict:
-        out = (C.c_uint32 * 5)()
-        N.check(self.lib.bp_batch_tuning(self.handle, out, 5), "bp_batch_tuning")
-        return dict(zip(["threads", "warp_max", "blocks", "cta_worlds", "warp_worlds"], list(out)))
+        out = (C.c_uint32 * 6)()
+        N.check(self.lib.bp_batch_tuning(self.handle, out, 6), "bp_batch_tuning")
+        return dict(zip(["threads", "warp_max", "blocks", "cta_worlds", "warp_worlds", "group_width"], list(out)))
 
 
 def static_polygon_edges(points, first_id: int, owner_id: int | None = None) -> np.ndarray:
@@ -287,7 +288,7 @@ class Server:
 
     def __init__(self, max_worlds: int, context: Context | None = None, *, hbm_budget_bytes: int = 0,
                  max_batch_worlds: int = 0, streams: int = 0, threads_per_world: int = 0, warp_world_max: int = 0,
-                 per_world: bool = False):
+                 group_width: int = 0, per_world: bool = False):
         self.ctx = context or default_context()
         self.lib = self.ctx.lib
         cfg = N.ServerConfig()
@@ -297,6 +298,7 @@ class Server:
         cfg.streams = streams
         cfg.threads_per_world = threads_per_world
         cfg.warp_world_max = warp_world_max
+        cfg.group_width = group_width
         cfg.flags = N.SERVER_PER_WORLD if per_world else 0
         handle = C.c_void_p()
         N.check(self.lib.bp_server_create(self.ctx.handle, C.byref(cfg), C.byref(handle)), "bp_server_create")

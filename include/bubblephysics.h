@@ -321,9 +321,11 @@ enum {
 typedef struct bp_batch_config {
     uint32_t flags;                  /* BP_BATCH_* */
     uint32_t threads_per_world;      /* threads per block of the persistent launch, 0 = automatic (autotuner or 256) */
-    uint32_t warp_world_max;         /* worlds of at most this many bubbles are stepped by one warp; 0 = automatic
-                                        (autotuner or 64); UINT32_MAX = no warp teams */
-    uint32_t reserved;
+    uint32_t warp_world_max;         /* worlds of at most this many bubbles go to the group queue (a group of
+                                        group_width threads per world); 0 = automatic (autotuner or 64);
+                                        UINT32_MAX = no group queue */
+    uint32_t group_width;            /* threads of one group-queue team: 32, 64, 128 or 256, at most the block
+                                        width; 0 = automatic (autotuner or 32) */
 } bp_batch_config;
 
 int bp_batch_create(bp_context* context, uint32_t world_count, const bp_world_desc* descs,
@@ -342,8 +344,8 @@ int bp_batch_read_state(bp_batch* batch, float* center_velocity, uint64_t bubble
 /* Sum of the adjacency degrees of all bubbles of the last grid build (mean degree = sum / bubbles); used to count
  * the algorithmic bytes of a substep. */
 int bp_batch_adjacency_entries(bp_batch* batch, uint64_t* entries);
-/* Schedule of the batched launch: [0] threads per block, [1] largest world stepped by one warp, [2] blocks of the
- * persistent launch, [3] worlds stepped by a whole block, [4] worlds stepped by one warp. */
+/* Schedule of the batched launch: [0] threads per block, [1] largest world of the group queue, [2] blocks of the
+ * persistent launch, [3] worlds stepped by a whole block, [4] worlds of the group queue, [5] threads of one group. */
 int bp_batch_tuning(bp_batch* batch, uint32_t* values, uint32_t count);
 
 /* ---- contours (draw-only output of the step) ------------------------------------------------------------------ */
@@ -444,8 +446,11 @@ typedef struct bp_server_config {
     uint32_t max_batch_worlds;       /* worlds per batched launch; 0 = no limit */
     uint32_t streams;                /* batches in flight at once; 0 = 8 */
     uint32_t threads_per_world;      /* block width for worlds stepped by a block (128, 256, 512); 0 = 512 */
-    uint32_t warp_world_max;         /* worlds of at most this many bubbles get one warp; 0 = 64, UINT32_MAX = none */
+    uint32_t warp_world_max;         /* worlds of at most this many bubbles go to the group queue (a group of
+                                        group_width threads per world); 0 = 64, UINT32_MAX = none */
     uint32_t flags;                  /* BP_SERVER_* */
+    uint32_t group_width;            /* threads of one group-queue team: 32, 64, 128 or 256; 0 = 32 */
+    uint32_t reserved;
 } bp_server_config;
 
 /* A finished request. Times are seconds of bp_server_clock(). 136 bytes. */
