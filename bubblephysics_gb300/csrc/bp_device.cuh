@@ -207,10 +207,10 @@ __host__ __device__ inline uint32_t contour_samples(float r, float maxEdge, uint
     return count < stride ? count : stride;
 }
 
-// Bytes of a world's shared-memory workspace: per bubble 88 B of hot state, per segment and body a 32 B box, per body
-// a 16 B pose; the 15 parts are each padded to 16 bytes.
+// Bytes of a world's shared-memory workspace: per bubble 104 B of hot state (88 B of state and 16 B of grid cell), per
+// segment and body a 32 B box, per body a 16 B pose; the 16 parts are each padded to 16 bytes.
 __host__ __device__ inline uint32_t workspace_bytes(uint32_t n, uint32_t s, uint32_t nb) {
-    return n * 88u + s * 32u + nb * 48u + 15u * 16u;
+    return n * 104u + s * 32u + nb * 48u + 16u * 16u;
 }
 
 // ------------------------------------------------------------------------------------------------------------------

@@ -20,7 +20,8 @@ namespace bp {
 // compiles its own copy of the device code.
 namespace {
 
-constexpr uint32_t kValid = 0x40000000u;  // bubble is in the grid of the current build
+constexpr uint32_t kValid = 0x40000000u;        // bubble is in the grid of the current build
+constexpr uint32_t kStartFinite = 0x20000000u;  // the step-start centre is finite (set when the step begins)
 constexpr uint32_t kLive = 0xffu;         // mask of the public flags
 
 // Optional per-phase cycle counters (leader thread's clock) for profiling builds (-DBP_PHASE_TIMING).
@@ -431,7 +432,7 @@ __device__ __forceinline__ void body_hit(const DState& S, const DWorld& W, uint3
 // of row j; whether row j kept i is checked once every row is built (finish_adjacency).
 __device__ __forceinline__ void lower_pair(const DState& S, const DWorld& W, uint32_t i, uint32_t j, uint32_t* adjRow,
                                            uint32_t& kept, uint32_t& total) {
-    if (!finite2(S.start[W.boff + j])) return;
+    if (!(S.flags[W.boff + j] & kStartFinite)) return;
     if (!pair_accepts(S, W, j, i)) return;
     ++total;
     insert_sorted(adjRow, kept, W.k, j);
@@ -447,7 +448,7 @@ __device__ void emit_row(const DState& S, const DWorld& W, const uint32_t* bucke
     uint32_t* row = S.candRow + W.rowOff + (uint64_t)i * k;
     uint32_t* adjRow = S.adj + W.rowOff + (uint64_t)i * k;
     uint32_t lowerKept = 0, lowerTotal = 0;
-    if (!(S.flags[g] & kValid) || !finite2(S.start[g])) {
+    if (!(S.flags[g] & kValid) || !(S.flags[g] & kStartFinite)) {
         S.candCount[g] = make_uint2(0u, 0u);
         S.pairTotal[g] = 0u;
         if (S.flags[g] & kValid) {  // a valid cell with a non-finite step start: no row, but lower pairs still count
@@ -600,7 +601,7 @@ __device__ void build_adjacency(const DState& S, const DWorld& W, const uint32_t
                 for_each_in_cell(S.cell, W, buckets, entries, B, c.x + dx, c.y + dy, [&](uint32_t j) {
                     if (j >= i) return;
                     uint32_t gj = W.boff + j;
-                    if (!finite2(S.start[gj])) return;
+                    if (!(S.flags[gj] & kStartFinite)) return;
                     if (!pair_accepts(S, W, j, i)) return;
                     if (S.pairTotal[gj] > k && !row_contains(S.candRow + W.rowOff + (uint64_t)j * k, S.candCount[gj].x, i)) return;
                     ++demanded;
@@ -1205,6 +1206,7 @@ __device__ bool stage_world(const DState& G, DState& S, const DWorld& W, const T
     uint32_t* flags = carve<uint32_t>(p, n);
     uint32_t* deg = carve<uint32_t>(p, n);
     uint32_t* pairTotal = carve<uint32_t>(p, n);
+    longlong2* cell = carve<longlong2>(p, n);
     RigidBox* segBox = carve<RigidBox>(p, W.s);
     RigidBox* bodyBox = carve<RigidBox>(p, W.nb);
     float4* bpose = carve<float4>(p, W.nb);
@@ -1229,6 +1231,7 @@ __device__ bool stage_world(const DState& G, DState& S, const DWorld& W, const T
         S.flags = flags - W.boff;
         S.deg = deg - W.boff;
         S.pairTotal = pairTotal - W.boff;
+        S.cell = cell - W.boff;
         S.segBox = segBox - W.soff;
         S.bodyBox = bodyBox - W.bodyOff;
         S.bpose = bpose - W.bodyOff;
@@ -1290,7 +1293,9 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
         if (f & kRemoved) continue;
         ++liveLocal;
         S.result[g] = 0u;
-        S.start[g] = S.pos[g];
+        const float2 p0 = S.pos[g];
+        S.start[g] = p0;
+        S.flags[g] = finite2(p0) ? (f | kStartFinite) : (f & ~kStartFinite);
         if ((f & BP_BUBBLE_ENABLED) && (f & BP_BUBBLE_STATIC)) {
             S.vel[g] = f2(0.0f, 0.0f);
             S.rotw[g].y = 0.0f;
@@ -1489,7 +1494,7 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
     if (status == BP_OK) {
         for (uint32_t i = r; i < n; i += T) {
             uint32_t g = W.boff + i;
-            uint32_t f = S.flags[g] & ~kValid;
+            uint32_t f = S.flags[g] & ~(kValid | kStartFinite);
             if (G.result[g] == 1u) f |= kRemoved;
             float2 p = S.pos[g], v = S.vel[g];
             G.flags[g] = f;
@@ -1505,6 +1510,7 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
             G.candCount[g] = S.candCount[g];
             G.pairTotal[g] = S.pairTotal[g];
             G.deg[g] = S.deg[g];
+            G.cell[g] = S.cell[g];
         }
         for (uint32_t bi = r; bi < W.nb; bi += T) G.pBody[W.bodyOff + bi] = G.body[W.bodyOff + bi];
     } else {
@@ -1519,6 +1525,7 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
             G.candCount[g] = S.candCount[g];
             G.pairTotal[g] = S.pairTotal[g];
             G.deg[g] = S.deg[g];
+            G.cell[g] = S.cell[g];
         }
         for (uint32_t bi = r; bi < W.nb; bi += T) G.body[W.bodyOff + bi] = G.pBody[W.bodyOff + bi];
         if (team.leader()) G.failed[wi] = 1u;
