@@ -192,6 +192,9 @@ CONTACT_DTYPE = np.dtype({"names": ["participants", "kind", "feature", "normal",
 SENSOR_EVENT_DTYPE = np.dtype({"names": ["sensor", "object", "kind", "point", "object_kind"],
                                "formats": ["<i8", "<i8", "<u4", ("<f4", 2), "<u4"],
                                "offsets": [0, 8, 16, 20, 28], "itemsize": 32})
+CONTACT_EVENT_DTYPE = np.dtype({"names": ["kind", "reserved", "objects", "point", "normal", "impulse", "reserved2"],
+                                "formats": ["<u4", "<u4", ("<i8", 2), ("<f4", 2), ("<f4", 2), "<f4", "<f4"],
+                                "offsets": [0, 4, 8, 24, 32, 40, 44], "itemsize": 48})
 KEY_DTYPE = np.dtype({"names": ["kind", "reserved", "first", "second"], "formats": ["<u4", "<u4", "<i8", "<i8"],
                       "offsets": [0, 4, 8, 16], "itemsize": 24})
 REPORT_DTYPE = np.dtype({"names": [n for n, _ in StepReport._fields_],
@@ -227,6 +230,10 @@ _SIGNATURES = {
     "bp_world_step": (C.c_int, [_P, C.c_uint32, _P]),
     "bp_world_read_bubbles": (C.c_int, [_P, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
     "bp_world_read_contacts": (C.c_int, [_P, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
+    "bp_world_contact_events": (C.c_int, [_P, _P, C.c_uint32, _P, C.c_uint32, _P, C.c_uint32, C.c_float, _P, C.c_uint32,
+                                          C.POINTER(C.c_uint32)]),
+    "bp_world_set_contact_history": (C.c_int, [_P, _P, C.c_uint32]),
+    "bp_world_read_contact_history": (C.c_int, [_P, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
     "bp_world_read_candidates": (C.c_int, [_P, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
     "bp_world_read_cells": (C.c_int, [_P, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
     "bp_world_read_rigid_keys": (C.c_int, [_P, _P, C.c_uint32, C.POINTER(C.c_uint32)]),

@@ -33,6 +33,7 @@ static_assert(sizeof(bp_contact) == 64, "bp_contact layout");
 static_assert(sizeof(bp_candidate_key) == 24, "bp_candidate_key layout");
 static_assert(sizeof(bp_sensor) == 48 && sizeof(bp_sensor_event) == 32, "sensor record layouts");
 static_assert(sizeof(bp_contour_config) == 16, "bp_contour_config layout");
+static_assert(sizeof(bp_contact_event) == 48, "bp_contact_event layout");
 static_assert(offsetof(bp_bubble, center) == 8 && offsetof(bp_bubble, flags) == 60, "bp_bubble offsets");
 static_assert(offsetof(bp_step_report, limiter_object) == 40, "bp_step_report offsets");
 
@@ -1144,6 +1145,165 @@ int bp_world_read_sensor_events(bp_world* world, bp_sensor_event* out, uint32_t 
     const uint32_t m = std::min(std::min(c, capacity), ws.sensorEventCapacity);
     if (out && m) err = cudaMemcpy(out, ws.dSensorEvents, m * sizeof(bp_sensor_event), cudaMemcpyDeviceToHost);
     return cuda_status(err);
+}
+
+// ---- contact events ---------------------------------------------------------------------------------------------
+
+}  // extern "C"
+
+namespace {
+// Grows the history buffers to hold `keys` pair keys, keeping the current history.
+cudaError_t history_reserve(WorldSet::EventState& ev, uint32_t keys) {
+    if (keys <= ev.historyCap) return cudaSuccess;
+    const uint32_t cap = std::max({keys, 2u * ev.historyCap, 256u});
+    unsigned long long* fresh[2] = {nullptr, nullptr};
+    cudaError_t err = cudaMalloc(&fresh[0], 2ull * cap * sizeof(unsigned long long));
+    if (!err) err = cudaMalloc(&fresh[1], 2ull * cap * sizeof(unsigned long long));
+    if (!err && ev.historyCount)
+        err = cudaMemcpy(fresh[0], ev.history[ev.current], 2ull * ev.historyCount * sizeof(unsigned long long),
+                         cudaMemcpyDeviceToDevice);
+    if (err) {
+        cudaFree(fresh[0]);
+        cudaFree(fresh[1]);
+        return err;
+    }
+    cudaFree(ev.history[0]);
+    cudaFree(ev.history[1]);
+    ev.history[0] = fresh[0];
+    ev.history[1] = fresh[1];
+    ev.current = 0;
+    ev.historyCap = cap;
+    return cudaSuccess;
+}
+
+size_t align256(size_t v) { return (v + 255u) & ~(size_t)255u; }
+}  // namespace
+
+extern "C" {
+
+int bp_world_set_contact_history(bp_world* world, const int64_t* pairs, uint32_t pair_count) {
+    if (!world || (!pairs && pair_count)) return BP_E_INVALID;
+    WorldSet& ws = world->set;
+    DeviceGuard guard(ws.ctx->device);
+    std::vector<std::pair<uint64_t, uint64_t>> keys(pair_count);
+    for (uint32_t q = 0; q < pair_count; ++q) {
+        const uint64_t a = (uint64_t)pairs[2 * q], b = (uint64_t)pairs[2 * q + 1];
+        keys[q] = a <= b ? std::make_pair(a, b) : std::make_pair(b, a);
+    }
+    std::sort(keys.begin(), keys.end());
+    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+    WorldSet::EventState& ev = ws.events;
+    ev.historyCount = 0;
+    cudaError_t err = history_reserve(ev, (uint32_t)keys.size());
+    if (err) return cuda_status(err);
+    std::vector<unsigned long long> flat(2 * keys.size());
+    for (size_t q = 0; q < keys.size(); ++q) { flat[2 * q] = keys[q].first; flat[2 * q + 1] = keys[q].second; }
+    if (!flat.empty())
+        err = cudaMemcpy(ev.history[ev.current], flat.data(), flat.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice);
+    if (err) return cuda_status(err);
+    ev.historyCount = (uint32_t)keys.size();
+    return BP_OK;
+}
+
+int bp_world_read_contact_history(bp_world* world, int64_t* pairs, uint32_t capacity, uint32_t* count) {
+    if (!world) return BP_E_INVALID;
+    WorldSet& ws = world->set;
+    const WorldSet::EventState& ev = ws.events;
+    if (count) *count = ev.historyCount;
+    if (!pairs || !ev.historyCount) return BP_OK;
+    DeviceGuard guard(ws.ctx->device);
+    const uint32_t m = std::min(capacity, ev.historyCount);
+    cudaError_t err = m ? cudaMemcpy(pairs, ev.history[ev.current], 2ull * m * sizeof(int64_t), cudaMemcpyDeviceToHost)
+                        : cudaSuccess;
+    return cuda_status(err);
+}
+
+int bp_world_contact_events(bp_world* world, const int64_t* interested_ids, uint32_t interested_count,
+                            const int64_t* removed_ids, uint32_t removed_count, const bp_contact* extra,
+                            uint32_t extra_count, float step_seconds, bp_contact_event* out, uint32_t capacity,
+                            uint32_t* count) {
+    if (!world || (!interested_ids && interested_count) || (!removed_ids && removed_count) ||
+        (!extra && extra_count) || (!out && capacity) || !(step_seconds > 0.0f) || !std::isfinite(step_seconds))
+        return BP_E_INVALID;
+    WorldSet& ws = world->set;
+    if (ws.inflight) return BP_E_INFLIGHT;
+    DeviceGuard guard(ws.ctx->device);
+    cudaStream_t st = ws.ctx->stream;
+    const DWorld& W = ws.hWorlds[0];
+    uint32_t deviceCount = 0;
+    cudaError_t err = cudaMemcpy(&deviceCount, ws.S.contactCount, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    if (err) return cuda_status(err);
+    const uint32_t records = deviceCount + extra_count;
+    std::vector<int64_t> interested(interested_ids, interested_ids + interested_count);
+    std::vector<int64_t> removed(removed_ids, removed_ids + removed_count);
+    std::sort(interested.begin(), interested.end());
+    std::sort(removed.begin(), removed.end());
+    WorldSet::EventState& ev = ws.events;
+    err = history_reserve(ev, std::max(records, ev.historyCount));
+    if (err) return cuda_status(err);
+    uint32_t pow2 = 1;
+    while (pow2 < records) pow2 <<= 1;
+    // scratch: entries | order | heads | interested | removed | extra | events | counts
+    size_t off[9];
+    off[0] = 0;
+    off[1] = off[0] + align256((size_t)records * event_entry_bytes());
+    off[2] = off[1] + align256((size_t)pow2 * 4u);
+    off[3] = off[2] + align256((size_t)records * 4u);
+    off[4] = off[3] + align256((size_t)interested_count * 8u);
+    off[5] = off[4] + align256((size_t)removed_count * 8u);
+    off[6] = off[5] + align256((size_t)extra_count * sizeof(bp_contact));
+    off[7] = off[6] + align256((size_t)capacity * sizeof(bp_contact_event));
+    off[8] = off[7] + align256(2u * sizeof(uint32_t));
+    if (off[8] > ev.scratchBytes) {
+        cudaFree(ev.scratch);
+        ev.scratch = nullptr;
+        ev.scratchBytes = 0;
+        err = cudaMalloc(&ev.scratch, off[8]);
+        if (err) return cuda_status(err);
+        ev.scratchBytes = off[8];
+    }
+    char* base = (char*)ev.scratch;
+    if (interested_count)
+        err = cudaMemcpyAsync(base + off[3], interested.data(), interested_count * 8ull, cudaMemcpyHostToDevice, st);
+    if (!err && removed_count)
+        err = cudaMemcpyAsync(base + off[4], removed.data(), removed_count * 8ull, cudaMemcpyHostToDevice, st);
+    if (!err && extra_count)
+        err = cudaMemcpyAsync(base + off[5], extra, extra_count * sizeof(bp_contact), cudaMemcpyHostToDevice, st);
+    if (err) return cuda_status(err);
+    uint32_t* counts = (uint32_t*)(base + off[7]);
+    EventArgsHost a;
+    a.records = ws.S.contacts + W.contactOff;
+    a.deviceCount = deviceCount;
+    a.extra = (const bp_contact*)(base + off[5]);
+    a.extraCount = extra_count;
+    a.ids = ws.S.id + W.boff;
+    a.segments = ws.S.seg + W.soff;
+    a.interested = (const int64_t*)(base + off[3]);
+    a.interestedCount = interested_count;
+    a.removed = (const int64_t*)(base + off[4]);
+    a.removedCount = removed_count;
+    a.history = ev.history[ev.current];
+    a.historyCount = ev.historyCount;
+    a.nextHistory = ev.history[ev.current ^ 1u];
+    a.nextHistoryCount = counts + 1;
+    a.step = step_seconds;
+    a.entries = base + off[0];
+    a.order = (uint32_t*)(base + off[1]);
+    a.heads = (uint32_t*)(base + off[2]);
+    a.out = (bp_contact_event*)(base + off[6]);
+    a.capacity = capacity;
+    a.count = counts;
+    err = launch_contact_events(a, st);
+    uint32_t hc[2] = {0u, 0u};
+    if (!err) err = cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, st);
+    if (!err) err = cudaStreamSynchronize(st);
+    if (!err && out && std::min(hc[0], capacity))
+        err = cudaMemcpy(out, base + off[6], std::min(hc[0], capacity) * sizeof(bp_contact_event), cudaMemcpyDeviceToHost);
+    if (err) return cuda_status(err);
+    ev.current ^= 1u;
+    ev.historyCount = hc[1];
+    if (count) *count = hc[0];
+    return BP_OK;
 }
 
 int bp_world_read_substeps(bp_world* world, float* out, uint32_t capacity, uint32_t* count) {

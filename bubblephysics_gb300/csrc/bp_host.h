@@ -36,6 +36,33 @@ cudaError_t launch_sensors(const DState& S, const DWorld& W, const void* sensors
                            bp_sensor_event* events, uint32_t capacity, uint32_t* count, cudaStream_t stream);
 size_t sensor_record_bytes();
 void sensor_to_device(const bp_sensor& in, void* out);
+// Contact began / ended events of one world's last step (bp_events.cu). Scratch: `entries` (event_entry_bytes() per
+// record), `order` (a power of two >= records words), `heads` (records words).
+struct EventArgsHost {
+    const DContact* records;
+    uint32_t deviceCount;
+    const bp_contact* extra;
+    uint32_t extraCount;
+    const int64_t* ids;
+    const DSegment* segments;
+    const int64_t* interested;
+    uint32_t interestedCount;
+    const int64_t* removed;
+    uint32_t removedCount;
+    const unsigned long long* history;
+    uint32_t historyCount;
+    unsigned long long* nextHistory;
+    uint32_t* nextHistoryCount;
+    float step;
+    void* entries;
+    uint32_t* order;
+    uint32_t* heads;
+    bp_contact_event* out;
+    uint32_t capacity;
+    uint32_t* count;
+};
+cudaError_t launch_contact_events(const EventArgsHost& args, cudaStream_t stream);
+size_t event_entry_bytes();
 cudaError_t launch_contours(const DState& S, const DWorld& W, float maxEdge, float tension, float clearance,
                             uint32_t stride, float2* points, uint32_t* counts, float* level, float* shape,
                             cudaStream_t stream);
@@ -153,6 +180,14 @@ struct WorldSet {
     uint32_t* dSensorCount = nullptr;
     uint32_t sensorCount = 0, sensorEventCapacity = 0;
     std::vector<void*> sensorAllocations;
+    // contact events (bp_world_contact_events): the history of pair keys (double-buffered on the device), the scratch
+    // of the compaction and the staging of its inputs and outputs, grown as needed
+    struct EventState {
+        unsigned long long* history[2] = {nullptr, nullptr};
+        uint32_t historyCap = 0, historyCount = 0, current = 0;
+        void* scratch = nullptr;
+        size_t scratchBytes = 0;
+    } events;
     cudaMemPool_t pool = nullptr;           // stream-ordered pool (server worlds); null: plain cudaMalloc
     bool planOnly = false;                  // server worlds: built without the batch schedule
     bool measureOnly = false;               // count the device bytes of a build without allocating or uploading
@@ -161,6 +196,9 @@ struct WorldSet {
     ~WorldSet() {
         if (graph) cudaGraphExecDestroy(graph);
         for (void* p : sensorAllocations) cudaFree(p);
+        cudaFree(events.history[0]);
+        cudaFree(events.history[1]);
+        cudaFree(events.scratch);
         for (void* p : allocations) {
             if (pool) cudaFreeAsync(p, ctx->stream);
             else cudaFree(p);

@@ -1101,7 +1101,9 @@ __device__ bool apply_region(const DState& S, const DWorld& W, uint32_t g, uint3
     return true;
 }
 
-// Contact record of candidate (i, kind, other); returns false when inactive (penetration <= -sepTol).
+// Contact record of candidate (i, kind, other); returns false when inactive (penetration <= -sepTol). With kFull
+// false only the activity is decided (the geometry up to the penetration; no law, nothing written): the counting pass.
+template <bool kFull>
 __device__ bool contact_record(const DState& S, const DWorld& W, uint32_t i, uint32_t kind, uint32_t other, DContact& out) {
     const uint32_t g = W.boff + i;
     float2 apos = S.pos[g];
@@ -1159,6 +1161,7 @@ __device__ bool contact_record(const DState& S, const DWorld& W, uint32_t i, uin
         }
     }
     if (!(pen > -W.sepTol)) return false;
+    if (!kFull) return true;
     float force;
     if (kind == 0u) {
         float4 pb = S.phys[W.boff + other];
@@ -1401,8 +1404,9 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
             uint2 cc = S.candCount[g];
             const uint32_t* crow = S.candRow + W.rowOff + (uint64_t)i * W.k;
             DContact tmp;
-            for (uint32_t e = 0; e < cc.x; ++e) cp += contact_record(S, W, i, 0u, crow[e], tmp) ? 1u : 0u;
-            for (uint32_t e = cc.x; e < cc.x + cc.y; ++e) cs += contact_record(S, W, i, 1u, crow[e] & kIndexMask, tmp) ? 1u : 0u;
+            for (uint32_t e = 0; e < cc.x; ++e) cp += contact_record<false>(S, W, i, 0u, crow[e], tmp) ? 1u : 0u;
+            for (uint32_t e = cc.x; e < cc.x + cc.y; ++e)
+                cs += contact_record<false>(S, W, i, 1u, crow[e] & kIndexMask, tmp) ? 1u : 0u;
         }
         S.scanA[g] = cp;
         S.scanB[g] = cs;
@@ -1426,7 +1430,7 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
         DContact rec;
         for (uint32_t e = 0; e < cc.x + cc.y; ++e) {
             uint32_t kind = e < cc.x ? 0u : 1u;
-            if (!contact_record(S, W, i, kind, crow[e] & kIndexMask, rec)) continue;
+            if (!contact_record<true>(S, W, i, kind, crow[e] & kIndexMask, rec)) continue;
             uint32_t slot = kind == 0u ? op++ : os++;
             if (!finite2(rec.normal) || !finite2(rec.point) || !isfinite(rec.impulse) || !isfinite(rec.penetration)) nonfinite = 1u;
             if (slot < W.contactCap) S.contacts[W.contactOff + slot] = rec;

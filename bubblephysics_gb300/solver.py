@@ -116,6 +116,38 @@ class World:
     def contacts(self) -> np.ndarray:
         return self._read(self.lib.bp_world_read_contacts, N.CONTACT_DTYPE, "bp_world_read_contacts")
 
+    def contact_events(self, interested, removed=(), step: float | None = None, extra=None,
+                       capacity: int = 0) -> np.ndarray:
+        """Contact began / ended events of the last step, compacted on the device (bp_world_contact_events):
+        interested / removed are object ids, extra a CONTACT_DTYPE array of records the step does not make (e.g.
+        bubble-body contacts), step the step's duration (the world's time step by default)."""
+        ids = np.ascontiguousarray(np.asarray(list(interested), np.int64))
+        gone = np.ascontiguousarray(np.asarray(list(removed), np.int64))
+        more = np.zeros(0, N.CONTACT_DTYPE) if extra is None else np.ascontiguousarray(extra, N.CONTACT_DTYPE)
+        dt = float(self.spec.time_step if step is None else step)
+        cap = capacity or max(64, 2 * (len(self.contacts()) + more.size + self.contact_history().shape[0]))
+        out = np.zeros(cap, N.CONTACT_EVENT_DTYPE)
+        count = C.c_uint32()
+        N.check(self.lib.bp_world_contact_events(self.handle, N.ptr(ids), ids.size, N.ptr(gone), gone.size,
+                                                 N.ptr(more), more.size, dt, C.c_void_p(out.ctypes.data), cap,
+                                                 C.byref(count)), "bp_world_contact_events")
+        return out[:min(count.value, cap)]
+
+    def set_contact_history(self, pairs):
+        arr = np.ascontiguousarray(np.asarray(pairs, np.int64).reshape(-1, 2))
+        N.check(self.lib.bp_world_set_contact_history(self.handle, N.ptr(arr), arr.shape[0]),
+                "bp_world_set_contact_history")
+
+    def contact_history(self) -> np.ndarray:
+        count = C.c_uint32()
+        N.check(self.lib.bp_world_read_contact_history(self.handle, None, 0, C.byref(count)),
+                "bp_world_read_contact_history")
+        out = np.zeros((count.value, 2), np.int64)
+        if count.value:
+            N.check(self.lib.bp_world_read_contact_history(self.handle, C.c_void_p(out.ctypes.data), count.value,
+                                                           C.byref(count)), "bp_world_read_contact_history")
+        return out
+
     def candidates(self) -> np.ndarray:
         return self._read(self.lib.bp_world_read_candidates, N.KEY_DTYPE, "bp_world_read_candidates")
 

@@ -359,6 +359,21 @@ typedef struct bp_contour_config {
     uint32_t stride;                 /* samples reserved per bubble; 0 = the largest sample count of the world */
 } bp_contour_config;
 
+/* ---- contact events (NativePublicWorld.contactTransitions, NativePublicWorld.swift:340-391) -------------------- */
+
+/* A contact began / ended event. 48 bytes. objects: the pair, the smaller id (compared as unsigned 64-bit values)
+ * first. For a began event: point = the records' penetration-weighted mean point, normal = their summed normal from
+ * objects[0] towards objects[1], normalised, impulse = their summed F dt^2 divided by the step. */
+typedef struct bp_contact_event {
+    uint32_t kind;                   /* 0 began, 1 ended */
+    uint32_t reserved;
+    int64_t objects[2];
+    float point[2];
+    float normal[2];
+    float impulse;
+    float reserved2;
+} bp_contact_event;
+
 /* Contours of the world's published state, built on the device (nativeAccumulateContactPressure,
  * nativeGenerateContoursFused and nativePrepareRenderDataGrouped, NativePostSolveKernels:280-527: one ray per sample cut
  * by the one-sided segments and by the chord r (1 - eps) of every overlapping pair, 13 smoothing passes, the
@@ -490,6 +505,23 @@ int bp_server_read_bubbles(bp_server* server, uint32_t world, bp_bubble* out, ui
 int bp_server_read_stats(bp_server* server, bp_server_stats* out);
 /* Monotonic host clock in seconds (the time base of bp_server_completion). */
 double bp_server_clock(void);
+
+/* Contact began / ended events of the world's last step, compacted on the device from its contact records (bubble
+ * pairs, and bubble-segment records reported as the segment's owner), then `extra` caller records (participants[0] a
+ * bubble id, participants[1] the other object's id, normal from the bubble; e.g. bubble-body contacts the step does
+ * not record). A record counts when its penetration or impulse is positive and either object is in interested_ids.
+ * The world keeps the previous step's pair set (its contact history): began = pairs not in it, ended = its pairs that
+ * are gone or lost an object in removed_ids (none when both were removed). Events are began (ascending pair), then
+ * ended (ascending); the history becomes this step's pairs without removed objects. At most `capacity` events are
+ * written, *count = all of them. step_seconds divides the impulses (the step's duration). */
+int bp_world_contact_events(bp_world* world, const int64_t* interested_ids, uint32_t interested_count,
+                            const int64_t* removed_ids, uint32_t removed_count, const bp_contact* extra,
+                            uint32_t extra_count, float step_seconds, bp_contact_event* out, uint32_t capacity,
+                            uint32_t* count);
+/* Replaces the world's contact history (2 ids per pair, any order; e.g. when a world is rebuilt mid-run). */
+int bp_world_set_contact_history(bp_world* world, const int64_t* pairs, uint32_t pair_count);
+/* Reads the contact history (2 ids per pair, ascending pairs); with pairs = NULL, *count = the pair count. */
+int bp_world_read_contact_history(bp_world* world, int64_t* pairs, uint32_t capacity, uint32_t* count);
 
 /* ---- allocation-free step (no counterpart in the reference) ---------------------------------------------------- */
 

@@ -1938,6 +1938,109 @@ int bpo_world_read_trace(void* handle, double* out, uint32_t capacity, uint32_t*
     return BP_OK;
 }
 
+// Contact began / ended events of one step (NativePublicWorld.contactTransitions, NativePublicWorld.swift:347-391) over
+// a step's contact records in id form (bp_contact, as bp_world_read_contacts gives them; kind 1 participants[1] is a
+// segment id, reported as its owner when it has one, else skipped; other kinds are id pairs with the normal from the
+// first). A record counts when penetration > 0 or impulse > 0 (:373) and either object is interested (:354). Per key
+// (ids ordered as unsigned 64-bit values) the sums run in record order in float (:357-359): point * weight with weight
+// = max(penetration, 0) + 1e-4, weight, normal from the key's first object (a segment record's normal is negated,
+// :375-376), impulse / step. Events: began for keys not in the history, ascending (:384-389), then ended for history
+// keys not current, ascending (:390-392); with `removed` ids the host world's rule: a pair that lost one object ends,
+// a pair that lost both reports nothing, and the new history drops pairs with a removed object.
+int bpo_contact_events(const bp_contact* records, uint32_t count, const int64_t* seg_ids, const int64_t* seg_owners,
+                       const uint8_t* seg_has_owner, uint32_t seg_count, const int64_t* interested, uint32_t ni,
+                       const uint64_t* history, uint32_t nh, const int64_t* removed, uint32_t nr, float step,
+                       bp_contact_event* out, uint32_t capacity, uint32_t* event_count, uint64_t* next_history,
+                       uint32_t* next_count) {
+    struct Sum { float px = 0, py = 0, w = 0, nx = 0, ny = 0, imp = 0; };
+    typedef std::pair<uint64_t, uint64_t> Key;
+    std::vector<int64_t> in(interested, interested + ni), rm(removed, removed + nr);
+    std::sort(in.begin(), in.end());
+    std::sort(rm.begin(), rm.end());
+    auto has = [](const std::vector<int64_t>& v, int64_t id) { return std::binary_search(v.begin(), v.end(), id); };
+    std::vector<std::pair<Key, Sum>> sums;  // keys in first-seen order; looked up linearly through an index
+    std::vector<std::pair<Key, size_t>> index;
+    for (uint32_t r = 0; r < count; ++r) {
+        const bp_contact& c = records[r];
+        const int64_t first = c.participants[0];
+        int64_t second = c.participants[1];
+        float nfx = c.normal[0], nfy = c.normal[1];
+        if (c.kind == 1u) {
+            bool found = false;
+            for (uint32_t q = 0; q < seg_count; ++q)
+                if (seg_ids[q] == second) { found = seg_has_owner[q] != 0; second = seg_owners[q]; break; }
+            if (!found) continue;
+            nfx = -nfx;
+            nfy = -nfy;
+        }
+        if (!(c.penetration > 0.0f || c.impulse > 0.0f)) continue;
+        if (!has(in, first) && !has(in, second)) continue;
+        const uint64_t uf = (uint64_t)first, us = (uint64_t)second;
+        const bool firstLow = uf <= us;
+        const Key key = firstLow ? Key(uf, us) : Key(us, uf);
+        size_t at = sums.size();
+        for (const auto& e : index)
+            if (e.first == key) { at = e.second; break; }
+        if (at == sums.size()) { sums.push_back({key, Sum()}); index.push_back({key, at}); }
+        Sum& m = sums[at].second;
+        const float w = std::fmax(c.penetration, 0.0f) + 1e-4f;
+        m.px = m.px + c.point[0] * w;
+        m.py = m.py + c.point[1] * w;
+        m.w = m.w + w;
+        m.nx = m.nx + (firstLow ? nfx : -nfx);
+        m.ny = m.ny + (firstLow ? nfy : -nfy);
+        m.imp = m.imp + c.impulse / step;
+    }
+    std::sort(sums.begin(), sums.end(), [](const std::pair<Key, Sum>& a, const std::pair<Key, Sum>& b) { return a.first < b.first; });
+    std::vector<Key> hist;
+    for (uint32_t q = 0; q < nh; ++q) hist.push_back(Key(history[2 * q], history[2 * q + 1]));
+    std::sort(hist.begin(), hist.end());
+    uint32_t n = 0;
+    auto emit = [&](const bp_contact_event& e) {
+        if (n < capacity) out[n] = e;
+        ++n;
+    };
+    std::vector<Key> current;
+    for (const auto& kv : sums) {
+        current.push_back(kv.first);
+        if (std::binary_search(hist.begin(), hist.end(), kv.first)) continue;
+        const Sum& m = kv.second;
+        bp_contact_event e;
+        std::memset(&e, 0, sizeof(e));
+        e.kind = 0u;
+        e.objects[0] = (int64_t)kv.first.first;
+        e.objects[1] = (int64_t)kv.first.second;
+        e.point[0] = m.px / m.w;
+        e.point[1] = m.py / m.w;
+        const float length = std::sqrt(m.nx * m.nx + m.ny * m.ny);
+        e.normal[0] = length > 0.0f ? m.nx / length : 0.0f;
+        e.normal[1] = length > 0.0f ? m.ny / length : 0.0f;
+        e.impulse = m.imp;
+        emit(e);
+    }
+    for (const Key& k : hist) {
+        const bool r0 = has(rm, (int64_t)k.first), r1 = has(rm, (int64_t)k.second);
+        if (r0 && r1) continue;
+        if (!r0 && !r1 && std::binary_search(current.begin(), current.end(), k)) continue;
+        bp_contact_event e;
+        std::memset(&e, 0, sizeof(e));
+        e.kind = 1u;
+        e.objects[0] = (int64_t)k.first;
+        e.objects[1] = (int64_t)k.second;
+        emit(e);
+    }
+    uint32_t kept = 0;
+    for (const Key& k : current) {
+        if (has(rm, (int64_t)k.first) || has(rm, (int64_t)k.second)) continue;
+        next_history[2 * kept] = k.first;
+        next_history[2 * kept + 1] = k.second;
+        ++kept;
+    }
+    *event_count = n;
+    *next_count = kept;
+    return BP_OK;
+}
+
 // Contact law known-answer entry (same layout as bp_device_contact_law): 8 floats in and out per case.
 int bpo_contact_law(uint32_t mode, int precision, const double* in, double* out, uint32_t count) {
     for (uint32_t c = 0; c < count; ++c) {

@@ -56,6 +56,8 @@ def library() -> C.CDLL:
             "bpo_world_set_trace": (C.c_int, [P, C.c_int]),
             "bpo_world_read_trace": (C.c_int, [P, P, C.c_uint32, C.POINTER(C.c_uint32)]),
             "bpo_contact_law": (C.c_int, [C.c_uint32, C.c_int, P, P, C.c_uint32]),
+            "bpo_contact_events": (C.c_int, [P, C.c_uint32, P, P, P, C.c_uint32, P, C.c_uint32, P, C.c_uint32, P,
+                                             C.c_uint32, C.c_float, P, C.c_uint32, P, P, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -208,6 +210,28 @@ def step_worlds_reports(worlds: list[OracleWorld], steps: int, threads: int = 0)
     out = np.zeros((max(steps, 1), len(worlds)), N.REPORT_DTYPE)
     lib.bpo_worlds_step_reports(arr, len(worlds), steps, threads, C.c_void_p(out.ctypes.data))
     return out[:steps]
+
+
+def contact_events(records: np.ndarray, segments: np.ndarray, interested, history, removed=(), step: float = 1 / 60):
+    """Contact began / ended events of one step from its contact records (CONTACT_DTYPE, id form; extra records
+    appended) and the world's segments (their owners): (events CONTACT_EVENT_DTYPE, new history (pairs, 2))."""
+    rec = np.ascontiguousarray(records, N.CONTACT_DTYPE)
+    seg_ids = np.ascontiguousarray(segments["id"], np.int64)
+    seg_owners = np.ascontiguousarray(segments["owner_id"], np.int64)
+    has_owner = np.ascontiguousarray((segments["flags"] & N.SEGMENT_HAS_OWNER) != 0, np.uint8)
+    ids = np.ascontiguousarray(np.asarray(list(interested), np.int64))
+    gone = np.ascontiguousarray(np.asarray(list(removed), np.int64))
+    hist = np.ascontiguousarray(np.asarray(history, np.int64).reshape(-1, 2)).view(np.uint64)
+    cap = 2 * (rec.size + hist.shape[0]) + 1
+    out = np.zeros(cap, N.CONTACT_EVENT_DTYPE)
+    nxt = np.zeros((rec.size + 1, 2), np.uint64)
+    n_ev, n_hist = C.c_uint32(), C.c_uint32()
+    ptr = lambda a: C.c_void_p(a.ctypes.data) if a.size else None
+    library().bpo_contact_events(ptr(rec), rec.size, ptr(seg_ids), ptr(seg_owners), ptr(has_owner), seg_ids.size,
+                                 ptr(ids), ids.size, ptr(hist), hist.shape[0], ptr(gone), gone.size, float(step),
+                                 C.c_void_p(out.ctypes.data), cap, C.byref(n_ev), C.c_void_p(nxt.ctypes.data),
+                                 C.byref(n_hist))
+    return out[:n_ev.value], nxt[:n_hist.value].view(np.int64)
 
 
 def set_threads(threads: int) -> int:
