@@ -26,7 +26,7 @@ BODY_POLYGON, BODY_CIRCLE, BODY_CAPSULE = 0, 1, 2
 BODY_STATIC, BODY_KINEMATIC = 1, 2
 WORLD_HAS_REGION, WORLD_MINIMUM_MARGIN_ONLY, WORLD_ASSERT_EVERY_SUBSTEP, WORLD_INJECT_STATE, \
     WORLD_NO_END_ASSERTION, WORLD_FORCE_MULTI_CTA, WORLD_RIGID_TREE, WORLD_NO_RIGID_TREE = 1, 2, 4, 8, 16, 32, 64, 128
-BATCH_PER_WORLD_LAUNCH, BATCH_USE_GRAPH, BATCH_AUTOTUNE = 1, 2, 4
+BATCH_PER_WORLD_LAUNCH, BATCH_USE_GRAPH, BATCH_AUTOTUNE, BATCH_NO_STAGING = 1, 2, 4, 8
 TERM_REMAINING, TERM_STIFFNESS, TERM_DISTANCE, TERM_MARGIN = range(4)
 VIOLATION_NONE, VIOLATION_PAIR, VIOLATION_INSIDE_BODY, VIOLATION_EDGE_SIDE = range(4)
 

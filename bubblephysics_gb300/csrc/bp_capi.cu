@@ -1346,6 +1346,14 @@ int bp_batch_create(bp_context* context, uint32_t world_count, const bp_world_de
     if (st != BP_OK) { delete b; context_unref(context); return st; }
     if (config) {
         b->set.flags = config->flags;
+        if (config->flags & BP_BATCH_NO_STAGING) {
+            b->set.staging = false;
+            if (schedule(b->set, b->set.threads, b->set.warpMax, b->set.groupWidth) != cudaSuccess) {
+                delete b;
+                context_unref(context);
+                return BP_E_CUDA;
+            }
+        }
         uint32_t t = config->threads_per_world ? config->threads_per_world : b->set.threads;
         uint32_t wm = config->warp_world_max == 0xffffffffu ? 0u : (config->warp_world_max ? config->warp_world_max : b->set.warpMax);
         uint32_t gw = config->group_width ? config->group_width : b->set.groupWidth;

@@ -1498,17 +1498,24 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
     // contact records: count per bubble, scan, write (kind-major candidate order)
     for (uint32_t i = r; i < n; i += T) {
         uint32_t g = W.boff + i;
-        uint32_t cp = 0, cs = 0;
+        uint32_t cp = 0, cs = 0, active0 = 0, active1 = 0;  // which of the first 64 candidates are active
         if (!removed(S, g)) {
             uint2 cc = S.candCount[g];
             const uint32_t* crow = S.candRow + W.rowOff + (uint64_t)i * W.k;
             DContact tmp;
-            for (uint32_t e = 0; e < cc.x; ++e) cp += contact_record<false>(S, W, i, 0u, crow[e], tmp) ? 1u : 0u;
-            for (uint32_t e = cc.x; e < cc.x + cc.y; ++e)
-                cs += contact_record<false>(S, W, i, 1u, crow[e] & kIndexMask, tmp) ? 1u : 0u;
+            for (uint32_t e = 0; e < cc.x + cc.y; ++e) {
+                const uint32_t kind = e < cc.x ? 0u : 1u;
+                if (!contact_record<false>(S, W, i, kind, crow[e] & kIndexMask, tmp)) continue;
+                if (kind == 0u) ++cp; else ++cs;
+                if (e < 32u) active0 |= 1u << e;
+                else if (e < 64u) active1 |= 1u << (e - 32u);
+            }
         }
         S.scanA[g] = cp;
         S.scanB[g] = cs;
+        // the non-contact accelerations are not needed again this step: their slot keeps the activity bits for the
+        // writing pass (stored as raw bits)
+        S.a0[g] = f2(__uint_as_float(active0), __uint_as_float(active1));
         if (!removed(S, g)) {
             // non-finite state (nativeCheckFinite, NPK:5-27), and whether the bubble left the box the assertion's
             // candidate-row shortcut relies on (see assert_contacts)
@@ -1527,9 +1534,12 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
         uint2 cc = S.candCount[g];
         const uint32_t* crow = S.candRow + W.rowOff + (uint64_t)i * W.k;
         uint32_t op = S.scanA[g], os = pairsAll + S.scanB[g];
+        const float2 bits = S.a0[g];
+        const uint32_t active0 = __float_as_uint(bits.x), active1 = __float_as_uint(bits.y);
         DContact rec;
         for (uint32_t e = 0; e < cc.x + cc.y; ++e) {
             uint32_t kind = e < cc.x ? 0u : 1u;
+            if (e < 32u ? !((active0 >> e) & 1u) : (e < 64u && !((active1 >> (e - 32u)) & 1u))) continue;
             if (!contact_record<true>(S, W, i, kind, crow[e] & kIndexMask, rec)) continue;
             uint32_t slot = kind == 0u ? op++ : os++;
             if (!finite2(rec.normal) || !finite2(rec.point) || !isfinite(rec.impulse) || !isfinite(rec.penetration)) nonfinite = 1u;

@@ -218,7 +218,7 @@ class Batch:
     per_world_launch=True, the plain path: one launch per world, one after another)."""
 
     def __init__(self, specs: list[WorldSpec], context: Context | None = None, *, per_world_launch=False,
-                 use_graph=True, autotune=False, threads_per_world=0, warp_world_max=0, group_width=0):
+                 use_graph=True, autotune=False, threads_per_world=0, warp_world_max=0, group_width=0, staging=True):
         self.ctx = context or default_context()
         self.lib = self.ctx.lib
         self.specs = specs
@@ -227,7 +227,7 @@ class Batch:
         inputs = (N.WorldInput * len(specs))(*[p.input for p in packed])
         cfg = N.BatchConfig()
         cfg.flags = (N.BATCH_PER_WORLD_LAUNCH if per_world_launch else 0) | (N.BATCH_USE_GRAPH if use_graph else 0) | \
-                    (N.BATCH_AUTOTUNE if autotune else 0)
+                    (N.BATCH_AUTOTUNE if autotune else 0) | (0 if staging else N.BATCH_NO_STAGING)
         cfg.threads_per_world = threads_per_world
         cfg.warp_world_max = warp_world_max
         cfg.group_width = group_width

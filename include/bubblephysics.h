@@ -315,7 +315,9 @@ int bp_world_read_rigid_keys(bp_world* world, uint64_t* out, uint32_t capacity, 
 enum {
     BP_BATCH_PER_WORLD_LAUNCH = 1u, /* step each world with its own launch, one after another (the plain path) */
     BP_BATCH_USE_GRAPH = 2u,        /* capture the per-step launches in a CUDA graph and replay it */
-    BP_BATCH_AUTOTUNE = 4u          /* choose threads per world per size class by timing on first use */
+    BP_BATCH_AUTOTUNE = 4u,         /* choose the block width, group-queue threshold and group width by timing on first
+                                       use */
+    BP_BATCH_NO_STAGING = 8u        /* step every world from global memory (no shared-memory workspace) */
 };
 
 typedef struct bp_batch_config {
