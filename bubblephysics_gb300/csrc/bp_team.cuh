@@ -293,6 +293,24 @@ struct GroupTeam {
     }
 };
 
+// GPU-scope memory operations of the grid barrier.
+__device__ __forceinline__ unsigned int ld_acquire(const unsigned int* p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned int atom_add_acq_rel(unsigned int* p, unsigned int v) {
+    unsigned int old;
+    asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+__device__ __forceinline__ void red_add_release(unsigned int* p, unsigned int v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_relaxed(unsigned int* p, unsigned int v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 // ----------------------------------------------------------------------------------------------------------------
 // Grid team: every block of a cooperative launch works on one world. Partials go through global memory with
 // alternating parity so a reduction never overwrites partials another block may still read; each parity has four
@@ -318,28 +336,27 @@ struct GridTeam {
     __device__ void shared_sync() const { __syncthreads(); }
     __device__ bool ok() const { return !failed; }
 
-    // Bounded grid barrier (generation counter). Returns false when any block gave up waiting.
+    // Bounded grid barrier (generation counter). Returns false when any block gave up waiting. Arrival is an
+    // acquire-release add (the block's writes, ordered before it by the block barrier, are released; the other blocks'
+    // are acquired by the last arriver), the last arriver releases the next generation, and the waiters acquire it.
     __device__ bool sync() const {
         __syncthreads();
         if (threadIdx.x == 0) {
-            volatile unsigned int* gen = bar + 1;
-            unsigned int g = *gen;
-            __threadfence();
-            unsigned int arrived = atomicAdd(bar, 1u);
+            unsigned int* gen = bar + 1;
+            const unsigned int g = ld_acquire(gen);
+            const unsigned int arrived = atom_add_acq_rel(bar, 1u);
             if (arrived == gridDim.x - 1) {
-                atomicExch(bar, 0u);
-                __threadfence();
-                atomicAdd(bar + 1, 1u);
+                st_relaxed(bar, 0u);
+                red_add_release(gen, 1u);
             } else {
                 unsigned long long spins = 0;
-                while (*gen == g) {
-                    if (*(volatile uint32_t*)err != 0u) break;
+                while (ld_acquire(gen) == g) {
+                    if (ld_acquire(err) != 0u) break;
                     if (++spins > kBarrierSpinLimit) { atomicOr(err, 1u); break; }
-                    __nanosleep(64);
+                    __nanosleep(32);
                 }
             }
-            __threadfence();
-            sh->bcastU[7] = *(volatile uint32_t*)err;
+            sh->bcastU[7] = ld_acquire(err);
         }
         __syncthreads();
         failed = sh->bcastU[7] != 0u;
