@@ -486,6 +486,85 @@ def run_ours(args, rank, world_size, local_rank):
     return 0
 
 
+def run_case(name: str) -> int:
+    """One small launch of a chosen kernel for profilers (ncu -k ... python bench.py --case NAME); prints its status.
+      batch     persistent_step_kernel, schedule_kernel, accumulate_kernel: 4 steps of the 4,096-world batch, autotuned
+      batch512  the same with a fixed schedule (512-thread blocks, worlds of <= 64 bubbles in 64-thread groups)
+      large     large_step_kernel: 3 steps of the 65,536-bubble world
+      served    served_step_kernel: 3 rounds of one-step requests over 512 resident worlds
+      contour   contour_kernel: contours of the 65,536-bubble world after 3 steps
+      hit       hit_test_kernel: 65,536 query points on the 256-bubble world
+      sensor    sensor_overlap_kernel, sensor_compact_kernel: 64 circle sensors on the 256-bubble world
+      events    contact_events_kernel: contact events of the 256-bubble world, 3 steps
+      noalloc   noalloc_step_kernel: 3 allocation-free steps of the 256-bubble world"""
+    import ctypes as C
+    from bubblephysics_gb300 import _native as N
+    from bubblephysics_gb300 import scenes
+    from bubblephysics_gb300.solver import Batch, Context, Server, World
+    ctx = Context(0)
+    if name in ("batch", "batch512"):
+        kw = dict(autotune=True) if name == "batch" else dict(threads_per_world=512, warp_world_max=64, group_width=64)
+        b = Batch(scenes.batched_worlds(4096, seed=3), ctx, use_graph=True, **kw)
+        st, r = b.step(4)
+        print("status", st, "ms per step", float(r["gpu_ms"][0]) / 4, b.tuning())
+        return 0 if st == N.OK else 1
+    if name == "large":
+        st, r = World(scenes.large_world(), ctx).step(3)
+        print("status", st, "substeps", r["substep_count"].tolist())
+        return 0 if st == N.OK else 1
+    if name == "served":
+        worlds = scenes.serving_worlds(512, seed=5)
+        server = Server(len(worlds), ctx)
+        for spec in worlds:
+            server.add_world(spec)
+        statuses = set()
+        for _ in range(3):
+            for w in range(len(worlds)):
+                server.submit(w, 1)
+            statuses |= set(server.drain()["status"].tolist())
+        print("statuses", sorted(statuses))
+        return 0 if statuses == {N.OK} else 1
+    spec = scenes.large_world() if name == "contour" else scenes.plain_world(seed=1)
+    world = World(spec, ctx)
+    if name == "sensor":
+        sensors = []
+        for q in range(64):
+            s = N.Sensor()
+            s.id = 10_000 + q
+            s.position[:] = [float(20 + (q % 8) * 45), float(40 + (q // 8) * 80)]
+            s.radius = 30.0
+            s.flags = N.SENSOR_ENTER_EVENTS | N.SENSOR_EXIT_EVENTS
+            sensors.append(s)
+        world.set_sensors(sensors)
+    st, _ = world.step(3)
+    if name == "contour":
+        print("contour ms", world.contours()[-1])
+    elif name == "hit":
+        points = np.random.default_rng(1).uniform([0, 0], [375, 700], (65536, 2)).astype(np.float32)
+        print("hits", int(world.hit_test(points)[2].sum()))
+    elif name == "sensor":
+        print("sensor events", len(world.sensor_events()))
+    elif name == "events":
+        ids = set(int(i) for i in spec.bubbles["id"])
+        for _ in range(3):
+            world.step(1)
+            print("events", world.contact_events(ids).size)
+    elif name == "noalloc":
+        import torch
+        spec.candidate_limit = 32
+        bubbles = torch.from_numpy(spec.bubbles.view(np.uint8).copy()).cuda()
+        segments = torch.from_numpy(np.ascontiguousarray(spec.segments).view(np.uint8).copy()).cuda()
+        reports = torch.zeros(3 * 96, dtype=torch.uint8, device="cuda")
+        st = N.library().bp_world_step_noalloc(C.byref(spec.desc()), C.c_void_p(bubbles.data_ptr()),
+                                               spec.bubble_count, C.c_void_p(segments.data_ptr()),
+                                               len(spec.segments), 3, C.c_void_p(reports.data_ptr()), None)
+        torch.cuda.synchronize()
+    else:
+        raise SystemExit(f"unknown case {name}")
+    print("status", st)
+    return 0 if st == N.OK else 1
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -502,8 +581,11 @@ def main():
     p.add_argument("--serve-requests", type=int, default=20000, help="requests of the serving stream (0: skip)")
     p.add_argument("--serve-rate", type=float, default=50000.0, help="Poisson arrival rate of the serving stream")
     p.add_argument("--no-autotune", action="store_true", help="keep the default schedule (profiling runs)")
+    p.add_argument("--case", default=None, help="run one small case of one kernel for a profiler (see run_case)")
     args = p.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.case:
+        return run_case(args.case)
     rank = env_int("RANK", 0)
     world_size = env_int("WORLD_SIZE", 1)
     local_rank = env_int("LOCAL_RANK", 0)
