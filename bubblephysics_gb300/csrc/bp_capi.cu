@@ -400,7 +400,6 @@ int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc
     S.bpose = ws.alloc<float4>(nbo, err);
     S.segBox = ws.alloc<RigidBox>(ns, err);
     S.bodyBox = ws.alloc<RigidBox>(nbo, err);
-    S.tileMask = ws.alloc<uint32_t>((uint64_t)count * kTileMaskWords, err);
     ws.dSingle = ws.alloc<uint32_t>(count, err);
     for (uint32_t w : ws.largeWorlds) ws.largeMaxN = std::max(ws.largeMaxN, ws.hWorlds[w].n);
     ws.largeB = next_pow2(std::max<uint32_t>(2u * ws.largeMaxN, 64u));

@@ -144,13 +144,6 @@ struct DState {
     float4* bpose;             // per body: pose at the current step fraction (position.xy, cos, sin)
     RigidBox* segBox;          // per segment
     RigidBox* bodyBox;         // per body (rebuilt every step: kinematic bodies move)
-    // Rigid tiles of a world without a tree (1..127 segments + bodies): an 8 x 8 grid over the rigid objects' bounding
-    // box, each tile a 128-bit mask of the objects (segments, then bodies) whose boxes, widened by the build's reach,
-    // touch it. kTileMaskWords per world from world index * kTileMaskWords (in the workspace when staged).
-    uint32_t* tileMask;
-    float4 tileGeom;           // origin x, y and tiles per unit x, y of this step's grid (per team)
-    uint32_t tilesOn;          // 1: the loops over rigid objects visit only the objects of the query's tiles
-    uint32_t tilePad[3];
     // LBVH over the rigid leaves of worlds with W.tree set (entries from W.treeOff, s + nb per world)
     unsigned long long* tKeys;     // sorted keys (morton << 32 | leaf)
     unsigned long long* tKeysAlt;  // radix-sort ping-pong
@@ -214,17 +207,10 @@ __host__ __device__ inline uint32_t contour_samples(float r, float maxEdge, uint
     return count < stride ? count : stride;
 }
 
-constexpr uint32_t kTiles = 8;                                  // tiles per axis of the rigid tile grid
-constexpr uint32_t kTileWords = 4;                              // 128 rigid objects per tile mask
-constexpr uint32_t kTileMaskWords = kTiles * kTiles * kTileWords;
-constexpr uint32_t kTileMaxObjects = 32u * kTileWords - 1u;     // worlds with more rigid objects use the tree or loops
-
-__host__ __device__ inline bool tiles_fit(uint32_t s, uint32_t nb) { return s + nb > 0u && s + nb <= kTileMaxObjects; }
-
 // Bytes of a world's shared-memory workspace: per bubble 104 B of hot state (88 B of state and 16 B of grid cell), per
-// segment and body a 32 B box, per body a 16 B pose, the rigid tile masks; the 17 parts are each padded to 16 bytes.
+// segment and body a 32 B box, per body a 16 B pose; the 16 parts are each padded to 16 bytes.
 __host__ __device__ inline uint32_t workspace_bytes(uint32_t n, uint32_t s, uint32_t nb) {
-    return n * 104u + s * 32u + nb * 48u + (tiles_fit(s, nb) ? 4u * kTileMaskWords : 0u) + 17u * 16u;
+    return n * 104u + s * 32u + nb * 48u + 16u * 16u;
 }
 
 // ------------------------------------------------------------------------------------------------------------------

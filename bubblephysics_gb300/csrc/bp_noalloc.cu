@@ -56,7 +56,6 @@ struct NoAllocLayout {
         S.pRotw = take<float2>(base, kNaN); S.pResult = take<uint32_t>(base, kNaN); S.pFlags = take<uint32_t>(base, kNaN);
         S.seg = take<DSegment>(base, kNaS);
         S.segBox = take<RigidBox>(base, kNaS);
-        S.tileMask = take<uint32_t>(base, kTileMaskWords);
         S.contacts = take<DContact>(base, kNaContacts);
         S.failed = take<uint32_t>(base, 1);
         S.scanA = take<uint32_t>(base, kNaN); S.scanB = take<uint32_t>(base, kNaN);

@@ -387,50 +387,6 @@ __device__ __forceinline__ bool body_accepts(const DState& S, const DWorld& W, c
     return !(hi.x < bodyLow.x || hi.y < bodyLow.y || bodyHigh.x < lo.x || bodyHigh.y < lo.y);
 }
 
-// Rigid tiles (see DState::tileMask). A box of the query meets the tiles from tile_of(lo) to tile_of(hi) on each axis;
-// tile_of is monotone, so any point of a query box that also lies in an object's widened box falls in a tile both
-// mark. The loops over rigid objects therefore visit every object the exact tests can accept, in ascending index
-// order, and run those tests unchanged: the results are the brute-force loops' results.
-__device__ __forceinline__ uint32_t tile_of(float x, float origin, float perUnit) {
-    return (uint32_t)clampf(floorf((x - origin) * perUnit), 0.0f, (float)(kTiles - 1u));
-}
-
-// Visits the rigid objects o in [first, last) (segments 0..s-1, then bodies s..s+nb-1) whose tiles meet the box
-// [lo, hi], ascending; f(o) returns true to stop. Without tiles every object of the range is visited.
-template <class F>
-__device__ __forceinline__ void for_each_rigid(const DState& S, float2 lo, float2 hi, uint32_t first, uint32_t last, F&& f) {
-    if (!S.tilesOn) {
-        for (uint32_t o = first; o < last; ++o)
-            if (f(o)) return;
-        return;
-    }
-    const float4 gm = S.tileGeom;
-    const uint32_t x0 = tile_of(lo.x, gm.x, gm.z), x1 = tile_of(hi.x, gm.x, gm.z);
-    const uint32_t y0 = tile_of(lo.y, gm.y, gm.w), y1 = tile_of(hi.y, gm.y, gm.w);
-    uint32_t m[kTileWords];
-#pragma unroll
-    for (uint32_t w = 0; w < kTileWords; ++w) m[w] = 0u;
-    for (uint32_t y = y0; y <= y1; ++y)
-        for (uint32_t x = x0; x <= x1; ++x) {
-            const uint32_t* t = S.tileMask + (y * kTiles + x) * kTileWords;
-#pragma unroll
-            for (uint32_t w = 0; w < kTileWords; ++w) m[w] |= t[w];
-        }
-#pragma unroll
-    for (uint32_t w = 0; w < kTileWords; ++w) {
-        const uint32_t base = 32u * w;
-        if (base >= last || base + 32u <= first) continue;
-        uint32_t bits = m[w];
-        if (first > base) bits &= ~0u << (first - base);
-        if (last < base + 32u) bits &= (1u << (last - base)) - 1u;
-        while (bits) {
-            const uint32_t o = base + (uint32_t)(__ffs(bits) - 1);
-            bits &= bits - 1u;
-            if (f(o)) return;
-        }
-    }
-}
-
 // Insert `value` into a row kept sorted ascending with at most `limit` entries (nativeInsertCandidate, NGK:238-251).
 __device__ __forceinline__ void insert_sorted(uint32_t* row, uint32_t& count, uint32_t limit, uint32_t value) {
     uint32_t loc;
@@ -564,13 +520,11 @@ __device__ void emit_row(const DState& S, const DWorld& W, const uint32_t* bucke
                    });
         count += segKept;
     } else {
-        const float2 p = S.pos[g];
-        for_each_rigid(S, p, p, 0u, W.s, [&](uint32_t sj) {
-            if (!segment_accepts(S, W, i, sj)) return false;
+        for (uint32_t sj = 0; sj < W.s; ++sj) {
+            if (!segment_accepts(S, W, i, sj)) continue;
             ++segTotal;
             if (count < k) row[count++] = (1u << kKindShift) | sj;
-            return false;
-        });
+        }
     }
     S.candCount[g] = make_uint2(pairs, count - pairs);
     S.pairTotal[g] = total;
@@ -678,18 +632,13 @@ __device__ void build_adjacency(const DState& S, const DWorld& W, const uint32_t
                            insert_sorted(row, deg, k, (2u << kKindShift) | bi);
                        });
         }
-    } else if (W.nb) {
-        const float2 c = S.pos[g];
-        for_each_rigid(S, c, c, W.s, W.s + W.nb, [&](uint32_t o) {
-            const uint32_t bi = o - W.s;
-            const RigidBox rb = S.bodyBox[W.bodyOff + bi];
-            if (!rb.flags || !body_accepts(S, W, rb, bi, i)) return false;
-            uint32_t total = S.bodyTotal[W.bodyOff + bi];
-            if (total > k && !row_contains(S.bodyRow + W.bodyRowOff + (uint64_t)bi * k, k, i)) return false;
-            ++demanded;
-            if (deg < k) row[deg++] = (2u << kKindShift) | bi;
-            return false;
-        });
+    } else for (uint32_t bi = 0; bi < W.nb; ++bi) {
+        const RigidBox rb = S.bodyBox[W.bodyOff + bi];
+        if (!rb.flags || !body_accepts(S, W, rb, bi, i)) continue;
+        uint32_t total = S.bodyTotal[W.bodyOff + bi];
+        if (total > k && !row_contains(S.bodyRow + W.bodyRowOff + (uint64_t)bi * k, k, i)) continue;
+        ++demanded;
+        if (deg < k) row[deg++] = (2u << kKindShift) | bi;
     }
     S.deg[g] = deg;
     overflow += demanded - deg;
@@ -736,26 +685,8 @@ __device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, cons
     for (uint32_t b = r; b < B; b += T) buckets[b] = 0u;
     if (kTree)
         for (uint32_t bi = r; bi < W.nb; bi += T) S.bodyTotal[W.bodyOff + bi] = 0u;
-    if (S.tilesOn)
-        for (uint32_t w = r; w < kTileMaskWords; w += T) S.tileMask[w] = 0u;
     team.sync();
     BP_SUBPHASE(13);
-    // rigid tiles of this build: every object marks the tiles its box widened by the build's reach touches (a
-    // segment by cw >= r + m + sepTol, a body also by its hull radius; both with a rounding margin)
-    if (S.tilesOn) {
-        const float4 gm = S.tileGeom;
-        for (uint32_t o = r; o < W.s + W.nb; o += T) {
-            const RigidBox rb = o < W.s ? S.segBox[W.soff + o] : S.bodyBox[W.bodyOff + o - W.s];
-            const float4 b = rb.box;
-            const float big = fmaxf(fmaxf(fabsf(b.x), fabsf(b.z)), fmaxf(fabsf(b.y), fabsf(b.w)));
-            const float e = cw + (o < W.s ? 0.0f : __uint_as_float(rb.pad)) + 1e-3f + 1e-5f * big;
-            const uint32_t x0 = tile_of(b.x - e, gm.x, gm.z), x1 = tile_of(b.z + e, gm.x, gm.z);
-            const uint32_t y0 = tile_of(b.y - e, gm.y, gm.w), y1 = tile_of(b.w + e, gm.y, gm.w);
-            for (uint32_t y = y0; y <= y1; ++y)
-                for (uint32_t x = x0; x <= x1; ++x)
-                    atomicOr(S.tileMask + (y * kTiles + x) * kTileWords + (o >> 5), 1u << (o & 31u));
-        }
-    }
     // cells (nativeBuildGrid, NGK:179-189) and bucket counts
     for (uint32_t i = r; i < n; i += T) {
         uint32_t g = W.boff + i;
@@ -999,13 +930,9 @@ __device__ bool assert_bubble(const DState& S, const DWorld& W, const uint32_t* 
                            if (leaf < W.s || leaf - W.s >= insideOf) return;
                            if (insideBody(leaf - W.s)) insideOf = leaf - W.s;
                        });
-    } else if (W.nb) {
-        for_each_rigid(S, f2(center.x - cs, center.y - cs), f2(center.x + cs, center.y + cs), W.s, W.s + W.nb,
-                       [&](uint32_t o) {
-                           if (!insideBody(o - W.s)) return false;
-                           insideOf = o - W.s;
-                           return true;
-                       });
+    } else {
+        for (uint32_t bi = 0; bi < W.nb; ++bi)
+            if (insideBody(bi)) { insideOf = bi; break; }
     }
     if (insideOf != 0xffffffffu) {
         v.kind = BP_VIOLATION_INSIDE_BODY; v.a = S.id[g]; v.b = S.body[W.bodyOff + insideOf].id; v.edge = 0; v.distance = 0.0f;
@@ -1049,15 +976,11 @@ __device__ bool assert_bubble(const DState& S, const DWorld& W, const uint32_t* 
                            if (leaf >= W.s || leaf >= crossed) return;
                            if (crossesEdge(leaf, after)) { crossed = leaf; crossedAfter = after; }
                        });
-    } else if (W.s) {
-        for_each_rigid(S, f2(pathLo.x - slack, pathLo.y - slack), f2(pathHi.x + slack, pathHi.y + slack), 0u, W.s,
-                       [&](uint32_t e) {
-                           float after;
-                           if (!crossesEdge(e, after)) return false;
-                           crossed = e;
-                           crossedAfter = after;
-                           return true;
-                       });
+    } else {
+        for (uint32_t e = 0; e < W.s; ++e) {
+            float after;
+            if (crossesEdge(e, after)) { crossed = e; crossedAfter = after; break; }
+        }
     }
     if (crossed != 0xffffffffu) {
         const DSegment& sg = S.seg[W.soff + crossed];
@@ -1289,7 +1212,6 @@ __device__ bool stage_world(const DState& G, DState& S, const DWorld& W, const T
     RigidBox* segBox = carve<RigidBox>(p, W.s);
     RigidBox* bodyBox = carve<RigidBox>(p, W.nb);
     float4* bpose = carve<float4>(p, W.nb);
-    uint32_t* tiles = tiles_fit(W.s, W.nb) ? carve<uint32_t>(p, kTileMaskWords) : nullptr;
     for (uint32_t i = r; i < n; i += T) {
         uint32_t g = W.boff + i;
         phys[i] = G.phys[g];
@@ -1315,7 +1237,6 @@ __device__ bool stage_world(const DState& G, DState& S, const DWorld& W, const T
         S.segBox = segBox - W.soff;
         S.bodyBox = bodyBox - W.bodyOff;
         S.bpose = bpose - W.bodyOff;
-        if (tiles) S.tileMask = tiles;
     }
     team.sync();
     return true;
@@ -1353,8 +1274,6 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
     if (team.shared_leader()) {
         ts.W = G.worlds[wi];
         ts.S = G;
-        ts.S.tileMask = G.tileMask ? G.tileMask + (uint64_t)wi * kTileMaskWords : nullptr;  // this world's masks
-        ts.S.tilesOn = 0u;
     }
     team.shared_sync();
     const DWorld& W = ts.W;
@@ -1406,28 +1325,6 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
     const uint32_t live = team.sum(liveLocal);
     // the tree-capable instantiation carries the LBVH code; a kernel for worlds without trees is compiled without it
     const bool useTree = kTreeCapable && W.tree && build_rigid_tree(S, W, wi, team);
-    if (!useTree && S.tileMask != nullptr && tiles_fit(W.s, W.nb)) {
-        // the rigid tile grid of this step: 8 x 8 tiles over the bounding box of the segments' and bodies' boxes
-        uint32_t v[4] = {0u, 0u, 0u, 0u};
-        for (uint32_t o = r; o < W.s + W.nb; o += T) {
-            const float4 b = o < W.s ? S.segBox[W.soff + o].box : S.bodyBox[W.bodyOff + o - W.s].box;
-            if (!isfinite(b.x) || !isfinite(b.y) || !isfinite(b.z) || !isfinite(b.w)) { v[0] = 0xffffffffu; continue; }
-            v[0] = max(v[0], float_order(b.z));
-            v[1] = max(v[1], float_order(b.w));
-            v[2] = max(v[2], ~float_order(b.x));
-            v[3] = max(v[3], ~float_order(b.y));
-        }
-        team.template reduce4<0xfu>(v);
-        if (team.shared_leader() && v[0] != 0xffffffffu) {
-            const float lox = float_unorder(~v[2]), loy = float_unorder(~v[3]);
-            const float ex = float_unorder(v[0]) - lox, ey = float_unorder(v[1]) - loy;
-            float px = ex > 0.0f ? (float)kTiles / ex : 0.0f, py = ey > 0.0f ? (float)kTiles / ey : 0.0f;
-            if (!isfinite(px)) px = 0.0f;
-            if (!isfinite(py)) py = 0.0f;
-            S.tileGeom = make_float4(lox, loy, px, py);
-            S.tilesOn = 1u;  // read after the barriers of the build
-        }
-    }
     Ctl c;
     c.timeX = W.dt;
     c.timeY = live == 0u ? W.dt : 0.0f;
