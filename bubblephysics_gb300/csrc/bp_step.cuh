@@ -675,13 +675,11 @@ __device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, cons
         S.ref[g] = p;
         cwl = fmaxf(cwl, 2.0f * (radius + m) + W.sepTol);  // nativePrepareGrid, NGK:163-177
     }
+    const float fraction = c.timeX > 0.0f ? clampf(c.timeY / c.timeX, 0.0f, 1.0f) : 1.0f;
+    if (W.nb) refresh_poses(S, W, team, fraction);  // read by the forces below, after several barriers
     BP_SUBPHASE(12);
     float cw = team.fmax(cwl);
     cw = fmaxf(cw, kFltMin);
-    // poses at this fraction, read by the forces below after several barriers; written only after the barrier above,
-    // since a build can follow the last substep's force pass (which reads the poses) without one
-    const float fraction = c.timeX > 0.0f ? clampf(c.timeY / c.timeX, 0.0f, 1.0f) : 1.0f;
-    if (W.nb) refresh_poses(S, W, team, fraction);
     for (uint32_t b = r; b < B; b += T) buckets[b] = 0u;
     if (kTree)
         for (uint32_t bi = r; bi < W.nb; bi += T) S.bodyTotal[W.bodyOff + bi] = 0u;
@@ -725,7 +723,7 @@ __device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, cons
         else
             for (uint32_t bi = warp; bi < W.nb; bi += warps) emit_body_row(S, W, bi, lane, overflow, maxPer);
     }
-    if (W.nb) team.sync();  // body rows are read by the adjacency rows (the candidate rows' barrier is above)
+    team.sync();
     BP_SUBPHASE(16);
     w2 = ValOwner{-1.0f, 0u};
     mg = ValOwner{__int_as_float(0x7f800000), 0u};
@@ -1367,8 +1365,7 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
         mg = ValOwner{__int_as_float(0x7f800000), 0u};
         for (uint32_t i = r; i < n; i += T)
             if (!removed(S, W.boff + i)) force_kick(S, W, i, h, fraction, w2, mg);
-        // no barrier here: whatever reads other bubbles' new state next (the reduction of the next substep, the
-        // injection, the assertion, the end of the step) passes one first
+        team.sync();
         BP_PHASE(4);
         if (W.flags & BP_WORLD_INJECT_STATE) {
             if (c.cY == W.injectSubstep + 1u)
