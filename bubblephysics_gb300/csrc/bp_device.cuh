@@ -188,7 +188,7 @@ constexpr uint32_t kTeamStateWords = (uint32_t)((sizeof(TeamState) + 15u) / 16u 
 // Shared-memory slice of one group of the group queue, in 32-bit words: the group's TeamState, its reduction scratch
 // (groups wider than a warp; a BlockScratch), then its hash grid (B bucket ends, then the entries of its largest
 // world), then its workspace.
-constexpr uint32_t kGroupScratchWords = 588;
+constexpr uint32_t kGroupScratchWords = 308;
 __host__ __device__ inline uint32_t group_scratch_words(uint32_t width) {
     return kTeamStateWords + (width > 32u ? kGroupScratchWords : 0u);
 }

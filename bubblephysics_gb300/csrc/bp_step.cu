@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(1024) schedule_kernel(const DWorld* worlds, co
         }
     }
     // stable split into the two queues, in cost order
-    uint32_t nCta = 0, nWarp = 0, par = 0;
+    uint32_t nCta = 0, nWarp = 0;
     for (uint32_t base = 0; base < count; base += blockDim.x) {
         uint32_t i = base + threadIdx.x;
         uint32_t w = 0, isWarp = 0, valid = i < count ? 1u : 0u;
@@ -77,8 +77,8 @@ __global__ void __launch_bounds__(1024) schedule_kernel(const DWorld* worlds, co
             isWarp = (worlds[w].n <= warpMax && sub <= warpSubsteps) ? 1u : 0u;
         }
         uint32_t tw, tc;
-        uint32_t pw = block_excl_scan(valid & isWarp, &tw, sh, par);
-        uint32_t pc = block_excl_scan(valid & (isWarp ^ 1u), &tc, sh, par);
+        uint32_t pw = block_excl_scan(valid & isWarp, &tw, sh);
+        uint32_t pc = block_excl_scan(valid & (isWarp ^ 1u), &tc, sh);
         if (valid) {
             if (isWarp) warpList[nWarp + pw] = w;
             else ctaList[nCta + pc] = w;

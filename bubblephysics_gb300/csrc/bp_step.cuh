@@ -648,13 +648,9 @@ __device__ void build_adjacency(const DState& S, const DWorld& W, const uint32_t
 // ------------------------------------------------------------------------------------------------------------------
 // Grid build + candidates + adjacency (one build of nativeBroadphaseInGroup, NFK:1040-1134)
 // ------------------------------------------------------------------------------------------------------------------
-// Ends with the contact forces of the built state and the start-of-build acceleration (phase 2, NFK:776-779),
-// evaluated right after each bubble's adjacency row is made (the row is the only thing the forces need from the build),
-// and each thread's share of the first reduction: (max omega^2, owner) in w2 and (min margin bound, owner) in mg.
 template <class Team, bool kTree>
 __device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, const Team& team, uint32_t* buckets,
-                            uint32_t* entries, uint32_t B, uint32_t& buildOverflow, uint32_t& maxPerAll, uint32_t subWorld,
-                            ValOwner& w2, ValOwner& mg) {
+                            uint32_t* entries, uint32_t B, uint32_t& buildOverflow, uint32_t& maxPerAll, uint32_t subWorld) {
     const uint32_t n = W.n, T = team.size(), r = team.rank();
 #ifdef BP_PHASE_TIMING
     long long subMark = clock64();
@@ -675,8 +671,6 @@ __device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, cons
         S.ref[g] = p;
         cwl = fmaxf(cwl, 2.0f * (radius + m) + W.sepTol);  // nativePrepareGrid, NGK:163-177
     }
-    const float fraction = c.timeX > 0.0f ? clampf(c.timeY / c.timeX, 0.0f, 1.0f) : 1.0f;
-    if (W.nb) refresh_poses(S, W, team, fraction);  // read by the forces below, after several barriers
     BP_SUBPHASE(12);
     float cw = team.fmax(cwl);
     cw = fmaxf(cw, kFltMin);
@@ -725,11 +719,30 @@ __device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, cons
     }
     team.sync();
     BP_SUBPHASE(16);
+    for (uint32_t i = r; i < n; i += T) build_adjacency<kTree>(S, W, buckets, entries, B, i, overflow, maxPer);
+    team.sync();
+    BP_SUBPHASE(17);
+    uint32_t red[4] = {overflow, maxPer, 0u, 0u};
+    team.template reduce4<2u>(red);
+    buildOverflow = red[0];
+    maxPerAll = max(maxPerAll, red[1]);
+    BP_SUBPHASE(18);
+    return cw;
+}
+
+// Contact forces from the current state, then the start-of-build acceleration (phase 2, NFK:776-779). Also gives
+// each thread its share of the first reduction: (max omega^2, owner) and (min margin bound, owner).
+template <class Team>
+__device__ void initial_forces(const DState& S, const DWorld& W, const Ctl& c, const Team& team, ValOwner& w2, ValOwner& mg) {
+    const float fraction = c.timeX > 0.0f ? clampf(c.timeY / c.timeX, 0.0f, 1.0f) : 1.0f;
+    if (W.nb) {
+        refresh_poses(S, W, team, fraction);
+        team.sync();
+    }
     w2 = ValOwner{-1.0f, 0u};
     mg = ValOwner{__int_as_float(0x7f800000), 0u};
-    for (uint32_t i = r; i < n; i += T) {
-        build_adjacency<kTree>(S, W, buckets, entries, B, i, overflow, maxPer);
-        const uint32_t g = W.boff + i;
+    for (uint32_t i = team.rank(); i < W.n; i += team.size()) {
+        uint32_t g = W.boff + i;
         if (removed(S, g)) continue;
         float im = inv_mass(S, g), omega2;
         float2 F = contact_terms(S, W, i, fraction, im, omega2);
@@ -738,13 +751,7 @@ __device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, cons
         float m = margin_bound(S, g);
         if (m < mg.v) { mg.v = m; mg.o = i; }
     }
-    BP_SUBPHASE(17);
-    uint32_t red[4] = {overflow, maxPer, 0u, 0u};
-    team.template reduce4<2u>(red);
-    buildOverflow = red[0];
-    maxPerAll = max(maxPerAll, red[1]);
-    BP_SUBPHASE(18);
-    return cw;
+    team.sync();
 }
 
 // nativeReduceSubstepInGroup, NFK:625-736
@@ -1027,14 +1034,10 @@ __device__ void assertion_grid(const DState& S, const DWorld& W, const Team& tea
 // candidate test (reach = r_i + r_j + m_i + m_j + sepTol). Truncated rows, joint exclusions, injected states and region
 // wraps void that argument and take the grid path.
 template <class Team, bool kTree>
-// `moved` >= 0: the team-wide "a bubble left its build box" flag computed by the caller (the end of the step folds it
-// into another reduction); -1: computed here.
 __device__ uint32_t assert_contacts(const DState& S, const DWorld& W, const Team& team, uint32_t* buckets, uint32_t* entries,
-                                    uint32_t B, float cw, float fraction, bp_step_report* rep, bool rowsComplete,
-                                    int moved = -1) {
+                                    uint32_t B, float cw, float fraction, bp_step_report* rep, bool rowsComplete) {
     uint32_t unsafe = (!rowsComplete || W.njEnt || (W.flags & BP_WORLD_INJECT_STATE)) ? 1u : 0u;
-    if (!unsafe && moved >= 0) unsafe = (uint32_t)moved;
-    else if (!unsafe) {
+    if (!unsafe) {
         for (uint32_t i = team.rank(); i < W.n; i += team.size()) {
             uint32_t g = W.boff + i;
             if (removed(S, g)) continue;
@@ -1334,10 +1337,12 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
     float* history = S.history + (uint64_t)wi * kFrameLimit;
     uint32_t buildOverflow = 0, overflowMax = 0, maxPer = 0, rebuilds = 0;
     BP_PHASE(0);
-    ValOwner w2, mg;
-    float cw = useTree ? broadphase<Team, true>(S, W, c, team, buckets, entries, B, buildOverflow, maxPer, wi, w2, mg)
-                       : broadphase<Team, false>(S, W, c, team, buckets, entries, B, buildOverflow, maxPer, wi, w2, mg);
+    float cw = useTree ? broadphase<Team, true>(S, W, c, team, buckets, entries, B, buildOverflow, maxPer, wi)
+                       : broadphase<Team, false>(S, W, c, team, buckets, entries, B, buildOverflow, maxPer, wi);
     BP_PHASE(1);
+    ValOwner w2, mg;
+    initial_forces(S, W, c, team, w2, mg);
+    BP_PHASE(2);
     uint32_t violated = 0u;
     for (uint32_t iteration = 0; iteration < 2u * kFrameLimit + 2u; ++iteration) {
         if (!team.ok()) break;
@@ -1351,8 +1356,9 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
             c.cZ = 0u;
             overflowMax = max(overflowMax, buildOverflow);
             ++rebuilds;
-            cw = useTree ? broadphase<Team, true>(S, W, c, team, buckets, entries, B, buildOverflow, maxPer, wi, w2, mg)
-                         : broadphase<Team, false>(S, W, c, team, buckets, entries, B, buildOverflow, maxPer, wi, w2, mg);
+            cw = useTree ? broadphase<Team, true>(S, W, c, team, buckets, entries, B, buildOverflow, maxPer, wi)
+                         : broadphase<Team, false>(S, W, c, team, buckets, entries, B, buildOverflow, maxPer, wi);
+            initial_forces(S, W, c, team, w2, mg);
             BP_PHASE(1);
             continue;
         }
@@ -1383,13 +1389,14 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
     BP_PHASE(5);
 
     // ---- end of step ----
-    uint32_t removedCount = 0, wrapped = 0, nonfinite = 0, movedLocal = 0;
+    uint32_t removedCount = 0, wrapped = 0, nonfinite = 0;
     const bool stepDone = c.cW == 0u;
     if (stepDone && (W.flags & BP_WORLD_HAS_REGION))
         for (uint32_t i = r; i < n; i += T)
             if (!apply_region(S, W, W.boff + i, removedCount, wrapped)) nonfinite = 1u;
     team.sync();
     // contact records: count per bubble, scan, write (kind-major candidate order)
+    uint32_t pairsLocal = 0, segsLocal = 0;
     for (uint32_t i = r; i < n; i += T) {
         uint32_t g = W.boff + i;
         uint32_t cp = 0, cs = 0, active0 = 0, active1 = 0;  // which of the first 64 candidates are active
@@ -1410,17 +1417,16 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
         // the non-contact accelerations are not needed again this step: their slot keeps the activity bits for the
         // writing pass (stored as raw bits)
         S.a0[g] = f2(__uint_as_float(active0), __uint_as_float(active1));
-        if (!removed(S, g)) {
-            // non-finite state (nativeCheckFinite, NPK:5-27), and whether the bubble left the box the assertion's
-            // candidate-row shortcut relies on (see assert_contacts)
-            if (!finite2(S.pos[g]) || !finite2(S.start[g]) || !finite2(S.vel[g]) || !finite2(S.rotw[g])) nonfinite = 1u;
-            if (S.result[g] == 2u || !(len2(sub(S.pos[g], S.ref[g])) <= S.margin[g] + 0.5f * S.phys[g].x)) movedLocal = 1u;
-        }
+        pairsLocal += cp;
+        segsLocal += cs;
     }
     BP_PHASE(6);
-    team.sync();  // every bubble's counts are written before the scans read them
-    const uint32_t pairsAll = team.scan_inplace(S.scanA + W.boff, n);
-    const uint32_t segsAll = team.scan_inplace(S.scanB + W.boff, n);
+    uint32_t pc[4] = {pairsLocal, segsLocal, 0u, 0u};
+    team.template reduce4<0u>(pc);
+    const uint32_t pairsAll = pc[0];
+    const uint32_t segsAll = pc[1];
+    team.scan_inplace(S.scanA + W.boff, n);
+    team.scan_inplace(S.scanB + W.boff, n);
     uint32_t droppedLocal = 0;
     for (uint32_t i = r; i < n; i += T) {
         uint32_t g = W.boff + i;
@@ -1442,16 +1448,20 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
         }
     }
     BP_PHASE(7);
-    uint32_t nf[4] = {nonfinite, droppedLocal, movedLocal, 0u};
-    team.template reduce4<5u>(nf);
+    // non-finite state (nativeCheckFinite, NPK:5-27)
+    for (uint32_t i = r; i < n; i += T) {
+        uint32_t g = W.boff + i;
+        if (removed(S, g)) continue;
+        if (!finite2(S.pos[g]) || !finite2(S.start[g]) || !finite2(S.vel[g]) || !finite2(S.rotw[g])) nonfinite = 1u;
+    }
+    uint32_t nf[4] = {nonfinite, droppedLocal, 0u, 0u};
+    team.template reduce4<1u>(nf);
     const uint32_t anyNonfinite = nf[0];
     const uint32_t contactDropped = nf[1];
     BP_PHASE(8);
     if (!violated && stepDone && !(W.flags & BP_WORLD_NO_END_ASSERTION))
-        violated = useTree ? assert_contacts<Team, true>(S, W, team, buckets, entries, B, cw, 1.0f, rep, buildOverflow == 0u,
-                                                         (int)nf[2])
-                           : assert_contacts<Team, false>(S, W, team, buckets, entries, B, cw, 1.0f, rep,
-                                                          buildOverflow == 0u, (int)nf[2]);
+        violated = useTree ? assert_contacts<Team, true>(S, W, team, buckets, entries, B, cw, 1.0f, rep, buildOverflow == 0u)
+                           : assert_contacts<Team, false>(S, W, team, buckets, entries, B, cw, 1.0f, rep, buildOverflow == 0u);
     BP_PHASE(9);
     int status = BP_OK;
     if (c.cW != 0u) status = BP_E_SUBSTEP_LIMIT;

@@ -58,25 +58,21 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x) {
     return x;
 }
 
-// Shared scratch of the reductions of one block or group. Every array has two halves used by alternate reductions
-// (the team's parity counter picks the half), so a reduction needs a single barrier: each warp writes its partial
-// into this reduction's half, the shape synchronises once, and every warp then combines all partials itself. The
-// next reduction writes the other half, and the one after that can only start once every thread passed the next
-// reduction's barrier, i.e. finished reading this half.
+// Shared scratch used by the block-level primitives (one per CTA).
 struct BlockScratch {
-    float fv[2][32];
-    uint32_t uo[2][32];
-    float fv2[2][32];
-    uint32_t uo2[2][32];
-    uint32_t u[2][32];
-    uint32_t u4[2][4][32];
+    float fv[32];
+    uint32_t uo[32];
+    float fv2[32];
+    uint32_t uo2[32];
+    uint32_t u[33];
     float bcastF[4];
     uint32_t bcastU[8];
+    uint32_t u4[4][33];
 };
 
 // Threads that reduce together: the whole block (BlockShape), or a group of consecutive warps of it (GroupShape),
-// synchronised by a named barrier of its own so the groups of a block run independently. Every reduction below
-// contains one synchronisation of the shape, so it also orders the shared-memory writes made before it.
+// synchronised by a named barrier of its own so the groups of a block run independently. Every reduction below ends
+// with a synchronisation of the shape, so it also orders the shared-memory writes made before it.
 struct BlockShape {
     __device__ __forceinline__ uint32_t tid() const { return threadIdx.x; }
     __device__ __forceinline__ uint32_t count() const { return blockDim.x; }
@@ -96,107 +92,143 @@ struct GroupShape {
 
 // Four sums (kMaxMask bit c set: maximum instead of sum for component c) in one reduction over the shape.
 template <uint32_t kMaxMask, class Shape>
-__device__ __forceinline__ void shape_reduce4(uint32_t (&v)[4], BlockScratch& sh, const Shape& g, uint32_t& par) {
+__device__ __forceinline__ void shape_reduce4(uint32_t (&v)[4], BlockScratch& sh, const Shape& g) {
     const uint32_t lane = threadIdx.x & 31u, warp = g.tid() >> 5, nw = (g.count() + 31u) >> 5;
 #pragma unroll
     for (int c = 0; c < 4; ++c) v[c] = ((kMaxMask >> c) & 1u) ? warp_max(v[c]) : warp_sum(v[c]);
     if (nw == 1u) { g.sync(); return; }
-    const uint32_t p = par;
-    par ^= 1u;
+    g.sync();
     if (lane == 0) {
 #pragma unroll
-        for (int c = 0; c < 4; ++c) sh.u4[p][c][warp] = v[c];
+        for (int c = 0; c < 4; ++c) sh.u4[c][warp] = v[c];
+    }
+    g.sync();
+    if (warp == 0) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            uint32_t y = lane < nw ? sh.u4[c][lane] : 0u;
+            y = ((kMaxMask >> c) & 1u) ? warp_max(y) : warp_sum(y);
+            if (lane == 0) sh.u4[c][32] = y;
+        }
     }
     g.sync();
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        const uint32_t y = lane < nw ? sh.u4[p][c][lane] : 0u;
-        v[c] = ((kMaxMask >> c) & 1u) ? warp_max(y) : warp_sum(y);
-    }
+    for (int c = 0; c < 4; ++c) v[c] = sh.u4[c][32];
+}
+template <uint32_t kMaxMask> __device__ __forceinline__ void block_reduce4(uint32_t (&v)[4], BlockScratch& sh) {
+    shape_reduce4<kMaxMask>(v, sh, BlockShape{});
 }
 
-// (value, owner) reduction over the shape; result in every thread.
-template <bool kMax, class Shape>
-__device__ __forceinline__ ValOwner shape_pick(ValOwner x, BlockScratch& sh, const Shape& g, uint32_t& par) {
+// (value, owner) reduction over the shape; result broadcast to every thread.
+template <bool kMax, class Shape> __device__ __forceinline__ ValOwner shape_pick(ValOwner x, BlockScratch& sh, const Shape& g) {
     const uint32_t lane = threadIdx.x & 31u, warp = g.tid() >> 5, nw = (g.count() + 31u) >> 5;
     x = warp_pick<kMax>(x);
     if (nw == 1u) { g.sync(); return x; }
-    const uint32_t p = par;
-    par ^= 1u;
-    if (lane == 0) { sh.fv[p][warp] = x.v; sh.uo[p][warp] = x.o; }
     g.sync();
-    const ValOwner y = lane < nw ? ValOwner{sh.fv[p][lane], sh.uo[p][lane]} : x;
-    return warp_pick<kMax>(y);
+    if (lane == 0) { sh.fv[warp] = x.v; sh.uo[warp] = x.o; }
+    g.sync();
+    if (warp == 0) {
+        ValOwner y = lane < nw ? ValOwner{sh.fv[lane], sh.uo[lane]} : x;
+        y = warp_pick<kMax>(y);
+        if (lane == 0) { sh.fv[0] = y.v; sh.uo[0] = y.o; }
+    }
+    g.sync();
+    return ValOwner{sh.fv[0], sh.uo[0]};
+}
+template <bool kMax> __device__ __forceinline__ ValOwner block_pick(ValOwner x, BlockScratch& sh) {
+    return shape_pick<kMax>(x, sh, BlockShape{});
 }
 
-// Two (value, owner) reductions behind one barrier (kMaxA / kMaxB: maximum or minimum).
+// Two (value, owner) reductions in the barriers of one (kMaxA / kMaxB: maximum or minimum).
 template <bool kMaxA, bool kMaxB, class Shape>
-__device__ __forceinline__ void shape_pick2(ValOwner& a, ValOwner& b, BlockScratch& sh, const Shape& g, uint32_t& par) {
+__device__ __forceinline__ void shape_pick2(ValOwner& a, ValOwner& b, BlockScratch& sh, const Shape& g) {
     const uint32_t lane = threadIdx.x & 31u, warp = g.tid() >> 5, nw = (g.count() + 31u) >> 5;
     a = warp_pick<kMaxA>(a);
     b = warp_pick<kMaxB>(b);
     if (nw == 1u) { g.sync(); return; }
-    const uint32_t p = par;
-    par ^= 1u;
-    if (lane == 0) { sh.fv[p][warp] = a.v; sh.uo[p][warp] = a.o; sh.fv2[p][warp] = b.v; sh.uo2[p][warp] = b.o; }
     g.sync();
-    const ValOwner x = lane < nw ? ValOwner{sh.fv[p][lane], sh.uo[p][lane]} : a;
-    const ValOwner y = lane < nw ? ValOwner{sh.fv2[p][lane], sh.uo2[p][lane]} : b;
-    a = warp_pick<kMaxA>(x);
-    b = warp_pick<kMaxB>(y);
+    if (lane == 0) { sh.fv[warp] = a.v; sh.uo[warp] = a.o; sh.fv2[warp] = b.v; sh.uo2[warp] = b.o; }
+    g.sync();
+    if (warp == 0) {
+        ValOwner x = lane < nw ? ValOwner{sh.fv[lane], sh.uo[lane]} : a;
+        ValOwner y = lane < nw ? ValOwner{sh.fv2[lane], sh.uo2[lane]} : b;
+        x = warp_pick<kMaxA>(x);
+        y = warp_pick<kMaxB>(y);
+        if (lane == 0) { sh.fv[0] = x.v; sh.uo[0] = x.o; sh.fv2[0] = y.v; sh.uo2[0] = y.o; }
+    }
+    g.sync();
+    a = ValOwner{sh.fv[0], sh.uo[0]};
+    b = ValOwner{sh.fv2[0], sh.uo2[0]};
+}
+template <bool kMaxA, bool kMaxB>
+__device__ __forceinline__ void block_pick2(ValOwner& a, ValOwner& b, BlockScratch& sh) {
+    shape_pick2<kMaxA, kMaxB>(a, b, sh, BlockShape{});
 }
 
-template <class Shape>
-__device__ __forceinline__ uint32_t shape_reduce_u(uint32_t x, bool isMax, BlockScratch& sh, const Shape& g, uint32_t& par) {
+template <class Shape> __device__ __forceinline__ uint32_t shape_reduce_u(uint32_t x, bool isMax, BlockScratch& sh, const Shape& g) {
     const uint32_t lane = threadIdx.x & 31u, warp = g.tid() >> 5, nw = (g.count() + 31u) >> 5;
     x = isMax ? warp_max(x) : warp_sum(x);
     if (nw == 1u) { g.sync(); return x; }
-    const uint32_t p = par;
-    par ^= 1u;
-    if (lane == 0) sh.u[p][warp] = x;
     g.sync();
-    const uint32_t y = lane < nw ? sh.u[p][lane] : 0u;
-    return isMax ? warp_max(y) : warp_sum(y);
+    if (lane == 0) sh.u[warp] = x;
+    g.sync();
+    if (warp == 0) {
+        uint32_t y = lane < nw ? sh.u[lane] : 0u;
+        y = isMax ? warp_max(y) : warp_sum(y);
+        if (lane == 0) sh.u[32] = y;
+    }
+    g.sync();
+    return sh.u[32];
 }
+__device__ __forceinline__ uint32_t block_sum(uint32_t x, BlockScratch& sh) { return shape_reduce_u(x, false, sh, BlockShape{}); }
+__device__ __forceinline__ uint32_t block_max(uint32_t x, BlockScratch& sh) { return shape_reduce_u(x, true, sh, BlockShape{}); }
 
-template <class Shape> __device__ __forceinline__ float shape_fmax(float x, BlockScratch& sh, const Shape& g, uint32_t& par) {
+template <class Shape> __device__ __forceinline__ float shape_fmax(float x, BlockScratch& sh, const Shape& g) {
     const uint32_t lane = threadIdx.x & 31u, warp = g.tid() >> 5, nw = (g.count() + 31u) >> 5;
     x = warp_fmax(x);
     if (nw == 1u) { g.sync(); return x; }
-    const uint32_t p = par;
-    par ^= 1u;
-    if (lane == 0) sh.fv[p][warp] = x;
     g.sync();
-    const float y = lane < nw ? sh.fv[p][lane] : x;
-    return warp_fmax(y);
+    if (lane == 0) sh.fv[warp] = x;
+    g.sync();
+    if (warp == 0) {
+        float y = lane < nw ? sh.fv[lane] : x;
+        y = warp_fmax(y);
+        if (lane == 0) sh.fv[0] = y;
+    }
+    g.sync();
+    return sh.fv[0];
 }
+__device__ __forceinline__ float block_fmax(float x, BlockScratch& sh) { return shape_fmax(x, sh, BlockShape{}); }
 
 // Exclusive scan of one value per thread over the shape; *total receives the shape's total.
 template <class Shape>
-__device__ __forceinline__ uint32_t shape_excl_scan(uint32_t x, uint32_t* total, BlockScratch& sh, const Shape& g,
-                                                    uint32_t& par) {
+__device__ __forceinline__ uint32_t shape_excl_scan(uint32_t x, uint32_t* total, BlockScratch& sh, const Shape& g) {
     const uint32_t lane = threadIdx.x & 31u, warp = g.tid() >> 5, nw = (g.count() + 31u) >> 5;
-    const uint32_t incl = warp_incl_scan(x);
+    uint32_t incl = warp_incl_scan(x);
     if (nw == 1u) {
         *total = __shfl_sync(0xffffffffu, incl, 31);
         g.sync();
         return incl - x;
     }
-    const uint32_t p = par;
-    par ^= 1u;
-    if (lane == 31u) sh.u[p][warp] = incl;  // widths are multiples of 32: lane 31 ends each warp
     g.sync();
-    const uint32_t y = lane < nw ? sh.u[p][lane] : 0u;
-    const uint32_t s = warp_incl_scan(y);
-    *total = __shfl_sync(0xffffffffu, s, nw - 1u);
-    return __shfl_sync(0xffffffffu, s - y, warp) + incl - x;
+    if (lane == 31u || g.tid() == g.count() - 1) sh.u[warp] = incl;
+    g.sync();
+    if (warp == 0) {
+        uint32_t y = lane < nw ? sh.u[lane] : 0u;
+        uint32_t s = warp_incl_scan(y);
+        if (lane < nw) sh.u[lane] = s - y;
+        if (lane == nw - 1) sh.u[32] = s;
+    }
+    g.sync();
+    *total = sh.u[32];
+    return sh.u[warp] + incl - x;
+}
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t* total, BlockScratch& sh) {
+    return shape_excl_scan(x, total, sh, BlockShape{});
 }
 
-// Exclusive scan of `count` values in place over the shape (values in memory visible to the whole shape); returns the
-// total.
-template <class Shape>
-__device__ __forceinline__ uint32_t shape_scan_inplace(uint32_t* values, uint32_t count, BlockScratch& sh, const Shape& g,
-                                                       uint32_t& par) {
+// Exclusive scan of `count` values in place over the shape (values in memory visible to the whole shape).
+template <class Shape> __device__ __forceinline__ void shape_scan_inplace(uint32_t* values, uint32_t count, BlockScratch& sh, const Shape& g) {
     const uint32_t T = g.count(), r = g.tid();
     uint32_t per = (count + T - 1) / T;
     uint32_t first = min(r * per, count), last = min(first + per, count);
@@ -204,34 +236,9 @@ __device__ __forceinline__ uint32_t shape_scan_inplace(uint32_t* values, uint32_
     if (T == 32u) __syncwarp();
     for (uint32_t i = first; i < last; ++i) local += values[i];
     uint32_t total;
-    uint32_t running = shape_excl_scan(local, &total, sh, g, par);
+    uint32_t running = shape_excl_scan(local, &total, sh, g);
     for (uint32_t i = first; i < last; ++i) { uint32_t own = values[i]; values[i] = running; running += own; }
     g.sync();
-    return total;
-}
-
-// Whole-block forms.
-template <uint32_t kMaxMask> __device__ __forceinline__ void block_reduce4(uint32_t (&v)[4], BlockScratch& sh, uint32_t& par) {
-    shape_reduce4<kMaxMask>(v, sh, BlockShape{}, par);
-}
-template <bool kMax> __device__ __forceinline__ ValOwner block_pick(ValOwner x, BlockScratch& sh, uint32_t& par) {
-    return shape_pick<kMax>(x, sh, BlockShape{}, par);
-}
-template <bool kMaxA, bool kMaxB>
-__device__ __forceinline__ void block_pick2(ValOwner& a, ValOwner& b, BlockScratch& sh, uint32_t& par) {
-    shape_pick2<kMaxA, kMaxB>(a, b, sh, BlockShape{}, par);
-}
-__device__ __forceinline__ uint32_t block_sum(uint32_t x, BlockScratch& sh, uint32_t& par) {
-    return shape_reduce_u(x, false, sh, BlockShape{}, par);
-}
-__device__ __forceinline__ uint32_t block_max(uint32_t x, BlockScratch& sh, uint32_t& par) {
-    return shape_reduce_u(x, true, sh, BlockShape{}, par);
-}
-__device__ __forceinline__ float block_fmax(float x, BlockScratch& sh, uint32_t& par) {
-    return shape_fmax(x, sh, BlockShape{}, par);
-}
-__device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t* total, BlockScratch& sh, uint32_t& par) {
-    return shape_excl_scan(x, total, sh, BlockShape{}, par);
 }
 
 // ----------------------------------------------------------------------------------------------------------------
@@ -239,7 +246,6 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t* total,
 // ----------------------------------------------------------------------------------------------------------------
 struct CtaTeam {
     BlockScratch* sh;
-    mutable uint32_t par = 0;  // half of the scratch the next reduction uses
     __device__ uint32_t rank() const { return threadIdx.x; }
     __device__ uint32_t size() const { return blockDim.x; }
     __device__ bool leader() const { return threadIdx.x == 0; }
@@ -248,17 +254,17 @@ struct CtaTeam {
     __device__ bool shared_leader() const { return threadIdx.x == 0; }
     __device__ void shared_sync() const { __syncthreads(); }
     __device__ bool ok() const { return true; }
-    template <bool kMax> __device__ ValOwner pick(ValOwner x) const { return block_pick<kMax>(x, *sh, par); }
+    template <bool kMax> __device__ ValOwner pick(ValOwner x) const { return block_pick<kMax>(x, *sh); }
     template <bool kMaxA, bool kMaxB> __device__ void pick2(ValOwner& a, ValOwner& b) const {
-        block_pick2<kMaxA, kMaxB>(a, b, *sh, par);
+        block_pick2<kMaxA, kMaxB>(a, b, *sh);
     }
-    __device__ uint32_t sum(uint32_t x) const { return block_sum(x, *sh, par); }
-    __device__ uint32_t umax(uint32_t x) const { return block_max(x, *sh, par); }
-    __device__ float fmax(float x) const { return block_fmax(x, *sh, par); }
-    template <uint32_t kMaxMask> __device__ void reduce4(uint32_t (&v)[4]) const { block_reduce4<kMaxMask>(v, *sh, par); }
-    // Exclusive scan of `count` values in place (values live in memory visible to the whole team); returns the total.
-    __device__ uint32_t scan_inplace(uint32_t* values, uint32_t count) const {
-        return shape_scan_inplace(values, count, *sh, BlockShape{}, par);
+    __device__ uint32_t sum(uint32_t x) const { return block_sum(x, *sh); }
+    __device__ uint32_t umax(uint32_t x) const { return block_max(x, *sh); }
+    __device__ float fmax(float x) const { return block_fmax(x, *sh); }
+    template <uint32_t kMaxMask> __device__ void reduce4(uint32_t (&v)[4]) const { block_reduce4<kMaxMask>(v, *sh); }
+    // Exclusive scan of `count` values in place (values live in memory visible to the whole team).
+    __device__ void scan_inplace(uint32_t* values, uint32_t count) const {
+        shape_scan_inplace(values, count, *sh, BlockShape{});
     }
 };
 
@@ -270,7 +276,6 @@ struct CtaTeam {
 struct GroupTeam {
     BlockScratch* sh;  // the group's own scratch
     GroupShape g;
-    mutable uint32_t par = 0;
     __device__ uint32_t rank() const { return g.tid(); }
     __device__ uint32_t size() const { return g.width; }
     __device__ bool leader() const { return g.tid() == 0u; }
@@ -278,19 +283,15 @@ struct GroupTeam {
     __device__ bool shared_leader() const { return g.tid() == 0u; }
     __device__ void shared_sync() const { g.sync(); }
     __device__ bool ok() const { return true; }
-    template <bool kMax> __device__ ValOwner pick(ValOwner x) const { return shape_pick<kMax>(x, *sh, g, par); }
+    template <bool kMax> __device__ ValOwner pick(ValOwner x) const { return shape_pick<kMax>(x, *sh, g); }
     template <bool kMaxA, bool kMaxB> __device__ void pick2(ValOwner& a, ValOwner& b) const {
-        shape_pick2<kMaxA, kMaxB>(a, b, *sh, g, par);
+        shape_pick2<kMaxA, kMaxB>(a, b, *sh, g);
     }
-    __device__ uint32_t sum(uint32_t x) const { return shape_reduce_u(x, false, *sh, g, par); }
-    __device__ uint32_t umax(uint32_t x) const { return shape_reduce_u(x, true, *sh, g, par); }
-    __device__ float fmax(float x) const { return shape_fmax(x, *sh, g, par); }
-    template <uint32_t kMaxMask> __device__ void reduce4(uint32_t (&v)[4]) const {
-        shape_reduce4<kMaxMask>(v, *sh, g, par);
-    }
-    __device__ uint32_t scan_inplace(uint32_t* values, uint32_t count) const {
-        return shape_scan_inplace(values, count, *sh, g, par);
-    }
+    __device__ uint32_t sum(uint32_t x) const { return shape_reduce_u(x, false, *sh, g); }
+    __device__ uint32_t umax(uint32_t x) const { return shape_reduce_u(x, true, *sh, g); }
+    __device__ float fmax(float x) const { return shape_fmax(x, *sh, g); }
+    template <uint32_t kMaxMask> __device__ void reduce4(uint32_t (&v)[4]) const { shape_reduce4<kMaxMask>(v, *sh, g); }
+    __device__ void scan_inplace(uint32_t* values, uint32_t count) const { shape_scan_inplace(values, count, *sh, g); }
 };
 
 // GPU-scope memory operations of the grid barrier.
@@ -326,7 +327,6 @@ struct GridTeam {
     uint32_t* parity;        // per-thread copy lives in registers; this is unused storage
     mutable uint32_t par;
     mutable bool failed;
-    mutable uint32_t spar = 0;  // half of the block scratch the next block-level reduction uses
 
     __device__ uint32_t rank() const { return blockIdx.x * blockDim.x + threadIdx.x; }
     __device__ uint32_t size() const { return gridDim.x * blockDim.x; }
@@ -364,7 +364,7 @@ struct GridTeam {
     }
 
     template <bool kMax> __device__ ValOwner pick(ValOwner x) const {
-        x = block_pick<kMax>(x, *sh, spar);
+        x = block_pick<kMax>(x, *sh);
         uint32_t base = par * 4u * gridDim.x;
         if (threadIdx.x == 0) { pv[base + blockIdx.x] = x.v; po[base + blockIdx.x] = x.o; }
         par ^= 1u;
@@ -382,7 +382,7 @@ struct GridTeam {
         return ValOwner{sh->bcastF[0], sh->bcastU[0]};
     }
     template <bool kMaxA, bool kMaxB> __device__ void pick2(ValOwner& a, ValOwner& b) const {
-        block_pick2<kMaxA, kMaxB>(a, b, *sh, spar);
+        block_pick2<kMaxA, kMaxB>(a, b, *sh);
         const uint32_t base = par * 4u * gridDim.x, G = gridDim.x;
         if (threadIdx.x == 0) {
             pv[base + blockIdx.x] = a.v; po[base + blockIdx.x] = a.o;
@@ -408,7 +408,7 @@ struct GridTeam {
         b = ValOwner{sh->bcastF[2], sh->bcastU[3]};
     }
     __device__ uint32_t reduce_u(uint32_t x, bool isMax) const {
-        x = isMax ? block_max(x, *sh, spar) : block_sum(x, *sh, spar);
+        x = isMax ? block_max(x, *sh) : block_sum(x, *sh);
         uint32_t base = par * 4u * gridDim.x;
         if (threadIdx.x == 0) po[base + blockIdx.x] = x;
         par ^= 1u;
@@ -429,7 +429,7 @@ struct GridTeam {
     __device__ uint32_t umax(uint32_t x) const { return reduce_u(x, true); }
     // Four sums / maxima behind one grid barrier (kMaxMask bit c set: maximum for component c).
     template <uint32_t kMaxMask> __device__ void reduce4(uint32_t (&v)[4]) const {
-        block_reduce4<kMaxMask>(v, *sh, spar);
+        block_reduce4<kMaxMask>(v, *sh);
         const uint32_t base = par * 4u * gridDim.x, G = gridDim.x;
         if (threadIdx.x == 0) {
 #pragma unroll
@@ -447,15 +447,15 @@ struct GridTeam {
                     y = isMax ? max(y, z) : y + z;
                 }
                 y = isMax ? warp_max(y) : warp_sum(y);
-                if (threadIdx.x == 0) sh->bcastU[c] = y;
+                if (threadIdx.x == 0) sh->u4[c][32] = y;
             }
         }
         __syncthreads();
 #pragma unroll
-        for (int c = 0; c < 4; ++c) v[c] = sh->bcastU[c];
+        for (int c = 0; c < 4; ++c) v[c] = sh->u4[c][32];
     }
     __device__ float fmax(float x) const {
-        x = block_fmax(x, *sh, spar);
+        x = block_fmax(x, *sh);
         uint32_t base = par * 4u * gridDim.x;
         if (threadIdx.x == 0) pv[base + blockIdx.x] = x;
         par ^= 1u;
@@ -470,7 +470,7 @@ struct GridTeam {
         return sh->bcastF[1];
     }
     // Exclusive scan of `count` values in global memory: each block scans a contiguous chunk.
-    __device__ uint32_t scan_inplace(uint32_t* values, uint32_t count) const {
+    __device__ void scan_inplace(uint32_t* values, uint32_t count) const {
         uint32_t per = (count + gridDim.x - 1) / gridDim.x;
         uint32_t first = min(blockIdx.x * per, count), last = min(first + per, count);
         uint32_t tper = (last - first + blockDim.x - 1) / blockDim.x;
@@ -478,27 +478,20 @@ struct GridTeam {
         uint32_t local = 0;
         for (uint32_t i = tf; i < tl; ++i) local += __ldcg(values + i);
         uint32_t total;
-        uint32_t running = block_excl_scan(local, &total, *sh, spar);
+        uint32_t running = block_excl_scan(local, &total, *sh);
         uint32_t base = par * 4u * gridDim.x;
         if (threadIdx.x == 0) po[base + blockIdx.x] = total;
         par ^= 1u;
         sync();
         if (threadIdx.x == 0) {
-            uint32_t off = 0, all = 0;
-            for (uint32_t b = 0; b < gridDim.x; ++b) {
-                const uint32_t part = __ldcg(po + base + b);
-                if (b < blockIdx.x) off += part;
-                all += part;
-            }
+            uint32_t off = 0;
+            for (uint32_t b = 0; b < blockIdx.x; ++b) off += __ldcg(po + base + b);
             sh->bcastU[2] = off;
-            sh->bcastU[3] = all;
         }
         __syncthreads();
         running += sh->bcastU[2];
-        const uint32_t gridTotal = sh->bcastU[3];
         for (uint32_t i = tf; i < tl; ++i) { uint32_t own = __ldcg(values + i); values[i] = running; running += own; }
         sync();
-        return gridTotal;
     }
 };
 
