@@ -10,6 +10,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -457,8 +458,20 @@ int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc
 // Blocks of a whole-GPU step of a world of n bubbles: about one thread per bubble (at least 8 blocks), never more
 // than fit on the GPU at once. Every block takes part in every grid barrier, so blocks without bubbles only make the
 // barriers slower.
+// Bubbles per block of the whole-GPU team: kLargeBubblesPerBlock unless BP_LARGE_BUBBLES_PER_BLOCK overrides it (a
+// tuning knob: fewer blocks make each grid barrier cheaper and each phase longer).
+uint32_t large_bubbles_per_block() {
+    static const uint32_t value = [] {
+        const char* env = std::getenv("BP_LARGE_BUBBLES_PER_BLOCK");
+        const long v = env ? std::strtol(env, nullptr, 10) : 0;
+        return v >= 64 && v <= (1 << 16) ? (uint32_t)v : kLargeBubblesPerBlock;
+    }();
+    return value;
+}
+
 int large_blocks_for(const WorldSet& ws, uint32_t n) {
-    const int want = (int)((n + kLargeThreads - 1) / kLargeThreads);
+    const uint32_t per = large_bubbles_per_block();
+    const int want = (int)((n + per - 1) / per);
     return std::max(1, std::min(ws.largeBlocks, std::max(want, 8)));
 }
 

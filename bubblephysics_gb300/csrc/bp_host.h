@@ -83,6 +83,7 @@ using namespace bp;
 
 constexpr uint32_t kCtaMaxBubbles = 4096;
 constexpr int kLargeThreads = 512;
+constexpr uint32_t kLargeBubblesPerBlock = 512;  // bubbles per block of the whole-GPU team (one per thread)
 constexpr uint32_t kDefaultThreads = 256;
 constexpr uint32_t kDefaultWarpMax = 64;
 constexpr uint32_t kWarpSubsteps = 16;   // a world that took more substeps last step gets a whole block
