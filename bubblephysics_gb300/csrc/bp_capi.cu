@@ -101,6 +101,7 @@ bool group_layout(uint32_t threads, uint32_t groupWidth, uint32_t maxN, uint32_t
 // cost. Shared memory is sized so any world can be a CTA world and any world up to the threshold a group world.
 cudaError_t schedule(WorldSet& ws, uint32_t threads, uint32_t warpMax, uint32_t groupWidth) {
     groupWidth = std::min(std::max(groupWidth, 32u), threads);
+    if (threads % groupWidth) groupWidth = 32u;  // groups tile the block exactly
     ws.threads = threads;
     ws.warpMax = warpMax;
     ws.groupWidth = groupWidth;
@@ -560,7 +561,7 @@ cudaError_t autotune(WorldSet& ws) {
     cudaError_t err = take_snapshot(ws, snap);
     cudaStream_t st = ws.ctx->stream;
     // block width x group-queue threshold x group width; combinations whose group grids do not fit are skipped
-    const uint32_t widths[] = {256, 512};
+    const uint32_t widths[] = {256, 384, 512};
     const uint32_t warpMaxes[] = {0, 64, 128, 256, 512, 1024};
     const uint32_t groupWidths[] = {32, 64, 128};
     float best = 1e30f;
@@ -1358,7 +1359,7 @@ int bp_batch_create(bp_context* context, uint32_t world_count, const bp_world_de
         uint32_t gw = config->group_width ? config->group_width : b->set.groupWidth;
         uint32_t cap = 0;
         if (t % 32u || t > 512u || wm > kCtaMaxBubbles || (gw != 32u && gw != 64u && gw != 128u && gw != 256u) ||
-            gw > t || (wm && !group_layout(t, gw, wm, &cap))) {
+            gw > t || t % gw || (wm && !group_layout(t, gw, wm, &cap))) {
             delete b;
             context_unref(context);
             return BP_E_INVALID;

@@ -420,8 +420,9 @@ int bp_server_create(bp_context* context, const bp_server_config* config, bp_ser
     if (!s->cfg.warp_world_max) s->cfg.warp_world_max = kDefaultWarpMax;
     if (!s->cfg.group_width) s->cfg.group_width = kDefaultGroupWidth;
     const uint32_t gw = s->cfg.group_width;
-    if ((s->cfg.threads_per_world != 128 && s->cfg.threads_per_world != 256 && s->cfg.threads_per_world != 512) ||
-        (gw != 32 && gw != 64 && gw != 128 && gw != 256) || gw > s->cfg.threads_per_world) {
+    const uint32_t tw = s->cfg.threads_per_world;
+    if ((tw != 128 && tw != 256 && tw != 384 && tw != 512) || (gw != 32 && gw != 64 && gw != 128 && gw != 256) ||
+        gw > tw || tw % gw) {
         server_free(s);
         return BP_E_INVALID;
     }
