@@ -451,8 +451,14 @@ def run_ours(args, rank, world_size, local_rank):
     except Exception:
         traffic = None
     alg_per_launch = alg_bytes / max(kernel_launches, 1)
-    # the CPU baseline: the reference arm's measurement itself (same worlds, warm-up and timed steps)
-    leg = cpu_leg(specs, args.steps if args.cpu_steps <= 0 else min(args.cpu_steps, args.steps), args.warmup)
+    # the CPU baseline: the reference arm's measurement itself, run as the reference arm runs (a fresh process: this
+    # one holds the CUDA context, torch and the GPU work's threads, which slowed the oracle's OpenMP team by 2x)
+    cpu_steps = args.steps if args.cpu_steps <= 0 else min(args.cpu_steps, args.steps)
+    ref = subprocess.run([sys.executable, str(Path(__file__).resolve()), "--impl", "reference", "--steps", str(cpu_steps),
+                          "--warmup", str(args.warmup), "--worlds", str(args.worlds)], capture_output=True, text=True)
+    ref_line = json.loads(ref.stdout.strip().splitlines()[-1])
+    leg = {"value": ref_line["value"], "cores": ref_line["cpu_baseline"]["cores"],
+           "sample": ref_line["cpu_baseline"]["sample"]}
     lat = sorted(step_ms)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
@@ -474,7 +480,7 @@ def run_ours(args, rank, world_size, local_rank):
                      "algorithmic_bytes_per_launch": alg_per_launch,
                      "bytes_model": "76 + 40*k per bubble-substep, 96 + 8*k per bubble grid build (k = mean degree)"},
         "cpu_baseline": {"value": leg["value"], "unit": UNIT, "cores": leg["cores"], "kind": "port",
-                         "sample": cpu_sample_text(leg)},
+                         "sample": leg["sample"] + " (bench.py --impl reference, run as a separate process)"},
         "clocks": clocks,
         "gpu_launches": gpu_launches,
         "single_worlds": singles,
