@@ -21,7 +21,7 @@ SOURCES = ["bp_step.cu", "bp_noalloc.cu", "bp_capi.cu", "bp_aux.cu", "bp_server.
 # bp_step_variant.cu is compiled once per (kernel, block width, tree) variant: the persistent step kernels are the
 # largest functions of the library and compile in parallel this way.
 VARIANT_SOURCE = "bp_step_variant.cu"
-VARIANTS = [(kind, threads, tree) for kind in (0, 1) for threads in (128, 256, 384, 512) for tree in (0, 1)]
+VARIANTS = [(kind, threads, tree) for kind in (0, 1) for threads in (128, 256, 512) for tree in (0, 1)]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
               "-Xcompiler", "-fPIC,-ffp-contract=off", "-diag-suppress", "177"]

@@ -561,7 +561,7 @@ cudaError_t autotune(WorldSet& ws) {
     cudaError_t err = take_snapshot(ws, snap);
     cudaStream_t st = ws.ctx->stream;
     // block width x group-queue threshold x group width; combinations whose group grids do not fit are skipped
-    const uint32_t widths[] = {256, 384, 512};
+    const uint32_t widths[] = {256, 512};
     const uint32_t warpMaxes[] = {0, 64, 128, 256, 512, 1024};
     const uint32_t groupWidths[] = {32, 64, 128};
     float best = 1e30f;

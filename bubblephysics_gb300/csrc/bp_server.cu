@@ -421,7 +421,7 @@ int bp_server_create(bp_context* context, const bp_server_config* config, bp_ser
     if (!s->cfg.group_width) s->cfg.group_width = kDefaultGroupWidth;
     const uint32_t gw = s->cfg.group_width;
     const uint32_t tw = s->cfg.threads_per_world;
-    if ((tw != 128 && tw != 256 && tw != 384 && tw != 512) || (gw != 32 && gw != 64 && gw != 128 && gw != 256) ||
+    if ((tw != 128 && tw != 256 && tw != 512) || (gw != 32 && gw != 64 && gw != 128 && gw != 256) ||
         gw > tw || tw % gw) {
         server_free(s);
         return BP_E_INVALID;

@@ -105,10 +105,8 @@ size_t persistent_smem(const QueueArgs& q, uint32_t threads) {
     return (cta > warp ? cta : warp) * sizeof(uint32_t);
 }
 
-// Block width of the variant that serves `threads` (128, 256, 384 or 512).
-static uint32_t variant_width(uint32_t threads) {
-    return threads <= 128u ? 128u : threads <= 256u ? 256u : threads <= 384u ? 384u : 512u;
-}
+// Block width of the variant that serves `threads` (128, 256 or 512).
+static uint32_t variant_width(uint32_t threads) { return threads <= 128u ? 128u : threads <= 256u ? 256u : 512u; }
 
 cudaError_t launch_persistent(const DState& S, const QueueArgs& q, uint32_t threads, uint32_t blocks, cudaStream_t stream) {
     if (q.nCta + q.nWarp == 0u) return cudaSuccess;

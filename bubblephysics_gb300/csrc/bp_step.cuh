@@ -1648,7 +1648,7 @@ __global__ void __launch_bounds__(kThreads, 2) served_step_kernel(const DState* 
 // Launchers of one kernel variant (defined in bp_step_variant.cu, once per variant): a launch with `threads` threads
 // per block (at most the variant's width), the persistent kernel's blocks per SM at a dynamic shared-memory size, and
 // `prepare`, which raises the kernel's dynamic shared-memory limit.
-#define BP_STEP_VARIANTS(X) X(128, 0) X(256, 0) X(384, 0) X(512, 0) X(128, 1) X(256, 1) X(384, 1) X(512, 1)
+#define BP_STEP_VARIANTS(X) X(128, 0) X(256, 0) X(512, 0) X(128, 1) X(256, 1) X(512, 1)
 #define BP_DECLARE_VARIANT(T, R)                                                                                     \
     cudaError_t persistent_launch_##T##_##R(const DState& S, const QueueArgs& q, uint32_t threads, uint32_t blocks,  \
                                             size_t smem, cudaStream_t stream);                                      \

@@ -462,7 +462,7 @@ typedef struct bp_server_config {
     uint32_t max_worlds;             /* worlds the server can hold (resident or evicted) */
     uint32_t max_batch_worlds;       /* worlds per batched launch; 0 = no limit */
     uint32_t streams;                /* batches in flight at once; 0 = 8 */
-    uint32_t threads_per_world;      /* block width for worlds stepped by a block (128, 256, 384, 512); 0 = 512 */
+    uint32_t threads_per_world;      /* block width for worlds stepped by a block (128, 256, 512); 0 = 512 */
     uint32_t warp_world_max;         /* worlds of at most this many bubbles go to the group queue (a group of
                                         group_width threads per world); 0 = 64, UINT32_MAX = none */
     uint32_t flags;                  /* BP_SERVER_* */
