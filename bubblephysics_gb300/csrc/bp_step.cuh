@@ -12,6 +12,8 @@
 // Per-bubble arithmetic follows NFK / NGK operation order exactly; reductions pick the largest / smallest value with
 // the lower bubble index winning ties, which is order-independent, so every team shape gives bit-identical results.
 #pragma once
+#include <type_traits>
+
 #include "bp_team.cuh"
 #include "bp_tree.cuh"
 
@@ -62,6 +64,8 @@ __device__ __forceinline__ uint32_t grid_hash(long long cx, long long cy, uint32
 }
 
 __device__ __forceinline__ bool removed(const DState& S, uint32_t g) { return (S.flags[g] & kRemoved) != 0u; }
+
+template <class Team> constexpr bool kGridTeam = std::is_same<Team, GridTeam>::value;
 // nativeIsStatic / nativeInverseMass / nativeIsForceDriven / nativeEffectiveVelocity, NFK:388-392
 __device__ __forceinline__ bool is_static(uint32_t flags, float invMass) {
     return !(invMass > 0.0f) || ((flags & BP_BUBBLE_ENABLED) && (flags & BP_BUBBLE_STATIC));
@@ -717,7 +721,9 @@ __device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, cons
         else
             for (uint32_t bi = warp; bi < W.nb; bi += warps) emit_body_row(S, W, bi, lane, overflow, maxPer);
     }
-    team.sync();
+    // body rows are read by the adjacency rows; without bodies the whole-GPU team skips this grid barrier (the
+    // candidate rows' barrier is above). The block and group teams keep it: removing it measured slower there.
+    if (W.nb || !kGridTeam<Team>) team.sync();
     BP_SUBPHASE(16);
     for (uint32_t i = r; i < n; i += T) build_adjacency<kTree>(S, W, buckets, entries, B, i, overflow, maxPer);
     team.sync();
@@ -1371,7 +1377,11 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
         mg = ValOwner{__int_as_float(0x7f800000), 0u};
         for (uint32_t i = r; i < n; i += T)
             if (!removed(S, W.boff + i)) force_kick(S, W, i, h, fraction, w2, mg);
-        team.sync();
+        // The whole-GPU team needs no barrier here: whatever reads other bubbles' new state next (the next reduction,
+        // an injection, the assertion, the end of the step, a rebuild's grid reductions) passes one first, and the
+        // body poses the force pass reads are rewritten only behind several. The block and group teams keep it:
+        // removing it measured slower there.
+        if (!kGridTeam<Team>) team.sync();
         BP_PHASE(4);
         if (W.flags & BP_WORLD_INJECT_STATE) {
             if (c.cY == W.injectSubstep + 1u)
