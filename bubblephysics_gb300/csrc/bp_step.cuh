@@ -676,12 +676,21 @@ __device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, cons
         cwl = fmaxf(cwl, 2.0f * (radius + m) + W.sepTol);  // nativePrepareGrid, NGK:163-177
     }
     BP_SUBPHASE(12);
+    // The whole-GPU team clears the grid before the cell-width reduction, whose grid barrier then orders the clear
+    // before the cells (the last readers of the buckets passed barriers since); the other teams after it.
+    if (kGridTeam<Team>) {
+        for (uint32_t b = r; b < B; b += T) buckets[b] = 0u;
+        if (kTree)
+            for (uint32_t bi = r; bi < W.nb; bi += T) S.bodyTotal[W.bodyOff + bi] = 0u;
+    }
     float cw = team.fmax(cwl);
     cw = fmaxf(cw, kFltMin);
-    for (uint32_t b = r; b < B; b += T) buckets[b] = 0u;
-    if (kTree)
-        for (uint32_t bi = r; bi < W.nb; bi += T) S.bodyTotal[W.bodyOff + bi] = 0u;
-    team.sync();
+    if (!kGridTeam<Team>) {
+        for (uint32_t b = r; b < B; b += T) buckets[b] = 0u;
+        if (kTree)
+            for (uint32_t bi = r; bi < W.nb; bi += T) S.bodyTotal[W.bodyOff + bi] = 0u;
+        team.sync();
+    }
     BP_SUBPHASE(13);
     // cells (nativeBuildGrid, NGK:179-189) and bucket counts
     for (uint32_t i = r; i < n; i += T) {
@@ -757,7 +766,8 @@ __device__ void initial_forces(const DState& S, const DWorld& W, const Ctl& c, c
         float m = margin_bound(S, g);
         if (m < mg.v) { mg.v = m; mg.o = i; }
     }
-    team.sync();
+    // the next reduction's barrier orders these writes before any reader; the whole-GPU team saves this grid barrier
+    if (!kGridTeam<Team>) team.sync();
 }
 
 // nativeReduceSubstepInGroup, NFK:625-736
