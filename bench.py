@@ -424,8 +424,13 @@ def run_ours(args, rank, world_size, local_rank):
         _, freps = fused.step(args.per_world_steps)
         _, f1, _ = fused.counters()
         fms = float(freps["gpu_ms"][0])
-        per_world = {"value": (p1 - p0) / (pms / 1000.0), "unit": UNIT, "launches_per_step": (pl1 - pl0) // args.per_world_steps,
+        launches = (pl1 - pl0) // args.per_world_steps
+        per_world = {"value": (p1 - p0) / (pms / 1000.0), "unit": UNIT, "launches_per_step": launches,
                      "ms_per_step": pms / args.per_world_steps,
+                     "device_ms_per_launch": pms / args.per_world_steps / max(launches, 1),
+                     "note": "one launch per world, one world per block (a warp for worlds of <= 64 bubbles), "
+                             "launches back to back on one stream; device_ms_per_launch is the mean device time of a "
+                             "launch, i.e. of one world's step with one team",
                      "batched_same_steps": (f1 - f0) / (fms / 1000.0),
                      "speedup_batched_vs_per_world": ((f1 - f0) / fms) / ((p1 - p0) / pms) if pms > 0 and p1 > p0 else None,
                      "steps": args.per_world_steps}
