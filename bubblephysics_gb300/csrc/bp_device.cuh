@@ -138,6 +138,7 @@ struct DState {
     uint32_t* gpo;             // 2 x grid partial owners / counts
     uint32_t* gbuckets;        // hash grid buckets
     uint32_t* gentries;        // hash grid entries
+    float4* grecords;          // hash grid entry records (centre, radius, margin) in entry order
     unsigned int* barrier;     // grid barrier counters [arrivals, generation]
     uint32_t* errorFlag;       // bounded-wait failures
     unsigned long long* phaseCycles;  // kPhaseCount per world when built with BP_PHASE_TIMING, else null
@@ -172,6 +173,10 @@ struct QueueArgs {
 };
 
 __host__ __device__ inline uint32_t round4_words(uint32_t v) { return (v + 3u) & ~3u; }
+// Words of a team's hash grid in shared memory: B bucket ends and the entries of its largest world (padded to 16
+// bytes), then one 16-byte record per entry (centre, radius, margin of the entry's bubble) that the candidate scan reads
+// instead of the bubble's own arrays.
+__host__ __device__ inline uint32_t grid_words(uint32_t B, uint32_t maxN) { return round4_words(B + maxN) + 4u * maxN; }
 
 // Per-team copies of the world's table entry and state pointers, kept in SHARED memory for the whole step: S is the
 // state a team reads and writes (its hot arrays redirected into the shared-memory workspace when the world is staged),
@@ -193,7 +198,7 @@ __host__ __device__ inline uint32_t group_scratch_words(uint32_t width) {
     return kTeamStateWords + (width > 32u ? kGroupScratchWords : 0u);
 }
 __host__ __device__ inline uint32_t group_slice_words(const QueueArgs& q) {
-    return group_scratch_words(q.groupWidth) + round4_words(q.warpB + q.warpMaxN) + q.warpWsWords;
+    return group_scratch_words(q.groupWidth) + grid_words(q.warpB, q.warpMaxN) + q.warpWsWords;
 }
 
 constexpr float kPiF = 3.14159265358979323846f;
@@ -207,10 +212,10 @@ __host__ __device__ inline uint32_t contour_samples(float r, float maxEdge, uint
     return count < stride ? count : stride;
 }
 
-// Bytes of a world's shared-memory workspace: per bubble 104 B of hot state (88 B of state and 16 B of grid cell), per
-// segment and body a 32 B box, per body a 16 B pose; the 16 parts are each padded to 16 bytes.
+// Bytes of a world's shared-memory workspace: per bubble 88 B of hot state, per segment and body a 32 B box, per body
+// a 16 B pose; the 15 parts are each padded to 16 bytes.
 __host__ __device__ inline uint32_t workspace_bytes(uint32_t n, uint32_t s, uint32_t nb) {
-    return n * 104u + s * 32u + nb * 48u + 16u * 16u;
+    return n * 88u + s * 32u + nb * 48u + 15u * 16u;
 }
 
 // ------------------------------------------------------------------------------------------------------------------

@@ -87,7 +87,9 @@ constexpr uint32_t kLargeBubblesPerBlock = 512;  // bubbles per block of the who
 constexpr uint32_t kDefaultThreads = 256;
 constexpr uint32_t kDefaultWarpMax = 64;
 constexpr uint32_t kWarpSubsteps = 16;   // a world that took more substeps last step gets a whole block
-constexpr uint32_t kCtaWorkspaceCap = 80u * 1024u;   // shared-memory workspace of a block team (2 blocks per SM, L1 keeps ~90 KB)
+// shared-memory workspace of a block team: with the grid of 1,024-bubble worlds and its records a block takes 92 KB
+// (2 blocks per SM, L1 keeps ~60 KB)
+constexpr uint32_t kCtaWorkspaceCap = 64u * 1024u;
 constexpr uint32_t kWarpWorkspaceCap = 10u * 1024u;  // per warp of a group team
 constexpr uint32_t kDefaultGroupWidth = 32;
 constexpr uint32_t kMaxDynamicSmem = 200u * 1024u;   // per block, set on the kernels by prepare_kernels()
@@ -112,6 +114,8 @@ inline uint32_t next_pow2(uint32_t v) {
     return p;
 }
 inline uint32_t grid_buckets(uint32_t maxN) { return next_pow2(std::max<uint32_t>(2u * maxN, 32u)); }
+// Shared-memory bytes of a team's hash grid (bucket ends, entries, entry records) for worlds of up to maxN bubbles.
+inline uint32_t team_grid_bytes(uint32_t maxN) { return maxN ? 4u * grid_words(grid_buckets(maxN), maxN) : 0u; }
 inline uint32_t round4(uint32_t v) { return (v + 3u) & ~3u; }
 
 inline int cuda_status(cudaError_t e) {

@@ -131,7 +131,8 @@ __global__ void __launch_bounds__(256) noalloc_step_kernel(DState S, DWorld W, b
     }
     uint32_t* buckets = g_dynamic_smem;
     uint32_t* entries = g_dynamic_smem + B;
-    uint32_t* ws = g_dynamic_smem + round4_words(B + (n ? n : 1u));
+    float4* records = (float4*)(g_dynamic_smem + round4_words(B + (n ? n : 1u)));
+    uint32_t* ws = g_dynamic_smem + grid_words(B, n ? n : 1u);
     const uint32_t wsWords = workspace_bytes(n, W.s, 0u) / 4u + 4u;
     for (uint32_t s = 0; s < steps; ++s) {
         if (r == 0) {
@@ -141,7 +142,7 @@ __global__ void __launch_bounds__(256) noalloc_step_kernel(DState S, DWorld W, b
             ts.G.reports = reports + s;
         }
         __syncthreads();
-        world_step<CtaTeam, false>(ts.G, 0u, team, buckets, entries, B, ws, wsWords, ts);
+        world_step<CtaTeam, false>(ts.G, 0u, team, buckets, entries, records, B, ws, wsWords, ts);
         __syncthreads();
         if (S.failed[0]) {  // a failed step publishes nothing and stops the world: later steps report it
             for (uint32_t q = s + 1 + r; q < steps; q += T) {
@@ -200,7 +201,7 @@ extern "C" int bp_world_step_noalloc(const bp_world_desc* desc, bp_bubble* bubbl
     const uint32_t maxN = bubble_count ? bubble_count : 1u;
     uint32_t B = 32u;
     while (B < 2u * maxN) B <<= 1;
-    const size_t smem = ((size_t)round4_words(B + maxN) + workspace_bytes(bubble_count, segment_count, 0u) / 4u + 4u) * 4u;
+    const size_t smem = ((size_t)grid_words(B, maxN) + workspace_bytes(bubble_count, segment_count, 0u) / 4u + 4u) * 4u;
     noalloc_step_kernel<<<1, 256, smem, (cudaStream_t)stream>>>(S, W, bubbles, segments, steps, reports, B);
     return cudaGetLastError() == cudaSuccess ? BP_OK : BP_E_CUDA;
 }

@@ -10,7 +10,7 @@ __global__ void __launch_bounds__(512) large_step_kernel(DState S, uint32_t wi, 
     __shared__ BlockScratch sh;
     __shared__ TeamState ts;
     GridTeam team{&sh, S.barrier, S.errorFlag, S.gpv, S.gpo, nullptr, 0u, false};
-    world_step<GridTeam, true>(S, wi, team, S.gbuckets, S.gentries, B, nullptr, 0u, ts);
+    world_step<GridTeam, true>(S, wi, team, S.gbuckets, S.gentries, S.grecords, B, nullptr, 0u, ts);
 }
 
 // Contact law known-answer kernel: mode 0 eps(q), 1 wall law, 2 pair law; 8 floats in / out per case.
@@ -100,7 +100,7 @@ cudaError_t launch_schedule(const DState& S, const uint32_t* candidates, uint32_
 }
 
 size_t persistent_smem(const QueueArgs& q, uint32_t threads) {
-    size_t cta = (size_t)(q.nCta ? round4_words(q.ctaB + q.ctaMaxN) + q.ctaWsWords : 0);
+    size_t cta = (size_t)(q.nCta ? grid_words(q.ctaB, q.ctaMaxN) + q.ctaWsWords : 0);
     size_t warp = (size_t)(q.nWarp ? (threads / (q.groupWidth ? q.groupWidth : 32u)) * group_slice_words(q) : 0);
     return (cta > warp ? cta : warp) * sizeof(uint32_t);
 }
@@ -173,6 +173,9 @@ int large_max_blocks(int threads) {
 }
 
 cudaError_t launch_large(const DState& S, uint32_t wi, uint32_t B, int blocks, int threads, cudaStream_t stream) {
+    // the grid barrier counts arrivals from zero in every launch (the block count differs between worlds)
+    cudaError_t err = cudaMemsetAsync(S.barrier, 0, sizeof(unsigned int), stream);
+    if (err != cudaSuccess) return err;
     DState copy = S;
     void* args[] = {&copy, &wi, &B};
     return cudaLaunchCooperativeKernel((const void*)large_step_kernel, dim3(blocks), dim3(threads), args, 0, stream);

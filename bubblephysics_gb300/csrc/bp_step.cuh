@@ -446,8 +446,8 @@ __device__ __forceinline__ void lower_pair(const DState& S, const DWorld& W, uin
 // scan collects the lower pairs j < i into the adjacency row (their count goes to deg until finish_adjacency). With
 // the tree, the rigid traversal also registers i in the rows of the bodies that accept it.
 template <bool kTree>
-__device__ void emit_row(const DState& S, const DWorld& W, const uint32_t* buckets, const uint32_t* entries, uint32_t B,
-                         uint32_t i, uint32_t& overflow, uint32_t& maxPer) {
+__device__ void emit_row(const DState& S, const DWorld& W, const uint32_t* buckets, const uint32_t* entries,
+                         const float4* records, uint32_t B, uint32_t i, uint32_t& overflow, uint32_t& maxPer) {
     const uint32_t g = W.boff + i, k = W.k;
     uint32_t* row = S.candRow + W.rowOff + (uint64_t)i * k;
     uint32_t* adjRow = S.adj + W.rowOff + (uint64_t)i * k;
@@ -480,17 +480,40 @@ __device__ void emit_row(const DState& S, const DWorld& W, const uint32_t* bucke
     }
     longlong2 c = S.cell[g];
     uint32_t count = 0, total = 0;
+    // The pair rule (pair_accepts, and lower_pair for j < i) with its box test first, on the entry's record: reach and
+    // distances are computed in the same order of operations as the rule, so every decision is the rule's. The entry's
+    // own cell is read only for pairs within reach (another cell may share the bucket).
+    const float2 pi = S.pos[g];
+    const float ri = S.phys[g].x, mi = S.margin[g], tol = W.sepTol;
+    const uint2 fi = S.filter[g];
     for (int dx = -1; dx <= 1; ++dx)
-        for (int dy = -1; dy <= 1; ++dy)
-            for_each_in_cell(S.cell, W, buckets, entries, B, c.x + dx, c.y + dy, [&](uint32_t j) {
+        for (int dy = -1; dy <= 1; ++dy) {
+            const long long tx = c.x + dx, ty = c.y + dy;
+            const uint32_t h = grid_hash(tx, ty, B);
+            const uint32_t begin = h == 0u ? 0u : buckets[h - 1], end = buckets[h];
+            for (uint32_t e = begin; e < end; ++e) {
+                const float4 q = records[e];
+                const uint32_t j = entries[e];
+                if (j == i) continue;
+                const float reach = j < i ? q.z + ri + q.w + mi + tol : ri + q.z + mi + q.w + tol;
+                if (!(fabsf(pi.x - q.x) <= reach && fabsf(pi.y - q.y) <= reach)) continue;
+                const uint32_t gj = W.boff + j;
+                const longlong2 cj = S.cell[gj];
+                if (cj.x != tx || cj.y != ty) continue;
                 if (j < i) {
-                    lower_pair(S, W, i, j, adjRow, lowerKept, lowerTotal);
-                    return;
+                    if (!(S.flags[gj] & kStartFinite)) continue;
+                    if (!filter_accepts(S.filter[gj], fi)) continue;
+                    if (W.njEnt && joint_excluded(S, W, j, S.id[g])) continue;
+                    ++lowerTotal;
+                    insert_sorted(adjRow, lowerKept, k, j);
+                } else {
+                    if (!filter_accepts(fi, S.filter[gj])) continue;
+                    if (W.njEnt && joint_excluded(S, W, i, S.id[gj])) continue;
+                    ++total;
+                    insert_sorted(row, count, k, j);
                 }
-                if (j == i || !pair_accepts(S, W, i, j)) return;
-                ++total;
-                insert_sorted(row, count, k, j);
-            });
+            }
+        }
     S.deg[g] = lowerTotal;
     const uint32_t pairs = count;
     uint32_t segTotal = 0;
@@ -654,7 +677,7 @@ __device__ void build_adjacency(const DState& S, const DWorld& W, const uint32_t
 // ------------------------------------------------------------------------------------------------------------------
 template <class Team, bool kTree>
 __device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, const Team& team, uint32_t* buckets,
-                            uint32_t* entries, uint32_t B, uint32_t& buildOverflow, uint32_t& maxPerAll, uint32_t subWorld) {
+                            uint32_t* entries, float4* records, uint32_t B, uint32_t& buildOverflow, uint32_t& maxPerAll, uint32_t subWorld) {
     const uint32_t n = W.n, T = team.size(), r = team.rank();
 #ifdef BP_PHASE_TIMING
     long long subMark = clock64();
@@ -716,11 +739,13 @@ __device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, cons
         longlong2 cc = S.cell[g];
         uint32_t slot = atomicAdd(buckets + grid_hash(cc.x, cc.y, B), 1u);
         entries[slot] = i;
+        const float2 p = S.pos[g];
+        records[slot] = make_float4(p.x, p.y, S.phys[g].x, S.margin[g]);
     }
     team.sync();
     BP_SUBPHASE(14);
     uint32_t overflow = 0, maxPer = 0;
-    for (uint32_t i = r; i < n; i += T) emit_row<kTree>(S, W, buckets, entries, B, i, overflow, maxPer);
+    for (uint32_t i = r; i < n; i += T) emit_row<kTree>(S, W, buckets, entries, records, B, i, overflow, maxPer);
     team.sync();
     BP_SUBPHASE(15);
     {
@@ -1225,7 +1250,6 @@ __device__ bool stage_world(const DState& G, DState& S, const DWorld& W, const T
     uint32_t* flags = carve<uint32_t>(p, n);
     uint32_t* deg = carve<uint32_t>(p, n);
     uint32_t* pairTotal = carve<uint32_t>(p, n);
-    longlong2* cell = carve<longlong2>(p, n);
     RigidBox* segBox = carve<RigidBox>(p, W.s);
     RigidBox* bodyBox = carve<RigidBox>(p, W.nb);
     float4* bpose = carve<float4>(p, W.nb);
@@ -1250,7 +1274,6 @@ __device__ bool stage_world(const DState& G, DState& S, const DWorld& W, const T
         S.flags = flags - W.boff;
         S.deg = deg - W.boff;
         S.pairTotal = pairTotal - W.boff;
-        S.cell = cell - W.boff;
         S.segBox = segBox - W.soff;
         S.bodyBox = bodyBox - W.bodyOff;
         S.bpose = bpose - W.bodyOff;
@@ -1286,7 +1309,8 @@ template <class Team> __device__ void build_boxes(const DState& S, const DWorld&
 // ------------------------------------------------------------------------------------------------------------------
 // `ts` is the team's TeamState in shared memory (ts.S and ts.W are written here; G may be ts.G).
 template <class Team, bool kTreeCapable>
-__device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint32_t* buckets, uint32_t* entries, uint32_t B,
+__device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint32_t* buckets, uint32_t* entries,
+                           float4* records, uint32_t B,
                            uint32_t* ws, uint32_t wsWords, TeamState& ts) {
     if (team.shared_leader()) {
         ts.W = G.worlds[wi];
@@ -1353,8 +1377,8 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
     float* history = S.history + (uint64_t)wi * kFrameLimit;
     uint32_t buildOverflow = 0, overflowMax = 0, maxPer = 0, rebuilds = 0;
     BP_PHASE(0);
-    float cw = useTree ? broadphase<Team, true>(S, W, c, team, buckets, entries, B, buildOverflow, maxPer, wi)
-                       : broadphase<Team, false>(S, W, c, team, buckets, entries, B, buildOverflow, maxPer, wi);
+    float cw = useTree ? broadphase<Team, true>(S, W, c, team, buckets, entries, records, B, buildOverflow, maxPer, wi)
+                       : broadphase<Team, false>(S, W, c, team, buckets, entries, records, B, buildOverflow, maxPer, wi);
     BP_PHASE(1);
     ValOwner w2, mg;
     initial_forces(S, W, c, team, w2, mg);
@@ -1372,8 +1396,8 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
             c.cZ = 0u;
             overflowMax = max(overflowMax, buildOverflow);
             ++rebuilds;
-            cw = useTree ? broadphase<Team, true>(S, W, c, team, buckets, entries, B, buildOverflow, maxPer, wi)
-                         : broadphase<Team, false>(S, W, c, team, buckets, entries, B, buildOverflow, maxPer, wi);
+            cw = useTree ? broadphase<Team, true>(S, W, c, team, buckets, entries, records, B, buildOverflow, maxPer, wi)
+                         : broadphase<Team, false>(S, W, c, team, buckets, entries, records, B, buildOverflow, maxPer, wi);
             initial_forces(S, W, c, team, w2, mg);
             BP_PHASE(1);
             continue;
@@ -1574,6 +1598,11 @@ extern __shared__ __align__(16) uint32_t g_dynamic_smem[];
 
 static_assert(sizeof(BlockScratch) <= 4u * kGroupScratchWords, "a group's reduction scratch fits its slice");
 
+// Entry records of a CTA world's grid: after its bucket ends and entries (grid_words).
+__device__ __forceinline__ float4* cta_records(const QueueArgs& q) {
+    return (float4*)(g_dynamic_smem + round4_words(q.ctaB + q.ctaMaxN));
+}
+
 // Persistent step kernel: blocks pull worlds from two queues. CTA-team worlds (largest first) are stepped by a whole
 // block; then the block splits into groups of q.groupWidth threads (one warp or more), and every group pulls worlds of
 // the group queue on its own, so a block keeps blockDim / groupWidth worlds in flight. Dynamic shared memory holds the
@@ -1590,14 +1619,15 @@ __device__ __forceinline__ void group_queue(const QueueArgs& q, uint32_t nGroup,
     GroupTeam team{scratch > kTeamStateWords ? (BlockScratch*)(mine + kTeamStateWords) : &blockSh,
                    GroupShape{group * width, width, 1u + group}};
     uint32_t* grid = mine + scratch;
-    uint32_t* ws = q.warpWsWords ? grid + round4_words(q.warpB + q.warpMaxN) : nullptr;
+    float4* records = (float4*)(grid + round4_words(q.warpB + q.warpMaxN));
+    uint32_t* ws = q.warpWsWords ? grid + grid_words(q.warpB, q.warpMaxN) : nullptr;
     for (;;) {
         if (team.leader()) next[group] = atomicAdd(q.queue + 1, 1u);
         team.sync();
         const uint32_t slot = next[group];
         team.sync();
         if (slot >= nGroup) break;
-        step(q.warpList[slot], team, grid, grid + q.warpB, ws, ts);
+        step(q.warpList[slot], team, grid, grid + q.warpB, records, ws, ts);
         team.sync();
     }
 }
@@ -1616,13 +1646,14 @@ __global__ void __launch_bounds__(kThreads, 2) persistent_step_kernel(DState S, 
         const uint32_t slot = next[0];
         __syncthreads();
         if (slot >= nCta) break;
-        world_step<CtaTeam, kTree>(S, q.ctaList[slot], cta, g_dynamic_smem, g_dynamic_smem + q.ctaB, q.ctaB,
-                   q.ctaWsWords ? g_dynamic_smem + round4_words(q.ctaB + q.ctaMaxN) : nullptr, q.ctaWsWords, ctaState);
+        world_step<CtaTeam, kTree>(S, q.ctaList[slot], cta, g_dynamic_smem, g_dynamic_smem + q.ctaB, cta_records(q), q.ctaB,
+                                   q.ctaWsWords ? g_dynamic_smem + grid_words(q.ctaB, q.ctaMaxN) : nullptr, q.ctaWsWords,
+                                   ctaState);
         __syncthreads();
     }
     group_queue(q, nGroup, sh, next, [&](uint32_t wi, const GroupTeam& team, uint32_t* buckets, uint32_t* entries,
-                                         uint32_t* ws, TeamState& ts) {
-        world_step<GroupTeam, kTree>(S, wi, team, buckets, entries, q.warpB, ws, q.warpWsWords, ts);
+                                         float4* records, uint32_t* ws, TeamState& ts) {
+        world_step<GroupTeam, kTree>(S, wi, team, buckets, entries, records, q.warpB, ws, q.warpWsWords, ts);
     });
 }
 
@@ -1647,19 +1678,19 @@ __global__ void __launch_bounds__(kThreads, 2) served_step_kernel(const DState* 
             ctaState.G.reports = reports + e;
         }
         __syncthreads();
-        world_step<CtaTeam, kTree>(ctaState.G, 0u, cta, g_dynamic_smem, g_dynamic_smem + q.ctaB, q.ctaB,
-                                   q.ctaWsWords ? g_dynamic_smem + round4_words(q.ctaB + q.ctaMaxN) : nullptr, q.ctaWsWords,
+        world_step<CtaTeam, kTree>(ctaState.G, 0u, cta, g_dynamic_smem, g_dynamic_smem + q.ctaB, cta_records(q), q.ctaB,
+                                   q.ctaWsWords ? g_dynamic_smem + grid_words(q.ctaB, q.ctaMaxN) : nullptr, q.ctaWsWords,
                                    ctaState);
         __syncthreads();
     }
     group_queue(q, q.nWarp, sh, next, [&](uint32_t e, const GroupTeam& team, uint32_t* buckets, uint32_t* entries,
-                                          uint32_t* ws, TeamState& ts) {
+                                          float4* records, uint32_t* ws, TeamState& ts) {
         if (team.leader()) {
             ts.G = sets[entrySlot[e]];
             ts.G.reports = reports + e;
         }
         team.sync();
-        world_step<GroupTeam, kTree>(ts.G, 0u, team, buckets, entries, q.warpB, ws, q.warpWsWords, ts);
+        world_step<GroupTeam, kTree>(ts.G, 0u, team, buckets, entries, records, q.warpB, ws, q.warpWsWords, ts);
     });
 }
 

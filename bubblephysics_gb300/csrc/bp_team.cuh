@@ -8,7 +8,7 @@
 
 namespace bp {
 
-constexpr unsigned long long kBarrierSpinLimit = 20000000ull;  // about 1-4 s of __nanosleep(64) polls
+constexpr unsigned long long kBarrierSpinLimit = 20000000ull;  // about 1-4 s of __nanosleep(32) polls
 
 struct ValOwner {
     float v;
@@ -295,22 +295,17 @@ struct GroupTeam {
 };
 
 // GPU-scope memory operations of the grid barrier.
-__device__ __forceinline__ unsigned int ld_acquire(const unsigned int* p) {
+__device__ __forceinline__ unsigned int ld_relaxed(const unsigned int* p) {
     unsigned int v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ unsigned int atom_add_acq_rel(unsigned int* p, unsigned int v) {
+__device__ __forceinline__ unsigned int atom_add_release(unsigned int* p, unsigned int v) {
     unsigned int old;
-    asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    asm volatile("atom.add.release.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
     return old;
 }
-__device__ __forceinline__ void red_add_release(unsigned int* p, unsigned int v) {
-    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ void st_relaxed(unsigned int* p, unsigned int v) {
-    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 
 // ----------------------------------------------------------------------------------------------------------------
 // Grid team: every block of a cooperative launch works on one world. Partials go through global memory with
@@ -320,7 +315,7 @@ __device__ __forceinline__ void st_relaxed(unsigned int* p, unsigned int v) {
 // ----------------------------------------------------------------------------------------------------------------
 struct GridTeam {
     BlockScratch* sh;
-    unsigned int* bar;       // [0] arrivals, [1] generation
+    unsigned int* bar;       // [0] arrivals since the launch (zeroed before every launch)
     uint32_t* err;
     float* pv;               // 2 parities x 4 regions x gridDim.x partial values
     uint32_t* po;            // 2 parities x 4 regions x gridDim.x partial owners / counts
@@ -336,27 +331,23 @@ struct GridTeam {
     __device__ void shared_sync() const { __syncthreads(); }
     __device__ bool ok() const { return !failed; }
 
-    // Bounded grid barrier (generation counter). Returns false when any block gave up waiting. Arrival is an
-    // acquire-release add (the block's writes, ordered before it by the block barrier, are released; the other blocks'
-    // are acquired by the last arriver), the last arriver releases the next generation, and the waiters acquire it.
+    // Bounded grid barrier on a counter that only grows within a launch: the barrier a block enters with the counter
+    // at `old` ends when the counter reaches the next multiple of the grid size. Arrival is a release add (the block's
+    // writes, ordered before it by the block barrier, are released); the waiters poll relaxed and then acquire with one
+    // fence. Returns false when any block gave up waiting (the error word is polled every 64 spins).
     __device__ bool sync() const {
         __syncthreads();
         if (threadIdx.x == 0) {
-            unsigned int* gen = bar + 1;
-            const unsigned int g = ld_acquire(gen);
-            const unsigned int arrived = atom_add_acq_rel(bar, 1u);
-            if (arrived == gridDim.x - 1) {
-                st_relaxed(bar, 0u);
-                red_add_release(gen, 1u);
-            } else {
-                unsigned long long spins = 0;
-                while (ld_acquire(gen) == g) {
-                    if (ld_acquire(err) != 0u) break;
-                    if (++spins > kBarrierSpinLimit) { atomicOr(err, 1u); break; }
-                    __nanosleep(32);
-                }
+            const unsigned int old = atom_add_release(bar, 1u);
+            const unsigned int target = (old / gridDim.x + 1u) * gridDim.x;
+            unsigned long long spins = 0;
+            while ((int)(ld_relaxed(bar) - target) < 0) {
+                if ((++spins & 63u) == 0u && ld_relaxed(err) != 0u) break;
+                if (spins > kBarrierSpinLimit) { atomicOr(err, 1u); break; }
+                __nanosleep(32);
             }
-            sh->bcastU[7] = ld_acquire(err);
+            fence_acq_rel_gpu();
+            sh->bcastU[7] = ld_relaxed(err);
         }
         __syncthreads();
         failed = sh->bcastU[7] != 0u;
