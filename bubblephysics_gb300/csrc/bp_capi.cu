@@ -88,7 +88,7 @@ int validate(const bp_world_desc& d, const bp_world_input& in) {
 
 bool group_layout(uint32_t threads, uint32_t groupWidth, uint32_t maxN, uint32_t* wsCap) {
     const uint32_t groups = std::max(threads / std::max(groupWidth, 32u), 1u);
-    const uint32_t gridBytes = team_grid_bytes(maxN);
+    const uint32_t gridBytes = team_grid_bytes(maxN, std::max(groupWidth, 32u));
     const uint32_t fixed = 4u * group_scratch_words(groupWidth) + gridBytes;
     const uint32_t perGroup = kMaxDynamicSmem / groups;
     if (fixed + 16u > perGroup) return false;
@@ -118,7 +118,7 @@ cudaError_t schedule(WorldSet& ws, uint32_t threads, uint32_t warpMax, uint32_t 
         (W.n <= warpMax ? ws.warpWorlds : ws.ctaWorlds).push_back(w);
     }
     // workspace caps that keep one block within the dynamic shared memory limit
-    const uint32_t ctaGridBytes = team_grid_bytes(maxN);
+    const uint32_t ctaGridBytes = team_grid_bytes(maxN, threads);
     const uint32_t ctaCap = std::min(kCtaWorkspaceCap, kMaxDynamicSmem - std::min(kMaxDynamicSmem, ctaGridBytes));
     uint32_t warpCap = 0;
     if (maxWarpN && !group_layout(threads, groupWidth, maxWarpN, &warpCap)) return cudaErrorInvalidValue;
@@ -409,7 +409,9 @@ int build_set(WorldSet& ws, bp_context* ctx, uint32_t count, const bp_world_desc
     S.gpo = ws.alloc<uint32_t>(8ull * std::max(ws.largeBlocks, 1), err);
     S.gbuckets = ws.alloc<uint32_t>(ws.largeWorlds.empty() ? 1 : ws.largeB, err);
     S.gentries = ws.alloc<uint32_t>(std::max<uint32_t>(ws.largeMaxN, 1u), err);
-    S.grecords = ws.alloc<float4>(std::max<uint32_t>(ws.largeMaxN, 1u), err);
+    // entry records of the grid, and one slot per thread of the launch (the row-term passes)
+    S.grecords = ws.alloc<float4>(std::max<uint32_t>(std::max<uint32_t>(ws.largeMaxN, 1u),
+                                                     (uint32_t)std::max(ws.largeBlocks, 1) * kLargeThreads), err);
     S.barrier = ws.alloc<unsigned int>(2, err);
     S.errorFlag = ws.alloc<uint32_t>(1, err);
 #ifdef BP_PHASE_TIMING

@@ -174,9 +174,12 @@ struct QueueArgs {
 
 __host__ __device__ inline uint32_t round4_words(uint32_t v) { return (v + 3u) & ~3u; }
 // Words of a team's hash grid in shared memory: B bucket ends and the entries of its largest world (padded to 16
-// bytes), then one 16-byte record per entry (centre, radius, margin of the entry's bubble) that the candidate scan reads
-// instead of the bubble's own arrays.
-__host__ __device__ inline uint32_t grid_words(uint32_t B, uint32_t maxN) { return round4_words(B + maxN) + 4u * maxN; }
+// bytes), then 16-byte records: one per entry (centre, radius, margin of the entry's bubble) that the candidate scan
+// reads instead of the bubble's own arrays, and at least one per thread of the team (`width` threads), whose slots the
+// row-term passes use between grid builds.
+__host__ __device__ inline uint32_t grid_words(uint32_t B, uint32_t maxN, uint32_t width) {
+    return round4_words(B + maxN) + 4u * (maxN > width ? maxN : width);
+}
 
 // Per-team copies of the world's table entry and state pointers, kept in SHARED memory for the whole step: S is the
 // state a team reads and writes (its hot arrays redirected into the shared-memory workspace when the world is staged),
@@ -198,7 +201,8 @@ __host__ __device__ inline uint32_t group_scratch_words(uint32_t width) {
     return kTeamStateWords + (width > 32u ? kGroupScratchWords : 0u);
 }
 __host__ __device__ inline uint32_t group_slice_words(const QueueArgs& q) {
-    return group_scratch_words(q.groupWidth) + grid_words(q.warpB, q.warpMaxN) + q.warpWsWords;
+    return group_scratch_words(q.groupWidth) + grid_words(q.warpB, q.warpMaxN, q.groupWidth > 32u ? q.groupWidth : 32u) +
+           q.warpWsWords;
 }
 
 constexpr float kPiF = 3.14159265358979323846f;

@@ -114,8 +114,11 @@ inline uint32_t next_pow2(uint32_t v) {
     return p;
 }
 inline uint32_t grid_buckets(uint32_t maxN) { return next_pow2(std::max<uint32_t>(2u * maxN, 32u)); }
-// Shared-memory bytes of a team's hash grid (bucket ends, entries, entry records) for worlds of up to maxN bubbles.
-inline uint32_t team_grid_bytes(uint32_t maxN) { return maxN ? 4u * grid_words(grid_buckets(maxN), maxN) : 0u; }
+// Shared-memory bytes of the hash grid (bucket ends, entries, entry records) of a team of `width` threads for worlds of
+// up to maxN bubbles.
+inline uint32_t team_grid_bytes(uint32_t maxN, uint32_t width) {
+    return maxN ? 4u * grid_words(grid_buckets(maxN), maxN, width) : 0u;
+}
 inline uint32_t round4(uint32_t v) { return (v + 3u) & ~3u; }
 
 inline int cuda_status(cudaError_t e) {

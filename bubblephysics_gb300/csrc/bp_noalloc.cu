@@ -24,6 +24,7 @@ constexpr uint32_t kNaN = BP_NOALLOC_MAX_BUBBLES;
 constexpr uint32_t kNaS = BP_NOALLOC_MAX_SEGMENTS;
 constexpr uint32_t kNaK = BP_NOALLOC_MAX_CANDIDATE_LIMIT;
 constexpr uint32_t kNaContacts = kNaN * BP_NOALLOC_CONTACTS_PER_BUBBLE + 64u;
+constexpr uint32_t kNoAllocThreads = 256;  // one block steps the world
 
 // Carves the scratch layout (all offsets 256-byte aligned) from `base`; with base == 0 it returns the size.
 struct NoAllocLayout {
@@ -81,7 +82,7 @@ static_assert(noalloc_layout_bytes() <= noalloc_bytes(), "the scratch layout mus
 static __device__ __align__(256) unsigned char g_noalloc_scratch[noalloc_bytes()];
 
 // Unpacks the caller's records into the scratch state, steps `steps` times, packs the bubbles back (in place).
-__global__ void __launch_bounds__(256) noalloc_step_kernel(DState S, DWorld W, bp_bubble* bubbles, const bp_segment* segments,
+__global__ void __launch_bounds__(kNoAllocThreads) noalloc_step_kernel(DState S, DWorld W, bp_bubble* bubbles, const bp_segment* segments,
                                                            uint32_t steps, bp_step_report* reports, uint32_t B) {
     __shared__ BlockScratch sh;
     __shared__ TeamState ts;
@@ -132,7 +133,7 @@ __global__ void __launch_bounds__(256) noalloc_step_kernel(DState S, DWorld W, b
     uint32_t* buckets = g_dynamic_smem;
     uint32_t* entries = g_dynamic_smem + B;
     float4* records = (float4*)(g_dynamic_smem + round4_words(B + (n ? n : 1u)));
-    uint32_t* ws = g_dynamic_smem + grid_words(B, n ? n : 1u);
+    uint32_t* ws = g_dynamic_smem + grid_words(B, n ? n : 1u, blockDim.x);
     const uint32_t wsWords = workspace_bytes(n, W.s, 0u) / 4u + 4u;
     for (uint32_t s = 0; s < steps; ++s) {
         if (r == 0) {
@@ -201,7 +202,7 @@ extern "C" int bp_world_step_noalloc(const bp_world_desc* desc, bp_bubble* bubbl
     const uint32_t maxN = bubble_count ? bubble_count : 1u;
     uint32_t B = 32u;
     while (B < 2u * maxN) B <<= 1;
-    const size_t smem = ((size_t)grid_words(B, maxN) + workspace_bytes(bubble_count, segment_count, 0u) / 4u + 4u) * 4u;
-    noalloc_step_kernel<<<1, 256, smem, (cudaStream_t)stream>>>(S, W, bubbles, segments, steps, reports, B);
+    const size_t smem = ((size_t)grid_words(B, maxN, kNoAllocThreads) + workspace_bytes(bubble_count, segment_count, 0u) / 4u + 4u) * 4u;
+    noalloc_step_kernel<<<1, kNoAllocThreads, smem, (cudaStream_t)stream>>>(S, W, bubbles, segments, steps, reports, B);
     return cudaGetLastError() == cudaSuccess ? BP_OK : BP_E_CUDA;
 }

@@ -292,7 +292,7 @@ int launch(bp_server* s, Flight& f, const std::vector<uint32_t>& entries) {
     }
     const uint32_t threads = perWorld && nCta == 0 ? 32u : s->cfg.threads_per_world;
     const uint32_t groupWidth = std::min(s->cfg.group_width, threads);
-    const uint32_t ctaGridBytes = team_grid_bytes(maxCta);
+    const uint32_t ctaGridBytes = team_grid_bytes(maxCta, threads);
     const uint32_t ctaCap = std::min(kCtaWorkspaceCap, kMaxDynamicSmem - std::min(kMaxDynamicSmem, ctaGridBytes));
     uint32_t warpCap = 0;
     if (maxWarp && !group_layout(threads, groupWidth, maxWarp, &warpCap)) return BP_E_INVALID;

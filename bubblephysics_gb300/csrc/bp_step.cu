@@ -100,7 +100,7 @@ cudaError_t launch_schedule(const DState& S, const uint32_t* candidates, uint32_
 }
 
 size_t persistent_smem(const QueueArgs& q, uint32_t threads) {
-    size_t cta = (size_t)(q.nCta ? grid_words(q.ctaB, q.ctaMaxN) + q.ctaWsWords : 0);
+    size_t cta = (size_t)(q.nCta ? grid_words(q.ctaB, q.ctaMaxN, threads) + q.ctaWsWords : 0);
     size_t warp = (size_t)(q.nWarp ? (threads / (q.groupWidth ? q.groupWidth : 32u)) * group_slice_words(q) : 0);
     return (cta > warp ? cta : warp) * sizeof(uint32_t);
 }

@@ -178,78 +178,93 @@ __device__ __forceinline__ const uint32_t* adj_row(const DState& S, const DWorld
     return S.adj + W.rowOff + (uint64_t)i * W.k;
 }
 
-__device__ float2 contact_force(const DState& S, const DWorld& W, uint32_t i, float fraction) {
-    const uint32_t g = W.boff + i;
-    float2 total = f2(0.0f, 0.0f);
-    const float2 p = S.pos[g];
-    const float4 ph = S.phys[g];
-    const uint32_t* row = adj_row(S, W, i);
-    const uint32_t d = S.deg[g];
-    for (uint32_t e = 0; e < d; ++e) {
-        uint32_t entry = row[e], kind = entry >> kKindShift, j = entry & kIndexMask;
-        if (kind == 0u) {
-            uint32_t low = min(i, j), high = max(i, j);
-            uint32_t gl = W.boff + low, gh = W.boff + high;
-            float2 delta = sub(S.pos[gh], S.pos[gl]);
-            float dist = len2(delta);
-            float2 normal = dist > 0.0f ? dvd(delta, dist) : f2(1.0f, 0.0f);
-            float4 pl = S.phys[gl], phh = S.phys[gh];
-            Law law = pair_law(pl.z, pl.x, phh.z, phh.x, dist);
-            total = add(total, mul(normal, i == low ? -law.force : law.force));
-        } else if (kind == 1u) {
-            float2 normal;
-            float dist;
-            if (!wall_region(S.seg[W.soff + j], p, normal, dist) || !(dist < ph.x)) continue;
-            total = add(total, mul(normal, wall_law(ph.z, ph.x, dist).force));
-        } else {
-            Obstacle o = body_obstacle(S.bverts, S.btris, S.body[W.bodyOff + j], cached_pose(S, W, j), p);
-            total = add(total, mul(o.normal, wall_law(ph.z, ph.x, o.distance).force));
-        }
+// One adjacency entry's share of bubble i's contact force and omega^2 (the body of the row loop of
+// nativeBubbleContactForce, NFK:216-243, and nativeBubbleOmegaSquared, NFK:510-541, which read the same law
+// evaluations): x, y = the force term, z = the omega^2 term, w = which of the two the row sum adds (bit 0 force, bit 1
+// omega^2; a wall out of its region adds neither). p, ph and im are bubble i's centre, physical record and inverse mass.
+__device__ __forceinline__ float4 contact_term(const DState& S, const DWorld& W, uint32_t i, uint32_t entry, float2 p,
+                                               float4 ph, float im) {
+    const uint32_t kind = entry >> kKindShift, j = entry & kIndexMask;
+    if (kind == 0u) {
+        uint32_t low = min(i, j), high = max(i, j);
+        uint32_t gl = W.boff + low, gh = W.boff + high;
+        float2 delta = sub(S.pos[gh], S.pos[gl]);
+        float dist = len2(delta);
+        float2 normal = dist > 0.0f ? dvd(delta, dist) : f2(1.0f, 0.0f);
+        float4 pl = S.phys[gl], phh = S.phys[gh];
+        Law law = pair_law(pl.z, pl.x, phh.z, phh.x, dist);
+        float2 v = mul(normal, i == low ? -law.force : law.force);
+        if (!(im > 0.0f)) return make_float4(v.x, v.y, 0.0f, __uint_as_float(1u));
+        return make_float4(v.x, v.y, law.stiffness * (im + sqrtf(im * inv_mass(S, W.boff + j))), __uint_as_float(3u));
     }
-    return total;
+    if (kind == 1u) {
+        float2 normal;
+        float dist;
+        if (!wall_region(S.seg[W.soff + j], p, normal, dist) || !(dist < ph.x)) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        Law wl = wall_law(ph.z, ph.x, dist);
+        float2 v = mul(normal, wl.force);
+        return make_float4(v.x, v.y, wl.stiffness * im, __uint_as_float(3u));
+    }
+    Obstacle o = body_obstacle(S.bverts, S.btris, S.body[W.bodyOff + j], cached_pose(S, W, j), p);
+    Law wl = wall_law(ph.z, ph.x, o.distance);
+    float2 v = mul(o.normal, wl.force);
+    return make_float4(v.x, v.y, wl.stiffness * im, __uint_as_float(3u));
 }
 
-// One pass over the adjacency row giving both the contact force (nativeBubbleContactForce, NFK:216-243) and omega^2
-// (nativeBubbleOmegaSquared, NFK:510-541) from the same law evaluations: positions are the same in both, so each term
-// is bit-identical to evaluating the two functions separately; the sums keep their own row order.
-__device__ float2 contact_terms(const DState& S, const DWorld& W, uint32_t i, float fraction, float im, float& omega2) {
-    const uint32_t g = W.boff + i;
+// Row entries of a warp's bubbles spread evenly over its lanes. Lane l owns a row of `deg` entries (0 without one);
+// the warp's entries are numbered row by row in lane order, and in each round every lane evaluates the next entry,
+// `term(o, e)` = entry e of lane o's row, into its slot of `slots` (one float4 per lane of this warp). Each owner then
+// hands its own entries' values to `take` in row order, so a row sum adds the same terms in the same order as a
+// sequential loop over the row. The whole warp calls this together.
+template <class Term, class Take>
+__device__ __forceinline__ void warp_rows(uint32_t deg, float4* slots, Term&& term, Take&& take) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t start = deg;  // inclusive scan, then exclusive
+#pragma unroll
+    for (uint32_t d = 1; d < 32u; d <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, start, d);
+        if (lane >= d) start += v;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, start, 31);
+    start -= deg;
+    for (uint32_t t0 = 0; t0 < total; t0 += 32u) {
+        const uint32_t f = t0 + lane;
+        uint32_t o = 0;  // the last lane whose row starts at or before entry f
+#pragma unroll
+        for (uint32_t step = 16; step; step >>= 1) {
+            const uint32_t so = __shfl_sync(0xffffffffu, start, o + step);
+            if (so <= f) o += step;
+        }
+        const uint32_t first = __shfl_sync(0xffffffffu, start, o);
+        if (f < total) slots[lane] = term(o, f - first);
+        __syncwarp();
+        const uint32_t lo = max(start, t0), hi = min(start + deg, t0 + 32u);
+        for (uint32_t x = lo; x < hi; ++x) take(slots[x - t0]);
+        __syncwarp();
+    }
+}
+
+// Contact force and omega^2 of bubble i0 + lane for every lane of the warp (`has`: the lane's bubble takes part),
+// nativeBubbleContactForce + nativeBubbleOmegaSquared with the row entries spread over the warp (warp_rows).
+__device__ __forceinline__ float2 warp_contact_terms(const DState& S, const DWorld& W, uint32_t i0, bool has, float im,
+                                                     float4* slots, float& omega2) {
+    const uint32_t i = i0 + (threadIdx.x & 31u), g = W.boff + i;
     float2 total = f2(0.0f, 0.0f);
     float w2 = 0.0f;
-    const float2 p = S.pos[g];
-    const float4 ph = S.phys[g];
-    if (im > 0.0f && W.nbands) {
+    if (has && im > 0.0f && W.nbands) {
         const bp_band* band = find_by_bubble(S.bands + W.bandOff, W.nbands, S.id[g]);
         if (band) w2 = w2 + band->stiffness * im;
     }
-    const uint32_t* row = adj_row(S, W, i);
-    const uint32_t d = S.deg[g];
-    for (uint32_t e = 0; e < d; ++e) {
-        uint32_t entry = row[e], kind = entry >> kKindShift, j = entry & kIndexMask;
-        if (kind == 0u) {
-            uint32_t low = min(i, j), high = max(i, j);
-            uint32_t gl = W.boff + low, gh = W.boff + high;
-            float2 delta = sub(S.pos[gh], S.pos[gl]);
-            float dist = len2(delta);
-            float2 normal = dist > 0.0f ? dvd(delta, dist) : f2(1.0f, 0.0f);
-            float4 pl = S.phys[gl], phh = S.phys[gh];
-            Law law = pair_law(pl.z, pl.x, phh.z, phh.x, dist);
-            total = add(total, mul(normal, i == low ? -law.force : law.force));
-            if (im > 0.0f) w2 = w2 + law.stiffness * (im + sqrtf(im * inv_mass(S, W.boff + j)));
-        } else if (kind == 1u) {
-            float2 normal;
-            float dist;
-            if (!wall_region(S.seg[W.soff + j], p, normal, dist) || !(dist < ph.x)) continue;
-            Law wl = wall_law(ph.z, ph.x, dist);
-            total = add(total, mul(normal, wl.force));
-            w2 = w2 + wl.stiffness * im;
-        } else {
-            Obstacle o = body_obstacle(S.bverts, S.btris, S.body[W.bodyOff + j], cached_pose(S, W, j), p);
-            Law wl = wall_law(ph.z, ph.x, o.distance);
-            total = add(total, mul(o.normal, wl.force));
-            w2 = w2 + wl.stiffness * im;
-        }
-    }
+    warp_rows(has ? S.deg[g] : 0u, slots,
+              [&](uint32_t o, uint32_t e) {
+                  const uint32_t io = i0 + o, go = W.boff + io;
+                  return contact_term(S, W, io, adj_row(S, W, io)[e], S.pos[go], S.phys[go], inv_mass(S, go));
+              },
+              [&](float4 c) {
+                  const uint32_t use = __float_as_uint(c.w);
+                  if (use & 1u) total = add(total, f2(c.x, c.y));
+                  if (use & 2u) w2 = w2 + c.z;
+              });
     omega2 = im > 0.0f ? w2 : 0.0f;
     return total;
 }
@@ -289,54 +304,64 @@ __device__ float omega_squared(const DState& S, const DWorld& W, uint32_t i, flo
     return total;
 }
 
-__device__ float distance_bound(const DState& S, const DWorld& W, uint32_t i, float hMax, float fraction) {
-    const uint32_t g = W.boff + i;
+// One adjacency entry's distance bound for a movable bubble at p with the given velocity, radius and |acceleration|
+// (the body of the row loop of nativeBubbleDistanceBound, NFK:545-614); +inf for an entry that sets no bound.
+__device__ __forceinline__ float distance_term(const DState& S, const DWorld& W, uint32_t entry, float2 p, float2 velocity,
+                                               float radius, float accSelf, float hMax) {
     const float inf = __int_as_float(0x7f800000);
-    if (!(inv_mass(S, g) > 0.0f)) return inf;
-    const float2 p = S.pos[g], velocity = S.vel[g];
-    const float radius = S.phys[g].x;
-    const float accSelf = len2(S.acc[g]);
-    float best = inf;
-    const uint32_t* row = adj_row(S, W, i);
-    const uint32_t d = S.deg[g];
-    for (uint32_t e = 0; e < d; ++e) {
-        uint32_t entry = row[e], kind = entry >> kKindShift, j = entry & kIndexMask;
-        float dist, approach, accSum, reach, bodySpeed = 0.0f;
-        if (kind == 0u) {
-            uint32_t gj = W.boff + j;
-            float2 delta = sub(S.pos[gj], p);
-            dist = len2(delta);
-            float2 normal = dist > 0.0f ? dvd(delta, dist) : f2(1.0f, 0.0f);
-            approach = dot2(sub(velocity, eff_vel(S, gj)), normal);
-            accSum = accSelf + len2(S.acc[gj]);
-            reach = radius + S.phys[gj].x;
-        } else if (kind == 1u) {
-            float2 normal;
-            if (!wall_region(S.seg[W.soff + j], p, normal, dist)) continue;
-            approach = -dot2(velocity, normal);
-            accSum = accSelf;
-            reach = radius;
-        } else {
-            Obstacle o = body_obstacle(S.bverts, S.btris, S.body[W.bodyOff + j], cached_pose(S, W, j), p);
-            dist = o.distance;
-            approach = -dot2(velocity, o.normal);
-            bodySpeed = o.speedBound;
-            accSum = accSelf;
-            reach = radius;
-        }
-        bool active = dist < reach;
-        float dd = fmaxf(dist, reach * 1e-6f);
-        float speed;
-        if (active) speed = fabsf(approach) + bodySpeed;
-        else {
-            if (approach + bodySpeed + accSum * hMax * 0.5f <= 0.0f) continue;
-            speed = approach + bodySpeed;
-        }
-        float sq = sqrtf(speed * speed + accSum * dd * 0.5f);
-        float denominator = sq + speed;
-        if (!(denominator > 0.0f)) continue;
-        best = fminf(best, dd / (2.0f * denominator));
+    const uint32_t kind = entry >> kKindShift, j = entry & kIndexMask;
+    float dist, approach, accSum, reach, bodySpeed = 0.0f;
+    if (kind == 0u) {
+        uint32_t gj = W.boff + j;
+        float2 delta = sub(S.pos[gj], p);
+        dist = len2(delta);
+        float2 normal = dist > 0.0f ? dvd(delta, dist) : f2(1.0f, 0.0f);
+        approach = dot2(sub(velocity, eff_vel(S, gj)), normal);
+        accSum = accSelf + len2(S.acc[gj]);
+        reach = radius + S.phys[gj].x;
+    } else if (kind == 1u) {
+        float2 normal;
+        if (!wall_region(S.seg[W.soff + j], p, normal, dist)) return inf;
+        approach = -dot2(velocity, normal);
+        accSum = accSelf;
+        reach = radius;
+    } else {
+        Obstacle o = body_obstacle(S.bverts, S.btris, S.body[W.bodyOff + j], cached_pose(S, W, j), p);
+        dist = o.distance;
+        approach = -dot2(velocity, o.normal);
+        bodySpeed = o.speedBound;
+        accSum = accSelf;
+        reach = radius;
     }
+    bool active = dist < reach;
+    float dd = fmaxf(dist, reach * 1e-6f);
+    float speed;
+    if (active) speed = fabsf(approach) + bodySpeed;
+    else {
+        if (approach + bodySpeed + accSum * hMax * 0.5f <= 0.0f) return inf;
+        speed = approach + bodySpeed;
+    }
+    float sq = sqrtf(speed * speed + accSum * dd * 0.5f);
+    float denominator = sq + speed;
+    if (!(denominator > 0.0f)) return inf;
+    return dd / (2.0f * denominator);
+}
+
+// Distance bound of bubble i0 + lane for every lane of the warp (`has`: the lane's bubble takes part; an immovable
+// bubble sets none): the minimum over its row, entries spread over the warp (warp_rows).
+__device__ __forceinline__ float warp_distance_bound(const DState& S, const DWorld& W, uint32_t i0, bool has, float hMax,
+                                                     float4* slots) {
+    const uint32_t g = W.boff + i0 + (threadIdx.x & 31u);
+    float best = __int_as_float(0x7f800000);
+    const bool movable = has && inv_mass(S, g) > 0.0f;
+    warp_rows(movable ? S.deg[g] : 0u, slots,
+              [&](uint32_t o, uint32_t e) {
+                  const uint32_t io = i0 + o, go = W.boff + io;
+                  const float v = distance_term(S, W, adj_row(S, W, io)[e], S.pos[go], S.vel[go], S.phys[go].x,
+                                                len2(S.acc[go]), hMax);
+                  return make_float4(v, 0.0f, 0.0f, 0.0f);
+              },
+              [&](float4 c) { best = fminf(best, c.x); });
     return best;
 }
 
@@ -771,9 +796,11 @@ __device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, cons
 }
 
 // Contact forces from the current state, then the start-of-build acceleration (phase 2, NFK:776-779). Also gives
-// each thread its share of the first reduction: (max omega^2, owner) and (min margin bound, owner).
+// each thread its share of the first reduction: (max omega^2, owner) and (min margin bound, owner). `slots` holds one
+// float4 per thread of the team (the row terms of warp_rows).
 template <class Team>
-__device__ void initial_forces(const DState& S, const DWorld& W, const Ctl& c, const Team& team, ValOwner& w2, ValOwner& mg) {
+__device__ void initial_forces(const DState& S, const DWorld& W, const Ctl& c, const Team& team, ValOwner& w2, ValOwner& mg,
+                               float4* slots) {
     const float fraction = c.timeX > 0.0f ? clampf(c.timeY / c.timeX, 0.0f, 1.0f) : 1.0f;
     if (W.nb) {
         refresh_poses(S, W, team, fraction);
@@ -781,11 +808,13 @@ __device__ void initial_forces(const DState& S, const DWorld& W, const Ctl& c, c
     }
     w2 = ValOwner{-1.0f, 0u};
     mg = ValOwner{__int_as_float(0x7f800000), 0u};
-    for (uint32_t i = team.rank(); i < W.n; i += team.size()) {
-        uint32_t g = W.boff + i;
-        if (removed(S, g)) continue;
-        float im = inv_mass(S, g), omega2;
-        float2 F = contact_terms(S, W, i, fraction, im, omega2);
+    const uint32_t lane = team.rank() & 31u;
+    for (uint32_t i0 = team.rank() - lane; i0 < W.n; i0 += team.size()) {  // the whole warp iterates together
+        const uint32_t i = i0 + lane, g = W.boff + i;
+        const bool has = i < W.n && !removed(S, g);
+        float im = has ? inv_mass(S, g) : 0.0f, omega2;
+        float2 F = warp_contact_terms(S, W, i0, has, im, slots + (team.rank() - lane), omega2);
+        if (!has) continue;
         S.acc[g] = add(mul(F, im), S.a0[g]);
         if (omega2 > w2.v) { w2.v = omega2; w2.o = i; }
         float m = margin_bound(S, g);
@@ -798,7 +827,7 @@ __device__ void initial_forces(const DState& S, const DWorld& W, const Ctl& c, c
 // nativeReduceSubstepInGroup, NFK:625-736
 template <class Team>
 __device__ void reduce_substep(const DState& S, const DWorld& W, Ctl& c, const Team& team, float* history, ValOwner w2,
-                               ValOwner mg) {
+                               ValOwner mg, float4* slots) {
     const float inf = __int_as_float(0x7f800000);
     float remaining = c.timeX - c.timeY;
     bool over = !(remaining > 0.0f), stopped = c.cZ != 0u || c.cW != 0u, limited = c.cY >= kFrameLimit;
@@ -825,11 +854,12 @@ __device__ void reduce_substep(const DState& S, const DWorld& W, Ctl& c, const T
     const float stiffnessBound = w2.v > 0.0f ? 1.0f / sqrtf(w2.v) : inf;
     const float hMax = fminf(remaining, stiffnessBound);
     ValOwner db{inf, 0u};
-    for (uint32_t i = team.rank(); i < W.n; i += team.size()) {
-        uint32_t g = W.boff + i;
-        if (removed(S, g)) continue;
-        float v = distance_bound(S, W, i, hMax, fraction);
-        if (v < db.v) { db.v = v; db.o = i; }
+    const uint32_t lane = team.rank() & 31u;
+    for (uint32_t i0 = team.rank() - lane; i0 < W.n; i0 += team.size()) {  // the whole warp iterates together
+        const uint32_t i = i0 + lane;
+        const bool has = i < W.n && !removed(S, W.boff + i);
+        float v = warp_distance_bound(S, W, i0, has, hMax, slots + (team.rank() - lane));
+        if (has && v < db.v) { db.v = v; db.o = i; }
     }
     db = team.template pick<false>(db);
     if (mg.v <= 0.0f) {
@@ -882,16 +912,18 @@ __device__ __forceinline__ void kick_drift(const DState& S, const DWorld& W, uin
 
 // Contact forces from the new state and phase 1 (NFK:798-801): a = F / m + a0(x), second half kick. The same pass
 // gives omega^2 and the margin bound of the next reduction (same positions, velocities and accelerations it would read).
-__device__ __forceinline__ void force_kick(const DState& S, const DWorld& W, uint32_t i, float h, float fraction,
-                                           ValOwner& w2, ValOwner& mg) {
-    const uint32_t g = W.boff + i;
-    float im = inv_mass(S, g);
+// Bubble i0 + lane of every lane of the warp (`has`: the lane's bubble is live); the whole warp calls this together.
+__device__ __forceinline__ void force_kick(const DState& S, const DWorld& W, uint32_t i0, bool has, float h,
+                                           ValOwner& w2, ValOwner& mg, float4* slots) {
+    const uint32_t i = i0 + (threadIdx.x & 31u), g = W.boff + i;
+    const float im = has ? inv_mass(S, g) : 0.0f;
+    float omega2;
+    float2 F = warp_contact_terms(S, W, i0, has && im > 0.0f, im, slots, omega2);
+    if (!has) return;
     if (!(im > 0.0f)) {
         if (0.0f > w2.v) { w2.v = 0.0f; w2.o = i; }
         return;
     }
-    float omega2;
-    float2 F = contact_terms(S, W, i, fraction, im, omega2);
     uint32_t f = S.flags[g];
     float halfStep = 0.5f * h;
     float gamma = (f & BP_BUBBLE_FORCE_DRIVEN) ? fmaxf(S.phys[g].w, 0.0f) : 0.0f;
@@ -1381,12 +1413,12 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
                        : broadphase<Team, false>(S, W, c, team, buckets, entries, records, B, buildOverflow, maxPer, wi);
     BP_PHASE(1);
     ValOwner w2, mg;
-    initial_forces(S, W, c, team, w2, mg);
+    initial_forces(S, W, c, team, w2, mg, records);
     BP_PHASE(2);
     uint32_t violated = 0u;
     for (uint32_t iteration = 0; iteration < 2u * kFrameLimit + 2u; ++iteration) {
         if (!team.ok()) break;
-        reduce_substep(S, W, c, team, history, w2, mg);
+        reduce_substep(S, W, c, team, history, w2, mg, records);
         BP_PHASE(3);
         const float h = c.timeZ;
         const bool limited = c.cW != 0u, finished = !(c.timeX - c.timeY > 0.0f), rebuild = c.cZ != 0u;
@@ -1398,7 +1430,7 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
             ++rebuilds;
             cw = useTree ? broadphase<Team, true>(S, W, c, team, buckets, entries, records, B, buildOverflow, maxPer, wi)
                          : broadphase<Team, false>(S, W, c, team, buckets, entries, records, B, buildOverflow, maxPer, wi);
-            initial_forces(S, W, c, team, w2, mg);
+            initial_forces(S, W, c, team, w2, mg, records);
             BP_PHASE(1);
             continue;
         }
@@ -1409,8 +1441,10 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
         team.sync();
         w2 = ValOwner{-1.0f, 0u};
         mg = ValOwner{__int_as_float(0x7f800000), 0u};
-        for (uint32_t i = r; i < n; i += T)
-            if (!removed(S, W.boff + i)) force_kick(S, W, i, h, fraction, w2, mg);
+        for (uint32_t i0 = r - (r & 31u); i0 < n; i0 += T) {  // the whole warp iterates together
+            const uint32_t i = i0 + (r & 31u);
+            force_kick(S, W, i0, i < n && !removed(S, W.boff + i), h, w2, mg, records + (r - (r & 31u)));
+        }
         // The whole-GPU team needs no barrier here: whatever reads other bubbles' new state next (the next reduction,
         // an injection, the assertion, the end of the step, a rebuild's grid reductions) passes one first, and the
         // body poses the force pass reads are rewritten only behind several. The block and group teams keep it:
@@ -1620,7 +1654,7 @@ __device__ __forceinline__ void group_queue(const QueueArgs& q, uint32_t nGroup,
                    GroupShape{group * width, width, 1u + group}};
     uint32_t* grid = mine + scratch;
     float4* records = (float4*)(grid + round4_words(q.warpB + q.warpMaxN));
-    uint32_t* ws = q.warpWsWords ? grid + grid_words(q.warpB, q.warpMaxN) : nullptr;
+    uint32_t* ws = q.warpWsWords ? grid + grid_words(q.warpB, q.warpMaxN, width) : nullptr;
     for (;;) {
         if (team.leader()) next[group] = atomicAdd(q.queue + 1, 1u);
         team.sync();
@@ -1647,7 +1681,7 @@ __global__ void __launch_bounds__(kThreads, 2) persistent_step_kernel(DState S, 
         __syncthreads();
         if (slot >= nCta) break;
         world_step<CtaTeam, kTree>(S, q.ctaList[slot], cta, g_dynamic_smem, g_dynamic_smem + q.ctaB, cta_records(q), q.ctaB,
-                                   q.ctaWsWords ? g_dynamic_smem + grid_words(q.ctaB, q.ctaMaxN) : nullptr, q.ctaWsWords,
+                                   q.ctaWsWords ? g_dynamic_smem + grid_words(q.ctaB, q.ctaMaxN, blockDim.x) : nullptr, q.ctaWsWords,
                                    ctaState);
         __syncthreads();
     }
@@ -1679,7 +1713,7 @@ __global__ void __launch_bounds__(kThreads, 2) served_step_kernel(const DState* 
         }
         __syncthreads();
         world_step<CtaTeam, kTree>(ctaState.G, 0u, cta, g_dynamic_smem, g_dynamic_smem + q.ctaB, cta_records(q), q.ctaB,
-                                   q.ctaWsWords ? g_dynamic_smem + grid_words(q.ctaB, q.ctaMaxN) : nullptr, q.ctaWsWords,
+                                   q.ctaWsWords ? g_dynamic_smem + grid_words(q.ctaB, q.ctaMaxN, blockDim.x) : nullptr, q.ctaWsWords,
                                    ctaState);
         __syncthreads();
     }
