@@ -1006,6 +1006,25 @@ int bp_world_read_rigid_keys(bp_world* world, uint64_t* out, uint32_t capacity, 
     return cuda_status(err);
 }
 
+// The world's table of contour directions for sample counts up to `stride` (grown to the largest stride asked for).
+static cudaError_t contour_dirs(WorldSet& ws, uint32_t stride, const float2** out) {
+    if (stride > ws.contourDirStride) {
+        const std::vector<float2> dirs = contour_directions(stride);
+        float2* d = nullptr;
+        cudaError_t err = cudaMalloc(&d, dirs.size() * sizeof(float2));
+        if (!err) err = cudaMemcpy(d, dirs.data(), dirs.size() * sizeof(float2), cudaMemcpyHostToDevice);
+        if (err) {
+            cudaFree(d);
+            return err;
+        }
+        cudaFree(ws.dContourDirs);
+        ws.dContourDirs = d;
+        ws.contourDirStride = stride;
+    }
+    *out = ws.dContourDirs;
+    return cudaSuccess;
+}
+
 int bp_world_contours(bp_world* world, const bp_contour_config* config, float* points_xy, uint32_t* counts,
                       float* level, float* shape, uint32_t* stride_out, float* gpu_ms) {
     if (!world || !config) return BP_E_INVALID;
@@ -1029,12 +1048,14 @@ int bp_world_contours(bp_world* world, const bp_contour_config* config, float* p
     uint32_t* dCounts = nullptr;
     float* dLevel = nullptr;
     float* dShape = nullptr;
-    cudaError_t err = cudaMallocAsync(&dPoints, samples * sizeof(float2), st);
+    const float2* dDirs = nullptr;
+    cudaError_t err = contour_dirs(ws, stride, &dDirs);
+    if (!err) err = cudaMallocAsync(&dPoints, samples * sizeof(float2), st);
     if (!err) err = cudaMallocAsync(&dCounts, (size_t)W.n * sizeof(uint32_t), st);
     if (!err) err = cudaMallocAsync(&dLevel, samples * sizeof(float), st);
     if (!err) err = cudaMallocAsync(&dShape, (size_t)W.n * 6u * sizeof(float), st);
     if (!err) err = cudaEventRecord(ws.ctx->start, st);
-    if (!err) err = launch_contours(ws.S, W, maxEdge, tension, clearance, stride, dPoints, dCounts, dLevel, dShape, st);
+    if (!err) err = launch_contours(ws.S, W, maxEdge, tension, clearance, stride, dDirs, dPoints, dCounts, dLevel, dShape, st);
     if (!err) err = cudaEventRecord(ws.ctx->stop, st);
     if (!err && points_xy) err = cudaMemcpyAsync(points_xy, dPoints, samples * sizeof(float2), cudaMemcpyDeviceToHost, st);
     if (!err && counts) err = cudaMemcpyAsync(counts, dCounts, (size_t)W.n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
@@ -1067,7 +1088,9 @@ int bp_world_hit_test(bp_world* world, const bp_contour_config* config, const fl
     uint32_t *dLayers = nullptr, *dFound = nullptr;
     float *dLevel = nullptr, *dShape = nullptr;
     long long* dIds = nullptr;
-    cudaError_t err = cudaMallocAsync(&dPoints, samples * sizeof(float2), st0);
+    const float2* dDirs = nullptr;
+    cudaError_t err = contour_dirs(ws, stride, &dDirs);
+    if (!err) err = cudaMallocAsync(&dPoints, samples * sizeof(float2), st0);
     if (!err) err = cudaMallocAsync(&dCounts, std::max(W.n, 1u) * sizeof(uint32_t), st0);
     if (!err) err = cudaMallocAsync(&dLevel, samples * sizeof(float), st0);
     if (!err) err = cudaMallocAsync(&dShape, std::max(W.n, 1u) * 6ull * sizeof(float), st0);
@@ -1082,8 +1105,8 @@ int bp_world_hit_test(bp_world* world, const bp_contour_config* config, const fl
     if (!err) err = upload(dBubbleLayers, bubbleLayers.data(), W.n, st0);
     if (!err) err = upload(dSegLayers, ws.hSegLayers.data() + W.soff, W.s, st0);
     if (!err) err = upload(dBodyLayers, ws.hBodyLayers.data() + W.bodyOff, W.nb, st0);
-    if (!err) err = launch_contours(ws.S, W, config->max_edge, config->surface_tension, config->clearance, stride, dPoints,
-                                    dCounts, dLevel, dShape, st0);
+    if (!err) err = launch_contours(ws.S, W, config->max_edge, config->surface_tension, config->clearance, stride, dDirs,
+                                    dPoints, dCounts, dLevel, dShape, st0);
     if (!err) err = launch_hit_test(ws.S, W, dQueries, count, dPoints, dCounts, dShape, stride, dBubbleLayers, dSegLayers,
                                     dBodyLayers, dIds, dLayers, dFound, st0);
     if (!err) err = cudaMemcpyAsync(ids, dIds, count * sizeof(long long), cudaMemcpyDeviceToHost, st0);

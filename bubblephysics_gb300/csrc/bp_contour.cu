@@ -10,6 +10,9 @@
 // bounds, the effective radius and the largest deficit. Here one block steps one bubble through all three, one thread
 // per sample, with the deficits in shared memory; the serial majorant runs on one thread like the reference's (a chain
 // of float subtractions whose order fixes the bits).
+#include <cmath>
+#include <vector>
+
 #include "bp_device.cuh"
 
 namespace bp {
@@ -33,8 +36,8 @@ __device__ __forceinline__ float contour_ray_limit(float2 center, float2 directi
                                                                       : radius;
 }
 
-__global__ void __launch_bounds__(1024) contour_kernel(DState S, DWorld W, ContourArgs a, float2* points,
-                                                       uint32_t* counts, float* level, float* shape) {
+__global__ void __launch_bounds__(1024) contour_kernel(DState S, DWorld W, ContourArgs a, const float2* dirs,
+                                                       float2* points, uint32_t* counts, float* level, float* shape) {
     __shared__ float lvl[1024];
     __shared__ float part[32][6];
     __shared__ float seedMaximum;
@@ -49,8 +52,7 @@ __global__ void __launch_bounds__(1024) contour_kernel(DState S, DWorld W, Conto
     float2 direction = f2(1.0f, 0.0f);
     float deficit = 0.0f;
     if (active) {
-        const float angle = 2.0f * kPiF * (float)s / (float)count;
-        direction = f2(cosf(angle), sinf(angle));
+        direction = dirs[contour_dir_offset(count) + s];
         float limit = r;
         const uint2 fi = S.filter[g];
         for (uint32_t j = 0; j < W.s; ++j) {
@@ -236,14 +238,30 @@ cudaError_t launch_hit_test(const DState& S, const DWorld& W, const float2* quer
     return cudaGetLastError();
 }
 
+// Sample directions of every sample count from 1 to `stride` (contour_dir_offset): sample s of a count lies at the float
+// angle 2 pi s / count (the reference's expression), and its direction is the cosine and sine of that angle evaluated in
+// double precision and rounded to float. They are computed on the host once, so every build of the contours uses the
+// same directions.
+std::vector<float2> contour_directions(uint32_t stride) {
+    std::vector<float2> out(contour_dir_offset(stride + 1u));
+    for (uint32_t count = 1; count <= stride; ++count) {
+        float2* d = out.data() + contour_dir_offset(count);
+        for (uint32_t s = 0; s < count; ++s) {
+            const float angle = 2.0f * kPiF * (float)s / (float)count;
+            d[s] = make_float2((float)std::cos((double)angle), (float)std::sin((double)angle));
+        }
+    }
+    return out;
+}
+
 cudaError_t launch_contours(const DState& S, const DWorld& W, float maxEdge, float tension, float clearance,
-                            uint32_t stride, float2* points, uint32_t* counts, float* level, float* shape,
-                            cudaStream_t stream) {
+                            uint32_t stride, const float2* dirs, float2* points, uint32_t* counts, float* level,
+                            float* shape, cudaStream_t stream) {
     if (W.n == 0u) return cudaSuccess;
-    if (stride == 0u || stride > 1024u) return cudaErrorInvalidValue;
+    if (stride == 0u || stride > 1024u || !dirs) return cudaErrorInvalidValue;
     ContourArgs a{maxEdge, tension, clearance, stride};
     const uint32_t threads = (stride + 31u) & ~31u;
-    contour_kernel<<<W.n, threads, 0, stream>>>(S, W, a, points, counts, level, shape);
+    contour_kernel<<<W.n, threads, 0, stream>>>(S, W, a, dirs, points, counts, level, shape);
     return cudaGetLastError();
 }
 

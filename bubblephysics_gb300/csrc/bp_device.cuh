@@ -209,6 +209,10 @@ constexpr float kPiF = 3.14159265358979323846f;
 
 // Contour samples of a bubble of radius r (nativeAccumulateContactPressure, NativePostSolveKernels:292):
 // max(64, ceil((r / maxEdge) * 4 pi)), at most `stride`.
+// Index of the first direction of a bubble with `count` samples in the direction table (the tables of counts 1, 2, ...
+// one after another).
+__host__ __device__ inline uint32_t contour_dir_offset(uint32_t count) { return count * (count - 1u) / 2u; }
+
 __host__ __device__ inline uint32_t contour_samples(float r, float maxEdge, uint32_t stride) {
     const float q = (r / maxEdge) * (4.0f * kPiF);
     const uint32_t want = (uint32_t)ceilf(q);

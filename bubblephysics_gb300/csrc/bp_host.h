@@ -63,9 +63,10 @@ struct EventArgsHost {
 };
 cudaError_t launch_contact_events(const EventArgsHost& args, cudaStream_t stream);
 size_t event_entry_bytes();
+std::vector<float2> contour_directions(uint32_t stride);
 cudaError_t launch_contours(const DState& S, const DWorld& W, float maxEdge, float tension, float clearance,
-                            uint32_t stride, float2* points, uint32_t* counts, float* level, float* shape,
-                            cudaStream_t stream);
+                            uint32_t stride, const float2* dirs, float2* points, uint32_t* counts, float* level,
+                            float* shape, cudaStream_t stream);
 }  // namespace bp
 
 struct bp_context {
@@ -196,6 +197,9 @@ struct WorldSet {
         void* scratch = nullptr;
         size_t scratchBytes = 0;
     } events;
+    // contour sample directions of every count up to contourDirStride (contour_directions), uploaded on first use
+    float2* dContourDirs = nullptr;
+    uint32_t contourDirStride = 0;
     cudaMemPool_t pool = nullptr;           // stream-ordered pool (server worlds); null: plain cudaMalloc
     bool planOnly = false;                  // server worlds: built without the batch schedule
     bool measureOnly = false;               // count the device bytes of a build without allocating or uploading
@@ -207,6 +211,7 @@ struct WorldSet {
         cudaFree(events.history[0]);
         cudaFree(events.history[1]);
         cudaFree(events.scratch);
+        cudaFree(dContourDirs);
         for (void* p : allocations) {
             if (pool) cudaFreeAsync(p, ctx->stream);
             else cudaFree(p);

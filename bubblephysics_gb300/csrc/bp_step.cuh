@@ -216,10 +216,10 @@ __device__ __forceinline__ float4 contact_term(const DState& S, const DWorld& W,
 // `term(o, e)` = entry e of lane o's row, into its slot of `slots` (one float4 per lane of this warp). Each owner then
 // hands its own entries' values to `take` in row order, so a row sum adds the same terms in the same order as a
 // sequential loop over the row. The whole warp calls this together.
-template <class Term, class Take>
-__device__ __forceinline__ void warp_rows(uint32_t deg, float4* slots, Term&& term, Take&& take) {
+// Exclusive scan of the lanes' row lengths; returns the warp's total.
+__device__ __forceinline__ uint32_t warp_row_starts(uint32_t deg, uint32_t& start) {
     const uint32_t lane = threadIdx.x & 31u;
-    uint32_t start = deg;  // inclusive scan, then exclusive
+    start = deg;
 #pragma unroll
     for (uint32_t d = 1; d < 32u; d <<= 1) {
         const uint32_t v = __shfl_up_sync(0xffffffffu, start, d);
@@ -227,20 +227,50 @@ __device__ __forceinline__ void warp_rows(uint32_t deg, float4* slots, Term&& te
     }
     const uint32_t total = __shfl_sync(0xffffffffu, start, 31);
     start -= deg;
+    return total;
+}
+// The lane whose row holds entry f of the warp's numbering (the last lane whose row starts at or before f), and the
+// entry's index in that row.
+__device__ __forceinline__ uint32_t warp_row_owner(uint32_t start, uint32_t f, uint32_t& e) {
+    uint32_t o = 0;
+#pragma unroll
+    for (uint32_t step = 16; step; step >>= 1) {
+        const uint32_t so = __shfl_sync(0xffffffffu, start, o + step);
+        if (so <= f) o += step;
+    }
+    e = f - __shfl_sync(0xffffffffu, start, o);
+    return o;
+}
+
+template <class Term, class Take>
+__device__ __forceinline__ void warp_rows(uint32_t deg, float4* slots, Term&& term, Take&& take) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t start;
+    const uint32_t total = warp_row_starts(deg, start);
     for (uint32_t t0 = 0; t0 < total; t0 += 32u) {
         const uint32_t f = t0 + lane;
-        uint32_t o = 0;  // the last lane whose row starts at or before entry f
-#pragma unroll
-        for (uint32_t step = 16; step; step >>= 1) {
-            const uint32_t so = __shfl_sync(0xffffffffu, start, o + step);
-            if (so <= f) o += step;
-        }
-        const uint32_t first = __shfl_sync(0xffffffffu, start, o);
-        if (f < total) slots[lane] = term(o, f - first);
+        uint32_t e;
+        const uint32_t o = warp_row_owner(start, f, e);
+        if (f < total) slots[lane] = term(o, e);
         __syncwarp();
         const uint32_t lo = max(start, t0), hi = min(start + deg, t0 + 32u);
         for (uint32_t x = lo; x < hi; ++x) take(slots[x - t0]);
         __syncwarp();
+    }
+}
+
+// The same numbering without a row sum: `visit(o, e)` runs once for every entry e of every lane o's row, spread evenly
+// over the lanes (for passes whose per-entry results need no ordered combination). The whole warp calls this together.
+template <class Visit>
+__device__ __forceinline__ void warp_entries(uint32_t deg, Visit&& visit) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t start;
+    const uint32_t total = warp_row_starts(deg, start);
+    for (uint32_t t0 = 0; t0 < total; t0 += 32u) {
+        const uint32_t f = t0 + lane;
+        uint32_t e;
+        const uint32_t o = warp_row_owner(start, f, e);
+        if (f < total) visit(o, e);
     }
 }
 
@@ -470,9 +500,9 @@ __device__ __forceinline__ void lower_pair(const DState& S, const DWorld& W, uin
 // Forward candidate row of bubble i: pairs with j > i, then segments; k smallest keys (NGK:300-330). The same cell
 // scan collects the lower pairs j < i into the adjacency row (their count goes to deg until finish_adjacency). With
 // the tree, the rigid traversal also registers i in the rows of the bodies that accept it.
-template <bool kTree>
+template <bool kTree, bool kPrune>
 __device__ void emit_row(const DState& S, const DWorld& W, const uint32_t* buckets, const uint32_t* entries,
-                         const float4* records, uint32_t B, uint32_t i, uint32_t& overflow, uint32_t& maxPer) {
+                         const float4* records, uint32_t B, float cw, uint32_t i, uint32_t& overflow, uint32_t& maxPer) {
     const uint32_t g = W.boff + i, k = W.k;
     uint32_t* row = S.candRow + W.rowOff + (uint64_t)i * k;
     uint32_t* adjRow = S.adj + W.rowOff + (uint64_t)i * k;
@@ -511,33 +541,60 @@ __device__ void emit_row(const DState& S, const DWorld& W, const uint32_t* bucke
     const float2 pi = S.pos[g];
     const float ri = S.phys[g].x, mi = S.margin[g], tol = W.sepTol;
     const uint2 fi = S.filter[g];
-    for (int dx = -1; dx <= 1; ++dx)
-        for (int dy = -1; dy <= 1; ++dy) {
+    // With kPrune only the cells of the 3x3 block that meet the square of half-side R around the centre are scanned:
+    // they alone can hold a pair within reach, since every r_j + m_j is at most (cw - tol) / 2, so reach <= r_i + m_i +
+    // cw / 2 + |tol|; the relative slack covers every rounding of the reach, the box test and the cell coordinates
+    // (visiting a cell more is harmless, the rule decides). A non-finite R scans the whole block. This pays where
+    // entries are read from global memory; on staged worlds the whole block is scanned.
+    int x0 = -1, x1 = 1, y0 = -1, y1 = 1;
+    if (kPrune) {
+        const float reachMax = ri + mi + 0.5f * cw + fabsf(tol);
+        const float R = reachMax + 1e-4f * (fabsf(ri) + fabsf(mi) + cw + fabsf(tol) + fabsf(pi.x) + fabsf(pi.y)) + 1e-3f;
+        if (R < cw) {
+            const long long lx = (long long)clampf(floorf((pi.x - R) / cw), -4.0e18f, 4.0e18f);
+            const long long hx = (long long)clampf(floorf((pi.x + R) / cw), -4.0e18f, 4.0e18f);
+            const long long ly = (long long)clampf(floorf((pi.y - R) / cw), -4.0e18f, 4.0e18f);
+            const long long hy = (long long)clampf(floorf((pi.y + R) / cw), -4.0e18f, 4.0e18f);
+            if (lx >= c.x) x0 = 0;
+            if (hx <= c.x) x1 = 0;
+            if (ly >= c.y) y0 = 0;
+            if (hy <= c.y) y1 = 0;
+        }
+    }
+    for (int dx = x0; dx <= x1; ++dx)
+        for (int dy = y0; dy <= y1; ++dy) {
             const long long tx = c.x + dx, ty = c.y + dy;
             const uint32_t h = grid_hash(tx, ty, B);
             const uint32_t begin = h == 0u ? 0u : buckets[h - 1], end = buckets[h];
-            for (uint32_t e = begin; e < end; ++e) {
-                const float4 q = records[e];
-                const uint32_t j = entries[e];
-                if (j == i) continue;
+            auto visit = [&](const float4 q, const uint32_t j) {
+                if (j == i) return;
                 const float reach = j < i ? q.z + ri + q.w + mi + tol : ri + q.z + mi + q.w + tol;
-                if (!(fabsf(pi.x - q.x) <= reach && fabsf(pi.y - q.y) <= reach)) continue;
+                if (!(fabsf(pi.x - q.x) <= reach && fabsf(pi.y - q.y) <= reach)) return;
                 const uint32_t gj = W.boff + j;
                 const longlong2 cj = S.cell[gj];
-                if (cj.x != tx || cj.y != ty) continue;
+                if (cj.x != tx || cj.y != ty) return;
                 if (j < i) {
-                    if (!(S.flags[gj] & kStartFinite)) continue;
-                    if (!filter_accepts(S.filter[gj], fi)) continue;
-                    if (W.njEnt && joint_excluded(S, W, j, S.id[g])) continue;
+                    if (!(S.flags[gj] & kStartFinite)) return;
+                    if (!filter_accepts(S.filter[gj], fi)) return;
+                    if (W.njEnt && joint_excluded(S, W, j, S.id[g])) return;
                     ++lowerTotal;
                     insert_sorted(adjRow, lowerKept, k, j);
                 } else {
-                    if (!filter_accepts(fi, S.filter[gj])) continue;
-                    if (W.njEnt && joint_excluded(S, W, i, S.id[gj])) continue;
+                    if (!filter_accepts(fi, S.filter[gj])) return;
+                    if (W.njEnt && joint_excluded(S, W, i, S.id[gj])) return;
                     ++total;
                     insert_sorted(row, count, k, j);
                 }
-            }
+            };
+            uint32_t e = begin;
+            if (kPrune)  // entries in global memory: two loads in flight before the first test
+                for (; e + 1u < end; e += 2u) {
+                    const float4 q0 = records[e], q1 = records[e + 1u];
+                    const uint32_t j0 = entries[e], j1 = entries[e + 1u];
+                    visit(q0, j0);
+                    visit(q1, j1);
+                }
+            for (; e < end; ++e) visit(records[e], entries[e]);
         }
     S.deg[g] = lowerTotal;
     const uint32_t pairs = count;
@@ -770,7 +827,8 @@ __device__ float broadphase(const DState& S, const DWorld& W, const Ctl& c, cons
     team.sync();
     BP_SUBPHASE(14);
     uint32_t overflow = 0, maxPer = 0;
-    for (uint32_t i = r; i < n; i += T) emit_row<kTree>(S, W, buckets, entries, records, B, i, overflow, maxPer);
+    for (uint32_t i = r; i < n; i += T)
+        emit_row<kTree, kGridTeam<Team>>(S, W, buckets, entries, records, B, cw, i, overflow, maxPer);
     team.sync();
     BP_SUBPHASE(15);
     {
@@ -1475,28 +1533,65 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
     team.sync();
     // contact records: count per bubble, scan, write (kind-major candidate order)
     uint32_t pairsLocal = 0, segsLocal = 0;
-    for (uint32_t i = r; i < n; i += T) {
-        uint32_t g = W.boff + i;
-        uint32_t cp = 0, cs = 0, active0 = 0, active1 = 0;  // which of the first 64 candidates are active
-        if (!removed(S, g)) {
-            uint2 cc = S.candCount[g];
-            const uint32_t* crow = S.candRow + W.rowOff + (uint64_t)i * W.k;
-            DContact tmp;
-            for (uint32_t e = 0; e < cc.x + cc.y; ++e) {
-                const uint32_t kind = e < cc.x ? 0u : 1u;
-                if (!contact_record<false>(S, W, i, kind, crow[e] & kIndexMask, tmp)) continue;
-                if (kind == 0u) ++cp; else ++cs;
-                if (e < 32u) active0 |= 1u << e;
-                else if (e < 64u) active1 |= 1u << (e - 32u);
+    const uint32_t lane = r & 31u;
+    if (!kGridTeam<Team>) {
+        for (uint32_t i = r; i < n; i += T) {
+            uint32_t g = W.boff + i;
+            uint32_t cp = 0, cs = 0, active0 = 0, active1 = 0;  // which of the first 64 candidates are active
+            if (!removed(S, g)) {
+                uint2 cc = S.candCount[g];
+                const uint32_t* crow = S.candRow + W.rowOff + (uint64_t)i * W.k;
+                DContact tmp;
+                for (uint32_t e = 0; e < cc.x + cc.y; ++e) {
+                    const uint32_t kind = e < cc.x ? 0u : 1u;
+                    if (!contact_record<false>(S, W, i, kind, crow[e] & kIndexMask, tmp)) continue;
+                    if (kind == 0u) ++cp; else ++cs;
+                    if (e < 32u) active0 |= 1u << e;
+                    else if (e < 64u) active1 |= 1u << (e - 32u);
+                }
             }
+            S.scanA[g] = cp;
+            S.scanB[g] = cs;
+            // the non-contact accelerations are not needed again this step: their slot keeps the activity bits for
+            // the writing pass (stored as raw bits)
+            S.a0[g] = f2(__uint_as_float(active0), __uint_as_float(active1));
+            pairsLocal += cp;
+            segsLocal += cs;
         }
-        S.scanA[g] = cp;
-        S.scanB[g] = cs;
-        // the non-contact accelerations are not needed again this step: their slot keeps the activity bits for the
-        // writing pass (stored as raw bits)
-        S.a0[g] = f2(__uint_as_float(active0), __uint_as_float(active1));
-        pairsLocal += cp;
-        segsLocal += cs;
+    } else {
+        // The whole-GPU team spreads the candidate rows of a warp's bubbles over its lanes (warp_rows); each owner counts
+        // its own entries in row order. (The block and group teams measured faster with the plain loop above.)
+        for (uint32_t i0 = r - lane; i0 < n; i0 += T) {  // the whole warp iterates together
+            const uint32_t i = i0 + lane, g = W.boff + i;
+            const bool has = i < n && !removed(S, g);
+            const uint2 cc = has ? S.candCount[g] : make_uint2(0u, 0u);
+            uint32_t cp = 0, cs = 0, active0 = 0, active1 = 0, e = 0;  // which of the first 64 candidates are active
+            warp_rows(cc.x + cc.y, records + (r - lane),
+                      [&](uint32_t o, uint32_t eo) {
+                          const uint32_t io = i0 + o, go = W.boff + io;
+                          const uint32_t kind = eo < S.candCount[go].x ? 0u : 1u;
+                          const uint32_t* crow = S.candRow + W.rowOff + (uint64_t)io * W.k;
+                          DContact tmp;
+                          const bool on = contact_record<false>(S, W, io, kind, crow[eo] & kIndexMask, tmp);
+                          return make_float4(on ? 1.0f : 0.0f, 0.0f, 0.0f, 0.0f);
+                      },
+                      [&](float4 v) {
+                          if (v.x != 0.0f) {
+                              if (e < cc.x) ++cp; else ++cs;
+                              if (e < 32u) active0 |= 1u << e;
+                              else if (e < 64u) active1 |= 1u << (e - 32u);
+                          }
+                          ++e;
+                      });
+            if (i >= n) continue;
+            S.scanA[g] = cp;
+            S.scanB[g] = cs;
+            // the non-contact accelerations are not needed again this step: their slot keeps the activity bits for the
+            // writing pass (stored as raw bits)
+            S.a0[g] = f2(__uint_as_float(active0), __uint_as_float(active1));
+            pairsLocal += cp;
+            segsLocal += cs;
+        }
     }
     BP_PHASE(6);
     uint32_t pc[4] = {pairsLocal, segsLocal, 0u, 0u};
@@ -1505,24 +1600,68 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
     const uint32_t segsAll = pc[1];
     team.scan_inplace(S.scanA + W.boff, n);
     team.scan_inplace(S.scanB + W.boff, n);
+    // Records in row order per bubble (pairs at scanA, segments after all pairs at scanB).
     uint32_t droppedLocal = 0;
-    for (uint32_t i = r; i < n; i += T) {
-        uint32_t g = W.boff + i;
-        if (removed(S, g)) continue;
-        uint2 cc = S.candCount[g];
-        const uint32_t* crow = S.candRow + W.rowOff + (uint64_t)i * W.k;
-        uint32_t op = S.scanA[g], os = pairsAll + S.scanB[g];
-        const float2 bits = S.a0[g];
-        const uint32_t active0 = __float_as_uint(bits.x), active1 = __float_as_uint(bits.y);
-        DContact rec;
-        for (uint32_t e = 0; e < cc.x + cc.y; ++e) {
-            uint32_t kind = e < cc.x ? 0u : 1u;
-            if (e < 32u ? !((active0 >> e) & 1u) : (e < 64u && !((active1 >> (e - 32u)) & 1u))) continue;
-            if (!contact_record<true>(S, W, i, kind, crow[e] & kIndexMask, rec)) continue;
-            uint32_t slot = kind == 0u ? op++ : os++;
-            if (!finite2(rec.normal) || !finite2(rec.point) || !isfinite(rec.impulse) || !isfinite(rec.penetration)) nonfinite = 1u;
-            if (slot < W.contactCap) S.contacts[W.contactOff + slot] = rec;
-            else ++droppedLocal;
+    auto emit = [&](const DContact& rec, uint32_t slot) {
+        if (!finite2(rec.normal) || !finite2(rec.point) || !isfinite(rec.impulse) || !isfinite(rec.penetration)) nonfinite = 1u;
+        if (slot < W.contactCap) S.contacts[W.contactOff + slot] = rec;
+        else ++droppedLocal;
+    };
+    if (!kGridTeam<Team>) {
+        for (uint32_t i = r; i < n; i += T) {
+            uint32_t g = W.boff + i;
+            if (removed(S, g)) continue;
+            uint2 cc = S.candCount[g];
+            const uint32_t* crow = S.candRow + W.rowOff + (uint64_t)i * W.k;
+            uint32_t op = S.scanA[g], os = pairsAll + S.scanB[g];
+            const float2 bits = S.a0[g];
+            const uint32_t active0 = __float_as_uint(bits.x), active1 = __float_as_uint(bits.y);
+            DContact rec;
+            for (uint32_t e = 0; e < cc.x + cc.y; ++e) {
+                uint32_t kind = e < cc.x ? 0u : 1u;
+                if (e < 32u ? !((active0 >> e) & 1u) : (e < 64u && !((active1 >> (e - 32u)) & 1u))) continue;
+                if (!contact_record<true>(S, W, i, kind, crow[e] & kIndexMask, rec)) continue;
+                emit(rec, kind == 0u ? op++ : os++);
+            }
+        }
+    } else {
+        // The whole-GPU team spreads the first 64 entries of the warp's rows over its lanes: an active entry's slot is
+        // its owner's offset plus the active entries of its kind before it (the activity bits). Entries from 64 on
+        // follow in order on the owner's lane.
+        for (uint32_t i0 = r - lane; i0 < n; i0 += T) {  // the whole warp iterates together
+            const uint32_t i = i0 + lane, g = W.boff + i;
+            const bool has = i < n && !removed(S, g);
+            const uint2 cc = has ? S.candCount[g] : make_uint2(0u, 0u);
+            warp_entries(min(cc.x + cc.y, 64u), [&](uint32_t o, uint32_t e) {
+                const uint32_t io = i0 + o, go = W.boff + io;
+                const float2 bits = S.a0[go];
+                const unsigned long long active =
+                    (unsigned long long)__float_as_uint(bits.x) | ((unsigned long long)__float_as_uint(bits.y) << 32);
+                if (!((active >> e) & 1ull)) return;
+                const uint32_t pairs = S.candCount[go].x, kind = e < pairs ? 0u : 1u;
+                const uint32_t* crow = S.candRow + W.rowOff + (uint64_t)io * W.k;
+                DContact rec;
+                if (!contact_record<true>(S, W, io, kind, crow[e] & kIndexMask, rec)) return;
+                const unsigned long long below = active & ((1ull << e) - 1ull);
+                const unsigned long long pairMask = pairs >= 64u ? ~0ull : ((1ull << pairs) - 1ull);
+                const uint32_t slot = kind == 0u ? S.scanA[go] + (uint32_t)__popcll(below)
+                                                 : pairsAll + S.scanB[go] + (uint32_t)__popcll(below & ~pairMask);
+                emit(rec, slot);
+            });
+            if (!has || cc.x + cc.y <= 64u) continue;
+            const float2 bits = S.a0[g];
+            const unsigned long long active =
+                (unsigned long long)__float_as_uint(bits.x) | ((unsigned long long)__float_as_uint(bits.y) << 32);
+            const unsigned long long pairMask = cc.x >= 64u ? ~0ull : ((1ull << cc.x) - 1ull);
+            uint32_t op = S.scanA[g] + (uint32_t)__popcll(active & pairMask);
+            uint32_t os = pairsAll + S.scanB[g] + (uint32_t)__popcll(active & ~pairMask);
+            const uint32_t* crow = S.candRow + W.rowOff + (uint64_t)i * W.k;
+            DContact rec;
+            for (uint32_t e = 64u; e < cc.x + cc.y; ++e) {
+                const uint32_t kind = e < cc.x ? 0u : 1u;
+                if (!contact_record<true>(S, W, i, kind, crow[e] & kIndexMask, rec)) continue;
+                emit(rec, kind == 0u ? op++ : os++);
+            }
         }
     }
     BP_PHASE(7);

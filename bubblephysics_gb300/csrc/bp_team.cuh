@@ -474,10 +474,11 @@ struct GridTeam {
         if (threadIdx.x == 0) po[base + blockIdx.x] = total;
         par ^= 1u;
         sync();
-        if (threadIdx.x == 0) {
+        if (threadIdx.x < 32) {  // the totals of the blocks before this one, summed by one warp
             uint32_t off = 0;
-            for (uint32_t b = 0; b < blockIdx.x; ++b) off += __ldcg(po + base + b);
-            sh->bcastU[2] = off;
+            for (uint32_t b = threadIdx.x; b < blockIdx.x; b += 32) off += __ldcg(po + base + b);
+            off = warp_sum(off);
+            if (threadIdx.x == 0) sh->bcastU[2] = off;
         }
         __syncthreads();
         running += sh->bcastU[2];

@@ -1449,9 +1449,10 @@ static void world_contours(const World<float>& w, float maxEdge, float tension, 
         const float cx = w.pPos[i].x, cy = w.pPos[i].y;
         std::vector<float> dirx(count), diry(count), hard(count), lvl(count);
         for (uint32_t s = 0; s < count; ++s) {
+            // the CUDA path's host table: cosine and sine of the float angle in double precision, rounded to float
             float angle = 2.0f * pi * (float)s / (float)count;
-            dirx[s] = std::cos(angle);
-            diry[s] = std::sin(angle);
+            dirx[s] = (float)std::cos((double)angle);
+            diry[s] = (float)std::sin((double)angle);
             float limit = r;
             for (uint32_t j = 0; j < w.s; ++j) {
                 if (!filter_accepts(w.cat[i], w.mask[i], w.scat[j], w.smask[j])) continue;

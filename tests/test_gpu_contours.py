@@ -1,6 +1,6 @@
 """Contours on the GPU (bp_world_contours) against the oracle's restatement of the reference's contour passes
-(NativePostSolveKernels:268-527). The sample directions come from cosf / sinf, whose last bit may differ between CUDA
-and the host library, so points and levels are compared within a small tolerance; sample counts are exact."""
+(NativePostSolveKernels:268-527): sample counts, points, levels and shapes bit-exact. Both take the sample directions
+as the double-precision cosine and sine of the float angle, rounded to float."""
 import numpy as np
 import pytest
 
@@ -19,9 +19,9 @@ def compare(spec, ctx, steps, **cfg):
     pc, cc, lc, sc = cpu.contours(stride=pg.shape[1], **cfg)
     assert np.array_equal(cg, cc)
     mask = np.arange(pg.shape[1])[None, :] < cg[:, None]
-    assert np.abs(lg - lc)[mask].max(initial=0.0) <= 1e-3
-    assert np.abs(pg - pc)[mask].max(initial=0.0) <= 2e-3
-    assert np.abs(sg - sc).max() <= 2e-3
+    assert np.array_equal(lg[mask], lc[mask])
+    assert np.array_equal(pg[mask], pc[mask])
+    assert np.array_equal(sg, sc)
     return cg, lg, ms
 
 
