@@ -192,16 +192,19 @@ def workload_config(args, bubbles: int) -> dict:
             "l2": "inputs larger than L2: every step touches the state of all worlds (>129 MB)"}
 
 
-def single_world_rate(spec, ctx, steps: int, warmup: int, contours: bool = False) -> dict:
+def single_world_rate(spec, ctx, steps: int, warmup: int, contours: bool = False, stop_on_failure: bool = False) -> dict:
     """One world stepped through bp_world_step: device time per step (CUDA events on the library's stream) and
-    bubble-substeps per second over `steps` timed steps after `warmup` untimed ones."""
+    bubble-substeps per second over `steps` timed steps after `warmup` untimed ones. With stop_on_failure the timed
+    steps end at the first step that does not succeed (that step is not counted)."""
     from bubblephysics_gb300.solver import World
     world = World(spec, ctx)
-    status, _ = world.step(warmup)
+    status, _ = world.step(warmup) if warmup else (0, None)
     statuses, ms, subs = [status], [], 0
     for _ in range(steps):
         status, reps = world.step(1)
         statuses.append(status)
+        if stop_on_failure and status != 0:
+            break
         ms.append(float(reps["gpu_ms"][0]))
         subs += int(reps["substep_count"][0]) * spec.bubble_count
     keys = world.rigid_keys().size
@@ -213,28 +216,65 @@ def single_world_rate(spec, ctx, steps: int, warmup: int, contours: bool = False
         contour = {"ms": cms, "samples": int(counts.sum()), "samples_per_s": float(counts.sum()) / (cms / 1e3)}
     world.close()
     total_s = sum(ms) / 1000.0
+    done = len(ms)
     return {"bubbles": spec.bubble_count, "segments": len(spec.segments), "bodies": len(spec.bodies),
-            "steps": steps, "warmup": warmup, "ms_per_step": total_s * 1000.0 / max(steps, 1),
-            "substeps_per_step": subs / max(spec.bubble_count * steps, 1),
+            "steps": done, "warmup": warmup, "ms_per_step": total_s * 1000.0 / max(done, 1),
+            "substeps_per_step": subs / max(spec.bubble_count * done, 1),
             "value": subs / total_s if total_s > 0 else 0.0, "unit": UNIT, "statuses": sorted(set(statuses)),
             "rigid_tree_leaves": keys, "contours": contour}
 
 
-def single_worlds(ctx, steps: int) -> dict:
-    """The single-world workloads beside the batched headline: the large plain world (65,536 bubbles in 8192^2, grid
-    rebuilt almost every substep; whole-GPU team) and the rigid world (16,384 bubbles, ~4,000 static / kinematic
-    bodies in 4096^2, rigid candidates through the LBVH, and the same world by brute force for comparison)."""
+def single_worlds(ctx, steps: int, large_steps: int, rigid_steps: int) -> dict:
+    """The single-world workloads beside the batched headline: the plain world (256 bubbles in 375 x 700, its 60 steps
+    from the initial state), the large plain world (65,536 bubbles in 8192^2, grid rebuilt almost every substep;
+    whole-GPU team) and the rigid world (16,384 bubbles, ~4,000 static / kinematic bodies in 4096^2, rigid candidates
+    through the LBVH, and the same world by brute force for comparison)."""
     import dataclasses
     from bubblephysics_gb300 import _native as N
     from bubblephysics_gb300 import scenes
-    out = {"large_world": single_world_rate(scenes.large_world(), ctx, steps, 3, contours=True)}
+    out = {"plain_world": single_world_rate(scenes.plain_world(seed=1), ctx, 60, 0)}
+    out["large_world"] = single_world_rate(scenes.large_world(), ctx, steps, 3, contours=True)
+    # the large world's run from its initial state: the pile needs more substeps every step and reaches the frame limit
+    # of 1,024 substeps (BP_E_SUBSTEP_LIMIT) long before 600 steps; the run stops at the first failed step
+    full = single_world_rate(scenes.large_world(), ctx, large_steps, 0, stop_on_failure=True)
+    full["requested_steps"] = large_steps
+    out["large_world_from_start"] = full
     rigid = scenes.rigid_world()
-    out["rigid_world"] = single_world_rate(rigid, ctx, steps, 3)
+    out["rigid_world"] = single_world_rate(rigid, ctx, rigid_steps, 3)
     brute = dataclasses.replace(rigid, flags=rigid.flags | N.WORLD_NO_RIGID_TREE)
     out["rigid_world_brute_force"] = single_world_rate(brute, ctx, steps, 3)
     t, b = out["rigid_world"]["ms_per_step"], out["rigid_world_brute_force"]["ms_per_step"]
     out["rigid_world"]["speedup_vs_brute_force"] = b / t if t > 0 else None
     return out
+
+
+def plain_world_accuracy(ctx, checkpoints=(1, 10, 30, 60)) -> dict:
+    """Part of the CPU-baseline leg: the plain 256-bubble world stepped on the GPU (FP32) against the oracle's FP64 rerun
+    of the same steps (the checker). Largest |dx| and |dv| / largest |v| at each checkpoint, and whether the GPU state
+    equals the oracle's FP32 run bit for bit there. The world is a dense pile, so FP32 and FP64 separate over time
+    (chaotic contact order), while the FP32 runs stay identical."""
+    from oracle import oracle
+    from bubblephysics_gb300 import scenes
+    from bubblephysics_gb300.solver import World
+    spec = scenes.plain_world(seed=1)
+    gpu, f32, f64 = World(spec, ctx), oracle.OracleWorld(spec, 32), oracle.OracleWorld(spec, 64)
+    out, done = [], 0
+    for c in checkpoints:
+        gpu.step(c - done)
+        f32.step(c - done)
+        f64.step(c - done)
+        done = c
+        g, a = gpu.bubbles(), f32.bubbles()
+        ref = f64.state64()
+        pos = g["center"].astype(np.float64)
+        vel = g["velocity"].astype(np.float64)
+        vmax = max(float(np.abs(ref[:, 2:4]).max()), 1e-30)
+        out.append({"step": c, "max_abs_dx": float(np.abs(pos - ref[:, 0:2]).max()),
+                    "max_abs_dv_rel": float(np.abs(vel - ref[:, 2:4]).max()) / vmax,
+                    "gpu_equals_fp32_oracle": bool(np.array_equal(g["center"], a["center"]) and
+                                                   np.array_equal(g["velocity"], a["velocity"]))})
+    gpu.close()
+    return {"world": "plain world, 256 bubbles, seed 1", "checkpoints": out}
 
 
 def log(message: str):
@@ -443,7 +483,8 @@ def run_ours(args, rank, world_size, local_rank):
         return 0
 
     # single-world and serving measurements are one-GPU figures: they run in one-process runs only
-    singles = single_worlds(ctx, args.single_steps) if args.single_steps > 0 and world_size == 1 else None
+    singles = (single_worlds(ctx, args.single_steps, args.large_steps, args.rigid_steps)
+               if args.single_steps > 0 and world_size == 1 else None)
     served = serving(ctx, args) if args.serve_requests > 0 and world_size == 1 else None
     peak, peak_kind = load_peak()
     achieved = alg_bytes / device_s / 1e9 if device_s > 0 else 0.0
@@ -464,6 +505,7 @@ def run_ours(args, rank, world_size, local_rank):
     ref_line = json.loads(ref.stdout.strip().splitlines()[-1])
     leg = {"value": ref_line["value"], "cores": ref_line["cpu_baseline"]["cores"],
            "sample": ref_line["cpu_baseline"]["sample"]}
+    accuracy = plain_world_accuracy(ctx) if world_size == 1 else None
     lat = sorted(step_ms)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
@@ -486,6 +528,7 @@ def run_ours(args, rank, world_size, local_rank):
                      "bytes_model": "76 + 40*k per bubble-substep, 96 + 8*k per bubble grid build (k = mean degree)"},
         "cpu_baseline": {"value": leg["value"], "unit": UNIT, "cores": leg["cores"], "kind": "port",
                          "sample": leg["sample"] + " (bench.py --impl reference, run as a separate process)"},
+        "accuracy_fp32_vs_fp64": accuracy,
         "clocks": clocks,
         "gpu_launches": gpu_launches,
         "single_worlds": singles,
@@ -587,7 +630,10 @@ def main():
     p.add_argument("--per-world-steps", type=int, default=2)
     p.add_argument("--cpu-steps", type=int, default=0,
                    help="timed steps of the CPU baseline leg (0: the same as --steps, the reference arm's sample)")
-    p.add_argument("--single-steps", type=int, default=10, help="timed steps of each single-world workload (0: skip)")
+    p.add_argument("--single-steps", type=int, default=10,
+                   help="timed steps of the rigid world by brute force (0: skip the single worlds)")
+    p.add_argument("--large-steps", type=int, default=600, help="timed steps of the 65,536-bubble large world")
+    p.add_argument("--rigid-steps", type=int, default=300, help="timed steps of the rigid world")
     p.add_argument("--serve-worlds", type=int, default=8192)
     p.add_argument("--serve-requests", type=int, default=20000, help="requests of the serving stream (0: skip)")
     p.add_argument("--serve-rate", type=float, default=50000.0, help="Poisson arrival rate of the serving stream")
