@@ -545,6 +545,7 @@ def run_case(name: str) -> int:
       batch     persistent_step_kernel, schedule_kernel, accumulate_kernel: 4 steps of the 4,096-world batch, autotuned
       batch512  the same with a fixed schedule (512-thread blocks, worlds of <= 64 bubbles in 64-thread groups)
       large     large_step_kernel: 3 steps of the 65,536-bubble world
+      rigid     large_step_kernel: 3 steps of the 16,384-bubble rigid world (3,017 bodies, 5,652 edges, LBVH)
       served    served_step_kernel: 3 rounds of one-step requests over 512 resident worlds
       contour   contour_kernel: contours of the 65,536-bubble world after 3 steps
       hit       hit_test_kernel: 65,536 query points on the 256-bubble world
@@ -562,8 +563,8 @@ def run_case(name: str) -> int:
         st, r = b.step(4)
         print("status", st, "ms per step", float(r["gpu_ms"][0]) / 4, b.tuning())
         return 0 if st == N.OK else 1
-    if name == "large":
-        st, r = World(scenes.large_world(), ctx).step(3)
+    if name in ("large", "rigid"):
+        st, r = World(scenes.large_world() if name == "large" else scenes.rigid_world(), ctx).step(3)
         print("status", st, "substeps", r["substep_count"].tolist())
         return 0 if st == N.OK else 1
     if name == "served":
