@@ -32,9 +32,10 @@ def same(gpu, cpu, steps):
     assert sg == sc
     for key in ("status", "substep_count", "rebuild_count", "candidate_count", "body_candidate_count",
                 "candidate_overflow", "max_candidates_per_object", "contact_count", "limiter_term", "limiter_object",
-                "violation_kind", "removed_count", "wrapped_count"):
+                "violation_kind", "violation_edge", "removed_count", "wrapped_count"):
         assert rg[key].tolist() == rc[key].tolist(), key
     assert np.array_equal(rg["violation_objects"], rc["violation_objects"])
+    assert np.array_equal(rg["violation_distance"], rc["violation_distance"])
     bg, bc = gpu.bubbles(), cpu.bubbles()
     for f in ("center", "previous_center", "velocity", "rotation", "angular_velocity", "region_result"):
         assert np.array_equal(bg[f], bc[f]), (f, np.abs(bg[f].astype(np.float64) - bc[f]).max())
@@ -70,6 +71,17 @@ def test_injected_edge_crossing_on_gpu(ctx):
     cpu.set_injection(0, (100.0, 5.0))
     rep = same(gpu, cpu, 1)
     assert rep[0]["violation_kind"] == N.VIOLATION_EDGE_SIDE
+
+
+def test_natural_edge_crossing_on_gpu(ctx):
+    """Bubbles without contact stiffness run through the floor's bottom edge within one step, without injection.
+    The end-of-step assertion reports the crossing exactly as the oracle does: kind, objects, edge and distance."""
+    b = scenes.make_bubbles([(100.0, -10.0), (300.0, -40.0)], 12.0, velocities=[(0.0, 1200.0), (0.0, 1200.0)],
+                            masses=0.36, stiffness=0.0)
+    spec = scenes.WorldSpec(bubbles=b, segments=fixtures.floor_wall())
+    rep = same(World(spec, ctx), OracleWorld(spec, 32), 2)
+    assert rep[0]["status"] == N.E_CONTACT_VIOLATION and rep[0]["violation_kind"] == N.VIOLATION_EDGE_SIDE
+    assert rep[0]["violation_edge"] == 1000 and rep[0]["rebuild_count"] == 0
 
 
 def test_substep_limit_on_gpu(ctx):
