@@ -140,12 +140,29 @@ __device__ __forceinline__ int tree_delta(const unsigned long long* keys, int co
     return __clzll(keys[i] ^ keys[j]);
 }
 
+// Per-part cycle counters of the tree build for profiling builds (-DBP_PHASE_TIMING; phase ids 19-23).
+#ifdef BP_PHASE_TIMING
+#define BP_TREE_MARK(id)                                                                                 \
+    do {                                                                                                 \
+        if (team.leader() && S.phaseCycles) {                                                            \
+            const long long now_ = clock64();                                                            \
+            S.phaseCycles[(uint64_t)wi * kPhaseCount + (id)] += (unsigned long long)(now_ - treeMark);   \
+            treeMark = now_;                                                                             \
+        }                                                                                                \
+    } while (0)
+#else
+#define BP_TREE_MARK(id) do { } while (0)
+#endif
+
 // Builds the world's tree; false (uniform over the team) when the world has no leaves or a leaf box is not finite,
 // in which case the step uses the brute-force loops.
 template <class Team>
 __device__ bool build_rigid_tree(const DState& S, const DWorld& W, uint32_t wi, const Team& team) {
     const uint32_t L = W.s + W.nb, base = W.treeOff, T = team.size(), r = team.rank();
     team.sync();  // the boxes of this step are written
+#ifdef BP_PHASE_TIMING
+    long long treeMark = clock64();
+#endif
     uint32_t v[4] = {0u, 0u, 0u, 0u};
     for (uint32_t p = r; p < L; p += T) {
         const float4 b = leaf_box(S, W, p);
@@ -157,6 +174,7 @@ __device__ bool build_rigid_tree(const DState& S, const DWorld& W, uint32_t wi, 
         v[3] = max(v[3], ~float_order(cy));
     }
     team.template reduce4<0xfu>(v);
+    BP_TREE_MARK(19);
     const bool ok = L > 0u && v[0] != 0xffffffffu;
     if (team.leader()) S.tValid[wi] = ok ? 1u : 0u;
     if (!ok) return false;
@@ -171,7 +189,9 @@ __device__ bool build_rigid_tree(const DState& S, const DWorld& W, uint32_t wi, 
         keys[p] = ((unsigned long long)code << 32) | p;
     }
     team.sync();
+    BP_TREE_MARK(20);
     sort_leaf_keys(keys, S.tKeysAlt + base, S.tCounts + 16ull * base, L, team);
+    BP_TREE_MARK(21);
     if (L == 1u) return true;
     // hierarchy (Karras 2012, "Maximizing parallelism in the construction of BVHs, octrees and k-d trees")
     TreeNode* nodes = S.tNodes + base;
@@ -215,6 +235,7 @@ __device__ bool build_rigid_tree(const DState& S, const DWorld& W, uint32_t wi, 
         S.tVisit[base + node] = 0u;
     }
     team.sync();
+    BP_TREE_MARK(22);
     // bottom-up refit: the second child to reach a node carries the union to the parent
     for (uint32_t q = r; q < L; q += T) {
         float4 box = leaf_box_wide(S, W, (uint32_t)(keys[q] & 0xffffffffull));
@@ -231,6 +252,7 @@ __device__ bool build_rigid_tree(const DState& S, const DWorld& W, uint32_t wi, 
         }
     }
     team.sync();
+    BP_TREE_MARK(23);
     return true;
 }
 
