@@ -58,13 +58,14 @@ def algorithmic_bytes(bubble_substeps: float, bubble_builds: float, mean_degree:
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 50 ms from start() to stop(); each sample keeps its host
+    """nvidia-smi clocks and throttle reasons sampled every POLL_MS ms from start() to stop(); each sample keeps its host
     arrival time so the samples inside a sub-window (the timed steps) can be told apart from the rest."""
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
     NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    POLL_MS = 10  # the timed region of the default run lasts ~40 ms: several samples fall inside it
 
     def __init__(self, device: int):
         self.device = device
@@ -74,7 +75,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.POLL_MS)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -117,10 +118,10 @@ class ClockSampler:
             self.proc.kill()
         out = self._summary(self.lines)
         if timed is not None:
-            inside = self._summary([x for x in self.lines if timed[0] <= x[0] <= timed[1] + 0.06])
+            inside = self._summary([x for x in self.lines if timed[0] <= x[0] <= timed[1] + self.POLL_MS / 1000.0])
             out["timed_region"] = {"sm_mhz": inside["sm_mhz"], "reasons": inside["reasons"],
                                    "samples": inside["samples"], "seconds": timed[1] - timed[0]}
-            out["window"] = "warm-up, timed steps and end-to-end steps of the batched workload (50 ms polling)"
+            out["window"] = f"warm-up, timed steps and end-to-end steps of the batched workload ({self.POLL_MS} ms polling)"
         return out
 
 
@@ -551,7 +552,9 @@ def run_case(name: str) -> int:
       hit       hit_test_kernel: 65,536 query points on the 256-bubble world
       sensor    sensor_overlap_kernel, sensor_compact_kernel: 64 circle sensors on the 256-bubble world
       events    contact_events_kernel: contact events of the 256-bubble world, 3 steps
-      noalloc   noalloc_step_kernel: 3 allocation-free steps of the 256-bubble world"""
+      noalloc   noalloc_step_kernel: 3 allocation-free steps of the 256-bubble world
+      state     write_state_kernel, read_state_kernel, sum_kernel: the end-to-end state copies of the 4,096-world batch
+                (903 k bubbles) and its adjacency-entry count, 3 times each"""
     import ctypes as C
     from bubblephysics_gb300 import _native as N
     from bubblephysics_gb300 import scenes
@@ -563,6 +566,17 @@ def run_case(name: str) -> int:
         st, r = b.step(4)
         print("status", st, "ms per step", float(r["gpu_ms"][0]) / 4, b.tuning())
         return 0 if st == N.OK else 1
+    if name == "state":
+        b = Batch(scenes.batched_worlds(4096, seed=3), ctx, use_graph=True, threads_per_world=512, warp_world_max=64,
+                  group_width=64)
+        host, keep = pinned_buffer(int(b.sizes.sum()))
+        b.read_state(host)
+        for _ in range(3):
+            b.write_state(host)
+            b.read_state(host)
+            entries = b.adjacency_entries()
+        print("bubbles", int(b.sizes.sum()), "adjacency entries", entries)
+        return 0
     if name in ("large", "rigid"):
         st, r = World(scenes.large_world() if name == "large" else scenes.rigid_world(), ctx).step(3)
         print("status", st, "substeps", r["substep_count"].tolist())
