@@ -1,5 +1,7 @@
 // bp_aux.cu - small device kernels around the step: per-call report accumulation and the bulk state transfer used by
 // the host-buffer (end-to-end) path.
+#include <algorithm>
+
 #include "bp_device.cuh"
 
 namespace bp {
@@ -41,10 +43,17 @@ __global__ void read_state_kernel(float4* out, const float2* ppos, const float2*
     out[i] = make_float4(p.x, p.y, u.x, u.y);
 }
 
+// Sum of n 32-bit values (v 16-byte aligned: a device allocation), four per 16-byte load, then the tail.
 __global__ void sum_kernel(const uint32_t* v, uint64_t n, unsigned long long* total) {
     unsigned long long local = 0;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-        local += v[i];
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x, first = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t quads = n / 4u;
+    const uint4* q = (const uint4*)v;
+    for (uint64_t i = first; i < quads; i += stride) {
+        const uint4 x = q[i];
+        local += (unsigned long long)x.x + x.y + x.z + x.w;
+    }
+    for (uint64_t i = quads * 4u + first; i < n; i += stride) local += v[i];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) local += __shfl_xor_sync(0xffffffffu, local, off);
     if ((threadIdx.x & 31u) == 0u && local) atomicAdd(total, local);
@@ -52,7 +61,9 @@ __global__ void sum_kernel(const uint32_t* v, uint64_t n, unsigned long long* to
 
 cudaError_t launch_sum(const uint32_t* v, uint64_t n, unsigned long long* total, cudaStream_t stream) {
     if (!n) return cudaSuccess;
-    sum_kernel<<<256, 256, 0, stream>>>(v, n, total);
+    // one 16-byte load per thread where the values allow, at most 8 blocks per SM of 152
+    const uint64_t blocks = std::min<uint64_t>(std::max<uint64_t>((n / 4u + 255u) / 256u, 1u), 152u * 8u);
+    sum_kernel<<<(unsigned)blocks, 256, 0, stream>>>(v, n, total);
     return cudaGetLastError();
 }
 

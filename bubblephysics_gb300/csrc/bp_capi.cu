@@ -1433,11 +1433,29 @@ int bp_batch_read_bubbles(bp_batch* batch, uint32_t world, bp_bubble* out, uint3
     return read_bubbles(batch->set, world, out, capacity, count);
 }
 
+// The device address of a caller's host buffer of float4 records when the kernels can read or write it directly:
+// page-locked memory registered with CUDA (cudaHostAlloc / cudaHostRegister), 16-byte aligned; null otherwise (the
+// data then goes through the device staging array with a copy).
+static float4* direct_host_records(const void* p) {
+    if (((uintptr_t)p & 15u) != 0u) return nullptr;
+    cudaPointerAttributes attr{};
+    if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (attr.type != cudaMemoryTypeHost || !attr.devicePointer || ((uintptr_t)attr.devicePointer & 15u) != 0u)
+        return nullptr;
+    return (float4*)attr.devicePointer;
+}
+
 int bp_batch_write_state(bp_batch* batch, const float* cv, uint64_t bubble_count) {
     if (!batch || !cv) return BP_E_INVALID;
     WorldSet& ws = batch->set;
     if (bubble_count != ws.totalBubbles) return BP_E_INVALID;
     DeviceGuard guard(ws.ctx->device);
+    // page-locked records are read by the kernel across the host link: no staging copy
+    if (const float4* direct = direct_host_records(cv))
+        return cuda_status(launch_write_state(direct, ws.S.pos, ws.S.vel, ws.S.pPos, ws.S.pVel, bubble_count, ws.ctx->stream));
     cudaError_t err = cudaSuccess;
     if (!ws.dStaging) ws.dStaging = ws.alloc<float4>(ws.totalBubbles, err);
     if (!err) err = cudaMemcpyAsync(ws.dStaging, cv, bubble_count * sizeof(float4), cudaMemcpyHostToDevice, ws.ctx->stream);
@@ -1450,6 +1468,12 @@ int bp_batch_read_state(bp_batch* batch, float* cv, uint64_t bubble_count) {
     WorldSet& ws = batch->set;
     if (bubble_count != ws.totalBubbles) return BP_E_INVALID;
     DeviceGuard guard(ws.ctx->device);
+    // page-locked records are written by the kernel across the host link: no staging copy
+    if (float4* direct = direct_host_records(cv)) {
+        cudaError_t err = launch_read_state(direct, ws.S.pPos, ws.S.pVel, bubble_count, ws.ctx->stream);
+        if (!err) err = cudaStreamSynchronize(ws.ctx->stream);
+        return cuda_status(err);
+    }
     cudaError_t err = cudaSuccess;
     if (!ws.dStaging) ws.dStaging = ws.alloc<float4>(ws.totalBubbles, err);
     if (!err) err = launch_read_state(ws.dStaging, ws.S.pPos, ws.S.pVel, bubble_count, ws.ctx->stream);

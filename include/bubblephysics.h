@@ -340,7 +340,11 @@ int bp_batch_step(bp_batch* batch, uint32_t steps, bp_step_report* reports);
 /* Total bubbles and total substeps x bubbles advanced since creation (for throughput). */
 int bp_batch_counters(bp_batch* batch, uint64_t* bubble_count, uint64_t* bubble_substeps, uint64_t* launches);
 int bp_batch_read_bubbles(bp_batch* batch, uint32_t world, bp_bubble* out, uint32_t capacity, uint32_t* count);
-/* Bulk dynamic state of all worlds in world order: float4 (center.xy, velocity.xy) per bubble. */
+/* Bulk dynamic state of all worlds in world order: float4 (center.xy, velocity.xy) per bubble, in host memory.
+ * write_state is queued on the library's stream and returns at once (the buffer must stay unchanged until the next
+ * step or read completes); read_state returns when the data is in the buffer. A page-locked buffer (cudaHostAlloc or
+ * cudaHostRegister), 16-byte aligned, is read or written by the kernels themselves across the host link; any other
+ * buffer goes through a device staging array with a copy. */
 int bp_batch_write_state(bp_batch* batch, const float* center_velocity, uint64_t bubble_count);
 int bp_batch_read_state(bp_batch* batch, float* center_velocity, uint64_t bubble_count);
 /* Sum of the adjacency degrees of all bubbles of the last grid build (mean degree = sum / bubbles); used to count
