@@ -45,7 +45,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     """Compiles every CUDA translation unit for sm_103a and links the shared library. Returns its path."""
     nvcc = _nvcc()
     BUILD_DIR.mkdir(exist_ok=True)
-    headers = sorted(CSRC.glob("*.cuh")) + [PACKAGE_DIR.parent / "include" / "bubblephysics.h"]
+    headers = sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + [PACKAGE_DIR.parent / "include" / "bubblephysics.h"]
     objects = []
     jobs = []
     units = [(CSRC / name, BUILD_DIR / (name + ".o"), []) for name in SOURCES]
