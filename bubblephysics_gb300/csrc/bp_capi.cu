@@ -479,6 +479,12 @@ int large_blocks_for(const WorldSet& ws, uint32_t n) {
     return std::max(1, std::min(ws.largeBlocks, std::max(want, 8)));
 }
 
+// The whole-GPU step of world w; a world that builds a tree gets the key sort's histogram memory.
+cudaError_t launch_large_world(WorldSet& ws, uint32_t w, cudaStream_t st) {
+    return launch_large(ws.S, w, ws.largeB, large_blocks_for(ws, ws.hWorlds[w].n), kLargeThreads,
+                        ws.hWorlds[w].tree ? kRadixHistBytes : 0u, st);
+}
+
 cudaError_t launch_step(WorldSet& ws, bool perWorld, uint32_t only = 0xffffffffu) {
     cudaError_t err = cudaSuccess;
     cudaStream_t st = ws.ctx->stream;
@@ -486,7 +492,7 @@ cudaError_t launch_step(WorldSet& ws, bool perWorld, uint32_t only = 0xffffffffu
         const DWorld& W = ws.hWorlds[w];
         ws.launches++;
         if (W.n > kCtaMaxBubbles || (W.flags & BP_WORLD_FORCE_MULTI_CTA))
-            return launch_large(ws.S, w, ws.largeB, large_blocks_for(ws, ws.hWorlds[w].n), kLargeThreads, st);
+            return launch_large_world(ws, w, st);
         QueueArgs q{};
         q.queue = ws.dQueueSingle;
         q.countsOnDevice = 0u;
@@ -511,7 +517,7 @@ cudaError_t launch_step(WorldSet& ws, bool perWorld, uint32_t only = 0xffffffffu
     for (uint32_t w : ws.largeWorlds) {
         if (err != cudaSuccess) break;
         ws.launches++;
-        err = launch_large(ws.S, w, ws.largeB, large_blocks_for(ws, ws.hWorlds[w].n), kLargeThreads, st);
+        err = launch_large_world(ws, w, st);
     }
     return err;
 }

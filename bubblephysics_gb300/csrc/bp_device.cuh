@@ -209,6 +209,11 @@ constexpr float kPiF = 3.14159265358979323846f;
 
 // Contour samples of a bubble of radius r (nativeAccumulateContactPressure, NativePostSolveKernels:292):
 // max(64, ceil((r / maxEdge) * 4 pi)), at most `stride`.
+// The whole-GPU team's 8-bit key sort (one block of 16 warps): one 256-digit histogram per warp in dynamic shared
+// memory, given to the launches of worlds that build a tree.
+constexpr uint32_t kRadixWarps = 16u, kRadixDigits = 256u;
+constexpr uint32_t kRadixHistBytes = kRadixWarps * kRadixDigits * 4u;
+
 // Index of the first direction of a bubble with `count` samples in the direction table (the tables of counts 1, 2, ...
 // one after another).
 __host__ __device__ inline uint32_t contour_dir_offset(uint32_t count) { return count * (count - 1u) / 2u; }

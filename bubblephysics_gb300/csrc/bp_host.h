@@ -16,7 +16,8 @@ size_t persistent_smem(const QueueArgs& q, uint32_t threads);
 cudaError_t launch_schedule(const DState& S, const uint32_t* candidates, uint32_t count, uint32_t warpMax,
                             uint32_t warpSubsteps, uint32_t* ctaList, uint32_t* warpList, uint32_t* queue, cudaStream_t stream);
 int large_max_blocks(int threads);
-cudaError_t launch_large(const DState& S, uint32_t wi, uint32_t B, int blocks, int threads, cudaStream_t stream);
+cudaError_t launch_large(const DState& S, uint32_t wi, uint32_t B, int blocks, int threads, size_t smem,
+                         cudaStream_t stream);
 cudaError_t launch_contact_law(uint32_t mode, const float* in, float* out, uint32_t count, cudaStream_t stream);
 cudaError_t launch_accumulate(const bp_step_report* reports, bp_step_report* acc, const uint32_t* sizes,
                               unsigned long long* total, uint32_t count, cudaStream_t stream);

@@ -172,13 +172,14 @@ int large_max_blocks(int threads) {
     return sms * (perSm > 0 ? perSm : 1);
 }
 
-cudaError_t launch_large(const DState& S, uint32_t wi, uint32_t B, int blocks, int threads, cudaStream_t stream) {
+cudaError_t launch_large(const DState& S, uint32_t wi, uint32_t B, int blocks, int threads, size_t smem,
+                         cudaStream_t stream) {
     // the grid barrier counts arrivals from zero in every launch (the block count differs between worlds)
     cudaError_t err = cudaMemsetAsync(S.barrier, 0, sizeof(unsigned int), stream);
     if (err != cudaSuccess) return err;
     DState copy = S;
     void* args[] = {&copy, &wi, &B};
-    return cudaLaunchCooperativeKernel((const void*)large_step_kernel, dim3(blocks), dim3(threads), args, 0, stream);
+    return cudaLaunchCooperativeKernel((const void*)large_step_kernel, dim3(blocks), dim3(threads), args, smem, stream);
 }
 
 cudaError_t launch_contact_law(uint32_t mode, const float* in, float* out, uint32_t count, cudaStream_t stream) {

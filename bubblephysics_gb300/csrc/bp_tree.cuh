@@ -117,9 +117,56 @@ __device__ void tree_sort(unsigned long long* keys, unsigned long long* alt, uin
     }
 }
 
+// Stable LSD radix sort of `count` keys on bits 32..63 by one block of 16 warps (8-bit digits, 4 passes: the result
+// ends in `keys`). Warp w owns a contiguous chunk of the keys and walks it 32 keys at a time, in order. Each pass
+// builds the warp's digit histogram (shared memory), runs one block scan in digit-major, warp-minor order, and
+// scatters: lanes with the same digit take consecutive slots in lane order (__match_any_sync), so the sort is stable.
+// The histograms live in the launch's dynamic shared memory (kRadixHistBytes), which only launches that build a tree
+// ask for: static shared memory would take L1 from every launch of the kernel.
+extern __shared__ __align__(16) uint32_t g_radix_hist[];
+__device__ inline void block_radix_sort(unsigned long long* keys, unsigned long long* alt, uint32_t count,
+                                        const CtaTeam& block) {
+    uint32_t* hist = g_radix_hist;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t per = (count + kRadixWarps - 1u) / kRadixWarps;
+    const uint32_t first = min(warp * per, count), last = min(first + per, count);
+    const uint32_t below = (1u << lane) - 1u;
+    for (uint32_t pass = 0; pass < 4u; ++pass) {
+        const uint32_t shift = 32u + 8u * pass;
+        for (uint32_t d = lane; d < kRadixDigits; d += 32u) hist[d * kRadixWarps + warp] = 0u;
+        __syncwarp();
+        for (uint32_t base = first; base < last; base += 32u) {  // uniform over the warp
+            const uint32_t e = base + lane;
+            const bool in = e < last;
+            const uint32_t digit = in ? (uint32_t)(keys[e] >> shift) & 0xffu : 0u;
+            const uint32_t peers = __match_any_sync(0xffffffffu, in ? digit : kRadixDigits + lane);
+            if (in && (peers & below) == 0u) hist[digit * kRadixWarps + warp] += __popc(peers);
+            __syncwarp();
+        }
+        __syncthreads();
+        block.scan_inplace(hist, kRadixDigits * kRadixWarps);  // ends with a block barrier
+        for (uint32_t base = first; base < last; base += 32u) {
+            const uint32_t e = base + lane;
+            const bool in = e < last;
+            const unsigned long long key = in ? keys[e] : 0ull;
+            const uint32_t digit = (uint32_t)(key >> shift) & 0xffu;
+            const uint32_t peers = __match_any_sync(0xffffffffu, in ? digit : kRadixDigits + lane);
+            if (in) alt[hist[digit * kRadixWarps + warp] + __popc(peers & below)] = key;
+            __syncwarp();
+            if (in && (peers & below) == 0u) hist[digit * kRadixWarps + warp] += __popc(peers);
+            __syncwarp();
+        }
+        __syncthreads();
+        unsigned long long* t = keys;
+        keys = alt;
+        alt = t;
+    }
+}
+
 // Sort of a world's leaf keys by its team. The whole-GPU team sorts inside its first block (block barriers instead of
-// the ~32 grid barriers of eight team-wide passes: a few thousand keys sort faster than the grid can synchronise) and
-// the other blocks wait at one grid barrier.
+// the grid barriers of team-wide passes: a few thousand keys sort faster than the grid can synchronise), with the
+// 8-bit sort above when the block has 16 warps and the launch gave it the histogram memory, and the other blocks wait
+// at one grid barrier.
 template <class Team>
 __device__ __forceinline__ void sort_leaf_keys(unsigned long long* keys, unsigned long long* alt, uint32_t* counts,
                                                uint32_t count, const Team& team) {
@@ -129,7 +176,10 @@ __device__ __forceinline__ void sort_leaf_keys(unsigned long long* keys, unsigne
                                                uint32_t count, const GridTeam& team) {
     if (blockIdx.x == 0) {
         CtaTeam block{team.sh};
-        tree_sort(keys, alt, counts, count, block);
+        uint32_t dynamic;
+        asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dynamic));
+        if (blockDim.x == 32u * kRadixWarps && dynamic >= kRadixHistBytes) block_radix_sort(keys, alt, count, block);
+        else tree_sort(keys, alt, counts, count, block);
     }
     team.sync();
 }
