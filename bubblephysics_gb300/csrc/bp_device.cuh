@@ -155,7 +155,7 @@ struct DState {
     uint32_t* tValid;              // per world: 1 when the last step built its tree
 };
 
-constexpr uint32_t kPhaseCount = 24;
+constexpr uint32_t kPhaseCount = 26;  // profiling builds: 24 cycle counters, then the start and end times of the world's last step
 
 // Work queues of one persistent step launch (see persistent_step_kernel). The lists and their lengths live in device
 // memory so the on-device scheduler can reorder them between steps without a host round trip.

@@ -37,6 +37,15 @@ constexpr uint32_t kLive = 0xffu;         // mask of the public flags
         }                                                                                             \
     } while (0)
 #define BP_PHASE_START long long phaseMark = clock64()
+// global time (ns) of a point of the world's step, overwritten every step (slots 24 and 25: start and end)
+#define BP_STAMP(state, id)                                                                              \
+    do {                                                                                                 \
+        if (team.leader() && (state).phaseCycles) {                                                      \
+            unsigned long long t_;                                                                       \
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_));                                       \
+            (state).phaseCycles[(uint64_t)wi * kPhaseCount + (id)] = t_;                                 \
+        }                                                                                                \
+    } while (0)
 #define BP_SUBPHASE(id)                                                                                     \
     do {                                                                                                    \
         if (team.leader() && S.phaseCycles) {                                                               \
@@ -49,6 +58,7 @@ constexpr uint32_t kLive = 0xffu;         // mask of the public flags
 #else
 #define BP_PHASE(id) do { } while (0)
 #define BP_PHASE_START do { } while (0)
+#define BP_STAMP(state, id) do { } while (0)
 #define BP_SUBPHASE(id) do { } while (0)
 #endif
 
@@ -1416,6 +1426,7 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
         return;
     }
     DState& S = ts.S;
+    BP_STAMP(G, 24);
     stage_world(G, S, W, team, ws, wsWords);
     BP_PHASE_START;
     // nativeBeginStep (NFK:285-293)
@@ -1762,6 +1773,7 @@ __device__ void world_step(const DState& G, uint32_t wi, const Team& team, uint3
         if (team.leader()) G.failed[wi] = 1u;
     }
     BP_PHASE(10);
+    BP_STAMP(G, 25);
 }
 
 // ------------------------------------------------------------------------------------------------------------------
@@ -1776,11 +1788,11 @@ __device__ __forceinline__ float4* cta_records(const QueueArgs& q) {
     return (float4*)(g_dynamic_smem + round4_words(q.ctaB + q.ctaMaxN));
 }
 
-// Persistent step kernel: blocks pull worlds from two queues. CTA-team worlds (largest first) are stepped by a whole
-// block; then the block splits into groups of q.groupWidth threads (one warp or more), and every group pulls worlds of
-// the group queue on its own, so a block keeps blockDim / groupWidth worlds in flight. Dynamic shared memory holds the
-// hash grid: for a CTA world B bucket ends then its entries (then its workspace); for the group queue one slice per
-// group (group_slice_words).
+// Persistent step kernel: blocks pull worlds from two queues. First the block splits into groups of q.groupWidth
+// threads (one warp or more), and every group pulls worlds of the group queue on its own, so a block keeps
+// blockDim / groupWidth worlds in flight; then CTA-team worlds (largest first) are stepped by the whole block. Dynamic
+// shared memory holds the hash grid: for a CTA world B bucket ends then its entries (then its workspace); for the group
+// queue one slice per group (group_slice_words).
 template <class Next>
 __device__ __forceinline__ void group_queue(const QueueArgs& q, uint32_t nGroup, BlockScratch& blockSh, uint32_t* next,
                                             Next&& step) {
@@ -1813,6 +1825,13 @@ __global__ void __launch_bounds__(kThreads, 2) persistent_step_kernel(DState S, 
     CtaTeam cta{&sh};
     const uint32_t nCta = q.countsOnDevice ? *(volatile uint32_t*)(q.queue + 2) : q.nCta;
     const uint32_t nGroup = q.countsOnDevice ? *(volatile uint32_t*)(q.queue + 3) : q.nWarp;
+    // The group queue goes first: its worlds are cheap but slow to finish (many in flight per SM), and taken last they
+    // left a long drain at the end of the launch; the block-team queue ends with its cheapest worlds instead. The first
+    // block barrier of the block-team loop waits for every group of the block.
+    group_queue(q, nGroup, sh, next, [&](uint32_t wi, const GroupTeam& team, uint32_t* buckets, uint32_t* entries,
+                                         float4* records, uint32_t* ws, TeamState& ts) {
+        world_step<GroupTeam, kTree>(S, wi, team, buckets, entries, records, q.warpB, ws, q.warpWsWords, ts);
+    });
     for (;;) {
         if (threadIdx.x == 0) next[0] = atomicAdd(q.queue, 1u);
         __syncthreads();
@@ -1824,10 +1843,6 @@ __global__ void __launch_bounds__(kThreads, 2) persistent_step_kernel(DState S, 
                                    ctaState);
         __syncthreads();
     }
-    group_queue(q, nGroup, sh, next, [&](uint32_t wi, const GroupTeam& team, uint32_t* buckets, uint32_t* entries,
-                                         float4* records, uint32_t* ws, TeamState& ts) {
-        world_step<GroupTeam, kTree>(S, wi, team, buckets, entries, records, q.warpB, ws, q.warpWsWords, ts);
-    });
 }
 
 // Served step kernel: the same two queues over a batch of resident worlds that each keep their own device arrays.
@@ -1839,6 +1854,8 @@ __global__ void __launch_bounds__(kThreads, 2) served_step_kernel(const DState* 
     __shared__ uint32_t next[kThreads / 32];
     __shared__ TeamState ctaState;
     CtaTeam cta{&sh};
+    // Block-team worlds first: a serving batch is a few worlds, and its latency is that of its largest world, which
+    // must start at once (the batched kernel, which steps thousands of worlds for throughput, takes the groups first).
     for (;;) {
         if (threadIdx.x == 0) next[0] = atomicAdd(q.queue, 1u);
         __syncthreads();
