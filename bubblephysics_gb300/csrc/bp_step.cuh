@@ -571,41 +571,62 @@ __device__ void emit_row(const DState& S, const DWorld& W, const uint32_t* bucke
             if (hy <= c.y) y1 = 0;
         }
     }
-    for (int dx = x0; dx <= x1; ++dx)
-        for (int dy = y0; dy <= y1; ++dy) {
-            const long long tx = c.x + dx, ty = c.y + dy;
-            const uint32_t h = grid_hash(tx, ty, B);
-            const uint32_t begin = h == 0u ? 0u : buckets[h - 1], end = buckets[h];
-            auto visit = [&](const float4 q, const uint32_t j) {
-                if (j == i) return;
-                const float reach = j < i ? q.z + ri + q.w + mi + tol : ri + q.z + mi + q.w + tol;
-                if (!(fabsf(pi.x - q.x) <= reach && fabsf(pi.y - q.y) <= reach)) return;
-                const uint32_t gj = W.boff + j;
-                const longlong2 cj = S.cell[gj];
-                if (cj.x != tx || cj.y != ty) return;
-                if (j < i) {
-                    if (!(S.flags[gj] & kStartFinite)) return;
-                    if (!filter_accepts(S.filter[gj], fi)) return;
-                    if (W.njEnt && joint_excluded(S, W, j, S.id[g])) return;
-                    ++lowerTotal;
-                    insert_sorted(adjRow, lowerKept, k, j);
-                } else {
-                    if (!filter_accepts(fi, S.filter[gj])) return;
-                    if (W.njEnt && joint_excluded(S, W, i, S.id[gj])) return;
-                    ++total;
-                    insert_sorted(row, count, k, j);
-                }
-            };
-            uint32_t e = begin;
-            if (kPrune)  // entries in global memory: two loads in flight before the first test
-                for (; e + 1u < end; e += 2u) {
-                    const float4 q0 = records[e], q1 = records[e + 1u];
-                    const uint32_t j0 = entries[e], j1 = entries[e + 1u];
-                    visit(q0, j0);
-                    visit(q1, j1);
-                }
-            for (; e < end; ++e) visit(records[e], entries[e]);
+    // one cell of the scan: entries [begin, end) of the bucket of cell (tx, ty)
+    auto scan_cell = [&](const long long tx, const long long ty, const uint32_t begin, const uint32_t end) {
+        auto visit = [&](const float4 q, const uint32_t j) {
+            if (j == i) return;
+            const float reach = j < i ? q.z + ri + q.w + mi + tol : ri + q.z + mi + q.w + tol;
+            if (!(fabsf(pi.x - q.x) <= reach && fabsf(pi.y - q.y) <= reach)) return;
+            const uint32_t gj = W.boff + j;
+            const longlong2 cj = S.cell[gj];
+            if (cj.x != tx || cj.y != ty) return;
+            if (j < i) {
+                if (!(S.flags[gj] & kStartFinite)) return;
+                if (!filter_accepts(S.filter[gj], fi)) return;
+                if (W.njEnt && joint_excluded(S, W, j, S.id[g])) return;
+                ++lowerTotal;
+                insert_sorted(adjRow, lowerKept, k, j);
+            } else {
+                if (!filter_accepts(fi, S.filter[gj])) return;
+                if (W.njEnt && joint_excluded(S, W, i, S.id[gj])) return;
+                ++total;
+                insert_sorted(row, count, k, j);
+            }
+        };
+        uint32_t e = begin;
+        if (kPrune)  // entries in global memory: two loads in flight before the first test
+            for (; e + 1u < end; e += 2u) {
+                const float4 q0 = records[e], q1 = records[e + 1u];
+                const uint32_t j0 = entries[e], j1 = entries[e + 1u];
+                visit(q0, j0);
+                visit(q1, j1);
+            }
+        for (; e < end; ++e) visit(records[e], entries[e]);
+    };
+    if (kPrune) {
+        // the buckets live in global memory: every cell's bounds are loaded before the first cell is scanned
+        uint32_t cb[9], ce[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            const int dx = q / 3 - 1, dy = q % 3 - 1;
+            cb[q] = 0u;
+            ce[q] = 0u;
+            if (dx >= x0 && dx <= x1 && dy >= y0 && dy <= y1) {
+                const uint32_t h = grid_hash(c.x + dx, c.y + dy, B);
+                cb[q] = h == 0u ? 0u : buckets[h - 1];
+                ce[q] = buckets[h];
+            }
         }
+#pragma unroll
+        for (int q = 0; q < 9; ++q) scan_cell(c.x + (q / 3 - 1), c.y + (q % 3 - 1), cb[q], ce[q]);
+    } else {
+        for (int dx = x0; dx <= x1; ++dx)
+            for (int dy = y0; dy <= y1; ++dy) {
+                const long long tx = c.x + dx, ty = c.y + dy;
+                const uint32_t h = grid_hash(tx, ty, B);
+                scan_cell(tx, ty, h == 0u ? 0u : buckets[h - 1], buckets[h]);
+            }
+    }
     S.deg[g] = lowerTotal;
     const uint32_t pairs = count;
     uint32_t segTotal = 0;
