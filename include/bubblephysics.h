@@ -273,7 +273,7 @@ typedef struct bp_batch bp_batch;
 int bp_abi_version(void);
 /* Human-readable name of a status code (static string). */
 const char* bp_status_string(int status);
-/* Whether a CUDA device usable by this build is present (BP_OK) or not (BP_E_UNAVAILABLE). */
+/* Whether a CUDA device this library can run on is present (BP_OK) or not (BP_E_UNAVAILABLE). */
 int bp_device_available(int device);
 
 /* A context binds one CUDA device and one stream (NativeMetalSolver(device:), NativeMetalSolver.swift:355). */
