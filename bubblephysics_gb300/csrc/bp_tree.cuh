@@ -135,20 +135,26 @@ __device__ inline void block_radix_sort(unsigned long long* keys, unsigned long 
         const uint32_t shift = 32u + 8u * pass;
         for (uint32_t d = lane; d < kRadixDigits; d += 32u) hist[d * kRadixWarps + warp] = 0u;
         __syncwarp();
+        // each loop loads the next batch's key while it processes the current one
+        unsigned long long ahead = first + lane < last ? keys[first + lane] : 0ull;
         for (uint32_t base = first; base < last; base += 32u) {  // uniform over the warp
             const uint32_t e = base + lane;
             const bool in = e < last;
-            const uint32_t digit = in ? (uint32_t)(keys[e] >> shift) & 0xffu : 0u;
+            const unsigned long long key = ahead;
+            ahead = e + 32u < last ? keys[e + 32u] : 0ull;
+            const uint32_t digit = (uint32_t)(key >> shift) & 0xffu;
             const uint32_t peers = __match_any_sync(0xffffffffu, in ? digit : kRadixDigits + lane);
             if (in && (peers & below) == 0u) hist[digit * kRadixWarps + warp] += __popc(peers);
             __syncwarp();
         }
         __syncthreads();
         block.scan_inplace(hist, kRadixDigits * kRadixWarps);  // ends with a block barrier
+        ahead = first + lane < last ? keys[first + lane] : 0ull;
         for (uint32_t base = first; base < last; base += 32u) {
             const uint32_t e = base + lane;
             const bool in = e < last;
-            const unsigned long long key = in ? keys[e] : 0ull;
+            const unsigned long long key = ahead;
+            ahead = e + 32u < last ? keys[e + 32u] : 0ull;
             const uint32_t digit = (uint32_t)(key >> shift) & 0xffu;
             const uint32_t peers = __match_any_sync(0xffffffffu, in ? digit : kRadixDigits + lane);
             if (in) alt[hist[digit * kRadixWarps + warp] + __popc(peers & below)] = key;
