@@ -299,9 +299,10 @@ __device__ bool build_rigid_tree(const DState& S, const DWorld& W, uint32_t wi, 
         for (uint32_t depth = 0; depth < L; ++depth) {  // a path to the root has fewer than L nodes
             const uint32_t node = up >> 1, side = up & 1u;
             nodes[node].box[side] = box;
-            __threadfence();
-            if (atomicAdd(S.tVisit + base + node, 1u) == 0u) break;
-            __threadfence();
+            // one acquire-release add: it releases this child's box, and the second arriver acquires the sibling's
+            unsigned int arrived;
+            asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], 1;" : "=r"(arrived) : "l"(S.tVisit + base + node) : "memory");
+            if (arrived == 0u) break;
             box = box_union(box, __ldcg(&nodes[node].box[side ^ 1u]));
             up = __ldcg(&nodes[node].parent);
             if (up == kTreeNoParent) break;
