@@ -3,14 +3,15 @@
 // (kernel, block width, tree) variant per object file so the large instantiations compile in parallel; the launchers
 // and the small kernels live in bp_step.cu.
 //
-// One world is stepped by one "team": a thread block (batches of small and medium worlds, one block per world, all
-// worlds of a batch in one launch) or the whole grid of a cooperative launch (one large world). The team runs the
-// complete step of the reference's single-group kernel nativeSubstepLoopSingleGroup (NFK:1236-1307) - broadphase,
-// initial forces, the adaptive substep loop with in-step grid rebuilds, and the end-of-step work - so a batch costs
-// one launch per step whatever the substep counts of its worlds are.
+// One world is stepped by one "team" (bp_team.cuh): a group of warps of a block (small worlds, several per block), a
+// thread block (medium worlds) or the whole grid of a cooperative launch (one large world). All worlds of a batch run
+// in one launch. The team runs the complete step of the reference's single-group kernel nativeSubstepLoopSingleGroup
+// (NFK:1236-1307): broadphase, initial forces, the adaptive substep loop with in-step grid rebuilds, and the
+// end-of-step work. So a batch costs one launch per step whatever the substep counts of its worlds are.
 //
-// Per-bubble arithmetic follows NFK / NGK operation order exactly; reductions pick the largest / smallest value with
-// the lower bubble index winning ties, which is order-independent, so every team shape gives bit-identical results.
+// Per-bubble arithmetic follows NFK / NGK operation order exactly. Reductions pick the largest / smallest value with
+// the lower bubble index winning ties, which is order-independent. Row sums that are spread over a warp's lanes
+// (warp_rows) are still added by the owning lane in row order. So every team shape gives bit-identical results.
 #pragma once
 #include <type_traits>
 
