@@ -249,6 +249,50 @@ def single_worlds(ctx, steps: int, large_steps: int, rigid_steps: int) -> dict:
     return out
 
 
+def rigid_solver(steps: int = 50, warmup: int = 5, cpu_steps: int = 5) -> dict:
+    """The rigid solver passes (bp_rigid_predict, 8 rounds of bp_rigid_solve_joints in one launch, bp_rigid_finish)
+    on jointed chains of box links (every joint kind), at 64 x 32 and 256 x 32 links: device time per step and per
+    pass by CUDA events on the launching stream (the default stream, torch's current one), and the oracle's time per
+    step on one host core (the reference runs these passes as one Metal dispatch per kernel and round)."""
+    import torch
+    from bubblephysics_gb300 import scenes
+    from bubblephysics_gb300.rigid import ITERATIONS, RigidSolver
+    from oracle.oracle import OracleRigid
+    out = {}
+    for chains, links in ((64, 32), (256, 32)):
+        scene = scenes.jointed_chains(seed=6, chains=chains, links=links)
+        arrays = scene.joint_arrays()
+        solver = RigidSolver(scene.bodies, scene.vertices, scene.segments, arrays)
+        for _ in range(warmup):
+            solver.step(scene.dt, scene.region)
+        torch.cuda.synchronize()
+
+        def timed(fn, reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            for _ in range(reps):
+                fn()
+            b.record()
+            torch.cuda.synchronize()
+            return a.elapsed_time(b) / reps
+
+        step_ms = timed(lambda: solver.step(scene.dt, scene.region), steps)
+        passes = {"predict_ms": timed(lambda: solver.predict(scene.dt), steps),
+                  "joint_rounds_ms": timed(lambda: solver.solve_joints(scene.dt, ITERATIONS, ITERATIONS), steps),
+                  "finish_ms": timed(lambda: solver.finish(scene.region), steps)}
+        oracle = OracleRigid(scene.bodies, scene.vertices, scene.segments, arrays)
+        t0 = time.perf_counter()
+        for _ in range(cpu_steps):
+            oracle.step(scene.dt, scene.region)
+        cpu_ms = (time.perf_counter() - t0) * 1000.0 / cpu_steps
+        out[f"chains_{chains}x{links}"] = {
+            "bodies": len(scene.bodies), "joints": len(arrays.records), "segments": len(scene.segments),
+            "rounds": ITERATIONS, "ms_per_step": step_ms, "passes": passes, "safety": solver.safety(),
+            "launches_per_step": 4, "cpu_oracle_ms_per_step": cpu_ms, "cpu_cores": 1,
+            "note": "a step = the walls clear (a memset) + predict + the joint rounds + finish"}
+    return out
+
+
 def plain_world_accuracy(ctx, checkpoints=(1, 10, 30, 60)) -> dict:
     """Part of the CPU-baseline leg: the plain 256-bubble world stepped on the GPU (FP32) against the oracle's FP64 rerun
     of the same steps (the checker). Largest |dx| and |dv| / largest |v| at each checkpoint, and whether the GPU state
@@ -507,6 +551,7 @@ def run_ours(args, rank, world_size, local_rank):
     leg = {"value": ref_line["value"], "cores": ref_line["cpu_baseline"]["cores"],
            "sample": ref_line["cpu_baseline"]["sample"]}
     accuracy = plain_world_accuracy(ctx) if world_size == 1 else None
+    rigid = rigid_solver() if world_size == 1 and args.single_steps > 0 else None
     lat = sorted(step_ms)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
@@ -534,6 +579,7 @@ def run_ours(args, rank, world_size, local_rank):
         "gpu_launches": gpu_launches,
         "single_worlds": singles,
         "serving": served,
+        "rigid_solver": rigid,
     }
     print(json.dumps(line), flush=True)
     if dist:
@@ -554,12 +600,21 @@ def run_case(name: str) -> int:
       events    contact_events_kernel: contact events of the 256-bubble world, 3 steps
       noalloc   noalloc_step_kernel: 3 allocation-free steps of the 256-bubble world
       state     write_state_kernel, read_state_kernel, sum_kernel: the end-to-end state copies of the 4,096-world batch
-                (903 k bubbles) and its adjacency-entry count, 3 times each"""
+                (903 k bubbles) and its adjacency-entry count, 3 times each
+      chains    rigid_predict_kernel, rigid_joints_kernel, rigid_finish_kernel: 3 rigid steps of 256 x 32 jointed links"""
     import ctypes as C
     from bubblephysics_gb300 import _native as N
     from bubblephysics_gb300 import scenes
     from bubblephysics_gb300.solver import Batch, Context, Server, World
     ctx = Context(0)
+    if name == "chains":
+        from bubblephysics_gb300.rigid import RigidSolver
+        scene = scenes.jointed_chains(seed=6, chains=256, links=32)
+        solver = RigidSolver(scene.bodies, scene.vertices, scene.segments, scene.joint_arrays())
+        for _ in range(3):
+            solver.step(scene.dt, scene.region)
+        print("bodies", len(scene.bodies), "safety", solver.safety())
+        return 0 if solver.safety() == 0 else 1
     if name in ("batch", "batch512"):
         kw = dict(autotune=True) if name == "batch" else dict(threads_per_world=512, warp_world_max=64, group_width=64)
         b = Batch(scenes.batched_worlds(4096, seed=3), ctx, use_graph=True, **kw)

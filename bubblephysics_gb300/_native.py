@@ -197,6 +197,21 @@ CONTACT_EVENT_DTYPE = np.dtype({"names": ["kind", "reserved", "objects", "point"
                                 "offsets": [0, 4, 8, 24, 32, 40, 44], "itemsize": 48})
 KEY_DTYPE = np.dtype({"names": ["kind", "reserved", "first", "second"], "formats": ["<u4", "<u4", "<i8", "<i8"],
                       "offsets": [0, 4, 8, 16], "itemsize": 24})
+# rigid solver records (bp_rigid_body 160 B, bp_rigid_joint 96 B, bp_rigid_correction 64 B, bp_rigid_wall 48 B)
+RIGID_BODY_DTYPE = np.dtype({"names": ["id", "reserved0", "pose", "previous", "motion", "physical", "ranges", "flags",
+                                       "filter", "shape", "limits"],
+                             "formats": ["<u8", "<u8", ("<f4", 4), ("<f4", 4), ("<f4", 4), ("<f4", 4), ("<u4", 4),
+                                         ("<u4", 4), ("<u4", 4), ("<f4", 4), ("<f4", 4)],
+                             "offsets": [0, 8, 16, 32, 48, 64, 80, 96, 112, 128, 144], "itemsize": 160})
+RIGID_JOINT_DTYPE = np.dtype({"names": ["id", "reserved0", "ends", "anchors", "parameters", "limits", "state"],
+                              "formats": ["<u8", "<u8", ("<u4", 4), ("<f4", 4), ("<f4", 4), ("<f4", 4), ("<f4", 4)],
+                              "offsets": [0, 8, 16, 32, 48, 64, 80], "itemsize": 96})
+RIGID_CORRECTION_DTYPE = np.dtype({"names": ["first", "second", "velocity_first", "velocity_second"],
+                                   "formats": [("<f4", 4)] * 4, "offsets": [0, 16, 32, 48], "itemsize": 64})
+RIGID_WALL_DTYPE = np.dtype({"names": ["participants", "geometry", "extra"],
+                             "formats": [("<i8", 2), ("<f4", 4), ("<f4", 4)], "offsets": [0, 16, 32], "itemsize": 48})
+JOINT_WORLD_END = 0xFFFFFFFF
+RIGID_SAFETY_NONFINITE, RIGID_SAFETY_ROTATION_BUDGET, RIGID_SAFETY_INVALID = 1, 18, 256
 REPORT_DTYPE = np.dtype({"names": [n for n, _ in StepReport._fields_],
                          "formats": ["<i4"] + ["<u4"] * 9 + ["<i8", ("<i8", 2), "<i8", "<f4", "<f4", "<f4",
                                                              "<u4", "<u4", "<u4"],
@@ -267,6 +282,11 @@ _SIGNATURES = {
     "bp_server_read_bubbles": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
     "bp_server_read_stats": (C.c_int, [_P, C.POINTER(ServerStats)]),
     "bp_server_clock": (C.c_double, []),
+    "bp_rigid_predict": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32, _P, C.c_uint32, C.c_uint32, C.c_float, _P, _P,
+                                   C.c_uint32, _P, _P, _P]),
+    "bp_rigid_solve_joints": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32, _P, _P, C.c_uint32, _P, C.c_uint32, C.c_float,
+                                        C.c_uint32, C.c_uint32, _P, _P]),
+    "bp_rigid_finish": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32, C.POINTER(C.c_float), _P, _P]),
 }
 EXPORTED_SYMBOLS = tuple(_SIGNATURES)
 

@@ -17,7 +17,8 @@ PACKAGE_DIR = Path(__file__).resolve().parent
 CSRC = PACKAGE_DIR / "csrc"
 BUILD_DIR = PACKAGE_DIR / "_build"
 LIBRARY = PACKAGE_DIR / "libbubblephysics_gb300.so"
-SOURCES = ["bp_step.cu", "bp_noalloc.cu", "bp_capi.cu", "bp_aux.cu", "bp_server.cu", "bp_contour.cu", "bp_sensor.cu", "bp_events.cu"]
+SOURCES = ["bp_step.cu", "bp_noalloc.cu", "bp_capi.cu", "bp_aux.cu", "bp_server.cu", "bp_contour.cu", "bp_sensor.cu", "bp_events.cu",
+           "bp_rigid.cu"]
 # bp_step_variant.cu is compiled once per (kernel, block width, tree) variant: the persistent step kernels are the
 # largest functions of the library and compile in parallel this way.
 VARIANT_SOURCE = "bp_step_variant.cu"

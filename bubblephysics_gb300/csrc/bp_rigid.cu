@@ -1,0 +1,595 @@
+// bp_rigid.cu - the rigid body solver's predict, joint and finish passes on the caller's device arrays.
+//
+// The reference steps rigid bodies once per step, before the bubble substeps (NativeMetalSolver.swift:767-799):
+// nativeRigidPredict (NativePostSolveKernels.metal-source = NPK:66-115), body-pair candidates and CCD, then 8 rounds
+// of {nativeRigidContacts, nativeRigidApplyBodies, nativeSolveJoints, nativeApplyJointBodies, nativeRigidGuardWalls},
+// and nativeRigidFinish (NPK:172-198) after the bubble step. Here:
+//  - predict and finish: one thread per body, like the reference (each body's sweep is independent);
+//  - the joint rounds: ONE launch for all `iterations` rounds, one block of 512 threads. A round is a Jacobi pass:
+//    every joint computes both ends' corrections from the same body state (a thread per joint), then every body adds
+//    its joints' corrections in list order (a thread per body); __syncthreads() separates the two halves, so a round
+//    costs a block barrier instead of two kernel launches with a host-encoded memory barrier between them.
+// Records keep the reference's layouts (bp_rigid_body = NativeRigidBody, 160 B, ...), read as float4 / uint4 words.
+// Arithmetic is FP32 in the reference's operation order (built with -fmad=false). sin and cos are this library's own
+// float functions (sincos_cw), exp the float of the double-precision exp, so the CPU oracle gets the same bits.
+#include <cmath>
+
+#include "bp_device.cuh"
+
+namespace bp {
+
+struct __align__(16) RBody {
+    unsigned long long id, reserved;
+    float4 pose, previous, motion, physical;
+    uint4 ranges, flags, filter;
+    float4 shape, limits;
+};
+struct __align__(16) RJoint {
+    unsigned long long id, reserved;
+    uint4 ends;
+    float4 anchors, parameters, limits, state;
+};
+struct __align__(16) RCorrection {
+    float4 first, second, velocityFirst, velocitySecond;
+};
+struct __align__(16) RWall {
+    long long body, owner;
+    float4 geometry, extra;
+};
+static_assert(sizeof(RBody) == sizeof(bp_rigid_body), "bp_rigid_body layout");
+static_assert(sizeof(RJoint) == sizeof(bp_rigid_joint), "bp_rigid_joint layout");
+static_assert(sizeof(RCorrection) == sizeof(bp_rigid_correction), "bp_rigid_correction layout");
+static_assert(sizeof(RWall) == sizeof(bp_rigid_wall), "bp_rigid_wall layout");
+
+constexpr uint32_t kRigidThreads = 128;
+constexpr uint32_t kJointThreads = 512;
+constexpr size_t kJointCacheBytes = 200u * 1024u;  // per-body rotations + per-joint damping factors in shared memory
+constexpr float kFltEpsilon = 1.1920929e-7f;
+
+__device__ __forceinline__ bool finite4(float4 v) { return isfinite(v.x) && isfinite(v.y) && isfinite(v.z) && isfinite(v.w); }
+
+// sin and cos of a float angle, this library's own: Cody-Waite reduction by pi/2 (pi/2 split into three floats of
+// 8, 11 and 24 bits, so k * C1 and k * C2 are exact for |k| < 8192, |x| < 12867) and the Taylor series of sin and
+// cos on |r| <= pi/4 up to r^11 and r^12 (truncation below 1e-11), by Horner. Plain float operations in a fixed
+// order, so the CPU oracle computes the same bits; within 2 ulp of the exact values on |x| < 12867.
+__device__ __forceinline__ float2 sincos_cw(float x) {
+    if (!isfinite(x)) return f2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
+    const float k = rintf(x * 0x1.45f306p-1f);
+    const float r = ((x - k * 0x1.92p+0f) - k * 0x1.fb6p-12f) - k * -0x1.777a5cp-25f;
+    const float r2 = r * r;
+    const float sr = r + r * r2 * (-0x1.555556p-3f + r2 * (0x1.111112p-7f + r2 * (-0x1.a01a02p-13f +
+                                   r2 * (0x1.71de3ap-19f + r2 * -0x1.ae6456p-26f))));
+    const float cr = 1.0f + r2 * (-0x1.0p-1f + r2 * (0x1.555556p-5f + r2 * (-0x1.6c16c2p-10f +
+                                   r2 * (0x1.a01a02p-16f + r2 * (-0x1.27e4fcp-22f + r2 * 0x1.1eed8ep-29f)))));
+    const int q = (int)k & 3;
+    const float sn = q == 0 ? sr : q == 1 ? cr : q == 2 ? -sr : -cr;
+    const float cs = q == 0 ? cr : q == 1 ? -sr : q == 2 ? -cr : sr;
+    return f2(cs, sn);  // (cos, sin)
+}
+
+// nativeRotate (NativeGeometryKernels.metal-source = NGK:136-138)
+__device__ __forceinline__ float2 rotate_by(float2 p, float angle) {
+    const float2 cs = sincos_cw(angle);
+    return rot_cs(p, cs.x, cs.y);
+}
+
+__device__ __forceinline__ float2 normalized(float2 v) { return dvd(v, len2(v)); }
+
+// nativeClampLinearSpeed / nativeClampAngularSpeed (NGK:151-158)
+__device__ __forceinline__ float2 clamp_linear(float2 v, float limit) {
+    const float speed = len2(v);
+    return limit > 0.0f && speed > limit ? mul(v, limit / speed) : v;
+}
+__device__ __forceinline__ float clamp_angular(float w, float limit) { return limit > 0.0f ? clampf(w, -limit, limit) : w; }
+
+// Metal mix(x, y, t) = x + (y - x) * t, per component of (x, y, angle).
+__device__ __forceinline__ float3 mix3(float3 x, float3 y, float t) {
+    return make_float3(x.x + (y.x - x.x) * t, x.y + (y.y - x.y) * t, x.z + (y.z - x.z) * t);
+}
+
+// nativeCenterCrossing (NGK:583-622): does the point moving from `start` to `end` cross the segment that moves
+// linearly from (pa, pb) to (ca, cb) within the step? The signed area is quadratic in t: both roots are checked,
+// with the along-edge test at each; a collinear motion is checked by the minimum of r(t).(r(t) - edge(t)).
+__device__ bool center_crossing(float2 start, float2 end, float2 pa, float2 pb, float2 ca, float2 cb) {
+    const float2 e0 = sub(pb, pa);
+    const float2 de = sub(sub(cb, ca), e0);
+    const float2 r0 = sub(start, pa);
+    const float2 dr = sub(sub(end, start), sub(ca, pa));
+    const float a = cross2(de, dr), b = cross2(e0, dr) + cross2(de, r0);
+    const float c = cross2(e0, r0);
+    if (a == 0.0f && b == 0.0f && c == 0.0f) {
+        const float q0 = dot2(r0, sub(r0, e0));
+        if (q0 <= 0.0f) return false;
+        const float qa = dot2(dr, sub(dr, de));
+        const float qb = dot2(dr, sub(r0, e0)) + dot2(r0, sub(dr, de));
+        float minimum = fminf(q0, qa + qb + q0);
+        if (qa > 0.0f) {
+            const float t = clampf(-qb / (2.0f * qa), 0.0f, 1.0f);
+            minimum = fminf(minimum, (qa * t + qb) * t + q0);
+        }
+        return minimum <= 0.0f;
+    }
+    float roots[2] = {-1.0f, -1.0f};
+    if (fabsf(a) <= kFltEpsilon * fmaxf(fabsf(b), fabsf(c))) {
+        if (fabsf(b) > kFltMin) roots[0] = -c / b;
+    } else {
+        const float d = b * b - 4.0f * a * c;
+        if (d > 0.0f) {
+            const float q = -0.5f * (b + copysignf(sqrtf(d), b));
+            roots[0] = q / a;
+            roots[1] = fabsf(q) > kFltMin ? c / q : -1.0f;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const float t = roots[k];
+        if (!(t > 0.0f && t < 1.0f)) continue;
+        const float2 edge = add(e0, mul(de, t)), relative = add(r0, mul(dr, t));
+        const float square = dot2(edge, edge), along = dot2(relative, edge);
+        if (square > kFltMin && along >= 0.0f && along <= square) return true;
+    }
+    return false;
+}
+
+// nativeJointExcluded (NGK:254-258), with the partner list bounded by its array.
+__device__ __forceinline__ bool joint_excluded(const uint4* ranges, const unsigned long long* partners,
+                                               uint32_t partnerCount, uint32_t entity, unsigned long long partner) {
+    if (!ranges) return false;
+    const uint4 r = ranges[entity];
+    for (uint32_t i = 0; i < r.w; ++i) {
+        const uint32_t at = r.z + i;
+        if (at >= partnerCount) break;
+        if (partners[at] == partner) return true;
+    }
+    return false;
+}
+
+struct SweepInputs {
+    const float2* verts;
+    const bp_segment* segs;
+    uint32_t segmentCount, entity, partnerCount;
+    const uint4* jointRanges;
+    const unsigned long long* partners;
+};
+
+// The wall normal of a sweep hit: the segment's right normal, turned towards the vertex's start side.
+__device__ __forceinline__ float2 sweep_normal(float2 a, float2 b, float2 startVertex) {
+    const float2 edge = sub(b, a);
+    float2 normal = normalized(f2(edge.y, -edge.x));
+    if (dot2(sub(startVertex, a), normal) < 0.0f) normal = f2(-normal.x, -normal.y);
+    return normal;
+}
+
+// nativeRigidSweepCrossing (NPK:30-63): does the body moved from pose p to pose q cross a segment with a vertex, or
+// does a segment end cross one of its edges? The first hit gives the contact point, normal and the wall's owner.
+__device__ bool sweep_crossing(const RBody& b, float3 p, float3 q, const SweepInputs& in, float2& point,
+                               float2& normal, long long& owner) {
+    const uint32_t first = b.ranges.x, count = b.ranges.y;
+    for (uint32_t j = 0; j < in.segmentCount; ++j) {
+        const bp_segment& wall = in.segs[j];
+        const bool hasOwner = (wall.flags & BP_SEGMENT_HAS_OWNER) != 0u;
+        if ((unsigned long long)wall.owner_id == b.id && hasOwner) continue;
+        if (hasOwner && joint_excluded(in.jointRanges, in.partners, in.partnerCount, in.entity,
+                                       (unsigned long long)wall.owner_id))
+            continue;
+        if (!filter_accepts(make_uint2(b.filter.x, b.filter.y), make_uint2(wall.category, wall.mask))) continue;
+        const float2 wa = f2(wall.a[0], wall.a[1]), wb = f2(wall.b[0], wall.b[1]);
+        for (uint32_t k = 0; k < count; ++k) {
+            const float2 v = in.verts[first + k];
+            const float2 startVertex = add(f2(p.x, p.y), rotate_by(v, p.z));
+            const float2 endVertex = add(f2(q.x, q.y), rotate_by(v, q.z));
+            if (center_crossing(startVertex, endVertex, wa, wb, wa, wb)) {
+                point = closest_point(endVertex, wa, wb);
+                normal = sweep_normal(wa, wb, startVertex);
+                owner = wall.owner_id;
+                return true;
+            }
+            // a segment end must not pass through an edge of the body either
+            const float2 next = in.verts[first + (k + 1u) % count];
+            const float2 ps = add(f2(p.x, p.y), rotate_by(v, p.z)), pe = add(f2(p.x, p.y), rotate_by(next, p.z));
+            const float2 qs = add(f2(q.x, q.y), rotate_by(v, q.z)), qe = add(f2(q.x, q.y), rotate_by(next, q.z));
+            if (center_crossing(wa, wa, ps, pe, qs, qe) || center_crossing(wb, wb, ps, pe, qs, qe)) {
+                point = closest_point(endVertex, wa, wb);
+                normal = sweep_normal(wa, wb, startVertex);
+                owner = wall.owner_id;
+                return true;
+            }
+        }
+    }
+    return false;
+}
+
+__device__ __forceinline__ bool vertex_range_ok(const RBody& b, uint32_t vertexCount) {
+    return b.ranges.y <= vertexCount && b.ranges.x <= vertexCount - b.ranges.y;
+}
+
+// nativeRigidPredict (NPK:66-115)
+__global__ void __launch_bounds__(kRigidThreads) rigid_predict_kernel(RBody* bodies, uint32_t bodyCount, SweepInputs in,
+                                                                    uint32_t vertexCount, uint32_t bubbleCount,
+                                                                    float dt, RWall* walls, uint32_t* safety) {
+    const uint32_t index = blockIdx.x * blockDim.x + threadIdx.x;
+    if (index >= bodyCount) return;
+    RBody b = bodies[index];
+    b.previous.x = b.pose.x; b.previous.y = b.pose.y; b.pose.w = b.pose.z; b.flags.z = 0u;
+    if (b.flags.x) {
+        b.motion.x = 0.0f; b.motion.y = 0.0f; b.motion.z = 0.0f;
+        bodies[index] = b;
+        return;
+    }
+    b.motion.z *= (float)exp((double)(-b.motion.w * dt));
+    const float2 velocity = clamp_linear(f2(b.motion.x, b.motion.y), b.limits.x);
+    b.motion.x = velocity.x; b.motion.y = velocity.y;
+    b.motion.z = clamp_angular(b.motion.z, b.limits.y);
+    const float3 start = make_float3(b.pose.x, b.pose.y, b.pose.z);
+    b.pose.x += b.motion.x * dt; b.pose.y += b.motion.y * dt; b.pose.z += b.motion.z * dt;
+    if (!finite4(b.pose) || !finite4(b.motion)) {
+        atomicOr(safety, BP_RIGID_SAFETY_NONFINITE);
+        bodies[index] = b;
+        return;
+    }
+    if (b.filter.z) {  // a kinematic body follows its path: no damping stop, no wall, no neighbour
+        bodies[index] = b;
+        return;
+    }
+    if (!vertex_range_ok(b, vertexCount)) {
+        atomicOr(safety, BP_RIGID_SAFETY_INVALID);
+        bodies[index] = b;
+        return;
+    }
+    // conservative vertex sweep: the rotation is sampled every 0.05 rad, at most 128 samples
+    const float samples = ceilf(fabsf(b.pose.z - start.z) / 0.05f);
+    const uint32_t steps = samples > 128.0f ? 129u : max(1u, (uint32_t)samples);
+    if (steps > 128u) {
+        atomicOr(safety, BP_RIGID_SAFETY_ROTATION_BUDGET);
+        bodies[index] = b;
+        return;
+    }
+    SweepInputs sweep = in;
+    sweep.entity = bubbleCount + index;
+    const float3 end = make_float3(b.pose.x, b.pose.y, b.pose.z);
+    bool crossed = false;
+    float2 contactPoint = f2(0.0f, 0.0f), contactNormal = f2(0.0f, 0.0f);
+    long long contactOwner = 0;
+    float3 stopPose = start;
+    for (uint32_t sample = 0; sample < steps && !crossed; ++sample) {
+        const float3 p = mix3(start, end, (float)sample / (float)steps);
+        const float3 q = mix3(start, end, (float)(sample + 1u) / (float)steps);
+        crossed = sweep_crossing(b, p, q, sweep, contactPoint, contactNormal, contactOwner);
+        if (!crossed) continue;
+        // stop at the last pose without a crossing (12 bisections between p and q)
+        float3 last = p, hit = q;
+        for (uint32_t bisection = 0; bisection < 12u; ++bisection) {
+            const float3 middle = make_float3(0.5f * (last.x + hit.x), 0.5f * (last.y + hit.y), 0.5f * (last.z + hit.z));
+            float2 pointTmp, normalTmp;
+            long long ownerTmp;
+            if (sweep_crossing(b, p, middle, sweep, pointTmp, normalTmp, ownerTmp)) hit = middle;
+            else last = middle;
+        }
+        stopPose = last;
+    }
+    if (crossed) {
+        const float closing = fmaxf(0.0f, -dot2(f2(b.motion.x, b.motion.y), contactNormal));
+        const float stopped = b.physical.x > 0.0f ? closing / b.physical.x * dt : 0.0f;
+        b.pose.x = stopPose.x; b.pose.y = stopPose.y; b.pose.z = stopPose.z;
+        b.motion.x = 0.0f; b.motion.y = 0.0f; b.motion.z = 0.0f;
+        for (uint32_t j = 0; j < bodyCount; ++j) {
+            if (j != index && bodies[j].flags.x && bodies[j].id == (unsigned long long)contactOwner) {
+                RWall w;
+                w.body = (long long)b.id; w.owner = contactOwner;
+                w.geometry = make_float4(contactNormal.x, contactNormal.y, contactPoint.x, contactPoint.y);
+                w.extra = make_float4(stopped, 0.0f, 0.0f, 0.0f);
+                walls[index] = w;
+                break;
+            }
+        }
+    }
+    bodies[index] = b;
+}
+
+// nativeRigidFinish (NPK:172-198)
+__global__ void __launch_bounds__(kRigidThreads) rigid_finish_kernel(RBody* bodies, uint32_t bodyCount,
+                                                                   const float2* verts, uint32_t vertexCount,
+                                                                   float4 region, uint32_t* safety) {
+    const uint32_t index = blockIdx.x * blockDim.x + threadIdx.x;
+    if (index >= bodyCount) return;
+    RBody b = bodies[index];
+    if (!finite4(b.pose) || !finite4(b.previous) || !finite4(b.motion)) {
+        atomicOr(safety, BP_RIGID_SAFETY_NONFINITE);
+        return;
+    }
+    if (b.flags.x) return;
+    const float2 velocity = clamp_linear(f2(b.motion.x, b.motion.y), b.limits.x);
+    b.motion.x = velocity.x; b.motion.y = velocity.y;
+    b.motion.z = clamp_angular(b.motion.z, b.limits.y);
+    if (!vertex_range_ok(b, vertexCount)) {
+        atomicOr(safety, BP_RIGID_SAFETY_INVALID);
+        return;
+    }
+    float2 low = f2(INFINITY, INFINITY), high = f2(-INFINITY, -INFINITY);
+    for (uint32_t i = 0; i < b.ranges.y; ++i) {
+        const float2 v = add(f2(b.pose.x, b.pose.y), rotate_by(verts[b.ranges.x + i], b.pose.z));
+        low = vmin2(low, v);
+        high = vmax2(high, v);
+    }
+    // the core of a circle or capsule grows by its radius (0 for a polygon)
+    low = f2(low.x - b.shape.y, low.y - b.shape.y);
+    high = f2(high.x + b.shape.y, high.y + b.shape.y);
+    float2 shift = f2(0.0f, 0.0f);
+    const float2 size = f2(region.z - region.x, region.w - region.y);
+    const bool outside = high.x < region.x || high.y < region.y || low.x > region.z || low.y > region.w;
+    if (outside) {
+        if (!b.flags.y) {
+            b.flags.z = 1u;
+        } else {
+            if (high.x < region.x) shift.x = ceilf((region.x - high.x) / size.x) * size.x;
+            if (low.x > region.z) shift.x = -ceilf((low.x - region.z) / size.x) * size.x;
+            if (high.y < region.y) shift.y = ceilf((region.y - high.y) / size.y) * size.y;
+            if (low.y > region.w) shift.y = -ceilf((low.y - region.w) / size.y) * size.y;
+            b.pose.x += shift.x; b.pose.y += shift.y;
+            b.previous.x += shift.x; b.previous.y += shift.y;
+            b.flags.z = 2u;
+        }
+    }
+    bodies[index] = b;
+}
+
+// nativeJointEnd (NativeContactKernels.metal-source = NCK:451-464): an end is a world point or a body's anchor,
+// measured from the centre of mass (the anchor frame starts at the geometry origin, previous.zw the centroid).
+struct JointEnd {
+    float2 point, arm, velocity;
+    float inverseMass, inverseInertia, angle, omega;
+};
+
+__device__ __forceinline__ bool joint_end(uint32_t entity, float2 anchor, const RBody* bodies, uint32_t bodyCount,
+                                          uint32_t bubbleCount, const float2* trig, JointEnd& e) {
+    e.point = anchor; e.arm = f2(0.0f, 0.0f); e.velocity = f2(0.0f, 0.0f);
+    e.inverseMass = 0.0f; e.inverseInertia = 0.0f; e.angle = 0.0f; e.omega = 0.0f;
+    if (entity == BP_JOINT_WORLD_END) return true;
+    if (entity < bubbleCount || entity - bubbleCount >= bodyCount) return false;
+    const uint32_t at = entity - bubbleCount;
+    const RBody& b = bodies[at];
+    const float4 pose = b.pose, previous = b.previous, motion = b.motion, physical = b.physical;
+    const float2 cs = trig ? trig[at] : sincos_cw(pose.z);  // (cos, sin) of pose.z, cached per round when it fits
+    e.arm = rot_cs(sub(anchor, f2(previous.z, previous.w)), cs.x, cs.y);
+    e.point = add(f2(pose.x, pose.y), e.arm);
+    e.velocity = f2(motion.x, motion.y);
+    e.omega = motion.z;
+    e.angle = pose.z;
+    e.inverseMass = physical.x;
+    e.inverseInertia = physical.y;
+    return true;
+}
+
+__device__ __forceinline__ float2 perpendicular(float2 v) { return f2(-v.y, v.x); }
+
+// nativeSolveJoints (NCK:468-543): both ends' corrections of one joint from the current state.
+__device__ __forceinline__ float damping_decay(const RJoint& joint, float dt, uint32_t iterationCount) {
+    return (float)exp((double)(-joint.parameters.z * dt / (float)max(iterationCount, 1u)));
+}
+
+__device__ void solve_joint(RJoint& joint, RCorrection& out, const RBody* bodies, uint32_t bodyCount,
+                            uint32_t bubbleCount, float dt, uint32_t iterationCount, const float2* trig,
+                            const float* decays, uint32_t j, uint32_t* safety) {
+    JointEnd a, b;
+    const bool okA =
+        joint_end(joint.ends.x, f2(joint.anchors.x, joint.anchors.y), bodies, bodyCount, bubbleCount, trig, a);
+    const bool okB =
+        joint_end(joint.ends.y, f2(joint.anchors.z, joint.anchors.w), bodies, bodyCount, bubbleCount, trig, b);
+    float2 moveA = f2(0.0f, 0.0f), moveB = f2(0.0f, 0.0f), speedA = f2(0.0f, 0.0f), speedB = f2(0.0f, 0.0f);
+    float turnA = 0.0f, turnB = 0.0f, spinA = 0.0f, spinB = 0.0f;
+    if (!okA || !okB) {
+        atomicOr(safety, BP_RIGID_SAFETY_INVALID);
+        out.first = out.second = out.velocityFirst = out.velocitySecond = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        return;
+    }
+    const float2 pointA = perpendicular(a.arm), pointB = perpendicular(b.arm);
+    const uint32_t kind = joint.ends.z;
+    if (kind == 0u) {
+        const float2 delta = sub(b.point, a.point);
+        const float length = len2(delta);
+        const float2 n = length > 1e-6f ? dvd(delta, length) : f2(1.0f, 0.0f);
+        const float ca = cross2(a.arm, n), cb = cross2(b.arm, n);
+        const float w = a.inverseMass + b.inverseMass + a.inverseInertia * ca * ca + b.inverseInertia * cb * cb;
+        if (w > kFltMin) {
+            // XPBD: compliance / dt^2, lambda accumulated over the step (compliance 0 = rigid distance)
+            const float alpha = joint.parameters.y / (dt * dt);
+            const float lambda = (-(length - joint.parameters.x) - alpha * joint.state.x) / (w + alpha);
+            joint.state.x += lambda;
+            moveA = mul(mul(f2(-n.x, -n.y), a.inverseMass), lambda);
+            turnA = -ca * a.inverseInertia * lambda;
+            moveB = mul(mul(n, b.inverseMass), lambda);
+            turnB = cb * b.inverseInertia * lambda;
+            if (joint.parameters.z > 0.0f) {
+                // damping of the relative velocity along the joint, spread over the iterations (exp(-d dt) a step)
+                const float2 va = add(a.velocity, mul(pointA, a.omega)), vb = add(b.velocity, mul(pointB, b.omega));
+                const float relative = dot2(sub(vb, va), n);
+                const float decay = decays ? decays[j] : damping_decay(joint, dt, iterationCount);
+                const float impulse = -relative * (1.0f - decay) / w;
+                speedA = sub(speedA, mul(mul(n, a.inverseMass), impulse));
+                spinA -= ca * a.inverseInertia * impulse;
+                speedB = add(speedB, mul(mul(n, b.inverseMass), impulse));
+                spinB += cb * b.inverseInertia * impulse;
+            }
+        }
+    } else {
+        // hinge and weld: the two ends meet in a point (2x2 effective mass block)
+        const float weight = a.inverseMass + b.inverseMass;
+        const float k11 = weight + a.inverseInertia * pointA.x * pointA.x + b.inverseInertia * pointB.x * pointB.x;
+        const float k12 = a.inverseInertia * pointA.x * pointA.y + b.inverseInertia * pointB.x * pointB.y;
+        const float k22 = weight + a.inverseInertia * pointA.y * pointA.y + b.inverseInertia * pointB.y * pointB.y;
+        const float determinant = k11 * k22 - k12 * k12;
+        if (determinant > kFltMin) {
+            const float2 gap = sub(b.point, a.point);
+            const float2 impulse = dvd(f2(-(k22 * gap.x - k12 * gap.y), -(-k12 * gap.x + k11 * gap.y)), determinant);
+            moveA = mul(f2(-impulse.x, -impulse.y), a.inverseMass);
+            turnA = -a.inverseInertia * dot2(pointA, impulse);
+            moveB = mul(impulse, b.inverseMass);
+            turnB = b.inverseInertia * dot2(pointB, impulse);
+        }
+        const float inertia = a.inverseInertia + b.inverseInertia;
+        if (inertia > kFltMin) {
+            // relative angle after the point correction: turn of B - turn of A - reference angle
+            const float angle = (b.angle + turnB) - (a.angle + turnA) - joint.parameters.w;
+            float violation = 0.0f;
+            if (kind == 2u) violation = angle;
+            else if (joint.ends.w & 1u)
+                violation = angle < joint.limits.x ? angle - joint.limits.x
+                                                   : (angle > joint.limits.y ? angle - joint.limits.y : 0.0f);
+            if (violation != 0.0f) {
+                const float lambda = -violation / inertia;
+                turnA -= a.inverseInertia * lambda;
+                turnB += b.inverseInertia * lambda;
+            }
+            if (kind == 1u && (joint.ends.w & 2u)) {
+                // motor: towards the target relative angular velocity, total impulse of the step within torque x dt
+                const float relative = (b.omega + turnB / dt) - (a.omega + turnA / dt) - joint.limits.z;
+                const float limit = joint.limits.w * dt;
+                const float total = clampf(joint.state.y - relative / inertia, -limit, limit);
+                const float lambda = total - joint.state.y;
+                joint.state.y = total;
+                spinA -= a.inverseInertia * lambda;
+                spinB += b.inverseInertia * lambda;
+            }
+        }
+    }
+    out.first = make_float4(moveA.x, moveA.y, turnA, 0.0f);
+    out.second = make_float4(moveB.x, moveB.y, turnB, 0.0f);
+    out.velocityFirst = make_float4(moveA.x / dt + speedA.x, moveA.y / dt + speedA.y, turnA / dt + spinA, 0.0f);
+    out.velocitySecond = make_float4(moveB.x / dt + speedB.x, moveB.y / dt + speedB.y, turnB / dt + spinB, 0.0f);
+}
+
+// `iterations` rounds of nativeSolveJoints + nativeApplyJointBodies (NCK:468-562) in one block. With `cached`, the
+// dynamic shared memory holds (cos, sin) of every body's angle (refreshed by the body's own thread when the apply
+// turns it) and every joint's damping factor (constant over the launch): one rotation per body and round instead of
+// two per joint, one exp per joint and launch instead of one per joint and round. Same bits either way.
+__global__ void __launch_bounds__(kJointThreads) rigid_joints_kernel(RBody* bodies, uint32_t bodyCount, RJoint* joints,
+                                                                   uint32_t jointCount, RCorrection* corrections,
+                                                                   const uint2* references, uint32_t referenceCount,
+                                                                   const uint4* jointRanges, uint32_t bubbleCount,
+                                                                   float timeStep, uint32_t iterationCount,
+                                                                   uint32_t iterations, bool cached, uint32_t* safety) {
+    extern __shared__ float2 g_rigid_cache[];
+    const float dt = fmaxf(timeStep, 1e-6f);
+    float2* trig = cached ? g_rigid_cache : nullptr;
+    float* decays = cached ? reinterpret_cast<float*>(g_rigid_cache + bodyCount) : nullptr;
+    if (cached) {
+        for (uint32_t i = threadIdx.x; i < bodyCount; i += blockDim.x) trig[i] = sincos_cw(bodies[i].pose.z);
+        for (uint32_t j = threadIdx.x; j < jointCount; j += blockDim.x) decays[j] = damping_decay(joints[j], dt, iterationCount);
+        __syncthreads();
+    }
+    for (uint32_t round = 0; round < iterations; ++round) {
+        for (uint32_t j = threadIdx.x; j < jointCount; j += blockDim.x) {
+            RJoint joint = joints[j];
+            RCorrection c;
+            solve_joint(joint, c, bodies, bodyCount, bubbleCount, dt, iterationCount, trig, decays, j, safety);
+            corrections[j] = c;
+            joints[j] = joint;
+        }
+        __syncthreads();
+        // each body adds its joints' corrections in list order and averages them (Jacobi without overshoot)
+        for (uint32_t i = threadIdx.x; i < bodyCount; i += blockDim.x) {
+            const uint4 range = jointRanges[bubbleCount + i];
+            if (range.y == 0u) continue;
+            float3 delta = make_float3(0.0f, 0.0f, 0.0f), velocity = make_float3(0.0f, 0.0f, 0.0f);
+            bool ok = true;
+            for (uint32_t r = 0; r < range.y; ++r) {
+                const uint32_t at = range.x + r;
+                if (at >= referenceCount || references[at].x >= jointCount) { ok = false; break; }
+                const uint2 ref = references[at];
+                const RCorrection& c = corrections[ref.x];
+                const float4 d = ref.y ? c.second : c.first, v = ref.y ? c.velocitySecond : c.velocityFirst;
+                delta.x += d.x; delta.y += d.y; delta.z += d.z;
+                velocity.x += v.x; velocity.y += v.y; velocity.z += v.z;
+            }
+            if (!ok) {
+                atomicOr(safety, BP_RIGID_SAFETY_INVALID);
+                continue;
+            }
+            const float relax = 1.0f / (float)range.y;
+            float4 pose = bodies[i].pose, motion = bodies[i].motion;
+            pose.x += delta.x * relax; pose.y += delta.y * relax; pose.z += delta.z * relax;
+            motion.x += velocity.x * relax; motion.y += velocity.y * relax; motion.z += velocity.z * relax;
+            bodies[i].pose = pose;
+            bodies[i].motion = motion;
+            if (trig) trig[i] = sincos_cw(pose.z);
+        }
+        __syncthreads();
+    }
+}
+
+static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0u; }
+static bool aligned8(const void* p) { return ((uintptr_t)p & 7u) == 0u; }
+
+static int launch_status() { return cudaGetLastError() == cudaSuccess ? BP_OK : BP_E_CUDA; }
+
+}  // namespace bp
+
+extern "C" int bp_rigid_predict(bp_rigid_body* bodies, uint32_t body_count, const float* vertices_xy,
+                                uint32_t vertex_count, const bp_segment* segments, uint32_t segment_count,
+                                uint32_t bubble_count, float time_step, const uint32_t* joint_ranges,
+                                const uint64_t* joint_partners, uint32_t partner_count, bp_rigid_wall* walls,
+                                uint32_t* safety, void* stream) {
+    using namespace bp;
+    if (body_count == 0) return BP_OK;
+    if (!bodies || !walls || !safety || (!vertices_xy && vertex_count) || (!segments && segment_count) ||
+        (!joint_partners && partner_count))
+        return BP_E_INVALID;
+    if (!aligned16(bodies) || !aligned16(walls) || !aligned16(joint_ranges) || !aligned16(segments) ||
+        !aligned8(vertices_xy) || !aligned8(joint_partners))
+        return BP_E_INVALID;
+    if (!isfinite(time_step)) return BP_E_INVALID;
+    SweepInputs in;
+    in.verts = reinterpret_cast<const float2*>(vertices_xy);
+    in.segs = segments;
+    in.segmentCount = segment_count;
+    in.entity = 0;
+    in.partnerCount = joint_ranges ? partner_count : 0u;
+    in.jointRanges = reinterpret_cast<const uint4*>(joint_ranges);
+    in.partners = reinterpret_cast<const unsigned long long*>(joint_partners);
+    const uint32_t blocks = (body_count + kRigidThreads - 1u) / kRigidThreads;
+    rigid_predict_kernel<<<blocks, kRigidThreads, 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<RBody*>(bodies), body_count, in, vertex_count, bubble_count, time_step,
+        reinterpret_cast<RWall*>(walls), safety);
+    return launch_status();
+}
+
+extern "C" int bp_rigid_solve_joints(bp_rigid_body* bodies, uint32_t body_count, bp_rigid_joint* joints,
+                                     uint32_t joint_count, bp_rigid_correction* corrections,
+                                     const uint32_t* references, uint32_t reference_count,
+                                     const uint32_t* joint_ranges, uint32_t bubble_count, float time_step,
+                                     uint32_t iteration_count, uint32_t iterations, uint32_t* safety, void* stream) {
+    using namespace bp;
+    if (joint_count == 0 || iterations == 0) return BP_OK;
+    if (!bodies || !joints || !corrections || !joint_ranges || !safety || (!references && reference_count))
+        return BP_E_INVALID;
+    if (!aligned16(bodies) || !aligned16(joints) || !aligned16(corrections) || !aligned16(joint_ranges) ||
+        !aligned8(references))
+        return BP_E_INVALID;
+    if (!isfinite(time_step)) return BP_E_INVALID;
+    const size_t cacheBytes = (size_t)body_count * sizeof(float2) + (size_t)joint_count * sizeof(float);
+    const bool cached = cacheBytes <= kJointCacheBytes;
+    if (cached && cacheBytes > 48u * 1024u &&
+        cudaFuncSetAttribute(rigid_joints_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kJointCacheBytes) !=
+            cudaSuccess)
+        return BP_E_CUDA;
+    rigid_joints_kernel<<<1, kJointThreads, cached ? cacheBytes : 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<RBody*>(bodies), body_count, reinterpret_cast<RJoint*>(joints), joint_count,
+        reinterpret_cast<RCorrection*>(corrections), reinterpret_cast<const uint2*>(references), reference_count,
+        reinterpret_cast<const uint4*>(joint_ranges), bubble_count, time_step, iteration_count, iterations, cached,
+        safety);
+    return launch_status();
+}
+
+extern "C" int bp_rigid_finish(bp_rigid_body* bodies, uint32_t body_count, const float* vertices_xy,
+                               uint32_t vertex_count, const float* region, uint32_t* safety, void* stream) {
+    using namespace bp;
+    if (body_count == 0) return BP_OK;
+    if (!bodies || !region || !safety || (!vertices_xy && vertex_count)) return BP_E_INVALID;
+    if (!aligned16(bodies) || !aligned8(vertices_xy)) return BP_E_INVALID;
+    const float4 r = make_float4(region[0], region[1], region[2], region[3]);
+    const uint32_t blocks = (body_count + kRigidThreads - 1u) / kRigidThreads;
+    rigid_finish_kernel<<<blocks, kRigidThreads, 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<RBody*>(bodies), body_count, reinterpret_cast<const float2*>(vertices_xy), vertex_count, r,
+        safety);
+    return launch_status();
+}

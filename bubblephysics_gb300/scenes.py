@@ -431,3 +431,155 @@ def batched_worlds(count: int = 4096, seed: int = 3, n_min: int = 16, n_max: int
     sizes = np.exp(rng.uniform(math.log(n_min), math.log(n_max), count)).astype(np.int64)
     take = count if limit is None else min(limit, count)
     return [batched_world(rng, int(sizes[w]), world_index=w, max_bodies=max_bodies) for w in range(take)]
+
+
+# ---- rigid solver worlds -----------------------------------------------------------------------------------------
+
+class RigidScene:
+    """Records of a rigid-solver world: RIGID_BODY_DTYPE bodies, their vertices (local to the centre of mass),
+    SEGMENT_DTYPE static segments, the public joints, the bodies' object ids, the region and the step."""
+
+    def __init__(self, bodies, vertices, segments, joints, region, dt=DT):
+        self.bodies = bodies
+        self.vertices = np.asarray(vertices, np.float32).reshape(-1, 2)
+        self.segments = segments
+        self.joints = joints
+        self.body_ids = [int(i) for i in bodies["id"]]
+        self.region = tuple(float(v) for v in region)
+        self.dt = dt
+
+    def joint_arrays(self, bubble_ids=()):
+        from .rigid import prepare_joints
+        return prepare_joints(self.joints, list(bubble_ids), self.body_ids)
+
+
+def _rigid_body(bid, pose, vertex_offset, vertex_count, inverse_mass, inverse_inertia, radius, *, velocity=(0.0, 0.0),
+                spin=0.0, damping=0.0, static=False, kinematic=False, wrap=False, centroid=(0.0, 0.0),
+                speed_limits=(0.0, 0.0), category=1, mask=0xFFFFFFFF, restitution=0.0, friction=0.5):
+    b = np.zeros(1, N.RIGID_BODY_DTYPE)[0]
+    b["id"] = bid
+    b["pose"] = (pose[0], pose[1], pose[2], pose[2])
+    b["previous"] = (pose[0], pose[1], centroid[0], centroid[1])
+    b["motion"] = (velocity[0], velocity[1], spin, damping)
+    b["physical"] = (0.0 if static or kinematic else inverse_mass, 0.0 if static or kinematic else inverse_inertia,
+                     radius, friction)
+    b["ranges"] = (vertex_offset, vertex_count, 0, 0)
+    b["flags"] = (1 if static else 0, 1 if wrap else 0, 0, np.float32(restitution).view(np.uint32))
+    b["filter"] = (category, mask, 1 if kinematic else 0, 0)
+    b["limits"] = (speed_limits[0], speed_limits[1], 0.0, 0.0)
+    return b
+
+
+def _box(hx, hy, centroid=(0.0, 0.0)):
+    return [(-hx - centroid[0], -hy - centroid[1]), (hx - centroid[0], -hy - centroid[1]),
+            (hx - centroid[0], hy - centroid[1]), (-hx - centroid[0], hy - centroid[1])]
+
+
+def jointed_chains(seed: int = 6, chains: int = 64, links: int = 16, spacing: float = 40.0) -> RigidScene:
+    """Chains of box links hung from world points: every joint kind (hinges with and without limits and motors,
+    soft damped distance joints, welds), random initial swing, some links with a centroid offset, speed limits and
+    angular damping. The chains sit far inside the region and away from the floor segments, so no body meets
+    another body: the reference's body contacts and wall guard do nothing here."""
+    from .rigid import Joint
+    rng = np.random.default_rng(seed)
+    bodies, vertices, joints = [], [], []
+    jid = 1
+    for c in range(chains):
+        ax, ay = (c % 16) * spacing * 2.0, 2000.0 + (c // 16) * spacing * 3.0
+        prev = None
+        for i in range(links):
+            hx, hy = float(rng.uniform(0.8, 1.2)), float(rng.uniform(0.15, 0.3))
+            centroid = (float(rng.uniform(-0.1, 0.1)), 0.0) if rng.random() < 0.2 else (0.0, 0.0)
+            bid = 10_000 + c * links + i
+            mass = 4.0 * hx * hy
+            inertia = mass * ((2 * hx) ** 2 + (2 * hy) ** 2) / 12.0
+            cx = ax + (2 * i + 1) * 1.05 + centroid[0]
+            angle = float(rng.normal(0.0, 0.05))
+            offset = len(vertices)
+            vertices.extend(_box(hx, hy, centroid))
+            limits = (float(rng.choice([0.0, 60.0])), float(rng.choice([0.0, 30.0])))
+            bodies.append(_rigid_body(bid, (cx, ay, angle), offset, 4, 1.0 / mass, 1.0 / inertia,
+                                      math.hypot(hx, hy) + 0.1, velocity=tuple(rng.normal(0.0, 3.0, 2)),
+                                      spin=float(rng.normal(0.0, 1.0)), damping=float(rng.choice([0.0, 0.2])),
+                                      centroid=centroid, speed_limits=limits))
+            # anchors in the link's geometry frame (the centroid is subtracted inside the solver)
+            left, right = (-1.05, 0.0), (1.05, 0.0)
+            if prev is None:
+                kind = ("hinge", "weld", "distance")[c % 3]
+                joints.append(Joint(jid, bid, None, kind, anchor_a=left, anchor_b=(ax, ay), length=0.0,
+                                    softness=1e-4 if kind == "distance" else 0.0,
+                                    damping=2.0 if kind == "distance" else 0.0,
+                                    limits=(-0.8, 0.8) if c % 6 == 0 else None))
+            else:
+                pick = (c + i) % 7
+                if pick == 3:
+                    joints.append(Joint(jid, prev, bid, "distance", anchor_a=(1.05, 0.0), anchor_b=left,
+                                        length=0.05, softness=float(rng.choice([0.0, 1e-3])), damping=1.5))
+                elif pick == 5:
+                    joints.append(Joint(jid, prev, bid, "weld", anchor_a=(1.05, 0.0), anchor_b=left,
+                                        reference_angle=float(rng.normal(0.0, 0.1))))
+                else:
+                    joints.append(Joint(jid, prev, bid, "hinge", anchor_a=(1.05, 0.0), anchor_b=left,
+                                        limits=(-0.5, 0.5) if pick == 1 else None,
+                                        motor=(2.0, 50.0) if pick == 2 else None))
+            jid += 1
+            prev = bid
+    floor = polygon_edges([(-1000.0, -100.0), (4000.0, -100.0), (4000.0, -90.0), (-1000.0, -90.0)], 1_000_000)
+    order = np.argsort([int(b["id"]) for b in bodies], kind="stable")
+    return RigidScene(np.array([bodies[k] for k in order], N.RIGID_BODY_DTYPE), vertices, floor, joints,
+                      (-2000.0, -2000.0, 6000.0, 6000.0))
+
+
+def rigid_sweeps(seed: int = 7, movers: int = 96) -> RigidScene:
+    """Dynamic bodies flung at thin static walls within one step: the predict sweep stops them before the wall
+    (fast spins sample the rotation; one spin is over the 128-sample budget), kinematic bodies pass through,
+    filtered bodies and bodies joined to a wall's owner without collideConnected ignore it; walls owned by static
+    bodies leave a wall record. Some bodies start outside the region (removed or wrapped by the finish)."""
+    from .rigid import Joint
+    rng = np.random.default_rng(seed)
+    bodies, vertices, segments, joints = [], [], [], []
+    region = (0.0, 0.0, 1200.0, 1200.0)
+    walls = []
+    for w in range(6):
+        x0, y0 = 100.0 + 180.0 * w, 100.0
+        owner = 500 + w
+        pts = [(x0, y0), (x0 + 4.0, y0), (x0 + 4.0, y0 + 900.0), (x0, y0 + 900.0)]
+        offset = len(vertices)
+        vertices.extend([(px - x0 - 2.0, py - y0 - 450.0) for px, py in pts])
+        bodies.append(_rigid_body(owner, (x0 + 2.0, y0 + 450.0, 0.0), offset, 4, 0.0, 0.0, 451.0, static=True))
+        segs = polygon_edges(pts, 100_000 + 10 * w, owner_id=owner if w % 3 else None)
+        segments.extend(segs)
+        walls.append((x0, owner))
+    bid = 1000
+    for m in range(movers):
+        w = m % len(walls)
+        x0, owner = walls[w]
+        hx, hy = float(rng.uniform(2.0, 6.0)), float(rng.uniform(2.0, 6.0))
+        mass = 4.0 * hx * hy
+        inertia = mass * ((2 * hx) ** 2 + (2 * hy) ** 2) / 12.0
+        side = -1.0 if m % 2 else 1.0
+        start = (x0 + 2.0 - side * float(rng.uniform(10.0, 40.0)), float(rng.uniform(150.0, 950.0)))
+        speed = float(rng.uniform(2000.0, 6000.0)) * side
+        spin = float(rng.choice([0.0, rng.normal(0.0, 20.0), rng.normal(0.0, 150.0)]))
+        if m == 7:
+            spin = 450.0  # 7.5 rad in one step: over the 128-sample budget
+        kinematic = m % 11 == 4
+        category, mask = (2, 2) if m % 13 == 6 else (1, 0xFFFFFFFF)
+        offset = len(vertices)
+        vertices.extend(_box(hx, hy))
+        bodies.append(_rigid_body(bid, (start[0], start[1], float(rng.uniform(-3, 3))), offset, 4, 1.0 / mass,
+                                  1.0 / inertia, math.hypot(hx, hy), velocity=(speed, float(rng.normal(0, 200.0))),
+                                  spin=spin, damping=float(rng.choice([0.0, 0.5])), kinematic=kinematic,
+                                  category=category, mask=mask))
+        if m % 17 == 9:  # joined to the wall's owner without collideConnected: that wall is transparent
+            joints.append(Joint(len(joints) + 1, bid, owner, "distance", length=500.0, softness=1.0))
+        bid += 1
+    for k in range(8):  # outside the region: wrapped or removed by the finish
+        offset = len(vertices)
+        vertices.extend(_box(3.0, 3.0))
+        pos = [(-50.0, 600.0), (1300.0, 600.0), (600.0, -40.0), (600.0, 1290.0)][k % 4]
+        bodies.append(_rigid_body(bid, (pos[0], pos[1], 0.3 * k), offset, 4, 1.0 / 36.0, 1.0 / 216.0, 4.3,
+                                  velocity=(0.0, 0.0), wrap=k % 2 == 0))
+        bid += 1
+    return RigidScene(np.array(bodies, N.RIGID_BODY_DTYPE), vertices, np.array(segments, N.SEGMENT_DTYPE), joints,
+                      region, dt=DT)

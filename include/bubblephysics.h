@@ -9,8 +9,10 @@
  * (Sources/BubblePhysicsPublic/BubbleWorld.swift:270-283, Sources/BubblePhysicsNativeMetal/NativePublicWorld.swift:162-258).
  *
  * Conventions
- *  - Plain C: no torch or CUDA types. Every pointer argument is HOST memory owned by the caller; the library owns
- *    all device memory. Records are plain structs whose sizes are pinned by static asserts in the implementation.
+ *  - Plain C: no torch or CUDA types. Every pointer argument is HOST memory owned by the caller and the library
+ *    owns all device memory, except in the allocation-free step and the rigid solver calls, which take the
+ *    caller's DEVICE pointers. Records are plain structs whose sizes are pinned by static asserts in the
+ *    implementation.
  *  - Bubbles are passed sorted by id (signed 64-bit, strictly increasing), segments sorted by id, like
  *    NativePublicWorld.step sorts them (NativePublicWorld.swift:248-249). Indices in every output refer to that order.
  *  - Every function returns an int status (bp_status). A step that fails publishes nothing: the world keeps the
@@ -555,6 +557,101 @@ int bp_world_read_contact_history(bp_world* world, int64_t* pairs, uint32_t capa
 int bp_world_step_noalloc(const bp_world_desc* desc, bp_bubble* bubbles, uint32_t bubble_count,
                           const bp_segment* segments, uint32_t segment_count, uint32_t steps,
                           bp_step_report* reports, void* stream);
+
+/* ---- rigid body solver: predict, joints, finish -------------------------------------------------------------- */
+
+/* The rigid solver's records, laid out like the reference's so its buffers bind unchanged. Bodies step once per step,
+ * before the bubble substeps (NativeMetalSolver.swift:767-799): predict, body-pair candidates and CCD, then 8
+ * iterations of {body contacts, apply, joints, apply joints, wall guard}; the finish runs after the bubble step.
+ * This library implements predict, the joint pair and the finish; body-pair contacts, CCD and the wall guard
+ * (nativeRigidContacts .. nativeRigidGuardWalls) are not implemented. */
+
+/* One rigid body (NativeRigidBody, NativeRigidPolygonState.swift:25-40 / NativeGeometryKernels:35-41). 160 bytes. */
+typedef struct bp_rigid_body {
+    uint64_t id;
+    uint64_t reserved0;
+    float pose[4];               /* centre of mass x, y, angle, angle at the start of the step */
+    float previous[4];           /* centre of mass x, y at the start of the step; local centroid x, y */
+    float motion[4];             /* velocity x, y, angular velocity, angular damping */
+    float physical[4];           /* inverse mass, inverse moment of inertia, bounding radius, friction */
+    uint32_t ranges[4];          /* vertex offset, vertex count, convex triangle offset, triangle count */
+    uint32_t flags[4];           /* static, wraps at the region, region result (set here: 1 removed, 2 wrapped),
+                                    restitution (float bits) */
+    uint32_t filter[4];          /* category, mask, kinematic, layer */
+    float shape[4];              /* core kind (0 polygon, 1 circle, 2 capsule), core radius, half length, reserved */
+    float limits[4];             /* maximum linear speed, maximum angular speed (0 = none), CCD marker, reserved */
+} bp_rigid_body;
+
+/* One joint (NativeJointRecord, NativeJointState.swift:7-14). Ends are entities: bubbles 0..n-1, then bodies n..;
+ * BP_JOINT_WORLD_END is a world point (always end 0). Kind 0 distance, 1 hinge, 2 weld; flags 1 angle limits,
+ * 2 motor. 96 bytes. */
+#define BP_JOINT_WORLD_END 0xFFFFFFFFu
+typedef struct bp_rigid_joint {
+    uint64_t id;
+    uint64_t reserved0;
+    uint32_t ends[4];            /* end 0, end 1, kind, flags */
+    float anchors[4];            /* anchor of end 0, anchor of end 1 (body-local frame, or a world point) */
+    float parameters[4];         /* length, compliance, damping, reference angle */
+    float limits[4];             /* lower and upper angle, motor target angular velocity, maximum torque */
+    float state[4];              /* accumulated lambda of the step: distance, motor; two reserved */
+} bp_rigid_joint;
+
+/* Per-joint correction of the two ends (NativeRigidCorrection): pose delta and velocity delta. 64 bytes. */
+typedef struct bp_rigid_correction {
+    float first[4];
+    float second[4];
+    float velocity_first[4];
+    float velocity_second[4];
+} bp_rigid_correction;
+
+/* A body stopped by its sweep against a wall owned by a static body (NativeRigidWall). 48 bytes. */
+typedef struct bp_rigid_wall {
+    int64_t participants[2];     /* body id, owner id of the wall */
+    float geometry[4];           /* normal x, y; contact point x, y */
+    float extra[4];              /* normal momentum stopped by the sweep x dt; three reserved */
+} bp_rigid_wall;
+
+/* Safety bits OR-ed into *safety (the reference's safety word 3). */
+enum {
+    BP_RIGID_SAFETY_NONFINITE = 1u,         /* a pose or motion became non-finite */
+    BP_RIGID_SAFETY_ROTATION_BUDGET = 18u,  /* 2 | 16: a predict sweep needed more than 128 rotation samples */
+    BP_RIGID_SAFETY_INVALID = 256u          /* a record points outside its arrays: that body or joint is skipped
+                                               (no counterpart in the reference, which reads past its buffers) */
+};
+
+/* Every pointer below is a DEVICE pointer owned by the caller; `stream` is a cudaStream_t (NULL = default stream).
+ * The calls queue their work and return; they allocate nothing. `joint_ranges` holds one uint32 quadruple per entity
+ * (bubbles first, then bodies): start and count in `references`, start and count in `joint_partners`;
+ * `references` holds (joint index, side 0 or 1) pairs; `joint_partners` the sorted ids an entity does not collide
+ * with. joint_ranges may be NULL (no joints); otherwise it holds bubble_count + body_count quadruples. Record arrays and
+ * joint_ranges must be 16-byte aligned, vertices, references and partners 8-byte aligned (BP_E_INVALID otherwise). Rotations use the library's own float sin / cos
+ * (Cody-Waite reduction by pi/2, Taylor series on |r| <= pi/4; absolute error below 1e-7 for |angle| <= 1000);
+ * exponentials the float of the double-precision exp of the float argument. */
+
+/* nativeRigidPredict (NativePostSolveKernels:66-115): start-of-step pose, damping and speed limits, integration; a
+ * dynamic body sweeps its vertices against the segments (rotation sampled every 0.05 rad, at most 128 samples) and
+ * stops, after a 12-step bisection, at the last pose without a crossing; a stop at a wall of a static body writes
+ * walls[body]. bubble_count offsets the body entities in joint_ranges. Segments are static within the step. */
+int bp_rigid_predict(bp_rigid_body* bodies, uint32_t body_count, const float* vertices_xy, uint32_t vertex_count,
+                     const bp_segment* segments, uint32_t segment_count, uint32_t bubble_count, float time_step,
+                     const uint32_t* joint_ranges, const uint64_t* joint_partners, uint32_t partner_count,
+                     bp_rigid_wall* walls, uint32_t* safety, void* stream);
+
+/* `iterations` rounds of nativeSolveJoints then nativeApplyJointBodies (NativeContactKernels:446-562) in one launch:
+ * every joint computes both ends' corrections from the same state (XPBD distance with compliance and damping, hinge
+ * with limits and motor, weld), then every body adds its joints' corrections in list order times 1 / count.
+ * iteration_count is the solver's iteration count per step (the damping is spread over it); a caller that
+ * interleaves other work calls this with iterations = 1 each time. */
+int bp_rigid_solve_joints(bp_rigid_body* bodies, uint32_t body_count, bp_rigid_joint* joints, uint32_t joint_count,
+                          bp_rigid_correction* corrections, const uint32_t* references, uint32_t reference_count,
+                          const uint32_t* joint_ranges, uint32_t bubble_count, float time_step,
+                          uint32_t iteration_count, uint32_t iterations, uint32_t* safety, void* stream);
+
+/* nativeRigidFinish (NativePostSolveKernels:172-198): non-finite check, speed limits, then the region policy from
+ * the body's bounds (vertices plus core radius): removed (flags[2] = 1) or wrapped by whole region spans
+ * (flags[2] = 2). region = (min x, min y, max x, max y), read on the host at the call. */
+int bp_rigid_finish(bp_rigid_body* bodies, uint32_t body_count, const float* vertices_xy, uint32_t vertex_count,
+                    const float* region, uint32_t* safety, void* stream);
 
 /* ---- host helpers (reference host logic that feeds the path) -------------------------------------------------- */
 

@@ -2065,3 +2065,437 @@ int bpo_contact_law(uint32_t mode, int precision, const double* in, double* out,
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------------------------------
+// Rigid body solver: predict (NPK:66-115), joints (NCK:446-562) and finish (NPK:172-198), scalar float, one body or
+// joint after the other. sin and cos are the library's own float functions (sincos_cw), exp the float of the
+// double-precision exp of the float argument.
+// ---------------------------------------------------------------------------------------------------------------
+namespace rigid {
+
+const float kMin = std::numeric_limits<float>::min();
+const float kEps = std::numeric_limits<float>::epsilon();
+
+struct P2 { float x, y; };
+inline P2 p2(float x, float y) { return P2{x, y}; }
+inline P2 operator+(P2 a, P2 b) { return p2(a.x + b.x, a.y + b.y); }
+inline P2 operator-(P2 a, P2 b) { return p2(a.x - b.x, a.y - b.y); }
+inline P2 operator*(P2 a, float s) { return p2(a.x * s, a.y * s); }
+inline P2 operator/(P2 a, float s) { return p2(a.x / s, a.y / s); }
+inline P2 neg(P2 a) { return p2(-a.x, -a.y); }
+inline float dot(P2 a, P2 b) { return a.x * b.x + a.y * b.y; }
+inline float cross(P2 a, P2 b) { return a.x * b.y - a.y * b.x; }
+inline float length(P2 a) { return std::sqrt(a.x * a.x + a.y * a.y); }
+inline float clampf(float v, float lo, float hi) { return std::fmin(std::fmax(v, lo), hi); }
+
+// The library's float sin / cos: Cody-Waite reduction by pi/2 in three float parts (1.5703125, 11 and 24 more
+// bits), Taylor series of sin and cos on |r| <= pi/4 to r^11 / r^12, Horner; (cos, sin) of x.
+inline P2 sincos_cw(float x) {
+    if (!std::isfinite(x)) return p2(std::numeric_limits<float>::quiet_NaN(), std::numeric_limits<float>::quiet_NaN());
+    const float k = std::rint(x * 0x1.45f306p-1f);
+    const float r = ((x - k * 0x1.92p+0f) - k * 0x1.fb6p-12f) - k * -0x1.777a5cp-25f;
+    const float r2 = r * r;
+    const float sr = r + r * r2 * (-0x1.555556p-3f + r2 * (0x1.111112p-7f + r2 * (-0x1.a01a02p-13f +
+                                   r2 * (0x1.71de3ap-19f + r2 * -0x1.ae6456p-26f))));
+    const float cr = 1.0f + r2 * (-0x1.0p-1f + r2 * (0x1.555556p-5f + r2 * (-0x1.6c16c2p-10f +
+                                   r2 * (0x1.a01a02p-16f + r2 * (-0x1.27e4fcp-22f + r2 * 0x1.1eed8ep-29f)))));
+    const int q = (int)k & 3;
+    const float sn = q == 0 ? sr : q == 1 ? cr : q == 2 ? -sr : -cr;
+    const float cs = q == 0 ? cr : q == 1 ? -sr : q == 2 ? -cr : sr;
+    return p2(cs, sn);
+}
+
+// nativeRotate (NGK:136-138)
+inline P2 rotate(P2 p, float angle) {
+    const P2 cs = sincos_cw(angle);
+    return p2(p.x * cs.x - p.y * cs.y, p.x * cs.y + p.y * cs.x);
+}
+// nativeClosestPoint (NGK:436-440)
+inline P2 closest(P2 p, P2 a, P2 b) {
+    const P2 edge = b - a;
+    const float square = dot(edge, edge);
+    return a + edge * (square > kMin ? clampf(dot(p - a, edge) / square, 0.0f, 1.0f) : 0.0f);
+}
+// nativeClampLinearSpeed / nativeClampAngularSpeed (NGK:151-158)
+inline P2 clamp_speed(P2 v, float limit) {
+    const float speed = length(v);
+    return limit > 0 && speed > limit ? v * (limit / speed) : v;
+}
+inline float clamp_spin(float w, float limit) { return limit > 0 ? clampf(w, -limit, limit) : w; }
+inline bool finite4(const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]) && std::isfinite(v[3]); }
+
+// nativeCenterCrossing (NGK:583-622); the segment moves from (pa, pb) to (ca, cb).
+bool center_crossing(P2 start, P2 end, P2 pa, P2 pb, P2 ca, P2 cb) {
+    const P2 e0 = pb - pa, de = (cb - ca) - e0, r0 = start - pa, dr = (end - start) - (ca - pa);
+    const float a = cross(de, dr), b = cross(e0, dr) + cross(de, r0), c = cross(e0, r0);
+    if (a == 0 && b == 0 && c == 0) {
+        const float q0 = dot(r0, r0 - e0);
+        if (q0 <= 0) return false;
+        const float qa = dot(dr, dr - de);
+        const float qb = dot(dr, r0 - e0) + dot(r0, dr - de);
+        float minimum = std::fmin(q0, qa + qb + q0);
+        if (qa > 0) {
+            const float t = clampf(-qb / (2 * qa), 0.0f, 1.0f);
+            minimum = std::fmin(minimum, (qa * t + qb) * t + q0);
+        }
+        return minimum <= 0;
+    }
+    float roots[2] = {-1, -1};
+    if (std::fabs(a) <= kEps * std::fmax(std::fabs(b), std::fabs(c))) {
+        if (std::fabs(b) > kMin) roots[0] = -c / b;
+    } else {
+        const float d = b * b - 4 * a * c;
+        if (d > 0) {
+            const float q = -0.5f * (b + std::copysign(std::sqrt(d), b));
+            roots[0] = q / a;
+            roots[1] = std::fabs(q) > kMin ? c / q : -1;
+        }
+    }
+    for (int k = 0; k < 2; ++k) {
+        const float t = roots[k];
+        if (!(t > 0 && t < 1)) continue;
+        const P2 edge = e0 + de * t, relative = r0 + dr * t;
+        const float square = dot(edge, edge), along = dot(relative, edge);
+        if (square > kMin && along >= 0 && along <= square) return true;
+    }
+    return false;
+}
+
+// nativeJointExcluded (NGK:254-258)
+bool excluded(const uint32_t* ranges, const uint64_t* partners, uint32_t partnerCount, uint32_t entity, uint64_t partner) {
+    if (!ranges) return false;
+    const uint32_t* r = ranges + 4 * (size_t)entity;
+    for (uint32_t i = 0; i < r[3]; ++i) {
+        if (r[2] + i >= partnerCount) break;
+        if (partners[r[2] + i] == partner) return true;
+    }
+    return false;
+}
+
+struct Pose { float x, y, a; };
+inline Pose lerp(Pose s, Pose e, float t) { return Pose{s.x + (e.x - s.x) * t, s.y + (e.y - s.y) * t, s.a + (e.a - s.a) * t}; }
+
+struct Sweep {
+    const float* verts;
+    const bp_segment* segs;
+    uint32_t segmentCount, entity, partnerCount;
+    const uint32_t* ranges;
+    const uint64_t* partners;
+};
+
+P2 hit_normal(P2 a, P2 b, P2 startVertex) {
+    const P2 edge = b - a;
+    const P2 raw = p2(edge.y, -edge.x);
+    P2 n = raw / length(raw);
+    if (dot(startVertex - a, n) < 0) n = neg(n);
+    return n;
+}
+
+// nativeRigidSweepCrossing (NPK:30-63)
+bool sweep_crossing(const bp_rigid_body& b, Pose p, Pose q, const Sweep& in, P2& point, P2& normal, int64_t& owner) {
+    for (uint32_t j = 0; j < in.segmentCount; ++j) {
+        const bp_segment& wall = in.segs[j];
+        const bool hasOwner = (wall.flags & BP_SEGMENT_HAS_OWNER) != 0;
+        if ((uint64_t)wall.owner_id == b.id && hasOwner) continue;
+        if (hasOwner && excluded(in.ranges, in.partners, in.partnerCount, in.entity, (uint64_t)wall.owner_id)) continue;
+        if (!((b.filter[0] & wall.mask) != 0 && (wall.category & b.filter[1]) != 0)) continue;
+        const P2 A = p2(wall.a[0], wall.a[1]), B = p2(wall.b[0], wall.b[1]);
+        const uint32_t n = b.ranges[1];
+        for (uint32_t k = 0; k < n; ++k) {
+            const P2 v = p2(in.verts[2 * (b.ranges[0] + k)], in.verts[2 * (b.ranges[0] + k) + 1]);
+            const P2 sv = p2(p.x, p.y) + rotate(v, p.a), ev = p2(q.x, q.y) + rotate(v, q.a);
+            bool hit = center_crossing(sv, ev, A, B, A, B);
+            if (!hit) {
+                const uint32_t nk = b.ranges[0] + (k + 1) % n;
+                const P2 w = p2(in.verts[2 * nk], in.verts[2 * nk + 1]);
+                const P2 ps = p2(p.x, p.y) + rotate(v, p.a), pe = p2(p.x, p.y) + rotate(w, p.a);
+                const P2 qs = p2(q.x, q.y) + rotate(v, q.a), qe = p2(q.x, q.y) + rotate(w, q.a);
+                hit = center_crossing(A, A, ps, pe, qs, qe) || center_crossing(B, B, ps, pe, qs, qe);
+            }
+            if (hit) {
+                point = closest(ev, A, B);
+                normal = hit_normal(A, B, sv);
+                owner = wall.owner_id;
+                return true;
+            }
+        }
+    }
+    return false;
+}
+
+bool vertices_ok(const bp_rigid_body& b, uint32_t vertexCount) {
+    return b.ranges[1] <= vertexCount && b.ranges[0] <= vertexCount - b.ranges[1];
+}
+
+// nativeRigidPredict (NPK:66-115)
+void predict(bp_rigid_body* bodies, uint32_t count, const Sweep& base, uint32_t vertexCount, uint32_t bubbleCount,
+             float dt, bp_rigid_wall* walls, uint32_t* safety) {
+    for (uint32_t index = 0; index < count; ++index) {
+        bp_rigid_body b = bodies[index];
+        b.previous[0] = b.pose[0]; b.previous[1] = b.pose[1]; b.pose[3] = b.pose[2]; b.flags[2] = 0;
+        if (b.flags[0]) {
+            b.motion[0] = b.motion[1] = b.motion[2] = 0;
+            bodies[index] = b;
+            continue;
+        }
+        b.motion[2] = b.motion[2] * (float)std::exp((double)(-b.motion[3] * dt));
+        const P2 v = clamp_speed(p2(b.motion[0], b.motion[1]), b.limits[0]);
+        b.motion[0] = v.x; b.motion[1] = v.y;
+        b.motion[2] = clamp_spin(b.motion[2], b.limits[1]);
+        const Pose start{b.pose[0], b.pose[1], b.pose[2]};
+        b.pose[0] = b.pose[0] + b.motion[0] * dt;
+        b.pose[1] = b.pose[1] + b.motion[1] * dt;
+        b.pose[2] = b.pose[2] + b.motion[2] * dt;
+        if (!finite4(b.pose) || !finite4(b.motion)) { *safety |= BP_RIGID_SAFETY_NONFINITE; bodies[index] = b; continue; }
+        if (b.filter[2]) { bodies[index] = b; continue; }
+        if (!vertices_ok(b, vertexCount)) { *safety |= BP_RIGID_SAFETY_INVALID; bodies[index] = b; continue; }
+        const float samples = std::ceil(std::fabs(b.pose[2] - start.a) / 0.05f);
+        const uint32_t steps = samples > 128.0f ? 129u : std::max(1u, (uint32_t)samples);
+        if (steps > 128) { *safety |= BP_RIGID_SAFETY_ROTATION_BUDGET; bodies[index] = b; continue; }
+        Sweep in = base;
+        in.entity = bubbleCount + index;
+        const Pose end{b.pose[0], b.pose[1], b.pose[2]};
+        bool crossed = false;
+        P2 point = p2(0, 0), normal = p2(0, 0);
+        int64_t owner = 0;
+        Pose stop = start;
+        for (uint32_t sample = 0; sample < steps && !crossed; ++sample) {
+            const Pose p = lerp(start, end, (float)sample / (float)steps);
+            const Pose q = lerp(start, end, (float)(sample + 1) / (float)steps);
+            crossed = sweep_crossing(b, p, q, in, point, normal, owner);
+            if (!crossed) continue;
+            Pose last = p, hit = q;
+            for (int bisection = 0; bisection < 12; ++bisection) {
+                const Pose middle{0.5f * (last.x + hit.x), 0.5f * (last.y + hit.y), 0.5f * (last.a + hit.a)};
+                P2 tp, tn;
+                int64_t to;
+                if (sweep_crossing(b, p, middle, in, tp, tn, to)) hit = middle; else last = middle;
+            }
+            stop = last;
+        }
+        if (crossed) {
+            const float closing = std::fmax(0.0f, -dot(p2(b.motion[0], b.motion[1]), normal));
+            const float stopped = b.physical[0] > 0 ? closing / b.physical[0] * dt : 0.0f;
+            b.pose[0] = stop.x; b.pose[1] = stop.y; b.pose[2] = stop.a;
+            b.motion[0] = b.motion[1] = b.motion[2] = 0;
+            for (uint32_t j = 0; j < count; ++j) {
+                if (j != index && bodies[j].flags[0] && bodies[j].id == (uint64_t)owner) {
+                    bp_rigid_wall w{};
+                    w.participants[0] = (int64_t)b.id; w.participants[1] = owner;
+                    w.geometry[0] = normal.x; w.geometry[1] = normal.y; w.geometry[2] = point.x; w.geometry[3] = point.y;
+                    w.extra[0] = stopped;
+                    walls[index] = w;
+                    break;
+                }
+            }
+        }
+        bodies[index] = b;
+    }
+}
+
+// nativeRigidFinish (NPK:172-198)
+void finish(bp_rigid_body* bodies, uint32_t count, const float* verts, uint32_t vertexCount, const float* region,
+            uint32_t* safety) {
+    for (uint32_t index = 0; index < count; ++index) {
+        bp_rigid_body b = bodies[index];
+        if (!finite4(b.pose) || !finite4(b.previous) || !finite4(b.motion)) { *safety |= BP_RIGID_SAFETY_NONFINITE; continue; }
+        if (b.flags[0]) continue;
+        const P2 v = clamp_speed(p2(b.motion[0], b.motion[1]), b.limits[0]);
+        b.motion[0] = v.x; b.motion[1] = v.y;
+        b.motion[2] = clamp_spin(b.motion[2], b.limits[1]);
+        if (!vertices_ok(b, vertexCount)) { *safety |= BP_RIGID_SAFETY_INVALID; continue; }
+        const float inf = std::numeric_limits<float>::infinity();
+        float lowX = inf, lowY = inf, highX = -inf, highY = -inf;
+        for (uint32_t i = 0; i < b.ranges[1]; ++i) {
+            const uint32_t at = b.ranges[0] + i;
+            const P2 w = p2(b.pose[0], b.pose[1]) + rotate(p2(verts[2 * at], verts[2 * at + 1]), b.pose[2]);
+            lowX = std::fmin(lowX, w.x); lowY = std::fmin(lowY, w.y);
+            highX = std::fmax(highX, w.x); highY = std::fmax(highY, w.y);
+        }
+        lowX = lowX - b.shape[1]; lowY = lowY - b.shape[1];
+        highX = highX + b.shape[1]; highY = highY + b.shape[1];
+        const float sizeX = region[2] - region[0], sizeY = region[3] - region[1];
+        float shiftX = 0, shiftY = 0;
+        if (highX < region[0] || highY < region[1] || lowX > region[2] || lowY > region[3]) {
+            if (!b.flags[1]) {
+                b.flags[2] = 1;
+            } else {
+                if (highX < region[0]) shiftX = std::ceil((region[0] - highX) / sizeX) * sizeX;
+                if (lowX > region[2]) shiftX = -std::ceil((lowX - region[2]) / sizeX) * sizeX;
+                if (highY < region[1]) shiftY = std::ceil((region[1] - highY) / sizeY) * sizeY;
+                if (lowY > region[3]) shiftY = -std::ceil((lowY - region[3]) / sizeY) * sizeY;
+                b.pose[0] = b.pose[0] + shiftX; b.pose[1] = b.pose[1] + shiftY;
+                b.previous[0] = b.previous[0] + shiftX; b.previous[1] = b.previous[1] + shiftY;
+                b.flags[2] = 2;
+            }
+        }
+        bodies[index] = b;
+    }
+}
+
+// nativeJointEnd (NCK:451-464)
+struct End { P2 point, arm, velocity; float im, ii, angle, omega; };
+
+bool end_of(uint32_t entity, P2 anchor, const bp_rigid_body* bodies, uint32_t count, uint32_t bubbleCount, End& e) {
+    e = End{anchor, p2(0, 0), p2(0, 0), 0, 0, 0, 0};
+    if (entity == BP_JOINT_WORLD_END) return true;
+    if (entity < bubbleCount || entity - bubbleCount >= count) return false;
+    const bp_rigid_body& b = bodies[entity - bubbleCount];
+    e.arm = rotate(anchor - p2(b.previous[2], b.previous[3]), b.pose[2]);
+    e.point = p2(b.pose[0], b.pose[1]) + e.arm;
+    e.velocity = p2(b.motion[0], b.motion[1]);
+    e.omega = b.motion[2];
+    e.angle = b.pose[2];
+    e.im = b.physical[0];
+    e.ii = b.physical[1];
+    return true;
+}
+
+// nativeSolveJoints (NCK:468-543)
+void solve(bp_rigid_joint& joint, bp_rigid_correction& out, const bp_rigid_body* bodies, uint32_t count,
+           uint32_t bubbleCount, float dt, uint32_t iterationCount, uint32_t* safety) {
+    std::memset(&out, 0, sizeof(out));
+    End a, b;
+    const bool okA = end_of(joint.ends[0], p2(joint.anchors[0], joint.anchors[1]), bodies, count, bubbleCount, a);
+    const bool okB = end_of(joint.ends[1], p2(joint.anchors[2], joint.anchors[3]), bodies, count, bubbleCount, b);
+    if (!okA || !okB) { *safety |= BP_RIGID_SAFETY_INVALID; return; }
+    P2 moveA = p2(0, 0), moveB = p2(0, 0), speedA = p2(0, 0), speedB = p2(0, 0);
+    float turnA = 0, turnB = 0, spinA = 0, spinB = 0;
+    const P2 perpA = p2(-a.arm.y, a.arm.x), perpB = p2(-b.arm.y, b.arm.x);
+    const uint32_t kind = joint.ends[2];
+    if (kind == 0) {
+        const P2 delta = b.point - a.point;
+        const float len = length(delta);
+        const P2 n = len > 1e-6f ? delta / len : p2(1, 0);
+        const float ca = cross(a.arm, n), cb = cross(b.arm, n);
+        const float w = a.im + b.im + a.ii * ca * ca + b.ii * cb * cb;
+        if (w > kMin) {
+            const float alpha = joint.parameters[1] / (dt * dt);
+            const float lambda = (-(len - joint.parameters[0]) - alpha * joint.state[0]) / (w + alpha);
+            joint.state[0] = joint.state[0] + lambda;
+            moveA = neg(n) * a.im * lambda;
+            turnA = -ca * a.ii * lambda;
+            moveB = n * b.im * lambda;
+            turnB = cb * b.ii * lambda;
+            if (joint.parameters[2] > 0) {
+                const float relative = dot((b.velocity + perpB * b.omega) - (a.velocity + perpA * a.omega), n);
+                const float decay = (float)std::exp((double)(-joint.parameters[2] * dt / (float)std::max(iterationCount, 1u)));
+                const float impulse = -relative * (1.0f - decay) / w;
+                speedA = speedA - n * a.im * impulse;
+                spinA = spinA - ca * a.ii * impulse;
+                speedB = speedB + n * b.im * impulse;
+                spinB = spinB + cb * b.ii * impulse;
+            }
+        }
+    } else {
+        const float weight = a.im + b.im;
+        const float k11 = weight + a.ii * perpA.x * perpA.x + b.ii * perpB.x * perpB.x;
+        const float k12 = a.ii * perpA.x * perpA.y + b.ii * perpB.x * perpB.y;
+        const float k22 = weight + a.ii * perpA.y * perpA.y + b.ii * perpB.y * perpB.y;
+        const float det = k11 * k22 - k12 * k12;
+        if (det > kMin) {
+            const P2 gap = b.point - a.point;
+            const P2 impulse = p2(-(k22 * gap.x - k12 * gap.y), -(-k12 * gap.x + k11 * gap.y)) / det;
+            moveA = neg(impulse) * a.im;
+            turnA = -a.ii * dot(perpA, impulse);
+            moveB = impulse * b.im;
+            turnB = b.ii * dot(perpB, impulse);
+        }
+        const float inertia = a.ii + b.ii;
+        if (inertia > kMin) {
+            const float angle = (b.angle + turnB) - (a.angle + turnA) - joint.parameters[3];
+            float violation = 0;
+            if (kind == 2) violation = angle;
+            else if (joint.ends[3] & 1u)
+                violation = angle < joint.limits[0] ? angle - joint.limits[0] : (angle > joint.limits[1] ? angle - joint.limits[1] : 0.0f);
+            if (violation != 0) {
+                const float lambda = -violation / inertia;
+                turnA = turnA - a.ii * lambda;
+                turnB = turnB + b.ii * lambda;
+            }
+            if (kind == 1 && (joint.ends[3] & 2u)) {
+                const float relative = (b.omega + turnB / dt) - (a.omega + turnA / dt) - joint.limits[2];
+                const float limit = joint.limits[3] * dt;
+                const float total = clampf(joint.state[1] - relative / inertia, -limit, limit);
+                const float lambda = total - joint.state[1];
+                joint.state[1] = total;
+                spinA = spinA - a.ii * lambda;
+                spinB = spinB + b.ii * lambda;
+            }
+        }
+    }
+    out.first[0] = moveA.x; out.first[1] = moveA.y; out.first[2] = turnA;
+    out.second[0] = moveB.x; out.second[1] = moveB.y; out.second[2] = turnB;
+    out.velocity_first[0] = moveA.x / dt + speedA.x; out.velocity_first[1] = moveA.y / dt + speedA.y;
+    out.velocity_first[2] = turnA / dt + spinA;
+    out.velocity_second[0] = moveB.x / dt + speedB.x; out.velocity_second[1] = moveB.y / dt + speedB.y;
+    out.velocity_second[2] = turnB / dt + spinB;
+}
+
+}  // namespace rigid
+
+extern "C" {
+
+// (cos, sin) pairs of the library's float sin / cos, for the accuracy test against double precision.
+int bpo_sincos(const float* x, float* out, uint32_t count) {
+    for (uint32_t i = 0; i < count; ++i) {
+        const rigid::P2 cs = rigid::sincos_cw(x[i]);
+        out[2 * i] = cs.x;
+        out[2 * i + 1] = cs.y;
+    }
+    return BP_OK;
+}
+
+int bpo_rigid_predict(bp_rigid_body* bodies, uint32_t body_count, const float* vertices_xy, uint32_t vertex_count,
+                      const bp_segment* segments, uint32_t segment_count, uint32_t bubble_count, float time_step,
+                      const uint32_t* joint_ranges, const uint64_t* joint_partners, uint32_t partner_count,
+                      bp_rigid_wall* walls, uint32_t* safety) {
+    rigid::Sweep in{vertices_xy, segments, segment_count, 0, joint_ranges ? partner_count : 0u, joint_ranges, joint_partners};
+    rigid::predict(bodies, body_count, in, vertex_count, bubble_count, time_step, walls, safety);
+    return BP_OK;
+}
+
+// `iterations` Jacobi rounds of nativeSolveJoints (every joint from the same state) then nativeApplyJointBodies
+// (NCK:546-562: each body adds its list's corrections in order, times 1 / count).
+int bpo_rigid_solve_joints(bp_rigid_body* bodies, uint32_t body_count, bp_rigid_joint* joints, uint32_t joint_count,
+                           bp_rigid_correction* corrections, const uint32_t* references, uint32_t reference_count,
+                           const uint32_t* joint_ranges, uint32_t bubble_count, float time_step,
+                           uint32_t iteration_count, uint32_t iterations, uint32_t* safety) {
+    if (joint_count == 0) return BP_OK;
+    const float dt = std::fmax(time_step, 1e-6f);
+    for (uint32_t round = 0; round < iterations; ++round) {
+        for (uint32_t j = 0; j < joint_count; ++j)
+            rigid::solve(joints[j], corrections[j], bodies, body_count, bubble_count, dt, iteration_count, safety);
+        for (uint32_t i = 0; i < body_count; ++i) {
+            const uint32_t* range = joint_ranges + 4 * (size_t)(bubble_count + i);
+            if (range[1] == 0) continue;
+            float delta[3] = {0, 0, 0}, velocity[3] = {0, 0, 0};
+            bool ok = true;
+            for (uint32_t r = 0; r < range[1]; ++r) {
+                const uint32_t at = range[0] + r;
+                if (at >= reference_count || references[2 * at] >= joint_count) { ok = false; break; }
+                const bp_rigid_correction& c = corrections[references[2 * at]];
+                const bool second = references[2 * at + 1] != 0;
+                for (int q = 0; q < 3; ++q) {
+                    delta[q] = delta[q] + (second ? c.second[q] : c.first[q]);
+                    velocity[q] = velocity[q] + (second ? c.velocity_second[q] : c.velocity_first[q]);
+                }
+            }
+            if (!ok) { *safety |= BP_RIGID_SAFETY_INVALID; continue; }
+            const float relax = 1.0f / (float)range[1];
+            for (int q = 0; q < 3; ++q) {
+                bodies[i].pose[q] = bodies[i].pose[q] + delta[q] * relax;
+                bodies[i].motion[q] = bodies[i].motion[q] + velocity[q] * relax;
+            }
+        }
+    }
+    return BP_OK;
+}
+
+int bpo_rigid_finish(bp_rigid_body* bodies, uint32_t body_count, const float* vertices_xy, uint32_t vertex_count,
+                     const float* region, uint32_t* safety) {
+    rigid::finish(bodies, body_count, vertices_xy, vertex_count, region, safety);
+    return BP_OK;
+}
+
+}  // extern "C"

@@ -58,6 +58,12 @@ def library() -> C.CDLL:
             "bpo_contact_law": (C.c_int, [C.c_uint32, C.c_int, P, P, C.c_uint32]),
             "bpo_contact_events": (C.c_int, [P, C.c_uint32, P, P, P, C.c_uint32, P, C.c_uint32, P, C.c_uint32, P,
                                              C.c_uint32, C.c_float, P, C.c_uint32, P, P, P]),
+            "bpo_rigid_predict": (C.c_int, [P, C.c_uint32, P, C.c_uint32, P, C.c_uint32, C.c_uint32, C.c_float, P, P,
+                                            C.c_uint32, P, P]),
+            "bpo_rigid_solve_joints": (C.c_int, [P, C.c_uint32, P, C.c_uint32, P, P, C.c_uint32, P, C.c_uint32,
+                                                 C.c_float, C.c_uint32, C.c_uint32, P]),
+            "bpo_rigid_finish": (C.c_int, [P, C.c_uint32, P, C.c_uint32, P, P]),
+            "bpo_sincos": (C.c_int, [P, P, C.c_uint32]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -243,3 +249,77 @@ def contact_law(mode: int, cases: np.ndarray, precision: int = 32) -> np.ndarray
     out = np.zeros_like(cases)
     library().bpo_contact_law(mode, precision, C.c_void_p(cases.ctypes.data), C.c_void_p(out.ctypes.data), cases.shape[0])
     return out
+
+
+def sincos(x: np.ndarray) -> np.ndarray:
+    """(cos, sin) of float32 angles by the library's own float sin / cos (the oracle's copy)."""
+    x = np.ascontiguousarray(x, np.float32)
+    out = np.zeros((x.size, 2), np.float32)
+    library().bpo_sincos(C.c_void_p(x.ctypes.data), C.c_void_p(out.ctypes.data), x.size)
+    return out
+
+
+class OracleRigid:
+    """The rigid solver passes on host arrays (the oracle of bubblephysics_gb300.rigid.RigidSolver): predict
+    (NPK:66-115), the joint rounds (NCK:446-562) and finish (NPK:172-198), same arguments and record layouts."""
+
+    def __init__(self, bodies, vertices, segments=None, joints=None, bubble_count: int = 0):
+        self.body_records = np.array(bodies, N.RIGID_BODY_DTYPE)
+        self.vertices = np.ascontiguousarray(np.asarray(vertices, np.float32).reshape(-1, 2))
+        self.segments = np.zeros(0, N.SEGMENT_DTYPE) if segments is None else np.array(segments, N.SEGMENT_DTYPE)
+        self.bubble_count = bubble_count
+        if joints is not None and len(joints.records):
+            self.joint_records = np.array(joints.records, N.RIGID_JOINT_DTYPE)
+            self.references = np.ascontiguousarray(joints.references, np.uint32)
+            self.ranges = np.ascontiguousarray(joints.ranges, np.uint32)
+            self.partners = np.ascontiguousarray(joints.partners, np.uint64)
+        else:
+            self.joint_records = np.zeros(0, N.RIGID_JOINT_DTYPE)
+            self.references = np.zeros((0, 2), np.uint32)
+            self.ranges = None
+            self.partners = np.zeros(0, np.uint64)
+        self.corrections = np.zeros(len(self.joint_records), N.RIGID_CORRECTION_DTYPE)
+        self.wall_records = np.zeros(len(self.body_records), N.RIGID_WALL_DTYPE)
+        self.safety_word = np.zeros(1, np.uint32)
+
+    @staticmethod
+    def _p(a):
+        return None if a is None else C.c_void_p(a.ctypes.data)
+
+    def predict(self, dt: float) -> None:
+        self.wall_records[:] = np.zeros(1, N.RIGID_WALL_DTYPE)
+        library().bpo_rigid_predict(self._p(self.body_records), len(self.body_records), self._p(self.vertices),
+                                    self.vertices.shape[0], self._p(self.segments), len(self.segments),
+                                    self.bubble_count, dt, self._p(self.ranges), self._p(self.partners),
+                                    self.partners.size, self._p(self.wall_records), self._p(self.safety_word))
+
+    def solve_joints(self, dt: float, rounds: int = 8, iteration_count: int = 8) -> None:
+        if not len(self.joint_records):
+            return
+        library().bpo_rigid_solve_joints(self._p(self.body_records), len(self.body_records),
+                                         self._p(self.joint_records), len(self.joint_records),
+                                         self._p(self.corrections), self._p(self.references),
+                                         self.references.shape[0], self._p(self.ranges), self.bubble_count, dt,
+                                         iteration_count, rounds, self._p(self.safety_word))
+
+    def finish(self, region) -> None:
+        r = np.asarray(region, np.float32)
+        library().bpo_rigid_finish(self._p(self.body_records), len(self.body_records), self._p(self.vertices),
+                                   self.vertices.shape[0], self._p(r), self._p(self.safety_word))
+
+    def step(self, dt: float, region, iterations: int = 8) -> None:
+        self.predict(dt)
+        self.solve_joints(dt, iterations, iterations)
+        self.finish(region)
+
+    def bodies(self) -> np.ndarray:
+        return self.body_records.copy()
+
+    def joints(self) -> np.ndarray:
+        return self.joint_records.copy()
+
+    def walls(self) -> np.ndarray:
+        return self.wall_records.copy()
+
+    def safety(self) -> int:
+        return int(self.safety_word[0])

@@ -1,0 +1,307 @@
+"""Rigid solver passes on the CPU: the oracle (predict, joint rounds, finish) against an independent numpy float32
+restatement of the joint rounds and the finish, the joint records against the reference's preparation rules
+(NativeJointState.swift:61-141), the library's float sin / cos against double precision, and the physics the
+reference's kernels promise (a sweep stops a body before a thin wall; rigid joints close their gap).
+
+The reference's own tests hold no numbers for these kernels (they run on Metal), so the oracle is pinned by the
+second restatement and by these properties."""
+import numpy as np
+import pytest
+
+from bubblephysics_gb300 import _native as N
+from bubblephysics_gb300 import scenes
+from bubblephysics_gb300.rigid import Joint, prepare_joints
+from oracle.oracle import OracleRigid, sincos
+
+F = np.float32
+
+
+# ---- the library's float sin / cos ---------------------------------------------------------------------------
+
+def np_sincos(x):
+    """numpy float32 restatement of the Cody-Waite / Taylor sin and cos (cos, sin)."""
+    x = np.asarray(x, F)
+    k = np.rint(x * F(float.fromhex("0x1.45f306p-1")))
+    c1, c2, c3 = (F(float.fromhex(h)) for h in ("0x1.92p+0", "0x1.fb6p-12", "-0x1.777a5cp-25"))
+    r = ((x - k * c1) - k * c2) - k * c3
+    r2 = r * r
+    s = [F(float.fromhex(h)) for h in ("-0x1.555556p-3", "0x1.111112p-7", "-0x1.a01a02p-13", "0x1.71de3ap-19",
+                                       "-0x1.ae6456p-26")]
+    c = [F(float.fromhex(h)) for h in ("-0x1.0p-1", "0x1.555556p-5", "-0x1.6c16c2p-10", "0x1.a01a02p-16",
+                                       "-0x1.27e4fcp-22", "0x1.1eed8ep-29")]
+    sr = r + r * r2 * (s[0] + r2 * (s[1] + r2 * (s[2] + r2 * (s[3] + r2 * s[4]))))
+    cr = F(1) + r2 * (c[0] + r2 * (c[1] + r2 * (c[2] + r2 * (c[3] + r2 * (c[4] + r2 * c[5])))))
+    q = k.astype(np.int64) & 3
+    sn = np.select([q == 0, q == 1, q == 2], [sr, cr, -sr], -cr).astype(F)
+    cs = np.select([q == 0, q == 1, q == 2], [cr, -sr, -cr], sr).astype(F)
+    return cs, sn
+
+
+def test_sincos_is_within_the_stated_error_and_matches_its_restatement():
+    rng = np.random.default_rng(3)
+    x = np.concatenate([rng.uniform(-1000, 1000, 200_000), np.arange(-400, 400) * np.pi / 4]).astype(F)
+    got = sincos(x)
+    cs, sn = np_sincos(x)
+    assert np.array_equal(got[:, 0], cs) and np.array_equal(got[:, 1], sn)
+    for k, f in enumerate((np.cos, np.sin)):
+        exact = f(x.astype(np.float64))
+        err = np.abs(got[:, k].astype(np.float64) - exact)
+        assert err.max() < 1e-7
+        big = np.abs(exact) >= 0.25
+        ulp = np.spacing(np.abs(exact[big]).astype(F)).astype(np.float64)
+        assert (err[big] / ulp).max() <= 1.5
+    assert np.isnan(sincos(np.array([np.inf, np.nan], F))).all()
+
+
+# ---- joint records ---------------------------------------------------------------------------------------------
+
+def test_joint_records_follow_the_reference_preparation():
+    bubbles, bodies = [5, 6], [100, 200, 300]
+    joints = [
+        Joint(9, 200, 300, "hinge", anchor_a=(1, 0), anchor_b=(-1, 0), limits=(-1, 1), motor=(2, 3)),
+        Joint(3, 100, None, "distance", anchor_a=(0.5, 0), anchor_b=(7, 8), length=2, softness=0.1, damping=4),
+        Joint(4, 5, 100, "weld"),                           # a bubble end: only the no-collision exclusion stays
+        Joint(5, 100, 999, "weld"),                         # unknown body: dropped
+        Joint(7, 100, 200, "weld", reference_angle=0.25, collide_connected=True),
+        Joint(8, 300, 100, "distance", length=1.0),
+    ]
+    a = prepare_joints(joints, bubbles, bodies)
+    assert a.records["id"].tolist() == [3, 7, 8, 9]          # sorted by id
+    world = a.records[0]
+    assert world["ends"].tolist() == [N.JOINT_WORLD_END, 2, 0, 0]   # the world is end 0, the body end 1
+    assert world["anchors"].tolist() == [7, 8, 0.5, 0]
+    assert a.records[1]["ends"].tolist() == [2, 3, 2, 0] and a.records[1]["parameters"][3] == F(0.25)
+    assert a.records[3]["ends"].tolist() == [3, 4, 1, 3] and a.records[3]["limits"].tolist() == [-1, 1, 2, 3]
+    # body 100 (entity 2): joints 3 (side 1), 7 (side 0), 8 (side 1); partners: bubble 5 and body 300
+    r = a.ranges[2]
+    assert a.references[r[0]:r[0] + r[1]].tolist() == [[0, 1], [1, 0], [2, 1]]
+    assert a.partners[r[2]:r[2] + r[3]].tolist() == [5, 300]
+    assert a.partners[a.ranges[0][2]:a.ranges[0][2] + a.ranges[0][3]].tolist() == [100]   # bubble 5
+    empty = prepare_joints([Joint(4, 5, 100, "weld")], bubbles, bodies)
+    assert len(empty.records) == 0 and not empty.ranges.any() and empty.partners.size == 0
+
+
+# ---- joint rounds: numpy restatement ------------------------------------------------------------------------------
+
+def np_joint_rounds(bodies, joints, refs, ranges, bubble_count, dt, iteration_count, rounds):
+    """Independent float32 restatement of nativeSolveJoints + nativeApplyJointBodies (NCK:446-562), every joint
+    of a round from the same state (vectorised over joints), then each body's list summed in order."""
+    bodies, joints = bodies.copy(), joints.copy()
+    dt = max(F(dt), F(1e-6))
+    ends, anchors, params, lims = joints["ends"], joints["anchors"], joints["parameters"], joints["limits"]
+    kind, flags = ends[:, 2], ends[:, 3]
+    tiny = np.finfo(F).tiny
+    decay = np.exp((-params[:, 2] * dt / F(max(iteration_count, 1))).astype(np.float64)).astype(F)
+
+    def end(e, anchor):
+        world = e == N.JOINT_WORLD_END
+        idx = np.where(world, 0, e.astype(np.int64) - bubble_count)
+        b = bodies[idx]
+        cs, sn = np_sincos(b["pose"][:, 2])
+        lx, ly = anchor[:, 0] - b["previous"][:, 2], anchor[:, 1] - b["previous"][:, 3]
+        ax, ay = lx * cs - ly * sn, lx * sn + ly * cs
+        z = F(0)
+        sel = lambda v, w=z: np.where(world, w, v).astype(F)
+        return dict(px=sel(b["pose"][:, 0] + ax, anchor[:, 0]), py=sel(b["pose"][:, 1] + ay, anchor[:, 1]),
+                    ax=sel(ax), ay=sel(ay), vx=sel(b["motion"][:, 0]), vy=sel(b["motion"][:, 1]),
+                    w=sel(b["motion"][:, 2]), im=sel(b["physical"][:, 0]), ii=sel(b["physical"][:, 1]),
+                    ang=sel(b["pose"][:, 2]))
+
+    for _ in range(rounds):
+        A, B = end(ends[:, 0], anchors[:, :2]), end(ends[:, 1], anchors[:, 2:])
+        n_j = len(joints)
+        mAx, mAy, mBx, mBy, tA, tB = (np.zeros(n_j, F) for _ in range(6))
+        sAx, sAy, sBx, sBy, wA, wB = (np.zeros(n_j, F) for _ in range(6))
+        pAx, pAy, pBx, pBy = -A["ay"], A["ax"], -B["ay"], B["ax"]
+        for j in range(n_j):  # the scalar branches, per joint, in float32
+            a = {k: v[j] for k, v in A.items()}
+            b = {k: v[j] for k, v in B.items()}
+            if kind[j] == 0:
+                dx, dy = b["px"] - a["px"], b["py"] - a["py"]
+                length = np.sqrt(dx * dx + dy * dy)
+                nx, ny = (dx / length, dy / length) if length > F(1e-6) else (F(1), F(0))
+                ca, cb = a["ax"] * ny - a["ay"] * nx, b["ax"] * ny - b["ay"] * nx
+                w = a["im"] + b["im"] + a["ii"] * ca * ca + b["ii"] * cb * cb
+                if w > tiny:
+                    alpha = params[j, 1] / (dt * dt)
+                    lam = (-(length - params[j, 0]) - alpha * joints[j]["state"][0]) / (w + alpha)
+                    joints[j]["state"][0] = joints[j]["state"][0] + lam
+                    mAx[j], mAy[j] = -nx * a["im"] * lam, -ny * a["im"] * lam
+                    tA[j] = -ca * a["ii"] * lam
+                    mBx[j], mBy[j] = nx * b["im"] * lam, ny * b["im"] * lam
+                    tB[j] = cb * b["ii"] * lam
+                    if params[j, 2] > 0:
+                        rvx = (b["vx"] + pBx[j] * b["w"]) - (a["vx"] + pAx[j] * a["w"])
+                        rvy = (b["vy"] + pBy[j] * b["w"]) - (a["vy"] + pAy[j] * a["w"])
+                        rel = rvx * nx + rvy * ny
+                        imp = -rel * (F(1) - decay[j]) / w
+                        sAx[j], sAy[j] = F(0) - nx * a["im"] * imp, F(0) - ny * a["im"] * imp
+                        wA[j] = F(0) - ca * a["ii"] * imp
+                        sBx[j], sBy[j] = F(0) + nx * b["im"] * imp, F(0) + ny * b["im"] * imp
+                        wB[j] = F(0) + cb * b["ii"] * imp
+            else:
+                weight = a["im"] + b["im"]
+                k11 = weight + a["ii"] * pAx[j] * pAx[j] + b["ii"] * pBx[j] * pBx[j]
+                k12 = a["ii"] * pAx[j] * pAy[j] + b["ii"] * pBx[j] * pBy[j]
+                k22 = weight + a["ii"] * pAy[j] * pAy[j] + b["ii"] * pBy[j] * pBy[j]
+                det = k11 * k22 - k12 * k12
+                if det > tiny:
+                    gx, gy = b["px"] - a["px"], b["py"] - a["py"]
+                    ix, iy = -(k22 * gx - k12 * gy) / det, -(-k12 * gx + k11 * gy) / det
+                    mAx[j], mAy[j] = -ix * a["im"], -iy * a["im"]
+                    tA[j] = -a["ii"] * (pAx[j] * ix + pAy[j] * iy)
+                    mBx[j], mBy[j] = ix * b["im"], iy * b["im"]
+                    tB[j] = b["ii"] * (pBx[j] * ix + pBy[j] * iy)
+                inertia = a["ii"] + b["ii"]
+                if inertia > tiny:
+                    ang = (b["ang"] + tB[j]) - (a["ang"] + tA[j]) - params[j, 3]
+                    v = F(0)
+                    if kind[j] == 2:
+                        v = ang
+                    elif flags[j] & 1:
+                        v = ang - lims[j, 0] if ang < lims[j, 0] else (ang - lims[j, 1] if ang > lims[j, 1] else F(0))
+                    if v != 0:
+                        lam = -v / inertia
+                        tA[j], tB[j] = tA[j] - a["ii"] * lam, tB[j] + b["ii"] * lam
+                    if kind[j] == 1 and flags[j] & 2:
+                        rel = (b["w"] + tB[j] / dt) - (a["w"] + tA[j] / dt) - lims[j, 2]
+                        limit = lims[j, 3] * dt
+                        total = min(max(joints[j]["state"][1] - rel / inertia, -limit), limit)
+                        lam = total - joints[j]["state"][1]
+                        joints[j]["state"][1] = total
+                        wA[j], wB[j] = F(0) - a["ii"] * lam, F(0) + b["ii"] * lam
+        first = np.stack([mAx, mAy, tA], 1)
+        second = np.stack([mBx, mBy, tB], 1)
+        vfirst = np.stack([mAx / dt + sAx, mAy / dt + sAy, tA / dt + wA], 1)
+        vsecond = np.stack([mBx / dt + sBx, mBy / dt + sBy, tB / dt + wB], 1)
+        for i in range(len(bodies)):
+            start, count = ranges[bubble_count + i][:2]
+            if count == 0:
+                continue
+            delta, vel = np.zeros(3, F), np.zeros(3, F)
+            for ref in refs[start:start + count]:
+                delta = delta + (second if ref[1] else first)[ref[0]]
+                vel = vel + (vsecond if ref[1] else vfirst)[ref[0]]
+            relax = F(1) / F(count)
+            bodies[i]["pose"][:3] = bodies[i]["pose"][:3] + delta * relax
+            bodies[i]["motion"][:3] = bodies[i]["motion"][:3] + vel * relax
+    return bodies, joints
+
+
+def test_joint_rounds_match_the_numpy_restatement_bit_for_bit():
+    scene = scenes.jointed_chains(seed=11, chains=6, links=6)
+    arrays = scene.joint_arrays()
+    oracle = OracleRigid(scene.bodies, scene.vertices, scene.segments, arrays)
+    for step in range(3):
+        start = oracle.bodies()
+        joints = oracle.joints()
+        joints["state"] = 0  # the host clears the accumulated lambdas each step
+        oracle.joint_records["state"] = 0
+        want_b, want_j = np_joint_rounds(start, joints, arrays.references, arrays.ranges, 0, scene.dt, 8, 8)
+        assert not np.array_equal(want_b["pose"], start["pose"])
+        oracle.solve_joints(scene.dt, 8, 8)
+        assert oracle.safety() == 0
+        assert np.array_equal(oracle.bodies()["pose"], want_b["pose"]), step
+        assert np.array_equal(oracle.bodies()["motion"], want_b["motion"]), step
+        assert np.array_equal(oracle.joints()["state"], want_j["state"]), step
+        oracle.predict(scene.dt)
+
+
+def test_rigid_joints_close_their_gap():
+    """One round of a rigid world hinge on a body without rotation inertia puts the anchor on the world point; a
+    rigid distance joint restores its length; a motor's impulse stays within torque x dt."""
+    body = scenes._rigid_body(1, (3.0, 1.0, 0.0), 0, 4, 1.0, 0.0, 1.0)
+    verts = scenes._box(1.0, 0.5)
+    for kind, length in (("hinge", 0.0), ("distance", 2.0)):
+        arrays = prepare_joints([Joint(1, 1, None, kind, anchor_a=(-1.0, 0.0), anchor_b=(0.0, 0.0), length=length)],
+                                [], [1])
+        o = OracleRigid(np.array([body]), verts, None, arrays)
+        o.solve_joints(1 / 60, 1, 8)
+        p = o.bodies()[0]["pose"]
+        gap = np.hypot(p[0] - 1.0, p[1])
+        assert abs(gap - length) < 1e-6, (kind, gap)
+    spinning = scenes._rigid_body(1, (0.0, 0.0, 0.0), 0, 4, 1.0, 2.0, 1.0, spin=10.0)
+    arrays = prepare_joints([Joint(1, 1, None, "hinge", motor=(0.0, 3.0))], [], [1])
+    o = OracleRigid(np.array([spinning]), verts, None, arrays)
+    o.solve_joints(1 / 60, 8, 8)
+    assert abs(o.joints()[0]["state"][1]) <= F(3.0) * F(1 / 60) * (1 + 1e-6)
+    assert o.bodies()[0]["motion"][2] < 10.0
+
+
+# ---- predict and finish --------------------------------------------------------------------------------------------
+
+def test_predict_stops_bodies_before_thin_walls():
+    scene = scenes.rigid_sweeps()
+    arrays = scene.joint_arrays()
+    o = OracleRigid(scene.bodies, scene.vertices, scene.segments, arrays)
+    before = o.bodies()
+    o.predict(scene.dt)
+    after, walls = o.bodies(), o.walls()
+    assert o.safety() & N.RIGID_SAFETY_ROTATION_BUDGET == N.RIGID_SAFETY_ROTATION_BUDGET
+    excluded_owners = {(j.body_a, j.body_b) for j in scene.joints}
+    wall_x = {500 + w: 100.0 + 180.0 * w for w in range(6)}
+    checked = 0
+    for k, (b0, b1) in enumerate(zip(before, after)):
+        if b0["flags"][0] or b0["id"] < 1000 or b0["id"] >= 1000 + 96:
+            continue
+        m = int(b0["id"]) - 1000
+        owner = 500 + m % 6
+        x0 = wall_x[owner]
+        if b0["filter"][2]:  # kinematic: straight through
+            assert b1["pose"][0] == F(b0["pose"][0] + b0["motion"][0] * F(scene.dt))
+            continue
+        if m == 7 or b0["filter"][0] == 2 or (int(b0["id"]), owner) in excluded_owners:
+            continue
+        verts = scene.vertices[b1["ranges"][0]:b1["ranges"][0] + 4].astype(np.float64)
+        c, s = np.cos(float(b1["pose"][2])), np.sin(float(b1["pose"][2]))
+        xs = b1["pose"][0] + verts[:, 0] * c - verts[:, 1] * s
+        if b0["motion"][0] > 0:
+            assert xs.max() <= x0 + 1e-3, (m, xs.max(), x0)
+        else:
+            assert xs.min() >= x0 + 4.0 - 1e-3, (m, xs.min(), x0)
+        assert not b1["motion"][:3].any()
+        if m % 6 % 3:  # walls with an owner leave a record pointing back to the start side
+            assert walls[k]["participants"].tolist() == [int(b0["id"]), owner]
+            assert np.sign(walls[k]["geometry"][0]) == -np.sign(b0["motion"][0])
+        checked += 1
+    assert checked > 40
+
+
+def np_finish(bodies, verts, region):
+    """Independent restatement of nativeRigidFinish's region policy (NPK:172-198) for bodies at rest."""
+    out = bodies.copy()
+    rx0, ry0, rx1, ry1 = (F(v) for v in region)
+    for b in out:
+        if b["flags"][0]:
+            continue
+        v = verts[b["ranges"][0]:b["ranges"][0] + b["ranges"][1]]
+        cs, sn = np_sincos(np.full(len(v), b["pose"][2], F))
+        xs = b["pose"][0] + (v[:, 0] * cs - v[:, 1] * sn)
+        ys = b["pose"][1] + (v[:, 0] * sn + v[:, 1] * cs)
+        lo = np.array([xs.min(), ys.min()], F) - b["shape"][1]
+        hi = np.array([xs.max(), ys.max()], F) + b["shape"][1]
+        if hi[0] < rx0 or hi[1] < ry0 or lo[0] > rx1 or lo[1] > ry1:
+            if not b["flags"][1]:
+                b["flags"][2] = 1
+            else:
+                size = (rx1 - rx0, ry1 - ry0)
+                shift = np.zeros(2, F)
+                if hi[0] < rx0: shift[0] = np.ceil((rx0 - hi[0]) / size[0]) * size[0]
+                if lo[0] > rx1: shift[0] = -np.ceil((lo[0] - rx1) / size[0]) * size[0]
+                if hi[1] < ry0: shift[1] = np.ceil((ry0 - hi[1]) / size[1]) * size[1]
+                if lo[1] > ry1: shift[1] = -np.ceil((lo[1] - ry1) / size[1]) * size[1]
+                b["pose"][:2] = b["pose"][:2] + shift
+                b["previous"][:2] = b["previous"][:2] + shift
+                b["flags"][2] = 2
+    return out
+
+
+def test_finish_removes_or_wraps_bodies_outside_the_region():
+    scene = scenes.rigid_sweeps()
+    o = OracleRigid(scene.bodies, scene.vertices, scene.segments, None)
+    start = o.bodies()
+    o.finish(scene.region)
+    got = o.bodies()
+    want = np_finish(start, scene.vertices, scene.region)
+    assert np.array_equal(got["pose"], want["pose"]) and np.array_equal(got["flags"], want["flags"])
+    assert (got["flags"][:, 2] == 1).sum() == 4 and (got["flags"][:, 2] == 2).sum() == 4
