@@ -251,7 +251,8 @@ def single_worlds(ctx, steps: int, large_steps: int, rigid_steps: int) -> dict:
 
 def rigid_solver(steps: int = 50, warmup: int = 5, cpu_steps: int = 5) -> dict:
     """The rigid solver passes (bp_rigid_predict, 8 rounds of bp_rigid_solve_joints in one launch, bp_rigid_finish)
-    on jointed chains of box links (every joint kind), at 64 x 32 and 256 x 32 links: device time per step and per
+    on jointed chains of box links (every joint kind), at 8 x 32 links (all rounds in one block), 64 x 32 and 256 x 32
+    links (two grid launches per round): device time per step and per
     pass by CUDA events on the launching stream (the default stream, torch's current one), and the oracle's time per
     step on one host core (the reference runs these passes as one Metal dispatch per kernel and round)."""
     import torch
@@ -259,7 +260,7 @@ def rigid_solver(steps: int = 50, warmup: int = 5, cpu_steps: int = 5) -> dict:
     from bubblephysics_gb300.rigid import ITERATIONS, RigidSolver
     from oracle.oracle import OracleRigid
     out = {}
-    for chains, links in ((64, 32), (256, 32)):
+    for chains, links in ((8, 32), (64, 32), (256, 32)):
         scene = scenes.jointed_chains(seed=6, chains=chains, links=links)
         arrays = scene.joint_arrays()
         solver = RigidSolver(scene.bodies, scene.vertices, scene.segments, arrays)
@@ -288,8 +289,10 @@ def rigid_solver(steps: int = 50, warmup: int = 5, cpu_steps: int = 5) -> dict:
         out[f"chains_{chains}x{links}"] = {
             "bodies": len(scene.bodies), "joints": len(arrays.records), "segments": len(scene.segments),
             "rounds": ITERATIONS, "ms_per_step": step_ms, "passes": passes, "safety": solver.safety(),
-            "launches_per_step": 4, "cpu_oracle_ms_per_step": cpu_ms, "cpu_cores": 1,
+            "launches_per_step": 4 if len(arrays.records) <= 512 else 3 + 2 * ITERATIONS,
+            "cpu_oracle_ms_per_step": cpu_ms, "cpu_cores": 1,
             "note": "a step = the walls clear (a memset) + predict + the joint rounds + finish"}
+        out[f"chains_{chains}x{links}"]["speedup_vs_cpu_oracle"] = cpu_ms / step_ms if step_ms > 0 else None
     return out
 
 

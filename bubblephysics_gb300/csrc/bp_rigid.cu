@@ -5,10 +5,10 @@
 // of {nativeRigidContacts, nativeRigidApplyBodies, nativeSolveJoints, nativeApplyJointBodies, nativeRigidGuardWalls},
 // and nativeRigidFinish (NPK:172-198) after the bubble step. Here:
 //  - predict and finish: one thread per body, like the reference (each body's sweep is independent);
-//  - the joint rounds: ONE launch for all `iterations` rounds, one block of 512 threads. A round is a Jacobi pass:
-//    every joint computes both ends' corrections from the same body state (a thread per joint), then every body adds
-//    its joints' corrections in list order (a thread per body); __syncthreads() separates the two halves, so a round
-//    costs a block barrier instead of two kernel launches with a host-encoded memory barrier between them.
+//  - the joint rounds: a round is a Jacobi pass: every joint computes both ends' corrections from the same body state
+//    (a thread per joint), then every body adds its joints' corrections in list order (a thread per body). A small
+//    world (<= 512 joints, <= 1,024 bodies) runs all rounds in ONE launch of one 512-thread block, the halves
+//    separated by __syncthreads(); a larger one runs two grid launches per round, so all SMs share the work.
 // Records keep the reference's layouts (bp_rigid_body = NativeRigidBody, 160 B, ...), read as float4 / uint4 words.
 // Arithmetic is FP32 in the reference's operation order (built with -fmad=false). sin and cos are this library's own
 // float functions (sincos_cw), exp the float of the double-precision exp, so the CPU oracle gets the same bits.
@@ -42,8 +42,11 @@ static_assert(sizeof(RCorrection) == sizeof(bp_rigid_correction), "bp_rigid_corr
 static_assert(sizeof(RWall) == sizeof(bp_rigid_wall), "bp_rigid_wall layout");
 
 constexpr uint32_t kRigidThreads = 128;
-constexpr uint32_t kJointThreads = 512;
-constexpr size_t kJointCacheBytes = 200u * 1024u;  // per-body rotations + per-joint damping factors in shared memory
+constexpr uint32_t kJointThreads = 512;     // the one block of a small world's joint rounds
+constexpr uint32_t kRoundThreads = 128;     // the grid launches of a larger world's rounds
+// A world with at most this many joints and bodies runs all rounds in one block (its rotation and damping cache is
+// at most 10 KB of shared memory); a larger one runs two grid launches per round.
+constexpr uint32_t kSingleBlockJoints = 512, kSingleBlockBodies = 1024;
 constexpr float kFltEpsilon = 1.1920929e-7f;
 
 __device__ __forceinline__ bool finite4(float4 v) { return isfinite(v.x) && isfinite(v.y) && isfinite(v.z) && isfinite(v.w); }
@@ -458,25 +461,52 @@ __device__ void solve_joint(RJoint& joint, RCorrection& out, const RBody* bodies
     out.velocitySecond = make_float4(moveB.x / dt + speedB.x, moveB.y / dt + speedB.y, turnB / dt + spinB, 0.0f);
 }
 
-// `iterations` rounds of nativeSolveJoints + nativeApplyJointBodies (NCK:468-562) in one block. With `cached`, the
-// dynamic shared memory holds (cos, sin) of every body's angle (refreshed by the body's own thread when the apply
-// turns it) and every joint's damping factor (constant over the launch): one rotation per body and round instead of
-// two per joint, one exp per joint and launch instead of one per joint and round. Same bits either way.
+// nativeApplyJointBodies (NCK:546-562) for body i: the body adds its joints' corrections in list order and averages
+// them (Jacobi without overshoot); `trig`, when given, gets the (cos, sin) of the body's new angle.
+__device__ __forceinline__ void apply_joint_corrections(uint32_t i, RBody* bodies, const RCorrection* corrections,
+                                                        const uint2* references, uint32_t referenceCount,
+                                                        uint32_t jointCount, const uint4* jointRanges,
+                                                        uint32_t bubbleCount, float2* trig, uint32_t* safety) {
+    const uint4 range = jointRanges[bubbleCount + i];
+    if (range.y == 0u) return;
+    float3 delta = make_float3(0.0f, 0.0f, 0.0f), velocity = make_float3(0.0f, 0.0f, 0.0f);
+    for (uint32_t r = 0; r < range.y; ++r) {
+        const uint32_t at = range.x + r;
+        if (at >= referenceCount || references[at].x >= jointCount) {
+            atomicOr(safety, BP_RIGID_SAFETY_INVALID);
+            return;
+        }
+        const uint2 ref = references[at];
+        const RCorrection& c = corrections[ref.x];
+        const float4 d = ref.y ? c.second : c.first, v = ref.y ? c.velocitySecond : c.velocityFirst;
+        delta.x += d.x; delta.y += d.y; delta.z += d.z;
+        velocity.x += v.x; velocity.y += v.y; velocity.z += v.z;
+    }
+    const float relax = 1.0f / (float)range.y;
+    float4 pose = bodies[i].pose, motion = bodies[i].motion;
+    pose.x += delta.x * relax; pose.y += delta.y * relax; pose.z += delta.z * relax;
+    motion.x += velocity.x * relax; motion.y += velocity.y * relax; motion.z += velocity.z * relax;
+    bodies[i].pose = pose;
+    bodies[i].motion = motion;
+    if (trig) trig[i] = sincos_cw(pose.z);
+}
+
+// Small worlds: all `iterations` rounds of nativeSolveJoints + nativeApplyJointBodies (NCK:468-562) in one block,
+// the two halves of a round separated by __syncthreads(). The dynamic shared memory holds (cos, sin) of every body's
+// angle (refreshed by the body's own thread after its apply) and every joint's damping factor (constant over the
+// launch): one rotation per body and round instead of two per joint, one exp per joint and launch.
 __global__ void __launch_bounds__(kJointThreads) rigid_joints_kernel(RBody* bodies, uint32_t bodyCount, RJoint* joints,
                                                                    uint32_t jointCount, RCorrection* corrections,
                                                                    const uint2* references, uint32_t referenceCount,
                                                                    const uint4* jointRanges, uint32_t bubbleCount,
-                                                                   float timeStep, uint32_t iterationCount,
-                                                                   uint32_t iterations, bool cached, uint32_t* safety) {
+                                                                   float dt, uint32_t iterationCount,
+                                                                   uint32_t iterations, uint32_t* safety) {
     extern __shared__ float2 g_rigid_cache[];
-    const float dt = fmaxf(timeStep, 1e-6f);
-    float2* trig = cached ? g_rigid_cache : nullptr;
-    float* decays = cached ? reinterpret_cast<float*>(g_rigid_cache + bodyCount) : nullptr;
-    if (cached) {
-        for (uint32_t i = threadIdx.x; i < bodyCount; i += blockDim.x) trig[i] = sincos_cw(bodies[i].pose.z);
-        for (uint32_t j = threadIdx.x; j < jointCount; j += blockDim.x) decays[j] = damping_decay(joints[j], dt, iterationCount);
-        __syncthreads();
-    }
+    float2* trig = g_rigid_cache;
+    float* decays = reinterpret_cast<float*>(g_rigid_cache + bodyCount);
+    for (uint32_t i = threadIdx.x; i < bodyCount; i += blockDim.x) trig[i] = sincos_cw(bodies[i].pose.z);
+    for (uint32_t j = threadIdx.x; j < jointCount; j += blockDim.x) decays[j] = damping_decay(joints[j], dt, iterationCount);
+    __syncthreads();
     for (uint32_t round = 0; round < iterations; ++round) {
         for (uint32_t j = threadIdx.x; j < jointCount; j += blockDim.x) {
             RJoint joint = joints[j];
@@ -486,35 +516,39 @@ __global__ void __launch_bounds__(kJointThreads) rigid_joints_kernel(RBody* bodi
             joints[j] = joint;
         }
         __syncthreads();
-        // each body adds its joints' corrections in list order and averages them (Jacobi without overshoot)
-        for (uint32_t i = threadIdx.x; i < bodyCount; i += blockDim.x) {
-            const uint4 range = jointRanges[bubbleCount + i];
-            if (range.y == 0u) continue;
-            float3 delta = make_float3(0.0f, 0.0f, 0.0f), velocity = make_float3(0.0f, 0.0f, 0.0f);
-            bool ok = true;
-            for (uint32_t r = 0; r < range.y; ++r) {
-                const uint32_t at = range.x + r;
-                if (at >= referenceCount || references[at].x >= jointCount) { ok = false; break; }
-                const uint2 ref = references[at];
-                const RCorrection& c = corrections[ref.x];
-                const float4 d = ref.y ? c.second : c.first, v = ref.y ? c.velocitySecond : c.velocityFirst;
-                delta.x += d.x; delta.y += d.y; delta.z += d.z;
-                velocity.x += v.x; velocity.y += v.y; velocity.z += v.z;
-            }
-            if (!ok) {
-                atomicOr(safety, BP_RIGID_SAFETY_INVALID);
-                continue;
-            }
-            const float relax = 1.0f / (float)range.y;
-            float4 pose = bodies[i].pose, motion = bodies[i].motion;
-            pose.x += delta.x * relax; pose.y += delta.y * relax; pose.z += delta.z * relax;
-            motion.x += velocity.x * relax; motion.y += velocity.y * relax; motion.z += velocity.z * relax;
-            bodies[i].pose = pose;
-            bodies[i].motion = motion;
-            if (trig) trig[i] = sincos_cw(pose.z);
-        }
+        for (uint32_t i = threadIdx.x; i < bodyCount; i += blockDim.x)
+            apply_joint_corrections(i, bodies, corrections, references, referenceCount, jointCount, jointRanges,
+                                    bubbleCount, trig, safety);
         __syncthreads();
     }
+}
+
+// Larger worlds: one round is two grid launches, a thread per joint, then a thread per body (the launch boundary is
+// the round's barrier), so every SM works on it; rotations and damping factors are computed in place (same bits).
+__global__ void __launch_bounds__(kRoundThreads) rigid_joint_round_kernel(RBody* bodies, uint32_t bodyCount,
+                                                                        RJoint* joints, uint32_t jointCount,
+                                                                        RCorrection* corrections, uint32_t bubbleCount,
+                                                                        float dt, uint32_t iterationCount,
+                                                                        uint32_t* safety) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= jointCount) return;
+    RJoint joint = joints[j];
+    RCorrection c;
+    solve_joint(joint, c, bodies, bodyCount, bubbleCount, dt, iterationCount, nullptr, nullptr, j, safety);
+    corrections[j] = c;
+    joints[j] = joint;
+}
+
+__global__ void __launch_bounds__(kRoundThreads) rigid_apply_round_kernel(RBody* bodies, uint32_t bodyCount,
+                                                                        const RCorrection* corrections,
+                                                                        const uint2* references,
+                                                                        uint32_t referenceCount, uint32_t jointCount,
+                                                                        const uint4* jointRanges, uint32_t bubbleCount,
+                                                                        uint32_t* safety) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= bodyCount) return;
+    apply_joint_corrections(i, bodies, corrections, references, referenceCount, jointCount, jointRanges, bubbleCount,
+                            nullptr, safety);
 }
 
 static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0u; }
@@ -566,17 +600,30 @@ extern "C" int bp_rigid_solve_joints(bp_rigid_body* bodies, uint32_t body_count,
         !aligned8(references))
         return BP_E_INVALID;
     if (!isfinite(time_step)) return BP_E_INVALID;
-    const size_t cacheBytes = (size_t)body_count * sizeof(float2) + (size_t)joint_count * sizeof(float);
-    const bool cached = cacheBytes <= kJointCacheBytes;
-    if (cached && cacheBytes > 48u * 1024u &&
-        cudaFuncSetAttribute(rigid_joints_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kJointCacheBytes) !=
-            cudaSuccess)
-        return BP_E_CUDA;
-    rigid_joints_kernel<<<1, kJointThreads, cached ? cacheBytes : 0, (cudaStream_t)stream>>>(
-        reinterpret_cast<RBody*>(bodies), body_count, reinterpret_cast<RJoint*>(joints), joint_count,
-        reinterpret_cast<RCorrection*>(corrections), reinterpret_cast<const uint2*>(references), reference_count,
-        reinterpret_cast<const uint4*>(joint_ranges), bubble_count, time_step, iteration_count, iterations, cached,
-        safety);
+    const float dt = fmaxf(time_step, 1e-6f);
+    RBody* b = reinterpret_cast<RBody*>(bodies);
+    RJoint* jn = reinterpret_cast<RJoint*>(joints);
+    RCorrection* c = reinterpret_cast<RCorrection*>(corrections);
+    const uint2* refs = reinterpret_cast<const uint2*>(references);
+    const uint4* ranges = reinterpret_cast<const uint4*>(joint_ranges);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (joint_count <= kSingleBlockJoints && body_count <= kSingleBlockBodies) {
+        const size_t cacheBytes = (size_t)body_count * sizeof(float2) + (size_t)joint_count * sizeof(float);
+        rigid_joints_kernel<<<1, kJointThreads, cacheBytes, s>>>(b, body_count, jn, joint_count, c, refs,
+                                                                reference_count, ranges, bubble_count, dt,
+                                                                iteration_count, iterations, safety);
+        return launch_status();
+    }
+    const uint32_t jointBlocks = (joint_count + kRoundThreads - 1u) / kRoundThreads;
+    const uint32_t bodyBlocks = (body_count + kRoundThreads - 1u) / kRoundThreads;
+    for (uint32_t round = 0; round < iterations; ++round) {
+        rigid_joint_round_kernel<<<jointBlocks, kRoundThreads, 0, s>>>(b, body_count, jn, joint_count, c, bubble_count,
+                                                                      dt, iteration_count, safety);
+        if (body_count)
+            rigid_apply_round_kernel<<<bodyBlocks, kRoundThreads, 0, s>>>(b, body_count, c, refs, reference_count,
+                                                                         joint_count, ranges, bubble_count, safety);
+        if (cudaPeekAtLastError() != cudaSuccess) break;
+    }
     return launch_status();
 }
 
