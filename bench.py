@@ -250,49 +250,68 @@ def single_worlds(ctx, steps: int, large_steps: int, rigid_steps: int) -> dict:
 
 
 def rigid_solver(steps: int = 50, warmup: int = 5, cpu_steps: int = 5) -> dict:
-    """The rigid solver passes (bp_rigid_predict, 8 rounds of bp_rigid_solve_joints in one launch, bp_rigid_finish)
-    on jointed chains of box links (every joint kind), at 8 x 32 links (all rounds in one block), 64 x 32 and 256 x 32
-    links (two grid launches per round): device time per step and per
-    pass by CUDA events on the launching stream (the default stream, torch's current one), and the oracle's time per
-    step on one host core (the reference runs these passes as one Metal dispatch per kernel and round)."""
+    """The rigid solver on two workloads: jointed chains of box links (every joint kind; 8 x 32, 64 x 32 and
+    256 x 32 links), whose bodies meet no other body, stepped by predict + the joint rounds + finish; and a pile of
+    256 boxes, circles and capsules dropped on static floors, stepped by the reference's whole rigid step (body-pair
+    rows, CCD, 8 rounds of contacts + joints + wall guard). Device time per step and per pass by CUDA events on the
+    launching stream (the default stream, torch's current one); the oracle's time per step on one host core."""
     import torch
     from bubblephysics_gb300 import scenes
     from bubblephysics_gb300.rigid import ITERATIONS, RigidSolver
     from oracle.oracle import OracleRigid
+
+    def timed(fn, reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
     out = {}
     for chains, links in ((8, 32), (64, 32), (256, 32)):
         scene = scenes.jointed_chains(seed=6, chains=chains, links=links)
         arrays = scene.joint_arrays()
         solver = RigidSolver(scene.bodies, scene.vertices, scene.segments, arrays)
         for _ in range(warmup):
-            solver.step(scene.dt, scene.region)
+            solver.step_without_contacts(scene.dt, scene.region)
         torch.cuda.synchronize()
-
-        def timed(fn, reps):
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record()
-            for _ in range(reps):
-                fn()
-            b.record()
-            torch.cuda.synchronize()
-            return a.elapsed_time(b) / reps
-
-        step_ms = timed(lambda: solver.step(scene.dt, scene.region), steps)
+        step_ms = timed(lambda: solver.step_without_contacts(scene.dt, scene.region), steps)
         passes = {"predict_ms": timed(lambda: solver.predict(scene.dt), steps),
                   "joint_rounds_ms": timed(lambda: solver.solve_joints(scene.dt, ITERATIONS, ITERATIONS), steps),
                   "finish_ms": timed(lambda: solver.finish(scene.region), steps)}
         oracle = OracleRigid(scene.bodies, scene.vertices, scene.segments, arrays)
         t0 = time.perf_counter()
         for _ in range(cpu_steps):
-            oracle.step(scene.dt, scene.region)
+            oracle.step_without_contacts(scene.dt, scene.region)
         cpu_ms = (time.perf_counter() - t0) * 1000.0 / cpu_steps
         out[f"chains_{chains}x{links}"] = {
             "bodies": len(scene.bodies), "joints": len(arrays.records), "segments": len(scene.segments),
             "rounds": ITERATIONS, "ms_per_step": step_ms, "passes": passes, "safety": solver.safety(),
             "launches_per_step": 4 if len(arrays.records) <= 512 else 3 + 2 * ITERATIONS,
-            "cpu_oracle_ms_per_step": cpu_ms, "cpu_cores": 1,
+            "cpu_oracle_ms_per_step": cpu_ms, "cpu_cores": 1, "speedup_vs_cpu_oracle": cpu_ms / step_ms,
             "note": "a step = the walls clear (a memset) + predict + the joint rounds + finish"}
-        out[f"chains_{chains}x{links}"]["speedup_vs_cpu_oracle"] = cpu_ms / step_ms if step_ms > 0 else None
+    scene = scenes.rigid_pile()
+    arrays = scene.joint_arrays()
+    solver = RigidSolver(scene.bodies, scene.vertices, scene.segments, arrays, triangles=scene.triangles, row_width=32)
+    oracle = OracleRigid(scene.bodies, scene.vertices, scene.segments, arrays, triangles=scene.triangles, row_width=32)
+    for _ in range(warmup):
+        solver.step(scene.dt, scene.region)
+        oracle.step(scene.dt, scene.region)
+    torch.cuda.synchronize()
+    step_ms = timed(lambda: solver.step(scene.dt, scene.region), steps)
+    t0 = time.perf_counter()
+    for _ in range(cpu_steps):
+        oracle.step(scene.dt, scene.region)
+    cpu_ms = (time.perf_counter() - t0) * 1000.0 / cpu_steps
+    rows, counts = solver.candidates()
+    out["pile_256"] = {
+        "bodies": len(scene.bodies), "joints": len(arrays.records), "row_width": 32,
+        "row_entries": int(counts[:, 0].sum()), "ms_per_step": step_ms, "safety": solver.safety(),
+        "launches_per_step": 5 + 4 * ITERATIONS + 1, "cpu_oracle_ms_per_step": cpu_ms, "cpu_cores": 1,
+        "speedup_vs_cpu_oracle": cpu_ms / step_ms,
+        "note": "the reference's whole rigid step, after 5 warm-up steps (the pile falling onto the floors)"}
     return out
 
 
@@ -604,18 +623,27 @@ def run_case(name: str) -> int:
       noalloc   noalloc_step_kernel: 3 allocation-free steps of the 256-bubble world
       state     write_state_kernel, read_state_kernel, sum_kernel: the end-to-end state copies of the 4,096-world batch
                 (903 k bubbles) and its adjacency-entry count, 3 times each
-      chains    rigid_predict_kernel, rigid_joints_kernel, rigid_finish_kernel: 3 rigid steps of 256 x 32 jointed links"""
+      chains    rigid_predict_kernel, rigid_joint_round_kernel, rigid_apply_round_kernel, rigid_finish_kernel: 3 steps
+                of 256 x 32 jointed links without body contacts
+      pile      every rigid kernel: 3 whole rigid steps of 256 boxes, circles and capsules dropped on static floors"""
     import ctypes as C
     from bubblephysics_gb300 import _native as N
     from bubblephysics_gb300 import scenes
     from bubblephysics_gb300.solver import Batch, Context, Server, World
     ctx = Context(0)
-    if name == "chains":
+    if name in ("chains", "pile"):
         from bubblephysics_gb300.rigid import RigidSolver
-        scene = scenes.jointed_chains(seed=6, chains=256, links=32)
-        solver = RigidSolver(scene.bodies, scene.vertices, scene.segments, scene.joint_arrays())
+        if name == "chains":
+            scene = scenes.jointed_chains(seed=6, chains=256, links=32)
+            solver = RigidSolver(scene.bodies, scene.vertices, scene.segments, scene.joint_arrays())
+            step = solver.step_without_contacts
+        else:
+            scene = scenes.rigid_pile()
+            solver = RigidSolver(scene.bodies, scene.vertices, scene.segments, scene.joint_arrays(),
+                                 triangles=scene.triangles, row_width=32)
+            step = solver.step
         for _ in range(3):
-            solver.step(scene.dt, scene.region)
+            step(scene.dt, scene.region)
         print("bodies", len(scene.bodies), "safety", solver.safety())
         return 0 if solver.safety() == 0 else 1
     if name in ("batch", "batch512"):

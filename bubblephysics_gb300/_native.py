@@ -210,6 +210,8 @@ RIGID_CORRECTION_DTYPE = np.dtype({"names": ["first", "second", "velocity_first"
                                    "formats": [("<f4", 4)] * 4, "offsets": [0, 16, 32, 48], "itemsize": 64})
 RIGID_WALL_DTYPE = np.dtype({"names": ["participants", "geometry", "extra"],
                              "formats": [("<i8", 2), ("<f4", 4), ("<f4", 4)], "offsets": [0, 16, 32], "itemsize": 48})
+RIGID_CANDIDATE_DTYPE = np.dtype({"names": ["participants", "metadata"], "formats": [("<i8", 2), ("<u4", 4)],
+                                  "offsets": [0, 16], "itemsize": 32})
 JOINT_WORLD_END = 0xFFFFFFFF
 RIGID_SAFETY_NONFINITE, RIGID_SAFETY_ROTATION_BUDGET, RIGID_SAFETY_INVALID = 1, 18, 256
 REPORT_DTYPE = np.dtype({"names": [n for n, _ in StepReport._fields_],
@@ -287,6 +289,13 @@ _SIGNATURES = {
     "bp_rigid_solve_joints": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32, _P, _P, C.c_uint32, _P, C.c_uint32, C.c_float,
                                         C.c_uint32, C.c_uint32, _P, _P]),
     "bp_rigid_finish": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32, C.POINTER(C.c_float), _P, _P]),
+    "bp_rigid_body_candidates": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P, C.c_uint32, C.c_uint32, _P, _P, _P,
+                                           _P]),
+    "bp_rigid_ccd": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32, _P, C.c_uint32, _P, _P, C.c_uint32, _P, _P]),
+    "bp_rigid_solve_contacts": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32, _P, C.c_uint32, _P, _P, C.c_uint32, _P,
+                                          _P, _P]),
+    "bp_rigid_guard_walls": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32, _P, C.c_uint32, C.c_uint32, _P, _P,
+                                       C.c_uint32, _P, _P]),
 }
 EXPORTED_SYMBOLS = tuple(_SIGNATURES)
 

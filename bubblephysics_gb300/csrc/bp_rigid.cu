@@ -551,6 +551,553 @@ __global__ void __launch_bounds__(kRoundThreads) rigid_apply_round_kernel(RBody*
                             nullptr, safety);
 }
 
+// ---- body contacts, body-pair rows, CCD, wall guard ----------------------------------------------------------
+
+struct __align__(16) RCandidate {
+    long long first, second;  // participants
+    uint4 meta;               // kind, lower index, higher index, float bits of the summed normal lambda
+};
+static_assert(sizeof(RCandidate) == sizeof(bp_rigid_candidate), "bp_rigid_candidate layout");
+
+struct Geo {
+    const float2* verts;
+    uint32_t vertexCount;
+    const uint4* tris;
+    uint32_t triangleCount;
+};
+
+__device__ __forceinline__ bool is_round(const RBody& b) { return b.shape.x > 0.5f; }
+__device__ __forceinline__ bool immovable(const RBody& b) { return b.flags.x != 0u || b.filter.z != 0u; }
+__device__ __forceinline__ bool accepts(const RBody& a, const RBody& b) {
+    return filter_accepts(make_uint2(a.filter.x, a.filter.y), make_uint2(b.filter.x, b.filter.y));
+}
+__device__ __forceinline__ float dist2(float2 a, float2 b) { return len2(sub(a, b)); }
+__device__ __forceinline__ float2 neg2(float2 a) { return f2(-a.x, -a.y); }
+__device__ __forceinline__ float2 pose_xy(const RBody& b) { return f2(b.pose.x, b.pose.y); }
+
+// nativeRigidVertex (NGK:139-141)
+__device__ __forceinline__ float2 world_vertex(const Geo& g, const RBody& b, uint32_t i) {
+    return add(pose_xy(b), rotate_by(g.verts[b.ranges.x + i], b.pose.z));
+}
+
+// A body's vertex and triangle ranges lie inside the arrays and its triangles index its own vertices.
+__device__ bool geometry_ok(const Geo& g, const RBody& b) {
+    if (!vertex_range_ok(b, g.vertexCount)) return false;
+    if (b.ranges.w > g.triangleCount || b.ranges.z > g.triangleCount - b.ranges.w) return false;
+    for (uint32_t i = 0; i < b.ranges.w; ++i) {
+        const uint4 t = g.tris[b.ranges.z + i];
+        if (t.x >= b.ranges.y || t.y >= b.ranges.y || t.z >= b.ranges.y) return false;
+    }
+    return is_round(b) ? b.ranges.y >= 1u : true;
+}
+
+// nativeSegmentDistance (NGK:444-462)
+__device__ float segment_distance(float2 a, float2 b, float2 c, float2 d, float2& pa, float2& pb) {
+    const float2 r = sub(b, a), s = sub(d, c);
+    const float denominator = cross2(r, s);
+    if (fabsf(denominator) > 1e-12f) {
+        const float2 qp = sub(c, a);
+        const float t = cross2(qp, s) / denominator, u = cross2(qp, r) / denominator;
+        if (t >= 0.0f && t <= 1.0f && u >= 0.0f && u <= 1.0f) { pa = add(a, mul(r, t)); pb = pa; return 0.0f; }
+    }
+    float best = INFINITY;
+    float2 cp = closest_point(a, c, d);
+    float value = dist2(a, cp);
+    if (value < best) { best = value; pa = a; pb = cp; }
+    cp = closest_point(b, c, d); value = dist2(b, cp);
+    if (value < best) { best = value; pa = b; pb = cp; }
+    cp = closest_point(c, a, b); value = dist2(c, cp);
+    if (value < best) { best = value; pa = cp; pb = c; }
+    cp = closest_point(d, a, b); value = dist2(d, cp);
+    if (value < best) { best = value; pa = cp; pb = d; }
+    return best;
+}
+
+struct Core { float2 a, b; float radius; };
+// nativeRoundCoreOf (NGK:466-472)
+__device__ __forceinline__ Core core_of(const Geo& g, const RBody& b) {
+    Core c;
+    c.a = world_vertex(g, b, 0);
+    c.b = b.ranges.y > 1u ? world_vertex(g, b, 1) : c.a;
+    c.radius = b.shape.y;
+    return c;
+}
+
+// nativeRigidInside (NGK:477-490)
+__device__ bool rigid_inside_body(const Geo& g, float2 p, const RBody& b) {
+    if (is_round(b)) {
+        const Core c = core_of(g, b);
+        return dist2(p, closest_point(p, c.a, c.b)) <= c.radius;
+    }
+    const float2 local = rotate_by(sub(p, pose_xy(b)), -b.pose.z);
+    for (uint32_t i = 0; i < b.ranges.w; ++i) {
+        const uint4 t = g.tris[b.ranges.z + i];
+        const float2 A = g.verts[b.ranges.x + t.x], B = g.verts[b.ranges.x + t.y], C = g.verts[b.ranges.x + t.z];
+        if (cross2(sub(B, A), sub(local, A)) >= 0.0f && cross2(sub(C, B), sub(local, B)) >= 0.0f &&
+            cross2(sub(A, C), sub(local, C)) >= 0.0f)
+            return true;
+    }
+    return false;
+}
+
+// nativeRoundContact (NGK:546-581)
+__device__ bool round_contact(const Core& A, const Core& B, float2 fallback, float2& normal, float& depth,
+                              float2& point) {
+    float2 pa, pb;
+    const float separation = segment_distance(A.a, A.b, B.a, B.b, pa, pb);
+    if (separation > 1e-4f) {
+        normal = dvd(sub(pb, pa), separation);
+        depth = A.radius + B.radius - separation;
+        point = mul(add(add(pa, mul(normal, A.radius)), sub(pb, mul(normal, B.radius))), 0.5f);
+        return true;
+    }
+    float2 axes[2];
+    uint32_t axisCount = 0;
+    const float2 ea = sub(A.b, A.a), eb = sub(B.b, B.a);
+    const float la = len2(ea), lb = len2(eb);
+    if (la > 1e-6f) axes[axisCount++] = dvd(f2(-ea.y, ea.x), la);
+    if (lb > 1e-6f) axes[axisCount++] = dvd(f2(-eb.y, eb.x), lb);
+    float2 axis = fallback;
+    float overlap = 0.0f, orientation = 1.0f, best = INFINITY;
+    for (uint32_t i = 0; i < axisCount; ++i) {
+        const float2 c = axes[i];
+        const float amin = fminf(dot2(A.a, c), dot2(A.b, c)), amax = fmaxf(dot2(A.a, c), dot2(A.b, c));
+        const float bmin = fminf(dot2(B.a, c), dot2(B.b, c)), bmax = fmaxf(dot2(B.a, c), dot2(B.b, c));
+        const float plus = amax - bmin, minus = bmax - amin;
+        const float value = fminf(plus, minus);
+        if (value < best) {
+            best = value; axis = c; overlap = value;
+            if (fabsf(plus - minus) < 1e-6f) orientation = dot2(c, fallback) >= 0.0f ? 1.0f : -1.0f;
+            else orientation = plus < minus ? 1.0f : -1.0f;
+        }
+    }
+    normal = mul(axis, orientation);
+    depth = overlap + A.radius + B.radius;
+    point = mul(add(pa, pb), 0.5f);
+    return true;
+}
+
+// nativeTriangleContact (NCK:248-275)
+__device__ bool triangle_contact(const float2* a, const float2* b, float2& normal, float& depth, float2& point) {
+    depth = INFINITY;
+    for (int shape = 0; shape < 2; ++shape)
+        for (int edge = 0; edge < 3; ++edge) {
+            const float2 delta = shape == 0 ? sub(a[(edge + 1) % 3], a[edge]) : sub(b[(edge + 1) % 3], b[edge]);
+            const float magnitude = len2(delta);
+            if (magnitude <= kFltMin) return false;
+            const float2 axis = dvd(f2(-delta.y, delta.x), magnitude);
+            float amin = INFINITY, amax = -INFINITY, bmin = INFINITY, bmax = -INFINITY;
+            for (int k = 0; k < 3; ++k) {
+                const float pa = dot2(a[k], axis), pb = dot2(b[k], axis);
+                amin = fminf(amin, pa); amax = fmaxf(amax, pa);
+                bmin = fminf(bmin, pb); bmax = fmaxf(bmax, pb);
+            }
+            if (amax < bmin || bmax < amin) return false;
+            const float plus = amax - bmin, minus = bmax - amin;
+            const float overlap = fminf(plus, minus);
+            if (overlap < depth) { depth = overlap; normal = plus < minus ? axis : neg2(axis); }
+        }
+    float maxA = -INFINITY, minB = INFINITY;
+    float2 pa = f2(0.0f, 0.0f), pb = f2(0.0f, 0.0f);
+    uint32_t na = 0, nb = 0;
+    for (int k = 0; k < 3; ++k) { maxA = fmaxf(maxA, dot2(a[k], normal)); minB = fminf(minB, dot2(b[k], normal)); }
+    for (int k = 0; k < 3; ++k) {
+        if (dot2(a[k], normal) >= maxA - 1e-5f) { pa = add(pa, a[k]); ++na; }
+        if (dot2(b[k], normal) <= minB + 1e-5f) { pb = add(pb, b[k]); ++nb; }
+    }
+    point = mul(add(dvd(pa, (float)na), dvd(pb, (float)nb)), 0.5f);
+    return true;
+}
+
+__device__ __forceinline__ float2 outward_of(float2 p, float2 q) {
+    const float2 edge = sub(q, p);
+    const float size = len2(edge);
+    return size > kFltMin ? dvd(f2(edge.y, -edge.x), size) : f2(0.0f, 1.0f);
+}
+
+// nativeRoundPolygonContact (NCK:277-333): normal from the round core R to the polygon P.
+__device__ bool round_polygon_contact(const Geo& g, const Core& R, const RBody& P, float2& normal, float& depth,
+                                      float2& point) {
+    const uint32_t count = P.ranges.y;
+    float insideDepth = -1.0f;
+    float2 insideOutward = f2(0.0f, 0.0f), insidePoint = f2(0.0f, 0.0f);
+    const uint32_t endpoints = (R.b.x != R.a.x || R.b.y != R.a.y) ? 2u : 1u;
+    uint32_t insideEndpoints = 0;
+    for (uint32_t k = 0; k < endpoints; ++k) {
+        const float2 endpoint = k == 0 ? R.a : R.b;
+        if (!rigid_inside_body(g, endpoint, P)) continue;
+        ++insideEndpoints;
+        float nearest = INFINITY;
+        float2 nearestPoint = f2(0.0f, 0.0f), nearestOutward = f2(0.0f, 0.0f);
+        for (uint32_t e = 0; e < count; ++e) {
+            const float2 p = world_vertex(g, P, e), q = world_vertex(g, P, (e + 1u) % count);
+            const float2 c = closest_point(endpoint, p, q);
+            const float d = dist2(endpoint, c);
+            if (d < nearest) { nearest = d; nearestPoint = c; nearestOutward = outward_of(p, q); }
+        }
+        if (nearest > insideDepth) { insideDepth = nearest; insidePoint = nearestPoint; insideOutward = nearestOutward; }
+    }
+    if (insideEndpoints == endpoints) {
+        normal = neg2(insideOutward); depth = R.radius + insideDepth; point = insidePoint;
+        return true;
+    }
+    float best = INFINITY;
+    float2 pc = f2(0.0f, 0.0f), pe = f2(0.0f, 0.0f);
+    for (uint32_t e = 0; e < count; ++e) {
+        const float2 p = world_vertex(g, P, e), q = world_vertex(g, P, (e + 1u) % count);
+        float2 ca, ce;
+        const float d = segment_distance(R.a, R.b, p, q, ca, ce);
+        if (d < best) { best = d; pc = ca; pe = ce; }
+    }
+    if (best > 1e-4f) {
+        normal = dvd(sub(pe, pc), best); depth = R.radius - best; point = pe;
+        return true;
+    }
+    float minimum = INFINITY;
+    float2 minimumOutward = f2(0.0f, 1.0f), minimumPoint = pe;
+    for (uint32_t e = 0; e < count; ++e) {
+        const float2 p = world_vertex(g, P, e), q = world_vertex(g, P, (e + 1u) % count);
+        const float2 edge = sub(q, p);
+        const float size = len2(edge);
+        if (size <= kFltMin) continue;
+        const float2 outward = dvd(f2(edge.y, -edge.x), size);
+        const float da = dot2(sub(R.a, p), outward), db = dot2(sub(R.b, p), outward);
+        const float d = R.radius - fminf(da, db);
+        if (d < minimum) {
+            minimum = d; minimumOutward = outward;
+            minimumPoint = sub(da <= db ? R.a : R.b, mul(outward, fminf(da, db)));
+        }
+    }
+    normal = neg2(minimumOutward); depth = isfinite(minimum) ? minimum : R.radius; point = minimumPoint;
+    return true;
+}
+
+// nativeRoundCoreCrossesPolygon (NCK:335-344)
+__device__ bool round_core_crosses_polygon(const Geo& g, const Core& R, const RBody& P) {
+    if (rigid_inside_body(g, R.a, P) || rigid_inside_body(g, R.b, P)) return true;
+    for (uint32_t e = 0; e < P.ranges.y; ++e) {
+        const float2 p = world_vertex(g, P, e), q = world_vertex(g, P, (e + 1u) % P.ranges.y);
+        float2 ca, ce;
+        if (segment_distance(R.a, R.b, p, q, ca, ce) <= 1e-4f) return true;
+    }
+    return false;
+}
+
+// nativeRigidPairContact (NCK:348-373): normal from a to b; false = the shapes do not overlap.
+__device__ bool pair_contact(const Geo& g, const RBody& a, const RBody& b, float2& n, float& depth, float2& point) {
+    const bool aRound = is_round(a), bRound = is_round(b);
+    if (aRound && bRound) return round_contact(core_of(g, a), core_of(g, b), f2(1.0f, 0.0f), n, depth, point);
+    if (aRound != bRound) {
+        const RBody& round = aRound ? a : b;
+        const RBody& polygon = aRound ? b : a;
+        float2 normal;
+        if (!round_polygon_contact(g, core_of(g, round), polygon, normal, depth, point)) return false;
+        n = aRound ? normal : neg2(normal);
+        return true;
+    }
+    bool found = false;
+    for (uint32_t i = 0; i < a.ranges.w; ++i)
+        for (uint32_t j = 0; j < b.ranges.w; ++j) {
+            const uint4 ta = g.tris[a.ranges.z + i], tb = g.tris[b.ranges.z + j];
+            const float2 av[3] = {world_vertex(g, a, ta.x), world_vertex(g, a, ta.y), world_vertex(g, a, ta.z)};
+            const float2 bv[3] = {world_vertex(g, b, tb.x), world_vertex(g, b, tb.y), world_vertex(g, b, tb.z)};
+            float2 normal, p;
+            float d;
+            if (triangle_contact(av, bv, normal, d, p) && (!found || d > depth)) {
+                found = true; depth = d; n = normal; point = p;
+            }
+        }
+    return found;
+}
+
+// nativeKeyLess / nativeInsertCandidate (NGK:230-251)
+__device__ __forceinline__ bool key_less(const RCandidate& a, const RCandidate& b) {
+    if (a.meta.x != b.meta.x) return a.meta.x < b.meta.x;
+    if (a.first != b.first) return a.first < b.first;
+    return a.second < b.second;
+}
+__device__ void insert_candidate(RCandidate* row, uint32_t& count, uint32_t& dropped, uint32_t limit,
+                                 const RCandidate& value) {
+    uint32_t location;
+    if (count < limit) location = count++;
+    else {
+        ++dropped;
+        if (!key_less(value, row[limit - 1u])) return;
+        location = limit - 1u;
+    }
+    while (location > 0u && key_less(value, row[location - 1u])) { row[location] = row[location - 1u]; --location; }
+    row[location] = value;
+}
+
+// nativeEmitBodyCandidates, body pairs (NGK:394-415): one thread per body and row.
+__global__ void __launch_bounds__(kRoundThreads) rigid_candidates_kernel(const RBody* bodies, uint32_t bodyCount,
+                                                                       uint32_t bubbleCount, const uint4* jointRanges,
+                                                                       const unsigned long long* partners,
+                                                                       uint32_t partnerCount, uint32_t limit,
+                                                                       RCandidate* rows, uint2* rowCounts,
+                                                                       uint32_t* overflow) {
+    const uint32_t index = blockIdx.x * blockDim.x + threadIdx.x;
+    if (index >= bodyCount) return;
+    RCandidate* row = rows + (size_t)index * limit;
+    uint32_t count = 0, dropped = 0;
+    for (uint32_t other = 0; other < bodyCount; ++other) {
+        if (other == index) continue;
+        const uint32_t low = min(index, other), high = max(index, other);
+        const RBody& a = bodies[low];
+        const RBody& c = bodies[high];
+        if (immovable(a) && immovable(c)) continue;
+        if (!accepts(a, c)) continue;
+        if (joint_excluded(jointRanges, partners, partnerCount, bubbleCount + index, bodies[other].id)) continue;
+        const float2 start = sub(f2(a.previous.x, a.previous.y), f2(c.previous.x, c.previous.y));
+        const float2 end = sub(pose_xy(a), pose_xy(c));
+        const float2 travel = sub(end, start);
+        const float travelSquared = dot2(travel, travel);
+        const float t = travelSquared > kFltMin ? clampf(-dot2(start, travel) / travelSquared, 0.0f, 1.0f) : 0.0f;
+        const float radius = 1.25f * (a.physical.z + c.physical.z);
+        const float2 closest = add(start, mul(travel, t));
+        if (!(dot2(closest, closest) <= radius * radius)) continue;
+        RCandidate value;
+        value.first = (long long)a.id; value.second = (long long)c.id;
+        value.meta = make_uint4(3u, low, high, 0u);
+        insert_candidate(row, count, dropped, limit, value);
+    }
+    rowCounts[index] = make_uint2(count, 0u);
+    if (dropped) atomicAdd(overflow, dropped);
+    atomicMax(overflow + 1, count + dropped);
+}
+
+__device__ __forceinline__ bool candidate_ok(const RCandidate& c, uint32_t count) {
+    return c.meta.y < count && c.meta.z < count;
+}
+
+// nativeRigidOverlapAt / nativeRigidTimeOfImpact (NPK:200-233)
+__device__ bool overlap_at(const Geo& g, RBody a, RBody b, float t) {
+    a.pose.x = a.previous.x + (a.pose.x - a.previous.x) * t; a.pose.y = a.previous.y + (a.pose.y - a.previous.y) * t;
+    a.pose.z = a.pose.w + (a.pose.z - a.pose.w) * t;
+    b.pose.x = b.previous.x + (b.pose.x - b.previous.x) * t; b.pose.y = b.previous.y + (b.pose.y - b.previous.y) * t;
+    b.pose.z = b.pose.w + (b.pose.z - b.pose.w) * t;
+    float2 n, point;
+    float depth;
+    return pair_contact(g, a, b, n, depth, point) && depth > 1e-3f;
+}
+__device__ float time_of_impact(const Geo& g, const RBody& a, const RBody& b) {
+    const float2 da = sub(pose_xy(a), f2(a.previous.x, a.previous.y));
+    const float2 db = sub(pose_xy(b), f2(b.previous.x, b.previous.y));
+    const float travel = len2(sub(da, db)) + fabsf(a.pose.z - a.pose.w) * a.physical.z +
+                         fabsf(b.pose.z - b.pose.w) * b.physical.z;
+    if (!(travel > 0.5f)) return 2.0f;
+    if (overlap_at(g, a, b, 0.0f)) return 2.0f;
+    const float samples = ceilf(travel / 0.5f);
+    const uint32_t steps = samples >= 64.0f ? 64u : max(2u, (uint32_t)samples);
+    float last = 0.0f;
+    for (uint32_t step = 1; step <= steps; ++step) {
+        const float t = (float)step / (float)steps;
+        if (!overlap_at(g, a, b, t)) { last = t; continue; }
+        float low = last, high = t;
+        for (int bisection = 0; bisection < 12; ++bisection) {
+            const float middle = 0.5f * (low + high);
+            if (overlap_at(g, a, b, middle)) high = middle; else low = middle;
+        }
+        return low;
+    }
+    return 2.0f;
+}
+
+// nativeRigidResolveCCD (NPK:235-250): the earliest impact of the body's row, kept in its own limits.z (1 + t).
+__global__ void __launch_bounds__(kRoundThreads) rigid_ccd_resolve_kernel(RBody* bodies, uint32_t bodyCount, Geo g,
+                                                                        const RCandidate* rows,
+                                                                        const uint2* rowCounts, uint32_t width,
+                                                                        uint32_t* safety) {
+    const uint32_t index = blockIdx.x * blockDim.x + threadIdx.x;
+    if (index >= bodyCount) return;
+    float earliest = 2.0f;
+    if (!immovable(bodies[index])) {
+        const uint2 rc = rowCounts[index];
+        const uint32_t n = min(rc.x, width);
+        for (uint32_t slot = rc.y; slot < n; ++slot) {
+            const RCandidate c = rows[(size_t)index * width + slot];
+            if (c.meta.x != 3u) continue;
+            if (!candidate_ok(c, bodyCount)) { atomicOr(safety, BP_RIGID_SAFETY_INVALID); continue; }
+            const RBody a = bodies[c.meta.y], b = bodies[c.meta.z];
+            if (!geometry_ok(g, a) || !geometry_ok(g, b)) { atomicOr(safety, BP_RIGID_SAFETY_INVALID); continue; }
+            earliest = fminf(earliest, time_of_impact(g, a, b));
+        }
+    }
+    bodies[index].limits.z = earliest <= 1.0f ? 1.0f + earliest : 0.0f;
+}
+
+// nativeRigidApplyCCD (NPK:253-263)
+__global__ void __launch_bounds__(kRoundThreads) rigid_ccd_apply_kernel(RBody* bodies, uint32_t bodyCount) {
+    const uint32_t index = blockIdx.x * blockDim.x + threadIdx.x;
+    if (index >= bodyCount) return;
+    float4 pose = bodies[index].pose, limits = bodies[index].limits;
+    const float4 previous = bodies[index].previous;
+    if (limits.z >= 1.0f) {
+        const float t = limits.z - 1.0f;
+        pose.x = previous.x + (pose.x - previous.x) * t;
+        pose.y = previous.y + (pose.y - previous.y) * t;
+        pose.z = pose.w + (pose.z - pose.w) * t;
+    }
+    limits.z = 0.0f;
+    bodies[index].pose = pose;
+    bodies[index].limits = limits;
+}
+
+// nativeRigidContacts (NCK:375-427): one thread per row slot.
+__global__ void __launch_bounds__(kRoundThreads) rigid_contacts_kernel(const RBody* bodies, uint32_t bodyCount, Geo g,
+                                                                     RCandidate* rows, const uint2* rowCounts,
+                                                                     uint32_t width, RCorrection* corrections,
+                                                                     uint32_t* safety) {
+    const size_t index = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t owner = (uint32_t)(index / width), slot = (uint32_t)(index % width);
+    if (owner >= bodyCount || slot >= min(rowCounts[owner].x, width)) return;
+    RCandidate& candidate = rows[index];
+    const RCorrection previous = corrections[index];
+    RCorrection result;
+    result.first = make_float4(0.0f, 0.0f, 0.0f, previous.first.w);
+    result.second = make_float4(0.0f, 0.0f, 0.0f, previous.second.w);
+    result.velocityFirst = make_float4(0.0f, 0.0f, 0.0f, previous.velocityFirst.w);
+    result.velocitySecond = make_float4(0.0f, 0.0f, 0.0f, previous.velocitySecond.w);
+    const uint4 meta = candidate.meta;
+    if (meta.x != 3u) { corrections[index] = result; return; }
+    if (meta.y >= bodyCount || meta.z >= bodyCount) {
+        atomicOr(safety, BP_RIGID_SAFETY_INVALID);
+        corrections[index] = result;
+        return;
+    }
+    const uint32_t ai = meta.y, bi = meta.z;
+    const RBody a = bodies[ai], b = bodies[bi];
+    if (ai >= bi || (immovable(a) && immovable(b))) { corrections[index] = result; return; }
+    if (!geometry_ok(g, a) || !geometry_ok(g, b)) {
+        atomicOr(safety, BP_RIGID_SAFETY_INVALID);
+        corrections[index] = result;
+        return;
+    }
+    const float2 end = sub(pose_xy(a), pose_xy(b));
+    const float radius = a.physical.z + b.physical.z, radiusSquared = radius * radius;
+    if (dot2(end, end) > radiusSquared) { corrections[index] = result; return; }
+    float2 n, point;
+    float depth;
+    if (!pair_contact(g, a, b, n, depth, point)) { corrections[index] = result; return; }
+    const float wa = a.physical.x, wb = b.physical.x, ia = a.physical.y, ib = b.physical.y;
+    const float2 ra = sub(point, pose_xy(a)), rb = sub(point, pose_xy(b));
+    const float2 va = f2(a.motion.x, a.motion.y), vb = f2(b.motion.x, b.motion.y);
+    const float spinA = a.motion.z, spinB = b.motion.z;
+    const float frictionA = a.physical.w, frictionB = b.physical.w;
+    const float restitutionA = __uint_as_float(a.flags.w), restitutionB = __uint_as_float(b.flags.w);
+    const float ca = cross2(ra, n), cb = cross2(rb, n), denom = wa + wb + ia * ca * ca + ib * cb * cb;
+    if (depth < -0.001f || denom <= kFltMin) { corrections[index] = result; return; }
+    const float lambda = fmaxf(0.0f, depth) / denom * 0.5f;
+    candidate.meta.w = __float_as_uint(__uint_as_float(meta.w) + lambda);
+    const float2 moveA = mul(mul(neg2(n), wa), lambda), moveB = mul(mul(n, wb), lambda);
+    result.first = make_float4(moveA.x, moveA.y, -ca * ia * lambda, n.x);
+    result.second = make_float4(moveB.x, moveB.y, cb * ib * lambda, n.y);
+    const float closing = dot2(sub(vb, va), n) + spinB * cb - spinA * ca;
+    const float friction = sqrtf(fmaxf(0.0f, frictionA * frictionB));
+    const float restitution = fmaxf(restitutionA, restitutionB);
+    const float impulse = fmaxf(0.0f, -closing) * (1.0f + restitution) / denom * 0.5f;
+    const float2 tangent = f2(-n.y, n.x);
+    const float tangentSpeed = dot2(sub(vb, va), tangent) + spinB * cross2(rb, tangent) - spinA * cross2(ra, tangent);
+    const float tangentImpulse = -tangentSpeed * friction / denom * 0.5f;
+    const float2 vA = sub(mul(mul(neg2(n), wa), impulse), mul(mul(tangent, wa), tangentImpulse));
+    const float2 vB = add(mul(mul(n, wb), impulse), mul(mul(tangent, wb), tangentImpulse));
+    result.velocityFirst = make_float4(vA.x, vA.y, -ca * ia * impulse - cross2(ra, tangent) * ia * tangentImpulse,
+                                       point.x);
+    result.velocitySecond = make_float4(vB.x, vB.y, cb * ib * impulse + cross2(rb, tangent) * ib * tangentImpulse,
+                                        point.y);
+    corrections[index] = result;
+}
+
+// nativeRigidApplyBodies (NCK:429-444)
+__global__ void __launch_bounds__(kRoundThreads) rigid_apply_bodies_kernel(RBody* bodies, uint32_t bodyCount,
+                                                                         const RCandidate* rows,
+                                                                         const uint2* rowCounts, uint32_t width,
+                                                                         const RCorrection* corrections) {
+    const uint32_t index = blockIdx.x * blockDim.x + threadIdx.x;
+    if (index >= bodyCount) return;
+    float3 delta = make_float3(0.0f, 0.0f, 0.0f), velocity = make_float3(0.0f, 0.0f, 0.0f);
+    const uint32_t n = min(rowCounts[index].x, width);
+    for (uint32_t slot = 0; slot < n; ++slot) {
+        const size_t at = (size_t)index * width + slot;
+        const uint4 meta = rows[at].meta;
+        const bool first = meta.x == 3u && meta.y == index;
+        const RCorrection& c = corrections[at];
+        const float4 d = first ? c.first : c.second, v = first ? c.velocityFirst : c.velocitySecond;
+        delta.x += d.x; delta.y += d.y; delta.z += d.z;
+        velocity.x += v.x; velocity.y += v.y; velocity.z += v.z;
+    }
+    float4 pose = bodies[index].pose, motion = bodies[index].motion;
+    pose.x += delta.x; pose.y += delta.y; pose.z += delta.z;
+    motion.x += velocity.x; motion.y += velocity.y; motion.z += velocity.z;
+    bodies[index].pose = pose;
+    bodies[index].motion = motion;
+}
+
+// nativeRigidGuardWalls (NPK:118-170): one thread per dynamic body; static bodies are never written.
+__global__ void __launch_bounds__(kRoundThreads) rigid_guard_kernel(RBody* bodies, uint32_t bodyCount, Geo g,
+                                                                  uint32_t bubbleCount, const uint4* jointRanges,
+                                                                  const unsigned long long* partners,
+                                                                  uint32_t partnerCount, uint32_t* safety) {
+    const uint32_t index = blockIdx.x * blockDim.x + threadIdx.x;
+    if (index >= bodyCount) return;
+    if (bodies[index].flags.x || bodies[index].filter.z) return;
+    RBody b = bodies[index];
+    if (!geometry_ok(g, b)) { atomicOr(safety, BP_RIGID_SAFETY_INVALID); return; }
+    for (uint32_t j = 0; j < bodyCount; ++j) {
+        if (!bodies[j].flags.x) continue;
+        const RBody wall = bodies[j];
+        if (is_round(wall) || !accepts(b, wall)) continue;
+        if (joint_excluded(jointRanges, partners, partnerCount, bubbleCount + index, wall.id)) continue;
+        if (!geometry_ok(g, wall)) { atomicOr(safety, BP_RIGID_SAFETY_INVALID); continue; }
+        const uint32_t wn = wall.ranges.y;
+        for (uint32_t k = 0; k < b.ranges.y; ++k) {
+            const float2 p = world_vertex(g, b, k);
+            const float2 start = add(f2(b.previous.x, b.previous.y), rotate_by(g.verts[b.ranges.x + k], b.pose.w));
+            const bool inside = rigid_inside_body(g, p, wall);
+            bool startedInside = rigid_inside_body(g, start, wall);
+            if (startedInside)
+                for (uint32_t e = 0; e < wn; ++e) {
+                    const float2 ea = world_vertex(g, wall, e), eb = world_vertex(g, wall, (e + 1u) % wn);
+                    if (dist2(start, closest_point(start, ea, eb)) < 1e-5f) { startedInside = false; break; }
+                }
+            float nearest = INFINITY, depth = 0.0f;
+            float2 normal = f2(0.0f, 0.0f);
+            for (uint32_t e = 0; e < wn; ++e) {
+                const float2 ea = world_vertex(g, wall, e), eb = world_vertex(g, wall, (e + 1u) % wn);
+                const float2 direction = sub(eb, ea);
+                const float2 out = normalized(f2(direction.y, -direction.x));
+                const float signedStart = dot2(sub(start, ea), out);
+                const bool onBoundary = dist2(start, closest_point(start, ea, eb)) < 1e-5f;
+                const bool crossing = signedStart >= -1e-5f && (center_crossing(start, p, ea, eb, ea, eb) ||
+                                                                 (onBoundary && dot2(sub(p, ea), out) < 0.0f));
+                if (!inside && !crossing) continue;
+                if (inside && !startedInside && signedStart < -1e-5f) continue;
+                const float2 c = closest_point(p, ea, eb);
+                const float d = (crossing || !startedInside) ? dist2(start, closest_point(start, ea, eb)) : dist2(p, c);
+                if (d < nearest) { nearest = d; normal = out; depth = fmaxf(0.0f, -dot2(sub(p, c), out)); }
+            }
+            if (isfinite(nearest) && depth > 0.0f) {
+                if (is_round(b)) {
+                    RBody old = b;
+                    old.pose.x = b.previous.x; old.pose.y = b.previous.y; old.pose.z = b.pose.w;
+                    if (round_core_crosses_polygon(g, core_of(g, old), wall)) break;
+                }
+                const float2 shift = mul(normal, depth + 1e-5f);
+                b.pose.x += shift.x; b.pose.y += shift.y;
+                const float2 r = sub(p, pose_xy(b));
+                const float lever = cross2(r, normal);
+                const float speed = dot2(f2(b.motion.x, b.motion.y), normal) + b.motion.z * lever;
+                const float denom = b.physical.x + b.physical.y * lever * lever;
+                const float impulse = fmaxf(0.0f, -speed) / fmaxf(denom, kFltMin);
+                const float2 dv = mul(mul(normal, b.physical.x), impulse);
+                b.motion.x += dv.x; b.motion.y += dv.y;
+                b.motion.z += lever * b.physical.y * impulse;
+            }
+        }
+    }
+    bodies[index] = b;
+}
+
 static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0u; }
 static bool aligned8(const void* p) { return ((uintptr_t)p & 7u) == 0u; }
 
@@ -638,5 +1185,98 @@ extern "C" int bp_rigid_finish(bp_rigid_body* bodies, uint32_t body_count, const
     rigid_finish_kernel<<<blocks, kRigidThreads, 0, (cudaStream_t)stream>>>(
         reinterpret_cast<RBody*>(bodies), body_count, reinterpret_cast<const float2*>(vertices_xy), vertex_count, r,
         safety);
+    return launch_status();
+}
+
+extern "C" int bp_rigid_body_candidates(const bp_rigid_body* bodies, uint32_t body_count, uint32_t bubble_count,
+                                        const uint32_t* joint_ranges, const uint64_t* joint_partners,
+                                        uint32_t partner_count, uint32_t row_width, bp_rigid_candidate* rows,
+                                        uint32_t* row_counts, uint32_t* overflow, void* stream) {
+    using namespace bp;
+    if (body_count == 0) return BP_OK;
+    if (!bodies || !rows || !row_counts || !overflow || row_width == 0 || (!joint_partners && partner_count))
+        return BP_E_INVALID;
+    if (!aligned16(bodies) || !aligned16(rows) || !aligned8(row_counts) || !aligned16(joint_ranges) ||
+        !aligned8(joint_partners))
+        return BP_E_INVALID;
+    const uint32_t blocks = (body_count + kRoundThreads - 1u) / kRoundThreads;
+    rigid_candidates_kernel<<<blocks, kRoundThreads, 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<const RBody*>(bodies), body_count, bubble_count, reinterpret_cast<const uint4*>(joint_ranges),
+        reinterpret_cast<const unsigned long long*>(joint_partners), joint_ranges ? partner_count : 0u, row_width,
+        reinterpret_cast<RCandidate*>(rows), reinterpret_cast<uint2*>(row_counts), overflow);
+    return launch_status();
+}
+
+namespace bp {
+static bool geometry_args(const float* vertices_xy, uint32_t vertex_count, const uint32_t* triangles,
+                          uint32_t triangle_count, Geo& g) {
+    if ((!vertices_xy && vertex_count) || (!triangles && triangle_count)) return false;
+    if (!aligned8(vertices_xy) || !aligned16(triangles)) return false;
+    g.verts = reinterpret_cast<const float2*>(vertices_xy);
+    g.vertexCount = vertex_count;
+    g.tris = reinterpret_cast<const uint4*>(triangles);
+    g.triangleCount = triangle_count;
+    return true;
+}
+}  // namespace bp
+
+extern "C" int bp_rigid_ccd(bp_rigid_body* bodies, uint32_t body_count, const float* vertices_xy, uint32_t vertex_count,
+                            const uint32_t* triangles, uint32_t triangle_count, const bp_rigid_candidate* rows,
+                            const uint32_t* row_counts, uint32_t row_width, uint32_t* safety, void* stream) {
+    using namespace bp;
+    if (body_count == 0) return BP_OK;
+    Geo g;
+    if (!bodies || !rows || !row_counts || !safety || row_width == 0 || !aligned16(bodies) || !aligned16(rows) ||
+        !aligned8(row_counts) || !geometry_args(vertices_xy, vertex_count, triangles, triangle_count, g))
+        return BP_E_INVALID;
+    const uint32_t blocks = (body_count + kRoundThreads - 1u) / kRoundThreads;
+    cudaStream_t s = (cudaStream_t)stream;
+    RBody* b = reinterpret_cast<RBody*>(bodies);
+    rigid_ccd_resolve_kernel<<<blocks, kRoundThreads, 0, s>>>(b, body_count, g, reinterpret_cast<const RCandidate*>(rows),
+                                                              reinterpret_cast<const uint2*>(row_counts), row_width,
+                                                              safety);
+    rigid_ccd_apply_kernel<<<blocks, kRoundThreads, 0, s>>>(b, body_count);
+    return launch_status();
+}
+
+extern "C" int bp_rigid_solve_contacts(bp_rigid_body* bodies, uint32_t body_count, const float* vertices_xy,
+                                       uint32_t vertex_count, const uint32_t* triangles, uint32_t triangle_count,
+                                       bp_rigid_candidate* rows, const uint32_t* row_counts, uint32_t row_width,
+                                       bp_rigid_correction* corrections, uint32_t* safety, void* stream) {
+    using namespace bp;
+    if (body_count == 0) return BP_OK;
+    Geo g;
+    if (!bodies || !rows || !row_counts || !corrections || !safety || row_width == 0 || !aligned16(bodies) ||
+        !aligned16(rows) || !aligned8(row_counts) || !aligned16(corrections) ||
+        !geometry_args(vertices_xy, vertex_count, triangles, triangle_count, g))
+        return BP_E_INVALID;
+    const size_t slots = (size_t)body_count * row_width;
+    if (slots > 0x7fffffffull) return BP_E_CAPACITY;
+    cudaStream_t s = (cudaStream_t)stream;
+    RBody* b = reinterpret_cast<RBody*>(bodies);
+    RCandidate* r = reinterpret_cast<RCandidate*>(rows);
+    const uint2* rc = reinterpret_cast<const uint2*>(row_counts);
+    RCorrection* c = reinterpret_cast<RCorrection*>(corrections);
+    rigid_contacts_kernel<<<(uint32_t)((slots + kRoundThreads - 1u) / kRoundThreads), kRoundThreads, 0, s>>>(
+        b, body_count, g, r, rc, row_width, c, safety);
+    rigid_apply_bodies_kernel<<<(body_count + kRoundThreads - 1u) / kRoundThreads, kRoundThreads, 0, s>>>(
+        b, body_count, r, rc, row_width, c);
+    return launch_status();
+}
+
+extern "C" int bp_rigid_guard_walls(bp_rigid_body* bodies, uint32_t body_count, const float* vertices_xy,
+                                    uint32_t vertex_count, const uint32_t* triangles, uint32_t triangle_count,
+                                    uint32_t bubble_count, const uint32_t* joint_ranges,
+                                    const uint64_t* joint_partners, uint32_t partner_count, uint32_t* safety,
+                                    void* stream) {
+    using namespace bp;
+    if (body_count == 0) return BP_OK;
+    Geo g;
+    if (!bodies || !safety || (!joint_partners && partner_count) || !aligned16(bodies) || !aligned16(joint_ranges) ||
+        !aligned8(joint_partners) || !geometry_args(vertices_xy, vertex_count, triangles, triangle_count, g))
+        return BP_E_INVALID;
+    rigid_guard_kernel<<<(body_count + kRoundThreads - 1u) / kRoundThreads, kRoundThreads, 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<RBody*>(bodies), body_count, g, bubble_count, reinterpret_cast<const uint4*>(joint_ranges),
+        reinterpret_cast<const unsigned long long*>(joint_partners), joint_ranges ? partner_count : 0u, safety);
     return launch_status();
 }

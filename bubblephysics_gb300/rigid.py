@@ -1,12 +1,11 @@
-"""Host side of the rigid body solver passes: joint records built like the reference's NativeJointState.prepare
-(Sources/BubblePhysicsNativeMetal/NativeJointState.swift:61-141), and the device passes bp_rigid_predict,
-bp_rigid_solve_joints and bp_rigid_finish on device buffers that this module owns.
+"""Host side of the rigid body solver: joint records built like the reference's NativeJointState.prepare
+(Sources/BubblePhysicsNativeMetal/NativeJointState.swift:61-141), and `RigidSolver`, which holds one world's rigid
+arrays in device memory and runs the library's rigid passes on them (bp_rigid_predict, bp_rigid_body_candidates,
+bp_rigid_ccd, bp_rigid_solve_contacts, bp_rigid_solve_joints, bp_rigid_guard_walls, bp_rigid_finish).
 
-The reference runs, once per step (NativeMetalSolver.swift:767-799): nativeRigidPredict, body-pair candidates and
-CCD, then 8 rounds of {body contacts, apply, nativeSolveJoints, nativeApplyJointBodies, wall guard}, and
-nativeRigidFinish after the bubble step. This library implements predict, the joint rounds and the finish; body-pair
-contacts, CCD and the wall guard are not implemented, so `RigidSolver.step` is the reference's step for bodies that
-meet no other body (jointed chains and mechanisms, bodies against segments).
+`RigidSolver.step` is the reference's rigid step (NativeMetalSolver.swift:767-799, 919): predict, body-pair rows,
+CCD, 8 rounds of {body contacts + apply, joints + apply, wall guard}, and the finish (which the reference runs after
+the bubble step).
 
 Device memory comes from torch (plumbing only); every computation runs in the library's CUDA kernels.
 """
@@ -136,7 +135,8 @@ class RigidSolver:
     arrays. The walls array (one record per body) is cleared before each predict."""
 
     def __init__(self, bodies: np.ndarray, vertices: np.ndarray, segments: Optional[np.ndarray] = None,
-                 joints: Optional[JointArrays] = None, bubble_count: int = 0, stream=None):
+                 joints: Optional[JointArrays] = None, bubble_count: int = 0, stream=None,
+                 triangles: Optional[np.ndarray] = None, row_width: int = 16):
         torch = self.torch = _torch()
         self.lib = N.library()
         self.stream = stream
@@ -157,6 +157,16 @@ class RigidSolver:
         self.d_vertices = dev(np.asarray(vertices, np.float32).reshape(-1, 2))
         self.d_segments = dev(np.zeros(0, N.SEGMENT_DTYPE) if segments is None else np.asarray(segments, N.SEGMENT_DTYPE))
         self.d_walls = torch.zeros(max(self.body_count, 1) * N.RIGID_WALL_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+        tris = np.zeros((0, 4), np.uint32) if triangles is None else np.asarray(triangles, np.uint32).reshape(-1, 4)
+        self.triangle_count = int(tris.shape[0])
+        self.d_triangles = dev(tris)
+        self.row_width = row_width
+        slots = max(self.body_count, 1) * row_width
+        self.d_rows = torch.zeros(slots * N.RIGID_CANDIDATE_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+        self.d_row_counts = torch.zeros(max(self.body_count, 1) * 2, dtype=torch.int32, device="cuda")
+        self.d_contact_corrections = torch.zeros(slots * N.RIGID_CORRECTION_DTYPE.itemsize, dtype=torch.uint8,
+                                                 device="cuda")
+        self.d_overflow = torch.zeros(4, dtype=torch.int32, device="cuda")
         self.d_safety = torch.zeros(4, dtype=torch.int32, device="cuda")
         if joints is not None and self.joint_count:
             self.d_joints = dev(joints.records)
@@ -204,11 +214,66 @@ class RigidSolver:
                                          self.vertex_count, r, self._p(self.d_safety), self._stream()),
                 "bp_rigid_finish")
 
+    def _geometry(self):
+        return (self._p(self.d_vertices), self.vertex_count,
+                self._p(self.d_triangles) if self.triangle_count else None, self.triangle_count)
+
+    def body_candidates(self) -> None:
+        """Body-pair rows (nativeRigidEmitCandidates, body pairs: NativeGeometryKernels:394-415)."""
+        N.check(self.lib.bp_rigid_body_candidates(self._p(self.d_bodies), self.body_count, self.bubble_count,
+                                                  self._p(self.d_ranges), self._p(self.d_partners),
+                                                  self.partner_count, self.row_width, self._p(self.d_rows),
+                                                  self._p(self.d_row_counts), self._p(self.d_overflow),
+                                                  self._stream()), "bp_rigid_body_candidates")
+
+    def ccd(self) -> None:
+        """Body-body CCD (nativeRigidResolveCCD + nativeRigidApplyCCD, NativePostSolveKernels:200-263)."""
+        N.check(self.lib.bp_rigid_ccd(self._p(self.d_bodies), self.body_count, *self._geometry(), self._p(self.d_rows),
+                                      self._p(self.d_row_counts), self.row_width, self._p(self.d_safety),
+                                      self._stream()), "bp_rigid_ccd")
+
+    def solve_contacts(self) -> None:
+        """One contact round (nativeRigidContacts + nativeRigidApplyBodies, NativeContactKernels:375-444)."""
+        N.check(self.lib.bp_rigid_solve_contacts(self._p(self.d_bodies), self.body_count, *self._geometry(),
+                                                 self._p(self.d_rows), self._p(self.d_row_counts), self.row_width,
+                                                 self._p(self.d_contact_corrections), self._p(self.d_safety),
+                                                 self._stream()), "bp_rigid_solve_contacts")
+
+    def guard_walls(self) -> None:
+        """The wall guard (nativeRigidGuardWalls, NativePostSolveKernels:118-170)."""
+        N.check(self.lib.bp_rigid_guard_walls(self._p(self.d_bodies), self.body_count, *self._geometry(),
+                                              self.bubble_count, self._p(self.d_ranges), self._p(self.d_partners),
+                                              self.partner_count, self._p(self.d_safety), self._stream()),
+                "bp_rigid_guard_walls")
+
     def step(self, dt: float, region: Sequence[float], iterations: int = ITERATIONS) -> None:
-        """The implemented rigid passes in the reference's order: predict, the joint rounds, finish."""
+        """One rigid step in the reference's order (NativeMetalSolver.swift:767-799, 919): predict, body-pair rows,
+        CCD, `iterations` rounds of {contacts, one joint round, wall guard}, finish."""
+        self.predict(dt)
+        self.body_candidates()
+        self.ccd()
+        for _ in range(iterations):
+            self.solve_contacts()
+            self.solve_joints(dt, 1, iterations)
+            self.guard_walls()
+        self.finish(region)
+
+    def step_without_contacts(self, dt: float, region: Sequence[float], iterations: int = ITERATIONS) -> None:
+        """The same step for a world whose bodies meet no other body and no static polygon (jointed mechanisms):
+        predict, all joint rounds in one call, finish - the same results in 3 to 2 + 2 x iterations launches."""
         self.predict(dt)
         self.solve_joints(dt, iterations, iterations)
         self.finish(region)
+
+    def candidates(self):
+        self.torch.cuda.synchronize()
+        rows = self.d_rows[:self.body_count * self.row_width * 32].cpu().numpy().view(N.RIGID_CANDIDATE_DTYPE)
+        counts = self.d_row_counts[:self.body_count * 2].cpu().numpy().view(np.uint32).reshape(-1, 2)
+        return rows.reshape(-1, self.row_width).copy(), counts.copy()
+
+    def overflow(self):
+        self.torch.cuda.synchronize()
+        return self.d_overflow[:2].cpu().numpy().view(np.uint32).copy()
 
     def bodies(self) -> np.ndarray:
         self.torch.cuda.synchronize()

@@ -439,9 +439,10 @@ class RigidScene:
     """Records of a rigid-solver world: RIGID_BODY_DTYPE bodies, their vertices (local to the centre of mass),
     SEGMENT_DTYPE static segments, the public joints, the bodies' object ids, the region and the step."""
 
-    def __init__(self, bodies, vertices, segments, joints, region, dt=DT):
+    def __init__(self, bodies, vertices, segments, joints, region, dt=DT, triangles=()):
         self.bodies = bodies
         self.vertices = np.asarray(vertices, np.float32).reshape(-1, 2)
+        self.triangles = np.asarray(triangles, np.uint32).reshape(-1, 4)
         self.segments = segments
         self.joints = joints
         self.body_ids = [int(i) for i in bodies["id"]]
@@ -583,3 +584,78 @@ def rigid_sweeps(seed: int = 7, movers: int = 96) -> RigidScene:
         bid += 1
     return RigidScene(np.array(bodies, N.RIGID_BODY_DTYPE), vertices, np.array(segments, N.SEGMENT_DTYPE), joints,
                       region, dt=DT)
+
+
+def _shape_record(body, kind, core_radius=0.0, half_length=0.0):
+    body["shape"] = (float(kind), core_radius, half_length, 0.0)
+    return body
+
+
+def rigid_pile(seed: int = 8, count: int = 256, columns: int = 16) -> RigidScene:
+    """Dynamic boxes, circles and capsules dropped in columns onto a static floor and ramps, some pairs joined
+    (with and without collideConnected): every part of the rigid step works here - body-pair rows, CCD of fast
+    bodies, polygon / round contacts with friction and restitution, the wall guard against the static polygons, and
+    the joint rounds. Bodies start just apart and fall at 60-240 units/s (the rigid predict applies no gravity)."""
+    from .rigid import Joint
+    rng = np.random.default_rng(seed)
+    bodies, vertices, triangles, joints = [], [], [], []
+
+    def polygon(points):
+        offset, tri = len(vertices), len(triangles)
+        vertices.extend(points)
+        for k in range(1, len(points) - 1):
+            triangles.append((0, k, k + 1, 0))
+        return offset, len(points), tri, len(points) - 2
+
+    def add_static_box(bid, cx, cy, hx, hy, angle=0.0):
+        off, n, tri, nt = polygon(_box(hx, hy))
+        b = _rigid_body(bid, (cx, cy, angle), off, n, 0.0, 0.0, math.hypot(hx, hy), static=True)
+        b["ranges"] = (off, n, tri, nt)
+        bodies.append(b)
+
+    add_static_box(1, 0.0, -10.0, 600.0, 10.0)
+    add_static_box(2, -300.0, 80.0, 120.0, 6.0, 0.35)
+    add_static_box(3, 300.0, 80.0, 120.0, 6.0, -0.35)
+    spacing = 18.0
+    bid = 100
+    for k in range(count):
+        col, row = k % columns, k // columns
+        cx = (col - columns / 2 + 0.5) * spacing + float(rng.uniform(-1.0, 1.0))
+        cy = 40.0 + row * spacing + float(rng.uniform(0.0, 2.0))
+        kind = k % 3
+        vy = -float(rng.uniform(60.0, 240.0))
+        vx = float(rng.normal(0.0, 20.0))
+        spin = float(rng.normal(0.0, 2.0))
+        if kind == 0:  # box
+            hx, hy = float(rng.uniform(4.0, 7.0)), float(rng.uniform(3.0, 6.0))
+            off, n, tri, nt = polygon(_box(hx, hy))
+            mass = 4.0 * hx * hy
+            inertia = mass * ((2 * hx) ** 2 + (2 * hy) ** 2) / 12.0
+            b = _rigid_body(bid, (cx, cy, float(rng.uniform(-0.5, 0.5))), off, n, 1.0 / mass, 1.0 / inertia,
+                            math.hypot(hx, hy), velocity=(vx, vy), spin=spin, restitution=float(rng.choice([0.0, 0.3])),
+                            friction=float(rng.uniform(0.2, 0.8)))
+            b["ranges"] = (off, n, tri, nt)
+        elif kind == 1:  # circle
+            r = float(rng.uniform(3.0, 6.0))
+            off = len(vertices)
+            vertices.append((0.0, 0.0))
+            mass = math.pi * r * r
+            b = _rigid_body(bid, (cx, cy, 0.0), off, 1, 1.0 / mass, 2.0 / (mass * r * r), r, velocity=(vx, vy),
+                            spin=spin, friction=float(rng.uniform(0.2, 0.8)))
+            _shape_record(b, 1, r)
+        else:  # capsule
+            r, h = float(rng.uniform(2.0, 4.0)), float(rng.uniform(2.0, 5.0))
+            off = len(vertices)
+            vertices.extend([(-h, 0.0), (h, 0.0)])
+            mass = math.pi * r * r + 4.0 * h * r
+            inertia = mass * ((2 * h) ** 2 / 12.0 + r * r / 2.0)
+            b = _rigid_body(bid, (cx, cy, float(rng.uniform(-1.0, 1.0))), off, 2, 1.0 / mass, 1.0 / inertia, h + r,
+                            velocity=(vx, vy), spin=spin, restitution=0.2, friction=0.5)
+            _shape_record(b, 2, r, h)
+        bodies.append(b)
+        if k >= columns and k % 7 == 0:  # joined to the body below it
+            joints.append(Joint(len(joints) + 1, bid - columns, bid, "distance", length=spacing, softness=1e-3,
+                                collide_connected=k % 2 == 0))
+        bid += 1
+    return RigidScene(np.array(bodies, N.RIGID_BODY_DTYPE), vertices, np.zeros(0, N.SEGMENT_DTYPE), joints,
+                      (-2000.0, -2000.0, 2000.0, 4000.0), triangles=triangles)

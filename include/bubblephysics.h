@@ -558,13 +558,12 @@ int bp_world_step_noalloc(const bp_world_desc* desc, bp_bubble* bubbles, uint32_
                           const bp_segment* segments, uint32_t segment_count, uint32_t steps,
                           bp_step_report* reports, void* stream);
 
-/* ---- rigid body solver: predict, joints, finish -------------------------------------------------------------- */
+/* ---- rigid body solver ------------------------------------------------------------------------------------------ */
 
 /* The rigid solver's records, laid out like the reference's so its buffers bind unchanged. Bodies step once per step,
  * before the bubble substeps (NativeMetalSolver.swift:767-799): predict, body-pair candidates and CCD, then 8
  * iterations of {body contacts, apply, joints, apply joints, wall guard}; the finish runs after the bubble step.
- * This library implements predict, the joint pair and the finish; body-pair contacts, CCD and the wall guard
- * (nativeRigidContacts .. nativeRigidGuardWalls) are not implemented. */
+ * Each entry below replaces one of those kernels (or kernel pairs) on the caller's device arrays. */
 
 /* One rigid body (NativeRigidBody, NativeRigidPolygonState.swift:25-40 / NativeGeometryKernels:35-41). 160 bytes. */
 typedef struct bp_rigid_body {
@@ -611,6 +610,14 @@ typedef struct bp_rigid_wall {
     float extra[4];              /* normal momentum stopped by the sweep x dt; three reserved */
 } bp_rigid_wall;
 
+/* One body-pair candidate of a body's row (NativeCandidate, NativeGeometryKernels:30): participants are the two
+ * bodies' ids; metadata = (kind 3, lower body index, higher body index, float bits of the row's summed normal lambda
+ * of the step). Rows are `row_width` entries per body, sorted by (kind, participants). 32 bytes. */
+typedef struct bp_rigid_candidate {
+    int64_t participants[2];
+    uint32_t metadata[4];
+} bp_rigid_candidate;
+
 /* Safety bits OR-ed into *safety (the reference's safety word 3). */
 enum {
     BP_RIGID_SAFETY_NONFINITE = 1u,         /* a pose or motion became non-finite */
@@ -652,6 +659,42 @@ int bp_rigid_solve_joints(bp_rigid_body* bodies, uint32_t body_count, bp_rigid_j
  * (flags[2] = 2). region = (min x, min y, max x, max y), read on the host at the call. */
 int bp_rigid_finish(bp_rigid_body* bodies, uint32_t body_count, const float* vertices_xy, uint32_t vertex_count,
                     const float* region, uint32_t* safety, void* stream);
+
+/* Body-pair rows (nativeRigidEmitCandidates in its body-pair mode, NativeGeometryKernels:394-415): for each body, the
+ * other bodies (not both immovable, filters accepting, not joined without collideConnected) whose swept centre
+ * distance comes within 1.25 x the sum of bounding radii; the `row_width` smallest keys are kept in order.
+ * row_counts gets (entries, 0) per body; overflow[0] += dropped entries, overflow[1] = max(overflow[1], wanted). */
+int bp_rigid_body_candidates(const bp_rigid_body* bodies, uint32_t body_count, uint32_t bubble_count,
+                             const uint32_t* joint_ranges, const uint64_t* joint_partners, uint32_t partner_count,
+                             uint32_t row_width, bp_rigid_candidate* rows, uint32_t* row_counts, uint32_t* overflow,
+                             void* stream);
+
+/* Body-body CCD (nativeRigidResolveCCD then nativeRigidApplyCCD, NativePostSolveKernels:200-263): every movable
+ * body finds the earliest time of impact on its row's pairs (sampled every 0.5 units of travel, at most 64 samples,
+ * 12 bisections; a pair overlapping at the start is left to the contacts), then moves back along its step to it.
+ * `triangles` are uint32 quadruples (three indices into the body's vertex range, one unused), like the reference's
+ * uint4 buffer; triangle_count counts quadruples. */
+int bp_rigid_ccd(bp_rigid_body* bodies, uint32_t body_count, const float* vertices_xy, uint32_t vertex_count,
+                 const uint32_t* triangles, uint32_t triangle_count, const bp_rigid_candidate* rows,
+                 const uint32_t* row_counts, uint32_t row_width, uint32_t* safety, void* stream);
+
+/* One contact round (nativeRigidContacts then nativeRigidApplyBodies, NativeContactKernels:375-444): every row slot
+ * computes its pair's contact (polygon triangles by SAT, circle / capsule cores, round against polygon) and the
+ * pair's half position and velocity corrections with friction (geometric mean) and restitution (maximum), adding
+ * the normal lambda to the slot's metadata[3]; then every body adds its row's corrections in order. `corrections`
+ * has row_width entries per body. */
+int bp_rigid_solve_contacts(bp_rigid_body* bodies, uint32_t body_count, const float* vertices_xy,
+                            uint32_t vertex_count, const uint32_t* triangles, uint32_t triangle_count,
+                            bp_rigid_candidate* rows, const uint32_t* row_counts, uint32_t row_width,
+                            bp_rigid_correction* corrections, uint32_t* safety, void* stream);
+
+/* The wall guard (nativeRigidGuardWalls, NativePostSolveKernels:118-170): each dynamic body's vertices against the
+ * static polygon bodies; a vertex that entered one (or crossed an edge within the step) is pushed out along the
+ * nearest edge's normal and the approaching velocity is removed. */
+int bp_rigid_guard_walls(bp_rigid_body* bodies, uint32_t body_count, const float* vertices_xy, uint32_t vertex_count,
+                         const uint32_t* triangles, uint32_t triangle_count, uint32_t bubble_count,
+                         const uint32_t* joint_ranges, const uint64_t* joint_partners, uint32_t partner_count,
+                         uint32_t* safety, void* stream);
 
 /* ---- host helpers (reference host logic that feeds the path) -------------------------------------------------- */
 

@@ -2432,6 +2432,461 @@ void solve(bp_rigid_joint& joint, bp_rigid_correction& out, const bp_rigid_body*
     out.velocity_second[2] = turnB / dt + spinB;
 }
 
+// ---- body contacts, candidates, CCD, wall guard -------------------------------------------------------------
+
+inline bool is_round(const bp_rigid_body& b) { return b.shape[0] > 0.5f; }
+inline bool immovable(const bp_rigid_body& b) { return b.flags[0] != 0 || b.filter[2] != 0; }
+inline bool accepts(const uint32_t* a, const uint32_t* b) { return (a[0] & b[1]) != 0 && (b[0] & a[1]) != 0; }
+inline float distance(P2 a, P2 b) { return length(a - b); }
+
+struct Geo {
+    const float* verts;
+    uint32_t vertexCount;
+    const uint32_t* tris;  // uint4 per triangle (indices into the body's vertex range, pad)
+    uint32_t triangleCount;
+};
+
+inline P2 local_vertex(const Geo& g, const bp_rigid_body& b, uint32_t i) {
+    const uint32_t at = b.ranges[0] + i;
+    return p2(g.verts[2 * at], g.verts[2 * at + 1]);
+}
+// nativeRigidVertex (NGK:139-141)
+inline P2 world_vertex(const Geo& g, const bp_rigid_body& b, uint32_t i) {
+    return p2(b.pose[0], b.pose[1]) + rotate(local_vertex(g, b, i), b.pose[2]);
+}
+
+// A body's vertex and triangle ranges lie inside the arrays and its triangles index its own vertices.
+bool geometry_ok(const Geo& g, const bp_rigid_body& b) {
+    if (!vertices_ok(b, g.vertexCount)) return false;
+    if (b.ranges[3] > g.triangleCount || b.ranges[2] > g.triangleCount - b.ranges[3]) return false;
+    for (uint32_t i = 0; i < b.ranges[3]; ++i) {
+        const uint32_t* t = g.tris + 4 * (size_t)(b.ranges[2] + i);
+        if (t[0] >= b.ranges[1] || t[1] >= b.ranges[1] || t[2] >= b.ranges[1]) return false;
+    }
+    return is_round(b) ? b.ranges[1] >= 1 : true;
+}
+
+// nativeSegmentDistance (NGK:444-462)
+float segment_distance(P2 a, P2 b, P2 c, P2 d, P2& pa, P2& pb) {
+    const P2 r = b - a, s = d - c;
+    const float denominator = cross(r, s);
+    if (std::fabs(denominator) > 1e-12f) {
+        const P2 qp = c - a;
+        const float t = cross(qp, s) / denominator, u = cross(qp, r) / denominator;
+        if (t >= 0 && t <= 1 && u >= 0 && u <= 1) { pa = a + r * t; pb = pa; return 0; }
+    }
+    float best = std::numeric_limits<float>::infinity();
+    P2 cp = closest(a, c, d);
+    float value = distance(a, cp);
+    if (value < best) { best = value; pa = a; pb = cp; }
+    cp = closest(b, c, d); value = distance(b, cp);
+    if (value < best) { best = value; pa = b; pb = cp; }
+    cp = closest(c, a, b); value = distance(c, cp);
+    if (value < best) { best = value; pa = cp; pb = c; }
+    cp = closest(d, a, b); value = distance(d, cp);
+    if (value < best) { best = value; pa = cp; pb = d; }
+    return best;
+}
+
+struct Core { P2 a, b; float radius; };
+// nativeRoundCoreOf (NGK:466-472)
+Core core_of(const Geo& g, const bp_rigid_body& b) {
+    Core c;
+    c.a = world_vertex(g, b, 0);
+    c.b = b.ranges[1] > 1 ? world_vertex(g, b, 1) : c.a;
+    c.radius = b.shape[1];
+    return c;
+}
+
+// nativeRigidInside (NGK:477-490)
+bool rigid_inside(const Geo& g, P2 p, const bp_rigid_body& b) {
+    if (is_round(b)) {
+        const Core c = core_of(g, b);
+        return distance(p, closest(p, c.a, c.b)) <= c.radius;
+    }
+    const P2 local = rotate(p - p2(b.pose[0], b.pose[1]), -b.pose[2]);
+    for (uint32_t i = 0; i < b.ranges[3]; ++i) {
+        const uint32_t* t = g.tris + 4 * (size_t)(b.ranges[2] + i);
+        const P2 A = local_vertex(g, b, t[0]), B = local_vertex(g, b, t[1]), C = local_vertex(g, b, t[2]);
+        if (cross(B - A, local - A) >= 0 && cross(C - B, local - B) >= 0 && cross(A - C, local - C) >= 0) return true;
+    }
+    return false;
+}
+
+// nativeRoundContact (NGK:546-581)
+bool round_contact(const Core& A, const Core& B, P2 fallback, P2& normal, float& depth, P2& point) {
+    P2 pa, pb;
+    const float separation = segment_distance(A.a, A.b, B.a, B.b, pa, pb);
+    if (separation > 1e-4f) {
+        normal = (pb - pa) / separation;
+        depth = A.radius + B.radius - separation;
+        point = ((pa + normal * A.radius) + (pb - normal * B.radius)) * 0.5f;
+        return true;
+    }
+    P2 axes[2];
+    uint32_t axisCount = 0;
+    const P2 ea = A.b - A.a, eb = B.b - B.a;
+    const float la = length(ea), lb = length(eb);
+    if (la > 1e-6f) axes[axisCount++] = p2(-ea.y, ea.x) / la;
+    if (lb > 1e-6f) axes[axisCount++] = p2(-eb.y, eb.x) / lb;
+    P2 axis = fallback;
+    float overlap = 0, orientation = 1, best = std::numeric_limits<float>::infinity();
+    for (uint32_t i = 0; i < axisCount; ++i) {
+        const P2 c = axes[i];
+        const float amin = std::fmin(dot(A.a, c), dot(A.b, c)), amax = std::fmax(dot(A.a, c), dot(A.b, c));
+        const float bmin = std::fmin(dot(B.a, c), dot(B.b, c)), bmax = std::fmax(dot(B.a, c), dot(B.b, c));
+        const float plus = amax - bmin, minus = bmax - amin;
+        const float value = std::fmin(plus, minus);
+        if (value < best) {
+            best = value; axis = c; overlap = value;
+            if (std::fabs(plus - minus) < 1e-6f) orientation = dot(c, fallback) >= 0 ? 1.0f : -1.0f;
+            else orientation = plus < minus ? 1.0f : -1.0f;
+        }
+    }
+    normal = axis * orientation;
+    depth = overlap + A.radius + B.radius;
+    point = (pa + pb) * 0.5f;
+    return true;
+}
+
+// nativeTriangleContact (NCK:248-275)
+bool triangle_contact(const P2* a, const P2* b, P2& normal, float& depth, P2& point) {
+    depth = std::numeric_limits<float>::infinity();
+    for (int shape = 0; shape < 2; ++shape)
+        for (int edge = 0; edge < 3; ++edge) {
+            const P2 delta = shape == 0 ? a[(edge + 1) % 3] - a[edge] : b[(edge + 1) % 3] - b[edge];
+            const float magnitude = length(delta);
+            if (magnitude <= kMin) return false;
+            const P2 axis = p2(-delta.y, delta.x) / magnitude;
+            float amin = std::numeric_limits<float>::infinity(), amax = -amin, bmin = amin, bmax = -amin;
+            for (int k = 0; k < 3; ++k) {
+                const float pa = dot(a[k], axis), pb = dot(b[k], axis);
+                amin = std::fmin(amin, pa); amax = std::fmax(amax, pa);
+                bmin = std::fmin(bmin, pb); bmax = std::fmax(bmax, pb);
+            }
+            if (amax < bmin || bmax < amin) return false;
+            const float plus = amax - bmin, minus = bmax - amin;
+            const float overlap = std::fmin(plus, minus);
+            if (overlap < depth) { depth = overlap; normal = plus < minus ? axis : neg(axis); }
+        }
+    float maxA = -std::numeric_limits<float>::infinity(), minB = std::numeric_limits<float>::infinity();
+    P2 pa = p2(0, 0), pb = p2(0, 0);
+    uint32_t na = 0, nb = 0;
+    for (int k = 0; k < 3; ++k) { maxA = std::fmax(maxA, dot(a[k], normal)); minB = std::fmin(minB, dot(b[k], normal)); }
+    for (int k = 0; k < 3; ++k) {
+        if (dot(a[k], normal) >= maxA - 1e-5f) { pa = pa + a[k]; ++na; }
+        if (dot(b[k], normal) <= minB + 1e-5f) { pb = pb + b[k]; ++nb; }
+    }
+    point = (pa / (float)na + pb / (float)nb) * 0.5f;
+    return true;
+}
+
+inline P2 outward_of(P2 p, P2 q) {
+    const P2 edge = q - p;
+    const float size = length(edge);
+    return size > kMin ? p2(edge.y, -edge.x) / size : p2(0, 1);
+}
+
+// nativeRoundPolygonContact (NCK:277-333): normal from the round core R to the polygon P.
+bool round_polygon_contact(const Geo& g, const Core& R, const bp_rigid_body& P, P2& normal, float& depth, P2& point) {
+    const uint32_t count = P.ranges[1];
+    float insideDepth = -1;
+    P2 insideOutward = p2(0, 0), insidePoint = p2(0, 0);
+    const uint32_t endpoints = (R.b.x != R.a.x || R.b.y != R.a.y) ? 2u : 1u;
+    uint32_t insideEndpoints = 0;
+    for (uint32_t k = 0; k < endpoints; ++k) {
+        const P2 endpoint = k == 0 ? R.a : R.b;
+        if (!rigid_inside(g, endpoint, P)) continue;
+        ++insideEndpoints;
+        float nearest = std::numeric_limits<float>::infinity();
+        P2 nearestPoint = p2(0, 0), nearestOutward = p2(0, 0);
+        for (uint32_t e = 0; e < count; ++e) {
+            const P2 p = world_vertex(g, P, e), q = world_vertex(g, P, (e + 1) % count);
+            const P2 c = closest(endpoint, p, q);
+            const float d = distance(endpoint, c);
+            if (d < nearest) { nearest = d; nearestPoint = c; nearestOutward = outward_of(p, q); }
+        }
+        if (nearest > insideDepth) { insideDepth = nearest; insidePoint = nearestPoint; insideOutward = nearestOutward; }
+    }
+    if (insideEndpoints == endpoints) {
+        normal = neg(insideOutward); depth = R.radius + insideDepth; point = insidePoint;
+        return true;
+    }
+    float best = std::numeric_limits<float>::infinity();
+    P2 pc = p2(0, 0), pe = p2(0, 0);
+    for (uint32_t e = 0; e < count; ++e) {
+        const P2 p = world_vertex(g, P, e), q = world_vertex(g, P, (e + 1) % count);
+        P2 ca, ce;
+        const float d = segment_distance(R.a, R.b, p, q, ca, ce);
+        if (d < best) { best = d; pc = ca; pe = ce; }
+    }
+    if (best > 1e-4f) {
+        normal = (pe - pc) / best; depth = R.radius - best; point = pe;
+        return true;
+    }
+    float minimum = std::numeric_limits<float>::infinity();
+    P2 minimumOutward = p2(0, 1), minimumPoint = pe;
+    for (uint32_t e = 0; e < count; ++e) {
+        const P2 p = world_vertex(g, P, e), q = world_vertex(g, P, (e + 1) % count);
+        const P2 edge = q - p;
+        const float size = length(edge);
+        if (size <= kMin) continue;
+        const P2 outward = p2(edge.y, -edge.x) / size;
+        const float da = dot(R.a - p, outward), db = dot(R.b - p, outward);
+        const float d = R.radius - std::fmin(da, db);
+        if (d < minimum) {
+            minimum = d; minimumOutward = outward;
+            minimumPoint = (da <= db ? R.a : R.b) - outward * std::fmin(da, db);
+        }
+    }
+    normal = neg(minimumOutward); depth = std::isfinite(minimum) ? minimum : R.radius; point = minimumPoint;
+    return true;
+}
+
+// nativeRoundCoreCrossesPolygon (NCK:335-344)
+bool round_core_crosses_polygon(const Geo& g, const Core& R, const bp_rigid_body& P) {
+    if (rigid_inside(g, R.a, P) || rigid_inside(g, R.b, P)) return true;
+    for (uint32_t e = 0; e < P.ranges[1]; ++e) {
+        const P2 p = world_vertex(g, P, e), q = world_vertex(g, P, (e + 1) % P.ranges[1]);
+        P2 ca, ce;
+        if (segment_distance(R.a, R.b, p, q, ca, ce) <= 1e-4f) return true;
+    }
+    return false;
+}
+
+// nativeRigidPairContact (NCK:348-373): normal from a to b; false = the shapes do not overlap.
+bool pair_contact(const Geo& g, const bp_rigid_body& a, const bp_rigid_body& b, P2& n, float& depth, P2& point) {
+    const bool aRound = is_round(a), bRound = is_round(b);
+    if (aRound && bRound) return round_contact(core_of(g, a), core_of(g, b), p2(1, 0), n, depth, point);
+    if (aRound != bRound) {
+        const bp_rigid_body& round = aRound ? a : b;
+        const bp_rigid_body& polygon = aRound ? b : a;
+        P2 normal;
+        if (!round_polygon_contact(g, core_of(g, round), polygon, normal, depth, point)) return false;
+        n = aRound ? normal : neg(normal);
+        return true;
+    }
+    bool found = false;
+    for (uint32_t i = 0; i < a.ranges[3]; ++i)
+        for (uint32_t j = 0; j < b.ranges[3]; ++j) {
+            const uint32_t* ta = g.tris + 4 * (size_t)(a.ranges[2] + i);
+            const uint32_t* tb = g.tris + 4 * (size_t)(b.ranges[2] + j);
+            const P2 av[3] = {world_vertex(g, a, ta[0]), world_vertex(g, a, ta[1]), world_vertex(g, a, ta[2])};
+            const P2 bv[3] = {world_vertex(g, b, tb[0]), world_vertex(g, b, tb[1]), world_vertex(g, b, tb[2])};
+            P2 normal, p;
+            float d;
+            if (triangle_contact(av, bv, normal, d, p) && (!found || d > depth)) { found = true; depth = d; n = normal; point = p; }
+        }
+    return found;
+}
+
+// nativeKeyLess / nativeInsertCandidate (NGK:230-251): a row keeps its `limit` smallest keys in order.
+bool key_less(const bp_rigid_candidate& a, const bp_rigid_candidate& b) {
+    if (a.metadata[0] != b.metadata[0]) return a.metadata[0] < b.metadata[0];
+    if (a.participants[0] != b.participants[0]) return a.participants[0] < b.participants[0];
+    return a.participants[1] < b.participants[1];
+}
+void insert_candidate(bp_rigid_candidate* row, uint32_t& count, uint32_t& dropped, uint32_t limit,
+                      const bp_rigid_candidate& value) {
+    uint32_t location;
+    if (count < limit) location = count++;
+    else {
+        ++dropped;
+        if (!key_less(value, row[limit - 1])) return;
+        location = limit - 1;
+    }
+    while (location > 0 && key_less(value, row[location - 1])) { row[location] = row[location - 1]; --location; }
+    row[location] = value;
+}
+
+// nativeEmitBodyCandidates, body pairs (NGK:394-415, mode `bodies`)
+void body_candidates(const bp_rigid_body* bodies, uint32_t count, uint32_t bubbleCount, const uint32_t* ranges,
+                     const uint64_t* partners, uint32_t partnerCount, uint32_t limit, bp_rigid_candidate* rows,
+                     uint32_t* rowCounts, uint32_t* overflow) {
+    for (uint32_t index = 0; index < count; ++index) {
+        bp_rigid_candidate* row = rows + (size_t)index * limit;
+        uint32_t n = 0, dropped = 0;
+        for (uint32_t other = 0; other < count; ++other) {
+            if (other == index) continue;
+            const uint32_t low = std::min(index, other), high = std::max(index, other);
+            const bp_rigid_body& a = bodies[low];
+            const bp_rigid_body& c = bodies[high];
+            if (immovable(a) && immovable(c)) continue;
+            if (!accepts(a.filter, c.filter)) continue;
+            if (excluded(ranges, partners, partnerCount, bubbleCount + index, bodies[other].id)) continue;
+            const P2 start = p2(a.previous[0], a.previous[1]) - p2(c.previous[0], c.previous[1]);
+            const P2 end = p2(a.pose[0], a.pose[1]) - p2(c.pose[0], c.pose[1]);
+            const P2 travel = end - start;
+            const float travelSquared = dot(travel, travel);
+            const float t = travelSquared > kMin ? clampf(-dot(start, travel) / travelSquared, 0.0f, 1.0f) : 0.0f;
+            const float radius = 1.25f * (a.physical[2] + c.physical[2]);
+            const P2 closestPoint = start + travel * t;
+            if (!(dot(closestPoint, closestPoint) <= radius * radius)) continue;
+            bp_rigid_candidate value{};
+            value.participants[0] = (int64_t)a.id; value.participants[1] = (int64_t)c.id;
+            value.metadata[0] = 3; value.metadata[1] = low; value.metadata[2] = high; value.metadata[3] = 0;
+            insert_candidate(row, n, dropped, limit, value);
+        }
+        rowCounts[2 * index] = n;
+        rowCounts[2 * index + 1] = 0;  // no bubble candidates in the body-pair rows
+        overflow[0] += dropped;
+        overflow[1] = std::max(overflow[1], n + dropped);
+    }
+}
+
+inline float as_float(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
+inline uint32_t as_uint(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
+
+// A candidate row entry points at bodies inside the array.
+inline bool candidate_ok(const bp_rigid_candidate& c, uint32_t count) { return c.metadata[1] < count && c.metadata[2] < count; }
+
+// nativeRigidContacts (NCK:375-427), one row slot.
+void contact_slot(const Geo& g, const bp_rigid_body* bodies, uint32_t count, bp_rigid_candidate& candidate,
+                  bp_rigid_correction& correction, uint32_t* safety) {
+    const bp_rigid_correction previous = correction;
+    bp_rigid_correction result{};
+    result.first[3] = previous.first[3]; result.second[3] = previous.second[3];
+    result.velocity_first[3] = previous.velocity_first[3]; result.velocity_second[3] = previous.velocity_second[3];
+    correction = result;
+    if (candidate.metadata[0] != 3) return;
+    if (!candidate_ok(candidate, count)) { *safety |= BP_RIGID_SAFETY_INVALID; return; }
+    const uint32_t ai = candidate.metadata[1], bi = candidate.metadata[2];
+    const bp_rigid_body& a = bodies[ai];
+    const bp_rigid_body& b = bodies[bi];
+    if (ai >= bi || (immovable(a) && immovable(b))) return;
+    if (!geometry_ok(g, a) || !geometry_ok(g, b)) { *safety |= BP_RIGID_SAFETY_INVALID; return; }
+    const P2 end = p2(a.pose[0], a.pose[1]) - p2(b.pose[0], b.pose[1]);
+    const float radius = a.physical[2] + b.physical[2], radiusSquared = radius * radius;
+    if (dot(end, end) > radiusSquared) return;
+    P2 n, point;
+    float depth;
+    if (!pair_contact(g, a, b, n, depth, point)) return;
+    const float wa = a.physical[0], wb = b.physical[0], ia = a.physical[1], ib = b.physical[1];
+    const P2 ra = point - p2(a.pose[0], a.pose[1]), rb = point - p2(b.pose[0], b.pose[1]);
+    const P2 va = p2(a.motion[0], a.motion[1]), vb = p2(b.motion[0], b.motion[1]);
+    const float spinA = a.motion[2], spinB = b.motion[2];
+    const float frictionA = a.physical[3], frictionB = b.physical[3];
+    const float restitutionA = as_float(a.flags[3]), restitutionB = as_float(b.flags[3]);
+    const float ca = cross(ra, n), cb = cross(rb, n), denom = wa + wb + ia * ca * ca + ib * cb * cb;
+    if (depth < -0.001f || denom <= kMin) return;
+    const float lambda = std::fmax(0.0f, depth) / denom * 0.5f;
+    candidate.metadata[3] = as_uint(as_float(candidate.metadata[3]) + lambda);
+    const P2 moveA = neg(n) * wa * lambda, moveB = n * wb * lambda;
+    correction.first[0] = moveA.x; correction.first[1] = moveA.y; correction.first[2] = -ca * ia * lambda;
+    correction.first[3] = n.x;
+    correction.second[0] = moveB.x; correction.second[1] = moveB.y; correction.second[2] = cb * ib * lambda;
+    correction.second[3] = n.y;
+    const float closing = dot(vb - va, n) + spinB * cb - spinA * ca;
+    const float friction = std::sqrt(std::fmax(0.0f, frictionA * frictionB));
+    const float restitution = std::fmax(restitutionA, restitutionB);
+    const float impulse = std::fmax(0.0f, -closing) * (1.0f + restitution) / denom * 0.5f;
+    const P2 tangent = p2(-n.y, n.x);
+    const float tangentSpeed = dot(vb - va, tangent) + spinB * cross(rb, tangent) - spinA * cross(ra, tangent);
+    const float tangentImpulse = -tangentSpeed * friction / denom * 0.5f;
+    const P2 vA = neg(n) * wa * impulse - tangent * wa * tangentImpulse;
+    const P2 vB = n * wb * impulse + tangent * wb * tangentImpulse;
+    correction.velocity_first[0] = vA.x; correction.velocity_first[1] = vA.y;
+    correction.velocity_first[2] = -ca * ia * impulse - cross(ra, tangent) * ia * tangentImpulse;
+    correction.velocity_first[3] = point.x;
+    correction.velocity_second[0] = vB.x; correction.velocity_second[1] = vB.y;
+    correction.velocity_second[2] = cb * ib * impulse + cross(rb, tangent) * ib * tangentImpulse;
+    correction.velocity_second[3] = point.y;
+}
+
+// nativeRigidOverlapAt / nativeRigidTimeOfImpact (NPK:200-233)
+bool overlap_at(const Geo& g, bp_rigid_body a, bp_rigid_body b, float t) {
+    a.pose[0] = a.previous[0] + (a.pose[0] - a.previous[0]) * t; a.pose[1] = a.previous[1] + (a.pose[1] - a.previous[1]) * t;
+    a.pose[2] = a.pose[3] + (a.pose[2] - a.pose[3]) * t;
+    b.pose[0] = b.previous[0] + (b.pose[0] - b.previous[0]) * t; b.pose[1] = b.previous[1] + (b.pose[1] - b.previous[1]) * t;
+    b.pose[2] = b.pose[3] + (b.pose[2] - b.pose[3]) * t;
+    P2 n, point;
+    float depth;
+    return pair_contact(g, a, b, n, depth, point) && depth > 1e-3f;
+}
+float time_of_impact(const Geo& g, const bp_rigid_body& a, const bp_rigid_body& b) {
+    const P2 da = p2(a.pose[0], a.pose[1]) - p2(a.previous[0], a.previous[1]);
+    const P2 db = p2(b.pose[0], b.pose[1]) - p2(b.previous[0], b.previous[1]);
+    const float travel = length(da - db) + std::fabs(a.pose[2] - a.pose[3]) * a.physical[2] +
+                         std::fabs(b.pose[2] - b.pose[3]) * b.physical[2];
+    if (!(travel > 0.5f)) return 2;
+    if (overlap_at(g, a, b, 0)) return 2;
+    const float samples = std::ceil(travel / 0.5f);
+    const uint32_t steps = samples >= 64.0f ? 64u : std::max(2u, (uint32_t)samples);
+    float last = 0;
+    for (uint32_t step = 1; step <= steps; ++step) {
+        const float t = (float)step / (float)steps;
+        if (!overlap_at(g, a, b, t)) { last = t; continue; }
+        float low = last, high = t;
+        for (int bisection = 0; bisection < 12; ++bisection) {
+            const float middle = 0.5f * (low + high);
+            if (overlap_at(g, a, b, middle)) high = middle; else low = middle;
+        }
+        return low;
+    }
+    return 2;
+}
+
+// nativeRigidGuardWalls (NPK:118-170), one body.
+void guard_body(const Geo& g, bp_rigid_body* bodies, uint32_t count, uint32_t index, uint32_t bubbleCount,
+                const uint32_t* ranges, const uint64_t* partners, uint32_t partnerCount, uint32_t* safety) {
+    if (bodies[index].flags[0] || bodies[index].filter[2]) return;
+    bp_rigid_body b = bodies[index];
+    if (!geometry_ok(g, b)) { *safety |= BP_RIGID_SAFETY_INVALID; return; }
+    for (uint32_t j = 0; j < count; ++j) {
+        const bp_rigid_body& wall = bodies[j];
+        if (!wall.flags[0] || is_round(wall) || !accepts(b.filter, wall.filter)) continue;
+        if (excluded(ranges, partners, partnerCount, bubbleCount + index, wall.id)) continue;
+        if (!geometry_ok(g, wall)) { *safety |= BP_RIGID_SAFETY_INVALID; continue; }
+        const uint32_t wn = wall.ranges[1];
+        for (uint32_t k = 0; k < b.ranges[1]; ++k) {
+            const P2 p = world_vertex(g, b, k);
+            const P2 start = p2(b.previous[0], b.previous[1]) + rotate(local_vertex(g, b, k), b.pose[3]);
+            const bool inside = rigid_inside(g, p, wall);
+            bool startedInside = rigid_inside(g, start, wall);
+            if (startedInside)
+                for (uint32_t e = 0; e < wn; ++e) {
+                    const P2 ea = world_vertex(g, wall, e), eb = world_vertex(g, wall, (e + 1) % wn);
+                    if (distance(start, closest(start, ea, eb)) < 1e-5f) { startedInside = false; break; }
+                }
+            float nearest = std::numeric_limits<float>::infinity(), depth = 0;
+            P2 normal = p2(0, 0);
+            for (uint32_t e = 0; e < wn; ++e) {
+                const P2 ea = world_vertex(g, wall, e), eb = world_vertex(g, wall, (e + 1) % wn);
+                const P2 direction = eb - ea;
+                const P2 raw = p2(direction.y, -direction.x);
+                const P2 out = raw / length(raw);
+                const float signedStart = dot(start - ea, out);
+                const bool onBoundary = distance(start, closest(start, ea, eb)) < 1e-5f;
+                const bool crossing = signedStart >= -1e-5f &&
+                                      (center_crossing(start, p, ea, eb, ea, eb) || (onBoundary && dot(p - ea, out) < 0));
+                if (!inside && !crossing) continue;
+                if (inside && !startedInside && signedStart < -1e-5f) continue;
+                const P2 c = closest(p, ea, eb);
+                const float d = (crossing || !startedInside) ? distance(start, closest(start, ea, eb)) : distance(p, c);
+                if (d < nearest) { nearest = d; normal = out; depth = std::fmax(0.0f, -dot(p - c, out)); }
+            }
+            if (std::isfinite(nearest) && depth > 0) {
+                if (is_round(b)) {
+                    bp_rigid_body old = b;
+                    old.pose[0] = b.previous[0]; old.pose[1] = b.previous[1]; old.pose[2] = b.pose[3];
+                    if (round_core_crosses_polygon(g, core_of(g, old), wall)) break;
+                }
+                const P2 shift = normal * (depth + 1e-5f);
+                b.pose[0] = b.pose[0] + shift.x; b.pose[1] = b.pose[1] + shift.y;
+                const P2 r = p - p2(b.pose[0], b.pose[1]);
+                const float lever = cross(r, normal);
+                const float speed = dot(p2(b.motion[0], b.motion[1]), normal) + b.motion[2] * lever;
+                const float denom = b.physical[0] + b.physical[1] * lever * lever;
+                const float impulse = std::fmax(0.0f, -speed) / std::fmax(denom, kMin);
+                const P2 dv = normal * b.physical[0] * impulse;
+                b.motion[0] = b.motion[0] + dv.x; b.motion[1] = b.motion[1] + dv.y;
+                b.motion[2] = b.motion[2] + lever * b.physical[1] * impulse;
+            }
+        }
+    }
+    bodies[index] = b;
+}
+
 }  // namespace rigid
 
 extern "C" {
@@ -2495,6 +2950,95 @@ int bpo_rigid_solve_joints(bp_rigid_body* bodies, uint32_t body_count, bp_rigid_
 int bpo_rigid_finish(bp_rigid_body* bodies, uint32_t body_count, const float* vertices_xy, uint32_t vertex_count,
                      const float* region, uint32_t* safety) {
     rigid::finish(bodies, body_count, vertices_xy, vertex_count, region, safety);
+    return BP_OK;
+}
+
+int bpo_rigid_body_candidates(const bp_rigid_body* bodies, uint32_t body_count, uint32_t bubble_count,
+                              const uint32_t* joint_ranges, const uint64_t* joint_partners, uint32_t partner_count,
+                              uint32_t row_width, bp_rigid_candidate* rows, uint32_t* row_counts, uint32_t* overflow) {
+    rigid::body_candidates(bodies, body_count, bubble_count, joint_ranges, joint_partners,
+                           joint_ranges ? partner_count : 0u, row_width, rows, row_counts, overflow);
+    return BP_OK;
+}
+
+// nativeRigidResolveCCD then nativeRigidApplyCCD (NPK:235-263): every body's earliest impact from the state before
+// any body moves back, then the moves.
+int bpo_rigid_ccd(bp_rigid_body* bodies, uint32_t body_count, const float* vertices_xy, uint32_t vertex_count,
+                  const uint32_t* triangles, uint32_t triangle_count, const bp_rigid_candidate* rows,
+                  const uint32_t* row_counts, uint32_t row_width, uint32_t* safety) {
+    const rigid::Geo g{vertices_xy, vertex_count, triangles, triangle_count};
+    std::vector<float> marker(body_count, 0.0f);
+    for (uint32_t index = 0; index < body_count; ++index) {
+        float earliest = 2;
+        if (!rigid::immovable(bodies[index])) {
+            const uint32_t n = std::min(row_counts[2 * index], row_width);
+            for (uint32_t slot = row_counts[2 * index + 1]; slot < n; ++slot) {
+                const bp_rigid_candidate& c = rows[(size_t)index * row_width + slot];
+                if (c.metadata[0] != 3) continue;
+                if (!rigid::candidate_ok(c, body_count) || !rigid::geometry_ok(g, bodies[c.metadata[1]]) ||
+                    !rigid::geometry_ok(g, bodies[c.metadata[2]])) { *safety |= BP_RIGID_SAFETY_INVALID; continue; }
+                earliest = std::fmin(earliest, rigid::time_of_impact(g, bodies[c.metadata[1]], bodies[c.metadata[2]]));
+            }
+        }
+        marker[index] = earliest <= 1 ? 1 + earliest : 0;
+    }
+    for (uint32_t index = 0; index < body_count; ++index) {
+        bp_rigid_body& b = bodies[index];
+        b.limits[2] = marker[index];
+        if (b.limits[2] >= 1) {
+            const float t = b.limits[2] - 1;
+            b.pose[0] = b.previous[0] + (b.pose[0] - b.previous[0]) * t;
+            b.pose[1] = b.previous[1] + (b.pose[1] - b.previous[1]) * t;
+            b.pose[2] = b.pose[3] + (b.pose[2] - b.pose[3]) * t;
+        }
+        b.limits[2] = 0;
+    }
+    return BP_OK;
+}
+
+// One round of nativeRigidContacts (every slot from the same state) then nativeRigidApplyBodies (NCK:375-444).
+int bpo_rigid_solve_contacts(bp_rigid_body* bodies, uint32_t body_count, const float* vertices_xy, uint32_t vertex_count,
+                             const uint32_t* triangles, uint32_t triangle_count, bp_rigid_candidate* rows,
+                             const uint32_t* row_counts, uint32_t row_width, bp_rigid_correction* corrections,
+                             uint32_t* safety) {
+    const rigid::Geo g{vertices_xy, vertex_count, triangles, triangle_count};
+    for (uint32_t owner = 0; owner < body_count; ++owner) {
+        const uint32_t n = std::min(row_counts[2 * owner], row_width);
+        for (uint32_t slot = 0; slot < n; ++slot) {
+            const size_t at = (size_t)owner * row_width + slot;
+            rigid::contact_slot(g, bodies, body_count, rows[at], corrections[at], safety);
+        }
+    }
+    for (uint32_t index = 0; index < body_count; ++index) {
+        float delta[3] = {0, 0, 0}, velocity[3] = {0, 0, 0};
+        const uint32_t n = std::min(row_counts[2 * index], row_width);
+        for (uint32_t slot = 0; slot < n; ++slot) {
+            const size_t at = (size_t)index * row_width + slot;
+            const bool first = rows[at].metadata[0] == 3 && rows[at].metadata[1] == index;
+            const bp_rigid_correction& c = corrections[at];
+            for (int q = 0; q < 3; ++q) {
+                delta[q] = delta[q] + (first ? c.first[q] : c.second[q]);
+                velocity[q] = velocity[q] + (first ? c.velocity_first[q] : c.velocity_second[q]);
+            }
+        }
+        for (int q = 0; q < 3; ++q) {
+            bodies[index].pose[q] = bodies[index].pose[q] + delta[q];
+            bodies[index].motion[q] = bodies[index].motion[q] + velocity[q];
+        }
+    }
+    return BP_OK;
+}
+
+// nativeRigidGuardWalls (NPK:118-170): each dynamic body in turn against the static polygons; a body only writes
+// itself and reads static bodies, so the order does not matter.
+int bpo_rigid_guard_walls(bp_rigid_body* bodies, uint32_t body_count, const float* vertices_xy, uint32_t vertex_count,
+                          const uint32_t* triangles, uint32_t triangle_count, uint32_t bubble_count,
+                          const uint32_t* joint_ranges, const uint64_t* joint_partners, uint32_t partner_count,
+                          uint32_t* safety) {
+    const rigid::Geo g{vertices_xy, vertex_count, triangles, triangle_count};
+    for (uint32_t index = 0; index < body_count; ++index)
+        rigid::guard_body(g, bodies, body_count, index, bubble_count, joint_ranges, joint_partners,
+                          joint_ranges ? partner_count : 0u, safety);
     return BP_OK;
 }
 

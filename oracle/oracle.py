@@ -64,6 +64,13 @@ def library() -> C.CDLL:
                                                  C.c_float, C.c_uint32, C.c_uint32, P]),
             "bpo_rigid_finish": (C.c_int, [P, C.c_uint32, P, C.c_uint32, P, P]),
             "bpo_sincos": (C.c_int, [P, P, C.c_uint32]),
+            "bpo_rigid_body_candidates": (C.c_int, [P, C.c_uint32, C.c_uint32, P, P, C.c_uint32, C.c_uint32, P, P,
+                                                    P]),
+            "bpo_rigid_ccd": (C.c_int, [P, C.c_uint32, P, C.c_uint32, P, C.c_uint32, P, P, C.c_uint32, P]),
+            "bpo_rigid_solve_contacts": (C.c_int, [P, C.c_uint32, P, C.c_uint32, P, C.c_uint32, P, P, C.c_uint32, P,
+                                                   P]),
+            "bpo_rigid_guard_walls": (C.c_int, [P, C.c_uint32, P, C.c_uint32, P, C.c_uint32, C.c_uint32, P, P,
+                                                C.c_uint32, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -261,11 +268,20 @@ def sincos(x: np.ndarray) -> np.ndarray:
 
 class OracleRigid:
     """The rigid solver passes on host arrays (the oracle of bubblephysics_gb300.rigid.RigidSolver): predict
-    (NPK:66-115), the joint rounds (NCK:446-562) and finish (NPK:172-198), same arguments and record layouts."""
+    (NPK:66-115), body-pair rows, CCD, contact rounds, the joint rounds (NCK:375-562), the wall guard and finish
+    (NPK:118-263), same arguments and record layouts."""
 
-    def __init__(self, bodies, vertices, segments=None, joints=None, bubble_count: int = 0):
+    def __init__(self, bodies, vertices, segments=None, joints=None, bubble_count: int = 0, triangles=None,
+                 row_width: int = 16):
         self.body_records = np.array(bodies, N.RIGID_BODY_DTYPE)
         self.vertices = np.ascontiguousarray(np.asarray(vertices, np.float32).reshape(-1, 2))
+        self.triangles = np.ascontiguousarray(np.zeros((0, 4), np.uint32) if triangles is None
+                                              else np.asarray(triangles, np.uint32).reshape(-1, 4))
+        self.row_width = row_width
+        self.rows = np.zeros(max(len(self.body_records), 1) * row_width, N.RIGID_CANDIDATE_DTYPE)
+        self.row_counts = np.zeros((max(len(self.body_records), 1), 2), np.uint32)
+        self.contact_corrections = np.zeros(max(len(self.body_records), 1) * row_width, N.RIGID_CORRECTION_DTYPE)
+        self.overflow_words = np.zeros(2, np.uint32)
         self.segments = np.zeros(0, N.SEGMENT_DTYPE) if segments is None else np.array(segments, N.SEGMENT_DTYPE)
         self.bubble_count = bubble_count
         if joints is not None and len(joints.records):
@@ -307,10 +323,51 @@ class OracleRigid:
         library().bpo_rigid_finish(self._p(self.body_records), len(self.body_records), self._p(self.vertices),
                                    self.vertices.shape[0], self._p(r), self._p(self.safety_word))
 
-    def step(self, dt: float, region, iterations: int = 8) -> None:
+    def _geometry(self):
+        return (self._p(self.vertices), self.vertices.shape[0], self._p(self.triangles), self.triangles.shape[0])
+
+    def body_candidates(self) -> None:
+        library().bpo_rigid_body_candidates(self._p(self.body_records), len(self.body_records), self.bubble_count,
+                                            self._p(self.ranges), self._p(self.partners), self.partners.size,
+                                            self.row_width, self._p(self.rows), self._p(self.row_counts),
+                                            self._p(self.overflow_words))
+
+    def ccd(self) -> None:
+        library().bpo_rigid_ccd(self._p(self.body_records), len(self.body_records), *self._geometry(),
+                                self._p(self.rows), self._p(self.row_counts), self.row_width, self._p(self.safety_word))
+
+    def solve_contacts(self) -> None:
+        library().bpo_rigid_solve_contacts(self._p(self.body_records), len(self.body_records), *self._geometry(),
+                                           self._p(self.rows), self._p(self.row_counts), self.row_width,
+                                           self._p(self.contact_corrections), self._p(self.safety_word))
+
+    def guard_walls(self) -> None:
+        library().bpo_rigid_guard_walls(self._p(self.body_records), len(self.body_records), *self._geometry(),
+                                        self.bubble_count, self._p(self.ranges), self._p(self.partners),
+                                        self.partners.size, self._p(self.safety_word))
+
+    def step_without_contacts(self, dt: float, region, iterations: int = 8) -> None:
         self.predict(dt)
         self.solve_joints(dt, iterations, iterations)
         self.finish(region)
+
+    def overflow_counts(self):
+        return self.overflow_words.copy()
+
+    def step(self, dt: float, region, iterations: int = 8) -> None:
+        """The reference's rigid step order: predict, body-pair rows, CCD, `iterations` rounds of {contacts, one
+        joint round, wall guard}, finish."""
+        self.predict(dt)
+        self.body_candidates()
+        self.ccd()
+        for _ in range(iterations):
+            self.solve_contacts()
+            self.solve_joints(dt, 1, iterations)
+            self.guard_walls()
+        self.finish(region)
+
+    def candidates(self) -> np.ndarray:
+        return self.rows.reshape(-1, self.row_width).copy(), self.row_counts.copy()
 
     def bodies(self) -> np.ndarray:
         return self.body_records.copy()

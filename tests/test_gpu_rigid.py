@@ -98,3 +98,26 @@ def test_records_outside_their_arrays_are_skipped_and_flagged(ctx):
         side.step(scene.dt, scene.region, ITERATIONS)
     same_state(gpu, cpu, "invalid records")
     assert gpu.safety() & N.RIGID_SAFETY_INVALID
+
+
+@pytest.mark.parametrize("row_width", [32, 8])  # 8: the floors' rows overflow and keep their smallest keys
+def test_pile_whole_rigid_step_matches_the_oracle(ctx, row_width):
+    """Boxes, circles and capsules dropped on static floors: body-pair rows, CCD, contact rounds with friction and
+    restitution, joint rounds and the wall guard, 25 steps of the reference's whole rigid step."""
+    scene = scenes.rigid_pile(count=192)
+    arrays = scene.joint_arrays()
+    gpu = RigidSolver(scene.bodies, scene.vertices, scene.segments, arrays, triangles=scene.triangles,
+                      row_width=row_width)
+    cpu = OracleRigid(scene.bodies, scene.vertices, scene.segments, arrays, triangles=scene.triangles,
+                      row_width=row_width)
+    for step in range(25):
+        for side in (gpu, cpu):
+            side.step(scene.dt, scene.region)
+        same_state(gpu, cpu, f"step {step}")
+        (rows_g, counts_g), (rows_c, counts_c) = gpu.candidates(), cpu.candidates()
+        assert np.array_equal(counts_g, counts_c), f"step {step}: row counts"
+        for i, n in enumerate(counts_g[:, 0]):
+            assert np.array_equal(rows_g[i, :n]["participants"], rows_c[i, :n]["participants"]), (step, i)
+            assert np.array_equal(rows_g[i, :n]["metadata"], rows_c[i, :n]["metadata"]), (step, i)
+        assert np.array_equal(gpu.overflow(), cpu.overflow_counts()), f"step {step}: overflow"
+    assert (rows_g["metadata"][:, :, 3] != 0).any()  # contacts carried normal impulses

@@ -305,3 +305,63 @@ def test_finish_removes_or_wraps_bodies_outside_the_region():
     want = np_finish(start, scene.vertices, scene.region)
     assert np.array_equal(got["pose"], want["pose"]) and np.array_equal(got["flags"], want["flags"])
     assert (got["flags"][:, 2] == 1).sum() == 4 and (got["flags"][:, 2] == 2).sum() == 4
+
+
+# ---- body contacts, rows, CCD, wall guard ---------------------------------------------------------------------------
+
+def pile_oracle(row_width=32, **kw):
+    scene = scenes.rigid_pile(**kw)
+    arrays = scene.joint_arrays()
+    return scene, OracleRigid(scene.bodies, scene.vertices, scene.segments, arrays, triangles=scene.triangles,
+                              row_width=row_width)
+
+
+def test_body_pair_rows_are_sorted_and_symmetric():
+    scene, o = pile_oracle()
+    o.predict(scene.dt)
+    o.body_candidates()
+    rows, counts = o.candidates()
+    assert counts[:, 1].sum() == 0 and counts[:, 0].sum() > 0
+    pairs = set()
+    for i, (row, n) in enumerate(zip(rows, counts[:, 0])):
+        keys = [(int(c["metadata"][0]), int(c["participants"][0]), int(c["participants"][1])) for c in row[:n]]
+        assert keys == sorted(keys)
+        for c in row[:n]:
+            low, high = int(c["metadata"][1]), int(c["metadata"][2])
+            assert c["metadata"][0] == 3 and low < high and i in (low, high)
+            pairs.add((low, high, i))
+    full = {i for i, n in enumerate(counts[:, 0]) if n < o.row_width}  # rows that dropped nothing
+    for low, high, owner in pairs:
+        other = high if owner == low else low
+        if other in full:
+            assert (low, high, other) in pairs
+
+
+def test_pile_settles_on_the_floor_without_tunnelling():
+    scene, o = pile_oracle()
+    for _ in range(60):
+        o.step(scene.dt, scene.region)
+    b = o.bodies()
+    assert o.safety() == 0 and np.isfinite(b["pose"]).all()
+    dynamic = b["flags"][:, 0] == 0
+    # every dynamic body's centre stays above the floor's top face (y = 0) by more than a fraction of its size
+    assert (b["pose"][dynamic, 1] > 0.5).all(), b["pose"][dynamic, 1].min()
+    assert np.abs(b["motion"][dynamic, :2]).max() < 250.0
+    assert (o.rows["metadata"][:, 3] != 0).sum() > 100  # contacts carried normal impulses
+
+
+def test_ccd_stops_a_fast_body_before_it_passes_through_another():
+    from bubblephysics_gb300.rigid import prepare_joints
+    verts = scenes._box(20.0, 20.0) + scenes._box(2.0, 2.0)
+    tris = [(0, 1, 2, 0), (0, 2, 3, 0)] * 2
+    wall = scenes._rigid_body(1, (0.0, 0.0, 0.0), 0, 4, 0.0, 0.0, 28.3, static=True)
+    wall["ranges"] = (0, 4, 0, 2)
+    bullet = scenes._rigid_body(2, (-60.0, 0.0, 0.0), 4, 4, 1 / 16, 1 / 43, 2.9, velocity=(6000.0, 0.0))
+    bullet["ranges"] = (4, 4, 2, 2)
+    o = OracleRigid(np.array([wall, bullet]), verts, None, None, triangles=tris)
+    o.predict(1 / 60)
+    assert o.bodies()[1]["pose"][0] > 20.0  # the integration alone carries it through the wall
+    o.body_candidates()
+    o.ccd()
+    x = float(o.bodies()[1]["pose"][0])
+    assert -24.0 < x < -21.0, x  # stopped at the wall's near face (half widths 20 + 2)
