@@ -829,41 +829,57 @@ __device__ void insert_candidate(RCandidate* row, uint32_t& count, uint32_t& dro
     row[location] = value;
 }
 
-// nativeEmitBodyCandidates, body pairs (NGK:394-415): one thread per body and row.
+// nativeEmitBodyCandidates, body pairs (NGK:394-415): one warp per body and row. The lanes test 32 other bodies at
+// a time and lane 0 inserts the hits in increasing index order, the order of the reference's one-thread loop.
 __global__ void __launch_bounds__(kRoundThreads) rigid_candidates_kernel(const RBody* bodies, uint32_t bodyCount,
                                                                        uint32_t bubbleCount, const uint4* jointRanges,
                                                                        const unsigned long long* partners,
                                                                        uint32_t partnerCount, uint32_t limit,
                                                                        RCandidate* rows, uint2* rowCounts,
                                                                        uint32_t* overflow) {
-    const uint32_t index = blockIdx.x * blockDim.x + threadIdx.x;
-    if (index >= bodyCount) return;
+    const uint32_t index = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (index >= bodyCount) return;  // whole warps
     RCandidate* row = rows + (size_t)index * limit;
     uint32_t count = 0, dropped = 0;
-    for (uint32_t other = 0; other < bodyCount; ++other) {
-        if (other == index) continue;
-        const uint32_t low = min(index, other), high = max(index, other);
-        const RBody& a = bodies[low];
-        const RBody& c = bodies[high];
-        if (immovable(a) && immovable(c)) continue;
-        if (!accepts(a, c)) continue;
-        if (joint_excluded(jointRanges, partners, partnerCount, bubbleCount + index, bodies[other].id)) continue;
-        const float2 start = sub(f2(a.previous.x, a.previous.y), f2(c.previous.x, c.previous.y));
-        const float2 end = sub(pose_xy(a), pose_xy(c));
-        const float2 travel = sub(end, start);
-        const float travelSquared = dot2(travel, travel);
-        const float t = travelSquared > kFltMin ? clampf(-dot2(start, travel) / travelSquared, 0.0f, 1.0f) : 0.0f;
-        const float radius = 1.25f * (a.physical.z + c.physical.z);
-        const float2 closest = add(start, mul(travel, t));
-        if (!(dot2(closest, closest) <= radius * radius)) continue;
-        RCandidate value;
-        value.first = (long long)a.id; value.second = (long long)c.id;
-        value.meta = make_uint4(3u, low, high, 0u);
-        insert_candidate(row, count, dropped, limit, value);
+    for (uint32_t base = 0; base < bodyCount; base += 32u) {
+        const uint32_t other = base + lane;
+        bool hit = false;
+        if (other < bodyCount && other != index) {
+            const uint32_t low = min(index, other), high = max(index, other);
+            const RBody& a = bodies[low];
+            const RBody& c = bodies[high];
+            hit = !(immovable(a) && immovable(c)) && accepts(a, c) &&
+                  !joint_excluded(jointRanges, partners, partnerCount, bubbleCount + index, bodies[other].id);
+            if (hit) {
+                const float2 start = sub(f2(a.previous.x, a.previous.y), f2(c.previous.x, c.previous.y));
+                const float2 end = sub(pose_xy(a), pose_xy(c));
+                const float2 travel = sub(end, start);
+                const float travelSquared = dot2(travel, travel);
+                const float t =
+                    travelSquared > kFltMin ? clampf(-dot2(start, travel) / travelSquared, 0.0f, 1.0f) : 0.0f;
+                const float radius = 1.25f * (a.physical.z + c.physical.z);
+                const float2 closest = add(start, mul(travel, t));
+                hit = dot2(closest, closest) <= radius * radius;
+            }
+        }
+        unsigned int hits = __ballot_sync(0xffffffffu, hit);
+        if (lane == 0u) {
+            while (hits) {
+                const uint32_t o = base + (uint32_t)(__ffs(hits) - 1);
+                hits &= hits - 1u;
+                const uint32_t low = min(index, o), high = max(index, o);
+                RCandidate value;
+                value.first = (long long)bodies[low].id; value.second = (long long)bodies[high].id;
+                value.meta = make_uint4(3u, low, high, 0u);
+                insert_candidate(row, count, dropped, limit, value);
+            }
+        }
     }
-    rowCounts[index] = make_uint2(count, 0u);
-    if (dropped) atomicAdd(overflow, dropped);
-    atomicMax(overflow + 1, count + dropped);
+    if (lane == 0u) {
+        rowCounts[index] = make_uint2(count, 0u);
+        if (dropped) atomicAdd(overflow, dropped);
+        atomicMax(overflow + 1, count + dropped);
+    }
 }
 
 __device__ __forceinline__ bool candidate_ok(const RCandidate& c, uint32_t count) {
@@ -903,18 +919,19 @@ __device__ float time_of_impact(const Geo& g, const RBody& a, const RBody& b) {
     return 2.0f;
 }
 
-// nativeRigidResolveCCD (NPK:235-250): the earliest impact of the body's row, kept in its own limits.z (1 + t).
+// nativeRigidResolveCCD (NPK:235-250): the earliest impact of the body's row, kept in its own limits.z (1 + t). One
+// warp per body, a lane per row slot; the minimum does not depend on the order of the slots.
 __global__ void __launch_bounds__(kRoundThreads) rigid_ccd_resolve_kernel(RBody* bodies, uint32_t bodyCount, Geo g,
                                                                         const RCandidate* rows,
                                                                         const uint2* rowCounts, uint32_t width,
                                                                         uint32_t* safety) {
-    const uint32_t index = blockIdx.x * blockDim.x + threadIdx.x;
-    if (index >= bodyCount) return;
+    const uint32_t index = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (index >= bodyCount) return;  // whole warps
     float earliest = 2.0f;
     if (!immovable(bodies[index])) {
         const uint2 rc = rowCounts[index];
         const uint32_t n = min(rc.x, width);
-        for (uint32_t slot = rc.y; slot < n; ++slot) {
+        for (uint32_t slot = rc.y + lane; slot < n; slot += 32u) {
             const RCandidate c = rows[(size_t)index * width + slot];
             if (c.meta.x != 3u) continue;
             if (!candidate_ok(c, bodyCount)) { atomicOr(safety, BP_RIGID_SAFETY_INVALID); continue; }
@@ -923,7 +940,10 @@ __global__ void __launch_bounds__(kRoundThreads) rigid_ccd_resolve_kernel(RBody*
             earliest = fminf(earliest, time_of_impact(g, a, b));
         }
     }
-    bodies[index].limits.z = earliest <= 1.0f ? 1.0f + earliest : 0.0f;
+#pragma unroll
+    for (int offset = 16; offset > 0; offset >>= 1) earliest = fminf(earliest, __shfl_xor_sync(0xffffffffu, earliest, offset));
+    __syncwarp();
+    if (lane == 0u) bodies[index].limits.z = earliest <= 1.0f ? 1.0f + earliest : 0.0f;
 }
 
 // nativeRigidApplyCCD (NPK:253-263)
@@ -1043,6 +1063,10 @@ __global__ void __launch_bounds__(kRoundThreads) rigid_guard_kernel(RBody* bodie
     if (bodies[index].flags.x || bodies[index].filter.z) return;
     RBody b = bodies[index];
     if (!geometry_ok(g, b)) { atomicOr(safety, BP_RIGID_SAFETY_INVALID); return; }
+    // the guard moves a body without turning it: one (cos, sin) of its end angle and one of its start angle serve
+    // every vertex; each wall's pose is fixed, so one pair per wall serves all its vertices (the same bits as
+    // rotating each vertex by its angle)
+    const float2 bodyCS = sincos_cw(b.pose.z), startCS = sincos_cw(b.pose.w);
     for (uint32_t j = 0; j < bodyCount; ++j) {
         if (!bodies[j].flags.x) continue;
         const RBody wall = bodies[j];
@@ -1050,20 +1074,36 @@ __global__ void __launch_bounds__(kRoundThreads) rigid_guard_kernel(RBody* bodie
         if (joint_excluded(jointRanges, partners, partnerCount, bubbleCount + index, wall.id)) continue;
         if (!geometry_ok(g, wall)) { atomicOr(safety, BP_RIGID_SAFETY_INVALID); continue; }
         const uint32_t wn = wall.ranges.y;
+        const float2 wallCS = sincos_cw(wall.pose.z), wallInverse = sincos_cw(-wall.pose.z);
+        const float2 wallAt = pose_xy(wall);
+        auto wall_vertex = [&](uint32_t e) { return add(wallAt, rot_cs(g.verts[wall.ranges.x + e], wallCS.x, wallCS.y)); };
+        // nativeRigidInside for the polygon wall (NGK:485-490)
+        auto inside_wall = [&](float2 q) {
+            const float2 local = rot_cs(sub(q, wallAt), wallInverse.x, wallInverse.y);
+            for (uint32_t i = 0; i < wall.ranges.w; ++i) {
+                const uint4 t = g.tris[wall.ranges.z + i];
+                const float2 A = g.verts[wall.ranges.x + t.x], B = g.verts[wall.ranges.x + t.y];
+                const float2 C = g.verts[wall.ranges.x + t.z];
+                if (cross2(sub(B, A), sub(local, A)) >= 0.0f && cross2(sub(C, B), sub(local, B)) >= 0.0f &&
+                    cross2(sub(A, C), sub(local, C)) >= 0.0f)
+                    return true;
+            }
+            return false;
+        };
         for (uint32_t k = 0; k < b.ranges.y; ++k) {
-            const float2 p = world_vertex(g, b, k);
-            const float2 start = add(f2(b.previous.x, b.previous.y), rotate_by(g.verts[b.ranges.x + k], b.pose.w));
-            const bool inside = rigid_inside_body(g, p, wall);
-            bool startedInside = rigid_inside_body(g, start, wall);
+            const float2 p = add(pose_xy(b), rot_cs(g.verts[b.ranges.x + k], bodyCS.x, bodyCS.y));
+            const float2 start = add(f2(b.previous.x, b.previous.y), rot_cs(g.verts[b.ranges.x + k], startCS.x, startCS.y));
+            const bool inside = inside_wall(p);
+            bool startedInside = inside_wall(start);
             if (startedInside)
                 for (uint32_t e = 0; e < wn; ++e) {
-                    const float2 ea = world_vertex(g, wall, e), eb = world_vertex(g, wall, (e + 1u) % wn);
+                    const float2 ea = wall_vertex(e), eb = wall_vertex((e + 1u) % wn);
                     if (dist2(start, closest_point(start, ea, eb)) < 1e-5f) { startedInside = false; break; }
                 }
             float nearest = INFINITY, depth = 0.0f;
             float2 normal = f2(0.0f, 0.0f);
             for (uint32_t e = 0; e < wn; ++e) {
-                const float2 ea = world_vertex(g, wall, e), eb = world_vertex(g, wall, (e + 1u) % wn);
+                const float2 ea = wall_vertex(e), eb = wall_vertex((e + 1u) % wn);
                 const float2 direction = sub(eb, ea);
                 const float2 out = normalized(f2(direction.y, -direction.x));
                 const float signedStart = dot2(sub(start, ea), out);
@@ -1199,7 +1239,7 @@ extern "C" int bp_rigid_body_candidates(const bp_rigid_body* bodies, uint32_t bo
     if (!aligned16(bodies) || !aligned16(rows) || !aligned8(row_counts) || !aligned16(joint_ranges) ||
         !aligned8(joint_partners))
         return BP_E_INVALID;
-    const uint32_t blocks = (body_count + kRoundThreads - 1u) / kRoundThreads;
+    const uint32_t blocks = (uint32_t)(((size_t)body_count * 32u + kRoundThreads - 1u) / kRoundThreads);
     rigid_candidates_kernel<<<blocks, kRoundThreads, 0, (cudaStream_t)stream>>>(
         reinterpret_cast<const RBody*>(bodies), body_count, bubble_count, reinterpret_cast<const uint4*>(joint_ranges),
         reinterpret_cast<const unsigned long long*>(joint_partners), joint_ranges ? partner_count : 0u, row_width,
@@ -1230,11 +1270,13 @@ extern "C" int bp_rigid_ccd(bp_rigid_body* bodies, uint32_t body_count, const fl
         !aligned8(row_counts) || !geometry_args(vertices_xy, vertex_count, triangles, triangle_count, g))
         return BP_E_INVALID;
     const uint32_t blocks = (body_count + kRoundThreads - 1u) / kRoundThreads;
+    const uint32_t warpBlocks = (uint32_t)(((size_t)body_count * 32u + kRoundThreads - 1u) / kRoundThreads);
     cudaStream_t s = (cudaStream_t)stream;
     RBody* b = reinterpret_cast<RBody*>(bodies);
-    rigid_ccd_resolve_kernel<<<blocks, kRoundThreads, 0, s>>>(b, body_count, g, reinterpret_cast<const RCandidate*>(rows),
-                                                              reinterpret_cast<const uint2*>(row_counts), row_width,
-                                                              safety);
+    rigid_ccd_resolve_kernel<<<warpBlocks, kRoundThreads, 0, s>>>(b, body_count, g,
+                                                                  reinterpret_cast<const RCandidate*>(rows),
+                                                                  reinterpret_cast<const uint2*>(row_counts),
+                                                                  row_width, safety);
     rigid_ccd_apply_kernel<<<blocks, kRoundThreads, 0, s>>>(b, body_count);
     return launch_status();
 }
