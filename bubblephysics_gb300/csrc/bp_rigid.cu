@@ -1053,89 +1053,132 @@ __global__ void __launch_bounds__(kRoundThreads) rigid_apply_bodies_kernel(RBody
     bodies[index].motion = motion;
 }
 
-// nativeRigidGuardWalls (NPK:118-170): one thread per dynamic body; static bodies are never written.
+// nativeRigidGuardWalls (NPK:118-170): one warp per dynamic body; static bodies are never written. The walls, the
+// vertices of the body and their corrections stay in the reference's order (a correction moves the body before its
+// next vertex); within one vertex the lanes split the wall's triangles and edges: "inside" is an OR over triangles,
+// the start-on-the-boundary test an OR over edges, and the nearest edge the smallest (distance, edge index) pair,
+// which is the edge the reference's strict "<" loop keeps. Every lane keeps the same copy of the body.
 __global__ void __launch_bounds__(kRoundThreads) rigid_guard_kernel(RBody* bodies, uint32_t bodyCount, Geo g,
                                                                   uint32_t bubbleCount, const uint4* jointRanges,
                                                                   const unsigned long long* partners,
                                                                   uint32_t partnerCount, uint32_t* safety) {
-    const uint32_t index = blockIdx.x * blockDim.x + threadIdx.x;
-    if (index >= bodyCount) return;
+    const uint32_t index = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (index >= bodyCount) return;  // whole warps
     if (bodies[index].flags.x || bodies[index].filter.z) return;
     RBody b = bodies[index];
-    if (!geometry_ok(g, b)) { atomicOr(safety, BP_RIGID_SAFETY_INVALID); return; }
+    if (!geometry_ok(g, b)) {
+        if (lane == 0u) atomicOr(safety, BP_RIGID_SAFETY_INVALID);
+        return;
+    }
     // the guard moves a body without turning it: one (cos, sin) of its end angle and one of its start angle serve
     // every vertex; each wall's pose is fixed, so one pair per wall serves all its vertices (the same bits as
     // rotating each vertex by its angle)
     const float2 bodyCS = sincos_cw(b.pose.z), startCS = sincos_cw(b.pose.w);
-    for (uint32_t j = 0; j < bodyCount; ++j) {
-        if (!bodies[j].flags.x) continue;
-        const RBody wall = bodies[j];
-        if (is_round(wall) || !accepts(b, wall)) continue;
-        if (joint_excluded(jointRanges, partners, partnerCount, bubbleCount + index, wall.id)) continue;
-        if (!geometry_ok(g, wall)) { atomicOr(safety, BP_RIGID_SAFETY_INVALID); continue; }
-        const uint32_t wn = wall.ranges.y;
-        const float2 wallCS = sincos_cw(wall.pose.z), wallInverse = sincos_cw(-wall.pose.z);
-        const float2 wallAt = pose_xy(wall);
-        auto wall_vertex = [&](uint32_t e) { return add(wallAt, rot_cs(g.verts[wall.ranges.x + e], wallCS.x, wallCS.y)); };
-        // nativeRigidInside for the polygon wall (NGK:485-490)
-        auto inside_wall = [&](float2 q) {
-            const float2 local = rot_cs(sub(q, wallAt), wallInverse.x, wallInverse.y);
-            for (uint32_t i = 0; i < wall.ranges.w; ++i) {
-                const uint4 t = g.tris[wall.ranges.z + i];
-                const float2 A = g.verts[wall.ranges.x + t.x], B = g.verts[wall.ranges.x + t.y];
-                const float2 C = g.verts[wall.ranges.x + t.z];
-                if (cross2(sub(B, A), sub(local, A)) >= 0.0f && cross2(sub(C, B), sub(local, B)) >= 0.0f &&
-                    cross2(sub(A, C), sub(local, C)) >= 0.0f)
-                    return true;
+    for (uint32_t base = 0; base < bodyCount; base += 32u) {
+        // the lanes find this chunk's walls; they are then visited in index order
+        const uint32_t candidate = base + lane;
+        bool isWall = false;
+        if (candidate < bodyCount && bodies[candidate].flags.x) {
+            const RBody& w = bodies[candidate];
+            isWall = !is_round(w) && accepts(b, w) &&
+                     !joint_excluded(jointRanges, partners, partnerCount, bubbleCount + index, w.id);
+        }
+        unsigned int walls = __ballot_sync(0xffffffffu, isWall);
+        while (walls) {
+            const uint32_t j = base + (uint32_t)(__ffs(walls) - 1);
+            walls &= walls - 1u;
+            const RBody wall = bodies[j];
+            if (!geometry_ok(g, wall)) {
+                if (lane == 0u) atomicOr(safety, BP_RIGID_SAFETY_INVALID);
+                continue;
             }
-            return false;
-        };
-        for (uint32_t k = 0; k < b.ranges.y; ++k) {
-            const float2 p = add(pose_xy(b), rot_cs(g.verts[b.ranges.x + k], bodyCS.x, bodyCS.y));
-            const float2 start = add(f2(b.previous.x, b.previous.y), rot_cs(g.verts[b.ranges.x + k], startCS.x, startCS.y));
-            const bool inside = inside_wall(p);
-            bool startedInside = inside_wall(start);
-            if (startedInside)
-                for (uint32_t e = 0; e < wn; ++e) {
+            const uint32_t wn = wall.ranges.y, wt = wall.ranges.w;
+            const float2 wallCS = sincos_cw(wall.pose.z), wallInverse = sincos_cw(-wall.pose.z);
+            const float2 wallAt = pose_xy(wall);
+            auto wall_vertex = [&](uint32_t e) {
+                return add(wallAt, rot_cs(g.verts[wall.ranges.x + e], wallCS.x, wallCS.y));
+            };
+            // nativeRigidInside for the polygon wall (NGK:485-490), the triangles split over the lanes
+            auto inside_wall = [&](float2 q) {
+                const float2 local = rot_cs(sub(q, wallAt), wallInverse.x, wallInverse.y);
+                bool in = false;
+                for (uint32_t i = lane; i < wt; i += 32u) {
+                    const uint4 t = g.tris[wall.ranges.z + i];
+                    const float2 A = g.verts[wall.ranges.x + t.x], B = g.verts[wall.ranges.x + t.y];
+                    const float2 C = g.verts[wall.ranges.x + t.z];
+                    in = in || (cross2(sub(B, A), sub(local, A)) >= 0.0f && cross2(sub(C, B), sub(local, B)) >= 0.0f &&
+                                cross2(sub(A, C), sub(local, C)) >= 0.0f);
+                }
+                return __any_sync(0xffffffffu, in) != 0;
+            };
+            for (uint32_t k = 0; k < b.ranges.y; ++k) {
+                const float2 p = add(pose_xy(b), rot_cs(g.verts[b.ranges.x + k], bodyCS.x, bodyCS.y));
+                const float2 start =
+                    add(f2(b.previous.x, b.previous.y), rot_cs(g.verts[b.ranges.x + k], startCS.x, startCS.y));
+                const bool inside = inside_wall(p);
+                bool startedInside = inside_wall(start);
+                if (startedInside) {
+                    bool onEdge = false;
+                    for (uint32_t e = lane; e < wn; e += 32u) {
+                        const float2 ea = wall_vertex(e), eb = wall_vertex((e + 1u) % wn);
+                        onEdge = onEdge || dist2(start, closest_point(start, ea, eb)) < 1e-5f;
+                    }
+                    if (__any_sync(0xffffffffu, onEdge)) startedInside = false;
+                }
+                // each lane's nearest edge among its own (increasing e, strict <), then the warp's smallest pair
+                float nearest = INFINITY, depth = 0.0f;
+                float2 normal = f2(0.0f, 0.0f);
+                uint32_t nearestEdge = 0xffffffffu;
+                for (uint32_t e = lane; e < wn; e += 32u) {
                     const float2 ea = wall_vertex(e), eb = wall_vertex((e + 1u) % wn);
-                    if (dist2(start, closest_point(start, ea, eb)) < 1e-5f) { startedInside = false; break; }
+                    const float2 direction = sub(eb, ea);
+                    const float2 out = normalized(f2(direction.y, -direction.x));
+                    const float signedStart = dot2(sub(start, ea), out);
+                    const bool onBoundary = dist2(start, closest_point(start, ea, eb)) < 1e-5f;
+                    const bool crossing = signedStart >= -1e-5f && (center_crossing(start, p, ea, eb, ea, eb) ||
+                                                                     (onBoundary && dot2(sub(p, ea), out) < 0.0f));
+                    if (!inside && !crossing) continue;
+                    if (inside && !startedInside && signedStart < -1e-5f) continue;
+                    const float2 c = closest_point(p, ea, eb);
+                    const float d =
+                        (crossing || !startedInside) ? dist2(start, closest_point(start, ea, eb)) : dist2(p, c);
+                    if (d < nearest) {
+                        nearest = d; normal = out; depth = fmaxf(0.0f, -dot2(sub(p, c), out)); nearestEdge = e;
+                    }
                 }
-            float nearest = INFINITY, depth = 0.0f;
-            float2 normal = f2(0.0f, 0.0f);
-            for (uint32_t e = 0; e < wn; ++e) {
-                const float2 ea = wall_vertex(e), eb = wall_vertex((e + 1u) % wn);
-                const float2 direction = sub(eb, ea);
-                const float2 out = normalized(f2(direction.y, -direction.x));
-                const float signedStart = dot2(sub(start, ea), out);
-                const bool onBoundary = dist2(start, closest_point(start, ea, eb)) < 1e-5f;
-                const bool crossing = signedStart >= -1e-5f && (center_crossing(start, p, ea, eb, ea, eb) ||
-                                                                 (onBoundary && dot2(sub(p, ea), out) < 0.0f));
-                if (!inside && !crossing) continue;
-                if (inside && !startedInside && signedStart < -1e-5f) continue;
-                const float2 c = closest_point(p, ea, eb);
-                const float d = (crossing || !startedInside) ? dist2(start, closest_point(start, ea, eb)) : dist2(p, c);
-                if (d < nearest) { nearest = d; normal = out; depth = fmaxf(0.0f, -dot2(sub(p, c), out)); }
-            }
-            if (isfinite(nearest) && depth > 0.0f) {
-                if (is_round(b)) {
-                    RBody old = b;
-                    old.pose.x = b.previous.x; old.pose.y = b.previous.y; old.pose.z = b.pose.w;
-                    if (round_core_crosses_polygon(g, core_of(g, old), wall)) break;
+#pragma unroll
+                for (int offset = 16; offset > 0; offset >>= 1) {
+                    const float od = __shfl_xor_sync(0xffffffffu, nearest, offset);
+                    const uint32_t oe = __shfl_xor_sync(0xffffffffu, nearestEdge, offset);
+                    const float onx = __shfl_xor_sync(0xffffffffu, normal.x, offset);
+                    const float ony = __shfl_xor_sync(0xffffffffu, normal.y, offset);
+                    const float odepth = __shfl_xor_sync(0xffffffffu, depth, offset);
+                    if (oe != 0xffffffffu && (nearestEdge == 0xffffffffu || od < nearest || (od == nearest && oe < nearestEdge))) {
+                        nearest = od; nearestEdge = oe; normal = f2(onx, ony); depth = odepth;
+                    }
                 }
-                const float2 shift = mul(normal, depth + 1e-5f);
-                b.pose.x += shift.x; b.pose.y += shift.y;
-                const float2 r = sub(p, pose_xy(b));
-                const float lever = cross2(r, normal);
-                const float speed = dot2(f2(b.motion.x, b.motion.y), normal) + b.motion.z * lever;
-                const float denom = b.physical.x + b.physical.y * lever * lever;
-                const float impulse = fmaxf(0.0f, -speed) / fmaxf(denom, kFltMin);
-                const float2 dv = mul(mul(normal, b.physical.x), impulse);
-                b.motion.x += dv.x; b.motion.y += dv.y;
-                b.motion.z += lever * b.physical.y * impulse;
+                if (nearestEdge == 0xffffffffu) { nearest = INFINITY; depth = 0.0f; }
+                if (isfinite(nearest) && depth > 0.0f) {
+                    if (is_round(b)) {
+                        RBody old = b;
+                        old.pose.x = b.previous.x; old.pose.y = b.previous.y; old.pose.z = b.pose.w;
+                        if (round_core_crosses_polygon(g, core_of(g, old), wall)) break;
+                    }
+                    const float2 shift = mul(normal, depth + 1e-5f);
+                    b.pose.x += shift.x; b.pose.y += shift.y;
+                    const float2 r = sub(p, pose_xy(b));
+                    const float lever = cross2(r, normal);
+                    const float speed = dot2(f2(b.motion.x, b.motion.y), normal) + b.motion.z * lever;
+                    const float denom = b.physical.x + b.physical.y * lever * lever;
+                    const float impulse = fmaxf(0.0f, -speed) / fmaxf(denom, kFltMin);
+                    const float2 dv = mul(mul(normal, b.physical.x), impulse);
+                    b.motion.x += dv.x; b.motion.y += dv.y;
+                    b.motion.z += lever * b.physical.y * impulse;
+                }
             }
         }
     }
-    bodies[index] = b;
+    if (lane == 0u) bodies[index] = b;
 }
 
 static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0u; }
@@ -1317,7 +1360,8 @@ extern "C" int bp_rigid_guard_walls(bp_rigid_body* bodies, uint32_t body_count, 
     if (!bodies || !safety || (!joint_partners && partner_count) || !aligned16(bodies) || !aligned16(joint_ranges) ||
         !aligned8(joint_partners) || !geometry_args(vertices_xy, vertex_count, triangles, triangle_count, g))
         return BP_E_INVALID;
-    rigid_guard_kernel<<<(body_count + kRoundThreads - 1u) / kRoundThreads, kRoundThreads, 0, (cudaStream_t)stream>>>(
+    const uint32_t warpBlocks = (uint32_t)(((size_t)body_count * 32u + kRoundThreads - 1u) / kRoundThreads);
+    rigid_guard_kernel<<<warpBlocks, kRoundThreads, 0, (cudaStream_t)stream>>>(
         reinterpret_cast<RBody*>(bodies), body_count, g, bubble_count, reinterpret_cast<const uint4*>(joint_ranges),
         reinterpret_cast<const unsigned long long*>(joint_partners), joint_ranges ? partner_count : 0u, safety);
     return launch_status();
