@@ -365,3 +365,131 @@ def test_ccd_stops_a_fast_body_before_it_passes_through_another():
     o.ccd()
     x = float(o.bodies()[1]["pose"][0])
     assert -24.0 < x < -21.0, x  # stopped at the wall's near face (half widths 20 + 2)
+
+
+# ---- pair contact: numpy restatement (NCK:248-373, NGK:444-581) ---------------------------------------------------
+
+def _f(*v):
+    return np.array(v, F)
+
+
+def np_len(v):
+    return np.sqrt(v[0] * v[0] + v[1] * v[1])
+
+
+def np_dot(a, b):
+    return a[0] * b[0] + a[1] * b[1]
+
+
+def np_cross(a, b):
+    return a[0] * b[1] - a[1] * b[0]
+
+
+def np_closest(p, a, b):
+    e = b - a
+    sq = np_dot(e, e)
+    t = min(max(np_dot(p - a, e) / sq, F(0)), F(1)) if sq > np.finfo(F).tiny else F(0)
+    return a + e * t
+
+
+def np_segment_distance(a, b, c, d):
+    r, s = b - a, d - c
+    den = np_cross(r, s)
+    if abs(den) > F(1e-12):
+        qp = c - a
+        t, u = np_cross(qp, s) / den, np_cross(qp, r) / den
+        if 0 <= t <= 1 and 0 <= u <= 1:
+            pa = a + r * t
+            return F(0), pa, pa
+    best, pa, pb = F(np.inf), None, None
+    for p, q, first in ((a, (c, d), True), (b, (c, d), True), (c, (a, b), False), (d, (a, b), False)):
+        cp = np_closest(p, *q)
+        v = np_len(p - cp)
+        if v < best:
+            best, pa, pb = v, (p if first else cp), (cp if first else p)
+    return best, pa, pb
+
+
+def np_vertex(body, verts, i):
+    cs, sn = np_sincos(np.array([body["pose"][2]], F))
+    v = verts[body["ranges"][0] + i]
+    return _f(body["pose"][0] + (v[0] * cs[0] - v[1] * sn[0]), body["pose"][1] + (v[0] * sn[0] + v[1] * cs[0]))
+
+
+def np_triangle_contact(a, b):
+    depth, normal = F(np.inf), None
+    for shape in (a, b):
+        for e in range(3):
+            delta = shape[(e + 1) % 3] - shape[e]
+            m = np_len(delta)
+            axis = _f(-delta[1], delta[0]) / m
+            pa, pb = [np_dot(x, axis) for x in a], [np_dot(x, axis) for x in b]
+            amin, amax, bmin, bmax = min(pa), max(pa), min(pb), max(pb)
+            if amax < bmin or bmax < amin:
+                return None
+            plus, minus = amax - bmin, bmax - amin
+            overlap = min(plus, minus)
+            if overlap < depth:
+                depth, normal = overlap, (axis if plus < minus else -axis)
+    max_a = max(np_dot(x, normal) for x in a)
+    min_b = min(np_dot(x, normal) for x in b)
+    pa, pb, na, nb = _f(0, 0), _f(0, 0), 0, 0
+    for k in range(3):
+        if np_dot(a[k], normal) >= max_a - F(1e-5):
+            pa, na = pa + a[k], na + 1
+        if np_dot(b[k], normal) <= min_b + F(1e-5):
+            pb, nb = pb + b[k], nb + 1
+    return normal, depth, (pa / F(na) + pb / F(nb)) * F(0.5)
+
+
+def np_round_contact(A, B):
+    sep, pa, pb = np_segment_distance(A[0], A[1], B[0], B[1])
+    assert sep > F(1e-4)  # the test pairs are apart at the cores
+    n = (pb - pa) / sep
+    return n, A[2] + B[2] - sep, ((pa + n * A[2]) + (pb - n * B[2])) * F(0.5)
+
+
+def two_body_contact(a, b, verts, tris):
+    """(normal, point, lambda) of the pair's first row slot after one contact round of the oracle."""
+    o = OracleRigid(np.array([a, b]), verts, None, None, triangles=tris, row_width=4)
+    o.body_candidates()
+    o.solve_contacts()
+    c = o.contact_corrections[0]
+    lam = o.rows[0]["metadata"][3].view(F)
+    return _f(c["first"][3], c["second"][3]), _f(c["velocity_first"][3], c["velocity_second"][3]), lam
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_pair_contacts_match_the_numpy_restatement(seed):
+    rng = np.random.default_rng(seed)
+    tris = [(0, 1, 2, 0), (0, 2, 3, 0), (0, 1, 2, 0), (0, 2, 3, 0)]
+    # two overlapping boxes: triangle SAT, the deepest piece
+    verts = np.array(scenes._box(3.0, 2.0) + scenes._box(2.5, 1.5), F)
+    a = scenes._rigid_body(1, (0.0, 0.0, float(rng.uniform(-0.3, 0.3))), 0, 4, 0.1, 0.01, 3.7)
+    b = scenes._rigid_body(2, (float(rng.uniform(3.5, 4.5)), float(rng.uniform(-1, 1)), float(rng.uniform(-0.3, 0.3))),
+                           4, 4, 0.1, 0.01, 3.0)
+    a["ranges"], b["ranges"] = (0, 4, 0, 2), (4, 4, 2, 2)
+    n, point, lam = two_body_contact(a, b, verts, tris)
+    best = None
+    for ta in ((0, 1, 2), (0, 2, 3)):
+        for tb in ((0, 1, 2), (0, 2, 3)):
+            got = np_triangle_contact([np_vertex(a, verts, i) for i in ta], [np_vertex(b, verts, i) for i in tb])
+            if got is not None and (best is None or got[1] > best[1]):
+                best = got
+    assert best is not None
+    assert np.array_equal(n, best[0]) and np.array_equal(point, best[2])
+    ra, rb = point - a["pose"][:2], point - b["pose"][:2]
+    ca, cb = np_cross(ra, n), np_cross(rb, n)
+    denom = F(0.1) + F(0.1) + F(0.01) * ca * ca + F(0.01) * cb * cb
+    assert lam == max(F(0), best[1]) / denom * F(0.5)
+    # two capsules whose cores are apart: segment distance of the cores
+    verts = np.array([(-2.0, 0.0), (2.0, 0.0), (-1.5, 0.0), (1.5, 0.0)], F)
+    a = scenes._shape_record(scenes._rigid_body(1, (0.0, 0.0, float(rng.uniform(-1, 1))), 0, 2, 0.2, 0.05, 3.0), 2, 1.0, 2.0)
+    b = scenes._shape_record(scenes._rigid_body(2, (float(rng.uniform(0.5, 2.0)), float(rng.uniform(1.2, 1.8)),
+                                                    float(rng.uniform(-1, 1))), 2, 2, 0.2, 0.05, 2.5), 2, 1.0, 1.5)
+    n, point, lam = two_body_contact(a, b, verts, [])
+    A = (np_vertex(a, verts, 0), np_vertex(a, verts, 1), F(1.0))
+    B = (np_vertex(b, verts, 0), np_vertex(b, verts, 1), F(1.0))
+    want_n, want_depth, want_point = np_round_contact(A, B)
+    assert np.array_equal(n, want_n) and np.array_equal(point, want_point)
+    assert want_depth > 0 and lam > 0
