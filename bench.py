@@ -573,7 +573,12 @@ def run_ours(args, rank, world_size, local_rank):
     leg = {"value": ref_line["value"], "cores": ref_line["cpu_baseline"]["cores"],
            "sample": ref_line["cpu_baseline"]["sample"]}
     accuracy = plain_world_accuracy(ctx) if world_size == 1 else None
-    rigid = rigid_solver() if world_size == 1 and args.single_steps > 0 else None
+    rigid = None
+    if world_size == 1 and args.single_steps > 0:
+        try:
+            rigid = rigid_solver()
+        except Exception as exc:  # the headline line is printed whatever happens to this side measurement
+            rigid = {"error": f"{type(exc).__name__}: {exc}"}
     lat = sorted(step_ms)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
