@@ -1,10 +1,13 @@
-// bp_rigid.cu - the rigid body solver's predict, joint and finish passes on the caller's device arrays.
+// bp_rigid.cu - the rigid body solver on the caller's device arrays: predict, body-pair rows, CCD, contact rounds,
+// joint rounds, the wall guard and the finish, one entry per reference kernel (or kernel pair).
 //
 // The reference steps rigid bodies once per step, before the bubble substeps (NativeMetalSolver.swift:767-799):
 // nativeRigidPredict (NativePostSolveKernels.metal-source = NPK:66-115), body-pair candidates and CCD, then 8 rounds
 // of {nativeRigidContacts, nativeRigidApplyBodies, nativeSolveJoints, nativeApplyJointBodies, nativeRigidGuardWalls},
 // and nativeRigidFinish (NPK:172-198) after the bubble step. Here:
-//  - predict and finish: one thread per body, like the reference (each body's sweep is independent);
+//  - predict, finish, the contact apply and the CCD moves: one thread per body; the contacts: one thread per row slot;
+//  - body-pair rows, CCD and the wall guard: one warp per body (see each kernel for how the lanes split the work
+//    without changing the reference's order of insertion or correction);
 //  - the joint rounds: a round is a Jacobi pass: every joint computes both ends' corrections from the same body state
 //    (a thread per joint), then every body adds its joints' corrections in list order (a thread per body). A small
 //    world (<= 512 joints, <= 1,024 bodies) runs all rounds in ONE launch of one 512-thread block, the halves

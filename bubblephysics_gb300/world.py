@@ -1181,7 +1181,8 @@ def stage(pending: list, state: _State, region) -> tuple[_State, list, list]:
                           if EventInterest.DID_REPLACE in before or EventInterest.DID_REPLACE in _interest_of(trial, i)]
         if rejection is None and tx.operations and any(b.desc.motion_role in DYNAMIC_ROLES for b in trial.bodies.values()):
             # judged on the state after the whole transaction, reported at its last operation
-            # (NativeCompleteStepper.validate; the rigid solver for worlds of dynamic bodies alone is not built here)
+            # (NativeCompleteStepper.validate; a world of dynamic bodies alone steps through rigid.RigidSolver, which
+            # this world API does not drive)
             reason = TransactionRejectionReason.UNSUPPORTED_BUBBLE_WITH_DYNAMIC_RIGID_BODY if trial.bubbles else \
                 TransactionRejectionReason.UNSUPPORTED_OPERATION
             rejection = TransactionRejection(len(tx.operations) - 1, reason, "validate")
