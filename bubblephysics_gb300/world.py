@@ -15,8 +15,10 @@ polygons (polygons become one-sided edges like NativePublicWorld.step), kinemati
 sensors (circle or polygon; enteredSensor / exitedSensor events of bubbles), physics materials, global force, impulses
 and motion-role changes; each published bubble state carries its contour's effective radius and bounds
 (bp_world_contours) and hit_test answers on the published state (bp_world_hit_test). Operations of the reference
-outside this path (merges, splits, joints, force fields, drives other than kinematic, render state) are rejected with
-TransactionRejectionReason.UNSUPPORTED_OPERATION naming the operation, so a caller sees what is missing. The world
+outside this path (merges, splits, force fields, drives other than kinematic, render state) are rejected with
+TransactionRejectionReason.UNSUPPORTED_OPERATION naming the operation, so a caller sees what is missing. Joints are
+staged with the reference's checks (duplicateJointID, jointNotFound, unsupportedJointBody, ...); one can only be
+kept next to a dynamic rigid body, which this world rejects at the end of the transaction, so none survives a step. The world
 steps on the GPU (World, bp_world_step); there is no CPU fallback.
 """
 from __future__ import annotations
@@ -461,6 +463,9 @@ class TransactionRejectionReason(Enum):
     DRIVE_NOT_ACTIVE = "driveNotActive"                      # detail: object id
     INCOMPATIBLE_TRANSITION_VALUE = "incompatibleTransitionValue"
     UNSUPPORTED_BUBBLE_WITH_DYNAMIC_RIGID_BODY = "unsupportedBubbleWithDynamicRigidBody"
+    DUPLICATE_JOINT_ID = "duplicateJointID"                  # detail: joint id
+    JOINT_NOT_FOUND = "jointNotFound"                        # detail: joint id
+    UNSUPPORTED_JOINT_BODY = "unsupportedJointBody"          # detail: joint id
 
 
 @dataclass(frozen=True)
@@ -476,6 +481,7 @@ class TransactionReceipt:
     created_object_ids: tuple
     removed_object_ids: tuple
     replaced_object_ids: tuple
+    removed_joint_ids: tuple = ()   # ascending: removed by remove_joint or with a body they joined
 
 
 @dataclass(frozen=True)
@@ -578,6 +584,13 @@ class WorldTransaction:
 
     def remove(self, object_id: int) -> "WorldTransaction":
         return self._with("remove", object_id)
+
+    def add_joint(self, joint) -> "WorldTransaction":
+        """`joint` is a rigid.Joint (WorldTransaction.addJoint, Model/WorldTransaction.swift:121)."""
+        return self._with("addJoint", joint)
+
+    def remove_joint(self, joint_id: int) -> "WorldTransaction":
+        return self._with("removeJoint", joint_id)
 
     def replace(self, object_id: int, obj) -> "WorldTransaction":
         return self._with("replace", object_id, obj)
@@ -684,13 +697,14 @@ class _State:
     transitions: dict = field(default_factory=dict)          # target -> ParameterTransition
     transition_progress: dict = field(default_factory=dict)  # target -> (initial value, elapsed seconds)
     fields: dict = field(default_factory=dict)               # id -> ForceFieldDescriptor
+    joints: dict = field(default_factory=dict)               # joint id -> rigid.Joint
 
     def copy(self) -> "_State":
         return _State(dict(self.materials),
                       {k: replace(v, position=v.position.copy(), velocity=v.velocity.copy()) for k, v in self.bubbles.items()},
                       {k: replace(v, position=v.position.copy(), velocity=v.velocity.copy()) for k, v in self.bodies.items()},
                       self.global_force, dict(self.sensors), self.fixed_time_step, self.next_drive_id,
-                      dict(self.transitions), dict(self.transition_progress), dict(self.fields))
+                      dict(self.transitions), dict(self.transition_progress), dict(self.fields), dict(self.joints))
 
 
 def _finite(*values) -> bool:
@@ -907,10 +921,59 @@ def _validate_body(desc: RigidBodyDescriptor, state: _State, region) -> Transact
     return None
 
 
+def _add_joint(joint, state: _State):
+    """TransactionStager.add(_ joint:) (TransactionStager.swift:444-470) with the Joint initialiser's checks
+    (Model/Joints.swift:56-66): a new id; finite anchors and reference angle; two different objects; distance length,
+    softness and damping not negative; every drive-like value within 1e6; ends that are bubbles or rigid bodies; and
+    at least one movable rigid body (dynamic, motor- or player-driven) and no bubble or path-driven end
+    (jointBodiesAreSupported). Returns the rejection or None (the joint is then kept)."""
+    if joint.id in state.joints:
+        return TransactionRejectionReason.DUPLICATE_JOINT_ID, joint.id
+    if joint.body_b is not None and joint.body_b == joint.body_a:
+        return TransactionRejectionReason.INVALID_VALUE, "joint.bodies"
+    checks = [("joint.anchorA", tuple(joint.anchor_a)), ("joint.anchorB", tuple(joint.anchor_b)),
+              ("joint.referenceAngle", (joint.reference_angle,))]
+    if joint.kind == "distance":
+        checks += [("joint.length", (joint.length,)), ("joint.softness", (joint.softness,)),
+                   ("joint.damping", (joint.damping,))]
+        for name, value in (("joint.length", joint.length), ("joint.softness", joint.softness),
+                            ("joint.damping", joint.damping)):
+            if _finite(value) and value < 0:
+                return TransactionRejectionReason.INVALID_VALUE, name
+    elif joint.kind == "hinge":
+        if joint.limits is not None:
+            checks += [("hinge.lower", (joint.limits[0],)), ("hinge.upper", (joint.limits[1],))]
+        if joint.motor is not None:
+            checks += [("hinge.motor.targetAngularVelocity", (joint.motor[0],))]
+    elif joint.kind != "weld":
+        return TransactionRejectionReason.INVALID_VALUE, "joint.kind"
+    for name, values in checks:
+        if not _finite(*values) or any(abs(float(np.float32(v))) > MAXIMUM_DRIVE_MAGNITUDE for v in values):
+            return TransactionRejectionReason.INVALID_VALUE, name
+    ends = [joint.body_a] + ([joint.body_b] if joint.body_b is not None else [])
+    for oid in ends:
+        if oid in state.sensors or oid in state.fields:
+            return TransactionRejectionReason.INCOMPATIBLE_OBJECT_KIND, oid
+        if oid not in state.bubbles and oid not in state.bodies:
+            return TransactionRejectionReason.OBJECT_NOT_FOUND, oid
+    movable = False
+    for oid in ends:
+        if oid in state.bubbles:  # no joints with bubbles in the v4 engine
+            return TransactionRejectionReason.UNSUPPORTED_JOINT_BODY, joint.id
+        role = state.bodies[oid].desc.motion_role
+        if role == MotionRole.PATH_DRIVEN:
+            return TransactionRejectionReason.UNSUPPORTED_JOINT_BODY, joint.id
+        movable = movable or role in (MotionRole.DYNAMIC, MotionRole.MOTOR_DRIVEN, MotionRole.PLAYER_DRIVEN)
+    if not movable:
+        return TransactionRejectionReason.UNSUPPORTED_JOINT_BODY, joint.id
+    state.joints[joint.id] = joint
+    return None
+
+
 def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None, dict]:
     """Applies one operation to `state` (a staging copy); returns (rejection reason, {created, removed, replaced})."""
     kind, args = op[0], op[1:]
-    touched = {"created": [], "removed": [], "replaced": []}
+    touched = {"created": [], "removed": [], "replaced": [], "removed_joints": []}
     if kind in ("add", "replace"):
         obj = args[-1]
         if kind == "replace":
@@ -968,6 +1031,19 @@ def _apply(op, state: _State, region) -> tuple[TransactionRejectionReason | None
                 state.sensors.pop(oid, None) is None and state.fields.pop(oid, None) is None:
             return TransactionRejectionReason.OBJECT_NOT_FOUND, touched
         touched["removed"].append(oid)
+        # removing an object removes its joints (TransactionStager.removeJoints, TransactionStager.swift:437-443)
+        for jid in [j for j, joint in state.joints.items() if oid in (joint.body_a, joint.body_b)]:
+            del state.joints[jid]
+            touched["removed_joints"].append(jid)
+        return None, touched
+    if kind == "addJoint":
+        return _add_joint(args[0], state), touched
+    if kind == "removeJoint":  # TransactionStager.swift:370-373
+        jid = args[0]
+        if jid not in state.joints:
+            return (TransactionRejectionReason.JOINT_NOT_FOUND, jid), touched
+        del state.joints[jid]
+        touched["removed_joints"].append(jid)
         return None, touched
     if kind == "updatePhysicsMaterial":
         mid, material = args
@@ -1158,7 +1234,7 @@ def stage(pending: list, state: _State, region) -> tuple[_State, list, list]:
     current = state
     for token, tx in pending:
         trial = current.copy()
-        created, removed, replaced_ids = [], [], []
+        created, removed, replaced_ids, removed_joints = [], [], [], []
         rejection = None
         tx_events = []
         for index, op in enumerate(tx.operations):
@@ -1173,6 +1249,7 @@ def stage(pending: list, state: _State, region) -> tuple[_State, list, list]:
                 break
             created += touched["created"]
             removed += touched["removed"]
+            removed_joints += touched["removed_joints"]
             replaced_ids += touched["replaced"]
             tx_events += [WorldEvent("didAdd", (i,)) for i in touched["created"]
                           if EventInterest.DID_ADD in _interest_of(trial, i)]
@@ -1190,7 +1267,8 @@ def stage(pending: list, state: _State, region) -> tuple[_State, list, list]:
             events.append(WorldEvent("transactionRejected", token=token, rejection=rejection))
             continue
         current = trial
-        receipts.append(TransactionReceipt(token, tuple(created), tuple(removed), tuple(replaced_ids)))
+        receipts.append(TransactionReceipt(token, tuple(created), tuple(removed), tuple(replaced_ids),
+                                           tuple(sorted(removed_joints))))
         events += tx_events
     return current, receipts, events
 
