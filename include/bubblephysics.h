@@ -644,10 +644,11 @@ int bp_rigid_predict(bp_rigid_body* bodies, uint32_t body_count, const float* ve
                      const uint32_t* joint_ranges, const uint64_t* joint_partners, uint32_t partner_count,
                      bp_rigid_wall* walls, uint32_t* safety, void* stream);
 
-/* `iterations` rounds of nativeSolveJoints then nativeApplyJointBodies (NativeContactKernels:446-562) in one launch:
- * every joint computes both ends' corrections from the same state (XPBD distance with compliance and damping, hinge
- * with limits and motor, weld), then every body adds its joints' corrections in list order times 1 / count.
- * iteration_count is the solver's iteration count per step (the damping is spread over it); a caller that
+/* `iterations` rounds of nativeSolveJoints then nativeApplyJointBodies (NativeContactKernels:446-562): every joint
+ * computes both ends' corrections from the same state (XPBD distance with compliance and damping, hinge with limits
+ * and motor, weld), then every body adds its joints' corrections in list order times 1 / count. A world of at most
+ * 512 joints and 1,024 bodies runs all rounds in one launch, a larger one two launches per round; the results are
+ * the same. iteration_count is the solver's iteration count per step (the damping is spread over it); a caller that
  * interleaves other work calls this with iterations = 1 each time. */
 int bp_rigid_solve_joints(bp_rigid_body* bodies, uint32_t body_count, bp_rigid_joint* joints, uint32_t joint_count,
                           bp_rigid_correction* corrections, const uint32_t* references, uint32_t reference_count,
