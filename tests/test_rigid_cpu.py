@@ -493,3 +493,115 @@ def test_pair_contacts_match_the_numpy_restatement(seed):
     want_n, want_depth, want_point = np_round_contact(A, B)
     assert np.array_equal(n, want_n) and np.array_equal(point, want_point)
     assert want_depth > 0 and lam > 0
+
+
+# ---- wall guard: numpy restatement (NPK:118-170) --------------------------------------------------------------------
+
+def np_center_crossing_static(start, end, a, b):
+    """nativeCenterCrossing (NGK:583-622) for a segment that does not move."""
+    e0, de = b - a, _f(0, 0)
+    r0, dr = start - a, end - start
+    a_ = np_cross(de, dr)
+    b_ = np_cross(e0, dr) + np_cross(de, r0)
+    c = np_cross(e0, r0)
+    if a_ == 0 and b_ == 0 and c == 0:
+        q0 = np_dot(r0, r0 - e0)
+        if q0 <= 0:
+            return False
+        qa = np_dot(dr, dr - de)
+        qb = np_dot(dr, r0 - e0) + np_dot(r0, dr - de)
+        minimum = min(q0, qa + qb + q0)
+        if qa > 0:
+            t = min(max(-qb / (F(2) * qa), F(0)), F(1))
+            minimum = min(minimum, (qa * t + qb) * t + q0)
+        return minimum <= 0
+    roots = [F(-1), F(-1)]
+    if abs(a_) <= np.finfo(F).eps * max(abs(b_), abs(c)):
+        if abs(b_) > np.finfo(F).tiny:
+            roots[0] = -c / b_
+    for t in roots:
+        if not (0 < t < 1):
+            continue
+        edge, rel = e0 + de * t, r0 + dr * t
+        sq, along = np_dot(edge, edge), np_dot(rel, edge)
+        if sq > np.finfo(F).tiny and 0 <= along <= sq:
+            return True
+    return False
+
+
+def np_inside_polygon(p, body, verts, tris):
+    cs, sn = np_sincos(np.array([-body["pose"][2]], F))
+    d = p - body["pose"][:2]
+    local = _f(d[0] * cs[0] - d[1] * sn[0], d[0] * sn[0] + d[1] * cs[0])
+    for t in tris[body["ranges"][2]:body["ranges"][2] + body["ranges"][3]]:
+        A, B, C = (verts[body["ranges"][0] + k] for k in t[:3])
+        if np_cross(B - A, local - A) >= 0 and np_cross(C - B, local - B) >= 0 and np_cross(A - C, local - C) >= 0:
+            return True
+    return False
+
+
+def np_guard(b, wall, verts, tris):
+    """nativeRigidGuardWalls for one dynamic polygon body against one static polygon wall."""
+    b = b.copy()
+    wn = wall["ranges"][1]
+    wv = [np_vertex(wall, verts, e) for e in range(wn)]
+    for k in range(b["ranges"][1]):
+        p = np_vertex(b, verts, k)
+        cs, sn = np_sincos(np.array([b["pose"][3]], F))
+        v = verts[b["ranges"][0] + k]
+        start = _f(b["previous"][0] + (v[0] * cs[0] - v[1] * sn[0]), b["previous"][1] + (v[0] * sn[0] + v[1] * cs[0]))
+        inside, started = np_inside_polygon(p, wall, verts, tris), np_inside_polygon(start, wall, verts, tris)
+        if started and any(np_len(start - np_closest(start, wv[e], wv[(e + 1) % wn])) < F(1e-5) for e in range(wn)):
+            started = False
+        nearest, normal, depth = F(np.inf), None, F(0)
+        for e in range(wn):
+            ea, eb = wv[e], wv[(e + 1) % wn]
+            direction = eb - ea
+            raw = _f(direction[1], -direction[0])
+            out = raw / np_len(raw)
+            signed_start = np_dot(start - ea, out)
+            on_boundary = np_len(start - np_closest(start, ea, eb)) < F(1e-5)
+            crossing = signed_start >= F(-1e-5) and (np_center_crossing_static(start, p, ea, eb) or
+                                                     (on_boundary and np_dot(p - ea, out) < 0))
+            if not inside and not crossing:
+                continue
+            if inside and not started and signed_start < F(-1e-5):
+                continue
+            c = np_closest(p, ea, eb)
+            d = np_len(start - np_closest(start, ea, eb)) if (crossing or not started) else np_len(p - c)
+            if d < nearest:
+                nearest, normal, depth = d, out, max(F(0), -np_dot(p - c, out))
+        if np.isfinite(nearest) and depth > 0:
+            shift = normal * (depth + F(1e-5))
+            b["pose"][:2] = b["pose"][:2] + shift
+            r = p - b["pose"][:2]
+            lever = np_cross(r, normal)
+            speed = np_dot(b["motion"][:2], normal) + b["motion"][2] * lever
+            denom = b["physical"][0] + b["physical"][1] * lever * lever
+            impulse = max(F(0), -speed) / max(denom, np.finfo(F).tiny)
+            b["motion"][:2] = b["motion"][:2] + normal * b["physical"][0] * impulse
+            b["motion"][2] = b["motion"][2] + lever * b["physical"][1] * impulse
+    return b
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_wall_guard_matches_the_numpy_restatement(seed):
+    rng = np.random.default_rng(100 + seed)
+    verts = np.array(scenes._box(50.0, 5.0) + scenes._box(3.0, 2.0), F)
+    tris = np.array([(0, 1, 2, 0), (0, 2, 3, 0)] * 2, np.uint32)
+    floor = scenes._rigid_body(1, (0.0, 0.0, float(rng.uniform(-0.2, 0.2))), 0, 4, 0.0, 0.0, 50.3, static=True)
+    floor["ranges"] = (0, 4, 0, 2)
+    # a box that entered the floor's top face during the step (or started on it)
+    y0 = float(rng.uniform(7.0, 9.0))
+    y1 = float(rng.uniform(4.0, 6.5))
+    box = scenes._rigid_body(2, (float(rng.uniform(-20, 20)), y1, float(rng.uniform(-0.4, 0.4))), 4, 4, 1 / 24, 1 / 104,
+                             3.7, velocity=(float(rng.normal(0, 5)), -60.0), spin=float(rng.normal(0, 1)))
+    box["previous"][:2] = (box["pose"][0], y0)
+    box["pose"][3] = box["pose"][2] - F(rng.uniform(-0.05, 0.05))
+    box["ranges"] = (4, 4, 2, 2)
+    o = OracleRigid(np.array([floor, box]), verts, None, None, triangles=tris)
+    o.guard_walls()
+    got = o.bodies()[1]
+    want = np_guard(box, floor, verts, tris)
+    assert np.array_equal(got["pose"], want["pose"]) and np.array_equal(got["motion"], want["motion"])
+    assert not np.array_equal(got["pose"], box["pose"])  # the guard pushed it out
