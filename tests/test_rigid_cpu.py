@@ -605,3 +605,75 @@ def test_wall_guard_matches_the_numpy_restatement(seed):
     want = np_guard(box, floor, verts, tris)
     assert np.array_equal(got["pose"], want["pose"]) and np.array_equal(got["motion"], want["motion"])
     assert not np.array_equal(got["pose"], box["pose"])  # the guard pushed it out
+
+
+# ---- CCD: numpy restatement (NPK:200-263) ---------------------------------------------------------------------------
+
+def np_box_pair_depth(a, b, verts):
+    """nativeRigidPairContact for two boxes of two triangles each: the deepest triangle pair's depth, or None."""
+    best = None
+    for ta in ((0, 1, 2), (0, 2, 3)):
+        for tb in ((0, 1, 2), (0, 2, 3)):
+            got = np_triangle_contact([np_vertex(a, verts, i) for i in ta], [np_vertex(b, verts, i) for i in tb])
+            if got is not None and (best is None or got[1] > best):
+                best = got[1]
+    return best
+
+
+def np_at(body, t):
+    out = body.copy()
+    out["pose"][0] = body["previous"][0] + (body["pose"][0] - body["previous"][0]) * t
+    out["pose"][1] = body["previous"][1] + (body["pose"][1] - body["previous"][1]) * t
+    out["pose"][2] = body["pose"][3] + (body["pose"][2] - body["pose"][3]) * t
+    return out
+
+
+def np_time_of_impact(a, b, verts):
+    def overlap(t):
+        d = np_box_pair_depth(np_at(a, t), np_at(b, t), verts)
+        return d is not None and d > F(1e-3)
+    da, db = a["pose"][:2] - a["previous"][:2], b["pose"][:2] - b["previous"][:2]
+    travel = np_len(da - db) + abs(a["pose"][2] - a["pose"][3]) * a["physical"][2] + \
+        abs(b["pose"][2] - b["pose"][3]) * b["physical"][2]
+    if not travel > F(0.5) or overlap(F(0)):
+        return F(2)
+    samples = np.ceil(travel / F(0.5))
+    steps = 64 if samples >= 64 else max(2, int(samples))
+    last = F(0)
+    for step in range(1, steps + 1):
+        t = F(step) / F(steps)
+        if not overlap(t):
+            last = t
+            continue
+        low, high = last, t
+        for _ in range(12):
+            middle = F(0.5) * (low + high)
+            if overlap(middle):
+                high = middle
+            else:
+                low = middle
+        return low
+    return F(2)
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_ccd_matches_the_numpy_restatement(seed):
+    rng = np.random.default_rng(200 + seed)
+    verts = np.array(scenes._box(20.0, 20.0) + scenes._box(2.0, 2.0), F)
+    tris = [(0, 1, 2, 0), (0, 2, 3, 0)] * 2
+    wall = scenes._rigid_body(1, (0.0, 0.0, float(rng.uniform(-0.3, 0.3))), 0, 4, 0.0, 0.0, 28.3, static=True)
+    wall["ranges"] = (0, 4, 0, 2)
+    bullet = scenes._rigid_body(2, (-60.0, float(rng.uniform(-10, 10)), float(rng.uniform(-1, 1))), 4, 4, 1 / 16,
+                                1 / 43, 2.9, velocity=(float(rng.uniform(4000, 7000)), float(rng.normal(0, 300))),
+                                spin=float(rng.normal(0, 2)))
+    bullet["ranges"] = (4, 4, 2, 2)
+    o = OracleRigid(np.array([wall, bullet]), verts, None, None, triangles=tris)
+    o.predict(1 / 60)
+    moved = o.bodies()
+    o.body_candidates()
+    o.ccd()
+    t = np_time_of_impact(moved[0], moved[1], verts)  # the pair (lower index, higher index) of the bullet's row
+    assert t <= 1
+    want = np_at(moved[1], t)
+    got = o.bodies()[1]
+    assert np.array_equal(got["pose"][:3], want["pose"][:3]) and got["limits"][2] == 0
