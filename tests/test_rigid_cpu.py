@@ -449,14 +449,42 @@ def np_round_contact(A, B):
     return n, A[2] + B[2] - sep, ((pa + n * A[2]) + (pb - n * B[2])) * F(0.5)
 
 
-def two_body_contact(a, b, verts, tris):
-    """(normal, point, lambda) of the pair's first row slot after one contact round of the oracle."""
+def two_body_contact(a, b, verts, tris, full=False):
+    """(normal, point, lambda) of the pair's first row slot after one contact round of the oracle (and the whole
+    correction record with full=True)."""
     o = OracleRigid(np.array([a, b]), verts, None, None, triangles=tris, row_width=4)
     o.body_candidates()
     o.solve_contacts()
     c = o.contact_corrections[0]
     lam = o.rows[0]["metadata"][3].view(F)
-    return _f(c["first"][3], c["second"][3]), _f(c["velocity_first"][3], c["velocity_second"][3]), lam
+    out = (_f(c["first"][3], c["second"][3]), _f(c["velocity_first"][3], c["velocity_second"][3]), lam)
+    return out + (c,) if full else out
+
+
+def np_contact_correction(a, b, n, point, depth):
+    """The corrections of nativeRigidContacts (NCK:398-426) for a found contact: (first, second, velocity first,
+    velocity second) xyz."""
+    wa, wb, ia, ib = a["physical"][0], b["physical"][0], a["physical"][1], b["physical"][1]
+    ra, rb = point - a["pose"][:2], point - b["pose"][:2]
+    va, vb = a["motion"][:2], b["motion"][:2]
+    spin_a, spin_b = a["motion"][2], b["motion"][2]
+    ca, cb = np_cross(ra, n), np_cross(rb, n)
+    denom = wa + wb + ia * ca * ca + ib * cb * cb
+    lam = max(F(0), depth) / denom * F(0.5)
+    first = np.append(-n * wa * lam, -ca * ia * lam)
+    second = np.append(n * wb * lam, cb * ib * lam)
+    closing = np_dot(vb - va, n) + spin_b * cb - spin_a * ca
+    friction = np.sqrt(max(F(0), a["physical"][3] * b["physical"][3]))
+    restitution = max(a["flags"][3:4].view(F)[0], b["flags"][3:4].view(F)[0])
+    impulse = max(F(0), -closing) * (F(1) + restitution) / denom * F(0.5)
+    tangent = _f(-n[1], n[0])
+    tangent_speed = np_dot(vb - va, tangent) + spin_b * np_cross(rb, tangent) - spin_a * np_cross(ra, tangent)
+    tangent_impulse = -tangent_speed * friction / denom * F(0.5)
+    vfirst = np.append(-n * wa * impulse - tangent * wa * tangent_impulse,
+                       -ca * ia * impulse - np_cross(ra, tangent) * ia * tangent_impulse)
+    vsecond = np.append(n * wb * impulse + tangent * wb * tangent_impulse,
+                        cb * ib * impulse + np_cross(rb, tangent) * ib * tangent_impulse)
+    return lam, [x.astype(F) for x in (first, second, vfirst, vsecond)]
 
 
 @pytest.mark.parametrize("seed", range(6))
@@ -465,11 +493,14 @@ def test_pair_contacts_match_the_numpy_restatement(seed):
     tris = [(0, 1, 2, 0), (0, 2, 3, 0), (0, 1, 2, 0), (0, 2, 3, 0)]
     # two overlapping boxes: triangle SAT, the deepest piece
     verts = np.array(scenes._box(3.0, 2.0) + scenes._box(2.5, 1.5), F)
-    a = scenes._rigid_body(1, (0.0, 0.0, float(rng.uniform(-0.3, 0.3))), 0, 4, 0.1, 0.01, 3.7)
+    a = scenes._rigid_body(1, (0.0, 0.0, float(rng.uniform(-0.3, 0.3))), 0, 4, 0.1, 0.01, 3.7,
+                           velocity=tuple(rng.normal(0, 20, 2)), spin=float(rng.normal(0, 2)), friction=0.6,
+                           restitution=0.25)
     b = scenes._rigid_body(2, (float(rng.uniform(3.5, 4.5)), float(rng.uniform(-1, 1)), float(rng.uniform(-0.3, 0.3))),
-                           4, 4, 0.1, 0.01, 3.0)
+                           4, 4, 0.1, 0.01, 3.0, velocity=tuple(rng.normal(0, 20, 2)), spin=float(rng.normal(0, 2)),
+                           friction=0.3, restitution=0.1)
     a["ranges"], b["ranges"] = (0, 4, 0, 2), (4, 4, 2, 2)
-    n, point, lam = two_body_contact(a, b, verts, tris)
+    n, point, lam, record = two_body_contact(a, b, verts, tris, full=True)
     best = None
     for ta in ((0, 1, 2), (0, 2, 3)):
         for tb in ((0, 1, 2), (0, 2, 3)):
@@ -478,15 +509,17 @@ def test_pair_contacts_match_the_numpy_restatement(seed):
                 best = got
     assert best is not None
     assert np.array_equal(n, best[0]) and np.array_equal(point, best[2])
-    ra, rb = point - a["pose"][:2], point - b["pose"][:2]
-    ca, cb = np_cross(ra, n), np_cross(rb, n)
-    denom = F(0.1) + F(0.1) + F(0.01) * ca * ca + F(0.01) * cb * cb
-    assert lam == max(F(0), best[1]) / denom * F(0.5)
+    want_lam, want = np_contact_correction(a, b, best[0], best[2], best[1])
+    assert lam == want_lam
+    for field, expected in zip(("first", "second", "velocity_first", "velocity_second"), want):
+        assert np.array_equal(record[field][:3], expected), field
     # two capsules whose cores are apart: segment distance of the cores
     verts = np.array([(-2.0, 0.0), (2.0, 0.0), (-1.5, 0.0), (1.5, 0.0)], F)
-    a = scenes._shape_record(scenes._rigid_body(1, (0.0, 0.0, float(rng.uniform(-1, 1))), 0, 2, 0.2, 0.05, 3.0), 2, 1.0, 2.0)
-    b = scenes._shape_record(scenes._rigid_body(2, (float(rng.uniform(0.5, 2.0)), float(rng.uniform(1.2, 1.8)),
-                                                    float(rng.uniform(-1, 1))), 2, 2, 0.2, 0.05, 2.5), 2, 1.0, 1.5)
+    rc = np.random.default_rng(500 + seed)  # cores tilted at most 0.2 rad, 1.2-1.8 apart: separated, overlapping radii
+    a = scenes._shape_record(scenes._rigid_body(1, (0.0, 0.0, float(rc.uniform(-0.2, 0.2))), 0, 2, 0.2, 0.05, 3.0), 2,
+                             1.0, 2.0)
+    b = scenes._shape_record(scenes._rigid_body(2, (float(rc.uniform(0.5, 2.0)), float(rc.uniform(1.2, 1.8)),
+                                                    float(rc.uniform(-0.2, 0.2))), 2, 2, 0.2, 0.05, 2.5), 2, 1.0, 1.5)
     n, point, lam = two_body_contact(a, b, verts, [])
     A = (np_vertex(a, verts, 0), np_vertex(a, verts, 1), F(1.0))
     B = (np_vertex(b, verts, 0), np_vertex(b, verts, 1), F(1.0))
